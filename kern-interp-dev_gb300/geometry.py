@@ -1,0 +1,240 @@
+"""Boundary discretizations and right-hand sides for the solver's workloads.
+
+Every workload is a seeded synthetic boundary: Gauss-Legendre panel
+quadrature on closed curves (the reference ships no panel boundary; its
+Boundary subclasses fill the same public arrays, kern_interp/boundaries/
+boundary.h:47-64: points and normals interleaved per node, weights,
+curvatures, hole descriptors, boundary values).
+
+Conventions follow the reference's circle/annulus boundaries
+(kern_interp/boundaries/circle.cpp:8-32, annulus.cpp:8-58): the outer curve
+has outward normals and positive curvature; each hole carries normals
+pointing into the hole and negative curvature.
+"""
+from dataclasses import dataclass, field
+import numpy as np
+
+
+@dataclass
+class Problem:
+    points: np.ndarray            # (n, 2) node coordinates
+    normals: np.ndarray           # (n, 2) unit normals
+    weights: np.ndarray           # (n,) quadrature weights (arc length)
+    curvatures: np.ndarray        # (n,) signed curvature
+    hole_centers: np.ndarray = field(default_factory=lambda: np.zeros((0, 2)))
+    hole_start: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    hole_count: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    name: str = ""
+
+    @property
+    def n(self):
+        return self.points.shape[0]
+
+    @property
+    def n_holes(self):
+        return self.hole_centers.shape[0]
+
+
+def gauss_legendre(q):
+    x, w = np.polynomial.legendre.leggauss(q)
+    return x, w
+
+
+def _panel_curve(fun, t_breaks, q):
+    """Discretize a closed parametric curve z(t) with q-node GL panels whose
+    parameter breakpoints are t_breaks (len = panels + 1).  fun(t) returns
+    (z, dz, d2z) as complex arrays."""
+    x, w = gauss_legendre(q)
+    a, b = t_breaks[:-1], t_breaks[1:]
+    half = 0.5 * (b - a)
+    t = (0.5 * (a + b))[:, None] + half[:, None] * x[None, :]
+    t = t.ravel()
+    wt = (half[:, None] * w[None, :]).ravel()
+    z, dz, d2z = fun(t)
+    speed = np.abs(dz)
+    tangent = dz / speed
+    normal = -1j * tangent                  # outward for counter-clockwise curves
+    kappa = np.imag(np.conj(dz) * d2z) / speed ** 3
+    return z, normal, wt * speed, kappa
+
+
+def _equal_arclength_breaks(fun, panels, oversample=64):
+    """Parameter breakpoints on [0, 2pi] that split the curve into panels of
+    equal arc length (monotone interpolation of a fine arc-length table)."""
+    m = panels * oversample
+    t = np.linspace(0.0, 2 * np.pi, m + 1)
+    mid = 0.5 * (t[:-1] + t[1:])
+    _, dz, _ = fun(mid)
+    s = np.concatenate([[0.0], np.cumsum(np.abs(dz) * (t[1] - t[0]))])
+    targets = np.linspace(0.0, s[-1], panels + 1)
+    br = np.interp(targets, s, t)
+    br[0], br[-1] = 0.0, 2 * np.pi
+    return br
+
+
+def star(panels=256, q=16, amp=0.3, k=5):
+    """Star curve r(theta) = 1 + amp cos(k theta), equal-theta panels."""
+    def fun(t):
+        r = 1 + amp * np.cos(k * t)
+        dr = -amp * k * np.sin(k * t)
+        d2r = -amp * k * k * np.cos(k * t)
+        e = np.exp(1j * t)
+        z = r * e
+        dz = (dr + 1j * r) * e
+        d2z = (d2r + 2j * dr - r) * e
+        return z, dz, d2z
+    z, nrm, w, kap = _panel_curve(fun, np.linspace(0, 2 * np.pi, panels + 1), q)
+    return Problem(np.stack([z.real, z.imag], 1), np.stack([nrm.real, nrm.imag], 1),
+                   w, kap, name="star")
+
+
+def circle(n, radius=0.25):
+    """The reference's circle test boundary (kern_interp/boundaries/circle.cpp:8-32):
+    n equispaced nodes, trapezoid weights."""
+    ang = np.arange(n) * 2.0 * np.pi / n
+    pts = np.stack([radius * np.cos(ang), radius * np.sin(ang)], 1)
+    nrm = np.stack([np.cos(ang), np.sin(ang)], 1)
+    return Problem(pts, nrm, np.full(n, 2 * np.pi * radius / n), np.full(n, 1.0 / radius),
+                   name="circle")
+
+
+def _ellipse_fun(c, a, b, phi):
+    rot = np.exp(1j * phi)
+
+    def fun(t):
+        z = c + rot * (a * np.cos(t) + 1j * b * np.sin(t))
+        dz = rot * (-a * np.sin(t) + 1j * b * np.cos(t))
+        d2z = rot * (-a * np.cos(t) - 1j * b * np.sin(t))
+        return z, dz, d2z
+    return fun
+
+
+def _ellipse_perimeter(a, b):
+    h = ((a - b) / (a + b)) ** 2
+    return np.pi * (a + b) * (1 + 3 * h / (10 + np.sqrt(4 - 3 * h)))
+
+
+def sample_ellipses(n_holes, rng, axis_lo=0.02, axis_hi=0.06, r_max=1.8, gap=0.01,
+                    max_tries=200000):
+    """Non-overlapping ellipses: semi-axes U(axis_lo, axis_hi), uniform
+    orientation, centres rejection-sampled in |x| < r_max with the bounding
+    circles (major semi-axis) at least `gap` apart."""
+    cs, ax, ph = [], [], []
+    tries = 0
+    while len(cs) < n_holes:
+        tries += 1
+        if tries > max_tries:
+            raise RuntimeError("could not place %d holes" % n_holes)
+        c = rng.uniform(-r_max, r_max, 2)
+        if np.hypot(*c) >= r_max:
+            continue
+        a, b = rng.uniform(axis_lo, axis_hi, 2)
+        phi = rng.uniform(0, 2 * np.pi)
+        rad = max(a, b)
+        ok = all(np.hypot(*(c - c2)) >= rad + max(a2) + gap for c2, a2 in zip(cs, ax))
+        if ok:
+            cs.append(c)
+            ax.append((a, b))
+            ph.append(phi)
+    return np.array(cs), np.array(ax), np.array(ph)
+
+
+def disc_with_ellipses(n_unknowns=1 << 20, n_holes=64, radius=2.0, seed=1, q=16):
+    """Disc of radius `radius` minus `n_holes` ellipses, q-node GL panels with
+    equal node density per unit arc length; n_unknowns must be a multiple of q."""
+    rng = np.random.default_rng(seed)
+    cs, ax, ph = sample_ellipses(n_holes, rng)
+    lens = [2 * np.pi * radius] + [_ellipse_perimeter(a, b) for a, b in ax]
+    lens = np.array(lens)
+    total_panels = n_unknowns // q
+    if total_panels * q != n_unknowns:
+        raise ValueError("n_unknowns must be a multiple of q")
+    raw = total_panels * lens / lens.sum()
+    panels = np.maximum(np.floor(raw).astype(int), 2)
+    rem = total_panels - panels.sum()
+    order = np.argsort(-(raw - np.floor(raw)))
+    i = 0
+    while rem != 0:
+        j = order[i % len(order)]
+        if rem > 0:
+            panels[j] += 1
+            rem -= 1
+        elif panels[j] > 2:
+            panels[j] -= 1
+            rem += 1
+        i += 1
+
+    def outer(t):
+        e = np.exp(1j * t)
+        return radius * e, 1j * radius * e, -radius * e
+    pts, nrm, wts, kap = [], [], [], []
+    z, n_, w, k = _panel_curve(outer, np.linspace(0, 2 * np.pi, panels[0] + 1), q)
+    pts.append(z); nrm.append(n_); wts.append(w); kap.append(k)
+    starts, counts = [], []
+    off = z.size
+    for h in range(n_holes):
+        fun = _ellipse_fun(cs[h, 0] + 1j * cs[h, 1], ax[h, 0], ax[h, 1], ph[h])
+        br = _equal_arclength_breaks(fun, panels[h + 1])
+        z, n_, w, k = _panel_curve(fun, br, q)
+        # holes: normals into the hole, negative curvature
+        pts.append(z); nrm.append(-n_); wts.append(w); kap.append(-k)
+        starts.append(off); counts.append(z.size)
+        off += z.size
+    z = np.concatenate(pts); n_ = np.concatenate(nrm)
+    return Problem(np.stack([z.real, z.imag], 1), np.stack([n_.real, n_.imag], 1),
+                   np.concatenate(wts), np.concatenate(kap),
+                   hole_centers=cs.copy(), hole_start=np.array(starts, np.int32),
+                   hole_count=np.array(counts, np.int32), name="disc_with_ellipses")
+
+
+def laplace_source_rhs(prob, sources):
+    """Boundary values of u(x) = log|x - y| / (2 pi) for each source y (one
+    column per source), the field the reference's SINGLE_ELECTRON condition
+    uses (kern_interp/boundaries/boundary.cpp:69-74)."""
+    sources = np.atleast_2d(sources)
+    d = prob.points[:, None, :] - sources[None, :, :]
+    return np.log(np.hypot(d[..., 0], d[..., 1])) / (2 * np.pi)
+
+
+def laplace_source_field(targets, sources):
+    sources = np.atleast_2d(sources)
+    d = targets[:, None, :] - sources[None, :, :]
+    return np.log(np.hypot(d[..., 0], d[..., 1])) / (2 * np.pi)
+
+
+def random_sources(n, rng, r_lo=2.5, r_hi=4.0):
+    r = rng.uniform(r_lo, r_hi, n)
+    t = rng.uniform(0, 2 * np.pi, n)
+    return np.stack([r * np.cos(t), r * np.sin(t)], 1)
+
+
+def disc_targets(n, rng, radius=0.5):
+    """n points uniform in the disc of the given radius."""
+    r = radius * np.sqrt(rng.uniform(0, 1, n))
+    t = rng.uniform(0, 2 * np.pi, n)
+    return np.stack([r * np.cos(t), r * np.sin(t)], 1)
+
+
+def domain_targets(prob, n, rng, radius=1.9, margin=0.02):
+    """n points inside the outer disc and outside every hole's bounding circle."""
+    out = []
+    while len(out) < n:
+        p = disc_targets(1, rng, radius)[0]
+        ok = True
+        for c in prob.hole_centers:
+            if np.hypot(*(p - c)) < 0.06 + margin:
+                ok = False
+                break
+        if ok:
+            out.append(p)
+    return np.array(out)
+
+
+def star_c1():
+    """4,096-unknown star r = 1 + 0.3 cos 5 theta: 256 panels x 16 nodes,
+    source y0 = (3, 3), 100 interior targets uniform in r < 0.5 (seed 0)."""
+    prob = star(256, 16)
+    src = np.array([[3.0, 3.0]])
+    rng = np.random.default_rng(0)
+    tg = disc_targets(100, rng, 0.5)
+    return prob, src, tg

@@ -1,0 +1,149 @@
+"""CPU oracle for the skeletonization solver: TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+package, and only as the checker / the timed reference CPU path.  The product
+path (the CUDA library behind include/ki_gpu.h) never imports it.
+
+  * ``port``  -- oracle/port/ki_port.cpp, a C++ restatement of the
+    reference's factor and solve (kern_interp/skel_factorization,
+    kern_interp/kernel, kern_interp/quadtree), compiled by ``build_port``;
+  * ``ref``   -- the reference's own sources compiled by oracle/build_ref.py
+    (only where the reference tree is present).
+"""
+import ctypes
+import glob
+import hashlib
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SRC = os.path.join(HERE, "port", "ki_port.cpp")
+PORT_LIB = os.path.join(HERE, "port", "libkiport.so")
+
+_blas = None
+
+
+def load_openblas():
+    """Load scipy's bundled OpenBLAS into the process (RTLD_GLOBAL) so the
+    port and the reference build can resolve LAPACK symbols."""
+    global _blas
+    if _blas is None:
+        import scipy
+        libs = os.path.join(os.path.dirname(os.path.dirname(scipy.__file__)), "scipy.libs")
+        cands = sorted(glob.glob(os.path.join(libs, "libscipy_openblas*.so")))
+        if not cands:
+            raise RuntimeError("scipy's bundled OpenBLAS not found")
+        _blas = ctypes.CDLL(cands[0], mode=ctypes.RTLD_GLOBAL)
+    return _blas
+
+
+def build_port(force=False):
+    """Compile the C++ restatement (gcc, OpenMP) into oracle/port/libkiport.so."""
+    src = open(PORT_SRC, "rb").read()
+    stamp = hashlib.sha1(src).hexdigest()
+    stamp_file = PORT_LIB + ".stamp"
+    if (not force and os.path.exists(PORT_LIB) and os.path.exists(stamp_file)
+            and open(stamp_file).read() == stamp):
+        return PORT_LIB
+    subprocess.run(["g++", "-O2", "-fopenmp", "-std=c++17", "-fPIC", "-shared",
+                    PORT_SRC, "-o", PORT_LIB, "-ldl"], check=True)
+    with open(stamp_file, "w") as f:
+        f.write(stamp)
+    return PORT_LIB
+
+
+_P = ctypes.c_void_p
+
+
+def _dp(a):
+    return a.ctypes.data_as(_P)
+
+
+class _Lib:
+    def __init__(self, path, prefix, has_params):
+        load_openblas()
+        self.lib = ctypes.CDLL(path)
+        self.prefix = prefix
+        self.has_params = has_params
+        f = getattr(self.lib, prefix + "_solve")
+        base = [ctypes.c_int] * 4 + [_P] * 4 + [ctypes.c_int] + [_P] * 4 + \
+               [ctypes.c_int, ctypes.c_double, ctypes.c_int]
+        if has_params:
+            base += [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+        f.argtypes = base + [_P] * 3
+        f.restype = ctypes.c_int
+        self.solve_fn = f
+
+
+def solve(prob, rhs, tol, threads=1, leaf=64, proxy=128, ratio=2.0, min_compress=64,
+          solution_dim=1, pde=0, impl="port"):
+    """Factor + solve with the oracle.  rhs: (N, nrhs).  Returns (mu, alpha,
+    stats) with mu (N, nrhs), alpha (n_border, nrhs), stats dict."""
+    if impl == "port":
+        lib = _Lib(build_port(), "kiport", True)
+    else:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("_ki_build_ref", os.path.join(HERE, "build_ref.py"))
+        br = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(br)
+        lib = _Lib(br.build(leaf=leaf, proxy=proxy, ratio=ratio, min_compress=min_compress),
+                   "kiref", False)
+    rhs = np.asarray(rhs, dtype=np.float64)
+    if rhs.ndim == 1:
+        rhs = rhs[:, None]
+    N = prob.n * solution_dim
+    nrhs = rhs.shape[1]
+    c = 1 if solution_dim == 1 else 3
+    nb = c * prob.n_holes
+    pts = np.ascontiguousarray(prob.points, np.float64)
+    nrm = np.ascontiguousarray(prob.normals, np.float64)
+    wts = np.ascontiguousarray(prob.weights, np.float64)
+    cur = np.ascontiguousarray(prob.curvatures, np.float64)
+    hc = np.ascontiguousarray(prob.hole_centers, np.float64).reshape(-1)
+    hs = np.ascontiguousarray(prob.hole_start, np.int32)
+    hn = np.ascontiguousarray(prob.hole_count, np.int32)
+    b = np.asfortranarray(rhs)
+    mu = np.zeros((N, nrhs), order="F")
+    alpha = np.zeros((max(nb, 1), nrhs), order="F")
+    st = np.zeros(8)
+    args = [prob.n, 2, solution_dim, pde, _dp(pts), _dp(nrm), _dp(wts), _dp(cur),
+            prob.n_holes, _dp(hc), _dp(hs), _dp(hn), _dp(b), nrhs, tol, threads]
+    if lib.has_params:
+        args += [leaf, proxy, ratio, min_compress]
+    args += [_dp(mu), _dp(alpha), _dp(st)]
+    rc = lib.solve_fn(*args)
+    if rc != 0:
+        msg = ""
+        if impl == "port":
+            lib.lib.kiport_last_error.restype = ctypes.c_char_p
+            msg = lib.lib.kiport_last_error().decode()
+        raise RuntimeError("oracle solve failed: " + msg)
+    stats = dict(factor_s=st[0], solve_s=st[1], levels=int(st[2]), root=int(st[3]),
+                 compressed=int(st[4]), redundant=int(st[5]))
+    return mu, alpha[:nb], stats
+
+
+def dense_matrix(prob, solution_dim=1):
+    """Dense Nystrom matrix of the reference kernel (Kernel::operator())."""
+    lib = ctypes.CDLL(build_port())
+    N = prob.n * solution_dim
+    out = np.zeros((N, N), order="F")
+    lib.kiport_dense.argtypes = [ctypes.c_int, ctypes.c_int] + [_P] * 5
+    lib.kiport_dense(prob.n, solution_dim, _dp(np.ascontiguousarray(prob.points)),
+                     _dp(np.ascontiguousarray(prob.normals)),
+                     _dp(np.ascontiguousarray(prob.weights)),
+                     _dp(np.ascontiguousarray(prob.curvatures)), _dp(out))
+    return out
+
+
+def laplace_forward(prob, targets, mu):
+    """u(x) = sum_s K(x, s) mu_s at domain points (Kernel::apply_forward with
+    forward=true, kern_interp/kernel/kernel.cpp:809-825; the 2D Laplace
+    forward entry equals the off-diagonal entry with target normal 0)."""
+    d = targets[:, None, :] - prob.points[None, :, :]
+    rn = (d * prob.normals[None]).sum(-1)
+    r2 = (d ** 2).sum(-1)
+    K = -prob.weights[None] / (2 * np.pi) * rn / r2
+    return K @ mu

@@ -1,0 +1,886 @@
+// CPU restatement of the reference's recursive-skeletonization factor and
+// solve (kern_interp), used as the ORACLE: the checker in tests and the
+// timed CPU baseline in bench.py.  TEST INFRASTRUCTURE ONLY -- the product
+// path never links, loads or calls it.
+//
+// Each function names the reference function it restates (paths relative to
+// the reference project).  The dense linear algebra calls the same LAPACK
+// routines as the reference (dgeqp3, dtrtrs, dgetrf, dgetrs, dgemm), resolved
+// at run time from whichever OpenBLAS the caller has loaded into the process
+// (scipy's bundled build, whose symbols may carry a "scipy_" prefix).
+//
+// Deliberate differences, none of which changes the arithmetic:
+//  * Schur-update gathering (quadtree/quadtree.cpp:1545-1632) uses a hash map
+//    from DOF to position instead of the reference's quadratic list scan.
+//  * The ID matrix's update blocks for near rows (kernel/kernel.cpp:612-619)
+//    are omitted: descendants' updates only touch DOFs inside the box, so
+//    those blocks are identically zero.
+//  * multiply_connected_solve handles every right-hand-side column at once
+//    (the reference handles column 0 only, skel_factorization.cpp:915-916);
+//    each column's arithmetic is the same.
+#include <dlfcn.h>
+#include <omp.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------- LAPACK --
+typedef void (*dgeqp3_t)(const int*, const int*, double*, const int*, int*, double*,
+                         double*, const int*, int*);
+typedef void (*dgetrf_t)(const int*, const int*, double*, const int*, int*, int*);
+typedef void (*dgetrs_t)(const char*, const int*, const int*, const double*, const int*,
+                         const int*, double*, const int*, int*, size_t);
+typedef void (*dtrtrs_t)(const char*, const char*, const char*, const int*, const int*,
+                         const double*, const int*, double*, const int*, int*, size_t,
+                         size_t, size_t);
+typedef void (*dgemm_t)(const char*, const char*, const int*, const int*, const int*,
+                        const double*, const double*, const int*, const double*,
+                        const int*, const double*, double*, const int*, size_t, size_t);
+typedef void (*setthreads_t)(int);
+
+struct Lapack {
+  dgeqp3_t dgeqp3 = nullptr;
+  dgetrf_t dgetrf = nullptr;
+  dgetrs_t dgetrs = nullptr;
+  dtrtrs_t dtrtrs = nullptr;
+  dgemm_t dgemm = nullptr;
+  setthreads_t set_threads = nullptr;
+};
+
+void* find_symbol(const char* name) {
+  std::string pre = std::string("scipy_") + name;
+  void* p = dlsym(RTLD_DEFAULT, pre.c_str());
+  if (!p) p = dlsym(RTLD_DEFAULT, name);
+  return p;
+}
+
+const Lapack& lapack() {
+  static Lapack L = [] {
+    Lapack l;
+    l.dgeqp3 = (dgeqp3_t)find_symbol("dgeqp3_");
+    l.dgetrf = (dgetrf_t)find_symbol("dgetrf_");
+    l.dgetrs = (dgetrs_t)find_symbol("dgetrs_");
+    l.dtrtrs = (dtrtrs_t)find_symbol("dtrtrs_");
+    l.dgemm = (dgemm_t)find_symbol("dgemm_");
+    l.set_threads = (setthreads_t)find_symbol("openblas_set_num_threads");
+    return l;
+  }();
+  return L;
+}
+
+// ---------------------------------------------------------------- Matrix --
+// Column-major owning matrix with the reference's ki_Mat semantics
+// (ki_mat.h:19-104): lda == height.
+struct Mat {
+  int h = 0, w = 0;
+  std::vector<double> a;
+  Mat() {}
+  Mat(int h_, int w_) : h(h_), w(w_), a((size_t)h_ * w_, 0.0) {}
+  double& operator()(int i, int j) { return a[i + (size_t)h * j]; }
+  double operator()(int i, int j) const { return a[i + (size_t)h * j]; }
+  double* data() { return a.data(); }
+  const double* data() const { return a.data(); }
+};
+
+// C = alpha * op(A) op(B) + beta * C  (ki_Mat::operator*, ki_mat.cpp:328-335)
+void gemm(bool ta, bool tb, double alpha, const Mat& A, const Mat& B, double beta, Mat* C) {
+  int m = ta ? A.w : A.h, k = ta ? A.h : A.w, n = tb ? B.h : B.w;
+  if (C->h != m || C->w != n) *C = Mat(m, n);
+  if (m == 0 || n == 0) return;
+  if (k == 0) {
+    for (auto& v : C->a) v *= beta;
+    return;
+  }
+  char ca = ta ? 'T' : 'N', cb = tb ? 'T' : 'N';
+  int lda = std::max(1, A.h), ldb = std::max(1, B.h), ldc = std::max(1, C->h);
+  lapack().dgemm(&ca, &cb, &m, &n, &k, &alpha, A.data(), &lda, B.data(), &ldb, &beta,
+                 C->data(), &ldc, 1, 1);
+}
+
+Mat mul(const Mat& A, const Mat& B, bool ta = false, bool tb = false) {
+  Mat C;
+  gemm(ta, tb, 1.0, A, B, 0.0, &C);
+  return C;
+}
+
+Mat sub(const Mat& A, const std::vector<int>& I, const std::vector<int>& J) {
+  Mat R((int)I.size(), (int)J.size());
+  for (size_t j = 0; j < J.size(); j++)
+    for (size_t i = 0; i < I.size(); i++) R((int)i, (int)j) = A(I[i], J[j]);
+  return R;
+}
+
+// LU with partial pivoting (ki_Mat::LU_factorize, ki_mat.cpp:445-453).
+void lu(Mat* A, std::vector<int>* piv) {
+  int n = A->h, info = 0, lda = std::max(1, n);
+  piv->assign(n, 0);
+  if (n == 0) return;
+  lapack().dgetrf(&n, &n, A->data(), &lda, piv->data(), &info);
+  if (info < 0) throw std::runtime_error("dgetrf failed");
+}
+
+// B <- op(A)^-1 B using an LU factor (dgetrs; ki_mat.cpp:455-513).
+void lu_solve(const Mat& LU, const std::vector<int>& piv, bool trans, Mat* B) {
+  int n = LU.h, nrhs = B->w, info = 0, lda = std::max(1, n), ldb = std::max(1, B->h);
+  if (n == 0 || nrhs == 0) return;
+  char t = trans ? 'T' : 'N';
+  lapack().dgetrs(&t, &n, &nrhs, LU.data(), &lda, piv.data(), B->data(), &ldb, &info, 1);
+  if (info != 0) throw std::runtime_error("dgetrs failed");
+}
+
+Mat transpose(const Mat& A) {
+  Mat T(A.w, A.h);
+  for (int j = 0; j < A.w; j++)
+    for (int i = 0; i < A.h; i++) T(j, i) = A(i, j);
+  return T;
+}
+
+// Interpolative decomposition by column-pivoted QR (ki_Mat::id,
+// ki_mat.cpp:525-568): k = first i >= 1 with |R_ii| < tol |R_00|, 0 when no
+// such i exists; T = R11^-1 R12 (k x (n-k)); perm = 0-based pivots.
+int interp_decomp(Mat M, double tol, std::vector<int>* perm, Mat* T) {
+  int m = M.h, n = M.w, info = 0, lda = std::max(1, m);
+  std::vector<int> jpvt(n, 0);
+  std::vector<double> tau(std::min(m, n) + 1);
+  int lwork = -1;
+  double wq = 0;
+  lapack().dgeqp3(&m, &n, M.data(), &lda, jpvt.data(), tau.data(), &wq, &lwork, &info);
+  lwork = std::max(1, (int)wq);
+  std::vector<double> work(lwork);
+  lapack().dgeqp3(&m, &n, M.data(), &lda, jpvt.data(), tau.data(), work.data(), &lwork, &info);
+  if (info != 0) throw std::runtime_error("dgeqp3 failed");
+  int k = 0;
+  double thresh = std::fabs(tol * M(0, 0));
+  for (int i = 1; i < std::min(m, n); i++) {
+    if (std::fabs(M(i, i)) < thresh) {
+      k = i;
+      break;
+    }
+  }
+  if (k == 0) return 0;
+  perm->resize(n);
+  for (int i = 0; i < n; i++) (*perm)[i] = jpvt[i] - 1;
+  int r = n - k;
+  char U = 'U', N = 'N';
+  dtrtrs_t trs = lapack().dtrtrs;
+  trs(&U, &N, &N, &k, &r, M.data(), &lda, M.data() + (size_t)lda * k, &lda, &info, 1, 1, 1);
+  if (info != 0) throw std::runtime_error("dtrtrs failed");
+  *T = Mat(k, r);
+  for (int j = 0; j < r; j++)
+    for (int i = 0; i < k; i++) (*T)(i, j) = M(i, k + j);
+  return k;
+}
+
+// ---------------------------------------------------------------- Kernel --
+struct Geometry {
+  int n_points = 0, sol_dim = 1, pde = 0;
+  const double* pts = nullptr;   // interleaved (x, y)
+  const double* nrm = nullptr;   // interleaved
+  const double* wts = nullptr;
+  const double* curv = nullptr;
+};
+
+// Kernel::one_d_kern / two_d_kern (kernel/kernel.cpp:33-87).
+inline double entry(const Geometry& g, int tgt_dof, int src_dof, const double* tp,
+                    const double* tn, const double* sp, const double* sn, double sw,
+                    double sc) {
+  double r1 = tp[0] - sp[0], r2 = tp[1] - sp[1];
+  if (g.sol_dim == 1) {
+    if (r1 == 0. && r2 == 0.) return 0.5 + 0.5 * sc * sw * (1.0 / (2 * M_PI));
+    return -sw * (1.0 / (2 * M_PI)) * (r1 * sn[0] + r2 * sn[1]) / (r1 * r1 + r2 * r2);
+  }
+  int tpar = tgt_dof % 2, spar = src_dof % 2;
+  double r[2] = {r1, r2};
+  double scale = 1 / M_PI;
+  int is_diag = (tpar + spar + 1) % 2;
+  if (r1 == 0. && r2 == 0.) {
+    return -0.5 * is_diag + (1 - 2 * is_diag) * 0.5 * sc * sw * scale * sn[(tpar + 1) % 2] *
+               sn[(spar + 1) % 2] +
+           sw * tn[tpar] * sn[spar];
+  }
+  double rr = r1 * r1 + r2 * r2;
+  return sw * scale * (r1 * sn[0] + r2 * sn[1]) / (rr * rr) * r[tpar] * r[spar] +
+         sw * tn[tpar] * sn[spar];
+}
+
+// Kernel::operator() (kernel/kernel.cpp:304-360): dense block K(tgt, src).
+Mat kernel_block(const Geometry& g, const std::vector<int>& tgt, const std::vector<int>& src) {
+  Mat R((int)tgt.size(), (int)src.size());
+  for (size_t j = 0; j < src.size(); j++) {
+    int sp = src[j] / g.sol_dim;
+    const double* s = g.pts + 2 * sp;
+    const double* sn = g.nrm + 2 * sp;
+    double sw = g.wts[sp], sc = g.curv ? g.curv[sp] : 0.;
+    for (size_t i = 0; i < tgt.size(); i++) {
+      int tpi = tgt[i] / g.sol_dim;
+      R((int)i, (int)j) = entry(g, tgt[i], src[j], g.pts + 2 * tpi, g.nrm + 2 * tpi, s, sn, sw, sc);
+    }
+  }
+  return R;
+}
+
+// Kernel::get_proxy_mat (kernel/kernel.cpp:646-717), 2D.
+Mat proxy_block(const Geometry& g, const double* c, int P, double r, const std::vector<int>& box) {
+  double pw = 2.0 * M_PI * r / P;
+  int c_dim = g.sol_dim;
+  int lda = c_dim * 2 * P;
+  Mat R(lda, (int)box.size());
+  for (size_t j = 0; j < box.size(); j++) {
+    int bp = box[j] / g.sol_dim;
+    const double* b = g.pts + 2 * bp;
+    const double* bn = g.nrm + 2 * bp;
+    double bw = g.wts[bp];
+    for (int i = 0; i < P; i++) {
+      double ang = 2 * M_PI * i * (1.0 / P);
+      double pp[2] = {c[0] + r * std::cos(ang), c[1] + r * std::sin(ang)};
+      double pn[2] = {std::cos(ang), std::sin(ang)};
+      if (c_dim == 1) {
+        R(i, (int)j) = entry(g, 0, 0, pp, pn, b, bn, bw, 0);
+        R(P + i, (int)j) = entry(g, 0, 0, b, bn, pp, pn, pw, 0);
+      } else {
+        for (int par = 0; par < 2; par++) {
+          R(2 * i + par, (int)j) = entry(g, par, box[j], pp, pn, b, bn, bw, 0);
+          R(2 * P + 2 * i + par, (int)j) = entry(g, box[j], par, b, bn, pp, pn, pw, 0);
+        }
+      }
+    }
+  }
+  return R;
+}
+
+// ------------------------------------------------------------------ Tree --
+struct Node {
+  int level = 0;
+  bool leaf = true, compressed = false;
+  double c[2] = {0, 0}, side = 0;
+  int parent = -1;
+  std::vector<int> children, neighbors;
+  std::vector<int> orig, act, skel, red, near, perm;
+  Mat T, L, U, Xlu, S;
+  std::vector<int> piv;
+};
+
+struct Params {
+  int leaf = 64, proxy = 128, min_compress = 64;
+  double ratio = 2.0, tol = 1e-10;
+  int threads = 1;
+};
+
+struct Tree {
+  Geometry g;
+  Params p;
+  std::vector<Node> nodes;
+  std::vector<std::vector<int>> levels;
+  Mat allskel_lu, U, Psi, S_lu;
+  std::vector<int> allskel_piv, S_piv;
+
+  int new_node() {
+    nodes.emplace_back();
+    return (int)nodes.size() - 1;
+  }
+
+  // QuadTree::node_subdivide (quadtree/quadtree.cpp:372-413).
+  void subdivide(int ni) {
+    nodes[ni].leaf = false;
+    int kids[4];
+    for (int ci = 0; ci < 4; ci++) {
+      int k = new_node();
+      kids[ci] = k;
+      Node& n = nodes[ni];
+      Node& ch = nodes[k];
+      ch.c[0] = n.c[0] + ((ci & 2) ? n.side / 4. : -n.side / 4.);
+      ch.c[1] = n.c[1] + ((ci & 1) ? n.side / 4. : -n.side / 4.);
+      ch.level = n.level + 1;
+      ch.side = n.side / 2.0;
+      ch.parent = ni;
+    }
+    Node& n = nodes[ni];
+    for (int ci = 0; ci < 4; ci++) n.children.push_back(kids[ci]);
+    if ((int)levels.size() < n.level + 2) levels.emplace_back();
+    for (int ci = 0; ci < 4; ci++) levels[n.level + 1].push_back(kids[ci]);
+    std::vector<int> orig = n.orig;
+    double cx = n.c[0], cy = n.c[1];
+    for (size_t idx = 0; idx < orig.size(); idx += g.sol_dim) {
+      int dof = orig[idx];
+      int pt = dof / g.sol_dim;
+      int ci = (g.pts[2 * pt] >= cx ? 2 : 0) + (g.pts[2 * pt + 1] >= cy ? 1 : 0);
+      for (int s = 0; s < g.sol_dim; s++) nodes[kids[ci]].orig.push_back(dof + s);
+    }
+    for (int ci = 0; ci < 4; ci++)
+      if ((int)nodes[kids[ci]].orig.size() > p.leaf) subdivide(kids[ci]);
+  }
+
+  // QuadTree::recursive_add (quadtree/quadtree.cpp:317-344).
+  void add(int ni, int pt) {
+    for (int s = 0; s < g.sol_dim; s++) nodes[ni].orig.push_back(g.sol_dim * pt + s);
+    if (!nodes[ni].leaf) {
+      int ci = (g.pts[2 * pt] >= nodes[ni].c[0] ? 2 : 0) + (g.pts[2 * pt + 1] >= nodes[ni].c[1] ? 1 : 0);
+      add(nodes[ni].children[ci], pt);
+    } else if ((int)nodes[ni].orig.size() > p.leaf) {
+      subdivide(ni);
+    }
+  }
+
+  // QuadTree::get_descendent_neighbors (quadtree/quadtree.cpp:292-314).
+  void descendent_neighbors(int big, int small) {
+    bool nb = true;
+    for (int d = 0; d < 2; d++) {
+      double dist = std::fabs(nodes[big].c[d] - nodes[small].c[d]);
+      double pred = (nodes[big].side + nodes[small].side) / 2.;
+      if (dist - pred > 1e-9) {
+        nb = false;
+        break;
+      }
+    }
+    if (nb) {
+      nodes[big].neighbors.push_back(small);
+      nodes[small].neighbors.push_back(big);
+    }
+    for (int ch : std::vector<int>(nodes[small].children)) descendent_neighbors(big, ch);
+  }
+
+  // QuadTree::compute_neighbor_lists (quadtree/quadtree.cpp:192-237).
+  void neighbor_lists() {
+    for (size_t l = 0; l < levels.size(); l++) {
+      for (int a : levels[l]) {
+        int par = nodes[a].parent;
+        if (par >= 0) {
+          for (int sib : nodes[par].children)
+            if (sib != a) nodes[a].neighbors.push_back(sib);
+          for (int pn : std::vector<int>(nodes[par].neighbors)) {
+            for (int cousin : nodes[pn].children) {
+              if (nodes[cousin].level != nodes[a].level) continue;
+              double dx = nodes[a].c[0] - nodes[cousin].c[0], dy = nodes[a].c[1] - nodes[cousin].c[1];
+              double dist = std::sqrt(dx * dx + dy * dy);
+              if (dist < nodes[a].side * std::sqrt(2.0) + 1e-9) nodes[a].neighbors.push_back(cousin);
+            }
+          }
+        }
+        if (nodes[a].leaf) {
+          for (size_t k = 0; k < nodes[a].neighbors.size(); k++) {
+            int nb = nodes[a].neighbors[k];
+            if (nodes[nb].level != nodes[a].level) continue;
+            for (int ch : std::vector<int>(nodes[nb].children)) descendent_neighbors(a, ch);
+          }
+        }
+      }
+    }
+  }
+
+  // QuadTree::initialize_tree (quadtree/quadtree.cpp:240-287).
+  void build() {
+    double mn = g.pts[0], mx = g.pts[0];
+    for (int i = 0; i < 2 * g.n_points; i++) {
+      mn = std::min(mn, g.pts[i]);
+      mx = std::max(mx, g.pts[i]);
+    }
+    double tmin = mn - 0.01, tmax = mx + 0.01;
+    int root = new_node();
+    nodes[root].c[0] = nodes[root].c[1] = (tmin + tmax) / 2.0;
+    nodes[root].side = tmax - tmin;
+    levels.push_back({root});
+    nodes.reserve(8 * (g.n_points * g.sol_dim / std::max(1, p.leaf) + 4));
+    for (int i = 0; i < g.n_points; i++) add(root, i);
+    neighbor_lists();
+  }
+
+  // QuadTree::remove_inactive_dofs_at_box (quadtree/quadtree.cpp:1172-1204).
+  void refresh_box(int ni) {
+    Node& n = nodes[ni];
+    n.skel.clear();
+    n.red.clear();
+    n.act.clear();
+    if (!n.leaf) {
+      for (int ch : n.children) {
+        const Node& c = nodes[ch];
+        const std::vector<int>& src = c.compressed ? c.skel : c.act;
+        n.act.insert(n.act.end(), src.begin(), src.end());
+      }
+    } else {
+      n.act = n.orig;
+    }
+  }
+
+  // QuadTree::remove_inactive_dofs_at_level (quadtree/quadtree.cpp:1142-1169).
+  void refresh_level(int l) {
+    for (int ni : levels[l])
+      if (!nodes[ni].compressed) refresh_box(ni);
+    for (int ni : levels[l]) {
+      Node& a = nodes[ni];
+      a.near.clear();
+      for (int nb : a.neighbors) {
+        const Node& b = nodes[nb];
+        if (b.level > a.level) continue;
+        const std::vector<int>& src = b.leaf ? b.orig : b.act;
+        a.near.insert(a.near.end(), src.begin(), src.end());
+      }
+    }
+  }
+
+  // Kernel::get_id_mat (kernel/kernel.cpp:432-641).
+  Mat id_matrix(int ni) {
+    const Node& n = nodes[ni];
+    const std::vector<int>& A = n.act;
+    std::vector<int> outside;
+    bool proxy = true;
+    if (n.level == 1 || n.level == 2) {
+      proxy = false;
+      for (int o : levels[n.level])
+        if (o != ni) outside.insert(outside.end(), nodes[o].act.begin(), nodes[o].act.end());
+      if (n.level == 2) {
+        for (int l = n.level - 1; l >= 0; l--)
+          for (int o : levels[l])
+            if (nodes[o].leaf) outside.insert(outside.end(), nodes[o].orig.begin(), nodes[o].orig.end());
+      }
+    } else {
+      double rad = std::sqrt(2.0) * p.ratio * (n.side / 2);
+      for (int dof : n.near) {
+        int pt = dof / g.sol_dim;
+        double dx = n.c[0] - g.pts[2 * pt], dy = n.c[1] - g.pts[2 * pt + 1];
+        double dist = std::sqrt(dx * dx + dy * dy);
+        if (dist < rad) outside.push_back(dof);
+      }
+    }
+    Mat Kia = kernel_block(g, outside, A);
+    Mat Kai = kernel_block(g, A, outside);
+    Mat pxy;
+    if (proxy) {
+      double rad = (n.side / 2) * std::sqrt(2.0) * p.ratio;
+      pxy = proxy_block(g, n.c, p.proxy, rad, A);
+    }
+    int o = (int)outside.size();
+    Mat M(2 * o + pxy.h, (int)A.size());
+    for (int j = 0; j < (int)A.size(); j++) {
+      for (int i = 0; i < o; i++) M(i, j) = Kia(i, j);
+      for (int i = 0; i < o; i++) M(o + i, j) = Kai(j, i);
+      for (int i = 0; i < pxy.h; i++) M(2 * o + i, j) = pxy(i, j);
+    }
+    return M;
+  }
+
+  // get_descendents_updates / get_update (quadtree/quadtree.cpp:1545-1632):
+  // sum of the Schur updates of every compressed strict descendant,
+  // restricted to rows x cols.
+  void add_descendant_updates(int ni, const std::vector<int>& rows, const std::vector<int>& cols,
+                              Mat* upd) {
+    std::unordered_map<int, int> rpos, cpos;
+    for (size_t i = 0; i < rows.size(); i++) rpos[rows[i]] = (int)i;
+    for (size_t j = 0; j < cols.size(); j++) cpos[cols[j]] = (int)j;
+    std::vector<int> stack(nodes[ni].children.begin(), nodes[ni].children.end());
+    while (!stack.empty()) {
+      int d = stack.back();
+      stack.pop_back();
+      const Node& nd = nodes[d];
+      for (int ch : nd.children) stack.push_back(ch);
+      if (!nd.compressed) continue;
+      std::vector<std::pair<int, int>> sr, sc;
+      for (size_t s = 0; s < nd.skel.size(); s++) {
+        auto it = rpos.find(nd.skel[s]);
+        if (it != rpos.end()) sr.push_back({(int)s, it->second});
+        auto jt = cpos.find(nd.skel[s]);
+        if (jt != cpos.end()) sc.push_back({(int)s, jt->second});
+      }
+      for (auto& b : sc)
+        for (auto& a : sr) (*upd)(a.second, b.second) += nd.S(a.first, b.first);
+    }
+  }
+
+  // SkelFactorization::decouple (skel_factorization.cpp:91-127).
+  void decouple(int ni) {
+    Node& n = nodes[ni];
+    int k = n.T.h, r = n.T.w;
+    Mat upd((int)n.act.size(), (int)n.act.size());
+    add_descendant_updates(ni, n.act, n.act, &upd);
+    Mat K = kernel_block(g, n.act, n.act);
+    for (size_t i = 0; i < K.a.size(); i++) K.a[i] -= upd.a[i];
+    std::vector<int> s(n.perm.begin(), n.perm.begin() + k), rr(n.perm.begin() + k, n.perm.end());
+    Mat Kss = sub(K, s, s), Ksr = sub(K, s, rr), Krs = sub(K, rr, s), Krr = sub(K, rr, rr);
+    Mat Krs_t = Krs;
+    gemm(true, false, -1.0, n.T, Kss, 1.0, &Krs_t);           // K_rs - T^T K_ss
+    Mat X = Krr;
+    gemm(true, false, -1.0, n.T, Ksr, 1.0, &X);                // - T^T K_sr
+    gemm(false, false, -1.0, Krs_t, n.T, 1.0, &X);             // - K~_rs T
+    Mat Ksr_t = Ksr;
+    gemm(false, false, -1.0, Kss, n.T, 1.0, &Ksr_t);           // K_sr - K_ss T
+    n.Xlu = X;
+    lu(&n.Xlu, &n.piv);
+    // L = K~_sr X^-1  via  X^T L^T = K~_sr^T
+    Mat Lt = transpose(Ksr_t);
+    lu_solve(n.Xlu, n.piv, true, &Lt);
+    n.L = transpose(Lt);
+    n.U = Krs_t;
+    lu_solve(n.Xlu, n.piv, false, &n.U);
+    n.S = mul(n.L, Krs_t);
+    (void)r;
+    n.compressed = true;
+  }
+
+  // SkelFactorization::id_compress (skel_factorization.cpp:36-58).
+  int id_compress(int ni) {
+    Node& n = nodes[ni];
+    Mat M = id_matrix(ni);
+    if (M.h == 0) return 0;
+    std::vector<int> perm;
+    Mat T;
+    int k = interp_decomp(std::move(M), p.tol, &perm, &T);
+    if (k == 0) return 0;
+    n.T = T;
+    n.perm = perm;
+    n.skel.clear();
+    n.red.clear();
+    for (int i = 0; i < k; i++) n.skel.push_back(n.act[perm[i]]);
+    for (size_t i = k; i < perm.size(); i++) n.red.push_back(n.act[perm[i]]);
+    return T.w;
+  }
+
+  std::vector<int> allskel, allred;
+
+  // SkelFactorization::skeletonize (skel_factorization.cpp:173-551).
+  void skeletonize() {
+    if (lapack().set_threads) lapack().set_threads(1);
+    int L = (int)levels.size();
+    for (int l = L - 1; l >= 1; l--) {
+      refresh_level(l);
+      const std::vector<int>& lv = levels[l];
+      std::vector<char> err(lv.size(), 0);
+#pragma omp parallel for num_threads(p.threads) schedule(dynamic, 1)
+      for (int i = 0; i < (int)lv.size(); i++) {
+        int ni = lv[i];
+        if (nodes[ni].compressed || (int)nodes[ni].act.size() < p.min_compress) continue;
+        try {
+          if (id_compress(ni) == 0) continue;
+          decouple(ni);
+        } catch (...) {
+          err[i] = 1;
+        }
+      }
+      for (char e : err)
+        if (e) throw std::runtime_error("LAPACK failure during skeletonization");
+    }
+    for (int l = L - 1; l >= 0; l--) refresh_level(l);
+    allskel = nodes[levels[0][0]].act;
+    Mat A;
+    if (!allskel.empty()) {
+      Mat upd((int)allskel.size(), (int)allskel.size());
+      add_descendant_updates(levels[0][0], allskel, allskel, &upd);
+      A = kernel_block(g, allskel, allskel);
+      for (size_t i = 0; i < A.a.size(); i++) A.a[i] -= upd.a[i];
+    }
+    int N = g.n_points * g.sol_dim;
+    std::vector<char> is_skel(N, 0);
+    for (int s : allskel) is_skel[s] = 1;
+    allred.clear();
+    for (int i = 0; i < N; i++)
+      if (!is_skel[i]) allred.push_back(i);
+    if (U.w == 0) {
+      allskel_lu = A;
+      lu(&allskel_lu, &allskel_piv);
+      return;
+    }
+    // Bordered system (skel_factorization.cpp:311-547).
+    std::unordered_map<int, int> red_pos;
+    for (size_t i = 0; i < allred.size(); i++) red_pos[allred[i]] = (int)i;
+    Mat mU = U, mPsiT = transpose(Psi);
+    up_sweep(&mU, false);
+    psi_sweep(&mPsiT);
+    Mat Psi_m = transpose(mPsiT);
+    Mat DinvC = sub(mU, allred, range(mU.w));
+    diag_solve_small(&DinvC, red_pos);
+    int ns = (int)allskel.size(), nh = Psi.h;
+    Mat S(ns + nh, ns + nh);
+    Mat PsiR = sub(Psi_m, range(nh), allred), PsiS = sub(Psi_m, range(nh), allskel);
+    Mat Us = sub(mU, allskel, range(U.w));
+    Mat corr = mul(PsiR, DinvC);
+    for (int j = 0; j < ns; j++)
+      for (int i = 0; i < ns; i++) S(i, j) = A(i, j);
+    for (int j = 0; j < ns; j++)
+      for (int i = 0; i < nh; i++) S(ns + i, j) = PsiS(i, j);
+    for (int j = 0; j < nh; j++)
+      for (int i = 0; i < ns; i++) S(i, ns + j) = Us(i, j);
+    for (int j = 0; j < nh; j++)
+      for (int i = 0; i < nh; i++) S(ns + i, ns + j) = -(i == j ? 1.0 : 0.0) - corr(i, j);
+    S_lu = S;
+    lu(&S_lu, &S_piv);
+  }
+
+  static std::vector<int> range(int n) {
+    std::vector<int> r(n);
+    for (int i = 0; i < n; i++) r[i] = i;
+    return r;
+  }
+
+  // apply_sweep_matrix (skel_factorization.cpp:555-572): x(b) += op(M) x(a).
+  static void sweep(const Mat& M, bool trans, double sign, Mat* x, const std::vector<int>& a,
+                    const std::vector<int>& b) {
+    if (a.empty() || b.empty()) return;
+    Mat xa = sub(*x, a, range(x->w));
+    Mat prod;
+    gemm(trans, false, sign, M, xa, 0.0, &prod);
+    for (int j = 0; j < x->w; j++)
+      for (size_t i = 0; i < b.size(); i++) (*x)(b[i], j) += prod((int)i, j);
+  }
+
+  // Upward pass of SkelFactorization::solve (skel_factorization.cpp:626-673).
+  void up_sweep(Mat* x, bool with_diag) {
+    int L = (int)levels.size();
+    for (int l = L - 1; l >= 0; l--) {
+      const std::vector<int>& lv = levels[l];
+#pragma omp parallel for num_threads(p.threads) schedule(dynamic, 4)
+      for (int i = 0; i < (int)lv.size(); i++) {
+        const Node& n = nodes[lv[i]];
+        if (!n.compressed) continue;
+        sweep(n.T, true, -1.0, x, n.skel, n.red);
+        sweep(n.L, false, -1.0, x, n.red, n.skel);
+      }
+    }
+    if (with_diag) diag_solve(x);
+  }
+
+  // Transposed down-sweep applied to Psi^T (skel_factorization.cpp:416-465).
+  void psi_sweep(Mat* x) {
+    int L = (int)levels.size();
+    for (int l = L - 1; l >= 0; l--) {
+      const std::vector<int>& lv = levels[l];
+#pragma omp parallel for num_threads(p.threads) schedule(dynamic, 4)
+      for (int i = 0; i < (int)lv.size(); i++) {
+        const Node& n = nodes[lv[i]];
+        if (!n.compressed) continue;
+        sweep(n.T, true, -1.0, x, n.skel, n.red);
+        sweep(n.U, true, -1.0, x, n.red, n.skel);
+      }
+    }
+  }
+
+  // apply_diag_inv_matrix over all boxes (skel_factorization.cpp:676-687).
+  void diag_solve(Mat* x) {
+    std::vector<int> all;
+    for (int l = (int)levels.size() - 1; l >= 0; l--)
+      for (int ni : levels[l]) all.push_back(ni);
+#pragma omp parallel for num_threads(p.threads) schedule(dynamic, 4)
+    for (int i = 0; i < (int)all.size(); i++) {
+      const Node& n = nodes[all[i]];
+      if (!n.compressed || n.red.empty()) continue;
+      Mat xr = sub(*x, n.red, range(x->w));
+      lu_solve(n.Xlu, n.piv, false, &xr);
+      for (int j = 0; j < x->w; j++)
+        for (size_t q = 0; q < n.red.size(); q++) (*x)(n.red[q], j) = xr((int)q, j);
+    }
+  }
+
+  // The same on a matrix indexed by position within allred.
+  void diag_solve_small(Mat* x, const std::unordered_map<int, int>& red_pos) {
+    std::vector<int> all;
+    for (int l = (int)levels.size() - 1; l >= 0; l--)
+      for (int ni : levels[l]) all.push_back(ni);
+#pragma omp parallel for num_threads(p.threads) schedule(dynamic, 4)
+    for (int i = 0; i < (int)all.size(); i++) {
+      const Node& n = nodes[all[i]];
+      if (!n.compressed || n.red.empty()) continue;
+      std::vector<int> sm;
+      for (int d : n.red) sm.push_back(red_pos.at(d));
+      Mat xr = sub(*x, sm, range(x->w));
+      lu_solve(n.Xlu, n.piv, false, &xr);
+      for (int j = 0; j < x->w; j++)
+        for (size_t q = 0; q < sm.size(); q++) (*x)(sm[q], j) = xr((int)q, j);
+    }
+  }
+
+  // Downward pass (skel_factorization.cpp:725-777).
+  void down_sweep(Mat* x) {
+    int L = (int)levels.size();
+    for (int l = 0; l < L; l++) {
+      const std::vector<int>& lv = levels[l];
+#pragma omp parallel for num_threads(p.threads) schedule(dynamic, 4)
+      for (int i = (int)lv.size() - 1; i >= 0; i--) {
+        const Node& n = nodes[lv[i]];
+        if (!n.compressed) continue;
+        sweep(n.U, false, -1.0, x, n.skel, n.red);
+        sweep(n.T, false, -1.0, x, n.red, n.skel);
+      }
+    }
+  }
+
+  // SkelFactorization::solve (skel_factorization.cpp:595-778).
+  void solve(Mat* x) {
+    up_sweep(x, true);
+    if (!allskel.empty()) {
+      Mat xs = sub(*x, allskel, range(x->w));
+      lu_solve(allskel_lu, allskel_piv, false, &xs);
+      for (int j = 0; j < x->w; j++)
+        for (size_t q = 0; q < allskel.size(); q++) (*x)(allskel[q], j) = xs((int)q, j);
+    }
+    down_sweep(x);
+  }
+
+  // SkelFactorization::multiply_connected_solve (skel_factorization.cpp:781-1141).
+  void mc_solve(Mat* mu, Mat* alpha) {
+    std::unordered_map<int, int> red_pos;
+    for (size_t i = 0; i < allred.size(); i++) red_pos[allred[i]] = (int)i;
+    Mat mU = U, mPsiT = transpose(Psi);
+    up_sweep(mu, false);
+    up_sweep(&mU, false);
+    Mat w = sub(*mu, allred, range(mu->w));
+    Mat z = sub(*mu, allskel, range(mu->w));
+    psi_sweep(&mPsiT);
+    Mat Psi_m = transpose(mPsiT);
+    Mat Dw = w;
+    diag_solve_small(&Dw, red_pos);
+    int ns = (int)allskel.size(), nh = Psi.h, nc = mu->w;
+    Mat PsiR = sub(Psi_m, range(nh), allred);
+    Mat t = mul(PsiR, Dw);
+    Mat M(ns + nh, nc);
+    for (int j = 0; j < nc; j++) {
+      for (int i = 0; i < ns; i++) M(i, j) = z(i, j);
+      for (int i = 0; i < nh; i++) M(ns + i, j) = -t(i, j);
+    }
+    lu_solve(S_lu, S_piv, false, &M);
+    *alpha = Mat(nh, nc);
+    for (int j = 0; j < nc; j++)
+      for (int i = 0; i < nh; i++) (*alpha)(i, j) = M(ns + i, j);
+    Mat Ur = sub(mU, allred, range(mU.w));
+    Mat Nm = w;
+    gemm(false, false, -1.0, Ur, *alpha, 1.0, &Nm);
+    diag_solve_small(&Nm, red_pos);
+    for (int j = 0; j < nc; j++) {
+      for (size_t q = 0; q < allred.size(); q++) (*mu)(allred[q], j) = Nm((int)q, j);
+      for (int q = 0; q < ns; q++) (*mu)(allskel[q], j) = M(q, j);
+    }
+    down_sweep(mu);
+  }
+};
+
+thread_local std::string g_err;
+
+}  // namespace
+
+extern "C" {
+
+const char* kiport_last_error() { return g_err.c_str(); }
+
+// Factor + solve, the same contract as the reference driver's kiref_solve:
+// column-major rhs (N x nrhs), outputs mu (N x nrhs) and alpha
+// (n_border x nrhs).  stats: [0] factor s, [1] solve s, [2] levels,
+// [3] root skeleton size, [4] compressed boxes, [5] redundant DOFs.
+int kiport_solve(int n_points, int domain_dim, int solution_dim, int pde,
+                 const double* points, const double* normals, const double* weights,
+                 const double* curvatures, int n_holes, const double* hole_centers,
+                 const int* hole_start, const int* hole_count, const double* rhs, int nrhs,
+                 double id_tol, int threads, int leaf, int proxy, double ratio,
+                 int min_compress, double* mu_out, double* alpha_out, double* stats) {
+  try {
+    if (domain_dim != 2) throw std::runtime_error("only 2D boundaries are supported");
+    if (!lapack().dgeqp3 || !lapack().dgemm)
+      throw std::runtime_error("LAPACK symbols not found: load OpenBLAS first");
+    Tree t;
+    t.g.n_points = n_points;
+    t.g.sol_dim = solution_dim;
+    t.g.pde = pde;
+    t.g.pts = points;
+    t.g.nrm = normals;
+    t.g.wts = weights;
+    t.g.curv = curvatures;
+    t.p.tol = id_tol;
+    t.p.threads = std::max(1, threads);
+    t.p.leaf = leaf;
+    t.p.proxy = proxy;
+    t.p.ratio = ratio;
+    t.p.min_compress = min_compress;
+    int N = n_points * solution_dim;
+    double t0 = omp_get_wtime();
+    t.build();
+    if (n_holes > 0) {
+      int c = solution_dim == 1 ? 1 : 3;
+      t.U = Mat(N, c * n_holes);
+      t.Psi = Mat(c * n_holes, N);
+      for (int h = 0; h < n_holes; h++) {
+        const double* hc = hole_centers + 2 * h;
+        for (int p = 0; p < n_points; p++) {
+          double rx = points[2 * p] - hc[0], ry = points[2 * p + 1] - hc[1];
+          double rn = std::sqrt(rx * rx + ry * ry);
+          if (solution_dim == 1) {
+            t.U(p, h) = std::log(rn);          // initialize_U_mat, linear_solve.cpp:37-45
+          } else {                               // linear_solve.cpp:77-97
+            double sc = 1.0 / (4 * M_PI), r2 = rn * rn;
+            t.U(2 * p, 3 * h) = sc * (std::log(1 / rn) + rx * rx / r2);
+            t.U(2 * p + 1, 3 * h) = sc * (ry * rx / r2);
+            t.U(2 * p, 3 * h + 1) = sc * (rx * ry / r2);
+            t.U(2 * p + 1, 3 * h + 1) = sc * (std::log(1 / rn) + ry * ry / r2);
+            t.U(2 * p, 3 * h + 2) = ry * (sc / r2);
+            t.U(2 * p + 1, 3 * h + 2) = -rx * (sc / r2);
+          }
+        }
+        for (int p = hole_start[h]; p < hole_start[h] + hole_count[h]; p++) {
+          double w = weights[p];
+          if (solution_dim == 1) {
+            t.Psi(h, p) = w;
+          } else {
+            t.Psi(3 * h, 2 * p) = w;
+            t.Psi(3 * h + 1, 2 * p + 1) = w;
+            t.Psi(3 * h + 2, 2 * p) = w * points[2 * p + 1];
+            t.Psi(3 * h + 2, 2 * p + 1) = -w * points[2 * p];
+          }
+        }
+      }
+    }
+    t.skeletonize();
+    double t1 = omp_get_wtime();
+    Mat x(N, nrhs);
+    std::memcpy(x.data(), rhs, sizeof(double) * (size_t)N * nrhs);
+    if (n_holes > 0) {
+      Mat alpha;
+      t.mc_solve(&x, &alpha);
+      if (alpha_out) std::memcpy(alpha_out, alpha.data(), sizeof(double) * alpha.a.size());
+    } else {
+      t.solve(&x);
+    }
+    double t2 = omp_get_wtime();
+    std::memcpy(mu_out, x.data(), sizeof(double) * (size_t)N * nrhs);
+    if (stats) {
+      int comp = 0;
+      long red = 0;
+      for (auto& n : t.nodes)
+        if (n.compressed) {
+          comp++;
+          red += (long)n.red.size();
+        }
+      stats[0] = t1 - t0;
+      stats[1] = t2 - t1;
+      stats[2] = (double)t.levels.size();
+      stats[3] = (double)t.allskel.size();
+      stats[4] = comp;
+      stats[5] = (double)red;
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
+// Dense kernel matrix K(all, all), column-major (Kernel::operator()).
+int kiport_dense(int n_points, int solution_dim, const double* points, const double* normals,
+                 const double* weights, const double* curvatures, double* out) {
+  Geometry g;
+  g.n_points = n_points;
+  g.sol_dim = solution_dim;
+  g.pts = points;
+  g.nrm = normals;
+  g.wts = weights;
+  g.curv = curvatures;
+  int N = n_points * solution_dim;
+  std::vector<int> all(N);
+  for (int i = 0; i < N; i++) all[i] = i;
+  Mat K = kernel_block(g, all, all);
+  std::memcpy(out, K.data(), sizeof(double) * (size_t)N * N);
+  return 0;
+}
+
+}  // extern "C"

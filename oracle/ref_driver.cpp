@@ -1,0 +1,170 @@
+// Driver around the UNMODIFIED reference CPU solver (kern_interp), compiled
+// from the reference's own sources by oracle/build_ref.py into oracle/_ref/.
+//
+// TEST INFRASTRUCTURE ONLY.  Nothing in the product links, loads or calls
+// this file; tests and the fixture generator use it as the checker.
+//
+// It exposes one extern "C" entry point that mirrors the reference's
+// boundary_integral_solve flow (kern_interp/linear_solve.cpp:257-303):
+//   Boundary data -> QuadTree::initialize_tree -> SkelFactorization::skeletonize
+//   -> SkelFactorization::solve / multiply_connected_solve (one column at a
+//   time, because multiply_connected_solve handles column 0 only,
+//   kern_interp/skel_factorization/skel_factorization.cpp:915-916).
+// Hole border matrices are built from node ranges: U with the reference's own
+// initialize_U_mat (centres only, kern_interp/linear_solve.cpp:19-107) and Psi
+// from the ranges, because the reference's circle-membership test in
+// initialize_Psi_mat (kern_interp/linear_solve.cpp:137) misclassifies
+// non-circular holes.
+#include <omp.h>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "kern_interp/boundaries/boundary.h"
+#include "kern_interp/kernel/kernel.h"
+#include "kern_interp/linear_solve.h"
+#include "kern_interp/quadtree/quadtree.h"
+#include "kern_interp/skel_factorization/skel_factorization.h"
+
+namespace {
+
+using kern_interp::Boundary;
+using kern_interp::BoundaryCondition;
+using kern_interp::PointVec;
+
+// A Boundary whose data vectors are filled directly from caller arrays.
+class ArrayBoundary : public Boundary {
+ public:
+  std::unique_ptr<Boundary> clone() const override {
+    return std::unique_ptr<Boundary>(new ArrayBoundary(*this));
+  }
+  void initialize(int, BoundaryCondition) override {}
+  bool is_in_domain(const PointVec&) const override { return true; }
+};
+
+}  // namespace
+
+extern "C" {
+
+// Stats written by kiref_solve (doubles): [0] factor seconds, [1] solve
+// seconds (all columns), [2] number of tree levels, [3] root skeleton size,
+// [4] number of compressed boxes, [5] sum of redundant DOFs.
+int kiref_solve(int n_points, int domain_dim, int solution_dim, int pde,
+                const double* points, const double* normals,
+                const double* weights, const double* curvatures,
+                int n_holes, const double* hole_centers,
+                const int* hole_start, const int* hole_count,
+                const double* rhs, int nrhs, double id_tol, int threads,
+                double* mu_out, double* alpha_out, double* stats) {
+  const int d = domain_dim;
+  const int N = n_points * solution_dim;
+  // As the reference's experiment drivers do before factorizing
+  // (kern_interp/experiments/pde_acc.cpp:97): one BLAS thread per box.
+  openblas_set_num_threads(1);
+  ArrayBoundary boundary;
+  boundary.points.assign(points, points + (size_t)n_points * d);
+  boundary.normals.assign(normals, normals + (size_t)n_points * d);
+  boundary.weights.assign(weights, weights + n_points);
+  if (curvatures) boundary.curvatures.assign(curvatures, curvatures + n_points);
+  for (int h = 0; h < n_holes; h++) {
+    kern_interp::Hole hole;
+    std::vector<double> c(hole_centers + (size_t)h * d, hole_centers + (size_t)(h + 1) * d);
+    hole.center = PointVec(c);
+    hole.radius = 0.;
+    hole.num_nodes = hole_count[h];
+    boundary.holes.push_back(hole);
+  }
+  boundary.num_outer_nodes = n_points;
+  if (n_holes > 0) boundary.num_outer_nodes = hole_start[0];
+  boundary.boundary_values = kern_interp::ki_Mat(N, 1);
+
+  kern_interp::Kernel kernel(solution_dim, d, (kern_interp::Kernel::Pde)pde,
+                             &boundary, std::vector<double>());
+  kern_interp::QuadTree quadtree;
+  quadtree.initialize_tree(&boundary, solution_dim, d);
+
+  if (n_holes > 0) {
+    quadtree.U = kern_interp::initialize_U_mat(kernel.pde, boundary.holes,
+                                               boundary.points, d);
+    // Psi from node ranges (Laplace: weights; Stokes 2D: reference layout).
+    int c = quadtree.U.width() / n_holes;
+    kern_interp::ki_Mat Psi(c * n_holes, N);
+    for (int h = 0; h < n_holes; h++) {
+      for (int p = hole_start[h]; p < hole_start[h] + hole_count[h]; p++) {
+        double w = weights[p];
+        if (solution_dim == 1) {
+          Psi.set(h, p, w);
+        } else {
+          double x = points[2 * p], y = points[2 * p + 1];
+          Psi.set(3 * h, 2 * p, w);
+          Psi.set(3 * h + 1, 2 * p + 1, w);
+          Psi.set(3 * h + 2, 2 * p, w * y);
+          Psi.set(3 * h + 2, 2 * p + 1, -w * x);
+        }
+      }
+    }
+    quadtree.Psi = Psi;
+  }
+
+  kern_interp::SkelFactorization skel(id_tol, threads);
+  double t0 = omp_get_wtime();
+  skel.skeletonize(kernel, &quadtree);
+  double t1 = omp_get_wtime();
+  for (int col = 0; col < nrhs; col++) {
+    kern_interp::ki_Mat f(N, 1);
+    std::memcpy(f.mat, rhs + (size_t)col * N, sizeof(double) * N);
+    kern_interp::ki_Mat mu(N, 1);
+    if (n_holes > 0) {
+      kern_interp::ki_Mat alpha(quadtree.U.width(), 1);
+      skel.multiply_connected_solve(quadtree, &mu, &alpha, f);
+      if (alpha_out)
+        std::memcpy(alpha_out + (size_t)col * quadtree.U.width(), alpha.mat,
+                    sizeof(double) * quadtree.U.width());
+    } else {
+      skel.solve(quadtree, &mu, f);
+    }
+    std::memcpy(mu_out + (size_t)col * N, mu.mat, sizeof(double) * N);
+  }
+  double t2 = omp_get_wtime();
+  if (stats) {
+    int compressed = 0;
+    long redundant = 0;
+    for (auto* level : quadtree.levels)
+      for (auto* node : level->nodes)
+        if (node->compressed) {
+          compressed++;
+          redundant += node->dof_lists.redundant.size();
+        }
+    stats[0] = t1 - t0;
+    stats[1] = t2 - t1;
+    stats[2] = quadtree.levels.size();
+    stats[3] = quadtree.root->dof_lists.active_box.size();
+    stats[4] = compressed;
+    stats[5] = (double)redundant;
+  }
+  return 0;
+}
+
+// Dense Nystrom matrix K(all, all) of the reference kernel
+// (Kernel::operator(), kern_interp/kernel/kernel.cpp:304-360), column-major.
+int kiref_dense(int n_points, int domain_dim, int solution_dim, int pde,
+                const double* points, const double* normals,
+                const double* weights, const double* curvatures, double* out) {
+  const int d = domain_dim;
+  const int N = n_points * solution_dim;
+  ArrayBoundary boundary;
+  boundary.points.assign(points, points + (size_t)n_points * d);
+  boundary.normals.assign(normals, normals + (size_t)n_points * d);
+  boundary.weights.assign(weights, weights + n_points);
+  if (curvatures) boundary.curvatures.assign(curvatures, curvatures + n_points);
+  kern_interp::Kernel kernel(solution_dim, d, (kern_interp::Kernel::Pde)pde,
+                             &boundary, std::vector<double>());
+  std::vector<int> all(N);
+  for (int i = 0; i < N; i++) all[i] = i;
+  kern_interp::ki_Mat K = kernel(all, all);
+  std::memcpy(out, K.mat, sizeof(double) * (size_t)N * N);
+  return 0;
+}
+
+}  // extern "C"
