@@ -1,0 +1,153 @@
+/*
+ * ki_gpu.h -- C ABI of the GB300 recursive-skeletonization solver.
+ *
+ * Drop-in boundary for the reference's factor-and-solve path (kern_interp,
+ * C++ namespace kern_interp).  Each entry point names the reference function
+ * whose role it takes; all reference paths are relative to that project.
+ *
+ * Conventions
+ *  - Plain C types only; matrices are column-major doubles with an explicit
+ *    leading dimension, like the reference's ki_Mat (kern_interp/ki_mat.h:19-104).
+ *  - Every function returns a ki_status; on failure ki_last_error() returns a
+ *    message for the calling thread.  No function asserts or exits (the
+ *    reference asserts on LAPACK failures, kern_interp/ki_mat.cpp:452-565).
+ *  - A ki_factor owns its device memory and a CUDA stream.  Calls on one
+ *    handle must not overlap; distinct handles are independent.
+ */
+#ifndef KI_GPU_H_
+#define KI_GPU_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  KI_OK = 0,
+  KI_ERR_ARG = 1,      /* invalid argument (sizes, NULL pointers, non-finite data) */
+  KI_ERR_CUDA = 2,     /* CUDA runtime error or no usable GPU */
+  KI_ERR_NUMERIC = 3,  /* singular pivot / non-finite value during factorization */
+  KI_ERR_TIMEOUT = 4,  /* a bounded device wait gave up */
+  KI_ERR_OOM = 5,      /* device allocation failed */
+  KI_ERR_STATE = 6     /* call not valid for this handle (e.g. wrong problem kind) */
+} ki_status;
+
+/* Kernel::Pde (kern_interp/kernel/kernel.h:19-24). */
+typedef enum {
+  KI_PDE_LAPLACE = 0,
+  KI_PDE_LAPLACE_NEUMANN = 1,
+  KI_PDE_GAUSS = 2,
+  KI_PDE_STOKES = 3
+} ki_pde;
+
+typedef enum {
+  KI_PRECISION_FP64 = 0,   /* plain form: every stage in FP64 (the reference's arithmetic) */
+  KI_PRECISION_FP32 = 1    /* FP32 factorization (preconditioner for refinement) */
+} ki_precision;
+
+/*
+ * Problem description: the data a reference Boundary carries
+ * (kern_interp/boundaries/boundary.h:47-64) plus the tree/proxy parameters the
+ * reference fixes as macros (MAX_LEAF_DOFS quadtree/quadtree.h:11,
+ * NUM_PROXY_POINTS / RADIUS_RATIO kernel/kernel.h:13-14,
+ * MIN_DOFS_TO_COMPRESS skel_factorization/skel_factorization.h:12) and the
+ * SkelFactorization constructor's id_tol
+ * (skel_factorization/skel_factorization.h:27).  Zero parameters take the
+ * reference defaults (64, 128, 2.0, 64).
+ */
+typedef struct {
+  int n_points;              /* boundary nodes */
+  int domain_dimension;      /* 2 */
+  int solution_dimension;    /* 1 (Laplace) or 2 (Stokes) */
+  int pde;                   /* ki_pde */
+  const double* points;      /* 2*n_points, interleaved (x, y) */
+  const double* normals;     /* 2*n_points, interleaved */
+  const double* weights;     /* n_points quadrature weights */
+  const double* curvatures;  /* n_points, may be NULL (treated as 0) */
+  int n_holes;               /* multiply connected: number of holes */
+  const double* hole_centers;    /* 2*n_holes */
+  const int* hole_node_start;    /* first node of each hole */
+  const int* hole_node_count;    /* nodes of each hole */
+  int max_leaf_dofs;
+  int num_proxy_points;
+  double radius_ratio;
+  int min_dofs_to_compress;
+  double id_tol;
+  int precision;             /* ki_precision */
+} ki_problem_desc;
+
+typedef struct ki_factor ki_factor;
+
+typedef struct {
+  int n_dofs;           /* unknowns */
+  int n_levels;         /* tree levels */
+  int n_compressed;     /* boxes compressed */
+  long n_redundant;     /* DOFs eliminated below the root */
+  int n_root;           /* root skeleton size */
+  int n_border;         /* bordered unknowns (holes x border columns) */
+  double factor_seconds;
+  long device_bytes;    /* device memory held by the factorization */
+} ki_factor_info;
+
+/*
+ * Build the tree (QuadTree::initialize_tree, quadtree/quadtree.cpp:240-287)
+ * and skeletonize (SkelFactorization::skeletonize,
+ * skel_factorization/skel_factorization.cpp:173-551) on the current GPU.
+ */
+int ki_factor_create(const ki_problem_desc* desc, ki_factor** out);
+
+/* Release a factorization (QuadTree destructor). */
+int ki_factor_destroy(ki_factor* f);
+
+/* Factorization statistics. */
+int ki_factor_get_info(const ki_factor* f, ki_factor_info* info);
+
+/*
+ * Apply the inverse to nrhs right-hand sides held in HOST memory:
+ * SkelFactorization::solve (skel_factorization.cpp:595-778) for simply
+ * connected problems, multiply_connected_solve (:781-1141, generalised to
+ * every column) otherwise; linear_solve (linear_solve.cpp:202-227) is the
+ * reference's wrapper over both.  b: n_dofs x nrhs (ldb), x: n_dofs x nrhs
+ * (ldx), alpha: n_border x nrhs (ldalpha, may be NULL when n_border == 0).
+ * x may alias b.
+ */
+int ki_solve(ki_factor* f, const double* b, int ldb, int nrhs, double* x, int ldx,
+             double* alpha, int ldalpha);
+
+/*
+ * The same with DEVICE pointers; runs on `stream` (a cudaStream_t, NULL for
+ * the handle's own stream) and returns without synchronizing.
+ */
+int ki_solve_device(ki_factor* f, const double* d_b, int ldb, int nrhs, double* d_x, int ldx,
+                    double* d_alpha, int ldalpha, void* stream);
+
+/*
+ * y = K x with the dense FP64 Nystrom operator of the problem, x and y in
+ * HOST memory (n_dofs x ncols): the reference's dense residual check
+ * (solve_err, linear_solve.cpp:379-425, via Kernel::operator(),
+ * kernel/kernel.cpp:304-360).  When the problem has holes the border term
+ * U*alpha is added if alpha != NULL.  Cost O(n_dofs^2 * ncols).
+ */
+int ki_apply(ki_factor* f, const double* x, int ldx, int ncols, const double* alpha,
+             int ldalpha, double* y, int ldy);
+
+/*
+ * Solution at domain points: u = K_forward mu (+ U_forward alpha), HOST
+ * buffers (Kernel::apply_forward, kernel/kernel.cpp:809-825, and the
+ * U_forward term of schur_solve, linear_solve.cpp:241-249).
+ * targets: 2*n_targets interleaved; out: (n_targets*solution_dimension) x ncols.
+ */
+int ki_eval_targets(ki_factor* f, const double* targets, int n_targets, const double* mu,
+                    int ldmu, int ncols, const double* alpha, int ldalpha, double* out,
+                    int ldout);
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char* ki_last_error(void);
+
+/* Library version string. */
+const char* ki_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KI_GPU_H_ */

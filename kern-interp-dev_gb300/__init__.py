@@ -1,0 +1,307 @@
+"""kern_interp_gb300 -- Python mirror of the reference's factor-and-solve
+surface over the GB300 C-ABI library (include/ki_gpu.h, libki_gpu.so).
+
+The classes keep the reference's names and argument meaning
+(kern_interp, C++ namespace kern_interp):
+
+  Boundary            kern_interp/boundaries/boundary.h:47-64 (public data)
+  Kernel              kern_interp/kernel/kernel.h:18-66
+  QuadTree            kern_interp/quadtree/quadtree.h:111-149 (initialize_tree)
+  SkelFactorization   kern_interp/skel_factorization/skel_factorization.h:20-58
+  linear_solve        kern_interp/linear_solve.h:29-31
+  boundary_integral_solve   kern_interp/linear_solve.h:17-19
+
+Matrices cross the boundary as column-major float64 arrays (the reference's
+ki_Mat layout).  There is no CPU fallback: every call runs on the GPU, and
+loading fails loudly when the library is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libki_gpu.so")
+
+KI_OK, KI_ERR_ARG, KI_ERR_CUDA, KI_ERR_NUMERIC, KI_ERR_TIMEOUT, KI_ERR_OOM, KI_ERR_STATE = range(7)
+PDE_LAPLACE, PDE_LAPLACE_NEUMANN, PDE_GAUSS, PDE_STOKES = range(4)
+PRECISION_FP64, PRECISION_FP32 = 0, 1
+
+EXPORTED = ["ki_factor_create", "ki_factor_destroy", "ki_factor_get_info", "ki_solve",
+            "ki_solve_device", "ki_apply", "ki_eval_targets", "ki_last_error", "ki_version"]
+
+
+class KiError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("ki error %d: %s" % (code, msg))
+        self.code = code
+
+
+class _Desc(ctypes.Structure):
+    _fields_ = [("n_points", ctypes.c_int), ("domain_dimension", ctypes.c_int),
+                ("solution_dimension", ctypes.c_int), ("pde", ctypes.c_int),
+                ("points", ctypes.c_void_p), ("normals", ctypes.c_void_p),
+                ("weights", ctypes.c_void_p), ("curvatures", ctypes.c_void_p),
+                ("n_holes", ctypes.c_int), ("hole_centers", ctypes.c_void_p),
+                ("hole_node_start", ctypes.c_void_p), ("hole_node_count", ctypes.c_void_p),
+                ("max_leaf_dofs", ctypes.c_int), ("num_proxy_points", ctypes.c_int),
+                ("radius_ratio", ctypes.c_double), ("min_dofs_to_compress", ctypes.c_int),
+                ("id_tol", ctypes.c_double), ("precision", ctypes.c_int)]
+
+
+class _Info(ctypes.Structure):
+    _fields_ = [("n_dofs", ctypes.c_int), ("n_levels", ctypes.c_int),
+                ("n_compressed", ctypes.c_int), ("n_redundant", ctypes.c_long),
+                ("n_root", ctypes.c_int), ("n_border", ctypes.c_int),
+                ("factor_seconds", ctypes.c_double), ("device_bytes", ctypes.c_long)]
+
+
+_lib = None
+
+
+def load_library(path=None):
+    """Load libki_gpu.so (raises OSError when it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise OSError("libki_gpu.so not found at %s: run __graft_entry__.build()" % p)
+    lib = ctypes.CDLL(p)
+    V = ctypes.c_void_p
+    I = ctypes.c_int
+    lib.ki_factor_create.argtypes = [ctypes.POINTER(_Desc), ctypes.POINTER(V)]
+    lib.ki_factor_destroy.argtypes = [V]
+    lib.ki_factor_get_info.argtypes = [V, ctypes.POINTER(_Info)]
+    lib.ki_solve.argtypes = [V, V, I, I, V, I, V, I]
+    lib.ki_solve_device.argtypes = [V, V, I, I, V, I, V, I, V]
+    lib.ki_apply.argtypes = [V, V, I, I, V, I, V, I]
+    lib.ki_eval_targets.argtypes = [V, V, I, V, I, I, V, I, V, I]
+    lib.ki_last_error.restype = ctypes.c_char_p
+    lib.ki_version.restype = ctypes.c_char_p
+    for name in EXPORTED:
+        getattr(lib, name)
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _check(rc):
+    if rc != KI_OK:
+        raise KiError(rc, load_library().ki_last_error().decode())
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Factor:
+    """One factorization on the GPU (owns a ki_factor handle)."""
+
+    def __init__(self, points, normals, weights, curvatures=None, id_tol=1e-10,
+                 solution_dimension=1, pde=PDE_LAPLACE, hole_centers=None, hole_start=None,
+                 hole_count=None, max_leaf_dofs=64, num_proxy_points=128, radius_ratio=2.0,
+                 min_dofs_to_compress=64, precision=PRECISION_FP64):
+        lib = load_library()
+        self._keep = [np.ascontiguousarray(points, np.float64).reshape(-1),
+                      np.ascontiguousarray(normals, np.float64).reshape(-1),
+                      np.ascontiguousarray(weights, np.float64).reshape(-1)]
+        self._keep.append(None if curvatures is None else
+                          np.ascontiguousarray(curvatures, np.float64).reshape(-1))
+        nh = 0 if hole_centers is None else int(np.asarray(hole_centers).shape[0])
+        hc = np.ascontiguousarray(hole_centers, np.float64).reshape(-1) if nh else None
+        hs = np.ascontiguousarray(hole_start, np.int32) if nh else None
+        hn = np.ascontiguousarray(hole_count, np.int32) if nh else None
+        self._keep += [hc, hs, hn]
+        n = self._keep[2].shape[0]
+        d = _Desc(n, 2, solution_dimension, pde, _ptr(self._keep[0]), _ptr(self._keep[1]),
+                  _ptr(self._keep[2]), _ptr(self._keep[3]), nh, _ptr(hc), _ptr(hs), _ptr(hn),
+                  max_leaf_dofs, num_proxy_points, radius_ratio, min_dofs_to_compress,
+                  id_tol, precision)
+        h = ctypes.c_void_p()
+        _check(lib.ki_factor_create(ctypes.byref(d), ctypes.byref(h)))
+        self._h = h
+        self.n_dofs = n * solution_dimension
+        self.n_points = n
+        self.solution_dimension = solution_dimension
+        self.n_border = nh * (1 if solution_dimension == 1 else 3)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().ki_factor_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        i = _Info()
+        _check(load_library().ki_factor_get_info(self._h, ctypes.byref(i)))
+        return {f: getattr(i, f) for f, _ in _Info._fields_}
+
+    def solve(self, b):
+        """x (and alpha for holes) with b: (n_dofs,) or (n_dofs, nrhs)."""
+        b = np.asarray(b, np.float64)
+        vec = b.ndim == 1
+        B = np.asfortranarray(b.reshape(self.n_dofs, -1))
+        nrhs = B.shape[1]
+        X = np.zeros_like(B, order="F")
+        A = np.zeros((max(1, self.n_border), nrhs), order="F")
+        _check(load_library().ki_solve(self._h, _ptr(B), self.n_dofs, nrhs, _ptr(X), self.n_dofs,
+                                       _ptr(A), max(1, self.n_border)))
+        x = X[:, 0] if vec else X
+        if self.n_border:
+            return x, (A[:, 0] if vec else A)
+        return x
+
+    def solve_device(self, d_b, d_x, nrhs, d_alpha=0, stream=0):
+        """Device-pointer solve (integers: cudaMalloc'd addresses, column-major)."""
+        _check(load_library().ki_solve_device(self._h, ctypes.c_void_p(d_b), self.n_dofs, nrhs,
+                                              ctypes.c_void_p(d_x), self.n_dofs,
+                                              ctypes.c_void_p(d_alpha) if d_alpha else None,
+                                              max(1, self.n_border),
+                                              ctypes.c_void_p(stream) if stream else None))
+
+    def apply(self, x, alpha=None):
+        """Dense FP64 operator y = K x (+ U alpha) on the GPU."""
+        x = np.asarray(x, np.float64)
+        vec = x.ndim == 1
+        X = np.asfortranarray(x.reshape(self.n_dofs, -1))
+        Y = np.zeros_like(X, order="F")
+        A = None
+        if alpha is not None:
+            A = np.asfortranarray(np.asarray(alpha, np.float64).reshape(self.n_border, -1))
+        _check(load_library().ki_apply(self._h, _ptr(X), self.n_dofs, X.shape[1], _ptr(A),
+                                       max(1, self.n_border), _ptr(Y), self.n_dofs))
+        return Y[:, 0] if vec else Y
+
+    def eval_targets(self, targets, mu, alpha=None):
+        targets = np.ascontiguousarray(targets, np.float64).reshape(-1, 2)
+        mu = np.asarray(mu, np.float64)
+        vec = mu.ndim == 1
+        M = np.asfortranarray(mu.reshape(self.n_dofs, -1))
+        nt = targets.shape[0] * self.solution_dimension
+        out = np.zeros((nt, M.shape[1]), order="F")
+        A = None
+        if alpha is not None:
+            A = np.asfortranarray(np.asarray(alpha, np.float64).reshape(self.n_border, -1))
+        _check(load_library().ki_eval_targets(self._h, _ptr(targets), targets.shape[0], _ptr(M),
+                                              self.n_dofs, M.shape[1], _ptr(A),
+                                              max(1, self.n_border), _ptr(out), nt))
+        return out[:, 0] if vec else out
+
+
+# ----------------------------------------------------------- reference mirror
+
+class Boundary:
+    """Boundary data (kern_interp/boundaries/boundary.h:47-64).  points and
+    normals are interleaved (x, y) per node; holes is a list of
+    (center, node_start, node_count)."""
+
+    def __init__(self, points, normals, weights, curvatures=None, holes=(), boundary_values=None):
+        self.points = np.asarray(points, np.float64).reshape(-1)
+        self.normals = np.asarray(normals, np.float64).reshape(-1)
+        self.weights = np.asarray(weights, np.float64)
+        self.curvatures = None if curvatures is None else np.asarray(curvatures, np.float64)
+        self.holes = list(holes)
+        self.boundary_values = boundary_values
+
+    @classmethod
+    def from_problem(cls, prob, boundary_values=None):
+        holes = [(prob.hole_centers[h], int(prob.hole_start[h]), int(prob.hole_count[h]))
+                 for h in range(prob.n_holes)]
+        return cls(prob.points, prob.normals, prob.weights, prob.curvatures, holes, boundary_values)
+
+
+class Kernel:
+    """Kernel(solution_dimension, domain_dimension, pde, boundary, domain_points)
+    (kern_interp/kernel/kernel.h:38-66)."""
+    LAPLACE, LAPLACE_NEUMANN, GAUSS, STOKES = range(4)
+
+    def __init__(self, solution_dimension, domain_dimension, pde, boundary, domain_points=()):
+        self.solution_dimension = solution_dimension
+        self.domain_dimension = domain_dimension
+        self.pde = pde
+        self.boundary = boundary
+        self.domain_points = np.asarray(domain_points, np.float64).reshape(-1)
+
+
+class QuadTree:
+    """QuadTree::initialize_tree (kern_interp/quadtree/quadtree.h:122-123).
+    The tree itself is built on the factorization path; this object carries
+    the boundary, the parameters the reference fixes as macros, and (after
+    skeletonize) the factorization -- the reference stores its factors in
+    the tree too (quadtree.h:61-63, 118-119)."""
+
+    def __init__(self, max_leaf_dofs=64):
+        self.max_leaf_dofs = max_leaf_dofs
+        self.boundary = None
+        self.factor = None
+
+    def initialize_tree(self, boundary, solution_dimension, domain_dimension):
+        if domain_dimension != 2:
+            raise KiError(KI_ERR_ARG, "only domain_dimension 2 is supported")
+        self.boundary = boundary
+        self.solution_dimension = solution_dimension
+        self.domain_dimension = domain_dimension
+
+
+class SkelFactorization:
+    """SkelFactorization(id_tol, fact_threads) (skel_factorization.h:27).
+    fact_threads is accepted for signature parity and ignored (the GPU
+    processes every box of a level in one launch)."""
+
+    def __init__(self, id_tol, fact_threads=1, num_proxy_points=128, radius_ratio=2.0,
+                 min_dofs_to_compress=64, precision=PRECISION_FP64):
+        self.id_tol = id_tol
+        self.fact_threads = fact_threads
+        self.num_proxy_points = num_proxy_points
+        self.radius_ratio = radius_ratio
+        self.min_dofs_to_compress = min_dofs_to_compress
+        self.precision = precision
+
+    def skeletonize(self, kernel, quadtree):
+        b = quadtree.boundary
+        holes = b.holes
+        hc = np.array([h[0] for h in holes]) if holes else None
+        hs = np.array([h[1] for h in holes], np.int32) if holes else None
+        hn = np.array([h[2] for h in holes], np.int32) if holes else None
+        if quadtree.factor is not None:
+            quadtree.factor.close()
+        quadtree.factor = Factor(b.points, b.normals, b.weights, b.curvatures, self.id_tol,
+                                 kernel.solution_dimension, kernel.pde, hc, hs, hn,
+                                 quadtree.max_leaf_dofs, self.num_proxy_points, self.radius_ratio,
+                                 self.min_dofs_to_compress, self.precision)
+
+    def solve(self, quadtree, b):
+        return quadtree.factor.solve(b)
+
+    def multiply_connected_solve(self, quadtree, b):
+        return quadtree.factor.solve(b)
+
+
+def linear_solve(skel_factorization, quadtree, f):
+    """mu (and alpha when the boundary has holes) (linear_solve.cpp:202-227)."""
+    return quadtree.factor.solve(f)
+
+
+def boundary_integral_solve(kernel, boundary, quadtree, id_tol, fact_threads, domain_points,
+                            **params):
+    """Factor, solve with boundary.boundary_values and evaluate at the domain
+    points (linear_solve.cpp:257-303; without the is_in_domain masking, which
+    needs the reference's concrete Boundary classes)."""
+    skel = SkelFactorization(id_tol, fact_threads, **params)
+    quadtree.initialize_tree(boundary, kernel.solution_dimension, kernel.domain_dimension)
+    skel.skeletonize(kernel, quadtree)
+    res = linear_solve(skel, quadtree, boundary.boundary_values)
+    targets = np.asarray(domain_points, np.float64).reshape(-1, 2)
+    if isinstance(res, tuple):
+        mu, alpha = res
+        return quadtree.factor.eval_targets(targets, mu, alpha)
+    return quadtree.factor.eval_targets(targets, res)
+
+
+from . import geometry  # noqa: E402,F401

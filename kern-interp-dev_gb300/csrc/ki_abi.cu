@@ -1,0 +1,507 @@
+// C ABI (include/ki_gpu.h) over the GPU factorization.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/ki_gpu.h"
+#include "ki_common.cuh"
+#include "ki_factor.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct ArgError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct StateError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+#define KI_CHECK_CUDA(call)                                                              \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      throw std::runtime_error(std::string("CUDA error: ") + cudaGetErrorString(e_));   \
+  } while (0)
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+template <typename F>
+int guarded(F&& f) {
+  try {
+    g_last_error.clear();
+    f();
+    return KI_OK;
+  } catch (const ArgError& e) {
+    return fail(KI_ERR_ARG, e.what());
+  } catch (const StateError& e) {
+    return fail(KI_ERR_STATE, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(KI_ERR_OOM, "host allocation failed");
+  } catch (const std::invalid_argument& e) {
+    return fail(KI_ERR_ARG, e.what());
+  } catch (const std::runtime_error& e) {
+    std::string m = e.what();
+    if (m.find("allocation failed") != std::string::npos || m.find("out of memory") != std::string::npos)
+      return fail(KI_ERR_OOM, m);
+    if (m.find("singular") != std::string::npos || m.find("non-finite") != std::string::npos)
+      return fail(KI_ERR_NUMERIC, m);
+    return fail(KI_ERR_CUDA, m);
+  } catch (...) {
+    return fail(KI_ERR_CUDA, "unknown error");
+  }
+}
+
+// b (column-major, ld) -> x (DOF-major, ld = ncols), with precision change.
+template <typename Tin, typename Tout>
+__global__ void k_to_dofmajor(const Tin* b, int ldb, int n, int ncols, Tout* x) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * ncols;
+       e += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(e % n), c = (int)(e / n);
+    x[(size_t)i * ncols + c] = Tout(b[i + (size_t)ldb * c]);
+  }
+}
+
+template <typename Tin, typename Tout>
+__global__ void k_from_dofmajor(const Tin* x, int n, int ncols, Tout* b, int ldb) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * ncols;
+       e += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(e % n), c = (int)(e / n);
+    b[i + (size_t)ldb * c] = Tout(x[(size_t)i * ncols + c]);
+  }
+}
+
+// alpha (row-major nb x ncols) -> column-major (ld)
+template <typename Tin>
+__global__ void k_alpha_out(const Tin* a, int nb, int ncols, double* out, int ld) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nb * ncols; e += gridDim.x * blockDim.x) {
+    int i = e / ncols, c = e % ncols;
+    out[i + (size_t)ld * c] = double(a[e]);
+  }
+}
+
+// Dense FP64 operator apply y = K x (+ U alpha), one thread per target DOF,
+// sources staged through shared memory.
+constexpr int kApplyThreads = 128;
+constexpr int kApplyTile = 128;
+constexpr int kApplyCols = 8;
+
+__global__ void k_dense_apply(ki::Points<double> P, int n_points, int sol_dim, const double* x,
+                              int ldx, int ncols, double* y, int ldy) {
+  __shared__ double sx[kApplyTile], sy[kApplyTile], snx[kApplyTile], sny[kApplyTile],
+      sw[kApplyTile], sk[kApplyTile];
+  const int N = n_points * sol_dim;
+  const int tdof = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c0 = blockIdx.y * kApplyCols;
+  const int nc = min(kApplyCols, ncols - c0);
+  double acc[kApplyCols];
+  for (int c = 0; c < kApplyCols; c++) acc[c] = 0.0;
+  int tp = tdof < N ? tdof / sol_dim : 0;
+  double tx = P.x[tp], ty = P.y[tp], tnx = P.nx[tp], tny = P.ny[tp];
+  for (int base = 0; base < n_points; base += kApplyTile) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < kApplyTile; i += blockDim.x) {
+      int p = base + i;
+      if (p < n_points) {
+        sx[i] = P.x[p]; sy[i] = P.y[p]; snx[i] = P.nx[p]; sny[i] = P.ny[p]; sw[i] = P.w[p];
+        sk[i] = P.kappa[p];
+      }
+    }
+    __syncthreads();
+    if (tdof >= N) continue;
+    int lim = min(kApplyTile, n_points - base);
+    for (int i = 0; i < lim; i++) {
+      for (int sp = 0; sp < sol_dim; sp++) {
+        int sdof = (base + i) * sol_dim + sp;
+        double kv;
+        if (sol_dim == 1)
+          kv = ki::laplace_entry<double>(tx, ty, sx[i], sy[i], snx[i], sny[i], sw[i], sk[i]);
+        else
+          kv = ki::stokes_entry<double>(tdof & 1, sp, tx, ty, tnx, tny, sx[i], sy[i], snx[i],
+                                        sny[i], sw[i], sk[i]);
+        for (int c = 0; c < nc; c++) acc[c] += kv * x[sdof + (size_t)ldx * (c0 + c)];
+      }
+    }
+  }
+  if (tdof < N)
+    for (int c = 0; c < nc; c++) y[tdof + (size_t)ldy * (c0 + c)] = acc[c];
+}
+
+// Forward evaluation at domain targets (target normal 0, reference forward
+// mode), plus the border term.
+__global__ void k_forward(ki::Points<double> P, int n_points, int sol_dim, const double* tg,
+                          int nt, const double* mu, int ldmu, int ncols, double* out, int ldout) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int NT = nt * sol_dim;
+  if (t >= NT) return;
+  int tp = t / sol_dim;
+  double tx = tg[2 * tp], ty = tg[2 * tp + 1];
+  for (int c = 0; c < ncols; c++) {
+    double acc = 0.0;
+    for (int p = 0; p < n_points; p++) {
+      for (int sp = 0; sp < sol_dim; sp++) {
+        double kv;
+        if (sol_dim == 1)
+          kv = ki::laplace_entry<double>(tx, ty, P.x[p], P.y[p], P.nx[p], P.ny[p], P.w[p], P.kappa[p]);
+        else
+          kv = ki::stokes_entry<double>(t & 1, sp, tx, ty, 0.0, 0.0, P.x[p], P.y[p], P.nx[p],
+                                        P.ny[p], P.w[p], P.kappa[p]);
+        acc += kv * mu[p * sol_dim + sp + (size_t)ldmu * c];
+      }
+    }
+    out[t + (size_t)ldout * c] = acc;
+  }
+}
+
+// U alpha for Laplace holes (initialize_U_mat, linear_solve.cpp:37-45:
+// U(i, h) = log|x_i - c_h|) and Stokes 2D (:77-97).
+__global__ void k_border_apply(const double* px, const double* py, int stride, int n_points, int sol_dim,
+                               const double* hc, int nh, const double* alpha, int lda, int ncols,
+                               double* y, int ldy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_points) return;
+  for (int c = 0; c < ncols; c++) {
+    double a0 = 0, a1 = 0;
+    for (int h = 0; h < nh; h++) {
+      double rx = px[(size_t)stride * i] - hc[2 * h], ry = py[(size_t)stride * i] - hc[2 * h + 1];
+      double rn = sqrt(rx * rx + ry * ry);
+      if (sol_dim == 1) {
+        a0 += log(rn) * alpha[h + (size_t)lda * c];
+      } else {
+        double sc = 1.0 / (4 * ki::kPi), r2 = rn * rn;
+        const double* al = alpha + 3 * h + (size_t)lda * c;
+        a0 += sc * (log(1 / rn) + rx * rx / r2) * al[0] + sc * (rx * ry / r2) * al[1] + ry * (sc / r2) * al[2];
+        a1 += sc * (ry * rx / r2) * al[0] + sc * (log(1 / rn) + ry * ry / r2) * al[1] - rx * (sc / r2) * al[2];
+      }
+    }
+    if (sol_dim == 1) {
+      y[i + (size_t)ldy * c] += a0;
+    } else {
+      y[2 * i + (size_t)ldy * c] += a0;
+      y[2 * i + 1 + (size_t)ldy * c] += a1;
+    }
+  }
+}
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  cudaStream_t s = nullptr;
+  DevBuf(size_t n, cudaStream_t st) : s(st) {
+    cudaError_t e = cudaMallocAsync((void**)&p, sizeof(T) * (n ? n : 1), st);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      throw std::runtime_error("device allocation failed");
+    }
+  }
+  ~DevBuf() {
+    if (p) cudaFreeAsync(p, s);
+  }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+};
+
+int grid_for(size_t n) { return (int)std::min<size_t>(4096, (n + 255) / 256 + 1); }
+
+}  // namespace
+
+struct ki_factor {
+  int precision = KI_PRECISION_FP64;
+  int sol_dim = 1;
+  int n_points = 0;
+  int n_dofs = 0;
+  int n_holes = 0;
+  int n_border = 0;
+  cudaStream_t stream = nullptr;
+  std::unique_ptr<ki::Factorization<double>> f64;
+  std::unique_ptr<ki::Factorization<float>> f32;
+  // FP64 geometry on the device (apply / evaluation)
+  double* d_geo = nullptr;
+  double* d_holes = nullptr;
+  ki::Points<double> P{};
+  ~ki_factor() {
+    f64.reset();
+    f32.reset();
+    if (d_geo) cudaFree(d_geo);
+    if (d_holes) cudaFree(d_holes);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+template <typename T>
+void solve_impl(ki_factor* f, ki::Factorization<T>& F, const double* d_b, int ldb, int nrhs,
+                double* d_x, int ldx, double* d_alpha, int ldalpha, cudaStream_t s) {
+  const int N = f->n_dofs;
+  DevBuf<T> work((size_t)N * nrhs, s);
+  DevBuf<T> al((size_t)std::max(1, f->n_border) * nrhs, s);
+  k_to_dofmajor<double, T><<<grid_for((size_t)N * nrhs), 256, 0, s>>>(d_b, ldb, N, nrhs, work.p);
+  KI_CHECK_CUDA(cudaGetLastError());
+  cudaStream_t saved = F.stream;
+  F.stream = s;
+  try {
+    ki::solve_device<T>(F, work.p, nrhs, al.p);
+  } catch (...) {
+    F.stream = saved;
+    throw;
+  }
+  F.stream = saved;
+  k_from_dofmajor<T, double><<<grid_for((size_t)N * nrhs), 256, 0, s>>>(work.p, N, nrhs, d_x, ldx);
+  KI_CHECK_CUDA(cudaGetLastError());
+  if (f->n_border > 0 && d_alpha) {
+    k_alpha_out<T><<<grid_for((size_t)f->n_border * nrhs), 256, 0, s>>>(al.p, f->n_border, nrhs,
+                                                                       d_alpha, ldalpha);
+    KI_CHECK_CUDA(cudaGetLastError());
+  }
+}
+
+void check_desc(const ki_problem_desc* d) {
+  if (!d) throw ArgError("desc is NULL");
+  if (d->domain_dimension != 2) throw ArgError("only domain_dimension 2 is supported");
+  if (d->n_points <= 0) throw ArgError("n_points must be positive");
+  if (!d->points || !d->normals || !d->weights) throw ArgError("points/normals/weights must be non-NULL");
+  if (d->pde == KI_PDE_LAPLACE) {
+    if (d->solution_dimension != 1) throw ArgError("Laplace needs solution_dimension 1");
+  } else if (d->pde == KI_PDE_STOKES) {
+    if (d->solution_dimension != 2) throw ArgError("Stokes (2D) needs solution_dimension 2");
+  } else {
+    throw ArgError("pde must be KI_PDE_LAPLACE or KI_PDE_STOKES");
+  }
+  if (!(d->id_tol > 0) || !std::isfinite(d->id_tol)) throw ArgError("id_tol must be positive");
+  if (d->precision != KI_PRECISION_FP64 && d->precision != KI_PRECISION_FP32)
+    throw ArgError("unknown precision");
+  if (d->n_holes < 0) throw ArgError("n_holes must be >= 0");
+  if (d->n_holes > 0 && (!d->hole_centers || !d->hole_node_start || !d->hole_node_count))
+    throw ArgError("hole arrays must be non-NULL when n_holes > 0");
+  for (int h = 0; h < d->n_holes; h++) {
+    int s = d->hole_node_start[h], c = d->hole_node_count[h];
+    if (s < 0 || c <= 0 || s + c > d->n_points) throw ArgError("hole node range out of bounds");
+  }
+  for (long i = 0; i < 2L * d->n_points; i++)
+    if (!std::isfinite(d->points[i]) || !std::isfinite(d->normals[i]))
+      throw ArgError("non-finite point or normal");
+  for (int i = 0; i < d->n_points; i++) {
+    if (!std::isfinite(d->weights[i])) throw ArgError("non-finite weight");
+    if (d->curvatures && !std::isfinite(d->curvatures[i])) throw ArgError("non-finite curvature");
+  }
+  if (d->max_leaf_dofs < 0 || d->num_proxy_points < 0 || d->min_dofs_to_compress < 0 ||
+      d->radius_ratio < 0)
+    throw ArgError("tree/proxy parameters must be >= 0 (0 = reference default)");
+}
+
+}  // namespace
+
+extern "C" {
+
+int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
+  return guarded([&] {
+    if (!out) throw ArgError("out is NULL");
+    *out = nullptr;
+    check_desc(desc);
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
+      cudaGetLastError();
+      throw std::runtime_error("no CUDA device available");
+    }
+    std::unique_ptr<ki_factor> f(new ki_factor());
+    f->precision = desc->precision;
+    f->sol_dim = desc->solution_dimension;
+    f->n_points = desc->n_points;
+    f->n_dofs = desc->n_points * desc->solution_dimension;
+    f->n_holes = desc->n_holes;
+    f->n_border = desc->n_holes * (desc->solution_dimension == 1 ? 1 : 3);
+    KI_CHECK_CUDA(cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking));
+    ki::Params prm;
+    prm.sol_dim = desc->solution_dimension;
+    prm.max_leaf_dofs = desc->max_leaf_dofs ? desc->max_leaf_dofs : 64;
+    prm.num_proxy_points = desc->num_proxy_points ? desc->num_proxy_points : 128;
+    prm.radius_ratio = desc->radius_ratio > 0 ? desc->radius_ratio : 2.0;
+    prm.min_dofs_to_compress = desc->min_dofs_to_compress ? desc->min_dofs_to_compress : 64;
+    prm.id_tol = desc->id_tol;
+    ki::HoleDesc holes;
+    holes.n_holes = desc->n_holes;
+    for (int h = 0; h < desc->n_holes; h++) {
+      holes.centers.push_back(desc->hole_centers[2 * h]);
+      holes.centers.push_back(desc->hole_centers[2 * h + 1]);
+      holes.start.push_back(desc->hole_node_start[h]);
+      holes.count.push_back(desc->hole_node_count[h]);
+    }
+    // FP64 geometry for apply / evaluation (SoA)
+    const int n = desc->n_points;
+    std::vector<double> geo((size_t)6 * n);
+    for (int i = 0; i < n; i++) {
+      geo[i] = desc->points[2 * i];
+      geo[n + i] = desc->points[2 * i + 1];
+      geo[2 * (size_t)n + i] = desc->normals[2 * i];
+      geo[3 * (size_t)n + i] = desc->normals[2 * i + 1];
+      geo[4 * (size_t)n + i] = desc->weights[i];
+      geo[5 * (size_t)n + i] = desc->curvatures ? desc->curvatures[i] : 0.0;
+    }
+    KI_CHECK_CUDA(cudaMalloc(&f->d_geo, sizeof(double) * geo.size()));
+    KI_CHECK_CUDA(cudaMemcpy(f->d_geo, geo.data(), sizeof(double) * geo.size(), cudaMemcpyHostToDevice));
+    f->P = ki::Points<double>{f->d_geo, f->d_geo + n, f->d_geo + 2 * (size_t)n,
+                              f->d_geo + 3 * (size_t)n, f->d_geo + 4 * (size_t)n,
+                              f->d_geo + 5 * (size_t)n};
+    if (desc->n_holes > 0) {
+      KI_CHECK_CUDA(cudaMalloc(&f->d_holes, sizeof(double) * 2 * desc->n_holes));
+      KI_CHECK_CUDA(cudaMemcpy(f->d_holes, desc->hole_centers, sizeof(double) * 2 * desc->n_holes,
+                               cudaMemcpyHostToDevice));
+    }
+    if (f->precision == KI_PRECISION_FP64)
+      f->f64 = ki::factorize<double>(prm, n, desc->points, desc->normals, desc->weights,
+                                     desc->curvatures, holes, f->stream);
+    else
+      f->f32 = ki::factorize<float>(prm, n, desc->points, desc->normals, desc->weights,
+                                    desc->curvatures, holes, f->stream);
+    *out = f.release();
+  });
+}
+
+int ki_factor_destroy(ki_factor* f) {
+  return guarded([&] { delete f; });
+}
+
+int ki_factor_get_info(const ki_factor* f, ki_factor_info* info) {
+  return guarded([&] {
+    if (!f || !info) throw ArgError("NULL argument");
+    std::memset(info, 0, sizeof(*info));
+    info->n_dofs = f->n_dofs;
+    info->n_border = f->n_border;
+    auto fill = [&](const auto& F) {
+      info->n_levels = F.tree.num_levels();
+      info->n_compressed = F.n_compressed;
+      info->n_redundant = F.n_redundant;
+      info->n_root = F.n_root;
+      info->factor_seconds = F.factor_seconds;
+      info->device_bytes = (long)F.device_bytes;
+    };
+    if (f->f64) fill(*f->f64);
+    if (f->f32) fill(*f->f32);
+  });
+}
+
+int ki_solve_device(ki_factor* f, const double* d_b, int ldb, int nrhs, double* d_x, int ldx,
+                    double* d_alpha, int ldalpha, void* stream) {
+  return guarded([&] {
+    if (!f) throw ArgError("factor is NULL");
+    if (nrhs < 0 || ldb < f->n_dofs || ldx < f->n_dofs) throw ArgError("bad leading dimension / nrhs");
+    if (f->n_border > 0 && d_alpha && ldalpha < f->n_border) throw ArgError("bad ldalpha");
+    if (nrhs == 0) return;
+    if (!d_b || !d_x) throw ArgError("NULL b or x");
+    cudaStream_t s = stream ? (cudaStream_t)stream : f->stream;
+    if (f->f64) solve_impl<double>(f, *f->f64, d_b, ldb, nrhs, d_x, ldx, d_alpha, ldalpha, s);
+    else solve_impl<float>(f, *f->f32, d_b, ldb, nrhs, d_x, ldx, d_alpha, ldalpha, s);
+  });
+}
+
+int ki_solve(ki_factor* f, const double* b, int ldb, int nrhs, double* x, int ldx, double* alpha,
+             int ldalpha) {
+  return guarded([&] {
+    if (!f) throw ArgError("factor is NULL");
+    if (nrhs < 0 || ldb < f->n_dofs || ldx < f->n_dofs) throw ArgError("bad leading dimension / nrhs");
+    if (f->n_border > 0 && alpha && ldalpha < f->n_border) throw ArgError("bad ldalpha");
+    if (nrhs == 0) return;
+    if (!b || !x) throw ArgError("NULL b or x");
+    cudaStream_t s = f->stream;
+    const int N = f->n_dofs;
+    DevBuf<double> db((size_t)N * nrhs, s), dx((size_t)N * nrhs, s);
+    DevBuf<double> da((size_t)std::max(1, f->n_border) * nrhs, s);
+    KI_CHECK_CUDA(cudaMemcpy2DAsync(db.p, sizeof(double) * N, b, sizeof(double) * ldb,
+                                    sizeof(double) * N, nrhs, cudaMemcpyHostToDevice, s));
+    if (f->f64) solve_impl<double>(f, *f->f64, db.p, N, nrhs, dx.p, N, da.p, f->n_border, s);
+    else solve_impl<float>(f, *f->f32, db.p, N, nrhs, dx.p, N, da.p, f->n_border, s);
+    KI_CHECK_CUDA(cudaMemcpy2DAsync(x, sizeof(double) * ldx, dx.p, sizeof(double) * N,
+                                    sizeof(double) * N, nrhs, cudaMemcpyDeviceToHost, s));
+    if (f->n_border > 0 && alpha)
+      KI_CHECK_CUDA(cudaMemcpy2DAsync(alpha, sizeof(double) * ldalpha, da.p,
+                                      sizeof(double) * f->n_border, sizeof(double) * f->n_border,
+                                      nrhs, cudaMemcpyDeviceToHost, s));
+    KI_CHECK_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ki_apply(ki_factor* f, const double* x, int ldx, int ncols, const double* alpha, int ldalpha,
+             double* y, int ldy) {
+  return guarded([&] {
+    if (!f || !x || !y) throw ArgError("NULL argument");
+    const int N = f->n_dofs;
+    if (ncols < 0 || ldx < N || ldy < N) throw ArgError("bad leading dimension / ncols");
+    if (ncols == 0) return;
+    cudaStream_t s = f->stream;
+    DevBuf<double> dx((size_t)N * ncols, s), dy((size_t)N * ncols, s);
+    KI_CHECK_CUDA(cudaMemcpy2DAsync(dx.p, sizeof(double) * N, x, sizeof(double) * ldx,
+                                    sizeof(double) * N, ncols, cudaMemcpyHostToDevice, s));
+    dim3 grid((N + kApplyThreads - 1) / kApplyThreads, (ncols + kApplyCols - 1) / kApplyCols);
+    k_dense_apply<<<grid, kApplyThreads, 0, s>>>(f->P, f->n_points, f->sol_dim, dx.p, N, ncols, dy.p, N);
+    KI_CHECK_CUDA(cudaGetLastError());
+    if (f->n_border > 0 && alpha) {
+      if (ldalpha < f->n_border) throw ArgError("bad ldalpha");
+      DevBuf<double> da((size_t)f->n_border * ncols, s);
+      KI_CHECK_CUDA(cudaMemcpy2DAsync(da.p, sizeof(double) * f->n_border, alpha,
+                                      sizeof(double) * ldalpha, sizeof(double) * f->n_border,
+                                      ncols, cudaMemcpyHostToDevice, s));
+      k_border_apply<<<(f->n_points + 127) / 128, 128, 0, s>>>(
+          f->P.x, f->P.y, 1, f->n_points, f->sol_dim, f->d_holes, f->n_holes, da.p, f->n_border,
+          ncols, dy.p, N);
+      KI_CHECK_CUDA(cudaGetLastError());
+      KI_CHECK_CUDA(cudaMemcpy2DAsync(y, sizeof(double) * ldy, dy.p, sizeof(double) * N,
+                                      sizeof(double) * N, ncols, cudaMemcpyDeviceToHost, s));
+      KI_CHECK_CUDA(cudaStreamSynchronize(s));
+      return;
+    }
+    KI_CHECK_CUDA(cudaMemcpy2DAsync(y, sizeof(double) * ldy, dy.p, sizeof(double) * N,
+                                    sizeof(double) * N, ncols, cudaMemcpyDeviceToHost, s));
+    KI_CHECK_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ki_eval_targets(ki_factor* f, const double* targets, int n_targets, const double* mu, int ldmu,
+                    int ncols, const double* alpha, int ldalpha, double* out, int ldout) {
+  return guarded([&] {
+    if (!f || !targets || !mu || !out) throw ArgError("NULL argument");
+    const int N = f->n_dofs;
+    const int NT = n_targets * f->sol_dim;
+    if (n_targets < 0 || ncols < 0 || ldmu < N || ldout < NT) throw ArgError("bad sizes");
+    if (n_targets == 0 || ncols == 0) return;
+    cudaStream_t s = f->stream;
+    DevBuf<double> dt((size_t)2 * n_targets, s), dm((size_t)N * ncols, s), dout((size_t)NT * ncols, s);
+    KI_CHECK_CUDA(cudaMemcpyAsync(dt.p, targets, sizeof(double) * 2 * n_targets, cudaMemcpyHostToDevice, s));
+    KI_CHECK_CUDA(cudaMemcpy2DAsync(dm.p, sizeof(double) * N, mu, sizeof(double) * ldmu,
+                                    sizeof(double) * N, ncols, cudaMemcpyHostToDevice, s));
+    k_forward<<<(NT + 127) / 128, 128, 0, s>>>(f->P, f->n_points, f->sol_dim, dt.p, n_targets, dm.p,
+                                               N, ncols, dout.p, NT);
+    KI_CHECK_CUDA(cudaGetLastError());
+    if (f->n_border > 0 && alpha) {
+      if (ldalpha < f->n_border) throw ArgError("bad ldalpha");
+      DevBuf<double> da((size_t)f->n_border * ncols, s);
+      KI_CHECK_CUDA(cudaMemcpy2DAsync(da.p, sizeof(double) * f->n_border, alpha,
+                                      sizeof(double) * ldalpha, sizeof(double) * f->n_border,
+                                      ncols, cudaMemcpyHostToDevice, s));
+      k_border_apply<<<(n_targets + 127) / 128, 128, 0, s>>>(dt.p, dt.p + 1, 2, n_targets, f->sol_dim,
+                                                             f->d_holes, f->n_holes, da.p,
+                                                             f->n_border, ncols, dout.p, NT);
+      KI_CHECK_CUDA(cudaGetLastError());
+      KI_CHECK_CUDA(cudaStreamSynchronize(s));
+    }
+    KI_CHECK_CUDA(cudaMemcpy2DAsync(out, sizeof(double) * ldout, dout.p, sizeof(double) * NT,
+                                    sizeof(double) * NT, ncols, cudaMemcpyDeviceToHost, s));
+    KI_CHECK_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+const char* ki_last_error(void) { return g_last_error.c_str(); }
+
+const char* ki_version(void) { return "kern-interp-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

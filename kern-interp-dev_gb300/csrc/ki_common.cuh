@@ -1,0 +1,182 @@
+// Shared device-side definitions: point data, the Nystrom kernel entries and
+// small CTA-cooperative dense linear-algebra helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace ki {
+
+// Point data, structure-of-arrays, resident in HBM for the whole factorization.
+template <typename T>
+struct Points {
+  const T* x;
+  const T* y;
+  const T* nx;
+  const T* ny;
+  const T* w;
+  const T* kappa;
+};
+
+constexpr double kPi = 3.14159265358979323846;
+
+// Nystrom entry K(target dof, source dof) of the 2D double-layer kernels.
+// Laplace: Kernel::one_d_kern (kern_interp/kernel/kernel.cpp:33-43);
+// Stokes:  Kernel::two_d_kern (kern_interp/kernel/kernel.cpp:65-87).
+// r = t - s; an exactly coincident pair takes the diagonal limit.
+template <typename T>
+__device__ __forceinline__ T laplace_entry(T tx, T ty, T sx, T sy, T snx, T sny, T sw, T sk) {
+  T r1 = tx - sx, r2 = ty - sy;
+  if (r1 == T(0) && r2 == T(0)) return T(0.5) + T(0.5) * sk * sw * T(1.0 / (2 * kPi));
+  return -sw * T(1.0 / (2 * kPi)) * (r1 * snx + r2 * sny) / (r1 * r1 + r2 * r2);
+}
+
+template <typename T>
+__device__ __forceinline__ T stokes_entry(int tpar, int spar, T tx, T ty, T tnx, T tny, T sx,
+                                          T sy, T snx, T sny, T sw, T sk) {
+  T r1 = tx - sx, r2 = ty - sy;
+  T sn[2] = {snx, sny};
+  T tn[2] = {tnx, tny};
+  int is_diag = (tpar + spar + 1) % 2;
+  if (r1 == T(0) && r2 == T(0)) {
+    return T(-0.5) * T(is_diag) +
+           T(1 - 2 * is_diag) * T(0.5) * sk * sw * T(1.0 / kPi) * sn[(tpar + 1) % 2] *
+               sn[(spar + 1) % 2] +
+           sw * tn[tpar] * sn[spar];
+  }
+  T r[2] = {r1, r2};
+  T rr = r1 * r1 + r2 * r2;
+  return sw * T(1.0 / kPi) * (r1 * snx + r2 * sny) / (rr * rr) * r[tpar] * r[spar] +
+         sw * tn[tpar] * sn[spar];
+}
+
+// Entry between two boundary DOFs (sol_dim 1: Laplace, 2: Stokes).
+template <typename T>
+__device__ __forceinline__ T kernel_entry(const Points<T>& P, int sol_dim, int tdof, int sdof) {
+  if (sol_dim == 1) {
+    return laplace_entry<T>(P.x[tdof], P.y[tdof], P.x[sdof], P.y[sdof], P.nx[sdof], P.ny[sdof],
+                            P.w[sdof], P.kappa[sdof]);
+  }
+  int tp = tdof >> 1, sp = sdof >> 1;
+  return stokes_entry<T>(tdof & 1, sdof & 1, P.x[tp], P.y[tp], P.nx[tp], P.ny[tp], P.x[sp],
+                         P.y[sp], P.nx[sp], P.ny[sp], P.w[sp], P.kappa[sp]);
+}
+
+// ------------------------------------------------------------------------
+// CTA-cooperative dense helpers on column-major matrices (shared or global
+// memory).  All threads of the block must call them.
+
+// C(m x n) = beta*C + alpha * op(A) * op(B); op(A) is m x kk.
+template <typename T>
+__device__ void cta_gemm(int m, int n, int kk, T alpha, const T* A, int lda, bool ta,
+                         const T* B, int ldb, bool tb, T beta, T* C, int ldc) {
+  for (int idx = threadIdx.x; idx < m * n; idx += blockDim.x) {
+    int i = idx % m, j = idx / m;
+    T acc = T(0);
+    for (int l = 0; l < kk; l++) {
+      T a = ta ? A[l + (size_t)lda * i] : A[i + (size_t)lda * l];
+      T b = tb ? B[j + (size_t)ldb * l] : B[l + (size_t)ldb * j];
+      acc += a * b;
+    }
+    C[i + (size_t)ldc * j] = (beta == T(0) ? T(0) : beta * C[i + (size_t)ldc * j]) + alpha * acc;
+  }
+}
+
+// In-place LU with partial pivoting (dgetrf semantics, 0-based pivots:
+// row i was swapped with piv[i]).  Returns the first zero pivot + 1, or 0.
+template <typename T>
+__device__ int cta_lu(int n, T* A, int lda, int* piv, int* s_flag, T* s_red, int* s_idx) {
+  int info = 0;
+  for (int j = 0; j < n; j++) {
+    // pivot search: warp 0 scans rows j..n-1
+    if (threadIdx.x < 32) {
+      T best = T(-1);
+      int bi = j;
+      for (int i = j + threadIdx.x; i < n; i += 32) {
+        T v = fabs(A[i + (size_t)lda * j]);
+        if (v > best) { best = v; bi = i; }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        T ov = __shfl_down_sync(0xffffffff, best, o);
+        int oi = __shfl_down_sync(0xffffffff, bi, o);
+        if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+      }
+      if (threadIdx.x == 0) { *s_idx = bi; *s_red = best; }
+    }
+    __syncthreads();
+    int p = *s_idx;
+    T pv = *s_red;
+    if (threadIdx.x == 0) piv[j] = p;
+    if (p != j) {
+      for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        T t = A[j + (size_t)lda * c];
+        A[j + (size_t)lda * c] = A[p + (size_t)lda * c];
+        A[p + (size_t)lda * c] = t;
+      }
+    }
+    __syncthreads();
+    if (pv == T(0)) {
+      if (info == 0) info = j + 1;
+      continue;
+    }
+    T d = A[j + (size_t)lda * j];
+    for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) A[i + (size_t)lda * j] /= d;
+    __syncthreads();
+    int rows = n - j - 1;
+    for (int idx = threadIdx.x; idx < rows * rows; idx += blockDim.x) {
+      int i = j + 1 + idx % rows, c = j + 1 + idx / rows;
+      A[i + (size_t)lda * c] -= A[i + (size_t)lda * j] * A[j + (size_t)lda * c];
+    }
+    __syncthreads();
+  }
+  (void)s_flag;
+  return info;
+}
+
+// B(n x nrhs) <- A^-1 B (trans=false) or A^-T B (trans=true) from cta_lu.
+template <typename T>
+__device__ void cta_lu_solve(int n, const T* LU, int lda, const int* piv, bool trans, T* B,
+                             int ldb, int nrhs) {
+  if (!trans) {
+    // apply row swaps, forward (unit L), backward (U); one thread per column
+    for (int c = threadIdx.x; c < nrhs; c += blockDim.x) {
+      T* b = B + (size_t)ldb * c;
+      for (int i = 0; i < n; i++) {
+        int p = piv[i];
+        if (p != i) { T t = b[i]; b[i] = b[p]; b[p] = t; }
+      }
+      for (int i = 0; i < n; i++) {
+        T s = b[i];
+        for (int l = 0; l < i; l++) s -= LU[i + (size_t)lda * l] * b[l];
+        b[i] = s;
+      }
+      for (int i = n - 1; i >= 0; i--) {
+        T s = b[i];
+        for (int l = i + 1; l < n; l++) s -= LU[i + (size_t)lda * l] * b[l];
+        b[i] = s / LU[i + (size_t)lda * i];
+      }
+    }
+  } else {
+    // A^T = U^T L^T P : solve U^T y = b, L^T z = y, then undo swaps reversed
+    for (int c = threadIdx.x; c < nrhs; c += blockDim.x) {
+      T* b = B + (size_t)ldb * c;
+      for (int i = 0; i < n; i++) {
+        T s = b[i];
+        for (int l = 0; l < i; l++) s -= LU[l + (size_t)lda * i] * b[l];
+        b[i] = s / LU[i + (size_t)lda * i];
+      }
+      for (int i = n - 1; i >= 0; i--) {
+        T s = b[i];
+        for (int l = i + 1; l < n; l++) s -= LU[l + (size_t)lda * i] * b[l];
+        b[i] = s;
+      }
+      for (int i = n - 1; i >= 0; i--) {
+        int p = piv[i];
+        if (p != i) { T t = b[i]; b[i] = b[p]; b[p] = t; }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+}  // namespace ki

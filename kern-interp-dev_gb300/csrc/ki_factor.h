@@ -1,0 +1,90 @@
+// GPU recursive-skeletonization factorization: host-side orchestration.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "ki_tree.h"
+
+namespace ki {
+
+struct Params {
+  int sol_dim = 1;            // 1: Laplace, 2: Stokes (2D)
+  int max_leaf_dofs = 64;     // MAX_LEAF_DOFS
+  int num_proxy_points = 128; // NUM_PROXY_POINTS
+  double radius_ratio = 2.0;  // RADIUS_RATIO: proxy radius = ratio*sqrt(2)*side/2
+  int min_dofs_to_compress = 64;
+  double id_tol = 1e-10;
+};
+
+// Device status word written by kernels that can fail (non-finite data,
+// singular pivot); read back by the host after each stage.
+enum DeviceError : int { kDevOk = 0, kDevNonFinite = 1, kDevSingular = 2 };
+
+// Per-level description of the compressed boxes, kept for the solve sweeps.
+struct LevelFactor {
+  int n_comp = 0;          // compressed boxes in this level
+  void* d_tasks = nullptr; // device array of per-box sweep descriptors
+  int max_n = 0;           // largest active set among them
+};
+
+template <typename T>
+struct Factorization {
+  Params prm;
+  Tree tree;
+  cudaStream_t stream = nullptr;
+  int N = 0;           // DOFs
+  int n_points = 0;
+  // point data (device, SoA, precision T)
+  T *d_x = nullptr, *d_y = nullptr, *d_nx = nullptr, *d_ny = nullptr, *d_w = nullptr,
+    *d_kappa = nullptr;
+  std::vector<LevelFactor> levels;   // index = tree level
+  // root
+  int n_root = 0;
+  int* d_root_idx = nullptr;  // allskel DOF list
+  T* d_root_lu = nullptr;     // LU of the root block (or the bordered S)
+  int* d_root_piv = nullptr;
+  int n_border = 0;           // border columns (holes x c)
+  int n_root_sys = 0;         // n_root + n_border
+  // bordered data (multiply connected)
+  T* d_Umod = nullptr;        // N x nb, DOF-major: swept U
+  T* d_PsiTmod = nullptr;     // N x nb, DOF-major: swept Psi^T
+  unsigned char* d_is_skel = nullptr;  // N flags
+  int* d_err = nullptr;       // device status word
+  // statistics
+  int n_compressed = 0;
+  long n_redundant = 0;
+  std::vector<int> rank_hist;
+  double factor_seconds = 0;
+  size_t device_bytes = 0;
+  std::vector<void*> owned;   // device allocations to free
+
+  ~Factorization();
+  void* alloc(size_t bytes);
+};
+
+struct HoleDesc {
+  int n_holes = 0;
+  std::vector<double> centers;   // 2 per hole
+  std::vector<int> start, count; // node ranges
+};
+
+// Build the tree and skeletonize on `stream`.  Throws std::runtime_error on
+// failure (message says which stage).
+template <typename T>
+std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, const double* points,
+                                            const double* normals, const double* weights,
+                                            const double* curvatures, const HoleDesc& holes,
+                                            cudaStream_t stream);
+
+// Solve with the factorization: x (device, DOF-major N x ncols, ld = ncols)
+// is overwritten with the solution; alpha (device, n_border x ncols,
+// row-major) receives the border unknowns of a multiply connected problem.
+template <typename T>
+void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha);
+
+}  // namespace ki
