@@ -1,0 +1,371 @@
+"""Benchmark: recursive-skeletonization factor + solve on one GB300.
+
+Workload (default): 2D Laplace Dirichlet double-layer BIE on the disc of
+radius 2 minus 64 ellipses (semi-axes U(0.02, 0.06), seed 1), 16-node
+Gauss-Legendre panels, 1,048,576 unknowns, ID tolerance 1e-8, 32 right-hand
+sides from unit point sources at |y| in [2.5, 4] (seed 2).  One step = one
+factorization (tree + skeletonization + bordered system) and one solve of all
+32 right-hand sides.  Metric: DOF/s = unknowns x right-hand sides / step time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--precision fp64|fp32] [--n UNKNOWNS] [--nrhs R] [--tol T]
+
+`value` is timed with the right-hand sides resident in HBM (ki_solve_device);
+`e2e` through the host-buffer C-ABI call (ki_solve), host<->device copies of
+the right-hand sides and solutions inside the timed region.  --impl reference
+times the CPU oracle (a C++ restatement of the reference's factor and solve,
+linked to OpenBLAS) on the host cores.  With N > 1 (torchrun) every rank
+factors and solves its own copy of the problem (replicas; the path has no
+exchange step), rank 0 prints the line.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--holes", type=int, default=64)
+    ap.add_argument("--nrhs", type=int, default=32)
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--residual-rows", type=int, default=2048)
+    ap.add_argument("--cpu-sample-n", type=int, default=1 << 18)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_problem(pkg, n, holes, nrhs):
+    g = pkg.geometry
+    prob = g.disc_with_ellipses(n, holes, seed=1)
+    rng = np.random.default_rng(2)
+    src = g.random_sources(nrhs, rng)
+    rhs = g.laplace_source_rhs(prob, src)
+    return prob, src, rhs
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for nm, v in zip(names, s[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.samples)}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def residual_sample(fac, prob, rhs, mu, alpha, nrows, seed=9):
+    """Relative residual ||K mu + U alpha - f|| / ||f|| estimated from a
+    uniform sample of rows with the dense FP64 operator."""
+    N = rhs.shape[0]
+    rng = np.random.default_rng(seed)
+    rows = np.sort(rng.choice(N, size=min(nrows, N), replace=False)).astype(np.int32)
+    y = fac.apply_rows(rows, mu, alpha)
+    r = y - rhs[rows]
+    est = np.sqrt(N / rows.size * (r ** 2).sum(0)) / np.linalg.norm(rhs, axis=0)
+    return float(est.max()), float(np.median(est))
+
+
+def cpu_oracle_run(prob, rhs, tol, threads):
+    import oracle
+    t0 = time.perf_counter()
+    mu, alpha, st = oracle.solve(prob, rhs, tol, threads=threads)
+    t1 = time.perf_counter()
+    return t1 - t0, st, mu, alpha
+
+
+def run_reference(args, rank, world):
+    """CPU arm: the oracle port on the host cores (all threads)."""
+    import __graft_entry__ as g
+    pkg = g.load_package()
+    if rank != 0:
+        return
+    import oracle
+    oracle.build_port()
+    threads = os.cpu_count() or 1
+    n = min(args.n, args.cpu_sample_n)
+    prob, src, rhs = make_problem(pkg, n, args.holes, args.nrhs)
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_oracle_run(prob, rhs, args.tol, threads)
+    times = []
+    for _ in range(args.steps):
+        dt, st, _, _ = cpu_oracle_run(prob, rhs, args.tol, threads)
+        times.append(dt)
+    t = float(np.mean(times))
+    value = n * args.nrhs / t
+    line = {
+        "metric": "factor+solve DOF/s (unknowns x rhs / s) at ID tol %g" % args.tol,
+        "value": value, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": "laplace2d_disc_minus_%d_ellipses" % args.holes,
+                   "unknowns": n, "nrhs": args.nrhs, "id_tol": args.tol,
+                   "full_workload_unknowns": args.n},
+        "cpu_baseline": {"value": value, "unit": "DOF/s", "cores": threads, "kind": "port",
+                         "sample": "%d unknowns (the full workload's geometry at this size), "
+                                   "%d rhs, factor+solve per step" % (n, args.nrhs)},
+        "e2e": {"value": value, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    import torch
+    torch.cuda.set_device(local)
+    import __graft_entry__ as g
+    pkg = g.load_package()
+    prec = pkg.PRECISION_FP64 if args.precision == "fp64" else pkg.PRECISION_FP32
+    prob, src, rhs = make_problem(pkg, args.n, args.holes, args.nrhs)
+    N = prob.n
+    nrhs = args.nrhs
+    kw = dict(id_tol=args.tol, hole_centers=prob.hole_centers, hole_start=prob.hole_start,
+              hole_count=prob.hole_count, precision=prec)
+    # inputs resident in HBM for the `value` leg
+    rhs_f = np.asfortranarray(rhs)
+    d_b = torch.from_numpy(rhs_f.T.copy()).to("cuda")          # (nrhs, N): column c at row c
+    d_x = torch.empty_like(d_b)
+    nb = prob.n_holes
+    d_a = torch.empty((nrhs, max(1, nb)), dtype=torch.float64, device="cuda")
+    pin_b = torch.from_numpy(rhs_f.T.copy()).pin_memory()
+    pin_x = torch.empty_like(pin_b).pin_memory()
+    pin_a = torch.empty((nrhs, max(1, nb)), dtype=torch.float64).pin_memory()
+
+    def step_device():
+        fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, **kw)
+        fac.solve_device(d_b.data_ptr(), d_x.data_ptr(), nrhs, d_a.data_ptr())
+        torch.cuda.synchronize()
+        return fac
+
+    def step_host():
+        fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, **kw)
+        lib = pkg.load_library()
+        pkg._check(lib.ki_solve(fac._h, pin_b.data_ptr(), N, nrhs, pin_x.data_ptr(), N,
+                                pin_a.data_ptr(), max(1, nb)))
+        return fac
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        f = step_device()
+        f.close()
+    # ---- value: device-resident right-hand sides
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stage_runs = []
+    with ClockSampler(local) as clk:
+        ev0.record()
+        for _ in range(args.steps):
+            fac = step_device()
+            prof = fac.profile()
+            stage_runs.append(prof["factor"])
+            level_stats = prof.get("levels", [])
+            info = fac.info()
+            fac.close()
+        ev1.record()
+        torch.cuda.synchronize()
+    barrier()
+    t_dev = ev0.elapsed_time(ev1) / 1e3 / args.steps
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_dev], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    # ---- e2e: host buffers through the C ABI
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        fac = step_host()
+        fac.close()
+    e1.record()
+    torch.cuda.synchronize()
+    barrier()
+    t_e2e = e0.elapsed_time(e1) / 1e3 / args.steps
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_e2e], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+
+    # ---- accuracy of the last solution (sampled dense FP64 residual, analytic field)
+    fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, **kw)
+    fac.set_profiling(True)
+    res = fac.solve(rhs)
+    mu, alpha = res if isinstance(res, tuple) else (res, None)
+    solve_prof = fac.profile()["solve"]
+    rmax, rmed = residual_sample(fac, prob, rhs, mu, alpha, args.residual_rows)
+    rng = np.random.default_rng(4)
+    tg = pkg.geometry.domain_targets(prob, 64, rng)
+    u = fac.eval_targets(tg, mu, alpha)
+    ue = pkg.geometry.laplace_source_field(tg, src)
+    pde_err = float(np.abs(u - ue).max() / np.abs(ue).max())
+    fac.close()
+
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    # ---- roofline of the dominant kernel (average over the timed steps)
+    agg = {}
+    for run in stage_runs:
+        for s in run:
+            a = agg.setdefault(s["stage"], {"ms": 0.0, "flops": 0.0, "bytes": 0.0, "launches": 0})
+            for k in ("ms", "flops", "bytes", "launches"):
+                a[k] += s[k]
+    fam = {}
+    for k, v in agg.items():
+        f = fam.setdefault(k.split("@")[0], {"ms": 0.0, "flops": 0.0, "bytes": 0.0, "launches": 0})
+        for q in ("ms", "flops", "bytes", "launches"):
+            f[q] += v[q]
+    top = max(fam.items(), key=lambda kv: kv[1]["ms"])
+    peaks, peak_src = load_peaks()
+    name, a = top
+    sec = a["ms"] / 1e3
+    ach_tflops = a["flops"] / sec / 1e12 if sec > 0 else 0.0
+    roofline = {"bound": "tensor", "kernel": name, "achieved": ach_tflops,
+                "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
+                "frac": ach_tflops / peaks.get("bf16_tflops", 1.0), "traffic": None,
+                "peak_source": peak_src,
+                "note": "FP64/FP32 CUDA-core work; frac is against the measured bf16 tensor peak",
+                "launches_per_step": a["launches"] / args.steps,
+                "ms_per_step": a["ms"] / args.steps}
+    stage_table = {k: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps,
+                       "gflop_per_step": v["flops"] / args.steps / 1e9} for k, v in agg.items()}
+    launches = int(sum(v["launches"] for v in agg.values()) / args.steps)
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            n_cpu = min(args.n, args.cpu_sample_n)
+            p2, _, r2 = make_problem(pkg, n_cpu, args.holes, nrhs)
+            thr = os.cpu_count() or 1
+            dt, st, _, _ = cpu_oracle_run(p2, r2, args.tol, thr)
+            cpu = {"value": n_cpu * nrhs / dt, "unit": "DOF/s", "cores": thr, "kind": "port",
+                   "sample": "%d unknowns of the same geometry family, %d rhs, one factor+solve (%.1f s)"
+                             % (n_cpu, nrhs, dt)}
+        except Exception as e:  # reported, not fatal
+            cpu = {"value": None, "unit": "DOF/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": "failed: %s" % e}
+
+    units = N * nrhs * world
+    h2d = N * nrhs * 8 + prob.n * 6 * 8
+    d2h = N * nrhs * 8 + max(1, nb) * nrhs * 8
+    line = {
+        "metric": "factor+solve DOF/s (unknowns x rhs / s) at ID tol %g" % args.tol,
+        "value": units / t_dev, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_dev * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32 factor, f64 residual check",
+        "data": "synthetic (seeded boundary and sources)",
+        "config": {"workload": "laplace2d_disc_minus_%d_ellipses" % args.holes, "unknowns": N,
+                   "nrhs": nrhs, "id_tol": args.tol, "precision": args.precision,
+                   "leaf": 64, "proxy": 128, "l2": "factor working set >> 129 MB L2 (no flush needed)",
+                   "levels": info["n_levels"], "root_skeleton": info["n_root"],
+                   "compressed_boxes": info["n_compressed"]},
+        "e2e": {"value": units / t_e2e, "unit": "DOF/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e * 1e3},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "stages": stage_table,
+        "solve_stages": solve_prof,
+        "level_stats": level_stats,
+        "accuracy": {"residual_est_max": rmax, "residual_est_median": rmed,
+                     "residual_rows_sampled": args.residual_rows, "pde_rel_err": pde_err},
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

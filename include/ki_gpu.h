@@ -131,6 +131,14 @@ int ki_apply(ki_factor* f, const double* x, int ldx, int ncols, const double* al
              int ldalpha, double* y, int ldy);
 
 /*
+ * The same restricted to the listed DOFs: y (nrows x ncols, ldy) = rows of
+ * K x (+ U alpha).  Cost O(nrows * n_dofs * ncols): a sampled residual check
+ * at sizes where the full dense product is out of reach.
+ */
+int ki_apply_rows(ki_factor* f, const int* rows, int nrows, const double* x, int ldx, int ncols,
+                  const double* alpha, int ldalpha, double* y, int ldy);
+
+/*
  * Solution at domain points: u = K_forward mu (+ U_forward alpha), HOST
  * buffers (Kernel::apply_forward, kernel/kernel.cpp:809-825, and the
  * U_forward term of schur_solve, linear_solve.cpp:241-249).
@@ -139,6 +147,17 @@ int ki_apply(ki_factor* f, const double* x, int ldx, int ncols, const double* al
 int ki_eval_targets(ki_factor* f, const double* targets, int n_targets, const double* mu,
                     int ldmu, int ncols, const double* alpha, int ldalpha, double* out,
                     int ldout);
+
+/*
+ * Per-stage device times (CUDA events on the handle's stream) as a JSON
+ * string: {"factor": [{"stage", "launches", "ms", "flops", "bytes"}...],
+ * "solve": [...]}; flops/bytes are the algorithmic counts of each stage.
+ * No reference counterpart (the reference prints omp_get_wtime totals,
+ * kern_interp/linear_solve.cpp:275-279).  Solves are recorded only after
+ * ki_factor_set_profiling(f, 1).
+ */
+int ki_factor_get_profile(ki_factor* f, char* buf, int len);
+int ki_factor_set_profiling(ki_factor* f, int on);
 
 /* Message of the last failure on the calling thread ("" if none). */
 const char* ki_last_error(void);

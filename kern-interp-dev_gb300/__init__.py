@@ -28,7 +28,8 @@ PDE_LAPLACE, PDE_LAPLACE_NEUMANN, PDE_GAUSS, PDE_STOKES = range(4)
 PRECISION_FP64, PRECISION_FP32 = 0, 1
 
 EXPORTED = ["ki_factor_create", "ki_factor_destroy", "ki_factor_get_info", "ki_solve",
-            "ki_solve_device", "ki_apply", "ki_eval_targets", "ki_last_error", "ki_version"]
+            "ki_solve_device", "ki_apply", "ki_eval_targets", "ki_last_error", "ki_version",
+            "ki_factor_get_profile", "ki_factor_set_profiling", "ki_apply_rows"]
 
 
 class KiError(RuntimeError):
@@ -77,6 +78,9 @@ def load_library(path=None):
     lib.ki_solve_device.argtypes = [V, V, I, I, V, I, V, I, V]
     lib.ki_apply.argtypes = [V, V, I, I, V, I, V, I]
     lib.ki_eval_targets.argtypes = [V, V, I, V, I, I, V, I, V, I]
+    lib.ki_apply_rows.argtypes = [V, V, I, V, I, I, V, I, V, I]
+    lib.ki_factor_get_profile.argtypes = [V, ctypes.c_char_p, I]
+    lib.ki_factor_set_profiling.argtypes = [V, I]
     lib.ki_last_error.restype = ctypes.c_char_p
     lib.ki_version.restype = ctypes.c_char_p
     for name in EXPORTED:
@@ -142,6 +146,16 @@ class Factor:
         _check(load_library().ki_factor_get_info(self._h, ctypes.byref(i)))
         return {f: getattr(i, f) for f, _ in _Info._fields_}
 
+    def profile(self):
+        """Per-stage device times and algorithmic counts (dict)."""
+        import json
+        buf = ctypes.create_string_buffer(1 << 16)
+        _check(load_library().ki_factor_get_profile(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
+    def set_profiling(self, on=True):
+        _check(load_library().ki_factor_set_profiling(self._h, 1 if on else 0))
+
     def solve(self, b):
         """x (and alpha for holes) with b: (n_dofs,) or (n_dofs, nrhs)."""
         b = np.asarray(b, np.float64)
@@ -177,6 +191,20 @@ class Factor:
         _check(load_library().ki_apply(self._h, _ptr(X), self.n_dofs, X.shape[1], _ptr(A),
                                        max(1, self.n_border), _ptr(Y), self.n_dofs))
         return Y[:, 0] if vec else Y
+
+    def apply_rows(self, rows, x, alpha=None):
+        """Rows of the dense FP64 operator product K x (+ U alpha)."""
+        rows = np.ascontiguousarray(rows, np.int32)
+        x = np.asarray(x, np.float64)
+        X = np.asfortranarray(x.reshape(self.n_dofs, -1))
+        Y = np.zeros((rows.size, X.shape[1]), order="F")
+        A = None
+        if alpha is not None:
+            A = np.asfortranarray(np.asarray(alpha, np.float64).reshape(self.n_border, -1))
+        _check(load_library().ki_apply_rows(self._h, _ptr(rows), rows.size, _ptr(X), self.n_dofs,
+                                            X.shape[1], _ptr(A), max(1, self.n_border), _ptr(Y),
+                                            max(1, rows.size)))
+        return Y
 
     def eval_targets(self, targets, mu, alpha=None):
         targets = np.ascontiguousarray(targets, np.float64).reshape(-1, 2)

@@ -2,6 +2,8 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -97,16 +99,17 @@ constexpr int kApplyTile = 128;
 constexpr int kApplyCols = 8;
 
 __global__ void k_dense_apply(ki::Points<double> P, int n_points, int sol_dim, const double* x,
-                              int ldx, int ncols, double* y, int ldy) {
+                              int ldx, int ncols, double* y, int ldy, const int* rows, int nrows) {
   __shared__ double sx[kApplyTile], sy[kApplyTile], snx[kApplyTile], sny[kApplyTile],
       sw[kApplyTile], sk[kApplyTile];
-  const int N = n_points * sol_dim;
-  const int tdof = blockIdx.x * blockDim.x + threadIdx.x;
+  const int N = rows ? nrows : n_points * sol_dim;
+  const int trow = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tdof = rows ? (trow < nrows ? rows[trow] : 0) : trow;
   const int c0 = blockIdx.y * kApplyCols;
   const int nc = min(kApplyCols, ncols - c0);
   double acc[kApplyCols];
   for (int c = 0; c < kApplyCols; c++) acc[c] = 0.0;
-  int tp = tdof < N ? tdof / sol_dim : 0;
+  int tp = trow < N ? tdof / sol_dim : 0;
   double tx = P.x[tp], ty = P.y[tp], tnx = P.nx[tp], tny = P.ny[tp];
   for (int base = 0; base < n_points; base += kApplyTile) {
     __syncthreads();
@@ -118,7 +121,7 @@ __global__ void k_dense_apply(ki::Points<double> P, int n_points, int sol_dim, c
       }
     }
     __syncthreads();
-    if (tdof >= N) continue;
+    if (trow >= N) continue;
     int lim = min(kApplyTile, n_points - base);
     for (int i = 0; i < lim; i++) {
       for (int sp = 0; sp < sol_dim; sp++) {
@@ -133,8 +136,8 @@ __global__ void k_dense_apply(ki::Points<double> P, int n_points, int sol_dim, c
       }
     }
   }
-  if (tdof < N)
-    for (int c = 0; c < nc; c++) y[tdof + (size_t)ldy * (c0 + c)] = acc[c];
+  if (trow < N)
+    for (int c = 0; c < nc; c++) y[trow + (size_t)ldy * (c0 + c)] = acc[c];
 }
 
 // Forward evaluation at domain targets (target normal 0, reference forward
@@ -167,7 +170,32 @@ __global__ void k_forward(ki::Points<double> P, int n_points, int sol_dim, const
 // U(i, h) = log|x_i - c_h|) and Stokes 2D (:77-97).
 __global__ void k_border_apply(const double* px, const double* py, int stride, int n_points, int sol_dim,
                                const double* hc, int nh, const double* alpha, int lda, int ncols,
-                               double* y, int ldy) {
+                               double* y, int ldy, const int* rows = nullptr, int nrows = 0) {
+  if (rows) {
+    // row subset: one thread per listed DOF
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nrows) return;
+    const int dof = rows[q], p = dof / sol_dim, comp = dof % sol_dim;
+    for (int c = 0; c < ncols; c++) {
+      double acc = 0;
+      for (int h = 0; h < nh; h++) {
+        double rx = px[(size_t)stride * p] - hc[2 * h], ry = py[(size_t)stride * p] - hc[2 * h + 1];
+        double rn = sqrt(rx * rx + ry * ry);
+        if (sol_dim == 1) {
+          acc += log(rn) * alpha[h + (size_t)lda * c];
+        } else {
+          double sc = 1.0 / (4 * ki::kPi), r2 = rn * rn;
+          const double* al = alpha + 3 * h + (size_t)lda * c;
+          if (comp == 0)
+            acc += sc * (log(1 / rn) + rx * rx / r2) * al[0] + sc * (rx * ry / r2) * al[1] + ry * (sc / r2) * al[2];
+          else
+            acc += sc * (ry * rx / r2) * al[0] + sc * (log(1 / rn) + ry * ry / r2) * al[1] - rx * (sc / r2) * al[2];
+        }
+      }
+      y[q + (size_t)ldy * c] += acc;
+    }
+    return;
+  }
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_points) return;
   for (int c = 0; c < ncols; c++) {
@@ -443,7 +471,8 @@ int ki_apply(ki_factor* f, const double* x, int ldx, int ncols, const double* al
     KI_CHECK_CUDA(cudaMemcpy2DAsync(dx.p, sizeof(double) * N, x, sizeof(double) * ldx,
                                     sizeof(double) * N, ncols, cudaMemcpyHostToDevice, s));
     dim3 grid((N + kApplyThreads - 1) / kApplyThreads, (ncols + kApplyCols - 1) / kApplyCols);
-    k_dense_apply<<<grid, kApplyThreads, 0, s>>>(f->P, f->n_points, f->sol_dim, dx.p, N, ncols, dy.p, N);
+    k_dense_apply<<<grid, kApplyThreads, 0, s>>>(f->P, f->n_points, f->sol_dim, dx.p, N, ncols, dy.p, N,
+                                                 nullptr, 0);
     KI_CHECK_CUDA(cudaGetLastError());
     if (f->n_border > 0 && alpha) {
       if (ldalpha < f->n_border) throw ArgError("bad ldalpha");
@@ -462,6 +491,43 @@ int ki_apply(ki_factor* f, const double* x, int ldx, int ncols, const double* al
     }
     KI_CHECK_CUDA(cudaMemcpy2DAsync(y, sizeof(double) * ldy, dy.p, sizeof(double) * N,
                                     sizeof(double) * N, ncols, cudaMemcpyDeviceToHost, s));
+    KI_CHECK_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ki_apply_rows(ki_factor* f, const int* rows, int nrows, const double* x, int ldx, int ncols,
+                  const double* alpha, int ldalpha, double* y, int ldy) {
+  return guarded([&] {
+    if (!f || !rows || !x || !y) throw ArgError("NULL argument");
+    const int N = f->n_dofs;
+    if (nrows < 0 || ncols < 0 || ldx < N || ldy < nrows) throw ArgError("bad sizes");
+    for (int i = 0; i < nrows; i++)
+      if (rows[i] < 0 || rows[i] >= N) throw ArgError("row index out of range");
+    if (nrows == 0 || ncols == 0) return;
+    cudaStream_t s = f->stream;
+    DevBuf<double> dx((size_t)N * ncols, s), dy((size_t)nrows * ncols, s);
+    DevBuf<int> dr((size_t)nrows, s);
+    KI_CHECK_CUDA(cudaMemcpyAsync(dr.p, rows, sizeof(int) * nrows, cudaMemcpyHostToDevice, s));
+    KI_CHECK_CUDA(cudaMemcpy2DAsync(dx.p, sizeof(double) * N, x, sizeof(double) * ldx,
+                                    sizeof(double) * N, ncols, cudaMemcpyHostToDevice, s));
+    dim3 grid((nrows + kApplyThreads - 1) / kApplyThreads, (ncols + kApplyCols - 1) / kApplyCols);
+    k_dense_apply<<<grid, kApplyThreads, 0, s>>>(f->P, f->n_points, f->sol_dim, dx.p, N, ncols,
+                                                 dy.p, nrows, dr.p, nrows);
+    KI_CHECK_CUDA(cudaGetLastError());
+    if (f->n_border > 0 && alpha) {
+      if (ldalpha < f->n_border) throw ArgError("bad ldalpha");
+      DevBuf<double> da((size_t)f->n_border * ncols, s);
+      KI_CHECK_CUDA(cudaMemcpy2DAsync(da.p, sizeof(double) * f->n_border, alpha,
+                                      sizeof(double) * ldalpha, sizeof(double) * f->n_border,
+                                      ncols, cudaMemcpyHostToDevice, s));
+      k_border_apply<<<(nrows + 127) / 128, 128, 0, s>>>(f->P.x, f->P.y, 1, f->n_points, f->sol_dim,
+                                                         f->d_holes, f->n_holes, da.p, f->n_border,
+                                                         ncols, dy.p, nrows, dr.p, nrows);
+      KI_CHECK_CUDA(cudaGetLastError());
+      KI_CHECK_CUDA(cudaStreamSynchronize(s));
+    }
+    KI_CHECK_CUDA(cudaMemcpy2DAsync(y, sizeof(double) * ldy, dy.p, sizeof(double) * nrows,
+                                    sizeof(double) * nrows, ncols, cudaMemcpyDeviceToHost, s));
     KI_CHECK_CUDA(cudaStreamSynchronize(s));
   });
 }
@@ -497,6 +563,57 @@ int ki_eval_targets(ki_factor* f, const double* targets, int n_targets, const do
     KI_CHECK_CUDA(cudaMemcpy2DAsync(out, sizeof(double) * ldout, dout.p, sizeof(double) * NT,
                                     sizeof(double) * NT, ncols, cudaMemcpyDeviceToHost, s));
     KI_CHECK_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ki_factor_set_profiling(ki_factor* f, int on) {
+  return guarded([&] {
+    if (!f) throw ArgError("factor is NULL");
+    if (f->f64) f->f64->profile_solve = on != 0;
+    if (f->f32) f->f32->profile_solve = on != 0;
+  });
+}
+
+int ki_factor_get_profile(ki_factor* f, char* buf, int len) {
+  return guarded([&] {
+    if (!f || !buf || len <= 0) throw ArgError("NULL argument");
+    auto dump = [](const std::vector<ki::StageSum>& v) {
+      std::string o = "[";
+      for (size_t i = 0; i < v.size(); i++) {
+        char tmp[256];
+        snprintf(tmp, sizeof(tmp),
+                 "%s{\"stage\": \"%s\", \"launches\": %d, \"ms\": %.6f, \"flops\": %.6e, \"bytes\": %.6e}",
+                 i ? ", " : "", v[i].stage.c_str(), v[i].launches, v[i].ms, v[i].flops, v[i].bytes);
+        o += tmp;
+      }
+      return o + "]";
+    };
+    std::string j;
+    auto fill = [&](auto& F) {
+      auto now = F.collect();
+      if (!now.empty()) F.solve_prof = now;
+      std::string lv = "[";
+      for (size_t i = 0; i < F.level_stats.size(); i++) {
+        const auto& q = F.level_stats[i];
+        char tmp[512];
+        snprintf(tmp, sizeof(tmp),
+                 "%s{\"level\": %d, \"boxes\": %d, \"id_boxes\": %d, \"compressed\": %d, "
+                 "\"max_n\": %d, \"mean_n\": %.1f, \"max_m\": %d, \"mean_m\": %.1f, "
+                 "\"max_k\": %d, \"mean_k\": %.1f, \"modes\": [%d, %d, %d]}",
+                 i ? ", " : "", q.level, q.boxes, q.id_boxes, q.compressed, q.max_n,
+                 q.sum_n / std::max(1, q.id_boxes), q.max_m, q.sum_m / std::max(1, q.id_boxes),
+                 q.max_k, q.sum_k / std::max(1, q.id_boxes), q.mode_count[0], q.mode_count[1],
+                 q.mode_count[2]);
+        lv += tmp;
+      }
+      lv += "]";
+      j = "{\"factor\": " + dump(F.factor_prof) + ", \"solve\": " + dump(F.solve_prof) +
+          ", \"levels\": " + lv + "}";
+    };
+    if (f->f64) fill(*f->f64);
+    if (f->f32) fill(*f->f32);
+    if ((int)j.size() + 1 > len) throw ArgError("profile buffer too small");
+    std::memcpy(buf, j.c_str(), j.size() + 1);
   });
 }
 

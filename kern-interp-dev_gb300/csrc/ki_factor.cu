@@ -32,6 +32,7 @@
 #include <string>
 
 #include "ki_common.cuh"
+#include "ki_dense.h"
 
 namespace ki {
 
@@ -58,7 +59,53 @@ void* Factorization<T>::alloc(size_t bytes) {
 }
 
 template <typename T>
+void Factorization<T>::stage_begin(const char* name, double flops, double bytes) {
+  StageRec r;
+  r.stage = name;
+  r.flops = flops;
+  r.bytes = bytes;
+  KI_CUDA(cudaEventCreate(&r.a));
+  KI_CUDA(cudaEventCreate(&r.b));
+  KI_CUDA(cudaEventRecord(r.a, stream));
+  prof_open.push_back(r);
+}
+
+template <typename T>
+void Factorization<T>::stage_end() {
+  KI_CUDA(cudaEventRecord(prof_open.back().b, stream));
+}
+
+template <typename T>
+std::vector<StageSum> Factorization<T>::collect() {
+  std::vector<StageSum> out;
+  for (auto& r : prof_open) {
+    float ms = 0;
+    KI_CUDA(cudaEventSynchronize(r.b));
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+    StageSum* d = nullptr;
+    for (auto& o : out)
+      if (o.stage == r.stage) d = &o;
+    if (!d) {
+      out.push_back(StageSum{r.stage});
+      d = &out.back();
+    }
+    d->launches++;
+    d->ms += ms;
+    d->flops += r.flops;
+    d->bytes += r.bytes;
+  }
+  prof_open.clear();
+  return out;
+}
+
+template <typename T>
 Factorization<T>::~Factorization() {
+  for (auto& r : prof_open) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
   for (void* p : owned) cudaFreeAsync(p, stream);
   if (stream) cudaStreamSynchronize(stream);
 }
@@ -167,37 +214,60 @@ __device__ __forceinline__ T id_entry(const Points<T>& P, int sol_dim, int row, 
 }
 
 // Interpolative decomposition of one box per CTA.
+//
+// Thread-per-column formulation: every dot product and update runs inside
+// one thread over a column (no cross-lane reductions), which keeps the FP64
+// instruction count at the algorithmic 2 FMAs per matrix entry and step.
+// R (n x n triangle) and the 32-row block B are row-major, so the threads of
+// a warp touch consecutive columns.  Shared-memory layout (dynamic):
+//   B (32 x ldB) | hu (2 x 32 Householder tails) | vn1 (n) | vn2 (n) | perm (n) |
+//   R (n x ldR) when it fits (mode 0); mode 1 keeps R in the global scratch.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, const int64_t* seg_off,
-                                                  const int* seg_len, int* ipool, int* iscratch, T* tws,
-                                                  Points<T> P, int sol_dim, int nprox,
-                                                  const double* pcos, const double* psin,
-                                                  double tol, int* k_out, int* err) {
-  const IdTask t = tasks[blockIdx.x];
+__global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_base,
+                                                  const int64_t* seg_off, const int* seg_len,
+                                                  int* ipool, int* iscratch, T* tws, Points<T> P,
+                                                  int sol_dim, int nprox, const double* pcos,
+                                                  const double* psin, double tol, int* k_out,
+                                                  int* m_out, int mode) {
+  extern __shared__ __align__(16) unsigned char id_smem[];
+  const int task = task_base + blockIdx.x;
+  const IdTask t = tasks[task];
   const int n = t.n;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarps = nth >> 5;
   __shared__ int s_cnt;
-  __shared__ int s_scan[kThreads];
-  __shared__ T s_tau, s_beta, s_red;
-  __shared__ int s_piv, s_k, s_stop;
+  __shared__ int s_scan[64];
+  __shared__ int s_piv, s_k;
+  __shared__ T s_tau[2], s_beta;
 
   int* rows = iscratch + t.rows;
   const int* act = ipool + t.act;
-  int* perm = iscratch + t.perm;
-  T* R = tws + t.ws;
-  T* B = R + (size_t)n * n;
-  T* vn1 = B + (size_t)kFoldRows * n;
-  T* vn2 = vn1 + n;
-  T* Tout = vn2 + n;
+  T* gws = tws + t.ws;   // global scratch: R (n*n) | Tout (n*n/4+1)
+  const int ldB = n;
+  size_t off = 0;
+  T* B = reinterpret_cast<T*>(id_smem);
+  off += sizeof(T) * (size_t)kFoldRows * ldB;
+  T* hu = reinterpret_cast<T*>(id_smem + off);   // [2][n] reflector tails (fold: 32, CPQR: n)
+  off += sizeof(T) * 2 * (size_t)max(n, kFoldRows);
+  T* vn1 = reinterpret_cast<T*>(id_smem + off);
+  off += sizeof(T) * (size_t)n;
+  T* vn2 = reinterpret_cast<T*>(id_smem + off);
+  off += sizeof(T) * (size_t)n;
+  int* perm = reinterpret_cast<int*>(id_smem + off);
+  off += sizeof(int) * (size_t)n;
+  off = (off + 15) & ~size_t(15);
+  const int ldR = mode == 0 ? (n | 1) : n;
+  T* R = mode == 0 ? reinterpret_cast<T*>(id_smem + off) : gws;
+  T* Tout = gws + (size_t)n * n;
 
   // 1. candidate rows, optionally filtered to the proxy circle, order kept
-  if (threadIdx.x == 0) s_cnt = 0;
+  if (tid == 0) s_cnt = 0;
   __syncthreads();
   for (int s = t.seg_begin; s < t.seg_end; s++) {
     const int* src = ipool + seg_off[s];
     int len = seg_len[s];
-    for (int base = 0; base < len; base += blockDim.x) {
-      int i = base + threadIdx.x;
+    for (int base = 0; base < len; base += nth) {
+      int i = base + tid;
       int keep = 0, dof = 0;
       if (i < len) {
         dof = src[i];
@@ -210,119 +280,155 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, const int6
           keep = dist < t.rad_filter;
         }
       }
-      s_scan[threadIdx.x] = keep;
-      __syncthreads();
-      for (int o = 1; o < blockDim.x; o <<= 1) {
-        int v = threadIdx.x >= o ? s_scan[threadIdx.x - o] : 0;
-        __syncthreads();
-        s_scan[threadIdx.x] += v;
-        __syncthreads();
+      int v = keep;
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffff, v, o);
+        if (lane >= o) v += y;
       }
-      if (keep) rows[s_cnt + s_scan[threadIdx.x] - 1] = dof;
+      if (lane == 31) s_scan[warp] = v;
       __syncthreads();
-      if (threadIdx.x == blockDim.x - 1) s_cnt += s_scan[threadIdx.x];
+      if (warp == 0) {
+        int wv = lane < nwarps ? s_scan[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+          int y = __shfl_up_sync(0xffffffff, wv, o);
+          if (lane >= o) wv += y;
+        }
+        if (lane < nwarps) s_scan[32 + lane] = wv;
+      }
+      __syncthreads();
+      int before = warp > 0 ? s_scan[32 + warp - 1] : 0;
+      if (keep) rows[s_cnt + before + v - 1] = dof;
+      int total = s_scan[32 + nwarps - 1];
+      __syncthreads();
+      if (tid == 0) s_cnt += total;
       __syncthreads();
     }
   }
   const int nI = s_cnt;
   const int nprox_rows = t.mode == 0 ? 2 * nprox * sol_dim : 0;
   const int m = 2 * nI + nprox_rows;
+  if (tid == 0) m_out[task] = m;
 
-  // 2. TSQR: R <- qr([R; B]) for successive row blocks B of the ID matrix
-  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) R[idx] = T(0);
+  // 2. TSQR: R <- qr([R; B]) for successive 32-row blocks B of the ID
+  //    matrix.  The thread that owns column j+1 forms reflector j+1 right
+  //    after updating that column (look-ahead), so one barrier per column.
+  for (int idx = tid; idx < n * n; idx += nth) R[(idx / n) * (size_t)ldR + idx % n] = T(0);
   __syncthreads();
+  auto reflect = [&](int j, int buf) {
+    // reflector of [R(j,j); B(:,j)] by one thread; tail -> hu[buf], tau -> s_tau[buf]
+    T alpha = R[(size_t)j * ldR + j];
+    T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+#pragma unroll
+    for (int i = 0; i < kFoldRows; i += 4) {
+      T b0 = B[(size_t)i * ldB + j], b1 = B[(size_t)(i + 1) * ldB + j];
+      T b2 = B[(size_t)(i + 2) * ldB + j], b3 = B[(size_t)(i + 3) * ldB + j];
+      s0 += b0 * b0; s1 += b1 * b1; s2 += b2 * b2; s3 += b3 * b3;
+    }
+    T sigma = (s0 + s1) + (s2 + s3);
+    T tau = T(0), beta = alpha, scale = T(0);
+    if (sigma != T(0)) {
+      T nrm = sqrt(alpha * alpha + sigma);
+      beta = alpha >= T(0) ? -nrm : nrm;
+      tau = (beta - alpha) / beta;
+      scale = T(1) / (alpha - beta);
+    }
+#pragma unroll
+    for (int i = 0; i < kFoldRows; i++) hu[buf * kFoldRows + i] = B[(size_t)i * ldB + j] * scale;
+    s_tau[buf] = tau;
+    R[(size_t)j * ldR + j] = beta;
+  };
   for (int r0 = 0; r0 < m; r0 += kFoldRows) {
-    for (int idx = threadIdx.x; idx < kFoldRows * n; idx += blockDim.x) {
-      int i = idx % kFoldRows, j = idx / kFoldRows;
+    for (int idx = tid; idx < kFoldRows * n; idx += nth) {
+      int j = idx % n, i = idx / n;
       int row = r0 + i;
       T v = T(0);
       if (row < m)
         v = id_entry<T>(P, sol_dim, row, nI, rows, act[j], nprox, pcos, psin, t.cx, t.cy,
                         t.rad_proxy);
-      B[i + (size_t)kFoldRows * j] = v;
+      B[(size_t)i * ldB + j] = v;
     }
     __syncthreads();
+    if (tid == 0) reflect(0, 0);
+    __syncthreads();
     for (int j = 0; j < n; j++) {
-      if (warp == 0) {
-        T b = B[lane + (size_t)kFoldRows * j];
-        T sigma = warp_sum(b * b);
-        T alpha = R[j + (size_t)n * j];
-        T tau = T(0), beta = alpha, scale = T(0);
-        if (sigma != T(0)) {
-          T nrm = sqrt(alpha * alpha + sigma);
-          beta = alpha >= T(0) ? -nrm : nrm;
-          tau = (beta - alpha) / beta;
-          scale = T(1) / (alpha - beta);
-        }
-        B[lane + (size_t)kFoldRows * j] = b * scale;   // u (v = [1; u])
-        if (lane == 0) { s_tau = tau; s_beta = beta; }
-      }
-      __syncthreads();
-      T tau = s_tau;
+      const int buf = j & 1;
+      const T tau = s_tau[buf];
       if (tau != T(0)) {
-        T u = B[lane + (size_t)kFoldRows * j];
-        for (int c = j + 1 + warp; c < n; c += nwarps) {
-          T bc = B[lane + (size_t)kFoldRows * c];
-          T rjc = R[j + (size_t)n * c];
-          T w = (warp_sum(u * bc) + rjc) * tau;
-          B[lane + (size_t)kFoldRows * c] = bc - w * u;
-          if (lane == 0) R[j + (size_t)n * c] = rjc - w;
+        const T* u = hu + buf * kFoldRows;
+        for (int c = j + 1 + tid; c < n; c += nth) {
+          T w0 = R[(size_t)j * ldR + c], w1 = T(0), w2 = T(0), w3 = T(0);
+#pragma unroll
+          for (int i = 0; i < kFoldRows; i += 4) {
+            w0 += u[i] * B[(size_t)i * ldB + c];
+            w1 += u[i + 1] * B[(size_t)(i + 1) * ldB + c];
+            w2 += u[i + 2] * B[(size_t)(i + 2) * ldB + c];
+            w3 += u[i + 3] * B[(size_t)(i + 3) * ldB + c];
+          }
+          T w = ((w0 + w1) + (w2 + w3)) * tau;
+          R[(size_t)j * ldR + c] -= w;
+#pragma unroll
+          for (int i = 0; i < kFoldRows; i++) B[(size_t)i * ldB + c] -= w * u[i];
+          if (c == j + 1) reflect(j + 1, buf ^ 1);
         }
+      } else if (j + 1 < n && tid == 0) {   // column j+1 belongs to thread 0
+        reflect(j + 1, buf ^ 1);
       }
-      if (threadIdx.x == 0) R[j + (size_t)n * j] = s_beta;
       __syncthreads();
     }
   }
 
   // 3. column-pivoted QR of the n x n triangle (LAPACK xGEQP3/xLAQP2 norm
   //    downdating with recomputation after cancellation), stopping at the
-  //    first |R_jj| < tol |R_00| for j >= 1
-  for (int c = warp; c < n; c += nwarps) {
+  //    first |R_jj| < tol |R_00| for j >= 1.  Thread per column again.
+  for (int c = tid; c < n; c += nth) {
     T s = T(0);
-    for (int i = lane; i <= c; i += 32) s += R[i + (size_t)n * c] * R[i + (size_t)n * c];
-    s = warp_sum(s);
-    if (lane == 0) { vn1[c] = sqrt(s); vn2[c] = vn1[c]; perm[c] = c; }
+    for (int i = 0; i <= c; i++) s += R[(size_t)i * ldR + c] * R[(size_t)i * ldR + c];
+    vn1[c] = sqrt(s);
+    vn2[c] = vn1[c];
+    perm[c] = c;
   }
-  if (threadIdx.x == 0) { s_k = 0; s_stop = 0; }
+  if (tid == 0) s_k = 0;
   __syncthreads();
   T thresh = T(0);
   const int jmax = min(n, m);
   for (int j = 0; j < jmax; j++) {
+    // pivot: first index of the largest partial norm (norms are >= 0, so
+    // their bit patterns order like the values)
     if (warp == 0) {
-      T best = T(-1);
+      long long best = -1;
       int bi = j;
       for (int c = j + lane; c < n; c += 32) {
-        T v = vn1[c];
+        long long v = (long long)__double_as_longlong((double)vn1[c]);
         if (v > best) { best = v; bi = c; }
       }
       for (int o = 16; o > 0; o >>= 1) {
-        T ov = __shfl_down_sync(0xffffffff, best, o);
+        long long ov = __shfl_down_sync(0xffffffff, best, o);
         int oi = __shfl_down_sync(0xffffffff, bi, o);
         if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
       }
       if (lane == 0) s_piv = bi;
     }
     __syncthreads();
-    int p = s_piv;
+    const int p = s_piv;
     if (p != j) {
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        T a = R[i + (size_t)n * j];
-        R[i + (size_t)n * j] = R[i + (size_t)n * p];
-        R[i + (size_t)n * p] = a;
+      for (int i = tid; i < n; i += nth) {
+        T a = R[(size_t)i * ldR + j];
+        R[(size_t)i * ldR + j] = R[(size_t)i * ldR + p];
+        R[(size_t)i * ldR + p] = a;
       }
-      if (threadIdx.x == 0) {
+      if (tid == 0) {
         int a = perm[j]; perm[j] = perm[p]; perm[p] = a;
         T v = vn1[j]; vn1[j] = vn1[p]; vn1[p] = v;
         v = vn2[j]; vn2[j] = vn2[p]; vn2[p] = v;
       }
+      __syncthreads();
     }
-    __syncthreads();
-    // Householder for R(j:n, j)
+    // reflector of R(j:n, j) by warp 0; tail -> hu[0..], scalars -> shared
     if (warp == 0) {
-      T sigma = T(0);
-      for (int i = j + 1 + lane; i < n; i += 32) sigma += R[i + (size_t)n * j] * R[i + (size_t)n * j];
-      sigma = warp_sum(sigma);
-      T alpha = R[j + (size_t)n * j];
+      T sg = T(0);
+      for (int i = j + 1 + lane; i < n; i += 32) sg += R[(size_t)i * ldR + j] * R[(size_t)i * ldR + j];
+      T sigma = warp_sum(sg);
+      T alpha = R[(size_t)j * ldR + j];
       T tau = T(0), beta = alpha, scale = T(0);
       if (sigma != T(0)) {
         T nrm = sqrt(alpha * alpha + sigma);
@@ -330,78 +436,85 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, const int6
         tau = (beta - alpha) / beta;
         scale = T(1) / (alpha - beta);
       }
-      for (int i = j + 1 + lane; i < n; i += 32) R[i + (size_t)n * j] *= scale;
-      if (lane == 0) {
-        s_tau = tau;
-        s_beta = beta;
-        R[j + (size_t)n * j] = beta;
-      }
+      for (int i = j + 1 + lane; i < n; i += 32) hu[i] = R[(size_t)i * ldR + j] * scale;
+      if (lane == 0) { s_tau[0] = tau; s_beta = beta; }
     }
     __syncthreads();
-    T beta = s_beta;
+    const T beta = s_beta, tau = s_tau[0];
     if (j == 0) thresh = fabs(T(tol) * beta);
     if (j >= 1 && fabs(beta) < thresh) {
-      if (threadIdx.x == 0) s_k = j;
+      if (tid == 0) s_k = j;
       break;
     }
-    T tau = s_tau;
-    for (int c = j + 1 + warp; c < n; c += nwarps) {
+    for (int c = j + 1 + tid; c < n; c += nth) {
       if (tau != T(0)) {
-        T rjc0 = R[j + (size_t)n * c];
-        T part = T(0);
-        for (int i = j + 1 + lane; i < n; i += 32) part += R[i + (size_t)n * j] * R[i + (size_t)n * c];
-        T w = (warp_sum(part) + rjc0) * tau;
-        for (int i = j + 1 + lane; i < n; i += 32) R[i + (size_t)n * c] -= w * R[i + (size_t)n * j];
-        if (lane == 0) R[j + (size_t)n * c] = rjc0 - w;
-        __syncwarp();
+        T w0 = R[(size_t)j * ldR + c], w1 = T(0);
+        int i = j + 1;
+        for (; i + 1 < n; i += 2) {
+          w0 += hu[i] * R[(size_t)i * ldR + c];
+          w1 += hu[i + 1] * R[(size_t)(i + 1) * ldR + c];
+        }
+        if (i < n) w0 += hu[i] * R[(size_t)i * ldR + c];
+        T w = (w0 + w1) * tau;
+        R[(size_t)j * ldR + c] -= w;
+        for (int q = j + 1; q < n; q++) R[(size_t)q * ldR + c] -= w * hu[q];
       }
       // norm downdate of column c (xLAQP2), recomputed after cancellation
-      T rjc = R[j + (size_t)n * c];
+      T rjc = R[(size_t)j * ldR + c];
       T v1 = vn1[c];
-      int recompute = 0;
-      T newv = v1;
       if (v1 != T(0)) {
         T temp = fabs(rjc) / v1;
         temp = T(1) - temp * temp;
         temp = temp < T(0) ? T(0) : temp;
         T q = v1 / vn2[c];
         T temp2 = temp * q * q;
-        if (temp2 <= tol3z<T>()) recompute = 1;
-        else newv = v1 * sqrt(temp);
+        if (temp2 <= tol3z<T>()) {
+          T s2 = T(0);
+          for (int i = j + 1; i < n; i++) s2 += R[(size_t)i * ldR + c] * R[(size_t)i * ldR + c];
+          vn1[c] = sqrt(s2);
+          vn2[c] = vn1[c];
+        } else {
+          vn1[c] = v1 * sqrt(temp);
+        }
       }
-      if (recompute) {
-        T s2 = T(0);
-        for (int i = j + 1 + lane; i < n; i += 32) s2 += R[i + (size_t)n * c] * R[i + (size_t)n * c];
-        newv = sqrt(warp_sum(s2));
-      }
-      __syncwarp();
-      if (lane == 0) {
-        vn1[c] = newv;
-        if (recompute) vn2[c] = newv;
-      }
-      __syncwarp();
     }
+    if (tid == 0) R[(size_t)j * ldR + j] = beta;
     __syncthreads();
   }
   __syncthreads();
   const int k = s_k;
-  if (threadIdx.x == 0) k_out[blockIdx.x] = k;
+  if (tid == 0) k_out[task] = k;
+  int* gperm = iscratch + t.perm;
+  for (int i = tid; i < n; i += nth) gperm[i] = perm[i];
   if (k == 0) return;
   const int r = n - k;
 
-  // 4. T = R11^-1 R12 (k x r), one thread per column, and the permuted list
-  for (int c = threadIdx.x; c < r; c += blockDim.x) {
-    T* tc = Tout + (size_t)k * c;
-    const T* rc = R + (size_t)n * (k + c);
+  // 4. T = R11^-1 R12 in place over R12 (one thread per column), then out
+  for (int c = k + tid; c < n; c += nth) {
     for (int i = k - 1; i >= 0; i--) {
-      T s = rc[i];
-      for (int l = i + 1; l < k; l++) s -= R[i + (size_t)n * l] * tc[l];
-      tc[i] = s / R[i + (size_t)n * i];
+      T s = R[(size_t)i * ldR + c];
+      for (int l = i + 1; l < k; l++) s -= R[(size_t)i * ldR + l] * R[(size_t)l * ldR + c];
+      R[(size_t)i * ldR + c] = s / R[(size_t)i * ldR + i];
     }
   }
+  __syncthreads();
+  for (int e = tid; e < k * r; e += nth) {
+    int i = e % k, c = e / k;
+    Tout[e] = R[(size_t)i * ldR + k + c];
+  }
   int* pact = ipool + t.pact;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) pact[i] = act[perm[i]];
-  (void)err;
+  for (int i = tid; i < n; i += nth) pact[i] = act[perm[i]];
+}
+
+// Shared-memory bytes of k_id for a box of n active DOFs: mode 0 keeps the
+// triangle in shared memory, mode 1 in the global scratch.
+template <typename T>
+size_t id_smem_bytes(int n, int mode) {
+  size_t b = sizeof(T) * (size_t)kFoldRows * n + sizeof(T) * 2 * (size_t)std::max(n, kFoldRows) +
+             sizeof(T) * 2 * (size_t)n + sizeof(int) * (size_t)n;
+  b = (b + 15) & ~size_t(15);
+  if (mode == 0) b += sizeof(T) * (size_t)n * (n | 1);
+  return b;
 }
 
 // Self block K_BN of a box (kernel entries plus children's accumulated
@@ -430,17 +543,22 @@ __global__ void k_assemble(const AsmTask<T>* tasks, const int* ipool, Points<T> 
 }
 
 // Schur-complement elimination of a compressed box
-// (SkelFactorization::decouple, skel_factorization.cpp:91-127).
+// (SkelFactorization::decouple, skel_factorization.cpp:91-127).  Working set
+// P (n x n, permuted K_BN) | Wrs (r x k) | Lt (r x k) | X (r x r) in shared
+// memory when it fits (smem != 0), else in the global scratch t.ws.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_schur(const SchurTask<T>* tasks, int* err) {
-  const SchurTask<T> t = tasks[blockIdx.x];
+__global__ void __launch_bounds__(kThreads) k_schur(const SchurTask<T>* tasks, int task_base,
+                                                     int smem, int* err) {
+  extern __shared__ __align__(16) unsigned char sc_smem[];
+  const SchurTask<T> t = tasks[task_base + blockIdx.x];
   const int n = t.n, k = t.k, r = n - k;
   __shared__ T s_red;
   __shared__ int s_idx, s_flag;
-  T* Pm = t.ws;                       // permuted K_BN
-  T* Wrs = Pm + (size_t)n * n;        // r x k
-  T* Wsr = Wrs + (size_t)r * k;       // k x r
-  T* Lt = Wsr + (size_t)k * r;        // r x k
+  T* base = smem ? reinterpret_cast<T*>(sc_smem) : t.ws;
+  T* Pm = base;                       // n x n
+  T* Wrs = Pm + (size_t)n * n;        // r x k : K~_rs
+  T* Lt = Wrs + (size_t)r * k;        // r x k : K~_sr^T, then L^T
+  T* X = smem ? Lt + (size_t)r * k : t.X;   // r x r (global mode: in place in the output)
   for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
     int i = idx % n, j = idx / n;
     Pm[idx] = t.K[t.perm[i] + (size_t)n * t.perm[j]];
@@ -452,62 +570,48 @@ __global__ void __launch_bounds__(kThreads) k_schur(const SchurTask<T>* tasks, i
   const T* Krs = Pm + k;
   const T* Krr = Pm + k + (size_t)n * k;
   const T* Tm = t.Tin;
-  // K~_rs = K_rs - T^T K_ss  (r x k)
   for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
     int i = idx % r, j = idx / r;
-    Wrs[idx] = Krs[i + (size_t)n * j];
+    Wrs[idx] = Krs[i + (size_t)n * j];        // K_rs
+    Lt[idx] = Ksr[j + (size_t)n * i];         // K_sr^T
   }
-  __syncthreads();
-  cta_gemm<T>(r, k, k, T(-1), Tm, k, true, Kss, n, false, T(1), Wrs, r);
-  // X = K_rr - T^T K_sr - K~_rs T  (r x r)
   for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) {
     int i = idx % r, j = idx / r;
-    t.X[idx] = Krr[i + (size_t)n * j];
-  }
-  // K~_sr = K_sr - K_ss T  (k x r)
-  for (int idx = threadIdx.x; idx < k * r; idx += blockDim.x) {
-    int i = idx % k, j = idx / k;
-    Wsr[idx] = Ksr[i + (size_t)n * j];
+    X[idx] = Krr[i + (size_t)n * j];
   }
   __syncthreads();
-  cta_gemm<T>(r, r, k, T(-1), Tm, k, true, Ksr, n, false, T(1), t.X, r);
+  // K~_rs = K_rs - T^T K_ss ;  K~_sr^T = K_sr^T - T^T K_ss^T ;  X -= T^T K_sr
+  cta_gemm<T>(r, k, k, T(-1), Tm, k, true, Kss, n, false, T(1), Wrs, r);
+  cta_gemm<T>(r, k, k, T(-1), Tm, k, true, Kss, n, true, T(1), Lt, r);
+  cta_gemm<T>(r, r, k, T(-1), Tm, k, true, Ksr, n, false, T(1), X, r);
   __syncthreads();
-  cta_gemm<T>(r, r, k, T(-1), Wrs, r, false, Tm, k, false, T(1), t.X, r);
-  cta_gemm<T>(k, r, k, T(-1), Kss, n, false, Tm, k, false, T(1), Wsr, k);
+  // X -= K~_rs T
+  cta_gemm<T>(r, r, k, T(-1), Wrs, r, false, Tm, k, false, T(1), X, r);
   __syncthreads();
-  int info = cta_lu<T>(r, t.X, r, t.piv, &s_flag, &s_red, &s_idx);
+  int info = cta_lu<T>(r, X, r, t.piv, &s_flag, &s_red, &s_idx);
   if (info != 0 && threadIdx.x == 0) atomicMax(err, (int)kDevSingular);
-  // U = X^-1 K~_rs (r x k)
-  for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) t.U[idx] = Wrs[idx];
-  // L^T = X^-T K~_sr^T (r x k)
-  for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
-    int i = idx % r, j = idx / r;
-    Lt[idx] = Wsr[j + (size_t)k * i];
-  }
+  // L^T = X^-T K~_sr^T
+  cta_lu_solve<T>(r, X, r, t.piv, true, Lt, r, k);
+  // A~ = K_ss - L K~_rs  (k x k), L = Lt^T
+  for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) t.Atil[idx] = Kss[idx % k + (size_t)n * (idx / k)];
   __syncthreads();
-  cta_lu_solve<T>(r, t.X, r, t.piv, false, t.U, r, k);
-  cta_lu_solve<T>(r, t.X, r, t.piv, true, Lt, r, k);
+  cta_gemm<T>(k, k, r, T(-1), Lt, r, true, Wrs, r, false, T(1), t.Atil, k);
+  __syncthreads();
+  // U = X^-1 K~_rs (in place on Wrs)
+  cta_lu_solve<T>(r, X, r, t.piv, false, Wrs, r, k);
+  for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) t.U[idx] = Wrs[idx];
   for (int idx = threadIdx.x; idx < k * r; idx += blockDim.x) {
     int i = idx % k, j = idx / k;
     t.L[idx] = Lt[j + (size_t)r * i];
   }
-  __syncthreads();
-  // A~ = K_ss - L K~_rs  (k x k)
-  for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) {
-    int i = idx % k, j = idx / k;
-    t.Atil[idx] = Kss[i + (size_t)n * j];
-  }
-  __syncthreads();
-  cta_gemm<T>(k, k, r, T(-1), t.L, k, false, Wrs, r, false, T(1), t.Atil, k);
+  if (smem)
+    for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) t.X[idx] = X[idx];
 }
 
-// Dense LU of the root block on one CTA.
 template <typename T>
-__global__ void k_root_lu(T* A, int n, int* piv, int* err) {
-  __shared__ T s_red;
-  __shared__ int s_idx, s_flag;
-  int info = cta_lu<T>(n, A, n, piv, &s_flag, &s_red, &s_idx);
-  if (info != 0 && threadIdx.x == 0) atomicMax(err, (int)kDevSingular);
+size_t schur_bytes(int n, int k) {
+  size_t r = n - k;
+  return sizeof(T) * ((size_t)n * n + 2 * r * k + r * r);
 }
 
 template <typename T>
@@ -600,25 +704,182 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
     cta_lu_solve<T>(r, t.X, r, t.piv, false, xr, n, nc);
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < n * nc; idx += blockDim.x) {
-    int i = idx % n, c = idx / n;
-    x[(size_t)t.pact[i] * ldx + c0 + c] = sx[idx];
+  const int lo = mode == kDiag ? k : 0;   // the diagonal solve changes x_r only
+  for (int idx = threadIdx.x; idx < (n - lo) * nc; idx += blockDim.x) {
+    int i = lo + idx % (n - lo), c = idx / (n - lo);
+    x[(size_t)t.pact[i] * ldx + c0 + c] = sx[i + (size_t)n * c];
   }
 }
 
-// Root solve: y = A^-1 x[idx] (dense LU), scattered back.
+// ws (n x ncols, column-major) <-> rows idx of the DOF-major x
 template <typename T>
-__global__ void k_root_solve(const T* LU, const int* piv, const int* idx, int n, T* x, int ldx,
-                             int ncols, T* ws) {
-  for (int e = threadIdx.x; e < n * ncols; e += blockDim.x) {
+__global__ void k_gather_rows(const T* x, int ldx, const int* idx, int n, int ncols, T* ws) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * ncols; e += gridDim.x * blockDim.x) {
     int i = e % n, c = e / n;
     ws[e] = x[(size_t)idx[i] * ldx + c];
   }
-  __syncthreads();
-  cta_lu_solve<T>(n, LU, n, piv, false, ws, n, ncols);
-  for (int e = threadIdx.x; e < n * ncols; e += blockDim.x) {
+}
+
+template <typename T>
+__global__ void k_scatter_rows(T* x, int ldx, const int* idx, int n, int ncols, const T* ws) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * ncols; e += gridDim.x * blockDim.x) {
     int i = e % n, c = e / n;
     x[(size_t)idx[i] * ldx + c] = ws[e];
+  }
+}
+
+// ------------------------------------------------------- bordered system --
+// Border matrices of a multiply connected problem, DOF-major (row = DOF,
+// nb columns): U (initialize_U_mat, kern_interp/linear_solve.cpp:19-107) and
+// Psi^T (initialize_Psi_mat, :110-199, membership from node ranges).
+template <typename T>
+__global__ void k_border_init(Points<T> P, const double* px, const double* py, const double* pw,
+                              int n_points, int sol_dim, const double* hc, int nh,
+                              const int* hole_of, T* U, T* PsiT) {
+  const int nb = sol_dim == 1 ? nh : 3 * nh;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n_points; p += gridDim.x * blockDim.x) {
+    double x = px[2 * (size_t)p], y = py[2 * (size_t)p];   // interleaved input
+    int hp = hole_of[p];
+    if (sol_dim == 1) {
+      for (int h = 0; h < nh; h++) {
+        double rx = x - hc[2 * h], ry = y - hc[2 * h + 1];
+        U[(size_t)p * nb + h] = T(log(sqrt(rx * rx + ry * ry)));
+        PsiT[(size_t)p * nb + h] = T(h == hp ? pw[p] : 0.0);
+      }
+    } else {
+      T* u0 = U + (size_t)(2 * p) * nb;
+      T* u1 = U + (size_t)(2 * p + 1) * nb;
+      T* q0 = PsiT + (size_t)(2 * p) * nb;
+      T* q1 = PsiT + (size_t)(2 * p + 1) * nb;
+      for (int h = 0; h < nh; h++) {
+        double rx = x - hc[2 * h], ry = y - hc[2 * h + 1];
+        double rn = sqrt(rx * rx + ry * ry), r2 = rn * rn, sc = 1.0 / (4 * kPi);
+        u0[3 * h] = T(sc * (log(1 / rn) + rx * rx / r2));
+        u1[3 * h] = T(sc * (ry * rx / r2));
+        u0[3 * h + 1] = T(sc * (rx * ry / r2));
+        u1[3 * h + 1] = T(sc * (log(1 / rn) + ry * ry / r2));
+        u0[3 * h + 2] = T(ry * (sc / r2));
+        u1[3 * h + 2] = T(-rx * (sc / r2));
+        double w = h == hp ? pw[p] : 0.0;
+        q0[3 * h] = T(w);
+        q1[3 * h] = T(0);
+        q0[3 * h + 1] = T(0);
+        q1[3 * h + 1] = T(w);
+        q0[3 * h + 2] = T(w * y);
+        q1[3 * h + 2] = T(-w * x);
+      }
+    }
+  }
+  (void)P;
+}
+
+__global__ void k_mark(const int* idx, int n, unsigned char* mask) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) mask[idx[i]] = 1;
+}
+
+// Partial sums over row chunks of  out(a, c) = sum_{i not skeleton} A(i, a) B(i, c)
+// (A: N x na, B: N x nc, both DOF-major); deterministic two-stage reduction.
+constexpr int kRedRows = 1024;
+template <typename T>
+__global__ void k_reduce_partial(const T* A, int na, const T* B, int nc, int N,
+                                 const unsigned char* mask, T* partial) {
+  extern __shared__ unsigned char red_smem[];
+  T* As = reinterpret_cast<T*>(red_smem);           // 32 x na
+  T* Bs = As + 32 * (size_t)na;                      // 32 x nc
+  const int r0 = blockIdx.x * kRedRows;
+  const int r1 = min(N, r0 + kRedRows);
+  const int nout = na * nc;
+  T acc[16];
+  for (int q = 0; q < 16; q++) acc[q] = T(0);
+  for (int t0 = r0; t0 < r1; t0 += 32) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * na; e += blockDim.x) {
+      int i = t0 + e / na;
+      As[e] = (i < r1 && !mask[i]) ? A[(size_t)i * na + e % na] : T(0);
+    }
+    for (int e = threadIdx.x; e < 32 * nc; e += blockDim.x) {
+      int i = t0 + e / nc;
+      Bs[e] = i < r1 ? B[(size_t)i * nc + e % nc] : T(0);
+    }
+    __syncthreads();
+    for (int q = 0; q < 16; q++) {
+      int o = threadIdx.x + q * blockDim.x;
+      if (o >= nout) break;
+      int a = o % na, c = o / na;
+      T sum = T(0);
+      for (int i = 0; i < 32; i++) sum += As[i * na + a] * Bs[i * nc + c];
+      acc[q] += sum;
+    }
+  }
+  T* out = partial + (size_t)blockIdx.x * nout;
+  for (int q = 0; q < 16; q++) {
+    int o = threadIdx.x + q * blockDim.x;
+    if (o >= nout) break;
+    out[o] = acc[q];
+  }
+}
+
+template <typename T>
+__global__ void k_reduce_final(const T* partial, int nparts, int nout, T* out) {
+  for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < nout; o += gridDim.x * blockDim.x) {
+    T acc = T(0);
+    for (int p = 0; p < nparts; p++) acc += partial[(size_t)p * nout + o];
+    out[o] = acc;
+  }
+}
+
+// Bordered root system S = [A_root, U~_s; Psi~_s, -I - Psi~_r D^-1 U~_r]
+// (skel_factorization.cpp:524-542).
+template <typename T>
+__global__ void k_assemble_S(const T* A, int nr, const int* idx, const T* Um, const T* PsiTm,
+                             const T* corr, int nb, T* S) {
+  const int ns = nr + nb;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)ns * ns;
+       e += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(e % ns), j = (int)(e / ns);
+    T v;
+    if (i < nr && j < nr) v = A[i + (size_t)nr * j];
+    else if (i >= nr && j < nr) v = PsiTm[(size_t)idx[j] * nb + (i - nr)];
+    else if (i < nr && j >= nr) v = Um[(size_t)idx[i] * nb + (j - nr)];
+    else v = -(i == j ? T(1) : T(0)) - corr[(i - nr) + (size_t)nb * (j - nr)];
+    S[e] = v;
+  }
+}
+
+// M = [x(allskel, :); -t]  ((nr + nb) x nc, column-major)
+template <typename T>
+__global__ void k_mc_rhs(const T* x, int ldx, const int* idx, int nr, const T* t, int nb, int nc,
+                         T* M) {
+  const int ns = nr + nb;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ns * nc; e += gridDim.x * blockDim.x) {
+    int i = e % ns, c = e / ns;
+    M[e] = i < nr ? x[(size_t)idx[i] * ldx + c] : -t[(i - nr) + (size_t)nb * c];
+  }
+}
+
+// x(i, :) -= U~(i, :) alpha for redundant rows (N = w - U~_r alpha).
+template <typename T>
+__global__ void k_mc_update(T* x, int nc, const T* Um, int nb, const T* M, int nr, int N,
+                            const unsigned char* mask) {
+  const int ns = nr + nb;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)N * nc;
+       e += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(e / nc), c = (int)(e % nc);
+    if (mask[i]) continue;
+    T acc = T(0);
+    for (int b = 0; b < nb; b++) acc += Um[(size_t)i * nb + b] * M[nr + b + (size_t)ns * c];
+    x[e] -= acc;
+  }
+}
+
+// x(allskel, :) = M(0:nr, :), alpha (row-major nb x nc) = M(nr:, :)
+template <typename T>
+__global__ void k_mc_finish(T* x, int nc, const int* idx, const T* M, int nr, int nb, T* alpha) {
+  const int ns = nr + nb;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ns * nc; e += gridDim.x * blockDim.x) {
+    int i = e % ns, c = e / ns;
+    if (i < nr) x[(size_t)idx[i] * nc + c] = M[e];
+    else if (alpha) alpha[(size_t)(i - nr) * nc + c] = M[e];
   }
 }
 
@@ -653,6 +914,39 @@ struct HostBox {
 }  // namespace
 
 template <typename T>
+void launch_sweep(Factorization<T>& F, int l, int mode, T* x, int ncols, cudaStream_t s) {
+  LevelFactor& LF = F.levels[l];
+  if (LF.n_comp == 0 || ncols == 0) return;
+  int cw = std::max(1, std::min(ncols, (int)(96 * 1024 / (sizeof(T) * std::max(1, LF.max_n)))));
+  cw = std::min(cw, 32);
+  dim3 grid(LF.n_comp, (ncols + cw - 1) / cw);
+  size_t sm = sizeof(T) * (size_t)LF.max_n * cw;
+  if (sm > 200 * 1024) throw std::runtime_error("box too large for the sweep kernel");
+  if (sm > 48 * 1024)
+    KI_CUDA(cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  k_sweep<T><<<grid, kThreads, sm, s>>>(reinterpret_cast<SweepTask<T>*>(LF.d_tasks), x, ncols,
+                                        ncols, cw, mode);
+  KI_CUDA(cudaGetLastError());
+}
+
+// out (na x nc, column-major) = sum over non-skeleton rows of A(i,:)^T B(i,:)
+template <typename T>
+void reduce_rows(Factorization<T>& F, const T* A, int na, const T* B, int nc, T* out,
+                 cudaStream_t s) {
+  int parts = (F.N + kRedRows - 1) / kRedRows;
+  T* partial = nullptr;
+  KI_CUDA(cudaMallocAsync((void**)&partial, sizeof(T) * (size_t)parts * na * nc + 16, s));
+  if (na * nc > 16 * 256) throw std::runtime_error("border too wide for the row reduction");
+  size_t sm = sizeof(T) * 32 * (size_t)(na + nc);
+  if (sm > 48 * 1024)
+    KI_CUDA(cudaFuncSetAttribute(k_reduce_partial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  k_reduce_partial<T><<<parts, 256, sm, s>>>(A, na, B, nc, F.N, F.d_is_skel, partial);
+  k_reduce_final<T><<<std::max(1, (na * nc + 255) / 256), 256, 0, s>>>(partial, parts, na * nc, out);
+  KI_CUDA(cudaGetLastError());
+  KI_CUDA(cudaFreeAsync(partial, s));
+}
+
+template <typename T>
 std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, const double* points,
                                             const double* normals, const double* weights,
                                             const double* curvatures, const HoleDesc& holes,
@@ -671,8 +965,12 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
   cudaStream_t s = stream;
 
   // point data
+  double* d_pts_in = nullptr;
+  double* d_w_in = nullptr;
   {
     double* d_in = (double*)F->alloc(sizeof(double) * (size_t)n_points * 6);
+    d_pts_in = d_in;
+    d_w_in = d_in + 4 * (size_t)n_points;
     KI_CUDA(cudaMemcpyAsync(d_in, points, sizeof(double) * 2 * n_points, cudaMemcpyHostToDevice, s));
     KI_CUDA(cudaMemcpyAsync(d_in + 2 * (size_t)n_points, normals, sizeof(double) * 2 * n_points,
                             cudaMemcpyHostToDevice, s));
@@ -754,7 +1052,11 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     if (!atasks.empty()) {
       ActiveTask* d_at = (ActiveTask*)F->alloc(sizeof(ActiveTask) * atasks.size());
       upload(d_at, atasks, s);
+      double nb = 0;
+      for (auto& a : atasks) nb += 8.0 * (a.len[0] + a.len[1] + a.len[2] + a.len[3]);
+      F->stage_begin("active_lists", 0, nb);
       k_build_active<<<(unsigned)atasks.size(), 128, 0, s>>>(d_at, ipool);
+      F->stage_end();
       KI_CUDA(cudaGetLastError());
     }
     if (l == 0) break;
@@ -798,7 +1100,11 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     if (!asm_tasks.empty()) {
       AsmTask<T>* d_as = (AsmTask<T>*)F->alloc(sizeof(AsmTask<T>) * asm_tasks.size());
       upload(d_as, asm_tasks, s);
+      double ne = 0;
+      for (auto& a : asm_tasks) ne += (double)a.n * a.n;
+      F->stage_begin("assemble", 12.0 * ne, (double)sizeof(T) * ne);
       k_assemble<T><<<(unsigned)asm_tasks.size(), kThreads, 0, s>>>(d_as, ipool, P, sd);
+      F->stage_end();
       KI_CUDA(cudaGetLastError());
     }
 
@@ -850,7 +1156,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       rows_cap += cand + 1;
       int64_t n = h.n;
       it.ws = ws_cap;
-      ws_cap += n * n + kFoldRows * n + 2 * n + n * n / 4 + 1;
+      ws_cap += n * n + n * n / 4 + 1;
       it.perm = perm_cap;
       perm_cap += n;
       itasks.push_back(it);
@@ -866,6 +1172,30 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       pact_top += it.n;
     }
     for (size_t i = 0; i < comp.size(); i++) hb[comp[i]].pact = itasks[i].pact;
+    // group the boxes by where the ID working set fits: triangle in shared
+    // memory (mode 0), triangle in global scratch (1), everything global (2)
+    const size_t smem_cap = 225 * 1024;
+    std::vector<int> mode_of(itasks.size());
+    for (size_t i = 0; i < itasks.size(); i++) {
+      int n = itasks[i].n;
+      mode_of[i] = id_smem_bytes<T>(n, 0) <= smem_cap ? 0 : 1;
+    }
+    {
+      std::vector<size_t> order(itasks.size());
+      std::iota(order.begin(), order.end(), 0);
+      std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return mode_of[a] < mode_of[b]; });
+      std::vector<IdTask> it2;
+      std::vector<int> comp2, mode2;
+      for (size_t o : order) {
+        it2.push_back(itasks[o]);
+        comp2.push_back(comp[o]);
+        mode2.push_back(mode_of[o]);
+      }
+      itasks.swap(it2);
+      comp.swap(comp2);
+      mode_of.swap(mode2);
+      for (size_t i = 0; i < comp.size(); i++) hb[comp[i]].pact = itasks[i].pact;
+    }
     IdTask* d_it = (IdTask*)F->alloc(sizeof(IdTask) * itasks.size());
     int64_t* d_soff = (int64_t*)F->alloc(sizeof(int64_t) * (seg_off.size() + 1));
     int* d_slen = (int*)F->alloc(sizeof(int) * (seg_len.size() + 1));
@@ -873,13 +1203,60 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     upload(d_it, itasks, s);
     upload(d_soff, seg_off, s);
     upload(d_slen, seg_len, s);
-    k_id<T><<<(unsigned)itasks.size(), kThreads, 0, s>>>(d_it, d_soff, d_slen, ipool, d_irows, d_tws, P, sd,
-                                                         np, d_pcs, d_pcs + np, prm.id_tol, d_k,
-                                                         F->d_err);
+    int* d_m = (int*)F->alloc(sizeof(int) * itasks.size());
+    std::string id_name = "id@L" + std::to_string(l);
+    F->stage_begin(id_name.c_str(), 0, 0);
+    size_t id_rec = F->prof_open.size() - 1;
+    for (int md = 0; md < 3; md++) {
+      int first = -1, cnt = 0;
+      size_t sm = 0;
+      for (size_t i = 0; i < itasks.size(); i++)
+        if (mode_of[i] == md) {
+          if (first < 0) first = (int)i;
+          cnt++;
+          sm = std::max(sm, id_smem_bytes<T>(itasks[i].n, md));
+        }
+      if (cnt == 0) continue;
+      if (sm > smem_cap) throw std::runtime_error("box too large for the ID kernel");
+      KI_CUDA(cudaFuncSetAttribute(k_id<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
+      k_id<T><<<(unsigned)cnt, kThreads, sm, s>>>(d_it, first, d_soff, d_slen, ipool, d_irows, d_tws,
+                                                  P, sd, np, d_pcs, d_pcs + np, prm.id_tol, d_k,
+                                                  d_m, md);
+      KI_CUDA(cudaGetLastError());
+    }
+    F->stage_end();
     KI_CUDA(cudaGetLastError());
-    std::vector<int> kh(itasks.size());
+    std::vector<int> kh(itasks.size()), mh(itasks.size());
     KI_CUDA(cudaMemcpyAsync(kh.data(), d_k, sizeof(int) * kh.size(), cudaMemcpyDeviceToHost, s));
+    KI_CUDA(cudaMemcpyAsync(mh.data(), d_m, sizeof(int) * mh.size(), cudaMemcpyDeviceToHost, s));
     KI_CUDA(cudaStreamSynchronize(s));
+    {
+      LevelStat ls;
+      ls.level = l;
+      ls.boxes = (int)lv.size();
+      ls.id_boxes = (int)itasks.size();
+      for (size_t i = 0; i < itasks.size(); i++) {
+        ls.max_n = std::max(ls.max_n, itasks[i].n);
+        ls.max_m = std::max(ls.max_m, mh[i]);
+        ls.max_k = std::max(ls.max_k, kh[i]);
+        ls.sum_n += itasks[i].n;
+        ls.sum_m += mh[i];
+        ls.sum_k += kh[i];
+        ls.compressed += kh[i] > 0;
+        ls.mode_count[mode_of[i]]++;
+      }
+      F->level_stats.push_back(ls);
+    }
+    {
+      double fl = 0, by = 0;
+      for (size_t i = 0; i < itasks.size(); i++) {
+        double m = mh[i], n = itasks[i].n, k = kh[i] > 0 ? kh[i] : std::min(m, n), r = n - k;
+        fl += std::max(0.0, 4 * m * n * k - 2 * k * k * (m + n) + 4.0 / 3.0 * k * k * k + k * k * r);
+        by += sizeof(T) * (double)k * r;
+      }
+      F->prof_open[id_rec].flops = fl;
+      F->prof_open[id_rec].bytes = by;
+    }
 
     // ---- Schur elimination of the compressed boxes
     std::vector<int> ci_list;
@@ -914,7 +1291,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       t.n = n;
       t.k = k;
       t.perm = d_irows + itasks[i].perm;
-      t.Tin = d_tws + itasks[i].ws + (int64_t)n * n + kFoldRows * (int64_t)n + 2 * (int64_t)n;
+      t.Tin = d_tws + itasks[i].ws + (int64_t)n * n;   // Tout of k_id
       t.Tout = d_Tp + o_tr;
       t.L = d_LUp + 2 * o_tr;
       t.U = d_LUp + 2 * o_tr + (int64_t)k * r;
@@ -947,8 +1324,33 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       LF.max_n = std::max(LF.max_n, n);
     }
     SchurTask<T>* d_st = (SchurTask<T>*)F->alloc(sizeof(SchurTask<T>) * st.size());
-    upload(d_st, st, s);
-    k_schur<T><<<(unsigned)st.size(), kThreads, 0, s>>>(d_st, F->d_err);
+    double sf = 0, sb = 0;
+    for (auto& q : st) {
+      double k = q.k, r = q.n - q.k, n = q.n;
+      sf += 2 * r * k * k + 4 * r * r * k + 2 * k * k * r + 2.0 / 3.0 * r * r * r + 4 * r * r * k + 2 * k * k * r;
+      sb += sizeof(T) * (n * n + 3 * k * r + r * r + k * k);
+    }
+    std::string sc_name = "schur@L" + std::to_string(l);
+    F->stage_begin(sc_name.c_str(), sf, sb);
+    {
+      // shared-memory boxes first, then the ones whose working set is global
+      const size_t cap = 225 * 1024;
+      std::vector<SchurTask<T>> st2;
+      size_t sm = 0;
+      int n_sm = 0;
+      for (auto& q : st)
+        if (schur_bytes<T>(q.n, q.k) <= cap) { st2.push_back(q); sm = std::max(sm, schur_bytes<T>(q.n, q.k)); n_sm++; }
+      for (auto& q : st)
+        if (schur_bytes<T>(q.n, q.k) > cap) st2.push_back(q);
+      upload(d_st, st2, s);
+      if (n_sm > 0) {
+        KI_CUDA(cudaFuncSetAttribute(k_schur<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
+        k_schur<T><<<(unsigned)n_sm, kThreads, sm, s>>>(d_st, 0, 1, F->d_err);
+      }
+      if ((int)st2.size() > n_sm)
+        k_schur<T><<<(unsigned)(st2.size() - n_sm), kThreads, 0, s>>>(d_st, n_sm, 0, F->d_err);
+    }
+    F->stage_end();
     KI_CUDA(cudaGetLastError());
     SweepTask<T>* d_sw = (SweepTask<T>*)F->alloc(sizeof(SweepTask<T>) * sw.size());
     upload(d_sw, sw, s);
@@ -986,17 +1388,69 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       KI_CUDA(cudaMemcpyAsync(d_as, &at, sizeof(at), cudaMemcpyHostToDevice, s));
       k_assemble<T><<<1, kThreads, 0, s>>>(d_as, ipool, P, sd);
       KI_CUDA(cudaGetLastError());
-      if (holes.n_holes > 0) throw std::runtime_error("multiply connected problems: not yet supported");
-      F->d_root_lu = A;
-      F->d_root_piv = (int*)F->alloc(sizeof(int) * h.n);
-      k_root_lu<T><<<1, 1024, 0, s>>>(A, h.n, F->d_root_piv, F->d_err);
-      KI_CUDA(cudaGetLastError());
-      F->n_root_sys = h.n;
+      F->d_is_skel = (unsigned char*)F->alloc(N);
+      KI_CUDA(cudaMemsetAsync(F->d_is_skel, 0, N, s));
+      k_mark<<<std::max(1, (h.n + 255) / 256), 256, 0, s>>>(F->d_root_idx, h.n, F->d_is_skel);
+      if (holes.n_holes == 0) {
+        F->d_root_lu = A;
+        F->d_root_piv = (int*)F->alloc(sizeof(int) * h.n);
+        F->stage_begin("root_lu", 2.0 / 3.0 * (double)h.n * h.n * h.n, (double)sizeof(T) * h.n * h.n);
+        dense_lu<T>(A, h.n, F->d_root_piv, F->d_err, s);
+        F->stage_end();
+        KI_CUDA(cudaGetLastError());
+        F->n_root_sys = h.n;
+      } else {
+        // Bordered system (skel_factorization.cpp:311-547): sweep U and Psi^T
+        // through every level, apply X_rr^-1 to U's redundant rows, form and
+        // factor S.
+        const int nh = holes.n_holes;
+        const int nb = sd == 1 ? nh : 3 * nh;
+        F->n_border = nb;
+        std::vector<int> hole_of(n_points, -1);
+        for (int q = 0; q < nh; q++)
+          for (int p = holes.start[q]; p < holes.start[q] + holes.count[q]; p++) hole_of[p] = q;
+        int* d_hole_of = (int*)F->alloc(sizeof(int) * n_points);
+        upload(d_hole_of, hole_of, s);
+        double* d_hc = (double*)F->alloc(sizeof(double) * 2 * nh);
+        upload(d_hc, holes.centers, s);
+        F->d_Umod = (T*)F->alloc(Tsz * (size_t)N * nb);
+        F->d_PsiTmod = (T*)F->alloc(Tsz * (size_t)N * nb);
+        k_border_init<T><<<std::min(2048, (n_points + 255) / 256), 256, 0, s>>>(
+            P, d_pts_in, d_pts_in + 1, d_w_in, n_points, sd, d_hc, nh, d_hole_of, F->d_Umod,
+            F->d_PsiTmod);
+        KI_CUDA(cudaGetLastError());
+        F->stage_begin("border_sweeps", 0, 0);
+        for (int l = L - 1; l >= 1; l--) {
+          launch_sweep<T>(*F, l, kUp, F->d_Umod, nb, s);
+          launch_sweep<T>(*F, l, kPsi, F->d_PsiTmod, nb, s);
+        }
+        T* dD = nullptr;
+        KI_CUDA(cudaMallocAsync((void**)&dD, Tsz * (size_t)N * nb, s));
+        KI_CUDA(cudaMemcpyAsync(dD, F->d_Umod, Tsz * (size_t)N * nb, cudaMemcpyDeviceToDevice, s));
+        for (int l = L - 1; l >= 1; l--) launch_sweep<T>(*F, l, kDiag, dD, nb, s);
+        T* corr = (T*)F->alloc(Tsz * (size_t)nb * nb);
+        reduce_rows<T>(*F, F->d_PsiTmod, nb, dD, nb, corr, s);
+        F->stage_end();
+        KI_CUDA(cudaFreeAsync(dD, s));
+        const int ns = h.n + nb;
+        T* S = (T*)F->alloc(Tsz * (size_t)ns * ns);
+        k_assemble_S<T><<<std::min(4096, (int)(((size_t)ns * ns + 255) / 256)), 256, 0, s>>>(
+            A, h.n, F->d_root_idx, F->d_Umod, F->d_PsiTmod, corr, nb, S);
+        KI_CUDA(cudaGetLastError());
+        F->d_root_lu = S;
+        F->d_root_piv = (int*)F->alloc(sizeof(int) * ns);
+        F->stage_begin("root_lu", 2.0 / 3.0 * (double)ns * ns * ns, (double)sizeof(T) * ns * ns);
+        dense_lu<T>(S, ns, F->d_root_piv, F->d_err, s);
+        F->stage_end();
+        KI_CUDA(cudaGetLastError());
+        F->n_root_sys = ns;
+      }
     }
   }
   int herr = 0;
   KI_CUDA(cudaMemcpyAsync(&herr, F->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
   KI_CUDA(cudaStreamSynchronize(s));
+  F->factor_prof = F->collect();
   if (herr == kDevSingular) throw std::runtime_error("singular pivot in a Schur or root LU factorization");
   if (herr == kDevNonFinite) throw std::runtime_error("non-finite values in the factorization");
   F->factor_seconds =
@@ -1008,29 +1462,69 @@ template <typename T>
 void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha) {
   cudaStream_t s = F.stream;
   const int L = (int)F.levels.size();
-  auto launch = [&](int l, int mode) {
-    LevelFactor& LF = F.levels[l];
-    if (LF.n_comp == 0) return;
-    int cw = std::max(1, std::min(ncols, (int)(96 * 1024 / (sizeof(T) * std::max(1, LF.max_n)))));
-    cw = std::min(cw, 32);
-    dim3 grid(LF.n_comp, (ncols + cw - 1) / cw);
-    size_t sm = sizeof(T) * (size_t)LF.max_n * cw;
-    if (sm > 200 * 1024) throw std::runtime_error("box too large for the sweep kernel");
-    if (sm > 48 * 1024)
-      KI_CUDA(cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_sweep<T><<<grid, kThreads, sm, s>>>(reinterpret_cast<SweepTask<T>*>(LF.d_tasks), d_x, ncols, ncols,
-                                          cw, mode);
-    KI_CUDA(cudaGetLastError());
-  };
-  for (int l = L - 1; l >= 1; l--) launch(l, kUpDiag);
-  if (F.n_root > 0) {
-    T* ws = (T*)F.alloc(sizeof(T) * (size_t)F.n_root * ncols);
-    k_root_solve<T><<<1, 1024, 0, s>>>(F.d_root_lu, F.d_root_piv, F.d_root_idx, F.n_root, d_x,
-                                       ncols, ncols, ws);
-    KI_CUDA(cudaGetLastError());
+  const int nr = F.n_root;
+  const bool prof = F.profile_solve;
+  auto sb = [&](const char* name) { if (prof) F.stage_begin(name, 0, 0); };
+  auto se = [&]() { if (prof) F.stage_end(); };
+  if (F.n_border == 0) {
+    // SkelFactorization::solve (skel_factorization.cpp:595-778); the diagonal
+    // solves are fused into the upward pass (each box's redundant rows are
+    // final once its level has been swept).
+    for (int l = L - 1; l >= 1; l--) {
+      sb("sweep_up");
+      launch_sweep<T>(F, l, kUpDiag, d_x, ncols, s);
+      se();
+    }
+    if (nr > 0) {
+      sb("root_solve");
+      T* ws = nullptr;
+      KI_CUDA(cudaMallocAsync((void**)&ws, sizeof(T) * (size_t)nr * ncols + 16, s));
+      int gb = std::max(1, std::min(4096, (nr * ncols + 255) / 256));
+      k_gather_rows<T><<<gb, 256, 0, s>>>(d_x, ncols, F.d_root_idx, nr, ncols, ws);
+      dense_lu_solve<T>(F.d_root_lu, nr, F.d_root_piv, ws, nr, ncols, false, s);
+      k_scatter_rows<T><<<gb, 256, 0, s>>>(d_x, ncols, F.d_root_idx, nr, ncols, ws);
+      se();
+      KI_CUDA(cudaGetLastError());
+      KI_CUDA(cudaFreeAsync(ws, s));
+    }
+    for (int l = 1; l < L; l++) {
+      sb("sweep_down");
+      launch_sweep<T>(F, l, kDown, d_x, ncols, s);
+      se();
+    }
+    return;
   }
-  for (int l = 1; l < L; l++) launch(l, kDown);
-  (void)d_alpha;
+  // SkelFactorization::multiply_connected_solve (skel_factorization.cpp:781-1141),
+  // every column at once.
+  const int nb = F.n_border, ns = nr + nb, N = F.N;
+  sb("sweep_up");
+  for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kUp, d_x, ncols, s);
+  se();
+  sb("border_solve");
+  T *Dw = nullptr, *t = nullptr, *M = nullptr;
+  KI_CUDA(cudaMallocAsync((void**)&Dw, sizeof(T) * (size_t)N * ncols + 16, s));
+  KI_CUDA(cudaMallocAsync((void**)&t, sizeof(T) * (size_t)nb * ncols + 16, s));
+  KI_CUDA(cudaMallocAsync((void**)&M, sizeof(T) * (size_t)ns * ncols + 16, s));
+  KI_CUDA(cudaMemcpyAsync(Dw, d_x, sizeof(T) * (size_t)N * ncols, cudaMemcpyDeviceToDevice, s));
+  for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kDiag, Dw, ncols, s);
+  reduce_rows<T>(F, F.d_PsiTmod, nb, Dw, ncols, t, s);                 // Psi~_r D^-1 w
+  k_mc_rhs<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
+      d_x, ncols, F.d_root_idx, nr, t, nb, ncols, M);
+  dense_lu_solve<T>(F.d_root_lu, ns, F.d_root_piv, M, ns, ncols, false, s);
+  k_mc_update<T><<<std::min(8192, (int)(((size_t)N * ncols + 255) / 256)), 256, 0, s>>>(
+      d_x, ncols, F.d_Umod, nb, M, nr, N, F.d_is_skel);                // w - U~_r alpha
+  KI_CUDA(cudaGetLastError());
+  for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kDiag, d_x, ncols, s);
+  se();
+  k_mc_finish<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
+      d_x, ncols, F.d_root_idx, M, nr, nb, d_alpha);
+  KI_CUDA(cudaGetLastError());
+  sb("sweep_down");
+  for (int l = 1; l < L; l++) launch_sweep<T>(F, l, kDown, d_x, ncols, s);
+  se();
+  KI_CUDA(cudaFreeAsync(Dw, s));
+  KI_CUDA(cudaFreeAsync(t, s));
+  KI_CUDA(cudaFreeAsync(M, s));
 }
 
 template std::unique_ptr<Factorization<double>> factorize<double>(

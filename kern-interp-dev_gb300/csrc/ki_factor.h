@@ -32,6 +32,28 @@ struct LevelFactor {
   int max_n = 0;           // largest active set among them
 };
 
+// Device-time record of one launch group (CUDA events on the factor's stream).
+struct StageRec {
+  std::string stage;
+  cudaEvent_t a = nullptr, b = nullptr;
+  double flops = 0;     // algorithmic flops of the launch
+  double bytes = 0;     // algorithmic bytes of the launch
+};
+
+struct StageSum {
+  std::string stage;
+  int launches = 0;
+  double ms = 0, flops = 0, bytes = 0;
+};
+
+// Per-level shape statistics of the compressed boxes.
+struct LevelStat {
+  int level = 0, boxes = 0, id_boxes = 0, compressed = 0;
+  int max_n = 0, max_m = 0, max_k = 0;
+  double sum_n = 0, sum_m = 0, sum_k = 0;
+  int mode_count[3] = {0, 0, 0};
+};
+
 template <typename T>
 struct Factorization {
   Params prm;
@@ -59,6 +81,14 @@ struct Factorization {
   int n_compressed = 0;
   long n_redundant = 0;
   std::vector<int> rank_hist;
+  bool profile_solve = false;        // record stage events in solves
+  std::vector<StageRec> prof_open;   // launches recorded since the last collect
+  std::vector<StageSum> factor_prof; // per stage, factorization
+  std::vector<LevelStat> level_stats;
+  std::vector<StageSum> solve_prof;  // per stage, last solve
+  void stage_begin(const char* name, double flops, double bytes);
+  void stage_end();
+  std::vector<StageSum> collect();   // synchronizes the stream
   double factor_seconds = 0;
   size_t device_bytes = 0;
   std::vector<void*> owned;   // device allocations to free

@@ -1,0 +1,102 @@
+"""Generate the golden fixtures in this folder from the REFERENCE's own CPU
+solver (kern_interp, compiled from its sources by oracle/build_ref.py).
+
+Run in a container where the reference tree is available:
+    python tests/golden/make_golden.py
+Each fixture stores the reference's solution (mu, and alpha for holes) and
+statistics (levels, root skeleton size, compressed boxes, redundant DOFs),
+the input arrays themselves (boundary generators are not bit-reproducible
+across CPU architectures: libm and numpy differ in the last bits), and a
+SHA-1 of those inputs.  The inputs were made by
+kern-interp-dev_gb300/geometry.py (seeded).
+"""
+import hashlib
+import importlib.util
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+
+def load_geometry():
+    spec = importlib.util.spec_from_file_location(
+        "ki_geometry", os.path.join(ROOT, "kern-interp-dev_gb300", "geometry.py"))
+    g = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(g)
+    return g
+
+
+def input_hash(prob, rhs):
+    h = hashlib.sha1()
+    for a in (prob.points, prob.normals, prob.weights, prob.curvatures, rhs):
+        h.update(np.ascontiguousarray(a, np.float64).tobytes())
+    return h.hexdigest()
+
+
+def stokes_rhs(prob, src=(2.5, 0.0), force=(1.0, 0.5)):
+    """Boundary velocity of a 2D Stokeslet (interleaved per node)."""
+    d = prob.points - np.asarray(src)[None]
+    r2 = (d ** 2).sum(1)
+    f = np.asarray(force)
+    u = (-0.5 * np.log(r2)[:, None] * f[None] + d * (d @ f)[:, None] / r2[:, None]) / (4 * np.pi)
+    return u.reshape(-1, 1)
+
+
+def cases():
+    """(name, problem, rhs, params) for every fixture; shared with the tests."""
+    g = load_geometry()
+    out = []
+    prob, src, _ = g.star_c1()
+    out.append(("star_c1", prob, g.laplace_source_rhs(prob, src),
+                dict(tol=1e-10, proxy=64, ratio=1.5 / np.sqrt(2), leaf=64, min_compress=64,
+                     solution_dim=1, pde=0)))
+    prob = g.star(64, 16)
+    out.append(("star_1024_default", prob, g.laplace_source_rhs(prob, np.array([[3.0, 3.0]])),
+                dict(tol=1e-10, proxy=128, ratio=2.0, leaf=64, min_compress=64, solution_dim=1, pde=0)))
+    prob = g.circle(1000, 0.25)
+    out.append(("circle_1000", prob, g.laplace_source_rhs(prob, np.array([[-3.0, -2.0]])),
+                dict(tol=1e-10, proxy=128, ratio=2.0, leaf=64, min_compress=64, solution_dim=1, pde=0)))
+    prob = g.star(128, 16)
+    out.append(("star_2048_tol1e-4", prob, g.laplace_source_rhs(prob, np.array([[2.0, -2.5]])),
+                dict(tol=1e-4, proxy=128, ratio=2.0, leaf=64, min_compress=64, solution_dim=1, pde=0)))
+    prob = g.star(4, 16)
+    out.append(("star_64_root_leaf", prob, g.laplace_source_rhs(prob, np.array([[3.0, 3.0]])),
+                dict(tol=1e-10, proxy=128, ratio=2.0, leaf=64, min_compress=64, solution_dim=1, pde=0)))
+    prob = g.disc_with_ellipses(1 << 13, 6, seed=1)
+    rng = np.random.default_rng(2)
+    out.append(("disc6_8k", prob, g.laplace_source_rhs(prob, g.random_sources(3, rng)),
+                dict(tol=1e-10, proxy=128, ratio=2.0, leaf=64, min_compress=64, solution_dim=1, pde=0)))
+    prob = g.star(64, 16, amp=0.2, k=3)
+    out.append(("stokes_star_2048", prob, stokes_rhs(prob),
+                dict(tol=1e-10, proxy=128, ratio=2.0, leaf=64, min_compress=64, solution_dim=2, pde=3)))
+    return out
+
+
+def main():
+    import oracle
+    for name, prob, rhs, p in cases():
+        mu_cols, al_cols = [], []
+        st = None
+        for c in range(rhs.shape[1]):   # the reference's bordered solve handles one column
+            mu, al, st = oracle.solve(prob, rhs[:, c:c + 1], p["tol"], threads=8, leaf=p["leaf"],
+                                      proxy=p["proxy"], ratio=p["ratio"],
+                                      min_compress=p["min_compress"],
+                                      solution_dim=p["solution_dim"], pde=p["pde"], impl="ref")
+            mu_cols.append(mu[:, 0])
+            al_cols.append(al[:, 0] if al.size else np.zeros(0))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), mu=np.stack(mu_cols, 1),
+                            alpha=np.stack(al_cols, 1), input_sha1=input_hash(prob, rhs),
+                            points=prob.points, normals=prob.normals, weights=prob.weights,
+                            curvatures=prob.curvatures, rhs=rhs, hole_centers=prob.hole_centers,
+                            hole_start=prob.hole_start, hole_count=prob.hole_count,
+                            levels=st["levels"], root=st["root"], compressed=st["compressed"],
+                            redundant=st["redundant"])
+        print(name, prob.n, st)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,161 @@
+"""GPU parity through the C ABI: the CUDA factor + solve against the
+reference's own outputs (golden fixtures) and against the CPU oracle on
+freshly generated boundaries.  Tolerance (FP64 form): solution difference
+<= 10 x id_tol relative (max-norm), the bar the solver's documentation states."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = ["star_c1", "star_1024_default", "circle_1000", "star_2048_tol1e-4",
+          "star_64_root_leaf", "disc6_8k", "stokes_star_2048"]
+
+
+def factor_for(pkg, prob, p, precision=0):
+    return pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, id_tol=p["tol"],
+                      solution_dimension=p["solution_dim"], pde=p["pde"],
+                      hole_centers=prob.hole_centers if prob.n_holes else None,
+                      hole_start=prob.hole_start if prob.n_holes else None,
+                      hole_count=prob.hole_count if prob.n_holes else None,
+                      max_leaf_dofs=p["leaf"], num_proxy_points=p["proxy"],
+                      radius_ratio=p["ratio"], min_dofs_to_compress=p["min_compress"],
+                      precision=precision)
+
+
+def rel_max(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("name", GOLDEN)
+def test_gpu_matches_reference_fixture(pkg, golden_cases, name):
+    prob, rhs, p, data, h = golden_cases[name]
+    assert str(data["input_sha1"]) == h
+    fac = factor_for(pkg, prob, p)
+    res = fac.solve(rhs)
+    mu, alpha = res if isinstance(res, tuple) else (res, None)
+    assert rel_max(mu, data["mu"]) <= 10 * p["tol"]
+    info = fac.info()
+    assert info["n_levels"] == int(data["levels"])
+    assert info["n_root"] == int(data["root"])
+    assert info["n_compressed"] == int(data["compressed"])
+    assert info["n_redundant"] == int(data["redundant"])
+    if alpha is not None:
+        # the border unknowns of an exterior-source field vanish analytically
+        # (|alpha| ~ 1e-13): compare on the scale of the density
+        assert np.abs(alpha - data["alpha"]).max() <= 10 * p["tol"] * np.abs(data["mu"]).max()
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_gpu_matches_oracle_random_stars(pkg, oracle_mod, seed):
+    rng = np.random.default_rng(100 + seed)
+    amp = rng.uniform(0.1, 0.35)
+    k = int(rng.integers(2, 9))
+    panels = int(rng.integers(40, 400))
+    prob = pkg.geometry.star(panels, 16, amp=amp, k=k)
+    src = pkg.geometry.random_sources(2, rng)
+    f = pkg.geometry.laplace_source_rhs(prob, src)
+    tol = float(10.0 ** rng.uniform(-11, -5))
+    mu_ref, _, st = oracle_mod.solve(prob, f, tol, threads=4)
+    fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, id_tol=tol)
+    mu = fac.solve(f)
+    assert rel_max(mu, mu_ref) <= 10 * tol
+    assert fac.info()["n_root"] == st["root"]
+
+
+def test_gpu_holes_against_oracle_and_field(pkg, oracle_mod):
+    g = pkg.geometry
+    prob = g.disc_with_ellipses(1 << 15, 16, seed=7)
+    rng = np.random.default_rng(3)
+    src = g.random_sources(4, rng)
+    f = g.laplace_source_rhs(prob, src)
+    tol = 1e-10
+    mu_ref, al_ref, _ = oracle_mod.solve(prob, f, tol, threads=8)
+    fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, id_tol=tol,
+                     hole_centers=prob.hole_centers, hole_start=prob.hole_start,
+                     hole_count=prob.hole_count)
+    mu, al = fac.solve(f)
+    assert rel_max(mu, mu_ref) <= 10 * tol
+    assert np.abs(al - al_ref).max() <= 10 * tol * np.abs(mu_ref).max()
+    tg = g.domain_targets(prob, 40, rng)
+    u = fac.eval_targets(tg, mu, al)
+    ue = g.laplace_source_field(tg, src)
+    assert np.abs(u - ue).max() <= 1e-8 * np.abs(ue).max()
+
+
+def test_gpu_multi_rhs_equals_single_columns(pkg):
+    g = pkg.geometry
+    prob = g.star(256, 16)
+    rng = np.random.default_rng(5)
+    F = g.laplace_source_rhs(prob, g.random_sources(33, rng))
+    fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, id_tol=1e-9)
+    X = fac.solve(F)
+    for c in (0, 17, 32):
+        np.testing.assert_array_equal(X[:, c], fac.solve(F[:, c]))
+
+
+def test_gpu_deterministic(pkg):
+    g = pkg.geometry
+    prob = g.disc_with_ellipses(1 << 13, 4, seed=11)
+    f = g.laplace_source_rhs(prob, np.array([[3.0, 0.5], [-2.6, 1.0]]))
+    kw = dict(id_tol=1e-9, hole_centers=prob.hole_centers, hole_start=prob.hole_start,
+              hole_count=prob.hole_count)
+    a = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, **kw).solve(f)
+    b = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, **kw).solve(f)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+
+
+@pytest.mark.parametrize("tol", [1e-6, 1e-10])
+def test_gpu_dense_residual(pkg, tol):
+    """Backward error against the dense FP64 operator (solve_err,
+    kern_interp/linear_solve.cpp:339-426) <= 50 id_tol
+    (kern_interp/kern_interp_test.cpp:29-32)."""
+    g = pkg.geometry
+    prob = g.star(1024, 16, amp=0.3, k=5)
+    f = g.laplace_source_rhs(prob, np.array([[3.0, 3.0], [0.0, -2.0]]))
+    fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, id_tol=tol)
+    mu = fac.solve(f)
+    r = fac.apply(mu) - f
+    assert np.linalg.norm(r) / np.linalg.norm(f) <= 50 * tol
+
+
+def test_gpu_nothing_compresses(pkg, oracle_mod):
+    """min_dofs_to_compress above every box: the root holds every DOF and the
+    factorization is a dense LU."""
+    g = pkg.geometry
+    prob = g.star(32, 16)
+    f = g.laplace_source_rhs(prob, np.array([[3.0, 3.0]]))
+    fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, id_tol=1e-10,
+                     min_dofs_to_compress=100000)
+    mu = fac.solve(f)
+    assert fac.info()["n_root"] == prob.n and fac.info()["n_compressed"] == 0
+    K = oracle_mod.dense_matrix(prob)
+    np.testing.assert_allclose(mu, np.linalg.solve(K, f), rtol=0, atol=1e-11 * np.abs(mu).max())
+
+
+def test_gpu_fp32_factorization_accuracy(pkg, oracle_mod):
+    """FP32 form: the factorization is a preconditioner-grade approximate
+    inverse; its solution stays within 1e-4 of the FP64 oracle."""
+    g = pkg.geometry
+    prob = g.star(256, 16)
+    f = g.laplace_source_rhs(prob, np.array([[3.0, 3.0]]))
+    ref, _, _ = oracle_mod.solve(prob, f, 1e-10, threads=4)
+    fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, id_tol=1e-5,
+                     precision=pkg.PRECISION_FP32)
+    mu = fac.solve(f)
+    assert rel_max(mu, ref) <= 1e-4
+
+
+def test_solve_device_pointer_path(pkg):
+    torch = pytest.importorskip("torch")
+    g = pkg.geometry
+    prob = g.star(128, 16)
+    F = g.laplace_source_rhs(prob, np.array([[3.0, 3.0], [-3.0, 2.5]]))
+    fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, id_tol=1e-10)
+    host = fac.solve(F)
+    db = torch.tensor(np.asfortranarray(F).T.copy(), dtype=torch.float64, device="cuda")  # (nrhs, N) rows = columns
+    dx = torch.empty_like(db)
+    torch.cuda.synchronize()
+    fac.solve_device(db.data_ptr(), dx.data_ptr(), F.shape[1])
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(dx.cpu().numpy().T, host)
