@@ -599,11 +599,11 @@ int ki_factor_get_profile(ki_factor* f, char* buf, int len) {
         snprintf(tmp, sizeof(tmp),
                  "%s{\"level\": %d, \"boxes\": %d, \"id_boxes\": %d, \"compressed\": %d, "
                  "\"max_n\": %d, \"mean_n\": %.1f, \"max_m\": %d, \"mean_m\": %.1f, "
-                 "\"max_k\": %d, \"mean_k\": %.1f, \"modes\": [%d, %d, %d]}",
+                 "\"max_k\": %d, \"mean_k\": %.1f, \"paths\": [%d, %d, %d, %d]}",
                  i ? ", " : "", q.level, q.boxes, q.id_boxes, q.compressed, q.max_n,
                  q.sum_n / std::max(1, q.id_boxes), q.max_m, q.sum_m / std::max(1, q.id_boxes),
                  q.max_k, q.sum_k / std::max(1, q.id_boxes), q.mode_count[0], q.mode_count[1],
-                 q.mode_count[2]);
+                 q.mode_count[2], q.mode_count[3]);
         lv += tmp;
       }
       lv += "]";

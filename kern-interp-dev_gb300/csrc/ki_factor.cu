@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <stdexcept>
@@ -101,7 +102,37 @@ std::vector<StageSum> Factorization<T>::collect() {
 }
 
 template <typename T>
+void Factorization<T>::fork() {
+  if (!fork_ev) {
+    KI_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+    for (int i = 0; i < kAux; i++) {
+      KI_CUDA(cudaStreamCreateWithFlags(&aux[i], cudaStreamNonBlocking));
+      KI_CUDA(cudaEventCreateWithFlags(&join_ev[i], cudaEventDisableTiming));
+    }
+  }
+  KI_CUDA(cudaEventRecord(fork_ev, stream));
+  for (int i = 0; i < kAux; i++) KI_CUDA(cudaStreamWaitEvent(aux[i], fork_ev, 0));
+}
+
+template <typename T>
+void Factorization<T>::join(int used) {
+  for (int i = 0; i < used && i < kAux; i++) {
+    KI_CUDA(cudaEventRecord(join_ev[i], aux[i]));
+    KI_CUDA(cudaStreamWaitEvent(stream, join_ev[i], 0));
+  }
+}
+
+template <typename T>
 Factorization<T>::~Factorization() {
+  if (stream) cudaStreamSynchronize(stream);
+  for (int i = 0; i < kAux; i++) {
+    if (aux[i]) {
+      cudaStreamSynchronize(aux[i]);
+      cudaStreamDestroy(aux[i]);
+    }
+    if (join_ev[i]) cudaEventDestroy(join_ev[i]);
+  }
+  if (fork_ev) cudaEventDestroy(fork_ev);
   for (auto& r : prof_open) {
     cudaEventDestroy(r.a);
     cudaEventDestroy(r.b);
@@ -228,7 +259,9 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
                                                   int* ipool, int* iscratch, T* tws, Points<T> P,
                                                   int sol_dim, int nprox, const double* pcos,
                                                   const double* psin, double tol, int* k_out,
-                                                  int* m_out, int mode) {
+                                                  int* m_out, int mode, int flags) {
+  // flags: 1 gather the rows (writes m), 2 fold the ID matrix into R,
+  //        4 R already formed (row-major n x n in the global scratch)
   extern __shared__ __align__(16) unsigned char id_smem[];
   const int task = task_base + blockIdx.x;
   const IdTask t = tasks[task];
@@ -261,6 +294,8 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   T* Tout = gws + (size_t)n * n;
 
   // 1. candidate rows, optionally filtered to the proxy circle, order kept
+  const int nprox_rows = t.mode == 0 ? 2 * nprox * sol_dim : 0;
+  if (flags & 1) {
   if (tid == 0) s_cnt = 0;
   __syncthreads();
   for (int s = t.seg_begin; s < t.seg_end; s++) {
@@ -304,27 +339,29 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
       __syncthreads();
     }
   }
-  const int nI = s_cnt;
-  const int nprox_rows = t.mode == 0 ? 2 * nprox * sol_dim : 0;
-  const int m = 2 * nI + nprox_rows;
-  if (tid == 0) m_out[task] = m;
+  if (tid == 0) m_out[task] = 2 * s_cnt + nprox_rows;
+  }
+  if (!(flags & 6)) return;
+  __syncthreads();
+  const int m = m_out[task];
+  const int nI = (m - nprox_rows) / 2;
 
   // 2. TSQR: R <- qr([R; B]) for successive 32-row blocks B of the ID
   //    matrix.  The thread that owns column j+1 forms reflector j+1 right
   //    after updating that column (look-ahead), so one barrier per column.
-  for (int idx = tid; idx < n * n; idx += nth) R[(idx / n) * (size_t)ldR + idx % n] = T(0);
+  if (flags & 4) {
+    if (mode == 0)
+      for (int idx = tid; idx < n * n; idx += nth) R[(idx / n) * (size_t)ldR + idx % n] = gws[idx];
+  } else {
+    for (int idx = tid; idx < n * n; idx += nth) R[(idx / n) * (size_t)ldR + idx % n] = T(0);
+  }
   __syncthreads();
+  // reflector of [R(j,j); B(:,j)] formed by warp 0 (lane i <-> row i of the
+  // block); tail -> hu[buf], tau -> s_tau[buf], beta -> R(j,j)
   auto reflect = [&](int j, int buf) {
-    // reflector of [R(j,j); B(:,j)] by one thread; tail -> hu[buf], tau -> s_tau[buf]
     T alpha = R[(size_t)j * ldR + j];
-    T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
-#pragma unroll
-    for (int i = 0; i < kFoldRows; i += 4) {
-      T b0 = B[(size_t)i * ldB + j], b1 = B[(size_t)(i + 1) * ldB + j];
-      T b2 = B[(size_t)(i + 2) * ldB + j], b3 = B[(size_t)(i + 3) * ldB + j];
-      s0 += b0 * b0; s1 += b1 * b1; s2 += b2 * b2; s3 += b3 * b3;
-    }
-    T sigma = (s0 + s1) + (s2 + s3);
+    T b = B[(size_t)lane * ldB + j];
+    T sigma = warp_sum(b * b);
     T tau = T(0), beta = alpha, scale = T(0);
     if (sigma != T(0)) {
       T nrm = sqrt(alpha * alpha + sigma);
@@ -332,12 +369,13 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
       tau = (beta - alpha) / beta;
       scale = T(1) / (alpha - beta);
     }
-#pragma unroll
-    for (int i = 0; i < kFoldRows; i++) hu[buf * kFoldRows + i] = B[(size_t)i * ldB + j] * scale;
-    s_tau[buf] = tau;
-    R[(size_t)j * ldR + j] = beta;
+    hu[buf * kFoldRows + lane] = b * scale;
+    if (lane == 0) {
+      s_tau[buf] = tau;
+      R[(size_t)j * ldR + j] = beta;
+    }
   };
-  for (int r0 = 0; r0 < m; r0 += kFoldRows) {
+  for (int r0 = 0; (flags & 2) && r0 < m; r0 += kFoldRows) {
     for (int idx = tid; idx < kFoldRows * n; idx += nth) {
       int j = idx % n, i = idx / n;
       int row = r0 + i;
@@ -348,7 +386,7 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
       B[(size_t)i * ldB + j] = v;
     }
     __syncthreads();
-    if (tid == 0) reflect(0, 0);
+    if (warp == 0) reflect(0, 0);
     __syncthreads();
     for (int j = 0; j < n; j++) {
       const int buf = j & 1;
@@ -368,9 +406,11 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
           R[(size_t)j * ldR + c] -= w;
 #pragma unroll
           for (int i = 0; i < kFoldRows; i++) B[(size_t)i * ldB + c] -= w * u[i];
-          if (c == j + 1) reflect(j + 1, buf ^ 1);
         }
-      } else if (j + 1 < n && tid == 0) {   // column j+1 belongs to thread 0
+      }
+      // column j+1 is owned by thread 0: warp 0 forms the next reflector
+      if (warp == 0 && j + 1 < n) {
+        __syncwarp();
         reflect(j + 1, buf ^ 1);
       }
       __syncthreads();
@@ -515,6 +555,222 @@ size_t id_smem_bytes(int n, int mode) {
   b = (b + 15) & ~size_t(15);
   if (mode == 0) b += sizeof(T) * (size_t)n * (n | 1);
   return b;
+}
+
+// ---------------------------------------------------------------- wide boxes --
+// Boxes whose ID matrix is tall (many rows, levels 1-2 in particular) or whose
+// triangle does not fit in shared memory: the ID matrix is formed explicitly
+// and reduced to its n x n triangle by a blocked Householder QR whose trailing
+// updates (compact WY) run on many CTAs; k_id then pivots the triangle.
+struct WideTask {
+  int task;            // index into the level's IdTask array
+  int n, m, nI;
+  int64_t M;           // T-pool offset of M (m x n, column-major, ld = m)
+  int64_t Tf;          // T-pool offset of the current panel's WY factor (kQrNb x kQrNb)
+  int64_t act, rows;   // ipool / iscratch offsets
+  double cx, cy, rad;
+  int64_t R;           // T-scratch offset (tws) of the row-major triangle for k_id
+};
+
+constexpr int kQrNb = 32;     // panel width
+constexpr int kQrTile = 32;   // trailing-update column tile
+constexpr int kQrRows = 64;   // rows staged per trailing-update pass
+
+template <typename T>
+__global__ void k_wide_assemble(const WideTask* tasks, T* wpool, const int* ipool, const int* iscratch,
+                                Points<T> P, int sol_dim, int nprox, const double* pcos,
+                                const double* psin) {
+  const WideTask t = tasks[blockIdx.x];
+  const int j0 = blockIdx.y * 8;
+  if (j0 >= t.n) return;
+  const int j1 = min(t.n, j0 + 8);
+  const int* act = ipool + t.act;
+  const int* rows = iscratch + t.rows;
+  T* M = wpool + t.M;
+  for (int j = j0; j < j1; j++) {
+    int a = act[j];
+    for (int row = threadIdx.x; row < t.m; row += blockDim.x)
+      M[row + (size_t)t.m * j] = id_entry<T>(P, sol_dim, row, t.nI, rows, a, nprox, pcos, psin,
+                                             t.cx, t.cy, t.rad);
+  }
+}
+
+// Block-wide sum of `cnt` per-thread values (cnt <= kQrNb); result in out[].
+template <typename T>
+__device__ void block_sum_vec(T* vals, int cnt, T* red /* [nwarps][kQrNb] */, T* out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int q = 0; q < cnt; q++) {
+    T v = warp_sum(vals[q]);
+    if (lane == 0) red[warp * kQrNb + q] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < cnt) {
+    T s = T(0);
+    for (int w = 0; w < nw; w++) s += red[w * kQrNb + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+// Householder QR of the panel M(p:m, p:p+w) in place (LAPACK xGEQR2 layout:
+// reflector tails below the diagonal, R on and above), plus the forward
+// column-wise WY factor T (xLARFT) of the panel.
+template <typename T>
+__global__ void __launch_bounds__(256) k_qr_panel(const WideTask* tasks, T* wpool, int p) {
+  const WideTask t = tasks[blockIdx.x];
+  if (p >= t.n) return;
+  const int m = t.m, w = min(kQrNb, t.n - p);
+  T* A = wpool + t.M;
+  T* Tf = wpool + t.Tf;
+  __shared__ T red[8 * kQrNb];
+  __shared__ T s_sum[kQrNb];
+  __shared__ T s_tau, s_beta, s_scale;
+  T vals[kQrNb];
+  for (int jj = 0; jj < w; jj++) {
+    const int j = p + jj;
+    // reflector of column j
+    T sg = T(0);
+    for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) sg += A[i + (size_t)m * j] * A[i + (size_t)m * j];
+    vals[0] = sg;
+    block_sum_vec<T>(vals, 1, red, s_sum);
+    if (threadIdx.x == 0) {
+      T sigma = s_sum[0], alpha = A[j + (size_t)m * j];
+      T tau = T(0), beta = alpha, scale = T(0);
+      if (sigma != T(0)) {
+        T nrm = sqrt(alpha * alpha + sigma);
+        beta = alpha >= T(0) ? -nrm : nrm;
+        tau = (beta - alpha) / beta;
+        scale = T(1) / (alpha - beta);
+      }
+      s_tau = tau; s_beta = beta; s_scale = scale;
+    }
+    __syncthreads();
+    const T tau = s_tau, scale = s_scale;
+    for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) A[i + (size_t)m * j] *= scale;
+    __syncthreads();
+    if (threadIdx.x == 0) A[j + (size_t)m * j] = s_beta;
+    // one pass over the rows: z_l = V(:,l)^T v_j for l < jj (WY factor) and
+    // the dots of the remaining panel columns with v_j
+    const int nz = jj, nd = w - jj - 1;
+    for (int q = 0; q < nz + nd; q++) vals[q] = T(0);
+    for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
+      T v = A[i + (size_t)m * j];
+      for (int q = 0; q < nz; q++) vals[q] += A[i + (size_t)m * (p + q)] * v;
+      for (int q = 0; q < nd; q++) vals[nz + q] += A[i + (size_t)m * (j + 1 + q)] * v;
+    }
+    block_sum_vec<T>(vals, nz + nd, red, s_sum);
+    // remaining panel columns: c -= tau (v^T c) v
+    for (int q = 0; q < nd; q++) {
+      const int c = j + 1 + q;
+      const T wq = (A[j + (size_t)m * c] + s_sum[nz + q]) * tau;
+      for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) A[i + (size_t)m * c] -= wq * A[i + (size_t)m * j];
+      __syncthreads();
+      if (threadIdx.x == 0) A[j + (size_t)m * c] -= wq;
+    }
+    // WY factor column jj: T(0:jj, jj) = -tau T(0:jj,0:jj) z, z_l += V(j, l)
+    if (threadIdx.x == 0) {
+      T z[kQrNb];
+      for (int l = 0; l < nz; l++) z[l] = s_sum[l] + A[j + (size_t)m * (p + l)];
+      for (int l = 0; l < nz; l++) {
+        T acc = T(0);
+        for (int q = l; q < nz; q++) acc += Tf[l + kQrNb * q] * z[q];
+        Tf[l + kQrNb * jj] = -tau * acc;
+      }
+      Tf[jj + kQrNb * jj] = tau;
+    }
+    __syncthreads();
+  }
+}
+
+// Trailing update A(p:m, c0:c0+32) <- (I - V T V^T)^T A(p:m, c0:c0+32).
+template <typename T>
+__global__ void __launch_bounds__(256) k_qr_update(const WideTask* tasks, T* wpool, int p) {
+  const WideTask t = tasks[blockIdx.x];
+  const int m = t.m, n = t.n;
+  if (p >= n) return;
+  const int w = min(kQrNb, n - p);
+  const int c0 = p + w + blockIdx.y * kQrTile;
+  if (c0 >= n) return;
+  const int tc = min(kQrTile, n - c0);
+  T* A = wpool + t.M;
+  const T* Tf = wpool + t.Tf;
+  __shared__ T Vs[kQrRows][kQrNb + 1];
+  __shared__ T As[kQrRows][kQrTile + 1];
+  __shared__ T Ws[kQrNb][kQrTile + 1];
+  const int tid = threadIdx.x;
+  // W = V^T A  (w x tc); thread owns entries e = tid + 256 q
+  T acc[4] = {T(0), T(0), T(0), T(0)};
+  for (int r0 = p; r0 < m; r0 += kQrRows) {
+    for (int e = tid; e < kQrRows * kQrNb; e += blockDim.x) {
+      int i = e / kQrNb, l = e % kQrNb, row = r0 + i;
+      T v = T(0);
+      if (row < m && l < w) v = row > p + l ? A[row + (size_t)m * (p + l)] : (row == p + l ? T(1) : T(0));
+      Vs[i][l] = v;
+    }
+    for (int e = tid; e < kQrRows * kQrTile; e += blockDim.x) {
+      int i = e / kQrTile, c = e % kQrTile, row = r0 + i;
+      As[i][c] = (row < m && c < tc) ? A[row + (size_t)m * (c0 + c)] : T(0);
+    }
+    __syncthreads();
+    for (int q = 0; q < 4; q++) {
+      int e = tid + 256 * q, l = e / kQrTile, c = e % kQrTile;
+      T s0 = T(0), s1 = T(0);
+      for (int i = 0; i < kQrRows; i += 2) {
+        s0 += Vs[i][l] * As[i][c];
+        s1 += Vs[i + 1][l] * As[i + 1][c];
+      }
+      acc[q] += s0 + s1;
+    }
+    __syncthreads();
+  }
+  for (int q = 0; q < 4; q++) {
+    int e = tid + 256 * q;
+    Ws[e / kQrTile][e % kQrTile] = acc[q];
+  }
+  __syncthreads();
+  // W <- T^T W (T upper triangular -> T^T lower)
+  for (int q = 0; q < 4; q++) {
+    int e = tid + 256 * q, l = e / kQrTile, c = e % kQrTile;
+    T s = T(0);
+    for (int r = 0; r <= l && r < w; r++) s += Tf[r + kQrNb * l] * Ws[r][c];
+    acc[q] = l < w ? s : T(0);
+  }
+  __syncthreads();
+  for (int q = 0; q < 4; q++) {
+    int e = tid + 256 * q;
+    Ws[e / kQrTile][e % kQrTile] = acc[q];
+  }
+  __syncthreads();
+  // A -= V W
+  for (int r0 = p; r0 < m; r0 += kQrRows) {
+    for (int e = tid; e < kQrRows * kQrNb; e += blockDim.x) {
+      int i = e / kQrNb, l = e % kQrNb, row = r0 + i;
+      T v = T(0);
+      if (row < m && l < w) v = row > p + l ? A[row + (size_t)m * (p + l)] : (row == p + l ? T(1) : T(0));
+      Vs[i][l] = v;
+    }
+    __syncthreads();
+    for (int e = tid; e < kQrRows * kQrTile; e += blockDim.x) {
+      int i = e / kQrTile, c = e % kQrTile, row = r0 + i;
+      if (row >= m || c >= tc) continue;
+      T s = T(0);
+      for (int l = 0; l < w; l++) s += Vs[i][l] * Ws[l][c];
+      A[row + (size_t)m * (c0 + c)] -= s;
+    }
+    __syncthreads();
+  }
+}
+
+// Upper triangle of M (column-major) -> row-major n x n scratch for k_id.
+template <typename T>
+__global__ void k_wide_triangle(const WideTask* tasks, const T* wpool, T* tws) {
+  const WideTask t = tasks[blockIdx.x];
+  const T* M = wpool + t.M;
+  T* R = tws + t.R;
+  for (int e = threadIdx.x; e < t.n * t.n; e += blockDim.x) {
+    int i = e / t.n, c = e % t.n;
+    R[e] = (i <= c && i < t.m) ? M[i + (size_t)t.m * c] : T(0);
+  }
 }
 
 // Self block K_BN of a box (kernel entries plus children's accumulated
@@ -1172,63 +1428,160 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       pact_top += it.n;
     }
     for (size_t i = 0; i < comp.size(); i++) hb[comp[i]].pact = itasks[i].pact;
-    // group the boxes by where the ID working set fits: triangle in shared
-    // memory (mode 0), triangle in global scratch (1), everything global (2)
     const size_t smem_cap = 225 * 1024;
-    std::vector<int> mode_of(itasks.size());
-    for (size_t i = 0; i < itasks.size(); i++) {
-      int n = itasks[i].n;
-      mode_of[i] = id_smem_bytes<T>(n, 0) <= smem_cap ? 0 : 1;
-    }
-    {
-      std::vector<size_t> order(itasks.size());
-      std::iota(order.begin(), order.end(), 0);
-      std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return mode_of[a] < mode_of[b]; });
-      std::vector<IdTask> it2;
-      std::vector<int> comp2, mode2;
-      for (size_t o : order) {
-        it2.push_back(itasks[o]);
-        comp2.push_back(comp[o]);
-        mode2.push_back(mode_of[o]);
-      }
-      itasks.swap(it2);
-      comp.swap(comp2);
-      mode_of.swap(mode2);
-      for (size_t i = 0; i < comp.size(); i++) hb[comp[i]].pact = itasks[i].pact;
-    }
     IdTask* d_it = (IdTask*)F->alloc(sizeof(IdTask) * itasks.size());
     int64_t* d_soff = (int64_t*)F->alloc(sizeof(int64_t) * (seg_off.size() + 1));
     int* d_slen = (int*)F->alloc(sizeof(int) * (seg_len.size() + 1));
     int* d_k = (int*)F->alloc(sizeof(int) * itasks.size());
+    int* d_m = (int*)F->alloc(sizeof(int) * itasks.size());
     upload(d_it, itasks, s);
     upload(d_soff, seg_off, s);
     upload(d_slen, seg_len, s);
-    int* d_m = (int*)F->alloc(sizeof(int) * itasks.size());
     std::string id_name = "id@L" + std::to_string(l);
     F->stage_begin(id_name.c_str(), 0, 0);
     size_t id_rec = F->prof_open.size() - 1;
-    for (int md = 0; md < 3; md++) {
+    // (a) row lists of every box (m is needed to pick the path)
+    KI_CUDA(cudaFuncSetAttribute(k_id<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
+    k_id<T><<<(unsigned)itasks.size(), kThreads, 0, s>>>(d_it, 0, d_soff, d_slen, ipool, d_irows, d_tws,
+                                                         P, sd, np, d_pcs, d_pcs + np, prm.id_tol,
+                                                         d_k, d_m, 0, 1);
+    KI_CUDA(cudaGetLastError());
+    std::vector<int> mh(itasks.size()), kh(itasks.size());
+    KI_CUDA(cudaMemcpyAsync(mh.data(), d_m, sizeof(int) * mh.size(), cudaMemcpyDeviceToHost, s));
+    KI_CUDA(cudaStreamSynchronize(s));
+    // (b) groups: [narrow, R in smem][narrow, R global][wide, R in smem][wide, R global];
+    //     wide = tall ID matrix (folded by the multi-CTA blocked QR) or a
+    //     triangle too large for shared memory
+    // row threshold of the wide path (environment override KI_WIDE_ROWS, used
+    // by the tests to drive every box through it)
+    int kWideRows = 1536;
+    if (const char* e = std::getenv("KI_WIDE_ROWS")) kWideRows = std::atoi(e);
+    std::vector<int> grp(itasks.size());
+    for (size_t i = 0; i < itasks.size(); i++) {
+      int n = itasks[i].n;
+      int md = id_smem_bytes<T>(n, 0) <= smem_cap ? 0 : 1;
+      bool wide = mh[i] > kWideRows || md == 1;
+      grp[i] = (wide ? 2 : 0) + md;
+    }
+    std::vector<int> mode_of(itasks.size());
+    {
+      std::vector<size_t> order(itasks.size());
+      std::iota(order.begin(), order.end(), 0);
+      std::stable_sort(order.begin(), order.end(), [&](size_t a2, size_t b2) {
+        return grp[a2] != grp[b2] ? grp[a2] < grp[b2] : itasks[a2].n < itasks[b2].n;
+      });
+      std::vector<IdTask> it2;
+      std::vector<int> comp2, grp2, m2;
+      for (size_t o : order) {
+        it2.push_back(itasks[o]);
+        comp2.push_back(comp[o]);
+        grp2.push_back(grp[o]);
+        m2.push_back(mh[o]);
+      }
+      itasks.swap(it2);
+      comp.swap(comp2);
+      grp.swap(grp2);
+      mh.swap(m2);
+      for (size_t i = 0; i < comp.size(); i++) {
+        hb[comp[i]].pact = itasks[i].pact;
+        mode_of[i] = grp[i] & 1;
+      }
+      upload(d_it, itasks, s);
+      upload(d_m, mh, s);
+    }
+    int next_aux = 0;
+    auto launch_range = [&](int g, int flags, cudaStream_t fixed) {
+      // tasks of group g are contiguous and sorted by n within the group (see
+      // the ordering above); launch them in bins of similar shared-memory
+      // size so that small boxes are not limited by the largest one's footprint
       int first = -1, cnt = 0;
-      size_t sm = 0;
       for (size_t i = 0; i < itasks.size(); i++)
-        if (mode_of[i] == md) {
+        if (grp[i] == g) {
           if (first < 0) first = (int)i;
           cnt++;
-          sm = std::max(sm, id_smem_bytes<T>(itasks[i].n, md));
         }
-      if (cnt == 0) continue;
-      if (sm > smem_cap) throw std::runtime_error("box too large for the ID kernel");
-      KI_CUDA(cudaFuncSetAttribute(k_id<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
-      k_id<T><<<(unsigned)cnt, kThreads, sm, s>>>(d_it, first, d_soff, d_slen, ipool, d_irows, d_tws,
-                                                  P, sd, np, d_pcs, d_pcs + np, prm.id_tol, d_k,
-                                                  d_m, md);
-      KI_CUDA(cudaGetLastError());
+      if (cnt == 0) return;
+      int b0 = first;
+      while (b0 < first + cnt) {
+        size_t sm0 = id_smem_bytes<T>(itasks[b0].n, g & 1);
+        // CTAs per SM at this footprint; extend the bin while it stays the same
+        int per_sm = std::max(1, (int)(228 * 1024 / (sm0 + 1024)));
+        int b1 = b0 + 1;
+        size_t sm = sm0;
+        while (b1 < first + cnt) {
+          size_t s1 = id_smem_bytes<T>(itasks[b1].n, g & 1);
+          if (std::max(1, (int)(228 * 1024 / (s1 + 1024))) != per_sm) break;
+          sm = std::max(sm, s1);
+          b1++;
+        }
+        if (sm > smem_cap) throw std::runtime_error("box too large for the ID kernel");
+        cudaStream_t st = fixed ? fixed : F->aux[(next_aux++) % (Factorization<T>::kAux - 1)];
+        k_id<T><<<(unsigned)(b1 - b0), kThreads, sm, st>>>(d_it, b0, d_soff, d_slen, ipool, d_irows,
+                                                           d_tws, P, sd, np, d_pcs, d_pcs + np,
+                                                           prm.id_tol, d_k, d_m, g & 1, flags);
+        KI_CUDA(cudaGetLastError());
+        b0 = b1;
+      }
+    };
+    // (c) narrow boxes: fused on-the-fly assembly + TSQR + CPQR, one CTA each;
+    //     size bins on aux streams 0..2, the wide path on aux stream 3, all
+    //     concurrent
+    F->fork();
+    launch_range(0, 2, nullptr);
+    launch_range(1, 2, nullptr);
+    // (d) wide boxes: explicit ID matrix, blocked Householder QR, then CPQR
+    {
+      std::vector<WideTask> wt;
+      int64_t mtot = 0;
+      int maxn = 0;
+      for (size_t i = 0; i < itasks.size(); i++) {
+        if (grp[i] < 2) continue;
+        WideTask w{};
+        w.task = (int)i;
+        w.n = itasks[i].n;
+        w.m = mh[i];
+        w.nI = (mh[i] - (itasks[i].mode == 0 ? 2 * np * sd : 0)) / 2;
+        w.M = mtot;
+        mtot += (int64_t)w.m * w.n;
+        w.act = itasks[i].act;
+        w.rows = itasks[i].rows;
+        w.cx = itasks[i].cx;
+        w.cy = itasks[i].cy;
+        w.rad = itasks[i].rad_proxy;
+        w.R = itasks[i].ws;
+        maxn = std::max(maxn, w.n);
+        wt.push_back(w);
+      }
+      cudaStream_t ws3 = F->aux[Factorization<T>::kAux - 1];
+      if (!wt.empty()) {
+        for (auto& w : wt) {
+          w.Tf = mtot;
+          mtot += kQrNb * kQrNb;
+        }
+        T* d_wpool = nullptr;
+        KI_CUDA(cudaMallocAsync((void**)&d_wpool, sizeof(T) * (mtot + 16), ws3));
+        WideTask* d_wt = nullptr;
+        KI_CUDA(cudaMallocAsync((void**)&d_wt, sizeof(WideTask) * wt.size(), ws3));
+        upload(d_wt, wt, ws3);
+        k_wide_assemble<T><<<dim3((unsigned)wt.size(), (maxn + 7) / 8), 256, 0, ws3>>>(
+            d_wt, d_wpool, ipool, d_irows, P, sd, np, d_pcs, d_pcs + np);
+        for (int p0 = 0; p0 < maxn; p0 += kQrNb) {
+          k_qr_panel<T><<<(unsigned)wt.size(), 256, 0, ws3>>>(d_wt, d_wpool, p0);
+          int tiles = (maxn - p0 - kQrNb + kQrTile - 1) / kQrTile;
+          if (tiles > 0) k_qr_update<T><<<dim3((unsigned)wt.size(), tiles), 256, 0, ws3>>>(d_wt, d_wpool, p0);
+        }
+        k_wide_triangle<T><<<(unsigned)wt.size(), 256, 0, ws3>>>(d_wt, d_wpool, d_tws);
+        KI_CUDA(cudaGetLastError());
+        launch_range(2, 4, ws3);
+        launch_range(3, 4, ws3);
+        KI_CUDA(cudaFreeAsync(d_wpool, ws3));
+        KI_CUDA(cudaFreeAsync(d_wt, ws3));
+      }
     }
+    F->join(Factorization<T>::kAux);
     F->stage_end();
     KI_CUDA(cudaGetLastError());
-    std::vector<int> kh(itasks.size()), mh(itasks.size());
     KI_CUDA(cudaMemcpyAsync(kh.data(), d_k, sizeof(int) * kh.size(), cudaMemcpyDeviceToHost, s));
-    KI_CUDA(cudaMemcpyAsync(mh.data(), d_m, sizeof(int) * mh.size(), cudaMemcpyDeviceToHost, s));
     KI_CUDA(cudaStreamSynchronize(s));
     {
       LevelStat ls;
@@ -1243,7 +1596,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         ls.sum_m += mh[i];
         ls.sum_k += kh[i];
         ls.compressed += kh[i] > 0;
-        ls.mode_count[mode_of[i]]++;
+        ls.mode_count[grp[i]]++;
       }
       F->level_stats.push_back(ls);
     }

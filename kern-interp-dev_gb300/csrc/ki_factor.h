@@ -51,7 +51,7 @@ struct LevelStat {
   int level = 0, boxes = 0, id_boxes = 0, compressed = 0;
   int max_n = 0, max_m = 0, max_k = 0;
   double sum_n = 0, sum_m = 0, sum_k = 0;
-  int mode_count[3] = {0, 0, 0};
+  int mode_count[4] = {0, 0, 0, 0};   // narrow/smem, narrow/global, wide/smem, wide/global
 };
 
 template <typename T>
@@ -59,6 +59,12 @@ struct Factorization {
   Params prm;
   Tree tree;
   cudaStream_t stream = nullptr;
+  // auxiliary streams: independent launch groups of a level run concurrently
+  static constexpr int kAux = 4;
+  cudaStream_t aux[kAux] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[kAux] = {};
+  void fork();                        // aux streams wait for `stream`
+  void join(int used);                // `stream` waits for aux[0..used)
   int N = 0;           // DOFs
   int n_points = 0;
   // point data (device, SoA, precision T)
