@@ -121,6 +121,27 @@ int ki_solve_device(ki_factor* f, const double* d_b, int ldb, int nrhs, double* 
                     double* d_alpha, int ldalpha, void* stream);
 
 /*
+ * ki_solve_device without any device allocation.  No counterpart in the
+ * reference.  For callers that cannot allocate device memory while solving:
+ * applications that reserve all device memory up front for their own
+ * allocator and account for every byte, and latency-critical loops that
+ * cannot absorb the implicit synchronization of cudaMalloc/cudaFree.
+ * Same arguments, stream and results as ki_solve_device; its temporaries
+ * come from one fixed 32 MiB device array that every GPU loading the
+ * library holds until the process exits.  Limit: the DOF-major copy of the
+ * right-hand sides plus the solve's temporaries must fit in those 32 MiB
+ * (about n_dofs * nrhs * 8 bytes for simply connected problems, twice that
+ * with holes); larger calls return KI_ERR_ARG with the size needed.
+ * The first call on a device looks up the array's device address (with that
+ * device current); make that first call before any stream capture.  All
+ * calls share the array and it keeps the last call's contents (nothing in it
+ * is read before being written): calls that overlap on the GPU -- on
+ * different streams or handles at the same time -- race.
+ */
+int ki_solve_device_noalloc(ki_factor* f, const double* d_b, int ldb, int nrhs, double* d_x,
+                            int ldx, double* d_alpha, int ldalpha, void* stream);
+
+/*
  * y = K x with the dense FP64 Nystrom operator of the problem, x and y in
  * HOST memory (n_dofs x ncols): the reference's dense residual check
  * (solve_err, linear_solve.cpp:379-425, via Kernel::operator(),

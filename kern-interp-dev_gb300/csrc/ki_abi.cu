@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -328,6 +329,72 @@ void check_desc(const ki_problem_desc* d) {
     throw ArgError("tree/proxy parameters must be >= 0 (0 = reference default)");
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free solve.  Callers that cannot allocate device memory while
+// solving -- applications that reserve all device memory up front for their
+// own allocator and account for every byte, or latency-critical loops that
+// cannot absorb the implicit synchronization of cudaMalloc/cudaFree -- call
+// ki_solve_device_noalloc.  Its temporaries live in this fixed, file-scope
+// device array instead of coming from the stream-ordered allocator.
+// Every GPU that loads the library holds the array until the process exits.
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;   // 32 MiB
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of g_noalloc_scratch per device, looked up once (with that
+// device current) on the first no-allocation call made on it.  The host-side
+// name g_noalloc_scratch is only a stand-in: never hand it to a kernel.
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[256] = {};
+
+void* noalloc_scratch_for_current_device() {
+  int dev = 0;
+  KI_CHECK_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) throw std::runtime_error("device index out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      throw std::runtime_error(std::string("cudaGetSymbolAddress of the no-allocation scratch failed: ") +
+                               cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = p;
+  }
+  return g_noalloc_ptr[dev];
+}
+
+template <typename T>
+void solve_impl_noalloc(ki_factor* f, ki::Factorization<T>& F, const double* d_b, int ldb,
+                        int nrhs, double* d_x, int ldx, double* d_alpha, int ldalpha,
+                        cudaStream_t s) {
+  const int N = f->n_dofs;
+  auto piece = [](size_t b) { return ((b + 255) & ~size_t(255)) + 256; };
+  const size_t need = piece(sizeof(T) * (size_t)N * nrhs) +
+                      piece(sizeof(T) * (size_t)std::max(1, f->n_border) * nrhs) +
+                      ki::solve_arena_bytes<T>(F, nrhs);
+  if (need > kNoAllocScratchBytes)
+    throw ArgError("ki_solve_device_noalloc: this solve needs " + std::to_string(need) +
+                   " bytes of scratch but the fixed scratch holds " +
+                   std::to_string(kNoAllocScratchBytes) +
+                   " bytes (32 MiB); use fewer right-hand sides per call or ki_solve_device");
+  ki::ScratchArena arena;
+  arena.base = static_cast<char*>(noalloc_scratch_for_current_device());
+  arena.size = kNoAllocScratchBytes;
+  T* work = static_cast<T*>(arena.take(sizeof(T) * (size_t)N * nrhs));
+  T* al = static_cast<T*>(arena.take(sizeof(T) * (size_t)std::max(1, f->n_border) * nrhs));
+  if (!work || !al) throw ArgError("ki_solve_device_noalloc: scratch exhausted");
+  // every temporary is written before it is read: nothing needs clearing
+  k_to_dofmajor<double, T><<<grid_for((size_t)N * nrhs), 256, 0, s>>>(d_b, ldb, N, nrhs, work);
+  KI_CHECK_CUDA(cudaGetLastError());
+  ki::solve_device_arena<T>(F, work, nrhs, al, arena, s);
+  k_from_dofmajor<T, double><<<grid_for((size_t)N * nrhs), 256, 0, s>>>(work, N, nrhs, d_x, ldx);
+  KI_CHECK_CUDA(cudaGetLastError());
+  if (f->n_border > 0 && d_alpha) {
+    k_alpha_out<T><<<grid_for((size_t)f->n_border * nrhs), 256, 0, s>>>(al, f->n_border, nrhs,
+                                                                       d_alpha, ldalpha);
+    KI_CHECK_CUDA(cudaGetLastError());
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -430,6 +497,20 @@ int ki_solve_device(ki_factor* f, const double* d_b, int ldb, int nrhs, double* 
     cudaStream_t s = stream ? (cudaStream_t)stream : f->stream;
     if (f->f64) solve_impl<double>(f, *f->f64, d_b, ldb, nrhs, d_x, ldx, d_alpha, ldalpha, s);
     else solve_impl<float>(f, *f->f32, d_b, ldb, nrhs, d_x, ldx, d_alpha, ldalpha, s);
+  });
+}
+
+int ki_solve_device_noalloc(ki_factor* f, const double* d_b, int ldb, int nrhs, double* d_x,
+                            int ldx, double* d_alpha, int ldalpha, void* stream) {
+  return guarded([&] {
+    if (!f) throw ArgError("factor is NULL");
+    if (nrhs < 0 || ldb < f->n_dofs || ldx < f->n_dofs) throw ArgError("bad leading dimension / nrhs");
+    if (f->n_border > 0 && d_alpha && ldalpha < f->n_border) throw ArgError("bad ldalpha");
+    if (nrhs == 0) return;
+    if (!d_b || !d_x) throw ArgError("NULL b or x");
+    cudaStream_t s = stream ? (cudaStream_t)stream : f->stream;
+    if (f->f64) solve_impl_noalloc<double>(f, *f->f64, d_b, ldb, nrhs, d_x, ldx, d_alpha, ldalpha, s);
+    else solve_impl_noalloc<float>(f, *f->f32, d_b, ldb, nrhs, d_x, ldx, d_alpha, ldalpha, s);
   });
 }
 

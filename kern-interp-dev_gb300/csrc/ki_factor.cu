@@ -1880,6 +1880,85 @@ void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha) {
   KI_CUDA(cudaFreeAsync(M, s));
 }
 
+// ---------------------------------------------------- arena-backed solve --
+// The solve of solve_device with its temporaries carved from a caller-owned
+// buffer instead of the stream-ordered allocator; the arithmetic and launch
+// sequence are the same.
+template <typename T>
+size_t solve_arena_bytes(const Factorization<T>& F, int ncols) {
+  auto piece = [](size_t b) { return ((b + 255) & ~size_t(255)) + 256; };
+  const size_t nr = F.n_root, nb = F.n_border, N = F.N, nc = ncols;
+  if (nb == 0) return piece(sizeof(T) * nr * nc);
+  const size_t parts = (N + kRedRows - 1) / kRedRows;
+  return piece(sizeof(T) * N * nc) + piece(sizeof(T) * nb * nc) + piece(sizeof(T) * (nr + nb) * nc) +
+         piece(sizeof(T) * parts * nb * nc);
+}
+
+template <typename T>
+static void reduce_rows_arena(Factorization<T>& F, const T* A, int na, const T* B, int nc, T* out,
+                              T* partial, cudaStream_t s) {
+  int parts = (F.N + kRedRows - 1) / kRedRows;
+  if (na * nc > 16 * 256) throw std::runtime_error("border too wide for the row reduction");
+  size_t sm = sizeof(T) * 32 * (size_t)(na + nc);
+  if (sm > 48 * 1024)
+    KI_CUDA(cudaFuncSetAttribute(k_reduce_partial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  k_reduce_partial<T><<<parts, 256, sm, s>>>(A, na, B, nc, F.N, F.d_is_skel, partial);
+  k_reduce_final<T><<<std::max(1, (na * nc + 255) / 256), 256, 0, s>>>(partial, parts, na * nc, out);
+  KI_CUDA(cudaGetLastError());
+}
+
+template <typename T>
+void solve_device_arena(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, ScratchArena& arena,
+                        cudaStream_t s) {
+  const int L = (int)F.levels.size();
+  const int nr = F.n_root;
+  auto take = [&](size_t bytes) {
+    void* p = arena.take(bytes);
+    if (!p) throw std::invalid_argument("scratch arena too small for this solve");
+    return (T*)p;
+  };
+  if (F.n_border == 0) {
+    for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kUpDiag, d_x, ncols, s);
+    if (nr > 0) {
+      T* ws = take(sizeof(T) * (size_t)nr * ncols);
+      int gb = std::max(1, std::min(4096, (nr * ncols + 255) / 256));
+      k_gather_rows<T><<<gb, 256, 0, s>>>(d_x, ncols, F.d_root_idx, nr, ncols, ws);
+      dense_lu_solve<T>(F.d_root_lu, nr, F.d_root_piv, ws, nr, ncols, false, s);
+      k_scatter_rows<T><<<gb, 256, 0, s>>>(d_x, ncols, F.d_root_idx, nr, ncols, ws);
+      KI_CUDA(cudaGetLastError());
+    }
+    for (int l = 1; l < L; l++) launch_sweep<T>(F, l, kDown, d_x, ncols, s);
+    return;
+  }
+  const int nb = F.n_border, ns = nr + nb, N = F.N;
+  T* Dw = take(sizeof(T) * (size_t)N * ncols);
+  T* t = take(sizeof(T) * (size_t)nb * ncols);
+  T* M = take(sizeof(T) * (size_t)ns * ncols);
+  T* partial = take(sizeof(T) * (size_t)((N + kRedRows - 1) / kRedRows) * nb * ncols);
+  for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kUp, d_x, ncols, s);
+  KI_CUDA(cudaMemcpyAsync(Dw, d_x, sizeof(T) * (size_t)N * ncols, cudaMemcpyDeviceToDevice, s));
+  for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kDiag, Dw, ncols, s);
+  reduce_rows_arena<T>(F, F.d_PsiTmod, nb, Dw, ncols, t, partial, s);
+  k_mc_rhs<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
+      d_x, ncols, F.d_root_idx, nr, t, nb, ncols, M);
+  dense_lu_solve<T>(F.d_root_lu, ns, F.d_root_piv, M, ns, ncols, false, s);
+  k_mc_update<T><<<std::min(8192, (int)(((size_t)N * ncols + 255) / 256)), 256, 0, s>>>(
+      d_x, ncols, F.d_Umod, nb, M, nr, N, F.d_is_skel);
+  KI_CUDA(cudaGetLastError());
+  for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kDiag, d_x, ncols, s);
+  k_mc_finish<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
+      d_x, ncols, F.d_root_idx, M, nr, nb, d_alpha);
+  KI_CUDA(cudaGetLastError());
+  for (int l = 1; l < L; l++) launch_sweep<T>(F, l, kDown, d_x, ncols, s);
+}
+
+template size_t solve_arena_bytes<double>(const Factorization<double>&, int);
+template size_t solve_arena_bytes<float>(const Factorization<float>&, int);
+template void solve_device_arena<double>(Factorization<double>&, double*, int, double*,
+                                         ScratchArena&, cudaStream_t);
+template void solve_device_arena<float>(Factorization<float>&, float*, int, float*, ScratchArena&,
+                                        cudaStream_t);
+
 template std::unique_ptr<Factorization<double>> factorize<double>(
     const Params&, int, const double*, const double*, const double*, const double*,
     const HoleDesc&, cudaStream_t);

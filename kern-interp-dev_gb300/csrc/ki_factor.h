@@ -117,6 +117,29 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
                                             const double* curvatures, const HoleDesc& holes,
                                             cudaStream_t stream);
 
+// A bump allocator over caller-provided device memory.
+struct ScratchArena {
+  char* base = nullptr;
+  size_t size = 0, used = 0;
+  void* take(size_t bytes) {
+    size_t off = (used + 255) & ~size_t(255);
+    if (off + bytes > size) return nullptr;
+    used = off + bytes;
+    return base + off;
+  }
+};
+
+// Device bytes solve_device_arena takes from its arena for ncols columns
+// (including 256-byte alignment of every piece).
+template <typename T>
+size_t solve_arena_bytes(const Factorization<T>& F, int ncols);
+
+// solve_device with every temporary taken from `arena` (no allocation, no
+// profiling events); `s` is the stream of the whole solve.
+template <typename T>
+void solve_device_arena(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, ScratchArena& arena,
+                        cudaStream_t s);
+
 // Solve with the factorization: x (device, DOF-major N x ncols, ld = ncols)
 // is overwritten with the solution; alpha (device, n_border x ncols,
 // row-major) receives the border unknowns of a multiply connected problem.
