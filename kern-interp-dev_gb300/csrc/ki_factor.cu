@@ -60,20 +60,24 @@ void* Factorization<T>::alloc(size_t bytes) {
 }
 
 template <typename T>
-void Factorization<T>::stage_begin(const char* name, double flops, double bytes) {
+void Factorization<T>::stage_begin(const char* name, double flops, double bytes, cudaStream_t on) {
   StageRec r;
   r.stage = name;
   r.flops = flops;
   r.bytes = bytes;
   KI_CUDA(cudaEventCreate(&r.a));
   KI_CUDA(cudaEventCreate(&r.b));
-  KI_CUDA(cudaEventRecord(r.a, stream));
+  KI_CUDA(cudaEventRecord(r.a, on ? on : stream));
+  prof_stack.push_back(prof_open.size());
   prof_open.push_back(r);
 }
 
 template <typename T>
-void Factorization<T>::stage_end() {
-  KI_CUDA(cudaEventRecord(prof_open.back().b, stream));
+void Factorization<T>::stage_end(cudaStream_t on) {
+  if (prof_stack.empty()) throw std::logic_error("stage_end without stage_begin");
+  size_t idx = prof_stack.back();
+  prof_stack.pop_back();
+  KI_CUDA(cudaEventRecord(prof_open[idx].b, on ? on : stream));
 }
 
 template <typename T>
@@ -82,7 +86,7 @@ std::vector<StageSum> Factorization<T>::collect() {
   for (auto& r : prof_open) {
     float ms = 0;
     KI_CUDA(cudaEventSynchronize(r.b));
-    cudaEventElapsedTime(&ms, r.a, r.b);
+    KI_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
     cudaEventDestroy(r.a);
     cudaEventDestroy(r.b);
     StageSum* d = nullptr;
@@ -253,7 +257,7 @@ __device__ __forceinline__ T id_entry(const Points<T>& P, int sol_dim, int row, 
 // a warp touch consecutive columns.  Shared-memory layout (dynamic):
 //   B (32 x ldB) | hu (2 x 32 Householder tails) | vn1 (n) | vn2 (n) | perm (n) |
 //   R (n x ldR) when it fits (mode 0); mode 1 keeps R in the global scratch.
-template <typename T>
+template <typename T, int FR>
 __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_base,
                                                   const int64_t* seg_off, const int* seg_len,
                                                   int* ipool, int* iscratch, T* tws, Points<T> P,
@@ -276,12 +280,12 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   int* rows = iscratch + t.rows;
   const int* act = ipool + t.act;
   T* gws = tws + t.ws;   // global scratch: R (n*n) | Tout (n*n/4+1)
-  const int ldB = n;
+  const int ldB = n | 1;
   size_t off = 0;
   T* B = reinterpret_cast<T*>(id_smem);
-  off += sizeof(T) * (size_t)kFoldRows * ldB;
+  off += sizeof(T) * (size_t)FR * ldB;
   T* hu = reinterpret_cast<T*>(id_smem + off);   // [2][n] reflector tails (fold: 32, CPQR: n)
-  off += sizeof(T) * 2 * (size_t)max(n, kFoldRows);
+  off += sizeof(T) * 2 * (size_t)max(n, FR);
   T* vn1 = reinterpret_cast<T*>(id_smem + off);
   off += sizeof(T) * (size_t)n;
   T* vn2 = reinterpret_cast<T*>(id_smem + off);
@@ -289,8 +293,16 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   int* perm = reinterpret_cast<int*>(id_smem + off);
   off += sizeof(int) * (size_t)n;
   off = (off + 15) & ~size_t(15);
-  const int ldR = mode == 0 ? (n | 1) : n;
+  // mode 2: the fold keeps the triangle packed by rows in shared memory
+  // (row i holds columns i..n-1), the pivoting then runs on a full copy in
+  // the global scratch
+  const bool packed = mode == 2;
+  int ldR = mode == 0 ? (n | 1) : n;
   T* R = mode == 0 ? reinterpret_cast<T*>(id_smem + off) : gws;
+  T* RF = packed ? reinterpret_cast<T*>(id_smem + off) : R;   // fold storage
+  auto rowbase = [&](int i) -> size_t {
+    return packed ? (size_t)i * n - (size_t)i * (i - 1) / 2 - i : (size_t)i * ldR;
+  };
   T* Tout = gws + (size_t)n * n;
 
   // 1. candidate rows, optionally filtered to the proxy circle, order kept
@@ -352,6 +364,8 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   if (flags & 4) {
     if (mode == 0)
       for (int idx = tid; idx < n * n; idx += nth) R[(idx / n) * (size_t)ldR + idx % n] = gws[idx];
+  } else if (packed) {
+    for (int idx = tid; idx < n * (n + 1) / 2; idx += nth) RF[idx] = T(0);
   } else {
     for (int idx = tid; idx < n * n; idx += nth) R[(idx / n) * (size_t)ldR + idx % n] = T(0);
   }
@@ -359,9 +373,15 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   // reflector of [R(j,j); B(:,j)] formed by warp 0 (lane i <-> row i of the
   // block); tail -> hu[buf], tau -> s_tau[buf], beta -> R(j,j)
   auto reflect = [&](int j, int buf) {
-    T alpha = R[(size_t)j * ldR + j];
-    T b = B[(size_t)lane * ldB + j];
-    T sigma = warp_sum(b * b);
+    T alpha = RF[rowbase(j) + j];
+    T b[FR / 32];
+    T sq = T(0);
+#pragma unroll
+    for (int q = 0; q < FR / 32; q++) {
+      b[q] = B[(size_t)(lane + 32 * q) * ldB + j];
+      sq += b[q] * b[q];
+    }
+    T sigma = warp_sum(sq);
     T tau = T(0), beta = alpha, scale = T(0);
     if (sigma != T(0)) {
       T nrm = sqrt(alpha * alpha + sigma);
@@ -369,14 +389,15 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
       tau = (beta - alpha) / beta;
       scale = T(1) / (alpha - beta);
     }
-    hu[buf * kFoldRows + lane] = b * scale;
+#pragma unroll
+    for (int q = 0; q < FR / 32; q++) hu[buf * FR + lane + 32 * q] = b[q] * scale;
     if (lane == 0) {
       s_tau[buf] = tau;
-      R[(size_t)j * ldR + j] = beta;
+      RF[rowbase(j) + j] = beta;
     }
   };
-  for (int r0 = 0; (flags & 2) && r0 < m; r0 += kFoldRows) {
-    for (int idx = tid; idx < kFoldRows * n; idx += nth) {
+  for (int r0 = 0; (flags & 2) && r0 < m; r0 += FR) {
+    for (int idx = tid; idx < FR * n; idx += nth) {
       int j = idx % n, i = idx / n;
       int row = r0 + i;
       T v = T(0);
@@ -392,20 +413,35 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
       const int buf = j & 1;
       const T tau = s_tau[buf];
       if (tau != T(0)) {
-        const T* u = hu + buf * kFoldRows;
-        for (int c = j + 1 + tid; c < n; c += nth) {
-          T w0 = R[(size_t)j * ldR + c], w1 = T(0), w2 = T(0), w3 = T(0);
+        // four threads per column (adjacent lanes), each over 8 interleaved
+        // rows of the block: every step spreads over up to 64 columns x 4
+        // lanes, i.e. all warps, and the column sum is two lane shuffles
+        const T* u = hu + buf * FR;
+        T* Rj = RF + rowbase(j);
+        const int cq = tid >> 2, rg = tid & 3;
+        for (int cb = j + 1; cb < n; cb += nth >> 2) {
+          const int c = cb + cq;
+          const bool on = c < n;
+          T p0 = T(0), p1 = T(0);
+          T rjc = T(0);
+          if (on) {
 #pragma unroll
-          for (int i = 0; i < kFoldRows; i += 4) {
-            w0 += u[i] * B[(size_t)i * ldB + c];
-            w1 += u[i + 1] * B[(size_t)(i + 1) * ldB + c];
-            w2 += u[i + 2] * B[(size_t)(i + 2) * ldB + c];
-            w3 += u[i + 3] * B[(size_t)(i + 3) * ldB + c];
+            for (int t = 0; t < FR / 4; t += 2) {
+              p0 += u[rg + 4 * t] * B[(size_t)(rg + 4 * t) * ldB + c];
+              p1 += u[rg + 4 * t + 4] * B[(size_t)(rg + 4 * t + 4) * ldB + c];
+            }
+            rjc = Rj[c];
           }
-          T w = ((w0 + w1) + (w2 + w3)) * tau;
-          R[(size_t)j * ldR + c] -= w;
+          T dot = p0 + p1;
+          dot += __shfl_xor_sync(0xffffffff, dot, 1);
+          dot += __shfl_xor_sync(0xffffffff, dot, 2);
+          if (on) {
+            const T w = (dot + rjc) * tau;
+            if (rg == 0) Rj[c] = rjc - w;
 #pragma unroll
-          for (int i = 0; i < kFoldRows; i++) B[(size_t)i * ldB + c] -= w * u[i];
+            for (int t = 0; t < FR / 4; t++)
+              B[(size_t)(rg + 4 * t) * ldB + c] -= w * u[rg + 4 * t];
+          }
         }
       }
       // column j+1 is owned by thread 0: warp 0 forms the next reflector
@@ -415,6 +451,14 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
       }
       __syncthreads();
     }
+  }
+
+  if (packed && (flags & 2)) {
+    for (int idx = tid; idx < n * n; idx += nth) {
+      int i = idx / n, c = idx % n;
+      gws[idx] = c >= i ? RF[rowbase(i) + c] : T(0);
+    }
+    __syncthreads();
   }
 
   // 3. column-pivoted QR of the n x n triangle (LAPACK xGEQP3/xLAQP2 norm
@@ -488,14 +532,16 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
     }
     for (int c = j + 1 + tid; c < n; c += nth) {
       if (tau != T(0)) {
-        T w0 = R[(size_t)j * ldR + c], w1 = T(0);
+        T w0 = R[(size_t)j * ldR + c], w1 = T(0), w2 = T(0), w3 = T(0);
         int i = j + 1;
-        for (; i + 1 < n; i += 2) {
+        for (; i + 3 < n; i += 4) {
           w0 += hu[i] * R[(size_t)i * ldR + c];
           w1 += hu[i + 1] * R[(size_t)(i + 1) * ldR + c];
+          w2 += hu[i + 2] * R[(size_t)(i + 2) * ldR + c];
+          w3 += hu[i + 3] * R[(size_t)(i + 3) * ldR + c];
         }
-        if (i < n) w0 += hu[i] * R[(size_t)i * ldR + c];
-        T w = (w0 + w1) * tau;
+        for (; i < n; i++) w0 += hu[i] * R[(size_t)i * ldR + c];
+        T w = ((w0 + w1) + (w2 + w3)) * tau;
         R[(size_t)j * ldR + c] -= w;
         for (int q = j + 1; q < n; q++) R[(size_t)q * ldR + c] -= w * hu[q];
       }
@@ -549,11 +595,12 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
 // Shared-memory bytes of k_id for a box of n active DOFs: mode 0 keeps the
 // triangle in shared memory, mode 1 in the global scratch.
 template <typename T>
-size_t id_smem_bytes(int n, int mode) {
-  size_t b = sizeof(T) * (size_t)kFoldRows * n + sizeof(T) * 2 * (size_t)std::max(n, kFoldRows) +
+size_t id_smem_bytes(int n, int mode, int fr = kFoldRows) {
+  size_t b = sizeof(T) * (size_t)fr * (n | 1) + sizeof(T) * 2 * (size_t)std::max(n, fr) +
              sizeof(T) * 2 * (size_t)n + sizeof(int) * (size_t)n;
   b = (b + 15) & ~size_t(15);
   if (mode == 0) b += sizeof(T) * (size_t)n * (n | 1);
+  if (mode == 2) b += sizeof(T) * (size_t)n * (n + 1) / 2;
   return b;
 }
 
@@ -595,16 +642,29 @@ __global__ void k_wide_assemble(const WideTask* tasks, T* wpool, const int* ipoo
   }
 }
 
-// Block-wide sum of `cnt` per-thread values (cnt <= kQrNb); result in out[].
+// Block-wide sums of kQrNb per-thread values at once: a butterfly inside each
+// warp leaves lane q with the warp's sum of value q (31 shuffles for 32
+// values), then lane q of every warp is added.  Result in out[0..kQrNb).
 template <typename T>
-__device__ void block_sum_vec(T* vals, int cnt, T* red /* [nwarps][kQrNb] */, T* out) {
+__device__ void block_sum_vec(T (&vals)[kQrNb], T* red /* [nwarps][kQrNb] */, T* out) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int q = 0; q < cnt; q++) {
-    T v = warp_sum(vals[q]);
-    if (lane == 0) red[warp * kQrNb + q] = v;
+#pragma unroll
+  for (int half = 16; half >= 1; half >>= 1) {
+    // keep values whose bit `half` matches the lane's, send the others
+    const bool upper = (lane & half) != 0;
+#pragma unroll
+    for (int q = 0; q < half; q++) {
+      T send = upper ? vals[q] : vals[q + half];
+      T keep = upper ? vals[q + half] : vals[q];
+      vals[q] = keep + __shfl_xor_sync(0xffffffff, send, half);
+    }
   }
+  // lane holds the warp sum of value index = bit-reversed bookkeeping: lane
+  // ends with value (lane) because each step kept the half selected by the
+  // lane's bit in order 16, 8, 4, 2, 1
+  red[warp * kQrNb + lane] = vals[0];
   __syncthreads();
-  if (threadIdx.x < cnt) {
+  if (threadIdx.x < kQrNb) {
     T s = T(0);
     for (int w = 0; w < nw; w++) s += red[w * kQrNb + threadIdx.x];
     out[threadIdx.x] = s;
@@ -624,6 +684,7 @@ __global__ void __launch_bounds__(256) k_qr_panel(const WideTask* tasks, T* wpoo
   T* Tf = wpool + t.Tf;
   __shared__ T red[8 * kQrNb];
   __shared__ T s_sum[kQrNb];
+  __shared__ T s_w[kQrNb];
   __shared__ T s_tau, s_beta, s_scale;
   T vals[kQrNb];
   for (int jj = 0; jj < w; jj++) {
@@ -631,10 +692,13 @@ __global__ void __launch_bounds__(256) k_qr_panel(const WideTask* tasks, T* wpoo
     // reflector of column j
     T sg = T(0);
     for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) sg += A[i + (size_t)m * j] * A[i + (size_t)m * j];
-    vals[0] = sg;
-    block_sum_vec<T>(vals, 1, red, s_sum);
+    T s1 = warp_sum(sg);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s1;
+    __syncthreads();
     if (threadIdx.x == 0) {
-      T sigma = s_sum[0], alpha = A[j + (size_t)m * j];
+      T sigma = T(0);
+      for (int q = 0; q < (int)(blockDim.x >> 5); q++) sigma += red[q];
+      T alpha = A[j + (size_t)m * j];
       T tau = T(0), beta = alpha, scale = T(0);
       if (sigma != T(0)) {
         T nrm = sqrt(alpha * alpha + sigma);
@@ -646,29 +710,32 @@ __global__ void __launch_bounds__(256) k_qr_panel(const WideTask* tasks, T* wpoo
     }
     __syncthreads();
     const T tau = s_tau, scale = s_scale;
-    for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) A[i + (size_t)m * j] *= scale;
-    __syncthreads();
-    if (threadIdx.x == 0) A[j + (size_t)m * j] = s_beta;
-    // one pass over the rows: z_l = V(:,l)^T v_j for l < jj (WY factor) and
-    // the dots of the remaining panel columns with v_j
+    // one pass over the rows (v = scaled column j): z_l = V(:,l)^T v (WY
+    // factor, l < jj) and d_c = c^T v for the remaining panel columns
     const int nz = jj, nd = w - jj - 1;
-    for (int q = 0; q < nz + nd; q++) vals[q] = T(0);
+#pragma unroll
+    for (int q = 0; q < kQrNb; q++) vals[q] = T(0);
+    for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
+      T v = A[i + (size_t)m * j] * scale;
+      A[i + (size_t)m * j] = v;
+#pragma unroll
+      for (int q = 0; q < kQrNb; q++) {
+        int col = q < nz ? p + q : j + 1 + (q - nz);
+        if (q < nz + nd) vals[q] += A[i + (size_t)m * col] * v;
+      }
+    }
+    block_sum_vec<T>(vals, red, s_sum);
+    if (threadIdx.x < nd) s_w[threadIdx.x] = (A[j + (size_t)m * (j + 1 + threadIdx.x)] + s_sum[nz + threadIdx.x]) * tau;
+    __syncthreads();
+    // remaining panel columns: c -= w_c v, all columns in one pass
     for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
       T v = A[i + (size_t)m * j];
-      for (int q = 0; q < nz; q++) vals[q] += A[i + (size_t)m * (p + q)] * v;
-      for (int q = 0; q < nd; q++) vals[nz + q] += A[i + (size_t)m * (j + 1 + q)] * v;
+      for (int q = 0; q < nd; q++) A[i + (size_t)m * (j + 1 + q)] -= s_w[q] * v;
     }
-    block_sum_vec<T>(vals, nz + nd, red, s_sum);
-    // remaining panel columns: c -= tau (v^T c) v
-    for (int q = 0; q < nd; q++) {
-      const int c = j + 1 + q;
-      const T wq = (A[j + (size_t)m * c] + s_sum[nz + q]) * tau;
-      for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) A[i + (size_t)m * c] -= wq * A[i + (size_t)m * j];
-      __syncthreads();
-      if (threadIdx.x == 0) A[j + (size_t)m * c] -= wq;
-    }
+    if (threadIdx.x < nd) A[j + (size_t)m * (j + 1 + threadIdx.x)] -= s_w[threadIdx.x];
+    if (threadIdx.x == 32) A[j + (size_t)m * j] = s_beta;
     // WY factor column jj: T(0:jj, jj) = -tau T(0:jj,0:jj) z, z_l += V(j, l)
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 64) {
       T z[kQrNb];
       for (int l = 0; l < nz; l++) z[l] = s_sum[l] + A[j + (size_t)m * (p + l)];
       for (int l = 0; l < nz; l++) {
@@ -864,10 +931,133 @@ __global__ void __launch_bounds__(kThreads) k_schur(const SchurTask<T>* tasks, i
     for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) t.X[idx] = X[idx];
 }
 
+// ------------------------------------------------- multi-CTA dense helpers --
+// C (m x n, ldc) = beta C + alpha op(A) op(B), op(A) m x kk: 64 x 64 output
+// tiles, 16-deep shared-memory stages, 4 x 4 outputs per thread.
+template <typename T>
+__global__ void __launch_bounds__(256) k_gemm(int m, int n, int kk, T alpha, const T* A, int lda,
+                                              int ta, const T* B, int ldb, int tb, T beta, T* C,
+                                              int ldc) {
+  __shared__ T As[16][64 + 1];
+  __shared__ T Bs[16][64 + 1];
+  const int r0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  T acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) acc[a][b] = T(0);
+  for (int l0 = 0; l0 < kk; l0 += 16) {
+    for (int e = threadIdx.x; e < 16 * 64; e += blockDim.x) {
+      int l = e % 16, i = e / 16;
+      int gi = r0 + i, gl = l0 + l;
+      T av = T(0);
+      if (gi < m && gl < kk) av = ta ? A[gl + (size_t)lda * gi] : A[gi + (size_t)lda * gl];
+      As[l][i] = av;
+      int gj = c0 + i;
+      T bv = T(0);
+      if (gj < n && gl < kk) bv = tb ? B[gj + (size_t)ldb * gl] : B[gl + (size_t)ldb * gj];
+      Bs[l][i] = bv;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int l = 0; l < 16; l++) {
+      T av[4], bv[4];
+#pragma unroll
+      for (int a = 0; a < 4; a++) av[a] = As[l][tx + 16 * a];
+#pragma unroll
+      for (int b = 0; b < 4; b++) bv[b] = Bs[l][ty + 16 * b];
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) acc[a][b] += av[a] * bv[b];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      int i = r0 + tx + 16 * a, j = c0 + ty + 16 * b;
+      if (i < m && j < n) {
+        T* c = C + i + (size_t)ldc * j;
+        *c = (beta == T(0) ? T(0) : beta * *c) + alpha * acc[a][b];
+      }
+    }
+}
+
+template <typename T>
+void gemm(cudaStream_t s, int m, int n, int kk, T alpha, const T* A, int lda, bool ta, const T* B,
+          int ldb, bool tb, T beta, T* C, int ldc) {
+  if (m <= 0 || n <= 0) return;
+  dim3 g((m + 63) / 64, (n + 63) / 64);
+  k_gemm<T><<<g, 256, 0, s>>>(m, n, kk, alpha, A, lda, ta, B, ldb, tb, beta, C, ldc);
+}
+
+// dst (rows x cols, ldd) = src block or its transpose (src rows/cols swapped)
+template <typename T>
+__global__ void k_copy_block(const T* src, int lds, int rows, int cols, int trans, T* dst, int ldd) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)rows * cols;
+       e += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(e % rows), j = (int)(e / rows);
+    dst[i + (size_t)ldd * j] = trans ? src[j + (size_t)lds * i] : src[i + (size_t)lds * j];
+  }
+}
+
+template <typename T>
+__global__ void k_perm_gather(const T* K, int n, const int* perm, T* P) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(e % n), j = (int)(e / n);
+    P[e] = K[perm[i] + (size_t)n * perm[j]];
+  }
+}
+
+template <typename T>
+void copy_block(cudaStream_t s, const T* src, int lds, int rows, int cols, bool trans, T* dst, int ldd) {
+  size_t ne = (size_t)rows * cols;
+  if (ne == 0) return;
+  k_copy_block<T><<<(int)std::min<size_t>(2048, (ne + 255) / 256), 256, 0, s>>>(src, lds, rows, cols,
+                                                                              trans, dst, ldd);
+}
+
 template <typename T>
 size_t schur_bytes(int n, int k) {
   size_t r = n - k;
   return sizeof(T) * ((size_t)n * n + 2 * r * k + r * r);
+}
+
+// SkelFactorization::decouple for a box whose working set does not fit in one
+// SM's shared memory: the same steps as k_schur as device-wide launches
+// (tiled GEMMs, blocked LU and triangular solves) on stream st.
+template <typename T>
+void schur_wide(const SchurTask<T>& t, int* d_err, cudaStream_t st) {
+  const int n = t.n, k = t.k, r = n - k;
+  T* Pm = t.ws;
+  T* Wrs = Pm + (size_t)n * n;
+  T* Lt = Wrs + (size_t)r * k;
+  T* X = t.X;
+  const T* Tm = t.Tin;
+  size_t ne = (size_t)n * n;
+  k_perm_gather<T><<<(int)std::min<size_t>(4096, (ne + 255) / 256), 256, 0, st>>>(t.K, n, t.perm, Pm);
+  KI_CUDA(cudaMemcpyAsync(t.Tout, t.Tin, sizeof(T) * (size_t)k * r, cudaMemcpyDeviceToDevice, st));
+  const T* Kss = Pm;
+  const T* Ksr = Pm + (size_t)n * k;
+  copy_block<T>(st, Pm + k, n, r, k, false, Wrs, r);              // K_rs
+  copy_block<T>(st, Ksr, n, r, k, true, Lt, r);                   // K_sr^T
+  copy_block<T>(st, Pm + k + (size_t)n * k, n, r, r, false, X, r);  // K_rr
+  gemm<T>(st, r, k, k, T(-1), Tm, k, true, Kss, n, false, T(1), Wrs, r);
+  gemm<T>(st, r, k, k, T(-1), Tm, k, true, Kss, n, true, T(1), Lt, r);
+  gemm<T>(st, r, r, k, T(-1), Tm, k, true, Ksr, n, false, T(1), X, r);
+  gemm<T>(st, r, r, k, T(-1), Wrs, r, false, Tm, k, false, T(1), X, r);
+  dense_lu<T>(X, r, t.piv, d_err, st);
+  dense_lu_solve<T>(X, r, t.piv, Lt, r, k, true, st);              // L^T
+  copy_block<T>(st, Kss, n, k, k, false, t.Atil, k);
+  gemm<T>(st, k, k, r, T(-1), Lt, r, true, Wrs, r, false, T(1), t.Atil, k);
+  dense_lu_solve<T>(X, r, t.piv, Wrs, r, k, false, st);            // U
+  KI_CUDA(cudaMemcpyAsync(t.U, Wrs, sizeof(T) * (size_t)r * k, cudaMemcpyDeviceToDevice, st));
+  copy_block<T>(st, Lt, r, k, r, true, t.L, k);                    // L = (L^T)^T
+  KI_CUDA(cudaGetLastError());
 }
 
 template <typename T>
@@ -1441,8 +1631,9 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     F->stage_begin(id_name.c_str(), 0, 0);
     size_t id_rec = F->prof_open.size() - 1;
     // (a) row lists of every box (m is needed to pick the path)
-    KI_CUDA(cudaFuncSetAttribute(k_id<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
-    k_id<T><<<(unsigned)itasks.size(), kThreads, 0, s>>>(d_it, 0, d_soff, d_slen, ipool, d_irows, d_tws,
+    KI_CUDA(cudaFuncSetAttribute(k_id<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
+    KI_CUDA(cudaFuncSetAttribute(k_id<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
+    k_id<T, 32><<<(unsigned)itasks.size(), kThreads, 0, s>>>(d_it, 0, d_soff, d_slen, ipool, d_irows, d_tws,
                                                          P, sd, np, d_pcs, d_pcs + np, prm.id_tol,
                                                          d_k, d_m, 0, 1);
     KI_CUDA(cudaGetLastError());
@@ -1456,12 +1647,18 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     // by the tests to drive every box through it)
     int kWideRows = 1536;
     if (const char* e = std::getenv("KI_WIDE_ROWS")) kWideRows = std::atoi(e);
+    // largest shared footprint with the full triangle in shared memory
+    // (environment override KI_ID_FULL_CAP, used by the tests)
+    size_t full_cap = smem_cap;
+    if (const char* e = std::getenv("KI_ID_FULL_CAP")) full_cap = (size_t)std::atol(e);
     std::vector<int> grp(itasks.size());
     for (size_t i = 0; i < itasks.size(); i++) {
       int n = itasks[i].n;
-      int md = id_smem_bytes<T>(n, 0) <= smem_cap ? 0 : 1;
-      bool wide = mh[i] > kWideRows || md == 1;
-      grp[i] = (wide ? 2 : 0) + md;
+      int md = id_smem_bytes<T>(n, 0) <= full_cap ? 0 : 1;
+      bool wide = mh[i] > kWideRows || (md == 1 && id_smem_bytes<T>(n, 2) > smem_cap);
+      // narrow groups: 0 triangle in shared memory, 1 packed triangle in
+      // shared memory (mode 2 of k_id); wide groups: 2 / 3 by triangle size
+      grp[i] = wide ? 2 + md : md;
     }
     std::vector<int> mode_of(itasks.size());
     {
@@ -1484,7 +1681,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       mh.swap(m2);
       for (size_t i = 0; i < comp.size(); i++) {
         hb[comp[i]].pact = itasks[i].pact;
-        mode_of[i] = grp[i] & 1;
+        mode_of[i] = grp[i];
       }
       upload(d_it, itasks, s);
       upload(d_m, mh, s);
@@ -1501,24 +1698,36 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
           cnt++;
         }
       if (cnt == 0) return;
+      const int kmode = g == 1 ? 2 : (g & 1);   // group -> k_id storage mode
+      // 64-row fold blocks (half the serial steps) where they fit
+      auto fold_rows = [&](int n) {
+        return (kmode != 1 && (flags & 2) && id_smem_bytes<T>(n, kmode, 64) <= smem_cap) ? 64 : 32;
+      };
       int b0 = first;
       while (b0 < first + cnt) {
-        size_t sm0 = id_smem_bytes<T>(itasks[b0].n, g & 1);
+        const int fr = fold_rows(itasks[b0].n);
+        size_t sm0 = id_smem_bytes<T>(itasks[b0].n, kmode, fr);
         // CTAs per SM at this footprint; extend the bin while it stays the same
         int per_sm = std::max(1, (int)(228 * 1024 / (sm0 + 1024)));
         int b1 = b0 + 1;
         size_t sm = sm0;
         while (b1 < first + cnt) {
-          size_t s1 = id_smem_bytes<T>(itasks[b1].n, g & 1);
+          if (fold_rows(itasks[b1].n) != fr) break;
+          size_t s1 = id_smem_bytes<T>(itasks[b1].n, kmode, fr);
           if (std::max(1, (int)(228 * 1024 / (s1 + 1024))) != per_sm) break;
           sm = std::max(sm, s1);
           b1++;
         }
         if (sm > smem_cap) throw std::runtime_error("box too large for the ID kernel");
         cudaStream_t st = fixed ? fixed : F->aux[(next_aux++) % (Factorization<T>::kAux - 1)];
-        k_id<T><<<(unsigned)(b1 - b0), kThreads, sm, st>>>(d_it, b0, d_soff, d_slen, ipool, d_irows,
-                                                           d_tws, P, sd, np, d_pcs, d_pcs + np,
-                                                           prm.id_tol, d_k, d_m, g & 1, flags);
+        if (fr == 64)
+          k_id<T, 64><<<(unsigned)(b1 - b0), kThreads, sm, st>>>(d_it, b0, d_soff, d_slen, ipool, d_irows,
+                                                                 d_tws, P, sd, np, d_pcs, d_pcs + np,
+                                                                 prm.id_tol, d_k, d_m, kmode, flags);
+        else
+          k_id<T, 32><<<(unsigned)(b1 - b0), kThreads, sm, st>>>(d_it, b0, d_soff, d_slen, ipool, d_irows,
+                                                                 d_tws, P, sd, np, d_pcs, d_pcs + np,
+                                                                 prm.id_tol, d_k, d_m, kmode, flags);
         KI_CUDA(cudaGetLastError());
         b0 = b1;
       }
@@ -1563,6 +1772,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         WideTask* d_wt = nullptr;
         KI_CUDA(cudaMallocAsync((void**)&d_wt, sizeof(WideTask) * wt.size(), ws3));
         upload(d_wt, wt, ws3);
+        std::string wq = "wide_qr@L" + std::to_string(l);
+        F->stage_begin(wq.c_str(), 0, 0, ws3);
         k_wide_assemble<T><<<dim3((unsigned)wt.size(), (maxn + 7) / 8), 256, 0, ws3>>>(
             d_wt, d_wpool, ipool, d_irows, P, sd, np, d_pcs, d_pcs + np);
         for (int p0 = 0; p0 < maxn; p0 += kQrNb) {
@@ -1572,8 +1783,12 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         }
         k_wide_triangle<T><<<(unsigned)wt.size(), 256, 0, ws3>>>(d_wt, d_wpool, d_tws);
         KI_CUDA(cudaGetLastError());
+        F->stage_end(ws3);
+        std::string wc = "wide_cpqr@L" + std::to_string(l);
+        F->stage_begin(wc.c_str(), 0, 0, ws3);
         launch_range(2, 4, ws3);
         launch_range(3, 4, ws3);
+        F->stage_end(ws3);
         KI_CUDA(cudaFreeAsync(d_wpool, ws3));
         KI_CUDA(cudaFreeAsync(d_wt, ws3));
       }
@@ -1687,21 +1902,37 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     F->stage_begin(sc_name.c_str(), sf, sb);
     {
       // shared-memory boxes first, then the ones whose working set is global
-      const size_t cap = 225 * 1024;
+      // (environment override KI_SCHUR_SMEM_CAP, used by the tests)
+      size_t cap = 225 * 1024;
+      if (const char* e = std::getenv("KI_SCHUR_SMEM_CAP")) cap = (size_t)std::atol(e);
       std::vector<SchurTask<T>> st2;
       size_t sm = 0;
       int n_sm = 0;
+      // three classes: shared-memory CTA per box; global-memory CTA per box
+      // (all in one launch); device-wide launches per box for the few very
+      // large ones (n above KI_SCHUR_WIDE_N, default 288)
+      int wide_n = 288;
+      if (const char* e = std::getenv("KI_SCHUR_WIDE_N")) wide_n = std::atoi(e);
       for (auto& q : st)
         if (schur_bytes<T>(q.n, q.k) <= cap) { st2.push_back(q); sm = std::max(sm, schur_bytes<T>(q.n, q.k)); n_sm++; }
+      int n_glob = 0;
       for (auto& q : st)
-        if (schur_bytes<T>(q.n, q.k) > cap) st2.push_back(q);
+        if (schur_bytes<T>(q.n, q.k) > cap && q.n <= wide_n) { st2.push_back(q); n_glob++; }
+      for (auto& q : st)
+        if (schur_bytes<T>(q.n, q.k) > cap && q.n > wide_n) st2.push_back(q);
       upload(d_st, st2, s);
       if (n_sm > 0) {
         KI_CUDA(cudaFuncSetAttribute(k_schur<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
         k_schur<T><<<(unsigned)n_sm, kThreads, sm, s>>>(d_st, 0, 1, F->d_err);
       }
-      if ((int)st2.size() > n_sm)
-        k_schur<T><<<(unsigned)(st2.size() - n_sm), kThreads, 0, s>>>(d_st, n_sm, 0, F->d_err);
+      if (n_glob > 0)
+        k_schur<T><<<(unsigned)n_glob, kThreads, 0, s>>>(d_st, n_sm, 0, F->d_err);
+      if ((int)st2.size() > n_sm + n_glob) {
+        F->fork();
+        for (size_t q = n_sm + n_glob; q < st2.size(); q++)
+          schur_wide<T>(st2[q], F->d_err, F->aux[(q - n_sm - n_glob) % Factorization<T>::kAux]);
+        F->join(Factorization<T>::kAux);
+      }
     }
     F->stage_end();
     KI_CUDA(cudaGetLastError());

@@ -89,11 +89,12 @@ struct Factorization {
   std::vector<int> rank_hist;
   bool profile_solve = false;        // record stage events in solves
   std::vector<StageRec> prof_open;   // launches recorded since the last collect
+  std::vector<size_t> prof_stack;    // open stages (nested begin/end pairs)
   std::vector<StageSum> factor_prof; // per stage, factorization
   std::vector<LevelStat> level_stats;
   std::vector<StageSum> solve_prof;  // per stage, last solve
-  void stage_begin(const char* name, double flops, double bytes);
-  void stage_end();
+  void stage_begin(const char* name, double flops, double bytes, cudaStream_t on = nullptr);
+  void stage_end(cudaStream_t on = nullptr);
   std::vector<StageSum> collect();   // synchronizes the stream
   double factor_seconds = 0;
   size_t device_bytes = 0;

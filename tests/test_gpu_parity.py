@@ -82,11 +82,18 @@ def test_gpu_holes_against_oracle_and_field(pkg, oracle_mod):
     assert np.abs(u - ue).max() <= 1e-8 * np.abs(ue).max()
 
 
-@pytest.mark.parametrize("wide_rows", ["0", "400"])
-def test_gpu_wide_path_matches_oracle(pkg, oracle_mod, monkeypatch, wide_rows):
-    """Boxes with tall ID matrices go through the explicit-matrix blocked QR;
-    forcing the row threshold down drives (nearly) every box through it."""
+@pytest.mark.parametrize("wide_rows,schur_cap,full_cap,schur_wide_n",
+                         [("0", "0", "230400", "0"), ("400", "225000", "230400", "288"),
+                          ("100000", "0", "0", "100000")])
+def test_gpu_wide_path_matches_oracle(pkg, oracle_mod, monkeypatch, wide_rows, schur_cap,
+                                      full_cap, schur_wide_n):
+    """Boxes with tall ID matrices go through the explicit-matrix blocked QR
+    and large boxes through the multi-CTA Schur elimination; forcing the
+    thresholds down drives (nearly) every box through them."""
     monkeypatch.setenv("KI_WIDE_ROWS", wide_rows)
+    monkeypatch.setenv("KI_SCHUR_SMEM_CAP", schur_cap)
+    monkeypatch.setenv("KI_ID_FULL_CAP", full_cap)            # 0: packed triangles
+    monkeypatch.setenv("KI_SCHUR_WIDE_N", schur_wide_n)       # 0: device-wide Schur
     g = pkg.geometry
     prob = g.disc_with_ellipses(1 << 13, 6, seed=5)
     f = g.laplace_source_rhs(prob, np.array([[3.0, 1.0]]))
@@ -99,7 +106,10 @@ def test_gpu_wide_path_matches_oracle(pkg, oracle_mod, monkeypatch, wide_rows):
     assert rel_max(mu, ref) <= 10 * tol
     assert fac.info()["n_root"] == st["root"]
     paths = [lv["paths"] for lv in fac.profile()["levels"]]
-    assert sum(p[2] + p[3] for p in paths) > 0
+    if wide_rows == "0":
+        assert sum(p[2] + p[3] for p in paths) > 0
+    if full_cap == "0":
+        assert sum(p[1] for p in paths) > 0
 
 
 def test_gpu_multi_rhs_equals_single_columns(pkg):
