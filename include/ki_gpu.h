@@ -180,6 +180,13 @@ int ki_eval_targets(ki_factor* f, const double* targets, int n_targets, const do
 int ki_factor_get_profile(ki_factor* f, char* buf, int len);
 int ki_factor_set_profiling(ki_factor* f, int on);
 
+/*
+ * FMA throughput of the current GPU's CUDA cores in GFLOP/s (FP64 and FP32),
+ * measured with register-resident independent FMA chains.  No reference
+ * counterpart: the compute denominators of the roofline figures.
+ */
+int ki_measure_fma_peak(double* fp64_gflops, double* fp32_gflops);
+
 /* Message of the last failure on the calling thread ("" if none). */
 const char* ki_last_error(void);
 

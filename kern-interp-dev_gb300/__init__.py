@@ -29,7 +29,8 @@ PRECISION_FP64, PRECISION_FP32 = 0, 1
 
 EXPORTED = ["ki_factor_create", "ki_factor_destroy", "ki_factor_get_info", "ki_solve",
             "ki_solve_device", "ki_apply", "ki_eval_targets", "ki_last_error", "ki_version",
-            "ki_factor_get_profile", "ki_factor_set_profiling", "ki_apply_rows"]
+            "ki_factor_get_profile", "ki_factor_set_profiling", "ki_apply_rows",
+            "ki_measure_fma_peak"]
 
 
 class KiError(RuntimeError):
@@ -81,6 +82,7 @@ def load_library(path=None):
     lib.ki_apply_rows.argtypes = [V, V, I, V, I, I, V, I, V, I]
     lib.ki_factor_get_profile.argtypes = [V, ctypes.c_char_p, I]
     lib.ki_factor_set_profiling.argtypes = [V, I]
+    lib.ki_measure_fma_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     lib.ki_last_error.restype = ctypes.c_char_p
     lib.ki_version.restype = ctypes.c_char_p
     for name in EXPORTED:
@@ -220,6 +222,13 @@ class Factor:
                                               self.n_dofs, M.shape[1], _ptr(A),
                                               max(1, self.n_border), _ptr(out), nt))
         return out[:, 0] if vec else out
+
+
+def measure_fma_peak():
+    """(FP64, FP32) CUDA-core FMA throughput of the current GPU, GFLOP/s."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    _check(load_library().ki_measure_fma_peak(ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value
 
 
 # ----------------------------------------------------------- reference mirror

@@ -395,6 +395,42 @@ void solve_impl_noalloc(ki_factor* f, ki::Factorization<T>& F, const double* d_b
   }
 }
 
+// FMA-throughput microbenchmark: register-resident independent FMA chains,
+// 8 CTAs of 256 threads per SM.  Gives the compute denominators of the
+// roofline for CUDA-core work (the pipe the factorization kernels use).
+template <typename T>
+__global__ void k_fma_peak(T* out, int iters) {
+  T a0 = T(threadIdx.x) * T(1e-3), a1 = a0 + T(1), a2 = a0 + T(2), a3 = a0 + T(3);
+  T a4 = a0 + T(4), a5 = a0 + T(5), a6 = a0 + T(6), a7 = a0 + T(7);
+  const T b = T(0.999999), c = T(1e-7);
+  for (int i = 0; i < iters; i++) {
+    a0 = a0 * b + c; a1 = a1 * b + c; a2 = a2 * b + c; a3 = a3 * b + c;
+    a4 = a4 * b + c; a5 = a5 * b + c; a6 = a6 * b + c; a7 = a7 * b + c;
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+template <typename T>
+double fma_peak_gflops(int sms, int iters) {
+  const int blocks = sms * 8, threads = 256;
+  T* out = nullptr;
+  KI_CHECK_CUDA(cudaMalloc(&out, sizeof(T) * blocks * threads));
+  k_fma_peak<T><<<blocks, threads>>>(out, 16);
+  cudaEvent_t e0, e1;
+  KI_CHECK_CUDA(cudaEventCreate(&e0));
+  KI_CHECK_CUDA(cudaEventCreate(&e1));
+  KI_CHECK_CUDA(cudaEventRecord(e0));
+  k_fma_peak<T><<<blocks, threads>>>(out, iters);
+  KI_CHECK_CUDA(cudaEventRecord(e1));
+  KI_CHECK_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  KI_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  return 2.0 * 8 * (double)iters * blocks * threads / (ms * 1e-3) / 1e9;
+}
+
 }  // namespace
 
 extern "C" {
@@ -695,6 +731,17 @@ int ki_factor_get_profile(ki_factor* f, char* buf, int len) {
     if (f->f32) fill(*f->f32);
     if ((int)j.size() + 1 > len) throw ArgError("profile buffer too small");
     std::memcpy(buf, j.c_str(), j.size() + 1);
+  });
+}
+
+int ki_measure_fma_peak(double* fp64_gflops, double* fp32_gflops) {
+  return guarded([&] {
+    if (!fp64_gflops || !fp32_gflops) throw ArgError("NULL argument");
+    int dev = 0, sms = 0;
+    KI_CHECK_CUDA(cudaGetDevice(&dev));
+    KI_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    *fp64_gflops = fma_peak_gflops<double>(sms, 20000);
+    *fp32_gflops = fma_peak_gflops<float>(sms, 200000);
   });
 }
 

@@ -179,4 +179,66 @@ __device__ void cta_lu_solve(int n, const T* LU, int lda, const int* piv, bool t
   __syncthreads();
 }
 
+// The same solves with every thread of the block: pivots by column, then
+// column-oriented substitution (one barrier per row), the update of the
+// remaining rows spread over (row, column) pairs.
+template <typename T>
+__device__ void cta_lu_solve_par(int n, const T* LU, int lda, const int* piv, bool trans, T* B,
+                                 int ldb, int nrhs) {
+  const int tid = threadIdx.x, nth = blockDim.x;
+  if (!trans) {
+    for (int c = tid; c < nrhs; c += nth) {
+      T* b = B + (size_t)ldb * c;
+      for (int i = 0; i < n; i++) {
+        int p = piv[i];
+        if (p != i) { T t = b[i]; b[i] = b[p]; b[p] = t; }
+      }
+    }
+    __syncthreads();
+    for (int l = 0; l < n - 1; l++) {          // unit lower
+      const int rows = n - 1 - l;
+      for (int e = tid; e < rows * nrhs; e += nth) {
+        int i = l + 1 + e % rows, c = e / rows;
+        B[i + (size_t)ldb * c] -= LU[i + (size_t)lda * l] * B[l + (size_t)ldb * c];
+      }
+      __syncthreads();
+    }
+    for (int l = n - 1; l >= 0; l--) {         // upper
+      for (int c = tid; c < nrhs; c += nth) B[l + (size_t)ldb * c] /= LU[l + (size_t)lda * l];
+      __syncthreads();
+      for (int e = tid; e < l * nrhs; e += nth) {
+        int i = e % l, c = e / l;
+        B[i + (size_t)ldb * c] -= LU[i + (size_t)lda * l] * B[l + (size_t)ldb * c];
+      }
+      __syncthreads();
+    }
+  } else {
+    for (int l = 0; l < n; l++) {              // U^T (lower, U's diagonal)
+      for (int c = tid; c < nrhs; c += nth) B[l + (size_t)ldb * c] /= LU[l + (size_t)lda * l];
+      __syncthreads();
+      const int rows = n - 1 - l;
+      for (int e = tid; e < rows * nrhs; e += nth) {
+        int i = l + 1 + e % rows, c = e / rows;
+        B[i + (size_t)ldb * c] -= LU[l + (size_t)lda * i] * B[l + (size_t)ldb * c];
+      }
+      __syncthreads();
+    }
+    for (int l = n - 1; l >= 1; l--) {         // L^T (unit upper)
+      for (int e = tid; e < l * nrhs; e += nth) {
+        int i = e % l, c = e / l;
+        B[i + (size_t)ldb * c] -= LU[l + (size_t)lda * i] * B[l + (size_t)ldb * c];
+      }
+      __syncthreads();
+    }
+    for (int c = tid; c < nrhs; c += nth) {
+      T* b = B + (size_t)ldb * c;
+      for (int i = n - 1; i >= 0; i--) {
+        int p = piv[i];
+        if (p != i) { T t = b[i]; b[i] = b[p]; b[p] = t; }
+      }
+    }
+  }
+  __syncthreads();
+}
+
 }  // namespace ki

@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   const int ldB = n | 1;
   size_t off = 0;
   T* B = reinterpret_cast<T*>(id_smem);
-  off += sizeof(T) * (size_t)FR * ldB;
+  if (flags & 2) off += sizeof(T) * (size_t)FR * ldB;   // the fold block exists only when folding
   T* hu = reinterpret_cast<T*>(id_smem + off);   // [2][n] reflector tails (fold: 32, CPQR: n)
   off += sizeof(T) * 2 * (size_t)max(n, FR);
   T* vn1 = reinterpret_cast<T*>(id_smem + off);
@@ -595,8 +595,8 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
 // Shared-memory bytes of k_id for a box of n active DOFs: mode 0 keeps the
 // triangle in shared memory, mode 1 in the global scratch.
 template <typename T>
-size_t id_smem_bytes(int n, int mode, int fr = kFoldRows) {
-  size_t b = sizeof(T) * (size_t)fr * (n | 1) + sizeof(T) * 2 * (size_t)std::max(n, fr) +
+size_t id_smem_bytes(int n, int mode, int fr = kFoldRows, int flags = 2) {
+  size_t b = ((flags & 2) ? sizeof(T) * (size_t)fr * (n | 1) : 0) + sizeof(T) * 2 * (size_t)std::max(n, fr) +
              sizeof(T) * 2 * (size_t)n + sizeof(int) * (size_t)n;
   b = (b + 15) & ~size_t(15);
   if (mode == 0) b += sizeof(T) * (size_t)n * (n | 1);
@@ -914,14 +914,14 @@ __global__ void __launch_bounds__(kThreads) k_schur(const SchurTask<T>* tasks, i
   int info = cta_lu<T>(r, X, r, t.piv, &s_flag, &s_red, &s_idx);
   if (info != 0 && threadIdx.x == 0) atomicMax(err, (int)kDevSingular);
   // L^T = X^-T K~_sr^T
-  cta_lu_solve<T>(r, X, r, t.piv, true, Lt, r, k);
+  cta_lu_solve_par<T>(r, X, r, t.piv, true, Lt, r, k);
   // A~ = K_ss - L K~_rs  (k x k), L = Lt^T
   for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) t.Atil[idx] = Kss[idx % k + (size_t)n * (idx / k)];
   __syncthreads();
   cta_gemm<T>(k, k, r, T(-1), Lt, r, true, Wrs, r, false, T(1), t.Atil, k);
   __syncthreads();
   // U = X^-1 K~_rs (in place on Wrs)
-  cta_lu_solve<T>(r, X, r, t.piv, false, Wrs, r, k);
+  cta_lu_solve_par<T>(r, X, r, t.piv, false, Wrs, r, k);
   for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) t.U[idx] = Wrs[idx];
   for (int idx = threadIdx.x; idx < k * r; idx += blockDim.x) {
     int i = idx % k, j = idx / k;
@@ -1128,7 +1128,7 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
       xs[l + (size_t)n * c] -= acc;
     }
     __syncthreads();
-    if (mode == kUpDiag) cta_lu_solve<T>(r, t.X, r, t.piv, false, xr, n, nc);
+    if (mode == kUpDiag) cta_lu_solve_par<T>(r, t.X, r, t.piv, false, xr, n, nc);
   } else if (mode == kDown) {
     // x_r -= U x_s
     for (int idx = threadIdx.x; idx < r * nc; idx += blockDim.x) {
@@ -1147,7 +1147,7 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
     }
     __syncthreads();
   } else if (mode == kDiag) {
-    cta_lu_solve<T>(r, t.X, r, t.piv, false, xr, n, nc);
+    cta_lu_solve_par<T>(r, t.X, r, t.piv, false, xr, n, nc);
   }
   __syncthreads();
   const int lo = mode == kDiag ? k : 0;   // the diagonal solve changes x_r only
@@ -1706,14 +1706,14 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       int b0 = first;
       while (b0 < first + cnt) {
         const int fr = fold_rows(itasks[b0].n);
-        size_t sm0 = id_smem_bytes<T>(itasks[b0].n, kmode, fr);
+        size_t sm0 = id_smem_bytes<T>(itasks[b0].n, kmode, fr, flags);
         // CTAs per SM at this footprint; extend the bin while it stays the same
         int per_sm = std::max(1, (int)(228 * 1024 / (sm0 + 1024)));
         int b1 = b0 + 1;
         size_t sm = sm0;
         while (b1 < first + cnt) {
           if (fold_rows(itasks[b1].n) != fr) break;
-          size_t s1 = id_smem_bytes<T>(itasks[b1].n, kmode, fr);
+          size_t s1 = id_smem_bytes<T>(itasks[b1].n, kmode, fr, flags);
           if (std::max(1, (int)(228 * 1024 / (s1 + 1024))) != per_sm) break;
           sm = std::max(sm, s1);
           b1++;
@@ -2004,16 +2004,22 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
             F->d_PsiTmod);
         KI_CUDA(cudaGetLastError());
         F->stage_begin("border_sweeps", 0, 0);
+        F->stage_begin("border_U_Psi", 0, 0);
         for (int l = L - 1; l >= 1; l--) {
           launch_sweep<T>(*F, l, kUp, F->d_Umod, nb, s);
           launch_sweep<T>(*F, l, kPsi, F->d_PsiTmod, nb, s);
         }
+        F->stage_end();
         T* dD = nullptr;
         KI_CUDA(cudaMallocAsync((void**)&dD, Tsz * (size_t)N * nb, s));
         KI_CUDA(cudaMemcpyAsync(dD, F->d_Umod, Tsz * (size_t)N * nb, cudaMemcpyDeviceToDevice, s));
+        F->stage_begin("border_Dinv", 0, 0);
         for (int l = L - 1; l >= 1; l--) launch_sweep<T>(*F, l, kDiag, dD, nb, s);
+        F->stage_end();
         T* corr = (T*)F->alloc(Tsz * (size_t)nb * nb);
+        F->stage_begin("border_corr", 0, 0);
         reduce_rows<T>(*F, F->d_PsiTmod, nb, dD, nb, corr, s);
+        F->stage_end();
         F->stage_end();
         KI_CUDA(cudaFreeAsync(dD, s));
         const int ns = h.n + nb;
@@ -2084,20 +2090,28 @@ void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha) {
   sb("sweep_up");
   for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kUp, d_x, ncols, s);
   se();
-  sb("border_solve");
+  sb("border_diag");
   T *Dw = nullptr, *t = nullptr, *M = nullptr;
   KI_CUDA(cudaMallocAsync((void**)&Dw, sizeof(T) * (size_t)N * ncols + 16, s));
   KI_CUDA(cudaMallocAsync((void**)&t, sizeof(T) * (size_t)nb * ncols + 16, s));
   KI_CUDA(cudaMallocAsync((void**)&M, sizeof(T) * (size_t)ns * ncols + 16, s));
   KI_CUDA(cudaMemcpyAsync(Dw, d_x, sizeof(T) * (size_t)N * ncols, cudaMemcpyDeviceToDevice, s));
   for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kDiag, Dw, ncols, s);
+  se();
+  sb("border_reduce");
   reduce_rows<T>(F, F.d_PsiTmod, nb, Dw, ncols, t, s);                 // Psi~_r D^-1 w
+  se();
+  sb("border_root");
   k_mc_rhs<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
       d_x, ncols, F.d_root_idx, nr, t, nb, ncols, M);
   dense_lu_solve<T>(F.d_root_lu, ns, F.d_root_piv, M, ns, ncols, false, s);
+  se();
+  sb("border_update");
   k_mc_update<T><<<std::min(8192, (int)(((size_t)N * ncols + 255) / 256)), 256, 0, s>>>(
       d_x, ncols, F.d_Umod, nb, M, nr, N, F.d_is_skel);                // w - U~_r alpha
   KI_CUDA(cudaGetLastError());
+  se();
+  sb("border_diag");
   for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kDiag, d_x, ncols, s);
   se();
   k_mc_finish<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
