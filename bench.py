@@ -8,7 +8,7 @@ factorization (tree + skeletonization + bordered system) and one solve of all
 32 right-hand sides.  Metric: DOF/s = unknowns x right-hand sides / step time.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--precision fp64|fp32] [--n UNKNOWNS] [--nrhs R] [--tol T]
+                  [--precision fp64|fp32] [--unknowns N] [--nrhs R] [--tol T]
 
 `value` is timed with the right-hand sides resident in HBM (ki_solve_device);
 `e2e` through the host-buffer C-ABI call (ki_solve), host<->device copies of
@@ -39,7 +39,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
-    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--unknowns", dest="n", type=int, default=1 << 20)
     ap.add_argument("--holes", type=int, default=64)
     ap.add_argument("--nrhs", type=int, default=32)
     ap.add_argument("--tol", type=float, default=1e-8)
@@ -50,10 +50,8 @@ def parse():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    import __graft_entry__ as g
+    return g.load_package().replicas.env()
 
 
 def make_problem(pkg, n, holes, nrhs):
@@ -180,15 +178,13 @@ def run_reference(args, rank, world):
 
 def main():
     args = parse()
-    rank, world, local = dist_env()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+    import __graft_entry__ as g
+    rep = g.load_package().replicas
+    rank, world, local = rep.env()
+    rep.init("nccl" if args.impl == "gb300" else "gloo")
     if args.impl == "reference":
         run_reference(args, rank, world)
-        if world > 1:
-            import torch.distributed as dist
-            dist.destroy_process_group()
+        rep.finish()
         return
     import torch
     torch.cuda.set_device(local)
@@ -223,10 +219,7 @@ def main():
                                 pin_a.data_ptr(), max(1, nb)))
         return fac
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+    barrier = rep.barrier
 
     for _ in range(args.warmup):
         f = step_device()
@@ -248,12 +241,7 @@ def main():
         ev1.record()
         torch.cuda.synchronize()
     barrier()
-    t_dev = ev0.elapsed_time(ev1) / 1e3 / args.steps
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_dev], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev = float(tt.item())
+    t_dev = rep.max_over_ranks(ev0.elapsed_time(ev1) / 1e3 / args.steps, device="cuda")
     # ---- e2e: host buffers through the C ABI
     barrier()
     torch.cuda.synchronize()
@@ -265,12 +253,7 @@ def main():
     e1.record()
     torch.cuda.synchronize()
     barrier()
-    t_e2e = e0.elapsed_time(e1) / 1e3 / args.steps
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_e2e], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt.item())
+    t_e2e = rep.max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps, device="cuda")
 
     # ---- accuracy of the last solution (sampled dense FP64 residual, analytic field)
     fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, **kw)
@@ -287,9 +270,7 @@ def main():
     fac.close()
 
     if rank != 0:
-        if world > 1:
-            import torch.distributed as dist
-            dist.destroy_process_group()
+        rep.finish()
         return
 
     # ---- roofline of the dominant kernel (average over the timed steps)
@@ -370,9 +351,7 @@ def main():
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    rep.finish()
 
 
 if __name__ == "__main__":

@@ -342,3 +342,4 @@ def boundary_integral_solve(kernel, boundary, quadtree, id_tol, fact_threads, do
 
 
 from . import geometry  # noqa: E402,F401
+from . import replicas  # noqa: E402,F401
