@@ -39,6 +39,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--workload", default="laplace2d_disc_ellipses",
+                    choices=["laplace2d_disc_ellipses", "stokes2d_disc_circles", "laplace2d_star"])
     ap.add_argument("--unknowns", dest="n", type=int, default=1 << 20)
     ap.add_argument("--holes", type=int, default=64)
     ap.add_argument("--nrhs", type=int, default=32)
@@ -54,13 +56,69 @@ def dist_env():
     return g.load_package().replicas.env()
 
 
-def make_problem(pkg, n, holes, nrhs):
-    g = pkg.geometry
-    prob = g.disc_with_ellipses(n, holes, seed=1)
-    rng = np.random.default_rng(2)
-    src = g.random_sources(nrhs, rng)
-    rhs = g.laplace_source_rhs(prob, src)
-    return prob, src, rhs
+WORKLOAD_NOTES = {
+    "laplace2d_disc_ellipses": "2D Laplace Dirichlet double layer, disc radius 2 minus ellipses "
+                               "(semi-axes U(0.02,0.06), seed 1), 16-node GL panels, unit point "
+                               "sources at |y| in [2.5,4] (seed 2)",
+    "stokes2d_disc_circles": "2D Stokes Dirichlet completed double layer, unit disc minus circles "
+                             "(radii U(0.005,0.02), gap 0.005, seed 3), 16-node GL panels, "
+                             "Stokeslet at (2.5,0) force (1,0.5) plus seeded Stokeslets",
+    "laplace2d_star": "2D Laplace star r=1+0.3cos(5t), 16-node GL panels, source (3,3)",
+}
+
+
+class Workload:
+    """Boundary, right-hand sides and the analytic interior field of one
+    benchmark workload (seeded synthetic data)."""
+
+    def __init__(self, pkg, name, n, holes, nrhs):
+        g = pkg.geometry
+        self.name = name
+        self.sol_dim, self.pde = 1, pkg.PDE_LAPLACE
+        if name == "stokes2d_disc_circles":
+            self.sol_dim, self.pde = 2, pkg.PDE_STOKES
+            self.prob = g.disc_with_circles(n // 2, holes, seed=3)
+            self.src, self.frc = g.stokes_c3_sources(nrhs)
+            self.rhs = g.stokes_rhs(self.prob, self.src, self.frc)
+            self.target_radius = 0.9
+        elif name == "laplace2d_star":
+            self.prob = g.star(n // 16, 16)
+            rng = np.random.default_rng(2)
+            self.src = np.concatenate([[[3.0, 3.0]], g.random_sources(nrhs - 1, rng)])[:nrhs]
+            self.rhs = g.laplace_source_rhs(self.prob, self.src)
+            self.target_radius = 0.5
+        else:
+            self.prob = g.disc_with_ellipses(n, holes, seed=1)
+            rng = np.random.default_rng(2)
+            self.src = g.random_sources(nrhs, rng)
+            self.rhs = g.laplace_source_rhs(self.prob, self.src)
+            self.target_radius = 1.9
+        self.n = self.prob.n * self.sol_dim
+
+    def factor_kw(self, tol, precision):
+        p = self.prob
+        kw = dict(id_tol=tol, solution_dimension=self.sol_dim, pde=self.pde, precision=precision)
+        if p.n_holes:
+            kw.update(hole_centers=p.hole_centers, hole_start=p.hole_start, hole_count=p.hole_count)
+        return kw
+
+    def field(self, pkg, targets):
+        g = pkg.geometry
+        if self.sol_dim == 2:
+            return np.stack([g.stokeslet_velocity(targets, y, f).reshape(-1)
+                             for y, f in zip(self.src, self.frc)], 1)
+        return g.laplace_source_field(targets, self.src)
+
+    def targets(self, pkg, count, rng):
+        g = pkg.geometry
+        if self.prob.n_holes:
+            return g.domain_targets(self.prob, count, rng, radius=self.target_radius)
+        return g.disc_targets(count, rng, self.target_radius)
+
+
+def make_problem(pkg, n, holes, nrhs, name="laplace2d_disc_ellipses"):
+    w = Workload(pkg, name, n, holes, nrhs)
+    return w.prob, w.src, w.rhs
 
 
 class ClockSampler:
@@ -132,10 +190,10 @@ def residual_sample(fac, prob, rhs, mu, alpha, nrows, seed=9):
     return float(est.max()), float(np.median(est))
 
 
-def cpu_oracle_run(prob, rhs, tol, threads):
+def cpu_oracle_run(prob, rhs, tol, threads, sol_dim=1, pde=0):
     import oracle
     t0 = time.perf_counter()
-    mu, alpha, st = oracle.solve(prob, rhs, tol, threads=threads)
+    mu, alpha, st = oracle.solve(prob, rhs, tol, threads=threads, solution_dim=sol_dim, pde=pde)
     t1 = time.perf_counter()
     return t1 - t0, st, mu, alpha
 
@@ -150,12 +208,13 @@ def run_reference(args, rank, world):
     oracle.build_port()
     threads = os.cpu_count() or 1
     n = min(args.n, args.cpu_sample_n)
-    prob, src, rhs = make_problem(pkg, n, args.holes, args.nrhs)
+    wl = Workload(pkg, args.workload, n, args.holes, args.nrhs)
+    n = wl.n
     for _ in range(max(0, min(args.warmup, 1))):
-        cpu_oracle_run(prob, rhs, args.tol, threads)
+        cpu_oracle_run(wl.prob, wl.rhs, args.tol, threads, wl.sol_dim, wl.pde)
     times = []
     for _ in range(args.steps):
-        dt, st, _, _ = cpu_oracle_run(prob, rhs, args.tol, threads)
+        dt, st, _, _ = cpu_oracle_run(wl.prob, wl.rhs, args.tol, threads, wl.sol_dim, wl.pde)
         times.append(dt)
     t = float(np.mean(times))
     value = n * args.nrhs / t
@@ -165,7 +224,7 @@ def run_reference(args, rank, world):
         "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": "laplace2d_disc_minus_%d_ellipses" % args.holes,
+        "config": {"workload": args.workload, "holes": args.holes,
                    "unknowns": n, "nrhs": args.nrhs, "id_tol": args.tol,
                    "full_workload_unknowns": args.n},
         "cpu_baseline": {"value": value, "unit": "DOF/s", "cores": threads, "kind": "port",
@@ -191,16 +250,16 @@ def main():
     import __graft_entry__ as g
     pkg = g.load_package()
     prec = pkg.PRECISION_FP64 if args.precision == "fp64" else pkg.PRECISION_FP32
-    prob, src, rhs = make_problem(pkg, args.n, args.holes, args.nrhs)
-    N = prob.n
+    wl = Workload(pkg, args.workload, args.n, args.holes, args.nrhs)
+    prob, src, rhs = wl.prob, wl.src, wl.rhs
+    N = wl.n
     nrhs = args.nrhs
-    kw = dict(id_tol=args.tol, hole_centers=prob.hole_centers, hole_start=prob.hole_start,
-              hole_count=prob.hole_count, precision=prec)
+    kw = wl.factor_kw(args.tol, prec)
     # inputs resident in HBM for the `value` leg
     rhs_f = np.asfortranarray(rhs)
     d_b = torch.from_numpy(rhs_f.T.copy()).to("cuda")          # (nrhs, N): column c at row c
     d_x = torch.empty_like(d_b)
-    nb = prob.n_holes
+    nb = prob.n_holes * (1 if wl.sol_dim == 1 else 3)
     d_a = torch.empty((nrhs, max(1, nb)), dtype=torch.float64, device="cuda")
     pin_b = torch.from_numpy(rhs_f.T.copy()).pin_memory()
     pin_x = torch.empty_like(pin_b).pin_memory()
@@ -263,9 +322,9 @@ def main():
     solve_prof = fac.profile()["solve"]
     rmax, rmed = residual_sample(fac, prob, rhs, mu, alpha, args.residual_rows)
     rng = np.random.default_rng(4)
-    tg = pkg.geometry.domain_targets(prob, 64, rng)
+    tg = wl.targets(pkg, 64, rng)
     u = fac.eval_targets(tg, mu, alpha)
-    ue = pkg.geometry.laplace_source_field(tg, src)
+    ue = wl.field(pkg, tg)
     pde_err = float(np.abs(u - ue).max() / np.abs(ue).max())
     fac.close()
 
@@ -313,9 +372,10 @@ def main():
     if not args.no_cpu_baseline:
         try:
             n_cpu = min(args.n, args.cpu_sample_n)
-            p2, _, r2 = make_problem(pkg, n_cpu, args.holes, nrhs)
+            w2 = Workload(pkg, args.workload, n_cpu, args.holes, nrhs)
+            n_cpu = w2.n
             thr = os.cpu_count() or 1
-            dt, st, _, _ = cpu_oracle_run(p2, r2, args.tol, thr)
+            dt, st, _, _ = cpu_oracle_run(w2.prob, w2.rhs, args.tol, thr, w2.sol_dim, w2.pde)
             cpu = {"value": n_cpu * nrhs / dt, "unit": "DOF/s", "cores": thr, "kind": "port",
                    "sample": "%d unknowns of the same geometry family, %d rhs, one factor+solve (%.1f s)"
                              % (n_cpu, nrhs, dt)}
@@ -333,7 +393,8 @@ def main():
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32 factor, f64 residual check",
         "data": "synthetic (seeded boundary and sources)",
-        "config": {"workload": "laplace2d_disc_minus_%d_ellipses" % args.holes, "unknowns": N,
+        "config": {"workload": args.workload, "holes": args.holes, "unknowns": N,
+                   "description": WORKLOAD_NOTES[args.workload],
                    "nrhs": nrhs, "id_tol": args.tol, "precision": args.precision,
                    "leaf": 64, "proxy": 128, "l2": "factor working set >> 129 MB L2 (no flush needed)",
                    "levels": info["n_levels"], "root_skeleton": info["n_root"],

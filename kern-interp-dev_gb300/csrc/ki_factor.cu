@@ -937,7 +937,14 @@ __global__ void __launch_bounds__(kThreads) k_schur(const SchurTask<T>* tasks, i
 template <typename T>
 __global__ void __launch_bounds__(256) k_gemm(int m, int n, int kk, T alpha, const T* A, int lda,
                                               int ta, const T* B, int ldb, int tb, T beta, T* C,
-                                              int ldc) {
+                                              int ldc, int kchunk, int64_t sA, int64_t sB,
+                                              int64_t sC) {
+  // split-K: slice z multiplies the k-range [z*kchunk, ...) into its own C
+  const int z = blockIdx.z;
+  A += z * sA;
+  B += z * sB;
+  C += z * sC;
+  kk = min(kchunk, kk - z * kchunk);
   __shared__ T As[16][64 + 1];
   __shared__ T Bs[16][64 + 1];
   const int r0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
@@ -991,7 +998,8 @@ void gemm(cudaStream_t s, int m, int n, int kk, T alpha, const T* A, int lda, bo
           int ldb, bool tb, T beta, T* C, int ldc) {
   if (m <= 0 || n <= 0) return;
   dim3 g((m + 63) / 64, (n + 63) / 64);
-  k_gemm<T><<<g, 256, 0, s>>>(m, n, kk, alpha, A, lda, ta, B, ldb, tb, beta, C, ldc);
+  k_gemm<T><<<g, 256, 0, s>>>(m, n, kk, alpha, A, lda, ta, B, ldb, tb, beta, C, ldc,
+                              std::max(kk, 1), 0, 0, 0);
 }
 
 // dst (rows x cols, ldd) = src block or its transpose (src rows/cols swapped)
@@ -1387,6 +1395,35 @@ void reduce_rows(Factorization<T>& F, const T* A, int na, const T* B, int nc, T*
   if (sm > 48 * 1024)
     KI_CUDA(cudaFuncSetAttribute(k_reduce_partial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   k_reduce_partial<T><<<parts, 256, sm, s>>>(A, na, B, nc, F.N, F.d_is_skel, partial);
+  k_reduce_final<T><<<std::max(1, (na * nc + 255) / 256), 256, 0, s>>>(partial, parts, na * nc, out);
+  KI_CUDA(cudaGetLastError());
+  KI_CUDA(cudaFreeAsync(partial, s));
+}
+
+// Rows of a DOF-major N x nc array whose flag is set are zeroed.
+template <typename T>
+__global__ void k_zero_rows(T* X, int nc, const unsigned char* mask, int N) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)N * nc;
+       e += (size_t)gridDim.x * blockDim.x)
+    if (mask[e / nc]) X[e] = T(0);
+}
+
+// out (na x nc) = sum over non-skeleton rows of A(i,:)^T B(i,:) for wide
+// borders: B's skeleton rows are zeroed in place (B is always a temporary),
+// then a split-K GEMM over row chunks and a fixed-order sum of the slices.
+template <typename T>
+void reduce_rows_wide(Factorization<T>& F, const T* A, int na, T* B, int nc, T* out,
+                      cudaStream_t s) {
+  const int N = F.N;
+  k_zero_rows<T><<<std::min(8192, (int)(((size_t)N * nc + 255) / 256)), 256, 0, s>>>(B, nc, F.d_is_skel, N);
+  const int chunk = 16384;
+  const int parts = (N + chunk - 1) / chunk;
+  T* partial = nullptr;
+  KI_CUDA(cudaMallocAsync((void**)&partial, sizeof(T) * (size_t)parts * na * nc + 16, s));
+  // DOF-major A is the column-major na x N matrix Ac; out = Ac * Bc^T
+  dim3 g((na + 63) / 64, (nc + 63) / 64, parts);
+  k_gemm<T><<<g, 256, 0, s>>>(na, nc, N, T(1), A, na, 0, B, nc, 1, T(0), partial, na, chunk,
+                              (int64_t)chunk * na, (int64_t)chunk * nc, (int64_t)na * nc);
   k_reduce_final<T><<<std::max(1, (na * nc + 255) / 256), 256, 0, s>>>(partial, parts, na * nc, out);
   KI_CUDA(cudaGetLastError());
   KI_CUDA(cudaFreeAsync(partial, s));
@@ -2018,7 +2055,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         F->stage_end();
         T* corr = (T*)F->alloc(Tsz * (size_t)nb * nb);
         F->stage_begin("border_corr", 0, 0);
-        reduce_rows<T>(*F, F->d_PsiTmod, nb, dD, nb, corr, s);
+        if (nb * nb <= 16 * 256) reduce_rows<T>(*F, F->d_PsiTmod, nb, dD, nb, corr, s);
+        else reduce_rows_wide<T>(*F, F->d_PsiTmod, nb, dD, nb, corr, s);
         F->stage_end();
         F->stage_end();
         KI_CUDA(cudaFreeAsync(dD, s));
@@ -2099,7 +2137,8 @@ void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha) {
   for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kDiag, Dw, ncols, s);
   se();
   sb("border_reduce");
-  reduce_rows<T>(F, F.d_PsiTmod, nb, Dw, ncols, t, s);                 // Psi~_r D^-1 w
+  if (nb * ncols <= 16 * 256) reduce_rows<T>(F, F.d_PsiTmod, nb, Dw, ncols, t, s);   // Psi~_r D^-1 w
+  else reduce_rows_wide<T>(F, F.d_PsiTmod, nb, Dw, ncols, t, s);
   se();
   sb("border_root");
   k_mc_rhs<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
@@ -2107,8 +2146,14 @@ void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha) {
   dense_lu_solve<T>(F.d_root_lu, ns, F.d_root_piv, M, ns, ncols, false, s);
   se();
   sb("border_update");
-  k_mc_update<T><<<std::min(8192, (int)(((size_t)N * ncols + 255) / 256)), 256, 0, s>>>(
-      d_x, ncols, F.d_Umod, nb, M, nr, N, F.d_is_skel);                // w - U~_r alpha
+  if (nb <= 64) {
+    k_mc_update<T><<<std::min(8192, (int)(((size_t)N * ncols + 255) / 256)), 256, 0, s>>>(
+        d_x, ncols, F.d_Umod, nb, M, nr, N, F.d_is_skel);              // w - U~_r alpha
+  } else {
+    // x (DOF-major = column-major ncols x N) -= alpha^T U~^T; skeleton rows
+    // are overwritten afterwards, so they need no mask
+    gemm<T>(s, ncols, N, nb, T(-1), M + nr, ns, true, F.d_Umod, nb, false, T(1), d_x, ncols);
+  }
   KI_CUDA(cudaGetLastError());
   se();
   sb("border_diag");

@@ -187,6 +187,103 @@ def disc_with_ellipses(n_unknowns=1 << 20, n_holes=64, radius=2.0, seed=1, q=16)
                    hole_count=np.array(counts, np.int32), name="disc_with_ellipses")
 
 
+def sample_circles(n_holes, rng, r_lo=0.005, r_hi=0.02, domain_radius=1.0, gap=0.005,
+                   max_tries=2000000):
+    """Non-overlapping circles with radii U(r_lo, r_hi), centres rejection-
+    sampled inside the disc, pairwise and boundary gaps at least `gap`."""
+    cs, rs = [], []
+    tries = 0
+    while len(cs) < n_holes:
+        tries += 1
+        if tries > max_tries:
+            raise RuntimeError("could not place %d circles" % n_holes)
+        r = rng.uniform(r_lo, r_hi)
+        c = rng.uniform(-domain_radius, domain_radius, 2)
+        if np.hypot(*c) + r + gap > domain_radius:
+            continue
+        if all(np.hypot(*(c - c2)) >= r + r2 + gap for c2, r2 in zip(cs, rs)):
+            cs.append(c)
+            rs.append(r)
+    return np.array(cs), np.array(rs)
+
+
+def disc_with_circles(n_points=1 << 18, n_holes=200, radius=1.0, seed=3, q=16):
+    """Disc minus `n_holes` circular holes (radii U(0.005, 0.02), gap 0.005),
+    q-node GL panels with equal node density per unit arc length."""
+    rng = np.random.default_rng(seed)
+    cs, rs = sample_circles(n_holes, rng, domain_radius=radius)
+    lens = np.concatenate([[2 * np.pi * radius], 2 * np.pi * rs])
+    total_panels = n_points // q
+    if total_panels * q != n_points:
+        raise ValueError("n_points must be a multiple of q")
+    raw = total_panels * lens / lens.sum()
+    panels = np.maximum(np.floor(raw).astype(int), 2)
+    rem = total_panels - panels.sum()
+    order = np.argsort(-(raw - np.floor(raw)))
+    i = 0
+    while rem != 0:
+        j = order[i % len(order)]
+        if rem > 0:
+            panels[j] += 1
+            rem -= 1
+        elif panels[j] > 2:
+            panels[j] -= 1
+            rem += 1
+        i += 1
+
+    def circ(c, r):
+        def fun(t):
+            e = np.exp(1j * t)
+            return c + r * e, 1j * r * e, -r * e
+        return fun
+    pts, nrm, wts, kap, starts, counts = [], [], [], [], [], []
+    z, n_, w, k = _panel_curve(circ(0j, radius), np.linspace(0, 2 * np.pi, panels[0] + 1), q)
+    pts.append(z); nrm.append(n_); wts.append(w); kap.append(k)
+    off = z.size
+    for h in range(n_holes):
+        z, n_, w, k = _panel_curve(circ(cs[h, 0] + 1j * cs[h, 1], rs[h]),
+                                   np.linspace(0, 2 * np.pi, panels[h + 1] + 1), q)
+        pts.append(z); nrm.append(-n_); wts.append(w); kap.append(-k)
+        starts.append(off); counts.append(z.size)
+        off += z.size
+    z = np.concatenate(pts); n_ = np.concatenate(nrm)
+    prob = Problem(np.stack([z.real, z.imag], 1), np.stack([n_.real, n_.imag], 1),
+                   np.concatenate(wts), np.concatenate(kap), hole_centers=cs.copy(),
+                   hole_start=np.array(starts, np.int32), hole_count=np.array(counts, np.int32),
+                   name="disc_with_circles")
+    prob.hole_radii = rs
+    return prob
+
+
+def stokeslet_velocity(x, y0, force):
+    """Velocity at points x of a 2D Stokeslet at y0 with force f (unit
+    viscosity): (1/4pi) (-log|r| f + (r.f) r / |r|^2), r = x - y0 -- the
+    kernel the reference's border matrix uses (kern_interp/linear_solve.cpp:77-97)."""
+    r = x - np.asarray(y0)[None]
+    r2 = (r ** 2).sum(1)
+    f = np.asarray(force, np.float64)
+    return (-0.5 * np.log(r2)[:, None] * f[None] + r * (r @ f)[:, None] / r2[:, None]) / (4 * np.pi)
+
+
+def stokes_rhs(prob, sources, forces):
+    """Boundary velocity (interleaved per node, one column per Stokeslet)."""
+    cols = [stokeslet_velocity(prob.points, y, f).reshape(-1) for y, f in zip(sources, forces)]
+    return np.stack(cols, 1)
+
+
+def stokes_c3_sources(nrhs, seed=3):
+    """The Stokeslet at (2.5, 0) with force (1, 0.5), then nrhs-1 seeded random
+    ones at |y| in [2.5, 4] with unit forces."""
+    rng = np.random.default_rng(seed + 1000)
+    src = [np.array([2.5, 0.0])]
+    frc = [np.array([1.0, 0.5])]
+    for _ in range(nrhs - 1):
+        src.append(random_sources(1, rng)[0])
+        a = rng.uniform(0, 2 * np.pi)
+        frc.append(np.array([np.cos(a), np.sin(a)]))
+    return np.array(src), np.array(frc)
+
+
 def laplace_source_rhs(prob, sources):
     """Boundary values of u(x) = log|x - y| / (2 pi) for each source y (one
     column per source), the field the reference's SINGLE_ELECTRON condition
@@ -216,13 +313,16 @@ def disc_targets(n, rng, radius=0.5):
 
 
 def domain_targets(prob, n, rng, radius=1.9, margin=0.02):
-    """n points inside the outer disc and outside every hole's bounding circle."""
+    """n points inside the disc of the given radius and outside every hole's
+    bounding circle (its radius when known, else the largest ellipse axis)."""
+    radii = getattr(prob, "hole_radii", None)
     out = []
     while len(out) < n:
         p = disc_targets(1, rng, radius)[0]
         ok = True
-        for c in prob.hole_centers:
-            if np.hypot(*(p - c)) < 0.06 + margin:
+        for h, c in enumerate(prob.hole_centers):
+            rh = radii[h] if radii is not None else 0.06
+            if np.hypot(*(p - c)) < rh + margin:
                 ok = False
                 break
         if ok:
