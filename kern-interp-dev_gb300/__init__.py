@@ -106,9 +106,15 @@ class Factor:
 
     def __init__(self, points, normals, weights, curvatures=None, id_tol=1e-10,
                  solution_dimension=1, pde=PDE_LAPLACE, hole_centers=None, hole_start=None,
-                 hole_count=None, max_leaf_dofs=64, num_proxy_points=128, radius_ratio=2.0,
-                 min_dofs_to_compress=64, precision=PRECISION_FP64):
+                 hole_count=None, max_leaf_dofs=64, num_proxy_points=0, radius_ratio=2.0,
+                 min_dofs_to_compress=64, precision=PRECISION_FP64, domain_dimension=None):
+        """points/normals: (n, dim) arrays, dim 2 or 3 (inferred unless given).
+        num_proxy_points 0 takes the reference default (128 on a circle in 2D,
+        the 8 x 4 theta x phi sphere = 32 in 3D)."""
         lib = load_library()
+        dim = int(domain_dimension or np.asarray(points).shape[-1])
+        if dim not in (2, 3):
+            raise ValueError("points must be (n, 2) or (n, 3)")
         self._keep = [np.ascontiguousarray(points, np.float64).reshape(-1),
                       np.ascontiguousarray(normals, np.float64).reshape(-1),
                       np.ascontiguousarray(weights, np.float64).reshape(-1)]
@@ -120,7 +126,7 @@ class Factor:
         hn = np.ascontiguousarray(hole_count, np.int32) if nh else None
         self._keep += [hc, hs, hn]
         n = self._keep[2].shape[0]
-        d = _Desc(n, 2, solution_dimension, pde, _ptr(self._keep[0]), _ptr(self._keep[1]),
+        d = _Desc(n, dim, solution_dimension, pde, _ptr(self._keep[0]), _ptr(self._keep[1]),
                   _ptr(self._keep[2]), _ptr(self._keep[3]), nh, _ptr(hc), _ptr(hs), _ptr(hn),
                   max_leaf_dofs, num_proxy_points, radius_ratio, min_dofs_to_compress,
                   id_tol, precision)
@@ -130,7 +136,8 @@ class Factor:
         self.n_dofs = n * solution_dimension
         self.n_points = n
         self.solution_dimension = solution_dimension
-        self.n_border = nh * (1 if solution_dimension == 1 else 3)
+        self.domain_dimension = dim
+        self.n_border = nh * (1 if solution_dimension == 1 else (3 if dim == 2 else 6))
 
     def close(self):
         if getattr(self, "_h", None):
@@ -209,7 +216,7 @@ class Factor:
         return Y
 
     def eval_targets(self, targets, mu, alpha=None):
-        targets = np.ascontiguousarray(targets, np.float64).reshape(-1, 2)
+        targets = np.ascontiguousarray(targets, np.float64).reshape(-1, self.domain_dimension)
         mu = np.asarray(mu, np.float64)
         vec = mu.ndim == 1
         M = np.asfortranarray(mu.reshape(self.n_dofs, -1))
@@ -235,7 +242,7 @@ def measure_fma_peak():
 
 class Boundary:
     """Boundary data (kern_interp/boundaries/boundary.h:47-64).  points and
-    normals are interleaved (x, y) per node; holes is a list of
+    normals are interleaved (x, y[, z]) per node; holes is a list of
     (center, node_start, node_count)."""
 
     def __init__(self, points, normals, weights, curvatures=None, holes=(), boundary_values=None):
@@ -279,8 +286,8 @@ class QuadTree:
         self.factor = None
 
     def initialize_tree(self, boundary, solution_dimension, domain_dimension):
-        if domain_dimension != 2:
-            raise KiError(KI_ERR_ARG, "only domain_dimension 2 is supported")
+        if domain_dimension not in (2, 3):
+            raise KiError(KI_ERR_ARG, "domain_dimension must be 2 or 3")
         self.boundary = boundary
         self.solution_dimension = solution_dimension
         self.domain_dimension = domain_dimension
@@ -291,7 +298,7 @@ class SkelFactorization:
     fact_threads is accepted for signature parity and ignored (the GPU
     processes every box of a level in one launch)."""
 
-    def __init__(self, id_tol, fact_threads=1, num_proxy_points=128, radius_ratio=2.0,
+    def __init__(self, id_tol, fact_threads=1, num_proxy_points=0, radius_ratio=2.0,
                  min_dofs_to_compress=64, precision=PRECISION_FP64):
         self.id_tol = id_tol
         self.fact_threads = fact_threads
@@ -308,10 +315,12 @@ class SkelFactorization:
         hn = np.array([h[2] for h in holes], np.int32) if holes else None
         if quadtree.factor is not None:
             quadtree.factor.close()
-        quadtree.factor = Factor(b.points, b.normals, b.weights, b.curvatures, self.id_tol,
-                                 kernel.solution_dimension, kernel.pde, hc, hs, hn,
-                                 quadtree.max_leaf_dofs, self.num_proxy_points, self.radius_ratio,
-                                 self.min_dofs_to_compress, self.precision)
+        dim = quadtree.domain_dimension
+        quadtree.factor = Factor(b.points.reshape(-1, dim), b.normals.reshape(-1, dim), b.weights,
+                                 b.curvatures, self.id_tol, kernel.solution_dimension, kernel.pde,
+                                 hc, hs, hn, quadtree.max_leaf_dofs, self.num_proxy_points,
+                                 self.radius_ratio, self.min_dofs_to_compress, self.precision,
+                                 domain_dimension=dim)
 
     def solve(self, quadtree, b):
         return quadtree.factor.solve(b)
@@ -334,7 +343,7 @@ def boundary_integral_solve(kernel, boundary, quadtree, id_tol, fact_threads, do
     quadtree.initialize_tree(boundary, kernel.solution_dimension, kernel.domain_dimension)
     skel.skeletonize(kernel, quadtree)
     res = linear_solve(skel, quadtree, boundary.boundary_values)
-    targets = np.asarray(domain_points, np.float64).reshape(-1, 2)
+    targets = np.asarray(domain_points, np.float64).reshape(-1, kernel.domain_dimension)
     if isinstance(res, tuple):
         mu, alpha = res
         return quadtree.factor.eval_targets(targets, mu, alpha)

@@ -99,19 +99,42 @@ constexpr int kApplyThreads = 128;
 constexpr int kApplyTile = 128;
 constexpr int kApplyCols = 8;
 
+// Kernel entry between a target (point data t*, DOF parity tpar) and a source
+// point (s*, parity spar), 2D or 3D (Kernel::operator() / get_3d,
+// kern_interp/kernel/kernel.cpp:304-429).  diag: the source point's 3D
+// diagonal data (used only when the two points coincide).
+__device__ __forceinline__ double pair_entry(int dim, int sol_dim, int tpar, int spar, double tx,
+                                             double ty, double tz, double tnx, double tny,
+                                             double tnz, double sx, double sy, double sz,
+                                             double snx, double sny, double snz, double sw,
+                                             double sk, const double* diag) {
+  if (dim == 3) {
+    if (sol_dim == 1)
+      return ki::laplace3_entry<double>(tx - sx, ty - sy, tz - sz, snx, sny, snz, sw,
+                                        diag ? diag[0] : 0.0);
+    return ki::stokes3_entry<double>(tpar, spar, tx - sx, ty - sy, tz - sz, tnx, tny, tnz, snx,
+                                     sny, snz, sw, diag);
+  }
+  if (sol_dim == 1) return ki::laplace_entry<double>(tx, ty, sx, sy, snx, sny, sw, sk);
+  return ki::stokes_entry<double>(tpar, spar, tx, ty, tnx, tny, sx, sy, snx, sny, sw, sk);
+}
+
 __global__ void k_dense_apply(ki::Points<double> P, int n_points, int sol_dim, const double* x,
                               int ldx, int ncols, double* y, int ldy, const int* rows, int nrows) {
-  __shared__ double sx[kApplyTile], sy[kApplyTile], snx[kApplyTile], sny[kApplyTile],
-      sw[kApplyTile], sk[kApplyTile];
+  __shared__ double sx[kApplyTile], sy[kApplyTile], sz[kApplyTile], snx[kApplyTile],
+      sny[kApplyTile], snz[kApplyTile], sw[kApplyTile], sk[kApplyTile];
+  const int dim = P.dim;
+  const int dpp = dim == 3 ? (sol_dim == 1 ? 1 : 9) : 0;
   const int N = rows ? nrows : n_points * sol_dim;
   const int trow = blockIdx.x * blockDim.x + threadIdx.x;
-  const int tdof = rows ? (trow < nrows ? rows[trow] : 0) : trow;
+  const int tdof = rows ? (trow < nrows ? rows[trow] : 0) : (trow < N ? trow : 0);
   const int c0 = blockIdx.y * kApplyCols;
   const int nc = min(kApplyCols, ncols - c0);
   double acc[kApplyCols];
   for (int c = 0; c < kApplyCols; c++) acc[c] = 0.0;
-  int tp = trow < N ? tdof / sol_dim : 0;
-  double tx = P.x[tp], ty = P.y[tp], tnx = P.nx[tp], tny = P.ny[tp];
+  const int tp = tdof / sol_dim, tpar = tdof - sol_dim * tp;
+  const double tx = P.x[tp], ty = P.y[tp], tnx = P.nx[tp], tny = P.ny[tp];
+  const double tz = dim == 3 ? P.z[tp] : 0.0, tnz = dim == 3 ? P.nz[tp] : 0.0;
   for (int base = 0; base < n_points; base += kApplyTile) {
     __syncthreads();
     for (int i = threadIdx.x; i < kApplyTile; i += blockDim.x) {
@@ -119,20 +142,19 @@ __global__ void k_dense_apply(ki::Points<double> P, int n_points, int sol_dim, c
       if (p < n_points) {
         sx[i] = P.x[p]; sy[i] = P.y[p]; snx[i] = P.nx[p]; sny[i] = P.ny[p]; sw[i] = P.w[p];
         sk[i] = P.kappa[p];
+        sz[i] = dim == 3 ? P.z[p] : 0.0;
+        snz[i] = dim == 3 ? P.nz[p] : 0.0;
       }
     }
     __syncthreads();
     if (trow >= N) continue;
     int lim = min(kApplyTile, n_points - base);
     for (int i = 0; i < lim; i++) {
+      const double* dg = dpp ? P.diag + (size_t)dpp * (base + i) : nullptr;
       for (int sp = 0; sp < sol_dim; sp++) {
         int sdof = (base + i) * sol_dim + sp;
-        double kv;
-        if (sol_dim == 1)
-          kv = ki::laplace_entry<double>(tx, ty, sx[i], sy[i], snx[i], sny[i], sw[i], sk[i]);
-        else
-          kv = ki::stokes_entry<double>(tdof & 1, sp, tx, ty, tnx, tny, sx[i], sy[i], snx[i],
-                                        sny[i], sw[i], sk[i]);
+        double kv = pair_entry(dim, sol_dim, tpar, sp, tx, ty, tz, tnx, tny, tnz, sx[i], sy[i],
+                               sz[i], snx[i], sny[i], snz[i], sw[i], sk[i], dg);
         for (int c = 0; c < nc; c++) acc[c] += kv * x[sdof + (size_t)ldx * (c0 + c)];
       }
     }
@@ -141,25 +163,26 @@ __global__ void k_dense_apply(ki::Points<double> P, int n_points, int sol_dim, c
     for (int c = 0; c < nc; c++) y[trow + (size_t)ldy * (c0 + c)] = acc[c];
 }
 
-// Forward evaluation at domain targets (target normal 0, reference forward
-// mode), plus the border term.
+// Forward evaluation at domain targets (target normal 0, the reference's
+// forward mode, kernel.cpp:335-339 / :390-400).  Targets: dim per point.
 __global__ void k_forward(ki::Points<double> P, int n_points, int sol_dim, const double* tg,
                           int nt, const double* mu, int ldmu, int ncols, double* out, int ldout) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int NT = nt * sol_dim;
   if (t >= NT) return;
-  int tp = t / sol_dim;
-  double tx = tg[2 * tp], ty = tg[2 * tp + 1];
+  const int dim = P.dim;
+  const int dpp = dim == 3 ? (sol_dim == 1 ? 1 : 9) : 0;
+  const int tp = t / sol_dim, tpar = t - sol_dim * tp;
+  const double tx = tg[(size_t)dim * tp], ty = tg[(size_t)dim * tp + 1];
+  const double tz = dim == 3 ? tg[3 * (size_t)tp + 2] : 0.0;
   for (int c = 0; c < ncols; c++) {
     double acc = 0.0;
     for (int p = 0; p < n_points; p++) {
+      const double* dg = dpp ? P.diag + (size_t)dpp * p : nullptr;
       for (int sp = 0; sp < sol_dim; sp++) {
-        double kv;
-        if (sol_dim == 1)
-          kv = ki::laplace_entry<double>(tx, ty, P.x[p], P.y[p], P.nx[p], P.ny[p], P.w[p], P.kappa[p]);
-        else
-          kv = ki::stokes_entry<double>(t & 1, sp, tx, ty, 0.0, 0.0, P.x[p], P.y[p], P.nx[p],
-                                        P.ny[p], P.w[p], P.kappa[p]);
+        double kv = pair_entry(dim, sol_dim, tpar, sp, tx, ty, tz, 0.0, 0.0, 0.0, P.x[p], P.y[p],
+                               dim == 3 ? P.z[p] : 0.0, P.nx[p], P.ny[p],
+                               dim == 3 ? P.nz[p] : 0.0, P.w[p], P.kappa[p], dg);
         acc += kv * mu[p * sol_dim + sp + (size_t)ldmu * c];
       }
     }
@@ -167,58 +190,54 @@ __global__ void k_forward(ki::Points<double> P, int n_points, int sol_dim, const
   }
 }
 
-// U alpha for Laplace holes (initialize_U_mat, linear_solve.cpp:37-45:
-// U(i, h) = log|x_i - c_h|) and Stokes 2D (:77-97).
-__global__ void k_border_apply(const double* px, const double* py, int stride, int n_points, int sol_dim,
-                               const double* hc, int nh, const double* alpha, int lda, int ncols,
-                               double* y, int ldy, const int* rows = nullptr, int nrows = 0) {
-  if (rows) {
-    // row subset: one thread per listed DOF
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nrows) return;
-    const int dof = rows[q], p = dof / sol_dim, comp = dof % sol_dim;
-    for (int c = 0; c < ncols; c++) {
-      double acc = 0;
-      for (int h = 0; h < nh; h++) {
-        double rx = px[(size_t)stride * p] - hc[2 * h], ry = py[(size_t)stride * p] - hc[2 * h + 1];
-        double rn = sqrt(rx * rx + ry * ry);
-        if (sol_dim == 1) {
-          acc += log(rn) * alpha[h + (size_t)lda * c];
-        } else {
-          double sc = 1.0 / (4 * ki::kPi), r2 = rn * rn;
-          const double* al = alpha + 3 * h + (size_t)lda * c;
-          if (comp == 0)
-            acc += sc * (log(1 / rn) + rx * rx / r2) * al[0] + sc * (rx * ry / r2) * al[1] + ry * (sc / r2) * al[2];
-          else
-            acc += sc * (ry * rx / r2) * al[0] + sc * (log(1 / rn) + ry * ry / r2) * al[1] - rx * (sc / r2) * al[2];
-        }
-      }
-      y[q + (size_t)ldy * c] += acc;
-    }
-    return;
+// Entry (component comp, border column k of one hole) of the border matrix U
+// (initialize_U_mat, kern_interp/linear_solve.cpp:19-107); r = x - hole centre.
+__device__ double border_u(int dim, int sol_dim, int comp, int k, const double* r) {
+  double r2 = 0;
+  for (int d = 0; d < dim; d++) r2 += r[d] * r[d];
+  const double rn = sqrt(r2);
+  if (sol_dim == 1) return dim == 2 ? log(rn) : 1.0 / rn;
+  if (dim == 2) {
+    const double sc = 1.0 / (4 * ki::kPi), q = rn * rn;
+    const double rx = r[0], ry = r[1];
+    if (k == 0) return comp == 0 ? sc * (log(1 / rn) + rx * rx / q) : sc * (ry * rx / q);
+    if (k == 1) return comp == 0 ? sc * (rx * ry / q) : sc * (log(1 / rn) + ry * ry / q);
+    return comp == 0 ? ry * (sc / q) : -rx * (sc / q);
   }
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_points) return;
+  const double rn3 = rn * rn * rn;
+  if (k < 3) return (1.0 / (8.0 * ki::kPi)) * ((comp == k ? 1.0 : 0.0) / rn + r[comp] * r[k] / rn3);
+  const double rot = -1.0 / (8.0 * ki::kPi * rn3);
+  const int b = k - 3;
+  if (comp == b) return 0.0;
+  // [r]_x entries: (0,1) -r2, (0,2) r1, (1,0) r2, (1,2) -r0, (2,0) -r1, (2,1) r0
+  const int o = 3 - comp - b;   // the remaining axis
+  const double sgn = ((comp + 1) % 3 == b) ? -1.0 : 1.0;
+  return rot * sgn * r[o];
+}
+
+// y += U alpha, one thread per listed DOF (rows != nullptr: DOF rows[q] of
+// the points; else DOF q).  Points: dim per point with the given stride
+// between points (SoA x with stride 1 and separate y/z, or interleaved).
+__global__ void k_border_apply(const double* px, const double* py, const double* pz, int stride,
+                               int n_points, int dim, int sol_dim, const double* hc, int nh,
+                               const double* alpha, int lda, int ncols, double* y, int ldy,
+                               const int* rows = nullptr, int nrows = 0) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nq = rows ? nrows : n_points * sol_dim;
+  if (q >= nq) return;
+  const int dof = rows ? rows[q] : q, p = dof / sol_dim, comp = dof - sol_dim * p;
+  const int cph = sol_dim == 1 ? 1 : (dim == 2 ? 3 : 6);
+  const double xp[3] = {px[(size_t)stride * p], py[(size_t)stride * p],
+                        dim == 3 ? pz[(size_t)stride * p] : 0.0};
   for (int c = 0; c < ncols; c++) {
-    double a0 = 0, a1 = 0;
+    double acc = 0;
     for (int h = 0; h < nh; h++) {
-      double rx = px[(size_t)stride * i] - hc[2 * h], ry = py[(size_t)stride * i] - hc[2 * h + 1];
-      double rn = sqrt(rx * rx + ry * ry);
-      if (sol_dim == 1) {
-        a0 += log(rn) * alpha[h + (size_t)lda * c];
-      } else {
-        double sc = 1.0 / (4 * ki::kPi), r2 = rn * rn;
-        const double* al = alpha + 3 * h + (size_t)lda * c;
-        a0 += sc * (log(1 / rn) + rx * rx / r2) * al[0] + sc * (rx * ry / r2) * al[1] + ry * (sc / r2) * al[2];
-        a1 += sc * (ry * rx / r2) * al[0] + sc * (log(1 / rn) + ry * ry / r2) * al[1] - rx * (sc / r2) * al[2];
-      }
+      double r[3];
+      for (int d = 0; d < dim; d++) r[d] = xp[d] - hc[dim * h + d];
+      const double* al = alpha + cph * h + (size_t)lda * c;
+      for (int k = 0; k < cph; k++) acc += border_u(dim, sol_dim, comp, k, r) * al[k];
     }
-    if (sol_dim == 1) {
-      y[i + (size_t)ldy * c] += a0;
-    } else {
-      y[2 * i + (size_t)ldy * c] += a0;
-      y[2 * i + 1 + (size_t)ldy * c] += a1;
-    }
+    y[q + (size_t)ldy * c] += acc;
   }
 }
 
@@ -246,6 +265,7 @@ int grid_for(size_t n) { return (int)std::min<size_t>(4096, (n + 255) / 256 + 1)
 
 struct ki_factor {
   int precision = KI_PRECISION_FP64;
+  int dim = 2;
   int sol_dim = 1;
   int n_points = 0;
   int n_dofs = 0;
@@ -297,13 +317,16 @@ void solve_impl(ki_factor* f, ki::Factorization<T>& F, const double* d_b, int ld
 
 void check_desc(const ki_problem_desc* d) {
   if (!d) throw ArgError("desc is NULL");
-  if (d->domain_dimension != 2) throw ArgError("only domain_dimension 2 is supported");
+  if (d->domain_dimension != 2 && d->domain_dimension != 3)
+    throw ArgError("domain_dimension must be 2 or 3");
+  const int dim = d->domain_dimension;
   if (d->n_points <= 0) throw ArgError("n_points must be positive");
   if (!d->points || !d->normals || !d->weights) throw ArgError("points/normals/weights must be non-NULL");
   if (d->pde == KI_PDE_LAPLACE) {
     if (d->solution_dimension != 1) throw ArgError("Laplace needs solution_dimension 1");
   } else if (d->pde == KI_PDE_STOKES) {
-    if (d->solution_dimension != 2) throw ArgError("Stokes (2D) needs solution_dimension 2");
+    if (d->solution_dimension != dim)
+      throw ArgError("Stokes needs solution_dimension equal to domain_dimension");
   } else {
     throw ArgError("pde must be KI_PDE_LAPLACE or KI_PDE_STOKES");
   }
@@ -317,7 +340,12 @@ void check_desc(const ki_problem_desc* d) {
     int s = d->hole_node_start[h], c = d->hole_node_count[h];
     if (s < 0 || c <= 0 || s + c > d->n_points) throw ArgError("hole node range out of bounds");
   }
-  for (long i = 0; i < 2L * d->n_points; i++)
+  if (dim == 3 && d->num_proxy_points > 0) {
+    int q = (int)std::lround(std::sqrt(d->num_proxy_points / 2.0));
+    if (q < 1 || 2 * q * q != d->num_proxy_points)
+      throw ArgError("3D num_proxy_points must be 2 q^2 (a theta x phi grid of 2q x q points)");
+  }
+  for (long i = 0; i < (long)dim * d->n_points; i++)
     if (!std::isfinite(d->points[i]) || !std::isfinite(d->normals[i]))
       throw ArgError("non-finite point or normal");
   for (int i = 0; i < d->n_points; i++) {
@@ -447,46 +475,59 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
     }
     std::unique_ptr<ki_factor> f(new ki_factor());
     f->precision = desc->precision;
+    const int dim = desc->domain_dimension;
+    f->dim = dim;
     f->sol_dim = desc->solution_dimension;
     f->n_points = desc->n_points;
     f->n_dofs = desc->n_points * desc->solution_dimension;
     f->n_holes = desc->n_holes;
-    f->n_border = desc->n_holes * (desc->solution_dimension == 1 ? 1 : 3);
+    f->n_border = desc->n_holes * ki::border_cols_per_hole(dim, desc->solution_dimension);
     KI_CHECK_CUDA(cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking));
     ki::Params prm;
+    prm.dim = dim;
     prm.sol_dim = desc->solution_dimension;
     prm.max_leaf_dofs = desc->max_leaf_dofs ? desc->max_leaf_dofs : 64;
-    prm.num_proxy_points = desc->num_proxy_points ? desc->num_proxy_points : 128;
+    // reference defaults: NUM_PROXY_POINTS = 128 (2D); the 3D proxy sphere is
+    // the Kernel constructor's 8 x 4 grid (kern_interp/kernel/kernel.h:44-62)
+    prm.num_proxy_points = desc->num_proxy_points ? desc->num_proxy_points : (dim == 2 ? 128 : 32);
     prm.radius_ratio = desc->radius_ratio > 0 ? desc->radius_ratio : 2.0;
     prm.min_dofs_to_compress = desc->min_dofs_to_compress ? desc->min_dofs_to_compress : 64;
     prm.id_tol = desc->id_tol;
     ki::HoleDesc holes;
     holes.n_holes = desc->n_holes;
     for (int h = 0; h < desc->n_holes; h++) {
-      holes.centers.push_back(desc->hole_centers[2 * h]);
-      holes.centers.push_back(desc->hole_centers[2 * h + 1]);
+      for (int d = 0; d < dim; d++) holes.centers.push_back(desc->hole_centers[dim * h + d]);
       holes.start.push_back(desc->hole_node_start[h]);
       holes.count.push_back(desc->hole_node_count[h]);
     }
     // FP64 geometry for apply / evaluation (SoA)
     const int n = desc->n_points;
-    std::vector<double> geo((size_t)6 * n);
+    std::vector<double> geo((size_t)8 * n, 0.0);
     for (int i = 0; i < n; i++) {
-      geo[i] = desc->points[2 * i];
-      geo[n + i] = desc->points[2 * i + 1];
-      geo[2 * (size_t)n + i] = desc->normals[2 * i];
-      geo[3 * (size_t)n + i] = desc->normals[2 * i + 1];
+      geo[i] = desc->points[(size_t)dim * i];
+      geo[n + i] = desc->points[(size_t)dim * i + 1];
+      geo[2 * (size_t)n + i] = desc->normals[(size_t)dim * i];
+      geo[3 * (size_t)n + i] = desc->normals[(size_t)dim * i + 1];
       geo[4 * (size_t)n + i] = desc->weights[i];
       geo[5 * (size_t)n + i] = desc->curvatures ? desc->curvatures[i] : 0.0;
+      if (dim == 3) {
+        geo[6 * (size_t)n + i] = desc->points[3 * (size_t)i + 2];
+        geo[7 * (size_t)n + i] = desc->normals[3 * (size_t)i + 2];
+      }
     }
     KI_CHECK_CUDA(cudaMalloc(&f->d_geo, sizeof(double) * geo.size()));
     KI_CHECK_CUDA(cudaMemcpy(f->d_geo, geo.data(), sizeof(double) * geo.size(), cudaMemcpyHostToDevice));
     f->P = ki::Points<double>{f->d_geo, f->d_geo + n, f->d_geo + 2 * (size_t)n,
                               f->d_geo + 3 * (size_t)n, f->d_geo + 4 * (size_t)n,
                               f->d_geo + 5 * (size_t)n};
+    f->P.dim = dim;
+    if (dim == 3) {
+      f->P.z = f->d_geo + 6 * (size_t)n;
+      f->P.nz = f->d_geo + 7 * (size_t)n;
+    }
     if (desc->n_holes > 0) {
-      KI_CHECK_CUDA(cudaMalloc(&f->d_holes, sizeof(double) * 2 * desc->n_holes));
-      KI_CHECK_CUDA(cudaMemcpy(f->d_holes, desc->hole_centers, sizeof(double) * 2 * desc->n_holes,
+      KI_CHECK_CUDA(cudaMalloc(&f->d_holes, sizeof(double) * dim * desc->n_holes));
+      KI_CHECK_CUDA(cudaMemcpy(f->d_holes, desc->hole_centers, sizeof(double) * dim * desc->n_holes,
                                cudaMemcpyHostToDevice));
     }
     if (f->precision == KI_PRECISION_FP64)
@@ -495,6 +536,8 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
     else
       f->f32 = ki::factorize<float>(prm, n, desc->points, desc->normals, desc->weights,
                                     desc->curvatures, holes, f->stream);
+    // the FP64 3D diagonal of the factorization serves the FP64 apply
+    f->P.diag = f->f64 ? f->f64->d_diag64 : f->f32->d_diag64;
     *out = f.release();
   });
 }
@@ -597,9 +640,9 @@ int ki_apply(ki_factor* f, const double* x, int ldx, int ncols, const double* al
       KI_CHECK_CUDA(cudaMemcpy2DAsync(da.p, sizeof(double) * f->n_border, alpha,
                                       sizeof(double) * ldalpha, sizeof(double) * f->n_border,
                                       ncols, cudaMemcpyHostToDevice, s));
-      k_border_apply<<<(f->n_points + 127) / 128, 128, 0, s>>>(
-          f->P.x, f->P.y, 1, f->n_points, f->sol_dim, f->d_holes, f->n_holes, da.p, f->n_border,
-          ncols, dy.p, N);
+      k_border_apply<<<(N + 127) / 128, 128, 0, s>>>(
+          f->P.x, f->P.y, f->P.z, 1, f->n_points, f->dim, f->sol_dim, f->d_holes, f->n_holes, da.p,
+          f->n_border, ncols, dy.p, N);
       KI_CHECK_CUDA(cudaGetLastError());
       KI_CHECK_CUDA(cudaMemcpy2DAsync(y, sizeof(double) * ldy, dy.p, sizeof(double) * N,
                                       sizeof(double) * N, ncols, cudaMemcpyDeviceToHost, s));
@@ -637,9 +680,9 @@ int ki_apply_rows(ki_factor* f, const int* rows, int nrows, const double* x, int
       KI_CHECK_CUDA(cudaMemcpy2DAsync(da.p, sizeof(double) * f->n_border, alpha,
                                       sizeof(double) * ldalpha, sizeof(double) * f->n_border,
                                       ncols, cudaMemcpyHostToDevice, s));
-      k_border_apply<<<(nrows + 127) / 128, 128, 0, s>>>(f->P.x, f->P.y, 1, f->n_points, f->sol_dim,
-                                                         f->d_holes, f->n_holes, da.p, f->n_border,
-                                                         ncols, dy.p, nrows, dr.p, nrows);
+      k_border_apply<<<(nrows + 127) / 128, 128, 0, s>>>(
+          f->P.x, f->P.y, f->P.z, 1, f->n_points, f->dim, f->sol_dim, f->d_holes, f->n_holes, da.p,
+          f->n_border, ncols, dy.p, nrows, dr.p, nrows);
       KI_CHECK_CUDA(cudaGetLastError());
       KI_CHECK_CUDA(cudaStreamSynchronize(s));
     }
@@ -658,8 +701,9 @@ int ki_eval_targets(ki_factor* f, const double* targets, int n_targets, const do
     if (n_targets < 0 || ncols < 0 || ldmu < N || ldout < NT) throw ArgError("bad sizes");
     if (n_targets == 0 || ncols == 0) return;
     cudaStream_t s = f->stream;
-    DevBuf<double> dt((size_t)2 * n_targets, s), dm((size_t)N * ncols, s), dout((size_t)NT * ncols, s);
-    KI_CHECK_CUDA(cudaMemcpyAsync(dt.p, targets, sizeof(double) * 2 * n_targets, cudaMemcpyHostToDevice, s));
+    const int dim = f->dim;
+    DevBuf<double> dt((size_t)dim * n_targets, s), dm((size_t)N * ncols, s), dout((size_t)NT * ncols, s);
+    KI_CHECK_CUDA(cudaMemcpyAsync(dt.p, targets, sizeof(double) * dim * n_targets, cudaMemcpyHostToDevice, s));
     KI_CHECK_CUDA(cudaMemcpy2DAsync(dm.p, sizeof(double) * N, mu, sizeof(double) * ldmu,
                                     sizeof(double) * N, ncols, cudaMemcpyHostToDevice, s));
     k_forward<<<(NT + 127) / 128, 128, 0, s>>>(f->P, f->n_points, f->sol_dim, dt.p, n_targets, dm.p,
@@ -671,9 +715,9 @@ int ki_eval_targets(ki_factor* f, const double* targets, int n_targets, const do
       KI_CHECK_CUDA(cudaMemcpy2DAsync(da.p, sizeof(double) * f->n_border, alpha,
                                       sizeof(double) * ldalpha, sizeof(double) * f->n_border,
                                       ncols, cudaMemcpyHostToDevice, s));
-      k_border_apply<<<(n_targets + 127) / 128, 128, 0, s>>>(dt.p, dt.p + 1, 2, n_targets, f->sol_dim,
-                                                             f->d_holes, f->n_holes, da.p,
-                                                             f->n_border, ncols, dout.p, NT);
+      k_border_apply<<<(NT + 127) / 128, 128, 0, s>>>(dt.p, dt.p + 1, dt.p + 2, dim, n_targets, dim,
+                                                      f->sol_dim, f->d_holes, f->n_holes, da.p,
+                                                      f->n_border, ncols, dout.p, NT);
       KI_CHECK_CUDA(cudaGetLastError());
       KI_CHECK_CUDA(cudaStreamSynchronize(s));
     }

@@ -8,6 +8,10 @@
 namespace ki {
 
 // Point data, structure-of-arrays, resident in HBM for the whole factorization.
+// 2D uses x, y, nx, ny, w, kappa; 3D adds z, nz and the precomputed diagonal
+// entries (Kernel::compute_diag_entries_3dlaplace / _3dstokes,
+// kern_interp/kernel/kernel.cpp:124-301): one per point for Laplace, a
+// row-major 3 x 3 tensor per point for Stokes.
 template <typename T>
 struct Points {
   const T* x;
@@ -16,6 +20,10 @@ struct Points {
   const T* ny;
   const T* w;
   const T* kappa;
+  const T* z = nullptr;
+  const T* nz = nullptr;
+  const T* diag = nullptr;
+  int dim = 2;
 };
 
 constexpr double kPi = 3.14159265358979323846;
@@ -50,9 +58,46 @@ __device__ __forceinline__ T stokes_entry(int tpar, int spar, T tx, T ty, T tnx,
          sw * tn[tpar] * sn[spar];
 }
 
-// Entry between two boundary DOFs (sol_dim 1: Laplace, 2: Stokes).
+// 3D Laplace double layer (Kernel::three_d_laplace, kernel.cpp:104-121):
+// -w/(4 pi) (r.n_s)/|r|^3, r = t - s; a coincident pair takes `diag`.
+template <typename T>
+__device__ __forceinline__ T laplace3_entry(T r1, T r2, T r3, T snx, T sny, T snz, T sw, T diag) {
+  if (r1 == T(0) && r2 == T(0) && r3 == T(0)) return diag;
+  T rr = r1 * r1 + r2 * r2 + r3 * r3;
+  return -sw * T(1.0 / (4 * kPi)) * (r1 * snx + r2 * sny + r3 * snz) / (rr * sqrt(rr));
+}
+
+// 3D Stokes completed double layer (Kernel::three_d_stokes, kernel.cpp:89-102):
+// -3/(4 pi) w (r.n_s) r_i r_j / |r|^5 + w n_t,i n_s,j; a coincident pair
+// takes the (i, j) element of the source point's diagonal tensor.
+template <typename T>
+__device__ __forceinline__ T stokes3_entry(int tpar, int spar, T r1, T r2, T r3, T tnx, T tny,
+                                           T tnz, T snx, T sny, T snz, T sw, const T* diag9) {
+  if (r1 == T(0) && r2 == T(0) && r3 == T(0)) return diag9 ? diag9[3 * tpar + spar] : T(0);
+  const T r[3] = {r1, r2, r3};
+  const T tn[3] = {tnx, tny, tnz};
+  const T sn[3] = {snx, sny, snz};
+  T rr = r1 * r1 + r2 * r2 + r3 * r3;
+  return sw * T(-3.0 / (4 * kPi)) * (r1 * snx + r2 * sny + r3 * snz) / (rr * rr * sqrt(rr)) *
+             r[tpar] * r[spar] +
+         sw * tn[tpar] * sn[spar];
+}
+
+// Entry between two boundary DOFs: 2D Laplace (sol_dim 1), 2D Stokes
+// (sol_dim 2, DOF 2p+i = node p component i), 3D Laplace (sol_dim 1), 3D
+// Stokes (sol_dim 3, DOF 3p+i).
 template <typename T>
 __device__ __forceinline__ T kernel_entry(const Points<T>& P, int sol_dim, int tdof, int sdof) {
+  if (P.dim == 3) {
+    if (sol_dim == 1)
+      return laplace3_entry<T>(P.x[tdof] - P.x[sdof], P.y[tdof] - P.y[sdof], P.z[tdof] - P.z[sdof],
+                               P.nx[sdof], P.ny[sdof], P.nz[sdof], P.w[sdof],
+                               P.diag ? P.diag[sdof] : T(0));
+    const int tp = tdof / 3, sp = sdof / 3;
+    return stokes3_entry<T>(tdof - 3 * tp, sdof - 3 * sp, P.x[tp] - P.x[sp], P.y[tp] - P.y[sp],
+                            P.z[tp] - P.z[sp], P.nx[tp], P.ny[tp], P.nz[tp], P.nx[sp], P.ny[sp],
+                            P.nz[sp], P.w[sp], P.diag ? P.diag + 9 * (size_t)sp : nullptr);
+  }
   if (sol_dim == 1) {
     return laplace_entry<T>(P.x[tdof], P.y[tdof], P.x[sdof], P.y[sdof], P.nx[sdof], P.ny[sdof],
                             P.w[sdof], P.kappa[sdof]);
@@ -60,6 +105,11 @@ __device__ __forceinline__ T kernel_entry(const Points<T>& P, int sol_dim, int t
   int tp = tdof >> 1, sp = sdof >> 1;
   return stokes_entry<T>(tdof & 1, sdof & 1, P.x[tp], P.y[tp], P.nx[tp], P.ny[tp], P.x[sp],
                          P.y[sp], P.nx[sp], P.ny[sp], P.w[sp], P.kappa[sp]);
+}
+
+// Point of a DOF.
+__device__ __forceinline__ int dof_point(int dof, int sol_dim) {
+  return sol_dim == 1 ? dof : (sol_dim == 2 ? dof >> 1 : dof / 3);
 }
 
 // ------------------------------------------------------------------------

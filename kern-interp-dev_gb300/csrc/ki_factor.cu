@@ -167,8 +167,8 @@ __device__ __forceinline__ float warp_sum(float v) {
 struct ActiveTask {
   int64_t dst;        // ipool offset of the box's active list
   int nseg;
-  int64_t src[4];     // ipool offsets of the pieces (leaf: 1 piece)
-  int len[4];
+  int64_t src[kMaxChildren];   // ipool offsets of the pieces (leaf: 1 piece)
+  int len[kMaxChildren];
 };
 
 struct IdTask {
@@ -176,7 +176,7 @@ struct IdTask {
   int n;
   int seg_begin, seg_end;
   int mode;           // 0: inner-circle filter + proxy rows; 1: all candidates, no proxy
-  double cx, cy, rad_filter, rad_proxy;
+  double cx, cy, cz, rad_filter, rad_proxy;
   int64_t rows;       // iscratch offset of the row list (capacity = candidates)
   int64_t ws;         // T-scratch offset: R (n*n) | B (32*n) | vn1 (n) | vn2 (n) | Tout (n*n/4+1)
   int64_t perm;       // iscratch offset of the pivot order (n)
@@ -189,8 +189,8 @@ struct AsmTask {
   int n;
   T* out;             // n x n
   int nchild;         // 0 for a leaf
-  int coff[4], clen[4];
-  const T* ctile[4];  // child accumulated self-blocks (clen x clen)
+  int coff[kMaxChildren], clen[kMaxChildren];
+  const T* ctile[kMaxChildren];  // child accumulated self-blocks (clen x clen)
 };
 
 template <typename T>
@@ -218,34 +218,68 @@ __global__ void k_build_active(const ActiveTask* tasks, int* ipool) {
   }
 }
 
+// Proxy surface of unit radius (Kernel::get_proxy_mat, kern_interp/kernel/
+// kernel.cpp:646-717: 2D, n points equispaced on a circle; get_proxy_mat3d,
+// :720-790: 3D, a theta x phi grid with theta outer).  A box's proxy point i
+// is c + rad * u_i with outward normal u_i and weight 2 pi rad / n (2D) or
+// rad^2 * wu_i (3D, wu = Gauss-Legendre phi weight * sin(phi) * theta weight).
+struct ProxyTab {
+  const double* ux;
+  const double* uy;
+  const double* uz;   // 3D only
+  const double* wu;   // 3D only
+  int n;
+};
+
 // One ID-matrix entry, row `row` of the stacked matrix
 // [K(I,A); K(A,I)^T; box->proxy; proxy->box] (Kernel::get_id_mat,
 // kern_interp/kernel/kernel.cpp:565-640; proxy rows Kernel::get_proxy_mat,
-// :646-717), column = active DOF `adof`.
+// :646-790), column = active DOF `adof`.
 template <typename T>
 __device__ __forceinline__ T id_entry(const Points<T>& P, int sol_dim, int row, int nI,
-                                      const int* rows, int adof, int nprox, const double* pcos,
-                                      const double* psin, double cx, double cy, double rad) {
+                                      const int* rows, int adof, const ProxyTab& px, double cx,
+                                      double cy, double cz, double rad) {
   if (row < nI) return kernel_entry<T>(P, sol_dim, rows[row], adof);
   if (row < 2 * nI) return kernel_entry<T>(P, sol_dim, adof, rows[row - nI]);
-  int q = row - 2 * nI;
+  const int q = row - 2 * nI;
+  const int nprox = px.n;
+  if (P.dim == 3) {
+    const int ap = sol_dim == 1 ? adof : adof / 3;
+    const T bx = P.x[ap], by = P.y[ap], bz = P.z[ap];
+    const T bnx = P.nx[ap], bny = P.ny[ap], bnz = P.nz[ap], bw = P.w[ap];
+    const int half = sol_dim * nprox;
+    const int qq = q < half ? q : q - half;
+    const int i = sol_dim == 1 ? qq : qq / 3, par = qq - sol_dim * i;
+    const T ux = T(px.ux[i]), uy = T(px.uy[i]), uz = T(px.uz[i]);
+    const T rx = T(cx + rad * px.ux[i]) - bx, ry = T(cy + rad * px.uy[i]) - by,
+            rz = T(cz + rad * px.uz[i]) - bz;   // proxy - box
+    const T pw = T(rad * rad * px.wu[i]);
+    if (sol_dim == 1) {
+      if (q < half) return laplace3_entry<T>(rx, ry, rz, bnx, bny, bnz, bw, T(0));
+      return laplace3_entry<T>(-rx, -ry, -rz, ux, uy, uz, pw, T(0));
+    }
+    const int apar = adof - 3 * ap;
+    if (q < half)
+      return stokes3_entry<T>(par, apar, rx, ry, rz, ux, uy, uz, bnx, bny, bnz, bw, nullptr);
+    return stokes3_entry<T>(apar, par, -rx, -ry, -rz, bnx, bny, bnz, ux, uy, uz, pw, nullptr);
+  }
   int ap = sol_dim == 1 ? adof : (adof >> 1);
   T bx = P.x[ap], by = P.y[ap], bnx = P.nx[ap], bny = P.ny[ap], bw = P.w[ap];
   T pw = T(2.0 * kPi * rad / nprox);
   if (sol_dim == 1) {
     int i = q < nprox ? q : q - nprox;
-    T px = T(cx + rad * pcos[i]), py = T(cy + rad * psin[i]);
-    T pnx = T(pcos[i]), pny = T(psin[i]);
-    if (q < nprox) return laplace_entry<T>(px, py, bx, by, bnx, bny, bw, T(0));
-    return laplace_entry<T>(bx, by, px, py, pnx, pny, pw, T(0));
+    T ppx = T(cx + rad * px.ux[i]), ppy = T(cy + rad * px.uy[i]);
+    T pnx = T(px.ux[i]), pny = T(px.uy[i]);
+    if (q < nprox) return laplace_entry<T>(ppx, ppy, bx, by, bnx, bny, bw, T(0));
+    return laplace_entry<T>(bx, by, ppx, ppy, pnx, pny, pw, T(0));
   }
   int half = 2 * nprox;
   int qq = q < half ? q : q - half;
   int i = qq >> 1, par = qq & 1;
-  T px = T(cx + rad * pcos[i]), py = T(cy + rad * psin[i]);
-  T pnx = T(pcos[i]), pny = T(psin[i]);
-  if (q < half) return stokes_entry<T>(par, adof & 1, px, py, pnx, pny, bx, by, bnx, bny, bw, T(0));
-  return stokes_entry<T>(adof & 1, par, bx, by, bnx, bny, px, py, pnx, pny, pw, T(0));
+  T ppx = T(cx + rad * px.ux[i]), ppy = T(cy + rad * px.uy[i]);
+  T pnx = T(px.ux[i]), pny = T(px.uy[i]);
+  if (q < half) return stokes_entry<T>(par, adof & 1, ppx, ppy, pnx, pny, bx, by, bnx, bny, bw, T(0));
+  return stokes_entry<T>(adof & 1, par, bx, by, bnx, bny, ppx, ppy, pnx, pny, pw, T(0));
 }
 
 // Interpolative decomposition of one box per CTA.
@@ -261,8 +295,7 @@ template <typename T, int FR>
 __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_base,
                                                   const int64_t* seg_off, const int* seg_len,
                                                   int* ipool, int* iscratch, T* tws, Points<T> P,
-                                                  int sol_dim, int nprox, const double* pcos,
-                                                  const double* psin, double tol, int* k_out,
+                                                  int sol_dim, ProxyTab px, double tol, int* k_out,
                                                   int* m_out, int mode, int flags) {
   // flags: 1 gather the rows (writes m), 2 fold the ID matrix into R,
   //        4 R already formed (row-major n x n in the global scratch)
@@ -306,7 +339,7 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   T* Tout = gws + (size_t)n * n;
 
   // 1. candidate rows, optionally filtered to the proxy circle, order kept
-  const int nprox_rows = t.mode == 0 ? 2 * nprox * sol_dim : 0;
+  const int nprox_rows = t.mode == 0 ? 2 * px.n * sol_dim : 0;
   if (flags & 1) {
   if (tid == 0) s_cnt = 0;
   __syncthreads();
@@ -321,9 +354,14 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
         if (t.mode == 1) {
           keep = 1;
         } else {
-          int p = sol_dim == 1 ? dof : dof >> 1;
+          const int p = dof_point(dof, sol_dim);
           double dx = t.cx - (double)P.x[p], dy = t.cy - (double)P.y[p];
-          double dist = sqrt(dx * dx + dy * dy);
+          double d2 = dx * dx + dy * dy;
+          if (P.dim == 3) {
+            double dz = t.cz - (double)P.z[p];
+            d2 += dz * dz;
+          }
+          double dist = sqrt(d2);
           keep = dist < t.rad_filter;
         }
       }
@@ -402,7 +440,7 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
       int row = r0 + i;
       T v = T(0);
       if (row < m)
-        v = id_entry<T>(P, sol_dim, row, nI, rows, act[j], nprox, pcos, psin, t.cx, t.cy,
+        v = id_entry<T>(P, sol_dim, row, nI, rows, act[j], px, t.cx, t.cy, t.cz,
                         t.rad_proxy);
       B[(size_t)i * ldB + j] = v;
     }
@@ -615,7 +653,7 @@ struct WideTask {
   int64_t M;           // T-pool offset of M (m x n, column-major, ld = m)
   int64_t Tf;          // T-pool offset of the current panel's WY factor (kQrNb x kQrNb)
   int64_t act, rows;   // ipool / iscratch offsets
-  double cx, cy, rad;
+  double cx, cy, cz, rad;
   int64_t R;           // T-scratch offset (tws) of the row-major triangle for k_id
 };
 
@@ -625,8 +663,7 @@ constexpr int kQrRows = 64;   // rows staged per trailing-update pass
 
 template <typename T>
 __global__ void k_wide_assemble(const WideTask* tasks, T* wpool, const int* ipool, const int* iscratch,
-                                Points<T> P, int sol_dim, int nprox, const double* pcos,
-                                const double* psin) {
+                                Points<T> P, int sol_dim, ProxyTab px) {
   const WideTask t = tasks[blockIdx.x];
   const int j0 = blockIdx.y * 8;
   if (j0 >= t.n) return;
@@ -637,8 +674,8 @@ __global__ void k_wide_assemble(const WideTask* tasks, T* wpool, const int* ipoo
   for (int j = j0; j < j1; j++) {
     int a = act[j];
     for (int row = threadIdx.x; row < t.m; row += blockDim.x)
-      M[row + (size_t)t.m * j] = id_entry<T>(P, sol_dim, row, t.nI, rows, a, nprox, pcos, psin,
-                                             t.cx, t.cy, t.rad);
+      M[row + (size_t)t.m * j] = id_entry<T>(P, sol_dim, row, t.nI, rows, a, px, t.cx, t.cy,
+                                             t.cz, t.rad);
   }
 }
 
@@ -1185,22 +1222,27 @@ __global__ void k_scatter_rows(T* x, int ldx, const int* idx, int n, int ncols, 
 // ------------------------------------------------------- bordered system --
 // Border matrices of a multiply connected problem, DOF-major (row = DOF,
 // nb columns): U (initialize_U_mat, kern_interp/linear_solve.cpp:19-107) and
-// Psi^T (initialize_Psi_mat, :110-199, membership from node ranges).
+// Psi^T (initialize_Psi_mat, :110-199, membership from node ranges).  Input
+// coordinates are the interleaved FP64 arrays (dim per point).
 template <typename T>
-__global__ void k_border_init(Points<T> P, const double* px, const double* py, const double* pw,
-                              int n_points, int sol_dim, const double* hc, int nh,
-                              const int* hole_of, T* U, T* PsiT) {
-  const int nb = sol_dim == 1 ? nh : 3 * nh;
+__global__ void k_border_init(const double* pts, const double* pw, int n_points, int dim,
+                              int sol_dim, const double* hc, int nh, const int* hole_of, T* U,
+                              T* PsiT) {
+  const int c = border_cols_per_hole(dim, sol_dim);
+  const int nb = c * nh;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n_points; p += gridDim.x * blockDim.x) {
-    double x = px[2 * (size_t)p], y = py[2 * (size_t)p];   // interleaved input
-    int hp = hole_of[p];
+    const double* xp = pts + (size_t)dim * p;
+    const int hp = hole_of[p];
     if (sol_dim == 1) {
       for (int h = 0; h < nh; h++) {
-        double rx = x - hc[2 * h], ry = y - hc[2 * h + 1];
-        U[(size_t)p * nb + h] = T(log(sqrt(rx * rx + ry * ry)));
+        double r2 = 0;
+        for (int d = 0; d < dim; d++) r2 += (xp[d] - hc[dim * h + d]) * (xp[d] - hc[dim * h + d]);
+        double rn = sqrt(r2);
+        U[(size_t)p * nb + h] = T(dim == 2 ? log(rn) : 1.0 / rn);
         PsiT[(size_t)p * nb + h] = T(h == hp ? pw[p] : 0.0);
       }
-    } else {
+    } else if (dim == 2) {
+      const double x = xp[0], y = xp[1];
       T* u0 = U + (size_t)(2 * p) * nb;
       T* u1 = U + (size_t)(2 * p + 1) * nb;
       T* q0 = PsiT + (size_t)(2 * p) * nb;
@@ -1222,9 +1264,113 @@ __global__ void k_border_init(Points<T> P, const double* px, const double* py, c
         q0[3 * h + 2] = T(w * y);
         q1[3 * h + 2] = T(-w * x);
       }
+    } else {
+      // 3D Stokes: Stokeslet (1/8pi)(delta/|r| + r_i r_j/|r|^3) in columns
+      // 6h..6h+2, rotlet -(1/8pi|r|^3) [r]_x in 6h+3..6h+5 (linear_solve.cpp:49-76);
+      // Psi: weights on the diagonal, -w [r]_x^T for the rotation rows
+      // (r relative to the hole centre, :146-163)
+      for (int h = 0; h < nh; h++) {
+        const double r[3] = {xp[0] - hc[3 * h], xp[1] - hc[3 * h + 1], xp[2] - hc[3 * h + 2]};
+        const double rn = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+        const double rn3 = rn * rn * rn;
+        const double rot = -1.0 / (8.0 * kPi * rn3);
+        const double w = h == hp ? pw[p] : 0.0;
+        for (int a = 0; a < 3; a++) {
+          T* u = U + (size_t)(3 * p + a) * nb + 6 * h;
+          T* q = PsiT + (size_t)(3 * p + a) * nb + 6 * h;
+          for (int b = 0; b < 3; b++)
+            u[b] = T((1.0 / (8.0 * kPi)) * ((a == b ? 1.0 : 0.0) / rn + r[a] * r[b] / rn3));
+          for (int b = 0; b < 3; b++) q[b] = T(a == b ? w : 0.0);
+        }
+        T* u0 = U + (size_t)(3 * p) * nb + 6 * h;
+        T* u1 = U + (size_t)(3 * p + 1) * nb + 6 * h;
+        T* u2 = U + (size_t)(3 * p + 2) * nb + 6 * h;
+        u0[3] = T(0);            u0[4] = T(rot * -r[2]); u0[5] = T(rot * r[1]);
+        u1[3] = T(rot * r[2]);   u1[4] = T(0);           u1[5] = T(rot * -r[0]);
+        u2[3] = T(rot * -r[1]);  u2[4] = T(rot * r[0]);  u2[5] = T(0);
+        T* q0 = PsiT + (size_t)(3 * p) * nb + 6 * h;
+        T* q1 = PsiT + (size_t)(3 * p + 1) * nb + 6 * h;
+        T* q2 = PsiT + (size_t)(3 * p + 2) * nb + 6 * h;
+        q0[3] = T(0);            q0[4] = T(-w * -r[2]);  q0[5] = T(-w * r[1]);
+        q1[3] = T(-w * r[2]);    q1[4] = T(0);           q1[5] = T(-w * -r[0]);
+        q2[3] = T(-w * -r[1]);   q2[4] = T(-w * r[0]);   q2[5] = T(0);
+      }
     }
   }
-  (void)P;
+}
+
+// Diagonal entries of the 3D Nystrom matrices (Kernel::compute_diag_entries_
+// 3dlaplace / _3dstokes, kern_interp/kernel/kernel.cpp:124-301): row sums of
+// the off-diagonal kernel over the point's own surface (the outer surface
+// [0, n_outer) or its hole's node range), then 1 - sum (Laplace) / I - sum
+// (Stokes, every 3 x 3 block including the n_t n_s^T completion term) on the
+// outer surface and -sum on holes.  FP64, one thread per target point,
+// sources staged through shared memory; every thread adds its terms in
+// source order.
+constexpr int kDiagThreads = 128;
+constexpr int kDiagTile = 256;
+
+__global__ void __launch_bounds__(kDiagThreads) k_diag3(const double* pts, const double* nrm,
+                                                        const double* w, int n_points,
+                                                        const int* grp_lo, const int* grp_hi,
+                                                        int n_outer, int sol_dim, double* out) {
+  __shared__ double s[7][kDiagTile];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool on = t < n_points;
+  const int tc = on ? t : n_points - 1;
+  const int lo = grp_lo[tc], hi = grp_hi[tc];
+  // source range of the block: union of its targets' ranges
+  const int t0 = blockIdx.x * blockDim.x, t1 = min(n_points, t0 + (int)blockDim.x) - 1;
+  const int blo = grp_lo[t0], bhi = max(grp_hi[t0], grp_hi[t1]);
+  const double tx = pts[3 * (size_t)tc], ty = pts[3 * (size_t)tc + 1], tz = pts[3 * (size_t)tc + 2];
+  const double tn[3] = {nrm[3 * (size_t)tc], nrm[3 * (size_t)tc + 1], nrm[3 * (size_t)tc + 2]};
+  double acc[9];
+  for (int q = 0; q < 9; q++) acc[q] = 0.0;
+  for (int base = blo; base < bhi; base += kDiagTile) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < kDiagTile; i += blockDim.x) {
+      int p = base + i;
+      if (p < bhi) {
+        s[0][i] = pts[3 * (size_t)p]; s[1][i] = pts[3 * (size_t)p + 1]; s[2][i] = pts[3 * (size_t)p + 2];
+        s[3][i] = nrm[3 * (size_t)p]; s[4][i] = nrm[3 * (size_t)p + 1]; s[5][i] = nrm[3 * (size_t)p + 2];
+        s[6][i] = w[p];
+      }
+    }
+    __syncthreads();
+    const int i0 = max(0, lo - base), i1 = min(kDiagTile, hi - base);
+    for (int i = i0; i < i1; i++) {
+      if (base + i == t) continue;
+      const double r1 = tx - s[0][i], r2 = ty - s[1][i], r3 = tz - s[2][i];
+      const double rr = r1 * r1 + r2 * r2 + r3 * r3;
+      const double rn = r1 * s[3][i] + r2 * s[4][i] + r3 * s[5][i];
+      const double sw = s[6][i];
+      if (sol_dim == 1) {
+        acc[0] += -sw * (1.0 / (4 * kPi)) * rn / (rr * sqrt(rr));
+      } else {
+        const double r[3] = {r1, r2, r3};
+        const double sn[3] = {s[3][i], s[4][i], s[5][i]};
+        const double f = sw * (-3.0 / (4.0 * kPi)) * rn / (rr * rr * sqrt(rr));
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+          for (int b = 0; b < 3; b++) acc[3 * a + b] += f * r[a] * r[b] + sw * tn[a] * sn[b];
+      }
+    }
+  }
+  if (!on) return;
+  const double one = t < n_outer ? 1.0 : 0.0;
+  if (sol_dim == 1) {
+    out[t] = one - acc[0];
+  } else {
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) out[9 * (size_t)t + 3 * a + b] = (a == b ? one : 0.0) - acc[3 * a + b];
+  }
+}
+
+template <typename T>
+__global__ void k_convert(const double* a, size_t n, T* b) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = T(a[i]);
 }
 
 __global__ void k_mark(const int* idx, int n, unsigned char* mask) {
@@ -1337,14 +1483,21 @@ __global__ void k_mc_finish(T* x, int nc, const int* idx, const T* M, int nr, in
   }
 }
 
+// Interleaved FP64 input (dim per point) -> structure-of-arrays in the
+// factor precision.
 template <typename T>
 __global__ void k_fill_points(const double* pts, const double* nrm, const double* w,
-                              const double* kap, int n, T* x, T* y, T* nx, T* ny, T* ww, T* kk) {
+                              const double* kap, int n, int dim, T* x, T* y, T* z, T* nx, T* ny,
+                              T* nz, T* ww, T* kk) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    x[i] = T(pts[2 * i]);
-    y[i] = T(pts[2 * i + 1]);
-    nx[i] = T(nrm[2 * i]);
-    ny[i] = T(nrm[2 * i + 1]);
+    x[i] = T(pts[(size_t)dim * i]);
+    y[i] = T(pts[(size_t)dim * i + 1]);
+    nx[i] = T(nrm[(size_t)dim * i]);
+    ny[i] = T(nrm[(size_t)dim * i + 1]);
+    if (dim == 3) {
+      z[i] = T(pts[3 * (size_t)i + 2]);
+      nz[i] = T(nrm[3 * (size_t)i + 2]);
+    }
     ww[i] = T(w[i]);
     kk[i] = kap ? T(kap[i]) : T(0);
   }
@@ -1354,6 +1507,51 @@ template <typename T>
 void upload(T* dst, const std::vector<T>& v, cudaStream_t s) {
   if (!v.empty())
     KI_CUDA(cudaMemcpyAsync(dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
+}
+
+// Gauss-Legendre rule with n nodes on [a, b], ascending: Newton iteration on
+// the three-term recurrence of P_n from the Chebyshev-like initial guesses
+// cos(pi (i + 3/4) / (n + 1/2)).  (The reference calls the LGPL routine cgqf
+// for its proxy-sphere latitudes, kern_interp/kernel/kernel.h:48-54.)
+void gauss_legendre(int n, double a, double b, std::vector<double>* x, std::vector<double>* w) {
+  x->assign(n, 0.0);
+  w->assign(n, 0.0);
+  for (int i = 0; i < n; i++) {
+    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 1.0;
+    for (int it = 0; it < 100; it++) {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= n; k++) {
+        double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      if (n == 1) { p1 = z; p0 = 1.0; }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      double dz = p1 / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-16) break;
+    }
+    // recompute the derivative at the converged node
+    double p0 = 1.0, p1 = z;
+    for (int k = 2; k <= n; k++) {
+      double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    dp = n == 1 ? 1.0 : n * (z * p1 - p0) / (z * z - 1.0);
+    // node i of the descending order -> index n-1-i of the ascending one
+    (*x)[n - 1 - i] = 0.5 * (b - a) * z + 0.5 * (b + a);
+    (*w)[n - 1 - i] = (b - a) / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+// Latitude count of a 3D proxy sphere of P = 2 q^2 points (theta x phi grid
+// with twice as many longitudes as latitudes, the reference's 8 x 4 = 32).
+int proxy_phi_count(int P) {
+  int q = (int)std::lround(std::sqrt(P / 2.0));
+  if (q < 1 || 2 * q * q != P)
+    throw std::invalid_argument("3D num_proxy_points must be 2 q^2 (8, 32, 72, 128, ..., 512)");
+  return q;
 }
 
 struct HostBox {
@@ -1440,53 +1638,113 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
   F->stream = stream;
   F->n_points = n_points;
   Tree& tree = F->tree;
-  tree.build(points, n_points, prm.sol_dim, prm.max_leaf_dofs);
+  const int dim = prm.dim;
+  tree.build(points, n_points, dim, prm.sol_dim, prm.max_leaf_dofs);
   const int sd = prm.sol_dim;
+  const int nch = tree.n_children();
   const int N = tree.n_dofs;
   F->N = N;
   const int L = tree.num_levels();
   cudaStream_t s = stream;
 
-  // point data
+  // point data: interleaved FP64 input (points, normals: dim per point;
+  // weights; curvatures) -> SoA in precision T
   double* d_pts_in = nullptr;
+  double* d_nrm_in = nullptr;
   double* d_w_in = nullptr;
   {
-    double* d_in = (double*)F->alloc(sizeof(double) * (size_t)n_points * 6);
+    const size_t np_ = (size_t)n_points;
+    double* d_in = (double*)F->alloc(sizeof(double) * np_ * (2 * dim + 2));
     d_pts_in = d_in;
-    d_w_in = d_in + 4 * (size_t)n_points;
-    KI_CUDA(cudaMemcpyAsync(d_in, points, sizeof(double) * 2 * n_points, cudaMemcpyHostToDevice, s));
-    KI_CUDA(cudaMemcpyAsync(d_in + 2 * (size_t)n_points, normals, sizeof(double) * 2 * n_points,
-                            cudaMemcpyHostToDevice, s));
-    KI_CUDA(cudaMemcpyAsync(d_in + 4 * (size_t)n_points, weights, sizeof(double) * n_points,
-                            cudaMemcpyHostToDevice, s));
+    d_nrm_in = d_in + dim * np_;
+    d_w_in = d_in + 2 * dim * np_;
+    double* d_k_in = d_w_in + np_;
+    KI_CUDA(cudaMemcpyAsync(d_pts_in, points, sizeof(double) * dim * np_, cudaMemcpyHostToDevice, s));
+    KI_CUDA(cudaMemcpyAsync(d_nrm_in, normals, sizeof(double) * dim * np_, cudaMemcpyHostToDevice, s));
+    KI_CUDA(cudaMemcpyAsync(d_w_in, weights, sizeof(double) * np_, cudaMemcpyHostToDevice, s));
     if (curvatures)
-      KI_CUDA(cudaMemcpyAsync(d_in + 5 * (size_t)n_points, curvatures, sizeof(double) * n_points,
-                              cudaMemcpyHostToDevice, s));
-    T* d = (T*)F->alloc(sizeof(T) * (size_t)n_points * 6);
-    F->d_x = d; F->d_y = d + n_points; F->d_nx = d + 2 * (size_t)n_points;
-    F->d_ny = d + 3 * (size_t)n_points; F->d_w = d + 4 * (size_t)n_points;
-    F->d_kappa = d + 5 * (size_t)n_points;
+      KI_CUDA(cudaMemcpyAsync(d_k_in, curvatures, sizeof(double) * np_, cudaMemcpyHostToDevice, s));
+    T* d = (T*)F->alloc(sizeof(T) * np_ * 8);
+    F->d_x = d; F->d_y = d + np_; F->d_nx = d + 2 * np_;
+    F->d_ny = d + 3 * np_; F->d_w = d + 4 * np_;
+    F->d_kappa = d + 5 * np_;
+    if (dim == 3) {
+      F->d_z = d + 6 * np_;
+      F->d_nz = d + 7 * np_;
+    }
     k_fill_points<T><<<std::min(1024, (n_points + 255) / 256), 256, 0, s>>>(
-        d_in, d_in + 2 * (size_t)n_points, d_in + 4 * (size_t)n_points,
-        curvatures ? d_in + 5 * (size_t)n_points : nullptr, n_points, F->d_x, F->d_y, F->d_nx,
-        F->d_ny, F->d_w, F->d_kappa);
+        d_pts_in, d_nrm_in, d_w_in, curvatures ? d_k_in : nullptr, n_points, dim, F->d_x,
+        F->d_y, F->d_z, F->d_nx, F->d_ny, F->d_nz, F->d_w, F->d_kappa);
     KI_CUDA(cudaGetLastError());
   }
   Points<T> P{F->d_x, F->d_y, F->d_nx, F->d_ny, F->d_w, F->d_kappa};
+  P.dim = dim;
+  P.z = F->d_z;
+  P.nz = F->d_nz;
   F->d_err = (int*)F->alloc(sizeof(int));
   KI_CUDA(cudaMemsetAsync(F->d_err, 0, sizeof(int), s));
 
-  // proxy angles (Kernel::get_proxy_mat: ang = 2 pi i / P)
+  // 3D diagonal entries (Kernel::compute_diag_entries_3dlaplace/_3dstokes)
+  if (dim == 3) {
+    const int dpp = sd == 1 ? 1 : 9;
+    F->diag_per_point = dpp;
+    std::vector<int> glo(n_points), ghi(n_points);
+    const int n_outer = holes.n_holes > 0 ? holes.start[0] : n_points;
+    for (int p = 0; p < n_outer; p++) { glo[p] = 0; ghi[p] = n_outer; }
+    for (int h = 0; h < holes.n_holes; h++)
+      for (int p = holes.start[h]; p < holes.start[h] + holes.count[h]; p++) {
+        glo[p] = holes.start[h];
+        ghi[p] = holes.start[h] + holes.count[h];
+      }
+    int* d_g = (int*)F->alloc(sizeof(int) * 2 * (size_t)n_points);
+    KI_CUDA(cudaMemcpyAsync(d_g, glo.data(), sizeof(int) * n_points, cudaMemcpyHostToDevice, s));
+    KI_CUDA(cudaMemcpyAsync(d_g + n_points, ghi.data(), sizeof(int) * n_points, cudaMemcpyHostToDevice, s));
+    F->d_diag64 = (double*)F->alloc(sizeof(double) * (size_t)dpp * n_points);
+    F->stage_begin("diag3", (sd == 1 ? 20.0 : 80.0) * (double)n_points * n_points, 0);
+    k_diag3<<<(n_points + kDiagThreads - 1) / kDiagThreads, kDiagThreads, 0, s>>>(
+        d_pts_in, d_nrm_in, d_w_in, n_points, d_g, d_g + n_points, n_outer, sd, F->d_diag64);
+    F->stage_end();
+    KI_CUDA(cudaGetLastError());
+    // synchronize on the (host) group arrays before they go out of scope
+    KI_CUDA(cudaStreamSynchronize(s));
+    F->d_diag = (T*)F->alloc(sizeof(T) * (size_t)dpp * n_points);
+    k_convert<T><<<std::min(2048, (dpp * n_points + 255) / 256), 256, 0, s>>>(
+        F->d_diag64, (size_t)dpp * n_points, F->d_diag);
+    KI_CUDA(cudaGetLastError());
+    P.diag = F->d_diag;
+  }
+
+  // proxy surface of unit radius (Kernel::get_proxy_mat: 2D angle 2 pi i / P;
+  // Kernel::get_proxy_mat3d and the Kernel constructor, kernel/kernel.h:44-62:
+  // 3D theta_a = 2 pi a / n_theta, phi_b the Gauss-Legendre nodes on [0, pi],
+  // theta outer)
   const int np = prm.num_proxy_points;
-  double* d_pcs = (double*)F->alloc(sizeof(double) * 2 * std::max(np, 1));
+  double* d_ptab = (double*)F->alloc(sizeof(double) * 4 * std::max(np, 1));
+  ProxyTab ptab{d_ptab, d_ptab + np, d_ptab + 2 * np, d_ptab + 3 * np, np};
   {
-    std::vector<double> pc(2 * std::max(np, 1));
-    for (int i = 0; i < np; i++) {
-      double ang = 2 * M_PI * i * (1.0 / np);
-      pc[i] = std::cos(ang);
-      pc[np + i] = std::sin(ang);
+    std::vector<double> pt(4 * std::max(np, 1), 0.0);
+    if (dim == 2) {
+      for (int i = 0; i < np; i++) {
+        double ang = 2 * M_PI * i * (1.0 / np);
+        pt[i] = std::cos(ang);
+        pt[np + i] = std::sin(ang);
+      }
+    } else {
+      const int nphi = proxy_phi_count(np), ntheta = 2 * nphi;
+      std::vector<double> phi, phw;
+      gauss_legendre(nphi, 0.0, M_PI, &phi, &phw);
+      for (int a = 0; a < ntheta; a++) {
+        const double theta = 2 * M_PI * a * (1.0 / ntheta);
+        for (int b = 0; b < nphi; b++) {
+          const int i = a * nphi + b;
+          pt[i] = std::sin(phi[b]) * std::cos(theta);
+          pt[np + i] = std::sin(phi[b]) * std::sin(theta);
+          pt[2 * np + i] = std::cos(phi[b]);
+          pt[3 * np + i] = (phw[b] * std::sin(phi[b])) * (2 * M_PI / ntheta);
+        }
+      }
     }
-    upload(d_pcs, pc, s);
+    upload(d_ptab, pt, s);
   }
 
   // integer pool: dof_sorted | per-level active lists | permuted lists
@@ -1519,8 +1777,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         at.len[0] = h.n;
       } else {
         h.n = 0;
-        at.nseg = 4;
-        for (int ci = 0; ci < 4; ci++) {
+        at.nseg = nch;
+        for (int ci = 0; ci < nch; ci++) {
           const HostBox& c = hb[bx.child[ci]];
           at.src[ci] = c.compressed ? c.pact : c.act;
           at.len[ci] = c.compressed ? c.k : c.n;
@@ -1536,7 +1794,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       ActiveTask* d_at = (ActiveTask*)F->alloc(sizeof(ActiveTask) * atasks.size());
       upload(d_at, atasks, s);
       double nb = 0;
-      for (auto& a : atasks) nb += 8.0 * (a.len[0] + a.len[1] + a.len[2] + a.len[3]);
+      for (auto& a : atasks)
+        for (int q = 0; q < a.nseg; q++) nb += 8.0 * a.len[q];
       F->stage_begin("active_lists", 0, nb);
       k_build_active<<<(unsigned)atasks.size(), 128, 0, s>>>(d_at, ipool);
       F->stage_end();
@@ -1565,7 +1824,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         off += (int64_t)h.n * h.n;
         if (!bx.leaf) {
           int o = 0;
-          for (int ci = 0; ci < 4; ci++) {
+          for (int ci = 0; ci < nch; ci++) {
             const HostBox& c = hb[bx.child[ci]];
             int len = c.compressed ? c.k : c.n;
             if (len == 0) continue;
@@ -1608,12 +1867,14 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       IdTask it{};
       it.act = h.act;
       it.n = h.n;
-      it.cx = bx.cx;
-      it.cy = bx.cy;
+      it.cx = bx.c[0];
+      it.cy = bx.c[1];
+      it.cz = bx.c[2];
       it.seg_begin = (int)seg_off.size();
-      if (l == 1 || l == 2) {
+      if (l == 1 || (l == 2 && dim == 2)) {
         // Kernel::get_id_mat levels 1/2 (kernel.cpp:441-563): every other box of
         // the level, plus (level 2) the leaves of the levels above; no proxy.
+        // Level 2 takes this path in 2D only (`domain_dimension < 3`, :491).
         it.mode = 1;
         for (int o : lv)
           if (o != b) add_seg(hb[o].act, hb[o].n);
@@ -1623,8 +1884,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
               if (tree.boxes[o].leaf) add_seg(tree.boxes[o].orig_start, tree.boxes[o].orig_count);
       } else {
         it.mode = 0;
-        it.rad_filter = std::sqrt(2.0) * prm.radius_ratio * (bx.side / 2);
-        it.rad_proxy = (bx.side / 2) * std::sqrt(2.0) * prm.radius_ratio;
+        it.rad_filter = std::sqrt((double)dim) * prm.radius_ratio * (bx.side / 2);
+        it.rad_proxy = (bx.side / 2) * std::sqrt((double)dim) * prm.radius_ratio;
         for (int o : bx.coarse_nbrs) add_seg(tree.boxes[o].orig_start, tree.boxes[o].orig_count);
         for (int o : bx.same_nbrs) {
           const Box& ob = tree.boxes[o];
@@ -1671,7 +1932,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     KI_CUDA(cudaFuncSetAttribute(k_id<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
     KI_CUDA(cudaFuncSetAttribute(k_id<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
     k_id<T, 32><<<(unsigned)itasks.size(), kThreads, 0, s>>>(d_it, 0, d_soff, d_slen, ipool, d_irows, d_tws,
-                                                         P, sd, np, d_pcs, d_pcs + np, prm.id_tol,
+                                                         P, sd, ptab, prm.id_tol,
                                                          d_k, d_m, 0, 1);
     KI_CUDA(cudaGetLastError());
     std::vector<int> mh(itasks.size()), kh(itasks.size());
@@ -1759,11 +2020,11 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         cudaStream_t st = fixed ? fixed : F->aux[(next_aux++) % (Factorization<T>::kAux - 1)];
         if (fr == 64)
           k_id<T, 64><<<(unsigned)(b1 - b0), kThreads, sm, st>>>(d_it, b0, d_soff, d_slen, ipool, d_irows,
-                                                                 d_tws, P, sd, np, d_pcs, d_pcs + np,
+                                                                 d_tws, P, sd, ptab,
                                                                  prm.id_tol, d_k, d_m, kmode, flags);
         else
           k_id<T, 32><<<(unsigned)(b1 - b0), kThreads, sm, st>>>(d_it, b0, d_soff, d_slen, ipool, d_irows,
-                                                                 d_tws, P, sd, np, d_pcs, d_pcs + np,
+                                                                 d_tws, P, sd, ptab,
                                                                  prm.id_tol, d_k, d_m, kmode, flags);
         KI_CUDA(cudaGetLastError());
         b0 = b1;
@@ -1793,6 +2054,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         w.rows = itasks[i].rows;
         w.cx = itasks[i].cx;
         w.cy = itasks[i].cy;
+        w.cz = itasks[i].cz;
         w.rad = itasks[i].rad_proxy;
         w.R = itasks[i].ws;
         maxn = std::max(maxn, w.n);
@@ -1812,7 +2074,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         std::string wq = "wide_qr@L" + std::to_string(l);
         F->stage_begin(wq.c_str(), 0, 0, ws3);
         k_wide_assemble<T><<<dim3((unsigned)wt.size(), (maxn + 7) / 8), 256, 0, ws3>>>(
-            d_wt, d_wpool, ipool, d_irows, P, sd, np, d_pcs, d_pcs + np);
+            d_wt, d_wpool, ipool, d_irows, P, sd, ptab);
         for (int p0 = 0; p0 < maxn; p0 += kQrNb) {
           k_qr_panel<T><<<(unsigned)wt.size(), 256, 0, ws3>>>(d_wt, d_wpool, p0);
           int tiles = (maxn - p0 - kQrNb + kQrTile - 1) / kQrTile;
@@ -1994,7 +2256,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       at.out = A;
       if (!bx.leaf) {
         int o = 0;
-        for (int ci = 0; ci < 4; ci++) {
+        for (int ci = 0; ci < nch; ci++) {
           const HostBox& c = hb[bx.child[ci]];
           int len = c.compressed ? c.k : c.n;
           if (len == 0) continue;
@@ -2025,20 +2287,19 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         // through every level, apply X_rr^-1 to U's redundant rows, form and
         // factor S.
         const int nh = holes.n_holes;
-        const int nb = sd == 1 ? nh : 3 * nh;
+        const int nb = border_cols_per_hole(dim, sd) * nh;
         F->n_border = nb;
         std::vector<int> hole_of(n_points, -1);
         for (int q = 0; q < nh; q++)
           for (int p = holes.start[q]; p < holes.start[q] + holes.count[q]; p++) hole_of[p] = q;
         int* d_hole_of = (int*)F->alloc(sizeof(int) * n_points);
         upload(d_hole_of, hole_of, s);
-        double* d_hc = (double*)F->alloc(sizeof(double) * 2 * nh);
+        double* d_hc = (double*)F->alloc(sizeof(double) * dim * nh);
         upload(d_hc, holes.centers, s);
         F->d_Umod = (T*)F->alloc(Tsz * (size_t)N * nb);
         F->d_PsiTmod = (T*)F->alloc(Tsz * (size_t)N * nb);
         k_border_init<T><<<std::min(2048, (n_points + 255) / 256), 256, 0, s>>>(
-            P, d_pts_in, d_pts_in + 1, d_w_in, n_points, sd, d_hc, nh, d_hole_of, F->d_Umod,
-            F->d_PsiTmod);
+            d_pts_in, d_w_in, n_points, dim, sd, d_hc, nh, d_hole_of, F->d_Umod, F->d_PsiTmod);
         KI_CUDA(cudaGetLastError());
         F->stage_begin("border_sweeps", 0, 0);
         F->stage_begin("border_U_Psi", 0, 0);

@@ -13,10 +13,11 @@
 namespace ki {
 
 struct Params {
-  int sol_dim = 1;            // 1: Laplace, 2: Stokes (2D)
+  int dim = 2;                // domain dimension: 2 or 3
+  int sol_dim = 1;            // 1: Laplace, 2: Stokes (2D), 3: Stokes (3D)
   int max_leaf_dofs = 64;     // MAX_LEAF_DOFS
-  int num_proxy_points = 128; // NUM_PROXY_POINTS
-  double radius_ratio = 2.0;  // RADIUS_RATIO: proxy radius = ratio*sqrt(2)*side/2
+  int num_proxy_points = 128; // NUM_PROXY_POINTS (2D); 3D: theta x phi grid, 2 q^2 points
+  double radius_ratio = 2.0;  // RADIUS_RATIO: proxy radius = ratio*sqrt(dim)*side/2
   int min_dofs_to_compress = 64;
   double id_tol = 1e-10;
 };
@@ -69,7 +70,12 @@ struct Factorization {
   int n_points = 0;
   // point data (device, SoA, precision T)
   T *d_x = nullptr, *d_y = nullptr, *d_nx = nullptr, *d_ny = nullptr, *d_w = nullptr,
-    *d_kappa = nullptr;
+    *d_kappa = nullptr, *d_z = nullptr, *d_nz = nullptr;
+  // 3D diagonal entries (Kernel::compute_diag_entries_3dlaplace/_3dstokes):
+  // FP64 (kept for the FP64 operator apply) and in the factor precision
+  double* d_diag64 = nullptr;
+  T* d_diag = nullptr;
+  int diag_per_point = 0;   // 1 (Laplace), 9 (Stokes), 0 in 2D
   std::vector<LevelFactor> levels;   // index = tree level
   // root
   int n_root = 0;
@@ -104,9 +110,16 @@ struct Factorization {
   void* alloc(size_t bytes);
 };
 
+// Border columns per hole of the bordered system (initialize_U_mat,
+// kern_interp/linear_solve.cpp:19-107): Laplace 1, 2D Stokes 3 (Stokeslet x2
+// + rotlet), 3D Stokes 6 (Stokeslet x3 + rotlet x3).
+__host__ __device__ inline int border_cols_per_hole(int dim, int sol_dim) {
+  return sol_dim == 1 ? 1 : (dim == 2 ? 3 : 6);
+}
+
 struct HoleDesc {
   int n_holes = 0;
-  std::vector<double> centers;   // 2 per hole
+  std::vector<double> centers;   // dim per hole
   std::vector<int> start, count; // node ranges
 };
 

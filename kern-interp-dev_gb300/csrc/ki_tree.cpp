@@ -9,26 +9,42 @@ namespace ki {
 namespace {
 
 // Touching test of the reference's get_descendent_neighbors
-// (kern_interp/quadtree/quadtree.cpp:292-314): |dc_d| <= (s_a + s_b)/2 + 1e-9.
-bool touching(const Box& a, const Box& b) {
+// (kern_interp/quadtree/quadtree.cpp:292-314): |dc_d| <= (s_a + s_b)/2 + 1e-9
+// in every coordinate.
+bool touching(const Box& a, const Box& b, int dim) {
   double pred = (a.side + b.side) / 2.;
-  return !(std::fabs(a.cx - b.cx) - pred > 1e-9) && !(std::fabs(a.cy - b.cy) - pred > 1e-9);
+  for (int d = 0; d < dim; d++)
+    if (std::fabs(a.c[d] - b.c[d]) - pred > 1e-9) return false;
+  return true;
+}
+
+// Child index of a point (QuadTree::recursive_add / node_subdivide,
+// quadtree.cpp:324-330, 398-405): coordinate d at or above the centre adds
+// 2^(dim-1-d).
+inline int child_of(const double* p, const double* c, int dim) {
+  int ci = 0;
+  for (int d = 0; d < dim; d++)
+    if (p[d] >= c[d]) ci += 1 << (dim - 1 - d);
+  return ci;
 }
 
 }  // namespace
 
-void Tree::build(const double* pts, int n_points_, int sol_dim_, int max_leaf_dofs_) {
+void Tree::build(const double* pts, int n_points_, int dim_, int sol_dim_, int max_leaf_dofs_) {
+  dim = dim_;
   n_points = n_points_;
   sol_dim = sol_dim_;
   n_dofs = n_points * sol_dim;
   max_leaf_dofs = max_leaf_dofs_;
+  if (dim != 2 && dim != 3) throw std::invalid_argument("domain dimension must be 2 or 3");
   if (n_points <= 0) throw std::invalid_argument("no boundary points");
   if (max_leaf_dofs < 1) throw std::invalid_argument("max_leaf_dofs must be positive");
   boxes.clear();
   levels.clear();
+  const int nch = 1 << dim;
 
   double mn = pts[0], mx = pts[0];
-  for (int i = 0; i < 2 * n_points; i++) {
+  for (int i = 0; i < dim * n_points; i++) {
     if (!std::isfinite(pts[i])) throw std::invalid_argument("non-finite boundary coordinate");
     mn = std::min(mn, pts[i]);
     mx = std::max(mx, pts[i]);
@@ -46,7 +62,7 @@ void Tree::build(const double* pts, int n_points_, int sol_dim_, int max_leaf_do
 
   Box root;
   root.level = 0;
-  root.cx = root.cy = (tmin + tmax) / 2.0;
+  for (int d = 0; d < dim; d++) root.c[d] = (tmin + tmax) / 2.0;
   root.side = tmax - tmin;
   root.orig_count = n_dofs;
   boxes.push_back(root);
@@ -59,30 +75,27 @@ void Tree::build(const double* pts, int n_points_, int sol_dim_, int max_leaf_do
       if (boxes[b].orig_count <= max_leaf_dofs) continue;
       boxes[b].leaf = false;
       Range r = range[b];
-      double cx = boxes[b].cx, cy = boxes[b].cy, side = boxes[b].side;
-      int cnt[4] = {0, 0, 0, 0};
-      for (int i = r.lo; i < r.hi; i++) {
-        int p = work[i];
-        int ci = (pts[2 * p] >= cx ? 2 : 0) + (pts[2 * p + 1] >= cy ? 1 : 0);
-        cnt[ci]++;
-      }
-      int start[4];
+      double c[3] = {boxes[b].c[0], boxes[b].c[1], boxes[b].c[2]};
+      double side = boxes[b].side;
+      int cnt[kMaxChildren] = {};
+      for (int i = r.lo; i < r.hi; i++) cnt[child_of(pts + (size_t)dim * work[i], c, dim)]++;
+      int start[kMaxChildren];
       start[0] = r.lo;
-      for (int c = 1; c < 4; c++) start[c] = start[c - 1] + cnt[c - 1];
-      int pos[4] = {start[0], start[1], start[2], start[3]};
+      for (int ci = 1; ci < nch; ci++) start[ci] = start[ci - 1] + cnt[ci - 1];
+      int pos[kMaxChildren];
+      for (int ci = 0; ci < nch; ci++) pos[ci] = start[ci];
       for (int i = r.lo; i < r.hi; i++) {
         int p = work[i];
-        int ci = (pts[2 * p] >= cx ? 2 : 0) + (pts[2 * p + 1] >= cy ? 1 : 0);
-        tmp[pos[ci]++] = p;
+        tmp[pos[child_of(pts + (size_t)dim * p, c, dim)]++] = p;
       }
       std::copy(tmp.begin() + r.lo, tmp.begin() + r.hi, work.begin() + r.lo);
-      for (int ci = 0; ci < 4; ci++) {
+      for (int ci = 0; ci < nch; ci++) {
         Box ch;
         ch.level = (int)l + 1;
         ch.parent = b;
         // child centre exactly as QuadTree::node_subdivide (quadtree.cpp:377-388)
-        ch.cx = cx + ((ci & 2) ? side / 4. : -side / 4.);
-        ch.cy = cy + ((ci & 1) ? side / 4. : -side / 4.);
+        for (int d = 0; d < dim; d++)
+          ch.c[d] = c[d] + ((ci >> (dim - 1 - d)) & 1 ? side / 4. : -side / 4.);
         ch.side = side / 2.0;
         ch.orig_count = cnt[ci] * sol_dim;
         int id = (int)boxes.size();
@@ -108,7 +121,7 @@ void Tree::build(const double* pts, int n_points_, int sol_dim_, int max_leaf_do
       for (int i = range[b].lo; i < range[b].hi; i++)
         for (int s = 0; s < sol_dim; s++) dof_sorted.push_back(work[i] * sol_dim + s);
     } else {
-      for (int ci = 3; ci >= 0; ci--) stack.push_back(bx.child[ci]);
+      for (int ci = nch - 1; ci >= 0; ci--) stack.push_back(bx.child[ci]);
     }
   }
 
@@ -117,31 +130,33 @@ void Tree::build(const double* pts, int n_points_, int sol_dim_, int max_leaf_do
   for (auto& lv : levels)
     for (size_t i = 0; i < lv.size(); i++) boxes[lv[i]].level_pos = (int)i;
 
-  // Neighbours (quadtree.cpp:192-237): same-level touching boxes come from the
-  // parent's same-level neighbours' children; a box's coarser touching leaves
-  // are found among the parent's coarser leaves and the parent's same-level
-  // neighbours that are leaves.
+  // Neighbours (quadtree.cpp:192-237): same-level neighbours come from the
+  // parent's same-level neighbours' children (centre distance below
+  // side*sqrt(dim)); a box's coarser touching leaves are found among the
+  // parent's coarser leaves and the parent's same-level neighbours that are
+  // leaves.
+  const double sq = std::sqrt((double)dim);
   for (size_t l = 1; l < levels.size(); l++) {
     for (int b : levels[l]) {
       Box& bx = boxes[b];
       const Box& par = boxes[bx.parent];
-      for (int ci = 0; ci < 4; ci++)
+      for (int ci = 0; ci < nch; ci++)
         if (par.child[ci] != b) bx.same_nbrs.push_back(par.child[ci]);
       for (int pn : par.same_nbrs) {
         const Box& pb = boxes[pn];
         if (pb.leaf) {
-          if (touching(bx, pb)) bx.coarse_nbrs.push_back(pn);
+          if (touching(bx, pb, dim)) bx.coarse_nbrs.push_back(pn);
           continue;
         }
-        for (int ci = 0; ci < 4; ci++) {
+        for (int ci = 0; ci < nch; ci++) {
           const Box& cb = boxes[pb.child[ci]];
-          double dx = bx.cx - cb.cx, dy = bx.cy - cb.cy;
-          if (std::sqrt(dx * dx + dy * dy) < bx.side * std::sqrt(2.0) + 1e-9)
-            bx.same_nbrs.push_back(pb.child[ci]);
+          double d2 = 0;
+          for (int d = 0; d < dim; d++) d2 += (bx.c[d] - cb.c[d]) * (bx.c[d] - cb.c[d]);
+          if (std::sqrt(d2) < bx.side * sq + 1e-9) bx.same_nbrs.push_back(pb.child[ci]);
         }
       }
       for (int pn : par.coarse_nbrs)
-        if (touching(bx, boxes[pn])) bx.coarse_nbrs.push_back(pn);
+        if (touching(bx, boxes[pn], dim)) bx.coarse_nbrs.push_back(pn);
     }
   }
 }

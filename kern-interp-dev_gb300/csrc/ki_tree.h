@@ -1,12 +1,13 @@
-// Host-side adaptive quadtree over the boundary nodes.
+// Host-side adaptive quadtree (2D) / octree (3D) over the boundary nodes.
 //
 // Restates the tree of the reference's QuadTree (kern_interp/quadtree/
-// quadtree.cpp): the same root box (bounding square of all coordinates
+// quadtree.cpp): the same root box (bounding square/cube of all coordinates
 // +-0.01, :240-267), the same split rule (a box is subdivided while it holds
 // more than max_leaf_dofs DOFs, :336-339 / :409-411), the same child
-// numbering (x >= centre adds 2, y >= centre adds 1, :324-330) and the same
-// neighbour relation (every touching box of the same level plus, for the
-// "near" set, touching leaves of coarser levels, :192-237 / :292-314).
+// numbering (coordinate d >= centre adds 2^(dim-1-d), :324-330 / :378-388)
+// and the same neighbour relation (every box of the same level whose centre
+// lies within side*sqrt(dim), plus, for the "near" set, touching leaves of
+// coarser levels, :192-237 / :292-314).
 //
 // The layout differs on purpose: the tree is built top-down by stable
 // partition instead of point-by-point insertion, boxes of a level are kept in
@@ -20,28 +21,32 @@
 
 namespace ki {
 
+constexpr int kMaxChildren = 8;
+
 struct Box {
   int level = 0;
   int parent = -1;
-  int child[4] = {-1, -1, -1, -1};
+  int child[kMaxChildren] = {-1, -1, -1, -1, -1, -1, -1, -1};
   bool leaf = true;
-  double cx = 0, cy = 0, side = 0;
+  double c[3] = {0, 0, 0};   // centre
+  double side = 0;
   int orig_start = 0;   // leaf DOF range in dof_sorted (leaves only)
   int orig_count = 0;   // DOFs in the box (all boxes)
   int level_pos = 0;    // index within levels[level]
-  std::vector<int> same_nbrs;    // touching boxes of the same level
+  std::vector<int> same_nbrs;    // neighbouring boxes of the same level
   std::vector<int> coarse_nbrs;  // touching leaves of coarser levels
 };
 
 struct Tree {
-  int n_points = 0, sol_dim = 1, n_dofs = 0;
+  int dim = 2, n_points = 0, sol_dim = 1, n_dofs = 0;
   int max_leaf_dofs = 64;
   std::vector<Box> boxes;
   std::vector<std::vector<int>> levels;   // box ids per level, Morton order
   std::vector<int> dof_sorted;            // leaves' DOFs, leaf after leaf
 
-  // points: interleaved (x, y), n_points of them.
-  void build(const double* points, int n_points, int sol_dim, int max_leaf_dofs);
+  int n_children() const { return 1 << dim; }
+  // points: interleaved (x, y[, z]), n_points of them; dim 2 or 3.
+  void build(const double* points, int n_points, int dim, int sol_dim, int max_leaf_dofs);
   int num_levels() const { return (int)levels.size(); }
 };
 

@@ -338,3 +338,91 @@ def star_c1():
     rng = np.random.default_rng(0)
     tg = disc_targets(100, rng, 0.5)
     return prob, src, tg
+
+
+# ------------------------------------------------------------------- 3D --
+
+def fibonacci_sphere(n):
+    """n quasi-uniform unit vectors: z_i = 1 - (2i+1)/n, azimuth i times the
+    golden angle."""
+    i = np.arange(n, dtype=np.float64)
+    z = 1.0 - (2.0 * i + 1.0) / n
+    r = np.sqrt(np.maximum(0.0, 1.0 - z * z))
+    phi = i * np.pi * (3.0 - np.sqrt(5.0))
+    return np.stack([r * np.cos(phi), r * np.sin(phi), z], 1)
+
+
+def ellipsoid(n, axes=(1.0, 0.7, 0.5), center=(0.0, 0.0, 0.0), inward=False):
+    """Ellipsoid surface with semi-axes `axes`: Fibonacci-sphere nodes u_i
+    mapped by x = D u (D = diag(axes)), area weights (4 pi / n) times the
+    mapping's area Jacobian abc |D^-1 u|, unit normals D^-1 u / |D^-1 u|
+    (outward; `inward` flips them, for a hole).  Curvatures are not used by
+    the 3D kernels (the diagonal comes from row sums) and are zero."""
+    u = fibonacci_sphere(n)
+    D = np.asarray(axes, np.float64)
+    g = u / D[None]
+    gn = np.linalg.norm(g, axis=1)
+    pts = u * D[None] + np.asarray(center, np.float64)[None]
+    nrm = g / gn[:, None]
+    if inward:
+        nrm = -nrm
+    w = (4 * np.pi / n) * np.prod(D) * gn
+    return Problem(pts, nrm, w, np.zeros(n), hole_centers=np.zeros((0, 3)), name="ellipsoid")
+
+
+def spheres_with_holes(n_outer, hole_specs, outer_axes=(1.0, 1.0, 1.0)):
+    """Outer ellipsoid (outward normals) with interior spherical holes given as
+    (center, radius, n_nodes) (normals pointing into each hole, the
+    reference's convention for hole boundaries), the nodes of every hole after
+    the outer surface's."""
+    parts = [ellipsoid(n_outer, outer_axes)]
+    starts, counts, centers = [], [], []
+    off = n_outer
+    for c, r, m in hole_specs:
+        parts.append(ellipsoid(m, (r, r, r), center=c, inward=True))
+        starts.append(off)
+        counts.append(m)
+        centers.append(c)
+        off += m
+    return Problem(np.concatenate([p.points for p in parts]),
+                   np.concatenate([p.normals for p in parts]),
+                   np.concatenate([p.weights for p in parts]),
+                   np.zeros(off), hole_centers=np.array(centers, np.float64).reshape(-1, 3),
+                   hole_start=np.array(starts, np.int32), hole_count=np.array(counts, np.int32),
+                   name="spheres_with_holes")
+
+
+def laplace3_source_field(x, sources):
+    """u(x) = 1 / (4 pi |x - y|) for each source y (one column per source)."""
+    d = x[:, None, :] - np.asarray(sources, np.float64)[None]
+    return 1.0 / (4 * np.pi * np.linalg.norm(d, axis=2))
+
+
+def laplace3_source_rhs(prob, sources):
+    return laplace3_source_field(prob.points, sources)
+
+
+def stokeslet3_velocity(x, y0, force):
+    """Velocity of a 3D Stokeslet at y0 with force f (unit viscosity):
+    (1/8pi) (f/|r| + (r.f) r/|r|^3), r = x - y0 (the kernel of the
+    reference's 3D Stokes border columns, kern_interp/linear_solve.cpp:49-63)."""
+    r = x - np.asarray(y0)[None]
+    rn = np.linalg.norm(r, axis=1)
+    f = np.asarray(force, np.float64)
+    return (f[None] / rn[:, None] + r * (r @ f)[:, None] / rn[:, None] ** 3) / (8 * np.pi)
+
+
+def stokes3_rhs(prob, sources, forces):
+    """Boundary velocity (interleaved per node, one column per Stokeslet)."""
+    return np.stack([stokeslet3_velocity(prob.points, y, f).reshape(-1)
+                     for y, f in zip(sources, forces)], 1)
+
+
+def ellipsoid_targets(n, rng, axes=(1.0, 0.7, 0.5), scale=0.5):
+    """n points uniform in the ellipsoid scaled by `scale`."""
+    out = []
+    while len(out) < n:
+        p = rng.uniform(-1, 1, 3)
+        if (p ** 2).sum() < 1:
+            out.append(p * scale * np.asarray(axes))
+    return np.array(out)

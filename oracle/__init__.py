@@ -77,10 +77,15 @@ class _Lib:
         self.solve_fn = f
 
 
-def solve(prob, rhs, tol, threads=1, leaf=64, proxy=128, ratio=2.0, min_compress=64,
+def solve(prob, rhs, tol, threads=1, leaf=64, proxy=None, ratio=2.0, min_compress=64,
           solution_dim=1, pde=0, impl="port"):
     """Factor + solve with the oracle.  rhs: (N, nrhs).  Returns (mu, alpha,
-    stats) with mu (N, nrhs), alpha (n_border, nrhs), stats dict."""
+    stats) with mu (N, nrhs), alpha (n_border, nrhs), stats dict.  The
+    boundary's dimension is prob.points.shape[1]; proxy None takes the
+    reference default (128 in 2D, the fixed 32-point sphere in 3D)."""
+    dim = int(np.asarray(prob.points).shape[1])
+    if proxy is None:
+        proxy = 128 if dim == 2 else 0
     if impl == "port":
         lib = _Lib(build_port(), "kiport", True)
     else:
@@ -88,14 +93,17 @@ def solve(prob, rhs, tol, threads=1, leaf=64, proxy=128, ratio=2.0, min_compress
         spec = importlib.util.spec_from_file_location("_ki_build_ref", os.path.join(HERE, "build_ref.py"))
         br = importlib.util.module_from_spec(spec)
         spec.loader.exec_module(br)
-        lib = _Lib(br.build(leaf=leaf, proxy=proxy, ratio=ratio, min_compress=min_compress),
+        # the reference's 3D proxy sphere is fixed (kern_interp/kernel/kernel.h:44-62):
+        # NUM_PROXY_POINTS only matters in 2D
+        lib = _Lib(br.build(leaf=leaf, proxy=proxy if dim == 2 else 128, ratio=ratio,
+                            min_compress=min_compress),
                    "kiref", False)
     rhs = np.asarray(rhs, dtype=np.float64)
     if rhs.ndim == 1:
         rhs = rhs[:, None]
     N = prob.n * solution_dim
     nrhs = rhs.shape[1]
-    c = 1 if solution_dim == 1 else 3
+    c = 1 if solution_dim == 1 else (3 if dim == 2 else 6)
     nb = c * prob.n_holes
     pts = np.ascontiguousarray(prob.points, np.float64)
     nrm = np.ascontiguousarray(prob.normals, np.float64)
@@ -108,7 +116,7 @@ def solve(prob, rhs, tol, threads=1, leaf=64, proxy=128, ratio=2.0, min_compress
     mu = np.zeros((N, nrhs), order="F")
     alpha = np.zeros((max(nb, 1), nrhs), order="F")
     st = np.zeros(8)
-    args = [prob.n, 2, solution_dim, pde, _dp(pts), _dp(nrm), _dp(wts), _dp(cur),
+    args = [prob.n, dim, solution_dim, pde, _dp(pts), _dp(nrm), _dp(wts), _dp(cur),
             prob.n_holes, _dp(hc), _dp(hs), _dp(hn), _dp(b), nrhs, tol, threads]
     if lib.has_params:
         args += [leaf, proxy, ratio, min_compress]
@@ -126,15 +134,18 @@ def solve(prob, rhs, tol, threads=1, leaf=64, proxy=128, ratio=2.0, min_compress
 
 
 def dense_matrix(prob, solution_dim=1):
-    """Dense Nystrom matrix of the reference kernel (Kernel::operator())."""
+    """Dense Nystrom matrix of the reference kernel (Kernel::operator(); in
+    3D with the row-sum diagonal of a surface without holes)."""
     lib = ctypes.CDLL(build_port())
     N = prob.n * solution_dim
     out = np.zeros((N, N), order="F")
-    lib.kiport_dense.argtypes = [ctypes.c_int, ctypes.c_int] + [_P] * 5
-    lib.kiport_dense(prob.n, solution_dim, _dp(np.ascontiguousarray(prob.points)),
+    dim = int(np.asarray(prob.points).shape[1])
+    lib.kiport_dense_dim.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int] + [_P] * 5
+    curv = prob.curvatures if prob.curvatures is not None else np.zeros(prob.n)
+    lib.kiport_dense_dim(prob.n, dim, solution_dim, _dp(np.ascontiguousarray(prob.points)),
                      _dp(np.ascontiguousarray(prob.normals)),
-                     _dp(np.ascontiguousarray(prob.weights)),
-                     _dp(np.ascontiguousarray(prob.curvatures)), _dp(out))
+                         _dp(np.ascontiguousarray(prob.weights)),
+                         _dp(np.ascontiguousarray(curv)), _dp(out))
     return out
 
 

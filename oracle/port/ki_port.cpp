@@ -181,17 +181,36 @@ int interp_decomp(Mat M, double tol, std::vector<int>* perm, Mat* T) {
 
 // ---------------------------------------------------------------- Kernel --
 struct Geometry {
-  int n_points = 0, sol_dim = 1, pde = 0;
-  const double* pts = nullptr;   // interleaved (x, y)
+  int n_points = 0, dim = 2, sol_dim = 1, pde = 0;
+  const double* pts = nullptr;   // interleaved (x, y[, z])
   const double* nrm = nullptr;   // interleaved
   const double* wts = nullptr;
   const double* curv = nullptr;
+  std::vector<double> diag;      // 3D: 1 (Laplace) or 9 (Stokes) per point
+  std::vector<double> pxy_thetas, pxy_theta_w, pxy_phis, pxy_phi_w;   // 3D proxy sphere
 };
 
-// Kernel::one_d_kern / two_d_kern (kernel/kernel.cpp:33-87).
+// Kernel::one_d_kern / two_d_kern (kernel/kernel.cpp:33-87) and
+// three_d_laplace / three_d_stokes (:89-121).  diag: the source point's 3D
+// diagonal data (nullptr: zeros, as the proxy rows pass).
 inline double entry(const Geometry& g, int tgt_dof, int src_dof, const double* tp,
                     const double* tn, const double* sp, const double* sn, double sw,
-                    double sc) {
+                    double sc, const double* diag = nullptr) {
+  if (g.dim == 3) {
+    double r1 = tp[0] - sp[0], r2 = tp[1] - sp[1], r3 = tp[2] - sp[2];
+    if (g.sol_dim == 1) {
+      if (r1 == 0. && r2 == 0. && r3 == 0.) return diag ? diag[0] : 0.;
+      return -sw * (1.0 / (4 * M_PI)) * (r1 * sn[0] + r2 * sn[1] + r3 * sn[2]) /
+             std::pow(r1 * r1 + r2 * r2 + r3 * r3, 1.5);
+    }
+    int tpar = tgt_dof % 3, spar = src_dof % 3;
+    if (r1 == 0. && r2 == 0. && r3 == 0.) return diag ? diag[3 * tpar + spar] : 0.;
+    double r[3] = {r1, r2, r3};
+    double scale = -3.0 / (4.0 * M_PI);
+    return sw * scale * (r1 * sn[0] + r2 * sn[1] + r3 * sn[2]) /
+               std::pow(r1 * r1 + r2 * r2 + r3 * r3, 2.5) * r[tpar] * r[spar] +
+           sw * tn[tpar] * sn[spar];
+  }
   double r1 = tp[0] - sp[0], r2 = tp[1] - sp[1];
   if (g.sol_dim == 1) {
     if (r1 == 0. && r2 == 0.) return 0.5 + 0.5 * sc * sw * (1.0 / (2 * M_PI));
@@ -211,17 +230,20 @@ inline double entry(const Geometry& g, int tgt_dof, int src_dof, const double* t
          sw * tn[tpar] * sn[spar];
 }
 
-// Kernel::operator() (kernel/kernel.cpp:304-360): dense block K(tgt, src).
+// Kernel::operator() / get_3d (kernel/kernel.cpp:304-429): dense block K(tgt, src).
 Mat kernel_block(const Geometry& g, const std::vector<int>& tgt, const std::vector<int>& src) {
+  const int d = g.dim;
+  const int dpp = d == 3 ? (g.sol_dim == 1 ? 1 : 9) : 0;
   Mat R((int)tgt.size(), (int)src.size());
   for (size_t j = 0; j < src.size(); j++) {
     int sp = src[j] / g.sol_dim;
-    const double* s = g.pts + 2 * sp;
-    const double* sn = g.nrm + 2 * sp;
+    const double* s = g.pts + d * sp;
+    const double* sn = g.nrm + d * sp;
     double sw = g.wts[sp], sc = g.curv ? g.curv[sp] : 0.;
+    const double* dg = dpp ? g.diag.data() + (size_t)dpp * sp : nullptr;
     for (size_t i = 0; i < tgt.size(); i++) {
       int tpi = tgt[i] / g.sol_dim;
-      R((int)i, (int)j) = entry(g, tgt[i], src[j], g.pts + 2 * tpi, g.nrm + 2 * tpi, s, sn, sw, sc);
+      R((int)i, (int)j) = entry(g, tgt[i], src[j], g.pts + d * tpi, g.nrm + d * tpi, s, sn, sw, sc, dg);
     }
   }
   return R;
@@ -256,11 +278,149 @@ Mat proxy_block(const Geometry& g, const double* c, int P, double r, const std::
   return R;
 }
 
+// Kernel::get_proxy_mat3d (kernel/kernel.cpp:720-790): theta x phi grid,
+// theta outer; rows [0, c P) box -> proxy, [c P, 2 c P) proxy -> box.
+Mat proxy_block3(const Geometry& g, const double* c, double r, const std::vector<int>& box) {
+  std::vector<double> pp, pn, pw;
+  for (size_t i = 0; i < g.pxy_thetas.size(); i++) {
+    double theta = g.pxy_thetas[i];
+    for (size_t j = 0; j < g.pxy_phis.size(); j++) {
+      double phi = g.pxy_phis[j];
+      pp.push_back(c[0] + r * std::sin(phi) * std::cos(theta));
+      pp.push_back(c[1] + r * std::sin(phi) * std::sin(theta));
+      pp.push_back(c[2] + r * std::cos(phi));
+      pn.push_back(std::sin(phi) * std::cos(theta));
+      pn.push_back(std::sin(phi) * std::sin(theta));
+      pn.push_back(std::cos(phi));
+      pw.push_back(std::pow(r, 2) * g.pxy_phi_w[j] * g.pxy_theta_w[i]);
+    }
+  }
+  const int P = (int)pw.size(), cd = g.sol_dim;
+  const int lda = 2 * cd * P;
+  Mat R(lda, (int)box.size());
+  for (size_t j = 0; j < box.size(); j++) {
+    int bp = box[j] / cd;
+    const double* b = g.pts + 3 * bp;
+    const double* bn = g.nrm + 3 * bp;
+    double bw = g.wts[bp];
+    for (int i = 0; i < P; i++) {
+      const double* q = pp.data() + 3 * i;
+      const double* qn = pn.data() + 3 * i;
+      if (cd == 1) {
+        R(i, (int)j) = entry(g, 0, 0, q, qn, b, bn, bw, 0);
+        R(P + i, (int)j) = entry(g, 0, 0, b, bn, q, qn, pw[i], 0);
+      } else {
+        for (int par = 0; par < 3; par++) {
+          R(3 * i + par, (int)j) = entry(g, par, box[j], q, qn, b, bn, bw, 0);
+          R(3 * P + 3 * i + par, (int)j) = entry(g, box[j], par, b, bn, q, qn, pw[i], 0);
+        }
+      }
+    }
+  }
+  return R;
+}
+
+// Gauss-Legendre nodes/weights on [a, b], ascending, by Newton's method on
+// the Legendre recurrence (the reference calls cgqf for the proxy
+// latitudes, kernel/kernel.h:44-62).
+void gauss_legendre(int n, double a, double b, std::vector<double>* x, std::vector<double>* w) {
+  x->assign(n, 0.);
+  w->assign(n, 0.);
+  for (int i = 0; i < n; i++) {
+    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), pd = 1.;
+    for (int it = 0; it < 100; it++) {
+      double p0 = 1., p1 = z;
+      for (int k = 2; k <= n; k++) {
+        double p2 = ((2. * k - 1.) * z * p1 - (k - 1.) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      pd = n == 1 ? 1. : n * (z * p1 - p0) / (z * z - 1.);
+      double dz = p1 / pd;
+      z -= dz;
+      if (std::fabs(dz) < 1e-16) break;
+    }
+    double p0 = 1., p1 = z;
+    for (int k = 2; k <= n; k++) {
+      double p2 = ((2. * k - 1.) * z * p1 - (k - 1.) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    pd = n == 1 ? 1. : n * (z * p1 - p0) / (z * z - 1.);
+    (*x)[n - 1 - i] = 0.5 * (b - a) * z + 0.5 * (b + a);
+    (*w)[n - 1 - i] = (b - a) / ((1. - z * z) * pd * pd);
+  }
+}
+
+// The Kernel constructor's proxy sphere (kernel/kernel.h:44-62): n_theta
+// equispaced longitudes, n_theta/2 Gauss-Legendre latitudes on [0, pi],
+// latitude weight w_j sin(phi_j), longitude weight 2 pi / n_theta.
+void proxy_sphere(Geometry* g, int n_theta) {
+  int n_phi = n_theta / 2;
+  std::vector<double> ph, pw;
+  gauss_legendre(n_phi, 0., M_PI, &ph, &pw);
+  g->pxy_thetas.clear(); g->pxy_theta_w.clear(); g->pxy_phis.clear(); g->pxy_phi_w.clear();
+  for (int i = 0; i < n_theta; i++) {
+    g->pxy_thetas.push_back(2 * M_PI * i * (1.0 / n_theta));
+    g->pxy_theta_w.push_back(2 * M_PI / n_theta);
+  }
+  for (int j = 0; j < n_phi; j++) {
+    g->pxy_phis.push_back(ph[j]);
+    g->pxy_phi_w.push_back(pw[j] * std::sin(ph[j]));
+  }
+}
+
+// Kernel::compute_diag_entries_3dlaplace / _3dstokes (kernel/kernel.cpp:124-301):
+// row sums over the point's own surface (outer nodes [0, n_outer), or its
+// hole's range), then 1 - sum / I - sum on the outer surface, -sum on holes.
+void compute_diag3(Geometry* g, int n_outer, const std::vector<int>& hs, const std::vector<int>& hn,
+                   int threads) {
+  const int n = g->n_points;
+  const bool lap = g->sol_dim == 1;
+  g->diag.assign((size_t)n * (lap ? 1 : 9), 0.);
+  std::vector<int> lo(n), hi(n);
+  for (int p = 0; p < n_outer; p++) { lo[p] = 0; hi[p] = n_outer; }
+  for (size_t h = 0; h < hs.size(); h++)
+    for (int p = hs[h]; p < hs[h] + hn[h]; p++) { lo[p] = hs[h]; hi[p] = hs[h] + hn[h]; }
+  const double* P = g->pts;
+  const double* Nn = g->nrm;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 16)
+  for (int t = 0; t < n; t++) {
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int s = lo[t]; s < hi[t]; s++) {
+      if (s == t) continue;
+      double r1 = P[3 * t] - P[3 * s], r2 = P[3 * t + 1] - P[3 * s + 1], r3 = P[3 * t + 2] - P[3 * s + 2];
+      double sn[3] = {Nn[3 * s], Nn[3 * s + 1], Nn[3 * s + 2]};
+      double sw = g->wts[s];
+      if (lap) {
+        acc[0] += (-sw * (1.0 / (4 * M_PI)) * (r1 * sn[0] + r2 * sn[1] + r3 * sn[2]) /
+                   std::pow(r1 * r1 + r2 * r2 + r3 * r3, 1.5));
+      } else {
+        double r[3] = {r1, r2, r3};
+        double tn[3] = {Nn[3 * t], Nn[3 * t + 1], Nn[3 * t + 2]};
+        double scale = -3.0 / (4.0 * M_PI);
+        for (int a = 0; a < 3; a++)
+          for (int b = 0; b < 3; b++)
+            acc[3 * a + b] += sw * scale * (r1 * sn[0] + r2 * sn[1] + r3 * sn[2]) /
+                                  std::pow(r1 * r1 + r2 * r2 + r3 * r3, 2.5) * r[a] * r[b] +
+                              sw * tn[a] * sn[b];
+      }
+    }
+    double one = t < n_outer ? 1. : 0.;
+    if (lap) {
+      g->diag[t] = one - acc[0];
+    } else {
+      for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) g->diag[9 * (size_t)t + 3 * a + b] = (a == b ? one : 0.) - acc[3 * a + b];
+    }
+  }
+}
+
 // ------------------------------------------------------------------ Tree --
 struct Node {
   int level = 0;
   bool leaf = true, compressed = false;
-  double c[2] = {0, 0}, side = 0;
+  double c[3] = {0, 0, 0}, side = 0;
   int parent = -1;
   std::vector<int> children, neighbors;
   std::vector<int> orig, act, skel, red, near, perm;
@@ -287,34 +447,44 @@ struct Tree {
     return (int)nodes.size() - 1;
   }
 
+  // Child index (quadtree/quadtree.cpp:324-330, 398-405): coordinate d at or
+  // above the centre adds 2^(dim-1-d).
+  int child_index(int pt, const double* c) const {
+    int ci = 0;
+    for (int d = 0; d < g.dim; d++)
+      if (g.pts[g.dim * pt + d] >= c[d]) ci += 1 << (g.dim - 1 - d);
+    return ci;
+  }
+
   // QuadTree::node_subdivide (quadtree/quadtree.cpp:372-413).
   void subdivide(int ni) {
     nodes[ni].leaf = false;
-    int kids[4];
-    for (int ci = 0; ci < 4; ci++) {
+    const int nch = 1 << g.dim;
+    int kids[8];
+    for (int ci = 0; ci < nch; ci++) {
       int k = new_node();
       kids[ci] = k;
       Node& n = nodes[ni];
       Node& ch = nodes[k];
-      ch.c[0] = n.c[0] + ((ci & 2) ? n.side / 4. : -n.side / 4.);
-      ch.c[1] = n.c[1] + ((ci & 1) ? n.side / 4. : -n.side / 4.);
+      for (int d = 0; d < g.dim; d++)
+        ch.c[d] = n.c[d] + (((ci >> (g.dim - 1 - d)) & 1) ? n.side / 4. : -n.side / 4.);
       ch.level = n.level + 1;
       ch.side = n.side / 2.0;
       ch.parent = ni;
     }
     Node& n = nodes[ni];
-    for (int ci = 0; ci < 4; ci++) n.children.push_back(kids[ci]);
+    for (int ci = 0; ci < nch; ci++) n.children.push_back(kids[ci]);
     if ((int)levels.size() < n.level + 2) levels.emplace_back();
-    for (int ci = 0; ci < 4; ci++) levels[n.level + 1].push_back(kids[ci]);
+    for (int ci = 0; ci < nch; ci++) levels[n.level + 1].push_back(kids[ci]);
     std::vector<int> orig = n.orig;
-    double cx = n.c[0], cy = n.c[1];
+    double c[3] = {n.c[0], n.c[1], n.c[2]};
     for (size_t idx = 0; idx < orig.size(); idx += g.sol_dim) {
       int dof = orig[idx];
       int pt = dof / g.sol_dim;
-      int ci = (g.pts[2 * pt] >= cx ? 2 : 0) + (g.pts[2 * pt + 1] >= cy ? 1 : 0);
+      int ci = child_index(pt, c);
       for (int s = 0; s < g.sol_dim; s++) nodes[kids[ci]].orig.push_back(dof + s);
     }
-    for (int ci = 0; ci < 4; ci++)
+    for (int ci = 0; ci < nch; ci++)
       if ((int)nodes[kids[ci]].orig.size() > p.leaf) subdivide(kids[ci]);
   }
 
@@ -322,8 +492,7 @@ struct Tree {
   void add(int ni, int pt) {
     for (int s = 0; s < g.sol_dim; s++) nodes[ni].orig.push_back(g.sol_dim * pt + s);
     if (!nodes[ni].leaf) {
-      int ci = (g.pts[2 * pt] >= nodes[ni].c[0] ? 2 : 0) + (g.pts[2 * pt + 1] >= nodes[ni].c[1] ? 1 : 0);
-      add(nodes[ni].children[ci], pt);
+      add(nodes[ni].children[child_index(pt, nodes[ni].c)], pt);
     } else if ((int)nodes[ni].orig.size() > p.leaf) {
       subdivide(ni);
     }
@@ -332,7 +501,7 @@ struct Tree {
   // QuadTree::get_descendent_neighbors (quadtree/quadtree.cpp:292-314).
   void descendent_neighbors(int big, int small) {
     bool nb = true;
-    for (int d = 0; d < 2; d++) {
+    for (int d = 0; d < g.dim; d++) {
       double dist = std::fabs(nodes[big].c[d] - nodes[small].c[d]);
       double pred = (nodes[big].side + nodes[small].side) / 2.;
       if (dist - pred > 1e-9) {
@@ -358,9 +527,12 @@ struct Tree {
           for (int pn : std::vector<int>(nodes[par].neighbors)) {
             for (int cousin : nodes[pn].children) {
               if (nodes[cousin].level != nodes[a].level) continue;
-              double dx = nodes[a].c[0] - nodes[cousin].c[0], dy = nodes[a].c[1] - nodes[cousin].c[1];
-              double dist = std::sqrt(dx * dx + dy * dy);
-              if (dist < nodes[a].side * std::sqrt(2.0) + 1e-9) nodes[a].neighbors.push_back(cousin);
+              double dist = 0.;
+              for (int d = 0; d < g.dim; d++)
+                dist += std::pow(nodes[a].c[d] - nodes[cousin].c[d], 2);
+              dist = std::sqrt(dist);
+              if (dist < nodes[a].side * std::sqrt((double)g.dim) + 1e-9)
+                nodes[a].neighbors.push_back(cousin);
             }
           }
         }
@@ -378,13 +550,13 @@ struct Tree {
   // QuadTree::initialize_tree (quadtree/quadtree.cpp:240-287).
   void build() {
     double mn = g.pts[0], mx = g.pts[0];
-    for (int i = 0; i < 2 * g.n_points; i++) {
+    for (int i = 0; i < g.dim * g.n_points; i++) {
       mn = std::min(mn, g.pts[i]);
       mx = std::max(mx, g.pts[i]);
     }
     double tmin = mn - 0.01, tmax = mx + 0.01;
     int root = new_node();
-    nodes[root].c[0] = nodes[root].c[1] = (tmin + tmax) / 2.0;
+    for (int d = 0; d < g.dim; d++) nodes[root].c[d] = (tmin + tmax) / 2.0;
     nodes[root].side = tmax - tmin;
     levels.push_back({root});
     nodes.reserve(8 * (g.n_points * g.sol_dim / std::max(1, p.leaf) + 4));
@@ -431,7 +603,7 @@ struct Tree {
     const std::vector<int>& A = n.act;
     std::vector<int> outside;
     bool proxy = true;
-    if (n.level == 1 || n.level == 2) {
+    if (n.level == 1 || (n.level == 2 && g.dim < 3)) {
       proxy = false;
       for (int o : levels[n.level])
         if (o != ni) outside.insert(outside.end(), nodes[o].act.begin(), nodes[o].act.end());
@@ -441,11 +613,12 @@ struct Tree {
             if (nodes[o].leaf) outside.insert(outside.end(), nodes[o].orig.begin(), nodes[o].orig.end());
       }
     } else {
-      double rad = std::sqrt(2.0) * p.ratio * (n.side / 2);
+      double rad = std::sqrt((double)g.dim) * p.ratio * (n.side / 2);
       for (int dof : n.near) {
         int pt = dof / g.sol_dim;
-        double dx = n.c[0] - g.pts[2 * pt], dy = n.c[1] - g.pts[2 * pt + 1];
-        double dist = std::sqrt(dx * dx + dy * dy);
+        double dist = 0.;
+        for (int d = 0; d < g.dim; d++) dist += std::pow(n.c[d] - g.pts[g.dim * pt + d], 2);
+        dist = std::sqrt(dist);
         if (dist < rad) outside.push_back(dof);
       }
     }
@@ -453,8 +626,8 @@ struct Tree {
     Mat Kai = kernel_block(g, A, outside);
     Mat pxy;
     if (proxy) {
-      double rad = (n.side / 2) * std::sqrt(2.0) * p.ratio;
-      pxy = proxy_block(g, n.c, p.proxy, rad, A);
+      double rad = (n.side / 2) * std::sqrt((double)g.dim) * p.ratio;
+      pxy = g.dim == 3 ? proxy_block3(g, n.c, rad, A) : proxy_block(g, n.c, p.proxy, rad, A);
     }
     int o = (int)outside.size();
     Mat M(2 * o + pxy.h, (int)A.size());
@@ -763,6 +936,10 @@ thread_local std::string g_err;
 
 extern "C" {
 
+int kiport_dense_dim(int n_points, int domain_dim, int solution_dim, const double* points,
+                     const double* normals, const double* weights, const double* curvatures,
+                     double* out);
+
 const char* kiport_last_error() { return g_err.c_str(); }
 
 // Factor + solve, the same contract as the reference driver's kiref_solve:
@@ -776,11 +953,12 @@ int kiport_solve(int n_points, int domain_dim, int solution_dim, int pde,
                  double id_tol, int threads, int leaf, int proxy, double ratio,
                  int min_compress, double* mu_out, double* alpha_out, double* stats) {
   try {
-    if (domain_dim != 2) throw std::runtime_error("only 2D boundaries are supported");
+    if (domain_dim != 2 && domain_dim != 3) throw std::runtime_error("domain_dim must be 2 or 3");
     if (!lapack().dgeqp3 || !lapack().dgemm)
       throw std::runtime_error("LAPACK symbols not found: load OpenBLAS first");
     Tree t;
     t.g.n_points = n_points;
+    t.g.dim = domain_dim;
     t.g.sol_dim = solution_dim;
     t.g.pde = pde;
     t.g.pts = points;
@@ -790,13 +968,66 @@ int kiport_solve(int n_points, int domain_dim, int solution_dim, int pde,
     t.p.tol = id_tol;
     t.p.threads = std::max(1, threads);
     t.p.leaf = leaf;
+    if (proxy <= 0) proxy = domain_dim == 2 ? 128 : 32;
     t.p.proxy = proxy;
     t.p.ratio = ratio;
     t.p.min_compress = min_compress;
     int N = n_points * solution_dim;
     double t0 = omp_get_wtime();
+    if (domain_dim == 3) {
+      int q = (int)std::lround(std::sqrt(proxy / 2.0));
+      if (2 * q * q != proxy) throw std::runtime_error("3D proxy count must be 2 q^2");
+      proxy_sphere(&t.g, 2 * q);
+      std::vector<int> hs(hole_start, hole_start + n_holes), hn(hole_count, hole_count + n_holes);
+      compute_diag3(&t.g, n_holes > 0 ? hole_start[0] : n_points, hs, hn, t.p.threads);
+    }
     t.build();
-    if (n_holes > 0) {
+    if (n_holes > 0 && domain_dim == 3) {
+      // initialize_U_mat / initialize_Psi_mat, 3D (linear_solve.cpp:26-36, 49-76,
+      // 114-129, 146-163), hole membership from node ranges
+      int c = solution_dim == 1 ? 1 : 6;
+      t.U = Mat(N, c * n_holes);
+      t.Psi = Mat(c * n_holes, N);
+      for (int h = 0; h < n_holes; h++) {
+        const double* hc = hole_centers + 3 * h;
+        for (int p = 0; p < n_points; p++) {
+          double r[3] = {points[3 * p] - hc[0], points[3 * p + 1] - hc[1], points[3 * p + 2] - hc[2]};
+          double rn = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+          if (solution_dim == 1) {
+            t.U(p, h) = 1.0 / rn;
+            continue;
+          }
+          for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++)
+              t.U(3 * p + a, 6 * h + b) =
+                  (1.0 / (8.0 * M_PI)) * ((a == b ? 1 : 0) / rn + r[a] * r[b] / std::pow(rn, 3));
+          double rot = -1.0 / (8.0 * M_PI * std::pow(rn, 3));
+          t.U(3 * p, 6 * h + 4) = rot * (-r[2]);
+          t.U(3 * p, 6 * h + 5) = rot * (r[1]);
+          t.U(3 * p + 1, 6 * h + 3) = rot * (r[2]);
+          t.U(3 * p + 1, 6 * h + 5) = rot * (-r[0]);
+          t.U(3 * p + 2, 6 * h + 3) = rot * (-r[1]);
+          t.U(3 * p + 2, 6 * h + 4) = rot * (r[0]);
+        }
+        for (int p = hole_start[h]; p < hole_start[h] + hole_count[h]; p++) {
+          double w = weights[p];
+          if (solution_dim == 1) {
+            t.Psi(h, p) = w;
+            continue;
+          }
+          double r[3] = {points[3 * p] - hc[0], points[3 * p + 1] - hc[1], points[3 * p + 2] - hc[2]};
+          t.Psi(6 * h, 3 * p) = w;
+          t.Psi(6 * h + 1, 3 * p + 1) = w;
+          t.Psi(6 * h + 2, 3 * p + 2) = w;
+          t.Psi(6 * h + 4, 3 * p) = -w * (-r[2]);
+          t.Psi(6 * h + 5, 3 * p) = -w * (r[1]);
+          t.Psi(6 * h + 3, 3 * p + 1) = -w * (r[2]);
+          t.Psi(6 * h + 5, 3 * p + 1) = -w * (-r[0]);
+          t.Psi(6 * h + 3, 3 * p + 2) = -w * (-r[1]);
+          t.Psi(6 * h + 4, 3 * p + 2) = -w * (r[0]);
+        }
+      }
+    } else if (n_holes > 0) {
       int c = solution_dim == 1 ? 1 : 3;
       t.U = Mat(N, c * n_holes);
       t.Psi = Mat(c * n_holes, N);
@@ -865,16 +1096,25 @@ int kiport_solve(int n_points, int domain_dim, int solution_dim, int pde,
   }
 }
 
-// Dense kernel matrix K(all, all), column-major (Kernel::operator()).
+// Dense kernel matrix K(all, all), column-major (Kernel::operator()); 3D
+// with the diagonal of compute_diag3 (no holes).
 int kiport_dense(int n_points, int solution_dim, const double* points, const double* normals,
                  const double* weights, const double* curvatures, double* out) {
+  return kiport_dense_dim(n_points, 2, solution_dim, points, normals, weights, curvatures, out);
+}
+
+int kiport_dense_dim(int n_points, int domain_dim, int solution_dim, const double* points,
+                     const double* normals, const double* weights, const double* curvatures,
+                     double* out) {
   Geometry g;
   g.n_points = n_points;
+  g.dim = domain_dim;
   g.sol_dim = solution_dim;
   g.pts = points;
   g.nrm = normals;
   g.wts = weights;
   g.curv = curvatures;
+  if (domain_dim == 3) compute_diag3(&g, n_points, {}, {}, 8);
   int N = n_points * solution_dim;
   std::vector<int> all(N);
   for (int i = 0; i < N; i++) all[i] = i;

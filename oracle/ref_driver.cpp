@@ -81,13 +81,20 @@ int kiref_solve(int n_points, int domain_dim, int solution_dim, int pde,
 
   kern_interp::Kernel kernel(solution_dim, d, (kern_interp::Kernel::Pde)pde,
                              &boundary, std::vector<double>());
+  // 3D diagonals, as the reference's 3D drivers do before factorizing
+  // (kern_interp/experiments/ex1_concentric_spheres.cpp:88)
+  if (d == 3) {
+    if (solution_dim == 1) kernel.compute_diag_entries_3dlaplace(&boundary);
+    else kernel.compute_diag_entries_3dstokes(&boundary);
+  }
   kern_interp::QuadTree quadtree;
   quadtree.initialize_tree(&boundary, solution_dim, d);
 
   if (n_holes > 0) {
     quadtree.U = kern_interp::initialize_U_mat(kernel.pde, boundary.holes,
                                                boundary.points, d);
-    // Psi from node ranges (Laplace: weights; Stokes 2D: reference layout).
+    // Psi from node ranges (Laplace: weights; Stokes: reference layout,
+    // kern_interp/linear_solve.cpp:146-177).
     int c = quadtree.U.width() / n_holes;
     kern_interp::ki_Mat Psi(c * n_holes, N);
     for (int h = 0; h < n_holes; h++) {
@@ -95,6 +102,18 @@ int kiref_solve(int n_points, int domain_dim, int solution_dim, int pde,
         double w = weights[p];
         if (solution_dim == 1) {
           Psi.set(h, p, w);
+        } else if (d == 3) {
+          double r[3];
+          for (int q = 0; q < 3; q++) r[q] = points[3 * p + q] - hole_centers[3 * h + q];
+          Psi.set(6 * h, 3 * p, w);
+          Psi.set(6 * h + 1, 3 * p + 1, w);
+          Psi.set(6 * h + 2, 3 * p + 2, w);
+          Psi.set(6 * h + 4, 3 * p, -w * (-r[2]));
+          Psi.set(6 * h + 5, 3 * p, -w * (r[1]));
+          Psi.set(6 * h + 3, 3 * p + 1, -w * (r[2]));
+          Psi.set(6 * h + 5, 3 * p + 1, -w * (-r[0]));
+          Psi.set(6 * h + 3, 3 * p + 2, -w * (-r[1]));
+          Psi.set(6 * h + 4, 3 * p + 2, -w * (r[0]));
         } else {
           double x = points[2 * p], y = points[2 * p + 1];
           Psi.set(3 * h, 2 * p, w);
@@ -158,8 +177,13 @@ int kiref_dense(int n_points, int domain_dim, int solution_dim, int pde,
   boundary.normals.assign(normals, normals + (size_t)n_points * d);
   boundary.weights.assign(weights, weights + n_points);
   if (curvatures) boundary.curvatures.assign(curvatures, curvatures + n_points);
+  boundary.num_outer_nodes = n_points;
   kern_interp::Kernel kernel(solution_dim, d, (kern_interp::Kernel::Pde)pde,
                              &boundary, std::vector<double>());
+  if (d == 3) {
+    if (solution_dim == 1) kernel.compute_diag_entries_3dlaplace(&boundary);
+    else kernel.compute_diag_entries_3dstokes(&boundary);
+  }
   std::vector<int> all(N);
   for (int i = 0; i < N; i++) all[i] = i;
   kern_interp::ki_Mat K = kernel(all, all);

@@ -44,7 +44,7 @@ def golden_cases():
     for name, _, _, p in make_golden.cases():
         data = np.load(os.path.join(GOLDEN, name + ".npz"))
         prob = geo.Problem(data["points"], data["normals"], data["weights"], data["curvatures"],
-                           hole_centers=data["hole_centers"].reshape(-1, 2),
+                           hole_centers=data["hole_centers"].reshape(-1, data["points"].shape[1]),
                            hole_start=data["hole_start"], hole_count=data["hole_count"], name=name)
         rhs = data["rhs"]
         out[name] = (prob, rhs, p, data, make_golden.input_hash(prob, rhs))

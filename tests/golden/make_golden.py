@@ -73,12 +73,31 @@ def cases():
     prob = g.star(64, 16, amp=0.2, k=3)
     out.append(("stokes_star_2048", prob, stokes_rhs(prob),
                 dict(tol=1e-10, proxy=128, ratio=2.0, leaf=64, min_compress=64, solution_dim=2, pde=3)))
+    # 3D (octree, row-sum diagonals, proxy sphere; reference default proxy)
+    prob = g.ellipsoid(3000, (1.0, 0.7, 0.5))
+    out.append(("laplace3_ellipsoid_3000", prob,
+                g.laplace3_source_rhs(prob, np.array([[2.0, 1.0, 1.0], [-1.5, 2.0, 0.5]])),
+                dict(tol=1e-8, proxy=0, ratio=2.0, leaf=64, min_compress=64, solution_dim=1, pde=0)))
+    prob = g.ellipsoid(1500, (1.0, 0.6, 0.4))
+    out.append(("stokes3_ellipsoid_1500", prob,
+                g.stokes3_rhs(prob, np.array([[2.0, 1.0, 1.0]]), np.array([[1.0, 0.5, -0.3]])),
+                dict(tol=1e-7, proxy=0, ratio=2.0, leaf=64, min_compress=64, solution_dim=3, pde=3)))
+    prob = g.spheres_with_holes(2400, [((0.2, 0.1, -0.1), 0.3, 600)])
+    out.append(("laplace3_sphere_hole", prob,
+                g.laplace3_source_rhs(prob, np.array([[2.0, 1.0, 1.0]])),
+                dict(tol=1e-8, proxy=0, ratio=2.0, leaf=64, min_compress=64, solution_dim=1, pde=0)))
+    prob = g.spheres_with_holes(1200, [((0.1, -0.2, 0.1), 0.35, 400)])
+    out.append(("stokes3_sphere_hole", prob,
+                g.stokes3_rhs(prob, np.array([[2.0, 1.0, 1.0]]), np.array([[1.0, 0.5, -0.3]])),
+                dict(tol=1e-7, proxy=0, ratio=2.0, leaf=64, min_compress=64, solution_dim=3, pde=3)))
     return out
 
 
-def main():
+def main(only=None):
     import oracle
     for name, prob, rhs, p in cases():
+        if only and name not in only:
+            continue
         mu_cols, al_cols = [], []
         st = None
         for c in range(rhs.shape[1]):   # the reference's bordered solve handles one column
@@ -99,4 +118,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or None)

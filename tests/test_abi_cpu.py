@@ -44,7 +44,10 @@ def _desc(pkg, prob, **kw):
     return pkg._Desc(**args), keep
 
 
-@pytest.mark.parametrize("bad", [dict(domain_dimension=3), dict(n_points=0), dict(id_tol=0.0),
+@pytest.mark.parametrize("bad", [dict(domain_dimension=4), dict(domain_dimension=1),
+                                 dict(domain_dimension=3, num_proxy_points=30),
+                                 dict(domain_dimension=3, pde=3, solution_dimension=2),
+                                 dict(n_points=0), dict(id_tol=0.0),
                                  dict(id_tol=float("nan")), dict(pde=1), dict(precision=7),
                                  dict(solution_dimension=2), dict(max_leaf_dofs=-1),
                                  dict(n_holes=1)])

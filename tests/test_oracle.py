@@ -23,7 +23,9 @@ def test_generators_reproduce_fixture_inputs(golden_cases, pkg):
 
 @pytest.mark.parametrize("name", ["star_c1", "star_1024_default", "circle_1000",
                                   "star_2048_tol1e-4", "star_64_root_leaf", "disc6_8k",
-                                  "stokes_star_2048"])
+                                  "stokes_star_2048", "laplace3_ellipsoid_3000",
+                                  "stokes3_ellipsoid_1500", "laplace3_sphere_hole",
+                                  "stokes3_sphere_hole"])
 def test_port_matches_reference_fixture(golden_cases, oracle_mod, name):
     prob, rhs, p, data, _ = golden_cases[name]
     mu, alpha, st = oracle_mod.solve(prob, rhs, p["tol"], threads=4, leaf=p["leaf"],
