@@ -38,9 +38,19 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp32"])
+    ap.add_argument("--target", type=float, default=1e-8,
+                    help="relative residual the refined forms reach")
+    ap.add_argument("--mixed-tol", type=float, default=1e-6,
+                    help="ID tolerance of the FP32 factorization of the mixed form")
+    ap.add_argument("--max-steps", type=int, default=10)
+    ap.add_argument("--no-refine", action="store_true",
+                    help="fp64: one plain solve (the reference's arithmetic), no refinement")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="mixed: do not also time the FP64 form at the same residual")
     ap.add_argument("--workload", default="laplace2d_disc_ellipses",
-                    choices=["laplace2d_disc_ellipses", "stokes2d_disc_circles", "laplace2d_star"])
+                    choices=["laplace2d_disc_ellipses", "stokes2d_disc_circles", "laplace2d_star",
+                             "laplace3d_ellipsoid"])
     ap.add_argument("--unknowns", dest="n", type=int, default=1 << 20)
     ap.add_argument("--holes", type=int, default=64)
     ap.add_argument("--nrhs", type=int, default=32)
@@ -64,6 +74,10 @@ WORKLOAD_NOTES = {
                              "(radii U(0.005,0.02), gap 0.005, seed 3), 16-node GL panels, "
                              "Stokeslet at (2.5,0) force (1,0.5) plus seeded Stokeslets",
     "laplace2d_star": "2D Laplace star r=1+0.3cos(5t), 16-node GL panels, source (3,3)",
+    "laplace3d_ellipsoid": "3D Laplace Dirichlet double layer on the ellipsoid (1,0.7,0.5), "
+                           "Fibonacci nodes with area-Jacobian weights, row-sum diagonal, octree "
+                           "leaf 128, 512-point proxy sphere, unit source at (2,1,1) plus seeded "
+                           "sources at |y| in [2.5,4]",
 }
 
 
@@ -75,7 +89,18 @@ class Workload:
         g = pkg.geometry
         self.name = name
         self.sol_dim, self.pde = 1, pkg.PDE_LAPLACE
-        if name == "stokes2d_disc_circles":
+        self.dim, self.leaf, self.proxy = 2, 64, 0
+        if name == "laplace3d_ellipsoid":
+            self.dim, self.leaf, self.proxy = 3, 128, 512
+            self.prob = g.ellipsoid(n, (1.0, 0.7, 0.5))
+            rng = np.random.default_rng(2)
+            extra = g.random_sources(max(0, nrhs - 1), rng)
+            ang = rng.uniform(-1, 1, len(extra))
+            extra3 = np.concatenate([extra * np.sqrt(1 - ang ** 2)[:, None],
+                                     (np.hypot(*extra.T) * ang)[:, None]], 1)
+            self.src = np.concatenate([[[2.0, 1.0, 1.0]], extra3])[:nrhs]
+            self.rhs = g.laplace3_source_rhs(self.prob, self.src)
+        elif name == "stokes2d_disc_circles":
             self.sol_dim, self.pde = 2, pkg.PDE_STOKES
             self.prob = g.disc_with_circles(n // 2, holes, seed=3)
             self.src, self.frc = g.stokes_c3_sources(nrhs)
@@ -95,15 +120,27 @@ class Workload:
             self.target_radius = 1.9
         self.n = self.prob.n * self.sol_dim
 
+    @property
+    def n_border(self):
+        c = 1 if self.sol_dim == 1 else (3 if self.dim == 2 else 6)
+        return self.prob.n_holes * c
+
+    def oracle_kw(self):
+        return dict(solution_dim=self.sol_dim, pde=self.pde, leaf=self.leaf,
+                    proxy=self.proxy or None)
+
     def factor_kw(self, tol, precision):
         p = self.prob
-        kw = dict(id_tol=tol, solution_dimension=self.sol_dim, pde=self.pde, precision=precision)
+        kw = dict(id_tol=tol, solution_dimension=self.sol_dim, pde=self.pde, precision=precision,
+                  max_leaf_dofs=self.leaf, num_proxy_points=self.proxy)
         if p.n_holes:
             kw.update(hole_centers=p.hole_centers, hole_start=p.hole_start, hole_count=p.hole_count)
         return kw
 
     def field(self, pkg, targets):
         g = pkg.geometry
+        if self.dim == 3:
+            return g.laplace3_source_field(targets, self.src)
         if self.sol_dim == 2:
             return np.stack([g.stokeslet_velocity(targets, y, f).reshape(-1)
                              for y, f in zip(self.src, self.frc)], 1)
@@ -111,6 +148,8 @@ class Workload:
 
     def targets(self, pkg, count, rng):
         g = pkg.geometry
+        if self.dim == 3:
+            return g.ellipsoid_targets(count, rng, (1.0, 0.7, 0.5))
         if self.prob.n_holes:
             return g.domain_targets(self.prob, count, rng, radius=self.target_radius)
         return g.disc_targets(count, rng, self.target_radius)
@@ -190,10 +229,10 @@ def residual_sample(fac, prob, rhs, mu, alpha, nrows, seed=9):
     return float(est.max()), float(np.median(est))
 
 
-def cpu_oracle_run(prob, rhs, tol, threads, sol_dim=1, pde=0):
+def cpu_oracle_run(prob, rhs, tol, threads, **kw):
     import oracle
     t0 = time.perf_counter()
-    mu, alpha, st = oracle.solve(prob, rhs, tol, threads=threads, solution_dim=sol_dim, pde=pde)
+    mu, alpha, st = oracle.solve(prob, rhs, tol, threads=threads, **kw)
     t1 = time.perf_counter()
     return t1 - t0, st, mu, alpha
 
@@ -211,10 +250,10 @@ def run_reference(args, rank, world):
     wl = Workload(pkg, args.workload, n, args.holes, args.nrhs)
     n = wl.n
     for _ in range(max(0, min(args.warmup, 1))):
-        cpu_oracle_run(wl.prob, wl.rhs, args.tol, threads, wl.sol_dim, wl.pde)
+        cpu_oracle_run(wl.prob, wl.rhs, args.tol, threads, **wl.oracle_kw())
     times = []
     for _ in range(args.steps):
-        dt, st, _, _ = cpu_oracle_run(wl.prob, wl.rhs, args.tol, threads, wl.sol_dim, wl.pde)
+        dt, st, _, _ = cpu_oracle_run(wl.prob, wl.rhs, args.tol, threads, **wl.oracle_kw())
         times.append(dt)
     t = float(np.mean(times))
     value = n * args.nrhs / t
@@ -249,59 +288,92 @@ def main():
     torch.cuda.set_device(local)
     import __graft_entry__ as g
     pkg = g.load_package()
-    prec = pkg.PRECISION_FP64 if args.precision == "fp64" else pkg.PRECISION_FP32
     wl = Workload(pkg, args.workload, args.n, args.holes, args.nrhs)
     prob, src, rhs = wl.prob, wl.src, wl.rhs
     N = wl.n
     nrhs = args.nrhs
-    kw = wl.factor_kw(args.tol, prec)
     # inputs resident in HBM for the `value` leg
     rhs_f = np.asfortranarray(rhs)
     d_b = torch.from_numpy(rhs_f.T.copy()).to("cuda")          # (nrhs, N): column c at row c
     d_x = torch.empty_like(d_b)
-    nb = prob.n_holes * (1 if wl.sol_dim == 1 else 3)
+    nb = wl.n_border
     d_a = torch.empty((nrhs, max(1, nb)), dtype=torch.float64, device="cuda")
     pin_b = torch.from_numpy(rhs_f.T.copy()).pin_memory()
     pin_x = torch.empty_like(pin_b).pin_memory()
     pin_a = torch.empty((nrhs, max(1, nb)), dtype=torch.float64).pin_memory()
-
-    def step_device():
-        fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, **kw)
-        fac.solve_device(d_b.data_ptr(), d_x.data_ptr(), nrhs, d_a.data_ptr())
-        torch.cuda.synchronize()
-        return fac
-
-    def step_host():
-        fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, **kw)
-        lib = pkg.load_library()
-        pkg._check(lib.ki_solve(fac._h, pin_b.data_ptr(), N, nrhs, pin_x.data_ptr(), N,
-                                pin_a.data_ptr(), max(1, nb)))
-        return fac
-
     barrier = rep.barrier
 
-    for _ in range(args.warmup):
-        f = step_device()
-        f.close()
-    # ---- value: device-resident right-hand sides
-    barrier()
-    torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    stage_runs = []
-    with ClockSampler(local) as clk:
-        ev0.record()
-        for _ in range(args.steps):
-            fac = step_device()
-            prof = fac.profile()
-            stage_runs.append(prof["factor"])
-            level_stats = prof.get("levels", [])
-            info = fac.info()
-            fac.close()
-        ev1.record()
+    def form(precision):
+        """(factor kwargs, refine?) of a form: mixed = FP32 factorization at
+        --mixed-tol refined against the FP64 operator to --target; fp64 =
+        FP64 factorization at --tol, refined to --target unless --no-refine;
+        fp32 = plain FP32 factorization and solve."""
+        if precision == "mixed":
+            return wl.factor_kw(args.mixed_tol, pkg.PRECISION_FP32), True
+        if precision == "fp64":
+            return wl.factor_kw(args.tol, pkg.PRECISION_FP64), not args.no_refine
+        return wl.factor_kw(args.tol, pkg.PRECISION_FP32), False
+
+    def run_form(precision, steps, warmup):
+        kw, refine = form(precision)
+        infos = []
+
+        def step_device():
+            fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, **kw)
+            if refine:
+                infos.append(fac.solve_refined_device(d_b.data_ptr(), d_x.data_ptr(), nrhs,
+                                                      d_a.data_ptr(), tol=args.target,
+                                                      max_steps=args.max_steps))
+            else:
+                fac.solve_device(d_b.data_ptr(), d_x.data_ptr(), nrhs, d_a.data_ptr())
+            torch.cuda.synchronize()
+            return fac
+
+        def step_host():
+            fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, **kw)
+            lib = pkg.load_library()
+            if refine:
+                info = pkg._RefineInfo()
+                pkg._check(lib.ki_solve_refined(fac._h, pin_b.data_ptr(), N, nrhs,
+                                                pin_x.data_ptr(), N, pin_a.data_ptr(), max(1, nb),
+                                                args.target, args.max_steps,
+                                                pkg.ctypes.byref(info)))
+            else:
+                pkg._check(lib.ki_solve(fac._h, pin_b.data_ptr(), N, nrhs, pin_x.data_ptr(), N,
+                                        pin_a.data_ptr(), max(1, nb)))
+            return fac
+
+        for _ in range(warmup):
+            step_device().close()
+        infos.clear()
+        # ---- value: device-resident right-hand sides
+        barrier()
         torch.cuda.synchronize()
-    barrier()
-    t_dev = rep.max_over_ranks(ev0.elapsed_time(ev1) / 1e3 / args.steps, device="cuda")
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        stage_runs, level_stats, info = [], [], None
+        with ClockSampler(local) as clk:
+            ev0.record()
+            for _ in range(steps):
+                fac = step_device()
+                prof = fac.profile()
+                stage_runs.append(prof["factor"])
+                level_stats = prof.get("levels", [])
+                info = fac.info()
+                fac.close()
+            ev1.record()
+            torch.cuda.synchronize()
+        barrier()
+        t_dev = rep.max_over_ranks(ev0.elapsed_time(ev1) / 1e3 / steps, device="cuda")
+        return dict(kw=kw, refine=refine, t_dev=t_dev, stage_runs=stage_runs,
+                    level_stats=level_stats, info=info, infos=list(infos), clk=clk.summary(),
+                    step_host=step_host)
+
+    main_form = run_form(args.precision, args.steps, args.warmup)
+    kw, refine = main_form["kw"], main_form["refine"]
+    t_dev, stage_runs = main_form["t_dev"], main_form["stage_runs"]
+    level_stats, info = main_form["level_stats"], main_form["info"]
     # ---- e2e: host buffers through the C ABI
+    step_host = main_form["step_host"]
     barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -314,11 +386,26 @@ def main():
     barrier()
     t_e2e = rep.max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps, device="cuda")
 
+    # ---- the FP64 form at the same target residual, for the comparison
+    compare = None
+    if args.precision == "mixed" and not args.no_compare:
+        c = run_form("fp64", max(1, min(args.steps, 2)), 1)
+        compare = {"form": "fp64 factorization at ID tol %g, refined to %g" % (args.tol, args.target),
+                   "ms_per_step": c["t_dev"] * 1e3, "value": N * nrhs * world / c["t_dev"],
+                   "unit": "DOF/s", "refine": c["infos"][-1] if c["infos"] else None,
+                   "speedup_of_mixed": c["t_dev"] / t_dev}
+
     # ---- accuracy of the last solution (sampled dense FP64 residual, analytic field)
     fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, **kw)
     fac.set_profiling(True)
-    res = fac.solve(rhs)
-    mu, alpha = res if isinstance(res, tuple) else (res, None)
+    rinfo = None
+    if refine:
+        out = fac.solve_refined(rhs, tol=args.target, max_steps=args.max_steps)
+        rinfo = out[-1]
+        mu, alpha = out[0], (out[1] if len(out) == 3 else None)
+    else:
+        res = fac.solve(rhs)
+        mu, alpha = res if isinstance(res, tuple) else (res, None)
     solve_prof = fac.profile()["solve"]
     rmax, rmed = residual_sample(fac, prob, rhs, mu, alpha, args.residual_rows)
     rng = np.random.default_rng(4)
@@ -375,7 +462,7 @@ def main():
             w2 = Workload(pkg, args.workload, n_cpu, args.holes, nrhs)
             n_cpu = w2.n
             thr = os.cpu_count() or 1
-            dt, st, _, _ = cpu_oracle_run(w2.prob, w2.rhs, args.tol, thr, w2.sol_dim, w2.pde)
+            dt, st, _, _ = cpu_oracle_run(w2.prob, w2.rhs, args.tol, thr, **w2.oracle_kw())
             cpu = {"value": n_cpu * nrhs / dt, "unit": "DOF/s", "cores": thr, "kind": "port",
                    "sample": "%d unknowns of the same geometry family, %d rhs, one factor+solve (%.1f s)"
                              % (n_cpu, nrhs, dt)}
@@ -384,31 +471,53 @@ def main():
                    "sample": "failed: %s" % e}
 
     units = N * nrhs * world
-    h2d = N * nrhs * 8 + prob.n * 6 * 8
+    h2d = N * nrhs * 8 + prob.n * (2 * wl.dim + 2) * 8
     d2h = N * nrhs * 8 + max(1, nb) * nrhs * 8
+    if refine:
+        metric = "factor+solve DOF/s (unknowns x rhs / s) at %g relative residual" % args.target
+    else:
+        metric = "factor+solve DOF/s (unknowns x rhs / s) at ID tol %g" % args.tol
+    dtype = {"fp64": "f64", "fp32": "f32",
+             "mixed": "f32 factorization and solves, f64 residuals (FMM)"}[args.precision]
+    refines = main_form["infos"]
     line = {
-        "metric": "factor+solve DOF/s (unknowns x rhs / s) at ID tol %g" % args.tol,
+        "metric": metric,
         "value": units / t_dev, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_dev * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f32 factor, f64 residual check",
+        "dtype": dtype,
         "data": "synthetic (seeded boundary and sources)",
         "config": {"workload": args.workload, "holes": args.holes, "unknowns": N,
                    "description": WORKLOAD_NOTES[args.workload],
-                   "nrhs": nrhs, "id_tol": args.tol, "precision": args.precision,
-                   "leaf": 64, "proxy": 128, "l2": "factor working set >> 129 MB L2 (no flush needed)",
+                   "nrhs": nrhs, "precision": args.precision,
+                   "id_tol": args.mixed_tol if args.precision == "mixed" else args.tol,
+                   "target_residual": args.target if refine else None,
+                   "leaf": wl.leaf, "proxy": wl.proxy or (128 if wl.dim == 2 else 32),
+                   "l2": "factor working set >> 129 MB L2 (no flush needed)",
                    "levels": info["n_levels"], "root_skeleton": info["n_root"],
                    "compressed_boxes": info["n_compressed"]},
         "e2e": {"value": units / t_e2e, "unit": "DOF/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e * 1e3},
         "gpu_launches": launches,
+        "gpu_launches_note": "factorization launches per step (CUDA-event stage records); each "
+                             "refinement step adds one solve's sweep launches, the FMM's ~3 per "
+                             "tree level and ~8 residual-norm launches" if refine else
+                             "factorization launches per step (CUDA-event stage records)",
+        "refinement": {"steps_per_solve": [r["steps"] for r in refines],
+                       "residual_first_solve": [r["residual0"] for r in refines],
+                       "residual_final": [r["residual"] for r in refines],
+                       "residual_operator": "FMM (2D Laplace)" if (wl.dim == 2 and wl.sol_dim == 1
+                                                                  and N >= 4096) else "dense FP64"}
+        if refine else None,
+        "fp64_form_same_residual": compare,
         "roofline": roofline,
         "stages": stage_table,
         "solve_stages": solve_prof,
         "level_stats": level_stats,
         "accuracy": {"residual_est_max": rmax, "residual_est_median": rmed,
-                     "residual_rows_sampled": args.residual_rows, "pde_rel_err": pde_err},
-        "clocks": clk.summary(),
+                     "residual_rows_sampled": args.residual_rows, "pde_rel_err": pde_err,
+                     "refined_residual": rinfo["residual"] if rinfo else None},
+        "clocks": main_form["clk"],
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)

@@ -152,6 +152,20 @@ int ki_apply(ki_factor* f, const double* x, int ldx, int ncols, const double* al
              int ldalpha, double* y, int ldy);
 
 /*
+ * The same product by a fast multipole method (2D Laplace problems only,
+ * KI_ERR_STATE otherwise): uniform-depth quadtree, 24-term Laurent/Taylor
+ * expansions of the Cauchy-sum form of the double layer, direct near field
+ * with the exact Nystrom entries; relative error ~1e-12.  O(n_dofs * ncols)
+ * work.  No reference counterpart (the reference's residual and forward
+ * evaluation are dense, kern_interp/linear_solve.cpp:339-426,
+ * kern_interp/kernel/kernel.cpp:799-825); it serves the residuals of
+ * ki_solve_refined, whose dense O(n_dofs^2) product is out of reach at a
+ * million unknowns.
+ */
+int ki_apply_fmm(ki_factor* f, const double* x, int ldx, int ncols, const double* alpha,
+                 int ldalpha, double* y, int ldy);
+
+/*
  * The same restricted to the listed DOFs: y (nrows x ncols, ldy) = rows of
  * K x (+ U alpha).  Cost O(nrows * n_dofs * ncols): a sampled residual check
  * at sizes where the full dense product is out of reach.
@@ -168,6 +182,40 @@ int ki_apply_rows(ki_factor* f, const int* rows, int nrows, const double* x, int
 int ki_eval_targets(ki_factor* f, const double* targets, int n_targets, const double* mu,
                     int ldmu, int ncols, const double* alpha, int ldalpha, double* out,
                     int ldout);
+
+/* Outcome of a refined solve. */
+typedef struct {
+  int steps;          /* refinement corrections applied after the first solve */
+  double residual0;   /* max over columns of ||[b;0] - A[x;alpha]|| / ||b|| after the first solve */
+  double residual;    /* the same after the last correction */
+} ki_refine_info;
+
+/*
+ * Solve to a relative residual `tol` by iterative refinement: x0 = M^-1 b
+ * with the handle's factorization M (FP32 or FP64), then, while the
+ * largest column residual ||[b;0] - A[x;alpha]|| / ||b|| of the FP64
+ * operator A (the dense Nystrom matrix K, bordered by [U; Psi -I] when the
+ * problem has holes) exceeds tol and fewer than max_steps corrections were
+ * made, [x;alpha] += M^-1 r.  No reference counterpart: the reference
+ * solves once with its FP64 factorization (linear_solve,
+ * kern_interp/linear_solve.cpp:202-227) and checks the residual separately
+ * (solve_err, :339-426).  HOST buffers as in ki_solve.  The residual's
+ * operator product is the FMM of ki_apply_fmm for 2D Laplace problems with
+ * at least 4096 unknowns (O(n_dofs * nrhs) per step), else the dense FP64
+ * product (O(n_dofs^2 * nrhs)); the environment variable
+ * KI_RESIDUAL_APPLY=dense|fmm overrides the choice.
+ */
+int ki_solve_refined(ki_factor* f, const double* b, int ldb, int nrhs, double* x, int ldx,
+                     double* alpha, int ldalpha, double tol, int max_steps, ki_refine_info* info);
+
+/*
+ * The same on DEVICE buffers with leading dimensions n_dofs (b, x) and
+ * n_border (alpha; required when the problem has holes), on `stream`
+ * (NULL: the handle's stream); returns after the stream has finished.
+ */
+int ki_solve_refined_device(ki_factor* f, const double* d_b, int nrhs, double* d_x,
+                            double* d_alpha, double tol, int max_steps, ki_refine_info* info,
+                            void* stream);
 
 /*
  * Per-stage device times (CUDA events on the handle's stream) as a JSON

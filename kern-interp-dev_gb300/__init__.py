@@ -30,7 +30,8 @@ PRECISION_FP64, PRECISION_FP32 = 0, 1
 EXPORTED = ["ki_factor_create", "ki_factor_destroy", "ki_factor_get_info", "ki_solve",
             "ki_solve_device", "ki_apply", "ki_eval_targets", "ki_last_error", "ki_version",
             "ki_factor_get_profile", "ki_factor_set_profiling", "ki_apply_rows",
-            "ki_measure_fma_peak"]
+            "ki_measure_fma_peak", "ki_solve_refined", "ki_solve_refined_device",
+            "ki_solve_device_noalloc", "ki_apply_fmm"]
 
 
 class KiError(RuntimeError):
@@ -49,6 +50,11 @@ class _Desc(ctypes.Structure):
                 ("max_leaf_dofs", ctypes.c_int), ("num_proxy_points", ctypes.c_int),
                 ("radius_ratio", ctypes.c_double), ("min_dofs_to_compress", ctypes.c_int),
                 ("id_tol", ctypes.c_double), ("precision", ctypes.c_int)]
+
+
+class _RefineInfo(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int), ("residual0", ctypes.c_double),
+                ("residual", ctypes.c_double)]
 
 
 class _Info(ctypes.Structure):
@@ -79,9 +85,14 @@ def load_library(path=None):
     lib.ki_solve_device.argtypes = [V, V, I, I, V, I, V, I, V]
     lib.ki_apply.argtypes = [V, V, I, I, V, I, V, I]
     lib.ki_eval_targets.argtypes = [V, V, I, V, I, I, V, I, V, I]
+    lib.ki_apply_fmm.argtypes = [V, V, I, I, V, I, V, I]
     lib.ki_apply_rows.argtypes = [V, V, I, V, I, I, V, I, V, I]
     lib.ki_factor_get_profile.argtypes = [V, ctypes.c_char_p, I]
     lib.ki_factor_set_profiling.argtypes = [V, I]
+    lib.ki_solve_refined.argtypes = [V, V, I, I, V, I, V, I, ctypes.c_double, I,
+                                     ctypes.POINTER(_RefineInfo)]
+    lib.ki_solve_refined_device.argtypes = [V, V, I, V, V, ctypes.c_double, I,
+                                            ctypes.POINTER(_RefineInfo), V]
     lib.ki_measure_fma_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     lib.ki_last_error.restype = ctypes.c_char_p
     lib.ki_version.restype = ctypes.c_char_p
@@ -180,6 +191,34 @@ class Factor:
             return x, (A[:, 0] if vec else A)
         return x
 
+    def solve_refined(self, b, tol=1e-8, max_steps=10):
+        """Iterative refinement against the FP64 operator (ki_solve_refined):
+        returns (x[, alpha], info dict with steps, residual0, residual)."""
+        b = np.asarray(b, np.float64)
+        vec = b.ndim == 1
+        B = np.asfortranarray(b.reshape(self.n_dofs, -1))
+        nrhs = B.shape[1]
+        X = np.zeros_like(B, order="F")
+        A = np.zeros((max(1, self.n_border), nrhs), order="F")
+        info = _RefineInfo()
+        _check(load_library().ki_solve_refined(self._h, _ptr(B), self.n_dofs, nrhs, _ptr(X),
+                                               self.n_dofs, _ptr(A), max(1, self.n_border),
+                                               tol, max_steps, ctypes.byref(info)))
+        res = dict(steps=info.steps, residual0=info.residual0, residual=info.residual)
+        x = X[:, 0] if vec else X
+        if self.n_border:
+            return x, (A[:, 0] if vec else A), res
+        return x, res
+
+    def solve_refined_device(self, d_b, d_x, nrhs, d_alpha=0, tol=1e-8, max_steps=10, stream=0):
+        """Device-pointer refined solve (column-major, ld = n_dofs / n_border)."""
+        info = _RefineInfo()
+        _check(load_library().ki_solve_refined_device(
+            self._h, ctypes.c_void_p(d_b), nrhs, ctypes.c_void_p(d_x),
+            ctypes.c_void_p(d_alpha) if d_alpha else None, tol, max_steps, ctypes.byref(info),
+            ctypes.c_void_p(stream) if stream else None))
+        return dict(steps=info.steps, residual0=info.residual0, residual=info.residual)
+
     def solve_device(self, d_b, d_x, nrhs, d_alpha=0, stream=0):
         """Device-pointer solve (integers: cudaMalloc'd addresses, column-major)."""
         _check(load_library().ki_solve_device(self._h, ctypes.c_void_p(d_b), self.n_dofs, nrhs,
@@ -199,6 +238,19 @@ class Factor:
             A = np.asfortranarray(np.asarray(alpha, np.float64).reshape(self.n_border, -1))
         _check(load_library().ki_apply(self._h, _ptr(X), self.n_dofs, X.shape[1], _ptr(A),
                                        max(1, self.n_border), _ptr(Y), self.n_dofs))
+        return Y[:, 0] if vec else Y
+
+    def apply_fmm(self, x, alpha=None):
+        """K x (+ U alpha) by the fast multipole method (2D Laplace)."""
+        x = np.asarray(x, np.float64)
+        vec = x.ndim == 1
+        X = np.asfortranarray(x.reshape(self.n_dofs, -1))
+        Y = np.zeros_like(X, order="F")
+        A = None
+        if alpha is not None:
+            A = np.asfortranarray(np.asarray(alpha, np.float64).reshape(self.n_border, -1))
+        _check(load_library().ki_apply_fmm(self._h, _ptr(X), self.n_dofs, X.shape[1], _ptr(A),
+                                           max(1, self.n_border), _ptr(Y), self.n_dofs))
         return Y[:, 0] if vec else Y
 
     def apply_rows(self, rows, x, alpha=None):

@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -15,6 +16,7 @@
 #include "../../include/ki_gpu.h"
 #include "ki_common.cuh"
 #include "ki_factor.h"
+#include "ki_fmm.h"
 
 namespace {
 
@@ -277,12 +279,20 @@ struct ki_factor {
   // FP64 geometry on the device (apply / evaluation)
   double* d_geo = nullptr;
   double* d_holes = nullptr;
+  double* d_pts = nullptr;     // interleaved coordinates (dim per point)
+  int* d_hstart = nullptr;     // hole node ranges
+  int* d_hcount = nullptr;
   ki::Points<double> P{};
+  // fast FP64 operator apply (2D Laplace), built on first use
+  std::unique_ptr<ki::Fmm2d, ki::Fmm2dDeleter> fmm;
   ~ki_factor() {
+    fmm.reset();
     f64.reset();
     f32.reset();
     if (d_geo) cudaFree(d_geo);
     if (d_holes) cudaFree(d_holes);
+    if (d_pts) cudaFree(d_pts);
+    if (d_hstart) cudaFree(d_hstart);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -459,6 +469,282 @@ double fma_peak_gflops(int sms, int iters) {
   return 2.0 * 8 * (double)iters * blocks * threads / (ms * 1e-3) / 1e9;
 }
 
+// ---------------------------------------------------------------------------
+// Iterative refinement with an FP64 residual.  The bordered operator
+// [K U; Psi -I] (the reference's multiply connected system,
+// kern_interp/skel_factorization/skel_factorization.cpp:781-1141; plain K
+// without holes) is applied in FP64; the factorization (FP32 or FP64) solves
+// for the correction.
+
+// Entry (border row k of one hole, DOF component comp) of Psi
+// (initialize_Psi_mat, kern_interp/linear_solve.cpp:110-199): x absolute
+// coordinates, r = x - hole centre.
+__device__ double psi_entry(int dim, int sol_dim, int k, int comp, double w, const double* x,
+                            const double* r) {
+  if (sol_dim == 1) return w;
+  if (dim == 2) {
+    if (k < 2) return comp == k ? w : 0.0;
+    return comp == 0 ? w * x[1] : -w * x[0];
+  }
+  if (k < 3) return comp == k ? w : 0.0;
+  const int b = k - 3;
+  if (comp == b) return 0.0;
+  const int o = 3 - comp - b;
+  const double sgn = ((comp + 1) % 3 == b) ? -1.0 : 1.0;
+  return -w * sgn * r[o];
+}
+
+// y2 (n_border x ncols, column-major) = Psi mu - alpha: one block per
+// (border row, column), the hole's nodes summed in a fixed order.
+__global__ void k_psi_apply(const double* pts, const double* w, int dim, int sol_dim,
+                            const double* hc, const int* hstart, const int* hcount, int cph,
+                            const double* mu, int ldmu, const double* alpha, int lda, double* y2,
+                            int ldy) {
+  __shared__ double red[256];
+  const int row = blockIdx.x, c = blockIdx.y;
+  const int h = row / cph, k = row - cph * h;
+  double acc = 0.0;
+  for (int p = hstart[h] + threadIdx.x; p < hstart[h] + hcount[h]; p += blockDim.x) {
+    double x[3] = {pts[(size_t)dim * p], pts[(size_t)dim * p + 1],
+                   dim == 3 ? pts[3 * (size_t)p + 2] : 0.0};
+    double r[3];
+    for (int d = 0; d < dim; d++) r[d] = x[d] - hc[dim * h + d];
+    for (int comp = 0; comp < sol_dim; comp++)
+      acc += psi_entry(dim, sol_dim, k, comp, w[p], x, r) * mu[(size_t)p * sol_dim + comp + (size_t)ldmu * c];
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) y2[row + (size_t)ldy * c] = red[0] - alpha[row + (size_t)lda * c];
+}
+
+// Per-column sums of squares of an (n x ncols, ld) column-major array:
+// partial sums per block (fixed order), then a fixed-order final sum.
+constexpr int kNormBlocks = 64;
+__global__ void k_colsq_partial(const double* a, int n, int ld, double* part) {
+  __shared__ double red[256];
+  const int c = blockIdx.y;
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double v = a[i + (size_t)ld * c];
+    acc += v * v;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x + (size_t)gridDim.x * c] = red[0];
+}
+
+__global__ void k_colsq_final(const double* part, int nparts, int ncols, double* out, int accumulate) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncols) return;
+  double s = 0.0;
+  for (int q = 0; q < nparts; q++) s += part[q + (size_t)nparts * c];
+  out[c] = accumulate ? out[c] + s : s;
+}
+
+// r = b - y (b may be null: r = -y), column-major with leading dimensions.
+__global__ void k_residual(const double* b, int ldb, const double* y, int ldy, int n, int ncols,
+                           double* r, int ldr) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * ncols;
+       e += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(e % n), c = (int)(e / n);
+    r[i + (size_t)ldr * c] = (b ? b[i + (size_t)ldb * c] : 0.0) - y[i + (size_t)ldy * c];
+  }
+}
+
+// x (column-major, ldx) += d (DOF-major in precision T, ld = ncols).
+template <typename T>
+__global__ void k_add_dofmajor(const T* d, int n, int ncols, double* x, int ldx) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * ncols;
+       e += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(e % n), c = (int)(e / n);
+    x[i + (size_t)ldx * c] += double(d[(size_t)i * ncols + c]);
+  }
+}
+
+// column-major (ld) FP64 -> row-major (n x ncols) precision T, and back with +=.
+template <typename T>
+__global__ void k_to_rowmajor(const double* a, int lda, int n, int ncols, T* out) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * ncols; e += gridDim.x * blockDim.x) {
+    int i = e % n, c = e / n;
+    out[(size_t)i * ncols + c] = T(a[i + (size_t)lda * c]);
+  }
+}
+
+template <typename T>
+__global__ void k_add_rowmajor(const T* d, int n, int ncols, double* a, int lda) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * ncols; e += gridDim.x * blockDim.x) {
+    int i = e % n, c = e / n;
+    a[i + (size_t)lda * c] += double(d[(size_t)i * ncols + c]);
+  }
+}
+
+// y1 = K mu + U alpha, y2 = Psi mu - alpha (FP64, column-major, ld = N / nb).
+void apply_bordered(ki_factor* f, const double* mu, const double* alpha, int ncols, double* y1,
+                    double* y2, cudaStream_t s);
+
+// Per-column relative residual of [mu; alpha] for right-hand side b:
+// returns max over columns of ||[b;0] - A[mu;alpha]|| / ||b||, leaves r1/r2.
+double residual_norms(ki_factor* f, const double* b, const double* mu, const double* alpha,
+                      int ncols, double* r1, double* r2, double* work, std::vector<double>* rel,
+                      cudaStream_t s) {
+  const int N = f->n_dofs, nb = f->n_border;
+  apply_bordered(f, mu, alpha, ncols, r1, r2, s);
+  k_residual<<<grid_for((size_t)N * ncols), 256, 0, s>>>(b, N, r1, N, N, ncols, r1, N);
+  if (nb > 0) k_residual<<<grid_for((size_t)nb * ncols), 256, 0, s>>>(nullptr, 0, r2, nb, nb, ncols, r2, nb);
+  KI_CHECK_CUDA(cudaGetLastError());
+  // work: part (kNormBlocks x ncols) | sq_r (ncols) | sq_b (ncols)
+  double* part = work;
+  double* sq = work + (size_t)kNormBlocks * ncols;
+  double* sqb = sq + ncols;
+  k_colsq_partial<<<dim3(kNormBlocks, ncols), 256, 0, s>>>(r1, N, N, part);
+  k_colsq_final<<<(ncols + 127) / 128, 128, 0, s>>>(part, kNormBlocks, ncols, sq, 0);
+  if (nb > 0) {
+    k_colsq_partial<<<dim3(1, ncols), 256, 0, s>>>(r2, nb, nb, part);
+    k_colsq_final<<<(ncols + 127) / 128, 128, 0, s>>>(part, 1, ncols, sq, 1);
+  }
+  k_colsq_partial<<<dim3(kNormBlocks, ncols), 256, 0, s>>>(b, N, N, part);
+  k_colsq_final<<<(ncols + 127) / 128, 128, 0, s>>>(part, kNormBlocks, ncols, sqb, 0);
+  KI_CHECK_CUDA(cudaGetLastError());
+  std::vector<double> h(2 * (size_t)ncols);
+  KI_CHECK_CUDA(cudaMemcpyAsync(h.data(), sq, sizeof(double) * 2 * ncols, cudaMemcpyDeviceToHost, s));
+  KI_CHECK_CUDA(cudaStreamSynchronize(s));
+  double worst = 0.0;
+  rel->assign(ncols, 0.0);
+  for (int c = 0; c < ncols; c++) {
+    double v = h[ncols + c] > 0 ? std::sqrt(h[c] / h[ncols + c]) : std::sqrt(h[c]);
+    (*rel)[c] = v;
+    worst = std::max(worst, v);
+  }
+  return worst;
+}
+
+// One correction: [mu; alpha] += M^-1 [r1; r2], M the factorization (precision T).
+template <typename T>
+void correct(ki_factor* f, ki::Factorization<T>& F, const double* r1, const double* r2, int ncols,
+             double* mu, double* alpha, cudaStream_t s) {
+  const int N = f->n_dofs, nb = f->n_border;
+  DevBuf<T> work((size_t)N * ncols, s), al((size_t)std::max(1, nb) * ncols, s),
+      g((size_t)std::max(1, nb) * ncols, s);
+  k_to_dofmajor<double, T><<<grid_for((size_t)N * ncols), 256, 0, s>>>(r1, N, N, ncols, work.p);
+  if (nb > 0) k_to_rowmajor<T><<<grid_for((size_t)nb * ncols), 256, 0, s>>>(r2, nb, nb, ncols, g.p);
+  KI_CHECK_CUDA(cudaGetLastError());
+  cudaStream_t saved = F.stream;
+  F.stream = s;
+  try {
+    ki::solve_device<T>(F, work.p, ncols, al.p, nb > 0 ? g.p : nullptr);
+  } catch (...) {
+    F.stream = saved;
+    throw;
+  }
+  F.stream = saved;
+  k_add_dofmajor<T><<<grid_for((size_t)N * ncols), 256, 0, s>>>(work.p, N, ncols, mu, N);
+  if (nb > 0) k_add_rowmajor<T><<<grid_for((size_t)nb * ncols), 256, 0, s>>>(al.p, nb, ncols, alpha, nb);
+  KI_CHECK_CUDA(cudaGetLastError());
+}
+
+// Refined solve on device buffers (b, mu: N x ncols, alpha: nb x ncols,
+// column-major with ld = N / nb).
+void refined_solve(ki_factor* f, const double* b, int ncols, double* mu, double* alpha,
+                   double tol, int max_steps, ki_refine_info* info, cudaStream_t s) {
+  const int N = f->n_dofs, nb = f->n_border;
+  DevBuf<double> r1((size_t)N * ncols, s), r2((size_t)std::max(1, nb) * ncols, s),
+      work((size_t)(kNormBlocks + 2) * ncols, s);
+  KI_CHECK_CUDA(cudaMemsetAsync(mu, 0, sizeof(double) * (size_t)N * ncols, s));
+  if (nb > 0) KI_CHECK_CUDA(cudaMemsetAsync(alpha, 0, sizeof(double) * (size_t)nb * ncols, s));
+  KI_CHECK_CUDA(cudaMemcpyAsync(r1.p, b, sizeof(double) * (size_t)N * ncols, cudaMemcpyDeviceToDevice, s));
+  if (nb > 0) KI_CHECK_CUDA(cudaMemsetAsync(r2.p, 0, sizeof(double) * (size_t)nb * ncols, s));
+  auto corr = [&] {
+    if (f->f64) correct<double>(f, *f->f64, r1.p, r2.p, ncols, mu, alpha, s);
+    else correct<float>(f, *f->f32, r1.p, r2.p, ncols, mu, alpha, s);
+  };
+  corr();   // x0 = M^-1 b
+  std::vector<double> rel;
+  double res = residual_norms(f, b, mu, alpha, ncols, r1.p, r2.p, work.p, &rel, s);
+  info->residual0 = res;
+  int steps = 0;
+  while (res > tol && steps < max_steps) {
+    corr();
+    steps++;
+    res = residual_norms(f, b, mu, alpha, ncols, r1.p, r2.p, work.p, &rel, s);
+  }
+  info->steps = steps;
+  info->residual = res;
+}
+
+}  // namespace
+
+// The bordered FP64 operator: K by the FMM (2D Laplace, n_dofs >= 4096 or
+// KI_RESIDUAL_APPLY=fmm) or the dense Nystrom apply (one thread per target
+// DOF, sources through shared memory; KI_RESIDUAL_APPLY=dense forces it),
+// border columns, Psi rows.
+namespace {
+bool fmm_capable(const ki_factor* f) { return f->dim == 2 && f->sol_dim == 1; }
+
+ki::Fmm2d& fmm_for(ki_factor* f, cudaStream_t s) {
+  if (!f->fmm) {
+    // geometry back from the device copy (the handle keeps no host arrays)
+    const int n = f->n_points;
+    std::vector<double> geo((size_t)6 * n), pts(2 * (size_t)n), nrm(2 * (size_t)n);
+    KI_CHECK_CUDA(cudaMemcpyAsync(geo.data(), f->d_geo, sizeof(double) * geo.size(),
+                                  cudaMemcpyDeviceToHost, s));
+    KI_CHECK_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < n; i++) {
+      pts[2 * i] = geo[i];
+      pts[2 * i + 1] = geo[n + i];
+      nrm[2 * i] = geo[2 * (size_t)n + i];
+      nrm[2 * i + 1] = geo[3 * (size_t)n + i];
+    }
+    int p = 24;
+    if (const char* e = std::getenv("KI_FMM_P")) p = std::atoi(e);
+    f->fmm = ki::fmm2d_build(pts.data(), nrm.data(), geo.data() + 4 * (size_t)n,
+                             geo.data() + 5 * (size_t)n, n, p, s);
+  }
+  return *f->fmm;
+}
+
+bool use_fmm(const ki_factor* f) {
+  if (!fmm_capable(f)) return false;
+  const char* e = std::getenv("KI_RESIDUAL_APPLY");
+  if (e && std::string(e) == "dense") return false;
+  if (e && std::string(e) == "fmm") return true;
+  return f->n_dofs >= 4096;
+}
+
+void apply_K(ki_factor* f, const double* mu, int ncols, double* y1, cudaStream_t s, bool fast) {
+  const int N = f->n_dofs;
+  if (fast) {
+    ki::fmm2d_apply(fmm_for(f, s), mu, N, ncols, y1, N, s);
+    return;
+  }
+  dim3 grid((N + kApplyThreads - 1) / kApplyThreads, (ncols + kApplyCols - 1) / kApplyCols);
+  k_dense_apply<<<grid, kApplyThreads, 0, s>>>(f->P, f->n_points, f->sol_dim, mu, N, ncols, y1, N,
+                                               nullptr, 0);
+  KI_CHECK_CUDA(cudaGetLastError());
+}
+
+void apply_bordered(ki_factor* f, const double* mu, const double* alpha, int ncols, double* y1,
+                    double* y2, cudaStream_t s) {
+  const int N = f->n_dofs, nb = f->n_border;
+  apply_K(f, mu, ncols, y1, s, use_fmm(f));
+  if (nb > 0) {
+    k_border_apply<<<(N + 127) / 128, 128, 0, s>>>(f->P.x, f->P.y, f->P.z, 1, f->n_points, f->dim,
+                                                   f->sol_dim, f->d_holes, f->n_holes, alpha, nb,
+                                                   ncols, y1, N);
+    const int cph = nb / f->n_holes;
+    k_psi_apply<<<dim3(nb, ncols), 256, 0, s>>>(f->d_pts, f->P.w, f->dim, f->sol_dim, f->d_holes,
+                                                f->d_hstart, f->d_hcount, cph, mu, N, alpha, nb,
+                                                y2, nb);
+    KI_CHECK_CUDA(cudaGetLastError());
+  }
+}
 }  // namespace
 
 extern "C" {
@@ -529,7 +815,16 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
       KI_CHECK_CUDA(cudaMalloc(&f->d_holes, sizeof(double) * dim * desc->n_holes));
       KI_CHECK_CUDA(cudaMemcpy(f->d_holes, desc->hole_centers, sizeof(double) * dim * desc->n_holes,
                                cudaMemcpyHostToDevice));
+      KI_CHECK_CUDA(cudaMalloc(&f->d_hstart, sizeof(int) * 2 * desc->n_holes));
+      f->d_hcount = f->d_hstart + desc->n_holes;
+      KI_CHECK_CUDA(cudaMemcpy(f->d_hstart, desc->hole_node_start, sizeof(int) * desc->n_holes,
+                               cudaMemcpyHostToDevice));
+      KI_CHECK_CUDA(cudaMemcpy(f->d_hcount, desc->hole_node_count, sizeof(int) * desc->n_holes,
+                               cudaMemcpyHostToDevice));
     }
+    KI_CHECK_CUDA(cudaMalloc(&f->d_pts, sizeof(double) * dim * (size_t)n));
+    KI_CHECK_CUDA(cudaMemcpy(f->d_pts, desc->points, sizeof(double) * dim * (size_t)n,
+                             cudaMemcpyHostToDevice));
     if (f->precision == KI_PRECISION_FP64)
       f->f64 = ki::factorize<double>(prm, n, desc->points, desc->normals, desc->weights,
                                      desc->curvatures, holes, f->stream);
@@ -655,6 +950,36 @@ int ki_apply(ki_factor* f, const double* x, int ldx, int ncols, const double* al
   });
 }
 
+int ki_apply_fmm(ki_factor* f, const double* x, int ldx, int ncols, const double* alpha,
+                 int ldalpha, double* y, int ldy) {
+  return guarded([&] {
+    if (!f || !x || !y) throw ArgError("NULL argument");
+    if (!fmm_capable(f)) throw StateError("ki_apply_fmm: 2D Laplace problems only");
+    const int N = f->n_dofs, nb = f->n_border;
+    if (ncols < 0 || ldx < N || ldy < N) throw ArgError("bad leading dimension / ncols");
+    if (ncols == 0) return;
+    cudaStream_t s = f->stream;
+    DevBuf<double> dx((size_t)N * ncols, s), dy((size_t)N * ncols, s);
+    KI_CHECK_CUDA(cudaMemcpy2DAsync(dx.p, sizeof(double) * N, x, sizeof(double) * ldx,
+                                    sizeof(double) * N, ncols, cudaMemcpyHostToDevice, s));
+    apply_K(f, dx.p, ncols, dy.p, s, true);
+    if (nb > 0 && alpha) {
+      if (ldalpha < nb) throw ArgError("bad ldalpha");
+      DevBuf<double> da((size_t)nb * ncols, s);
+      KI_CHECK_CUDA(cudaMemcpy2DAsync(da.p, sizeof(double) * nb, alpha, sizeof(double) * ldalpha,
+                                      sizeof(double) * nb, ncols, cudaMemcpyHostToDevice, s));
+      k_border_apply<<<(N + 127) / 128, 128, 0, s>>>(f->P.x, f->P.y, f->P.z, 1, f->n_points, f->dim,
+                                                     f->sol_dim, f->d_holes, f->n_holes, da.p, nb,
+                                                     ncols, dy.p, N);
+      KI_CHECK_CUDA(cudaGetLastError());
+      KI_CHECK_CUDA(cudaStreamSynchronize(s));
+    }
+    KI_CHECK_CUDA(cudaMemcpy2DAsync(y, sizeof(double) * ldy, dy.p, sizeof(double) * N,
+                                    sizeof(double) * N, ncols, cudaMemcpyDeviceToHost, s));
+    KI_CHECK_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
 int ki_apply_rows(ki_factor* f, const int* rows, int nrows, const double* x, int ldx, int ncols,
                   const double* alpha, int ldalpha, double* y, int ldy) {
   return guarded([&] {
@@ -723,6 +1048,47 @@ int ki_eval_targets(ki_factor* f, const double* targets, int n_targets, const do
     }
     KI_CHECK_CUDA(cudaMemcpy2DAsync(out, sizeof(double) * ldout, dout.p, sizeof(double) * NT,
                                     sizeof(double) * NT, ncols, cudaMemcpyDeviceToHost, s));
+    KI_CHECK_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ki_solve_refined_device(ki_factor* f, const double* d_b, int nrhs, double* d_x,
+                            double* d_alpha, double tol, int max_steps, ki_refine_info* info,
+                            void* stream) {
+  return guarded([&] {
+    if (!f || !info) throw ArgError("NULL argument");
+    if (nrhs < 0 || max_steps < 0 || !(tol >= 0)) throw ArgError("bad nrhs / max_steps / tol");
+    std::memset(info, 0, sizeof(*info));
+    if (nrhs == 0) return;
+    if (!d_b || !d_x || (f->n_border > 0 && !d_alpha)) throw ArgError("NULL b, x or alpha");
+    cudaStream_t s = stream ? (cudaStream_t)stream : f->stream;
+    refined_solve(f, d_b, nrhs, d_x, d_alpha, tol, max_steps, info, s);
+    KI_CHECK_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ki_solve_refined(ki_factor* f, const double* b, int ldb, int nrhs, double* x, int ldx,
+                     double* alpha, int ldalpha, double tol, int max_steps, ki_refine_info* info) {
+  return guarded([&] {
+    if (!f || !info) throw ArgError("NULL argument");
+    const int N = f->n_dofs, nb = f->n_border;
+    if (nrhs < 0 || ldb < N || ldx < N || max_steps < 0 || !(tol >= 0))
+      throw ArgError("bad leading dimension / nrhs / max_steps / tol");
+    if (nb > 0 && alpha && ldalpha < nb) throw ArgError("bad ldalpha");
+    std::memset(info, 0, sizeof(*info));
+    if (nrhs == 0) return;
+    if (!b || !x) throw ArgError("NULL b or x");
+    cudaStream_t s = f->stream;
+    DevBuf<double> db((size_t)N * nrhs, s), dx((size_t)N * nrhs, s),
+        da((size_t)std::max(1, nb) * nrhs, s);
+    KI_CHECK_CUDA(cudaMemcpy2DAsync(db.p, sizeof(double) * N, b, sizeof(double) * ldb,
+                                    sizeof(double) * N, nrhs, cudaMemcpyHostToDevice, s));
+    refined_solve(f, db.p, nrhs, dx.p, da.p, tol, max_steps, info, s);
+    KI_CHECK_CUDA(cudaMemcpy2DAsync(x, sizeof(double) * ldx, dx.p, sizeof(double) * N,
+                                    sizeof(double) * N, nrhs, cudaMemcpyDeviceToHost, s));
+    if (nb > 0 && alpha)
+      KI_CHECK_CUDA(cudaMemcpy2DAsync(alpha, sizeof(double) * ldalpha, da.p, sizeof(double) * nb,
+                                      sizeof(double) * nb, nrhs, cudaMemcpyDeviceToHost, s));
     KI_CHECK_CUDA(cudaStreamSynchronize(s));
   });
 }

@@ -24,7 +24,20 @@ struct Points {
   const T* nz = nullptr;
   const T* diag = nullptr;
   int dim = 2;
+  // FP32 form: low parts of the coordinates (x = x + xl exactly to ~2^-48
+  // relative), so that differences of nearby points are formed without the
+  // cancellation of rounded absolute coordinates; nullptr in FP64.
+  const T* xl = nullptr;
+  const T* yl = nullptr;
+  const T* zl = nullptr;
 };
+
+// Coordinate difference a - b from (hi, lo) pairs: hi[a] - hi[b] is exact for
+// nearby points (Sterbenz), so the difference keeps full relative accuracy.
+template <typename T>
+__device__ __forceinline__ T pdiff(const T* hi, const T* lo, int a, int b) {
+  return lo ? (hi[a] - hi[b]) + (lo[a] - lo[b]) : hi[a] - hi[b];
+}
 
 constexpr double kPi = 3.14159265358979323846;
 
@@ -33,16 +46,19 @@ constexpr double kPi = 3.14159265358979323846;
 // Stokes:  Kernel::two_d_kern (kern_interp/kernel/kernel.cpp:65-87).
 // r = t - s; an exactly coincident pair takes the diagonal limit.
 template <typename T>
-__device__ __forceinline__ T laplace_entry(T tx, T ty, T sx, T sy, T snx, T sny, T sw, T sk) {
-  T r1 = tx - sx, r2 = ty - sy;
+__device__ __forceinline__ T laplace_entry_r(T r1, T r2, T snx, T sny, T sw, T sk) {
   if (r1 == T(0) && r2 == T(0)) return T(0.5) + T(0.5) * sk * sw * T(1.0 / (2 * kPi));
   return -sw * T(1.0 / (2 * kPi)) * (r1 * snx + r2 * sny) / (r1 * r1 + r2 * r2);
 }
 
 template <typename T>
-__device__ __forceinline__ T stokes_entry(int tpar, int spar, T tx, T ty, T tnx, T tny, T sx,
-                                          T sy, T snx, T sny, T sw, T sk) {
-  T r1 = tx - sx, r2 = ty - sy;
+__device__ __forceinline__ T laplace_entry(T tx, T ty, T sx, T sy, T snx, T sny, T sw, T sk) {
+  return laplace_entry_r<T>(tx - sx, ty - sy, snx, sny, sw, sk);
+}
+
+template <typename T>
+__device__ __forceinline__ T stokes_entry_r(int tpar, int spar, T r1, T r2, T tnx, T tny,
+                                            T snx, T sny, T sw, T sk) {
   T sn[2] = {snx, sny};
   T tn[2] = {tnx, tny};
   int is_diag = (tpar + spar + 1) % 2;
@@ -56,6 +72,12 @@ __device__ __forceinline__ T stokes_entry(int tpar, int spar, T tx, T ty, T tnx,
   T rr = r1 * r1 + r2 * r2;
   return sw * T(1.0 / kPi) * (r1 * snx + r2 * sny) / (rr * rr) * r[tpar] * r[spar] +
          sw * tn[tpar] * sn[spar];
+}
+
+template <typename T>
+__device__ __forceinline__ T stokes_entry(int tpar, int spar, T tx, T ty, T tnx, T tny, T sx,
+                                          T sy, T snx, T sny, T sw, T sk) {
+  return stokes_entry_r<T>(tpar, spar, tx - sx, ty - sy, tnx, tny, snx, sny, sw, sk);
 }
 
 // 3D Laplace double layer (Kernel::three_d_laplace, kernel.cpp:104-121):
@@ -90,21 +112,22 @@ template <typename T>
 __device__ __forceinline__ T kernel_entry(const Points<T>& P, int sol_dim, int tdof, int sdof) {
   if (P.dim == 3) {
     if (sol_dim == 1)
-      return laplace3_entry<T>(P.x[tdof] - P.x[sdof], P.y[tdof] - P.y[sdof], P.z[tdof] - P.z[sdof],
-                               P.nx[sdof], P.ny[sdof], P.nz[sdof], P.w[sdof],
-                               P.diag ? P.diag[sdof] : T(0));
+      return laplace3_entry<T>(pdiff(P.x, P.xl, tdof, sdof), pdiff(P.y, P.yl, tdof, sdof),
+                               pdiff(P.z, P.zl, tdof, sdof), P.nx[sdof], P.ny[sdof], P.nz[sdof],
+                               P.w[sdof], P.diag ? P.diag[sdof] : T(0));
     const int tp = tdof / 3, sp = sdof / 3;
-    return stokes3_entry<T>(tdof - 3 * tp, sdof - 3 * sp, P.x[tp] - P.x[sp], P.y[tp] - P.y[sp],
-                            P.z[tp] - P.z[sp], P.nx[tp], P.ny[tp], P.nz[tp], P.nx[sp], P.ny[sp],
-                            P.nz[sp], P.w[sp], P.diag ? P.diag + 9 * (size_t)sp : nullptr);
+    return stokes3_entry<T>(tdof - 3 * tp, sdof - 3 * sp, pdiff(P.x, P.xl, tp, sp),
+                            pdiff(P.y, P.yl, tp, sp), pdiff(P.z, P.zl, tp, sp), P.nx[tp], P.ny[tp],
+                            P.nz[tp], P.nx[sp], P.ny[sp], P.nz[sp], P.w[sp],
+                            P.diag ? P.diag + 9 * (size_t)sp : nullptr);
   }
   if (sol_dim == 1) {
-    return laplace_entry<T>(P.x[tdof], P.y[tdof], P.x[sdof], P.y[sdof], P.nx[sdof], P.ny[sdof],
-                            P.w[sdof], P.kappa[sdof]);
+    return laplace_entry_r<T>(pdiff(P.x, P.xl, tdof, sdof), pdiff(P.y, P.yl, tdof, sdof),
+                              P.nx[sdof], P.ny[sdof], P.w[sdof], P.kappa[sdof]);
   }
   int tp = tdof >> 1, sp = sdof >> 1;
-  return stokes_entry<T>(tdof & 1, sdof & 1, P.x[tp], P.y[tp], P.nx[tp], P.ny[tp], P.x[sp],
-                         P.y[sp], P.nx[sp], P.ny[sp], P.w[sp], P.kappa[sp]);
+  return stokes_entry_r<T>(tdof & 1, sdof & 1, pdiff(P.x, P.xl, tp, sp), pdiff(P.y, P.yl, tp, sp),
+                           P.nx[tp], P.ny[tp], P.nx[sp], P.ny[sp], P.w[sp], P.kappa[sp]);
 }
 
 // Point of a DOF.

@@ -223,37 +223,65 @@ __global__ void k_build_active(const ActiveTask* tasks, int* ipool) {
 // :720-790: 3D, a theta x phi grid with theta outer).  A box's proxy point i
 // is c + rad * u_i with outward normal u_i and weight 2 pi rad / n (2D) or
 // rad^2 * wu_i (3D, wu = Gauss-Legendre phi weight * sin(phi) * theta weight).
+// Tables in the factor precision.
+template <typename T>
 struct ProxyTab {
-  const double* ux;
-  const double* uy;
-  const double* uz;   // 3D only
-  const double* wu;   // 3D only
+  const T* ux;
+  const T* uy;
+  const T* uz;   // 3D only
+  const T* wu;   // 3D only
   int n;
 };
+
+// A box's proxy geometry in the factor precision: the centre split as
+// hi + lo (so that box-point offsets b - c keep full relative accuracy in
+// FP32), the radius and the 2D proxy weight 2 pi rad / n.
+template <typename T>
+struct ProxyBox {
+  T hx, hy, hz, lx, ly, lz;
+  T rad, pw2;
+};
+
+template <typename T>
+__device__ __forceinline__ ProxyBox<T> proxy_box(double cx, double cy, double cz, double rad,
+                                                 int nprox) {
+  ProxyBox<T> b;
+  b.hx = T(cx); b.lx = T(cx - (double)b.hx);
+  b.hy = T(cy); b.ly = T(cy - (double)b.hy);
+  b.hz = T(cz); b.lz = T(cz - (double)b.hz);
+  b.rad = T(rad);
+  b.pw2 = T(2.0 * kPi * rad / nprox);
+  return b;
+}
 
 // One ID-matrix entry, row `row` of the stacked matrix
 // [K(I,A); K(A,I)^T; box->proxy; proxy->box] (Kernel::get_id_mat,
 // kern_interp/kernel/kernel.cpp:565-640; proxy rows Kernel::get_proxy_mat,
-// :646-790), column = active DOF `adof`.
+// :646-790), column = active DOF `adof`.  Proxy offsets are formed as
+// rad u - (b - c).
 template <typename T>
 __device__ __forceinline__ T id_entry(const Points<T>& P, int sol_dim, int row, int nI,
-                                      const int* rows, int adof, const ProxyTab& px, double cx,
-                                      double cy, double cz, double rad) {
+                                      const int* rows, int adof, const ProxyTab<T>& px,
+                                      const ProxyBox<T>& c) {
   if (row < nI) return kernel_entry<T>(P, sol_dim, rows[row], adof);
   if (row < 2 * nI) return kernel_entry<T>(P, sol_dim, adof, rows[row - nI]);
   const int q = row - 2 * nI;
   const int nprox = px.n;
+  const int ap = dof_point(adof, sol_dim);
+  const T bcx = (P.x[ap] - c.hx) + ((P.xl ? P.xl[ap] : T(0)) - c.lx);
+  const T bcy = (P.y[ap] - c.hy) + ((P.yl ? P.yl[ap] : T(0)) - c.ly);
+  const T bnx = P.nx[ap], bny = P.ny[ap], bw = P.w[ap];
+  const int half = sol_dim * nprox;
+  const int qq = q < half ? q : q - half;
+  const int i = sol_dim == 1 ? qq : qq / sol_dim, par = qq - sol_dim * i;
+  const T ux = px.ux[i], uy = px.uy[i];
+  const T rx = c.rad * ux - bcx, ry = c.rad * uy - bcy;   // proxy - box
   if (P.dim == 3) {
-    const int ap = sol_dim == 1 ? adof : adof / 3;
-    const T bx = P.x[ap], by = P.y[ap], bz = P.z[ap];
-    const T bnx = P.nx[ap], bny = P.ny[ap], bnz = P.nz[ap], bw = P.w[ap];
-    const int half = sol_dim * nprox;
-    const int qq = q < half ? q : q - half;
-    const int i = sol_dim == 1 ? qq : qq / 3, par = qq - sol_dim * i;
-    const T ux = T(px.ux[i]), uy = T(px.uy[i]), uz = T(px.uz[i]);
-    const T rx = T(cx + rad * px.ux[i]) - bx, ry = T(cy + rad * px.uy[i]) - by,
-            rz = T(cz + rad * px.uz[i]) - bz;   // proxy - box
-    const T pw = T(rad * rad * px.wu[i]);
+    const T bcz = (P.z[ap] - c.hz) + ((P.zl ? P.zl[ap] : T(0)) - c.lz);
+    const T uz = px.uz[i];
+    const T rz = c.rad * uz - bcz;
+    const T bnz = P.nz[ap];
+    const T pw = c.rad * c.rad * px.wu[i];
     if (sol_dim == 1) {
       if (q < half) return laplace3_entry<T>(rx, ry, rz, bnx, bny, bnz, bw, T(0));
       return laplace3_entry<T>(-rx, -ry, -rz, ux, uy, uz, pw, T(0));
@@ -263,23 +291,13 @@ __device__ __forceinline__ T id_entry(const Points<T>& P, int sol_dim, int row, 
       return stokes3_entry<T>(par, apar, rx, ry, rz, ux, uy, uz, bnx, bny, bnz, bw, nullptr);
     return stokes3_entry<T>(apar, par, -rx, -ry, -rz, bnx, bny, bnz, ux, uy, uz, pw, nullptr);
   }
-  int ap = sol_dim == 1 ? adof : (adof >> 1);
-  T bx = P.x[ap], by = P.y[ap], bnx = P.nx[ap], bny = P.ny[ap], bw = P.w[ap];
-  T pw = T(2.0 * kPi * rad / nprox);
   if (sol_dim == 1) {
-    int i = q < nprox ? q : q - nprox;
-    T ppx = T(cx + rad * px.ux[i]), ppy = T(cy + rad * px.uy[i]);
-    T pnx = T(px.ux[i]), pny = T(px.uy[i]);
-    if (q < nprox) return laplace_entry<T>(ppx, ppy, bx, by, bnx, bny, bw, T(0));
-    return laplace_entry<T>(bx, by, ppx, ppy, pnx, pny, pw, T(0));
+    if (q < half) return laplace_entry_r<T>(rx, ry, bnx, bny, bw, T(0));
+    return laplace_entry_r<T>(-rx, -ry, ux, uy, c.pw2, T(0));
   }
-  int half = 2 * nprox;
-  int qq = q < half ? q : q - half;
-  int i = qq >> 1, par = qq & 1;
-  T ppx = T(cx + rad * px.ux[i]), ppy = T(cy + rad * px.uy[i]);
-  T pnx = T(px.ux[i]), pny = T(px.uy[i]);
-  if (q < half) return stokes_entry<T>(par, adof & 1, ppx, ppy, pnx, pny, bx, by, bnx, bny, bw, T(0));
-  return stokes_entry<T>(adof & 1, par, bx, by, bnx, bny, ppx, ppy, pnx, pny, pw, T(0));
+  const int apar = adof & 1;
+  if (q < half) return stokes_entry_r<T>(par, apar, rx, ry, ux, uy, bnx, bny, bw, T(0));
+  return stokes_entry_r<T>(apar, par, -rx, -ry, bnx, bny, ux, uy, c.pw2, T(0));
 }
 
 // Interpolative decomposition of one box per CTA.
@@ -295,7 +313,7 @@ template <typename T, int FR>
 __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_base,
                                                   const int64_t* seg_off, const int* seg_len,
                                                   int* ipool, int* iscratch, T* tws, Points<T> P,
-                                                  int sol_dim, ProxyTab px, double tol, int* k_out,
+                                                  int sol_dim, ProxyTab<T> px, double tol, int* k_out,
                                                   int* m_out, int mode, int flags) {
   // flags: 1 gather the rows (writes m), 2 fold the ID matrix into R,
   //        4 R already formed (row-major n x n in the global scratch)
@@ -355,10 +373,11 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
           keep = 1;
         } else {
           const int p = dof_point(dof, sol_dim);
-          double dx = t.cx - (double)P.x[p], dy = t.cy - (double)P.y[p];
+          double dx = t.cx - ((double)P.x[p] + (P.xl ? (double)P.xl[p] : 0.0));
+          double dy = t.cy - ((double)P.y[p] + (P.yl ? (double)P.yl[p] : 0.0));
           double d2 = dx * dx + dy * dy;
           if (P.dim == 3) {
-            double dz = t.cz - (double)P.z[p];
+            double dz = t.cz - ((double)P.z[p] + (P.zl ? (double)P.zl[p] : 0.0));
             d2 += dz * dz;
           }
           double dist = sqrt(d2);
@@ -434,14 +453,14 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
       RF[rowbase(j) + j] = beta;
     }
   };
+  const ProxyBox<T> pbox = proxy_box<T>(t.cx, t.cy, t.cz, t.rad_proxy, px.n);
   for (int r0 = 0; (flags & 2) && r0 < m; r0 += FR) {
     for (int idx = tid; idx < FR * n; idx += nth) {
       int j = idx % n, i = idx / n;
       int row = r0 + i;
       T v = T(0);
       if (row < m)
-        v = id_entry<T>(P, sol_dim, row, nI, rows, act[j], px, t.cx, t.cy, t.cz,
-                        t.rad_proxy);
+        v = id_entry<T>(P, sol_dim, row, nI, rows, act[j], px, pbox);
       B[(size_t)i * ldB + j] = v;
     }
     __syncthreads();
@@ -663,7 +682,7 @@ constexpr int kQrRows = 64;   // rows staged per trailing-update pass
 
 template <typename T>
 __global__ void k_wide_assemble(const WideTask* tasks, T* wpool, const int* ipool, const int* iscratch,
-                                Points<T> P, int sol_dim, ProxyTab px) {
+                                Points<T> P, int sol_dim, ProxyTab<T> px) {
   const WideTask t = tasks[blockIdx.x];
   const int j0 = blockIdx.y * 8;
   if (j0 >= t.n) return;
@@ -671,11 +690,11 @@ __global__ void k_wide_assemble(const WideTask* tasks, T* wpool, const int* ipoo
   const int* act = ipool + t.act;
   const int* rows = iscratch + t.rows;
   T* M = wpool + t.M;
+  const ProxyBox<T> pbox = proxy_box<T>(t.cx, t.cy, t.cz, t.rad, px.n);
   for (int j = j0; j < j1; j++) {
     int a = act[j];
     for (int row = threadIdx.x; row < t.m; row += blockDim.x)
-      M[row + (size_t)t.m * j] = id_entry<T>(P, sol_dim, row, t.nI, rows, a, px, t.cx, t.cy,
-                                             t.cz, t.rad);
+      M[row + (size_t)t.m * j] = id_entry<T>(P, sol_dim, row, t.nI, rows, a, px, pbox);
   }
 }
 
@@ -1449,11 +1468,14 @@ __global__ void k_assemble_S(const T* A, int nr, const int* idx, const T* Um, co
 // M = [x(allskel, :); -t]  ((nr + nb) x nc, column-major)
 template <typename T>
 __global__ void k_mc_rhs(const T* x, int ldx, const int* idx, int nr, const T* t, int nb, int nc,
-                         T* M) {
+                         T* M, const T* g = nullptr) {
+  // g: right-hand side of the border rows (Psi mu - alpha = g), row-major
+  // nb x nc; absent for the reference's problem (g = 0)
   const int ns = nr + nb;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ns * nc; e += gridDim.x * blockDim.x) {
     int i = e % ns, c = e / ns;
-    M[e] = i < nr ? x[(size_t)idx[i] * ldx + c] : -t[(i - nr) + (size_t)nb * c];
+    M[e] = i < nr ? x[(size_t)idx[i] * ldx + c]
+                  : (g ? g[(size_t)(i - nr) * nc + c] : T(0)) - t[(i - nr) + (size_t)nb * c];
   }
 }
 
@@ -1488,10 +1510,15 @@ __global__ void k_mc_finish(T* x, int nc, const int* idx, const T* M, int nr, in
 template <typename T>
 __global__ void k_fill_points(const double* pts, const double* nrm, const double* w,
                               const double* kap, int n, int dim, T* x, T* y, T* z, T* nx, T* ny,
-                              T* nz, T* ww, T* kk) {
+                              T* nz, T* ww, T* kk, T* lo) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     x[i] = T(pts[(size_t)dim * i]);
     y[i] = T(pts[(size_t)dim * i + 1]);
+    if (lo) {   // x = x_hi + x_lo
+      lo[i] = T(pts[(size_t)dim * i] - (double)x[i]);
+      lo[n + i] = T(pts[(size_t)dim * i + 1] - (double)y[i]);
+      if (dim == 3) lo[2 * (size_t)n + i] = T(pts[3 * (size_t)i + 2] - (double)T(pts[3 * (size_t)i + 2]));
+    }
     nx[i] = T(nrm[(size_t)dim * i]);
     ny[i] = T(nrm[(size_t)dim * i + 1]);
     if (dim == 3) {
@@ -1664,7 +1691,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     KI_CUDA(cudaMemcpyAsync(d_w_in, weights, sizeof(double) * np_, cudaMemcpyHostToDevice, s));
     if (curvatures)
       KI_CUDA(cudaMemcpyAsync(d_k_in, curvatures, sizeof(double) * np_, cudaMemcpyHostToDevice, s));
-    T* d = (T*)F->alloc(sizeof(T) * np_ * 8);
+    T* d = (T*)F->alloc(sizeof(T) * np_ * 11);
     F->d_x = d; F->d_y = d + np_; F->d_nx = d + 2 * np_;
     F->d_ny = d + 3 * np_; F->d_w = d + 4 * np_;
     F->d_kappa = d + 5 * np_;
@@ -1672,15 +1699,25 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       F->d_z = d + 6 * np_;
       F->d_nz = d + 7 * np_;
     }
+    // FP32: low parts of the coordinates
+    T* lo = sizeof(T) < sizeof(double) ? d + 8 * np_ : nullptr;
     k_fill_points<T><<<std::min(1024, (n_points + 255) / 256), 256, 0, s>>>(
         d_pts_in, d_nrm_in, d_w_in, curvatures ? d_k_in : nullptr, n_points, dim, F->d_x,
-        F->d_y, F->d_z, F->d_nx, F->d_ny, F->d_nz, F->d_w, F->d_kappa);
+        F->d_y, F->d_z, F->d_nx, F->d_ny, F->d_nz, F->d_w, F->d_kappa, lo);
+    if (lo) {
+      F->d_xl = lo;
+      F->d_yl = lo + np_;
+      if (dim == 3) F->d_zl = lo + 2 * np_;
+    }
     KI_CUDA(cudaGetLastError());
   }
   Points<T> P{F->d_x, F->d_y, F->d_nx, F->d_ny, F->d_w, F->d_kappa};
   P.dim = dim;
   P.z = F->d_z;
   P.nz = F->d_nz;
+  P.xl = F->d_xl;
+  P.yl = F->d_yl;
+  P.zl = F->d_zl;
   F->d_err = (int*)F->alloc(sizeof(int));
   KI_CUDA(cudaMemsetAsync(F->d_err, 0, sizeof(int), s));
 
@@ -1719,8 +1756,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
   // 3D theta_a = 2 pi a / n_theta, phi_b the Gauss-Legendre nodes on [0, pi],
   // theta outer)
   const int np = prm.num_proxy_points;
-  double* d_ptab = (double*)F->alloc(sizeof(double) * 4 * std::max(np, 1));
-  ProxyTab ptab{d_ptab, d_ptab + np, d_ptab + 2 * np, d_ptab + 3 * np, np};
+  T* d_ptab = (T*)F->alloc(sizeof(T) * 4 * std::max(np, 1));
+  ProxyTab<T> ptab{d_ptab, d_ptab + np, d_ptab + 2 * np, d_ptab + 3 * np, np};
   {
     std::vector<double> pt(4 * std::max(np, 1), 0.0);
     if (dim == 2) {
@@ -1744,7 +1781,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         }
       }
     }
-    upload(d_ptab, pt, s);
+    std::vector<T> ptT(pt.begin(), pt.end());
+    upload(d_ptab, ptT, s);
   }
 
   // integer pool: dof_sorted | per-level active lists | permuted lists
@@ -2348,7 +2386,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
 }
 
 template <typename T>
-void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha) {
+void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, const T* d_g) {
   cudaStream_t s = F.stream;
   const int L = (int)F.levels.size();
   const int nr = F.n_root;
@@ -2403,7 +2441,7 @@ void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha) {
   se();
   sb("border_root");
   k_mc_rhs<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
-      d_x, ncols, F.d_root_idx, nr, t, nb, ncols, M);
+      d_x, ncols, F.d_root_idx, nr, t, nb, ncols, M, d_g);
   dense_lu_solve<T>(F.d_root_lu, ns, F.d_root_piv, M, ns, ncols, false, s);
   se();
   sb("border_update");
@@ -2516,8 +2554,8 @@ template std::unique_ptr<Factorization<double>> factorize<double>(
 template std::unique_ptr<Factorization<float>> factorize<float>(
     const Params&, int, const double*, const double*, const double*, const double*,
     const HoleDesc&, cudaStream_t);
-template void solve_device<double>(Factorization<double>&, double*, int, double*);
-template void solve_device<float>(Factorization<float>&, float*, int, float*);
+template void solve_device<double>(Factorization<double>&, double*, int, double*, const double*);
+template void solve_device<float>(Factorization<float>&, float*, int, float*, const float*);
 template struct Factorization<double>;
 template struct Factorization<float>;
 

@@ -71,6 +71,8 @@ struct Factorization {
   // point data (device, SoA, precision T)
   T *d_x = nullptr, *d_y = nullptr, *d_nx = nullptr, *d_ny = nullptr, *d_w = nullptr,
     *d_kappa = nullptr, *d_z = nullptr, *d_nz = nullptr;
+  // FP32 form: low parts of the coordinates (nullptr in FP64)
+  T *d_xl = nullptr, *d_yl = nullptr, *d_zl = nullptr;
   // 3D diagonal entries (Kernel::compute_diag_entries_3dlaplace/_3dstokes):
   // FP64 (kept for the FP64 operator apply) and in the factor precision
   double* d_diag64 = nullptr;
@@ -157,7 +159,10 @@ void solve_device_arena(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, Scra
 // Solve with the factorization: x (device, DOF-major N x ncols, ld = ncols)
 // is overwritten with the solution; alpha (device, n_border x ncols,
 // row-major) receives the border unknowns of a multiply connected problem.
+// g (optional, row-major n_border x ncols): right-hand side of the border
+// rows, Psi mu - alpha = g (zero in the reference's problem; refinement
+// corrections carry one).
 template <typename T>
-void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha);
+void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, const T* d_g = nullptr);
 
 }  // namespace ki

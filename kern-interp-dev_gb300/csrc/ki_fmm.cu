@@ -1,0 +1,534 @@
+// Uniform-depth 2D FMM for the Laplace double-layer Nystrom operator (see
+// ki_fmm.h).  Host: Morton-sorted points, one tree level per refinement
+// step down to a leaf level with about 40 points per non-empty leaf, near
+// lists (the 3 x 3 leaf neighbourhood) and interaction lists (children of
+// the parent's neighbours that are not adjacent), translation matrices.
+// Device, FP64: P2M per leaf, M2M up, M2L per box over its interaction list
+// (the matrix depends only on the integer offset between the two boxes, so
+// 49 matrices serve every level), L2L down, and per leaf the local
+// expansion plus the direct near-field sum with the exact kernel entries.
+// All 32 columns of a pass share every kernel-entry and translation-matrix
+// load.
+#include "ki_fmm.h"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+namespace ki {
+
+namespace {
+
+#define KI_FMM_CUDA(call)                                                                  \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      throw std::runtime_error(std::string("CUDA error (fmm): ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+constexpr int kCols = 32;        // columns per pass
+constexpr int kMaxP = 32;        // expansion terms (upper bound)
+constexpr int kChunk = 32;       // source points staged per shared-memory chunk
+constexpr double kPi2 = 6.283185307179586476925286766559;
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c) {   // a*b + c
+  return make_double2(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
+}
+
+// q[i + n c] = nw[i] * mu[perm[i] + ldmu c]  (sorted order)
+__global__ void k_charges(const double2* nw, const int* perm, int n, const double* mu, int ldmu,
+                          int c0, int nc, double2* q) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * nc;
+       e += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(e % n), c = (int)(e / n);
+    double m = mu[perm[i] + (size_t)ldmu * (c0 + c)];
+    q[e] = make_double2(nw[i].x * m, nw[i].y * m);
+  }
+}
+
+// Multipole expansion of every leaf: me[(g nc + c) p + k] = sum_s q_s w_s^k,
+// w_s = (z_s - centre) / side.
+__global__ void k_p2m(const int* leaf_start, const int* leaf_box, const double2* centre,
+                      double side, const double2* z, const double2* q, int n, int nc, int p,
+                      double2* me) {
+  __shared__ double2 pw[kChunk][kMaxP];
+  __shared__ double2 qs[kChunk][kCols];
+  const int lf = blockIdx.x, g = leaf_box[lf];
+  const int s0 = leaf_start[lf], s1 = leaf_start[lf + 1];
+  const double2 c = centre[g];
+  const int nout = p * nc;
+  double2 acc[4];
+  for (int r = 0; r < 4; r++) acc[r] = make_double2(0, 0);
+  for (int base = s0; base < s1; base += kChunk) {
+    const int cnt = min(kChunk, s1 - base);
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+      double2 w = make_double2((z[base + i].x - c.x) / side, (z[base + i].y - c.y) / side);
+      double2 t = make_double2(1, 0);
+      for (int k = 0; k < p; k++) {
+        pw[i][k] = t;
+        t = cmul(t, w);
+      }
+    }
+    for (int e = threadIdx.x; e < cnt * nc; e += blockDim.x) {
+      int i = e % cnt, cc = e / cnt;
+      qs[i][cc] = q[base + i + (size_t)n * cc];
+    }
+    __syncthreads();
+    for (int r = 0; r < 4; r++) {
+      int o = threadIdx.x + r * blockDim.x;
+      if (o >= nout) break;
+      int k = o % p, cc = o / p;
+      double2 a = acc[r];
+      for (int i = 0; i < cnt; i++) a = cfma(qs[i][cc], pw[i][k], a);
+      acc[r] = a;
+    }
+  }
+  for (int r = 0; r < 4; r++) {
+    int o = threadIdx.x + r * blockDim.x;
+    if (o >= nout) break;
+    me[(size_t)g * nout + o] = acc[r];
+  }
+}
+
+// Multipole of each box of one level from its children (M2M):
+// me[P] = sum_children T_pos me[C], T_pos lower triangular p x p.
+__global__ void k_m2m(int b0, const int* child, const int* child_pos, const double2* T, int nc,
+                      int p, double2* me) {
+  const int g = b0 + blockIdx.x;
+  const int nout = p * nc;
+  for (int o = threadIdx.x; o < nout; o += blockDim.x) {
+    const int k = o % p, cc = o / p;
+    double2 a = make_double2(0, 0);
+    for (int q = 0; q < 4; q++) {
+      const int ch = child[4 * g + q];
+      if (ch < 0) continue;
+      const double2* Tm = T + (size_t)child_pos[ch] * p * p + (size_t)k * p;
+      const double2* src = me + (size_t)ch * nout + (size_t)cc * p;
+      for (int j = 0; j <= k; j++) a = cfma(Tm[j], src[j], a);
+    }
+    me[(size_t)g * nout + o] = a;
+  }
+}
+
+// Local expansion contributions over the interaction list (M2L): for every
+// box g of one level, le[g] = (1/side) sum_v M_code(v) me[src(v)].
+__global__ void k_m2l(int b0, const int* v_off, const int* v_src, const int* v_code,
+                      const double2* M, double inv_side, int nc, int p, const double2* me,
+                      double2* le) {
+  __shared__ double2 sm_me[kCols * kMaxP];
+  __shared__ double2 sm_M[kMaxP * kMaxP];
+  const int g = b0 + blockIdx.x;
+  const int nout = p * nc;
+  double2 acc[4];
+  for (int r = 0; r < 4; r++) acc[r] = make_double2(0, 0);
+  for (int v = v_off[g]; v < v_off[g + 1]; v++) {
+    __syncthreads();
+    const double2* src = me + (size_t)v_src[v] * nout;
+    for (int e = threadIdx.x; e < nout; e += blockDim.x) sm_me[e] = src[e];
+    const double2* Mm = M + (size_t)v_code[v] * p * p;
+    for (int e = threadIdx.x; e < p * p; e += blockDim.x) sm_M[e] = Mm[e];
+    __syncthreads();
+    for (int r = 0; r < 4; r++) {
+      int o = threadIdx.x + r * blockDim.x;
+      if (o >= nout) break;
+      const int m = o % p, cc = o / p;
+      double2 a = acc[r];
+      const double2* row = sm_M + m * p;
+      const double2* x = sm_me + cc * p;
+      for (int k = 0; k < p; k++) a = cfma(row[k], x[k], a);
+      acc[r] = a;
+    }
+  }
+  for (int r = 0; r < 4; r++) {
+    int o = threadIdx.x + r * blockDim.x;
+    if (o >= nout) break;
+    le[(size_t)g * nout + o] = make_double2(acc[r].x * inv_side, acc[r].y * inv_side);
+  }
+}
+
+// Local expansion of each box of one level += its parent's, translated (L2L):
+// le[C] += S_pos le[P], S_pos upper triangular.
+__global__ void k_l2l(int b0, const int* parent, const int* child_pos, const double2* S, int nc,
+                      int p, double2* le) {
+  const int g = b0 + blockIdx.x;
+  const int par = parent[g];
+  const int nout = p * nc;
+  const double2* Sm = S + (size_t)child_pos[g] * p * p;
+  for (int o = threadIdx.x; o < nout; o += blockDim.x) {
+    const int j = o % p, cc = o / p;
+    const double2* src = le + (size_t)par * nout + (size_t)cc * p;
+    double2 a = le[(size_t)g * nout + o];
+    for (int m = j; m < p; m++) a = cfma(Sm[(size_t)j * p + m], src[m], a);
+    le[(size_t)g * nout + o] = a;
+  }
+}
+
+// Per leaf: far field from the local expansion, near field by direct
+// summation over the 3 x 3 leaf neighbourhood (exact entries, the
+// coincident point excluded), diagonal term; written unsorted into y.
+__global__ void k_l2p_p2p(const int* leaf_start, const int* leaf_box, const int* near_off,
+                          const int* near_leaf, const double2* centre, double side,
+                          const double2* z, const double* diag, const int* perm, const double2* q,
+                          const double2* le, int n, int nc, int p, const double* mu, int ldmu,
+                          int c0, double* y, int ldy) {
+  __shared__ double2 sz[kChunk];
+  __shared__ double2 sq[kChunk][kCols];
+  __shared__ double2 sle[kCols * kMaxP];
+  const int lf = blockIdx.x, g = leaf_box[lf];
+  const int t0 = leaf_start[lf], t1 = leaf_start[lf + 1];
+  const double2 c = centre[g];
+  const int nout = p * nc;
+  for (int e = threadIdx.x; e < nout; e += blockDim.x) sle[e] = le[(size_t)g * nout + e];
+  for (int tb = t0; tb < t1; tb += blockDim.x) {
+    const int t = tb + threadIdx.x;
+    const bool on = t < t1;
+    const double2 zt = on ? z[t] : make_double2(0, 0);
+    double acc[kCols];
+#pragma unroll
+    for (int cc = 0; cc < kCols; cc++) acc[cc] = 0.0;
+    __syncthreads();
+    if (on) {
+      // far field: Re sum_m le_m w^m
+      const double2 w = make_double2((zt.x - c.x) / side, (zt.y - c.y) / side);
+      double2 pw = make_double2(1, 0);
+      for (int m = 0; m < p; m++) {
+#pragma unroll
+        for (int cc = 0; cc < kCols; cc++) {
+          if (cc < nc) {
+            const double2 b = sle[cc * p + m];
+            acc[cc] += b.x * pw.x - b.y * pw.y;
+          }
+        }
+        pw = cmul(pw, w);
+      }
+    }
+    for (int v = near_off[lf]; v < near_off[lf + 1]; v++) {
+      const int sl = near_leaf[v];
+      const int s0 = leaf_start[sl], s1 = leaf_start[sl + 1];
+      for (int base = s0; base < s1; base += kChunk) {
+        const int cnt = min(kChunk, s1 - base);
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) sz[i] = z[base + i];
+        for (int e = threadIdx.x; e < cnt * nc; e += blockDim.x) {
+          int i = e % cnt, cc = e / cnt;
+          sq[i][cc] = q[base + i + (size_t)n * cc];
+        }
+        __syncthreads();
+        if (!on) continue;
+        for (int i = 0; i < cnt; i++) {
+          if (base + i == t) continue;
+          const double dx = zt.x - sz[i].x, dy = zt.y - sz[i].y;
+          const double inv = 1.0 / (dx * dx + dy * dy);
+          const double rx = dx * inv, ry = -dy * inv;   // 1 / (t - s)
+#pragma unroll
+          for (int cc = 0; cc < kCols; cc++)
+            if (cc < nc) acc[cc] += sq[i][cc].x * rx - sq[i][cc].y * ry;
+        }
+      }
+    }
+    if (on) {
+      const int orig = perm[t];
+#pragma unroll
+      for (int cc = 0; cc < kCols; cc++)
+        if (cc < nc)
+          y[orig + (size_t)ldy * (c0 + cc)] =
+              acc[cc] + diag[t] * mu[orig + (size_t)ldmu * (c0 + cc)];
+    }
+  }
+}
+
+uint64_t morton(uint32_t ix, uint32_t iy) {
+  uint64_t k = 0;
+  for (int b = 0; b < 32; b++) {
+    k |= (uint64_t)((ix >> b) & 1u) << (2 * b + 1);
+    k |= (uint64_t)((iy >> b) & 1u) << (2 * b);
+  }
+  return k;
+}
+
+void demorton(uint64_t k, uint32_t* ix, uint32_t* iy) {
+  *ix = *iy = 0;
+  for (int b = 0; b < 32; b++) {
+    *ix |= (uint32_t)((k >> (2 * b + 1)) & 1u) << b;
+    *iy |= (uint32_t)((k >> (2 * b)) & 1u) << b;
+  }
+}
+
+double binom(int n, int k) {
+  double r = 1;
+  for (int i = 1; i <= k; i++) r = r * (n - k + i) / i;
+  return std::round(r);
+}
+
+template <typename V>
+V* upload_vec(const std::vector<V>& v, std::vector<void*>* owned, cudaStream_t s) {
+  V* d = nullptr;
+  KI_FMM_CUDA(cudaMalloc((void**)&d, sizeof(V) * std::max<size_t>(1, v.size())));
+  owned->push_back(d);
+  if (!v.empty())
+    KI_FMM_CUDA(cudaMemcpyAsync(d, v.data(), sizeof(V) * v.size(), cudaMemcpyHostToDevice, s));
+  return d;
+}
+
+}  // namespace
+
+struct Fmm2d {
+  int n = 0, p = 0, L = 0, nleaf = 0, nbox = 0;
+  long m2l_pairs = 0, near_pairs = 0;
+  double lo = 0, side0 = 0;
+  std::vector<int> lvl_off;   // global box index range of each level
+  int *d_perm = nullptr, *d_leaf_start = nullptr, *d_leaf_box = nullptr;
+  int *d_near_off = nullptr, *d_near_leaf = nullptr;
+  int *d_child = nullptr, *d_parent = nullptr, *d_child_pos = nullptr;
+  int *d_v_off = nullptr, *d_v_src = nullptr, *d_v_code = nullptr;
+  double2 *d_z = nullptr, *d_nw = nullptr, *d_centre = nullptr;
+  double2 *d_T = nullptr, *d_S = nullptr, *d_M = nullptr;
+  double* d_diag = nullptr;
+  std::vector<void*> owned;
+  ~Fmm2d() {
+    for (void* q : owned) cudaFree(q);
+  }
+};
+
+void Fmm2dDeleter::operator()(Fmm2d* f) const { delete f; }
+
+std::unique_ptr<Fmm2d, Fmm2dDeleter> fmm2d_build(const double* pts, const double* nrm,
+                                                 const double* wts, const double* kap, int n,
+                                                 int p, cudaStream_t s) {
+  if (n <= 0) throw std::invalid_argument("fmm: no points");
+  if (p < 4 || p > kMaxP) throw std::invalid_argument("fmm: expansion order out of range");
+  std::unique_ptr<Fmm2d, Fmm2dDeleter> F(new Fmm2d());
+  F->n = n;
+  F->p = p;
+  double mn = pts[0], mx = pts[0];
+  for (int i = 0; i < 2 * n; i++) {
+    mn = std::min(mn, pts[i]);
+    mx = std::max(mx, pts[i]);
+  }
+  F->lo = mn - 0.01;
+  F->side0 = (mx + 0.01) - F->lo;
+  auto cell = [&](double x, int L) {
+    long m = 1L << L;
+    long i = (long)std::floor((x - F->lo) / F->side0 * m);
+    return (uint32_t)std::min(m - 1, std::max(0L, i));
+  };
+  // Morton keys at the finest admissible level, one sort; a coarser level's
+  // key is a right shift, so the leaf level (refined while the non-empty
+  // leaves hold more than 40 points on average) is found by linear scans.
+  constexpr int kLmax = 20;
+  std::vector<std::pair<uint64_t, int>> kp(n);
+  for (int i = 0; i < n; i++)
+    kp[i] = {morton(cell(pts[2 * i], kLmax), cell(pts[2 * i + 1], kLmax)), i};
+  std::sort(kp.begin(), kp.end());   // ties by point index: deterministic
+  int L = 2;
+  for (;; L++) {
+    const int sh = 2 * (kLmax - L);
+    long nl = 0;
+    for (int i = 0; i < n; i++)
+      if (i == 0 || (kp[i].first >> sh) != (kp[i - 1].first >> sh)) nl++;
+    if ((double)n / nl <= 40.0 || L >= kLmax) break;
+  }
+  F->L = L;
+  std::vector<int> order(n);
+  std::vector<uint64_t> key(n);
+  for (int i = 0; i < n; i++) {
+    order[i] = kp[i].second;
+    key[kp[i].second] = kp[i].first >> (2 * (kLmax - L));
+  }
+  // leaves and levels (global box index: level 0 first)
+  std::vector<std::vector<uint64_t>> lk(L + 1);
+  std::vector<int> leaf_start;
+  for (int i = 0; i < n; i++) {
+    uint64_t k = key[order[i]];
+    if (lk[L].empty() || lk[L].back() != k) {
+      lk[L].push_back(k);
+      leaf_start.push_back(i);
+    }
+  }
+  leaf_start.push_back(n);
+  for (int l = L - 1; l >= 0; l--)
+    for (uint64_t k : lk[l + 1])
+      if (lk[l].empty() || lk[l].back() != (k >> 2)) lk[l].push_back(k >> 2);
+  F->lvl_off.assign(L + 2, 0);
+  for (int l = 0; l <= L; l++) F->lvl_off[l + 1] = F->lvl_off[l] + (int)lk[l].size();
+  const int nbox = F->lvl_off[L + 1];
+  F->nbox = nbox;
+  F->nleaf = (int)lk[L].size();
+  std::vector<std::unordered_map<uint64_t, int>> idx(L + 1);
+  for (int l = 0; l <= L; l++)
+    for (size_t i = 0; i < lk[l].size(); i++) idx[l][lk[l][i]] = F->lvl_off[l] + (int)i;
+  std::vector<double2> centre(nbox);
+  std::vector<int> parent(nbox, -1), child(4 * (size_t)nbox, -1), child_pos(nbox, 0);
+  for (int l = 0; l <= L; l++) {
+    const double side = F->side0 / (double)(1L << l);
+    for (size_t i = 0; i < lk[l].size(); i++) {
+      uint32_t ix, iy;
+      demorton(lk[l][i], &ix, &iy);
+      int g = F->lvl_off[l] + (int)i;
+      centre[g] = make_double2(F->lo + (ix + 0.5) * side, F->lo + (iy + 0.5) * side);
+      child_pos[g] = (int)(lk[l][i] & 3u);
+      if (l > 0) {
+        int pg = idx[l - 1].at(lk[l][i] >> 2);
+        parent[g] = pg;
+        child[4 * (size_t)pg + child_pos[g]] = g;
+      }
+    }
+  }
+  // near lists (leaf indices) and interaction lists
+  std::vector<int> near_off(1, 0), near_leaf;
+  for (size_t i = 0; i < lk[L].size(); i++) {
+    uint32_t ix, iy;
+    demorton(lk[L][i], &ix, &iy);
+    for (int di = -1; di <= 1; di++)
+      for (int dj = -1; dj <= 1; dj++) {
+        long a = (long)ix + di, b = (long)iy + dj;
+        if (a < 0 || b < 0) continue;
+        auto it = idx[L].find(morton((uint32_t)a, (uint32_t)b));
+        if (it != idx[L].end()) near_leaf.push_back(it->second - F->lvl_off[L]);
+      }
+    near_off.push_back((int)near_leaf.size());
+  }
+  std::vector<int> v_off(1, 0), v_src, v_code;
+  for (int l = 0; l <= L; l++) {
+    for (size_t i = 0; i < lk[l].size(); i++) {
+      if (l >= 2) {
+        uint32_t ix, iy;
+        demorton(lk[l][i], &ix, &iy);
+        long px = ix >> 1, py = iy >> 1;
+        for (int a = -1; a <= 1; a++)
+          for (int b = -1; b <= 1; b++)
+            for (int u = 0; u < 2; u++)
+              for (int w = 0; w < 2; w++) {
+                long sx = 2 * (px + a) + u, sy = 2 * (py + b) + w;
+                if (sx < 0 || sy < 0) continue;
+                long di = (long)ix - sx, dj = (long)iy - sy;
+                if (std::labs(di) <= 1 && std::labs(dj) <= 1) continue;
+                auto it = idx[l].find(morton((uint32_t)sx, (uint32_t)sy));
+                if (it == idx[l].end()) continue;
+                v_src.push_back(it->second);
+                v_code.push_back((int)((di + 3) * 7 + (dj + 3)));
+              }
+      }
+      v_off.push_back((int)v_src.size());
+    }
+  }
+  F->m2l_pairs = (long)v_src.size();
+  F->near_pairs = (long)near_leaf.size();
+  // translation matrices
+  std::vector<double2> T(4 * (size_t)p * p), S(4 * (size_t)p * p), M(49 * (size_t)p * p);
+  for (int pos = 0; pos < 4; pos++) {
+    // child offset from the parent centre in units of the parent side
+    std::complex<double> d((pos & 2) ? 0.25 : -0.25, (pos & 1) ? 0.25 : -0.25);
+    for (int k = 0; k < p; k++)
+      for (int j = 0; j < p; j++) {
+        std::complex<double> t = 0, u = 0;
+        if (j <= k) t = binom(k, j) * std::pow(0.5, j) * std::pow(d, k - j);   // M2M
+        if (j <= k) u = binom(k, j) * std::pow(0.5, j) * std::pow(d, k - j);   // L2L (j<->m)
+        T[(size_t)pos * p * p + (size_t)k * p + j] = make_double2(t.real(), t.imag());
+        S[(size_t)pos * p * p + (size_t)j * p + k] = make_double2(u.real(), u.imag());
+      }
+  }
+  for (int di = -3; di <= 3; di++)
+    for (int dj = -3; dj <= 3; dj++) {
+      int code = (di + 3) * 7 + (dj + 3);
+      if (std::abs(di) <= 1 && std::abs(dj) <= 1) continue;
+      std::complex<double> rho = 1.0 / std::complex<double>(di, dj);
+      for (int m = 0; m < p; m++)
+        for (int k = 0; k < p; k++) {
+          std::complex<double> v = rho * binom(k + m, m) * ((m & 1) ? -1.0 : 1.0) * std::pow(rho, k + m);
+          M[(size_t)code * p * p + (size_t)m * p + k] = make_double2(v.real(), v.imag());
+        }
+    }
+  // sorted point data
+  std::vector<double2> z(n), nw(n);
+  std::vector<double> dg(n);
+  for (int i = 0; i < n; i++) {
+    int o = order[i];
+    z[i] = make_double2(pts[2 * o], pts[2 * o + 1]);
+    double w = wts[o] / kPi2;
+    nw[i] = make_double2(-w * nrm[2 * o], -w * nrm[2 * o + 1]);
+    // Kernel::one_d_kern's coincident-point limit (kernel.cpp:37-38)
+    dg[i] = 0.5 + 0.5 * (kap ? kap[o] : 0.0) * wts[o] * (1.0 / kPi2);
+  }
+  std::vector<int> leaf_box(F->nleaf);
+  for (int i = 0; i < F->nleaf; i++) leaf_box[i] = F->lvl_off[L] + i;
+  F->d_perm = upload_vec(order, &F->owned, s);
+  F->d_leaf_start = upload_vec(leaf_start, &F->owned, s);
+  F->d_leaf_box = upload_vec(leaf_box, &F->owned, s);
+  F->d_near_off = upload_vec(near_off, &F->owned, s);
+  F->d_near_leaf = upload_vec(near_leaf, &F->owned, s);
+  F->d_child = upload_vec(child, &F->owned, s);
+  F->d_parent = upload_vec(parent, &F->owned, s);
+  F->d_child_pos = upload_vec(child_pos, &F->owned, s);
+  F->d_v_off = upload_vec(v_off, &F->owned, s);
+  F->d_v_src = upload_vec(v_src, &F->owned, s);
+  F->d_v_code = upload_vec(v_code, &F->owned, s);
+  F->d_z = upload_vec(z, &F->owned, s);
+  F->d_nw = upload_vec(nw, &F->owned, s);
+  F->d_centre = upload_vec(centre, &F->owned, s);
+  F->d_T = upload_vec(T, &F->owned, s);
+  F->d_S = upload_vec(S, &F->owned, s);
+  F->d_M = upload_vec(M, &F->owned, s);
+  F->d_diag = upload_vec(dg, &F->owned, s);
+  KI_FMM_CUDA(cudaStreamSynchronize(s));
+  return F;
+}
+
+void fmm2d_apply(Fmm2d& F, const double* mu, int ldmu, int ncols, double* y, int ldy,
+                 cudaStream_t s) {
+  const int n = F.n, p = F.p, L = F.L, nbox = F.nbox;
+  const int nc_max = std::min(ncols, kCols);
+  double2 *q = nullptr, *me = nullptr, *le = nullptr;
+  KI_FMM_CUDA(cudaMallocAsync((void**)&q, sizeof(double2) * (size_t)n * nc_max, s));
+  KI_FMM_CUDA(cudaMallocAsync((void**)&me, sizeof(double2) * (size_t)nbox * p * nc_max, s));
+  KI_FMM_CUDA(cudaMallocAsync((void**)&le, sizeof(double2) * (size_t)nbox * p * nc_max, s));
+  for (int c0 = 0; c0 < ncols; c0 += kCols) {
+    const int nc = std::min(kCols, ncols - c0);
+    k_charges<<<(int)std::min<size_t>(8192, ((size_t)n * nc + 255) / 256), 256, 0, s>>>(
+        F.d_nw, F.d_perm, n, mu, ldmu, c0, nc, q);
+    k_p2m<<<F.nleaf, 256, 0, s>>>(F.d_leaf_start, F.d_leaf_box, F.d_centre,
+                                  F.side0 / (double)(1L << L), F.d_z, q, n, nc, p, me);
+    for (int l = L; l >= 1; l--) {
+      const int b0 = F.lvl_off[l - 1], cnt = F.lvl_off[l] - b0;
+      k_m2m<<<cnt, 256, 0, s>>>(b0, F.d_child, F.d_child_pos, F.d_T, nc, p, me);
+    }
+    KI_FMM_CUDA(cudaMemsetAsync(le, 0, sizeof(double2) * (size_t)F.lvl_off[2] * p * nc, s));
+    for (int l = 2; l <= L; l++) {
+      const int b0 = F.lvl_off[l], cnt = F.lvl_off[l + 1] - b0;
+      k_m2l<<<cnt, 256, 0, s>>>(b0, F.d_v_off, F.d_v_src, F.d_v_code, F.d_M,
+                                (double)(1L << l) / F.side0, nc, p, me, le);
+    }
+    for (int l = 3; l <= L; l++) {
+      const int b0 = F.lvl_off[l], cnt = F.lvl_off[l + 1] - b0;
+      k_l2l<<<cnt, 256, 0, s>>>(b0, F.d_parent, F.d_child_pos, F.d_S, nc, p, le);
+    }
+    k_l2p_p2p<<<F.nleaf, 64, 0, s>>>(F.d_leaf_start, F.d_leaf_box, F.d_near_off, F.d_near_leaf,
+                                     F.d_centre, F.side0 / (double)(1L << L), F.d_z, F.d_diag,
+                                     F.d_perm, q, le, n, nc, p, mu, ldmu, c0, y, ldy);
+    KI_FMM_CUDA(cudaGetLastError());
+  }
+  KI_FMM_CUDA(cudaFreeAsync(q, s));
+  KI_FMM_CUDA(cudaFreeAsync(me, s));
+  KI_FMM_CUDA(cudaFreeAsync(le, s));
+}
+
+void fmm2d_stats(const Fmm2d& f, int* level, int* leaves, int* boxes, long* m2l_pairs,
+                 long* near_pairs) {
+  *level = f.L;
+  *leaves = f.nleaf;
+  *boxes = f.nbox;
+  *m2l_pairs = f.m2l_pairs;
+  *near_pairs = f.near_pairs;
+}
+
+}  // namespace ki

@@ -1,0 +1,44 @@
+// Fast FP64 apply of the 2D Laplace double-layer Nystrom operator by a
+// uniform-depth fast multipole method, for the residuals of iterative
+// refinement.
+//
+// The operator is the reference's (Kernel::one_d_kern, kern_interp/kernel/
+// kernel.cpp:33-43): K(t, s) = -w_s/(2 pi) (r . n_s)/|r|^2, r = t - s, and the
+// curvature limit 1/2 + kappa_t w_t/(4 pi) on the diagonal.  With complex
+// coordinates, (r . n_s)/|r|^2 = Re(n_s / (t - s)), so
+//   (K mu)(t) = diag_t mu_t + Re sum_{s != t} q_s / (t - s),
+//   q_s = -(w_s / 2 pi) n_s mu_s,
+// a Cauchy sum: multipole (Laurent) expansions about box centres, local
+// (Taylor) expansions, and the classical translations.  Expansions are
+// scaled by the box side so every translation matrix has entries below one.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+
+namespace ki {
+
+struct Fmm2d;
+
+struct Fmm2dDeleter {
+  void operator()(Fmm2d* f) const;
+};
+
+// Build the tree and the translation operators for n points (interleaved
+// FP64 host arrays) with p expansion terms.  Throws std::runtime_error.
+std::unique_ptr<Fmm2d, Fmm2dDeleter> fmm2d_build(const double* points, const double* normals,
+                                                 const double* weights, const double* curvatures,
+                                                 int n, int p, cudaStream_t s);
+
+// y (n x ncols, column-major, ldy) = K mu (n x ncols, ldmu), device buffers,
+// on stream s.
+void fmm2d_apply(Fmm2d& f, const double* mu, int ldmu, int ncols, double* y, int ldy,
+                 cudaStream_t s);
+
+// Tree statistics (for reports): leaf level, leaves, boxes, M2L pairs,
+// near-field leaf pairs.
+void fmm2d_stats(const Fmm2d& f, int* level, int* leaves, int* boxes, long* m2l_pairs,
+                 long* near_pairs);
+
+}  // namespace ki
