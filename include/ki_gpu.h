@@ -235,6 +235,15 @@ int ki_factor_set_profiling(ki_factor* f, int on);
  */
 int ki_measure_fma_peak(double* fp64_gflops, double* fp32_gflops);
 
+/*
+ * The library allocates its device memory stream-ordered from a pool of its
+ * own (one per device) that keeps freed memory for reuse, so repeated
+ * factorizations and solves do not map fresh pages each time.  This returns
+ * the memory the pool holds but no live factorization uses.  No reference
+ * counterpart (the reference allocates host memory with new[]).
+ */
+int ki_trim_memory(void);
+
 /* Message of the last failure on the calling thread ("" if none). */
 const char* ki_last_error(void);
 

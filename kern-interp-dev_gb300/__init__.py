@@ -31,7 +31,7 @@ EXPORTED = ["ki_factor_create", "ki_factor_destroy", "ki_factor_get_info", "ki_s
             "ki_solve_device", "ki_apply", "ki_eval_targets", "ki_last_error", "ki_version",
             "ki_factor_get_profile", "ki_factor_set_profiling", "ki_apply_rows",
             "ki_measure_fma_peak", "ki_solve_refined", "ki_solve_refined_device",
-            "ki_solve_device_noalloc", "ki_apply_fmm"]
+            "ki_solve_device_noalloc", "ki_apply_fmm", "ki_trim_memory"]
 
 
 class KiError(RuntimeError):

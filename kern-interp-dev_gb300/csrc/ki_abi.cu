@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <future>
 #include <memory>
 #include <mutex>
 #include <new>
@@ -13,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "ki_pool.h"
 #include "../../include/ki_gpu.h"
 #include "ki_common.cuh"
 #include "ki_factor.h"
@@ -220,6 +222,10 @@ __device__ double border_u(int dim, int sol_dim, int comp, int k, const double* 
 // y += U alpha, one thread per listed DOF (rows != nullptr: DOF rows[q] of
 // the points; else DOF q).  Points: dim per point with the given stride
 // between points (SoA x with stride 1 and separate y/z, or interleaved).
+// Each U entry (a log or a reciprocal distance) is evaluated once and
+// applied to up to 32 columns held in registers.
+constexpr int kBorderCols = 32;
+
 __global__ void k_border_apply(const double* px, const double* py, const double* pz, int stride,
                                int n_points, int dim, int sol_dim, const double* hc, int nh,
                                const double* alpha, int lda, int ncols, double* y, int ldy,
@@ -231,15 +237,25 @@ __global__ void k_border_apply(const double* px, const double* py, const double*
   const int cph = sol_dim == 1 ? 1 : (dim == 2 ? 3 : 6);
   const double xp[3] = {px[(size_t)stride * p], py[(size_t)stride * p],
                         dim == 3 ? pz[(size_t)stride * p] : 0.0};
-  for (int c = 0; c < ncols; c++) {
-    double acc = 0;
+  for (int c0 = 0; c0 < ncols; c0 += kBorderCols) {
+    const int nc = min(kBorderCols, ncols - c0);
+    double acc[kBorderCols];
+#pragma unroll
+    for (int c = 0; c < kBorderCols; c++) acc[c] = 0.0;
     for (int h = 0; h < nh; h++) {
       double r[3];
       for (int d = 0; d < dim; d++) r[d] = xp[d] - hc[dim * h + d];
-      const double* al = alpha + cph * h + (size_t)lda * c;
-      for (int k = 0; k < cph; k++) acc += border_u(dim, sol_dim, comp, k, r) * al[k];
+      for (int k = 0; k < cph; k++) {
+        const double u = border_u(dim, sol_dim, comp, k, r);
+        const double* al = alpha + cph * h + k + (size_t)lda * c0;
+#pragma unroll
+        for (int c = 0; c < kBorderCols; c++)
+          if (c < nc) acc[c] += u * al[(size_t)lda * c];
+      }
     }
-    y[q + (size_t)ldy * c] += acc;
+#pragma unroll
+    for (int c = 0; c < kBorderCols; c++)
+      if (c < nc) y[q + (size_t)ldy * (c0 + c)] += acc[c];
   }
 }
 
@@ -248,7 +264,7 @@ struct DevBuf {
   T* p = nullptr;
   cudaStream_t s = nullptr;
   DevBuf(size_t n, cudaStream_t st) : s(st) {
-    cudaError_t e = cudaMallocAsync((void**)&p, sizeof(T) * (n ? n : 1), st);
+    cudaError_t e = ki::pool_malloc((void**)&p, sizeof(T) * (n ? n : 1), st);
     if (e != cudaSuccess) {
       cudaGetLastError();
       throw std::runtime_error("device allocation failed");
@@ -283,9 +299,17 @@ struct ki_factor {
   int* d_hstart = nullptr;     // hole node ranges
   int* d_hcount = nullptr;
   ki::Points<double> P{};
-  // fast FP64 operator apply (2D Laplace), built on first use
+  // fast FP64 operator apply (2D Laplace): its host plan is computed on a
+  // worker thread while the factorization runs, uploaded on first use
+  std::future<std::unique_ptr<ki::Fmm2dPlan, ki::Fmm2dPlanDeleter>> fmm_plan;
   std::unique_ptr<ki::Fmm2d, ki::Fmm2dDeleter> fmm;
   ~ki_factor() {
+    if (fmm_plan.valid()) {
+      try {
+        fmm_plan.get();
+      } catch (...) {
+      }
+    }
     fmm.reset();
     f64.reset();
     f32.reset();
@@ -588,15 +612,15 @@ __global__ void k_add_rowmajor(const T* d, int n, int ncols, double* a, int lda)
 
 // y1 = K mu + U alpha, y2 = Psi mu - alpha (FP64, column-major, ld = N / nb).
 void apply_bordered(ki_factor* f, const double* mu, const double* alpha, int ncols, double* y1,
-                    double* y2, cudaStream_t s);
+                    double* y2, cudaStream_t s, double target);
 
 // Per-column relative residual of [mu; alpha] for right-hand side b:
 // returns max over columns of ||[b;0] - A[mu;alpha]|| / ||b||, leaves r1/r2.
 double residual_norms(ki_factor* f, const double* b, const double* mu, const double* alpha,
                       int ncols, double* r1, double* r2, double* work, std::vector<double>* rel,
-                      cudaStream_t s) {
+                      cudaStream_t s, double target) {
   const int N = f->n_dofs, nb = f->n_border;
-  apply_bordered(f, mu, alpha, ncols, r1, r2, s);
+  apply_bordered(f, mu, alpha, ncols, r1, r2, s, target);
   k_residual<<<grid_for((size_t)N * ncols), 256, 0, s>>>(b, N, r1, N, N, ncols, r1, N);
   if (nb > 0) k_residual<<<grid_for((size_t)nb * ncols), 256, 0, s>>>(nullptr, 0, r2, nb, nb, ncols, r2, nb);
   KI_CHECK_CUDA(cudaGetLastError());
@@ -667,13 +691,13 @@ void refined_solve(ki_factor* f, const double* b, int ncols, double* mu, double*
   };
   corr();   // x0 = M^-1 b
   std::vector<double> rel;
-  double res = residual_norms(f, b, mu, alpha, ncols, r1.p, r2.p, work.p, &rel, s);
+  double res = residual_norms(f, b, mu, alpha, ncols, r1.p, r2.p, work.p, &rel, s, tol);
   info->residual0 = res;
   int steps = 0;
   while (res > tol && steps < max_steps) {
     corr();
     steps++;
-    res = residual_norms(f, b, mu, alpha, ncols, r1.p, r2.p, work.p, &rel, s);
+    res = residual_norms(f, b, mu, alpha, ncols, r1.p, r2.p, work.p, &rel, s, tol);
   }
   info->steps = steps;
   info->residual = res;
@@ -688,7 +712,30 @@ void refined_solve(ki_factor* f, const double* b, int ncols, double* mu, double*
 namespace {
 bool fmm_capable(const ki_factor* f) { return f->dim == 2 && f->sol_dim == 1; }
 
+// Expansion terms of the FMM plan (translation matrices for every lower
+// order are leading blocks, so one plan serves any accuracy).
+int fmm_order() {
+  int p = 32;
+  if (const char* e = std::getenv("KI_FMM_P")) p = std::atoi(e);
+  return p;
+}
+
+// Terms for a refinement target: the smallest order whose expected relative
+// error, 1.4e-8 * 0.43^(p - 16) (measured max-norm error of K x for random x
+// on the 2D Laplace disc-with-ellipses family at 1,048,576 unknowns: 1.4e-8
+// at 16 terms, 4.8e-10 at 20, 1.6e-11 at 24), is 50x below the target.
+int fmm_order_for(double target, int plan_order) {
+  if (const char* e = std::getenv("KI_FMM_P")) return std::atoi(e);
+  int p = 12;
+  while (p < plan_order && 1.4e-8 * std::pow(0.43, p - 16) > target / 50) p++;
+  return p;
+}
+
 ki::Fmm2d& fmm_for(ki_factor* f, cudaStream_t s) {
+  if (!f->fmm && f->fmm_plan.valid()) {
+    auto plan = f->fmm_plan.get();
+    f->fmm = ki::fmm2d_upload(*plan, s);
+  }
   if (!f->fmm) {
     // geometry back from the device copy (the handle keeps no host arrays)
     const int n = f->n_points;
@@ -702,10 +749,8 @@ ki::Fmm2d& fmm_for(ki_factor* f, cudaStream_t s) {
       nrm[2 * i] = geo[2 * (size_t)n + i];
       nrm[2 * i + 1] = geo[3 * (size_t)n + i];
     }
-    int p = 24;
-    if (const char* e = std::getenv("KI_FMM_P")) p = std::atoi(e);
     f->fmm = ki::fmm2d_build(pts.data(), nrm.data(), geo.data() + 4 * (size_t)n,
-                             geo.data() + 5 * (size_t)n, n, p, s);
+                             geo.data() + 5 * (size_t)n, n, fmm_order(), s);
   }
   return *f->fmm;
 }
@@ -718,10 +763,13 @@ bool use_fmm(const ki_factor* f) {
   return f->n_dofs >= 4096;
 }
 
-void apply_K(ki_factor* f, const double* mu, int ncols, double* y1, cudaStream_t s, bool fast) {
+// fast: FMM with `order` terms (0: 24, relative error ~2e-11)
+void apply_K(ki_factor* f, const double* mu, int ncols, double* y1, cudaStream_t s, bool fast,
+             int order = 0) {
   const int N = f->n_dofs;
   if (fast) {
-    ki::fmm2d_apply(fmm_for(f, s), mu, N, ncols, y1, N, s);
+    ki::Fmm2d& F = fmm_for(f, s);
+    ki::fmm2d_apply(F, mu, N, ncols, y1, N, s, order > 0 ? order : std::min(24, ki::fmm2d_order(F)));
     return;
   }
   dim3 grid((N + kApplyThreads - 1) / kApplyThreads, (ncols + kApplyCols - 1) / kApplyCols);
@@ -731,9 +779,10 @@ void apply_K(ki_factor* f, const double* mu, int ncols, double* y1, cudaStream_t
 }
 
 void apply_bordered(ki_factor* f, const double* mu, const double* alpha, int ncols, double* y1,
-                    double* y2, cudaStream_t s) {
+                    double* y2, cudaStream_t s, double target) {
   const int N = f->n_dofs, nb = f->n_border;
-  apply_K(f, mu, ncols, y1, s, use_fmm(f));
+  const bool fast = use_fmm(f);
+  apply_K(f, mu, ncols, y1, s, fast, fast ? fmm_order_for(target, ki::fmm2d_order(fmm_for(f, s))) : 0);
   if (nb > 0) {
     k_border_apply<<<(N + 127) / 128, 128, 0, s>>>(f->P.x, f->P.y, f->P.z, 1, f->n_points, f->dim,
                                                    f->sol_dim, f->d_holes, f->n_holes, alpha, nb,
@@ -825,6 +874,40 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
     KI_CHECK_CUDA(cudaMalloc(&f->d_pts, sizeof(double) * dim * (size_t)n));
     KI_CHECK_CUDA(cudaMemcpy(f->d_pts, desc->points, sizeof(double) * dim * (size_t)n,
                              cudaMemcpyHostToDevice));
+    // 2D Laplace: the FMM plan for refinement residuals, on a worker thread
+    // concurrent with the factorization (it copies the caller's arrays first;
+    // this call returns only after the copy)
+    std::promise<void> copied;
+    std::future<void> copied_f = copied.get_future();
+    bool planning = false;
+    if (fmm_capable(f.get()) && f->n_dofs >= 4096 && !std::getenv("KI_NO_FMM_PREPLAN")) {
+      planning = true;
+      const double *pp = desc->points, *nn = desc->normals, *ww = desc->weights,
+                   *kk = desc->curvatures;
+      const int order = fmm_order();
+      f->fmm_plan = std::async(std::launch::async, [pp, nn, ww, kk, n, order, &copied] {
+        std::vector<double> P, Nn, W, K;
+        try {
+          P.assign(pp, pp + 2 * (size_t)n);
+          Nn.assign(nn, nn + 2 * (size_t)n);
+          W.assign(ww, ww + n);
+          if (kk) K.assign(kk, kk + n);
+          else K.assign(n, 0.0);
+        } catch (...) {
+          copied.set_value();
+          throw;
+        }
+        copied.set_value();
+        return ki::fmm2d_plan(P.data(), Nn.data(), W.data(), K.data(), n, order);
+      });
+    }
+    struct WaitCopy {   // the caller's arrays stay valid until the worker has copied them
+      bool on;
+      std::future<void>& fut;
+      ~WaitCopy() {
+        if (on) fut.wait();
+      }
+    } wait_copy{planning, copied_f};
     if (f->precision == KI_PRECISION_FP64)
       f->f64 = ki::factorize<double>(prm, n, desc->points, desc->normals, desc->weights,
                                      desc->curvatures, holes, f->stream);
@@ -1153,6 +1236,10 @@ int ki_measure_fma_peak(double* fp64_gflops, double* fp32_gflops) {
     *fp64_gflops = fma_peak_gflops<double>(sms, 20000);
     *fp32_gflops = fma_peak_gflops<float>(sms, 200000);
   });
+}
+
+int ki_trim_memory(void) {
+  return guarded([&] { KI_CHECK_CUDA(ki::pool_trim()); });
 }
 
 const char* ki_last_error(void) { return g_last_error.c_str(); }

@@ -19,6 +19,7 @@
 //                    box's accumulated self-block K_ss - L K~_rs
 //
 // The host reads back only the ranks of each level (to size the next level).
+#include "ki_pool.h"
 #include "ki_factor.h"
 
 #include <cuda_runtime.h>
@@ -49,7 +50,7 @@ template <typename T>
 void* Factorization<T>::alloc(size_t bytes) {
   void* p = nullptr;
   if (bytes == 0) bytes = 16;
-  cudaError_t e = cudaMallocAsync(&p, bytes, stream);
+  cudaError_t e = pool_malloc(&p, bytes, stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
     throw std::runtime_error(std::string("device allocation failed: ") + cudaGetErrorString(e));
@@ -1614,7 +1615,7 @@ void reduce_rows(Factorization<T>& F, const T* A, int na, const T* B, int nc, T*
                  cudaStream_t s) {
   int parts = (F.N + kRedRows - 1) / kRedRows;
   T* partial = nullptr;
-  KI_CUDA(cudaMallocAsync((void**)&partial, sizeof(T) * (size_t)parts * na * nc + 16, s));
+  KI_CUDA(pool_malloc((void**)&partial, sizeof(T) * (size_t)parts * na * nc + 16, s));
   if (na * nc > 16 * 256) throw std::runtime_error("border too wide for the row reduction");
   size_t sm = sizeof(T) * 32 * (size_t)(na + nc);
   if (sm > 48 * 1024)
@@ -1644,7 +1645,7 @@ void reduce_rows_wide(Factorization<T>& F, const T* A, int na, T* B, int nc, T* 
   const int chunk = 16384;
   const int parts = (N + chunk - 1) / chunk;
   T* partial = nullptr;
-  KI_CUDA(cudaMallocAsync((void**)&partial, sizeof(T) * (size_t)parts * na * nc + 16, s));
+  KI_CUDA(pool_malloc((void**)&partial, sizeof(T) * (size_t)parts * na * nc + 16, s));
   // DOF-major A is the column-major na x N matrix Ac; out = Ac * Bc^T
   dim3 g((na + 63) / 64, (nc + 63) / 64, parts);
   k_gemm<T><<<g, 256, 0, s>>>(na, nc, N, T(1), A, na, 0, B, nc, 1, T(0), partial, na, chunk,
@@ -2105,9 +2106,9 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
           mtot += kQrNb * kQrNb;
         }
         T* d_wpool = nullptr;
-        KI_CUDA(cudaMallocAsync((void**)&d_wpool, sizeof(T) * (mtot + 16), ws3));
+        KI_CUDA(pool_malloc((void**)&d_wpool, sizeof(T) * (mtot + 16), ws3));
         WideTask* d_wt = nullptr;
-        KI_CUDA(cudaMallocAsync((void**)&d_wt, sizeof(WideTask) * wt.size(), ws3));
+        KI_CUDA(pool_malloc((void**)&d_wt, sizeof(WideTask) * wt.size(), ws3));
         upload(d_wt, wt, ws3);
         std::string wq = "wide_qr@L" + std::to_string(l);
         F->stage_begin(wq.c_str(), 0, 0, ws3);
@@ -2347,7 +2348,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         }
         F->stage_end();
         T* dD = nullptr;
-        KI_CUDA(cudaMallocAsync((void**)&dD, Tsz * (size_t)N * nb, s));
+        KI_CUDA(pool_malloc((void**)&dD, Tsz * (size_t)N * nb, s));
         KI_CUDA(cudaMemcpyAsync(dD, F->d_Umod, Tsz * (size_t)N * nb, cudaMemcpyDeviceToDevice, s));
         F->stage_begin("border_Dinv", 0, 0);
         for (int l = L - 1; l >= 1; l--) launch_sweep<T>(*F, l, kDiag, dD, nb, s);
@@ -2405,7 +2406,7 @@ void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, const T* d
     if (nr > 0) {
       sb("root_solve");
       T* ws = nullptr;
-      KI_CUDA(cudaMallocAsync((void**)&ws, sizeof(T) * (size_t)nr * ncols + 16, s));
+      KI_CUDA(pool_malloc((void**)&ws, sizeof(T) * (size_t)nr * ncols + 16, s));
       int gb = std::max(1, std::min(4096, (nr * ncols + 255) / 256));
       k_gather_rows<T><<<gb, 256, 0, s>>>(d_x, ncols, F.d_root_idx, nr, ncols, ws);
       dense_lu_solve<T>(F.d_root_lu, nr, F.d_root_piv, ws, nr, ncols, false, s);
@@ -2429,9 +2430,9 @@ void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, const T* d
   se();
   sb("border_diag");
   T *Dw = nullptr, *t = nullptr, *M = nullptr;
-  KI_CUDA(cudaMallocAsync((void**)&Dw, sizeof(T) * (size_t)N * ncols + 16, s));
-  KI_CUDA(cudaMallocAsync((void**)&t, sizeof(T) * (size_t)nb * ncols + 16, s));
-  KI_CUDA(cudaMallocAsync((void**)&M, sizeof(T) * (size_t)ns * ncols + 16, s));
+  KI_CUDA(pool_malloc((void**)&Dw, sizeof(T) * (size_t)N * ncols + 16, s));
+  KI_CUDA(pool_malloc((void**)&t, sizeof(T) * (size_t)nb * ncols + 16, s));
+  KI_CUDA(pool_malloc((void**)&M, sizeof(T) * (size_t)ns * ncols + 16, s));
   KI_CUDA(cudaMemcpyAsync(Dw, d_x, sizeof(T) * (size_t)N * ncols, cudaMemcpyDeviceToDevice, s));
   for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kDiag, Dw, ncols, s);
   se();

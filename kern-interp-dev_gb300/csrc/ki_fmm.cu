@@ -9,6 +9,7 @@
 // expansion plus the direct near-field sum with the exact kernel entries.
 // All 32 columns of a pass share every kernel-entry and translation-matrix
 // load.
+#include "ki_pool.h"
 #include "ki_fmm.h"
 
 #include <algorithm>
@@ -101,50 +102,77 @@ __global__ void k_p2m(const int* leaf_start, const int* leaf_box, const double2*
 }
 
 // Multipole of each box of one level from its children (M2M):
-// me[P] = sum_children T_pos me[C], T_pos lower triangular p x p.
-__global__ void k_m2m(int b0, const int* child, const int* child_pos, const double2* T, int nc,
-                      int p, double2* me) {
+// me[P] = sum_children T_pos me[C], T_pos lower triangular (matrix leading
+// dimension ldm >= p).  Each child's expansions and its matrix are staged in
+// shared memory; output (k, c) is thread c + nc k.
+__global__ void k_m2m(int b0, const int* child, const int* child_pos, const double2* T, int ldm,
+                      int nc, int p, double2* me) {
+  __shared__ double2 sm_x[kCols * (kMaxP + 1)];
+  __shared__ double2 sm_T[kMaxP * kMaxP];
   const int g = b0 + blockIdx.x;
-  const int nout = p * nc;
-  for (int o = threadIdx.x; o < nout; o += blockDim.x) {
-    const int k = o % p, cc = o / p;
-    double2 a = make_double2(0, 0);
-    for (int q = 0; q < 4; q++) {
-      const int ch = child[4 * g + q];
-      if (ch < 0) continue;
-      const double2* Tm = T + (size_t)child_pos[ch] * p * p + (size_t)k * p;
-      const double2* src = me + (size_t)ch * nout + (size_t)cc * p;
-      for (int j = 0; j <= k; j++) a = cfma(Tm[j], src[j], a);
+  const int nout = p * nc, ld = p + 1;
+  double2 acc[4];
+  for (int r = 0; r < 4; r++) acc[r] = make_double2(0, 0);
+  for (int q = 0; q < 4; q++) {
+    const int ch = child[4 * g + q];
+    if (ch < 0) continue;
+    __syncthreads();
+    const double2* src = me + (size_t)ch * nout;
+    for (int e = threadIdx.x; e < nout; e += blockDim.x) sm_x[(e / p) * ld + e % p] = src[e];
+    const double2* Tm = T + (size_t)child_pos[ch] * ldm * ldm;
+    for (int e = threadIdx.x; e < p * p; e += blockDim.x) sm_T[e] = Tm[(size_t)(e / p) * ldm + e % p];
+    __syncthreads();
+    for (int r = 0; r < 4; r++) {
+      int o = threadIdx.x + r * blockDim.x;
+      if (o >= nout) break;
+      const int cc = o % nc, k = o / nc;
+      double2 a = acc[r];
+      const double2* row = sm_T + k * p;
+      const double2* x = sm_x + cc * ld;
+      for (int j = 0; j <= k; j++) a = cfma(row[j], x[j], a);
+      acc[r] = a;
     }
-    me[(size_t)g * nout + o] = a;
+  }
+  for (int r = 0; r < 4; r++) {
+    int o = threadIdx.x + r * blockDim.x;
+    if (o >= nout) break;
+    const int cc = o % nc, k = o / nc;
+    me[(size_t)g * nout + (size_t)cc * p + k] = acc[r];
   }
 }
 
 // Local expansion contributions over the interaction list (M2L): for every
-// box g of one level, le[g] = (1/side) sum_v M_code(v) me[src(v)].
+// box g of one level, le[g] = (1/side) sum_v M_code(v) me[src(v)].  Output
+// (m, c) is thread c + nc m, so a warp shares one matrix row (broadcast) and
+// reads 32 columns of the staged multipole tile (row stride p + 1 doubles2:
+// conflict-free).
 __global__ void k_m2l(int b0, const int* v_off, const int* v_src, const int* v_code,
-                      const double2* M, double inv_side, int nc, int p, const double2* me,
-                      double2* le) {
-  __shared__ double2 sm_me[kCols * kMaxP];
+                      const double2* M, int ldm, double inv_side, int nc, int p,
+                      const double2* me, double2* le) {
+  __shared__ double2 sm_me[kCols * (kMaxP + 1)];
   __shared__ double2 sm_M[kMaxP * kMaxP];
   const int g = b0 + blockIdx.x;
   const int nout = p * nc;
+  const int ld = p + 1;
   double2 acc[4];
   for (int r = 0; r < 4; r++) acc[r] = make_double2(0, 0);
   for (int v = v_off[g]; v < v_off[g + 1]; v++) {
     __syncthreads();
     const double2* src = me + (size_t)v_src[v] * nout;
-    for (int e = threadIdx.x; e < nout; e += blockDim.x) sm_me[e] = src[e];
-    const double2* Mm = M + (size_t)v_code[v] * p * p;
-    for (int e = threadIdx.x; e < p * p; e += blockDim.x) sm_M[e] = Mm[e];
+    for (int e = threadIdx.x; e < nout; e += blockDim.x) {
+      const int k = e % p, cc = e / p;
+      sm_me[cc * ld + k] = src[e];
+    }
+    const double2* Mm = M + (size_t)v_code[v] * ldm * ldm;
+    for (int e = threadIdx.x; e < p * p; e += blockDim.x) sm_M[e] = Mm[(size_t)(e / p) * ldm + e % p];
     __syncthreads();
     for (int r = 0; r < 4; r++) {
       int o = threadIdx.x + r * blockDim.x;
       if (o >= nout) break;
-      const int m = o % p, cc = o / p;
+      const int cc = o % nc, m = o / nc;
       double2 a = acc[r];
       const double2* row = sm_M + m * p;
-      const double2* x = sm_me + cc * p;
+      const double2* x = sm_me + cc * ld;
       for (int k = 0; k < p; k++) a = cfma(row[k], x[k], a);
       acc[r] = a;
     }
@@ -152,35 +180,62 @@ __global__ void k_m2l(int b0, const int* v_off, const int* v_src, const int* v_c
   for (int r = 0; r < 4; r++) {
     int o = threadIdx.x + r * blockDim.x;
     if (o >= nout) break;
-    le[(size_t)g * nout + o] = make_double2(acc[r].x * inv_side, acc[r].y * inv_side);
+    const int cc = o % nc, m = o / nc;
+    le[(size_t)g * nout + (size_t)cc * p + m] = make_double2(acc[r].x * inv_side, acc[r].y * inv_side);
   }
 }
 
 // Local expansion of each box of one level += its parent's, translated (L2L):
-// le[C] += S_pos le[P], S_pos upper triangular.
-__global__ void k_l2l(int b0, const int* parent, const int* child_pos, const double2* S, int nc,
-                      int p, double2* le) {
+// le[C] += S_pos le[P], S_pos upper triangular (leading dimension ldm); the
+// parent's expansions and the matrix staged in shared memory, output (j, c)
+// is thread c + nc j.
+__global__ void k_l2l(int b0, const int* parent, const int* child_pos, const double2* S, int ldm,
+                      int nc, int p, double2* le) {
+  __shared__ double2 sm_x[kCols * (kMaxP + 1)];
+  __shared__ double2 sm_S[kMaxP * kMaxP];
   const int g = b0 + blockIdx.x;
   const int par = parent[g];
-  const int nout = p * nc;
-  const double2* Sm = S + (size_t)child_pos[g] * p * p;
+  const int nout = p * nc, ld = p + 1;
+  const double2* src = le + (size_t)par * nout;
+  for (int e = threadIdx.x; e < nout; e += blockDim.x) sm_x[(e / p) * ld + e % p] = src[e];
+  const double2* Sm = S + (size_t)child_pos[g] * ldm * ldm;
+  for (int e = threadIdx.x; e < p * p; e += blockDim.x) sm_S[e] = Sm[(size_t)(e / p) * ldm + e % p];
+  __syncthreads();
   for (int o = threadIdx.x; o < nout; o += blockDim.x) {
-    const int j = o % p, cc = o / p;
-    const double2* src = le + (size_t)par * nout + (size_t)cc * p;
-    double2 a = le[(size_t)g * nout + o];
-    for (int m = j; m < p; m++) a = cfma(Sm[(size_t)j * p + m], src[m], a);
-    le[(size_t)g * nout + o] = a;
+    const int cc = o % nc, j = o / nc;
+    const size_t dst = (size_t)g * nout + (size_t)cc * p + j;
+    double2 a = le[dst];
+    const double2* row = sm_S + j * p;
+    const double2* x = sm_x + cc * ld;
+    for (int m = j; m < p; m++) a = cfma(row[m], x[m], a);
+    le[dst] = a;
   }
+}
+
+// 1/x for a positive FP64 x (a squared distance): the correctly rounded
+// single-precision reciprocal as the seed, refined by two Newton-Raphson
+// steps y <- y + y (1 - x y) (the relative error squares each step: ~1e-7,
+// ~1e-14, then FP64 rounding).  x stays within the single-precision normal
+// range (squared distances between boundary nodes of unit-scale geometry).
+__device__ __forceinline__ double recip_nr(double x) {
+  double y = (double)__frcp_rn((float)x);
+  double e = fma(-x, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-x, y, 1.0);
+  return fma(y, e, y);
 }
 
 // Per leaf: far field from the local expansion, near field by direct
 // summation over the 3 x 3 leaf neighbourhood (exact entries, the
-// coincident point excluded), diagonal term; written unsorted into y.
-__global__ void k_l2p_p2p(const int* leaf_start, const int* leaf_box, const int* near_off,
-                          const int* near_leaf, const double2* centre, double side,
-                          const double2* z, const double* diag, const int* perm, const double2* q,
-                          const double2* le, int n, int nc, int p, const double* mu, int ldmu,
-                          int c0, double* y, int ldy) {
+// coincident point excluded), diagonal term; written unsorted into y.  One
+// thread per target with all 32 columns in registers.
+constexpr int kP2PThreads = 64;
+
+__global__ void __launch_bounds__(kP2PThreads)
+    k_l2p_p2p(const int* leaf_start, const int* leaf_box, const int* near_off,
+              const int* near_leaf, const double2* centre, double side, const double2* z,
+              const double* diag, const int* perm, const double2* q, const double2* le, int n,
+              int nc, int p, const double* mu, int ldmu, int c0, double* y, int ldy) {
   __shared__ double2 sz[kChunk];
   __shared__ double2 sq[kChunk][kCols];
   __shared__ double2 sle[kCols * kMaxP];
@@ -228,7 +283,7 @@ __global__ void k_l2p_p2p(const int* leaf_start, const int* leaf_box, const int*
         for (int i = 0; i < cnt; i++) {
           if (base + i == t) continue;
           const double dx = zt.x - sz[i].x, dy = zt.y - sz[i].y;
-          const double inv = 1.0 / (dx * dx + dy * dy);
+          const double inv = recip_nr(dx * dx + dy * dy);
           const double rx = dx * inv, ry = -dy * inv;   // 1 / (t - s)
 #pragma unroll
           for (int cc = 0; cc < kCols; cc++)
@@ -273,7 +328,7 @@ double binom(int n, int k) {
 template <typename V>
 V* upload_vec(const std::vector<V>& v, std::vector<void*>* owned, cudaStream_t s) {
   V* d = nullptr;
-  KI_FMM_CUDA(cudaMalloc((void**)&d, sizeof(V) * std::max<size_t>(1, v.size())));
+  KI_FMM_CUDA(pool_malloc((void**)&d, sizeof(V) * std::max<size_t>(1, v.size()), s));
   owned->push_back(d);
   if (!v.empty())
     KI_FMM_CUDA(cudaMemcpyAsync(d, v.data(), sizeof(V) * v.size(), cudaMemcpyHostToDevice, s));
@@ -295,19 +350,32 @@ struct Fmm2d {
   double2 *d_T = nullptr, *d_S = nullptr, *d_M = nullptr;
   double* d_diag = nullptr;
   std::vector<void*> owned;
+  cudaStream_t stream = nullptr;   // the upload stream; frees are ordered on it
   ~Fmm2d() {
-    for (void* q : owned) cudaFree(q);
+    for (void* q : owned) cudaFreeAsync(q, stream);
   }
 };
 
 void Fmm2dDeleter::operator()(Fmm2d* f) const { delete f; }
 
-std::unique_ptr<Fmm2d, Fmm2dDeleter> fmm2d_build(const double* pts, const double* nrm,
-                                                 const double* wts, const double* kap, int n,
-                                                 int p, cudaStream_t s) {
+// Host-side plan: everything fmm2d_upload copies to the device.
+struct Fmm2dPlan {
+  int n = 0, p = 0, L = 0, nleaf = 0, nbox = 0;
+  double lo = 0, side0 = 0;
+  std::vector<int> lvl_off, order, leaf_start, leaf_box, near_off, near_leaf, child, parent,
+      child_pos, v_off, v_src, v_code;
+  std::vector<double2> z, nw, centre, T, S, M;
+  std::vector<double> diag;
+};
+
+void Fmm2dPlanDeleter::operator()(Fmm2dPlan* f) const { delete f; }
+
+std::unique_ptr<Fmm2dPlan, Fmm2dPlanDeleter> fmm2d_plan(const double* pts, const double* nrm,
+                                                        const double* wts, const double* kap,
+                                                        int n, int p) {
   if (n <= 0) throw std::invalid_argument("fmm: no points");
   if (p < 4 || p > kMaxP) throw std::invalid_argument("fmm: expansion order out of range");
-  std::unique_ptr<Fmm2d, Fmm2dDeleter> F(new Fmm2d());
+  std::unique_ptr<Fmm2dPlan, Fmm2dPlanDeleter> F(new Fmm2dPlan());
   F->n = n;
   F->p = p;
   double mn = pts[0], mx = pts[0];
@@ -422,8 +490,6 @@ std::unique_ptr<Fmm2d, Fmm2dDeleter> fmm2d_build(const double* pts, const double
       v_off.push_back((int)v_src.size());
     }
   }
-  F->m2l_pairs = (long)v_src.size();
-  F->near_pairs = (long)near_leaf.size();
   // translation matrices
   std::vector<double2> T(4 * (size_t)p * p), S(4 * (size_t)p * p), M(49 * (size_t)p * p);
   for (int pos = 0; pos < 4; pos++) {
@@ -462,36 +528,77 @@ std::unique_ptr<Fmm2d, Fmm2dDeleter> fmm2d_build(const double* pts, const double
   }
   std::vector<int> leaf_box(F->nleaf);
   for (int i = 0; i < F->nleaf; i++) leaf_box[i] = F->lvl_off[L] + i;
-  F->d_perm = upload_vec(order, &F->owned, s);
-  F->d_leaf_start = upload_vec(leaf_start, &F->owned, s);
-  F->d_leaf_box = upload_vec(leaf_box, &F->owned, s);
-  F->d_near_off = upload_vec(near_off, &F->owned, s);
-  F->d_near_leaf = upload_vec(near_leaf, &F->owned, s);
-  F->d_child = upload_vec(child, &F->owned, s);
-  F->d_parent = upload_vec(parent, &F->owned, s);
-  F->d_child_pos = upload_vec(child_pos, &F->owned, s);
-  F->d_v_off = upload_vec(v_off, &F->owned, s);
-  F->d_v_src = upload_vec(v_src, &F->owned, s);
-  F->d_v_code = upload_vec(v_code, &F->owned, s);
-  F->d_z = upload_vec(z, &F->owned, s);
-  F->d_nw = upload_vec(nw, &F->owned, s);
-  F->d_centre = upload_vec(centre, &F->owned, s);
-  F->d_T = upload_vec(T, &F->owned, s);
-  F->d_S = upload_vec(S, &F->owned, s);
-  F->d_M = upload_vec(M, &F->owned, s);
-  F->d_diag = upload_vec(dg, &F->owned, s);
+  F->order = std::move(order);
+  F->leaf_start = std::move(leaf_start);
+  F->leaf_box = std::move(leaf_box);
+  F->near_off = std::move(near_off);
+  F->near_leaf = std::move(near_leaf);
+  F->child = std::move(child);
+  F->parent = std::move(parent);
+  F->child_pos = std::move(child_pos);
+  F->v_off = std::move(v_off);
+  F->v_src = std::move(v_src);
+  F->v_code = std::move(v_code);
+  F->z = std::move(z);
+  F->nw = std::move(nw);
+  F->centre = std::move(centre);
+  F->T = std::move(T);
+  F->S = std::move(S);
+  F->M = std::move(M);
+  F->diag = std::move(dg);
+  return F;
+}
+
+std::unique_ptr<Fmm2d, Fmm2dDeleter> fmm2d_upload(const Fmm2dPlan& P, cudaStream_t s) {
+  std::unique_ptr<Fmm2d, Fmm2dDeleter> F(new Fmm2d());
+  F->stream = s;
+  F->n = P.n;
+  F->p = P.p;
+  F->L = P.L;
+  F->nleaf = P.nleaf;
+  F->nbox = P.nbox;
+  F->lo = P.lo;
+  F->side0 = P.side0;
+  F->lvl_off = P.lvl_off;
+  F->m2l_pairs = (long)P.v_src.size();
+  F->near_pairs = (long)P.near_leaf.size();
+  F->d_perm = upload_vec(P.order, &F->owned, s);
+  F->d_leaf_start = upload_vec(P.leaf_start, &F->owned, s);
+  F->d_leaf_box = upload_vec(P.leaf_box, &F->owned, s);
+  F->d_near_off = upload_vec(P.near_off, &F->owned, s);
+  F->d_near_leaf = upload_vec(P.near_leaf, &F->owned, s);
+  F->d_child = upload_vec(P.child, &F->owned, s);
+  F->d_parent = upload_vec(P.parent, &F->owned, s);
+  F->d_child_pos = upload_vec(P.child_pos, &F->owned, s);
+  F->d_v_off = upload_vec(P.v_off, &F->owned, s);
+  F->d_v_src = upload_vec(P.v_src, &F->owned, s);
+  F->d_v_code = upload_vec(P.v_code, &F->owned, s);
+  F->d_z = upload_vec(P.z, &F->owned, s);
+  F->d_nw = upload_vec(P.nw, &F->owned, s);
+  F->d_centre = upload_vec(P.centre, &F->owned, s);
+  F->d_T = upload_vec(P.T, &F->owned, s);
+  F->d_S = upload_vec(P.S, &F->owned, s);
+  F->d_M = upload_vec(P.M, &F->owned, s);
+  F->d_diag = upload_vec(P.diag, &F->owned, s);
   KI_FMM_CUDA(cudaStreamSynchronize(s));
   return F;
 }
 
+std::unique_ptr<Fmm2d, Fmm2dDeleter> fmm2d_build(const double* pts, const double* nrm,
+                                                 const double* wts, const double* kap, int n,
+                                                 int p, cudaStream_t s) {
+  return fmm2d_upload(*fmm2d_plan(pts, nrm, wts, kap, n, p), s);
+}
+
 void fmm2d_apply(Fmm2d& F, const double* mu, int ldmu, int ncols, double* y, int ldy,
-                 cudaStream_t s) {
-  const int n = F.n, p = F.p, L = F.L, nbox = F.nbox;
+                 cudaStream_t s, int order) {
+  const int n = F.n, L = F.L, nbox = F.nbox, ldm = F.p;
+  const int p = order > 0 ? std::min(order, F.p) : F.p;
   const int nc_max = std::min(ncols, kCols);
   double2 *q = nullptr, *me = nullptr, *le = nullptr;
-  KI_FMM_CUDA(cudaMallocAsync((void**)&q, sizeof(double2) * (size_t)n * nc_max, s));
-  KI_FMM_CUDA(cudaMallocAsync((void**)&me, sizeof(double2) * (size_t)nbox * p * nc_max, s));
-  KI_FMM_CUDA(cudaMallocAsync((void**)&le, sizeof(double2) * (size_t)nbox * p * nc_max, s));
+  KI_FMM_CUDA(pool_malloc((void**)&q, sizeof(double2) * (size_t)n * nc_max, s));
+  KI_FMM_CUDA(pool_malloc((void**)&me, sizeof(double2) * (size_t)nbox * p * nc_max, s));
+  KI_FMM_CUDA(pool_malloc((void**)&le, sizeof(double2) * (size_t)nbox * p * nc_max, s));
   for (int c0 = 0; c0 < ncols; c0 += kCols) {
     const int nc = std::min(kCols, ncols - c0);
     k_charges<<<(int)std::min<size_t>(8192, ((size_t)n * nc + 255) / 256), 256, 0, s>>>(
@@ -500,27 +607,30 @@ void fmm2d_apply(Fmm2d& F, const double* mu, int ldmu, int ncols, double* y, int
                                   F.side0 / (double)(1L << L), F.d_z, q, n, nc, p, me);
     for (int l = L; l >= 1; l--) {
       const int b0 = F.lvl_off[l - 1], cnt = F.lvl_off[l] - b0;
-      k_m2m<<<cnt, 256, 0, s>>>(b0, F.d_child, F.d_child_pos, F.d_T, nc, p, me);
+      k_m2m<<<cnt, 256, 0, s>>>(b0, F.d_child, F.d_child_pos, F.d_T, ldm, nc, p, me);
     }
     KI_FMM_CUDA(cudaMemsetAsync(le, 0, sizeof(double2) * (size_t)F.lvl_off[2] * p * nc, s));
     for (int l = 2; l <= L; l++) {
       const int b0 = F.lvl_off[l], cnt = F.lvl_off[l + 1] - b0;
-      k_m2l<<<cnt, 256, 0, s>>>(b0, F.d_v_off, F.d_v_src, F.d_v_code, F.d_M,
+      k_m2l<<<cnt, 256, 0, s>>>(b0, F.d_v_off, F.d_v_src, F.d_v_code, F.d_M, ldm,
                                 (double)(1L << l) / F.side0, nc, p, me, le);
     }
     for (int l = 3; l <= L; l++) {
       const int b0 = F.lvl_off[l], cnt = F.lvl_off[l + 1] - b0;
-      k_l2l<<<cnt, 256, 0, s>>>(b0, F.d_parent, F.d_child_pos, F.d_S, nc, p, le);
+      k_l2l<<<cnt, 256, 0, s>>>(b0, F.d_parent, F.d_child_pos, F.d_S, ldm, nc, p, le);
     }
-    k_l2p_p2p<<<F.nleaf, 64, 0, s>>>(F.d_leaf_start, F.d_leaf_box, F.d_near_off, F.d_near_leaf,
-                                     F.d_centre, F.side0 / (double)(1L << L), F.d_z, F.d_diag,
-                                     F.d_perm, q, le, n, nc, p, mu, ldmu, c0, y, ldy);
+    k_l2p_p2p<<<F.nleaf, kP2PThreads, 0, s>>>(
+        F.d_leaf_start, F.d_leaf_box, F.d_near_off, F.d_near_leaf, F.d_centre,
+        F.side0 / (double)(1L << L), F.d_z, F.d_diag, F.d_perm, q, le, n, nc, p, mu, ldmu, c0, y,
+        ldy);
     KI_FMM_CUDA(cudaGetLastError());
   }
   KI_FMM_CUDA(cudaFreeAsync(q, s));
   KI_FMM_CUDA(cudaFreeAsync(me, s));
   KI_FMM_CUDA(cudaFreeAsync(le, s));
 }
+
+int fmm2d_order(const Fmm2d& f) { return f.p; }
 
 void fmm2d_stats(const Fmm2d& f, int* level, int* leaves, int* boxes, long* m2l_pairs,
                  long* near_pairs) {

@@ -20,21 +20,40 @@
 namespace ki {
 
 struct Fmm2d;
+struct Fmm2dPlan;
 
 struct Fmm2dDeleter {
   void operator()(Fmm2d* f) const;
 };
+struct Fmm2dPlanDeleter {
+  void operator()(Fmm2dPlan* f) const;
+};
 
-// Build the tree and the translation operators for n points (interleaved
-// FP64 host arrays) with p expansion terms.  Throws std::runtime_error.
+// Host part of the build: tree, lists and translation matrices for n points
+// (interleaved FP64 host arrays) with p expansion terms.  Pure host work,
+// safe on a worker thread.  Throws std::invalid_argument.
+std::unique_ptr<Fmm2dPlan, Fmm2dPlanDeleter> fmm2d_plan(const double* points,
+                                                        const double* normals,
+                                                        const double* weights,
+                                                        const double* curvatures, int n, int p);
+
+// Device part: upload a plan.  Throws std::runtime_error.
+std::unique_ptr<Fmm2d, Fmm2dDeleter> fmm2d_upload(const Fmm2dPlan& plan, cudaStream_t s);
+
+// Both steps.
 std::unique_ptr<Fmm2d, Fmm2dDeleter> fmm2d_build(const double* points, const double* normals,
                                                  const double* weights, const double* curvatures,
                                                  int n, int p, cudaStream_t s);
 
 // y (n x ncols, column-major, ldy) = K mu (n x ncols, ldmu), device buffers,
-// on stream s.
+// on stream s, with `order` <= the plan's expansion terms (0: all of them);
+// the translation matrices of a lower order are leading blocks of the
+// plan's.
 void fmm2d_apply(Fmm2d& f, const double* mu, int ldmu, int ncols, double* y, int ldy,
-                 cudaStream_t s);
+                 cudaStream_t s, int order = 0);
+
+// Expansion terms the plan was built with.
+int fmm2d_order(const Fmm2d& f);
 
 // Tree statistics (for reports): leaf level, leaves, boxes, M2L pairs,
 // near-field leaf pairs.
