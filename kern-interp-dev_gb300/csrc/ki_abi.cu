@@ -123,27 +123,48 @@ __device__ __forceinline__ double pair_entry(int dim, int sol_dim, int tpar, int
   return ki::stokes_entry<double>(tpar, spar, tx, ty, tnx, tny, sx, sy, snx, sny, sw, sk);
 }
 
+// Dense FP64 product over one chunk of source points (blockIdx.z):
+// out[z][row + ldo c] = sum over the chunk's sources of K(target(row), s) x_s.
+// Targets are boundary DOFs (rows[row], or row itself when rows is null; the
+// target normal is the DOF's own) or, when tg is given, domain points
+// (dim coordinates per point, target normal 0: the reference's forward mode,
+// kernel.cpp:335-339 / :390-400).  One thread per target row, sources staged
+// through shared memory, kApplyCols columns per blockIdx.y.  With one chunk
+// the block writes y directly; otherwise partial sums are reduced in a fixed
+// order by k_chunk_reduce.
 __global__ void k_dense_apply(ki::Points<double> P, int n_points, int sol_dim, const double* x,
-                              int ldx, int ncols, double* y, int ldy, const int* rows, int nrows) {
+                              int ldx, int ncols, double* out, int ldo, size_t chunk_stride,
+                              int chunk_pts, const int* rows, int nrows, const double* tg) {
   __shared__ double sx[kApplyTile], sy[kApplyTile], sz[kApplyTile], snx[kApplyTile],
       sny[kApplyTile], snz[kApplyTile], sw[kApplyTile], sk[kApplyTile];
   const int dim = P.dim;
   const int dpp = dim == 3 ? (sol_dim == 1 ? 1 : 9) : 0;
-  const int N = rows ? nrows : n_points * sol_dim;
+  const int N = (rows || tg) ? nrows : n_points * sol_dim;
   const int trow = blockIdx.x * blockDim.x + threadIdx.x;
   const int tdof = rows ? (trow < nrows ? rows[trow] : 0) : (trow < N ? trow : 0);
   const int c0 = blockIdx.y * kApplyCols;
   const int nc = min(kApplyCols, ncols - c0);
+  const int s_lo = blockIdx.z * chunk_pts, s_hi = min(n_points, s_lo + chunk_pts);
+  double* o = out + chunk_stride * blockIdx.z;
   double acc[kApplyCols];
   for (int c = 0; c < kApplyCols; c++) acc[c] = 0.0;
   const int tp = tdof / sol_dim, tpar = tdof - sol_dim * tp;
-  const double tx = P.x[tp], ty = P.y[tp], tnx = P.nx[tp], tny = P.ny[tp];
-  const double tz = dim == 3 ? P.z[tp] : 0.0, tnz = dim == 3 ? P.nz[tp] : 0.0;
-  for (int base = 0; base < n_points; base += kApplyTile) {
+  double tx, ty, tz, tnx, tny, tnz;
+  if (tg) {
+    tx = tg[(size_t)dim * tp];
+    ty = tg[(size_t)dim * tp + 1];
+    tz = dim == 3 ? tg[3 * (size_t)tp + 2] : 0.0;
+    tnx = tny = tnz = 0.0;
+  } else {
+    tx = P.x[tp]; ty = P.y[tp]; tnx = P.nx[tp]; tny = P.ny[tp];
+    tz = dim == 3 ? P.z[tp] : 0.0;
+    tnz = dim == 3 ? P.nz[tp] : 0.0;
+  }
+  for (int base = s_lo; base < s_hi; base += kApplyTile) {
     __syncthreads();
     for (int i = threadIdx.x; i < kApplyTile; i += blockDim.x) {
       int p = base + i;
-      if (p < n_points) {
+      if (p < s_hi) {
         sx[i] = P.x[p]; sy[i] = P.y[p]; snx[i] = P.nx[p]; sny[i] = P.ny[p]; sw[i] = P.w[p];
         sk[i] = P.kappa[p];
         sz[i] = dim == 3 ? P.z[p] : 0.0;
@@ -152,7 +173,7 @@ __global__ void k_dense_apply(ki::Points<double> P, int n_points, int sol_dim, c
     }
     __syncthreads();
     if (trow >= N) continue;
-    int lim = min(kApplyTile, n_points - base);
+    int lim = min(kApplyTile, s_hi - base);
     for (int i = 0; i < lim; i++) {
       const double* dg = dpp ? P.diag + (size_t)dpp * (base + i) : nullptr;
       for (int sp = 0; sp < sol_dim; sp++) {
@@ -164,33 +185,18 @@ __global__ void k_dense_apply(ki::Points<double> P, int n_points, int sol_dim, c
     }
   }
   if (trow < N)
-    for (int c = 0; c < nc; c++) y[trow + (size_t)ldy * (c0 + c)] = acc[c];
+    for (int c = 0; c < nc; c++) o[trow + (size_t)ldo * (c0 + c)] = acc[c];
 }
 
-// Forward evaluation at domain targets (target normal 0, the reference's
-// forward mode, kernel.cpp:335-339 / :390-400).  Targets: dim per point.
-__global__ void k_forward(ki::Points<double> P, int n_points, int sol_dim, const double* tg,
-                          int nt, const double* mu, int ldmu, int ncols, double* out, int ldout) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int NT = nt * sol_dim;
-  if (t >= NT) return;
-  const int dim = P.dim;
-  const int dpp = dim == 3 ? (sol_dim == 1 ? 1 : 9) : 0;
-  const int tp = t / sol_dim, tpar = t - sol_dim * tp;
-  const double tx = tg[(size_t)dim * tp], ty = tg[(size_t)dim * tp + 1];
-  const double tz = dim == 3 ? tg[3 * (size_t)tp + 2] : 0.0;
-  for (int c = 0; c < ncols; c++) {
-    double acc = 0.0;
-    for (int p = 0; p < n_points; p++) {
-      const double* dg = dpp ? P.diag + (size_t)dpp * p : nullptr;
-      for (int sp = 0; sp < sol_dim; sp++) {
-        double kv = pair_entry(dim, sol_dim, tpar, sp, tx, ty, tz, 0.0, 0.0, 0.0, P.x[p], P.y[p],
-                               dim == 3 ? P.z[p] : 0.0, P.nx[p], P.ny[p],
-                               dim == 3 ? P.nz[p] : 0.0, P.w[p], P.kappa[p], dg);
-        acc += kv * mu[p * sol_dim + sp + (size_t)ldmu * c];
-      }
-    }
-    out[t + (size_t)ldout * c] = acc;
+// y[row + ldy c] = sum over chunks z (in order) of part[z][row + nrows c].
+__global__ void k_chunk_reduce(const double* part, int nchunks, int nrows, int ncols, double* y,
+                               int ldy) {
+  const size_t tot = (size_t)nrows * ncols;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot;
+       e += (size_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int z = 0; z < nchunks; z++) s += part[tot * z + e];
+    y[(e % nrows) + (size_t)ldy * (e / nrows)] = s;
   }
 }
 
@@ -278,6 +284,40 @@ struct DevBuf {
 };
 
 int grid_for(size_t n) { return (int)std::min<size_t>(4096, (n + 255) / 256 + 1); }
+
+// y (nrows x ncols, ldy) = dense FP64 product for the given targets (see
+// k_dense_apply): all boundary DOFs (rows == tg == null, nrows = N), listed
+// DOFs, or domain points.  Few target rows get the source range split into
+// chunks so that the launch still fills the GPU; their partial sums are
+// added in a fixed order.
+void dense_product(const ki::Points<double>& P, int n_points, int sol_dim, const double* x,
+                   int ldx, int ncols, double* y, int ldy, const int* rows, int nrows,
+                   const double* tg, cudaStream_t s) {
+  const int N = (rows || tg) ? nrows : n_points * sol_dim;
+  if (N == 0 || ncols == 0) return;
+  const int gx = (N + kApplyThreads - 1) / kApplyThreads;
+  const int gy = (ncols + kApplyCols - 1) / kApplyCols;
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int chunks = std::max(1, std::min((4 * sms + gx * gy - 1) / (gx * gy), n_points / kApplyTile));
+  chunks = std::min(chunks, 1024);
+  const int chunk_pts = (n_points + chunks - 1) / chunks;
+  chunks = (n_points + chunk_pts - 1) / chunk_pts;
+  if (chunks == 1) {
+    k_dense_apply<<<dim3(gx, gy, 1), kApplyThreads, 0, s>>>(P, n_points, sol_dim, x, ldx, ncols,
+                                                           y, ldy, 0, chunk_pts, rows, nrows, tg);
+    KI_CHECK_CUDA(cudaGetLastError());
+    return;
+  }
+  const size_t stride = (size_t)N * ncols;
+  DevBuf<double> part(stride * chunks, s);
+  k_dense_apply<<<dim3(gx, gy, chunks), kApplyThreads, 0, s>>>(P, n_points, sol_dim, x, ldx, ncols,
+                                                              part.p, N, stride, chunk_pts, rows,
+                                                              nrows, tg);
+  k_chunk_reduce<<<grid_for(stride), 256, 0, s>>>(part.p, chunks, N, ncols, y, ldy);
+  KI_CHECK_CUDA(cudaGetLastError());
+}
 
 }  // namespace
 
@@ -772,10 +812,7 @@ void apply_K(ki_factor* f, const double* mu, int ncols, double* y1, cudaStream_t
     ki::fmm2d_apply(F, mu, N, ncols, y1, N, s, order > 0 ? order : std::min(24, ki::fmm2d_order(F)));
     return;
   }
-  dim3 grid((N + kApplyThreads - 1) / kApplyThreads, (ncols + kApplyCols - 1) / kApplyCols);
-  k_dense_apply<<<grid, kApplyThreads, 0, s>>>(f->P, f->n_points, f->sol_dim, mu, N, ncols, y1, N,
-                                               nullptr, 0);
-  KI_CHECK_CUDA(cudaGetLastError());
+  dense_product(f->P, f->n_points, f->sol_dim, mu, N, ncols, y1, N, nullptr, 0, nullptr, s);
 }
 
 void apply_bordered(ki_factor* f, const double* mu, const double* alpha, int ncols, double* y1,
@@ -1008,10 +1045,7 @@ int ki_apply(ki_factor* f, const double* x, int ldx, int ncols, const double* al
     DevBuf<double> dx((size_t)N * ncols, s), dy((size_t)N * ncols, s);
     KI_CHECK_CUDA(cudaMemcpy2DAsync(dx.p, sizeof(double) * N, x, sizeof(double) * ldx,
                                     sizeof(double) * N, ncols, cudaMemcpyHostToDevice, s));
-    dim3 grid((N + kApplyThreads - 1) / kApplyThreads, (ncols + kApplyCols - 1) / kApplyCols);
-    k_dense_apply<<<grid, kApplyThreads, 0, s>>>(f->P, f->n_points, f->sol_dim, dx.p, N, ncols, dy.p, N,
-                                                 nullptr, 0);
-    KI_CHECK_CUDA(cudaGetLastError());
+    dense_product(f->P, f->n_points, f->sol_dim, dx.p, N, ncols, dy.p, N, nullptr, 0, nullptr, s);
     if (f->n_border > 0 && alpha) {
       if (ldalpha < f->n_border) throw ArgError("bad ldalpha");
       DevBuf<double> da((size_t)f->n_border * ncols, s);
@@ -1078,10 +1112,8 @@ int ki_apply_rows(ki_factor* f, const int* rows, int nrows, const double* x, int
     KI_CHECK_CUDA(cudaMemcpyAsync(dr.p, rows, sizeof(int) * nrows, cudaMemcpyHostToDevice, s));
     KI_CHECK_CUDA(cudaMemcpy2DAsync(dx.p, sizeof(double) * N, x, sizeof(double) * ldx,
                                     sizeof(double) * N, ncols, cudaMemcpyHostToDevice, s));
-    dim3 grid((nrows + kApplyThreads - 1) / kApplyThreads, (ncols + kApplyCols - 1) / kApplyCols);
-    k_dense_apply<<<grid, kApplyThreads, 0, s>>>(f->P, f->n_points, f->sol_dim, dx.p, N, ncols,
-                                                 dy.p, nrows, dr.p, nrows);
-    KI_CHECK_CUDA(cudaGetLastError());
+    dense_product(f->P, f->n_points, f->sol_dim, dx.p, N, ncols, dy.p, nrows, dr.p, nrows, nullptr,
+                  s);
     if (f->n_border > 0 && alpha) {
       if (ldalpha < f->n_border) throw ArgError("bad ldalpha");
       DevBuf<double> da((size_t)f->n_border * ncols, s);
@@ -1114,8 +1146,7 @@ int ki_eval_targets(ki_factor* f, const double* targets, int n_targets, const do
     KI_CHECK_CUDA(cudaMemcpyAsync(dt.p, targets, sizeof(double) * dim * n_targets, cudaMemcpyHostToDevice, s));
     KI_CHECK_CUDA(cudaMemcpy2DAsync(dm.p, sizeof(double) * N, mu, sizeof(double) * ldmu,
                                     sizeof(double) * N, ncols, cudaMemcpyHostToDevice, s));
-    k_forward<<<(NT + 127) / 128, 128, 0, s>>>(f->P, f->n_points, f->sol_dim, dt.p, n_targets, dm.p,
-                                               N, ncols, dout.p, NT);
+    dense_product(f->P, f->n_points, f->sol_dim, dm.p, N, ncols, dout.p, NT, nullptr, NT, dt.p, s);
     KI_CHECK_CUDA(cudaGetLastError());
     if (f->n_border > 0 && alpha) {
       if (ldalpha < f->n_border) throw ArgError("bad ldalpha");
