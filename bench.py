@@ -48,6 +48,10 @@ def parse():
                     help="fp64: one plain solve (the reference's arithmetic), no refinement")
     ap.add_argument("--no-compare", action="store_true",
                     help="mixed: do not also time the FP64 form at the same residual")
+    ap.add_argument("--learned-rank", default="on", choices=["on", "off"],
+                    help="mixed: size sketched IDs with the shipped rank predictor")
+    ap.add_argument("--compare-learned", action="store_true",
+                    help="mixed: also time the mixed form without the rank predictor")
     ap.add_argument("--workload", default="laplace2d_disc_ellipses",
                     choices=["laplace2d_disc_ellipses", "stokes2d_disc_circles", "laplace2d_star",
                              "laplace3d_ellipsoid"])
@@ -308,11 +312,14 @@ def main():
         --mixed-tol refined against the FP64 operator to --target; fp64 =
         FP64 factorization at --tol, refined to --target unless --no-refine;
         fp32 = plain FP32 factorization and solve."""
-        if precision == "mixed":
-            return wl.factor_kw(args.mixed_tol, pkg.PRECISION_FP32), True
+        if precision in ("mixed", "mixed-plain"):
+            kw = wl.factor_kw(args.mixed_tol, pkg.PRECISION_FP32)
+            if precision == "mixed" and args.learned_rank == "on":
+                kw["rank_model"] = "default"
+            return kw, True
         if precision == "fp64":
             return wl.factor_kw(args.tol, pkg.PRECISION_FP64), not args.no_refine
-        return wl.factor_kw(args.tol, pkg.PRECISION_FP32), False
+        return wl.factor_kw(args.mixed_tol, pkg.PRECISION_FP32), False
 
     def run_form(precision, steps, warmup):
         kw, refine = form(precision)
@@ -386,6 +393,16 @@ def main():
     barrier()
     t_e2e = rep.max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps, device="cuda")
 
+    # ---- the mixed form without the rank predictor (what the network gains)
+    learned = None
+    if args.precision == "mixed" and args.learned_rank == "on":
+        learned = {"boxes_sketched": info.get("n_sketched"), "fallbacks": info.get("n_fallback")}
+        if args.compare_learned:
+            c = run_form("mixed-plain", max(1, min(args.steps, 2)), 1)
+            learned.update({"without_predictor_ms_per_step": c["t_dev"] * 1e3,
+                            "with_predictor_ms_per_step": t_dev * 1e3,
+                            "speedup_from_predictor": c["t_dev"] / t_dev,
+                            "refine_without": c["infos"][-1] if c["infos"] else None})
     # ---- the FP64 form at the same target residual, for the comparison
     compare = None
     if args.precision == "mixed" and not args.no_compare:
@@ -510,6 +527,7 @@ def main():
                                                                   and N >= 4096) else "dense FP64"}
         if refine else None,
         "fp64_form_same_residual": compare,
+        "learned_rank": learned,
         "roofline": roofline,
         "stages": stage_table,
         "solve_stages": solve_prof,

@@ -41,7 +41,7 @@ typedef enum {
 
 typedef enum {
   KI_PRECISION_FP64 = 0,   /* plain form: every stage in FP64 (the reference's arithmetic) */
-  KI_PRECISION_FP32 = 1    /* FP32 factorization (preconditioner for refinement) */
+  KI_PRECISION_FP32 = 1    /* FP32 factorization (preconditioner for refinement); id_tol >= 5e-8 */
 } ki_precision;
 
 /*
@@ -73,6 +73,14 @@ typedef struct {
   int min_dofs_to_compress;
   double id_tol;
   int precision;             /* ki_precision */
+  /* Learned rank predictor (no reference counterpart): a model blob of
+   * ki_rank_model_floats() floats (see ki_rank_model_train) or NULL.  Used by
+   * FP32 factorizations only: each box whose ID fits the shared-memory kernel
+   * is compressed from a random sketch of l = min(n, 1.25 k^ + 8) rows, k^
+   * the predicted rank; a sketch that does not reveal the rank within l
+   * pivots is recompressed by the plain ID.  FP64 factorizations ignore it
+   * (they keep the reference's deterministic ID). */
+  const float* rank_model;
 } ki_problem_desc;
 
 typedef struct ki_factor ki_factor;
@@ -86,6 +94,8 @@ typedef struct {
   int n_border;         /* bordered unknowns (holes x border columns) */
   double factor_seconds;
   long device_bytes;    /* device memory held by the factorization */
+  int n_sketched;       /* boxes compressed from a sketch (learned rank) */
+  int n_fallback;       /* sketches recompressed by the plain ID */
 } ki_factor_info;
 
 /*
@@ -234,6 +244,35 @@ int ki_factor_set_profiling(ki_factor* f, int on);
  * counterpart: the compute denominators of the roofline figures.
  */
 int ki_measure_fma_peak(double* fp64_gflops, double* fp32_gflops);
+
+/*
+ * Learned rank predictor (no reference counterpart): a 12-64-64-1 MLP
+ * (ReLU hidden layers, logistic output) mapping per-box features to the rank
+ * fraction k/n of the box's interpolative decomposition, trained and
+ * evaluated by the library's own FP32 CUDA kernels.  Feature rows are the
+ * first 12 floats of the box log below.
+ *
+ * ki_rank_model_floats: size of a model blob (feature mean and scale,
+ *   weights, biases).
+ * ki_rank_model_train: full-batch Adam on the mean squared error over n
+ *   samples (features: n x 12 row-major, ratios: n); the blob is initialized
+ *   from the data (feature standardization) and `seed` (weights), trained for
+ *   `epochs` steps of rate `lr`, and written to `model`; `loss` receives the
+ *   final mean squared error.  Deterministic for given inputs.
+ * ki_rank_model_predict: ratios (n) for n feature rows.
+ * ki_rank_model_grad: the loss and its gradient with respect to the blob
+ *   (the standardization entries get zero) -- for checking the kernels.
+ * ki_factor_get_box_log: per ID box of the factorization, 15 floats: the 12
+ *   features, the box's active DOFs n, its rank k (0: not compressed) and its
+ *   level; at most max_rows rows are written, *rows receives the total.
+ */
+int ki_rank_model_floats(void);
+int ki_rank_model_train(const float* features, const float* ratios, int n, int epochs, float lr,
+                        unsigned seed, float* model, float* loss);
+int ki_rank_model_predict(const float* model, const float* features, int n, float* ratios);
+int ki_rank_model_grad(const float* model, const float* features, const float* ratios, int n,
+                       float* grad, float* loss);
+int ki_factor_get_box_log(const ki_factor* f, float* out, int max_rows, int* rows);
 
 /*
  * The library allocates its device memory stream-ordered from a pool of its

@@ -31,7 +31,11 @@ EXPORTED = ["ki_factor_create", "ki_factor_destroy", "ki_factor_get_info", "ki_s
             "ki_solve_device", "ki_apply", "ki_eval_targets", "ki_last_error", "ki_version",
             "ki_factor_get_profile", "ki_factor_set_profiling", "ki_apply_rows",
             "ki_measure_fma_peak", "ki_solve_refined", "ki_solve_refined_device",
-            "ki_solve_device_noalloc", "ki_apply_fmm", "ki_trim_memory"]
+            "ki_solve_device_noalloc", "ki_apply_fmm", "ki_trim_memory", "ki_rank_model_floats",
+            "ki_rank_model_train", "ki_rank_model_predict", "ki_rank_model_grad",
+            "ki_factor_get_box_log"]
+RANK_MODEL_PATH = os.path.join(HERE, "rank_model.npy")
+BOX_LOG_COLUMNS = 15   # 12 features, n, k, level
 
 
 class KiError(RuntimeError):
@@ -49,7 +53,8 @@ class _Desc(ctypes.Structure):
                 ("hole_node_start", ctypes.c_void_p), ("hole_node_count", ctypes.c_void_p),
                 ("max_leaf_dofs", ctypes.c_int), ("num_proxy_points", ctypes.c_int),
                 ("radius_ratio", ctypes.c_double), ("min_dofs_to_compress", ctypes.c_int),
-                ("id_tol", ctypes.c_double), ("precision", ctypes.c_int)]
+                ("id_tol", ctypes.c_double), ("precision", ctypes.c_int),
+                ("rank_model", ctypes.c_void_p)]
 
 
 class _RefineInfo(ctypes.Structure):
@@ -61,7 +66,8 @@ class _Info(ctypes.Structure):
     _fields_ = [("n_dofs", ctypes.c_int), ("n_levels", ctypes.c_int),
                 ("n_compressed", ctypes.c_int), ("n_redundant", ctypes.c_long),
                 ("n_root", ctypes.c_int), ("n_border", ctypes.c_int),
-                ("factor_seconds", ctypes.c_double), ("device_bytes", ctypes.c_long)]
+                ("factor_seconds", ctypes.c_double), ("device_bytes", ctypes.c_long),
+                ("n_sketched", ctypes.c_int), ("n_fallback", ctypes.c_int)]
 
 
 _lib = None
@@ -93,6 +99,11 @@ def load_library(path=None):
                                      ctypes.POINTER(_RefineInfo)]
     lib.ki_solve_refined_device.argtypes = [V, V, I, V, V, ctypes.c_double, I,
                                             ctypes.POINTER(_RefineInfo), V]
+    F = ctypes.POINTER(ctypes.c_float)
+    lib.ki_rank_model_train.argtypes = [V, V, I, I, ctypes.c_float, ctypes.c_uint, V, F]
+    lib.ki_rank_model_predict.argtypes = [V, V, I, V]
+    lib.ki_rank_model_grad.argtypes = [V, V, V, I, V, F]
+    lib.ki_factor_get_box_log.argtypes = [V, V, I, ctypes.POINTER(I)]
     lib.ki_measure_fma_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     lib.ki_last_error.restype = ctypes.c_char_p
     lib.ki_version.restype = ctypes.c_char_p
@@ -118,10 +129,13 @@ class Factor:
     def __init__(self, points, normals, weights, curvatures=None, id_tol=1e-10,
                  solution_dimension=1, pde=PDE_LAPLACE, hole_centers=None, hole_start=None,
                  hole_count=None, max_leaf_dofs=64, num_proxy_points=0, radius_ratio=2.0,
-                 min_dofs_to_compress=64, precision=PRECISION_FP64, domain_dimension=None):
+                 min_dofs_to_compress=64, precision=PRECISION_FP64, domain_dimension=None,
+                 rank_model=None):
         """points/normals: (n, dim) arrays, dim 2 or 3 (inferred unless given).
         num_proxy_points 0 takes the reference default (128 on a circle in 2D,
-        the 8 x 4 theta x phi sphere = 32 in 3D)."""
+        the 8 x 4 theta x phi sphere = 32 in 3D).  rank_model: a learned rank
+        predictor blob (float32 array; "default" loads rank_model.npy) that
+        FP32 factorizations use to size sketched IDs."""
         lib = load_library()
         dim = int(domain_dimension or np.asarray(points).shape[-1])
         if dim not in (2, 3):
@@ -136,11 +150,15 @@ class Factor:
         hs = np.ascontiguousarray(hole_start, np.int32) if nh else None
         hn = np.ascontiguousarray(hole_count, np.int32) if nh else None
         self._keep += [hc, hs, hn]
+        if isinstance(rank_model, str) and rank_model == "default":
+            rank_model = load_rank_model()
+        rm = None if rank_model is None else np.ascontiguousarray(rank_model, np.float32)
+        self._keep.append(rm)
         n = self._keep[2].shape[0]
         d = _Desc(n, dim, solution_dimension, pde, _ptr(self._keep[0]), _ptr(self._keep[1]),
                   _ptr(self._keep[2]), _ptr(self._keep[3]), nh, _ptr(hc), _ptr(hs), _ptr(hn),
                   max_leaf_dofs, num_proxy_points, radius_ratio, min_dofs_to_compress,
-                  id_tol, precision)
+                  id_tol, precision, _ptr(rm))
         h = ctypes.c_void_p()
         _check(lib.ki_factor_create(ctypes.byref(d), ctypes.byref(h)))
         self._h = h
@@ -165,6 +183,16 @@ class Factor:
         i = _Info()
         _check(load_library().ki_factor_get_info(self._h, ctypes.byref(i)))
         return {f: getattr(i, f) for f, _ in _Info._fields_}
+
+    def box_log(self):
+        """(rows, 15) float32: per ID box the 12 predictor features, n, k, level."""
+        lib = load_library()
+        rows = ctypes.c_int()
+        _check(lib.ki_factor_get_box_log(self._h, None, 0, ctypes.byref(rows)))
+        out = np.zeros((rows.value, BOX_LOG_COLUMNS), np.float32)
+        if rows.value:
+            _check(lib.ki_factor_get_box_log(self._h, _ptr(out), rows.value, ctypes.byref(rows)))
+        return out
 
     def profile(self):
         """Per-stage device times and algorithmic counts (dict)."""
@@ -281,6 +309,45 @@ class Factor:
                                               self.n_dofs, M.shape[1], _ptr(A),
                                               max(1, self.n_border), _ptr(out), nt))
         return out[:, 0] if vec else out
+
+
+def rank_model_floats():
+    return int(load_library().ki_rank_model_floats())
+
+
+def load_rank_model(path=None):
+    """The trained rank-predictor blob shipped with the package."""
+    return np.load(path or RANK_MODEL_PATH).astype(np.float32)
+
+
+def rank_model_train(features, ratios, epochs=2000, lr=3e-3, seed=0):
+    """Train the rank MLP on the GPU; returns (model blob, final MSE)."""
+    X = np.ascontiguousarray(features, np.float32)
+    y = np.ascontiguousarray(ratios, np.float32)
+    m = np.zeros(rank_model_floats(), np.float32)
+    loss = ctypes.c_float()
+    _check(load_library().ki_rank_model_train(_ptr(X), _ptr(y), X.shape[0], epochs, lr, seed,
+                                              _ptr(m), ctypes.byref(loss)))
+    return m, float(loss.value)
+
+
+def rank_model_predict(model, features):
+    X = np.ascontiguousarray(features, np.float32)
+    out = np.zeros(X.shape[0], np.float32)
+    _check(load_library().ki_rank_model_predict(_ptr(np.ascontiguousarray(model, np.float32)),
+                                                _ptr(X), X.shape[0], _ptr(out)))
+    return out
+
+
+def rank_model_grad(model, features, ratios):
+    """(loss, gradient) of the mean squared error, from the GPU kernels."""
+    X = np.ascontiguousarray(features, np.float32)
+    y = np.ascontiguousarray(ratios, np.float32)
+    g = np.zeros(rank_model_floats(), np.float32)
+    loss = ctypes.c_float()
+    _check(load_library().ki_rank_model_grad(_ptr(np.ascontiguousarray(model, np.float32)), _ptr(X),
+                                             _ptr(y), X.shape[0], _ptr(g), ctypes.byref(loss)))
+    return float(loss.value), g
 
 
 def measure_fma_peak():

@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdint>
 #include <cstdlib>
 #include <algorithm>
 #include <cstdio>
@@ -19,6 +20,7 @@
 #include "ki_common.cuh"
 #include "ki_factor.h"
 #include "ki_fmm.h"
+#include "ki_mlp.h"
 
 namespace {
 
@@ -336,6 +338,7 @@ struct ki_factor {
   double* d_geo = nullptr;
   double* d_holes = nullptr;
   double* d_pts = nullptr;     // interleaved coordinates (dim per point)
+  float* d_rank_model = nullptr;   // learned rank predictor (FP32 factorizations)
   int* d_hstart = nullptr;     // hole node ranges
   int* d_hcount = nullptr;
   ki::Points<double> P{};
@@ -356,6 +359,7 @@ struct ki_factor {
     if (d_geo) cudaFree(d_geo);
     if (d_holes) cudaFree(d_holes);
     if (d_pts) cudaFree(d_pts);
+    if (d_rank_model) cudaFree(d_rank_model);
     if (d_hstart) cudaFree(d_hstart);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -407,6 +411,9 @@ void check_desc(const ki_problem_desc* d) {
   if (!(d->id_tol > 0) || !std::isfinite(d->id_tol)) throw ArgError("id_tol must be positive");
   if (d->precision != KI_PRECISION_FP64 && d->precision != KI_PRECISION_FP32)
     throw ArgError("unknown precision");
+  if (d->precision == KI_PRECISION_FP32 && d->id_tol < 5e-8)
+    throw ArgError("an FP32 factorization needs id_tol >= 5e-8 (FP32 rounding); use "
+                   "ki_solve_refined to reach tighter residuals");
   if (d->n_holes < 0) throw ArgError("n_holes must be >= 0");
   if (d->n_holes > 0 && (!d->hole_centers || !d->hole_node_start || !d->hole_node_count))
     throw ArgError("hole arrays must be non-NULL when n_holes > 0");
@@ -865,6 +872,14 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
     prm.radius_ratio = desc->radius_ratio > 0 ? desc->radius_ratio : 2.0;
     prm.min_dofs_to_compress = desc->min_dofs_to_compress ? desc->min_dofs_to_compress : 64;
     prm.id_tol = desc->id_tol;
+    if (desc->rank_model && desc->precision == KI_PRECISION_FP32) {
+      for (int i = 0; i < ki::kMlpModelFloats; i++)
+        if (!std::isfinite(desc->rank_model[i])) throw ArgError("non-finite rank model");
+      KI_CHECK_CUDA(cudaMalloc(&f->d_rank_model, sizeof(float) * ki::kMlpModelFloats));
+      KI_CHECK_CUDA(cudaMemcpy(f->d_rank_model, desc->rank_model, sizeof(float) * ki::kMlpModelFloats,
+                               cudaMemcpyHostToDevice));
+      prm.rank_model = f->d_rank_model;
+    }
     ki::HoleDesc holes;
     holes.n_holes = desc->n_holes;
     for (int h = 0; h < desc->n_holes; h++) {
@@ -974,6 +989,8 @@ int ki_factor_get_info(const ki_factor* f, ki_factor_info* info) {
       info->n_root = F.n_root;
       info->factor_seconds = F.factor_seconds;
       info->device_bytes = (long)F.device_bytes;
+      info->n_sketched = F.n_sketched;
+      info->n_fallback = F.n_fallback;
     };
     if (f->f64) fill(*f->f64);
     if (f->f32) fill(*f->f32);
@@ -1266,6 +1283,91 @@ int ki_measure_fma_peak(double* fp64_gflops, double* fp32_gflops) {
     KI_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     *fp64_gflops = fma_peak_gflops<double>(sms, 20000);
     *fp32_gflops = fma_peak_gflops<float>(sms, 200000);
+  });
+}
+
+int ki_rank_model_floats(void) { return ki::kMlpModelFloats; }
+
+int ki_rank_model_train(const float* features, const float* ratios, int n, int epochs, float lr,
+                        unsigned seed, float* model, float* loss) {
+  return guarded([&] {
+    if (!features || !ratios || !model || !loss) throw ArgError("NULL argument");
+    if (n <= 0 || epochs < 0 || !(lr > 0)) throw ArgError("bad n / epochs / lr");
+    const int F = ki::kMlpIn, H = ki::kMlpHidden;
+    for (long i = 0; i < (long)n * F; i++)
+      if (!std::isfinite(features[i])) throw ArgError("non-finite feature");
+    for (int i = 0; i < n; i++)
+      if (!(ratios[i] >= 0 && ratios[i] <= 1)) throw ArgError("ratios must lie in [0, 1]");
+    std::vector<float> m(ki::kMlpModelFloats, 0.f);
+    // standardization from the data
+    for (int f = 0; f < F; f++) {
+      double s1 = 0, s2 = 0;
+      for (int i = 0; i < n; i++) { s1 += features[(size_t)i * F + f]; s2 += (double)features[(size_t)i * F + f] * features[(size_t)i * F + f]; }
+      double mu = s1 / n, var = std::max(0.0, s2 / n - mu * mu);
+      m[ki::kMlpMean + f] = (float)mu;
+      m[ki::kMlpScale + f] = (float)(var > 1e-12 ? std::sqrt(var) : 1.0);
+    }
+    // He-scaled uniform weights from a 64-bit linear congruential generator
+    uint64_t st = 0x9E3779B97F4A7C15ull ^ seed;
+    auto unif = [&]() {
+      st = st * 6364136223846793005ull + 1442695040888963407ull;
+      return (float)((st >> 40) * (1.0 / 16777216.0)) * 2.f - 1.f;
+    };
+    const float a1 = std::sqrt(6.f / F), a2 = std::sqrt(6.f / H);
+    for (int e = 0; e < H * F; e++) m[ki::kMlpW1 + e] = a1 * unif();
+    for (int e = 0; e < H * H; e++) m[ki::kMlpW2 + e] = a2 * unif();
+    for (int e = 0; e < H; e++) m[ki::kMlpW3 + e] = a2 * unif();
+    cudaStream_t s = nullptr;
+    DevBuf<float> dm(ki::kMlpModelFloats, s), dx((size_t)n * F, s), dy(n, s);
+    KI_CHECK_CUDA(cudaMemcpyAsync(dm.p, m.data(), sizeof(float) * m.size(), cudaMemcpyHostToDevice, s));
+    KI_CHECK_CUDA(cudaMemcpyAsync(dx.p, features, sizeof(float) * (size_t)n * F, cudaMemcpyHostToDevice, s));
+    KI_CHECK_CUDA(cudaMemcpyAsync(dy.p, ratios, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    *loss = ki::mlp_train(dm.p, dx.p, dy.p, n, epochs, lr, s);
+    KI_CHECK_CUDA(cudaMemcpyAsync(model, dm.p, sizeof(float) * m.size(), cudaMemcpyDeviceToHost, s));
+    KI_CHECK_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ki_rank_model_predict(const float* model, const float* features, int n, float* ratios) {
+  return guarded([&] {
+    if (!model || !features || !ratios) throw ArgError("NULL argument");
+    if (n < 0) throw ArgError("bad n");
+    if (n == 0) return;
+    cudaStream_t s = nullptr;
+    DevBuf<float> dm(ki::kMlpModelFloats, s), dx((size_t)n * ki::kMlpIn, s), dy(n, s);
+    KI_CHECK_CUDA(cudaMemcpyAsync(dm.p, model, sizeof(float) * ki::kMlpModelFloats, cudaMemcpyHostToDevice, s));
+    KI_CHECK_CUDA(cudaMemcpyAsync(dx.p, features, sizeof(float) * (size_t)n * ki::kMlpIn, cudaMemcpyHostToDevice, s));
+    ki::mlp_predict(dm.p, dx.p, n, dy.p, s);
+    KI_CHECK_CUDA(cudaMemcpyAsync(ratios, dy.p, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+    KI_CHECK_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ki_rank_model_grad(const float* model, const float* features, const float* ratios, int n,
+                       float* grad, float* loss) {
+  return guarded([&] {
+    if (!model || !features || !ratios || !grad || !loss) throw ArgError("NULL argument");
+    if (n <= 0) throw ArgError("bad n");
+    cudaStream_t s = nullptr;
+    DevBuf<float> dm(ki::kMlpModelFloats, s), dx((size_t)n * ki::kMlpIn, s), dy(n, s),
+        dg(ki::kMlpModelFloats, s);
+    KI_CHECK_CUDA(cudaMemcpyAsync(dm.p, model, sizeof(float) * ki::kMlpModelFloats, cudaMemcpyHostToDevice, s));
+    KI_CHECK_CUDA(cudaMemcpyAsync(dx.p, features, sizeof(float) * (size_t)n * ki::kMlpIn, cudaMemcpyHostToDevice, s));
+    KI_CHECK_CUDA(cudaMemcpyAsync(dy.p, ratios, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    ki::mlp_loss_grad(dm.p, dx.p, dy.p, n, dg.p, loss, s);
+    KI_CHECK_CUDA(cudaMemcpyAsync(grad, dg.p, sizeof(float) * ki::kMlpModelFloats, cudaMemcpyDeviceToHost, s));
+    KI_CHECK_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ki_factor_get_box_log(const ki_factor* f, float* out, int max_rows, int* rows) {
+  return guarded([&] {
+    if (!f || !rows || (max_rows > 0 && !out)) throw ArgError("NULL argument");
+    const std::vector<float>& log = f->f64 ? f->f64->box_log : f->f32->box_log;
+    const int total = (int)(log.size() / 15);
+    *rows = total;
+    const int w = std::min(total, std::max(0, max_rows));
+    if (w > 0) std::memcpy(out, log.data(), sizeof(float) * 15 * (size_t)w);
   });
 }
 

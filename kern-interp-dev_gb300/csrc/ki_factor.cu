@@ -35,6 +35,7 @@
 
 #include "ki_common.cuh"
 #include "ki_dense.h"
+#include "ki_mlp.h"
 
 namespace ki {
 
@@ -178,6 +179,7 @@ struct IdTask {
   int seg_begin, seg_end;
   int mode;           // 0: inner-circle filter + proxy rows; 1: all candidates, no proxy
   double cx, cy, cz, rad_filter, rad_proxy;
+  double side;        // box side length
   int64_t rows;       // iscratch offset of the row list (capacity = candidates)
   int64_t ws;         // T-scratch offset: R (n*n) | B (32*n) | vn1 (n) | vn2 (n) | Tout (n*n/4+1)
   int64_t perm;       // iscratch offset of the pivot order (n)
@@ -315,9 +317,15 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
                                                   const int64_t* seg_off, const int* seg_len,
                                                   int* ipool, int* iscratch, T* tws, Points<T> P,
                                                   int sol_dim, ProxyTab<T> px, double tol, int* k_out,
-                                                  int* m_out, int mode, int flags) {
+                                                  int* m_out, int mode, int flags,
+                                                  const int* sketch_l) {
   // flags: 1 gather the rows (writes m), 2 fold the ID matrix into R,
   //        4 R already formed (row-major n x n in the global scratch)
+  // sketch_l (optional, per task): with 0 < l < n and the triangle in shared
+  // memory (mode 0), the ID matrix M is compressed to the l x n sketch
+  // Y = Omega M (Omega: random signs) instead of being folded into R, and the
+  // column-pivoted QR runs on Y (randomized ID).  When Y does not reveal the
+  // rank within l pivots the box is flagged (k = -1) for the plain ID.
   extern __shared__ __align__(16) unsigned char id_smem[];
   const int task = task_base + blockIdx.x;
   const IdTask t = tasks[task];
@@ -415,7 +423,48 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   __syncthreads();
   const int m = m_out[task];
   const int nI = (m - nprox_rows) / 2;
+  const int lsk = (sketch_l && mode == 0 && (flags & 2)) ? sketch_l[task] : 0;
+  const bool sketch = lsk > 0 && lsk < n;
+  const int rowsR = sketch ? lsk : n;   // rows of the matrix the pivoted QR runs on
 
+  // 2a. Sketch: Y (lsk x n, in R's place) = sum over 32/64-row blocks B of
+  //     S_B B, S_B[q][i] = +-1 from a hash of (box, row, q).
+  if (sketch) {
+    for (int idx = tid; idx < lsk * n; idx += nth) R[(idx / n) * (size_t)ldR + idx % n] = T(0);
+    const ProxyBox<T> pb = proxy_box<T>(t.cx, t.cy, t.cz, t.rad_proxy, px.n);
+    uint32_t* sgn = reinterpret_cast<uint32_t*>(hu);   // FR rows x ceil(lsk/32) words
+    const int words = (lsk + 31) >> 5;
+    for (int r0 = 0; r0 < m; r0 += FR) {
+      __syncthreads();
+      for (int idx = tid; idx < FR * n; idx += nth) {
+        int j = idx % n, i = idx / n;
+        int row = r0 + i;
+        B[(size_t)i * ldB + j] =
+            row < m ? id_entry<T>(P, sol_dim, row, nI, rows, act[j], px, pb) : T(0);
+      }
+      for (int idx = tid; idx < FR * words; idx += nth) {
+        // lowbias32 integer hash (C. Wellons) of (box's active offset, row, word)
+        uint32_t x = (uint32_t)(t.act * 2654435761u) ^ (uint32_t)((r0 + idx / words) * 40503u) ^
+                     (uint32_t)((idx % words) * 2246822519u);
+        x ^= x >> 16; x *= 0x7feb352du; x ^= x >> 15; x *= 0x846ca68bu; x ^= x >> 16;
+        sgn[idx] = x;
+      }
+      __syncthreads();
+      for (int idx = tid; idx < lsk * n; idx += nth) {
+        const int q = idx / n, c = idx % n;
+        T acc = T(0);
+#pragma unroll 8
+        for (int i = 0; i < FR; i++) {
+          const T b = B[(size_t)i * ldB + c];
+          acc += ((sgn[i * words + (q >> 5)] >> (q & 31)) & 1u) ? -b : b;
+        }
+        R[(size_t)q * ldR + c] += acc;
+      }
+    }
+    __syncthreads();
+  }
+
+  if (!sketch) {
   // 2. TSQR: R <- qr([R; B]) for successive 32-row blocks B of the ID
   //    matrix.  The thread that owns column j+1 forms reflector j+1 right
   //    after updating that column (look-ahead), so one barrier per column.
@@ -518,13 +567,15 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
     }
     __syncthreads();
   }
+  }   // !sketch
 
   // 3. column-pivoted QR of the n x n triangle (LAPACK xGEQP3/xLAQP2 norm
   //    downdating with recomputation after cancellation), stopping at the
   //    first |R_jj| < tol |R_00| for j >= 1.  Thread per column again.
   for (int c = tid; c < n; c += nth) {
     T s = T(0);
-    for (int i = 0; i <= c; i++) s += R[(size_t)i * ldR + c] * R[(size_t)i * ldR + c];
+    const int ilast = sketch ? rowsR - 1 : c;   // the triangle is zero below the diagonal
+    for (int i = 0; i <= ilast; i++) s += R[(size_t)i * ldR + c] * R[(size_t)i * ldR + c];
     vn1[c] = sqrt(s);
     vn2[c] = vn1[c];
     perm[c] = c;
@@ -532,7 +583,7 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   if (tid == 0) s_k = 0;
   __syncthreads();
   T thresh = T(0);
-  const int jmax = min(n, m);
+  const int jmax = min(min(n, m), rowsR);
   for (int j = 0; j < jmax; j++) {
     // pivot: first index of the largest partial norm (norms are >= 0, so
     // their bit patterns order like the values)
@@ -553,7 +604,7 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
     __syncthreads();
     const int p = s_piv;
     if (p != j) {
-      for (int i = tid; i < n; i += nth) {
+      for (int i = tid; i < rowsR; i += nth) {
         T a = R[(size_t)i * ldR + j];
         R[(size_t)i * ldR + j] = R[(size_t)i * ldR + p];
         R[(size_t)i * ldR + p] = a;
@@ -568,7 +619,7 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
     // reflector of R(j:n, j) by warp 0; tail -> hu[0..], scalars -> shared
     if (warp == 0) {
       T sg = T(0);
-      for (int i = j + 1 + lane; i < n; i += 32) sg += R[(size_t)i * ldR + j] * R[(size_t)i * ldR + j];
+      for (int i = j + 1 + lane; i < rowsR; i += 32) sg += R[(size_t)i * ldR + j] * R[(size_t)i * ldR + j];
       T sigma = warp_sum(sg);
       T alpha = R[(size_t)j * ldR + j];
       T tau = T(0), beta = alpha, scale = T(0);
@@ -578,7 +629,7 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
         tau = (beta - alpha) / beta;
         scale = T(1) / (alpha - beta);
       }
-      for (int i = j + 1 + lane; i < n; i += 32) hu[i] = R[(size_t)i * ldR + j] * scale;
+      for (int i = j + 1 + lane; i < rowsR; i += 32) hu[i] = R[(size_t)i * ldR + j] * scale;
       if (lane == 0) { s_tau[0] = tau; s_beta = beta; }
     }
     __syncthreads();
@@ -592,16 +643,16 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
       if (tau != T(0)) {
         T w0 = R[(size_t)j * ldR + c], w1 = T(0), w2 = T(0), w3 = T(0);
         int i = j + 1;
-        for (; i + 3 < n; i += 4) {
+        for (; i + 3 < rowsR; i += 4) {
           w0 += hu[i] * R[(size_t)i * ldR + c];
           w1 += hu[i + 1] * R[(size_t)(i + 1) * ldR + c];
           w2 += hu[i + 2] * R[(size_t)(i + 2) * ldR + c];
           w3 += hu[i + 3] * R[(size_t)(i + 3) * ldR + c];
         }
-        for (; i < n; i++) w0 += hu[i] * R[(size_t)i * ldR + c];
+        for (; i < rowsR; i++) w0 += hu[i] * R[(size_t)i * ldR + c];
         T w = ((w0 + w1) + (w2 + w3)) * tau;
         R[(size_t)j * ldR + c] -= w;
-        for (int q = j + 1; q < n; q++) R[(size_t)q * ldR + c] -= w * hu[q];
+        for (int q = j + 1; q < rowsR; q++) R[(size_t)q * ldR + c] -= w * hu[q];
       }
       // norm downdate of column c (xLAQP2), recomputed after cancellation
       T rjc = R[(size_t)j * ldR + c];
@@ -614,7 +665,7 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
         T temp2 = temp * q * q;
         if (temp2 <= tol3z<T>()) {
           T s2 = T(0);
-          for (int i = j + 1; i < n; i++) s2 += R[(size_t)i * ldR + c] * R[(size_t)i * ldR + c];
+          for (int i = j + 1; i < rowsR; i++) s2 += R[(size_t)i * ldR + c] * R[(size_t)i * ldR + c];
           vn1[c] = sqrt(s2);
           vn2[c] = vn1[c];
         } else {
@@ -627,6 +678,11 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   }
   __syncthreads();
   const int k = s_k;
+  if (sketch && k == 0 && jmax == rowsR) {
+    // the sketch did not reveal the rank: recompress with the plain ID
+    if (tid == 0) k_out[task] = -1;
+    return;
+  }
   if (tid == 0) k_out[task] = k;
   int* gperm = iscratch + t.perm;
   for (int i = tid; i < n; i += nth) gperm[i] = perm[i];
@@ -648,6 +704,103 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   }
   int* pact = ipool + t.pact;
   for (int i = tid; i < n; i += nth) pact[i] = act[perm[i]];
+}
+
+// Features of the learned rank predictor for every ID box of a level (one
+// thread per box), and with a model the predicted sketch size
+// l = min(n, ceil((1 + margin) k^) + oversample), k^ = n * MLP(features):
+//   0 log2 n            1 level / (levels - 1)   2 log2(m + 1)   3 log2(nI + 1)
+//   4 dim == 3          5 solution dim / 3       6 -log10(tol) / 10
+//   7 proxy-free box (levels 1-2)   8-10 eigenvalues of the covariance of
+//   the box's active points / side^2 (descending)   11 |mean - centre| / side.
+template <typename T>
+__global__ void __launch_bounds__(128) k_box_features(const IdTask* tasks, int ntask,
+                                                      const int* ipool, Points<T> P, int sol_dim,
+                                                      const int* m_arr, int nprox_rows,
+                                                      float level_frac, float tol_feat,
+                                                      const float* model, float margin,
+                                                      int oversample, float* feat, int* l_out) {
+  __shared__ float sm[kMlpModelFloats];
+  if (model)
+    for (int e = threadIdx.x; e < kMlpModelFloats; e += blockDim.x) sm[e] = model[e];
+  __syncthreads();
+  const int task = blockIdx.x * blockDim.x + threadIdx.x;
+  if (task >= ntask) return;
+  const IdTask t = tasks[task];
+  const int n = t.n, m = m_arr[task];
+  const int* act = ipool + t.act;
+  const double c[3] = {t.cx, t.cy, t.cz};
+  double s1[3] = {0, 0, 0}, s2[6] = {0, 0, 0, 0, 0, 0};
+  const int dim = P.dim;
+  int prev = -1;
+  int cnt = 0;
+  for (int j = 0; j < n; j++) {
+    const int p = dof_point(act[j], sol_dim);
+    if (p == prev) continue;   // the DOFs of one node are adjacent
+    prev = p;
+    double x[3] = {(double)P.x[p] + (P.xl ? (double)P.xl[p] : 0.0),
+                   (double)P.y[p] + (P.yl ? (double)P.yl[p] : 0.0),
+                   dim == 3 ? (double)P.z[p] + (P.zl ? (double)P.zl[p] : 0.0) : c[2]};
+    for (int d = 0; d < 3; d++) x[d] -= c[d];
+    for (int d = 0; d < 3; d++) s1[d] += x[d];
+    s2[0] += x[0] * x[0]; s2[1] += x[1] * x[1]; s2[2] += x[2] * x[2];
+    s2[3] += x[0] * x[1]; s2[4] += x[0] * x[2]; s2[5] += x[1] * x[2];
+    cnt++;
+  }
+  const double inv = cnt ? 1.0 / cnt : 0.0, side2 = t.side * t.side;
+  double mu[3] = {s1[0] * inv, s1[1] * inv, s1[2] * inv};
+  // covariance a11 a22 a33 a12 a13 a23
+  double a[6] = {s2[0] * inv - mu[0] * mu[0], s2[1] * inv - mu[1] * mu[1],
+                 s2[2] * inv - mu[2] * mu[2], s2[3] * inv - mu[0] * mu[1],
+                 s2[4] * inv - mu[0] * mu[2], s2[5] * inv - mu[1] * mu[2]};
+  double ev[3] = {0, 0, 0};
+  if (dim == 2) {
+    const double h = 0.5 * (a[0] + a[1]), d = sqrt(0.25 * (a[0] - a[1]) * (a[0] - a[1]) + a[3] * a[3]);
+    ev[0] = h + d;
+    ev[1] = h - d;
+  } else {
+    // symmetric 3 x 3 eigenvalues by the trigonometric method (O. K. Smith, 1961)
+    const double p1 = a[3] * a[3] + a[4] * a[4] + a[5] * a[5];
+    const double q = (a[0] + a[1] + a[2]) / 3.0;
+    if (p1 == 0.0) {
+      ev[0] = a[0]; ev[1] = a[1]; ev[2] = a[2];
+    } else {
+      const double p2 = (a[0] - q) * (a[0] - q) + (a[1] - q) * (a[1] - q) + (a[2] - q) * (a[2] - q) + 2 * p1;
+      const double pp = sqrt(p2 / 6.0);
+      const double b0 = (a[0] - q) / pp, b1 = (a[1] - q) / pp, b2 = (a[2] - q) / pp;
+      const double b3 = a[3] / pp, b4 = a[4] / pp, b5 = a[5] / pp;
+      double r = 0.5 * (b0 * (b1 * b2 - b5 * b5) - b3 * (b3 * b2 - b5 * b4) + b4 * (b3 * b5 - b1 * b4));
+      r = fmin(1.0, fmax(-1.0, r));
+      const double phi = acos(r) / 3.0;
+      ev[0] = q + 2 * pp * cos(phi);
+      ev[2] = q + 2 * pp * cos(phi + 2.0943951023931957);
+      ev[1] = 3 * q - ev[0] - ev[2];
+    }
+  }
+  for (int i = 0; i < 2; i++)   // descending
+    for (int j = 0; j < 2 - i; j++)
+      if (ev[j] < ev[j + 1]) { double tmp = ev[j]; ev[j] = ev[j + 1]; ev[j + 1] = tmp; }
+  const int nI = (m - (t.mode == 0 ? nprox_rows : 0)) / 2;
+  float f[kMlpIn];
+  f[0] = log2f((float)n);
+  f[1] = level_frac;
+  f[2] = log2f((float)m + 1.f);
+  f[3] = log2f((float)nI + 1.f);
+  f[4] = dim == 3 ? 1.f : 0.f;
+  f[5] = sol_dim / 3.f;
+  f[6] = tol_feat;
+  f[7] = t.mode == 1 ? 1.f : 0.f;
+  f[8] = (float)(fmax(ev[0], 0.0) / side2);
+  f[9] = (float)(fmax(ev[1], 0.0) / side2);
+  f[10] = (float)(fmax(ev[2], 0.0) / side2);
+  f[11] = (float)(sqrt(mu[0] * mu[0] + mu[1] * mu[1] + mu[2] * mu[2]) / t.side);
+  for (int q = 0; q < kMlpIn; q++) feat[(size_t)task * kMlpIn + q] = f[q];
+  int l = 0;
+  if (model) {
+    const float khat = (float)n * mlp_forward_one(sm, f);
+    l = min(n, (int)ceilf((1.f + margin) * khat) + oversample);
+  }
+  l_out[task] = l;
 }
 
 // Shared-memory bytes of k_id for a box of n active DOFs: mode 0 keeps the
@@ -1910,6 +2063,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       it.cy = bx.c[1];
       it.cz = bx.c[2];
       it.seg_begin = (int)seg_off.size();
+      it.side = bx.side;
       if (l == 1 || (l == 2 && dim == 2)) {
         // Kernel::get_id_mat levels 1/2 (kernel.cpp:441-563): every other box of
         // the level, plus (level 2) the leaves of the levels above; no proxy.
@@ -1972,9 +2126,21 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     KI_CUDA(cudaFuncSetAttribute(k_id<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
     k_id<T, 32><<<(unsigned)itasks.size(), kThreads, 0, s>>>(d_it, 0, d_soff, d_slen, ipool, d_irows, d_tws,
                                                          P, sd, ptab, prm.id_tol,
-                                                         d_k, d_m, 0, 1);
+                                                         d_k, d_m, 0, 1, nullptr);
     KI_CUDA(cudaGetLastError());
-    std::vector<int> mh(itasks.size()), kh(itasks.size());
+    // per-box features of the rank predictor and, with a model, the sketch sizes
+    const int ntask = (int)itasks.size();
+    float* d_feat = (float*)F->alloc(sizeof(float) * kMlpIn * (size_t)ntask);
+    int* d_lsk = (int*)F->alloc(sizeof(int) * (size_t)ntask);
+    k_box_features<T><<<(ntask + 127) / 128, 128, 0, s>>>(
+        d_it, ntask, ipool, P, sd, d_m, 2 * np * sd, L > 1 ? (float)l / (float)(L - 1) : 0.f,
+        (float)(-std::log10(prm.id_tol) / 10.0), prm.rank_model, prm.sketch_margin,
+        prm.sketch_oversample, d_feat, d_lsk);
+    KI_CUDA(cudaGetLastError());
+    std::vector<int> mh(itasks.size()), kh(itasks.size()), lh(itasks.size());
+    std::vector<float> fh(kMlpIn * (size_t)ntask);
+    KI_CUDA(cudaMemcpyAsync(lh.data(), d_lsk, sizeof(int) * lh.size(), cudaMemcpyDeviceToHost, s));
+    KI_CUDA(cudaMemcpyAsync(fh.data(), d_feat, sizeof(float) * fh.size(), cudaMemcpyDeviceToHost, s));
     KI_CUDA(cudaMemcpyAsync(mh.data(), d_m, sizeof(int) * mh.size(), cudaMemcpyDeviceToHost, s));
     KI_CUDA(cudaStreamSynchronize(s));
     // (b) groups: [narrow, R in smem][narrow, R global][wide, R in smem][wide, R global];
@@ -2005,24 +2171,32 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         return grp[a2] != grp[b2] ? grp[a2] < grp[b2] : itasks[a2].n < itasks[b2].n;
       });
       std::vector<IdTask> it2;
-      std::vector<int> comp2, grp2, m2;
+      std::vector<int> comp2, grp2, m2, l2;
+      std::vector<float> f2;
       for (size_t o : order) {
         it2.push_back(itasks[o]);
         comp2.push_back(comp[o]);
         grp2.push_back(grp[o]);
         m2.push_back(mh[o]);
+        // sketches only where the triangle sits in shared memory (group 0)
+        l2.push_back(grp[o] == 0 ? lh[o] : 0);
+        f2.insert(f2.end(), fh.begin() + kMlpIn * o, fh.begin() + kMlpIn * (o + 1));
       }
       itasks.swap(it2);
       comp.swap(comp2);
       grp.swap(grp2);
       mh.swap(m2);
+      lh.swap(l2);
+      fh.swap(f2);
       for (size_t i = 0; i < comp.size(); i++) {
         hb[comp[i]].pact = itasks[i].pact;
         mode_of[i] = grp[i];
       }
       upload(d_it, itasks, s);
       upload(d_m, mh, s);
+      upload(d_lsk, lh, s);
     }
+    const bool sketching = prm.rank_model != nullptr;
     int next_aux = 0;
     auto launch_range = [&](int g, int flags, cudaStream_t fixed) {
       // tasks of group g are contiguous and sorted by n within the group (see
@@ -2060,11 +2234,13 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         if (fr == 64)
           k_id<T, 64><<<(unsigned)(b1 - b0), kThreads, sm, st>>>(d_it, b0, d_soff, d_slen, ipool, d_irows,
                                                                  d_tws, P, sd, ptab,
-                                                                 prm.id_tol, d_k, d_m, kmode, flags);
+                                                                 prm.id_tol, d_k, d_m, kmode, flags,
+                                                                 sketching && g == 0 ? d_lsk : nullptr);
         else
           k_id<T, 32><<<(unsigned)(b1 - b0), kThreads, sm, st>>>(d_it, b0, d_soff, d_slen, ipool, d_irows,
                                                                  d_tws, P, sd, ptab,
-                                                                 prm.id_tol, d_k, d_m, kmode, flags);
+                                                                 prm.id_tol, d_k, d_m, kmode, flags,
+                                                                 sketching && g == 0 ? d_lsk : nullptr);
         KI_CUDA(cudaGetLastError());
         b0 = b1;
       }
@@ -2136,6 +2312,48 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     KI_CUDA(cudaGetLastError());
     KI_CUDA(cudaMemcpyAsync(kh.data(), d_k, sizeof(int) * kh.size(), cudaMemcpyDeviceToHost, s));
     KI_CUDA(cudaStreamSynchronize(s));
+    if (sketching) {
+      // boxes whose sketch did not reveal the rank (k = -1): the plain ID
+      std::vector<int> fb;
+      for (size_t i = 0; i < kh.size(); i++) {
+        if (lh[i] > 0 && lh[i] < itasks[i].n) F->n_sketched++;
+        if (kh[i] < 0) fb.push_back((int)i);
+      }
+      if (!fb.empty()) {
+        std::vector<IdTask> t2;
+        std::vector<int> m2;
+        size_t sm = 0;
+        for (int i : fb) {
+          t2.push_back(itasks[i]);
+          m2.push_back(mh[i]);
+          sm = std::max(sm, id_smem_bytes<T>(itasks[i].n, 0, 32, 2));
+        }
+        IdTask* d_t2 = (IdTask*)F->alloc(sizeof(IdTask) * t2.size());
+        int* d_m2 = (int*)F->alloc(sizeof(int) * t2.size());
+        int* d_k2 = (int*)F->alloc(sizeof(int) * t2.size());
+        upload(d_t2, t2, s);
+        upload(d_m2, m2, s);
+        std::string fname = "id_fallback@L" + std::to_string(l);
+        F->stage_begin(fname.c_str(), 0, 0);
+        k_id<T, 32><<<(unsigned)t2.size(), kThreads, sm, s>>>(d_t2, 0, d_soff, d_slen, ipool, d_irows,
+                                                              d_tws, P, sd, ptab, prm.id_tol, d_k2,
+                                                              d_m2, 0, 2, nullptr);
+        F->stage_end();
+        KI_CUDA(cudaGetLastError());
+        std::vector<int> k2(t2.size());
+        KI_CUDA(cudaMemcpyAsync(k2.data(), d_k2, sizeof(int) * k2.size(), cudaMemcpyDeviceToHost, s));
+        KI_CUDA(cudaStreamSynchronize(s));
+        for (size_t j = 0; j < fb.size(); j++) kh[fb[j]] = k2[j];
+        F->n_fallback += (int)fb.size();
+      }
+    }
+    // box log: the predictor's features, n, the rank and the level of every ID box
+    for (size_t i = 0; i < kh.size(); i++) {
+      F->box_log.insert(F->box_log.end(), fh.begin() + kMlpIn * i, fh.begin() + kMlpIn * (i + 1));
+      F->box_log.push_back((float)itasks[i].n);
+      F->box_log.push_back((float)kh[i]);
+      F->box_log.push_back((float)l);
+    }
     {
       LevelStat ls;
       ls.level = l;

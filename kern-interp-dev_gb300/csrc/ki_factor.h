@@ -20,6 +20,12 @@ struct Params {
   double radius_ratio = 2.0;  // RADIUS_RATIO: proxy radius = ratio*sqrt(dim)*side/2
   int min_dofs_to_compress = 64;
   double id_tol = 1e-10;
+  // learned rank predictor (device model blob, ki_mlp.h) or null: with a model
+  // the ID of every box whose triangle fits in shared memory is a sketched ID
+  // of l = min(n, ceil((1 + sketch_margin) k^) + sketch_oversample) rows
+  const float* rank_model = nullptr;
+  float sketch_margin = 0.25f;
+  int sketch_oversample = 8;
 };
 
 // Device status word written by kernels that can fail (non-finite data,
@@ -94,6 +100,9 @@ struct Factorization {
   // statistics
   int n_compressed = 0;
   long n_redundant = 0;
+  int n_sketched = 0;                // boxes compressed from a sketch
+  int n_fallback = 0;                // sketches that did not reveal the rank
+  std::vector<float> box_log;        // per ID box: 12 features, n, k, level
   std::vector<int> rank_hist;
   bool profile_solve = false;        // record stage events in solves
   std::vector<StageRec> prof_open;   // launches recorded since the last collect
