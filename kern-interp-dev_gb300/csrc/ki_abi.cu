@@ -770,11 +770,11 @@ int fmm_order() {
 // Terms for a refinement target: the smallest order whose expected relative
 // error, 1.4e-8 * 0.43^(p - 16) (measured max-norm error of K x for random x
 // on the 2D Laplace disc-with-ellipses family at 1,048,576 unknowns: 1.4e-8
-// at 16 terms, 4.8e-10 at 20, 1.6e-11 at 24), is 50x below the target.
+// at 16 terms, 4.8e-10 at 20, 1.6e-11 at 24), is 20x below the target.
 int fmm_order_for(double target, int plan_order) {
   if (const char* e = std::getenv("KI_FMM_P")) return std::atoi(e);
   int p = 12;
-  while (p < plan_order && 1.4e-8 * std::pow(0.43, p - 16) > target / 50) p++;
+  while (p < plan_order && 1.4e-8 * std::pow(0.43, p - 16) > target / 20) p++;
   return p;
 }
 

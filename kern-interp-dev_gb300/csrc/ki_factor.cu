@@ -423,13 +423,25 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   __syncthreads();
   const int m = m_out[task];
   const int nI = (m - nprox_rows) / 2;
-  const int lsk = (sketch_l && mode == 0 && (flags & 2)) ? sketch_l[task] : 0;
-  const bool sketch = lsk > 0 && lsk < n;
+  // a sketch is folded here only with the triangle in shared memory; an R
+  // formed beforehand (flags 4) may be an lsk x n sketch in either mode
+  const int lsk_in = sketch_l ? sketch_l[task] : 0;
+  const int lsk = (flags & 2) ? (mode == 0 ? lsk_in : 0) : ((flags & 4) ? lsk_in : 0);
+  // folded sketches need l < n (else the triangle is cheaper); a formed
+  // sketch may have l = n rows (a full-size randomized ID, no fallback)
+  const bool sketch = (flags & 2) ? (lsk > 0 && lsk < n) : (lsk > 0 && lsk <= n);
+  const bool sketch_fold = sketch && (flags & 2);
   const int rowsR = sketch ? lsk : n;   // rows of the matrix the pivoted QR runs on
 
   // 2a. Sketch: Y (lsk x n, in R's place) = sum over 32/64-row blocks B of
   //     S_B B, S_B[q][i] = +-1 from a hash of (box, row, q).
-  if (sketch) {
+  if (sketch && !sketch_fold) {
+    // a sketch formed by k_wide_sketch: row-major lsk x n in the global scratch
+    if (mode == 0)
+      for (int idx = tid; idx < lsk * n; idx += nth) R[(idx / n) * (size_t)ldR + idx % n] = gws[idx];
+    __syncthreads();
+  }
+  if (sketch_fold) {
     for (int idx = tid; idx < lsk * n; idx += nth) R[(idx / n) * (size_t)ldR + idx % n] = T(0);
     const ProxyBox<T> pb = proxy_box<T>(t.cx, t.cy, t.cz, t.rad_proxy, px.n);
     uint32_t* sgn = reinterpret_cast<uint32_t*>(hu);   // FR rows x ceil(lsk/32) words
@@ -678,7 +690,7 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   }
   __syncthreads();
   const int k = s_k;
-  if (sketch && k == 0 && jmax == rowsR) {
+  if (sketch && k == 0 && jmax == rowsR && rowsR < n) {
     // the sketch did not reveal the rank: recompress with the plain ID
     if (tid == 0) k_out[task] = -1;
     return;
@@ -719,7 +731,8 @@ __global__ void __launch_bounds__(128) k_box_features(const IdTask* tasks, int n
                                                       const int* m_arr, int nprox_rows,
                                                       float level_frac, float tol_feat,
                                                       const float* model, float margin,
-                                                      int oversample, float* feat, int* l_out) {
+                                                      int oversample, float* feat, int* l_out,
+                                                      float* khat_out) {
   __shared__ float sm[kMlpModelFloats];
   if (model)
     for (int e = threadIdx.x; e < kMlpModelFloats; e += blockDim.x) sm[e] = model[e];
@@ -796,11 +809,13 @@ __global__ void __launch_bounds__(128) k_box_features(const IdTask* tasks, int n
   f[11] = (float)(sqrt(mu[0] * mu[0] + mu[1] * mu[1] + mu[2] * mu[2]) / t.side);
   for (int q = 0; q < kMlpIn; q++) feat[(size_t)task * kMlpIn + q] = f[q];
   int l = 0;
+  float khat = 0.f;
   if (model) {
-    const float khat = (float)n * mlp_forward_one(sm, f);
+    khat = (float)n * mlp_forward_one(sm, f);
     l = min(n, (int)ceilf((1.f + margin) * khat) + oversample);
   }
   l_out[task] = l;
+  khat_out[task] = khat;
 }
 
 // Shared-memory bytes of k_id for a box of n active DOFs: mode 0 keeps the
@@ -828,6 +843,9 @@ struct WideTask {
   int64_t act, rows;   // ipool / iscratch offsets
   double cx, cy, cz, rad;
   int64_t R;           // T-scratch offset (tws) of the row-major triangle for k_id
+  int l;               // sketch rows (k_wide_sketch), 0 for the blocked QR
+  int chunks;          // row chunks of the sketch
+  int64_t part;        // T-pool offset of the sketch partials (chunks x l x n)
 };
 
 constexpr int kQrNb = 32;     // panel width
@@ -849,6 +867,80 @@ __global__ void k_wide_assemble(const WideTask* tasks, T* wpool, const int* ipoo
     int a = act[j];
     for (int row = threadIdx.x; row < t.m; row += blockDim.x)
       M[row + (size_t)t.m * j] = id_entry<T>(P, sol_dim, row, t.nI, rows, a, px, pbox);
+  }
+}
+
+// Sketched ID of a wide box: Y = Omega M (l x n) with M the box's ID matrix
+// (generated on the fly) and Omega random signs.  Grid (box, row chunk of
+// kSketchRows, column block of kSketchCols): each CTA sums its chunk into
+// its own partial, k_wide_sketch_reduce adds the partials in a fixed order
+// into the row-major sketch the ID kernel then pivots (flags 4).
+constexpr int kSketchRows = 256;
+constexpr int kSketchCols = 64;
+constexpr int kSketchSub = 32;   // rows generated per pass
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_wide_sketch(const WideTask* tasks, T* wpool,
+                                                     const int* ipool, const int* iscratch,
+                                                     Points<T> P, int sol_dim, ProxyTab<T> px) {
+  extern __shared__ __align__(16) unsigned char sk_smem[];
+  const WideTask t = tasks[blockIdx.x];
+  if (t.l <= 0) return;
+  const int r0 = blockIdx.y * kSketchRows, c0 = blockIdx.z * kSketchCols;
+  if (r0 >= t.m || c0 >= t.n) return;
+  const int r1 = min(t.m, r0 + kSketchRows), nc = min(kSketchCols, t.n - c0);
+  const int l = t.l, words = (l + 31) >> 5;
+  T* Y = reinterpret_cast<T*>(sk_smem);                  // l x kSketchCols
+  T* B = Y + (size_t)l * kSketchCols;                    // kSketchSub x kSketchCols
+  uint32_t* sgn = reinterpret_cast<uint32_t*>(B + kSketchSub * kSketchCols);
+  const int* act = ipool + t.act;
+  const int* rows = iscratch + t.rows;
+  const ProxyBox<T> pb = proxy_box<T>(t.cx, t.cy, t.cz, t.rad, px.n);
+  for (int e = threadIdx.x; e < l * kSketchCols; e += blockDim.x) Y[e] = T(0);
+  for (int rb = r0; rb < r1; rb += kSketchSub) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < kSketchSub * kSketchCols; e += blockDim.x) {
+      const int i = e / kSketchCols, c = e % kSketchCols, row = rb + i;
+      B[e] = (row < r1 && c < nc) ? id_entry<T>(P, sol_dim, row, t.nI, rows, act[c0 + c], px, pb)
+                                  : T(0);
+    }
+    for (int e = threadIdx.x; e < kSketchSub * words; e += blockDim.x) {
+      // lowbias32 integer hash (C. Wellons) of (box's active offset, row, word)
+      uint32_t x = (uint32_t)(t.act * 2654435761u) ^ (uint32_t)((rb + e / words) * 40503u) ^
+                   (uint32_t)((e % words) * 2246822519u);
+      x ^= x >> 16; x *= 0x7feb352du; x ^= x >> 15; x *= 0x846ca68bu; x ^= x >> 16;
+      sgn[e] = x;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < l * kSketchCols; e += blockDim.x) {
+      const int q = e / kSketchCols, c = e % kSketchCols;
+      T acc = T(0);
+#pragma unroll 8
+      for (int i = 0; i < kSketchSub; i++) {
+        const T b = B[i * kSketchCols + c];
+        acc += ((sgn[i * words + (q >> 5)] >> (q & 31)) & 1u) ? -b : b;
+      }
+      Y[e] += acc;
+    }
+  }
+  __syncthreads();
+  T* part = wpool + t.part + (size_t)blockIdx.y * l * t.n;
+  for (int e = threadIdx.x; e < l * nc; e += blockDim.x) {
+    const int q = e / nc, c = e % nc;
+    part[(size_t)q * t.n + c0 + c] = Y[q * kSketchCols + c];
+  }
+}
+
+template <typename T>
+__global__ void k_wide_sketch_reduce(const WideTask* tasks, const T* wpool, T* tws) {
+  const WideTask t = tasks[blockIdx.x];
+  if (t.l <= 0) return;
+  const size_t ln = (size_t)t.l * t.n;
+  T* Y = tws + t.R;
+  for (size_t e = threadIdx.x; e < ln; e += blockDim.x) {
+    T s = T(0);
+    for (int z = 0; z < t.chunks; z++) s += wpool[t.part + (size_t)z * ln + e];
+    Y[e] = s;
   }
 }
 
@@ -1294,7 +1386,11 @@ struct SweepTask {
   const T* U;    // r x k
   const T* X;    // r x r LU
   const int* piv;
+  const T* Xi;   // r x r explicit inverse (FP32 factorizations, r <= kInvMax) or null
 };
+
+// Largest redundant block whose inverse is formed explicitly for the sweeps.
+constexpr int kInvMax = 256;
 
 enum SweepMode : int {
   kUpDiag = 0,     // x_r -= T^T x_s; x_s -= L x_r; x_r <- X^-1 x_r
@@ -1306,6 +1402,44 @@ enum SweepMode : int {
 
 // x is DOF-major: row = DOF, ld = ldx; a CTA handles one box and a chunk of
 // `cw` columns starting at blockIdx.y * cw.
+// x_r <- X_rr^-1 x_r for one box's redundant rows (n x nc column-major block
+// in shared memory, leading dimension n): with the explicit inverse one
+// product (every thread an independent dot product, tmp: r x nc), else the
+// LU substitution.
+template <typename T>
+__device__ void diag_solve(const SweepTask<T>& t, T* xr, int n, int nc, T* tmp) {
+  const int r = t.n - t.k;
+  if (t.Xi) {
+    for (int idx = threadIdx.x; idx < r * nc; idx += blockDim.x) {
+      const int i = idx % r, c = idx / r;
+      T acc = T(0);
+      for (int j = 0; j < r; j++) acc += t.Xi[i + (size_t)r * j] * xr[j + (size_t)n * c];
+      tmp[idx] = acc;
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < r * nc; idx += blockDim.x)
+      xr[idx % r + (size_t)n * (idx / r)] = tmp[idx];
+    __syncthreads();
+  } else {
+    cta_lu_solve_par<T>(r, t.X, r, t.piv, false, xr, n, nc);
+  }
+}
+
+// Explicit inverses of the LU-factored redundant blocks (one CTA per box;
+// boxes without a Xi slot are skipped): Xi = I, then the LU substitution on
+// all r columns.
+template <typename T>
+__global__ void k_lu_inverse(const SweepTask<T>* tasks) {
+  const SweepTask<T> t = tasks[blockIdx.x];
+  if (!t.Xi) return;
+  const int r = t.n - t.k;
+  T* Xi = const_cast<T*>(t.Xi);
+  for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x)
+    Xi[idx] = (idx % r == idx / r) ? T(1) : T(0);
+  __syncthreads();
+  cta_lu_solve_par<T>(r, t.X, r, t.piv, false, Xi, r, r);
+}
+
 template <typename T>
 __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int cw, int mode) {
   extern __shared__ unsigned char smem_raw[];
@@ -1346,7 +1480,7 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
       xs[l + (size_t)n * c] -= acc;
     }
     __syncthreads();
-    if (mode == kUpDiag) cta_lu_solve_par<T>(r, t.X, r, t.piv, false, xr, n, nc);
+    if (mode == kUpDiag) diag_solve(t, xr, n, nc, sx + (size_t)n * nc);
   } else if (mode == kDown) {
     // x_r -= U x_s
     for (int idx = threadIdx.x; idx < r * nc; idx += blockDim.x) {
@@ -1365,7 +1499,7 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
     }
     __syncthreads();
   } else if (mode == kDiag) {
-    cta_lu_solve_par<T>(r, t.X, r, t.piv, false, xr, n, nc);
+    diag_solve(t, xr, n, nc, sx + (size_t)n * nc);
   }
   __syncthreads();
   const int lo = mode == kDiag ? k : 0;   // the diagonal solve changes x_r only
@@ -1750,10 +1884,12 @@ template <typename T>
 void launch_sweep(Factorization<T>& F, int l, int mode, T* x, int ncols, cudaStream_t s) {
   LevelFactor& LF = F.levels[l];
   if (LF.n_comp == 0 || ncols == 0) return;
-  int cw = std::max(1, std::min(ncols, (int)(96 * 1024 / (sizeof(T) * std::max(1, LF.max_n)))));
+  // shared memory: the box's rows (n x cw) and the inverse product's
+  // temporary (r x cw <= n x cw)
+  int cw = std::max(1, std::min(ncols, (int)(96 * 1024 / (2 * sizeof(T) * std::max(1, LF.max_n)))));
   cw = std::min(cw, 32);
   dim3 grid(LF.n_comp, (ncols + cw - 1) / cw);
-  size_t sm = sizeof(T) * (size_t)LF.max_n * cw;
+  size_t sm = 2 * sizeof(T) * (size_t)LF.max_n * cw;
   if (sm > 200 * 1024) throw std::runtime_error("box too large for the sweep kernel");
   if (sm > 48 * 1024)
     KI_CUDA(cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -2132,13 +2268,15 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     const int ntask = (int)itasks.size();
     float* d_feat = (float*)F->alloc(sizeof(float) * kMlpIn * (size_t)ntask);
     int* d_lsk = (int*)F->alloc(sizeof(int) * (size_t)ntask);
+    float* d_khat = (float*)F->alloc(sizeof(float) * (size_t)ntask);
     k_box_features<T><<<(ntask + 127) / 128, 128, 0, s>>>(
         d_it, ntask, ipool, P, sd, d_m, 2 * np * sd, L > 1 ? (float)l / (float)(L - 1) : 0.f,
         (float)(-std::log10(prm.id_tol) / 10.0), prm.rank_model, prm.sketch_margin,
-        prm.sketch_oversample, d_feat, d_lsk);
+        prm.sketch_oversample, d_feat, d_lsk, d_khat);
     KI_CUDA(cudaGetLastError());
     std::vector<int> mh(itasks.size()), kh(itasks.size()), lh(itasks.size());
-    std::vector<float> fh(kMlpIn * (size_t)ntask);
+    std::vector<float> fh(kMlpIn * (size_t)ntask), khat(itasks.size());
+    KI_CUDA(cudaMemcpyAsync(khat.data(), d_khat, sizeof(float) * khat.size(), cudaMemcpyDeviceToHost, s));
     KI_CUDA(cudaMemcpyAsync(lh.data(), d_lsk, sizeof(int) * lh.size(), cudaMemcpyDeviceToHost, s));
     KI_CUDA(cudaMemcpyAsync(fh.data(), d_feat, sizeof(float) * fh.size(), cudaMemcpyDeviceToHost, s));
     KI_CUDA(cudaMemcpyAsync(mh.data(), d_m, sizeof(int) * mh.size(), cudaMemcpyDeviceToHost, s));
@@ -2178,8 +2316,15 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         comp2.push_back(comp[o]);
         grp2.push_back(grp[o]);
         m2.push_back(mh[o]);
-        // sketches only where the triangle sits in shared memory (group 0)
-        l2.push_back(grp[o] == 0 ? lh[o] : 0);
+        // sketches for the shared-memory triangles (group 0) and the wide
+        // boxes (groups 2, 3; k_wide_sketch, up to 384 rows; their sketches are
+        // cheap next to a fallback, so they get twice the margin and
+        // oversampling), not for packed triangles
+        int lo = lh[o];
+        if (grp[o] >= 2 && prm.rank_model)
+          lo = std::min(itasks[o].n, (int)std::ceil((1.f + 2 * prm.sketch_margin) * khat[o]) +
+                                         2 * prm.sketch_oversample);
+        l2.push_back(grp[o] == 1 || (grp[o] >= 2 && lo > 384) ? 0 : lo);
         f2.insert(f2.end(), fh.begin() + kMlpIn * o, fh.begin() + kMlpIn * (o + 1));
       }
       itasks.swap(it2);
@@ -2235,12 +2380,12 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
           k_id<T, 64><<<(unsigned)(b1 - b0), kThreads, sm, st>>>(d_it, b0, d_soff, d_slen, ipool, d_irows,
                                                                  d_tws, P, sd, ptab,
                                                                  prm.id_tol, d_k, d_m, kmode, flags,
-                                                                 sketching && g == 0 ? d_lsk : nullptr);
+                                                                 sketching && g != 1 ? d_lsk : nullptr);
         else
           k_id<T, 32><<<(unsigned)(b1 - b0), kThreads, sm, st>>>(d_it, b0, d_soff, d_slen, ipool, d_irows,
                                                                  d_tws, P, sd, ptab,
                                                                  prm.id_tol, d_k, d_m, kmode, flags,
-                                                                 sketching && g == 0 ? d_lsk : nullptr);
+                                                                 sketching && g != 1 ? d_lsk : nullptr);
         KI_CUDA(cudaGetLastError());
         b0 = b1;
       }
@@ -2253,9 +2398,9 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     launch_range(1, 2, nullptr);
     // (d) wide boxes: explicit ID matrix, blocked Householder QR, then CPQR
     {
-      std::vector<WideTask> wt;
-      int64_t mtot = 0;
-      int maxn = 0;
+      std::vector<WideTask> wt, wsk;   // blocked-QR boxes, sketched boxes
+      int64_t mtot = 0, ptot = 0;
+      int maxn = 0, max_chunks = 0, max_cb = 0, max_l = 0;
       for (size_t i = 0; i < itasks.size(); i++) {
         if (grp[i] < 2) continue;
         WideTask w{};
@@ -2263,8 +2408,6 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         w.n = itasks[i].n;
         w.m = mh[i];
         w.nI = (mh[i] - (itasks[i].mode == 0 ? 2 * np * sd : 0)) / 2;
-        w.M = mtot;
-        mtot += (int64_t)w.m * w.n;
         w.act = itasks[i].act;
         w.rows = itasks[i].rows;
         w.cx = itasks[i].cx;
@@ -2272,39 +2415,71 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         w.cz = itasks[i].cz;
         w.rad = itasks[i].rad_proxy;
         w.R = itasks[i].ws;
+        if (sketching && lh[i] > 0 && lh[i] <= w.n && lh[i] <= 384) {
+          w.l = lh[i];
+          w.chunks = (w.m + kSketchRows - 1) / kSketchRows;
+          w.part = ptot;
+          ptot += (int64_t)w.chunks * w.l * w.n;
+          max_chunks = std::max(max_chunks, w.chunks);
+          max_cb = std::max(max_cb, (w.n + kSketchCols - 1) / kSketchCols);
+          max_l = std::max(max_l, w.l);
+          wsk.push_back(w);
+          continue;
+        }
+        w.M = mtot;
+        mtot += (int64_t)w.m * w.n;
         maxn = std::max(maxn, w.n);
         wt.push_back(w);
       }
       cudaStream_t ws3 = F->aux[Factorization<T>::kAux - 1];
-      if (!wt.empty()) {
-        for (auto& w : wt) {
-          w.Tf = mtot;
-          mtot += kQrNb * kQrNb;
-        }
-        T* d_wpool = nullptr;
-        KI_CUDA(pool_malloc((void**)&d_wpool, sizeof(T) * (mtot + 16), ws3));
-        WideTask* d_wt = nullptr;
-        KI_CUDA(pool_malloc((void**)&d_wt, sizeof(WideTask) * wt.size(), ws3));
-        upload(d_wt, wt, ws3);
+      if (!wt.empty() || !wsk.empty()) {
         std::string wq = "wide_qr@L" + std::to_string(l);
         F->stage_begin(wq.c_str(), 0, 0, ws3);
-        k_wide_assemble<T><<<dim3((unsigned)wt.size(), (maxn + 7) / 8), 256, 0, ws3>>>(
-            d_wt, d_wpool, ipool, d_irows, P, sd, ptab);
-        for (int p0 = 0; p0 < maxn; p0 += kQrNb) {
-          k_qr_panel<T><<<(unsigned)wt.size(), 256, 0, ws3>>>(d_wt, d_wpool, p0);
-          int tiles = (maxn - p0 - kQrNb + kQrTile - 1) / kQrTile;
-          if (tiles > 0) k_qr_update<T><<<dim3((unsigned)wt.size(), tiles), 256, 0, ws3>>>(d_wt, d_wpool, p0);
+        T* d_wpool = nullptr;
+        WideTask* d_wt = nullptr;
+        if (!wt.empty()) {
+          for (auto& w : wt) {
+            w.Tf = mtot;
+            mtot += kQrNb * kQrNb;
+          }
+          KI_CUDA(pool_malloc((void**)&d_wpool, sizeof(T) * (mtot + 16), ws3));
+          KI_CUDA(pool_malloc((void**)&d_wt, sizeof(WideTask) * wt.size(), ws3));
+          upload(d_wt, wt, ws3);
+          k_wide_assemble<T><<<dim3((unsigned)wt.size(), (maxn + 7) / 8), 256, 0, ws3>>>(
+              d_wt, d_wpool, ipool, d_irows, P, sd, ptab);
+          for (int p0 = 0; p0 < maxn; p0 += kQrNb) {
+            k_qr_panel<T><<<(unsigned)wt.size(), 256, 0, ws3>>>(d_wt, d_wpool, p0);
+            int tiles = (maxn - p0 - kQrNb + kQrTile - 1) / kQrTile;
+            if (tiles > 0) k_qr_update<T><<<dim3((unsigned)wt.size(), tiles), 256, 0, ws3>>>(d_wt, d_wpool, p0);
+          }
+          k_wide_triangle<T><<<(unsigned)wt.size(), 256, 0, ws3>>>(d_wt, d_wpool, d_tws);
+          KI_CUDA(cudaGetLastError());
         }
-        k_wide_triangle<T><<<(unsigned)wt.size(), 256, 0, ws3>>>(d_wt, d_wpool, d_tws);
-        KI_CUDA(cudaGetLastError());
+        T* d_spool = nullptr;
+        WideTask* d_wsk = nullptr;
+        if (!wsk.empty()) {
+          KI_CUDA(pool_malloc((void**)&d_spool, sizeof(T) * (ptot + 16), ws3));
+          KI_CUDA(pool_malloc((void**)&d_wsk, sizeof(WideTask) * wsk.size(), ws3));
+          upload(d_wsk, wsk, ws3);
+          const size_t skm = sizeof(T) * ((size_t)max_l * kSketchCols + kSketchSub * kSketchCols) +
+                             sizeof(uint32_t) * kSketchSub * ((max_l + 31) / 32);
+          KI_CUDA(cudaFuncSetAttribute(k_wide_sketch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem_cap));
+          k_wide_sketch<T><<<dim3((unsigned)wsk.size(), max_chunks, max_cb), 256, skm, ws3>>>(
+              d_wsk, d_spool, ipool, d_irows, P, sd, ptab);
+          k_wide_sketch_reduce<T><<<(unsigned)wsk.size(), 256, 0, ws3>>>(d_wsk, d_spool, d_tws);
+          KI_CUDA(cudaGetLastError());
+        }
         F->stage_end(ws3);
         std::string wc = "wide_cpqr@L" + std::to_string(l);
         F->stage_begin(wc.c_str(), 0, 0, ws3);
         launch_range(2, 4, ws3);
         launch_range(3, 4, ws3);
         F->stage_end(ws3);
-        KI_CUDA(cudaFreeAsync(d_wpool, ws3));
-        KI_CUDA(cudaFreeAsync(d_wt, ws3));
+        if (d_wpool) KI_CUDA(cudaFreeAsync(d_wpool, ws3));
+        if (d_wt) KI_CUDA(cudaFreeAsync(d_wt, ws3));
+        if (d_spool) KI_CUDA(cudaFreeAsync(d_spool, ws3));
+        if (d_wsk) KI_CUDA(cudaFreeAsync(d_wsk, ws3));
       }
     }
     F->join(Factorization<T>::kAux);
@@ -2316,18 +2491,31 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       // boxes whose sketch did not reveal the rank (k = -1): the plain ID
       std::vector<int> fb;
       for (size_t i = 0; i < kh.size(); i++) {
-        if (lh[i] > 0 && lh[i] < itasks[i].n) F->n_sketched++;
+        if (lh[i] > 0 && (lh[i] < itasks[i].n || grp[i] >= 2)) F->n_sketched++;
         if (kh[i] < 0) fb.push_back((int)i);
       }
       if (!fb.empty()) {
+        // mode 0 (triangle in shared memory) where it fits, else mode 1
+        // (triangle in the task's global scratch)
         std::vector<IdTask> t2;
         std::vector<int> m2;
-        size_t sm = 0;
-        for (int i : fb) {
-          t2.push_back(itasks[i]);
-          m2.push_back(mh[i]);
-          sm = std::max(sm, id_smem_bytes<T>(itasks[i].n, 0, 32, 2));
-        }
+        size_t sm[2] = {0, 0};
+        int cnt0 = 0;
+        for (int pass = 0; pass < 2; pass++)
+          for (int i : fb) {
+            const int md = id_smem_bytes<T>(itasks[i].n, 0, 32, 2) <= smem_cap ? 0 : 1;
+            if (md != pass) continue;
+            t2.push_back(itasks[i]);
+            m2.push_back(mh[i]);
+            sm[md] = std::max(sm[md], id_smem_bytes<T>(itasks[i].n, md, 32, 2));
+            if (md == 0) cnt0++;
+          }
+        if (sm[1] > smem_cap) throw std::runtime_error("box too large for the ID kernel");
+        std::vector<int> fb2;
+        for (int pass = 0; pass < 2; pass++)
+          for (int i : fb)
+            if ((id_smem_bytes<T>(itasks[i].n, 0, 32, 2) <= smem_cap ? 0 : 1) == pass) fb2.push_back(i);
+        fb.swap(fb2);
         IdTask* d_t2 = (IdTask*)F->alloc(sizeof(IdTask) * t2.size());
         int* d_m2 = (int*)F->alloc(sizeof(int) * t2.size());
         int* d_k2 = (int*)F->alloc(sizeof(int) * t2.size());
@@ -2335,9 +2523,14 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         upload(d_m2, m2, s);
         std::string fname = "id_fallback@L" + std::to_string(l);
         F->stage_begin(fname.c_str(), 0, 0);
-        k_id<T, 32><<<(unsigned)t2.size(), kThreads, sm, s>>>(d_t2, 0, d_soff, d_slen, ipool, d_irows,
-                                                              d_tws, P, sd, ptab, prm.id_tol, d_k2,
-                                                              d_m2, 0, 2, nullptr);
+        if (cnt0 > 0)
+          k_id<T, 32><<<(unsigned)cnt0, kThreads, sm[0], s>>>(d_t2, 0, d_soff, d_slen, ipool, d_irows,
+                                                               d_tws, P, sd, ptab, prm.id_tol, d_k2,
+                                                               d_m2, 0, 2, nullptr);
+        if ((int)t2.size() > cnt0)
+          k_id<T, 32><<<(unsigned)(t2.size() - cnt0), kThreads, sm[1], s>>>(
+              d_t2, cnt0, d_soff, d_slen, ipool, d_irows, d_tws, P, sd, ptab, prm.id_tol, d_k2, d_m2,
+              1, 2, nullptr);
         F->stage_end();
         KI_CUDA(cudaGetLastError());
         std::vector<int> k2(t2.size());
@@ -2492,9 +2685,31 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     }
     F->stage_end();
     KI_CUDA(cudaGetLastError());
+    if (sizeof(T) < sizeof(double)) {
+      // FP32: explicit inverses of the redundant blocks for the sweeps (the
+      // FP64 form keeps the reference's LU substitution)
+      int64_t xi_tot = 0;
+      for (auto& w : sw) {
+        const int64_t r = w.n - w.k;
+        if (r <= kInvMax) xi_tot += r * r;
+      }
+      T* d_xi = (T*)F->alloc(Tsz * (xi_tot + 1));
+      int64_t o = 0;
+      for (auto& w : sw) {
+        const int64_t r = w.n - w.k;
+        if (r <= kInvMax) {
+          w.Xi = d_xi + o;
+          o += r * r;
+        }
+      }
+    }
     SweepTask<T>* d_sw = (SweepTask<T>*)F->alloc(sizeof(SweepTask<T>) * sw.size());
     upload(d_sw, sw, s);
     LF.d_tasks = d_sw;
+    if (sizeof(T) < sizeof(double)) {
+      k_lu_inverse<T><<<(unsigned)sw.size(), kThreads, 0, s>>>(d_sw);
+      KI_CUDA(cudaGetLastError());
+    }
     for (int i : ci_list) F->rank_hist.push_back(kh[i]);
   }
 

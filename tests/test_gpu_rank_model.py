@@ -113,3 +113,23 @@ def test_learned_rank_sketched_factorization_in_mixed_solve(pkg):
     # the sketched factorization is an approximate inverse of comparable quality
     assert rl["residual0"] <= 10 * rp["residual0"] + 1e-6, (rp, rl)
     assert np.abs(mu_l - mu_p).max() <= 1e-8 * np.abs(mu_p).max()
+
+
+def test_underpredicting_model_falls_back_to_the_plain_id(pkg):
+    """A model that predicts near-zero ranks (output bias shifted down) makes
+    nearly every sketch too small: those boxes are recompressed by the plain
+    ID and the factorization is the same approximate inverse."""
+    prob, f, kw = _disc(pkg, 1 << 15, 16, 5)
+    bad = pkg.load_rank_model().copy()
+    bad[-1] -= 30.0
+    common = dict(id_tol=1e-6, precision=pkg.PRECISION_FP32, **kw)
+    plain = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, **common)
+    fb = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, rank_model=bad,
+                    **common)
+    info = fb.info()
+    assert info["n_sketched"] > 0 and info["n_fallback"] >= 0.9 * info["n_sketched"], info
+    assert info["n_compressed"] == plain.info()["n_compressed"]
+    assert info["n_root"] == plain.info()["n_root"]
+    mu_p = plain.solve(f)[0]
+    mu_f = fb.solve(f)[0]
+    assert np.abs(mu_f - mu_p).max() <= 1e-4 * np.abs(mu_p).max()
