@@ -325,8 +325,13 @@ def main():
         kw, refine = form(precision)
         infos = []
 
+        walls = []
+
         def step_device():
+            t0 = time.perf_counter()
             fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, **kw)
+            t1 = time.perf_counter()
+            fac.set_profiling(True)   # CUDA events around the solve's launch groups
             if refine:
                 infos.append(fac.solve_refined_device(d_b.data_ptr(), d_x.data_ptr(), nrhs,
                                                       d_a.data_ptr(), tol=args.target,
@@ -334,6 +339,8 @@ def main():
             else:
                 fac.solve_device(d_b.data_ptr(), d_x.data_ptr(), nrhs, d_a.data_ptr())
             torch.cuda.synchronize()
+            walls.append({"create_ms": (t1 - t0) * 1e3,
+                          "solve_ms": (time.perf_counter() - t1) * 1e3})
             return fac
 
         def step_host():
@@ -353,6 +360,8 @@ def main():
         for _ in range(warmup):
             step_device().close()
         infos.clear()
+        walls.clear()
+        hosts = []
         # ---- value: device-resident right-hand sides
         barrier()
         torch.cuda.synchronize()
@@ -363,17 +372,23 @@ def main():
             for _ in range(steps):
                 fac = step_device()
                 prof = fac.profile()
-                stage_runs.append(prof["factor"])
+                stage_runs.append(prof["factor"] + [dict(r, stage="refine:" + r["stage"])
+                                                    for r in prof.get("refine", [])])
                 level_stats = prof.get("levels", [])
+                hosts.append(prof.get("host", {}))
                 info = fac.info()
                 fac.close()
             ev1.record()
             torch.cuda.synchronize()
         barrier()
         t_dev = rep.max_over_ranks(ev0.elapsed_time(ev1) / 1e3 / steps, device="cuda")
+        host = {}
+        for rec in walls + hosts:
+            for k, v in rec.items():
+                host[k] = host.get(k, 0.0) + v / steps
         return dict(kw=kw, refine=refine, t_dev=t_dev, stage_runs=stage_runs,
                     level_stats=level_stats, info=info, infos=list(infos), clk=clk.summary(),
-                    step_host=step_host)
+                    step_host=step_host, host=host)
 
     main_form = run_form(args.precision, args.steps, args.warmup)
     kw, refine = main_form["kw"], main_form["refine"]
@@ -448,24 +463,51 @@ def main():
         f = fam.setdefault(k.split("@")[0], {"ms": 0.0, "flops": 0.0, "bytes": 0.0, "launches": 0})
         for q in ("ms", "flops", "bytes", "launches"):
             f[q] += v[q]
-    top = max(fam.items(), key=lambda kv: kv[1]["ms"])
+    # dominant stage family of the step (factorization stages and, for the
+    # refined forms, the refinement's: FMM near field, M2L, ...), excluding
+    # the correction solves (sweeps already listed as factor data) and groups
+    # without an algorithmic flop count
+    cand = {k: v for k, v in fam.items() if v["flops"] > 0}
+    top = max(cand.items(), key=lambda kv: kv[1]["ms"])
     peaks, peak_src = load_peaks()
     fp64_gf, fp32_gf = pkg.measure_fma_peak()
     name, a = top
     sec = a["ms"] / 1e3
     ach_tflops = a["flops"] / sec / 1e12 if sec > 0 else 0.0
-    cc_peak = (fp64_gf if args.precision == "fp64" else fp32_gf) / 1e3
-    roofline = {"bound": "fp64" if args.precision == "fp64" else "fp32",
-                "kernel": "k_id (%s stage: fused ID-matrix assembly, TSQR, column-pivoted QR)" % name,
+    if name.startswith("refine:fmm32"):
+        fp64_stage = False
+    elif name.startswith("refine:"):
+        fp64_stage = True
+    else:
+        fp64_stage = args.precision == "fp64"
+    cc_peak = (fp64_gf if fp64_stage else fp32_gf) / 1e3
+    describe = {
+        "refine:fmm_near": ("k_l2p_p2p (FMM near field: direct sum over the 3x3 leaf "
+                            "neighbourhood, 32 columns, plus the local expansions at the targets)",
+                            "near-field point pairs x (4 x 32 + 12) + targets x p x (4 x 32 + 6) "
+                            "flops / device time of the launches"),
+        "refine:fmm_m2l": ("k_m2l (FMM multipole-to-local translations)",
+                           "interaction pairs x p^2 x 32 columns x 8 flops / device time"),
+        "schur": ("k_schur (schur stage: per box, the redundant block's LU or inverse and the "
+                  "Schur updates of the skeleton and near-field blocks)",
+                  "algorithmic Schur-complement flops summed over the level's boxes / device "
+                  "time of the level's schur launches, summed over levels"),
+        "id": ("k_id (id stage: fused ID-matrix assembly, TSQR or sketch, column-pivoted QR)",
+               "algorithmic ID flops (4mnk - 2k^2(m+n) + 4/3 k^3 + k^2 r summed over the level's "
+               "boxes) / device time of the level's ID launches, summed over levels"),
+    }
+    kname, kdef = describe.get(name, (name, "algorithmic flops of the stage / its device time"))
+    share = a["ms"] / args.steps / (t_dev * 1e3)
+    roofline = {"bound": "fp64" if fp64_stage else "fp32",
+                "kernel": kname, "stage": name,
                 "achieved": ach_tflops, "peak": cc_peak, "unit": "TFLOP/s",
                 "frac": ach_tflops / cc_peak if cc_peak > 0 else None, "traffic": None,
+                "share_of_step": share,
                 "peak_source": "CUDA-core FMA peak measured on this GPU by ki_measure_fma_peak "
                                "(MEASURED_PEAKS.json lists only HBM copy and bf16 tensor peaks: "
                                "hbm %.0f GB/s, bf16 %.0f TFLOP/s, %s)" % (
                                    peaks.get("hbm_gbs", 0), peaks.get("bf16_tflops", 0), peak_src),
-                "achieved_definition": "algorithmic ID flops (4mnk - 2k^2(m+n) + 4/3 k^3 + k^2 r "
-                                       "summed over the level's boxes) / device time of the "
-                                       "level's ID launches, summed over levels",
+                "achieved_definition": kdef,
                 "launches_per_step": a["launches"] / args.steps,
                 "ms_per_step": a["ms"] / args.steps}
     stage_table = {k: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps,
@@ -523,11 +565,15 @@ def main():
         "refinement": {"steps_per_solve": [r["steps"] for r in refines],
                        "residual_first_solve": [r["residual0"] for r in refines],
                        "residual_final": [r["residual"] for r in refines],
-                       "residual_operator": "FMM (2D Laplace)" if (wl.dim == 2 and wl.sol_dim == 1
-                                                                  and N >= 4096) else "dense FP64"}
+                       "residual_updates": [r["updates"] for r in refines],
+                       "drift_bound": [r["drift_bound"] for r in refines],
+                       "residual_operator": "FMM (2D Laplace; FP64 at the target's order, "
+                                            "updates by the FP32 12-term FMM)"
+                       if (wl.dim == 2 and wl.sol_dim == 1 and N >= 4096) else "dense FP64"}
         if refine else None,
         "fp64_form_same_residual": compare,
         "learned_rank": learned,
+        "host_wall_ms_per_step": main_form["host"],
         "roofline": roofline,
         "stages": stage_table,
         "solve_stages": solve_prof,

@@ -176,6 +176,15 @@ int ki_apply_fmm(ki_factor* f, const double* x, int ldx, int ncols, const double
                  int ldalpha, double* y, int ldy);
 
 /*
+ * ki_apply_fmm with `order` expansion terms (0: 24; at most 32) and, with
+ * fp32 != 0, FP32 arithmetic for the charges, expansions, translations and
+ * near-field sums (the apply of refinement's residual updates; relative
+ * error ~1e-6 at 12 terms).
+ */
+int ki_apply_fmm_ex(ki_factor* f, const double* x, int ldx, int ncols, const double* alpha,
+                    int ldalpha, double* y, int ldy, int order, int fp32);
+
+/*
  * The same restricted to the listed DOFs: y (nrows x ncols, ldy) = rows of
  * K x (+ U alpha).  Cost O(nrows * n_dofs * ncols): a sampled residual check
  * at sizes where the full dense product is out of reach.
@@ -197,7 +206,12 @@ int ki_eval_targets(ki_factor* f, const double* targets, int n_targets, const do
 typedef struct {
   int steps;          /* refinement corrections applied after the first solve */
   double residual0;   /* max over columns of ||[b;0] - A[x;alpha]|| / ||b|| after the first solve */
-  double residual;    /* the same after the last correction */
+  double residual;    /* the same after the last correction: an upper bound, the updated
+                         residual plus drift_bound (max over columns) */
+  int updates;        /* corrections whose residual was updated (r -= A_low d) rather than
+                         recomputed */
+  double drift_bound; /* bound on the updated residuals' distance from the FP64 residual,
+                         relative to ||b|| (max over columns; 0 without updates) */
 } ki_refine_info;
 
 /*
@@ -213,7 +227,15 @@ typedef struct {
  * operator product is the FMM of ki_apply_fmm for 2D Laplace problems with
  * at least 4096 unknowns (O(n_dofs * nrhs) per step), else the dense FP64
  * product (O(n_dofs^2 * nrhs)); the environment variable
- * KI_RESIDUAL_APPLY=dense|fmm overrides the choice.
+ * KI_RESIDUAL_APPLY=dense|fmm overrides the choice.  With the FMM, a
+ * correction d whose residual change is small enough is followed by the
+ * update r -= A_low d, A_low the FMM in FP32 arithmetic at 12 terms
+ * (relative error eps_low = 1e-5 or better), instead of a new FP64 product:
+ * the update is taken while the accumulated bound eps_low * sum over
+ * updates of (||r_before|| + ||r_after||) / ||b|| (so that ||A d|| <=
+ * ||r_before|| + ||r_after||) stays below tol / 20 per column; the
+ * reported residual is the updated one plus that bound.
+ * KI_REFINE_UPDATE=0 recomputes the FP64 residual after every correction.
  */
 int ki_solve_refined(ki_factor* f, const double* b, int ldb, int nrhs, double* x, int ldx,
                      double* alpha, int ldalpha, double tol, int max_steps, ki_refine_info* info);

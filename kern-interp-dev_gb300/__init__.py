@@ -31,7 +31,7 @@ EXPORTED = ["ki_factor_create", "ki_factor_destroy", "ki_factor_get_info", "ki_s
             "ki_solve_device", "ki_apply", "ki_eval_targets", "ki_last_error", "ki_version",
             "ki_factor_get_profile", "ki_factor_set_profiling", "ki_apply_rows",
             "ki_measure_fma_peak", "ki_solve_refined", "ki_solve_refined_device",
-            "ki_solve_device_noalloc", "ki_apply_fmm", "ki_trim_memory", "ki_rank_model_floats",
+            "ki_solve_device_noalloc", "ki_apply_fmm", "ki_apply_fmm_ex", "ki_trim_memory", "ki_rank_model_floats",
             "ki_rank_model_train", "ki_rank_model_predict", "ki_rank_model_grad",
             "ki_factor_get_box_log"]
 RANK_MODEL_PATH = os.path.join(HERE, "rank_model.npy")
@@ -59,7 +59,8 @@ class _Desc(ctypes.Structure):
 
 class _RefineInfo(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_int), ("residual0", ctypes.c_double),
-                ("residual", ctypes.c_double)]
+                ("residual", ctypes.c_double), ("updates", ctypes.c_int),
+                ("drift_bound", ctypes.c_double)]
 
 
 class _Info(ctypes.Structure):
@@ -92,6 +93,7 @@ def load_library(path=None):
     lib.ki_apply.argtypes = [V, V, I, I, V, I, V, I]
     lib.ki_eval_targets.argtypes = [V, V, I, V, I, I, V, I, V, I]
     lib.ki_apply_fmm.argtypes = [V, V, I, I, V, I, V, I]
+    lib.ki_apply_fmm_ex.argtypes = [V, V, I, I, V, I, V, I, I, I]
     lib.ki_apply_rows.argtypes = [V, V, I, V, I, I, V, I, V, I]
     lib.ki_factor_get_profile.argtypes = [V, ctypes.c_char_p, I]
     lib.ki_factor_set_profiling.argtypes = [V, I]
@@ -232,7 +234,8 @@ class Factor:
         _check(load_library().ki_solve_refined(self._h, _ptr(B), self.n_dofs, nrhs, _ptr(X),
                                                self.n_dofs, _ptr(A), max(1, self.n_border),
                                                tol, max_steps, ctypes.byref(info)))
-        res = dict(steps=info.steps, residual0=info.residual0, residual=info.residual)
+        res = dict(steps=info.steps, residual0=info.residual0, residual=info.residual,
+                   updates=info.updates, drift_bound=info.drift_bound)
         x = X[:, 0] if vec else X
         if self.n_border:
             return x, (A[:, 0] if vec else A), res
@@ -245,7 +248,8 @@ class Factor:
             self._h, ctypes.c_void_p(d_b), nrhs, ctypes.c_void_p(d_x),
             ctypes.c_void_p(d_alpha) if d_alpha else None, tol, max_steps, ctypes.byref(info),
             ctypes.c_void_p(stream) if stream else None))
-        return dict(steps=info.steps, residual0=info.residual0, residual=info.residual)
+        return dict(steps=info.steps, residual0=info.residual0, residual=info.residual,
+                   updates=info.updates, drift_bound=info.drift_bound)
 
     def solve_device(self, d_b, d_x, nrhs, d_alpha=0, stream=0):
         """Device-pointer solve (integers: cudaMalloc'd addresses, column-major)."""
@@ -268,8 +272,9 @@ class Factor:
                                        max(1, self.n_border), _ptr(Y), self.n_dofs))
         return Y[:, 0] if vec else Y
 
-    def apply_fmm(self, x, alpha=None):
-        """K x (+ U alpha) by the fast multipole method (2D Laplace)."""
+    def apply_fmm(self, x, alpha=None, order=0, fp32=False):
+        """K x (+ U alpha) by the fast multipole method (2D Laplace); order:
+        expansion terms (0: 24), fp32: FP32 expansion arithmetic."""
         x = np.asarray(x, np.float64)
         vec = x.ndim == 1
         X = np.asfortranarray(x.reshape(self.n_dofs, -1))
@@ -277,8 +282,9 @@ class Factor:
         A = None
         if alpha is not None:
             A = np.asfortranarray(np.asarray(alpha, np.float64).reshape(self.n_border, -1))
-        _check(load_library().ki_apply_fmm(self._h, _ptr(X), self.n_dofs, X.shape[1], _ptr(A),
-                                           max(1, self.n_border), _ptr(Y), self.n_dofs))
+        _check(load_library().ki_apply_fmm_ex(self._h, _ptr(X), self.n_dofs, X.shape[1], _ptr(A),
+                                              max(1, self.n_border), _ptr(Y), self.n_dofs,
+                                              int(order), int(bool(fp32))))
         return Y[:, 0] if vec else Y
 
     def apply_rows(self, rows, x, alpha=None):

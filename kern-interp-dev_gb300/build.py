@@ -17,7 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libki_gpu.so")
 OBJ = os.path.join(ROOT, "_build", "obj")
 
-CU_SOURCES = ["ki_factor.cu", "ki_dense.cu", "ki_abi.cu", "ki_fmm.cu", "ki_pool.cu", "ki_mlp.cu"]
+CU_SOURCES = ["ki_factor.cu", "ki_dense.cu", "ki_abi.cu", "ki_fmm.cu", "ki_pool.cu", "ki_mlp.cu",
+              "ki_tree_gpu.cu"]
 CPP_SOURCES = ["ki_tree.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -1,6 +1,7 @@
 // C ABI (include/ki_gpu.h) over the GPU factorization.
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
@@ -204,26 +205,27 @@ __global__ void k_chunk_reduce(const double* part, int nchunks, int nrows, int n
 
 // Entry (component comp, border column k of one hole) of the border matrix U
 // (initialize_U_mat, kern_interp/linear_solve.cpp:19-107); r = x - hole centre.
-__device__ double border_u(int dim, int sol_dim, int comp, int k, const double* r) {
-  double r2 = 0;
+template <typename R>
+__device__ R border_u(int dim, int sol_dim, int comp, int k, const R* r) {
+  R r2 = 0;
   for (int d = 0; d < dim; d++) r2 += r[d] * r[d];
-  const double rn = sqrt(r2);
-  if (sol_dim == 1) return dim == 2 ? log(rn) : 1.0 / rn;
+  if (sol_dim == 1) return dim == 2 ? R(0.5) * log(r2) : R(1) / sqrt(r2);   // log |r|, 1/|r|
+  const R rn = sqrt(r2);
   if (dim == 2) {
-    const double sc = 1.0 / (4 * ki::kPi), q = rn * rn;
-    const double rx = r[0], ry = r[1];
+    const R sc = R(1.0 / (4 * ki::kPi)), q = rn * rn;
+    const R rx = r[0], ry = r[1];
     if (k == 0) return comp == 0 ? sc * (log(1 / rn) + rx * rx / q) : sc * (ry * rx / q);
     if (k == 1) return comp == 0 ? sc * (rx * ry / q) : sc * (log(1 / rn) + ry * ry / q);
     return comp == 0 ? ry * (sc / q) : -rx * (sc / q);
   }
-  const double rn3 = rn * rn * rn;
-  if (k < 3) return (1.0 / (8.0 * ki::kPi)) * ((comp == k ? 1.0 : 0.0) / rn + r[comp] * r[k] / rn3);
-  const double rot = -1.0 / (8.0 * ki::kPi * rn3);
+  const R rn3 = rn * rn * rn;
+  if (k < 3) return R(1.0 / (8.0 * ki::kPi)) * ((comp == k ? R(1) : R(0)) / rn + r[comp] * r[k] / rn3);
+  const R rot = R(-1.0 / (8.0 * ki::kPi)) / rn3;
   const int b = k - 3;
-  if (comp == b) return 0.0;
+  if (comp == b) return 0;
   // [r]_x entries: (0,1) -r2, (0,2) r1, (1,0) r2, (1,2) -r0, (2,0) -r1, (2,1) r0
   const int o = 3 - comp - b;   // the remaining axis
-  const double sgn = ((comp + 1) % 3 == b) ? -1.0 : 1.0;
+  const R sgn = ((comp + 1) % 3 == b) ? R(-1) : R(1);
   return rot * sgn * r[o];
 }
 
@@ -231,9 +233,12 @@ __device__ double border_u(int dim, int sol_dim, int comp, int k, const double* 
 // the points; else DOF q).  Points: dim per point with the given stride
 // between points (SoA x with stride 1 and separate y/z, or interleaved).
 // Each U entry (a log or a reciprocal distance) is evaluated once and
-// applied to up to 32 columns held in registers.
+// applied to up to 32 columns held in registers.  R: the arithmetic of the
+// entries and sums (float for the residual updates' low-accuracy apply; the
+// offsets from the hole centres are formed in FP64).
 constexpr int kBorderCols = 32;
 
+template <typename R = double>
 __global__ void k_border_apply(const double* px, const double* py, const double* pz, int stride,
                                int n_points, int dim, int sol_dim, const double* hc, int nh,
                                const double* alpha, int lda, int ncols, double* y, int ldy,
@@ -247,23 +252,23 @@ __global__ void k_border_apply(const double* px, const double* py, const double*
                         dim == 3 ? pz[(size_t)stride * p] : 0.0};
   for (int c0 = 0; c0 < ncols; c0 += kBorderCols) {
     const int nc = min(kBorderCols, ncols - c0);
-    double acc[kBorderCols];
+    R acc[kBorderCols];
 #pragma unroll
-    for (int c = 0; c < kBorderCols; c++) acc[c] = 0.0;
+    for (int c = 0; c < kBorderCols; c++) acc[c] = 0;
     for (int h = 0; h < nh; h++) {
-      double r[3];
-      for (int d = 0; d < dim; d++) r[d] = xp[d] - hc[dim * h + d];
+      R r[3];
+      for (int d = 0; d < dim; d++) r[d] = R(xp[d] - hc[dim * h + d]);
       for (int k = 0; k < cph; k++) {
-        const double u = border_u(dim, sol_dim, comp, k, r);
+        const R u = border_u<R>(dim, sol_dim, comp, k, r);
         const double* al = alpha + cph * h + k + (size_t)lda * c0;
 #pragma unroll
         for (int c = 0; c < kBorderCols; c++)
-          if (c < nc) acc[c] += u * al[(size_t)lda * c];
+          if (c < nc) acc[c] += u * R(al[(size_t)lda * c]);
       }
     }
 #pragma unroll
     for (int c = 0; c < kBorderCols; c++)
-      if (c < nc) y[q + (size_t)ldy * (c0 + c)] += acc[c];
+      if (c < nc) y[q + (size_t)ldy * (c0 + c)] += double(acc[c]);
   }
 }
 
@@ -342,18 +347,33 @@ struct ki_factor {
   int* d_hstart = nullptr;     // hole node ranges
   int* d_hcount = nullptr;
   ki::Points<double> P{};
-  // fast FP64 operator apply (2D Laplace): its host plan is computed on a
-  // worker thread while the factorization runs, uploaded on first use
-  std::future<std::unique_ptr<ki::Fmm2dPlan, ki::Fmm2dPlanDeleter>> fmm_plan;
+  // refinement profile (CUDA events; see ki_factor_set_profiling)
+  bool profile_refine = false;
+  std::vector<ki::StageRec> refine_open;
+  std::vector<ki::StageSum> refine_prof;
+  // fast FP64 operator apply (2D Laplace): planned and uploaded (on its own
+  // stream) by a worker thread while the factorization runs
+  std::future<std::unique_ptr<ki::Fmm2d, ki::Fmm2dDeleter>> fmm_ready;
+  cudaStream_t fmm_stream = nullptr;
   std::unique_ptr<ki::Fmm2d, ki::Fmm2dDeleter> fmm;
+  // host wall-clock milliseconds: create before the factorization (argument
+  // copies, geometry upload), the factorization call, waiting for the FMM
+  // worker
+  double host_prep_ms = 0, host_factor_ms = 0, fmm_wait_ms = 0;
   ~ki_factor() {
-    if (fmm_plan.valid()) {
+    for (auto& r : refine_open) {
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+    if (fmm_ready.valid()) {
       try {
-        fmm_plan.get();
+        fmm_ready.get();
       } catch (...) {
       }
     }
+    if (stream) cudaStreamSynchronize(stream);   // no apply still reads the FMM buffers
     fmm.reset();
+    if (fmm_stream) cudaStreamDestroy(fmm_stream);
     f64.reset();
     f32.reset();
     if (d_geo) cudaFree(d_geo);
@@ -630,13 +650,17 @@ __global__ void k_residual(const double* b, int ldb, const double* y, int ldy, i
   }
 }
 
-// x (column-major, ldx) += d (DOF-major in precision T, ld = ncols).
+// x (column-major, ldx) += d (DOF-major in precision T, ld = ncols); with
+// dcol, d is also stored there in FP64 (column-major, ld = n).
 template <typename T>
-__global__ void k_add_dofmajor(const T* d, int n, int ncols, double* x, int ldx) {
+__global__ void k_add_dofmajor(const T* d, int n, int ncols, double* x, int ldx,
+                               double* dcol = nullptr) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * ncols;
        e += (size_t)gridDim.x * blockDim.x) {
     int i = (int)(e % n), c = (int)(e / n);
-    x[i + (size_t)ldx * c] += double(d[(size_t)i * ncols + c]);
+    const double v = double(d[(size_t)i * ncols + c]);
+    x[i + (size_t)ldx * c] += v;
+    if (dcol) dcol[e] = v;
   }
 }
 
@@ -650,27 +674,87 @@ __global__ void k_to_rowmajor(const double* a, int lda, int n, int ncols, T* out
 }
 
 template <typename T>
-__global__ void k_add_rowmajor(const T* d, int n, int ncols, double* a, int lda) {
+__global__ void k_add_rowmajor(const T* d, int n, int ncols, double* a, int lda,
+                               double* dcol = nullptr) {
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * ncols; e += gridDim.x * blockDim.x) {
     int i = e % n, c = e / n;
-    a[i + (size_t)lda * c] += double(d[(size_t)i * ncols + c]);
+    const double v = double(d[(size_t)i * ncols + c]);
+    a[i + (size_t)lda * c] += v;
+    if (dcol) dcol[e] = v;
   }
 }
 
 // y1 = K mu + U alpha, y2 = Psi mu - alpha (FP64, column-major, ld = N / nb).
+// low: K by the FP32 FMM at kLowOrder terms (requires use_fmm).
 void apply_bordered(ki_factor* f, const double* mu, const double* alpha, int ncols, double* y1,
-                    double* y2, cudaStream_t s, double target);
+                    double* y2, cudaStream_t s, double target, ki::StageRecorder* rec,
+                    bool low = false);
+bool use_fmm(const ki_factor* f);
+
+// The low-accuracy apply of residual updates: FMM terms, and the relative
+// error (2-norm, per column) it is credited with.  12 terms leave a
+// truncation error near 4e-7 (1.4e-8 * 0.43^(12 - 16)); FP32 arithmetic adds
+// rounding of the same order; 1e-5 keeps a margin over both.
+constexpr int kLowOrder = 12;
+constexpr double kLowRelErr = 1e-5;
+
+// CUDA-event recorder of the refinement's launch groups (into the handle).
+struct RefineRecorder : ki::StageRecorder {
+  ki_factor* f;
+  cudaStream_t s;
+  RefineRecorder(ki_factor* f_, cudaStream_t s_) : f(f_), s(s_) {}
+  void begin(const char* name, double flops) override {
+    ki::StageRec r;
+    r.stage = name;
+    r.flops = flops;
+    KI_CHECK_CUDA(cudaEventCreate(&r.a));
+    KI_CHECK_CUDA(cudaEventCreate(&r.b));
+    KI_CHECK_CUDA(cudaEventRecord(r.a, s));
+    f->refine_open.push_back(r);
+  }
+  void end() override { KI_CHECK_CUDA(cudaEventRecord(f->refine_open.back().b, s)); }
+};
 
 // Per-column relative residual of [mu; alpha] for right-hand side b:
 // returns max over columns of ||[b;0] - A[mu;alpha]|| / ||b||, leaves r1/r2.
+double column_norms(ki_factor* f, const double* b, const double* r1, const double* r2, int ncols,
+                    double* work, std::vector<double>* rel, cudaStream_t s);
+
 double residual_norms(ki_factor* f, const double* b, const double* mu, const double* alpha,
                       int ncols, double* r1, double* r2, double* work, std::vector<double>* rel,
-                      cudaStream_t s, double target) {
+                      cudaStream_t s, double target, ki::StageRecorder* rec) {
   const int N = f->n_dofs, nb = f->n_border;
-  apply_bordered(f, mu, alpha, ncols, r1, r2, s, target);
+  apply_bordered(f, mu, alpha, ncols, r1, r2, s, target, rec);
+  if (rec) rec->begin("residual_other", 0);
   k_residual<<<grid_for((size_t)N * ncols), 256, 0, s>>>(b, N, r1, N, N, ncols, r1, N);
   if (nb > 0) k_residual<<<grid_for((size_t)nb * ncols), 256, 0, s>>>(nullptr, 0, r2, nb, nb, ncols, r2, nb);
   KI_CHECK_CUDA(cudaGetLastError());
+  const double worst = column_norms(f, b, r1, r2, ncols, work, rel, s);
+  if (rec) rec->end();
+  return worst;
+}
+
+// The residual update after a correction [d; d_alpha]: [r1; r2] -= A_low
+// [d; d_alpha] (y1, y2: scratch of the residual's shape), then the column
+// norms.
+double update_residual(ki_factor* f, const double* b, const double* d, const double* dal,
+                       int ncols, double* r1, double* r2, double* y1, double* y2, double* work,
+                       std::vector<double>* rel, cudaStream_t s, ki::StageRecorder* rec) {
+  const int N = f->n_dofs, nb = f->n_border;
+  apply_bordered(f, d, dal, ncols, y1, y2, s, 0.0, rec, true);
+  if (rec) rec->begin("residual_other", 0);
+  k_residual<<<grid_for((size_t)N * ncols), 256, 0, s>>>(r1, N, y1, N, N, ncols, r1, N);
+  if (nb > 0) k_residual<<<grid_for((size_t)nb * ncols), 256, 0, s>>>(r2, nb, y2, nb, nb, ncols, r2, nb);
+  KI_CHECK_CUDA(cudaGetLastError());
+  const double worst = column_norms(f, b, r1, r2, ncols, work, rel, s);
+  if (rec) rec->end();
+  return worst;
+}
+
+// Per-column ||[r1; r2]|| / ||b|| (host vector rel), returns the largest.
+double column_norms(ki_factor* f, const double* b, const double* r1, const double* r2, int ncols,
+                    double* work, std::vector<double>* rel, cudaStream_t s) {
+  const int N = f->n_dofs, nb = f->n_border;
   // work: part (kNormBlocks x ncols) | sq_r (ncols) | sq_b (ncols)
   double* part = work;
   double* sq = work + (size_t)kNormBlocks * ncols;
@@ -698,9 +782,12 @@ double residual_norms(ki_factor* f, const double* b, const double* mu, const dou
 }
 
 // One correction: [mu; alpha] += M^-1 [r1; r2], M the factorization (precision T).
+// With dcol / dal, the correction is also stored there in FP64 (column-
+// major, ld = N / nb).
 template <typename T>
 void correct(ki_factor* f, ki::Factorization<T>& F, const double* r1, const double* r2, int ncols,
-             double* mu, double* alpha, cudaStream_t s) {
+             double* mu, double* alpha, cudaStream_t s, double* dcol = nullptr,
+             double* dal = nullptr) {
   const int N = f->n_dofs, nb = f->n_border;
   DevBuf<T> work((size_t)N * ncols, s), al((size_t)std::max(1, nb) * ncols, s),
       g((size_t)std::max(1, nb) * ncols, s);
@@ -716,8 +803,9 @@ void correct(ki_factor* f, ki::Factorization<T>& F, const double* r1, const doub
     throw;
   }
   F.stream = saved;
-  k_add_dofmajor<T><<<grid_for((size_t)N * ncols), 256, 0, s>>>(work.p, N, ncols, mu, N);
-  if (nb > 0) k_add_rowmajor<T><<<grid_for((size_t)nb * ncols), 256, 0, s>>>(al.p, nb, ncols, alpha, nb);
+  k_add_dofmajor<T><<<grid_for((size_t)N * ncols), 256, 0, s>>>(work.p, N, ncols, mu, N, dcol);
+  if (nb > 0)
+    k_add_rowmajor<T><<<grid_for((size_t)nb * ncols), 256, 0, s>>>(al.p, nb, ncols, alpha, nb, dal);
   KI_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -732,22 +820,80 @@ void refined_solve(ki_factor* f, const double* b, int ncols, double* mu, double*
   if (nb > 0) KI_CHECK_CUDA(cudaMemsetAsync(alpha, 0, sizeof(double) * (size_t)nb * ncols, s));
   KI_CHECK_CUDA(cudaMemcpyAsync(r1.p, b, sizeof(double) * (size_t)N * ncols, cudaMemcpyDeviceToDevice, s));
   if (nb > 0) KI_CHECK_CUDA(cudaMemsetAsync(r2.p, 0, sizeof(double) * (size_t)nb * ncols, s));
-  auto corr = [&] {
-    if (f->f64) correct<double>(f, *f->f64, r1.p, r2.p, ncols, mu, alpha, s);
-    else correct<float>(f, *f->f32, r1.p, r2.p, ncols, mu, alpha, s);
+  RefineRecorder recorder(f, s);
+  ki::StageRecorder* rec = f->profile_refine ? &recorder : nullptr;
+  // residual updates (see ki_solve_refined): the low-accuracy FMM apply of
+  // the correction instead of a new FP64 product, while the accumulated
+  // drift bound stays below tol / 20
+  const char* ue = std::getenv("KI_REFINE_UPDATE");
+  const bool may_update = use_fmm(f) && !(ue && std::string(ue) == "0");
+  DevBuf<double> dcol(may_update ? (size_t)N * ncols : 1, s),
+      dal(may_update ? (size_t)std::max(1, nb) * ncols : 1, s),
+      y1(may_update ? (size_t)N * ncols : 1, s),
+      y2(may_update ? (size_t)std::max(1, nb) * ncols : 1, s);
+  auto corr = [&](bool keep) {
+    if (rec) rec->begin("precond_solve", 0);
+    double* dc = keep ? dcol.p : nullptr;
+    double* da = keep && nb > 0 ? dal.p : nullptr;
+    if (f->f64) correct<double>(f, *f->f64, r1.p, r2.p, ncols, mu, alpha, s, dc, da);
+    else correct<float>(f, *f->f32, r1.p, r2.p, ncols, mu, alpha, s, dc, da);
+    if (rec) rec->end();
   };
-  corr();   // x0 = M^-1 b
-  std::vector<double> rel;
-  double res = residual_norms(f, b, mu, alpha, ncols, r1.p, r2.p, work.p, &rel, s, tol);
+  corr(false);   // x0 = M^-1 b
+  std::vector<double> rel, rel_old;
+  double res = residual_norms(f, b, mu, alpha, ncols, r1.p, r2.p, work.p, &rel, s, tol, rec);
   info->residual0 = res;
-  int steps = 0;
-  while (res > tol && steps < max_steps) {
-    corr();
+  std::vector<double> drift(ncols, 0.0);
+  auto bound = [&] {
+    double w = 0.0;
+    for (int c = 0; c < ncols; c++) w = std::max(w, rel[c] + drift[c]);
+    return w;
+  };
+  int steps = 0, updates = 0;
+  while (bound() > tol && steps < max_steps) {
+    // an update is taken when even ||r_after|| = ||r_before|| keeps the
+    // accumulated bound below tol / 20 in every column
+    bool update = may_update;
+    for (int c = 0; c < ncols && update; c++)
+      update = drift[c] + kLowRelErr * 2.0 * rel[c] <= tol / 20;
+    corr(update);
     steps++;
-    res = residual_norms(f, b, mu, alpha, ncols, r1.p, r2.p, work.p, &rel, s, tol);
+    if (update) {
+      rel_old = rel;
+      res = update_residual(f, b, dcol.p, nb > 0 ? dal.p : nullptr, ncols, r1.p, r2.p, y1.p,
+                            y2.p, work.p, &rel, s, rec);
+      for (int c = 0; c < ncols; c++) drift[c] += kLowRelErr * (rel_old[c] + rel[c]);
+      updates++;
+    } else {
+      res = residual_norms(f, b, mu, alpha, ncols, r1.p, r2.p, work.p, &rel, s, tol, rec);
+      std::fill(drift.begin(), drift.end(), 0.0);
+    }
   }
   info->steps = steps;
-  info->residual = res;
+  info->residual = bound();
+  info->updates = updates;
+  info->drift_bound = *std::max_element(drift.begin(), drift.end());
+  if (rec) {
+    // aggregate this solve's records by stage
+    KI_CHECK_CUDA(cudaStreamSynchronize(s));
+    f->refine_prof.clear();
+    for (auto& r : f->refine_open) {
+      float ms = 0;
+      KI_CHECK_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+      auto it = std::find_if(f->refine_prof.begin(), f->refine_prof.end(),
+                             [&](const ki::StageSum& q) { return q.stage == r.stage; });
+      if (it == f->refine_prof.end()) {
+        f->refine_prof.push_back(ki::StageSum{r.stage, 0, 0, 0, 0});
+        it = f->refine_prof.end() - 1;
+      }
+      it->launches++;
+      it->ms += ms;
+      it->flops += r.flops;
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+    f->refine_open.clear();
+  }
 }
 
 }  // namespace
@@ -779,9 +925,11 @@ int fmm_order_for(double target, int plan_order) {
 }
 
 ki::Fmm2d& fmm_for(ki_factor* f, cudaStream_t s) {
-  if (!f->fmm && f->fmm_plan.valid()) {
-    auto plan = f->fmm_plan.get();
-    f->fmm = ki::fmm2d_upload(*plan, s);
+  if (!f->fmm && f->fmm_ready.valid()) {
+    const auto t0 = std::chrono::steady_clock::now();
+    f->fmm = f->fmm_ready.get();   // uploaded: the worker synchronized its stream
+    f->fmm_wait_ms = std::chrono::duration<double, std::milli>(
+                         std::chrono::steady_clock::now() - t0).count();
   }
   if (!f->fmm) {
     // geometry back from the device copy (the handle keeps no host arrays)
@@ -812,30 +960,42 @@ bool use_fmm(const ki_factor* f) {
 
 // fast: FMM with `order` terms (0: 24, relative error ~2e-11)
 void apply_K(ki_factor* f, const double* mu, int ncols, double* y1, cudaStream_t s, bool fast,
-             int order = 0) {
+             int order = 0, ki::StageRecorder* rec = nullptr,
+             ki::FmmArith arith = ki::FmmArith::kF64) {
   const int N = f->n_dofs;
   if (fast) {
     ki::Fmm2d& F = fmm_for(f, s);
-    ki::fmm2d_apply(F, mu, N, ncols, y1, N, s, order > 0 ? order : std::min(24, ki::fmm2d_order(F)));
+    ki::fmm2d_apply(F, mu, N, ncols, y1, N, s, order > 0 ? order : std::min(24, ki::fmm2d_order(F)),
+                    rec, arith);
     return;
   }
+  if (rec) rec->begin("dense_apply", 0);
   dense_product(f->P, f->n_points, f->sol_dim, mu, N, ncols, y1, N, nullptr, 0, nullptr, s);
+  if (rec) rec->end();
 }
 
 void apply_bordered(ki_factor* f, const double* mu, const double* alpha, int ncols, double* y1,
-                    double* y2, cudaStream_t s, double target) {
+                    double* y2, cudaStream_t s, double target, ki::StageRecorder* rec, bool low) {
   const int N = f->n_dofs, nb = f->n_border;
   const bool fast = use_fmm(f);
-  apply_K(f, mu, ncols, y1, s, fast, fast ? fmm_order_for(target, ki::fmm2d_order(fmm_for(f, s))) : 0);
+  if (low && !fast) throw std::logic_error("low-accuracy apply without the FMM");
+  if (low)
+    apply_K(f, mu, ncols, y1, s, true, kLowOrder, rec, ki::FmmArith::kF32);
+  else
+    apply_K(f, mu, ncols, y1, s, fast,
+            fast ? fmm_order_for(target, ki::fmm2d_order(fmm_for(f, s))) : 0, rec);
   if (nb > 0) {
-    k_border_apply<<<(N + 127) / 128, 128, 0, s>>>(f->P.x, f->P.y, f->P.z, 1, f->n_points, f->dim,
-                                                   f->sol_dim, f->d_holes, f->n_holes, alpha, nb,
-                                                   ncols, y1, N);
+    if (rec) rec->begin("border_apply", 0);
+    auto border = low ? k_border_apply<float> : k_border_apply<double>;
+    border<<<(N + 127) / 128, 128, 0, s>>>(f->P.x, f->P.y, f->P.z, 1, f->n_points, f->dim,
+                                           f->sol_dim, f->d_holes, f->n_holes, alpha, nb, ncols,
+                                           y1, N, nullptr, 0);
     const int cph = nb / f->n_holes;
     k_psi_apply<<<dim3(nb, ncols), 256, 0, s>>>(f->d_pts, f->P.w, f->dim, f->sol_dim, f->d_holes,
                                                 f->d_hstart, f->d_hcount, cph, mu, N, alpha, nb,
                                                 y2, nb);
     KI_CHECK_CUDA(cudaGetLastError());
+    if (rec) rec->end();
   }
 }
 }  // namespace
@@ -847,6 +1007,7 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
     if (!out) throw ArgError("out is NULL");
     *out = nullptr;
     check_desc(desc);
+    const auto t_create = std::chrono::steady_clock::now();
     int dev_count = 0;
     if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
       cudaGetLastError();
@@ -926,9 +1087,10 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
     KI_CHECK_CUDA(cudaMalloc(&f->d_pts, sizeof(double) * dim * (size_t)n));
     KI_CHECK_CUDA(cudaMemcpy(f->d_pts, desc->points, sizeof(double) * dim * (size_t)n,
                              cudaMemcpyHostToDevice));
-    // 2D Laplace: the FMM plan for refinement residuals, on a worker thread
-    // concurrent with the factorization (it copies the caller's arrays first;
-    // this call returns only after the copy)
+    // 2D Laplace: the FMM for refinement residuals, planned and uploaded by a
+    // worker thread on its own stream, concurrent with the factorization (it
+    // copies the caller's arrays first; this call returns only after the
+    // copy)
     std::promise<void> copied;
     std::future<void> copied_f = copied.get_future();
     bool planning = false;
@@ -937,7 +1099,11 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
       const double *pp = desc->points, *nn = desc->normals, *ww = desc->weights,
                    *kk = desc->curvatures;
       const int order = fmm_order();
-      f->fmm_plan = std::async(std::launch::async, [pp, nn, ww, kk, n, order, &copied] {
+      KI_CHECK_CUDA(cudaStreamCreateWithFlags(&f->fmm_stream, cudaStreamNonBlocking));
+      cudaStream_t us = f->fmm_stream;
+      int dev = 0;
+      KI_CHECK_CUDA(cudaGetDevice(&dev));
+      f->fmm_ready = std::async(std::launch::async, [pp, nn, ww, kk, n, order, us, dev, &copied] {
         std::vector<double> P, Nn, W, K;
         try {
           P.assign(pp, pp + 2 * (size_t)n);
@@ -950,7 +1116,9 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
           throw;
         }
         copied.set_value();
-        return ki::fmm2d_plan(P.data(), Nn.data(), W.data(), K.data(), n, order);
+        auto plan = ki::fmm2d_plan(P.data(), Nn.data(), W.data(), K.data(), n, order);
+        KI_CHECK_CUDA(cudaSetDevice(dev));   // the caller's device, not the thread default
+        return ki::fmm2d_upload(*plan, us);
       });
     }
     struct WaitCopy {   // the caller's arrays stay valid until the worker has copied them
@@ -960,12 +1128,16 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
         if (on) fut.wait();
       }
     } wait_copy{planning, copied_f};
+    const auto t_factor = std::chrono::steady_clock::now();
+    f->host_prep_ms = std::chrono::duration<double, std::milli>(t_factor - t_create).count();
     if (f->precision == KI_PRECISION_FP64)
       f->f64 = ki::factorize<double>(prm, n, desc->points, desc->normals, desc->weights,
                                      desc->curvatures, holes, f->stream);
     else
       f->f32 = ki::factorize<float>(prm, n, desc->points, desc->normals, desc->weights,
                                     desc->curvatures, holes, f->stream);
+    f->host_factor_ms = std::chrono::duration<double, std::milli>(
+                            std::chrono::steady_clock::now() - t_factor).count();
     // the FP64 3D diagonal of the factorization serves the FP64 apply
     f->P.diag = f->f64 ? f->f64->d_diag64 : f->f32->d_diag64;
     *out = f.release();
@@ -1086,9 +1258,15 @@ int ki_apply(ki_factor* f, const double* x, int ldx, int ncols, const double* al
 
 int ki_apply_fmm(ki_factor* f, const double* x, int ldx, int ncols, const double* alpha,
                  int ldalpha, double* y, int ldy) {
+  return ki_apply_fmm_ex(f, x, ldx, ncols, alpha, ldalpha, y, ldy, 0, 0);
+}
+
+int ki_apply_fmm_ex(ki_factor* f, const double* x, int ldx, int ncols, const double* alpha,
+                    int ldalpha, double* y, int ldy, int order, int fp32) {
   return guarded([&] {
     if (!f || !x || !y) throw ArgError("NULL argument");
     if (!fmm_capable(f)) throw StateError("ki_apply_fmm: 2D Laplace problems only");
+    if (order < 0 || order > 32) throw ArgError("order out of range");
     const int N = f->n_dofs, nb = f->n_border;
     if (ncols < 0 || ldx < N || ldy < N) throw ArgError("bad leading dimension / ncols");
     if (ncols == 0) return;
@@ -1096,7 +1274,8 @@ int ki_apply_fmm(ki_factor* f, const double* x, int ldx, int ncols, const double
     DevBuf<double> dx((size_t)N * ncols, s), dy((size_t)N * ncols, s);
     KI_CHECK_CUDA(cudaMemcpy2DAsync(dx.p, sizeof(double) * N, x, sizeof(double) * ldx,
                                     sizeof(double) * N, ncols, cudaMemcpyHostToDevice, s));
-    apply_K(f, dx.p, ncols, dy.p, s, true);
+    apply_K(f, dx.p, ncols, dy.p, s, true, order, nullptr,
+            fp32 ? ki::FmmArith::kF32 : ki::FmmArith::kF64);
     if (nb > 0 && alpha) {
       if (ldalpha < nb) throw ArgError("bad ldalpha");
       DevBuf<double> da((size_t)nb * ncols, s);
@@ -1229,6 +1408,7 @@ int ki_factor_set_profiling(ki_factor* f, int on) {
     if (!f) throw ArgError("factor is NULL");
     if (f->f64) f->f64->profile_solve = on != 0;
     if (f->f32) f->f32->profile_solve = on != 0;
+    f->profile_refine = on != 0;
   });
 }
 
@@ -1265,8 +1445,14 @@ int ki_factor_get_profile(ki_factor* f, char* buf, int len) {
         lv += tmp;
       }
       lv += "]";
+      char host[384];
+      snprintf(host, sizeof(host),
+               "{\"create_prep_ms\": %.3f, \"factor_call_ms\": %.3f, \"tree_ms\": %.3f, "
+               "\"fmm_wait_ms\": %.3f}",
+               f->host_prep_ms, f->host_factor_ms, F.tree_seconds * 1e3, f->fmm_wait_ms);
       j = "{\"factor\": " + dump(F.factor_prof) + ", \"solve\": " + dump(F.solve_prof) +
-          ", \"levels\": " + lv + "}";
+          ", \"refine\": " + dump(f->refine_prof) + ", \"levels\": " + lv +
+          ", \"host\": " + host + "}";
     };
     if (f->f64) fill(*f->f64);
     if (f->f32) fill(*f->f32);

@@ -36,6 +36,7 @@
 #include "ki_common.cuh"
 #include "ki_dense.h"
 #include "ki_mlp.h"
+#include "ki_tree_gpu.h"
 
 namespace ki {
 
@@ -1956,12 +1957,6 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
   F->n_points = n_points;
   Tree& tree = F->tree;
   const int dim = prm.dim;
-  tree.build(points, n_points, dim, prm.sol_dim, prm.max_leaf_dofs);
-  const int sd = prm.sol_dim;
-  const int nch = tree.n_children();
-  const int N = tree.n_dofs;
-  F->N = N;
-  const int L = tree.num_levels();
   cudaStream_t s = stream;
 
   // point data: interleaved FP64 input (points, normals: dim per point;
@@ -2001,6 +1996,33 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     }
     KI_CUDA(cudaGetLastError());
   }
+  // the tree: descent codes sorted on the GPU, boxes and lists on the host
+  // (KI_TREE_BUILD=host: the host partition build, also the fallback when
+  // the codes' depth does not reach the leaves)
+  {
+    const char* tb = std::getenv("KI_TREE_BUILD");
+    bool built = false;
+    if (!(tb && std::string(tb) == "host")) {
+      double c0 = 0, side0 = 0;
+      tree_root(points, n_points, dim, &c0, &side0);
+      const int depth = tree_code_depth(dim);
+      std::vector<uint64_t> codes(n_points);
+      std::vector<int> order(n_points);
+      tree_codes_sorted(d_pts_in, n_points, dim, c0, side0, depth, codes.data(), order.data(), s);
+      built = tree.build_from_codes(points, n_points, dim, prm.sol_dim, prm.max_leaf_dofs,
+                                    codes.data(), order.data(), depth);
+    }
+    if (!built) tree.build(points, n_points, dim, prm.sol_dim, prm.max_leaf_dofs);
+    F->tree_gpu = built;
+  }
+  F->tree_seconds =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  const int sd = prm.sol_dim;
+  const int nch = tree.n_children();
+  const int N = tree.n_dofs;
+  F->N = N;
+  const int L = tree.num_levels();
+
   Points<T> P{F->d_x, F->d_y, F->d_nx, F->d_ny, F->d_w, F->d_kappa};
   P.dim = dim;
   P.z = F->d_z;

@@ -114,6 +114,8 @@ struct Factorization {
   void stage_end(cudaStream_t on = nullptr);
   std::vector<StageSum> collect();   // synchronizes the stream
   double factor_seconds = 0;
+  double tree_seconds = 0;   // tree build (codes on the GPU, boxes on the host)
+  bool tree_gpu = false;      // the codes path built the tree (else the host partition)
   size_t device_bytes = 0;
   std::vector<void*> owned;   // device allocations to free
 

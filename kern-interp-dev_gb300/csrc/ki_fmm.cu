@@ -38,58 +38,105 @@ constexpr int kMaxP = 32;        // expansion terms (upper bound)
 constexpr int kChunk = 32;       // source points staged per shared-memory chunk
 constexpr double kPi2 = 6.283185307179586476925286766559;
 
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+// Complex values of the expansions: double2 (FP64 arithmetic) or float2
+// (FP32 arithmetic, the low-accuracy apply of residual updates).
+template <typename R> struct Cplx;
+template <> struct Cplx<double> { using type = double2; };
+template <> struct Cplx<float> { using type = float2; };
+template <typename R> using cplx_t = typename Cplx<R>::type;
+
+__device__ __forceinline__ double fmx(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fmx(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+template <typename V> __device__ __forceinline__ V czero() {
+  V r;
+  r.x = 0;
+  r.y = 0;
+  return r;
 }
-__device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c) {   // a*b + c
-  return make_double2(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
+template <typename V> __device__ __forceinline__ V cmul(V a, V b) {
+  V r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+template <typename V> __device__ __forceinline__ V cfma(V a, V b, V c) {   // a*b + c
+  V r;
+  r.x = fmx(a.x, b.x, fmx(-a.y, b.y, c.x));
+  r.y = fmx(a.x, b.y, fmx(a.y, b.x, c.y));
+  return r;
+}
+// an FP64 complex value rounded to the expansion type
+template <typename V> __device__ __forceinline__ V cround(double x, double y) {
+  V r;
+  r.x = (decltype(r.x))x;
+  r.y = (decltype(r.y))y;
+  return r;
 }
 
-// q[i + n c] = nw[i] * mu[perm[i] + ldmu c]  (sorted order)
+// q[i kCols + c] = nw[i] * mu[perm[i] + ldmu (c0 + c)]  (sorted order,
+// point-major: a point's columns are contiguous; product in FP64, rounded to
+// the expansion type).  Block (32, 8) per 32 points: columns read along the
+// points (coalesced in mu), written along the columns through shared memory.
+template <typename R>
 __global__ void k_charges(const double2* nw, const int* perm, int n, const double* mu, int ldmu,
-                          int c0, int nc, double2* q) {
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * nc;
-       e += (size_t)gridDim.x * blockDim.x) {
-    int i = (int)(e % n), c = (int)(e / n);
-    double m = mu[perm[i] + (size_t)ldmu * (c0 + c)];
-    q[e] = make_double2(nw[i].x * m, nw[i].y * m);
+                          int c0, int nc, cplx_t<R>* q) {
+  using V = cplx_t<R>;
+  __shared__ V tile[32][kCols + 1];
+  const int i0 = blockIdx.x * 32;
+  const int i = i0 + threadIdx.x;
+  if (i < n) {
+    const int o = perm[i];
+    const double2 w = nw[i];
+    for (int c = threadIdx.y; c < nc; c += blockDim.y) {
+      const double m = mu[o + (size_t)ldmu * (c0 + c)];
+      tile[threadIdx.x][c] = cround<V>(w.x * m, w.y * m);
+    }
+  }
+  __syncthreads();
+  const int cnt = min(32, n - i0);
+  for (int e = threadIdx.y * 32 + threadIdx.x; e < cnt * nc; e += 32 * blockDim.y) {
+    const int r = e / nc, c = e % nc;
+    q[(size_t)(i0 + r) * kCols + c] = tile[r][c];
   }
 }
 
 // Multipole expansion of every leaf: me[(g nc + c) p + k] = sum_s q_s w_s^k,
-// w_s = (z_s - centre) / side.
+// w_s = (z_s - centre) / side (formed in FP64).
+template <typename R>
 __global__ void k_p2m(const int* leaf_start, const int* leaf_box, const double2* centre,
-                      double side, const double2* z, const double2* q, int n, int nc, int p,
-                      double2* me) {
-  __shared__ double2 pw[kChunk][kMaxP];
-  __shared__ double2 qs[kChunk][kCols];
+                      double side, const double2* z, const cplx_t<R>* q, int n, int nc, int p,
+                      cplx_t<R>* me) {
+  using V = cplx_t<R>;
+  __shared__ V pw[kChunk][kMaxP];
+  __shared__ V qs[kChunk][kCols];
   const int lf = blockIdx.x, g = leaf_box[lf];
   const int s0 = leaf_start[lf], s1 = leaf_start[lf + 1];
   const double2 c = centre[g];
   const int nout = p * nc;
-  double2 acc[4];
-  for (int r = 0; r < 4; r++) acc[r] = make_double2(0, 0);
+  V acc[4];
+  for (int r = 0; r < 4; r++) acc[r] = czero<V>();
   for (int base = s0; base < s1; base += kChunk) {
     const int cnt = min(kChunk, s1 - base);
     __syncthreads();
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-      double2 w = make_double2((z[base + i].x - c.x) / side, (z[base + i].y - c.y) / side);
-      double2 t = make_double2(1, 0);
+      const V w = cround<V>((z[base + i].x - c.x) / side, (z[base + i].y - c.y) / side);
+      V t = cround<V>(1, 0);
       for (int k = 0; k < p; k++) {
         pw[i][k] = t;
         t = cmul(t, w);
       }
     }
     for (int e = threadIdx.x; e < cnt * nc; e += blockDim.x) {
-      int i = e % cnt, cc = e / cnt;
-      qs[i][cc] = q[base + i + (size_t)n * cc];
+      int i = e / nc, cc = e % nc;
+      qs[i][cc] = q[(size_t)(base + i) * kCols + cc];
     }
     __syncthreads();
     for (int r = 0; r < 4; r++) {
       int o = threadIdx.x + r * blockDim.x;
       if (o >= nout) break;
       int k = o % p, cc = o / p;
-      double2 a = acc[r];
+      V a = acc[r];
       for (int i = 0; i < cnt; i++) a = cfma(qs[i][cc], pw[i][k], a);
       acc[r] = a;
     }
@@ -105,30 +152,32 @@ __global__ void k_p2m(const int* leaf_start, const int* leaf_box, const double2*
 // me[P] = sum_children T_pos me[C], T_pos lower triangular (matrix leading
 // dimension ldm >= p).  Each child's expansions and its matrix are staged in
 // shared memory; output (k, c) is thread c + nc k.
-__global__ void k_m2m(int b0, const int* child, const int* child_pos, const double2* T, int ldm,
-                      int nc, int p, double2* me) {
-  __shared__ double2 sm_x[kCols * (kMaxP + 1)];
-  __shared__ double2 sm_T[kMaxP * kMaxP];
+template <typename R>
+__global__ void k_m2m(int b0, const int* child, const int* child_pos, const cplx_t<R>* T, int ldm,
+                      int nc, int p, cplx_t<R>* me) {
+  using V = cplx_t<R>;
+  __shared__ V sm_x[kCols * (kMaxP + 1)];
+  __shared__ V sm_T[kMaxP * kMaxP];
   const int g = b0 + blockIdx.x;
   const int nout = p * nc, ld = p + 1;
-  double2 acc[4];
-  for (int r = 0; r < 4; r++) acc[r] = make_double2(0, 0);
+  V acc[4];
+  for (int r = 0; r < 4; r++) acc[r] = czero<V>();
   for (int q = 0; q < 4; q++) {
     const int ch = child[4 * g + q];
     if (ch < 0) continue;
     __syncthreads();
-    const double2* src = me + (size_t)ch * nout;
+    const V* src = me + (size_t)ch * nout;
     for (int e = threadIdx.x; e < nout; e += blockDim.x) sm_x[(e / p) * ld + e % p] = src[e];
-    const double2* Tm = T + (size_t)child_pos[ch] * ldm * ldm;
+    const V* Tm = T + (size_t)child_pos[ch] * ldm * ldm;
     for (int e = threadIdx.x; e < p * p; e += blockDim.x) sm_T[e] = Tm[(size_t)(e / p) * ldm + e % p];
     __syncthreads();
     for (int r = 0; r < 4; r++) {
       int o = threadIdx.x + r * blockDim.x;
       if (o >= nout) break;
       const int cc = o % nc, k = o / nc;
-      double2 a = acc[r];
-      const double2* row = sm_T + k * p;
-      const double2* x = sm_x + cc * ld;
+      V a = acc[r];
+      const V* row = sm_T + k * p;
+      const V* x = sm_x + cc * ld;
       for (int j = 0; j <= k; j++) a = cfma(row[j], x[j], a);
       acc[r] = a;
     }
@@ -144,44 +193,50 @@ __global__ void k_m2m(int b0, const int* child, const int* child_pos, const doub
 // Local expansion contributions over the interaction list (M2L): for every
 // box g of one level, le[g] = (1/side) sum_v M_code(v) me[src(v)].  Output
 // (m, c) is thread c + nc m, so a warp shares one matrix row (broadcast) and
-// reads 32 columns of the staged multipole tile (row stride p + 1 doubles2:
-// conflict-free).
+// reads 32 columns of the staged multipole tile (row stride p + 1: conflict-
+// free).
+template <typename R>
 __global__ void k_m2l(int b0, const int* v_off, const int* v_src, const int* v_code,
-                      const double2* M, int ldm, double inv_side, int nc, int p,
-                      const double2* me, double2* le) {
-  __shared__ double2 sm_me[kCols * (kMaxP + 1)];
-  __shared__ double2 sm_M[kMaxP * kMaxP];
+                      const cplx_t<R>* M, int ldm, double inv_side, int nc, int p,
+                      const cplx_t<R>* me, cplx_t<R>* le) {
+  using V = cplx_t<R>;
+  __shared__ V sm_me[kCols * (kMaxP + 1)];
+  __shared__ V sm_M[kMaxP * kMaxP];
   const int g = b0 + blockIdx.x;
   const int nout = p * nc;
   const int ld = p + 1;
-  double2 acc[4];
-  for (int r = 0; r < 4; r++) acc[r] = make_double2(0, 0);
+  V acc[4];
+  for (int r = 0; r < 4; r++) acc[r] = czero<V>();
   for (int v = v_off[g]; v < v_off[g + 1]; v++) {
     __syncthreads();
-    const double2* src = me + (size_t)v_src[v] * nout;
+    const V* src = me + (size_t)v_src[v] * nout;
     for (int e = threadIdx.x; e < nout; e += blockDim.x) {
       const int k = e % p, cc = e / p;
       sm_me[cc * ld + k] = src[e];
     }
-    const double2* Mm = M + (size_t)v_code[v] * ldm * ldm;
+    const V* Mm = M + (size_t)v_code[v] * ldm * ldm;
     for (int e = threadIdx.x; e < p * p; e += blockDim.x) sm_M[e] = Mm[(size_t)(e / p) * ldm + e % p];
     __syncthreads();
     for (int r = 0; r < 4; r++) {
       int o = threadIdx.x + r * blockDim.x;
       if (o >= nout) break;
       const int cc = o % nc, m = o / nc;
-      double2 a = acc[r];
-      const double2* row = sm_M + m * p;
-      const double2* x = sm_me + cc * ld;
+      V a = acc[r];
+      const V* row = sm_M + m * p;
+      const V* x = sm_me + cc * ld;
       for (int k = 0; k < p; k++) a = cfma(row[k], x[k], a);
       acc[r] = a;
     }
   }
+  const R is = (R)inv_side;
   for (int r = 0; r < 4; r++) {
     int o = threadIdx.x + r * blockDim.x;
     if (o >= nout) break;
     const int cc = o % nc, m = o / nc;
-    le[(size_t)g * nout + (size_t)cc * p + m] = make_double2(acc[r].x * inv_side, acc[r].y * inv_side);
+    V out;
+    out.x = acc[r].x * is;
+    out.y = acc[r].y * is;
+    le[(size_t)g * nout + (size_t)cc * p + m] = out;
   }
 }
 
@@ -189,24 +244,26 @@ __global__ void k_m2l(int b0, const int* v_off, const int* v_src, const int* v_c
 // le[C] += S_pos le[P], S_pos upper triangular (leading dimension ldm); the
 // parent's expansions and the matrix staged in shared memory, output (j, c)
 // is thread c + nc j.
-__global__ void k_l2l(int b0, const int* parent, const int* child_pos, const double2* S, int ldm,
-                      int nc, int p, double2* le) {
-  __shared__ double2 sm_x[kCols * (kMaxP + 1)];
-  __shared__ double2 sm_S[kMaxP * kMaxP];
+template <typename R>
+__global__ void k_l2l(int b0, const int* parent, const int* child_pos, const cplx_t<R>* S, int ldm,
+                      int nc, int p, cplx_t<R>* le) {
+  using V = cplx_t<R>;
+  __shared__ V sm_x[kCols * (kMaxP + 1)];
+  __shared__ V sm_S[kMaxP * kMaxP];
   const int g = b0 + blockIdx.x;
   const int par = parent[g];
   const int nout = p * nc, ld = p + 1;
-  const double2* src = le + (size_t)par * nout;
+  const V* src = le + (size_t)par * nout;
   for (int e = threadIdx.x; e < nout; e += blockDim.x) sm_x[(e / p) * ld + e % p] = src[e];
-  const double2* Sm = S + (size_t)child_pos[g] * ldm * ldm;
+  const V* Sm = S + (size_t)child_pos[g] * ldm * ldm;
   for (int e = threadIdx.x; e < p * p; e += blockDim.x) sm_S[e] = Sm[(size_t)(e / p) * ldm + e % p];
   __syncthreads();
   for (int o = threadIdx.x; o < nout; o += blockDim.x) {
     const int cc = o % nc, j = o / nc;
     const size_t dst = (size_t)g * nout + (size_t)cc * p + j;
-    double2 a = le[dst];
-    const double2* row = sm_S + j * p;
-    const double2* x = sm_x + cc * ld;
+    V a = le[dst];
+    const V* row = sm_S + j * p;
+    const V* x = sm_x + cc * ld;
     for (int m = j; m < p; m++) a = cfma(row[m], x[m], a);
     le[dst] = a;
   }
@@ -225,80 +282,183 @@ __device__ __forceinline__ double recip_nr(double x) {
   return fma(y, e, y);
 }
 
+// Source coordinates staged for the near field: FP64 points, or for the FP32
+// apply each coordinate as an FP32 pair hi + lo (hi = fl(x), lo = fl(x - hi)),
+// so t - s = (t_hi - s_hi) + (t_lo - s_lo) keeps the full relative accuracy
+// of the difference of two nearby nodes (t_hi - s_hi is exact for nodes
+// within a factor of two of each other).
+template <typename R> struct NearPt;
+template <> struct NearPt<double> { using type = double2; };
+template <> struct NearPt<float> { using type = float4; };
+
+__device__ __forceinline__ void near_load(const double2* z, const float4*, int i, double2* out) {
+  *out = z[i];
+}
+__device__ __forceinline__ void near_load(const double2*, const float4* zf, int i, float4* out) {
+  *out = zf[i];
+}
+// (1/(t - s)) as (rx, ry) = (dx, -dy) / |t - s|^2
+__device__ __forceinline__ void near_recip(const double2& t, const double2& s, double* rx,
+                                           double* ry) {
+  const double dx = t.x - s.x, dy = t.y - s.y;
+  const double inv = recip_nr(dx * dx + dy * dy);
+  *rx = dx * inv;
+  *ry = -dy * inv;
+}
+__device__ __forceinline__ void near_recip(const float4& t, const float4& s, float* rx, float* ry) {
+  const float dx = (t.x - s.x) + (t.z - s.z), dy = (t.y - s.y) + (t.w - s.w);
+  const float inv = __frcp_rn(dx * dx + dy * dy);
+  *rx = dx * inv;
+  *ry = -dy * inv;
+}
+
 // Per leaf: far field from the local expansion, near field by direct
 // summation over the 3 x 3 leaf neighbourhood (exact entries, the
-// coincident point excluded), diagonal term; written unsorted into y.  One
-// thread per target with all 32 columns in registers.
-constexpr int kP2PThreads = 64;
+// coincident point excluded), diagonal term (FP64); written unsorted into y.
+//
+// Lanes are columns: a warp evaluates one target at a time for all 32
+// columns, so every FMA instruction has 32 useful lanes whatever the leaf's
+// size (a leaf holds 8 to 40 points).  The targets of a pass (up to 32)
+// are split over the four warps (target k of warp w: w + 4k, a warp-uniform
+// branch), each lane accumulating its column for its warp's targets.  Per
+// pass: the powers w_t^m of the targets and the kernel entries 1/(t - s) of
+// each 32-source chunk are formed once in shared memory (one entry per
+// thread) and broadcast to the lanes; charges and local expansions are read
+// [point or term][column] (conflict-free).  The output goes through shared
+// memory so that a warp writes 32 targets of one column.
+constexpr int kLeafThreads = 128;
+constexpr int kLeafWarps = kLeafThreads / 32;
+constexpr int kPassTargets = 32;
+constexpr int kWarpTargets = kPassTargets / kLeafWarps;
+constexpr int kSrcChunk = 32;
+static_assert(kSrcChunk == kMaxP, "bufA holds powers [t][m] and entries [t][s] in turn");
+static_assert(kPassTargets <= kCols, "bufB holds the output tile");
 
-__global__ void __launch_bounds__(kP2PThreads)
-    k_l2p_p2p(const int* leaf_start, const int* leaf_box, const int* near_off,
-              const int* near_leaf, const double2* centre, double side, const double2* z,
-              const double* diag, const int* perm, const double2* q, const double2* le, int n,
-              int nc, int p, const double* mu, int ldmu, int c0, double* y, int ldy) {
-  __shared__ double2 sz[kChunk];
-  __shared__ double2 sq[kChunk][kCols];
-  __shared__ double2 sle[kCols * kMaxP];
+template <typename R>
+__global__ void __launch_bounds__(kLeafThreads)
+    k_leaf_eval(const int* leaf_start, const int* leaf_box, const int* near_off,
+                const int* near_leaf, const double2* centre, double side, const double2* z,
+                const float4* zf, const double* diag, const int* perm, const cplx_t<R>* q,
+                const cplx_t<R>* le, int nc, int p, const double* mu, int ldmu, int c0,
+                double* y, int ldy) {
+  using V = cplx_t<R>;
+  using P = typename NearPt<R>::type;
+  __shared__ V bufA[kPassTargets * kMaxP];   // powers [t][m], then entries [t][s]
+  __shared__ V bufB[kSrcChunk * kCols];      // local expansion [m][c], charges [s][c], output
+  __shared__ P st[kPassTargets];
+  __shared__ P ss[kSrcChunk];
   const int lf = blockIdx.x, g = leaf_box[lf];
   const int t0 = leaf_start[lf], t1 = leaf_start[lf + 1];
   const double2 c = centre[g];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool col_on = lane < nc;
   const int nout = p * nc;
-  for (int e = threadIdx.x; e < nout; e += blockDim.x) sle[e] = le[(size_t)g * nout + e];
-  for (int tb = t0; tb < t1; tb += blockDim.x) {
-    const int t = tb + threadIdx.x;
-    const bool on = t < t1;
-    const double2 zt = on ? z[t] : make_double2(0, 0);
-    double acc[kCols];
-#pragma unroll
-    for (int cc = 0; cc < kCols; cc++) acc[cc] = 0.0;
-    __syncthreads();
-    if (on) {
-      // far field: Re sum_m le_m w^m
-      const double2 w = make_double2((zt.x - c.x) / side, (zt.y - c.y) / side);
-      double2 pw = make_double2(1, 0);
+  for (int tb = t0; tb < t1; tb += kPassTargets) {
+    const int nt = min(kPassTargets, t1 - tb);
+    __syncthreads();   // the previous pass's output is written
+    if (threadIdx.x < nt) {
+      const int t = tb + threadIdx.x;
+      near_load(z, zf, t, &st[threadIdx.x]);
+      const double2 zt = z[t];
+      const V w = cround<V>((zt.x - c.x) / side, (zt.y - c.y) / side);
+      V pw = cround<V>(1, 0);
       for (int m = 0; m < p; m++) {
-#pragma unroll
-        for (int cc = 0; cc < kCols; cc++) {
-          if (cc < nc) {
-            const double2 b = sle[cc * p + m];
-            acc[cc] += b.x * pw.x - b.y * pw.y;
-          }
-        }
+        bufA[threadIdx.x * kMaxP + m] = pw;
         pw = cmul(pw, w);
       }
     }
-    for (int v = near_off[lf]; v < near_off[lf + 1]; v++) {
-      const int sl = near_leaf[v];
-      const int s0 = leaf_start[sl], s1 = leaf_start[sl + 1];
-      for (int base = s0; base < s1; base += kChunk) {
-        const int cnt = min(kChunk, s1 - base);
-        __syncthreads();
-        for (int i = threadIdx.x; i < cnt; i += blockDim.x) sz[i] = z[base + i];
-        for (int e = threadIdx.x; e < cnt * nc; e += blockDim.x) {
-          int i = e % cnt, cc = e / cnt;
-          sq[i][cc] = q[base + i + (size_t)n * cc];
-        }
-        __syncthreads();
-        if (!on) continue;
-        for (int i = 0; i < cnt; i++) {
-          if (base + i == t) continue;
-          const double dx = zt.x - sz[i].x, dy = zt.y - sz[i].y;
-          const double inv = recip_nr(dx * dx + dy * dy);
-          const double rx = dx * inv, ry = -dy * inv;   // 1 / (t - s)
+    for (int e = threadIdx.x; e < nout; e += blockDim.x) {
+      const int m = e % p, cc = e / p;
+      bufB[m * kCols + cc] = le[(size_t)g * nout + e];
+    }
+    __syncthreads();
+    R acc[kWarpTargets];
 #pragma unroll
-          for (int cc = 0; cc < kCols; cc++)
-            if (cc < nc) acc[cc] += sq[i][cc].x * rx - sq[i][cc].y * ry;
+    for (int k = 0; k < kWarpTargets; k++) acc[k] = 0;
+    // far field: Re sum_m le_m w^m
+    if (col_on) {
+      for (int m = 0; m < p; m++) {
+        const V b = bufB[m * kCols + lane];
+#pragma unroll
+        for (int k = 0; k < kWarpTargets; k++) {
+          const int tt = warp + kLeafWarps * k;
+          if (tt < nt) {
+            const V a = bufA[tt * kMaxP + m];
+            acc[k] = fmx(b.x, a.x, fmx(-b.y, a.y, acc[k]));
+          }
         }
       }
     }
-    if (on) {
-      const int orig = perm[t];
+    // near field: Re sum_s q_s / (t - s)
+    for (int v = near_off[lf]; v < near_off[lf + 1]; v++) {
+      const int sl = near_leaf[v];
+      const int s0 = leaf_start[sl], s1 = leaf_start[sl + 1];
+      for (int base = s0; base < s1; base += kSrcChunk) {
+        const int cnt = min(kSrcChunk, s1 - base);
+        __syncthreads();   // readers of bufA / bufB done
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) near_load(z, zf, base + i, &ss[i]);
+        for (int e = threadIdx.x; e < cnt * nc; e += blockDim.x) {
+          const int i = e / nc, cc = e % nc;
+          bufB[i * kCols + cc] = q[(size_t)(base + i) * kCols + cc];
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < nt * cnt; e += blockDim.x) {
+          const int tt = e / cnt, i = e % cnt;
+          R rx = 0, ry = 0;
+          if (tb + tt != base + i) near_recip(st[tt], ss[i], &rx, &ry);
+          V en;
+          en.x = rx;
+          en.y = ry;
+          bufA[tt * kSrcChunk + i] = en;
+        }
+        __syncthreads();
+        if (col_on) {
+          for (int i = 0; i < cnt; i++) {
+            const V qv = bufB[i * kCols + lane];
 #pragma unroll
-      for (int cc = 0; cc < kCols; cc++)
-        if (cc < nc)
-          y[orig + (size_t)ldy * (c0 + cc)] =
-              acc[cc] + diag[t] * mu[orig + (size_t)ldmu * (c0 + cc)];
+            for (int k = 0; k < kWarpTargets; k++) {
+              const int tt = warp + kLeafWarps * k;
+              if (tt < nt) {
+                const V en = bufA[tt * kSrcChunk + i];
+                acc[k] = fmx(qv.x, en.x, fmx(-qv.y, en.y, acc[k]));
+              }
+            }
+          }
+        }
+      }
     }
+    __syncthreads();   // bufB becomes the output tile [t][c] (stride kCols + 1)
+    R* so = reinterpret_cast<R*>(bufB);
+    if (col_on) {
+#pragma unroll
+      for (int k = 0; k < kWarpTargets; k++) {
+        const int tt = warp + kLeafWarps * k;
+        if (tt < nt) so[tt * (kCols + 1) + lane] = acc[k];
+      }
+    }
+    __syncthreads();
+    const int tt = threadIdx.x % kPassTargets;
+    if (tt < nt) {
+      const int t = tb + tt, orig = perm[t];
+      const double dg = diag[t];
+      for (int cc = threadIdx.x / kPassTargets; cc < nc; cc += kLeafThreads / kPassTargets)
+        y[orig + (size_t)ldy * (c0 + cc)] =
+            (double)so[tt * (kCols + 1) + cc] + dg * mu[orig + (size_t)ldmu * (c0 + cc)];
+    }
+  }
+}
+
+// FP64 -> FP32 copies for the FP32 apply: complex arrays, and the sorted
+// points as hi/lo pairs.
+__global__ void k_round_cplx(const double2* a, size_t count, float2* out) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count;
+       e += (size_t)gridDim.x * blockDim.x)
+    out[e] = make_float2((float)a[e].x, (float)a[e].y);
+}
+__global__ void k_split_points(const double2* z, int n, float4* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float hx = (float)z[i].x, hy = (float)z[i].y;
+    out[i] = make_float4(hx, hy, (float)(z[i].x - (double)hx), (float)(z[i].y - (double)hy));
   }
 }
 
@@ -339,7 +499,7 @@ V* upload_vec(const std::vector<V>& v, std::vector<void*>* owned, cudaStream_t s
 
 struct Fmm2d {
   int n = 0, p = 0, L = 0, nleaf = 0, nbox = 0;
-  long m2l_pairs = 0, near_pairs = 0;
+  long m2l_pairs = 0, near_pairs = 0, near_point_pairs = 0;
   double lo = 0, side0 = 0;
   std::vector<int> lvl_off;   // global box index range of each level
   int *d_perm = nullptr, *d_leaf_start = nullptr, *d_leaf_box = nullptr;
@@ -349,6 +509,9 @@ struct Fmm2d {
   double2 *d_z = nullptr, *d_nw = nullptr, *d_centre = nullptr;
   double2 *d_T = nullptr, *d_S = nullptr, *d_M = nullptr;
   double* d_diag = nullptr;
+  // FP32 copies for the low-accuracy apply, made on its first use
+  float2 *d_T32 = nullptr, *d_S32 = nullptr, *d_M32 = nullptr;
+  float4* d_zf = nullptr;
   std::vector<void*> owned;
   cudaStream_t stream = nullptr;   // the upload stream; frees are ordered on it
   ~Fmm2d() {
@@ -361,6 +524,7 @@ void Fmm2dDeleter::operator()(Fmm2d* f) const { delete f; }
 // Host-side plan: everything fmm2d_upload copies to the device.
 struct Fmm2dPlan {
   int n = 0, p = 0, L = 0, nleaf = 0, nbox = 0;
+  long near_point_pairs = 0;   // (target, source) pairs of the near field, self excluded
   double lo = 0, side0 = 0;
   std::vector<int> lvl_off, order, leaf_start, leaf_box, near_off, near_leaf, child, parent,
       child_pos, v_off, v_src, v_code;
@@ -528,6 +692,13 @@ std::unique_ptr<Fmm2dPlan, Fmm2dPlanDeleter> fmm2d_plan(const double* pts, const
   }
   std::vector<int> leaf_box(F->nleaf);
   for (int i = 0; i < F->nleaf; i++) leaf_box[i] = F->lvl_off[L] + i;
+  for (int i = 0; i < F->nleaf; i++) {
+    long src = 0;
+    for (int v = near_off[i]; v < near_off[i + 1]; v++)
+      src += leaf_start[near_leaf[v] + 1] - leaf_start[near_leaf[v]];
+    F->near_point_pairs += (long)(leaf_start[i + 1] - leaf_start[i]) * src;
+  }
+  F->near_point_pairs -= n;
   F->order = std::move(order);
   F->leaf_start = std::move(leaf_start);
   F->leaf_box = std::move(leaf_box);
@@ -562,6 +733,7 @@ std::unique_ptr<Fmm2d, Fmm2dDeleter> fmm2d_upload(const Fmm2dPlan& P, cudaStream
   F->lvl_off = P.lvl_off;
   F->m2l_pairs = (long)P.v_src.size();
   F->near_pairs = (long)P.near_leaf.size();
+  F->near_point_pairs = P.near_point_pairs;
   F->d_perm = upload_vec(P.order, &F->owned, s);
   F->d_leaf_start = upload_vec(P.leaf_start, &F->owned, s);
   F->d_leaf_box = upload_vec(P.leaf_box, &F->owned, s);
@@ -590,44 +762,98 @@ std::unique_ptr<Fmm2d, Fmm2dDeleter> fmm2d_build(const double* pts, const double
   return fmm2d_upload(*fmm2d_plan(pts, nrm, wts, kap, n, p), s);
 }
 
-void fmm2d_apply(Fmm2d& F, const double* mu, int ldmu, int ncols, double* y, int ldy,
-                 cudaStream_t s, int order) {
+namespace {
+
+// The FP32 copies of the translation matrices and the hi/lo split points.
+void ensure_fp32(Fmm2d& F, cudaStream_t s) {
+  if (F.d_zf) return;
+  auto round = [&](const double2* a, size_t count) {
+    float2* d = nullptr;
+    KI_FMM_CUDA(pool_malloc((void**)&d, sizeof(float2) * count, s));
+    F.owned.push_back(d);
+    k_round_cplx<<<(int)std::min<size_t>(1024, (count + 255) / 256), 256, 0, s>>>(a, count, d);
+    return d;
+  };
+  const size_t pp = (size_t)F.p * F.p;
+  F.d_T32 = round(F.d_T, 4 * pp);
+  F.d_S32 = round(F.d_S, 4 * pp);
+  F.d_M32 = round(F.d_M, 49 * pp);
+  float4* zf = nullptr;
+  KI_FMM_CUDA(pool_malloc((void**)&zf, sizeof(float4) * (size_t)F.n, s));
+  F.owned.push_back(zf);
+  k_split_points<<<(F.n + 255) / 256, 256, 0, s>>>(F.d_z, F.n, zf);
+  KI_FMM_CUDA(cudaGetLastError());
+  F.d_zf = zf;
+}
+
+template <typename R>
+void apply_impl(Fmm2d& F, const cplx_t<R>* T, const cplx_t<R>* S, const cplx_t<R>* M,
+                const double* mu, int ldmu, int ncols, double* y, int ldy, cudaStream_t s, int p,
+                StageRecorder* rec, const char* const* names) {
+  using V = cplx_t<R>;
   const int n = F.n, L = F.L, nbox = F.nbox, ldm = F.p;
-  const int p = order > 0 ? std::min(order, F.p) : F.p;
   const int nc_max = std::min(ncols, kCols);
-  double2 *q = nullptr, *me = nullptr, *le = nullptr;
-  KI_FMM_CUDA(pool_malloc((void**)&q, sizeof(double2) * (size_t)n * nc_max, s));
-  KI_FMM_CUDA(pool_malloc((void**)&me, sizeof(double2) * (size_t)nbox * p * nc_max, s));
-  KI_FMM_CUDA(pool_malloc((void**)&le, sizeof(double2) * (size_t)nbox * p * nc_max, s));
+  V *q = nullptr, *me = nullptr, *le = nullptr;
+  KI_FMM_CUDA(pool_malloc((void**)&q, sizeof(V) * (size_t)n * kCols, s));
+  KI_FMM_CUDA(pool_malloc((void**)&me, sizeof(V) * (size_t)nbox * p * nc_max, s));
+  KI_FMM_CUDA(pool_malloc((void**)&le, sizeof(V) * (size_t)nbox * p * nc_max, s));
   for (int c0 = 0; c0 < ncols; c0 += kCols) {
     const int nc = std::min(kCols, ncols - c0);
-    k_charges<<<(int)std::min<size_t>(8192, ((size_t)n * nc + 255) / 256), 256, 0, s>>>(
-        F.d_nw, F.d_perm, n, mu, ldmu, c0, nc, q);
-    k_p2m<<<F.nleaf, 256, 0, s>>>(F.d_leaf_start, F.d_leaf_box, F.d_centre,
-                                  F.side0 / (double)(1L << L), F.d_z, q, n, nc, p, me);
+    // algorithmic flops (complex FMA = 8): P2M n p, M2M p(p+1)/2 per child
+    // link, M2L p^2 per interaction pair, L2L p(p+1)/2 per box below level 2,
+    // near field 4 nc + 12 per point pair, local expansion n p (4 nc + 6)
+    const double pp = p, cx = nc;
+    const int nl2 = F.lvl_off[L + 1] - F.lvl_off[3 > L ? L + 1 : 3];
+    if (rec) rec->begin(names[0], 8.0 * cx * ((double)n * pp + (double)(nbox - 1) * pp * (pp + 1) / 2));
+    k_charges<R><<<(n + 31) / 32, dim3(32, 8), 0, s>>>(F.d_nw, F.d_perm, n, mu, ldmu, c0, nc, q);
+    k_p2m<R><<<F.nleaf, 256, 0, s>>>(F.d_leaf_start, F.d_leaf_box, F.d_centre,
+                                     F.side0 / (double)(1L << L), F.d_z, q, n, nc, p, me);
     for (int l = L; l >= 1; l--) {
       const int b0 = F.lvl_off[l - 1], cnt = F.lvl_off[l] - b0;
-      k_m2m<<<cnt, 256, 0, s>>>(b0, F.d_child, F.d_child_pos, F.d_T, ldm, nc, p, me);
+      k_m2m<R><<<cnt, 256, 0, s>>>(b0, F.d_child, F.d_child_pos, T, ldm, nc, p, me);
     }
-    KI_FMM_CUDA(cudaMemsetAsync(le, 0, sizeof(double2) * (size_t)F.lvl_off[2] * p * nc, s));
+    if (rec) rec->end();
+    KI_FMM_CUDA(cudaMemsetAsync(le, 0, sizeof(V) * (size_t)F.lvl_off[2] * p * nc, s));
+    if (rec) rec->begin(names[1], 8.0 * cx * (double)F.m2l_pairs * pp * pp);
     for (int l = 2; l <= L; l++) {
       const int b0 = F.lvl_off[l], cnt = F.lvl_off[l + 1] - b0;
-      k_m2l<<<cnt, 256, 0, s>>>(b0, F.d_v_off, F.d_v_src, F.d_v_code, F.d_M, ldm,
-                                (double)(1L << l) / F.side0, nc, p, me, le);
+      k_m2l<R><<<cnt, 256, 0, s>>>(b0, F.d_v_off, F.d_v_src, F.d_v_code, M, ldm,
+                                   (double)(1L << l) / F.side0, nc, p, me, le);
     }
+    if (rec) rec->end();
+    if (rec) rec->begin(names[2], 8.0 * cx * (double)nl2 * pp * (pp + 1) / 2);
     for (int l = 3; l <= L; l++) {
       const int b0 = F.lvl_off[l], cnt = F.lvl_off[l + 1] - b0;
-      k_l2l<<<cnt, 256, 0, s>>>(b0, F.d_parent, F.d_child_pos, F.d_S, ldm, nc, p, le);
+      k_l2l<R><<<cnt, 256, 0, s>>>(b0, F.d_parent, F.d_child_pos, S, ldm, nc, p, le);
     }
-    k_l2p_p2p<<<F.nleaf, kP2PThreads, 0, s>>>(
+    if (rec) rec->end();
+    if (rec) rec->begin(names[3], (double)F.near_point_pairs * (4.0 * cx + 12.0) +
+                                  (double)n * pp * (4.0 * cx + 6.0));
+    k_leaf_eval<R><<<F.nleaf, kLeafThreads, 0, s>>>(
         F.d_leaf_start, F.d_leaf_box, F.d_near_off, F.d_near_leaf, F.d_centre,
-        F.side0 / (double)(1L << L), F.d_z, F.d_diag, F.d_perm, q, le, n, nc, p, mu, ldmu, c0, y,
-        ldy);
+        F.side0 / (double)(1L << L), F.d_z, F.d_zf, F.d_diag, F.d_perm, q, le, nc, p, mu, ldmu,
+        c0, y, ldy);
+    if (rec) rec->end();
     KI_FMM_CUDA(cudaGetLastError());
   }
   KI_FMM_CUDA(cudaFreeAsync(q, s));
   KI_FMM_CUDA(cudaFreeAsync(me, s));
   KI_FMM_CUDA(cudaFreeAsync(le, s));
+}
+
+}  // namespace
+
+void fmm2d_apply(Fmm2d& F, const double* mu, int ldmu, int ncols, double* y, int ldy,
+                 cudaStream_t s, int order, StageRecorder* rec, FmmArith arith) {
+  const int p = order > 0 ? std::min(order, F.p) : F.p;
+  if (arith == FmmArith::kF32) {
+    static const char* const names[4] = {"fmm32_upward", "fmm32_m2l", "fmm32_l2l", "fmm32_near"};
+    ensure_fp32(F, s);
+    apply_impl<float>(F, F.d_T32, F.d_S32, F.d_M32, mu, ldmu, ncols, y, ldy, s, p, rec, names);
+  } else {
+    static const char* const names[4] = {"fmm_upward", "fmm_m2l", "fmm_l2l", "fmm_near"};
+    apply_impl<double>(F, F.d_T, F.d_S, F.d_M, mu, ldmu, ncols, y, ldy, s, p, rec, names);
+  }
 }
 
 int fmm2d_order(const Fmm2d& f) { return f.p; }

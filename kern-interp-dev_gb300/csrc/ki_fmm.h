@@ -45,12 +45,31 @@ std::unique_ptr<Fmm2d, Fmm2dDeleter> fmm2d_build(const double* points, const dou
                                                  const double* weights, const double* curvatures,
                                                  int n, int p, cudaStream_t s);
 
+// Optional recorder of the apply's launch groups (CUDA events on the apply's
+// stream), with their algorithmic flops.
+struct StageRecorder {
+  virtual void begin(const char* name, double flops) = 0;
+  virtual void end() = 0;
+  virtual ~StageRecorder() = default;
+};
+
+// Arithmetic of the expansions and the near-field sums.  kF32: charges,
+// expansions, translations and near-field sums in FP32 (point differences
+// from hi/lo FP32 pairs, the diagonal term and the output in FP64), a
+// relative error near 1e-6 -- for applies whose result only needs that
+// accuracy (the residual updates of refinement, where the input is a small
+// correction).
+enum class FmmArith { kF64, kF32 };
+
 // y (n x ncols, column-major, ldy) = K mu (n x ncols, ldmu), device buffers,
 // on stream s, with `order` <= the plan's expansion terms (0: all of them);
 // the translation matrices of a lower order are leading blocks of the
-// plan's.
+// plan's.  Stages recorded: fmm_upward (charges, P2M, M2M), fmm_m2l, fmm_l2l,
+// fmm_near (local expansions at the targets and the direct near field);
+// with the prefix fmm32_ for kF32.
 void fmm2d_apply(Fmm2d& f, const double* mu, int ldmu, int ncols, double* y, int ldy,
-                 cudaStream_t s, int order = 0);
+                 cudaStream_t s, int order = 0, StageRecorder* rec = nullptr,
+                 FmmArith arith = FmmArith::kF64);
 
 // Expansion terms the plan was built with.
 int fmm2d_order(const Fmm2d& f);

@@ -3,6 +3,8 @@
 #include <algorithm>
 #include <cmath>
 #include <stdexcept>
+#include <thread>
+#include <vector>
 
 namespace ki {
 
@@ -28,28 +30,80 @@ inline int child_of(const double* p, const double* c, int dim) {
   return ci;
 }
 
+// fn(lo, hi) over [0, n) split into contiguous ranges on up to 16 threads
+// (one range, on the caller's thread, below 4096 items).
+template <typename Fn>
+void parallel_ranges(int n, Fn fn) {
+  const int hw = (int)std::thread::hardware_concurrency();
+  const int T = std::max(1, std::min(16, hw));
+  if (n < 4096 || T == 1) {
+    fn(0, n);
+    return;
+  }
+  const int chunk = (n + T - 1) / T;
+  std::vector<std::thread> th;
+  for (int t = 1; t < T; t++) {
+    const int lo = t * chunk, hi = std::min(n, lo + chunk);
+    if (lo < hi) th.emplace_back(fn, lo, hi);
+  }
+  fn(0, std::min(n, chunk));
+  for (auto& x : th) x.join();
+}
+
 }  // namespace
 
-void Tree::build(const double* pts, int n_points_, int dim_, int sol_dim_, int max_leaf_dofs_) {
-  dim = dim_;
-  n_points = n_points_;
-  sol_dim = sol_dim_;
-  n_dofs = n_points * sol_dim;
-  max_leaf_dofs = max_leaf_dofs_;
-  if (dim != 2 && dim != 3) throw std::invalid_argument("domain dimension must be 2 or 3");
+void tree_root(const double* pts, int n_points, int dim, double* centre, double* side) {
   if (n_points <= 0) throw std::invalid_argument("no boundary points");
-  if (max_leaf_dofs < 1) throw std::invalid_argument("max_leaf_dofs must be positive");
-  boxes.clear();
-  levels.clear();
-  const int nch = 1 << dim;
-
   double mn = pts[0], mx = pts[0];
   for (int i = 0; i < dim * n_points; i++) {
     if (!std::isfinite(pts[i])) throw std::invalid_argument("non-finite boundary coordinate");
     mn = std::min(mn, pts[i]);
     mx = std::max(mx, pts[i]);
   }
-  double tmin = mn - 0.01, tmax = mx + 0.01;
+  const double tmin = mn - 0.01, tmax = mx + 0.01;
+  *centre = (tmin + tmax) / 2.0;
+  *side = tmax - tmin;
+}
+
+namespace {
+
+void check_args(int dim, int n_points, int max_leaf_dofs) {
+  if (dim != 2 && dim != 3) throw std::invalid_argument("domain dimension must be 2 or 3");
+  if (n_points <= 0) throw std::invalid_argument("no boundary points");
+  if (max_leaf_dofs < 1) throw std::invalid_argument("max_leaf_dofs must be positive");
+}
+
+// Child ci of box b (centre exactly as QuadTree::node_subdivide,
+// quadtree.cpp:377-388), appended to the box list.
+int add_child(std::vector<Box>* boxes, int b, int ci, int level, int dim, int count) {
+  const Box& par = (*boxes)[b];
+  Box ch;
+  ch.level = level;
+  ch.parent = b;
+  for (int d = 0; d < dim; d++)
+    ch.c[d] = par.c[d] + ((ci >> (dim - 1 - d)) & 1 ? par.side / 4. : -par.side / 4.);
+  ch.side = par.side / 2.0;
+  ch.orig_count = count;
+  const int id = (int)boxes->size();
+  boxes->push_back(ch);
+  (*boxes)[b].child[ci] = id;
+  return id;
+}
+
+}  // namespace
+
+void Tree::build(const double* pts, int n_points_, int dim_, int sol_dim_, int max_leaf_dofs_) {
+  check_args(dim_, n_points_, max_leaf_dofs_);
+  dim = dim_;
+  n_points = n_points_;
+  sol_dim = sol_dim_;
+  n_dofs = n_points * sol_dim;
+  max_leaf_dofs = max_leaf_dofs_;
+  boxes.clear();
+  levels.clear();
+  const int nch = 1 << dim;
+  double c0, side0;
+  tree_root(pts, n_points, dim, &c0, &side0);
 
   // Top-down construction.  Each box owns a range [lo, hi) of `work`, a
   // permutation of point indices kept ascending within every box (stable
@@ -57,13 +111,12 @@ void Tree::build(const double* pts, int n_points_, int dim_, int sol_dim_, int m
   // original_box.
   std::vector<int> work(n_points), tmp(n_points);
   for (int i = 0; i < n_points; i++) work[i] = i;
-  struct Range { int lo, hi; };
-  std::vector<Range> range;
+  std::vector<std::pair<int, int>> range;
 
   Box root;
   root.level = 0;
-  for (int d = 0; d < dim; d++) root.c[d] = (tmin + tmax) / 2.0;
-  root.side = tmax - tmin;
+  for (int d = 0; d < dim; d++) root.c[d] = c0;
+  root.side = side0;
   root.orig_count = n_dofs;
   boxes.push_back(root);
   range.push_back({0, n_points});
@@ -74,40 +127,99 @@ void Tree::build(const double* pts, int n_points_, int dim_, int sol_dim_, int m
     for (int b : levels[l]) {
       if (boxes[b].orig_count <= max_leaf_dofs) continue;
       boxes[b].leaf = false;
-      Range r = range[b];
+      const int lo = range[b].first, hi = range[b].second;
       double c[3] = {boxes[b].c[0], boxes[b].c[1], boxes[b].c[2]};
-      double side = boxes[b].side;
       int cnt[kMaxChildren] = {};
-      for (int i = r.lo; i < r.hi; i++) cnt[child_of(pts + (size_t)dim * work[i], c, dim)]++;
+      for (int i = lo; i < hi; i++) cnt[child_of(pts + (size_t)dim * work[i], c, dim)]++;
       int start[kMaxChildren];
-      start[0] = r.lo;
+      start[0] = lo;
       for (int ci = 1; ci < nch; ci++) start[ci] = start[ci - 1] + cnt[ci - 1];
       int pos[kMaxChildren];
       for (int ci = 0; ci < nch; ci++) pos[ci] = start[ci];
-      for (int i = r.lo; i < r.hi; i++) {
+      for (int i = lo; i < hi; i++) {
         int p = work[i];
         tmp[pos[child_of(pts + (size_t)dim * p, c, dim)]++] = p;
       }
-      std::copy(tmp.begin() + r.lo, tmp.begin() + r.hi, work.begin() + r.lo);
+      std::copy(tmp.begin() + lo, tmp.begin() + hi, work.begin() + lo);
       for (int ci = 0; ci < nch; ci++) {
-        Box ch;
-        ch.level = (int)l + 1;
-        ch.parent = b;
-        // child centre exactly as QuadTree::node_subdivide (quadtree.cpp:377-388)
-        for (int d = 0; d < dim; d++)
-          ch.c[d] = c[d] + ((ci >> (dim - 1 - d)) & 1 ? side / 4. : -side / 4.);
-        ch.side = side / 2.0;
-        ch.orig_count = cnt[ci] * sol_dim;
-        int id = (int)boxes.size();
-        boxes.push_back(ch);
+        const int id = add_child(&boxes, b, ci, (int)l + 1, dim, cnt[ci] * sol_dim);
         range.push_back({start[ci], start[ci] + cnt[ci]});
-        boxes[b].child[ci] = id;
         next.push_back(id);
       }
     }
     if (!next.empty()) levels.push_back(next);
   }
+  finish(work, range);
+}
 
+bool Tree::build_from_codes(const double* pts, int n_points_, int dim_, int sol_dim_,
+                            int max_leaf_dofs_, const uint64_t* codes, const int* order,
+                            int depth) {
+  check_args(dim_, n_points_, max_leaf_dofs_);
+  dim = dim_;
+  n_points = n_points_;
+  sol_dim = sol_dim_;
+  n_dofs = n_points * sol_dim;
+  max_leaf_dofs = max_leaf_dofs_;
+  boxes.clear();
+  levels.clear();
+  const int nch = 1 << dim;
+  double c0, side0;
+  tree_root(pts, n_points, dim, &c0, &side0);
+  std::vector<std::pair<int, int>> range;
+  boxes.reserve((size_t)2 * nch * (n_points / max_leaf_dofs + 1) + 1);
+  range.reserve(boxes.capacity());
+  Box root;
+  root.level = 0;
+  for (int d = 0; d < dim; d++) root.c[d] = c0;
+  root.side = side0;
+  root.orig_count = n_dofs;
+  boxes.push_back(root);
+  range.push_back({0, n_points});
+  levels.push_back({0});
+  for (size_t l = 0; l < levels.size(); l++) {
+    std::vector<int> next;
+    for (int b : levels[l]) {
+      if (boxes[b].orig_count <= max_leaf_dofs) continue;
+      if ((int)l >= depth) {   // the codes end here: the caller builds by partition
+        boxes.clear();
+        levels.clear();
+        return false;
+      }
+      boxes[b].leaf = false;
+      const int lo = range[b].first, hi = range[b].second;
+      // the range shares the codes' first l digits; digit l + 1 ascends
+      const int shift = dim * (depth - 1 - (int)l);
+      int start[kMaxChildren + 1];
+      start[0] = lo;
+      start[nch] = hi;
+      for (int ci = 1; ci < nch; ci++)
+        start[ci] = (int)(std::partition_point(codes + start[ci - 1], codes + hi,
+                                               [&](uint64_t k) {
+                                                 return (int)((k >> shift) & (nch - 1)) < ci;
+                                               }) -
+                          codes);
+      for (int ci = 0; ci < nch; ci++) {
+        const int id = add_child(&boxes, b, ci, (int)l + 1, dim,
+                                 (start[ci + 1] - start[ci]) * sol_dim);
+        range.push_back({start[ci], start[ci + 1]});
+        next.push_back(id);
+      }
+    }
+    if (!next.empty()) levels.push_back(next);
+  }
+  // a leaf's points ascending by index (the codes ordered them by deeper digits)
+  std::vector<int> work(order, order + n_points);
+  parallel_ranges((int)boxes.size(), [&](int b0, int b1) {
+    for (int b = b0; b < b1; b++)
+      if (boxes[b].leaf) std::sort(work.begin() + range[b].first, work.begin() + range[b].second);
+  });
+  finish(work, range);
+  return true;
+}
+
+void Tree::finish(const std::vector<int>& work, const std::vector<std::pair<int, int>>& range) {
+  const int nch = 1 << dim;
   // Leaf DOF ranges in depth-first order.
   dof_sorted.clear();
   dof_sorted.reserve(n_dofs);
@@ -118,7 +230,7 @@ void Tree::build(const double* pts, int n_points_, int dim_, int sol_dim_, int m
     Box& bx = boxes[b];
     if (bx.leaf) {
       bx.orig_start = (int)dof_sorted.size();
-      for (int i = range[b].lo; i < range[b].hi; i++)
+      for (int i = range[b].first; i < range[b].second; i++)
         for (int s = 0; s < sol_dim; s++) dof_sorted.push_back(work[i] * sol_dim + s);
     } else {
       for (int ci = nch - 1; ci >= 0; ci--) stack.push_back(bx.child[ci]);
@@ -137,7 +249,10 @@ void Tree::build(const double* pts, int n_points_, int dim_, int sol_dim_, int m
   // leaves.
   const double sq = std::sqrt((double)dim);
   for (size_t l = 1; l < levels.size(); l++) {
-    for (int b : levels[l]) {
+    const std::vector<int>& lv = levels[l];
+    parallel_ranges((int)lv.size(), [&](int i0, int i1) {
+    for (int i = i0; i < i1; i++) {
+      const int b = lv[i];
       Box& bx = boxes[b];
       const Box& par = boxes[bx.parent];
       for (int ci = 0; ci < nch; ci++)
@@ -158,6 +273,7 @@ void Tree::build(const double* pts, int n_points_, int dim_, int sol_dim_, int m
       for (int pn : par.coarse_nbrs)
         if (touching(bx, boxes[pn], dim)) bx.coarse_nbrs.push_back(pn);
     }
+    });
   }
 }
 

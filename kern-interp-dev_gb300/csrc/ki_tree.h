@@ -17,6 +17,7 @@
 #pragma once
 
 #include <cstdint>
+#include <utility>
 #include <vector>
 
 namespace ki {
@@ -47,7 +48,26 @@ struct Tree {
   int n_children() const { return 1 << dim; }
   // points: interleaved (x, y[, z]), n_points of them; dim 2 or 3.
   void build(const double* points, int n_points, int dim, int sol_dim, int max_leaf_dofs);
+  // The same tree from the points' descent codes: code = the child indices
+  // of the boxes containing the point at levels 1..depth, dim bits each,
+  // level 1 most significant (computed with tree_root's box and the split
+  // rule's centre arithmetic), sorted ascending with ties by point index,
+  // `order` the point indices in that order.  Returns false (tree left
+  // empty) when a box at level `depth` would still be split.
+  bool build_from_codes(const double* points, int n_points, int dim, int sol_dim,
+                        int max_leaf_dofs, const uint64_t* codes, const int* order, int depth);
   int num_levels() const { return (int)levels.size(); }
+
+ private:
+  void finish(const std::vector<int>& work, const std::vector<std::pair<int, int>>& range);
 };
+
+// Root box of the points: centre (all coordinates equal) and side, the
+// bounding interval of every coordinate widened by 0.01 on both ends.
+// Throws std::invalid_argument on a non-finite coordinate or no points.
+void tree_root(const double* points, int n_points, int dim, double* centre, double* side);
+
+// Deepest descent code the 64-bit codes hold: 30 levels in 2D, 21 in 3D.
+inline int tree_code_depth(int dim) { return dim == 2 ? 30 : 21; }
 
 }  // namespace ki
