@@ -206,6 +206,75 @@ __device__ int cta_lu(int n, T* A, int lda, int* piv, int* s_flag, T* s_red, int
   return info;
 }
 
+// In-place inverse by Gauss-Jordan elimination with partial pivoting: at
+// step j the row of the largest |A(i, j)|, i >= j, is swapped into row j
+// (piv[j], device memory), row j is scaled by 1/pivot with A(j, j) taken as
+// 1, and column j is eliminated from every other row, A(i, j) becoming
+// -A(i, j)/pivot; the interchanges are finally undone on the columns in
+// reverse order.  colj: n entries of scratch (shared memory); s_val: 2.
+// Returns the first zero pivot + 1, or 0.
+template <typename T>
+__device__ int cta_gj_inverse(int n, T* A, int lda, int* piv, T* colj, T* s_val, int* s_idx) {
+  int info = 0;
+  for (int j = 0; j < n; j++) {
+    if (threadIdx.x < 32) {
+      T best = T(-1);
+      int bi = j;
+      for (int i = j + threadIdx.x; i < n; i += 32) {
+        T v = fabs(A[i + (size_t)lda * j]);
+        if (v > best) { best = v; bi = i; }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        T ov = __shfl_down_sync(0xffffffff, best, o);
+        int oi = __shfl_down_sync(0xffffffff, bi, o);
+        if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+      }
+      if (threadIdx.x == 0) {
+        *s_idx = bi;
+        s_val[0] = A[bi + (size_t)lda * j];
+        s_val[1] = A[j + (size_t)lda * j];
+        piv[j] = bi;
+      }
+    }
+    __syncthreads();
+    const int p = *s_idx;
+    const T pv = s_val[0], ajj = s_val[1];
+    if (pv == T(0)) {   // the same branch in every thread
+      if (info == 0) info = j + 1;
+      continue;
+    }
+    // column j after the interchange (rows other than j and p are not written here)
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+      colj[i] = (i == j) ? pv : (i == p ? ajj : A[i + (size_t)lda * j]);
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+      T a = A[j + (size_t)lda * c], b = A[p + (size_t)lda * c];
+      if (c == j) { a = ajj; b = pv; }
+      A[j + (size_t)lda * c] = (c == j ? T(1) : b) / pv;
+      if (p != j) A[p + (size_t)lda * c] = a;
+    }
+    __syncthreads();
+    const int m = n - 1;
+    for (int e = threadIdx.x; e < m * n; e += blockDim.x) {
+      const int ii = e % m, c = e / m;
+      const int i = ii < j ? ii : ii + 1;
+      if (c == j) A[i + (size_t)lda * j] = -colj[i] * A[j + (size_t)lda * j];
+      else A[i + (size_t)lda * c] -= colj[i] * A[j + (size_t)lda * c];
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    for (int j = n - 1; j >= 0; j--) {
+      const int q = piv[j];
+      if (q != j) {
+        T t = A[i + (size_t)lda * j];
+        A[i + (size_t)lda * j] = A[i + (size_t)lda * q];
+        A[i + (size_t)lda * q] = t;
+      }
+    }
+  __syncthreads();
+  return info;
+}
+
 // B(n x nrhs) <- A^-1 B (trans=false) or A^-T B (trans=true) from cta_lu.
 template <typename T>
 __device__ void cta_lu_solve(int n, const T* LU, int lda, const int* piv, bool trans, T* B,

@@ -210,6 +210,7 @@ struct SchurTask {
   int* piv;           // r
   T* Atil;            // k x k accumulated self-block
   T* ws;              // scratch: P (n*n) | Wrs (r*k) | Wsr (k*r) | Lt (r*k)
+  T* Xi;              // r x r explicit inverse of X (FP32 forms), or null
 };
 
 // ---------------------------------------------------------------- kernels --
@@ -1170,56 +1171,98 @@ __global__ void k_assemble(const AsmTask<T>* tasks, const int* ipool, Points<T> 
 
 // Schur-complement elimination of a compressed box
 // (SkelFactorization::decouple, skel_factorization.cpp:91-127).  Working set
-// P (n x n, permuted K_BN) | Wrs (r x k) | Lt (r x k) | X (r x r) in shared
-// memory when it fits (smem != 0), else in the global scratch t.ws.
+// K_ss (k x k) | Wrs (r x k) | Lt (r x k) | X (r x r) | r scratch entries in
+// shared memory when it fits (smem != 0), else in the global scratch t.ws
+// (X in place in the output).  The blocks are gathered from the box's self
+// block through the skeleton-first permutation; K_sr is held only
+// transposed (Lt), and K_rr only as X.  With t.Xi (FP32 forms, shared-
+// memory boxes) X is inverted in place by Gauss-Jordan elimination and L, U
+// are products with the inverse; otherwise X is LU-factored (the
+// reference's dgetrf / dgetrs) and L, U come from triangular solves.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_schur(const SchurTask<T>* tasks, int task_base,
                                                      int smem, int* err) {
   extern __shared__ __align__(16) unsigned char sc_smem[];
   const SchurTask<T> t = tasks[task_base + blockIdx.x];
   const int n = t.n, k = t.k, r = n - k;
-  __shared__ T s_red;
+  __shared__ T s_red, s_val[2];
   __shared__ int s_idx, s_flag;
   T* base = smem ? reinterpret_cast<T*>(sc_smem) : t.ws;
-  T* Pm = base;                       // n x n
-  T* Wrs = Pm + (size_t)n * n;        // r x k : K~_rs
-  T* Lt = Wrs + (size_t)r * k;        // r x k : K~_sr^T, then L^T
-  T* X = smem ? Lt + (size_t)r * k : t.X;   // r x r (global mode: in place in the output)
-  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
-    int i = idx % n, j = idx / n;
-    Pm[idx] = t.K[t.perm[i] + (size_t)n * t.perm[j]];
+  T* Kss = base;                      // k x k
+  T* Wrs = Kss + (size_t)k * k;       // r x k : K_rs, then K~_rs, then U
+  T* Lt = Wrs + (size_t)r * k;        // r x k : K_sr^T, then K~_sr^T, then L^T
+  T* X = smem ? Lt + (size_t)r * k : t.X;   // r x r
+  const int* pm = t.perm;
+  for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) {
+    const int i = idx % k, j = idx / k;
+    Kss[idx] = t.K[pm[i] + (size_t)n * pm[j]];
+  }
+  for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
+    const int i = idx % r, j = idx / r;
+    Wrs[idx] = t.K[pm[k + i] + (size_t)n * pm[j]];   // K_rs(i, j)
+    Lt[idx] = t.K[pm[j] + (size_t)n * pm[k + i]];    // K_sr(j, i)
+  }
+  for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) {
+    const int i = idx % r, j = idx / r;
+    X[idx] = t.K[pm[k + i] + (size_t)n * pm[k + j]];
   }
   for (int idx = threadIdx.x; idx < k * r; idx += blockDim.x) t.Tout[idx] = t.Tin[idx];
   __syncthreads();
-  const T* Kss = Pm;
-  const T* Ksr = Pm + (size_t)n * k;
-  const T* Krs = Pm + k;
-  const T* Krr = Pm + k + (size_t)n * k;
   const T* Tm = t.Tin;
-  for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
-    int i = idx % r, j = idx / r;
-    Wrs[idx] = Krs[i + (size_t)n * j];        // K_rs
-    Lt[idx] = Ksr[j + (size_t)n * i];         // K_sr^T
-  }
-  for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) {
-    int i = idx % r, j = idx / r;
-    X[idx] = Krr[i + (size_t)n * j];
-  }
+  // X -= T^T K_sr  (K_sr(l, j) = Lt[j + r l])
+  cta_gemm<T>(r, r, k, T(-1), Tm, k, true, Lt, r, true, T(1), X, r);
   __syncthreads();
-  // K~_rs = K_rs - T^T K_ss ;  K~_sr^T = K_sr^T - T^T K_ss^T ;  X -= T^T K_sr
-  cta_gemm<T>(r, k, k, T(-1), Tm, k, true, Kss, n, false, T(1), Wrs, r);
-  cta_gemm<T>(r, k, k, T(-1), Tm, k, true, Kss, n, true, T(1), Lt, r);
-  cta_gemm<T>(r, r, k, T(-1), Tm, k, true, Ksr, n, false, T(1), X, r);
+  // K~_rs = K_rs - T^T K_ss ;  K~_sr^T = K_sr^T - T^T K_ss^T
+  cta_gemm<T>(r, k, k, T(-1), Tm, k, true, Kss, k, false, T(1), Wrs, r);
+  cta_gemm<T>(r, k, k, T(-1), Tm, k, true, Kss, k, true, T(1), Lt, r);
   __syncthreads();
   // X -= K~_rs T
   cta_gemm<T>(r, r, k, T(-1), Wrs, r, false, Tm, k, false, T(1), X, r);
   __syncthreads();
+  if (smem && t.Xi) {
+    // X (kept in t.X for the refinement step) -> X^-1 in place
+    for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) t.X[idx] = X[idx];
+    __syncthreads();
+    int info = cta_gj_inverse<T>(r, X, r, t.piv, X + (size_t)r * r, s_val, &s_idx);
+    if (info != 0 && threadIdx.x == 0) atomicMax(err, (int)kDevSingular);
+    // U0 = X^-1 K~_rs (r x k), L0 = K~_sr X^-1 (k x r)
+    cta_gemm<T>(r, k, r, T(1), X, r, false, Wrs, r, false, T(0), t.U, r);
+    cta_gemm<T>(k, r, r, T(1), Lt, r, true, X, r, false, T(0), t.L, k);
+    __syncthreads();
+    // one step of refinement in the same precision (products with an explicit
+    // inverse are not backward stable; the corrected ones are):
+    // RU = K~_rs - X U0, RL = K~_sr - L0 X, then U = U0 + X^-1 RU, L = L0 + RL X^-1
+    T* RU = t.ws;
+    T* RL = t.ws + (size_t)r * k;
+    const T* X0 = t.X;
+    for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
+      const int i = idx % r, j = idx / r;
+      T acc = T(0);
+      for (int l = 0; l < r; l++) acc += X0[i + (size_t)r * l] * t.U[l + (size_t)r * j];
+      RU[idx] = Wrs[idx] - acc;
+    }
+    for (int idx = threadIdx.x; idx < k * r; idx += blockDim.x) {
+      const int i = idx % k, j = idx / k;
+      T acc = T(0);
+      for (int l = 0; l < r; l++) acc += t.L[i + (size_t)k * l] * X0[l + (size_t)r * j];
+      RL[idx] = Lt[j + (size_t)r * i] - acc;
+    }
+    __syncthreads();
+    cta_gemm<T>(r, k, r, T(1), X, r, false, RU, r, false, T(1), t.U, r);
+    cta_gemm<T>(k, r, r, T(1), RL, k, false, X, r, false, T(1), t.L, k);
+    // A~ = K_ss - L K~_rs
+    for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) t.Atil[idx] = Kss[idx];
+    for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) t.Xi[idx] = X[idx];
+    __syncthreads();
+    cta_gemm<T>(k, k, r, T(-1), t.L, k, false, Wrs, r, false, T(1), t.Atil, k);
+    return;
+  }
   int info = cta_lu<T>(r, X, r, t.piv, &s_flag, &s_red, &s_idx);
   if (info != 0 && threadIdx.x == 0) atomicMax(err, (int)kDevSingular);
   // L^T = X^-T K~_sr^T
   cta_lu_solve_par<T>(r, X, r, t.piv, true, Lt, r, k);
   // A~ = K_ss - L K~_rs  (k x k), L = Lt^T
-  for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) t.Atil[idx] = Kss[idx % k + (size_t)n * (idx / k)];
+  for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) t.Atil[idx] = Kss[idx];
   __syncthreads();
   cta_gemm<T>(k, k, r, T(-1), Lt, r, true, Wrs, r, false, T(1), t.Atil, k);
   __syncthreads();
@@ -1335,7 +1378,7 @@ void copy_block(cudaStream_t s, const T* src, int lds, int rows, int cols, bool 
 template <typename T>
 size_t schur_bytes(int n, int k) {
   size_t r = n - k;
-  return sizeof(T) * ((size_t)n * n + 2 * r * k + r * r);
+  return sizeof(T) * ((size_t)k * k + 2 * r * k + r * r + r);
 }
 
 // SkelFactorization::decouple for a box whose working set does not fit in one
@@ -2662,6 +2705,25 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       F->n_redundant += r;
       LF.max_n = std::max(LF.max_n, n);
     }
+    if (sizeof(T) < sizeof(double)) {
+      // FP32: explicit inverses of the redundant blocks for the sweeps (the
+      // FP64 form keeps the reference's LU substitution)
+      int64_t xi_tot = 0;
+      for (auto& w : sw) {
+        const int64_t r = w.n - w.k;
+        if (r <= kInvMax) xi_tot += r * r;
+      }
+      T* d_xi = (T*)F->alloc(Tsz * (xi_tot + 1));
+      int64_t o = 0;
+      for (size_t q = 0; q < sw.size(); q++) {
+        const int64_t r = sw[q].n - sw[q].k;
+        if (r <= kInvMax) {
+          sw[q].Xi = d_xi + o;
+          st[q].Xi = d_xi + o;
+          o += r * r;
+        }
+      }
+    }
     SchurTask<T>* d_st = (SchurTask<T>*)F->alloc(sizeof(SchurTask<T>) * st.size());
     double sf = 0, sb = 0;
     for (auto& q : st) {
@@ -2669,13 +2731,16 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       sf += 2 * r * k * k + 4 * r * r * k + 2 * k * k * r + 2.0 / 3.0 * r * r * r + 4 * r * r * k + 2 * k * k * r;
       sb += sizeof(T) * (n * n + 3 * k * r + r * r + k * k);
     }
+    // shared-memory working sets up to this size (environment override
+    // KI_SCHUR_SMEM_CAP, used by the tests)
+    size_t schur_cap = 225 * 1024;
+    if (const char* e = std::getenv("KI_SCHUR_SMEM_CAP")) schur_cap = (size_t)std::atol(e);
     std::string sc_name = "schur@L" + std::to_string(l);
     F->stage_begin(sc_name.c_str(), sf, sb);
     {
       // shared-memory boxes first, then the ones whose working set is global
       // (environment override KI_SCHUR_SMEM_CAP, used by the tests)
-      size_t cap = 225 * 1024;
-      if (const char* e = std::getenv("KI_SCHUR_SMEM_CAP")) cap = (size_t)std::atol(e);
+      const size_t cap = schur_cap;
       std::vector<SchurTask<T>> st2;
       size_t sm = 0;
       int n_sm = 0;
@@ -2691,46 +2756,57 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         if (schur_bytes<T>(q.n, q.k) > cap && q.n <= wide_n) { st2.push_back(q); n_glob++; }
       for (auto& q : st)
         if (schur_bytes<T>(q.n, q.k) > cap && q.n > wide_n) st2.push_back(q);
+      // shared-memory boxes ascending by footprint, launched in bins of equal
+      // CTAs per SM (each bin sized by its largest box) on the aux streams
+      std::stable_sort(st2.begin(), st2.begin() + n_sm, [](const SchurTask<T>& a, const SchurTask<T>& b) {
+        return schur_bytes<T>(a.n, a.k) < schur_bytes<T>(b.n, b.k);
+      });
+      (void)sm;
       upload(d_st, st2, s);
-      if (n_sm > 0) {
+      F->fork();
+      int next = 0;
+      if (n_sm > 0)
         KI_CUDA(cudaFuncSetAttribute(k_schur<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
-        k_schur<T><<<(unsigned)n_sm, kThreads, sm, s>>>(d_st, 0, 1, F->d_err);
+      auto per_sm = [](size_t bytes) { return std::max(1, (int)(228 * 1024 / (bytes + 1024))); };
+      for (int b0 = 0; b0 < n_sm;) {
+        const int ps = per_sm(schur_bytes<T>(st2[b0].n, st2[b0].k));
+        int b1 = b0 + 1;
+        while (b1 < n_sm && per_sm(schur_bytes<T>(st2[b1].n, st2[b1].k)) == ps) b1++;
+        const size_t bsm = schur_bytes<T>(st2[b1 - 1].n, st2[b1 - 1].k);
+        k_schur<T><<<(unsigned)(b1 - b0), kThreads, bsm, F->aux[(next++) % Factorization<T>::kAux]>>>(
+            d_st, b0, 1, F->d_err);
+        b0 = b1;
       }
       if (n_glob > 0)
-        k_schur<T><<<(unsigned)n_glob, kThreads, 0, s>>>(d_st, n_sm, 0, F->d_err);
-      if ((int)st2.size() > n_sm + n_glob) {
-        F->fork();
-        for (size_t q = n_sm + n_glob; q < st2.size(); q++)
-          schur_wide<T>(st2[q], F->d_err, F->aux[(q - n_sm - n_glob) % Factorization<T>::kAux]);
-        F->join(Factorization<T>::kAux);
-      }
+        k_schur<T><<<(unsigned)n_glob, kThreads, 0, F->aux[(next++) % Factorization<T>::kAux]>>>(
+            d_st, n_sm, 0, F->d_err);
+      for (size_t q = n_sm + n_glob; q < st2.size(); q++)
+        schur_wide<T>(st2[q], F->d_err, F->aux[(next++) % Factorization<T>::kAux]);
+      F->join(Factorization<T>::kAux);
     }
     F->stage_end();
     KI_CUDA(cudaGetLastError());
-    if (sizeof(T) < sizeof(double)) {
-      // FP32: explicit inverses of the redundant blocks for the sweeps (the
-      // FP64 form keeps the reference's LU substitution)
-      int64_t xi_tot = 0;
-      for (auto& w : sw) {
-        const int64_t r = w.n - w.k;
-        if (r <= kInvMax) xi_tot += r * r;
-      }
-      T* d_xi = (T*)F->alloc(Tsz * (xi_tot + 1));
-      int64_t o = 0;
-      for (auto& w : sw) {
-        const int64_t r = w.n - w.k;
-        if (r <= kInvMax) {
-          w.Xi = d_xi + o;
-          o += r * r;
-        }
-      }
-    }
     SweepTask<T>* d_sw = (SweepTask<T>*)F->alloc(sizeof(SweepTask<T>) * sw.size());
     upload(d_sw, sw, s);
     LF.d_tasks = d_sw;
     if (sizeof(T) < sizeof(double)) {
-      k_lu_inverse<T><<<(unsigned)sw.size(), kThreads, 0, s>>>(d_sw);
-      KI_CUDA(cudaGetLastError());
+      // inverses of the boxes k_schur factored by LU (global working set)
+      std::vector<SweepTask<T>> inv;
+      double xf = 0;
+      for (auto& w : sw)
+        if (w.Xi && schur_bytes<T>(w.n, w.k) > schur_cap) {
+          inv.push_back(w);
+          xf += 2.0 * std::pow((double)(w.n - w.k), 3);
+        }
+      if (!inv.empty()) {
+        SweepTask<T>* d_inv = (SweepTask<T>*)F->alloc(sizeof(SweepTask<T>) * inv.size());
+        upload(d_inv, inv, s);
+        std::string xi_name = "xinv@L" + std::to_string(l);
+        F->stage_begin(xi_name.c_str(), xf, 0);
+        k_lu_inverse<T><<<(unsigned)inv.size(), kThreads, 0, s>>>(d_inv);
+        F->stage_end();
+        KI_CUDA(cudaGetLastError());
+      }
     }
     for (int i : ci_list) F->rank_hist.push_back(kh[i]);
   }

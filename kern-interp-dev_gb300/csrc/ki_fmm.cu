@@ -11,6 +11,7 @@
 // load.
 #include "ki_pool.h"
 #include "ki_fmm.h"
+#include "ki_parallel.h"
 
 #include <algorithm>
 #include <cmath>
@@ -19,7 +20,6 @@
 #include <numeric>
 #include <stdexcept>
 #include <string>
-#include <unordered_map>
 #include <vector>
 
 namespace ki {
@@ -462,22 +462,104 @@ __global__ void k_split_points(const double2* z, int n, float4* out) {
   }
 }
 
-uint64_t morton(uint32_t ix, uint32_t iy) {
-  uint64_t k = 0;
-  for (int b = 0; b < 32; b++) {
-    k |= (uint64_t)((ix >> b) & 1u) << (2 * b + 1);
-    k |= (uint64_t)((iy >> b) & 1u) << (2 * b);
-  }
-  return k;
+// Morton key of a cell: bit b of ix at position 2b + 1, of iy at 2b.
+inline uint64_t spread2(uint32_t v) {
+  uint64_t x = v;
+  x = (x | (x << 16)) & 0x0000FFFF0000FFFFull;
+  x = (x | (x << 8)) & 0x00FF00FF00FF00FFull;
+  x = (x | (x << 4)) & 0x0F0F0F0F0F0F0F0Full;
+  x = (x | (x << 2)) & 0x3333333333333333ull;
+  x = (x | (x << 1)) & 0x5555555555555555ull;
+  return x;
+}
+inline uint32_t compact2(uint64_t x) {
+  x &= 0x5555555555555555ull;
+  x = (x | (x >> 1)) & 0x3333333333333333ull;
+  x = (x | (x >> 2)) & 0x0F0F0F0F0F0F0F0Full;
+  x = (x | (x >> 4)) & 0x00FF00FF00FF00FFull;
+  x = (x | (x >> 8)) & 0x0000FFFF0000FFFFull;
+  x = (x | (x >> 16)) & 0x00000000FFFFFFFFull;
+  return (uint32_t)x;
+}
+inline uint64_t morton(uint32_t ix, uint32_t iy) { return (spread2(ix) << 1) | spread2(iy); }
+inline void demorton(uint64_t k, uint32_t* ix, uint32_t* iy) {
+  *ix = compact2(k >> 1);
+  *iy = compact2(k);
 }
 
-void demorton(uint64_t k, uint32_t* ix, uint32_t* iy) {
-  *ix = *iy = 0;
-  for (int b = 0; b < 32; b++) {
-    *ix |= (uint32_t)((k >> (2 * b + 1)) & 1u) << b;
-    *iy |= (uint32_t)((k >> (2 * b)) & 1u) << b;
+// Stable least-significant-digit radix sort of (key, index) pairs by the
+// low `bits` bits of the keys (11-bit digits).  Each pass: per-part digit
+// histograms, offsets digit-major then part-major, and each part scattering
+// its keys in order -- stable whatever the number of parts.
+void radix_sort_pairs(std::vector<uint64_t>* key, std::vector<int>* idx, int bits) {
+  constexpr int D = 11, B = 1 << D;
+  const int n = (int)key->size();
+  std::vector<uint64_t> k2(n);
+  std::vector<int> i2(n);
+  const int parts = parallel_part_count(n, 1 << 16);
+  std::vector<std::vector<size_t>> cnt(parts, std::vector<size_t>(B));
+  for (int sh = 0; sh < bits; sh += D) {
+    const uint64_t* k = key->data();
+    const int* v = idx->data();
+    parallel_parts(n, [&](int t, int lo, int hi) {
+      std::fill(cnt[t].begin(), cnt[t].end(), 0);
+      for (int i = lo; i < hi; i++) cnt[t][(k[i] >> sh) & (B - 1)]++;
+    }, 1 << 16);
+    size_t run = 0;
+    for (int d = 0; d < B; d++)
+      for (int t = 0; t < parts; t++) {
+        const size_t c = cnt[t][d];
+        cnt[t][d] = run;
+        run += c;
+      }
+    parallel_parts(n, [&](int t, int lo, int hi) {
+      size_t* off = cnt[t].data();
+      for (int i = lo; i < hi; i++) {
+        const size_t o = off[(k[i] >> sh) & (B - 1)]++;
+        k2[o] = k[i];
+        i2[o] = v[i];
+      }
+    }, 1 << 16);
+    key->swap(k2);
+    idx->swap(i2);
   }
 }
+
+// Box key -> global box index for one level: open addressing, linear
+// probing, power-of-two table (keys are below 2^40, so ~0 marks a free slot).
+struct KeyIndex {
+  std::vector<uint64_t> keys;
+  std::vector<int> vals;
+  uint64_t mask = 0;
+  int shift = 64;
+  void build(const std::vector<uint64_t>& ks, int base) {
+    size_t cap = 16;
+    int lg = 4;
+    while (cap < 2 * ks.size()) {
+      cap <<= 1;
+      lg++;
+    }
+    keys.assign(cap, ~0ull);
+    vals.assign(cap, -1);
+    mask = cap - 1;
+    shift = 64 - lg;
+    for (size_t i = 0; i < ks.size(); i++) {
+      size_t h = slot(ks[i]);
+      while (keys[h] != ~0ull) h = (h + 1) & mask;
+      keys[h] = ks[i];
+      vals[h] = base + (int)i;
+    }
+  }
+  size_t slot(uint64_t k) const { return (size_t)((k * 0x9E3779B97F4A7C15ull) >> shift); }
+  int find(uint64_t k) const {
+    size_t h = slot(k);
+    for (;;) {
+      if (keys[h] == k) return vals[h];
+      if (keys[h] == ~0ull) return -1;
+      h = (h + 1) & mask;
+    }
+  }
+};
 
 double binom(int n, int k) {
   double r = 1;
@@ -554,34 +636,39 @@ std::unique_ptr<Fmm2dPlan, Fmm2dPlanDeleter> fmm2d_plan(const double* pts, const
     long i = (long)std::floor((x - F->lo) / F->side0 * m);
     return (uint32_t)std::min(m - 1, std::max(0L, i));
   };
-  // Morton keys at the finest admissible level, one sort; a coarser level's
-  // key is a right shift, so the leaf level (refined while the non-empty
-  // leaves hold more than 40 points on average) is found by linear scans.
+  // Morton keys at the finest admissible level, one stable sort (ties by
+  // point index); a coarser level's key is a right shift.  The leaf level is
+  // the first from 2 at which the non-empty leaves hold 40 points or fewer
+  // on average: consecutive sorted keys first differ at level
+  // kLmax - floor(msb(a ^ b) / 2), so one pass counts the boxes of every level.
   constexpr int kLmax = 20;
-  std::vector<std::pair<uint64_t, int>> kp(n);
-  for (int i = 0; i < n; i++)
-    kp[i] = {morton(cell(pts[2 * i], kLmax), cell(pts[2 * i + 1], kLmax)), i};
-  std::sort(kp.begin(), kp.end());   // ties by point index: deterministic
+  std::vector<uint64_t> skey(n);
+  std::vector<int> order(n);
+  parallel_ranges(n, [&](int lo, int hi) {
+    for (int i = lo; i < hi; i++) {
+      skey[i] = morton(cell(pts[2 * i], kLmax), cell(pts[2 * i + 1], kLmax));
+      order[i] = i;
+    }
+  });
+  radix_sort_pairs(&skey, &order, 2 * kLmax);
+  std::vector<long> first_diff(kLmax + 1, 0);
+  for (int i = 1; i < n; i++) {
+    const uint64_t d = skey[i] ^ skey[i - 1];
+    if (d) first_diff[kLmax - (63 - __builtin_clzll(d)) / 2]++;
+  }
   int L = 2;
   for (;; L++) {
-    const int sh = 2 * (kLmax - L);
-    long nl = 0;
-    for (int i = 0; i < n; i++)
-      if (i == 0 || (kp[i].first >> sh) != (kp[i - 1].first >> sh)) nl++;
+    long nl = 1;
+    for (int l = 0; l <= L; l++) nl += first_diff[l];
     if ((double)n / nl <= 40.0 || L >= kLmax) break;
   }
   F->L = L;
-  std::vector<int> order(n);
-  std::vector<uint64_t> key(n);
-  for (int i = 0; i < n; i++) {
-    order[i] = kp[i].second;
-    key[kp[i].second] = kp[i].first >> (2 * (kLmax - L));
-  }
   // leaves and levels (global box index: level 0 first)
   std::vector<std::vector<uint64_t>> lk(L + 1);
   std::vector<int> leaf_start;
+  const int shL = 2 * (kLmax - L);
   for (int i = 0; i < n; i++) {
-    uint64_t k = key[order[i]];
+    const uint64_t k = skey[i] >> shL;
     if (lk[L].empty() || lk[L].back() != k) {
       lk[L].push_back(k);
       leaf_start.push_back(i);
@@ -596,9 +683,8 @@ std::unique_ptr<Fmm2dPlan, Fmm2dPlanDeleter> fmm2d_plan(const double* pts, const
   const int nbox = F->lvl_off[L + 1];
   F->nbox = nbox;
   F->nleaf = (int)lk[L].size();
-  std::vector<std::unordered_map<uint64_t, int>> idx(L + 1);
-  for (int l = 0; l <= L; l++)
-    for (size_t i = 0; i < lk[l].size(); i++) idx[l][lk[l][i]] = F->lvl_off[l] + (int)i;
+  std::vector<KeyIndex> idx(L + 1);
+  for (int l = 0; l <= L; l++) idx[l].build(lk[l], F->lvl_off[l]);
   std::vector<double2> centre(nbox);
   std::vector<int> parent(nbox, -1), child(4 * (size_t)nbox, -1), child_pos(nbox, 0);
   for (int l = 0; l <= L; l++) {
@@ -610,48 +696,83 @@ std::unique_ptr<Fmm2dPlan, Fmm2dPlanDeleter> fmm2d_plan(const double* pts, const
       centre[g] = make_double2(F->lo + (ix + 0.5) * side, F->lo + (iy + 0.5) * side);
       child_pos[g] = (int)(lk[l][i] & 3u);
       if (l > 0) {
-        int pg = idx[l - 1].at(lk[l][i] >> 2);
+        int pg = idx[l - 1].find(lk[l][i] >> 2);
         parent[g] = pg;
         child[4 * (size_t)pg + child_pos[g]] = g;
       }
     }
   }
-  // near lists (leaf indices) and interaction lists
+  // near lists (leaf indices) and interaction lists, built in parallel parts
+  // and joined in box order
+  auto level_of = [&](int g) {
+    int l = 0;
+    while (F->lvl_off[l + 1] <= g) l++;
+    return l;
+  };
   std::vector<int> near_off(1, 0), near_leaf;
-  for (size_t i = 0; i < lk[L].size(); i++) {
-    uint32_t ix, iy;
-    demorton(lk[L][i], &ix, &iy);
-    for (int di = -1; di <= 1; di++)
-      for (int dj = -1; dj <= 1; dj++) {
-        long a = (long)ix + di, b = (long)iy + dj;
-        if (a < 0 || b < 0) continue;
-        auto it = idx[L].find(morton((uint32_t)a, (uint32_t)b));
-        if (it != idx[L].end()) near_leaf.push_back(it->second - F->lvl_off[L]);
+  {
+    const int nl = (int)lk[L].size();
+    const int parts = parallel_part_count(nl, 2048);
+    std::vector<std::vector<int>> pl(parts), pc(parts);
+    parallel_parts(nl, [&](int t, int lo, int hi) {
+      for (int i = lo; i < hi; i++) {
+        uint32_t ix, iy;
+        demorton(lk[L][i], &ix, &iy);
+        int c = 0;
+        for (int di = -1; di <= 1; di++)
+          for (int dj = -1; dj <= 1; dj++) {
+            long a = (long)ix + di, b = (long)iy + dj;
+            if (a < 0 || b < 0) continue;
+            const int f = idx[L].find(morton((uint32_t)a, (uint32_t)b));
+            if (f >= 0) {
+              pl[t].push_back(f - F->lvl_off[L]);
+              c++;
+            }
+          }
+        pc[t].push_back(c);
       }
-    near_off.push_back((int)near_leaf.size());
+    }, 2048);
+    for (int t = 0; t < parts; t++) {
+      near_leaf.insert(near_leaf.end(), pl[t].begin(), pl[t].end());
+      for (int c : pc[t]) near_off.push_back(near_off.back() + c);
+    }
   }
   std::vector<int> v_off(1, 0), v_src, v_code;
-  for (int l = 0; l <= L; l++) {
-    for (size_t i = 0; i < lk[l].size(); i++) {
-      if (l >= 2) {
-        uint32_t ix, iy;
-        demorton(lk[l][i], &ix, &iy);
-        long px = ix >> 1, py = iy >> 1;
-        for (int a = -1; a <= 1; a++)
-          for (int b = -1; b <= 1; b++)
-            for (int u = 0; u < 2; u++)
-              for (int w = 0; w < 2; w++) {
-                long sx = 2 * (px + a) + u, sy = 2 * (py + b) + w;
-                if (sx < 0 || sy < 0) continue;
-                long di = (long)ix - sx, dj = (long)iy - sy;
-                if (std::labs(di) <= 1 && std::labs(dj) <= 1) continue;
-                auto it = idx[l].find(morton((uint32_t)sx, (uint32_t)sy));
-                if (it == idx[l].end()) continue;
-                v_src.push_back(it->second);
-                v_code.push_back((int)((di + 3) * 7 + (dj + 3)));
-              }
+  {
+    const int parts = parallel_part_count(nbox, 2048);
+    std::vector<std::vector<int>> ps(parts), pcd(parts), pc(parts);
+    parallel_parts(nbox, [&](int t, int lo, int hi) {
+      if (lo >= hi) return;
+      int l = level_of(lo);
+      for (int g = lo; g < hi; g++) {
+        while (F->lvl_off[l + 1] <= g) l++;
+        int c = 0;
+        if (l >= 2) {
+          uint32_t ix, iy;
+          demorton(lk[l][g - F->lvl_off[l]], &ix, &iy);
+          long px = ix >> 1, py = iy >> 1;
+          for (int a = -1; a <= 1; a++)
+            for (int b = -1; b <= 1; b++)
+              for (int u = 0; u < 2; u++)
+                for (int w = 0; w < 2; w++) {
+                  long sx = 2 * (px + a) + u, sy = 2 * (py + b) + w;
+                  if (sx < 0 || sy < 0) continue;
+                  long di = (long)ix - sx, dj = (long)iy - sy;
+                  if (std::labs(di) <= 1 && std::labs(dj) <= 1) continue;
+                  const int f = idx[l].find(morton((uint32_t)sx, (uint32_t)sy));
+                  if (f < 0) continue;
+                  ps[t].push_back(f);
+                  pcd[t].push_back((int)((di + 3) * 7 + (dj + 3)));
+                  c++;
+                }
+        }
+        pc[t].push_back(c);
       }
-      v_off.push_back((int)v_src.size());
+    }, 2048);
+    for (int t = 0; t < parts; t++) {
+      v_src.insert(v_src.end(), ps[t].begin(), ps[t].end());
+      v_code.insert(v_code.end(), pcd[t].begin(), pcd[t].end());
+      for (int c : pc[t]) v_off.push_back(v_off.back() + c);
     }
   }
   // translation matrices
@@ -682,14 +803,16 @@ std::unique_ptr<Fmm2dPlan, Fmm2dPlanDeleter> fmm2d_plan(const double* pts, const
   // sorted point data
   std::vector<double2> z(n), nw(n);
   std::vector<double> dg(n);
-  for (int i = 0; i < n; i++) {
-    int o = order[i];
-    z[i] = make_double2(pts[2 * o], pts[2 * o + 1]);
-    double w = wts[o] / kPi2;
-    nw[i] = make_double2(-w * nrm[2 * o], -w * nrm[2 * o + 1]);
-    // Kernel::one_d_kern's coincident-point limit (kernel.cpp:37-38)
-    dg[i] = 0.5 + 0.5 * (kap ? kap[o] : 0.0) * wts[o] * (1.0 / kPi2);
-  }
+  parallel_ranges(n, [&](int lo, int hi) {
+    for (int i = lo; i < hi; i++) {
+      int o = order[i];
+      z[i] = make_double2(pts[2 * o], pts[2 * o + 1]);
+      double w = wts[o] / kPi2;
+      nw[i] = make_double2(-w * nrm[2 * o], -w * nrm[2 * o + 1]);
+      // Kernel::one_d_kern's coincident-point limit (kernel.cpp:37-38)
+      dg[i] = 0.5 + 0.5 * (kap ? kap[o] : 0.0) * wts[o] * (1.0 / kPi2);
+    }
+  });
   std::vector<int> leaf_box(F->nleaf);
   for (int i = 0; i < F->nleaf; i++) leaf_box[i] = F->lvl_off[L] + i;
   for (int i = 0; i < F->nleaf; i++) {

@@ -1,5 +1,7 @@
 #include "ki_tree.h"
 
+#include "ki_parallel.h"
+
 #include <algorithm>
 #include <cmath>
 #include <stdexcept>
@@ -28,26 +30,6 @@ inline int child_of(const double* p, const double* c, int dim) {
   for (int d = 0; d < dim; d++)
     if (p[d] >= c[d]) ci += 1 << (dim - 1 - d);
   return ci;
-}
-
-// fn(lo, hi) over [0, n) split into contiguous ranges on up to 16 threads
-// (one range, on the caller's thread, below 4096 items).
-template <typename Fn>
-void parallel_ranges(int n, Fn fn) {
-  const int hw = (int)std::thread::hardware_concurrency();
-  const int T = std::max(1, std::min(16, hw));
-  if (n < 4096 || T == 1) {
-    fn(0, n);
-    return;
-  }
-  const int chunk = (n + T - 1) / T;
-  std::vector<std::thread> th;
-  for (int t = 1; t < T; t++) {
-    const int lo = t * chunk, hi = std::min(n, lo + chunk);
-    if (lo < hi) th.emplace_back(fn, lo, hi);
-  }
-  fn(0, std::min(n, chunk));
-  for (auto& x : th) x.join();
 }
 
 }  // namespace
