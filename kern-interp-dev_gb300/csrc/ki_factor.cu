@@ -1493,10 +1493,13 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
   const int c0 = blockIdx.y * cw;
   const int nc = min(cw, ncols - c0);
   if (nc <= 0) return;
-  // sx: n x nc column-major (rows 0..k-1 skeleton, k..n-1 redundant)
+  // sx: n x nc column-major with an odd leading dimension (rows 0..k-1
+  // skeleton, k..n-1 redundant); gathered and scattered a row of columns
+  // per warp step (coalesced in x, conflict-free in sx)
+  const int ld = n | 1;
   for (int idx = threadIdx.x; idx < n * nc; idx += blockDim.x) {
-    int i = idx % n, c = idx / n;
-    sx[idx] = x[(size_t)t.pact[i] * ldx + c0 + c];
+    int i = idx / nc, c = idx % nc;
+    sx[i + (size_t)ld * c] = x[(size_t)t.pact[i] * ldx + c0 + c];
   }
   __syncthreads();
   T* xs = sx;
@@ -1507,8 +1510,8 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
       int i = idx % r, c = idx / r;
       T acc = T(0);
       const T* tc = t.Tm + (size_t)k * i;
-      for (int l = 0; l < k; l++) acc += tc[l] * xs[l + (size_t)n * c];
-      xr[i + (size_t)n * c] -= acc;
+      for (int l = 0; l < k; l++) acc += tc[l] * xs[l + (size_t)ld * c];
+      xr[i + (size_t)ld * c] -= acc;
     }
     __syncthreads();
     // x_s -= L x_r   or   x_s -= U^T x_r
@@ -1517,39 +1520,39 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
       T acc = T(0);
       if (mode == kPsi) {
         const T* uc = t.U + (size_t)r * l;
-        for (int i = 0; i < r; i++) acc += uc[i] * xr[i + (size_t)n * c];
+        for (int i = 0; i < r; i++) acc += uc[i] * xr[i + (size_t)ld * c];
       } else {
-        for (int i = 0; i < r; i++) acc += t.L[l + (size_t)k * i] * xr[i + (size_t)n * c];
+        for (int i = 0; i < r; i++) acc += t.L[l + (size_t)k * i] * xr[i + (size_t)ld * c];
       }
-      xs[l + (size_t)n * c] -= acc;
+      xs[l + (size_t)ld * c] -= acc;
     }
     __syncthreads();
-    if (mode == kUpDiag) diag_solve(t, xr, n, nc, sx + (size_t)n * nc);
+    if (mode == kUpDiag) diag_solve(t, xr, ld, nc, sx + (size_t)ld * nc);
   } else if (mode == kDown) {
     // x_r -= U x_s
     for (int idx = threadIdx.x; idx < r * nc; idx += blockDim.x) {
       int i = idx % r, c = idx / r;
       T acc = T(0);
-      for (int l = 0; l < k; l++) acc += t.U[i + (size_t)r * l] * xs[l + (size_t)n * c];
-      xr[i + (size_t)n * c] -= acc;
+      for (int l = 0; l < k; l++) acc += t.U[i + (size_t)r * l] * xs[l + (size_t)ld * c];
+      xr[i + (size_t)ld * c] -= acc;
     }
     __syncthreads();
     // x_s -= T x_r
     for (int idx = threadIdx.x; idx < k * nc; idx += blockDim.x) {
       int l = idx % k, c = idx / k;
       T acc = T(0);
-      for (int i = 0; i < r; i++) acc += t.Tm[l + (size_t)k * i] * xr[i + (size_t)n * c];
-      xs[l + (size_t)n * c] -= acc;
+      for (int i = 0; i < r; i++) acc += t.Tm[l + (size_t)k * i] * xr[i + (size_t)ld * c];
+      xs[l + (size_t)ld * c] -= acc;
     }
     __syncthreads();
   } else if (mode == kDiag) {
-    diag_solve(t, xr, n, nc, sx + (size_t)n * nc);
+    diag_solve(t, xr, ld, nc, sx + (size_t)ld * nc);
   }
   __syncthreads();
   const int lo = mode == kDiag ? k : 0;   // the diagonal solve changes x_r only
   for (int idx = threadIdx.x; idx < (n - lo) * nc; idx += blockDim.x) {
     int i = lo + idx % (n - lo), c = idx / (n - lo);
-    x[(size_t)t.pact[i] * ldx + c0 + c] = sx[i + (size_t)n * c];
+    x[(size_t)t.pact[i] * ldx + c0 + c] = sx[i + (size_t)ld * c];
   }
 }
 
@@ -1812,18 +1815,45 @@ __global__ void k_mc_rhs(const T* x, int ldx, const int* idx, int nr, const T* t
 }
 
 // x(i, :) -= U~(i, :) alpha for redundant rows (N = w - U~_r alpha).
+// x (DOF-major N x nc) -= U~ alpha on the rows whose mask is clear (U~: N x
+// nb row-major, alpha = rows nr.. of M, ns x nc column-major).  Lanes are
+// columns (blockIdx.y: a 32-column chunk), a warp takes one row at a time
+// with the U~ row broadcast, alpha staged in shared memory 64 border
+// columns at a time; each CTA owns a contiguous range of rows.
 template <typename T>
-__global__ void k_mc_update(T* x, int nc, const T* Um, int nb, const T* M, int nr, int N,
-                            const unsigned char* mask) {
+__global__ void __launch_bounds__(256) k_mc_update(T* x, int nc, const T* Um, int nb, const T* M,
+                                                   int nr, int N, const unsigned char* mask) {
+  __shared__ T A[64 * 32];
   const int ns = nr + nb;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)N * nc;
-       e += (size_t)gridDim.x * blockDim.x) {
-    int i = (int)(e / nc), c = (int)(e % nc);
-    if (mask[i]) continue;
-    T acc = T(0);
-    for (int b = 0; b < nb; b++) acc += Um[(size_t)i * nb + b] * M[nr + b + (size_t)ns * c];
-    x[e] -= acc;
+  const int c0 = blockIdx.y * 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int c = c0 + lane;
+  const int per = (N + gridDim.x - 1) / gridDim.x;
+  const int i0 = blockIdx.x * per, i1 = min(N, i0 + per);
+  for (int b0 = 0; b0 < nb; b0 += 64) {
+    const int bn = min(64, nb - b0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < 64 * 32; e += blockDim.x) {
+      const int b = e / 32, cc = e % 32;
+      A[e] = (b < bn && c0 + cc < nc) ? M[nr + b0 + b + (size_t)ns * (c0 + cc)] : T(0);
+    }
+    __syncthreads();
+    for (int i = i0 + warp; i < i1; i += nw) {
+      if (mask[i]) continue;
+      const T* u = Um + (size_t)i * nb + b0;
+      T acc = T(0);
+      for (int b = 0; b < bn; b++) acc += u[b] * A[b * 32 + lane];
+      if (c < nc) x[(size_t)i * nc + c] -= acc;
+    }
   }
+}
+
+template <typename T>
+void mc_update(T* x, int nc, const T* Um, int nb, const T* M, int nr, int N,
+               const unsigned char* mask, cudaStream_t s) {
+  if (N <= 0 || nc <= 0 || nb <= 0) return;
+  dim3 g((unsigned)std::max(1, std::min(4096, (N + 255) / 256)), (unsigned)((nc + 31) / 32));
+  k_mc_update<T><<<g, 256, 0, s>>>(x, nc, Um, nb, M, nr, N, mask);
 }
 
 // x(allskel, :) = M(0:nr, :), alpha (row-major nb x nc) = M(nr:, :)
@@ -1930,10 +1960,11 @@ void launch_sweep(Factorization<T>& F, int l, int mode, T* x, int ncols, cudaStr
   if (LF.n_comp == 0 || ncols == 0) return;
   // shared memory: the box's rows (n x cw) and the inverse product's
   // temporary (r x cw <= n x cw)
-  int cw = std::max(1, std::min(ncols, (int)(96 * 1024 / (2 * sizeof(T) * std::max(1, LF.max_n)))));
+  const int ldmax = std::max(1, LF.max_n) | 1;   // k_sweep's odd leading dimension
+  int cw = std::max(1, std::min(ncols, (int)(96 * 1024 / (2 * sizeof(T) * ldmax))));
   cw = std::min(cw, 32);
   dim3 grid(LF.n_comp, (ncols + cw - 1) / cw);
-  size_t sm = 2 * sizeof(T) * (size_t)LF.max_n * cw;
+  size_t sm = 2 * sizeof(T) * (size_t)ldmax * cw;
   if (sm > 200 * 1024) throw std::runtime_error("box too large for the sweep kernel");
   if (sm > 48 * 1024)
     KI_CUDA(cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -2978,8 +3009,7 @@ void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, const T* d
   se();
   sb("border_update");
   if (nb <= 64) {
-    k_mc_update<T><<<std::min(8192, (int)(((size_t)N * ncols + 255) / 256)), 256, 0, s>>>(
-        d_x, ncols, F.d_Umod, nb, M, nr, N, F.d_is_skel);              // w - U~_r alpha
+    mc_update<T>(d_x, ncols, F.d_Umod, nb, M, nr, N, F.d_is_skel, s);   // w - U~_r alpha
   } else {
     // x (DOF-major = column-major ncols x N) -= alpha^T U~^T; skeleton rows
     // are overwritten afterwards, so they need no mask
@@ -3063,8 +3093,7 @@ void solve_device_arena(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, Scra
   k_mc_rhs<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
       d_x, ncols, F.d_root_idx, nr, t, nb, ncols, M);
   dense_lu_solve<T>(F.d_root_lu, ns, F.d_root_piv, M, ns, ncols, false, s);
-  k_mc_update<T><<<std::min(8192, (int)(((size_t)N * ncols + 255) / 256)), 256, 0, s>>>(
-      d_x, ncols, F.d_Umod, nb, M, nr, N, F.d_is_skel);
+  mc_update<T>(d_x, ncols, F.d_Umod, nb, M, nr, N, F.d_is_skel, s);
   KI_CUDA(cudaGetLastError());
   for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kDiag, d_x, ncols, s);
   k_mc_finish<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
