@@ -486,8 +486,9 @@ def main():
                             "neighbourhood, 32 columns, plus the local expansions at the targets)",
                             "near-field point pairs x (4 x 32 + 12) + targets x p x (4 x 32 + 6) "
                             "flops / device time of the launches"),
-        "refine:fmm_m2l": ("k_m2l (FMM multipole-to-local translations)",
-                           "interaction pairs x p^2 x 32 columns x 8 flops / device time"),
+        "refine:fmm_m2l": ("k_m2l (FMM multipole-to-local translations, rotated form)",
+                           "interaction pairs x 32 columns x (4 p^2 + 14 p) flops (real p x p "
+                           "core times complex multipoles, 2p phase rotations) / device time"),
         "schur": ("k_schur (schur stage: per box, the redundant block's LU or inverse and the "
                   "Schur updates of the skeleton and near-field blocks)",
                   "algorithmic Schur-complement flops summed over the level's boxes / device "

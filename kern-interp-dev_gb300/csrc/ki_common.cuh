@@ -155,6 +155,26 @@ __device__ void cta_gemm(int m, int n, int kk, T alpha, const T* A, int lda, boo
   }
 }
 
+// f(i, c) for the elements e = threadIdx.x, threadIdx.x + blockDim.x, ... of
+// a rows x cols rectangle, i = e % rows, c = e / rows, advanced without a
+// division per element.
+template <typename F>
+__device__ __forceinline__ void cta_for_2d(int rows, int cols, F f) {
+  if (rows <= 0 || cols <= 0) return;
+  const int nth = blockDim.x;
+  int i = (int)threadIdx.x % rows, c = (int)threadIdx.x / rows;
+  const int di = nth % rows, dc = nth / rows;
+  while (c < cols) {
+    f(i, c);
+    i += di;
+    c += dc;
+    if (i >= rows) {
+      i -= rows;
+      c++;
+    }
+  }
+}
+
 // In-place LU with partial pivoting (dgetrf semantics, 0-based pivots:
 // row i was swapped with piv[i]).  Returns the first zero pivot + 1, or 0.
 template <typename T>
@@ -195,11 +215,11 @@ __device__ int cta_lu(int n, T* A, int lda, int* piv, int* s_flag, T* s_red, int
     T d = A[j + (size_t)lda * j];
     for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) A[i + (size_t)lda * j] /= d;
     __syncthreads();
-    int rows = n - j - 1;
-    for (int idx = threadIdx.x; idx < rows * rows; idx += blockDim.x) {
-      int i = j + 1 + idx % rows, c = j + 1 + idx / rows;
+    const int rows = n - j - 1;
+    cta_for_2d(rows, rows, [&](int ii, int cc) {
+      const int i = j + 1 + ii, c = j + 1 + cc;
       A[i + (size_t)lda * c] -= A[i + (size_t)lda * j] * A[j + (size_t)lda * c];
-    }
+    });
     __syncthreads();
   }
   (void)s_flag;
@@ -253,13 +273,12 @@ __device__ int cta_gj_inverse(int n, T* A, int lda, int* piv, T* colj, T* s_val,
       if (p != j) A[p + (size_t)lda * c] = a;
     }
     __syncthreads();
-    const int m = n - 1;
-    for (int e = threadIdx.x; e < m * n; e += blockDim.x) {
-      const int ii = e % m, c = e / m;
+    // elimination over the rows other than j (row j is scaled; A(j, j) = 1/pivot)
+    cta_for_2d(n - 1, n, [&](int ii, int c) {
       const int i = ii < j ? ii : ii + 1;
       if (c == j) A[i + (size_t)lda * j] = -colj[i] * A[j + (size_t)lda * j];
       else A[i + (size_t)lda * c] -= colj[i] * A[j + (size_t)lda * c];
-    }
+    });
     __syncthreads();
   }
   for (int i = threadIdx.x; i < n; i += blockDim.x)
@@ -338,38 +357,34 @@ __device__ void cta_lu_solve_par(int n, const T* LU, int lda, const int* piv, bo
     }
     __syncthreads();
     for (int l = 0; l < n - 1; l++) {          // unit lower
-      const int rows = n - 1 - l;
-      for (int e = tid; e < rows * nrhs; e += nth) {
-        int i = l + 1 + e % rows, c = e / rows;
+      cta_for_2d(n - 1 - l, nrhs, [&](int ii, int c) {
+        const int i = l + 1 + ii;
         B[i + (size_t)ldb * c] -= LU[i + (size_t)lda * l] * B[l + (size_t)ldb * c];
-      }
+      });
       __syncthreads();
     }
     for (int l = n - 1; l >= 0; l--) {         // upper
       for (int c = tid; c < nrhs; c += nth) B[l + (size_t)ldb * c] /= LU[l + (size_t)lda * l];
       __syncthreads();
-      for (int e = tid; e < l * nrhs; e += nth) {
-        int i = e % l, c = e / l;
+      cta_for_2d(l, nrhs, [&](int i, int c) {
         B[i + (size_t)ldb * c] -= LU[i + (size_t)lda * l] * B[l + (size_t)ldb * c];
-      }
+      });
       __syncthreads();
     }
   } else {
     for (int l = 0; l < n; l++) {              // U^T (lower, U's diagonal)
       for (int c = tid; c < nrhs; c += nth) B[l + (size_t)ldb * c] /= LU[l + (size_t)lda * l];
       __syncthreads();
-      const int rows = n - 1 - l;
-      for (int e = tid; e < rows * nrhs; e += nth) {
-        int i = l + 1 + e % rows, c = e / rows;
+      cta_for_2d(n - 1 - l, nrhs, [&](int ii, int c) {
+        const int i = l + 1 + ii;
         B[i + (size_t)ldb * c] -= LU[l + (size_t)lda * i] * B[l + (size_t)ldb * c];
-      }
+      });
       __syncthreads();
     }
     for (int l = n - 1; l >= 1; l--) {         // L^T (unit upper)
-      for (int e = tid; e < l * nrhs; e += nth) {
-        int i = e % l, c = e / l;
+      cta_for_2d(l, nrhs, [&](int i, int c) {
         B[i + (size_t)ldb * c] -= LU[l + (size_t)lda * i] * B[l + (size_t)ldb * c];
-      }
+      });
       __syncthreads();
     }
     for (int c = tid; c < nrhs; c += nth) {

@@ -211,7 +211,16 @@ struct SchurTask {
   T* Atil;            // k x k accumulated self-block
   T* ws;              // scratch: P (n*n) | Wrs (r*k) | Wsr (k*r) | Lt (r*k)
   T* Xi;              // r x r explicit inverse of X (FP32 forms), or null
+  int gj;             // Gauss-Jordan path in shared memory (forms Xi); else LU
 };
+
+// Shared-memory bytes of k_schur for a task on its path.
+template <typename T>
+size_t schur_bytes(int n, int k, bool inv);
+template <typename T>
+size_t schur_task_bytes(const SchurTask<T>& q) {
+  return schur_bytes<T>(q.n, q.k, q.gj != 0);
+}
 
 // ---------------------------------------------------------------- kernels --
 __global__ void k_build_active(const ActiveTask* tasks, int* ipool) {
@@ -305,6 +314,11 @@ __device__ __forceinline__ T id_entry(const Points<T>& P, int sol_dim, int row, 
   return stokes_entry_r<T>(apar, par, -rx, -ry, bnx, bny, ux, uy, c.pw2, T(0));
 }
 
+// Order-preserving integer key of a non-negative norm (FP32 keys avoid an
+// FP64 conversion in the FP32 kernels).
+__device__ __forceinline__ long long norm_key(double v) { return __double_as_longlong(v); }
+__device__ __forceinline__ long long norm_key(float v) { return (long long)__float_as_int(v); }
+
 // Interpolative decomposition of one box per CTA.
 //
 // Thread-per-column formulation: every dot product and update runs inside
@@ -371,6 +385,8 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   const int nprox_rows = t.mode == 0 ? 2 * px.n * sol_dim : 0;
   if (flags & 1) {
   if (tid == 0) s_cnt = 0;
+  // the box centre split hi + lo and the filter radius, for the FP32 filter
+  const ProxyBox<T> cb = proxy_box<T>(t.cx, t.cy, t.cz, t.rad_filter, 1);
   __syncthreads();
   for (int s = t.seg_begin; s < t.seg_end; s++) {
     const int* src = ipool + seg_off[s];
@@ -384,15 +400,28 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
           keep = 1;
         } else {
           const int p = dof_point(dof, sol_dim);
-          double dx = t.cx - ((double)P.x[p] + (P.xl ? (double)P.xl[p] : 0.0));
-          double dy = t.cy - ((double)P.y[p] + (P.yl ? (double)P.yl[p] : 0.0));
-          double d2 = dx * dx + dy * dy;
-          if (P.dim == 3) {
-            double dz = t.cz - ((double)P.z[p] + (P.zl ? (double)P.zl[p] : 0.0));
-            d2 += dz * dz;
+          if (sizeof(T) < sizeof(double)) {
+            // FP32 forms: the offset from the split centre in FP32 and the
+            // squared comparison (no FP64 arithmetic in the FP32 kernels)
+            const T dx = (cb.hx - P.x[p]) + (cb.lx - (P.xl ? P.xl[p] : T(0)));
+            const T dy = (cb.hy - P.y[p]) + (cb.ly - (P.yl ? P.yl[p] : T(0)));
+            T d2 = dx * dx + dy * dy;
+            if (P.dim == 3) {
+              const T dz = (cb.hz - P.z[p]) + (cb.lz - (P.zl ? P.zl[p] : T(0)));
+              d2 += dz * dz;
+            }
+            keep = d2 < cb.rad * cb.rad;
+          } else {
+            double dx = t.cx - ((double)P.x[p] + (P.xl ? (double)P.xl[p] : 0.0));
+            double dy = t.cy - ((double)P.y[p] + (P.yl ? (double)P.yl[p] : 0.0));
+            double d2 = dx * dx + dy * dy;
+            if (P.dim == 3) {
+              double dz = t.cz - ((double)P.z[p] + (P.zl ? (double)P.zl[p] : 0.0));
+              d2 += dz * dz;
+            }
+            double dist = sqrt(d2);
+            keep = dist < t.rad_filter;
           }
-          double dist = sqrt(d2);
-          keep = dist < t.rad_filter;
         }
       }
       int v = keep;
@@ -605,7 +634,7 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
       long long best = -1;
       int bi = j;
       for (int c = j + lane; c < n; c += 32) {
-        long long v = (long long)__double_as_longlong((double)vn1[c]);
+        long long v = norm_key(vn1[c]);
         if (v > best) { best = v; bi = c; }
       }
       for (int o = 16; o > 0; o >>= 1) {
@@ -1171,8 +1200,9 @@ __global__ void k_assemble(const AsmTask<T>* tasks, const int* ipool, Points<T> 
 
 // Schur-complement elimination of a compressed box
 // (SkelFactorization::decouple, skel_factorization.cpp:91-127).  Working set
-// K_ss (k x k) | Wrs (r x k) | Lt (r x k) | X (r x r) | r scratch entries in
-// shared memory when it fits (smem != 0), else in the global scratch t.ws
+// K_ss (k x k) | Wrs (r x k) | Lt (r x k) | X (r x r) | r scratch entries
+// (and, inverse path, X's copy, U0, L0) in shared memory when it fits
+// (smem != 0), else in the global scratch t.ws
 // (X in place in the output).  The blocks are gathered from the box's self
 // block through the skeleton-first permutation; K_sr is held only
 // transposed (Lt), and K_rr only as X.  With t.Xi (FP32 forms, shared-
@@ -1219,42 +1249,64 @@ __global__ void __launch_bounds__(kThreads) k_schur(const SchurTask<T>* tasks, i
   // X -= K~_rs T
   cta_gemm<T>(r, r, k, T(-1), Wrs, r, false, Tm, k, false, T(1), X, r);
   __syncthreads();
-  if (smem && t.Xi) {
-    // X (kept in t.X for the refinement step) -> X^-1 in place
-    for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) t.X[idx] = X[idx];
+  if (smem && t.gj) {
+    // shared memory after X: colj (r) | X0 (r x r) | U0 (r x k) | L0 (k x r)
+    T* colj = X + (size_t)r * r;
+    T* X0 = colj + r;
+    T* U0 = X0 + (size_t)r * r;
+    T* L0 = U0 + (size_t)r * k;
+    for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) X0[idx] = X[idx];
     __syncthreads();
-    int info = cta_gj_inverse<T>(r, X, r, t.piv, X + (size_t)r * r, s_val, &s_idx);
+    int info = cta_gj_inverse<T>(r, X, r, t.piv, colj, s_val, &s_idx);   // X <- X^-1
     if (info != 0 && threadIdx.x == 0) atomicMax(err, (int)kDevSingular);
     // U0 = X^-1 K~_rs (r x k), L0 = K~_sr X^-1 (k x r)
-    cta_gemm<T>(r, k, r, T(1), X, r, false, Wrs, r, false, T(0), t.U, r);
-    cta_gemm<T>(k, r, r, T(1), Lt, r, true, X, r, false, T(0), t.L, k);
+    cta_gemm<T>(r, k, r, T(1), X, r, false, Wrs, r, false, T(0), U0, r);
+    cta_gemm<T>(k, r, r, T(1), Lt, r, true, X, r, false, T(0), L0, k);
+    __syncthreads();
+    // A~ = K_ss - L0 K~_rs (the correction's share follows below)
+    for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) {
+      const int i = idx % k, j = idx / k;
+      T acc = T(0);
+      for (int l = 0; l < r; l++) acc += L0[i + (size_t)k * l] * Wrs[l + (size_t)r * j];
+      t.Atil[idx] = Kss[idx] - acc;
+    }
     __syncthreads();
     // one step of refinement in the same precision (products with an explicit
-    // inverse are not backward stable; the corrected ones are):
-    // RU = K~_rs - X U0, RL = K~_sr - L0 X, then U = U0 + X^-1 RU, L = L0 + RL X^-1
-    T* RU = t.ws;
-    T* RL = t.ws + (size_t)r * k;
-    const T* X0 = t.X;
+    // inverse are not backward stable; the corrected ones are): the residuals
+    // RU = K~_rs - X U0 and RL = K~_sr - L0 X, in place of K~_rs and K~_sr^T
     for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
       const int i = idx % r, j = idx / r;
       T acc = T(0);
-      for (int l = 0; l < r; l++) acc += X0[i + (size_t)r * l] * t.U[l + (size_t)r * j];
-      RU[idx] = Wrs[idx] - acc;
+      for (int l = 0; l < r; l++) acc += X0[i + (size_t)r * l] * U0[l + (size_t)r * j];
+      Wrs[idx] -= acc;
+    }
+    for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
+      const int j = idx % r, i = idx / r;   // Lt(j, i) = K~_sr(i, j)
+      T acc = T(0);
+      for (int l = 0; l < r; l++) acc += L0[i + (size_t)k * l] * X0[l + (size_t)r * j];
+      Lt[idx] -= acc;
+    }
+    __syncthreads();
+    // U = U0 + X^-1 RU, L = L0 + RL X^-1, A~ -= RL U0 (RL X^-1 K~_rs)
+    for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
+      const int i = idx % r, j = idx / r;
+      T acc = T(0);
+      for (int l = 0; l < r; l++) acc += X[i + (size_t)r * l] * Wrs[l + (size_t)r * j];
+      t.U[idx] = U0[idx] + acc;
     }
     for (int idx = threadIdx.x; idx < k * r; idx += blockDim.x) {
       const int i = idx % k, j = idx / k;
       T acc = T(0);
-      for (int l = 0; l < r; l++) acc += t.L[i + (size_t)k * l] * X0[l + (size_t)r * j];
-      RL[idx] = Lt[j + (size_t)r * i] - acc;
+      for (int l = 0; l < r; l++) acc += Lt[l + (size_t)r * i] * X[l + (size_t)r * j];
+      t.L[idx] = L0[idx] + acc;
     }
-    __syncthreads();
-    cta_gemm<T>(r, k, r, T(1), X, r, false, RU, r, false, T(1), t.U, r);
-    cta_gemm<T>(k, r, r, T(1), RL, k, false, X, r, false, T(1), t.L, k);
-    // A~ = K_ss - L K~_rs
-    for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) t.Atil[idx] = Kss[idx];
+    for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) {
+      const int i = idx % k, j = idx / k;
+      T acc = T(0);
+      for (int l = 0; l < r; l++) acc += Lt[l + (size_t)r * i] * U0[l + (size_t)r * j];
+      t.Atil[idx] -= acc;
+    }
     for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) t.Xi[idx] = X[idx];
-    __syncthreads();
-    cta_gemm<T>(k, k, r, T(-1), t.L, k, false, Wrs, r, false, T(1), t.Atil, k);
     return;
   }
   int info = cta_lu<T>(r, X, r, t.piv, &s_flag, &s_red, &s_idx);
@@ -1375,10 +1427,12 @@ void copy_block(cudaStream_t s, const T* src, int lds, int rows, int cols, bool 
                                                                               trans, dst, ldd);
 }
 
+// Shared-memory bytes of k_schur for a box: K_ss, K~_rs, K~_sr^T, X and r
+// scratch entries, plus (inverse path) X's copy, U0 and L0.
 template <typename T>
-size_t schur_bytes(int n, int k) {
+size_t schur_bytes(int n, int k, bool inv) {
   size_t r = n - k;
-  return sizeof(T) * ((size_t)k * k + 2 * r * k + r * r + r);
+  return sizeof(T) * ((size_t)k * k + 2 * r * k + r * r + r + (inv ? r * r + 2 * r * k : 0));
 }
 
 // SkelFactorization::decouple for a box whose working set does not fit in one
@@ -1431,6 +1485,7 @@ struct SweepTask {
   const T* X;    // r x r LU
   const int* piv;
   const T* Xi;   // r x r explicit inverse (FP32 factorizations, r <= kInvMax) or null
+  int Xi_formed; // (host bookkeeping) Xi written by k_schur's Gauss-Jordan path
 };
 
 // Largest redundant block whose inverse is formed explicitly for the sweeps.
@@ -1451,13 +1506,15 @@ enum SweepMode : int {
 // product (every thread an independent dot product, tmp: r x nc), else the
 // LU substitution.
 template <typename T>
-__device__ void diag_solve(const SweepTask<T>& t, T* xr, int n, int nc, T* tmp) {
+__device__ void diag_solve(const SweepTask<T>& t, T* xr, int n, int nc, T* tmp,
+                           const T* Xi = nullptr) {
   const int r = t.n - t.k;
   if (t.Xi) {
+    if (!Xi) Xi = t.Xi;
     for (int idx = threadIdx.x; idx < r * nc; idx += blockDim.x) {
       const int i = idx % r, c = idx / r;
       T acc = T(0);
-      for (int j = 0; j < r; j++) acc += t.Xi[i + (size_t)r * j] * xr[j + (size_t)n * c];
+      for (int j = 0; j < r; j++) acc += Xi[i + (size_t)r * j] * xr[j + (size_t)n * c];
       tmp[idx] = acc;
     }
     __syncthreads();
@@ -1469,23 +1526,18 @@ __device__ void diag_solve(const SweepTask<T>& t, T* xr, int n, int nc, T* tmp) 
   }
 }
 
-// Explicit inverses of the LU-factored redundant blocks (one CTA per box;
-// boxes without a Xi slot are skipped): Xi = I, then the LU substitution on
-// all r columns.
+// A (n x n, column-major) = I.
 template <typename T>
-__global__ void k_lu_inverse(const SweepTask<T>* tasks) {
-  const SweepTask<T> t = tasks[blockIdx.x];
-  if (!t.Xi) return;
-  const int r = t.n - t.k;
-  T* Xi = const_cast<T*>(t.Xi);
-  for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x)
-    Xi[idx] = (idx % r == idx / r) ? T(1) : T(0);
-  __syncthreads();
-  cta_lu_solve_par<T>(r, t.X, r, t.piv, false, Xi, r, r);
+__global__ void k_set_identity(T* A, int n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * n;
+       e += (size_t)gridDim.x * blockDim.x)
+    A[e] = (e % n == e / n) ? T(1) : T(0);
 }
 
+
 template <typename T>
-__global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int cw, int mode) {
+__global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int cw, int mode,
+                        int stage_mats) {
   extern __shared__ unsigned char smem_raw[];
   T* sx = reinterpret_cast<T*>(smem_raw);
   const SweepTask<T> t = tasks[blockIdx.x];
@@ -1495,8 +1547,19 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
   if (nc <= 0) return;
   // sx: n x nc column-major with an odd leading dimension (rows 0..k-1
   // skeleton, k..n-1 redundant); gathered and scattered a row of columns
-  // per warp step (coalesced in x, conflict-free in sx)
+  // per warp step (coalesced in x, conflict-free in sx).  With stage_mats
+  // (uniform over the launch) each factor matrix is copied into shared
+  // memory (after sx and the product temporary) before the phase that uses
+  // it, so its entries are read from global memory once instead of once per
+  // column.
   const int ld = n | 1;
+  T* ms = sx + 2 * (size_t)ld * cw;
+  auto stage = [&](const T* g, int count) -> const T* {
+    if (!stage_mats) return g;
+    for (int e = threadIdx.x; e < count; e += blockDim.x) ms[e] = g[e];
+    __syncthreads();
+    return ms;
+  };
   for (int idx = threadIdx.x; idx < n * nc; idx += blockDim.x) {
     int i = idx / nc, c = idx % nc;
     sx[i + (size_t)ld * c] = x[(size_t)t.pact[i] * ldx + c0 + c];
@@ -1506,52 +1569,57 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
   T* xr = sx + k;
   if (mode == kUpDiag || mode == kUp || mode == kPsi) {
     // x_r -= T^T x_s
+    const T* Tm = stage(t.Tm, k * r);
     for (int idx = threadIdx.x; idx < r * nc; idx += blockDim.x) {
       int i = idx % r, c = idx / r;
       T acc = T(0);
-      const T* tc = t.Tm + (size_t)k * i;
+      const T* tc = Tm + (size_t)k * i;
       for (int l = 0; l < k; l++) acc += tc[l] * xs[l + (size_t)ld * c];
       xr[i + (size_t)ld * c] -= acc;
     }
     __syncthreads();
     // x_s -= L x_r   or   x_s -= U^T x_r
+    const T* M = stage(mode == kPsi ? t.U : t.L, k * r);
     for (int idx = threadIdx.x; idx < k * nc; idx += blockDim.x) {
       int l = idx % k, c = idx / k;
       T acc = T(0);
       if (mode == kPsi) {
-        const T* uc = t.U + (size_t)r * l;
+        const T* uc = M + (size_t)r * l;
         for (int i = 0; i < r; i++) acc += uc[i] * xr[i + (size_t)ld * c];
       } else {
-        for (int i = 0; i < r; i++) acc += t.L[l + (size_t)k * i] * xr[i + (size_t)ld * c];
+        for (int i = 0; i < r; i++) acc += M[l + (size_t)k * i] * xr[i + (size_t)ld * c];
       }
       xs[l + (size_t)ld * c] -= acc;
     }
     __syncthreads();
-    if (mode == kUpDiag) diag_solve(t, xr, ld, nc, sx + (size_t)ld * nc);
+    if (mode == kUpDiag)
+      diag_solve(t, xr, ld, nc, sx + (size_t)ld * nc, t.Xi ? stage(t.Xi, r * r) : nullptr);
   } else if (mode == kDown) {
     // x_r -= U x_s
+    const T* U = stage(t.U, r * k);
     for (int idx = threadIdx.x; idx < r * nc; idx += blockDim.x) {
       int i = idx % r, c = idx / r;
       T acc = T(0);
-      for (int l = 0; l < k; l++) acc += t.U[i + (size_t)r * l] * xs[l + (size_t)ld * c];
+      for (int l = 0; l < k; l++) acc += U[i + (size_t)r * l] * xs[l + (size_t)ld * c];
       xr[i + (size_t)ld * c] -= acc;
     }
     __syncthreads();
     // x_s -= T x_r
+    const T* Tm = stage(t.Tm, k * r);
     for (int idx = threadIdx.x; idx < k * nc; idx += blockDim.x) {
       int l = idx % k, c = idx / k;
       T acc = T(0);
-      for (int i = 0; i < r; i++) acc += t.Tm[l + (size_t)k * i] * xr[i + (size_t)ld * c];
+      for (int i = 0; i < r; i++) acc += Tm[l + (size_t)k * i] * xr[i + (size_t)ld * c];
       xs[l + (size_t)ld * c] -= acc;
     }
     __syncthreads();
   } else if (mode == kDiag) {
-    diag_solve(t, xr, ld, nc, sx + (size_t)ld * nc);
+    diag_solve(t, xr, ld, nc, sx + (size_t)ld * nc, t.Xi ? stage(t.Xi, r * r) : nullptr);
   }
   __syncthreads();
   const int lo = mode == kDiag ? k : 0;   // the diagonal solve changes x_r only
   for (int idx = threadIdx.x; idx < (n - lo) * nc; idx += blockDim.x) {
-    int i = lo + idx % (n - lo), c = idx / (n - lo);
+    int i = lo + idx / nc, c = idx % nc;
     x[(size_t)t.pact[i] * ldx + c0 + c] = sx[i + (size_t)ld * c];
   }
 }
@@ -1954,6 +2022,38 @@ struct HostBox {
 
 }  // namespace
 
+// Shared-memory bytes k_sweep needs to stage a factor matrix of `entries`
+// entries (the largest of r^2 and k r over the launch's boxes), and the
+// largest dynamic shared memory a staged sweep may use.
+template <typename T>
+size_t sweep_stage_bytes(int entries) {
+  return sizeof(T) * (size_t)entries;
+}
+constexpr size_t kSweepStageCap = 96 * 1024;
+
+// The diagonal solves x_r <- X^-1 x_r of every level's boxes: one launch per
+// bin of the all-levels descriptor array.
+template <typename T>
+void launch_diag_all(Factorization<T>& F, T* x, int ncols, cudaStream_t s) {
+  if (!F.d_all_tasks || ncols == 0) return;
+  const SweepTask<T>* all = reinterpret_cast<const SweepTask<T>*>(F.d_all_tasks);
+  for (const auto& b : F.diag_bins) {
+    const int ldmax = std::max(1, b[2]) | 1;
+    int cw = std::max(1, std::min(ncols, (int)(96 * 1024 / (2 * sizeof(T) * ldmax))));
+    cw = std::min(cw, 32);
+    dim3 grid(b[1], (ncols + cw - 1) / cw);
+    size_t sm = 2 * sizeof(T) * (size_t)ldmax * cw;
+    if (sm > 200 * 1024) throw std::runtime_error("box too large for the sweep kernel");
+    const size_t mats = sweep_stage_bytes<T>(b[3]);
+    const int staged = sm + mats <= kSweepStageCap;
+    if (staged) sm += mats;
+    if (sm > 48 * 1024)
+      KI_CUDA(cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    k_sweep<T><<<grid, kThreads, sm, s>>>(all + b[0], x, ncols, ncols, cw, kDiag, staged);
+    KI_CUDA(cudaGetLastError());
+  }
+}
+
 template <typename T>
 void launch_sweep(Factorization<T>& F, int l, int mode, T* x, int ncols, cudaStream_t s) {
   LevelFactor& LF = F.levels[l];
@@ -1966,10 +2066,13 @@ void launch_sweep(Factorization<T>& F, int l, int mode, T* x, int ncols, cudaStr
   dim3 grid(LF.n_comp, (ncols + cw - 1) / cw);
   size_t sm = 2 * sizeof(T) * (size_t)ldmax * cw;
   if (sm > 200 * 1024) throw std::runtime_error("box too large for the sweep kernel");
+  const size_t mats = sweep_stage_bytes<T>(LF.max_mat);
+  const int staged = sm + mats <= kSweepStageCap;
+  if (staged) sm += mats;
   if (sm > 48 * 1024)
-    KI_CUDA(cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    KI_CUDA(cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   k_sweep<T><<<grid, kThreads, sm, s>>>(reinterpret_cast<SweepTask<T>*>(LF.d_tasks), x, ncols,
-                                        ncols, cw, mode);
+                                        ncols, cw, mode, staged);
   KI_CUDA(cudaGetLastError());
 }
 
@@ -2179,6 +2282,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
   int64_t pact_top = (int64_t)N * (L + 1);
 
   std::vector<HostBox> hb(tree.boxes.size());
+  std::vector<SweepTask<T>> all_sw;   // every level's sweep descriptors
   for (size_t b = 0; b < tree.boxes.size(); b++)
     if (tree.boxes[b].leaf) hb[b].n = tree.boxes[b].orig_count;
 
@@ -2735,6 +2839,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       F->n_compressed++;
       F->n_redundant += r;
       LF.max_n = std::max(LF.max_n, n);
+      LF.max_mat = std::max(LF.max_mat, std::max(r * r, k * r));
     }
     if (sizeof(T) < sizeof(double)) {
       // FP32: explicit inverses of the redundant blocks for the sweeps (the
@@ -2780,17 +2885,21 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       // large ones (n above KI_SCHUR_WIDE_N, default 288)
       int wide_n = 288;
       if (const char* e = std::getenv("KI_SCHUR_WIDE_N")) wide_n = std::atoi(e);
+      // FP32: the Gauss-Jordan path where its working set fits, else the LU
+      // path (its inverse formed afterwards, xinv)
+      for (auto& q : st) q.gj = (q.Xi && schur_bytes<T>(q.n, q.k, true) <= cap) ? 1 : 0;
       for (auto& q : st)
-        if (schur_bytes<T>(q.n, q.k) <= cap) { st2.push_back(q); sm = std::max(sm, schur_bytes<T>(q.n, q.k)); n_sm++; }
+        if (schur_task_bytes<T>(q) <= cap) { st2.push_back(q); sm = std::max(sm, schur_task_bytes<T>(q)); n_sm++; }
       int n_glob = 0;
       for (auto& q : st)
-        if (schur_bytes<T>(q.n, q.k) > cap && q.n <= wide_n) { st2.push_back(q); n_glob++; }
+        if (schur_task_bytes<T>(q) > cap && q.n <= wide_n) { st2.push_back(q); n_glob++; }
       for (auto& q : st)
-        if (schur_bytes<T>(q.n, q.k) > cap && q.n > wide_n) st2.push_back(q);
+        if (schur_task_bytes<T>(q) > cap && q.n > wide_n) st2.push_back(q);
+      for (size_t q = 0; q < st.size(); q++) sw[q].Xi_formed = st[q].gj;
       // shared-memory boxes ascending by footprint, launched in bins of equal
       // CTAs per SM (each bin sized by its largest box) on the aux streams
       std::stable_sort(st2.begin(), st2.begin() + n_sm, [](const SchurTask<T>& a, const SchurTask<T>& b) {
-        return schur_bytes<T>(a.n, a.k) < schur_bytes<T>(b.n, b.k);
+        return schur_task_bytes<T>(a) < schur_task_bytes<T>(b);
       });
       (void)sm;
       upload(d_st, st2, s);
@@ -2800,10 +2909,10 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         KI_CUDA(cudaFuncSetAttribute(k_schur<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
       auto per_sm = [](size_t bytes) { return std::max(1, (int)(228 * 1024 / (bytes + 1024))); };
       for (int b0 = 0; b0 < n_sm;) {
-        const int ps = per_sm(schur_bytes<T>(st2[b0].n, st2[b0].k));
+        const int ps = per_sm(schur_task_bytes<T>(st2[b0]));
         int b1 = b0 + 1;
-        while (b1 < n_sm && per_sm(schur_bytes<T>(st2[b1].n, st2[b1].k)) == ps) b1++;
-        const size_t bsm = schur_bytes<T>(st2[b1 - 1].n, st2[b1 - 1].k);
+        while (b1 < n_sm && per_sm(schur_task_bytes<T>(st2[b1])) == ps) b1++;
+        const size_t bsm = schur_task_bytes<T>(st2[b1 - 1]);
         k_schur<T><<<(unsigned)(b1 - b0), kThreads, bsm, F->aux[(next++) % Factorization<T>::kAux]>>>(
             d_st, b0, 1, F->d_err);
         b0 = b1;
@@ -2820,26 +2929,62 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     SweepTask<T>* d_sw = (SweepTask<T>*)F->alloc(sizeof(SweepTask<T>) * sw.size());
     upload(d_sw, sw, s);
     LF.d_tasks = d_sw;
+    all_sw.insert(all_sw.end(), sw.begin(), sw.end());
     if (sizeof(T) < sizeof(double)) {
       // inverses of the boxes k_schur factored by LU (global working set)
       std::vector<SweepTask<T>> inv;
       double xf = 0;
       for (auto& w : sw)
-        if (w.Xi && schur_bytes<T>(w.n, w.k) > schur_cap) {
+        if (w.Xi && !w.Xi_formed) {
           inv.push_back(w);
           xf += 2.0 * std::pow((double)(w.n - w.k), 3);
         }
       if (!inv.empty()) {
-        SweepTask<T>* d_inv = (SweepTask<T>*)F->alloc(sizeof(SweepTask<T>) * inv.size());
-        upload(d_inv, inv, s);
+        // Xi = I, then the device-wide blocked LU substitution, one box per
+        // aux stream
         std::string xi_name = "xinv@L" + std::to_string(l);
         F->stage_begin(xi_name.c_str(), xf, 0);
-        k_lu_inverse<T><<<(unsigned)inv.size(), kThreads, 0, s>>>(d_inv);
+        F->fork();
+        for (size_t q = 0; q < inv.size(); q++) {
+          const int r = inv[q].n - inv[q].k;
+          cudaStream_t as = F->aux[q % Factorization<T>::kAux];
+          T* Xi = const_cast<T*>(inv[q].Xi);
+          k_set_identity<T><<<std::max(1, std::min(1024, (r * r + 255) / 256)), 256, 0, as>>>(Xi, r);
+          dense_lu_solve<T>(inv[q].X, r, inv[q].piv, Xi, r, r, false, as);
+        }
+        F->join(Factorization<T>::kAux);
         F->stage_end();
         KI_CUDA(cudaGetLastError());
       }
     }
     for (int i : ci_list) F->rank_hist.push_back(kh[i]);
+  }
+
+  // all levels' sweep descriptors, ascending n, in bins of equal CTAs per SM
+  // at 32 columns (the diagonal solves of different levels touch disjoint
+  // redundant rows, so they run in one pass)
+  if (!all_sw.empty()) {
+    std::stable_sort(all_sw.begin(), all_sw.end(),
+                     [](const SweepTask<T>& a, const SweepTask<T>& b) { return a.n < b.n; });
+    auto per_sm = [](int n) {
+      const size_t sm = 2 * sizeof(T) * (size_t)(n | 1) * 32;
+      return std::max(1, (int)(228 * 1024 / (sm + 1024)));
+    };
+    for (int b0 = 0; b0 < (int)all_sw.size();) {
+      const int ps = per_sm(all_sw[b0].n);
+      int b1 = b0 + 1;
+      while (b1 < (int)all_sw.size() && per_sm(all_sw[b1].n) == ps) b1++;
+      int mm = 0;
+      for (int q = b0; q < b1; q++) {
+        const int r = all_sw[q].n - all_sw[q].k;
+        mm = std::max(mm, std::max(r * r, all_sw[q].k * r));
+      }
+      F->diag_bins.push_back({b0, b1 - b0, all_sw[b1 - 1].n, mm});
+      b0 = b1;
+    }
+    SweepTask<T>* d_all = (SweepTask<T>*)F->alloc(sizeof(SweepTask<T>) * all_sw.size());
+    upload(d_all, all_sw, s);
+    F->d_all_tasks = d_all;
   }
 
   // ---- root block
@@ -2913,7 +3058,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         KI_CUDA(pool_malloc((void**)&dD, Tsz * (size_t)N * nb, s));
         KI_CUDA(cudaMemcpyAsync(dD, F->d_Umod, Tsz * (size_t)N * nb, cudaMemcpyDeviceToDevice, s));
         F->stage_begin("border_Dinv", 0, 0);
-        for (int l = L - 1; l >= 1; l--) launch_sweep<T>(*F, l, kDiag, dD, nb, s);
+        launch_diag_all<T>(*F, dD, nb, s);
         F->stage_end();
         T* corr = (T*)F->alloc(Tsz * (size_t)nb * nb);
         F->stage_begin("border_corr", 0, 0);
@@ -2996,7 +3141,7 @@ void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, const T* d
   KI_CUDA(pool_malloc((void**)&t, sizeof(T) * (size_t)nb * ncols + 16, s));
   KI_CUDA(pool_malloc((void**)&M, sizeof(T) * (size_t)ns * ncols + 16, s));
   KI_CUDA(cudaMemcpyAsync(Dw, d_x, sizeof(T) * (size_t)N * ncols, cudaMemcpyDeviceToDevice, s));
-  for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kDiag, Dw, ncols, s);
+  launch_diag_all<T>(F, Dw, ncols, s);
   se();
   sb("border_reduce");
   if (nb * ncols <= 16 * 256) reduce_rows<T>(F, F.d_PsiTmod, nb, Dw, ncols, t, s);   // Psi~_r D^-1 w
@@ -3018,7 +3163,7 @@ void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, const T* d
   KI_CUDA(cudaGetLastError());
   se();
   sb("border_diag");
-  for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kDiag, d_x, ncols, s);
+  launch_diag_all<T>(F, d_x, ncols, s);
   se();
   k_mc_finish<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
       d_x, ncols, F.d_root_idx, M, nr, nb, d_alpha);
@@ -3088,14 +3233,14 @@ void solve_device_arena(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, Scra
   T* partial = take(sizeof(T) * (size_t)((N + kRedRows - 1) / kRedRows) * nb * ncols);
   for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kUp, d_x, ncols, s);
   KI_CUDA(cudaMemcpyAsync(Dw, d_x, sizeof(T) * (size_t)N * ncols, cudaMemcpyDeviceToDevice, s));
-  for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kDiag, Dw, ncols, s);
+  launch_diag_all<T>(F, Dw, ncols, s);
   reduce_rows_arena<T>(F, F.d_PsiTmod, nb, Dw, ncols, t, partial, s);
   k_mc_rhs<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
       d_x, ncols, F.d_root_idx, nr, t, nb, ncols, M);
   dense_lu_solve<T>(F.d_root_lu, ns, F.d_root_piv, M, ns, ncols, false, s);
   mc_update<T>(d_x, ncols, F.d_Umod, nb, M, nr, N, F.d_is_skel, s);
   KI_CUDA(cudaGetLastError());
-  for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kDiag, d_x, ncols, s);
+  launch_diag_all<T>(F, d_x, ncols, s);
   k_mc_finish<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
       d_x, ncols, F.d_root_idx, M, nr, nb, d_alpha);
   KI_CUDA(cudaGetLastError());

@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <memory>
 #include <string>
+#include <array>
 #include <vector>
 
 #include "ki_tree.h"
@@ -37,6 +38,7 @@ struct LevelFactor {
   int n_comp = 0;          // compressed boxes in this level
   void* d_tasks = nullptr; // device array of per-box sweep descriptors
   int max_n = 0;           // largest active set among them
+  int max_mat = 0;         // largest factor matrix among them: max(r^2, k r) entries
 };
 
 // Device-time record of one launch group (CUDA events on the factor's stream).
@@ -85,6 +87,11 @@ struct Factorization {
   T* d_diag = nullptr;
   int diag_per_point = 0;   // 1 (Laplace), 9 (Stokes), 0 in 2D
   std::vector<LevelFactor> levels;   // index = tree level
+  // every level's sweep descriptors in one device array, ascending active
+  // size, for the diagonal solves of all levels in one pass; bins of boxes
+  // launched together
+  void* d_all_tasks = nullptr;
+  std::vector<std::array<int, 4>> diag_bins;   // {first, count, largest n, largest r^2}
   // root
   int n_root = 0;
   int* d_root_idx = nullptr;  // allskel DOF list

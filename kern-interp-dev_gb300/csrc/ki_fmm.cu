@@ -74,42 +74,40 @@ template <typename V> __device__ __forceinline__ V cround(double x, double y) {
   return r;
 }
 
-// q[i kCols + c] = nw[i] * mu[perm[i] + ldmu (c0 + c)]  (sorted order,
-// point-major: a point's columns are contiguous; product in FP64, rounded to
-// the expansion type).  Block (32, 8) per 32 points: columns read along the
-// points (coalesced in mu), written along the columns through shared memory.
+// u[i kCols + c] = mu[perm[i] + ldmu (c0 + c)]: the densities in sorted
+// order, point-major (a point's columns contiguous), in the expansion type.
+// Block (32, 8) per 32 points: columns read along the points (coalesced in
+// mu), written along the columns through shared memory.
 template <typename R>
-__global__ void k_charges(const double2* nw, const int* perm, int n, const double* mu, int ldmu,
-                          int c0, int nc, cplx_t<R>* q) {
-  using V = cplx_t<R>;
-  __shared__ V tile[32][kCols + 1];
+__global__ void k_densities(const int* perm, int n, const double* mu, int ldmu, int c0, int nc,
+                            R* u) {
+  __shared__ R tile[32][kCols + 1];
   const int i0 = blockIdx.x * 32;
   const int i = i0 + threadIdx.x;
   if (i < n) {
     const int o = perm[i];
-    const double2 w = nw[i];
-    for (int c = threadIdx.y; c < nc; c += blockDim.y) {
-      const double m = mu[o + (size_t)ldmu * (c0 + c)];
-      tile[threadIdx.x][c] = cround<V>(w.x * m, w.y * m);
-    }
+    for (int c = threadIdx.y; c < nc; c += blockDim.y)
+      tile[threadIdx.x][c] = (R)mu[o + (size_t)ldmu * (c0 + c)];
   }
   __syncthreads();
   const int cnt = min(32, n - i0);
   for (int e = threadIdx.y * 32 + threadIdx.x; e < cnt * nc; e += 32 * blockDim.y) {
     const int r = e / nc, c = e % nc;
-    q[(size_t)(i0 + r) * kCols + c] = tile[r][c];
+    u[(size_t)(i0 + r) * kCols + c] = tile[r][c];
   }
 }
 
 // Multipole expansion of every leaf: me[(g nc + c) p + k] = sum_s q_s w_s^k,
-// w_s = (z_s - centre) / side (formed in FP64).
+// w_s = (z_s - centre) / side (formed in FP64), q_s = nw_s mu_s with mu_s
+// real: the column-independent factors nw_s w_s^k are formed once per point
+// and each column adds mu_s times them (real-by-complex products).
 template <typename R>
 __global__ void k_p2m(const int* leaf_start, const int* leaf_box, const double2* centre,
-                      double side, const double2* z, const cplx_t<R>* q, int n, int nc, int p,
+                      double side, const double2* z, const double2* nw, const R* u, int nc, int p,
                       cplx_t<R>* me) {
   using V = cplx_t<R>;
   __shared__ V pw[kChunk][kMaxP];
-  __shared__ V qs[kChunk][kCols];
+  __shared__ R us[kChunk][kCols];
   const int lf = blockIdx.x, g = leaf_box[lf];
   const int s0 = leaf_start[lf], s1 = leaf_start[lf + 1];
   const double2 c = centre[g];
@@ -121,7 +119,7 @@ __global__ void k_p2m(const int* leaf_start, const int* leaf_box, const double2*
     __syncthreads();
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
       const V w = cround<V>((z[base + i].x - c.x) / side, (z[base + i].y - c.y) / side);
-      V t = cround<V>(1, 0);
+      V t = cround<V>(nw[base + i].x, nw[base + i].y);
       for (int k = 0; k < p; k++) {
         pw[i][k] = t;
         t = cmul(t, w);
@@ -129,7 +127,7 @@ __global__ void k_p2m(const int* leaf_start, const int* leaf_box, const double2*
     }
     for (int e = threadIdx.x; e < cnt * nc; e += blockDim.x) {
       int i = e / nc, cc = e % nc;
-      qs[i][cc] = q[(size_t)(base + i) * kCols + cc];
+      us[i][cc] = u[(size_t)(base + i) * kCols + cc];
     }
     __syncthreads();
     for (int r = 0; r < 4; r++) {
@@ -137,7 +135,11 @@ __global__ void k_p2m(const int* leaf_start, const int* leaf_box, const double2*
       if (o >= nout) break;
       int k = o % p, cc = o / p;
       V a = acc[r];
-      for (int i = 0; i < cnt; i++) a = cfma(qs[i][cc], pw[i][k], a);
+      for (int i = 0; i < cnt; i++) {
+        const R m = us[i][cc];
+        a.x = fmx(m, pw[i][k].x, a.x);
+        a.y = fmx(m, pw[i][k].y, a.y);
+      }
       acc[r] = a;
     }
   }
@@ -191,17 +193,21 @@ __global__ void k_m2m(int b0, const int* child, const int* child_pos, const cplx
 }
 
 // Local expansion contributions over the interaction list (M2L): for every
-// box g of one level, le[g] = (1/side) sum_v M_code(v) me[src(v)].  Output
-// (m, c) is thread c + nc m, so a warp shares one matrix row (broadcast) and
-// reads 32 columns of the staged multipole tile (row stride p + 1: conflict-
-// free).
+// box g of one level, le[g] = (1/side) sum_v M_code(v) me[src(v)].  The
+// translation for offset d, M(m, k) = (-1)^m C(k+m, m) rho^(k+m+1) with
+// rho = 1/d, is applied in rotated form: with rho = |rho| e^(i phi),
+// M(m, k) = e^(i phi (m+1)) Rr(m, k) e^(i phi k), Rr real, so each pair
+// costs p^2 real-by-complex products (half the complex ones) plus 2p phase
+// rotations.  Output (m, c) is thread c + nc m: a warp shares one row of Rr
+// (broadcast) and reads 32 columns of the staged, rotated multipoles (row
+// stride p + 1: conflict-free).
 template <typename R>
 __global__ void k_m2l(int b0, const int* v_off, const int* v_src, const int* v_code,
-                      const cplx_t<R>* M, int ldm, double inv_side, int nc, int p,
+                      const R* Mr, const cplx_t<R>* Mph, int ldm, double inv_side, int nc, int p,
                       const cplx_t<R>* me, cplx_t<R>* le) {
   using V = cplx_t<R>;
   __shared__ V sm_me[kCols * (kMaxP + 1)];
-  __shared__ V sm_M[kMaxP * kMaxP];
+  __shared__ R sm_R[kMaxP * kMaxP];
   const int g = b0 + blockIdx.x;
   const int nout = p * nc;
   const int ld = p + 1;
@@ -210,22 +216,27 @@ __global__ void k_m2l(int b0, const int* v_off, const int* v_src, const int* v_c
   for (int v = v_off[g]; v < v_off[g + 1]; v++) {
     __syncthreads();
     const V* src = me + (size_t)v_src[v] * nout;
+    const int code = v_code[v];
+    const V* ph = Mph + (size_t)code * (ldm + 1);   // e^(i phi k), k = 0..ldm
     for (int e = threadIdx.x; e < nout; e += blockDim.x) {
       const int k = e % p, cc = e / p;
-      sm_me[cc * ld + k] = src[e];
+      sm_me[cc * ld + k] = cmul(ph[k], src[e]);
     }
-    const V* Mm = M + (size_t)v_code[v] * ldm * ldm;
-    for (int e = threadIdx.x; e < p * p; e += blockDim.x) sm_M[e] = Mm[(size_t)(e / p) * ldm + e % p];
+    const R* Rm = Mr + (size_t)code * ldm * ldm;
+    for (int e = threadIdx.x; e < p * p; e += blockDim.x) sm_R[e] = Rm[(size_t)(e / p) * ldm + e % p];
     __syncthreads();
     for (int r = 0; r < 4; r++) {
       int o = threadIdx.x + r * blockDim.x;
       if (o >= nout) break;
       const int cc = o % nc, m = o / nc;
-      V a = acc[r];
-      const V* row = sm_M + m * p;
+      V cm = czero<V>();
+      const R* row = sm_R + m * p;
       const V* x = sm_me + cc * ld;
-      for (int k = 0; k < p; k++) a = cfma(row[k], x[k], a);
-      acc[r] = a;
+      for (int k = 0; k < p; k++) {
+        cm.x = fmx(row[k], x[k].x, cm.x);
+        cm.y = fmx(row[k], x[k].y, cm.y);
+      }
+      acc[r] = cfma(ph[m + 1], cm, acc[r]);
     }
   }
   const R is = (R)inv_side;
@@ -297,19 +308,21 @@ __device__ __forceinline__ void near_load(const double2* z, const float4*, int i
 __device__ __forceinline__ void near_load(const double2*, const float4* zf, int i, float4* out) {
   *out = zf[i];
 }
-// (1/(t - s)) as (rx, ry) = (dx, -dy) / |t - s|^2
-__device__ __forceinline__ void near_recip(const double2& t, const double2& s, double* rx,
-                                           double* ry) {
+// The Nystrom entry Re(nw_s / (t - s)) = (nw_s . (t - s)) / |t - s|^2 of a
+// target t and a source s with nw_s = -(w_s / 2 pi) n_s.
+__device__ __forceinline__ double near_entry(const double2& t, const double2& s, double2 nws) {
   const double dx = t.x - s.x, dy = t.y - s.y;
-  const double inv = recip_nr(dx * dx + dy * dy);
-  *rx = dx * inv;
-  *ry = -dy * inv;
+  return (nws.x * dx + nws.y * dy) * recip_nr(dx * dx + dy * dy);
 }
-__device__ __forceinline__ void near_recip(const float4& t, const float4& s, float* rx, float* ry) {
+__device__ __forceinline__ float near_entry(const float4& t, const float4& s, float2 nws) {
   const float dx = (t.x - s.x) + (t.z - s.z), dy = (t.y - s.y) + (t.w - s.w);
-  const float inv = __frcp_rn(dx * dx + dy * dy);
-  *rx = dx * inv;
-  *ry = -dy * inv;
+  return (nws.x * dx + nws.y * dy) * __frcp_rn(dx * dx + dy * dy);
+}
+__device__ __forceinline__ void near_nw(const double2* nw, const float2*, int i, double2* out) {
+  *out = nw[i];
+}
+__device__ __forceinline__ void near_nw(const double2*, const float2* nw32, int i, float2* out) {
+  *out = nw32[i];
 }
 
 // Per leaf: far field from the local expansion, near field by direct
@@ -325,7 +338,9 @@ __device__ __forceinline__ void near_recip(const float4& t, const float4& s, flo
 // each 32-source chunk are formed once in shared memory (one entry per
 // thread) and broadcast to the lanes; charges and local expansions are read
 // [point or term][column] (conflict-free).  The output goes through shared
-// memory so that a warp writes 32 targets of one column.
+// memory so that a warp writes 32 targets of one column.  The near field is
+// the real Nystrom matrix times the real densities: one entry per pair, one
+// FMA per pair and column.
 constexpr int kLeafThreads = 128;
 constexpr int kLeafWarps = kLeafThreads / 32;
 constexpr int kPassTargets = 32;
@@ -338,15 +353,19 @@ template <typename R>
 __global__ void __launch_bounds__(kLeafThreads)
     k_leaf_eval(const int* leaf_start, const int* leaf_box, const int* near_off,
                 const int* near_leaf, const double2* centre, double side, const double2* z,
-                const float4* zf, const double* diag, const int* perm, const cplx_t<R>* q,
-                const cplx_t<R>* le, int nc, int p, const double* mu, int ldmu, int c0,
-                double* y, int ldy) {
+                const float4* zf, const double2* nw, const float2* nw32, const double* diag,
+                const int* perm, const R* u, const cplx_t<R>* le, int nc, int p,
+                const double* mu, int ldmu, int c0, double* y, int ldy) {
   using V = cplx_t<R>;
   using P = typename NearPt<R>::type;
-  __shared__ V bufA[kPassTargets * kMaxP];   // powers [t][m], then entries [t][s]
-  __shared__ V bufB[kSrcChunk * kCols];      // local expansion [m][c], charges [s][c], output
+  using W = cplx_t<R>;   // nw_s in the arithmetic type
+  __shared__ V bufA[kPassTargets * kMaxP];   // powers [t][m] (complex), then entries [t][s] (real)
+  __shared__ V bufB[kSrcChunk * kCols];      // local expansion [m][c], densities [s][c] (real), output
   __shared__ P st[kPassTargets];
   __shared__ P ss[kSrcChunk];
+  __shared__ W snw[kSrcChunk];
+  R* ent = reinterpret_cast<R*>(bufA);
+  R* dens = reinterpret_cast<R*>(bufB);
   const int lf = blockIdx.x, g = leaf_box[lf];
   const int t0 = leaf_start[lf], t1 = leaf_start[lf + 1];
   const double2 c = centre[g];
@@ -389,39 +408,34 @@ __global__ void __launch_bounds__(kLeafThreads)
         }
       }
     }
-    // near field: Re sum_s q_s / (t - s)
+    // near field: sum_s Re(nw_s / (t - s)) mu_s, one real entry per pair
     for (int v = near_off[lf]; v < near_off[lf + 1]; v++) {
       const int sl = near_leaf[v];
       const int s0 = leaf_start[sl], s1 = leaf_start[sl + 1];
       for (int base = s0; base < s1; base += kSrcChunk) {
         const int cnt = min(kSrcChunk, s1 - base);
         __syncthreads();   // readers of bufA / bufB done
-        for (int i = threadIdx.x; i < cnt; i += blockDim.x) near_load(z, zf, base + i, &ss[i]);
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+          near_load(z, zf, base + i, &ss[i]);
+          near_nw(nw, nw32, base + i, &snw[i]);
+        }
         for (int e = threadIdx.x; e < cnt * nc; e += blockDim.x) {
           const int i = e / nc, cc = e % nc;
-          bufB[i * kCols + cc] = q[(size_t)(base + i) * kCols + cc];
+          dens[i * kCols + cc] = u[(size_t)(base + i) * kCols + cc];
         }
         __syncthreads();
         for (int e = threadIdx.x; e < nt * cnt; e += blockDim.x) {
           const int tt = e / cnt, i = e % cnt;
-          R rx = 0, ry = 0;
-          if (tb + tt != base + i) near_recip(st[tt], ss[i], &rx, &ry);
-          V en;
-          en.x = rx;
-          en.y = ry;
-          bufA[tt * kSrcChunk + i] = en;
+          ent[tt * kSrcChunk + i] = (tb + tt != base + i) ? near_entry(st[tt], ss[i], snw[i]) : R(0);
         }
         __syncthreads();
         if (col_on) {
           for (int i = 0; i < cnt; i++) {
-            const V qv = bufB[i * kCols + lane];
+            const R dv = dens[i * kCols + lane];
 #pragma unroll
             for (int k = 0; k < kWarpTargets; k++) {
               const int tt = warp + kLeafWarps * k;
-              if (tt < nt) {
-                const V en = bufA[tt * kSrcChunk + i];
-                acc[k] = fmx(qv.x, en.x, fmx(-qv.y, en.y, acc[k]));
-              }
+              if (tt < nt) acc[k] = fmx(dv, ent[tt * kSrcChunk + i], acc[k]);
             }
           }
         }
@@ -454,6 +468,11 @@ __global__ void k_round_cplx(const double2* a, size_t count, float2* out) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count;
        e += (size_t)gridDim.x * blockDim.x)
     out[e] = make_float2((float)a[e].x, (float)a[e].y);
+}
+__global__ void k_round_real(const double* a, size_t count, float* out) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count;
+       e += (size_t)gridDim.x * blockDim.x)
+    out[e] = (float)a[e];
 }
 __global__ void k_split_points(const double2* z, int n, float4* out) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -589,10 +608,12 @@ struct Fmm2d {
   int *d_child = nullptr, *d_parent = nullptr, *d_child_pos = nullptr;
   int *d_v_off = nullptr, *d_v_src = nullptr, *d_v_code = nullptr;
   double2 *d_z = nullptr, *d_nw = nullptr, *d_centre = nullptr;
-  double2 *d_T = nullptr, *d_S = nullptr, *d_M = nullptr;
+  double2 *d_T = nullptr, *d_S = nullptr, *d_Mph = nullptr;
+  double* d_Mr = nullptr;
   double* d_diag = nullptr;
   // FP32 copies for the low-accuracy apply, made on its first use
-  float2 *d_T32 = nullptr, *d_S32 = nullptr, *d_M32 = nullptr;
+  float2 *d_T32 = nullptr, *d_S32 = nullptr, *d_Mph32 = nullptr, *d_nw32 = nullptr;
+  float* d_Mr32 = nullptr;
   float4* d_zf = nullptr;
   std::vector<void*> owned;
   cudaStream_t stream = nullptr;   // the upload stream; frees are ordered on it
@@ -610,7 +631,8 @@ struct Fmm2dPlan {
   double lo = 0, side0 = 0;
   std::vector<int> lvl_off, order, leaf_start, leaf_box, near_off, near_leaf, child, parent,
       child_pos, v_off, v_src, v_code;
-  std::vector<double2> z, nw, centre, T, S, M;
+  std::vector<double2> z, nw, centre, T, S, Mph;
+  std::vector<double> Mr;
   std::vector<double> diag;
 };
 
@@ -776,7 +798,8 @@ std::unique_ptr<Fmm2dPlan, Fmm2dPlanDeleter> fmm2d_plan(const double* pts, const
     }
   }
   // translation matrices
-  std::vector<double2> T(4 * (size_t)p * p), S(4 * (size_t)p * p), M(49 * (size_t)p * p);
+  std::vector<double2> T(4 * (size_t)p * p), S(4 * (size_t)p * p), Mph(49 * (size_t)(p + 1));
+  std::vector<double> Mr(49 * (size_t)p * p);
   for (int pos = 0; pos < 4; pos++) {
     // child offset from the parent centre in units of the parent side
     std::complex<double> d((pos & 2) ? 0.25 : -0.25, (pos & 1) ? 0.25 : -0.25);
@@ -793,12 +816,18 @@ std::unique_ptr<Fmm2dPlan, Fmm2dPlanDeleter> fmm2d_plan(const double* pts, const
     for (int dj = -3; dj <= 3; dj++) {
       int code = (di + 3) * 7 + (dj + 3);
       if (std::abs(di) <= 1 && std::abs(dj) <= 1) continue;
-      std::complex<double> rho = 1.0 / std::complex<double>(di, dj);
+      // rho = 1/d = |rho| e^(i phi): real part Rr(m, k) = (-1)^m C(k+m, m)
+      // |rho|^(k+m+1), phases e^(i phi k) for k = 0..p
+      const std::complex<double> rho = 1.0 / std::complex<double>(di, dj);
+      const double ar = std::abs(rho), phi = std::arg(rho);
       for (int m = 0; m < p; m++)
-        for (int k = 0; k < p; k++) {
-          std::complex<double> v = rho * binom(k + m, m) * ((m & 1) ? -1.0 : 1.0) * std::pow(rho, k + m);
-          M[(size_t)code * p * p + (size_t)m * p + k] = make_double2(v.real(), v.imag());
-        }
+        for (int k = 0; k < p; k++)
+          Mr[(size_t)code * p * p + (size_t)m * p + k] =
+              binom(k + m, m) * ((m & 1) ? -1.0 : 1.0) * std::pow(ar, k + m + 1);
+      for (int k = 0; k <= p; k++) {
+        const std::complex<double> e = std::polar(1.0, phi * k);
+        Mph[(size_t)code * (p + 1) + k] = make_double2(e.real(), e.imag());
+      }
     }
   // sorted point data
   std::vector<double2> z(n), nw(n);
@@ -838,7 +867,8 @@ std::unique_ptr<Fmm2dPlan, Fmm2dPlanDeleter> fmm2d_plan(const double* pts, const
   F->centre = std::move(centre);
   F->T = std::move(T);
   F->S = std::move(S);
-  F->M = std::move(M);
+  F->Mr = std::move(Mr);
+  F->Mph = std::move(Mph);
   F->diag = std::move(dg);
   return F;
 }
@@ -873,7 +903,8 @@ std::unique_ptr<Fmm2d, Fmm2dDeleter> fmm2d_upload(const Fmm2dPlan& P, cudaStream
   F->d_centre = upload_vec(P.centre, &F->owned, s);
   F->d_T = upload_vec(P.T, &F->owned, s);
   F->d_S = upload_vec(P.S, &F->owned, s);
-  F->d_M = upload_vec(P.M, &F->owned, s);
+  F->d_Mr = upload_vec(P.Mr, &F->owned, s);
+  F->d_Mph = upload_vec(P.Mph, &F->owned, s);
   F->d_diag = upload_vec(P.diag, &F->owned, s);
   KI_FMM_CUDA(cudaStreamSynchronize(s));
   return F;
@@ -900,7 +931,16 @@ void ensure_fp32(Fmm2d& F, cudaStream_t s) {
   const size_t pp = (size_t)F.p * F.p;
   F.d_T32 = round(F.d_T, 4 * pp);
   F.d_S32 = round(F.d_S, 4 * pp);
-  F.d_M32 = round(F.d_M, 49 * pp);
+  F.d_Mph32 = round(F.d_Mph, 49 * (size_t)(F.p + 1));
+  F.d_nw32 = round(F.d_nw, (size_t)F.n);
+  {
+    float* d = nullptr;
+    const size_t count = 49 * pp;
+    KI_FMM_CUDA(pool_malloc((void**)&d, sizeof(float) * count, s));
+    F.owned.push_back(d);
+    k_round_real<<<(int)std::min<size_t>(1024, (count + 255) / 256), 256, 0, s>>>(F.d_Mr, count, d);
+    F.d_Mr32 = d;
+  }
   float4* zf = nullptr;
   KI_FMM_CUDA(pool_malloc((void**)&zf, sizeof(float4) * (size_t)F.n, s));
   F.owned.push_back(zf);
@@ -910,37 +950,44 @@ void ensure_fp32(Fmm2d& F, cudaStream_t s) {
 }
 
 template <typename R>
-void apply_impl(Fmm2d& F, const cplx_t<R>* T, const cplx_t<R>* S, const cplx_t<R>* M,
+void apply_impl(Fmm2d& F, const cplx_t<R>* T, const cplx_t<R>* S, const R* Mr,
+                const cplx_t<R>* Mph,
                 const double* mu, int ldmu, int ncols, double* y, int ldy, cudaStream_t s, int p,
                 StageRecorder* rec, const char* const* names) {
   using V = cplx_t<R>;
   const int n = F.n, L = F.L, nbox = F.nbox, ldm = F.p;
   const int nc_max = std::min(ncols, kCols);
-  V *q = nullptr, *me = nullptr, *le = nullptr;
-  KI_FMM_CUDA(pool_malloc((void**)&q, sizeof(V) * (size_t)n * kCols, s));
+  R* q = nullptr;
+  V *me = nullptr, *le = nullptr;
+  KI_FMM_CUDA(pool_malloc((void**)&q, sizeof(R) * (size_t)n * kCols, s));
   KI_FMM_CUDA(pool_malloc((void**)&me, sizeof(V) * (size_t)nbox * p * nc_max, s));
   KI_FMM_CUDA(pool_malloc((void**)&le, sizeof(V) * (size_t)nbox * p * nc_max, s));
   for (int c0 = 0; c0 < ncols; c0 += kCols) {
     const int nc = std::min(kCols, ncols - c0);
-    // algorithmic flops (complex FMA = 8): P2M n p, M2M p(p+1)/2 per child
-    // link, M2L p^2 per interaction pair, L2L p(p+1)/2 per box below level 2,
-    // near field 4 nc + 12 per point pair, local expansion n p (4 nc + 6)
+    // algorithmic flops per column (complex FMA = 8, real-by-complex = 4):
+    // P2M 4 n p (+ 6 n p column-independent), M2M 8 p(p+1)/2 per child link,
+    // M2L (rotated) 4 p^2 + 14 p per interaction pair, L2L 8 p(p+1)/2 per box
+    // below level 2, near field 2 per point pair (+ 12 per pair for the
+    // entry), local expansion 4 n p (+ 6 n p)
     const double pp = p, cx = nc;
     const int nl2 = F.lvl_off[L + 1] - F.lvl_off[3 > L ? L + 1 : 3];
-    if (rec) rec->begin(names[0], 8.0 * cx * ((double)n * pp + (double)(nbox - 1) * pp * (pp + 1) / 2));
-    k_charges<R><<<(n + 31) / 32, dim3(32, 8), 0, s>>>(F.d_nw, F.d_perm, n, mu, ldmu, c0, nc, q);
+    if (rec) rec->begin(names[0], (double)n * pp * (4.0 * cx + 6.0) +
+                                  8.0 * cx * (double)(nbox - 1) * pp * (pp + 1) / 2);
+    k_densities<R><<<(n + 31) / 32, dim3(32, 8), 0, s>>>(F.d_perm, n, mu, ldmu, c0, nc, q);
     k_p2m<R><<<F.nleaf, 256, 0, s>>>(F.d_leaf_start, F.d_leaf_box, F.d_centre,
-                                     F.side0 / (double)(1L << L), F.d_z, q, n, nc, p, me);
+                                     F.side0 / (double)(1L << L), F.d_z, F.d_nw, q, nc, p, me);
     for (int l = L; l >= 1; l--) {
       const int b0 = F.lvl_off[l - 1], cnt = F.lvl_off[l] - b0;
       k_m2m<R><<<cnt, 256, 0, s>>>(b0, F.d_child, F.d_child_pos, T, ldm, nc, p, me);
     }
     if (rec) rec->end();
     KI_FMM_CUDA(cudaMemsetAsync(le, 0, sizeof(V) * (size_t)F.lvl_off[2] * p * nc, s));
-    if (rec) rec->begin(names[1], 8.0 * cx * (double)F.m2l_pairs * pp * pp);
+    // M2L in rotated form: p^2 real-by-complex products (4 flops) and 2p
+    // complex rotations per pair and column
+    if (rec) rec->begin(names[1], cx * (double)F.m2l_pairs * (4.0 * pp * pp + 14.0 * pp));
     for (int l = 2; l <= L; l++) {
       const int b0 = F.lvl_off[l], cnt = F.lvl_off[l + 1] - b0;
-      k_m2l<R><<<cnt, 256, 0, s>>>(b0, F.d_v_off, F.d_v_src, F.d_v_code, M, ldm,
+      k_m2l<R><<<cnt, 256, 0, s>>>(b0, F.d_v_off, F.d_v_src, F.d_v_code, Mr, Mph, ldm,
                                    (double)(1L << l) / F.side0, nc, p, me, le);
     }
     if (rec) rec->end();
@@ -950,12 +997,12 @@ void apply_impl(Fmm2d& F, const cplx_t<R>* T, const cplx_t<R>* S, const cplx_t<R
       k_l2l<R><<<cnt, 256, 0, s>>>(b0, F.d_parent, F.d_child_pos, S, ldm, nc, p, le);
     }
     if (rec) rec->end();
-    if (rec) rec->begin(names[3], (double)F.near_point_pairs * (4.0 * cx + 12.0) +
+    if (rec) rec->begin(names[3], (double)F.near_point_pairs * (2.0 * cx + 12.0) +
                                   (double)n * pp * (4.0 * cx + 6.0));
     k_leaf_eval<R><<<F.nleaf, kLeafThreads, 0, s>>>(
         F.d_leaf_start, F.d_leaf_box, F.d_near_off, F.d_near_leaf, F.d_centre,
-        F.side0 / (double)(1L << L), F.d_z, F.d_zf, F.d_diag, F.d_perm, q, le, nc, p, mu, ldmu,
-        c0, y, ldy);
+        F.side0 / (double)(1L << L), F.d_z, F.d_zf, F.d_nw, F.d_nw32, F.d_diag, F.d_perm, q, le,
+        nc, p, mu, ldmu, c0, y, ldy);
     if (rec) rec->end();
     KI_FMM_CUDA(cudaGetLastError());
   }
@@ -972,10 +1019,12 @@ void fmm2d_apply(Fmm2d& F, const double* mu, int ldmu, int ncols, double* y, int
   if (arith == FmmArith::kF32) {
     static const char* const names[4] = {"fmm32_upward", "fmm32_m2l", "fmm32_l2l", "fmm32_near"};
     ensure_fp32(F, s);
-    apply_impl<float>(F, F.d_T32, F.d_S32, F.d_M32, mu, ldmu, ncols, y, ldy, s, p, rec, names);
+    apply_impl<float>(F, F.d_T32, F.d_S32, F.d_Mr32, F.d_Mph32, mu, ldmu, ncols, y, ldy, s, p,
+                      rec, names);
   } else {
     static const char* const names[4] = {"fmm_upward", "fmm_m2l", "fmm_l2l", "fmm_near"};
-    apply_impl<double>(F, F.d_T, F.d_S, F.d_M, mu, ldmu, ncols, y, ldy, s, p, rec, names);
+    apply_impl<double>(F, F.d_T, F.d_S, F.d_Mr, F.d_Mph, mu, ldmu, ncols, y, ldy, s, p, rec,
+                       names);
   }
 }
 
