@@ -493,15 +493,41 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
         sgn[idx] = x;
       }
       __syncthreads();
-      for (int idx = tid; idx < lsk * n; idx += nth) {
-        const int q = idx / n, c = idx % n;
-        T acc = T(0);
-#pragma unroll 8
-        for (int i = 0; i < FR; i++) {
-          const T b = B[(size_t)i * ldB + c];
-          acc += ((sgn[i * words + (q >> 5)] >> (q & 31)) & 1u) ? -b : b;
+      // Y += S_B B with threads on (8 sketch rows, 1 column) tiles: one load
+      // of B(i, c) serves 8 rows.  The signs as +-1 entries (FMAs) in rows
+      // lsk.. of R, unused while sketching, when they fit; else bit tests.
+      const int lq = (lsk + 7) & ~7;
+      T* Sf = ((size_t)(n - lsk) * ldR >= (size_t)FR * lq) ? R + (size_t)lsk * ldR : nullptr;
+      if (Sf) {
+        for (int e = tid; e < FR * lq; e += nth) {
+          const int i = e / lq, q = e % lq;
+          Sf[e] = (q < lsk && ((sgn[i * words + (q >> 5)] >> (q & 31)) & 1u)) ? T(-1) : T(1);
         }
-        R[(size_t)q * ldR + c] += acc;
+        __syncthreads();
+      }
+      for (int it = tid; it < (lq / 8) * n; it += nth) {
+        const int c = it % n, q0 = (it / n) * 8;
+        T acc[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) acc[u] = T(0);
+        if (Sf) {
+          for (int i = 0; i < FR; i++) {
+            const T b = B[(size_t)i * ldB + c];
+            const T* srow = Sf + (size_t)i * lq + q0;
+#pragma unroll
+            for (int u = 0; u < 8; u++) acc[u] = fma(srow[u], b, acc[u]);
+          }
+        } else {
+          for (int i = 0; i < FR; i++) {
+            const T b = B[(size_t)i * ldB + c];
+            const uint32_t bits = sgn[i * words + (q0 >> 5)] >> (q0 & 31);
+#pragma unroll
+            for (int u = 0; u < 8; u++) acc[u] += ((bits >> u) & 1u) ? -b : b;
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+          if (q0 + u < lsk) R[(size_t)(q0 + u) * ldR + c] += acc[u];
       }
     }
     __syncthreads();
@@ -695,7 +721,18 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
         for (; i < rowsR; i++) w0 += hu[i] * R[(size_t)i * ldR + c];
         T w = ((w0 + w1) + (w2 + w3)) * tau;
         R[(size_t)j * ldR + c] -= w;
-        for (int q = j + 1; q < rowsR; q++) R[(size_t)q * ldR + c] -= w * hu[q];
+        // four rows per step with the loads issued together (the global-
+        // memory modes would otherwise wait one round trip per row)
+        int q = j + 1;
+        for (; q + 3 < rowsR; q += 4) {
+          T* r0 = R + (size_t)q * ldR + c;
+          const T a0 = r0[0], a1 = r0[ldR], a2 = r0[2 * (size_t)ldR], a3 = r0[3 * (size_t)ldR];
+          r0[0] = a0 - w * hu[q];
+          r0[ldR] = a1 - w * hu[q + 1];
+          r0[2 * (size_t)ldR] = a2 - w * hu[q + 2];
+          r0[3 * (size_t)ldR] = a3 - w * hu[q + 3];
+        }
+        for (; q < rowsR; q++) R[(size_t)q * ldR + c] -= w * hu[q];
       }
       // norm downdate of column c (xLAQP2), recomputed after cancellation
       T rjc = R[(size_t)j * ldR + c];
@@ -736,6 +773,7 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   for (int c = k + tid; c < n; c += nth) {
     for (int i = k - 1; i >= 0; i--) {
       T s = R[(size_t)i * ldR + c];
+#pragma unroll 8
       for (int l = i + 1; l < k; l++) s -= R[(size_t)i * ldR + l] * R[(size_t)l * ldR + c];
       R[(size_t)i * ldR + c] = s / R[(size_t)i * ldR + i];
     }
