@@ -238,6 +238,64 @@ __device__ R border_u(int dim, int sol_dim, int comp, int k, const R* r) {
 // offsets from the hole centres are formed in FP64).
 constexpr int kBorderCols = 32;
 
+// y (column-major, ldy) += U alpha for every DOF (points SoA, stride 1), the
+// tiled form: a CTA takes 32 DOFs, forms their U entries once into shared
+// memory (32 x nb), stages alpha 32 columns at a time, and lanes are columns
+// with warps on DOFs (the U entry broadcast, alpha conflict-free); the tile
+// goes out through shared memory so that a warp writes 32 DOFs of one
+// column.  Shared memory: sizeof(R) * (32 (nb + 1) + 32 nb + 32 * 33).
+constexpr int kBorderTile = 32;
+template <typename R>
+size_t border_tile_smem(int nb) {
+  return sizeof(R) * ((size_t)kBorderTile * (nb + 1) + (size_t)nb * 32 + kBorderTile * 33);
+}
+template <typename R>
+__global__ void __launch_bounds__(256) k_border_apply_tile(const double* px, const double* py,
+                                                           const double* pz, int n_points, int dim,
+                                                           int sol_dim, const double* hc, int nh,
+                                                           const double* alpha, int lda, int ncols,
+                                                           double* y, int ldy) {
+  extern __shared__ __align__(16) unsigned char bt_smem[];
+  const int cph = sol_dim == 1 ? 1 : (dim == 2 ? 3 : 6);
+  const int nb = nh * cph;
+  R* Us = reinterpret_cast<R*>(bt_smem);                 // [DOF][nb + 1]
+  R* As = Us + (size_t)kBorderTile * (nb + 1);           // [b][32]
+  R* out = As + (size_t)nb * 32;                         // [DOF][33]
+  const int N = n_points * sol_dim;
+  const int d0 = blockIdx.x * kBorderTile;
+  const int nd = min(kBorderTile, N - d0);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int e = threadIdx.x; e < nd * nb; e += blockDim.x) {
+    const int q = e / nb, b = e % nb;
+    const int dof = d0 + q, p = dof / sol_dim, comp = dof - sol_dim * p;
+    const int h = b / cph, kk = b - cph * h;
+    const double xp[3] = {px[p], py[p], dim == 3 ? pz[p] : 0.0};
+    R rr[3];
+    for (int d = 0; d < dim; d++) rr[d] = R(xp[d] - hc[dim * h + d]);
+    Us[(size_t)q * (nb + 1) + b] = border_u<R>(dim, sol_dim, comp, kk, rr);
+  }
+  for (int c0 = 0; c0 < ncols; c0 += 32) {
+    const int nc = min(32, ncols - c0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nb * 32; e += blockDim.x) {
+      const int b = e / 32, c = e % 32;
+      As[e] = c < nc ? R(alpha[b + (size_t)lda * (c0 + c)]) : R(0);
+    }
+    __syncthreads();
+    for (int q = warp; q < nd; q += nw) {
+      const R* u = Us + (size_t)q * (nb + 1);
+      R acc = R(0);
+      for (int b = 0; b < nb; b++) acc += u[b] * As[b * 32 + lane];
+      out[q * 33 + lane] = acc;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nd * nc; e += blockDim.x) {
+      const int c = e / nd, q = e % nd;
+      y[(d0 + q) + (size_t)ldy * (c0 + c)] += double(out[q * 33 + c]);
+    }
+  }
+}
+
 template <typename R = double>
 __global__ void k_border_apply(const double* px, const double* py, const double* pz, int stride,
                                int n_points, int dim, int sol_dim, const double* hc, int nh,
@@ -986,10 +1044,20 @@ void apply_bordered(ki_factor* f, const double* mu, const double* alpha, int nco
             fast ? fmm_order_for(target, ki::fmm2d_order(fmm_for(f, s))) : 0, rec);
   if (nb > 0) {
     if (rec) rec->begin("border_apply", 0);
-    auto border = low ? k_border_apply<float> : k_border_apply<double>;
-    border<<<(N + 127) / 128, 128, 0, s>>>(f->P.x, f->P.y, f->P.z, 1, f->n_points, f->dim,
-                                           f->sol_dim, f->d_holes, f->n_holes, alpha, nb, ncols,
-                                           y1, N, nullptr, 0);
+    const size_t tsm = low ? border_tile_smem<float>(nb) : border_tile_smem<double>(nb);
+    if (tsm <= 100 * 1024) {
+      auto tile = low ? k_border_apply_tile<float> : k_border_apply_tile<double>;
+      KI_CHECK_CUDA(cudaFuncSetAttribute(tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         100 * 1024));
+      tile<<<(N + kBorderTile - 1) / kBorderTile, 256, tsm, s>>>(
+          f->P.x, f->P.y, f->P.z, f->n_points, f->dim, f->sol_dim, f->d_holes, f->n_holes, alpha,
+          nb, ncols, y1, N);
+    } else {
+      auto border = low ? k_border_apply<float> : k_border_apply<double>;
+      border<<<(N + 127) / 128, 128, 0, s>>>(f->P.x, f->P.y, f->P.z, 1, f->n_points, f->dim,
+                                             f->sol_dim, f->d_holes, f->n_holes, alpha, nb, ncols,
+                                             y1, N, nullptr, 0);
+    }
     const int cph = nb / f->n_holes;
     k_psi_apply<<<dim3(nb, ncols), 256, 0, s>>>(f->d_pts, f->P.w, f->dim, f->sol_dim, f->d_holes,
                                                 f->d_hstart, f->d_hcount, cph, mu, N, alpha, nb,

@@ -319,6 +319,11 @@ __device__ __forceinline__ T id_entry(const Points<T>& P, int sol_dim, int row, 
 __device__ __forceinline__ long long norm_key(double v) { return __double_as_longlong(v); }
 __device__ __forceinline__ long long norm_key(float v) { return (long long)__float_as_int(v); }
 
+// Resident CTAs per SM k_id is compiled for: three in FP32 (the register
+// budget of the register-tiled sketch fold would otherwise allow two), two
+// in FP64 (no register spills).
+template <typename T> constexpr int kIdMinBlocks = sizeof(T) == 4 ? 3 : 2;
+
 // Interpolative decomposition of one box per CTA.
 //
 // Thread-per-column formulation: every dot product and update runs inside
@@ -329,7 +334,7 @@ __device__ __forceinline__ long long norm_key(float v) { return (long long)__flo
 //   B (32 x ldB) | hu (2 x 32 Householder tails) | vn1 (n) | vn2 (n) | perm (n) |
 //   R (n x ldR) when it fits (mode 0); mode 1 keeps R in the global scratch.
 template <typename T, int FR>
-__global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_base,
+__global__ void __launch_bounds__(kThreads, kIdMinBlocks<T>) k_id(const IdTask* tasks, int task_base,
                                                   const int64_t* seg_off, const int* seg_len,
                                                   int* ipool, int* iscratch, T* tws, Points<T> P,
                                                   int sol_dim, ProxyTab<T> px, double tol, int* k_out,
@@ -352,6 +357,15 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   __shared__ int s_scan[64];
   __shared__ int s_piv, s_k;
   __shared__ T s_tau[2], s_beta;
+
+  // the box's centre split hi + lo with the proxy and filter radii, formed
+  // once (FP64 arithmetic, slow in the FP32 kernels when every thread does it)
+  __shared__ ProxyBox<T> s_boxes[2];
+  if (tid == 0) {
+    s_boxes[0] = proxy_box<T>(t.cx, t.cy, t.cz, t.rad_proxy, px.n);
+    s_boxes[1] = proxy_box<T>(t.cx, t.cy, t.cz, t.rad_filter, 1);
+  }
+  __syncthreads();
 
   int* rows = iscratch + t.rows;
   const int* act = ipool + t.act;
@@ -386,7 +400,7 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   if (flags & 1) {
   if (tid == 0) s_cnt = 0;
   // the box centre split hi + lo and the filter radius, for the FP32 filter
-  const ProxyBox<T> cb = proxy_box<T>(t.cx, t.cy, t.cz, t.rad_filter, 1);
+  const ProxyBox<T> cb = s_boxes[1];
   __syncthreads();
   for (int s = t.seg_begin; s < t.seg_end; s++) {
     const int* src = ipool + seg_off[s];
@@ -474,7 +488,7 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
   }
   if (sketch_fold) {
     for (int idx = tid; idx < lsk * n; idx += nth) R[(idx / n) * (size_t)ldR + idx % n] = T(0);
-    const ProxyBox<T> pb = proxy_box<T>(t.cx, t.cy, t.cz, t.rad_proxy, px.n);
+    const ProxyBox<T> pb = s_boxes[0];
     uint32_t* sgn = reinterpret_cast<uint32_t*>(hu);   // FR rows x ceil(lsk/32) words
     const int words = (lsk + 31) >> 5;
     for (int r0 = 0; r0 < m; r0 += FR) {
@@ -572,7 +586,7 @@ __global__ void __launch_bounds__(kThreads) k_id(const IdTask* tasks, int task_b
       RF[rowbase(j) + j] = beta;
     }
   };
-  const ProxyBox<T> pbox = proxy_box<T>(t.cx, t.cy, t.cz, t.rad_proxy, px.n);
+  const ProxyBox<T> pbox = s_boxes[0];
   for (int r0 = 0; (flags & 2) && r0 < m; r0 += FR) {
     for (int idx = tid; idx < FR * n; idx += nth) {
       int j = idx % n, i = idx / n;
@@ -1253,13 +1267,16 @@ __global__ void __launch_bounds__(kThreads) k_schur(const SchurTask<T>* tasks, i
   extern __shared__ __align__(16) unsigned char sc_smem[];
   const SchurTask<T> t = tasks[task_base + blockIdx.x];
   const int n = t.n, k = t.k, r = n - k;
+  // r-row blocks in shared memory use an odd leading dimension, so that
+  // threads stepping along a row (transposed operands) hit distinct banks
+  const int ld = smem ? (r | 1) : r;
   __shared__ T s_red, s_val[2];
   __shared__ int s_idx, s_flag;
   T* base = smem ? reinterpret_cast<T*>(sc_smem) : t.ws;
   T* Kss = base;                      // k x k
   T* Wrs = Kss + (size_t)k * k;       // r x k : K_rs, then K~_rs, then U
-  T* Lt = Wrs + (size_t)r * k;        // r x k : K_sr^T, then K~_sr^T, then L^T
-  T* X = smem ? Lt + (size_t)r * k : t.X;   // r x r
+  T* Lt = Wrs + (size_t)ld * k;       // r x k : K_sr^T, then K~_sr^T, then L^T
+  T* X = smem ? Lt + (size_t)ld * k : t.X;   // r x r
   const int* pm = t.perm;
   for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) {
     const int i = idx % k, j = idx / k;
@@ -1267,45 +1284,45 @@ __global__ void __launch_bounds__(kThreads) k_schur(const SchurTask<T>* tasks, i
   }
   for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
     const int i = idx % r, j = idx / r;
-    Wrs[idx] = t.K[pm[k + i] + (size_t)n * pm[j]];   // K_rs(i, j)
-    Lt[idx] = t.K[pm[j] + (size_t)n * pm[k + i]];    // K_sr(j, i)
+    Wrs[i + (size_t)ld * j] = t.K[pm[k + i] + (size_t)n * pm[j]];   // K_rs(i, j)
+    Lt[i + (size_t)ld * j] = t.K[pm[j] + (size_t)n * pm[k + i]];    // K_sr(j, i)
   }
   for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) {
     const int i = idx % r, j = idx / r;
-    X[idx] = t.K[pm[k + i] + (size_t)n * pm[k + j]];
+    X[i + (size_t)ld * j] = t.K[pm[k + i] + (size_t)n * pm[k + j]];
   }
   for (int idx = threadIdx.x; idx < k * r; idx += blockDim.x) t.Tout[idx] = t.Tin[idx];
   __syncthreads();
   const T* Tm = t.Tin;
-  // X -= T^T K_sr  (K_sr(l, j) = Lt[j + r l])
-  cta_gemm<T>(r, r, k, T(-1), Tm, k, true, Lt, r, true, T(1), X, r);
+  // X -= T^T K_sr  (K_sr(l, j) = Lt[j + ld l])
+  cta_gemm<T>(r, r, k, T(-1), Tm, k, true, Lt, ld, true, T(1), X, ld);
   __syncthreads();
   // K~_rs = K_rs - T^T K_ss ;  K~_sr^T = K_sr^T - T^T K_ss^T
-  cta_gemm<T>(r, k, k, T(-1), Tm, k, true, Kss, k, false, T(1), Wrs, r);
-  cta_gemm<T>(r, k, k, T(-1), Tm, k, true, Kss, k, true, T(1), Lt, r);
+  cta_gemm<T>(r, k, k, T(-1), Tm, k, true, Kss, k, false, T(1), Wrs, ld);
+  cta_gemm<T>(r, k, k, T(-1), Tm, k, true, Kss, k, true, T(1), Lt, ld);
   __syncthreads();
   // X -= K~_rs T
-  cta_gemm<T>(r, r, k, T(-1), Wrs, r, false, Tm, k, false, T(1), X, r);
+  cta_gemm<T>(r, r, k, T(-1), Wrs, ld, false, Tm, k, false, T(1), X, ld);
   __syncthreads();
   if (smem && t.gj) {
     // shared memory after X: colj (r) | X0 (r x r) | U0 (r x k) | L0 (k x r)
-    T* colj = X + (size_t)r * r;
+    T* colj = X + (size_t)ld * r;
     T* X0 = colj + r;
-    T* U0 = X0 + (size_t)r * r;
-    T* L0 = U0 + (size_t)r * k;
-    for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) X0[idx] = X[idx];
+    T* U0 = X0 + (size_t)ld * r;
+    T* L0 = U0 + (size_t)ld * k;
+    for (int idx = threadIdx.x; idx < ld * r; idx += blockDim.x) X0[idx] = X[idx];
     __syncthreads();
-    int info = cta_gj_inverse<T>(r, X, r, t.piv, colj, s_val, &s_idx);   // X <- X^-1
+    int info = cta_gj_inverse<T>(r, X, ld, t.piv, colj, s_val, &s_idx);   // X <- X^-1
     if (info != 0 && threadIdx.x == 0) atomicMax(err, (int)kDevSingular);
     // U0 = X^-1 K~_rs (r x k), L0 = K~_sr X^-1 (k x r)
-    cta_gemm<T>(r, k, r, T(1), X, r, false, Wrs, r, false, T(0), U0, r);
-    cta_gemm<T>(k, r, r, T(1), Lt, r, true, X, r, false, T(0), L0, k);
+    cta_gemm<T>(r, k, r, T(1), X, ld, false, Wrs, ld, false, T(0), U0, ld);
+    cta_gemm<T>(k, r, r, T(1), Lt, ld, true, X, ld, false, T(0), L0, k);
     __syncthreads();
     // A~ = K_ss - L0 K~_rs (the correction's share follows below)
     for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) {
       const int i = idx % k, j = idx / k;
       T acc = T(0);
-      for (int l = 0; l < r; l++) acc += L0[i + (size_t)k * l] * Wrs[l + (size_t)r * j];
+      for (int l = 0; l < r; l++) acc += L0[i + (size_t)k * l] * Wrs[l + (size_t)ld * j];
       t.Atil[idx] = Kss[idx] - acc;
     }
     __syncthreads();
@@ -1315,56 +1332,59 @@ __global__ void __launch_bounds__(kThreads) k_schur(const SchurTask<T>* tasks, i
     for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
       const int i = idx % r, j = idx / r;
       T acc = T(0);
-      for (int l = 0; l < r; l++) acc += X0[i + (size_t)r * l] * U0[l + (size_t)r * j];
-      Wrs[idx] -= acc;
+      for (int l = 0; l < r; l++) acc += X0[i + (size_t)ld * l] * U0[l + (size_t)ld * j];
+      Wrs[i + (size_t)ld * j] -= acc;
     }
     for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
-      const int j = idx % r, i = idx / r;   // Lt(j, i) = K~_sr(i, j)
+      const int jj = idx % r, i = idx / r;   // Lt(jj, i) = K~_sr(i, jj)
       T acc = T(0);
-      for (int l = 0; l < r; l++) acc += L0[i + (size_t)k * l] * X0[l + (size_t)r * j];
-      Lt[idx] -= acc;
+      for (int l = 0; l < r; l++) acc += L0[i + (size_t)k * l] * X0[l + (size_t)ld * jj];
+      Lt[jj + (size_t)ld * i] -= acc;
     }
     __syncthreads();
     // U = U0 + X^-1 RU, L = L0 + RL X^-1, A~ -= RL U0 (RL X^-1 K~_rs)
     for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
       const int i = idx % r, j = idx / r;
       T acc = T(0);
-      for (int l = 0; l < r; l++) acc += X[i + (size_t)r * l] * Wrs[l + (size_t)r * j];
-      t.U[idx] = U0[idx] + acc;
+      for (int l = 0; l < r; l++) acc += X[i + (size_t)ld * l] * Wrs[l + (size_t)ld * j];
+      t.U[idx] = U0[i + (size_t)ld * j] + acc;
     }
     for (int idx = threadIdx.x; idx < k * r; idx += blockDim.x) {
       const int i = idx % k, j = idx / k;
       T acc = T(0);
-      for (int l = 0; l < r; l++) acc += Lt[l + (size_t)r * i] * X[l + (size_t)r * j];
+      for (int l = 0; l < r; l++) acc += Lt[l + (size_t)ld * i] * X[l + (size_t)ld * j];
       t.L[idx] = L0[idx] + acc;
     }
     for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) {
       const int i = idx % k, j = idx / k;
       T acc = T(0);
-      for (int l = 0; l < r; l++) acc += Lt[l + (size_t)r * i] * U0[l + (size_t)r * j];
+      for (int l = 0; l < r; l++) acc += Lt[l + (size_t)ld * i] * U0[l + (size_t)ld * j];
       t.Atil[idx] -= acc;
     }
-    for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) t.Xi[idx] = X[idx];
+    for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x)
+      t.Xi[idx] = X[idx % r + (size_t)ld * (idx / r)];
     return;
   }
-  int info = cta_lu<T>(r, X, r, t.piv, &s_flag, &s_red, &s_idx);
+  int info = cta_lu<T>(r, X, ld, t.piv, &s_flag, &s_red, &s_idx);
   if (info != 0 && threadIdx.x == 0) atomicMax(err, (int)kDevSingular);
   // L^T = X^-T K~_sr^T
-  cta_lu_solve_par<T>(r, X, r, t.piv, true, Lt, r, k);
+  cta_lu_solve_par<T>(r, X, ld, t.piv, true, Lt, ld, k);
   // A~ = K_ss - L K~_rs  (k x k), L = Lt^T
   for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) t.Atil[idx] = Kss[idx];
   __syncthreads();
-  cta_gemm<T>(k, k, r, T(-1), Lt, r, true, Wrs, r, false, T(1), t.Atil, k);
+  cta_gemm<T>(k, k, r, T(-1), Lt, ld, true, Wrs, ld, false, T(1), t.Atil, k);
   __syncthreads();
   // U = X^-1 K~_rs (in place on Wrs)
-  cta_lu_solve_par<T>(r, X, r, t.piv, false, Wrs, r, k);
-  for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) t.U[idx] = Wrs[idx];
+  cta_lu_solve_par<T>(r, X, ld, t.piv, false, Wrs, ld, k);
+  for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x)
+    t.U[idx] = Wrs[idx % r + (size_t)ld * (idx / r)];
   for (int idx = threadIdx.x; idx < k * r; idx += blockDim.x) {
     int i = idx % k, j = idx / k;
-    t.L[idx] = Lt[j + (size_t)r * i];
+    t.L[idx] = Lt[j + (size_t)ld * i];
   }
   if (smem)
-    for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) t.X[idx] = X[idx];
+    for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x)
+      t.X[idx] = X[idx % r + (size_t)ld * (idx / r)];
 }
 
 // ------------------------------------------------- multi-CTA dense helpers --
@@ -1469,8 +1489,8 @@ void copy_block(cudaStream_t s, const T* src, int lds, int rows, int cols, bool 
 // scratch entries, plus (inverse path) X's copy, U0 and L0.
 template <typename T>
 size_t schur_bytes(int n, int k, bool inv) {
-  size_t r = n - k;
-  return sizeof(T) * ((size_t)k * k + 2 * r * k + r * r + r + (inv ? r * r + 2 * r * k : 0));
+  const size_t r = n - k, ld = (size_t)((n - k) | 1);   // k_schur's odd leading dimension
+  return sizeof(T) * ((size_t)k * k + 2 * ld * k + ld * r + r + (inv ? ld * r + ld * k + k * r : 0));
 }
 
 // SkelFactorization::decouple for a box whose working set does not fit in one

@@ -281,16 +281,15 @@ __global__ void k_l2l(int b0, const int* parent, const int* child_pos, const cpl
 }
 
 // 1/x for a positive FP64 x (a squared distance): the correctly rounded
-// single-precision reciprocal as the seed, refined by two Newton-Raphson
-// steps y <- y + y (1 - x y) (the relative error squares each step: ~1e-7,
-// ~1e-14, then FP64 rounding).  x stays within the single-precision normal
-// range (squared distances between boundary nodes of unit-scale geometry).
+// single-precision reciprocal of fl32(x) as the seed (relative error below
+// 1.2e-7), refined by one Newton-Raphson step y <- y + y (1 - x y), which
+// squares the relative error (below 1.5e-14: far under the FMM's own
+// truncation error at any order it is run with).  x stays within the
+// single-precision normal range (squared distances between boundary nodes
+// of unit-scale geometry).
 __device__ __forceinline__ double recip_nr(double x) {
-  double y = (double)__frcp_rn((float)x);
-  double e = fma(-x, y, 1.0);
-  y = fma(y, e, y);
-  e = fma(-x, y, 1.0);
-  return fma(y, e, y);
+  const double y = (double)__frcp_rn((float)x);
+  return fma(y, fma(-x, y, 1.0), y);
 }
 
 // Source coordinates staged for the near field: FP64 points, or for the FP32
