@@ -421,7 +421,7 @@ def main():
     # ---- the FP64 form at the same target residual, for the comparison
     compare = None
     if args.precision == "mixed" and not args.no_compare:
-        c = run_form("fp64", max(1, min(args.steps, 2)), 1)
+        c = run_form("fp64", max(1, min(args.steps, 3)), 2)
         compare = {"form": "fp64 factorization at ID tol %g, refined to %g" % (args.tol, args.target),
                    "ms_per_step": c["t_dev"] * 1e3, "value": N * nrhs * world / c["t_dev"],
                    "unit": "DOF/s", "refine": c["infos"][-1] if c["infos"] else None,

@@ -2095,7 +2095,13 @@ template <typename T>
 void launch_diag_all(Factorization<T>& F, T* x, int ncols, cudaStream_t s) {
   if (!F.d_all_tasks || ncols == 0) return;
   const SweepTask<T>* all = reinterpret_cast<const SweepTask<T>*>(F.d_all_tasks);
+  // the bins are independent: on the aux streams when the caller's stream is
+  // the factorization's (their fork / join order against it)
+  const bool par = s == F.stream && F.diag_bins.size() > 1;
+  if (par) F.fork();
+  int next = 0;
   for (const auto& b : F.diag_bins) {
+    cudaStream_t st = par ? F.aux[(next++) % Factorization<T>::kAux] : s;
     const int ldmax = std::max(1, b[2]) | 1;
     int cw = std::max(1, std::min(ncols, (int)(96 * 1024 / (2 * sizeof(T) * ldmax))));
     cw = std::min(cw, 32);
@@ -2107,9 +2113,10 @@ void launch_diag_all(Factorization<T>& F, T* x, int ncols, cudaStream_t s) {
     if (staged) sm += mats;
     if (sm > 48 * 1024)
       KI_CUDA(cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    k_sweep<T><<<grid, kThreads, sm, s>>>(all + b[0], x, ncols, ncols, cw, kDiag, staged);
+    k_sweep<T><<<grid, kThreads, sm, st>>>(all + b[0], x, ncols, ncols, cw, kDiag, staged);
     KI_CUDA(cudaGetLastError());
   }
+  if (par) F.join(std::min(next, Factorization<T>::kAux));
 }
 
 template <typename T>
@@ -3107,10 +3114,13 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         KI_CUDA(cudaGetLastError());
         F->stage_begin("border_sweeps", 0, 0);
         F->stage_begin("border_U_Psi", 0, 0);
+        // U~ and Psi~^T are swept independently: one aux stream each
+        F->fork();
         for (int l = L - 1; l >= 1; l--) {
-          launch_sweep<T>(*F, l, kUp, F->d_Umod, nb, s);
-          launch_sweep<T>(*F, l, kPsi, F->d_PsiTmod, nb, s);
+          launch_sweep<T>(*F, l, kUp, F->d_Umod, nb, F->aux[0]);
+          launch_sweep<T>(*F, l, kPsi, F->d_PsiTmod, nb, F->aux[1]);
         }
+        F->join(2);
         F->stage_end();
         T* dD = nullptr;
         KI_CUDA(pool_malloc((void**)&dD, Tsz * (size_t)N * nb, s));
