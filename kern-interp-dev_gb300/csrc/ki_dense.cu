@@ -229,6 +229,87 @@ __global__ void k_tri_update(const T* LU, int lda, int p, int w, int r0, int r1,
   }
 }
 
+// The whole solve L U x = P b for one 32-column chunk of B per CTA, the chunk
+// held in shared memory (n x 32, odd leading dimension): pivots, then the
+// blocked forward and backward substitutions of the launches above in one
+// kernel -- each kNb-row diagonal block staged and solved one thread per
+// column, the rows below (above) it updated by every thread.  The same
+// operations in the same order as the multi-launch path.
+template <typename T>
+size_t fused_solve_smem(int n) {
+  return sizeof(T) * ((size_t)(n | 1) * 32 + (size_t)kNb * (kNb + 1));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_lu_solve_fused(const T* LU, int n, const int* piv, T* B,
+                                                        int ldb, int nrhs) {
+  extern __shared__ __align__(16) unsigned char fs_smem[];
+  const int ldx = n | 1;
+  T* X = reinterpret_cast<T*>(fs_smem);
+  T (*D)[kNb + 1] = reinterpret_cast<T (*)[kNb + 1]>(X + (size_t)ldx * 32);
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int c0 = blockIdx.x * 32, nc = min(32, nrhs - c0);
+  for (int e = tid; e < n * nc; e += nth) {
+    const int c = e / n, i = e % n;
+    X[i + (size_t)ldx * c] = B[i + (size_t)ldb * (c0 + c)];
+  }
+  __syncthreads();
+  if (tid < nc) {
+    T* x = X + (size_t)ldx * tid;
+    for (int i = 0; i < n; i++) {
+      const int r = piv[i];
+      if (r != i) { T t = x[i]; x[i] = x[r]; x[r] = t; }
+    }
+  }
+  __syncthreads();
+  auto stage = [&](int p, int w) {
+    for (int e = tid; e < w * w; e += nth) {
+      const int i = e % w, l = e / w;
+      D[i][l] = LU[p + i + (size_t)n * (p + l)];
+    }
+    __syncthreads();
+  };
+  auto update = [&](int p, int w, int r0, int r1) {   // X(r0:r1, :) -= LU(r0:r1, p:p+w) X(p:p+w, :)
+    const int rows = r1 - r0;
+    for (int e = tid; e < rows * nc; e += nth) {
+      const int i = r0 + e % rows, c = e / rows;
+      const T* xc = X + (size_t)ldx * c + p;
+      T acc = T(0);
+      for (int l = 0; l < w; l++) acc += LU[i + (size_t)n * (p + l)] * xc[l];
+      X[i + (size_t)ldx * c] -= acc;
+    }
+    __syncthreads();
+  };
+  for (int p = 0; p < n; p += kNb) {   // L y = b (unit lower)
+    const int w = min(kNb, n - p);
+    stage(p, w);
+    if (tid < nc) {
+      T* x = X + (size_t)ldx * tid + p;
+      for (int i = 0; i < w; i++)
+        for (int l = 0; l < i; l++) x[i] -= D[i][l] * x[l];
+    }
+    __syncthreads();
+    if (p + w < n) update(p, w, p + w, n);
+  }
+  for (int p = ((n - 1) / kNb) * kNb; p >= 0; p -= kNb) {   // U x = y
+    const int w = min(kNb, n - p);
+    stage(p, w);
+    if (tid < nc) {
+      T* x = X + (size_t)ldx * tid + p;
+      for (int i = w - 1; i >= 0; i--) {
+        for (int l = i + 1; l < w; l++) x[i] -= D[i][l] * x[l];
+        x[i] /= D[i][i];
+      }
+    }
+    __syncthreads();
+    if (p > 0) update(p, w, 0, p);
+  }
+  for (int e = tid; e < n * nc; e += nth) {
+    const int c = e / n, i = e % n;
+    B[i + (size_t)ldb * (c0 + c)] = X[i + (size_t)ldx * c];
+  }
+}
+
 }  // namespace
 
 template <typename T>
@@ -252,6 +333,14 @@ void dense_lu_solve(const T* LU, int n, const int* piv, T* B, int ldb, int nrhs,
                     cudaStream_t s) {
   if (n == 0 || nrhs == 0) return;
   dim3 cb((nrhs + 127) / 128);
+  if (!trans && fused_solve_smem<T>(n) <= 160 * 1024) {
+    KI_DENSE_CUDA(cudaFuncSetAttribute(k_lu_solve_fused<T>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
+    k_lu_solve_fused<T><<<(nrhs + 31) / 32, 256, fused_solve_smem<T>(n), s>>>(LU, n, piv, B, ldb,
+                                                                             nrhs);
+    KI_DENSE_CUDA(cudaGetLastError());
+    return;
+  }
   if (!trans) {
     k_apply_piv<T><<<cb, 128, 0, s>>>(B, ldb, nrhs, piv, n, false);
     for (int p = 0; p < n; p += kNb) {       // L y = b (unit lower)

@@ -511,7 +511,9 @@ __global__ void __launch_bounds__(kThreads, kIdMinBlocks<T>) k_id(const IdTask* 
       // of B(i, c) serves 8 rows.  The signs as +-1 entries (FMAs) in rows
       // lsk.. of R, unused while sketching, when they fit; else bit tests.
       const int lq = (lsk + 7) & ~7;
-      T* Sf = ((size_t)(n - lsk) * ldR >= (size_t)FR * lq) ? R + (size_t)lsk * ldR : nullptr;
+      // 16-byte aligned start (R is), so a thread's 8 signs load as two vectors
+      const size_t s0 = ((size_t)lsk * ldR + 3) & ~size_t(3);
+      T* Sf = ((size_t)n * ldR >= s0 + (size_t)FR * lq) ? R + s0 : nullptr;
       if (Sf) {
         for (int e = tid; e < FR * lq; e += nth) {
           const int i = e / lq, q = e % lq;
@@ -528,8 +530,18 @@ __global__ void __launch_bounds__(kThreads, kIdMinBlocks<T>) k_id(const IdTask* 
           for (int i = 0; i < FR; i++) {
             const T b = B[(size_t)i * ldB + c];
             const T* srow = Sf + (size_t)i * lq + q0;
+            T sv[8];
+            if (sizeof(T) == 4) {
+              const float4 v0 = *reinterpret_cast<const float4*>(srow);
+              const float4 v1 = *reinterpret_cast<const float4*>(srow + 4);
+              sv[0] = v0.x; sv[1] = v0.y; sv[2] = v0.z; sv[3] = v0.w;
+              sv[4] = v1.x; sv[5] = v1.y; sv[6] = v1.z; sv[7] = v1.w;
+            } else {
 #pragma unroll
-            for (int u = 0; u < 8; u++) acc[u] = fma(srow[u], b, acc[u]);
+              for (int u = 0; u < 8; u++) sv[u] = srow[u];
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) acc[u] = fma(sv[u], b, acc[u]);
           }
         } else {
           for (int i = 0; i < FR; i++) {

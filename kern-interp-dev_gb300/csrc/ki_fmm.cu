@@ -150,16 +150,19 @@ __global__ void k_p2m(const int* leaf_start, const int* leaf_box, const double2*
   }
 }
 
-// Multipole of each box of one level from its children (M2M):
-// me[P] = sum_children T_pos me[C], T_pos lower triangular (matrix leading
-// dimension ldm >= p).  Each child's expansions and its matrix are staged in
-// shared memory; output (k, c) is thread c + nc k.
+// Multipole of each box of one level from its children (M2M), in rotated
+// form: with the child offset d = |d| e^(i theta) (parent-side units),
+// T(k, j) = C(k, j) 0.5^j d^(k-j) = e^(i theta k) Tr(k, j) e^(-i theta j), Tr
+// real lower triangular (leading dimension ldm >= p), so
+// me[P]_k += e^(i theta k) sum_(j<=k) Tr(k, j) (e^(-i theta j) me[C]_j).
+// Each child's rotated expansions and its Tr are staged in shared memory;
+// output (k, c) is thread c + nc k.
 template <typename R>
-__global__ void k_m2m(int b0, const int* child, const int* child_pos, const cplx_t<R>* T, int ldm,
-                      int nc, int p, cplx_t<R>* me) {
+__global__ void k_m2m(int b0, const int* child, const int* child_pos, const R* Tr,
+                      const cplx_t<R>* Tph, int ldm, int nc, int p, cplx_t<R>* me) {
   using V = cplx_t<R>;
   __shared__ V sm_x[kCols * (kMaxP + 1)];
-  __shared__ V sm_T[kMaxP * kMaxP];
+  __shared__ R sm_T[kMaxP * kMaxP];
   const int g = b0 + blockIdx.x;
   const int nout = p * nc, ld = p + 1;
   V acc[4];
@@ -168,20 +171,30 @@ __global__ void k_m2m(int b0, const int* child, const int* child_pos, const cplx
     const int ch = child[4 * g + q];
     if (ch < 0) continue;
     __syncthreads();
+    const int pos = child_pos[ch];
+    const V* ph = Tph + (size_t)pos * ldm;   // e^(i theta k)
     const V* src = me + (size_t)ch * nout;
-    for (int e = threadIdx.x; e < nout; e += blockDim.x) sm_x[(e / p) * ld + e % p] = src[e];
-    const V* Tm = T + (size_t)child_pos[ch] * ldm * ldm;
+    for (int e = threadIdx.x; e < nout; e += blockDim.x) {
+      const int j = e % p, cc = e / p;
+      V cph = ph[j];
+      cph.y = -cph.y;
+      sm_x[cc * ld + j] = cmul(cph, src[e]);
+    }
+    const R* Tm = Tr + (size_t)pos * ldm * ldm;
     for (int e = threadIdx.x; e < p * p; e += blockDim.x) sm_T[e] = Tm[(size_t)(e / p) * ldm + e % p];
     __syncthreads();
     for (int r = 0; r < 4; r++) {
       int o = threadIdx.x + r * blockDim.x;
       if (o >= nout) break;
       const int cc = o % nc, k = o / nc;
-      V a = acc[r];
-      const V* row = sm_T + k * p;
+      V ck = czero<V>();
+      const R* row = sm_T + k * p;
       const V* x = sm_x + cc * ld;
-      for (int j = 0; j <= k; j++) a = cfma(row[j], x[j], a);
-      acc[r] = a;
+      for (int jj = 0; jj <= k; jj++) {
+        ck.x = fmx(row[jj], x[jj].x, ck.x);
+        ck.y = fmx(row[jj], x[jj].y, ck.y);
+      }
+      acc[r] = cfma(ph[k], ck, acc[r]);
     }
   }
   for (int r = 0; r < 4; r++) {
@@ -251,32 +264,44 @@ __global__ void k_m2l(int b0, const int* v_off, const int* v_src, const int* v_c
   }
 }
 
-// Local expansion of each box of one level += its parent's, translated (L2L):
-// le[C] += S_pos le[P], S_pos upper triangular (leading dimension ldm); the
-// parent's expansions and the matrix staged in shared memory, output (j, c)
+// Local expansion of each box of one level += its parent's, translated (L2L),
+// in rotated form: S(j, m) = C(m, j) 0.5^j d^(m-j) = e^(-i theta j) Sr(j, m)
+// e^(i theta m), Sr real upper triangular (leading dimension ldm), so
+// le[C]_j += e^(-i theta j) sum_(m>=j) Sr(j, m) (e^(i theta m) le[P]_m); the
+// parent's rotated expansions and Sr staged in shared memory, output (j, c)
 // is thread c + nc j.
 template <typename R>
-__global__ void k_l2l(int b0, const int* parent, const int* child_pos, const cplx_t<R>* S, int ldm,
-                      int nc, int p, cplx_t<R>* le) {
+__global__ void k_l2l(int b0, const int* parent, const int* child_pos, const R* Sr,
+                      const cplx_t<R>* Tph, int ldm, int nc, int p, cplx_t<R>* le) {
   using V = cplx_t<R>;
   __shared__ V sm_x[kCols * (kMaxP + 1)];
-  __shared__ V sm_S[kMaxP * kMaxP];
+  __shared__ R sm_S[kMaxP * kMaxP];
   const int g = b0 + blockIdx.x;
   const int par = parent[g];
+  const int pos = child_pos[g];
+  const V* ph = Tph + (size_t)pos * ldm;   // e^(i theta m)
   const int nout = p * nc, ld = p + 1;
   const V* src = le + (size_t)par * nout;
-  for (int e = threadIdx.x; e < nout; e += blockDim.x) sm_x[(e / p) * ld + e % p] = src[e];
-  const V* Sm = S + (size_t)child_pos[g] * ldm * ldm;
+  for (int e = threadIdx.x; e < nout; e += blockDim.x) {
+    const int m = e % p, cc = e / p;
+    sm_x[cc * ld + m] = cmul(ph[m], src[e]);
+  }
+  const R* Sm = Sr + (size_t)pos * ldm * ldm;
   for (int e = threadIdx.x; e < p * p; e += blockDim.x) sm_S[e] = Sm[(size_t)(e / p) * ldm + e % p];
   __syncthreads();
   for (int o = threadIdx.x; o < nout; o += blockDim.x) {
     const int cc = o % nc, j = o / nc;
     const size_t dst = (size_t)g * nout + (size_t)cc * p + j;
-    V a = le[dst];
-    const V* row = sm_S + j * p;
+    V cj = czero<V>();
+    const R* row = sm_S + j * p;
     const V* x = sm_x + cc * ld;
-    for (int m = j; m < p; m++) a = cfma(row[m], x[m], a);
-    le[dst] = a;
+    for (int m = j; m < p; m++) {
+      cj.x = fmx(row[m], x[m].x, cj.x);
+      cj.y = fmx(row[m], x[m].y, cj.y);
+    }
+    V cph = ph[j];
+    cph.y = -cph.y;
+    le[dst] = cfma(cph, cj, le[dst]);
   }
 }
 
@@ -607,12 +632,12 @@ struct Fmm2d {
   int *d_child = nullptr, *d_parent = nullptr, *d_child_pos = nullptr;
   int *d_v_off = nullptr, *d_v_src = nullptr, *d_v_code = nullptr;
   double2 *d_z = nullptr, *d_nw = nullptr, *d_centre = nullptr;
-  double2 *d_T = nullptr, *d_S = nullptr, *d_Mph = nullptr;
-  double* d_Mr = nullptr;
+  double2 *d_Tph = nullptr, *d_Mph = nullptr;
+  double *d_Tr = nullptr, *d_Sr = nullptr, *d_Mr = nullptr;
   double* d_diag = nullptr;
   // FP32 copies for the low-accuracy apply, made on its first use
-  float2 *d_T32 = nullptr, *d_S32 = nullptr, *d_Mph32 = nullptr, *d_nw32 = nullptr;
-  float* d_Mr32 = nullptr;
+  float2 *d_Tph32 = nullptr, *d_Mph32 = nullptr, *d_nw32 = nullptr;
+  float *d_Tr32 = nullptr, *d_Sr32 = nullptr, *d_Mr32 = nullptr;
   float4* d_zf = nullptr;
   std::vector<void*> owned;
   cudaStream_t stream = nullptr;   // the upload stream; frees are ordered on it
@@ -630,8 +655,8 @@ struct Fmm2dPlan {
   double lo = 0, side0 = 0;
   std::vector<int> lvl_off, order, leaf_start, leaf_box, near_off, near_leaf, child, parent,
       child_pos, v_off, v_src, v_code;
-  std::vector<double2> z, nw, centre, T, S, Mph;
-  std::vector<double> Mr;
+  std::vector<double2> z, nw, centre, Tph, Mph;
+  std::vector<double> Tr, Sr, Mr;
   std::vector<double> diag;
 };
 
@@ -797,19 +822,24 @@ std::unique_ptr<Fmm2dPlan, Fmm2dPlanDeleter> fmm2d_plan(const double* pts, const
     }
   }
   // translation matrices
-  std::vector<double2> T(4 * (size_t)p * p), S(4 * (size_t)p * p), Mph(49 * (size_t)(p + 1));
-  std::vector<double> Mr(49 * (size_t)p * p);
+  std::vector<double2> Tph(4 * (size_t)p), Mph(49 * (size_t)(p + 1));
+  std::vector<double> Tr(4 * (size_t)p * p, 0.0), Sr(4 * (size_t)p * p, 0.0),
+      Mr(49 * (size_t)p * p);
   for (int pos = 0; pos < 4; pos++) {
-    // child offset from the parent centre in units of the parent side
-    std::complex<double> d((pos & 2) ? 0.25 : -0.25, (pos & 1) ? 0.25 : -0.25);
-    for (int k = 0; k < p; k++)
-      for (int j = 0; j < p; j++) {
-        std::complex<double> t = 0, u = 0;
-        if (j <= k) t = binom(k, j) * std::pow(0.5, j) * std::pow(d, k - j);   // M2M
-        if (j <= k) u = binom(k, j) * std::pow(0.5, j) * std::pow(d, k - j);   // L2L (j<->m)
-        T[(size_t)pos * p * p + (size_t)k * p + j] = make_double2(t.real(), t.imag());
-        S[(size_t)pos * p * p + (size_t)j * p + k] = make_double2(u.real(), u.imag());
+    // child offset from the parent centre in units of the parent side,
+    // d = |d| e^(i theta): real cores C(k, j) 0.5^j |d|^(k-j) (M2M rows k,
+    // L2L rows j) and the phases e^(i theta k)
+    const std::complex<double> d((pos & 2) ? 0.25 : -0.25, (pos & 1) ? 0.25 : -0.25);
+    const double ad = std::abs(d), th = std::arg(d);
+    for (int k = 0; k < p; k++) {
+      const std::complex<double> e = std::polar(1.0, th * k);
+      Tph[(size_t)pos * p + k] = make_double2(e.real(), e.imag());
+      for (int j = 0; j <= k; j++) {
+        const double v = binom(k, j) * std::pow(0.5, j) * std::pow(ad, k - j);
+        Tr[(size_t)pos * p * p + (size_t)k * p + j] = v;   // M2M: row k, column j
+        Sr[(size_t)pos * p * p + (size_t)j * p + k] = v;   // L2L: row j, column m = k
       }
+    }
   }
   for (int di = -3; di <= 3; di++)
     for (int dj = -3; dj <= 3; dj++) {
@@ -864,8 +894,9 @@ std::unique_ptr<Fmm2dPlan, Fmm2dPlanDeleter> fmm2d_plan(const double* pts, const
   F->z = std::move(z);
   F->nw = std::move(nw);
   F->centre = std::move(centre);
-  F->T = std::move(T);
-  F->S = std::move(S);
+  F->Tr = std::move(Tr);
+  F->Sr = std::move(Sr);
+  F->Tph = std::move(Tph);
   F->Mr = std::move(Mr);
   F->Mph = std::move(Mph);
   F->diag = std::move(dg);
@@ -900,8 +931,9 @@ std::unique_ptr<Fmm2d, Fmm2dDeleter> fmm2d_upload(const Fmm2dPlan& P, cudaStream
   F->d_z = upload_vec(P.z, &F->owned, s);
   F->d_nw = upload_vec(P.nw, &F->owned, s);
   F->d_centre = upload_vec(P.centre, &F->owned, s);
-  F->d_T = upload_vec(P.T, &F->owned, s);
-  F->d_S = upload_vec(P.S, &F->owned, s);
+  F->d_Tr = upload_vec(P.Tr, &F->owned, s);
+  F->d_Sr = upload_vec(P.Sr, &F->owned, s);
+  F->d_Tph = upload_vec(P.Tph, &F->owned, s);
   F->d_Mr = upload_vec(P.Mr, &F->owned, s);
   F->d_Mph = upload_vec(P.Mph, &F->owned, s);
   F->d_diag = upload_vec(P.diag, &F->owned, s);
@@ -928,18 +960,19 @@ void ensure_fp32(Fmm2d& F, cudaStream_t s) {
     return d;
   };
   const size_t pp = (size_t)F.p * F.p;
-  F.d_T32 = round(F.d_T, 4 * pp);
-  F.d_S32 = round(F.d_S, 4 * pp);
+  F.d_Tph32 = round(F.d_Tph, 4 * (size_t)F.p);
   F.d_Mph32 = round(F.d_Mph, 49 * (size_t)(F.p + 1));
   F.d_nw32 = round(F.d_nw, (size_t)F.n);
-  {
+  auto round_real = [&](const double* a, size_t count) {
     float* d = nullptr;
-    const size_t count = 49 * pp;
     KI_FMM_CUDA(pool_malloc((void**)&d, sizeof(float) * count, s));
     F.owned.push_back(d);
-    k_round_real<<<(int)std::min<size_t>(1024, (count + 255) / 256), 256, 0, s>>>(F.d_Mr, count, d);
-    F.d_Mr32 = d;
-  }
+    k_round_real<<<(int)std::min<size_t>(1024, (count + 255) / 256), 256, 0, s>>>(a, count, d);
+    return d;
+  };
+  F.d_Mr32 = round_real(F.d_Mr, 49 * pp);
+  F.d_Tr32 = round_real(F.d_Tr, 4 * pp);
+  F.d_Sr32 = round_real(F.d_Sr, 4 * pp);
   float4* zf = nullptr;
   KI_FMM_CUDA(pool_malloc((void**)&zf, sizeof(float4) * (size_t)F.n, s));
   F.owned.push_back(zf);
@@ -949,7 +982,7 @@ void ensure_fp32(Fmm2d& F, cudaStream_t s) {
 }
 
 template <typename R>
-void apply_impl(Fmm2d& F, const cplx_t<R>* T, const cplx_t<R>* S, const R* Mr,
+void apply_impl(Fmm2d& F, const R* Tr, const R* Sr, const cplx_t<R>* Tph, const R* Mr,
                 const cplx_t<R>* Mph,
                 const double* mu, int ldmu, int ncols, double* y, int ldy, cudaStream_t s, int p,
                 StageRecorder* rec, const char* const* names) {
@@ -963,21 +996,21 @@ void apply_impl(Fmm2d& F, const cplx_t<R>* T, const cplx_t<R>* S, const R* Mr,
   KI_FMM_CUDA(pool_malloc((void**)&le, sizeof(V) * (size_t)nbox * p * nc_max, s));
   for (int c0 = 0; c0 < ncols; c0 += kCols) {
     const int nc = std::min(kCols, ncols - c0);
-    // algorithmic flops per column (complex FMA = 8, real-by-complex = 4):
-    // P2M 4 n p (+ 6 n p column-independent), M2M 8 p(p+1)/2 per child link,
-    // M2L (rotated) 4 p^2 + 14 p per interaction pair, L2L 8 p(p+1)/2 per box
-    // below level 2, near field 2 per point pair (+ 12 per pair for the
-    // entry), local expansion 4 n p (+ 6 n p)
+    // algorithmic flops per column (complex FMA = 8, real-by-complex = 4,
+    // rotation = 6): P2M 4 n p (+ 6 n p column-independent), M2M and L2L
+    // (rotated) 2 p(p+1) + 14 p per child link / per box below level 2, M2L
+    // (rotated) 4 p^2 + 14 p per interaction pair, near field 2 per point
+    // pair (+ 12 per pair for the entry), local expansion 4 n p (+ 6 n p)
     const double pp = p, cx = nc;
     const int nl2 = F.lvl_off[L + 1] - F.lvl_off[3 > L ? L + 1 : 3];
     if (rec) rec->begin(names[0], (double)n * pp * (4.0 * cx + 6.0) +
-                                  8.0 * cx * (double)(nbox - 1) * pp * (pp + 1) / 2);
+                                  cx * (double)(nbox - 1) * (2.0 * pp * (pp + 1) + 14.0 * pp));
     k_densities<R><<<(n + 31) / 32, dim3(32, 8), 0, s>>>(F.d_perm, n, mu, ldmu, c0, nc, q);
     k_p2m<R><<<F.nleaf, 256, 0, s>>>(F.d_leaf_start, F.d_leaf_box, F.d_centre,
                                      F.side0 / (double)(1L << L), F.d_z, F.d_nw, q, nc, p, me);
     for (int l = L; l >= 1; l--) {
       const int b0 = F.lvl_off[l - 1], cnt = F.lvl_off[l] - b0;
-      k_m2m<R><<<cnt, 256, 0, s>>>(b0, F.d_child, F.d_child_pos, T, ldm, nc, p, me);
+      k_m2m<R><<<cnt, 256, 0, s>>>(b0, F.d_child, F.d_child_pos, Tr, Tph, ldm, nc, p, me);
     }
     if (rec) rec->end();
     KI_FMM_CUDA(cudaMemsetAsync(le, 0, sizeof(V) * (size_t)F.lvl_off[2] * p * nc, s));
@@ -990,10 +1023,10 @@ void apply_impl(Fmm2d& F, const cplx_t<R>* T, const cplx_t<R>* S, const R* Mr,
                                    (double)(1L << l) / F.side0, nc, p, me, le);
     }
     if (rec) rec->end();
-    if (rec) rec->begin(names[2], 8.0 * cx * (double)nl2 * pp * (pp + 1) / 2);
+    if (rec) rec->begin(names[2], cx * (double)nl2 * (2.0 * pp * (pp + 1) + 14.0 * pp));
     for (int l = 3; l <= L; l++) {
       const int b0 = F.lvl_off[l], cnt = F.lvl_off[l + 1] - b0;
-      k_l2l<R><<<cnt, 256, 0, s>>>(b0, F.d_parent, F.d_child_pos, S, ldm, nc, p, le);
+      k_l2l<R><<<cnt, 256, 0, s>>>(b0, F.d_parent, F.d_child_pos, Sr, Tph, ldm, nc, p, le);
     }
     if (rec) rec->end();
     if (rec) rec->begin(names[3], (double)F.near_point_pairs * (2.0 * cx + 12.0) +
@@ -1018,12 +1051,12 @@ void fmm2d_apply(Fmm2d& F, const double* mu, int ldmu, int ncols, double* y, int
   if (arith == FmmArith::kF32) {
     static const char* const names[4] = {"fmm32_upward", "fmm32_m2l", "fmm32_l2l", "fmm32_near"};
     ensure_fp32(F, s);
-    apply_impl<float>(F, F.d_T32, F.d_S32, F.d_Mr32, F.d_Mph32, mu, ldmu, ncols, y, ldy, s, p,
-                      rec, names);
+    apply_impl<float>(F, F.d_Tr32, F.d_Sr32, F.d_Tph32, F.d_Mr32, F.d_Mph32, mu, ldmu, ncols, y,
+                      ldy, s, p, rec, names);
   } else {
     static const char* const names[4] = {"fmm_upward", "fmm_m2l", "fmm_l2l", "fmm_near"};
-    apply_impl<double>(F, F.d_T, F.d_S, F.d_Mr, F.d_Mph, mu, ldmu, ncols, y, ldy, s, p, rec,
-                       names);
+    apply_impl<double>(F, F.d_Tr, F.d_Sr, F.d_Tph, F.d_Mr, F.d_Mph, mu, ldmu, ncols, y, ldy, s,
+                       p, rec, names);
   }
 }
 

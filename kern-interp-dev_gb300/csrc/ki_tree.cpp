@@ -237,6 +237,7 @@ void Tree::finish(const std::vector<int>& work, const std::vector<std::pair<int,
       const int b = lv[i];
       Box& bx = boxes[b];
       const Box& par = boxes[bx.parent];
+      bx.same_nbrs.reserve(dim == 2 ? 8 : 26);   // at most the 3^dim - 1 surrounding boxes
       for (int ci = 0; ci < nch; ci++)
         if (par.child[ci] != b) bx.same_nbrs.push_back(par.child[ci]);
       for (int pn : par.same_nbrs) {
