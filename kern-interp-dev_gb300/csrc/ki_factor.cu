@@ -1722,10 +1722,38 @@ __global__ void k_border_init(const double* pts, const double* pw, int n_points,
                               T* PsiT) {
   const int c = border_cols_per_hole(dim, sol_dim);
   const int nb = c * nh;
+  extern __shared__ float bi_smem[];
+  float* s_ch = bi_smem;             // hole centres, FP32 high parts (FP32 Laplace path)
+  float* s_cl = bi_smem + dim * nh;  // and low parts
+  if (sol_dim == 1 && sizeof(T) < sizeof(double)) {
+    for (int e = threadIdx.x; e < dim * nh; e += blockDim.x) {
+      s_ch[e] = (float)hc[e];
+      s_cl[e] = (float)(hc[e] - (double)s_ch[e]);
+    }
+    __syncthreads();
+  }
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n_points; p += gridDim.x * blockDim.x) {
     const double* xp = pts + (size_t)dim * p;
     const int hp = hole_of[p];
-    if (sol_dim == 1) {
+    if (sol_dim == 1 && sizeof(T) < sizeof(double)) {
+      // FP32 forms: offsets from hi/lo splits of the point and of the hole
+      // centres (the latter formed once per CTA in shared memory), the log or
+      // reciprocal in FP32
+      float xh[3], xl[3];
+      for (int d = 0; d < dim; d++) {
+        xh[d] = (float)xp[d];
+        xl[d] = (float)(xp[d] - (double)xh[d]);
+      }
+      for (int h = 0; h < nh; h++) {
+        float r2 = 0.f;
+        for (int d = 0; d < dim; d++) {
+          const float dd = (xh[d] - s_ch[dim * h + d]) + (xl[d] - s_cl[dim * h + d]);
+          r2 += dd * dd;
+        }
+        U[(size_t)p * nb + h] = T(dim == 2 ? 0.5f * logf(r2) : 1.f / sqrtf(r2));
+        PsiT[(size_t)p * nb + h] = T(h == hp ? pw[p] : 0.0);
+      }
+    } else if (sol_dim == 1) {
       for (int h = 0; h < nh; h++) {
         double r2 = 0;
         for (int d = 0; d < dim; d++) r2 += (xp[d] - hc[dim * h + d]) * (xp[d] - hc[dim * h + d]);
@@ -3121,7 +3149,11 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         upload(d_hc, holes.centers, s);
         F->d_Umod = (T*)F->alloc(Tsz * (size_t)N * nb);
         F->d_PsiTmod = (T*)F->alloc(Tsz * (size_t)N * nb);
-        k_border_init<T><<<std::min(2048, (n_points + 255) / 256), 256, 0, s>>>(
+        const size_t bism = sd == 1 && sizeof(T) < sizeof(double) ? sizeof(float) * 2 * dim * nh : 0;
+        if (bism > 48 * 1024)
+          KI_CUDA(cudaFuncSetAttribute(k_border_init<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)bism));
+        k_border_init<T><<<std::min(2048, (n_points + 255) / 256), 256, bism, s>>>(
             d_pts_in, d_w_in, n_points, dim, sd, d_hc, nh, d_hole_of, F->d_Umod, F->d_PsiTmod);
         KI_CUDA(cudaGetLastError());
         F->stage_begin("border_sweeps", 0, 0);

@@ -8,7 +8,8 @@
 // Sort: least-significant-digit radix sort of the 64-bit codes with the
 // point indices as values, 8-bit digits, one pass per digit of the
 // dim * depth code bits.  Per pass: tile histograms (2048 keys per CTA),
-// one exclusive scan of the (digit, tile) counts in digit-major order, and
+// an exclusive scan of the (digit, tile) counts in digit-major order (each
+// digit's row by one CTA, then the digit totals), and
 // a stable scatter in which each warp ranks its keys among equal digits
 // with __match_any_sync and the tile's warps and rounds are taken in key
 // order.  Ties keep the input order, and the input starts in point order.
@@ -79,17 +80,19 @@ __global__ void k_rs_hist(const unsigned long long* keys, int n, int shift, int 
     hist[(size_t)b * ntile + blockIdx.x] = h[b];
 }
 
-// In-place exclusive scan of `count` entries, one CTA: per-thread serial
-// sums of contiguous runs, a scan of the run sums, then the runs.
-__global__ void k_rs_scan(unsigned* a, int count) {
+// In-place exclusive scan of each digit's row of tile counts (one CTA per
+// digit: per-thread serial sums of contiguous runs, a scan of the run sums,
+// then the runs), the row total to tot[digit].
+__global__ void k_rs_scan_rows(unsigned* hist, int ntile, unsigned* tot) {
   __shared__ unsigned part[kScanThreads];
-  const int per = (count + kScanThreads - 1) / kScanThreads;
-  const int lo = min(count, (int)threadIdx.x * per), hi = min(count, lo + per);
-  unsigned s = 0;
-  for (int i = lo; i < hi; i++) s += a[i];
-  part[threadIdx.x] = s;
+  unsigned* a = hist + (size_t)blockIdx.x * ntile;
+  const int per = (ntile + blockDim.x - 1) / blockDim.x;
+  const int lo = min(ntile, (int)threadIdx.x * per), hi = min(ntile, lo + per);
+  unsigned sum = 0;
+  for (int i = lo; i < hi; i++) sum += a[i];
+  part[threadIdx.x] = sum;
   __syncthreads();
-  for (int o = 1; o < kScanThreads; o <<= 1) {
+  for (int o = 1; o < (int)blockDim.x; o <<= 1) {
     const unsigned v = (int)threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
     __syncthreads();
     part[threadIdx.x] += v;
@@ -101,19 +104,35 @@ __global__ void k_rs_scan(unsigned* a, int count) {
     a[i] = run;
     run += v;
   }
+  if (threadIdx.x == blockDim.x - 1) tot[blockIdx.x] = part[threadIdx.x];
+}
+
+// Exclusive scan of the kRsBins digit totals (one CTA of kRsBins threads).
+__global__ void k_rs_scan_base(unsigned* tot) {
+  __shared__ unsigned part[kRsBins];
+  const unsigned v0 = tot[threadIdx.x];
+  part[threadIdx.x] = v0;
+  __syncthreads();
+  for (int o = 1; o < kRsBins; o <<= 1) {
+    const unsigned v = (int)threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  tot[threadIdx.x] = part[threadIdx.x] - v0;
 }
 
 // Stable scatter of one tile: rounds of 256 keys in key order; in a round,
 // warp w's keys follow warps 0..w-1's, and a lane's rank among its warp's
 // equal digits comes from __match_any_sync.
 __global__ void k_rs_scatter(const unsigned long long* keys, const int* vals, int n, int shift,
-                             int ntile, const unsigned* offs, unsigned long long* okeys,
-                             int* ovals) {
+                             int ntile, const unsigned* offs, const unsigned* dbase,
+                             unsigned long long* okeys, int* ovals) {
   __shared__ unsigned run[kRsBins];
   __shared__ unsigned wcnt[kRsWarps][kRsBins];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int b = threadIdx.x; b < kRsBins; b += blockDim.x)
-    run[b] = offs[(size_t)b * ntile + blockIdx.x];
+    run[b] = dbase[b] + offs[(size_t)b * ntile + blockIdx.x];
   const int base = blockIdx.x * kRsTile;
   for (int k = 0; k < kRsItems; k++) {
     for (int e = threadIdx.x; e < kRsWarps * kRsBins; e += blockDim.x) (&wcnt[0][0])[e] = 0;
@@ -169,7 +188,8 @@ void tree_codes_sorted(const double* d_points, int n, int dim, double centre, do
       keys[b] = (unsigned long long*)take(sizeof(unsigned long long) * n);
       vals[b] = (int*)take(sizeof(int) * n);
     }
-    hist = (unsigned*)take(sizeof(unsigned) * (size_t)kRsBins * ntile);
+    hist = (unsigned*)take(sizeof(unsigned) * ((size_t)kRsBins * ntile + kRsBins));
+    unsigned* tot = hist + (size_t)kRsBins * ntile;
     k_tree_codes<<<(n + 255) / 256, 256, 0, s>>>(d_points, n, dim, centre, side, depth, keys[0],
                                                  vals[0]);
     KI_TREE_CUDA(cudaGetLastError());
@@ -177,8 +197,9 @@ void tree_codes_sorted(const double* d_points, int n, int dim, double centre, do
     int cur = 0;
     for (int shift = 0; shift < bits; shift += 8) {
       k_rs_hist<<<ntile, kRsThreads, 0, s>>>(keys[cur], n, shift, ntile, hist);
-      k_rs_scan<<<1, kScanThreads, 0, s>>>(hist, kRsBins * ntile);
-      k_rs_scatter<<<ntile, kRsThreads, 0, s>>>(keys[cur], vals[cur], n, shift, ntile, hist,
+      k_rs_scan_rows<<<kRsBins, 256, 0, s>>>(hist, ntile, tot);
+      k_rs_scan_base<<<1, kRsBins, 0, s>>>(tot);
+      k_rs_scatter<<<ntile, kRsThreads, 0, s>>>(keys[cur], vals[cur], n, shift, ntile, hist, tot,
                                                 keys[1 - cur], vals[1 - cur]);
       KI_TREE_CUDA(cudaGetLastError());
       cur = 1 - cur;
