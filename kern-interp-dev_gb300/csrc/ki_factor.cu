@@ -814,7 +814,7 @@ __global__ void __launch_bounds__(kThreads, kIdMinBlocks<T>) k_id(const IdTask* 
 }
 
 // Features of the learned rank predictor for every ID box of a level (one
-// thread per box), and with a model the predicted sketch size
+// warp per box, four per CTA), and with a model the predicted sketch size
 // l = min(n, ceil((1 + margin) k^) + oversample), k^ = n * MLP(features):
 //   0 log2 n            1 level / (levels - 1)   2 log2(m + 1)   3 log2(nI + 1)
 //   4 dim == 3          5 solution dim / 3       6 -log10(tol) / 10
@@ -832,7 +832,11 @@ __global__ void __launch_bounds__(128) k_box_features(const IdTask* tasks, int n
   if (model)
     for (int e = threadIdx.x; e < kMlpModelFloats; e += blockDim.x) sm[e] = model[e];
   __syncthreads();
-  const int task = blockIdx.x * blockDim.x + threadIdx.x;
+  // one warp per box: lanes take the box's nodes and combine their sums by
+  // shuffles; the network's hidden units are split over the lanes
+  __shared__ float s_a1[4][kMlpHidden];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int task = blockIdx.x * (blockDim.x >> 5) + wib;
   if (task >= ntask) return;
   const IdTask t = tasks[task];
   const int n = t.n, m = m_arr[task];
@@ -840,12 +844,10 @@ __global__ void __launch_bounds__(128) k_box_features(const IdTask* tasks, int n
   const double c[3] = {t.cx, t.cy, t.cz};
   double s1[3] = {0, 0, 0}, s2[6] = {0, 0, 0, 0, 0, 0};
   const int dim = P.dim;
-  int prev = -1;
   int cnt = 0;
-  for (int j = 0; j < n; j++) {
+  for (int j = lane; j < n; j += 32) {
     const int p = dof_point(act[j], sol_dim);
-    if (p == prev) continue;   // the DOFs of one node are adjacent
-    prev = p;
+    if (j > 0 && dof_point(act[j - 1], sol_dim) == p) continue;   // a node's DOFs are adjacent
     double x[3] = {(double)P.x[p] + (P.xl ? (double)P.xl[p] : 0.0),
                    (double)P.y[p] + (P.yl ? (double)P.yl[p] : 0.0),
                    dim == 3 ? (double)P.z[p] + (P.zl ? (double)P.zl[p] : 0.0) : c[2]};
@@ -854,6 +856,11 @@ __global__ void __launch_bounds__(128) k_box_features(const IdTask* tasks, int n
     s2[0] += x[0] * x[0]; s2[1] += x[1] * x[1]; s2[2] += x[2] * x[2];
     s2[3] += x[0] * x[1]; s2[4] += x[0] * x[2]; s2[5] += x[1] * x[2];
     cnt++;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    for (int d = 0; d < 3; d++) s1[d] += __shfl_xor_sync(0xffffffffu, s1[d], o);
+    for (int d = 0; d < 6; d++) s2[d] += __shfl_xor_sync(0xffffffffu, s2[d], o);
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
   }
   const double inv = cnt ? 1.0 / cnt : 0.0, side2 = t.side * t.side;
   double mu[3] = {s1[0] * inv, s1[1] * inv, s1[2] * inv};
@@ -902,15 +909,34 @@ __global__ void __launch_bounds__(128) k_box_features(const IdTask* tasks, int n
   f[9] = (float)(fmax(ev[1], 0.0) / side2);
   f[10] = (float)(fmax(ev[2], 0.0) / side2);
   f[11] = (float)(sqrt(mu[0] * mu[0] + mu[1] * mu[1] + mu[2] * mu[2]) / t.side);
-  for (int q = 0; q < kMlpIn; q++) feat[(size_t)task * kMlpIn + q] = f[q];
+  if (lane < kMlpIn) feat[(size_t)task * kMlpIn + lane] = f[lane];
   int l = 0;
   float khat = 0.f;
   if (model) {
-    khat = (float)n * mlp_forward_one(sm, f);
+    // the forward pass of mlp_forward_one with lanes on hidden units
+    float xn[kMlpIn];
+    for (int q = 0; q < kMlpIn; q++) xn[q] = (f[q] - sm[kMlpMean + q]) / sm[kMlpScale + q];
+    for (int k = lane; k < kMlpHidden; k += 32) {
+      float z = sm[kMlpB1 + k];
+      for (int q = 0; q < kMlpIn; q++) z += sm[kMlpW1 + k * kMlpIn + q] * xn[q];
+      s_a1[wib][k] = z > 0.f ? z : 0.f;
+    }
+    __syncwarp();
+    float zo = 0.f;
+    for (int j = lane; j < kMlpHidden; j += 32) {
+      float z = sm[kMlpB2 + j];
+      for (int k = 0; k < kMlpHidden; k++) z += sm[kMlpW2 + j * kMlpHidden + k] * s_a1[wib][k];
+      zo += sm[kMlpW3 + j] * (z > 0.f ? z : 0.f);
+    }
+    for (int o = 16; o > 0; o >>= 1) zo += __shfl_xor_sync(0xffffffffu, zo, o);
+    zo += sm[kMlpB3];
+    khat = (float)n * (1.f / (1.f + expf(-zo)));
     l = min(n, (int)ceilf((1.f + margin) * khat) + oversample);
   }
-  l_out[task] = l;
-  khat_out[task] = khat;
+  if (lane == 0) {
+    l_out[task] = l;
+    khat_out[task] = khat;
+  }
 }
 
 // Shared-memory bytes of k_id for a box of n active DOFs: mode 0 keeps the
@@ -2291,6 +2317,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       std::vector<uint64_t> codes(n_points);
       std::vector<int> order(n_points);
       tree_codes_sorted(d_pts_in, n_points, dim, c0, side0, depth, codes.data(), order.data(), s);
+      F->tree_codes_seconds =
+          std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
       built = tree.build_from_codes(points, n_points, dim, prm.sol_dim, prm.max_leaf_dofs,
                                     codes.data(), order.data(), depth);
     }
@@ -2574,7 +2602,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     float* d_feat = (float*)F->alloc(sizeof(float) * kMlpIn * (size_t)ntask);
     int* d_lsk = (int*)F->alloc(sizeof(int) * (size_t)ntask);
     float* d_khat = (float*)F->alloc(sizeof(float) * (size_t)ntask);
-    k_box_features<T><<<(ntask + 127) / 128, 128, 0, s>>>(
+    k_box_features<T><<<(ntask + 3) / 4, 128, 0, s>>>(
         d_it, ntask, ipool, P, sd, d_m, 2 * np * sd, L > 1 ? (float)l / (float)(L - 1) : 0.f,
         (float)(-std::log10(prm.id_tol) / 10.0), prm.rank_model, prm.sketch_margin,
         prm.sketch_oversample, d_feat, d_lsk, d_khat);
