@@ -229,6 +229,23 @@ __device__ R border_u(int dim, int sol_dim, int comp, int k, const R* r) {
   return rot * sgn * r[o];
 }
 
+// FP64 SoA geometry (x, y, nx, ny, w, kappa, z, nz; n each) from the
+// interleaved inputs points (dim n) | normals (dim n) | weights | curvatures.
+__global__ void k_geo_soa(const double* in, int n, int dim, bool has_kappa, double* geo) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double* p = in + (size_t)dim * i;
+    const double* q = in + (size_t)dim * n + (size_t)dim * i;
+    geo[i] = p[0];
+    geo[n + i] = p[1];
+    geo[2 * (size_t)n + i] = q[0];
+    geo[3 * (size_t)n + i] = q[1];
+    geo[4 * (size_t)n + i] = in[2 * (size_t)dim * n + i];
+    geo[5 * (size_t)n + i] = has_kappa ? in[(2 * (size_t)dim + 1) * n + i] : 0.0;
+    geo[6 * (size_t)n + i] = dim == 3 ? p[2] : 0.0;
+    geo[7 * (size_t)n + i] = dim == 3 ? q[2] : 0.0;
+  }
+}
+
 // y += U alpha, one thread per listed DOF (rows != nullptr: DOF rows[q] of
 // the points; else DOF q).  Points: dim per point with the given stride
 // between points (SoA x with stride 1 and separate y/z, or interleaved).
@@ -1116,23 +1133,29 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
       holes.start.push_back(desc->hole_node_start[h]);
       holes.count.push_back(desc->hole_node_count[h]);
     }
-    // FP64 geometry for apply / evaluation (SoA)
+    // the caller's arrays uploaded once, interleaved as given: points (dim n) |
+    // normals (dim n) | weights (n) | curvatures (n); the factorization reads
+    // them in place, and the FP64 SoA geometry of the apply / evaluation
+    // kernels is formed from them on the device
     const int n = desc->n_points;
-    std::vector<double> geo((size_t)8 * n, 0.0);
-    for (int i = 0; i < n; i++) {
-      geo[i] = desc->points[(size_t)dim * i];
-      geo[n + i] = desc->points[(size_t)dim * i + 1];
-      geo[2 * (size_t)n + i] = desc->normals[(size_t)dim * i];
-      geo[3 * (size_t)n + i] = desc->normals[(size_t)dim * i + 1];
-      geo[4 * (size_t)n + i] = desc->weights[i];
-      geo[5 * (size_t)n + i] = desc->curvatures ? desc->curvatures[i] : 0.0;
-      if (dim == 3) {
-        geo[6 * (size_t)n + i] = desc->points[3 * (size_t)i + 2];
-        geo[7 * (size_t)n + i] = desc->normals[3 * (size_t)i + 2];
-      }
+    {
+      const size_t nn = (size_t)n;
+      KI_CHECK_CUDA(cudaMalloc(&f->d_pts, sizeof(double) * (2 * dim + 2) * nn));
+      double* d_in = f->d_pts;
+      KI_CHECK_CUDA(cudaMemcpyAsync(d_in, desc->points, sizeof(double) * dim * nn,
+                                    cudaMemcpyHostToDevice, f->stream));
+      KI_CHECK_CUDA(cudaMemcpyAsync(d_in + dim * nn, desc->normals, sizeof(double) * dim * nn,
+                                    cudaMemcpyHostToDevice, f->stream));
+      KI_CHECK_CUDA(cudaMemcpyAsync(d_in + 2 * dim * nn, desc->weights, sizeof(double) * nn,
+                                    cudaMemcpyHostToDevice, f->stream));
+      if (desc->curvatures)
+        KI_CHECK_CUDA(cudaMemcpyAsync(d_in + (2 * dim + 1) * nn, desc->curvatures,
+                                      sizeof(double) * nn, cudaMemcpyHostToDevice, f->stream));
+      KI_CHECK_CUDA(cudaMalloc(&f->d_geo, sizeof(double) * 8 * nn));
+      k_geo_soa<<<std::min(2048, (n + 255) / 256), 256, 0, f->stream>>>(
+          d_in, n, dim, desc->curvatures != nullptr, f->d_geo);
+      KI_CHECK_CUDA(cudaGetLastError());
     }
-    KI_CHECK_CUDA(cudaMalloc(&f->d_geo, sizeof(double) * geo.size()));
-    KI_CHECK_CUDA(cudaMemcpy(f->d_geo, geo.data(), sizeof(double) * geo.size(), cudaMemcpyHostToDevice));
     f->P = ki::Points<double>{f->d_geo, f->d_geo + n, f->d_geo + 2 * (size_t)n,
                               f->d_geo + 3 * (size_t)n, f->d_geo + 4 * (size_t)n,
                               f->d_geo + 5 * (size_t)n};
@@ -1152,9 +1175,7 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
       KI_CHECK_CUDA(cudaMemcpy(f->d_hcount, desc->hole_node_count, sizeof(int) * desc->n_holes,
                                cudaMemcpyHostToDevice));
     }
-    KI_CHECK_CUDA(cudaMalloc(&f->d_pts, sizeof(double) * dim * (size_t)n));
-    KI_CHECK_CUDA(cudaMemcpy(f->d_pts, desc->points, sizeof(double) * dim * (size_t)n,
-                             cudaMemcpyHostToDevice));
+
     // 2D Laplace: the FMM for refinement residuals, planned and uploaded by a
     // worker thread on its own stream, concurrent with the factorization (it
     // copies the caller's arrays first; this call returns only after the
@@ -1200,10 +1221,10 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
     f->host_prep_ms = std::chrono::duration<double, std::milli>(t_factor - t_create).count();
     if (f->precision == KI_PRECISION_FP64)
       f->f64 = ki::factorize<double>(prm, n, desc->points, desc->normals, desc->weights,
-                                     desc->curvatures, holes, f->stream);
+                                     desc->curvatures, holes, f->stream, f->d_pts);
     else
       f->f32 = ki::factorize<float>(prm, n, desc->points, desc->normals, desc->weights,
-                                    desc->curvatures, holes, f->stream);
+                                    desc->curvatures, holes, f->stream, f->d_pts);
     f->host_factor_ms = std::chrono::duration<double, std::milli>(
                             std::chrono::steady_clock::now() - t_factor).count();
     // the FP64 3D diagonal of the factorization serves the FP64 apply

@@ -2257,7 +2257,7 @@ template <typename T>
 std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, const double* points,
                                             const double* normals, const double* weights,
                                             const double* curvatures, const HoleDesc& holes,
-                                            cudaStream_t stream) {
+                                            cudaStream_t stream, const double* d_inputs) {
   auto t_start = std::chrono::steady_clock::now();
   auto F = std::make_unique<Factorization<T>>();
   F->prm = prm;
@@ -2274,16 +2274,19 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
   double* d_w_in = nullptr;
   {
     const size_t np_ = (size_t)n_points;
-    double* d_in = (double*)F->alloc(sizeof(double) * np_ * (2 * dim + 2));
+    double* d_in = d_inputs ? const_cast<double*>(d_inputs)
+                            : (double*)F->alloc(sizeof(double) * np_ * (2 * dim + 2));
     d_pts_in = d_in;
     d_nrm_in = d_in + dim * np_;
     d_w_in = d_in + 2 * dim * np_;
     double* d_k_in = d_w_in + np_;
-    KI_CUDA(cudaMemcpyAsync(d_pts_in, points, sizeof(double) * dim * np_, cudaMemcpyHostToDevice, s));
-    KI_CUDA(cudaMemcpyAsync(d_nrm_in, normals, sizeof(double) * dim * np_, cudaMemcpyHostToDevice, s));
-    KI_CUDA(cudaMemcpyAsync(d_w_in, weights, sizeof(double) * np_, cudaMemcpyHostToDevice, s));
-    if (curvatures)
-      KI_CUDA(cudaMemcpyAsync(d_k_in, curvatures, sizeof(double) * np_, cudaMemcpyHostToDevice, s));
+    if (!d_inputs) {
+      KI_CUDA(cudaMemcpyAsync(d_pts_in, points, sizeof(double) * dim * np_, cudaMemcpyHostToDevice, s));
+      KI_CUDA(cudaMemcpyAsync(d_nrm_in, normals, sizeof(double) * dim * np_, cudaMemcpyHostToDevice, s));
+      KI_CUDA(cudaMemcpyAsync(d_w_in, weights, sizeof(double) * np_, cudaMemcpyHostToDevice, s));
+      if (curvatures)
+        KI_CUDA(cudaMemcpyAsync(d_k_in, curvatures, sizeof(double) * np_, cudaMemcpyHostToDevice, s));
+    }
     T* d = (T*)F->alloc(sizeof(T) * np_ * 11);
     F->d_x = d; F->d_y = d + np_; F->d_nx = d + 2 * np_;
     F->d_ny = d + 3 * np_; F->d_w = d + 4 * np_;
@@ -2319,8 +2322,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       tree_codes_sorted(d_pts_in, n_points, dim, c0, side0, depth, codes.data(), order.data(), s);
       F->tree_codes_seconds =
           std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
-      built = tree.build_from_codes(points, n_points, dim, prm.sol_dim, prm.max_leaf_dofs,
-                                    codes.data(), order.data(), depth);
+      built = tree.build_from_codes(n_points, dim, prm.sol_dim, prm.max_leaf_dofs, codes.data(),
+                                    order.data(), depth, c0, side0);
     }
     if (!built) tree.build(points, n_points, dim, prm.sol_dim, prm.max_leaf_dofs);
     F->tree_gpu = built;
@@ -3396,10 +3399,10 @@ template void solve_device_arena<float>(Factorization<float>&, float*, int, floa
 
 template std::unique_ptr<Factorization<double>> factorize<double>(
     const Params&, int, const double*, const double*, const double*, const double*,
-    const HoleDesc&, cudaStream_t);
+    const HoleDesc&, cudaStream_t, const double*);
 template std::unique_ptr<Factorization<float>> factorize<float>(
     const Params&, int, const double*, const double*, const double*, const double*,
-    const HoleDesc&, cudaStream_t);
+    const HoleDesc&, cudaStream_t, const double*);
 template void solve_device<double>(Factorization<double>&, double*, int, double*, const double*);
 template void solve_device<float>(Factorization<float>&, float*, int, float*, const float*);
 template struct Factorization<double>;

@@ -147,10 +147,14 @@ struct HoleDesc {
 // Build the tree and skeletonize on `stream`.  Throws std::runtime_error on
 // failure (message says which stage).
 template <typename T>
+// d_inputs (optional): the same four arrays already on the device, laid out
+// points (dim n) | normals (dim n) | weights (n) | curvatures (n), kept alive
+// by the caller for the factorization's lifetime; otherwise they are copied.
 std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, const double* points,
                                             const double* normals, const double* weights,
                                             const double* curvatures, const HoleDesc& holes,
-                                            cudaStream_t stream);
+                                            cudaStream_t stream,
+                                            const double* d_inputs = nullptr);
 
 // A bump allocator over caller-provided device memory.
 struct ScratchArena {

@@ -134,9 +134,9 @@ void Tree::build(const double* pts, int n_points_, int dim_, int sol_dim_, int m
   finish(work, range);
 }
 
-bool Tree::build_from_codes(const double* pts, int n_points_, int dim_, int sol_dim_,
-                            int max_leaf_dofs_, const uint64_t* codes, const int* order,
-                            int depth) {
+bool Tree::build_from_codes(int n_points_, int dim_, int sol_dim_, int max_leaf_dofs_,
+                            const uint64_t* codes, const int* order, int depth, double c0,
+                            double side0) {
   check_args(dim_, n_points_, max_leaf_dofs_);
   dim = dim_;
   n_points = n_points_;
@@ -146,8 +146,6 @@ bool Tree::build_from_codes(const double* pts, int n_points_, int dim_, int sol_
   boxes.clear();
   levels.clear();
   const int nch = 1 << dim;
-  double c0, side0;
-  tree_root(pts, n_points, dim, &c0, &side0);
   std::vector<std::pair<int, int>> range;
   boxes.reserve((size_t)2 * nch * (n_points / max_leaf_dofs + 1) + 1);
   range.reserve(boxes.capacity());

@@ -54,8 +54,10 @@ struct Tree {
   // rule's centre arithmetic), sorted ascending with ties by point index,
   // `order` the point indices in that order.  Returns false (tree left
   // empty) when a box at level `depth` would still be split.
-  bool build_from_codes(const double* points, int n_points, int dim, int sol_dim,
-                        int max_leaf_dofs, const uint64_t* codes, const int* order, int depth);
+  // centre / side: the root box tree_root gave for these points.
+  bool build_from_codes(int n_points, int dim, int sol_dim, int max_leaf_dofs,
+                        const uint64_t* codes, const int* order, int depth, double centre,
+                        double side);
   int num_levels() const { return (int)levels.size(); }
 
  private:
