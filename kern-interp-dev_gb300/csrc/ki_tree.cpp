@@ -3,6 +3,7 @@
 #include "ki_parallel.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <stdexcept>
 #include <thread>
@@ -157,32 +158,49 @@ bool Tree::build_from_codes(int n_points_, int dim_, int sol_dim_, int max_leaf_
   boxes.push_back(root);
   range.push_back({0, n_points});
   levels.push_back({0});
+  std::vector<int> starts;
   for (size_t l = 0; l < levels.size(); l++) {
-    std::vector<int> next;
-    for (int b : levels[l]) {
-      if (boxes[b].orig_count <= max_leaf_dofs) continue;
-      if ((int)l >= depth) {   // the codes end here: the caller builds by partition
-        boxes.clear();
-        levels.clear();
-        return false;
+    const std::vector<int>& lv = levels[l];
+    // the child boundaries of every box of the level that splits (binary
+    // searches, in parallel): the range shares the codes' first l digits and
+    // digit l + 1 ascends
+    const int shift = dim * (depth - 1 - (int)l);
+    starts.assign(lv.size() * (nch + 1), -1);
+    std::atomic<bool> too_deep(false);
+    parallel_ranges((int)lv.size(), [&](int i0, int i1) {
+      for (int i = i0; i < i1; i++) {
+        const int b = lv[i];
+        if (boxes[b].orig_count <= max_leaf_dofs) continue;
+        if ((int)l >= depth) {
+          too_deep = true;
+          continue;
+        }
+        int* st = starts.data() + (size_t)i * (nch + 1);
+        const int lo = range[b].first, hi = range[b].second;
+        st[0] = lo;
+        st[nch] = hi;
+        for (int ci = 1; ci < nch; ci++)
+          st[ci] = (int)(std::partition_point(codes + st[ci - 1], codes + hi,
+                                              [&](uint64_t k) {
+                                                return (int)((k >> shift) & (nch - 1)) < ci;
+                                              }) -
+                         codes);
       }
+    }, 1024);
+    if (too_deep) {   // the codes end here: the caller builds by partition
+      boxes.clear();
+      levels.clear();
+      return false;
+    }
+    std::vector<int> next;
+    for (size_t i = 0; i < lv.size(); i++) {
+      const int* st = starts.data() + i * (nch + 1);
+      if (st[0] < 0) continue;
+      const int b = lv[i];
       boxes[b].leaf = false;
-      const int lo = range[b].first, hi = range[b].second;
-      // the range shares the codes' first l digits; digit l + 1 ascends
-      const int shift = dim * (depth - 1 - (int)l);
-      int start[kMaxChildren + 1];
-      start[0] = lo;
-      start[nch] = hi;
-      for (int ci = 1; ci < nch; ci++)
-        start[ci] = (int)(std::partition_point(codes + start[ci - 1], codes + hi,
-                                               [&](uint64_t k) {
-                                                 return (int)((k >> shift) & (nch - 1)) < ci;
-                                               }) -
-                          codes);
       for (int ci = 0; ci < nch; ci++) {
-        const int id = add_child(&boxes, b, ci, (int)l + 1, dim,
-                                 (start[ci + 1] - start[ci]) * sol_dim);
-        range.push_back({start[ci], start[ci + 1]});
+        const int id = add_child(&boxes, b, ci, (int)l + 1, dim, (st[ci + 1] - st[ci]) * sol_dim);
+        range.push_back({st[ci], st[ci + 1]});
         next.push_back(id);
       }
     }
@@ -200,22 +218,19 @@ bool Tree::build_from_codes(int n_points_, int dim_, int sol_dim_, int max_leaf_
 
 void Tree::finish(const std::vector<int>& work, const std::vector<std::pair<int, int>>& range) {
   const int nch = 1 << dim;
-  // Leaf DOF ranges in depth-first order.
-  dof_sorted.clear();
-  dof_sorted.reserve(n_dofs);
-  std::vector<int> stack = {0};
-  while (!stack.empty()) {
-    int b = stack.back();
-    stack.pop_back();
-    Box& bx = boxes[b];
-    if (bx.leaf) {
-      bx.orig_start = (int)dof_sorted.size();
-      for (int i = range[b].first; i < range[b].second; i++)
-        for (int s = 0; s < sol_dim; s++) dof_sorted.push_back(work[i] * sol_dim + s);
-    } else {
-      for (int ci = nch - 1; ci >= 0; ci--) stack.push_back(bx.child[ci]);
-    }
-  }
+  // Leaf DOF ranges in depth-first order.  Both builds keep `work` in that
+  // order (children in child order inside their parent's range), so a leaf's
+  // DOFs start at its range's first point: the list is `work` expanded by
+  // the solution dimension, filled in parallel.
+  dof_sorted.assign((size_t)n_dofs, 0);
+  parallel_ranges(n_points, [&](int lo, int hi) {
+    for (int i = lo; i < hi; i++)
+      for (int s = 0; s < sol_dim; s++) dof_sorted[(size_t)i * sol_dim + s] = work[i] * sol_dim + s;
+  });
+  parallel_ranges((int)boxes.size(), [&](int b0, int b1) {
+    for (int b = b0; b < b1; b++)
+      if (boxes[b].leaf) boxes[b].orig_start = range[b].first * sol_dim;
+  });
 
   // Levels in depth-first order (children of consecutive parents stay
   // consecutive, matching the BFS construction above), positions.
