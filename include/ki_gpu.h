@@ -305,6 +305,12 @@ int ki_factor_get_box_log(const ki_factor* f, float* out, int max_rows, int* row
  */
 int ki_trim_memory(void);
 
+/*
+ * Kernels the library has launched since it was loaded (every launch goes
+ * through one counted helper).  No reference counterpart.
+ */
+long long ki_launch_count(void);
+
 /* Message of the last failure on the calling thread ("" if none). */
 const char* ki_last_error(void);
 

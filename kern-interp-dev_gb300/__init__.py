@@ -31,7 +31,8 @@ EXPORTED = ["ki_factor_create", "ki_factor_destroy", "ki_factor_get_info", "ki_s
             "ki_solve_device", "ki_apply", "ki_eval_targets", "ki_last_error", "ki_version",
             "ki_factor_get_profile", "ki_factor_set_profiling", "ki_apply_rows",
             "ki_measure_fma_peak", "ki_solve_refined", "ki_solve_refined_device",
-            "ki_solve_device_noalloc", "ki_apply_fmm", "ki_apply_fmm_ex", "ki_trim_memory", "ki_rank_model_floats",
+            "ki_solve_device_noalloc", "ki_apply_fmm", "ki_apply_fmm_ex", "ki_trim_memory",
+            "ki_launch_count", "ki_rank_model_floats",
             "ki_rank_model_train", "ki_rank_model_predict", "ki_rank_model_grad",
             "ki_factor_get_box_log"]
 RANK_MODEL_PATH = os.path.join(HERE, "rank_model.npy")
@@ -94,6 +95,8 @@ def load_library(path=None):
     lib.ki_eval_targets.argtypes = [V, V, I, V, I, I, V, I, V, I]
     lib.ki_apply_fmm.argtypes = [V, V, I, I, V, I, V, I]
     lib.ki_apply_fmm_ex.argtypes = [V, V, I, I, V, I, V, I, I, I]
+    lib.ki_launch_count.restype = ctypes.c_longlong
+    lib.ki_launch_count.argtypes = []
     lib.ki_apply_rows.argtypes = [V, V, I, V, I, I, V, I, V, I]
     lib.ki_factor_get_profile.argtypes = [V, ctypes.c_char_p, I]
     lib.ki_factor_set_profiling.argtypes = [V, I]
@@ -477,3 +480,8 @@ def boundary_integral_solve(kernel, boundary, quadtree, id_tol, fact_threads, do
 
 from . import geometry  # noqa: E402,F401
 from . import replicas  # noqa: E402,F401
+
+
+def launch_count():
+    """Kernels the library has launched since it was loaded."""
+    return int(load_library().ki_launch_count())

@@ -16,6 +16,7 @@
 #include <string>
 #include <vector>
 
+#include "ki_launch.cuh"
 #include "ki_pool.h"
 #include "../../include/ki_gpu.h"
 #include "ki_common.cuh"
@@ -387,17 +388,17 @@ void dense_product(const ki::Points<double>& P, int n_points, int sol_dim, const
   const int chunk_pts = (n_points + chunks - 1) / chunks;
   chunks = (n_points + chunk_pts - 1) / chunk_pts;
   if (chunks == 1) {
-    k_dense_apply<<<dim3(gx, gy, 1), kApplyThreads, 0, s>>>(P, n_points, sol_dim, x, ldx, ncols,
+    ki::launch(k_dense_apply, dim3(gx, gy, 1), kApplyThreads, 0, s, P, n_points, sol_dim, x, ldx, ncols,
                                                            y, ldy, 0, chunk_pts, rows, nrows, tg);
     KI_CHECK_CUDA(cudaGetLastError());
     return;
   }
   const size_t stride = (size_t)N * ncols;
   DevBuf<double> part(stride * chunks, s);
-  k_dense_apply<<<dim3(gx, gy, chunks), kApplyThreads, 0, s>>>(P, n_points, sol_dim, x, ldx, ncols,
+  ki::launch(k_dense_apply, dim3(gx, gy, chunks), kApplyThreads, 0, s, P, n_points, sol_dim, x, ldx, ncols,
                                                               part.p, N, stride, chunk_pts, rows,
                                                               nrows, tg);
-  k_chunk_reduce<<<grid_for(stride), 256, 0, s>>>(part.p, chunks, N, ncols, y, ldy);
+  ki::launch(k_chunk_reduce, grid_for(stride), 256, 0, s, part.p, chunks, N, ncols, y, ldy);
   KI_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -468,7 +469,7 @@ void solve_impl(ki_factor* f, ki::Factorization<T>& F, const double* d_b, int ld
   const int N = f->n_dofs;
   DevBuf<T> work((size_t)N * nrhs, s);
   DevBuf<T> al((size_t)std::max(1, f->n_border) * nrhs, s);
-  k_to_dofmajor<double, T><<<grid_for((size_t)N * nrhs), 256, 0, s>>>(d_b, ldb, N, nrhs, work.p);
+  ki::launch(k_to_dofmajor<double, T>, grid_for((size_t)N * nrhs), 256, 0, s, d_b, ldb, N, nrhs, work.p);
   KI_CHECK_CUDA(cudaGetLastError());
   cudaStream_t saved = F.stream;
   F.stream = s;
@@ -479,10 +480,10 @@ void solve_impl(ki_factor* f, ki::Factorization<T>& F, const double* d_b, int ld
     throw;
   }
   F.stream = saved;
-  k_from_dofmajor<T, double><<<grid_for((size_t)N * nrhs), 256, 0, s>>>(work.p, N, nrhs, d_x, ldx);
+  ki::launch(k_from_dofmajor<T, double>, grid_for((size_t)N * nrhs), 256, 0, s, work.p, N, nrhs, d_x, ldx);
   KI_CHECK_CUDA(cudaGetLastError());
   if (f->n_border > 0 && d_alpha) {
-    k_alpha_out<T><<<grid_for((size_t)f->n_border * nrhs), 256, 0, s>>>(al.p, f->n_border, nrhs,
+    ki::launch(k_alpha_out<T>, grid_for((size_t)f->n_border * nrhs), 256, 0, s, al.p, f->n_border, nrhs,
                                                                        d_alpha, ldalpha);
     KI_CHECK_CUDA(cudaGetLastError());
   }
@@ -587,13 +588,13 @@ void solve_impl_noalloc(ki_factor* f, ki::Factorization<T>& F, const double* d_b
   T* al = static_cast<T*>(arena.take(sizeof(T) * (size_t)std::max(1, f->n_border) * nrhs));
   if (!work || !al) throw ArgError("ki_solve_device_noalloc: scratch exhausted");
   // every temporary is written before it is read: nothing needs clearing
-  k_to_dofmajor<double, T><<<grid_for((size_t)N * nrhs), 256, 0, s>>>(d_b, ldb, N, nrhs, work);
+  ki::launch(k_to_dofmajor<double, T>, grid_for((size_t)N * nrhs), 256, 0, s, d_b, ldb, N, nrhs, work);
   KI_CHECK_CUDA(cudaGetLastError());
   ki::solve_device_arena<T>(F, work, nrhs, al, arena, s);
-  k_from_dofmajor<T, double><<<grid_for((size_t)N * nrhs), 256, 0, s>>>(work, N, nrhs, d_x, ldx);
+  ki::launch(k_from_dofmajor<T, double>, grid_for((size_t)N * nrhs), 256, 0, s, work, N, nrhs, d_x, ldx);
   KI_CHECK_CUDA(cudaGetLastError());
   if (f->n_border > 0 && d_alpha) {
-    k_alpha_out<T><<<grid_for((size_t)f->n_border * nrhs), 256, 0, s>>>(al, f->n_border, nrhs,
+    ki::launch(k_alpha_out<T>, grid_for((size_t)f->n_border * nrhs), 256, 0, s, al, f->n_border, nrhs,
                                                                        d_alpha, ldalpha);
     KI_CHECK_CUDA(cudaGetLastError());
   }
@@ -619,12 +620,12 @@ double fma_peak_gflops(int sms, int iters) {
   const int blocks = sms * 8, threads = 256;
   T* out = nullptr;
   KI_CHECK_CUDA(cudaMalloc(&out, sizeof(T) * blocks * threads));
-  k_fma_peak<T><<<blocks, threads>>>(out, 16);
+  ki::launch(k_fma_peak<T>, blocks, threads, 0, 0, out, 16);
   cudaEvent_t e0, e1;
   KI_CHECK_CUDA(cudaEventCreate(&e0));
   KI_CHECK_CUDA(cudaEventCreate(&e1));
   KI_CHECK_CUDA(cudaEventRecord(e0));
-  k_fma_peak<T><<<blocks, threads>>>(out, iters);
+  ki::launch(k_fma_peak<T>, blocks, threads, 0, 0, out, iters);
   KI_CHECK_CUDA(cudaEventRecord(e1));
   KI_CHECK_CUDA(cudaEventSynchronize(e1));
   float ms = 0;
@@ -801,8 +802,8 @@ double residual_norms(ki_factor* f, const double* b, const double* mu, const dou
   const int N = f->n_dofs, nb = f->n_border;
   apply_bordered(f, mu, alpha, ncols, r1, r2, s, target, rec);
   if (rec) rec->begin("residual_other", 0);
-  k_residual<<<grid_for((size_t)N * ncols), 256, 0, s>>>(b, N, r1, N, N, ncols, r1, N);
-  if (nb > 0) k_residual<<<grid_for((size_t)nb * ncols), 256, 0, s>>>(nullptr, 0, r2, nb, nb, ncols, r2, nb);
+  ki::launch(k_residual, grid_for((size_t)N * ncols), 256, 0, s, b, N, r1, N, N, ncols, r1, N);
+  if (nb > 0) ki::launch(k_residual, grid_for((size_t)nb * ncols), 256, 0, s, nullptr, 0, r2, nb, nb, ncols, r2, nb);
   KI_CHECK_CUDA(cudaGetLastError());
   const double worst = column_norms(f, b, r1, r2, ncols, work, rel, s);
   if (rec) rec->end();
@@ -818,8 +819,8 @@ double update_residual(ki_factor* f, const double* b, const double* d, const dou
   const int N = f->n_dofs, nb = f->n_border;
   apply_bordered(f, d, dal, ncols, y1, y2, s, 0.0, rec, true);
   if (rec) rec->begin("residual_other", 0);
-  k_residual<<<grid_for((size_t)N * ncols), 256, 0, s>>>(r1, N, y1, N, N, ncols, r1, N);
-  if (nb > 0) k_residual<<<grid_for((size_t)nb * ncols), 256, 0, s>>>(r2, nb, y2, nb, nb, ncols, r2, nb);
+  ki::launch(k_residual, grid_for((size_t)N * ncols), 256, 0, s, r1, N, y1, N, N, ncols, r1, N);
+  if (nb > 0) ki::launch(k_residual, grid_for((size_t)nb * ncols), 256, 0, s, r2, nb, y2, nb, nb, ncols, r2, nb);
   KI_CHECK_CUDA(cudaGetLastError());
   const double worst = column_norms(f, b, r1, r2, ncols, work, rel, s);
   if (rec) rec->end();
@@ -834,14 +835,14 @@ double column_norms(ki_factor* f, const double* b, const double* r1, const doubl
   double* part = work;
   double* sq = work + (size_t)kNormBlocks * ncols;
   double* sqb = sq + ncols;
-  k_colsq_partial<<<dim3(kNormBlocks, ncols), 256, 0, s>>>(r1, N, N, part);
-  k_colsq_final<<<(ncols + 127) / 128, 128, 0, s>>>(part, kNormBlocks, ncols, sq, 0);
+  ki::launch(k_colsq_partial, dim3(kNormBlocks, ncols), 256, 0, s, r1, N, N, part);
+  ki::launch(k_colsq_final, (ncols + 127) / 128, 128, 0, s, part, kNormBlocks, ncols, sq, 0);
   if (nb > 0) {
-    k_colsq_partial<<<dim3(1, ncols), 256, 0, s>>>(r2, nb, nb, part);
-    k_colsq_final<<<(ncols + 127) / 128, 128, 0, s>>>(part, 1, ncols, sq, 1);
+    ki::launch(k_colsq_partial, dim3(1, ncols), 256, 0, s, r2, nb, nb, part);
+    ki::launch(k_colsq_final, (ncols + 127) / 128, 128, 0, s, part, 1, ncols, sq, 1);
   }
-  k_colsq_partial<<<dim3(kNormBlocks, ncols), 256, 0, s>>>(b, N, N, part);
-  k_colsq_final<<<(ncols + 127) / 128, 128, 0, s>>>(part, kNormBlocks, ncols, sqb, 0);
+  ki::launch(k_colsq_partial, dim3(kNormBlocks, ncols), 256, 0, s, b, N, N, part);
+  ki::launch(k_colsq_final, (ncols + 127) / 128, 128, 0, s, part, kNormBlocks, ncols, sqb, 0);
   KI_CHECK_CUDA(cudaGetLastError());
   std::vector<double> h(2 * (size_t)ncols);
   KI_CHECK_CUDA(cudaMemcpyAsync(h.data(), sq, sizeof(double) * 2 * ncols, cudaMemcpyDeviceToHost, s));
@@ -866,8 +867,8 @@ void correct(ki_factor* f, ki::Factorization<T>& F, const double* r1, const doub
   const int N = f->n_dofs, nb = f->n_border;
   DevBuf<T> work((size_t)N * ncols, s), al((size_t)std::max(1, nb) * ncols, s),
       g((size_t)std::max(1, nb) * ncols, s);
-  k_to_dofmajor<double, T><<<grid_for((size_t)N * ncols), 256, 0, s>>>(r1, N, N, ncols, work.p);
-  if (nb > 0) k_to_rowmajor<T><<<grid_for((size_t)nb * ncols), 256, 0, s>>>(r2, nb, nb, ncols, g.p);
+  ki::launch(k_to_dofmajor<double, T>, grid_for((size_t)N * ncols), 256, 0, s, r1, N, N, ncols, work.p);
+  if (nb > 0) ki::launch(k_to_rowmajor<T>, grid_for((size_t)nb * ncols), 256, 0, s, r2, nb, nb, ncols, g.p);
   KI_CHECK_CUDA(cudaGetLastError());
   cudaStream_t saved = F.stream;
   F.stream = s;
@@ -878,9 +879,9 @@ void correct(ki_factor* f, ki::Factorization<T>& F, const double* r1, const doub
     throw;
   }
   F.stream = saved;
-  k_add_dofmajor<T><<<grid_for((size_t)N * ncols), 256, 0, s>>>(work.p, N, ncols, mu, N, dcol);
+  ki::launch(k_add_dofmajor<T>, grid_for((size_t)N * ncols), 256, 0, s, work.p, N, ncols, mu, N, dcol);
   if (nb > 0)
-    k_add_rowmajor<T><<<grid_for((size_t)nb * ncols), 256, 0, s>>>(al.p, nb, ncols, alpha, nb, dal);
+    ki::launch(k_add_rowmajor<T>, grid_for((size_t)nb * ncols), 256, 0, s, al.p, nb, ncols, alpha, nb, dal);
   KI_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -1066,17 +1067,17 @@ void apply_bordered(ki_factor* f, const double* mu, const double* alpha, int nco
       auto tile = low ? k_border_apply_tile<float> : k_border_apply_tile<double>;
       KI_CHECK_CUDA(cudaFuncSetAttribute(tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          100 * 1024));
-      tile<<<(N + kBorderTile - 1) / kBorderTile, 256, tsm, s>>>(
+      ki::launch(tile, (N + kBorderTile - 1) / kBorderTile, 256, tsm, s,
           f->P.x, f->P.y, f->P.z, f->n_points, f->dim, f->sol_dim, f->d_holes, f->n_holes, alpha,
           nb, ncols, y1, N);
     } else {
       auto border = low ? k_border_apply<float> : k_border_apply<double>;
-      border<<<(N + 127) / 128, 128, 0, s>>>(f->P.x, f->P.y, f->P.z, 1, f->n_points, f->dim,
+      ki::launch(border, (N + 127) / 128, 128, 0, s, f->P.x, f->P.y, f->P.z, 1, f->n_points, f->dim,
                                              f->sol_dim, f->d_holes, f->n_holes, alpha, nb, ncols,
                                              y1, N, nullptr, 0);
     }
     const int cph = nb / f->n_holes;
-    k_psi_apply<<<dim3(nb, ncols), 256, 0, s>>>(f->d_pts, f->P.w, f->dim, f->sol_dim, f->d_holes,
+    ki::launch(k_psi_apply, dim3(nb, ncols), 256, 0, s, f->d_pts, f->P.w, f->dim, f->sol_dim, f->d_holes,
                                                 f->d_hstart, f->d_hcount, cph, mu, N, alpha, nb,
                                                 y2, nb);
     KI_CHECK_CUDA(cudaGetLastError());
@@ -1152,7 +1153,7 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
         KI_CHECK_CUDA(cudaMemcpyAsync(d_in + (2 * dim + 1) * nn, desc->curvatures,
                                       sizeof(double) * nn, cudaMemcpyHostToDevice, f->stream));
       KI_CHECK_CUDA(cudaMalloc(&f->d_geo, sizeof(double) * 8 * nn));
-      k_geo_soa<<<std::min(2048, (n + 255) / 256), 256, 0, f->stream>>>(
+      ki::launch(k_geo_soa, std::min(2048, (n + 255) / 256), 256, 0, f->stream,
           d_in, n, dim, desc->curvatures != nullptr, f->d_geo);
       KI_CHECK_CUDA(cudaGetLastError());
     }
@@ -1330,9 +1331,9 @@ int ki_apply(ki_factor* f, const double* x, int ldx, int ncols, const double* al
       KI_CHECK_CUDA(cudaMemcpy2DAsync(da.p, sizeof(double) * f->n_border, alpha,
                                       sizeof(double) * ldalpha, sizeof(double) * f->n_border,
                                       ncols, cudaMemcpyHostToDevice, s));
-      k_border_apply<<<(N + 127) / 128, 128, 0, s>>>(
+      ki::launch(k_border_apply<double>, (N + 127) / 128, 128, 0, s,
           f->P.x, f->P.y, f->P.z, 1, f->n_points, f->dim, f->sol_dim, f->d_holes, f->n_holes, da.p,
-          f->n_border, ncols, dy.p, N);
+          f->n_border, ncols, dy.p, N, (const int*)nullptr, 0);
       KI_CHECK_CUDA(cudaGetLastError());
       KI_CHECK_CUDA(cudaMemcpy2DAsync(y, sizeof(double) * ldy, dy.p, sizeof(double) * N,
                                       sizeof(double) * N, ncols, cudaMemcpyDeviceToHost, s));
@@ -1370,9 +1371,9 @@ int ki_apply_fmm_ex(ki_factor* f, const double* x, int ldx, int ncols, const dou
       DevBuf<double> da((size_t)nb * ncols, s);
       KI_CHECK_CUDA(cudaMemcpy2DAsync(da.p, sizeof(double) * nb, alpha, sizeof(double) * ldalpha,
                                       sizeof(double) * nb, ncols, cudaMemcpyHostToDevice, s));
-      k_border_apply<<<(N + 127) / 128, 128, 0, s>>>(f->P.x, f->P.y, f->P.z, 1, f->n_points, f->dim,
-                                                     f->sol_dim, f->d_holes, f->n_holes, da.p, nb,
-                                                     ncols, dy.p, N);
+      ki::launch(k_border_apply<double>, (N + 127) / 128, 128, 0, s, f->P.x, f->P.y, f->P.z, 1,
+                 f->n_points, f->dim, f->sol_dim, f->d_holes, f->n_holes, da.p, nb, ncols, dy.p, N,
+                 (const int*)nullptr, 0);
       KI_CHECK_CUDA(cudaGetLastError());
       KI_CHECK_CUDA(cudaStreamSynchronize(s));
     }
@@ -1405,9 +1406,9 @@ int ki_apply_rows(ki_factor* f, const int* rows, int nrows, const double* x, int
       KI_CHECK_CUDA(cudaMemcpy2DAsync(da.p, sizeof(double) * f->n_border, alpha,
                                       sizeof(double) * ldalpha, sizeof(double) * f->n_border,
                                       ncols, cudaMemcpyHostToDevice, s));
-      k_border_apply<<<(nrows + 127) / 128, 128, 0, s>>>(
+      ki::launch(k_border_apply<double>, (nrows + 127) / 128, 128, 0, s,
           f->P.x, f->P.y, f->P.z, 1, f->n_points, f->dim, f->sol_dim, f->d_holes, f->n_holes, da.p,
-          f->n_border, ncols, dy.p, nrows, dr.p, nrows);
+          f->n_border, ncols, dy.p, nrows, (const int*)dr.p, nrows);
       KI_CHECK_CUDA(cudaGetLastError());
       KI_CHECK_CUDA(cudaStreamSynchronize(s));
     }
@@ -1439,9 +1440,9 @@ int ki_eval_targets(ki_factor* f, const double* targets, int n_targets, const do
       KI_CHECK_CUDA(cudaMemcpy2DAsync(da.p, sizeof(double) * f->n_border, alpha,
                                       sizeof(double) * ldalpha, sizeof(double) * f->n_border,
                                       ncols, cudaMemcpyHostToDevice, s));
-      k_border_apply<<<(NT + 127) / 128, 128, 0, s>>>(dt.p, dt.p + 1, dt.p + 2, dim, n_targets, dim,
-                                                      f->sol_dim, f->d_holes, f->n_holes, da.p,
-                                                      f->n_border, ncols, dout.p, NT);
+      ki::launch(k_border_apply<double>, (NT + 127) / 128, 128, 0, s, dt.p, dt.p + 1, dt.p + 2,
+                 dim, n_targets, dim, f->sol_dim, f->d_holes, f->n_holes, da.p, f->n_border, ncols,
+                 dout.p, NT, (const int*)nullptr, 0);
       KI_CHECK_CUDA(cudaGetLastError());
       KI_CHECK_CUDA(cudaStreamSynchronize(s));
     }
@@ -1650,6 +1651,8 @@ int ki_factor_get_box_log(const ki_factor* f, float* out, int max_rows, int* row
 int ki_trim_memory(void) {
   return guarded([&] { KI_CHECK_CUDA(ki::pool_trim()); });
 }
+
+long long ki_launch_count(void) { return ki::launch_counter().load(); }
 
 const char* ki_last_error(void) { return g_last_error.c_str(); }
 

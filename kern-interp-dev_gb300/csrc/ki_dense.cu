@@ -10,6 +10,7 @@
 //   k_lu_gemm    A22 -= L21 U12, 64 x 64 output tiles staged in shared memory
 // Solves: pivots, then blocked forward/backward substitution whose
 // off-diagonal updates run on the whole GPU.
+#include "ki_launch.cuh"
 #include "ki_dense.h"
 
 #include <algorithm>
@@ -316,13 +317,13 @@ template <typename T>
 void dense_lu(T* A, int n, int* piv, int* err, cudaStream_t s) {
   for (int p = 0; p < n; p += kNb) {
     int w = std::min(kNb, n - p);
-    k_lu_panel<T><<<1, 1024, 0, s>>>(A, n, n, p, w, piv, err);
-    k_lu_swap<T><<<(n + 255) / 256, 256, 0, s>>>(A, n, n, p, w, piv);
+    ki::launch(k_lu_panel<T>, 1, 1024, 0, s, A, n, n, p, w, piv, err);
+    ki::launch(k_lu_swap<T>, (n + 255) / 256, 256, 0, s, A, n, n, p, w, piv);
     int rest = n - p - w;
     if (rest > 0) {
-      k_lu_trsm<T><<<(rest + 127) / 128, 128, 0, s>>>(A, n, n, p, w);
+      ki::launch(k_lu_trsm<T>, (rest + 127) / 128, 128, 0, s, A, n, n, p, w);
       dim3 g((rest + 63) / 64, (rest + 63) / 64);
-      k_lu_gemm<T><<<g, 256, 0, s>>>(A, n, n, p, w);
+      ki::launch(k_lu_gemm<T>, g, 256, 0, s, A, n, n, p, w);
     }
   }
   KI_DENSE_CUDA(cudaGetLastError());
@@ -336,47 +337,47 @@ void dense_lu_solve(const T* LU, int n, const int* piv, T* B, int ldb, int nrhs,
   if (!trans && fused_solve_smem<T>(n) <= 160 * 1024) {
     KI_DENSE_CUDA(cudaFuncSetAttribute(k_lu_solve_fused<T>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
-    k_lu_solve_fused<T><<<(nrhs + 31) / 32, 256, fused_solve_smem<T>(n), s>>>(LU, n, piv, B, ldb,
+    ki::launch(k_lu_solve_fused<T>, (nrhs + 31) / 32, 256, fused_solve_smem<T>(n), s, LU, n, piv, B, ldb,
                                                                              nrhs);
     KI_DENSE_CUDA(cudaGetLastError());
     return;
   }
   if (!trans) {
-    k_apply_piv<T><<<cb, 128, 0, s>>>(B, ldb, nrhs, piv, n, false);
+    ki::launch(k_apply_piv<T>, cb, 128, 0, s, B, ldb, nrhs, piv, n, false);
     for (int p = 0; p < n; p += kNb) {       // L y = b (unit lower)
       int w = std::min(kNb, n - p);
-      k_tri_block<T><<<cb, 128, 0, s>>>(LU, n, p, w, B, ldb, nrhs, true, false);
+      ki::launch(k_tri_block<T>, cb, 128, 0, s, LU, n, p, w, B, ldb, nrhs, true, false);
       if (p + w < n) {
         dim3 g((n - p - w + 127) / 128, (nrhs + 31) / 32);
-        k_tri_update<T><<<g, 128, 0, s>>>(LU, n, p, w, p + w, n, B, ldb, nrhs, false);
+        ki::launch(k_tri_update<T>, g, 128, 0, s, LU, n, p, w, p + w, n, B, ldb, nrhs, false);
       }
     }
     for (int p = ((n - 1) / kNb) * kNb; p >= 0; p -= kNb) {   // U x = y
       int w = std::min(kNb, n - p);
-      k_tri_block<T><<<cb, 128, 0, s>>>(LU, n, p, w, B, ldb, nrhs, false, false);
+      ki::launch(k_tri_block<T>, cb, 128, 0, s, LU, n, p, w, B, ldb, nrhs, false, false);
       if (p > 0) {
         dim3 g((p + 127) / 128, (nrhs + 31) / 32);
-        k_tri_update<T><<<g, 128, 0, s>>>(LU, n, p, w, 0, p, B, ldb, nrhs, false);
+        ki::launch(k_tri_update<T>, g, 128, 0, s, LU, n, p, w, 0, p, B, ldb, nrhs, false);
       }
     }
   } else {
     for (int p = 0; p < n; p += kNb) {       // U^T y = b (lower, U's diagonal)
       int w = std::min(kNb, n - p);
-      k_tri_block<T><<<cb, 128, 0, s>>>(LU, n, p, w, B, ldb, nrhs, true, true);
+      ki::launch(k_tri_block<T>, cb, 128, 0, s, LU, n, p, w, B, ldb, nrhs, true, true);
       if (p + w < n) {
         dim3 g((n - p - w + 127) / 128, (nrhs + 31) / 32);
-        k_tri_update<T><<<g, 128, 0, s>>>(LU, n, p, w, p + w, n, B, ldb, nrhs, true);
+        ki::launch(k_tri_update<T>, g, 128, 0, s, LU, n, p, w, p + w, n, B, ldb, nrhs, true);
       }
     }
     for (int p = ((n - 1) / kNb) * kNb; p >= 0; p -= kNb) {   // L^T x = y (unit upper)
       int w = std::min(kNb, n - p);
-      k_tri_block<T><<<cb, 128, 0, s>>>(LU, n, p, w, B, ldb, nrhs, false, true);
+      ki::launch(k_tri_block<T>, cb, 128, 0, s, LU, n, p, w, B, ldb, nrhs, false, true);
       if (p > 0) {
         dim3 g((p + 127) / 128, (nrhs + 31) / 32);
-        k_tri_update<T><<<g, 128, 0, s>>>(LU, n, p, w, 0, p, B, ldb, nrhs, true);
+        ki::launch(k_tri_update<T>, g, 128, 0, s, LU, n, p, w, 0, p, B, ldb, nrhs, true);
       }
     }
-    k_apply_piv<T><<<cb, 128, 0, s>>>(B, ldb, nrhs, piv, n, true);
+    ki::launch(k_apply_piv<T>, cb, 128, 0, s, B, ldb, nrhs, piv, n, true);
   }
   KI_DENSE_CUDA(cudaGetLastError());
 }

@@ -19,6 +19,7 @@
 //                    box's accumulated self-block K_ss - L K~_rs
 //
 // The host reads back only the ranks of each level (to size the next level).
+#include "ki_launch.cuh"
 #include "ki_pool.h"
 #include "ki_factor.h"
 
@@ -1492,7 +1493,7 @@ void gemm(cudaStream_t s, int m, int n, int kk, T alpha, const T* A, int lda, bo
           int ldb, bool tb, T beta, T* C, int ldc) {
   if (m <= 0 || n <= 0) return;
   dim3 g((m + 63) / 64, (n + 63) / 64);
-  k_gemm<T><<<g, 256, 0, s>>>(m, n, kk, alpha, A, lda, ta, B, ldb, tb, beta, C, ldc,
+  ki::launch(k_gemm<T>, g, 256, 0, s, m, n, kk, alpha, A, lda, ta, B, ldb, tb, beta, C, ldc,
                               std::max(kk, 1), 0, 0, 0);
 }
 
@@ -1519,7 +1520,7 @@ template <typename T>
 void copy_block(cudaStream_t s, const T* src, int lds, int rows, int cols, bool trans, T* dst, int ldd) {
   size_t ne = (size_t)rows * cols;
   if (ne == 0) return;
-  k_copy_block<T><<<(int)std::min<size_t>(2048, (ne + 255) / 256), 256, 0, s>>>(src, lds, rows, cols,
+  ki::launch(k_copy_block<T>, (int)std::min<size_t>(2048, (ne + 255) / 256), 256, 0, s, src, lds, rows, cols,
                                                                               trans, dst, ldd);
 }
 
@@ -1543,7 +1544,7 @@ void schur_wide(const SchurTask<T>& t, int* d_err, cudaStream_t st) {
   T* X = t.X;
   const T* Tm = t.Tin;
   size_t ne = (size_t)n * n;
-  k_perm_gather<T><<<(int)std::min<size_t>(4096, (ne + 255) / 256), 256, 0, st>>>(t.K, n, t.perm, Pm);
+  ki::launch(k_perm_gather<T>, (int)std::min<size_t>(4096, (ne + 255) / 256), 256, 0, st, t.K, n, t.perm, Pm);
   KI_CUDA(cudaMemcpyAsync(t.Tout, t.Tin, sizeof(T) * (size_t)k * r, cudaMemcpyDeviceToDevice, st));
   const T* Kss = Pm;
   const T* Ksr = Pm + (size_t)n * k;
@@ -2045,7 +2046,7 @@ void mc_update(T* x, int nc, const T* Um, int nb, const T* M, int nr, int N,
                const unsigned char* mask, cudaStream_t s) {
   if (N <= 0 || nc <= 0 || nb <= 0) return;
   dim3 g((unsigned)std::max(1, std::min(4096, (N + 255) / 256)), (unsigned)((nc + 31) / 32));
-  k_mc_update<T><<<g, 256, 0, s>>>(x, nc, Um, nb, M, nr, N, mask);
+  ki::launch(k_mc_update<T>, g, 256, 0, s, x, nc, Um, nb, M, nr, N, mask);
 }
 
 // x(allskel, :) = M(0:nr, :), alpha (row-major nb x nc) = M(nr:, :)
@@ -2179,7 +2180,7 @@ void launch_diag_all(Factorization<T>& F, T* x, int ncols, cudaStream_t s) {
     if (staged) sm += mats;
     if (sm > 48 * 1024)
       KI_CUDA(cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    k_sweep<T><<<grid, kThreads, sm, st>>>(all + b[0], x, ncols, ncols, cw, kDiag, staged);
+    ki::launch(k_sweep<T>, grid, kThreads, sm, st, all + b[0], x, ncols, ncols, cw, kDiag, staged);
     KI_CUDA(cudaGetLastError());
   }
   if (par) F.join(std::min(next, Factorization<T>::kAux));
@@ -2202,7 +2203,7 @@ void launch_sweep(Factorization<T>& F, int l, int mode, T* x, int ncols, cudaStr
   if (staged) sm += mats;
   if (sm > 48 * 1024)
     KI_CUDA(cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  k_sweep<T><<<grid, kThreads, sm, s>>>(reinterpret_cast<SweepTask<T>*>(LF.d_tasks), x, ncols,
+  ki::launch(k_sweep<T>, grid, kThreads, sm, s, reinterpret_cast<SweepTask<T>*>(LF.d_tasks), x, ncols,
                                         ncols, cw, mode, staged);
   KI_CUDA(cudaGetLastError());
 }
@@ -2218,8 +2219,8 @@ void reduce_rows(Factorization<T>& F, const T* A, int na, const T* B, int nc, T*
   size_t sm = sizeof(T) * 32 * (size_t)(na + nc);
   if (sm > 48 * 1024)
     KI_CUDA(cudaFuncSetAttribute(k_reduce_partial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  k_reduce_partial<T><<<parts, 256, sm, s>>>(A, na, B, nc, F.N, F.d_is_skel, partial);
-  k_reduce_final<T><<<std::max(1, (na * nc + 255) / 256), 256, 0, s>>>(partial, parts, na * nc, out);
+  ki::launch(k_reduce_partial<T>, parts, 256, sm, s, A, na, B, nc, F.N, F.d_is_skel, partial);
+  ki::launch(k_reduce_final<T>, std::max(1, (na * nc + 255) / 256), 256, 0, s, partial, parts, na * nc, out);
   KI_CUDA(cudaGetLastError());
   KI_CUDA(cudaFreeAsync(partial, s));
 }
@@ -2239,16 +2240,16 @@ template <typename T>
 void reduce_rows_wide(Factorization<T>& F, const T* A, int na, T* B, int nc, T* out,
                       cudaStream_t s) {
   const int N = F.N;
-  k_zero_rows<T><<<std::min(8192, (int)(((size_t)N * nc + 255) / 256)), 256, 0, s>>>(B, nc, F.d_is_skel, N);
+  ki::launch(k_zero_rows<T>, std::min(8192, (int)(((size_t)N * nc + 255) / 256)), 256, 0, s, B, nc, F.d_is_skel, N);
   const int chunk = 16384;
   const int parts = (N + chunk - 1) / chunk;
   T* partial = nullptr;
   KI_CUDA(pool_malloc((void**)&partial, sizeof(T) * (size_t)parts * na * nc + 16, s));
   // DOF-major A is the column-major na x N matrix Ac; out = Ac * Bc^T
   dim3 g((na + 63) / 64, (nc + 63) / 64, parts);
-  k_gemm<T><<<g, 256, 0, s>>>(na, nc, N, T(1), A, na, 0, B, nc, 1, T(0), partial, na, chunk,
+  ki::launch(k_gemm<T>, g, 256, 0, s, na, nc, N, T(1), A, na, 0, B, nc, 1, T(0), partial, na, chunk,
                               (int64_t)chunk * na, (int64_t)chunk * nc, (int64_t)na * nc);
-  k_reduce_final<T><<<std::max(1, (na * nc + 255) / 256), 256, 0, s>>>(partial, parts, na * nc, out);
+  ki::launch(k_reduce_final<T>, std::max(1, (na * nc + 255) / 256), 256, 0, s, partial, parts, na * nc, out);
   KI_CUDA(cudaGetLastError());
   KI_CUDA(cudaFreeAsync(partial, s));
 }
@@ -2297,7 +2298,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     }
     // FP32: low parts of the coordinates
     T* lo = sizeof(T) < sizeof(double) ? d + 8 * np_ : nullptr;
-    k_fill_points<T><<<std::min(1024, (n_points + 255) / 256), 256, 0, s>>>(
+    ki::launch(k_fill_points<T>, std::min(1024, (n_points + 255) / 256), 256, 0, s,
         d_pts_in, d_nrm_in, d_w_in, curvatures ? d_k_in : nullptr, n_points, dim, F->d_x,
         F->d_y, F->d_z, F->d_nx, F->d_ny, F->d_nz, F->d_w, F->d_kappa, lo);
     if (lo) {
@@ -2363,14 +2364,14 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     KI_CUDA(cudaMemcpyAsync(d_g + n_points, ghi.data(), sizeof(int) * n_points, cudaMemcpyHostToDevice, s));
     F->d_diag64 = (double*)F->alloc(sizeof(double) * (size_t)dpp * n_points);
     F->stage_begin("diag3", (sd == 1 ? 20.0 : 80.0) * (double)n_points * n_points, 0);
-    k_diag3<<<(n_points + kDiagThreads - 1) / kDiagThreads, kDiagThreads, 0, s>>>(
+    ki::launch(k_diag3, (n_points + kDiagThreads - 1) / kDiagThreads, kDiagThreads, 0, s,
         d_pts_in, d_nrm_in, d_w_in, n_points, d_g, d_g + n_points, n_outer, sd, F->d_diag64);
     F->stage_end();
     KI_CUDA(cudaGetLastError());
     // synchronize on the (host) group arrays before they go out of scope
     KI_CUDA(cudaStreamSynchronize(s));
     F->d_diag = (T*)F->alloc(sizeof(T) * (size_t)dpp * n_points);
-    k_convert<T><<<std::min(2048, (dpp * n_points + 255) / 256), 256, 0, s>>>(
+    ki::launch(k_convert<T>, std::min(2048, (dpp * n_points + 255) / 256), 256, 0, s,
         F->d_diag64, (size_t)dpp * n_points, F->d_diag);
     KI_CUDA(cudaGetLastError());
     P.diag = F->d_diag;
@@ -2461,7 +2462,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       for (auto& a : atasks)
         for (int q = 0; q < a.nseg; q++) nb += 8.0 * a.len[q];
       F->stage_begin("active_lists", 0, nb);
-      k_build_active<<<(unsigned)atasks.size(), 128, 0, s>>>(d_at, ipool);
+      ki::launch(k_build_active, (unsigned)atasks.size(), 128, 0, s, d_at, ipool);
       F->stage_end();
       KI_CUDA(cudaGetLastError());
     }
@@ -2509,7 +2510,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       double ne = 0;
       for (auto& a : asm_tasks) ne += (double)a.n * a.n;
       F->stage_begin("assemble", 12.0 * ne, (double)sizeof(T) * ne);
-      k_assemble<T><<<(unsigned)asm_tasks.size(), kThreads, 0, s>>>(d_as, ipool, P, sd);
+      ki::launch(k_assemble<T>, (unsigned)asm_tasks.size(), kThreads, 0, s, d_as, ipool, P, sd);
       F->stage_end();
       KI_CUDA(cudaGetLastError());
     }
@@ -2596,7 +2597,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     // (a) row lists of every box (m is needed to pick the path)
     KI_CUDA(cudaFuncSetAttribute(k_id<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
     KI_CUDA(cudaFuncSetAttribute(k_id<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
-    k_id<T, 32><<<(unsigned)itasks.size(), kThreads, 0, s>>>(d_it, 0, d_soff, d_slen, ipool, d_irows, d_tws,
+    ki::launch(k_id<T, 32>, (unsigned)itasks.size(), kThreads, 0, s, d_it, 0, d_soff, d_slen, ipool, d_irows, d_tws,
                                                          P, sd, ptab, prm.id_tol,
                                                          d_k, d_m, 0, 1, nullptr);
     KI_CUDA(cudaGetLastError());
@@ -2605,7 +2606,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     float* d_feat = (float*)F->alloc(sizeof(float) * kMlpIn * (size_t)ntask);
     int* d_lsk = (int*)F->alloc(sizeof(int) * (size_t)ntask);
     float* d_khat = (float*)F->alloc(sizeof(float) * (size_t)ntask);
-    k_box_features<T><<<(ntask + 3) / 4, 128, 0, s>>>(
+    ki::launch(k_box_features<T>, (ntask + 3) / 4, 128, 0, s,
         d_it, ntask, ipool, P, sd, d_m, 2 * np * sd, L > 1 ? (float)l / (float)(L - 1) : 0.f,
         (float)(-std::log10(prm.id_tol) / 10.0), prm.rank_model, prm.sketch_margin,
         prm.sketch_oversample, d_feat, d_lsk, d_khat);
@@ -2713,12 +2714,12 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         if (sm > smem_cap) throw std::runtime_error("box too large for the ID kernel");
         cudaStream_t st = fixed ? fixed : F->aux[(next_aux++) % (Factorization<T>::kAux - 1)];
         if (fr == 64)
-          k_id<T, 64><<<(unsigned)(b1 - b0), kThreads, sm, st>>>(d_it, b0, d_soff, d_slen, ipool, d_irows,
+          ki::launch(k_id<T, 64>, (unsigned)(b1 - b0), kThreads, sm, st, d_it, b0, d_soff, d_slen, ipool, d_irows,
                                                                  d_tws, P, sd, ptab,
                                                                  prm.id_tol, d_k, d_m, kmode, flags,
                                                                  sketching && g != 1 ? d_lsk : nullptr);
         else
-          k_id<T, 32><<<(unsigned)(b1 - b0), kThreads, sm, st>>>(d_it, b0, d_soff, d_slen, ipool, d_irows,
+          ki::launch(k_id<T, 32>, (unsigned)(b1 - b0), kThreads, sm, st, d_it, b0, d_soff, d_slen, ipool, d_irows,
                                                                  d_tws, P, sd, ptab,
                                                                  prm.id_tol, d_k, d_m, kmode, flags,
                                                                  sketching && g != 1 ? d_lsk : nullptr);
@@ -2781,14 +2782,14 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
           KI_CUDA(pool_malloc((void**)&d_wpool, sizeof(T) * (mtot + 16), ws3));
           KI_CUDA(pool_malloc((void**)&d_wt, sizeof(WideTask) * wt.size(), ws3));
           upload(d_wt, wt, ws3);
-          k_wide_assemble<T><<<dim3((unsigned)wt.size(), (maxn + 7) / 8), 256, 0, ws3>>>(
+          ki::launch(k_wide_assemble<T>, dim3((unsigned)wt.size(), (maxn + 7) / 8), 256, 0, ws3,
               d_wt, d_wpool, ipool, d_irows, P, sd, ptab);
           for (int p0 = 0; p0 < maxn; p0 += kQrNb) {
-            k_qr_panel<T><<<(unsigned)wt.size(), 256, 0, ws3>>>(d_wt, d_wpool, p0);
+            ki::launch(k_qr_panel<T>, (unsigned)wt.size(), 256, 0, ws3, d_wt, d_wpool, p0);
             int tiles = (maxn - p0 - kQrNb + kQrTile - 1) / kQrTile;
-            if (tiles > 0) k_qr_update<T><<<dim3((unsigned)wt.size(), tiles), 256, 0, ws3>>>(d_wt, d_wpool, p0);
+            if (tiles > 0) ki::launch(k_qr_update<T>, dim3((unsigned)wt.size(), tiles), 256, 0, ws3, d_wt, d_wpool, p0);
           }
-          k_wide_triangle<T><<<(unsigned)wt.size(), 256, 0, ws3>>>(d_wt, d_wpool, d_tws);
+          ki::launch(k_wide_triangle<T>, (unsigned)wt.size(), 256, 0, ws3, d_wt, d_wpool, d_tws);
           KI_CUDA(cudaGetLastError());
         }
         T* d_spool = nullptr;
@@ -2801,9 +2802,9 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
                              sizeof(uint32_t) * kSketchSub * ((max_l + 31) / 32);
           KI_CUDA(cudaFuncSetAttribute(k_wide_sketch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem_cap));
-          k_wide_sketch<T><<<dim3((unsigned)wsk.size(), max_chunks, max_cb), 256, skm, ws3>>>(
+          ki::launch(k_wide_sketch<T>, dim3((unsigned)wsk.size(), max_chunks, max_cb), 256, skm, ws3,
               d_wsk, d_spool, ipool, d_irows, P, sd, ptab);
-          k_wide_sketch_reduce<T><<<(unsigned)wsk.size(), 256, 0, ws3>>>(d_wsk, d_spool, d_tws);
+          ki::launch(k_wide_sketch_reduce<T>, (unsigned)wsk.size(), 256, 0, ws3, d_wsk, d_spool, d_tws);
           KI_CUDA(cudaGetLastError());
         }
         F->stage_end(ws3);
@@ -2860,11 +2861,11 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         std::string fname = "id_fallback@L" + std::to_string(l);
         F->stage_begin(fname.c_str(), 0, 0);
         if (cnt0 > 0)
-          k_id<T, 32><<<(unsigned)cnt0, kThreads, sm[0], s>>>(d_t2, 0, d_soff, d_slen, ipool, d_irows,
+          ki::launch(k_id<T, 32>, (unsigned)cnt0, kThreads, sm[0], s, d_t2, 0, d_soff, d_slen, ipool, d_irows,
                                                                d_tws, P, sd, ptab, prm.id_tol, d_k2,
                                                                d_m2, 0, 2, nullptr);
         if ((int)t2.size() > cnt0)
-          k_id<T, 32><<<(unsigned)(t2.size() - cnt0), kThreads, sm[1], s>>>(
+          ki::launch(k_id<T, 32>, (unsigned)(t2.size() - cnt0), kThreads, sm[1], s,
               d_t2, cnt0, d_soff, d_slen, ipool, d_irows, d_tws, P, sd, ptab, prm.id_tol, d_k2, d_m2,
               1, 2, nullptr);
         F->stage_end();
@@ -3049,12 +3050,12 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         int b1 = b0 + 1;
         while (b1 < n_sm && per_sm(schur_task_bytes<T>(st2[b1])) == ps) b1++;
         const size_t bsm = schur_task_bytes<T>(st2[b1 - 1]);
-        k_schur<T><<<(unsigned)(b1 - b0), kThreads, bsm, F->aux[(next++) % Factorization<T>::kAux]>>>(
+        ki::launch(k_schur<T>, (unsigned)(b1 - b0), kThreads, bsm, F->aux[(next++) % Factorization<T>::kAux],
             d_st, b0, 1, F->d_err);
         b0 = b1;
       }
       if (n_glob > 0)
-        k_schur<T><<<(unsigned)n_glob, kThreads, 0, F->aux[(next++) % Factorization<T>::kAux]>>>(
+        ki::launch(k_schur<T>, (unsigned)n_glob, kThreads, 0, F->aux[(next++) % Factorization<T>::kAux],
             d_st, n_sm, 0, F->d_err);
       for (size_t q = n_sm + n_glob; q < st2.size(); q++)
         schur_wide<T>(st2[q], F->d_err, F->aux[(next++) % Factorization<T>::kAux]);
@@ -3085,7 +3086,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
           const int r = inv[q].n - inv[q].k;
           cudaStream_t as = F->aux[q % Factorization<T>::kAux];
           T* Xi = const_cast<T*>(inv[q].Xi);
-          k_set_identity<T><<<std::max(1, std::min(1024, (r * r + 255) / 256)), 256, 0, as>>>(Xi, r);
+          ki::launch(k_set_identity<T>, std::max(1, std::min(1024, (r * r + 255) / 256)), 256, 0, as, Xi, r);
           dense_lu_solve<T>(inv[q].X, r, inv[q].piv, Xi, r, r, false, as);
         }
         F->join(Factorization<T>::kAux);
@@ -3151,11 +3152,11 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       }
       AsmTask<T>* d_as = (AsmTask<T>*)F->alloc(sizeof(AsmTask<T>));
       KI_CUDA(cudaMemcpyAsync(d_as, &at, sizeof(at), cudaMemcpyHostToDevice, s));
-      k_assemble<T><<<1, kThreads, 0, s>>>(d_as, ipool, P, sd);
+      ki::launch(k_assemble<T>, 1, kThreads, 0, s, d_as, ipool, P, sd);
       KI_CUDA(cudaGetLastError());
       F->d_is_skel = (unsigned char*)F->alloc(N);
       KI_CUDA(cudaMemsetAsync(F->d_is_skel, 0, N, s));
-      k_mark<<<std::max(1, (h.n + 255) / 256), 256, 0, s>>>(F->d_root_idx, h.n, F->d_is_skel);
+      ki::launch(k_mark, std::max(1, (h.n + 255) / 256), 256, 0, s, F->d_root_idx, h.n, F->d_is_skel);
       if (holes.n_holes == 0) {
         F->d_root_lu = A;
         F->d_root_piv = (int*)F->alloc(sizeof(int) * h.n);
@@ -3184,7 +3185,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         if (bism > 48 * 1024)
           KI_CUDA(cudaFuncSetAttribute(k_border_init<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)bism));
-        k_border_init<T><<<std::min(2048, (n_points + 255) / 256), 256, bism, s>>>(
+        ki::launch(k_border_init<T>, std::min(2048, (n_points + 255) / 256), 256, bism, s,
             d_pts_in, d_w_in, n_points, dim, sd, d_hc, nh, d_hole_of, F->d_Umod, F->d_PsiTmod);
         KI_CUDA(cudaGetLastError());
         F->stage_begin("border_sweeps", 0, 0);
@@ -3212,7 +3213,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         KI_CUDA(cudaFreeAsync(dD, s));
         const int ns = h.n + nb;
         T* S = (T*)F->alloc(Tsz * (size_t)ns * ns);
-        k_assemble_S<T><<<std::min(4096, (int)(((size_t)ns * ns + 255) / 256)), 256, 0, s>>>(
+        ki::launch(k_assemble_S<T>, std::min(4096, (int)(((size_t)ns * ns + 255) / 256)), 256, 0, s,
             A, h.n, F->d_root_idx, F->d_Umod, F->d_PsiTmod, corr, nb, S);
         KI_CUDA(cudaGetLastError());
         F->d_root_lu = S;
@@ -3258,9 +3259,9 @@ void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, const T* d
       T* ws = nullptr;
       KI_CUDA(pool_malloc((void**)&ws, sizeof(T) * (size_t)nr * ncols + 16, s));
       int gb = std::max(1, std::min(4096, (nr * ncols + 255) / 256));
-      k_gather_rows<T><<<gb, 256, 0, s>>>(d_x, ncols, F.d_root_idx, nr, ncols, ws);
+      ki::launch(k_gather_rows<T>, gb, 256, 0, s, d_x, ncols, F.d_root_idx, nr, ncols, ws);
       dense_lu_solve<T>(F.d_root_lu, nr, F.d_root_piv, ws, nr, ncols, false, s);
-      k_scatter_rows<T><<<gb, 256, 0, s>>>(d_x, ncols, F.d_root_idx, nr, ncols, ws);
+      ki::launch(k_scatter_rows<T>, gb, 256, 0, s, d_x, ncols, F.d_root_idx, nr, ncols, ws);
       se();
       KI_CUDA(cudaGetLastError());
       KI_CUDA(cudaFreeAsync(ws, s));
@@ -3291,7 +3292,7 @@ void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, const T* d
   else reduce_rows_wide<T>(F, F.d_PsiTmod, nb, Dw, ncols, t, s);
   se();
   sb("border_root");
-  k_mc_rhs<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
+  ki::launch(k_mc_rhs<T>, std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s,
       d_x, ncols, F.d_root_idx, nr, t, nb, ncols, M, d_g);
   dense_lu_solve<T>(F.d_root_lu, ns, F.d_root_piv, M, ns, ncols, false, s);
   se();
@@ -3308,7 +3309,7 @@ void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, const T* d
   sb("border_diag");
   launch_diag_all<T>(F, d_x, ncols, s);
   se();
-  k_mc_finish<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
+  ki::launch(k_mc_finish<T>, std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s,
       d_x, ncols, F.d_root_idx, M, nr, nb, d_alpha);
   KI_CUDA(cudaGetLastError());
   sb("sweep_down");
@@ -3341,8 +3342,8 @@ static void reduce_rows_arena(Factorization<T>& F, const T* A, int na, const T* 
   size_t sm = sizeof(T) * 32 * (size_t)(na + nc);
   if (sm > 48 * 1024)
     KI_CUDA(cudaFuncSetAttribute(k_reduce_partial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  k_reduce_partial<T><<<parts, 256, sm, s>>>(A, na, B, nc, F.N, F.d_is_skel, partial);
-  k_reduce_final<T><<<std::max(1, (na * nc + 255) / 256), 256, 0, s>>>(partial, parts, na * nc, out);
+  ki::launch(k_reduce_partial<T>, parts, 256, sm, s, A, na, B, nc, F.N, F.d_is_skel, partial);
+  ki::launch(k_reduce_final<T>, std::max(1, (na * nc + 255) / 256), 256, 0, s, partial, parts, na * nc, out);
   KI_CUDA(cudaGetLastError());
 }
 
@@ -3361,9 +3362,9 @@ void solve_device_arena(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, Scra
     if (nr > 0) {
       T* ws = take(sizeof(T) * (size_t)nr * ncols);
       int gb = std::max(1, std::min(4096, (nr * ncols + 255) / 256));
-      k_gather_rows<T><<<gb, 256, 0, s>>>(d_x, ncols, F.d_root_idx, nr, ncols, ws);
+      ki::launch(k_gather_rows<T>, gb, 256, 0, s, d_x, ncols, F.d_root_idx, nr, ncols, ws);
       dense_lu_solve<T>(F.d_root_lu, nr, F.d_root_piv, ws, nr, ncols, false, s);
-      k_scatter_rows<T><<<gb, 256, 0, s>>>(d_x, ncols, F.d_root_idx, nr, ncols, ws);
+      ki::launch(k_scatter_rows<T>, gb, 256, 0, s, d_x, ncols, F.d_root_idx, nr, ncols, ws);
       KI_CUDA(cudaGetLastError());
     }
     for (int l = 1; l < L; l++) launch_sweep<T>(F, l, kDown, d_x, ncols, s);
@@ -3378,13 +3379,13 @@ void solve_device_arena(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, Scra
   KI_CUDA(cudaMemcpyAsync(Dw, d_x, sizeof(T) * (size_t)N * ncols, cudaMemcpyDeviceToDevice, s));
   launch_diag_all<T>(F, Dw, ncols, s);
   reduce_rows_arena<T>(F, F.d_PsiTmod, nb, Dw, ncols, t, partial, s);
-  k_mc_rhs<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
-      d_x, ncols, F.d_root_idx, nr, t, nb, ncols, M);
+  ki::launch(k_mc_rhs<T>, std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s,
+      d_x, ncols, F.d_root_idx, nr, t, nb, ncols, M, (const T*)nullptr);
   dense_lu_solve<T>(F.d_root_lu, ns, F.d_root_piv, M, ns, ncols, false, s);
   mc_update<T>(d_x, ncols, F.d_Umod, nb, M, nr, N, F.d_is_skel, s);
   KI_CUDA(cudaGetLastError());
   launch_diag_all<T>(F, d_x, ncols, s);
-  k_mc_finish<T><<<std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s>>>(
+  ki::launch(k_mc_finish<T>, std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s,
       d_x, ncols, F.d_root_idx, M, nr, nb, d_alpha);
   KI_CUDA(cudaGetLastError());
   for (int l = 1; l < L; l++) launch_sweep<T>(F, l, kDown, d_x, ncols, s);

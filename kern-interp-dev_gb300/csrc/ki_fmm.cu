@@ -9,6 +9,7 @@
 // expansion plus the direct near-field sum with the exact kernel entries.
 // All 32 columns of a pass share every kernel-entry and translation-matrix
 // load.
+#include "ki_launch.cuh"
 #include "ki_pool.h"
 #include "ki_fmm.h"
 #include "ki_parallel.h"
@@ -956,7 +957,7 @@ void ensure_fp32(Fmm2d& F, cudaStream_t s) {
     float2* d = nullptr;
     KI_FMM_CUDA(pool_malloc((void**)&d, sizeof(float2) * count, s));
     F.owned.push_back(d);
-    k_round_cplx<<<(int)std::min<size_t>(1024, (count + 255) / 256), 256, 0, s>>>(a, count, d);
+    ki::launch(k_round_cplx, (int)std::min<size_t>(1024, (count + 255) / 256), 256, 0, s, a, count, d);
     return d;
   };
   const size_t pp = (size_t)F.p * F.p;
@@ -967,7 +968,7 @@ void ensure_fp32(Fmm2d& F, cudaStream_t s) {
     float* d = nullptr;
     KI_FMM_CUDA(pool_malloc((void**)&d, sizeof(float) * count, s));
     F.owned.push_back(d);
-    k_round_real<<<(int)std::min<size_t>(1024, (count + 255) / 256), 256, 0, s>>>(a, count, d);
+    ki::launch(k_round_real, (int)std::min<size_t>(1024, (count + 255) / 256), 256, 0, s, a, count, d);
     return d;
   };
   F.d_Mr32 = round_real(F.d_Mr, 49 * pp);
@@ -976,7 +977,7 @@ void ensure_fp32(Fmm2d& F, cudaStream_t s) {
   float4* zf = nullptr;
   KI_FMM_CUDA(pool_malloc((void**)&zf, sizeof(float4) * (size_t)F.n, s));
   F.owned.push_back(zf);
-  k_split_points<<<(F.n + 255) / 256, 256, 0, s>>>(F.d_z, F.n, zf);
+  ki::launch(k_split_points, (F.n + 255) / 256, 256, 0, s, F.d_z, F.n, zf);
   KI_FMM_CUDA(cudaGetLastError());
   F.d_zf = zf;
 }
@@ -1005,12 +1006,12 @@ void apply_impl(Fmm2d& F, const R* Tr, const R* Sr, const cplx_t<R>* Tph, const 
     const int nl2 = F.lvl_off[L + 1] - F.lvl_off[3 > L ? L + 1 : 3];
     if (rec) rec->begin(names[0], (double)n * pp * (4.0 * cx + 6.0) +
                                   cx * (double)(nbox - 1) * (2.0 * pp * (pp + 1) + 14.0 * pp));
-    k_densities<R><<<(n + 31) / 32, dim3(32, 8), 0, s>>>(F.d_perm, n, mu, ldmu, c0, nc, q);
-    k_p2m<R><<<F.nleaf, 256, 0, s>>>(F.d_leaf_start, F.d_leaf_box, F.d_centre,
+    ki::launch(k_densities<R>, (n + 31) / 32, dim3(32, 8), 0, s, F.d_perm, n, mu, ldmu, c0, nc, q);
+    ki::launch(k_p2m<R>, F.nleaf, 256, 0, s, F.d_leaf_start, F.d_leaf_box, F.d_centre,
                                      F.side0 / (double)(1L << L), F.d_z, F.d_nw, q, nc, p, me);
     for (int l = L; l >= 1; l--) {
       const int b0 = F.lvl_off[l - 1], cnt = F.lvl_off[l] - b0;
-      k_m2m<R><<<cnt, 256, 0, s>>>(b0, F.d_child, F.d_child_pos, Tr, Tph, ldm, nc, p, me);
+      ki::launch(k_m2m<R>, cnt, 256, 0, s, b0, F.d_child, F.d_child_pos, Tr, Tph, ldm, nc, p, me);
     }
     if (rec) rec->end();
     KI_FMM_CUDA(cudaMemsetAsync(le, 0, sizeof(V) * (size_t)F.lvl_off[2] * p * nc, s));
@@ -1019,19 +1020,19 @@ void apply_impl(Fmm2d& F, const R* Tr, const R* Sr, const cplx_t<R>* Tph, const 
     if (rec) rec->begin(names[1], cx * (double)F.m2l_pairs * (4.0 * pp * pp + 14.0 * pp));
     for (int l = 2; l <= L; l++) {
       const int b0 = F.lvl_off[l], cnt = F.lvl_off[l + 1] - b0;
-      k_m2l<R><<<cnt, 256, 0, s>>>(b0, F.d_v_off, F.d_v_src, F.d_v_code, Mr, Mph, ldm,
+      ki::launch(k_m2l<R>, cnt, 256, 0, s, b0, F.d_v_off, F.d_v_src, F.d_v_code, Mr, Mph, ldm,
                                    (double)(1L << l) / F.side0, nc, p, me, le);
     }
     if (rec) rec->end();
     if (rec) rec->begin(names[2], cx * (double)nl2 * (2.0 * pp * (pp + 1) + 14.0 * pp));
     for (int l = 3; l <= L; l++) {
       const int b0 = F.lvl_off[l], cnt = F.lvl_off[l + 1] - b0;
-      k_l2l<R><<<cnt, 256, 0, s>>>(b0, F.d_parent, F.d_child_pos, Sr, Tph, ldm, nc, p, le);
+      ki::launch(k_l2l<R>, cnt, 256, 0, s, b0, F.d_parent, F.d_child_pos, Sr, Tph, ldm, nc, p, le);
     }
     if (rec) rec->end();
     if (rec) rec->begin(names[3], (double)F.near_point_pairs * (2.0 * cx + 12.0) +
                                   (double)n * pp * (4.0 * cx + 6.0));
-    k_leaf_eval<R><<<F.nleaf, kLeafThreads, 0, s>>>(
+    ki::launch(k_leaf_eval<R>, F.nleaf, kLeafThreads, 0, s,
         F.d_leaf_start, F.d_leaf_box, F.d_near_off, F.d_near_leaf, F.d_centre,
         F.side0 / (double)(1L << L), F.d_z, F.d_zf, F.d_nw, F.d_nw32, F.d_diag, F.d_perm, q, le,
         nc, p, mu, ldmu, c0, y, ldy);

@@ -1,6 +1,7 @@
 // Rank-predictor MLP (see ki_mlp.h): forward, backward and Adam kernels.
 // Every reduction over samples is a fixed-order two-pass sum, so training is
 // deterministic for a given input.
+#include "ki_launch.cuh"
 #include "ki_mlp.h"
 
 #include <cmath>
@@ -154,14 +155,14 @@ struct Work {
 float loss_grad(Work& w, const float* model, const float* x, const float* y, int n) {
   cudaStream_t s = w.s;
   const int nb = (n + 127) / 128;
-  k_mlp_fwd<<<nb, 128, 0, s>>>(model, x, n, w.h1, w.h2, w.out);
-  k_mlp_bwd_samples<<<nb, 128, 0, s>>>(model, y, n, w.h1, w.h2, w.out, w.dO, w.g2, w.g1, w.sq);
-  k_standardize<<<(n * F + 255) / 256, 256, 0, s>>>(model, x, n, w.xn);
+  ki::launch(k_mlp_fwd, nb, 128, 0, s, model, x, n, w.h1, w.h2, w.out);
+  ki::launch(k_mlp_bwd_samples, nb, 128, 0, s, model, y, n, w.h1, w.h2, w.out, w.dO, w.g2, w.g1, w.sq);
+  ki::launch(k_standardize, (n * F + 255) / 256, 256, 0, s, model, x, n, w.xn);
   KI_MLP_CUDA(cudaMemsetAsync(w.grad, 0, sizeof(float) * kMlpModelFloats, s));
   auto outer = [&](const float* A, int p, const float* B, int q, float* g) {
     const int cnt = p * (B ? q : 1);
-    k_outer_partial<<<dim3((cnt + 127) / 128, kParts), 128, 0, s>>>(A, p, B, q, n, w.part);
-    k_outer_final<<<(cnt + 127) / 128, 128, 0, s>>>(w.part, cnt, g);
+    ki::launch(k_outer_partial, dim3((cnt + 127) / 128, kParts), 128, 0, s, A, p, B, q, n, w.part);
+    ki::launch(k_outer_final, (cnt + 127) / 128, 128, 0, s, w.part, cnt, g);
   };
   outer(w.g1, H, w.xn, F, w.grad + kW1);     // dW1[k][f] = sum G1[i][k] xn[i][f]
   outer(w.g1, H, nullptr, 1, w.grad + kB1);  // db1
@@ -203,7 +204,7 @@ float mlp_train(float* d_model, const float* d_x, const float* d_y, int n, int e
     loss = loss_grad(w, d_model, d_x, d_y, n);
     c1 *= b1;
     c2 *= b2;
-    k_adam<<<(kMlpModelFloats - kW1 + 255) / 256, 256, 0, s>>>(d_model, w.grad, mom,
+    ki::launch(k_adam, (kMlpModelFloats - kW1 + 255) / 256, 256, 0, s, d_model, w.grad, mom,
                                                                mom + kMlpModelFloats, lr, b1, b2,
                                                                1.f - c1, 1.f - c2);
     KI_MLP_CUDA(cudaGetLastError());
@@ -215,7 +216,7 @@ float mlp_train(float* d_model, const float* d_x, const float* d_y, int n, int e
 
 void mlp_predict(const float* d_model, const float* d_x, int n, float* d_out, cudaStream_t s) {
   if (n <= 0) return;
-  k_mlp_fwd<<<(n + 127) / 128, 128, 0, s>>>(d_model, d_x, n, nullptr, nullptr, d_out);
+  ki::launch(k_mlp_fwd, (n + 127) / 128, 128, 0, s, d_model, d_x, n, nullptr, nullptr, d_out);
   KI_MLP_CUDA(cudaGetLastError());
 }
 

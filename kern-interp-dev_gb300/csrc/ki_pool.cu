@@ -1,4 +1,5 @@
 #include "ki_pool.h"
+#include "ki_launch.cuh"
 
 #include <cstdint>
 #include <mutex>
@@ -39,6 +40,11 @@ cudaError_t pool_for_current_device(cudaMemPool_t* out) {
 }
 
 }  // namespace
+
+std::atomic<long long>& launch_counter() {
+  static std::atomic<long long> count(0);
+  return count;
+}
 
 cudaError_t pool_malloc(void** p, size_t bytes, cudaStream_t s) {
   cudaMemPool_t pool = nullptr;

@@ -13,6 +13,7 @@
 // a stable scatter in which each warp ranks its keys among equal digits
 // with __match_any_sync and the tile's warps and rounds are taken in key
 // order.  Ties keep the input order, and the input starts in point order.
+#include "ki_launch.cuh"
 #include "ki_tree_gpu.h"
 
 #include <algorithm>
@@ -190,16 +191,16 @@ void tree_codes_sorted(const double* d_points, int n, int dim, double centre, do
     }
     hist = (unsigned*)take(sizeof(unsigned) * ((size_t)kRsBins * ntile + kRsBins));
     unsigned* tot = hist + (size_t)kRsBins * ntile;
-    k_tree_codes<<<(n + 255) / 256, 256, 0, s>>>(d_points, n, dim, centre, side, depth, keys[0],
+    ki::launch(k_tree_codes, (n + 255) / 256, 256, 0, s, d_points, n, dim, centre, side, depth, keys[0],
                                                  vals[0]);
     KI_TREE_CUDA(cudaGetLastError());
     const int bits = dim * depth;
     int cur = 0;
     for (int shift = 0; shift < bits; shift += 8) {
-      k_rs_hist<<<ntile, kRsThreads, 0, s>>>(keys[cur], n, shift, ntile, hist);
-      k_rs_scan_rows<<<kRsBins, 256, 0, s>>>(hist, ntile, tot);
-      k_rs_scan_base<<<1, kRsBins, 0, s>>>(tot);
-      k_rs_scatter<<<ntile, kRsThreads, 0, s>>>(keys[cur], vals[cur], n, shift, ntile, hist, tot,
+      ki::launch(k_rs_hist, ntile, kRsThreads, 0, s, keys[cur], n, shift, ntile, hist);
+      ki::launch(k_rs_scan_rows, kRsBins, 256, 0, s, hist, ntile, tot);
+      ki::launch(k_rs_scan_base, 1, kRsBins, 0, s, tot);
+      ki::launch(k_rs_scatter, ntile, kRsThreads, 0, s, keys[cur], vals[cur], n, shift, ntile, hist, tot,
                                                 keys[1 - cur], vals[1 - cur]);
       KI_TREE_CUDA(cudaGetLastError());
       cur = 1 - cur;
