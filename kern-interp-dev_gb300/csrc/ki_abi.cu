@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <future>
 #include <memory>
 #include <mutex>
@@ -1179,10 +1180,20 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
 
     // 2D Laplace: the FMM for refinement residuals, planned and uploaded by a
     // worker thread on its own stream, concurrent with the factorization (it
-    // copies the caller's arrays first; this call returns only after the
-    // copy)
+    // copies the caller's arrays first, and this call returns only after the
+    // copy; it plans once the factorization's tree is built, so that the two
+    // do not compete for the host cores)
     std::promise<void> copied;
     std::future<void> copied_f = copied.get_future();
+    std::promise<void> tree_done;
+    std::shared_future<void> tree_done_f = tree_done.get_future().share();
+    bool tree_signalled = false;
+    auto signal_tree = [&] {
+      if (!tree_signalled) {
+        tree_signalled = true;
+        tree_done.set_value();
+      }
+    };
     bool planning = false;
     if (fmm_capable(f.get()) && f->n_dofs >= 4096 && !std::getenv("KI_NO_FMM_PREPLAN")) {
       planning = true;
@@ -1193,7 +1204,8 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
       cudaStream_t us = f->fmm_stream;
       int dev = 0;
       KI_CHECK_CUDA(cudaGetDevice(&dev));
-      f->fmm_ready = std::async(std::launch::async, [pp, nn, ww, kk, n, order, us, dev, &copied] {
+      f->fmm_ready = std::async(std::launch::async, [pp, nn, ww, kk, n, order, us, dev, &copied,
+                                                      tree_done_f] {
         std::vector<double> P, Nn, W, K;
         try {
           P.assign(pp, pp + 2 * (size_t)n);
@@ -1206,26 +1218,30 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
           throw;
         }
         copied.set_value();
+        tree_done_f.wait();
         auto plan = ki::fmm2d_plan(P.data(), Nn.data(), W.data(), K.data(), n, order);
         KI_CHECK_CUDA(cudaSetDevice(dev));   // the caller's device, not the thread default
         return ki::fmm2d_upload(*plan, us);
       });
     }
-    struct WaitCopy {   // the caller's arrays stay valid until the worker has copied them
+    struct WaitCopy {   // the caller's arrays stay valid until the worker has copied them;
+                        // the worker is released from its wait on every path out
       bool on;
       std::future<void>& fut;
+      std::function<void()> release;
       ~WaitCopy() {
+        release();
         if (on) fut.wait();
       }
-    } wait_copy{planning, copied_f};
+    } wait_copy{planning, copied_f, signal_tree};
     const auto t_factor = std::chrono::steady_clock::now();
     f->host_prep_ms = std::chrono::duration<double, std::milli>(t_factor - t_create).count();
     if (f->precision == KI_PRECISION_FP64)
       f->f64 = ki::factorize<double>(prm, n, desc->points, desc->normals, desc->weights,
-                                     desc->curvatures, holes, f->stream, f->d_pts);
+                                     desc->curvatures, holes, f->stream, f->d_pts, signal_tree);
     else
       f->f32 = ki::factorize<float>(prm, n, desc->points, desc->normals, desc->weights,
-                                    desc->curvatures, holes, f->stream, f->d_pts);
+                                    desc->curvatures, holes, f->stream, f->d_pts, signal_tree);
     f->host_factor_ms = std::chrono::duration<double, std::milli>(
                             std::chrono::steady_clock::now() - t_factor).count();
     // the FP64 3D diagonal of the factorization serves the FP64 apply

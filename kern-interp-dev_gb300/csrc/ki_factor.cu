@@ -2258,7 +2258,8 @@ template <typename T>
 std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, const double* points,
                                             const double* normals, const double* weights,
                                             const double* curvatures, const HoleDesc& holes,
-                                            cudaStream_t stream, const double* d_inputs) {
+                                            cudaStream_t stream, const double* d_inputs,
+                                            const std::function<void()>& after_tree) {
   auto t_start = std::chrono::steady_clock::now();
   auto F = std::make_unique<Factorization<T>>();
   F->prm = prm;
@@ -2329,6 +2330,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     if (!built) tree.build(points, n_points, dim, prm.sol_dim, prm.max_leaf_dofs);
     F->tree_gpu = built;
   }
+  if (after_tree) after_tree();
   F->tree_seconds =
       std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
   const int sd = prm.sol_dim;
@@ -3400,10 +3402,10 @@ template void solve_device_arena<float>(Factorization<float>&, float*, int, floa
 
 template std::unique_ptr<Factorization<double>> factorize<double>(
     const Params&, int, const double*, const double*, const double*, const double*,
-    const HoleDesc&, cudaStream_t, const double*);
+    const HoleDesc&, cudaStream_t, const double*, const std::function<void()>&);
 template std::unique_ptr<Factorization<float>> factorize<float>(
     const Params&, int, const double*, const double*, const double*, const double*,
-    const HoleDesc&, cudaStream_t, const double*);
+    const HoleDesc&, cudaStream_t, const double*, const std::function<void()>&);
 template void solve_device<double>(Factorization<double>&, double*, int, double*, const double*);
 template void solve_device<float>(Factorization<float>&, float*, int, float*, const float*);
 template struct Factorization<double>;

@@ -7,6 +7,7 @@
 #include <memory>
 #include <string>
 #include <array>
+#include <functional>
 #include <vector>
 
 #include "ki_tree.h"
@@ -147,6 +148,8 @@ struct HoleDesc {
 // Build the tree and skeletonize on `stream`.  Throws std::runtime_error on
 // failure (message says which stage).
 template <typename T>
+// after_tree (optional): called once the tree is built (the host work the
+// caller defers until the tree no longer competes for the CPU cores).
 // d_inputs (optional): the same four arrays already on the device, laid out
 // points (dim n) | normals (dim n) | weights (n) | curvatures (n), kept alive
 // by the caller for the factorization's lifetime; otherwise they are copied.
@@ -154,7 +157,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
                                             const double* normals, const double* weights,
                                             const double* curvatures, const HoleDesc& holes,
                                             cudaStream_t stream,
-                                            const double* d_inputs = nullptr);
+                                            const double* d_inputs = nullptr,
+                                            const std::function<void()>& after_tree = nullptr);
 
 // A bump allocator over caller-provided device memory.
 struct ScratchArena {
