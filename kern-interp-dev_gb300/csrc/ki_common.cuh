@@ -139,20 +139,87 @@ __device__ __forceinline__ int dof_point(int dof, int sol_dim) {
 // CTA-cooperative dense helpers on column-major matrices (shared or global
 // memory).  All threads of the block must call them.
 
+// Register-tiled body of cta_gemm_to: each thread owns TI x TJ outputs,
+// rows r0 + ii*mt and columns c0 + jj*nt (strided, so that consecutive
+// threads touch consecutive rows), and keeps TI + TJ operands in registers
+// per step of the inner dimension.  op(A)(i, l) = A[i*sai + l*sal] and
+// op(B)(l, j) = B[l*sbl + j*sbj].  Every output is the sum over l in
+// increasing order, as in the one-output-per-thread form.
+template <typename T, int TI, int TJ>
+__device__ __forceinline__ void cta_gemm_rt(int m, int n, int kk, T alpha, const T* A, int sai,
+                                            int sal, const T* B, int sbl, int sbj, T beta,
+                                            const T* Cin, int ldci, T* C, int ldc) {
+  const int mt = (m + TI - 1) / TI, nt = (n + TJ - 1) / TJ;
+  for (int t = threadIdx.x; t < mt * nt; t += blockDim.x) {
+    const int r0 = t % mt, c0 = t / mt;
+    int ia[TI], jb[TJ];
+#pragma unroll
+    for (int ii = 0; ii < TI; ii++) ia[ii] = min(r0 + ii * mt, m - 1) * sai;
+#pragma unroll
+    for (int jj = 0; jj < TJ; jj++) jb[jj] = min(c0 + jj * nt, n - 1) * sbj;
+    T acc[TI][TJ];
+#pragma unroll
+    for (int ii = 0; ii < TI; ii++)
+#pragma unroll
+      for (int jj = 0; jj < TJ; jj++) acc[ii][jj] = T(0);
+    int oa = 0, ob = 0;
+    for (int l = 0; l < kk; l++) {
+      T a[TI], b[TJ];
+#pragma unroll
+      for (int ii = 0; ii < TI; ii++) a[ii] = A[ia[ii] + oa];
+#pragma unroll
+      for (int jj = 0; jj < TJ; jj++) b[jj] = B[jb[jj] + ob];
+#pragma unroll
+      for (int ii = 0; ii < TI; ii++)
+#pragma unroll
+        for (int jj = 0; jj < TJ; jj++) acc[ii][jj] += a[ii] * b[jj];
+      oa += sal;
+      ob += sbl;
+    }
+#pragma unroll
+    for (int ii = 0; ii < TI; ii++)
+#pragma unroll
+      for (int jj = 0; jj < TJ; jj++) {
+        const int i = r0 + ii * mt, j = c0 + jj * nt;
+        if (i < m && j < n)
+          C[i + (size_t)ldc * j] =
+              (beta == T(0) ? T(0) : beta * Cin[i + (size_t)ldci * j]) + alpha * acc[ii][jj];
+      }
+  }
+}
+
+// C(m x n) = beta*Cin + alpha * op(A) * op(B); op(A) is m x kk; Cin may be C.
+// The thread tile (1x1, 2x2, 4x2 or 4x4 outputs) is the one with the fewest
+// instructions on a thread's path: rounds over the block times (FMAs + loads)
+// per inner step, ties to the larger tile (fewer loads in total).
+template <typename T>
+__device__ void cta_gemm_to(int m, int n, int kk, T alpha, const T* A, int lda, bool ta,
+                            const T* B, int ldb, bool tb, T beta, const T* Cin, int ldci, T* C,
+                            int ldc) {
+  if (m <= 0 || n <= 0) return;
+  const int sai = ta ? lda : 1, sal = ta ? 1 : lda;
+  const int sbl = tb ? ldb : 1, sbj = tb ? 1 : ldb;
+  const int nth = blockDim.x;
+  auto cost = [&](int ti, int tj) {
+    const int tiles = ((m + ti - 1) / ti) * ((n + tj - 1) / tj);
+    return ((tiles + nth - 1) / nth) * (ti * tj + ti + tj);
+  };
+  const int c11 = cost(1, 1), c22 = cost(2, 2), c42 = cost(4, 2), c44 = cost(4, 4);
+  if (c44 <= c42 && c44 <= c22 && c44 <= c11)
+    cta_gemm_rt<T, 4, 4>(m, n, kk, alpha, A, sai, sal, B, sbl, sbj, beta, Cin, ldci, C, ldc);
+  else if (c42 <= c22 && c42 <= c11)
+    cta_gemm_rt<T, 4, 2>(m, n, kk, alpha, A, sai, sal, B, sbl, sbj, beta, Cin, ldci, C, ldc);
+  else if (c22 <= c11)
+    cta_gemm_rt<T, 2, 2>(m, n, kk, alpha, A, sai, sal, B, sbl, sbj, beta, Cin, ldci, C, ldc);
+  else
+    cta_gemm_rt<T, 1, 1>(m, n, kk, alpha, A, sai, sal, B, sbl, sbj, beta, Cin, ldci, C, ldc);
+}
+
 // C(m x n) = beta*C + alpha * op(A) * op(B); op(A) is m x kk.
 template <typename T>
 __device__ void cta_gemm(int m, int n, int kk, T alpha, const T* A, int lda, bool ta,
                          const T* B, int ldb, bool tb, T beta, T* C, int ldc) {
-  for (int idx = threadIdx.x; idx < m * n; idx += blockDim.x) {
-    int i = idx % m, j = idx / m;
-    T acc = T(0);
-    for (int l = 0; l < kk; l++) {
-      T a = ta ? A[l + (size_t)lda * i] : A[i + (size_t)lda * l];
-      T b = tb ? B[j + (size_t)ldb * l] : B[l + (size_t)ldb * j];
-      acc += a * b;
-    }
-    C[i + (size_t)ldc * j] = (beta == T(0) ? T(0) : beta * C[i + (size_t)ldc * j]) + alpha * acc;
-  }
+  cta_gemm_to<T>(m, n, kk, alpha, A, lda, ta, B, ldb, tb, beta, C, ldc, C, ldc);
 }
 
 // f(i, c) for the elements e = threadIdx.x, threadIdx.x + blockDim.x, ... of

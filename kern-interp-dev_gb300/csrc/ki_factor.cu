@@ -1291,8 +1291,8 @@ __global__ void k_assemble(const AsmTask<T>* tasks, const int* ipool, Points<T> 
 
 // Schur-complement elimination of a compressed box
 // (SkelFactorization::decouple, skel_factorization.cpp:91-127).  Working set
-// K_ss (k x k) | Wrs (r x k) | Lt (r x k) | X (r x r) | r scratch entries
-// (and, inverse path, X's copy, U0, L0) in shared memory when it fits
+// K_ss (k x k) | T (k x r) | Wrs (r x k) | Lt (r x k) | X (r x r) | r scratch
+// entries (and, inverse path, X's copy, U0, L0) in shared memory when it fits
 // (smem != 0), else in the global scratch t.ws
 // (X in place in the output).  The blocks are gathered from the box's self
 // block through the skeleton-first permutation; K_sr is held only
@@ -1300,8 +1300,9 @@ __global__ void k_assemble(const AsmTask<T>* tasks, const int* ipool, Points<T> 
 // memory boxes) X is inverted in place by Gauss-Jordan elimination and L, U
 // are products with the inverse; otherwise X is LU-factored (the
 // reference's dgetrf / dgetrs) and L, U come from triangular solves.
+template <typename T> constexpr int kSchurMinBlocks = sizeof(T) == 4 ? 4 : 2;
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_schur(const SchurTask<T>* tasks, int task_base,
+__global__ void __launch_bounds__(kThreads, kSchurMinBlocks<T>) k_schur(const SchurTask<T>* tasks, int task_base,
                                                      int smem, int* err) {
   extern __shared__ __align__(16) unsigned char sc_smem[];
   const SchurTask<T> t = tasks[task_base + blockIdx.x];
@@ -1313,7 +1314,10 @@ __global__ void __launch_bounds__(kThreads) k_schur(const SchurTask<T>* tasks, i
   __shared__ int s_idx, s_flag;
   T* base = smem ? reinterpret_cast<T*>(sc_smem) : t.ws;
   T* Kss = base;                      // k x k
-  T* Wrs = Kss + (size_t)k * k;       // r x k : K_rs, then K~_rs, then U
+  // shared-memory boxes: T (k x r) staged with the odd leading dimension kt
+  const int kt = smem ? (k | 1) : k;
+  T* Ts = Kss + (size_t)k * k;
+  T* Wrs = smem ? Ts + (size_t)kt * r : Ts;   // r x k : K_rs, then K~_rs, then U
   T* Lt = Wrs + (size_t)ld * k;       // r x k : K_sr^T, then K~_sr^T, then L^T
   T* X = smem ? Lt + (size_t)ld * k : t.X;   // r x r
   const int* pm = t.perm;
@@ -1330,18 +1334,22 @@ __global__ void __launch_bounds__(kThreads) k_schur(const SchurTask<T>* tasks, i
     const int i = idx % r, j = idx / r;
     X[i + (size_t)ld * j] = t.K[pm[k + i] + (size_t)n * pm[k + j]];
   }
-  for (int idx = threadIdx.x; idx < k * r; idx += blockDim.x) t.Tout[idx] = t.Tin[idx];
+  for (int idx = threadIdx.x; idx < k * r; idx += blockDim.x) {
+    const T v = t.Tin[idx];
+    t.Tout[idx] = v;
+    if (smem) Ts[idx % k + (size_t)kt * (idx / k)] = v;
+  }
   __syncthreads();
-  const T* Tm = t.Tin;
+  const T* Tm = smem ? Ts : t.Tin;
   // X -= T^T K_sr  (K_sr(l, j) = Lt[j + ld l])
-  cta_gemm<T>(r, r, k, T(-1), Tm, k, true, Lt, ld, true, T(1), X, ld);
+  cta_gemm<T>(r, r, k, T(-1), Tm, kt, true, Lt, ld, true, T(1), X, ld);
   __syncthreads();
   // K~_rs = K_rs - T^T K_ss ;  K~_sr^T = K_sr^T - T^T K_ss^T
-  cta_gemm<T>(r, k, k, T(-1), Tm, k, true, Kss, k, false, T(1), Wrs, ld);
-  cta_gemm<T>(r, k, k, T(-1), Tm, k, true, Kss, k, true, T(1), Lt, ld);
+  cta_gemm<T>(r, k, k, T(-1), Tm, kt, true, Kss, k, false, T(1), Wrs, ld);
+  cta_gemm<T>(r, k, k, T(-1), Tm, kt, true, Kss, k, true, T(1), Lt, ld);
   __syncthreads();
   // X -= K~_rs T
-  cta_gemm<T>(r, r, k, T(-1), Wrs, ld, false, Tm, k, false, T(1), X, ld);
+  cta_gemm<T>(r, r, k, T(-1), Wrs, ld, false, Tm, kt, false, T(1), X, ld);
   __syncthreads();
   if (smem && t.gj) {
     // shared memory after X: colj (r) | X0 (r x r) | U0 (r x k) | L0 (k x r)
@@ -1358,48 +1366,19 @@ __global__ void __launch_bounds__(kThreads) k_schur(const SchurTask<T>* tasks, i
     cta_gemm<T>(k, r, r, T(1), Lt, ld, true, X, ld, false, T(0), L0, k);
     __syncthreads();
     // A~ = K_ss - L0 K~_rs (the correction's share follows below)
-    for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) {
-      const int i = idx % k, j = idx / k;
-      T acc = T(0);
-      for (int l = 0; l < r; l++) acc += L0[i + (size_t)k * l] * Wrs[l + (size_t)ld * j];
-      t.Atil[idx] = Kss[idx] - acc;
-    }
+    cta_gemm_to<T>(k, k, r, T(-1), L0, k, false, Wrs, ld, false, T(1), Kss, k, t.Atil, k);
     __syncthreads();
     // one step of refinement in the same precision (products with an explicit
     // inverse are not backward stable; the corrected ones are): the residuals
     // RU = K~_rs - X U0 and RL = K~_sr - L0 X, in place of K~_rs and K~_sr^T
-    for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
-      const int i = idx % r, j = idx / r;
-      T acc = T(0);
-      for (int l = 0; l < r; l++) acc += X0[i + (size_t)ld * l] * U0[l + (size_t)ld * j];
-      Wrs[i + (size_t)ld * j] -= acc;
-    }
-    for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
-      const int jj = idx % r, i = idx / r;   // Lt(jj, i) = K~_sr(i, jj)
-      T acc = T(0);
-      for (int l = 0; l < r; l++) acc += L0[i + (size_t)k * l] * X0[l + (size_t)ld * jj];
-      Lt[jj + (size_t)ld * i] -= acc;
-    }
+    // (RL^T = K~_sr^T - X^T L0^T)
+    cta_gemm<T>(r, k, r, T(-1), X0, ld, false, U0, ld, false, T(1), Wrs, ld);
+    cta_gemm<T>(r, k, r, T(-1), X0, ld, true, L0, k, true, T(1), Lt, ld);
     __syncthreads();
     // U = U0 + X^-1 RU, L = L0 + RL X^-1, A~ -= RL U0 (RL X^-1 K~_rs)
-    for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
-      const int i = idx % r, j = idx / r;
-      T acc = T(0);
-      for (int l = 0; l < r; l++) acc += X[i + (size_t)ld * l] * Wrs[l + (size_t)ld * j];
-      t.U[idx] = U0[i + (size_t)ld * j] + acc;
-    }
-    for (int idx = threadIdx.x; idx < k * r; idx += blockDim.x) {
-      const int i = idx % k, j = idx / k;
-      T acc = T(0);
-      for (int l = 0; l < r; l++) acc += Lt[l + (size_t)ld * i] * X[l + (size_t)ld * j];
-      t.L[idx] = L0[idx] + acc;
-    }
-    for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) {
-      const int i = idx % k, j = idx / k;
-      T acc = T(0);
-      for (int l = 0; l < r; l++) acc += Lt[l + (size_t)ld * i] * U0[l + (size_t)ld * j];
-      t.Atil[idx] -= acc;
-    }
+    cta_gemm_to<T>(r, k, r, T(1), X, ld, false, Wrs, ld, false, T(1), U0, ld, t.U, r);
+    cta_gemm_to<T>(k, r, r, T(1), Lt, ld, true, X, ld, false, T(1), L0, k, t.L, k);
+    cta_gemm<T>(k, k, r, T(-1), Lt, ld, true, U0, ld, false, T(1), t.Atil, k);
     for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x)
       t.Xi[idx] = X[idx % r + (size_t)ld * (idx / r)];
     return;
@@ -1524,12 +1503,14 @@ void copy_block(cudaStream_t s, const T* src, int lds, int rows, int cols, bool 
                                                                               trans, dst, ldd);
 }
 
-// Shared-memory bytes of k_schur for a box: K_ss, K~_rs, K~_sr^T, X and r
+// Shared-memory bytes of k_schur for a box: K_ss, T, K~_rs, K~_sr^T, X and r
 // scratch entries, plus (inverse path) X's copy, U0 and L0.
 template <typename T>
 size_t schur_bytes(int n, int k, bool inv) {
-  const size_t r = n - k, ld = (size_t)((n - k) | 1);   // k_schur's odd leading dimension
-  return sizeof(T) * ((size_t)k * k + 2 * ld * k + ld * r + r + (inv ? ld * r + ld * k + k * r : 0));
+  const size_t r = n - k, ld = (size_t)((n - k) | 1);   // k_schur's odd leading dimensions
+  const size_t kt = (size_t)(k | 1);
+  return sizeof(T) * ((size_t)k * k + kt * r + 2 * ld * k + ld * r + r +
+                      (inv ? ld * r + ld * k + k * r : 0));
 }
 
 // SkelFactorization::decouple for a box whose working set does not fit in one
