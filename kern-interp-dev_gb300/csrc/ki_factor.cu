@@ -324,6 +324,10 @@ __device__ __forceinline__ long long norm_key(float v) { return (long long)__flo
 // budget of the register-tiled sketch fold would otherwise allow two), two
 // in FP64 (no register spills).
 template <typename T> constexpr int kIdMinBlocks = sizeof(T) == 4 ? 3 : 2;
+// Block size of the FP32 launches whose boxes are too few to give every SM a
+// CTA (the upper levels' large boxes): twice the warps to hide the latency of
+// each CTA's serial pivot / reflector steps.
+constexpr int kIdBigThreads = 512;
 
 // Interpolative decomposition of one box per CTA.
 //
@@ -334,8 +338,8 @@ template <typename T> constexpr int kIdMinBlocks = sizeof(T) == 4 ? 3 : 2;
 // a warp touch consecutive columns.  Shared-memory layout (dynamic):
 //   B (32 x ldB) | hu (2 x 32 Householder tails) | vn1 (n) | vn2 (n) | perm (n) |
 //   R (n x ldR) when it fits (mode 0); mode 1 keeps R in the global scratch.
-template <typename T, int FR>
-__global__ void __launch_bounds__(kThreads, kIdMinBlocks<T>) k_id(const IdTask* tasks, int task_base,
+template <typename T, int FR, int NT = kThreads>
+__global__ void __launch_bounds__(NT, NT == kThreads ? kIdMinBlocks<T> : 1) k_id(const IdTask* tasks, int task_base,
                                                   const int64_t* seg_off, const int* seg_len,
                                                   int* ipool, int* iscratch, T* tws, Points<T> P,
                                                   int sol_dim, ProxyTab<T> px, double tol, int* k_out,
@@ -940,6 +944,34 @@ __global__ void __launch_bounds__(128) k_box_features(const IdTask* tasks, int n
   }
 }
 
+// Streaming multiprocessors of the current device.
+inline int device_sm_count() {
+  int dev = 0, n = 0;
+  KI_CUDA(cudaGetDevice(&dev));
+  KI_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+  return n;
+}
+
+// k_id with fr-row fold blocks over `grid` boxes; FP32 launches of fewer
+// boxes than SMs use kIdBigThreads threads per CTA.
+template <typename T, typename... A>
+void launch_k_id(int fr, unsigned grid, size_t smem, cudaStream_t st, A&&... args) {
+  static const int n_sm = device_sm_count();
+  if constexpr (sizeof(T) == 4) {
+    if ((int)grid < n_sm) {
+      if (fr == 64)
+        ki::launch(k_id<T, 64, kIdBigThreads>, grid, kIdBigThreads, smem, st, std::forward<A>(args)...);
+      else
+        ki::launch(k_id<T, 32, kIdBigThreads>, grid, kIdBigThreads, smem, st, std::forward<A>(args)...);
+      return;
+    }
+  }
+  if (fr == 64)
+    ki::launch(k_id<T, 64>, grid, kThreads, smem, st, std::forward<A>(args)...);
+  else
+    ki::launch(k_id<T, 32>, grid, kThreads, smem, st, std::forward<A>(args)...);
+}
+
 // Shared-memory bytes of k_id for a box of n active DOFs: mode 0 keeps the
 // triangle in shared memory, mode 1 in the global scratch.
 template <typename T>
@@ -1300,9 +1332,14 @@ __global__ void k_assemble(const AsmTask<T>* tasks, const int* ipool, Points<T> 
 // memory boxes) X is inverted in place by Gauss-Jordan elimination and L, U
 // are products with the inverse; otherwise X is LU-factored (the
 // reference's dgetrf / dgetrs) and L, U come from triangular solves.
-template <typename T> constexpr int kSchurMinBlocks = sizeof(T) == 4 ? 4 : 2;
+// Block sizes k_schur is compiled for: FP32 up to 1024 threads (64 registers,
+// so four 256-thread CTAs or one 1024-thread CTA per SM), FP64 256 threads
+// with two CTAs per SM.  Boxes whose shared working set leaves room for only
+// one or two CTAs per SM get the larger blocks (schur_threads).
+template <typename T> constexpr int kSchurMaxThreads = sizeof(T) == 4 ? 1024 : kThreads;
+template <typename T> constexpr int kSchurMinBlocks = sizeof(T) == 4 ? 1 : 2;
 template <typename T>
-__global__ void __launch_bounds__(kThreads, kSchurMinBlocks<T>) k_schur(const SchurTask<T>* tasks, int task_base,
+__global__ void __launch_bounds__(kSchurMaxThreads<T>, kSchurMinBlocks<T>) k_schur(const SchurTask<T>* tasks, int task_base,
                                                      int smem, int* err) {
   extern __shared__ __align__(16) unsigned char sc_smem[];
   const SchurTask<T> t = tasks[task_base + blockIdx.x];
@@ -1511,6 +1548,14 @@ size_t schur_bytes(int n, int k, bool inv) {
   const size_t kt = (size_t)(k | 1);
   return sizeof(T) * ((size_t)k * k + kt * r + 2 * ld * k + ld * r + r +
                       (inv ? ld * r + ld * k + k * r : 0));
+}
+
+// Threads of a k_schur CTA when `per_sm` CTAs run per SM: 256 when four or
+// more do (occupancy from CTAs), else enough to fill the SM's warps.
+template <typename T>
+int schur_threads(int per_sm) {
+  if (kSchurMaxThreads<T> <= kThreads || per_sm >= 4) return kThreads;
+  return per_sm == 3 ? 320 : (per_sm == 2 ? 512 : kSchurMaxThreads<T>);
 }
 
 // SkelFactorization::decouple for a box whose working set does not fit in one
@@ -2580,6 +2625,12 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     // (a) row lists of every box (m is needed to pick the path)
     KI_CUDA(cudaFuncSetAttribute(k_id<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
     KI_CUDA(cudaFuncSetAttribute(k_id<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
+    if constexpr (sizeof(T) == 4) {
+      KI_CUDA(cudaFuncSetAttribute(k_id<T, 32, kIdBigThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem_cap));
+      KI_CUDA(cudaFuncSetAttribute(k_id<T, 64, kIdBigThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem_cap));
+    }
     ki::launch(k_id<T, 32>, (unsigned)itasks.size(), kThreads, 0, s, d_it, 0, d_soff, d_slen, ipool, d_irows, d_tws,
                                                          P, sd, ptab, prm.id_tol,
                                                          d_k, d_m, 0, 1, nullptr);
@@ -2696,16 +2747,10 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         }
         if (sm > smem_cap) throw std::runtime_error("box too large for the ID kernel");
         cudaStream_t st = fixed ? fixed : F->aux[(next_aux++) % (Factorization<T>::kAux - 1)];
-        if (fr == 64)
-          ki::launch(k_id<T, 64>, (unsigned)(b1 - b0), kThreads, sm, st, d_it, b0, d_soff, d_slen, ipool, d_irows,
-                                                                 d_tws, P, sd, ptab,
-                                                                 prm.id_tol, d_k, d_m, kmode, flags,
-                                                                 sketching && g != 1 ? d_lsk : nullptr);
-        else
-          ki::launch(k_id<T, 32>, (unsigned)(b1 - b0), kThreads, sm, st, d_it, b0, d_soff, d_slen, ipool, d_irows,
-                                                                 d_tws, P, sd, ptab,
-                                                                 prm.id_tol, d_k, d_m, kmode, flags,
-                                                                 sketching && g != 1 ? d_lsk : nullptr);
+        launch_k_id<T>(fr, (unsigned)(b1 - b0), sm, st, (const IdTask*)d_it, b0,
+                       (const int64_t*)d_soff, (const int*)d_slen, ipool, d_irows, d_tws, P, sd, ptab,
+                       prm.id_tol, d_k, d_m, kmode, flags,
+                       (const int*)(sketching && g != 1 ? d_lsk : nullptr));
         KI_CUDA(cudaGetLastError());
         b0 = b1;
       }
@@ -2844,13 +2889,13 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         std::string fname = "id_fallback@L" + std::to_string(l);
         F->stage_begin(fname.c_str(), 0, 0);
         if (cnt0 > 0)
-          ki::launch(k_id<T, 32>, (unsigned)cnt0, kThreads, sm[0], s, d_t2, 0, d_soff, d_slen, ipool, d_irows,
-                                                               d_tws, P, sd, ptab, prm.id_tol, d_k2,
-                                                               d_m2, 0, 2, nullptr);
+          launch_k_id<T>(32, (unsigned)cnt0, sm[0], s, (const IdTask*)d_t2, 0, (const int64_t*)d_soff,
+                         (const int*)d_slen, ipool, d_irows, d_tws, P, sd, ptab, prm.id_tol, d_k2, d_m2,
+                         0, 2, (const int*)nullptr);
         if ((int)t2.size() > cnt0)
-          ki::launch(k_id<T, 32>, (unsigned)(t2.size() - cnt0), kThreads, sm[1], s,
-              d_t2, cnt0, d_soff, d_slen, ipool, d_irows, d_tws, P, sd, ptab, prm.id_tol, d_k2, d_m2,
-              1, 2, nullptr);
+          launch_k_id<T>(32, (unsigned)(t2.size() - cnt0), sm[1], s, (const IdTask*)d_t2, cnt0,
+                         (const int64_t*)d_soff, (const int*)d_slen, ipool, d_irows, d_tws, P, sd, ptab,
+                         prm.id_tol, d_k2, d_m2, 1, 2, (const int*)nullptr);
         F->stage_end();
         KI_CUDA(cudaGetLastError());
         std::vector<int> k2(t2.size());
@@ -3033,12 +3078,16 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         int b1 = b0 + 1;
         while (b1 < n_sm && per_sm(schur_task_bytes<T>(st2[b1])) == ps) b1++;
         const size_t bsm = schur_task_bytes<T>(st2[b1 - 1]);
-        ki::launch(k_schur<T>, (unsigned)(b1 - b0), kThreads, bsm, F->aux[(next++) % Factorization<T>::kAux],
+        // a bin of fewer boxes than SMs runs one CTA per SM whatever its footprint
+        static const int n_sm = device_sm_count();
+        ki::launch(k_schur<T>, (unsigned)(b1 - b0), schur_threads<T>(b1 - b0 < n_sm ? 1 : ps), bsm,
+            F->aux[(next++) % Factorization<T>::kAux],
             d_st, b0, 1, F->d_err);
         b0 = b1;
       }
       if (n_glob > 0)
-        ki::launch(k_schur<T>, (unsigned)n_glob, kThreads, 0, F->aux[(next++) % Factorization<T>::kAux],
+        ki::launch(k_schur<T>, (unsigned)n_glob, schur_threads<T>(1), 0,
+            F->aux[(next++) % Factorization<T>::kAux],
             d_st, n_sm, 0, F->d_err);
       for (size_t q = n_sm + n_glob; q < st2.size(); q++)
         schur_wide<T>(st2[q], F->d_err, F->aux[(next++) % Factorization<T>::kAux]);
