@@ -476,7 +476,8 @@ def main():
     name, a = top
     sec = a["ms"] / 1e3
     ach_tflops = a["flops"] / sec / 1e12 if sec > 0 else 0.0
-    if name.startswith("refine:fmm32"):
+    if name.startswith("refine:fmm32") or name == "refine:fmm_near":
+        # the FP64 apply's near field accumulates FP32 pairs on the FP32 pipes
         fp64_stage = False
     elif name.startswith("refine:"):
         fp64_stage = True
@@ -484,8 +485,9 @@ def main():
         fp64_stage = args.precision == "fp64"
     cc_peak = (fp64_gf if fp64_stage else fp32_gf) / 1e3
     describe = {
-        "refine:fmm_near": ("k_l2p_p2p (FMM near field: direct sum over the 3x3 leaf "
-                            "neighbourhood, 32 columns, plus the local expansions at the targets)",
+        "refine:fmm_near": ("k_leaf_eval (FMM leaf evaluation: local expansions at the targets "
+                            "in FP64, near field over the 3x3 leaf neighbourhood with FP64 "
+                            "entries and FP32-pair accumulation, 32 columns)",
                             "near-field point pairs x (4 x 32 + 12) + targets x p x (4 x 32 + 6) "
                             "flops / device time of the launches"),
         "refine:fmm_m2l": ("k_m2l (FMM multipole-to-local translations, rotated form)",

@@ -136,6 +136,52 @@ __device__ __forceinline__ int dof_point(int dof, int sol_dim) {
 }
 
 // ------------------------------------------------------------------------
+// FP32-pair arithmetic (a value as hi + lo, |lo| <= ulp(hi)/2) for FP64-accurate
+// sums on the FP32 pipes, which run at 64x the FP64 rate on this part.
+
+// An FP64 value as an FP32 pair: hi = fl(v), lo = fl(v - hi) (48 bits kept).
+__device__ __forceinline__ float2 split_pair(double v) {
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+
+// h + l += e * d for FP32 pairs (value = hi + lo): the product of the high
+// parts is split exactly (p + fma(e_h, d_h, -p)), the cross terms join its
+// error, and p enters the sum through Knuth's two-sum, whose rounding error
+// goes to l with the rest.  The _rn intrinsics keep the compiler from fusing
+// the separately rounded steps.  Each step adds an error near 2^-48 of the
+// partial sum, so a near-field sum of a few hundred pairs keeps ~1e-13
+// relative accuracy while the arithmetic runs on the FP32 pipes.
+__device__ __forceinline__ void pair_fma(float& h, float& l, float2 e, float2 d) {
+  const float p = __fmul_rn(e.x, d.x);
+  float q = fmaf(e.x, d.x, -p);
+  q = fmaf(e.x, d.y, q);
+  q = fmaf(e.y, d.x, q);
+  const float sum = __fadd_rn(h, p);
+  const float bp = __fsub_rn(sum, h);
+  const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(sum, bp)), __fsub_rn(p, bp));
+  l = __fadd_rn(l, __fadd_rn(err, q));
+  h = sum;
+}
+
+// Error-free transforms (Knuth's two-sum and two-difference, Dekker's fast
+// two-sum for |a| >= |b|): hi + lo equals the exact result.
+__device__ __forceinline__ void two_sum(float a, float b, float& hi, float& lo) {
+  hi = __fadd_rn(a, b);
+  const float bb = __fsub_rn(hi, a);
+  lo = __fadd_rn(__fsub_rn(a, __fsub_rn(hi, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void two_diff(float a, float b, float& hi, float& lo) {
+  hi = __fsub_rn(a, b);
+  const float bb = __fsub_rn(hi, a);
+  lo = __fsub_rn(__fsub_rn(a, __fsub_rn(hi, bb)), __fadd_rn(b, bb));
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& hi, float& lo) {
+  hi = __fadd_rn(a, b);
+  lo = __fsub_rn(b, __fsub_rn(hi, a));
+}
+
+// ------------------------------------------------------------------------
 // CTA-cooperative dense helpers on column-major matrices (shared or global
 // memory).  All threads of the block must call them.
 

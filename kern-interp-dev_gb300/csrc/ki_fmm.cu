@@ -9,6 +9,7 @@
 // expansion plus the direct near-field sum with the exact kernel entries.
 // All 32 columns of a pass share every kernel-entry and translation-matrix
 // load.
+#include "ki_common.cuh"
 #include "ki_launch.cuh"
 #include "ki_pool.h"
 #include "ki_fmm.h"
@@ -76,12 +77,13 @@ template <typename V> __device__ __forceinline__ V cround(double x, double y) {
 }
 
 // u[i kCols + c] = mu[perm[i] + ldmu (c0 + c)]: the densities in sorted
-// order, point-major (a point's columns contiguous), in the expansion type.
+// order, point-major (a point's columns contiguous), in the expansion type;
+// with u2 also as FP32 pairs (the FP64 apply's near field).
 // Block (32, 8) per 32 points: columns read along the points (coalesced in
 // mu), written along the columns through shared memory.
 template <typename R>
 __global__ void k_densities(const int* perm, int n, const double* mu, int ldmu, int c0, int nc,
-                            R* u) {
+                            R* u, float2* u2) {
   __shared__ R tile[32][kCols + 1];
   const int i0 = blockIdx.x * 32;
   const int i = i0 + threadIdx.x;
@@ -94,7 +96,12 @@ __global__ void k_densities(const int* perm, int n, const double* mu, int ldmu, 
   const int cnt = min(32, n - i0);
   for (int e = threadIdx.y * 32 + threadIdx.x; e < cnt * nc; e += 32 * blockDim.y) {
     const int r = e / nc, c = e % nc;
-    u[(size_t)(i0 + r) * kCols + c] = tile[r][c];
+    const R v = tile[r][c];
+    u[(size_t)(i0 + r) * kCols + c] = v;
+    if (u2) {   // the FP64 density as an FP32 pair hi + lo
+      const float h = (float)v;
+      u2[(size_t)(i0 + r) * kCols + c] = make_float2(h, (float)((double)v - (double)h));
+    }
   }
 }
 
@@ -306,48 +313,58 @@ __global__ void k_l2l(int b0, const int* parent, const int* child_pos, const R* 
   }
 }
 
-// 1/x for a positive FP64 x (a squared distance): the correctly rounded
-// single-precision reciprocal of fl32(x) as the seed (relative error below
-// 1.2e-7), refined by one Newton-Raphson step y <- y + y (1 - x y), which
-// squares the relative error (below 1.5e-14: far under the FMM's own
-// truncation error at any order it is run with).  x stays within the
-// single-precision normal range (squared distances between boundary nodes
-// of unit-scale geometry).
-__device__ __forceinline__ double recip_nr(double x) {
-  const double y = (double)__frcp_rn((float)x);
-  return fma(y, fma(-x, y, 1.0), y);
+// The Nystrom entry (nw_s . (t - s)) / |t - s|^2 in FP32-pair arithmetic from
+// pairs t, s, nw = (hi x, hi y, lo x, lo y): the difference by two_diff, the
+// dot products and squared distance with exact products (p = a b,
+// fma(a, b, -p)) and the low-order terms, the quotient by long division with
+// one remainder step (Dekker's double-length division, 1971): q1 = num_h / r2_h
+// through the rounded reciprocal, then (num - q1 r2) / r2_h.  Relative error
+// ~1e-13, far under the FMM truncation error; returned as a normalised pair.
+__device__ __forceinline__ float2 pair_entry(const float4& t, const float4& s, const float4& nw) {
+  float dxh, dxl, dyh, dyl;
+  two_diff(t.x, s.x, dxh, dxl);
+  two_diff(t.y, s.y, dyh, dyl);
+  fast_two_sum(dxh, __fadd_rn(dxl, __fsub_rn(t.z, s.z)), dxh, dxl);
+  fast_two_sum(dyh, __fadd_rn(dyl, __fsub_rn(t.w, s.w)), dyh, dyl);
+  // r2 = dx^2 + dy^2
+  const float a = __fmul_rn(dxh, dxh), b = __fmul_rn(dyh, dyh);
+  float r2h, r2l;
+  two_sum(a, b, r2h, r2l);
+  r2l = __fadd_rn(r2l, __fadd_rn(fmaf(dxh, dxh, -a), fmaf(dyh, dyh, -b)));
+  r2l = fmaf(2.f * dxh, dxl, fmaf(2.f * dyh, dyl, r2l));
+  fast_two_sum(r2h, r2l, r2h, r2l);
+  // num = nw . d
+  const float c = __fmul_rn(nw.x, dxh), d = __fmul_rn(nw.y, dyh);
+  float nh, nl;
+  two_sum(c, d, nh, nl);
+  nl = __fadd_rn(nl, __fadd_rn(fmaf(nw.x, dxh, -c), fmaf(nw.y, dyh, -d)));
+  nl = fmaf(nw.x, dxl, fmaf(nw.z, dxh, fmaf(nw.y, dyl, fmaf(nw.w, dyh, nl))));
+  fast_two_sum(nh, nl, nh, nl);
+  // q = num / r2
+  const float inv = __frcp_rn(r2h);
+  const float q1 = __fmul_rn(nh, inv);
+  const float p = __fmul_rn(q1, r2h);
+  float rem = __fsub_rn(nh, p);   // exact: p is within a factor two of nh
+  rem = __fsub_rn(rem, fmaf(q1, r2h, -p));
+  rem = fmaf(-q1, r2l, __fadd_rn(rem, nl));
+  float qh, ql;
+  fast_two_sum(q1, __fmul_rn(rem, inv), qh, ql);
+  return make_float2(qh, ql);
 }
 
-// Source coordinates staged for the near field: FP64 points, or for the FP32
-// apply each coordinate as an FP32 pair hi + lo (hi = fl(x), lo = fl(x - hi)),
-// so t - s = (t_hi - s_hi) + (t_lo - s_lo) keeps the full relative accuracy
-// of the difference of two nearby nodes (t_hi - s_hi is exact for nodes
-// within a factor of two of each other).
-template <typename R> struct NearPt;
-template <> struct NearPt<double> { using type = double2; };
-template <> struct NearPt<float> { using type = float4; };
+// Near-field points are staged as FP32 pairs (hi x, hi y, lo x, lo y), hi =
+// fl(x), lo = fl(x - hi), in both applies, so that differences of nearby nodes
+// keep their full relative accuracy; nw_s = -(w_s / 2 pi) n_s likewise as
+// pairs in the FP64 apply, rounded in the FP32 one.
+template <typename R> struct NearNw;
+template <> struct NearNw<double> { using type = float4; };
+template <> struct NearNw<float> { using type = float2; };
 
-__device__ __forceinline__ void near_load(const double2* z, const float4*, int i, double2* out) {
-  *out = z[i];
-}
-__device__ __forceinline__ void near_load(const double2*, const float4* zf, int i, float4* out) {
-  *out = zf[i];
-}
-// The Nystrom entry Re(nw_s / (t - s)) = (nw_s . (t - s)) / |t - s|^2 of a
-// target t and a source s with nw_s = -(w_s / 2 pi) n_s.
-__device__ __forceinline__ double near_entry(const double2& t, const double2& s, double2 nws) {
-  const double dx = t.x - s.x, dy = t.y - s.y;
-  return (nws.x * dx + nws.y * dy) * recip_nr(dx * dx + dy * dy);
-}
+// The Nystrom entry Re(nw_s / (t - s)) = (nw_s . (t - s)) / |t - s|^2 in FP32
+// (the FP32 apply): t - s = (t_hi - s_hi) + (t_lo - s_lo).
 __device__ __forceinline__ float near_entry(const float4& t, const float4& s, float2 nws) {
   const float dx = (t.x - s.x) + (t.z - s.z), dy = (t.y - s.y) + (t.w - s.w);
   return (nws.x * dx + nws.y * dy) * __frcp_rn(dx * dx + dy * dy);
-}
-__device__ __forceinline__ void near_nw(const double2* nw, const float2*, int i, double2* out) {
-  *out = nw[i];
-}
-__device__ __forceinline__ void near_nw(const double2*, const float2* nw32, int i, float2* out) {
-  *out = nw32[i];
 }
 
 // Per leaf: far field from the local expansion, near field by direct
@@ -378,16 +395,16 @@ template <typename R>
 __global__ void __launch_bounds__(kLeafThreads)
     k_leaf_eval(const int* leaf_start, const int* leaf_box, const int* near_off,
                 const int* near_leaf, const double2* centre, double side, const double2* z,
-                const float4* zf, const double2* nw, const float2* nw32, const double* diag,
-                const int* perm, const R* u, const cplx_t<R>* le, int nc, int p,
-                const double* mu, int ldmu, int c0, double* y, int ldy) {
+                const float4* zf, const float2* nw32, const float4* nwf,
+                const double* diag,
+                const int* perm, const R* u, const float2* u2, const cplx_t<R>* le, int nc,
+                int p, const double* mu, int ldmu, int c0, double* y, int ldy) {
   using V = cplx_t<R>;
-  using P = typename NearPt<R>::type;
-  using W = cplx_t<R>;   // nw_s in the arithmetic type
+  using W = typename NearNw<R>::type;
   __shared__ V bufA[kPassTargets * kMaxP];   // powers [t][m] (complex), then entries [t][s] (real)
   __shared__ V bufB[kSrcChunk * kCols];      // local expansion [m][c], densities [s][c] (real), output
-  __shared__ P st[kPassTargets];
-  __shared__ P ss[kSrcChunk];
+  __shared__ float4 st[kPassTargets];
+  __shared__ float4 ss[kSrcChunk];
   __shared__ W snw[kSrcChunk];
   R* ent = reinterpret_cast<R*>(bufA);
   R* dens = reinterpret_cast<R*>(bufB);
@@ -402,7 +419,7 @@ __global__ void __launch_bounds__(kLeafThreads)
     __syncthreads();   // the previous pass's output is written
     if (threadIdx.x < nt) {
       const int t = tb + threadIdx.x;
-      near_load(z, zf, t, &st[threadIdx.x]);
+      st[threadIdx.x] = zf[t];
       const double2 zt = z[t];
       const V w = cround<V>((zt.x - c.x) / side, (zt.y - c.y) / side);
       V pw = cround<V>(1, 0);
@@ -433,7 +450,52 @@ __global__ void __launch_bounds__(kLeafThreads)
         }
       }
     }
-    // near field: sum_s Re(nw_s / (t - s)) mu_s, one real entry per pair
+    // near field: sum_s Re(nw_s / (t - s)) mu_s, one real entry per pair.
+    // FP64 apply: entries (pair_entry) and densities as FP32 pairs, summed with
+    // pair_fma: the FP32 pipes instead of the FP64 pipe, which runs at 1/64 of
+    // their rate on this part.
+    if constexpr (sizeof(R) == 8) {
+      float2* ent2 = reinterpret_cast<float2*>(bufA);    // [t][s]
+      float2* dens2 = reinterpret_cast<float2*>(bufB);   // [s][c]
+      float nh[kWarpTargets], nl[kWarpTargets];
+#pragma unroll
+      for (int k = 0; k < kWarpTargets; k++) nh[k] = nl[k] = 0.f;
+      for (int v = near_off[lf]; v < near_off[lf + 1]; v++) {
+        const int sl = near_leaf[v];
+        const int s0 = leaf_start[sl], s1 = leaf_start[sl + 1];
+        for (int base = s0; base < s1; base += kSrcChunk) {
+          const int cnt = min(kSrcChunk, s1 - base);
+          __syncthreads();   // readers of bufA / bufB done
+          for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+            ss[i] = zf[base + i];
+            snw[i] = nwf[base + i];
+          }
+          for (int e = threadIdx.x; e < cnt * nc; e += blockDim.x) {
+            const int i = e / nc, cc = e % nc;
+            dens2[i * kCols + cc] = u2[(size_t)(base + i) * kCols + cc];
+          }
+          __syncthreads();
+          for (int e = threadIdx.x; e < nt * cnt; e += blockDim.x) {
+            const int tt = e / cnt, i = e % cnt;
+            ent2[tt * kSrcChunk + i] = (tb + tt != base + i) ? pair_entry(st[tt], ss[i], snw[i])
+                                                             : make_float2(0.f, 0.f);
+          }
+          __syncthreads();
+          if (col_on) {
+            for (int i = 0; i < cnt; i++) {
+              const float2 dv = dens2[i * kCols + lane];
+#pragma unroll
+              for (int k = 0; k < kWarpTargets; k++) {
+                const int tt = warp + kLeafWarps * k;
+                if (tt < nt) pair_fma(nh[k], nl[k], ent2[tt * kSrcChunk + i], dv);
+              }
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kWarpTargets; k++) acc[k] += (double)nh[k] + (double)nl[k];
+    } else
     for (int v = near_off[lf]; v < near_off[lf + 1]; v++) {
       const int sl = near_leaf[v];
       const int s0 = leaf_start[sl], s1 = leaf_start[sl + 1];
@@ -441,8 +503,8 @@ __global__ void __launch_bounds__(kLeafThreads)
         const int cnt = min(kSrcChunk, s1 - base);
         __syncthreads();   // readers of bufA / bufB done
         for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-          near_load(z, zf, base + i, &ss[i]);
-          near_nw(nw, nw32, base + i, &snw[i]);
+          ss[i] = zf[base + i];
+          snw[i] = nw32[base + i];
         }
         for (int e = threadIdx.x; e < cnt * nc; e += blockDim.x) {
           const int i = e / nc, cc = e % nc;
@@ -488,7 +550,7 @@ __global__ void __launch_bounds__(kLeafThreads)
 }
 
 // FP64 -> FP32 copies for the FP32 apply: complex arrays, and the sorted
-// points as hi/lo pairs.
+// points (and nw) as hi/lo pairs.
 __global__ void k_round_cplx(const double2* a, size_t count, float2* out) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count;
        e += (size_t)gridDim.x * blockDim.x)
@@ -640,6 +702,8 @@ struct Fmm2d {
   float2 *d_Tph32 = nullptr, *d_Mph32 = nullptr, *d_nw32 = nullptr;
   float *d_Tr32 = nullptr, *d_Sr32 = nullptr, *d_Mr32 = nullptr;
   float4* d_zf = nullptr;
+  // FP32 pairs (hi x, hi y, lo x, lo y) of nw for the FP64 apply's near field
+  float4* d_nwf = nullptr;
   std::vector<void*> owned;
   cudaStream_t stream = nullptr;   // the upload stream; frees are ordered on it
   ~Fmm2d() {
@@ -978,8 +1042,13 @@ void ensure_fp32(Fmm2d& F, cudaStream_t s) {
   KI_FMM_CUDA(pool_malloc((void**)&zf, sizeof(float4) * (size_t)F.n, s));
   F.owned.push_back(zf);
   ki::launch(k_split_points, (F.n + 255) / 256, 256, 0, s, F.d_z, F.n, zf);
+  float4* nwf = nullptr;
+  KI_FMM_CUDA(pool_malloc((void**)&nwf, sizeof(float4) * (size_t)F.n, s));
+  F.owned.push_back(nwf);
+  ki::launch(k_split_points, (F.n + 255) / 256, 256, 0, s, F.d_nw, F.n, nwf);
   KI_FMM_CUDA(cudaGetLastError());
   F.d_zf = zf;
+  F.d_nwf = nwf;
 }
 
 template <typename R>
@@ -993,6 +1062,9 @@ void apply_impl(Fmm2d& F, const R* Tr, const R* Sr, const cplx_t<R>* Tph, const 
   R* q = nullptr;
   V *me = nullptr, *le = nullptr;
   KI_FMM_CUDA(pool_malloc((void**)&q, sizeof(R) * (size_t)n * kCols, s));
+  // FP64 apply: the densities also as FP32 pairs for the near field
+  float2* q2 = nullptr;
+  if (sizeof(R) == 8) KI_FMM_CUDA(pool_malloc((void**)&q2, sizeof(float2) * (size_t)n * kCols, s));
   KI_FMM_CUDA(pool_malloc((void**)&me, sizeof(V) * (size_t)nbox * p * nc_max, s));
   KI_FMM_CUDA(pool_malloc((void**)&le, sizeof(V) * (size_t)nbox * p * nc_max, s));
   for (int c0 = 0; c0 < ncols; c0 += kCols) {
@@ -1006,7 +1078,8 @@ void apply_impl(Fmm2d& F, const R* Tr, const R* Sr, const cplx_t<R>* Tph, const 
     const int nl2 = F.lvl_off[L + 1] - F.lvl_off[3 > L ? L + 1 : 3];
     if (rec) rec->begin(names[0], (double)n * pp * (4.0 * cx + 6.0) +
                                   cx * (double)(nbox - 1) * (2.0 * pp * (pp + 1) + 14.0 * pp));
-    ki::launch(k_densities<R>, (n + 31) / 32, dim3(32, 8), 0, s, F.d_perm, n, mu, ldmu, c0, nc, q);
+    ki::launch(k_densities<R>, (n + 31) / 32, dim3(32, 8), 0, s, F.d_perm, n, mu, ldmu, c0, nc, q,
+               q2);
     ki::launch(k_p2m<R>, F.nleaf, 256, 0, s, F.d_leaf_start, F.d_leaf_box, F.d_centre,
                                      F.side0 / (double)(1L << L), F.d_z, F.d_nw, q, nc, p, me);
     for (int l = L; l >= 1; l--) {
@@ -1034,12 +1107,13 @@ void apply_impl(Fmm2d& F, const R* Tr, const R* Sr, const cplx_t<R>* Tph, const 
                                   (double)n * pp * (4.0 * cx + 6.0));
     ki::launch(k_leaf_eval<R>, F.nleaf, kLeafThreads, 0, s,
         F.d_leaf_start, F.d_leaf_box, F.d_near_off, F.d_near_leaf, F.d_centre,
-        F.side0 / (double)(1L << L), F.d_z, F.d_zf, F.d_nw, F.d_nw32, F.d_diag, F.d_perm, q, le,
-        nc, p, mu, ldmu, c0, y, ldy);
+        F.side0 / (double)(1L << L), F.d_z, F.d_zf, F.d_nw32, F.d_nwf, F.d_diag, F.d_perm, q,
+        (const float2*)q2, le, nc, p, mu, ldmu, c0, y, ldy);
     if (rec) rec->end();
     KI_FMM_CUDA(cudaGetLastError());
   }
   KI_FMM_CUDA(cudaFreeAsync(q, s));
+  if (q2) KI_FMM_CUDA(cudaFreeAsync(q2, s));
   KI_FMM_CUDA(cudaFreeAsync(me, s));
   KI_FMM_CUDA(cudaFreeAsync(le, s));
 }
@@ -1056,6 +1130,7 @@ void fmm2d_apply(Fmm2d& F, const double* mu, int ldmu, int ncols, double* y, int
                       ldy, s, p, rec, names);
   } else {
     static const char* const names[4] = {"fmm_upward", "fmm_m2l", "fmm_l2l", "fmm_near"};
+    ensure_fp32(F, s);   // the near field's point and nw pairs
     apply_impl<double>(F, F.d_Tr, F.d_Sr, F.d_Tph, F.d_Mr, F.d_Mph, mu, ldmu, ncols, y, ldy, s,
                        p, rec, names);
   }
