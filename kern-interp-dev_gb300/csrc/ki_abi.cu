@@ -262,7 +262,9 @@ constexpr int kBorderCols = 32;
 // memory (32 x nb), stages alpha 32 columns at a time, and lanes are columns
 // with warps on DOFs (the U entry broadcast, alpha conflict-free); the tile
 // goes out through shared memory so that a warp writes 32 DOFs of one
-// column.  Shared memory: sizeof(R) * (32 (nb + 1) + 32 nb + 32 * 33).
+// column.  Shared memory: sizeof(R) * (32 (nb + 1) + 32 nb + 32 * 33).  In
+// FP64 the entries and alpha are held as FP32 pairs and summed with pair_fma
+// (the FP32 pipes; the entries themselves are formed in FP64).
 constexpr int kBorderTile = 32;
 template <typename R>
 size_t border_tile_smem(int nb) {
@@ -291,21 +293,38 @@ __global__ void __launch_bounds__(256) k_border_apply_tile(const double* px, con
     const double xp[3] = {px[p], py[p], dim == 3 ? pz[p] : 0.0};
     R rr[3];
     for (int d = 0; d < dim; d++) rr[d] = R(xp[d] - hc[dim * h + d]);
-    Us[(size_t)q * (nb + 1) + b] = border_u<R>(dim, sol_dim, comp, kk, rr);
+    const R u = border_u<R>(dim, sol_dim, comp, kk, rr);
+    if constexpr (sizeof(R) == 8)   // FP64: the entries as FP32 pairs (same bytes)
+      reinterpret_cast<float2*>(Us)[(size_t)q * (nb + 1) + b] = ki::split_pair(u);
+    else
+      Us[(size_t)q * (nb + 1) + b] = u;
   }
   for (int c0 = 0; c0 < ncols; c0 += 32) {
     const int nc = min(32, ncols - c0);
     __syncthreads();
     for (int e = threadIdx.x; e < nb * 32; e += blockDim.x) {
       const int b = e / 32, c = e % 32;
-      As[e] = c < nc ? R(alpha[b + (size_t)lda * (c0 + c)]) : R(0);
+      const double a = c < nc ? alpha[b + (size_t)lda * (c0 + c)] : 0.0;
+      if constexpr (sizeof(R) == 8)
+        reinterpret_cast<float2*>(As)[e] = ki::split_pair(a);
+      else
+        As[e] = R(a);
     }
     __syncthreads();
     for (int q = warp; q < nd; q += nw) {
-      const R* u = Us + (size_t)q * (nb + 1);
-      R acc = R(0);
-      for (int b = 0; b < nb; b++) acc += u[b] * As[b * 32 + lane];
-      out[q * 33 + lane] = acc;
+      if constexpr (sizeof(R) == 8) {
+        // FP64 sums as FP32-pair products and sums (pair_fma) on the FP32 pipes
+        const float2* u = reinterpret_cast<const float2*>(Us) + (size_t)q * (nb + 1);
+        const float2* a = reinterpret_cast<const float2*>(As);
+        float ah = 0.f, al = 0.f;
+        for (int b = 0; b < nb; b++) ki::pair_fma(ah, al, u[b], a[b * 32 + lane]);
+        out[q * 33 + lane] = (double)ah + (double)al;
+      } else {
+        const R* u = Us + (size_t)q * (nb + 1);
+        R acc = R(0);
+        for (int b = 0; b < nb; b++) acc += u[b] * As[b * 32 + lane];
+        out[q * 33 + lane] = acc;
+      }
     }
     __syncthreads();
     for (int e = threadIdx.x; e < nd * nc; e += blockDim.x) {

@@ -40,14 +40,51 @@ constexpr int kMaxP = 32;        // expansion terms (upper bound)
 constexpr int kChunk = 32;       // source points staged per shared-memory chunk
 constexpr double kPi2 = 6.283185307179586476925286766559;
 
-// Complex values of the expansions: double2 (FP64 arithmetic) or float2
+// The FP64-accurate apply's arithmetic: an FP32 pair (value h + l, about 48
+// significant bits), operated on the FP32 pipes, which run at 64x the FP64
+// rate on this part.  Products split the high parts exactly (fma) and carry
+// the cross terms; sums use Knuth's two-sum.  Results are not renormalised
+// (l stays within a few ulps of h), which the first-order cross terms of the
+// next operation absorb; every step adds an error near 2^-47 of its operands,
+// far under the expansions' truncation error.  The _rn intrinsics keep the
+// compiler from fusing the separately rounded steps.
+struct pr {
+  float h, l;
+  pr() = default;
+  __host__ __device__ __forceinline__ pr(float hi, float lo) : h(hi), l(lo) {}
+  __device__ __forceinline__ pr(double v) {
+    h = (float)v;
+    l = (float)(v - (double)h);
+  }
+  __device__ __forceinline__ pr(int v) : h((float)v), l(0.f) {}
+  __device__ __forceinline__ explicit operator double() const { return (double)h + (double)l; }
+};
+__device__ __forceinline__ pr operator-(pr a) { return pr(-a.h, -a.l); }
+__device__ __forceinline__ pr operator*(pr a, pr b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return pr(p, e);
+}
+__device__ __forceinline__ pr operator+(pr a, pr b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  return pr(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ pr operator-(pr a, pr b) { return a + (-b); }
+struct cpr {
+  pr x, y;
+};
+
+// Complex values of the expansions: pairs (the FP64-accurate apply) or float2
 // (FP32 arithmetic, the low-accuracy apply of residual updates).
 template <typename R> struct Cplx;
-template <> struct Cplx<double> { using type = double2; };
+template <> struct Cplx<pr> { using type = cpr; };
 template <> struct Cplx<float> { using type = float2; };
 template <typename R> using cplx_t = typename Cplx<R>::type;
 
-__device__ __forceinline__ double fmx(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ pr fmx(pr a, pr b, pr c) { return c + a * b; }
 __device__ __forceinline__ float fmx(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
 template <typename V> __device__ __forceinline__ V czero() {
@@ -77,13 +114,12 @@ template <typename V> __device__ __forceinline__ V cround(double x, double y) {
 }
 
 // u[i kCols + c] = mu[perm[i] + ldmu (c0 + c)]: the densities in sorted
-// order, point-major (a point's columns contiguous), in the expansion type;
-// with u2 also as FP32 pairs (the FP64 apply's near field).
+// order, point-major (a point's columns contiguous), in the expansion type.
 // Block (32, 8) per 32 points: columns read along the points (coalesced in
 // mu), written along the columns through shared memory.
 template <typename R>
 __global__ void k_densities(const int* perm, int n, const double* mu, int ldmu, int c0, int nc,
-                            R* u, float2* u2) {
+                            R* u) {
   __shared__ R tile[32][kCols + 1];
   const int i0 = blockIdx.x * 32;
   const int i = i0 + threadIdx.x;
@@ -96,12 +132,7 @@ __global__ void k_densities(const int* perm, int n, const double* mu, int ldmu, 
   const int cnt = min(32, n - i0);
   for (int e = threadIdx.y * 32 + threadIdx.x; e < cnt * nc; e += 32 * blockDim.y) {
     const int r = e / nc, c = e % nc;
-    const R v = tile[r][c];
-    u[(size_t)(i0 + r) * kCols + c] = v;
-    if (u2) {   // the FP64 density as an FP32 pair hi + lo
-      const float h = (float)v;
-      u2[(size_t)(i0 + r) * kCols + c] = make_float2(h, (float)((double)v - (double)h));
-    }
+    u[(size_t)(i0 + r) * kCols + c] = tile[r][c];
   }
 }
 
@@ -357,7 +388,7 @@ __device__ __forceinline__ float2 pair_entry(const float4& t, const float4& s, c
 // keep their full relative accuracy; nw_s = -(w_s / 2 pi) n_s likewise as
 // pairs in the FP64 apply, rounded in the FP32 one.
 template <typename R> struct NearNw;
-template <> struct NearNw<double> { using type = float4; };
+template <> struct NearNw<pr> { using type = float4; };
 template <> struct NearNw<float> { using type = float2; };
 
 // The Nystrom entry Re(nw_s / (t - s)) = (nw_s . (t - s)) / |t - s|^2 in FP32
@@ -397,8 +428,8 @@ __global__ void __launch_bounds__(kLeafThreads)
                 const int* near_leaf, const double2* centre, double side, const double2* z,
                 const float4* zf, const float2* nw32, const float4* nwf,
                 const double* diag,
-                const int* perm, const R* u, const float2* u2, const cplx_t<R>* le, int nc,
-                int p, const double* mu, int ldmu, int c0, double* y, int ldy) {
+                const int* perm, const R* u, const cplx_t<R>* le, int nc, int p,
+                const double* mu, int ldmu, int c0, double* y, int ldy) {
   using V = cplx_t<R>;
   using W = typename NearNw<R>::type;
   __shared__ V bufA[kPassTargets * kMaxP];   // powers [t][m] (complex), then entries [t][s] (real)
@@ -454,7 +485,8 @@ __global__ void __launch_bounds__(kLeafThreads)
     // FP64 apply: entries (pair_entry) and densities as FP32 pairs, summed with
     // pair_fma: the FP32 pipes instead of the FP64 pipe, which runs at 1/64 of
     // their rate on this part.
-    if constexpr (sizeof(R) == 8) {
+    if constexpr (std::is_same<R, pr>::value) {
+      const float2* u2 = reinterpret_cast<const float2*>(u);   // the pairs' layout
       float2* ent2 = reinterpret_cast<float2*>(bufA);    // [t][s]
       float2* dens2 = reinterpret_cast<float2*>(bufB);   // [s][c]
       float nh[kWarpTargets], nl[kWarpTargets];
@@ -494,7 +526,7 @@ __global__ void __launch_bounds__(kLeafThreads)
         }
       }
 #pragma unroll
-      for (int k = 0; k < kWarpTargets; k++) acc[k] += (double)nh[k] + (double)nl[k];
+      for (int k = 0; k < kWarpTargets; k++) acc[k] = acc[k] + pr(nh[k], nl[k]);
     } else
     for (int v = near_off[lf]; v < near_off[lf + 1]; v++) {
       const int sl = near_leaf[v];
@@ -555,6 +587,19 @@ __global__ void k_round_cplx(const double2* a, size_t count, float2* out) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count;
        e += (size_t)gridDim.x * blockDim.x)
     out[e] = make_float2((float)a[e].x, (float)a[e].y);
+}
+// FP64 -> FP32 pairs for the FP64-accurate apply's tables.
+__global__ void k_pair_cplx(const double2* a, size_t count, cpr* out) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count;
+       e += (size_t)gridDim.x * blockDim.x) {
+    out[e].x = pr(a[e].x);
+    out[e].y = pr(a[e].y);
+  }
+}
+__global__ void k_pair_real(const double* a, size_t count, pr* out) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count;
+       e += (size_t)gridDim.x * blockDim.x)
+    out[e] = pr(a[e]);
 }
 __global__ void k_round_real(const double* a, size_t count, float* out) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count;
@@ -702,8 +747,11 @@ struct Fmm2d {
   float2 *d_Tph32 = nullptr, *d_Mph32 = nullptr, *d_nw32 = nullptr;
   float *d_Tr32 = nullptr, *d_Sr32 = nullptr, *d_Mr32 = nullptr;
   float4* d_zf = nullptr;
-  // FP32 pairs (hi x, hi y, lo x, lo y) of nw for the FP64 apply's near field
+  // FP32-pair copies for the FP64-accurate apply: nw (hi x, hi y, lo x, lo y)
+  // for the near field, and the translation tables
   float4* d_nwf = nullptr;
+  cpr *d_Tph2 = nullptr, *d_Mph2 = nullptr;
+  pr *d_Tr2 = nullptr, *d_Sr2 = nullptr, *d_Mr2 = nullptr;
   std::vector<void*> owned;
   cudaStream_t stream = nullptr;   // the upload stream; frees are ordered on it
   ~Fmm2d() {
@@ -1038,6 +1086,25 @@ void ensure_fp32(Fmm2d& F, cudaStream_t s) {
   F.d_Mr32 = round_real(F.d_Mr, 49 * pp);
   F.d_Tr32 = round_real(F.d_Tr, 4 * pp);
   F.d_Sr32 = round_real(F.d_Sr, 4 * pp);
+  auto pair_cplx = [&](const double2* a, size_t count) {
+    cpr* d = nullptr;
+    KI_FMM_CUDA(pool_malloc((void**)&d, sizeof(cpr) * count, s));
+    F.owned.push_back(d);
+    ki::launch(k_pair_cplx, (int)std::min<size_t>(1024, (count + 255) / 256), 256, 0, s, a, count, d);
+    return d;
+  };
+  auto pair_real = [&](const double* a, size_t count) {
+    pr* d = nullptr;
+    KI_FMM_CUDA(pool_malloc((void**)&d, sizeof(pr) * count, s));
+    F.owned.push_back(d);
+    ki::launch(k_pair_real, (int)std::min<size_t>(1024, (count + 255) / 256), 256, 0, s, a, count, d);
+    return d;
+  };
+  F.d_Tph2 = pair_cplx(F.d_Tph, 4 * (size_t)F.p);
+  F.d_Mph2 = pair_cplx(F.d_Mph, 49 * (size_t)(F.p + 1));
+  F.d_Mr2 = pair_real(F.d_Mr, 49 * pp);
+  F.d_Tr2 = pair_real(F.d_Tr, 4 * pp);
+  F.d_Sr2 = pair_real(F.d_Sr, 4 * pp);
   float4* zf = nullptr;
   KI_FMM_CUDA(pool_malloc((void**)&zf, sizeof(float4) * (size_t)F.n, s));
   F.owned.push_back(zf);
@@ -1062,9 +1129,6 @@ void apply_impl(Fmm2d& F, const R* Tr, const R* Sr, const cplx_t<R>* Tph, const 
   R* q = nullptr;
   V *me = nullptr, *le = nullptr;
   KI_FMM_CUDA(pool_malloc((void**)&q, sizeof(R) * (size_t)n * kCols, s));
-  // FP64 apply: the densities also as FP32 pairs for the near field
-  float2* q2 = nullptr;
-  if (sizeof(R) == 8) KI_FMM_CUDA(pool_malloc((void**)&q2, sizeof(float2) * (size_t)n * kCols, s));
   KI_FMM_CUDA(pool_malloc((void**)&me, sizeof(V) * (size_t)nbox * p * nc_max, s));
   KI_FMM_CUDA(pool_malloc((void**)&le, sizeof(V) * (size_t)nbox * p * nc_max, s));
   for (int c0 = 0; c0 < ncols; c0 += kCols) {
@@ -1078,8 +1142,7 @@ void apply_impl(Fmm2d& F, const R* Tr, const R* Sr, const cplx_t<R>* Tph, const 
     const int nl2 = F.lvl_off[L + 1] - F.lvl_off[3 > L ? L + 1 : 3];
     if (rec) rec->begin(names[0], (double)n * pp * (4.0 * cx + 6.0) +
                                   cx * (double)(nbox - 1) * (2.0 * pp * (pp + 1) + 14.0 * pp));
-    ki::launch(k_densities<R>, (n + 31) / 32, dim3(32, 8), 0, s, F.d_perm, n, mu, ldmu, c0, nc, q,
-               q2);
+    ki::launch(k_densities<R>, (n + 31) / 32, dim3(32, 8), 0, s, F.d_perm, n, mu, ldmu, c0, nc, q);
     ki::launch(k_p2m<R>, F.nleaf, 256, 0, s, F.d_leaf_start, F.d_leaf_box, F.d_centre,
                                      F.side0 / (double)(1L << L), F.d_z, F.d_nw, q, nc, p, me);
     for (int l = L; l >= 1; l--) {
@@ -1107,13 +1170,12 @@ void apply_impl(Fmm2d& F, const R* Tr, const R* Sr, const cplx_t<R>* Tph, const 
                                   (double)n * pp * (4.0 * cx + 6.0));
     ki::launch(k_leaf_eval<R>, F.nleaf, kLeafThreads, 0, s,
         F.d_leaf_start, F.d_leaf_box, F.d_near_off, F.d_near_leaf, F.d_centre,
-        F.side0 / (double)(1L << L), F.d_z, F.d_zf, F.d_nw32, F.d_nwf, F.d_diag, F.d_perm, q,
-        (const float2*)q2, le, nc, p, mu, ldmu, c0, y, ldy);
+        F.side0 / (double)(1L << L), F.d_z, F.d_zf, F.d_nw32, F.d_nwf, F.d_diag, F.d_perm, q, le,
+        nc, p, mu, ldmu, c0, y, ldy);
     if (rec) rec->end();
     KI_FMM_CUDA(cudaGetLastError());
   }
   KI_FMM_CUDA(cudaFreeAsync(q, s));
-  if (q2) KI_FMM_CUDA(cudaFreeAsync(q2, s));
   KI_FMM_CUDA(cudaFreeAsync(me, s));
   KI_FMM_CUDA(cudaFreeAsync(le, s));
 }
@@ -1130,8 +1192,8 @@ void fmm2d_apply(Fmm2d& F, const double* mu, int ldmu, int ncols, double* y, int
                       ldy, s, p, rec, names);
   } else {
     static const char* const names[4] = {"fmm_upward", "fmm_m2l", "fmm_l2l", "fmm_near"};
-    ensure_fp32(F, s);   // the near field's point and nw pairs
-    apply_impl<double>(F, F.d_Tr, F.d_Sr, F.d_Tph, F.d_Mr, F.d_Mph, mu, ldmu, ncols, y, ldy, s,
+    ensure_fp32(F, s);   // the pair tables and the near field's point and nw pairs
+    apply_impl<pr>(F, F.d_Tr2, F.d_Sr2, F.d_Tph2, F.d_Mr2, F.d_Mph2, mu, ldmu, ncols, y, ldy, s,
                        p, rec, names);
   }
 }
