@@ -407,6 +407,140 @@ __device__ int cta_gj_inverse(int n, T* A, int lda, int* piv, T* colj, T* s_val,
   return info;
 }
 
+// The same inverse with the matrix held in registers: lane x of warp w owns
+// rows x + 32 a (a < MA) and columns w + W b (b < MAXB), W warps, so that
+// each step is one FMA per owned element with the pivot column (per lane) and
+// the pivot row (broadcast per warp) read from shared memory.  Rows are not
+// swapped: step j takes as pivot the unused row p of largest |A(p, j)| (ties
+// to the lowest row; every warp finds it from the staged column, so no
+// barrier is spent on the search) and eliminates column j with it in place
+// (A(p, j) = 1/pivot, A(p, c) /= pivot, A(i, j) = -A(i, j)/pivot,
+// A(i, c) -= A(i, j) A(p, c)); the result is the inverse with rows and
+// columns permuted, X^-1(j, m) = A(p_j, c) with p_c = m, which the final store
+// undoes.  Two barriers per column.  Requires n <= 32 MA and n <= W MAXB;
+// scratch: 3n of T and 2n ints (shared).  piv[j] = p_j (device memory).
+// Returns the first zero pivot + 1, or 0.
+template <typename T, int MA, int MAXB>
+__device__ __noinline__ int cta_gj_inverse_reg(int n, T* A, int lda, int* piv, T* scratch) {
+  T* colbuf = scratch;                   // [2][n]: column j (double-buffered)
+  T* rowbuf = scratch + 2 * n;           // pivot row after scaling
+  int* spiv = reinterpret_cast<int*>(scratch + 3 * n);   // p_j
+  int* spinv = spiv + n;                  // j of pivot row p
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, W = blockDim.x >> 5;
+  T a[MA][MAXB];
+#pragma unroll
+  for (int ia = 0; ia < MA; ia++)
+#pragma unroll
+    for (int ib = 0; ib < MAXB; ib++) {
+      const int i = lane + 32 * ia, c = w + W * ib;
+      a[ia][ib] = (i < n && c < n) ? A[i + (size_t)lda * c] : T(0);
+    }
+  // column j of the register tile into colbuf[j & 1] (warp j % W, uniform)
+  auto stage_col = [&](int j) {
+    if (w != j % W) return;
+    const int jb = j / W;
+    T* dst = colbuf + (j & 1) * n;
+#pragma unroll
+    for (int ib = 0; ib < MAXB; ib++)
+      if (ib == jb)
+#pragma unroll
+        for (int ia = 0; ia < MA; ia++) {
+          const int i = lane + 32 * ia;
+          if (i < n) dst[i] = a[ia][ib];
+        }
+  };
+  stage_col(0);
+  unsigned used = 0;   // bit ia: row lane + 32 ia already a pivot row
+  int info = 0;
+  for (int j = 0; j < n; j++) {
+    const T* cj = colbuf + (j & 1) * n;
+    __syncthreads();   // column j staged; the previous step's readers of rowbuf done
+    T f[MA];
+    T best = T(-1);
+    int bi = n;
+#pragma unroll
+    for (int ia = 0; ia < MA; ia++) {
+      const int i = lane + 32 * ia;
+      f[ia] = i < n ? cj[i] : T(0);
+      if (i < n && !((used >> ia) & 1u)) {
+        T v = fabs(f[ia]);
+        if (!(v == v)) v = T(3e38);   // a NaN orders first, so the choice stays a valid row
+        if (v > best) { best = v; bi = i; }
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const T ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+    }
+    const int p = bi;
+    const int pa = p >> 5;
+    const bool p_mine = (p & 31) == lane;
+    if (p_mine) used |= 1u << pa;
+    if (threadIdx.x == 0) {
+      piv[j] = p;
+      spiv[j] = p;
+      spinv[p] = j;
+    }
+    const T pv = cj[p];
+    if (pv == T(0)) {   // the same branch in every thread
+      if (info == 0) info = j + 1;
+      if (j + 1 < n) stage_col(j + 1);
+      continue;
+    }
+    const T inv = T(1) / pv;
+    // the pivot row, scaled, by its owners (lane p % 32 of every warp)
+    if (p_mine) {
+#pragma unroll
+      for (int ia = 0; ia < MA; ia++)
+        if (ia == pa)
+#pragma unroll
+          for (int ib = 0; ib < MAXB; ib++) {
+            const int c = w + W * ib;
+            if (c < n) {
+              const T v = (c == j) ? inv : a[ia][ib] * inv;
+              a[ia][ib] = v;
+              rowbuf[c] = v;
+            }
+          }
+    }
+    __syncthreads();   // rowbuf written
+    // every other row: A(i, c) -= f_i A(p, c); column j: -f_i / pivot
+#pragma unroll
+    for (int ia = 0; ia < MA; ia++)
+      if (p_mine && ia == pa) f[ia] = T(0);
+#pragma unroll
+    for (int ib = 0; ib < MAXB; ib++) {
+      const int c = w + W * ib;
+      const T rb = c < n ? rowbuf[c] : T(0);
+#pragma unroll
+      for (int ia = 0; ia < MA; ia++) a[ia][ib] = fma(-f[ia], rb, a[ia][ib]);
+    }
+    if (w == j % W) {
+      const int jb = j / W;
+#pragma unroll
+      for (int ib = 0; ib < MAXB; ib++)
+        if (ib == jb)
+#pragma unroll
+          for (int ia = 0; ia < MA; ia++)
+            if (!(p_mine && ia == pa)) a[ia][ib] = -f[ia] * inv;
+    }
+    if (j + 1 < n) stage_col(j + 1);
+  }
+  __syncthreads();   // every step's pivots recorded
+  // X^-1(spinv[i], spiv[c]) = a(i, c)
+#pragma unroll
+  for (int ia = 0; ia < MA; ia++)
+#pragma unroll
+    for (int ib = 0; ib < MAXB; ib++) {
+      const int i = lane + 32 * ia, c = w + W * ib;
+      if (i < n && c < n) A[spinv[i] + (size_t)lda * spiv[c]] = a[ia][ib];
+    }
+  __syncthreads();
+  return info;
+}
+
 // B(n x nrhs) <- A^-1 B (trans=false) or A^-T B (trans=true) from cta_lu.
 template <typename T>
 __device__ void cta_lu_solve(int n, const T* LU, int lda, const int* piv, bool trans, T* B,

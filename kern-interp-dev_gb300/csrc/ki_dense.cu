@@ -230,26 +230,35 @@ __global__ void k_tri_update(const T* LU, int lda, int p, int w, int r0, int r1,
   }
 }
 
-// The whole solve L U x = P b for one 32-column chunk of B per CTA, the chunk
-// held in shared memory (n x 32, odd leading dimension): pivots, then the
+// The whole solve L U x = P b for one cw-column chunk of B per CTA (cw <= 32),
+// the chunk held in shared memory (n x cw, odd leading dimension): pivots, then the
 // blocked forward and backward substitutions of the launches above in one
 // kernel -- each kNb-row diagonal block staged and solved one thread per
 // column, the rows below (above) it updated by every thread.  The same
 // operations in the same order as the multi-launch path.
 template <typename T>
-size_t fused_solve_smem(int n) {
-  return sizeof(T) * ((size_t)(n | 1) * 32 + (size_t)kNb * (kNb + 1));
+size_t fused_solve_smem(int n, int cw = 32) {
+  return sizeof(T) * ((size_t)(n | 1) * cw + (size_t)kNb * (kNb + 1));
+}
+
+// Columns per CTA of the fused solve: narrower chunks when the right-hand
+// sides are few, so that about 16 CTAs share the substitutions (each reads
+// the factors from L2) instead of one or two.
+inline int fused_solve_cols(int nrhs) {
+  int cw = 32;
+  while (cw > 4 && (nrhs + cw - 1) / cw < 16) cw >>= 1;
+  return cw;
 }
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_lu_solve_fused(const T* LU, int n, const int* piv, T* B,
-                                                        int ldb, int nrhs) {
+                                                        int ldb, int nrhs, int cw) {
   extern __shared__ __align__(16) unsigned char fs_smem[];
   const int ldx = n | 1;
   T* X = reinterpret_cast<T*>(fs_smem);
-  T (*D)[kNb + 1] = reinterpret_cast<T (*)[kNb + 1]>(X + (size_t)ldx * 32);
+  T (*D)[kNb + 1] = reinterpret_cast<T (*)[kNb + 1]>(X + (size_t)ldx * cw);
   const int tid = threadIdx.x, nth = blockDim.x;
-  const int c0 = blockIdx.x * 32, nc = min(32, nrhs - c0);
+  const int c0 = blockIdx.x * cw, nc = min(cw, nrhs - c0);
   for (int e = tid; e < n * nc; e += nth) {
     const int c = e / n, i = e % n;
     X[i + (size_t)ldx * c] = B[i + (size_t)ldb * (c0 + c)];
@@ -334,11 +343,12 @@ void dense_lu_solve(const T* LU, int n, const int* piv, T* B, int ldb, int nrhs,
                     cudaStream_t s) {
   if (n == 0 || nrhs == 0) return;
   dim3 cb((nrhs + 127) / 128);
-  if (!trans && fused_solve_smem<T>(n) <= 160 * 1024) {
+  const int cw = fused_solve_cols(nrhs);
+  if (!trans && fused_solve_smem<T>(n, cw) <= 160 * 1024) {
     KI_DENSE_CUDA(cudaFuncSetAttribute(k_lu_solve_fused<T>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
-    ki::launch(k_lu_solve_fused<T>, (nrhs + 31) / 32, 256, fused_solve_smem<T>(n), s, LU, n, piv, B, ldb,
-                                                                             nrhs);
+    ki::launch(k_lu_solve_fused<T>, (nrhs + cw - 1) / cw, 256, fused_solve_smem<T>(n, cw), s, LU, n, piv,
+               B, ldb, nrhs, cw);
     KI_DENSE_CUDA(cudaGetLastError());
     return;
   }

@@ -1337,6 +1337,9 @@ __global__ void k_assemble(const AsmTask<T>* tasks, const int* ipool, Points<T> 
 // with two CTAs per SM.  Boxes whose shared working set leaves room for only
 // one or two CTAs per SM get the larger blocks (schur_threads).
 template <typename T> constexpr int kSchurMaxThreads = sizeof(T) == 4 ? 1024 : kThreads;
+// Register tile of the Gauss-Jordan inverse: up to kGjCols columns per warp
+// (X up to 64 rows and kGjCols W columns with W warps).
+constexpr int kGjCols = 8;
 template <typename T> constexpr int kSchurMinBlocks = sizeof(T) == 4 ? 1 : 2;
 template <typename T>
 __global__ void __launch_bounds__(kSchurMaxThreads<T>, kSchurMinBlocks<T>) k_schur(const SchurTask<T>* tasks, int task_base,
@@ -1389,14 +1392,18 @@ __global__ void __launch_bounds__(kSchurMaxThreads<T>, kSchurMinBlocks<T>) k_sch
   cta_gemm<T>(r, r, k, T(-1), Wrs, ld, false, Tm, kt, false, T(1), X, ld);
   __syncthreads();
   if (smem && t.gj) {
-    // shared memory after X: colj (r) | X0 (r x r) | U0 (r x k) | L0 (k x r)
+    // shared memory after X: scratch (5r) | X0 (r x r) | U0 (r x k) | L0 (k x r)
     T* colj = X + (size_t)ld * r;
-    T* X0 = colj + r;
+    T* X0 = colj + 5 * (size_t)r;
     T* U0 = X0 + (size_t)ld * r;
     T* L0 = U0 + (size_t)ld * k;
     for (int idx = threadIdx.x; idx < ld * r; idx += blockDim.x) X0[idx] = X[idx];
     __syncthreads();
-    int info = cta_gj_inverse<T>(r, X, ld, t.piv, colj, s_val, &s_idx);   // X <- X^-1
+    // X <- X^-1: in registers where the block's tile covers X, else in shared memory
+    const int W = blockDim.x >> 5;
+    const int info = (r <= 64 && r <= W * kGjCols)
+                         ? cta_gj_inverse_reg<T, 2, kGjCols>(r, X, ld, t.piv, colj)
+                         : cta_gj_inverse<T>(r, X, ld, t.piv, colj, s_val, &s_idx);
     if (info != 0 && threadIdx.x == 0) atomicMax(err, (int)kDevSingular);
     // U0 = X^-1 K~_rs (r x k), L0 = K~_sr X^-1 (k x r)
     cta_gemm<T>(r, k, r, T(1), X, ld, false, Wrs, ld, false, T(0), U0, ld);
@@ -1541,13 +1548,13 @@ void copy_block(cudaStream_t s, const T* src, int lds, int rows, int cols, bool 
 }
 
 // Shared-memory bytes of k_schur for a box: K_ss, T, K~_rs, K~_sr^T, X and r
-// scratch entries, plus (inverse path) X's copy, U0 and L0.
+// scratch entries, plus (inverse path) 4r more scratch, X's copy, U0 and L0.
 template <typename T>
 size_t schur_bytes(int n, int k, bool inv) {
   const size_t r = n - k, ld = (size_t)((n - k) | 1);   // k_schur's odd leading dimensions
   const size_t kt = (size_t)(k | 1);
   return sizeof(T) * ((size_t)k * k + kt * r + 2 * ld * k + ld * r + r +
-                      (inv ? ld * r + ld * k + k * r : 0));
+                      (inv ? 4 * r + ld * r + ld * k + k * r : 0));
 }
 
 // Threads of a k_schur CTA when `per_sm` CTAs run per SM: 256 when four or
