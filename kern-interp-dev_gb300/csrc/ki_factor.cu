@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
@@ -2670,11 +2671,19 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     // (environment override KI_ID_FULL_CAP, used by the tests)
     size_t full_cap = smem_cap;
     if (const char* e = std::getenv("KI_ID_FULL_CAP")) full_cap = (size_t)std::atol(e);
+    // a level of fewer boxes than SMs leaves most SMs idle while one CTA per
+    // box folds its rows: with a learned rank its tall boxes take the wide
+    // path instead (the sketch formed by many CTAs per box)
+    static const int n_sm = device_sm_count();
+    const int few_rows = ((int)itasks.size() < n_sm && prm.rank_model) ? 384 : INT_MAX;
     std::vector<int> grp(itasks.size());
+    std::vector<char> few(itasks.size(), 0);   // wide only for the level's few boxes
     for (size_t i = 0; i < itasks.size(); i++) {
       int n = itasks[i].n;
       int md = id_smem_bytes<T>(n, 0) <= full_cap ? 0 : 1;
-      bool wide = mh[i] > kWideRows || (md == 1 && id_smem_bytes<T>(n, 2) > smem_cap);
+      const bool tall = mh[i] > kWideRows || (md == 1 && id_smem_bytes<T>(n, 2) > smem_cap);
+      few[i] = !tall && mh[i] > few_rows;
+      const bool wide = tall || few[i];
       // narrow groups: 0 triangle in shared memory, 1 packed triangle in
       // shared memory (mode 2 of k_id); wide groups: 2 / 3 by triangle size
       grp[i] = wide ? 2 + md : md;
@@ -2698,8 +2707,10 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         // boxes (groups 2, 3; k_wide_sketch, up to 384 rows; their sketches are
         // cheap next to a fallback, so they get twice the margin and
         // oversampling), not for packed triangles
+        // (boxes routed wide only because the level is small keep the narrow
+        // path's sketch size)
         int lo = lh[o];
-        if (grp[o] >= 2 && prm.rank_model)
+        if (grp[o] >= 2 && prm.rank_model && !few[o])
           lo = std::min(itasks[o].n, (int)std::ceil((1.f + 2 * prm.sketch_margin) * khat[o]) +
                                          2 * prm.sketch_oversample);
         l2.push_back(grp[o] == 1 || (grp[o] >= 2 && lo > 384) ? 0 : lo);
@@ -2720,7 +2731,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       upload(d_lsk, lh, s);
     }
     const bool sketching = prm.rank_model != nullptr;
-    int next_aux = 0;
+    int next_aux = 0, n_streams = Factorization<T>::kAux - 1;
     auto launch_range = [&](int g, int flags, cudaStream_t fixed) {
       // tasks of group g are contiguous and sorted by n within the group (see
       // the ordering above); launch them in bins of similar shared-memory
@@ -2753,7 +2764,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
           b1++;
         }
         if (sm > smem_cap) throw std::runtime_error("box too large for the ID kernel");
-        cudaStream_t st = fixed ? fixed : F->aux[(next_aux++) % (Factorization<T>::kAux - 1)];
+        cudaStream_t st = fixed ? fixed : F->aux[(next_aux++) % n_streams];
         launch_k_id<T>(fr, (unsigned)(b1 - b0), sm, st, (const IdTask*)d_it, b0,
                        (const int64_t*)d_soff, (const int*)d_slen, ipool, d_irows, d_tws, P, sd, ptab,
                        prm.id_tol, d_k, d_m, kmode, flags,
@@ -2845,8 +2856,22 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         F->stage_end(ws3);
         std::string wc = "wide_cpqr@L" + std::to_string(l);
         F->stage_begin(wc.c_str(), 0, 0, ws3);
-        launch_range(2, 4, ws3);
-        launch_range(3, 4, ws3);
+        // the pivoted QRs of the wide boxes' sketches / triangles, bins spread
+        // over every aux stream (after the sketches on ws3; the upper levels
+        // have no narrow boxes to share them with), joined back into ws3
+        cudaEvent_t wev[Factorization<T>::kAux];
+        for (auto& e : wev) KI_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        KI_CUDA(cudaEventRecord(wev[0], ws3));
+        for (int i = 0; i + 1 < Factorization<T>::kAux; i++) KI_CUDA(cudaStreamWaitEvent(F->aux[i], wev[0], 0));
+        n_streams = Factorization<T>::kAux;
+        launch_range(2, 4, nullptr);
+        launch_range(3, 4, nullptr);
+        n_streams = Factorization<T>::kAux - 1;
+        for (int i = 0; i + 1 < Factorization<T>::kAux; i++) {
+          KI_CUDA(cudaEventRecord(wev[i + 1], F->aux[i]));
+          KI_CUDA(cudaStreamWaitEvent(ws3, wev[i + 1], 0));
+        }
+        for (auto& e : wev) KI_CUDA(cudaEventDestroy(e));
         F->stage_end(ws3);
         if (d_wpool) KI_CUDA(cudaFreeAsync(d_wpool, ws3));
         if (d_wt) KI_CUDA(cudaFreeAsync(d_wt, ws3));
