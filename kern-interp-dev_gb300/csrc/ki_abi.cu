@@ -268,7 +268,25 @@ constexpr int kBorderCols = 32;
 constexpr int kBorderTile = 32;
 template <typename R>
 size_t border_tile_smem(int nb) {
-  return sizeof(R) * ((size_t)kBorderTile * (nb + 1) + (size_t)nb * 32 + kBorderTile * 33);
+  const size_t b = sizeof(R) * ((size_t)kBorderTile * (nb + 1) + (size_t)nb * 32 + kBorderTile * 33);
+  // FP64: the 2D Laplace entries' FP32-pair inputs (points, hole centres, log table)
+  return sizeof(R) == 8 ? ((b + 15) & ~size_t(15)) + 16 * (size_t)(kBorderTile + nb) + 8 * 256 : b;
+}
+
+// log(1 + (j + 1/2)/256), j < 256, as FP32 pairs: the table of ki::pair_log,
+// copied in before each FP64 tile launch.
+__device__ float2 g_border_logc[256];
+const float2* border_log_table() {
+  static const std::vector<float2> tab = [] {
+    std::vector<float2> t(256);
+    for (int j = 0; j < 256; j++) {
+      const double v = std::log(1.0 + (j + 0.5) / 256.0);
+      const float h = (float)v;
+      t[j] = make_float2(h, (float)(v - (double)h));
+    }
+    return t;
+  }();
+  return tab.data();
 }
 template <typename R>
 __global__ void __launch_bounds__(256) k_border_apply_tile(const double* px, const double* py,
@@ -286,7 +304,33 @@ __global__ void __launch_bounds__(256) k_border_apply_tile(const double* px, con
   const int d0 = blockIdx.x * kBorderTile;
   const int nd = min(kBorderTile, N - d0);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int e = threadIdx.x; e < nd * nb; e += blockDim.x) {
+  // FP64, 2D Laplace: the entries 0.5 log |p - c_h|^2 in FP32-pair arithmetic
+  // (pair_dist2, pair_log) from the points and centres as pairs
+  const bool pair_entries = sizeof(R) == 8 && dim == 2 && sol_dim == 1;
+  if constexpr (sizeof(R) == 8) {
+    if (pair_entries) {
+      const size_t b0 = ((reinterpret_cast<unsigned char*>(out + kBorderTile * 33) - bt_smem) + 15) &
+                        ~size_t(15);
+      float4* spt = reinterpret_cast<float4*>(bt_smem + b0);
+      float4* shc = spt + kBorderTile;
+      float2* slog = reinterpret_cast<float2*>(shc + nh);
+      auto split4 = [](double x, double y) {
+        const float hx = (float)x, hy = (float)y;
+        return make_float4(hx, hy, (float)(x - (double)hx), (float)(y - (double)hy));
+      };
+      for (int i = threadIdx.x; i < 256; i += blockDim.x) slog[i] = g_border_logc[i];
+      for (int q = threadIdx.x; q < nd; q += blockDim.x) spt[q] = split4(px[d0 + q], py[d0 + q]);
+      for (int h = threadIdx.x; h < nh; h += blockDim.x) shc[h] = split4(hc[2 * h], hc[2 * h + 1]);
+      __syncthreads();
+      for (int e = threadIdx.x; e < nd * nb; e += blockDim.x) {
+        const int q = e / nb, b = e % nb;
+        const float2 r2 = ki::pair_dist2(spt[q], shc[b]);
+        const float2 lg = ki::pair_log(r2.x, r2.y, slog);
+        reinterpret_cast<float2*>(Us)[(size_t)q * (nb + 1) + b] = make_float2(0.5f * lg.x, 0.5f * lg.y);
+      }
+    }
+  }
+  for (int e = threadIdx.x; !pair_entries && e < nd * nb; e += blockDim.x) {
     const int q = e / nb, b = e % nb;
     const int dof = d0 + q, p = dof / sol_dim, comp = dof - sol_dim * p;
     const int h = b / cph, kk = b - cph * h;
@@ -1085,6 +1129,9 @@ void apply_bordered(ki_factor* f, const double* mu, const double* alpha, int nco
     const size_t tsm = low ? border_tile_smem<float>(nb) : border_tile_smem<double>(nb);
     if (tsm <= 100 * 1024) {
       auto tile = low ? k_border_apply_tile<float> : k_border_apply_tile<double>;
+      if (!low)
+        KI_CHECK_CUDA(cudaMemcpyToSymbolAsync(g_border_logc, border_log_table(), sizeof(float2) * 256, 0,
+                                              cudaMemcpyHostToDevice, s));
       KI_CHECK_CUDA(cudaFuncSetAttribute(tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          100 * 1024));
       ki::launch(tile, (N + kBorderTile - 1) / kBorderTile, 256, tsm, s,

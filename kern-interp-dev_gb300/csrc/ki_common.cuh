@@ -181,6 +181,67 @@ __device__ __forceinline__ void fast_two_sum(float a, float b, float& hi, float&
   lo = __fsub_rn(b, __fsub_rn(hi, a));
 }
 
+// Squared distance |t - s|^2 of two points given as FP32 pairs
+// (hi x, hi y, lo x, lo y), as a pair (value r2.x + r2.y).
+__device__ __forceinline__ float2 pair_dist2(const float4& t, const float4& s) {
+  float dxh, dxl, dyh, dyl;
+  two_diff(t.x, s.x, dxh, dxl);
+  two_diff(t.y, s.y, dyh, dyl);
+  fast_two_sum(dxh, __fadd_rn(dxl, __fsub_rn(t.z, s.z)), dxh, dxl);
+  fast_two_sum(dyh, __fadd_rn(dyl, __fsub_rn(t.w, s.w)), dyh, dyl);
+  const float a = __fmul_rn(dxh, dxh), b = __fmul_rn(dyh, dyh);
+  float r2h, r2l;
+  two_sum(a, b, r2h, r2l);
+  r2l = __fadd_rn(r2l, __fadd_rn(__fmaf_rn(dxh, dxh, -a), __fmaf_rn(dyh, dyh, -b)));
+  r2l = __fmaf_rn(2.f * dxh, dxl, __fmaf_rn(2.f * dyh, dyl, r2l));
+  fast_two_sum(r2h, r2l, r2h, r2l);
+  return make_float2(r2h, r2l);
+}
+
+// log(x) of a positive normal FP32 pair x = xh + xl, as a pair, by Tang's
+// table-driven method (ACM TOMS 16, 1990): x = 2^e m, m in [1, 2); with
+// c = 1 + (j + 1/2)/256 for the leading 8 bits j of m's fraction,
+// log x = e ln2 + log c + log1p(t), t = (m - c)/c, |t| <= 2^-9, where log c
+// comes from `logc` (pairs, formed in FP64 on the host) and log1p(t) from its
+// series t - t^2/2 + t^3/3 - t^4/4 + t^5/5 (the next term is below 2^-56), the
+// first two terms in pair arithmetic.  ln2 is split in three so that e ln2_h
+// is exact.  Absolute error about 2^-47 |log x|.
+__device__ __forceinline__ float2 pair_log(float xh, float xl, const float2* logc) {
+  constexpr double kLn2 = 0.69314718055994530942;
+  constexpr float kLn2H = 0.693145751953125f;   // 45426 / 2^16
+  constexpr float kLn2M = (float)(kLn2 - 0.693145751953125);
+  constexpr float kLn2L = (float)(kLn2 - 0.693145751953125 - (double)kLn2M);
+  const int bits = __float_as_int(xh);
+  const int e = ((bits >> 23) & 0xff) - 127;
+  const float m = __int_as_float((bits & 0x007fffff) | 0x3f800000);
+  const int j = (bits >> 15) & 0xff;
+  const float c = 1.f + ((float)j + 0.5f) * (1.f / 256.f);   // exact
+  const float dl = __fmul_rn(xl, __int_as_float((127 - e) << 23));   // xl 2^-e, exact
+  const float dh = __fsub_rn(m, c);                                   // exact (Sterbenz)
+  const float rc = __frcp_rn(c);
+  const float th = __fmul_rn(dh, rc);
+  const float tl = __fmul_rn(__fadd_rn(__fmaf_rn(-th, c, dh), dl), rc);
+  const float q = __fmul_rn(th, th);
+  const float qe = __fmaf_rn(th, th, -q);
+  const float rest = __fmul_rn(__fmul_rn(th, q),
+                               __fmaf_rn(-th, __fmaf_rn(-th, 0.2f, 0.25f), 1.f / 3.f));
+  float sh, sl;
+  two_sum(th, -0.5f * q, sh, sl);
+  sl = __fadd_rn(sl, __fadd_rn(__fsub_rn(tl, __fmaf_rn(0.5f, qe, th * tl)), rest));
+  const float2 lc = logc[j];
+  const float fe = (float)e;
+  const float pm = __fmul_rn(fe, kLn2M);
+  float s1, e1, s2, e2, s3, e3;
+  two_sum(fe * kLn2H, lc.x, s1, e1);
+  two_sum(s1, pm, s2, e2);
+  two_sum(s2, sh, s3, e3);
+  const float lo = __fadd_rn(__fadd_rn(__fadd_rn(e1, e2), __fadd_rn(e3, __fmaf_rn(fe, kLn2M, -pm))),
+                             __fadd_rn(__fmaf_rn(fe, kLn2L, lc.y), sl));
+  float rh, rl;
+  two_sum(s3, lo, rh, rl);
+  return make_float2(rh, rl);
+}
+
 // ------------------------------------------------------------------------
 // CTA-cooperative dense helpers on column-major matrices (shared or global
 // memory).  All threads of the block must call them.
