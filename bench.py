@@ -476,8 +476,9 @@ def main():
     name, a = top
     sec = a["ms"] / 1e3
     ach_tflops = a["flops"] / sec / 1e12 if sec > 0 else 0.0
-    if name.startswith("refine:fmm32") or name == "refine:fmm_near":
-        # the FP64 apply's near field accumulates FP32 pairs on the FP32 pipes
+    if name.startswith("refine:fmm") or name == "refine:border_apply":
+        # the FP32 FMM, and the FP64-accurate FMM and hole columns computed in
+        # FP32-pair arithmetic: all on the FP32 pipes
         fp64_stage = False
     elif name.startswith("refine:"):
         fp64_stage = True
