@@ -305,6 +305,17 @@ def main():
     pin_b = torch.from_numpy(rhs_f.T.copy()).pin_memory()
     pin_x = torch.empty_like(pin_b).pin_memory()
     pin_a = torch.empty((nrhs, max(1, nb)), dtype=torch.float64).pin_memory()
+
+    def pinned(a):
+        """A page-locked host copy of an array (made outside the timed region)."""
+        if a is None:
+            return None
+        return torch.from_numpy(np.ascontiguousarray(a, np.float64)).pin_memory().numpy()
+
+    # the geometry inputs, page-locked like the right-hand sides (the library
+    # uploads them once per factorization; both legs time that copy)
+    pin_geo = [pinned(prob.points), pinned(prob.normals), pinned(prob.weights),
+               pinned(prob.curvatures)]
     barrier = rep.barrier
 
     def form(precision):
@@ -329,7 +340,7 @@ def main():
 
         def step_device():
             t0 = time.perf_counter()
-            fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, **kw)
+            fac = pkg.Factor(*pin_geo, **kw)
             t1 = time.perf_counter()
             fac.set_profiling(True)   # CUDA events around the solve's launch groups
             if refine:
@@ -344,7 +355,7 @@ def main():
             return fac
 
         def step_host():
-            fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, **kw)
+            fac = pkg.Factor(*pin_geo, **kw)
             lib = pkg.load_library()
             if refine:
                 info = pkg._RefineInfo()
