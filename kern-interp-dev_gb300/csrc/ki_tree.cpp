@@ -57,24 +57,19 @@ void check_args(int dim, int n_points, int max_leaf_dofs) {
 }
 
 // Child ci of box b (centre exactly as QuadTree::node_subdivide,
-// quadtree.cpp:377-388) written into the list's slot id.
-void set_child(std::vector<Box>* boxes, int b, int ci, int id, int level, int dim, int count) {
-  Box& par = (*boxes)[b];
-  Box& ch = (*boxes)[id];
+// quadtree.cpp:377-388), appended to the box list.
+int add_child(std::vector<Box>* boxes, int b, int ci, int level, int dim, int count) {
+  const Box& par = (*boxes)[b];
+  Box ch;
   ch.level = level;
   ch.parent = b;
   for (int d = 0; d < dim; d++)
     ch.c[d] = par.c[d] + ((ci >> (dim - 1 - d)) & 1 ? par.side / 4. : -par.side / 4.);
   ch.side = par.side / 2.0;
   ch.orig_count = count;
-  par.child[ci] = id;
-}
-
-// The same child appended to the box list.
-int add_child(std::vector<Box>* boxes, int b, int ci, int level, int dim, int count) {
   const int id = (int)boxes->size();
-  boxes->emplace_back();
-  set_child(boxes, b, ci, id, level, dim, count);
+  boxes->push_back(ch);
+  (*boxes)[b].child[ci] = id;
   return id;
 }
 
@@ -197,30 +192,19 @@ bool Tree::build_from_codes(int n_points_, int dim_, int sol_dim_, int max_leaf_
       levels.clear();
       return false;
     }
-    // the children, numbered as the serial construction numbers them (parents
-    // in level order, children in child order), filled in parallel
-    std::vector<int> split;   // positions in lv of the boxes that split
-    for (size_t i = 0; i < lv.size(); i++)
-      if (starts[i * (nch + 1)] >= 0) split.push_back((int)i);
-    const int base = (int)boxes.size(), nnew = (int)split.size() * nch;
-    boxes.resize((size_t)base + nnew);
-    range.resize((size_t)base + nnew);
-    std::vector<int> next((size_t)nnew);
-    parallel_ranges((int)split.size(), [&](int s0, int s1) {
-      for (int si = s0; si < s1; si++) {
-        const int i = split[si], b = lv[i];
-        const int* st = starts.data() + (size_t)i * (nch + 1);
-        Box& par = boxes[b];
-        par.leaf = false;
-        for (int ci = 0; ci < nch; ci++) {
-          const int id = base + si * nch + ci;
-          set_child(&boxes, b, ci, id, (int)l + 1, dim, (st[ci + 1] - st[ci]) * sol_dim);
-          range[id] = {st[ci], st[ci + 1]};
-          next[(size_t)si * nch + ci] = id;
-        }
+    std::vector<int> next;
+    for (size_t i = 0; i < lv.size(); i++) {
+      const int* st = starts.data() + i * (nch + 1);
+      if (st[0] < 0) continue;
+      const int b = lv[i];
+      boxes[b].leaf = false;
+      for (int ci = 0; ci < nch; ci++) {
+        const int id = add_child(&boxes, b, ci, (int)l + 1, dim, (st[ci + 1] - st[ci]) * sol_dim);
+        range.push_back({st[ci], st[ci + 1]});
+        next.push_back(id);
       }
-    }, 1024);
-    if (!next.empty()) levels.push_back(std::move(next));
+    }
+    if (!next.empty()) levels.push_back(next);
   }
   // a leaf's points ascending by index (the codes ordered them by deeper digits)
   std::vector<int> work(order, order + n_points);
@@ -251,9 +235,7 @@ void Tree::finish(const std::vector<int>& work, const std::vector<std::pair<int,
   // Levels in depth-first order (children of consecutive parents stay
   // consecutive, matching the BFS construction above), positions.
   for (auto& lv : levels)
-    parallel_ranges((int)lv.size(), [&](int i0, int i1) {
-      for (int i = i0; i < i1; i++) boxes[lv[i]].level_pos = i;
-    });
+    for (size_t i = 0; i < lv.size(); i++) boxes[lv[i]].level_pos = (int)i;
 
   // Neighbours (quadtree.cpp:192-237): same-level neighbours come from the
   // parent's same-level neighbours' children (centre distance below
