@@ -480,7 +480,9 @@ __device__ int cta_gj_inverse(int n, T* A, int lda, int* piv, T* colj, T* s_val,
 // columns permuted, X^-1(j, m) = A(p_j, c) with p_c = m, which the final store
 // undoes.  Two barriers per column.  Requires n <= 32 MA and n <= W MAXB;
 // scratch: 3n of T and 2n ints (shared).  piv[j] = p_j (device memory).
-// Returns the first zero pivot + 1, or 0.
+// Returns the first zero pivot + 1, or 0.  Not inlined, so that the register
+// tile does not compete with the calling kernel's live values (inlined into
+// the 64-register Schur kernel it spilled about twice as much).
 template <typename T, int MA, int MAXB>
 __device__ __noinline__ int cta_gj_inverse_reg(int n, T* A, int lda, int* piv, T* scratch) {
   T* colbuf = scratch;                   // [2][n]: column j (double-buffered)
