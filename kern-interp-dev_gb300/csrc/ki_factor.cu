@@ -2242,22 +2242,39 @@ void launch_sweep(Factorization<T>& F, int l, int mode, T* x, int ncols, cudaStr
   KI_CUDA(cudaGetLastError());
 }
 
-// out (na x nc, column-major) = sum over non-skeleton rows of A(i,:)^T B(i,:)
+// Temporaries of one solve (or of the border set-up): taken from the
+// library's stream-ordered pool and released, in stream order, when the
+// Scratch goes out of scope; or carved from a caller's arena (the
+// no-allocation solve), which releases nothing.
 template <typename T>
-void reduce_rows(Factorization<T>& F, const T* A, int na, const T* B, int nc, T* out,
-                 cudaStream_t s) {
-  int parts = (F.N + kRedRows - 1) / kRedRows;
-  T* partial = nullptr;
-  KI_CUDA(pool_malloc((void**)&partial, sizeof(T) * (size_t)parts * na * nc + 16, s));
-  if (na * nc > 16 * 256) throw std::runtime_error("border too wide for the row reduction");
-  size_t sm = sizeof(T) * 32 * (size_t)(na + nc);
-  if (sm > 48 * 1024)
-    KI_CUDA(cudaFuncSetAttribute(k_reduce_partial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  ki::launch(k_reduce_partial<T>, parts, 256, sm, s, A, na, B, nc, F.N, F.d_is_skel, partial);
-  ki::launch(k_reduce_final<T>, std::max(1, (na * nc + 255) / 256), 256, 0, s, partial, parts, na * nc, out);
-  KI_CUDA(cudaGetLastError());
-  KI_CUDA(cudaFreeAsync(partial, s));
-}
+class Scratch {
+ public:
+  explicit Scratch(cudaStream_t s, ScratchArena* arena = nullptr) : s_(s), arena_(arena) {}
+  Scratch(const Scratch&) = delete;
+  Scratch& operator=(const Scratch&) = delete;
+  ~Scratch() {
+    for (void* p : owned_) cudaFreeAsync(p, s_);
+  }
+  // Bytes one take(elems) consumes at most, alignment included.
+  static size_t footprint(size_t elems) { return ((bytes(elems) + 255) & ~size_t(255)) + 256; }
+  T* take(size_t elems) {
+    if (arena_) {
+      void* p = arena_->take(bytes(elems));
+      if (!p) throw std::invalid_argument("scratch arena too small for this solve");
+      return static_cast<T*>(p);
+    }
+    void* p = nullptr;
+    KI_CUDA(pool_malloc(&p, bytes(elems), s_));
+    owned_.push_back(p);
+    return static_cast<T*>(p);
+  }
+
+ private:
+  static size_t bytes(size_t elems) { return sizeof(T) * elems + 16; }
+  cudaStream_t s_;
+  ScratchArena* arena_;
+  std::vector<void*> owned_;
+};
 
 // Rows of a DOF-major N x nc array whose flag is set are zeroed.
 template <typename T>
@@ -2267,25 +2284,50 @@ __global__ void k_zero_rows(T* X, int nc, const unsigned char* mask, int N) {
     if (mask[e / nc]) X[e] = T(0);
 }
 
-// out (na x nc) = sum over non-skeleton rows of A(i,:)^T B(i,:) for wide
-// borders: B's skeleton rows are zeroed in place (B is always a temporary),
-// then a split-K GEMM over row chunks and a fixed-order sum of the slices.
+// k_reduce_partial stages 32 rows of both operands in shared memory and
+// keeps na x nc accumulators per block: borders up to 4,096 products use
+// it, wider ones the split-K GEMM.
+constexpr int kRedWideChunk = 16384;
+inline bool reduce_is_narrow(int na, int nc) { return (long)na * nc <= 16 * 256; }
+
+// Elements of the partial-sum buffer reduce_rows takes for (na, nc).
+inline size_t reduce_rows_elems(int N, int na, int nc) {
+  const int chunk = reduce_is_narrow(na, nc) ? kRedRows : kRedWideChunk;
+  return (size_t)((N + chunk - 1) / chunk) * na * nc;
+}
+
+// out (na x nc, column-major) = sum over non-skeleton rows i of
+// A(i,:)^T B(i,:), A and B DOF-major (N x na, N x nc).  Narrow borders: one
+// block per 1,024 rows, then a fixed-order sum of the blocks' partials.
+// Wide borders: B's skeleton rows are zeroed in place (B must be a
+// temporary), then a split-K GEMM over 16,384-row chunks and a fixed-order
+// sum of the slices.
 template <typename T>
-void reduce_rows_wide(Factorization<T>& F, const T* A, int na, T* B, int nc, T* out,
-                      cudaStream_t s) {
+void reduce_rows(Factorization<T>& F, const T* A, int na, T* B, int nc, T* out, Scratch<T>& sc,
+                 cudaStream_t s) {
   const int N = F.N;
-  ki::launch(k_zero_rows<T>, std::min(8192, (int)(((size_t)N * nc + 255) / 256)), 256, 0, s, B, nc, F.d_is_skel, N);
-  const int chunk = 16384;
-  const int parts = (N + chunk - 1) / chunk;
-  T* partial = nullptr;
-  KI_CUDA(pool_malloc((void**)&partial, sizeof(T) * (size_t)parts * na * nc + 16, s));
+  T* partial = sc.take(reduce_rows_elems(N, na, nc));
+  if (reduce_is_narrow(na, nc)) {
+    const int parts = (N + kRedRows - 1) / kRedRows;
+    size_t sm = sizeof(T) * 32 * (size_t)(na + nc);
+    if (sm > 48 * 1024)
+      KI_CUDA(cudaFuncSetAttribute(k_reduce_partial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    ki::launch(k_reduce_partial<T>, parts, 256, sm, s, A, na, (const T*)B, nc, N, F.d_is_skel, partial);
+    ki::launch(k_reduce_final<T>, std::max(1, (na * nc + 255) / 256), 256, 0, s, (const T*)partial, parts,
+               na * nc, out);
+    KI_CUDA(cudaGetLastError());
+    return;
+  }
+  ki::launch(k_zero_rows<T>, std::min(8192, (int)(((size_t)N * nc + 255) / 256)), 256, 0, s, B, nc,
+             (const unsigned char*)F.d_is_skel, N);
+  const int parts = (N + kRedWideChunk - 1) / kRedWideChunk;
   // DOF-major A is the column-major na x N matrix Ac; out = Ac * Bc^T
   dim3 g((na + 63) / 64, (nc + 63) / 64, parts);
-  ki::launch(k_gemm<T>, g, 256, 0, s, na, nc, N, T(1), A, na, 0, B, nc, 1, T(0), partial, na, chunk,
-                              (int64_t)chunk * na, (int64_t)chunk * nc, (int64_t)na * nc);
-  ki::launch(k_reduce_final<T>, std::max(1, (na * nc + 255) / 256), 256, 0, s, partial, parts, na * nc, out);
+  ki::launch(k_gemm<T>, g, 256, 0, s, na, nc, N, T(1), A, na, 0, (const T*)B, nc, 1, T(0), partial, na,
+             kRedWideChunk, (int64_t)kRedWideChunk * na, (int64_t)kRedWideChunk * nc, (int64_t)na * nc);
+  ki::launch(k_reduce_final<T>, std::max(1, (na * nc + 255) / 256), 256, 0, s, (const T*)partial, parts,
+             na * nc, out);
   KI_CUDA(cudaGetLastError());
-  KI_CUDA(cudaFreeAsync(partial, s));
 }
 
 template <typename T>
@@ -3037,6 +3079,10 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       F->n_redundant += r;
       LF.max_n = std::max(LF.max_n, n);
       LF.max_mat = std::max(LF.max_mat, std::max(r * r, k * r));
+      LF.sum_kr += (double)k * r;
+      LF.sum_r2 += (double)r * r;
+      LF.sum_n += n;
+      LF.sum_r += r;
     }
     if (sizeof(T) < sizeof(double)) {
       // FP32: explicit inverses of the redundant blocks for the sweeps (the
@@ -3262,19 +3308,19 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         }
         F->join(2);
         F->stage_end();
-        T* dD = nullptr;
-        KI_CUDA(pool_malloc((void**)&dD, Tsz * (size_t)N * nb, s));
-        KI_CUDA(cudaMemcpyAsync(dD, F->d_Umod, Tsz * (size_t)N * nb, cudaMemcpyDeviceToDevice, s));
-        F->stage_begin("border_Dinv", 0, 0);
-        launch_diag_all<T>(*F, dD, nb, s);
-        F->stage_end();
         T* corr = (T*)F->alloc(Tsz * (size_t)nb * nb);
-        F->stage_begin("border_corr", 0, 0);
-        if (nb * nb <= 16 * 256) reduce_rows<T>(*F, F->d_PsiTmod, nb, dD, nb, corr, s);
-        else reduce_rows_wide<T>(*F, F->d_PsiTmod, nb, dD, nb, corr, s);
-        F->stage_end();
-        F->stage_end();
-        KI_CUDA(cudaFreeAsync(dD, s));
+        {
+          Scratch<T> sc(s);
+          T* dD = sc.take((size_t)N * nb);
+          KI_CUDA(cudaMemcpyAsync(dD, F->d_Umod, Tsz * (size_t)N * nb, cudaMemcpyDeviceToDevice, s));
+          F->stage_begin("border_Dinv", 0, 0);
+          launch_diag_all<T>(*F, dD, nb, s);
+          F->stage_end();
+          F->stage_begin("border_corr", 0, 0);
+          reduce_rows<T>(*F, F->d_PsiTmod, nb, dD, nb, corr, sc, s);
+          F->stage_end();
+          F->stage_end();
+        }
         const int ns = h.n + nb;
         T* S = (T*)F->alloc(Tsz * (size_t)ns * ns);
         ki::launch(k_assemble_S<T>, std::min(4096, (int)(((size_t)ns * ns + 255) / 256)), 256, 0, s,
@@ -3301,59 +3347,90 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
   return F;
 }
 
+// The factorization's solve (SkelFactorization::solve,
+// skel_factorization.cpp:595-778, and multiply_connected_solve, :781-1141),
+// every right-hand-side column at once, on F.stream.  Temporaries come from
+// `sc`; `prof` brackets the launch groups with profiling events.
 template <typename T>
-void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, const T* d_g) {
+static void solve_core(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, const T* d_g,
+                       Scratch<T>& sc, bool prof) {
   cudaStream_t s = F.stream;
   const int L = (int)F.levels.size();
   const int nr = F.n_root;
-  const bool prof = F.profile_solve;
-  auto sb = [&](const char* name) { if (prof) F.stage_begin(name, 0, 0); };
+  auto sb = [&](const char* name, double flops = 0, double bytes = 0) {
+    if (prof) F.stage_begin(name, flops, bytes);
+  };
   auto se = [&]() { if (prof) F.stage_end(); };
+  // Algorithmic work of the sweeps over levels [l0, l1): per box the two
+  // k x r factor matrices (T and L up, U and T down) and, with the diagonal
+  // solve, the r x r inverse or LU, each read once; the box's n rows of the
+  // ncols right-hand sides read and written (plus their indices); flops
+  // 4kr (+ 2r^2) per column.
+  const double sv = sizeof(T);
+  auto sweep_work = [&](int l0, int l1, bool diag, double* flops, double* bytes) {
+    double kr = 0, r2 = 0, n = 0;
+    for (int l = std::max(1, l0); l < l1; l++) {
+      kr += F.levels[l].sum_kr;
+      r2 += F.levels[l].sum_r2;
+      n += F.levels[l].sum_n;
+    }
+    *flops = (4 * kr + (diag ? 2 * r2 : 0)) * ncols;
+    *bytes = sv * (2 * kr + (diag ? r2 : 0)) + sv * 2 * n * ncols + 4 * n;
+  };
+  auto sb_sweep = [&](const char* name, int l0, int l1, bool diag) {
+    if (!prof) return;
+    double fl, by;
+    sweep_work(l0, l1, diag, &fl, &by);
+    F.stage_begin(name, fl, by);
+  };
+  // the diagonal solves alone: the r x r matrices and the redundant rows
+  auto sb_diag = [&](const char* name) {
+    if (!prof) return;
+    double r2 = 0, red = 0;
+    for (int l = 1; l < L; l++) {
+      r2 += F.levels[l].sum_r2;
+      red += F.levels[l].sum_r;
+    }
+    F.stage_begin(name, 2 * r2 * ncols, sv * r2 + sv * 2 * red * ncols + 4 * red);
+  };
   if (F.n_border == 0) {
-    // SkelFactorization::solve (skel_factorization.cpp:595-778); the diagonal
-    // solves are fused into the upward pass (each box's redundant rows are
-    // final once its level has been swept).
+    // the diagonal solves are fused into the upward pass (each box's
+    // redundant rows are final once its level has been swept)
     for (int l = L - 1; l >= 1; l--) {
-      sb("sweep_up");
+      sb_sweep("sweep_up", l, l + 1, true);
       launch_sweep<T>(F, l, kUpDiag, d_x, ncols, s);
       se();
     }
     if (nr > 0) {
       sb("root_solve");
-      T* ws = nullptr;
-      KI_CUDA(pool_malloc((void**)&ws, sizeof(T) * (size_t)nr * ncols + 16, s));
+      T* ws = sc.take((size_t)nr * ncols);
       int gb = std::max(1, std::min(4096, (nr * ncols + 255) / 256));
       ki::launch(k_gather_rows<T>, gb, 256, 0, s, d_x, ncols, F.d_root_idx, nr, ncols, ws);
       dense_lu_solve<T>(F.d_root_lu, nr, F.d_root_piv, ws, nr, ncols, false, s);
       ki::launch(k_scatter_rows<T>, gb, 256, 0, s, d_x, ncols, F.d_root_idx, nr, ncols, ws);
       se();
       KI_CUDA(cudaGetLastError());
-      KI_CUDA(cudaFreeAsync(ws, s));
     }
     for (int l = 1; l < L; l++) {
-      sb("sweep_down");
+      sb_sweep("sweep_down", l, l + 1, false);
       launch_sweep<T>(F, l, kDown, d_x, ncols, s);
       se();
     }
     return;
   }
-  // SkelFactorization::multiply_connected_solve (skel_factorization.cpp:781-1141),
-  // every column at once.
   const int nb = F.n_border, ns = nr + nb, N = F.N;
-  sb("sweep_up");
+  sb_sweep("sweep_up", 1, L, false);
   for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kUp, d_x, ncols, s);
   se();
-  sb("border_diag");
-  T *Dw = nullptr, *t = nullptr, *M = nullptr;
-  KI_CUDA(pool_malloc((void**)&Dw, sizeof(T) * (size_t)N * ncols + 16, s));
-  KI_CUDA(pool_malloc((void**)&t, sizeof(T) * (size_t)nb * ncols + 16, s));
-  KI_CUDA(pool_malloc((void**)&M, sizeof(T) * (size_t)ns * ncols + 16, s));
+  sb_diag("border_diag");
+  T* Dw = sc.take((size_t)N * ncols);
+  T* t = sc.take((size_t)nb * ncols);
+  T* M = sc.take((size_t)ns * ncols);
   KI_CUDA(cudaMemcpyAsync(Dw, d_x, sizeof(T) * (size_t)N * ncols, cudaMemcpyDeviceToDevice, s));
   launch_diag_all<T>(F, Dw, ncols, s);
   se();
   sb("border_reduce");
-  if (nb * ncols <= 16 * 256) reduce_rows<T>(F, F.d_PsiTmod, nb, Dw, ncols, t, s);   // Psi~_r D^-1 w
-  else reduce_rows_wide<T>(F, F.d_PsiTmod, nb, Dw, ncols, t, s);
+  reduce_rows<T>(F, F.d_PsiTmod, nb, Dw, ncols, t, sc, s);   // Psi~_r D^-1 w
   se();
   sb("border_root");
   ki::launch(k_mc_rhs<T>, std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s,
@@ -3370,89 +3447,49 @@ void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, const T* d
   }
   KI_CUDA(cudaGetLastError());
   se();
-  sb("border_diag");
+  sb_diag("border_diag");
   launch_diag_all<T>(F, d_x, ncols, s);
   se();
   ki::launch(k_mc_finish<T>, std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s,
       d_x, ncols, F.d_root_idx, M, nr, nb, d_alpha);
   KI_CUDA(cudaGetLastError());
-  sb("sweep_down");
+  sb_sweep("sweep_down", 1, L, false);
   for (int l = 1; l < L; l++) launch_sweep<T>(F, l, kDown, d_x, ncols, s);
   se();
-  KI_CUDA(cudaFreeAsync(Dw, s));
-  KI_CUDA(cudaFreeAsync(t, s));
-  KI_CUDA(cudaFreeAsync(M, s));
+}
+
+template <typename T>
+void solve_device(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, const T* d_g) {
+  Scratch<T> sc(F.stream);
+  solve_core<T>(F, d_x, ncols, d_alpha, d_g, sc, F.profile_solve);
 }
 
 // ---------------------------------------------------- arena-backed solve --
-// The solve of solve_device with its temporaries carved from a caller-owned
-// buffer instead of the stream-ordered allocator; the arithmetic and launch
-// sequence are the same.
+// solve_device with every temporary carved from a caller-owned buffer: the
+// same launch sequence (and so the same results), no allocation, no
+// profiling events.
 template <typename T>
 size_t solve_arena_bytes(const Factorization<T>& F, int ncols) {
-  auto piece = [](size_t b) { return ((b + 255) & ~size_t(255)) + 256; };
   const size_t nr = F.n_root, nb = F.n_border, N = F.N, nc = ncols;
-  if (nb == 0) return piece(sizeof(T) * nr * nc);
-  const size_t parts = (N + kRedRows - 1) / kRedRows;
-  return piece(sizeof(T) * N * nc) + piece(sizeof(T) * nb * nc) + piece(sizeof(T) * (nr + nb) * nc) +
-         piece(sizeof(T) * parts * nb * nc);
-}
-
-template <typename T>
-static void reduce_rows_arena(Factorization<T>& F, const T* A, int na, const T* B, int nc, T* out,
-                              T* partial, cudaStream_t s) {
-  int parts = (F.N + kRedRows - 1) / kRedRows;
-  if (na * nc > 16 * 256) throw std::runtime_error("border too wide for the row reduction");
-  size_t sm = sizeof(T) * 32 * (size_t)(na + nc);
-  if (sm > 48 * 1024)
-    KI_CUDA(cudaFuncSetAttribute(k_reduce_partial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  ki::launch(k_reduce_partial<T>, parts, 256, sm, s, A, na, B, nc, F.N, F.d_is_skel, partial);
-  ki::launch(k_reduce_final<T>, std::max(1, (na * nc + 255) / 256), 256, 0, s, partial, parts, na * nc, out);
-  KI_CUDA(cudaGetLastError());
+  if (nb == 0) return nr ? Scratch<T>::footprint(nr * nc) : 0;
+  return Scratch<T>::footprint(N * nc) + Scratch<T>::footprint(nb * nc) +
+         Scratch<T>::footprint((nr + nb) * nc) +
+         Scratch<T>::footprint(reduce_rows_elems(F.N, F.n_border, ncols));
 }
 
 template <typename T>
 void solve_device_arena(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, ScratchArena& arena,
                         cudaStream_t s) {
-  const int L = (int)F.levels.size();
-  const int nr = F.n_root;
-  auto take = [&](size_t bytes) {
-    void* p = arena.take(bytes);
-    if (!p) throw std::invalid_argument("scratch arena too small for this solve");
-    return (T*)p;
-  };
-  if (F.n_border == 0) {
-    for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kUpDiag, d_x, ncols, s);
-    if (nr > 0) {
-      T* ws = take(sizeof(T) * (size_t)nr * ncols);
-      int gb = std::max(1, std::min(4096, (nr * ncols + 255) / 256));
-      ki::launch(k_gather_rows<T>, gb, 256, 0, s, d_x, ncols, F.d_root_idx, nr, ncols, ws);
-      dense_lu_solve<T>(F.d_root_lu, nr, F.d_root_piv, ws, nr, ncols, false, s);
-      ki::launch(k_scatter_rows<T>, gb, 256, 0, s, d_x, ncols, F.d_root_idx, nr, ncols, ws);
-      KI_CUDA(cudaGetLastError());
-    }
-    for (int l = 1; l < L; l++) launch_sweep<T>(F, l, kDown, d_x, ncols, s);
-    return;
+  cudaStream_t saved = F.stream;
+  F.stream = s;
+  try {
+    Scratch<T> sc(s, &arena);
+    solve_core<T>(F, d_x, ncols, d_alpha, nullptr, sc, false);
+  } catch (...) {
+    F.stream = saved;
+    throw;
   }
-  const int nb = F.n_border, ns = nr + nb, N = F.N;
-  T* Dw = take(sizeof(T) * (size_t)N * ncols);
-  T* t = take(sizeof(T) * (size_t)nb * ncols);
-  T* M = take(sizeof(T) * (size_t)ns * ncols);
-  T* partial = take(sizeof(T) * (size_t)((N + kRedRows - 1) / kRedRows) * nb * ncols);
-  for (int l = L - 1; l >= 1; l--) launch_sweep<T>(F, l, kUp, d_x, ncols, s);
-  KI_CUDA(cudaMemcpyAsync(Dw, d_x, sizeof(T) * (size_t)N * ncols, cudaMemcpyDeviceToDevice, s));
-  launch_diag_all<T>(F, Dw, ncols, s);
-  reduce_rows_arena<T>(F, F.d_PsiTmod, nb, Dw, ncols, t, partial, s);
-  ki::launch(k_mc_rhs<T>, std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s,
-      d_x, ncols, F.d_root_idx, nr, t, nb, ncols, M, (const T*)nullptr);
-  dense_lu_solve<T>(F.d_root_lu, ns, F.d_root_piv, M, ns, ncols, false, s);
-  mc_update<T>(d_x, ncols, F.d_Umod, nb, M, nr, N, F.d_is_skel, s);
-  KI_CUDA(cudaGetLastError());
-  launch_diag_all<T>(F, d_x, ncols, s);
-  ki::launch(k_mc_finish<T>, std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s,
-      d_x, ncols, F.d_root_idx, M, nr, nb, d_alpha);
-  KI_CUDA(cudaGetLastError());
-  for (int l = 1; l < L; l++) launch_sweep<T>(F, l, kDown, d_x, ncols, s);
+  F.stream = saved;
 }
 
 template size_t solve_arena_bytes<double>(const Factorization<double>&, int);

@@ -40,6 +40,7 @@ struct LevelFactor {
   void* d_tasks = nullptr; // device array of per-box sweep descriptors
   int max_n = 0;           // largest active set among them
   int max_mat = 0;         // largest factor matrix among them: max(r^2, k r) entries
+  double sum_kr = 0, sum_r2 = 0, sum_n = 0, sum_r = 0;   // over the compressed boxes (sweep work)
 };
 
 // Device-time record of one launch group (CUDA events on the factor's stream).
