@@ -2,21 +2,26 @@
 
 Workload (default): 2D Laplace Dirichlet double-layer BIE on the disc of
 radius 2 minus 64 ellipses (semi-axes U(0.02, 0.06), seed 1), 16-node
-Gauss-Legendre panels, 1,048,576 unknowns, ID tolerance 1e-8, 32 right-hand
-sides from unit point sources at |y| in [2.5, 4] (seed 2).  One step = one
-factorization (tree + skeletonization + bordered system) and one solve of all
-32 right-hand sides.  Metric: DOF/s = unknowns x right-hand sides / step time.
+Gauss-Legendre panels, 1,048,576 unknowns, 32 right-hand sides from unit point
+sources at |y| in [2.5, 4] (seed 2).  One step = one factorization (tree +
+skeletonization + bordered system) and one solve of all 32 right-hand sides
+to a 1e-8 relative residual.  Metric: DOF/s = unknowns x right-hand sides /
+step time.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--precision fp64|fp32] [--unknowns N] [--nrhs R] [--tol T]
+                  [--precision mixed|fp64|fp32] [--unknowns N] [--nrhs R]
 
-`value` is timed with the right-hand sides resident in HBM (ki_solve_device);
-`e2e` through the host-buffer C-ABI call (ki_solve), host<->device copies of
-the right-hand sides and solutions inside the timed region.  --impl reference
-times the CPU oracle (a C++ restatement of the reference's factor and solve,
-linked to OpenBLAS) on the host cores.  With N > 1 (torchrun) every rank
-factors and solves its own copy of the problem (replicas; the path has no
-exchange step), rank 0 prints the line.
+`value` is timed with the right-hand sides resident in HBM
+(ki_solve_refined_device); `e2e` through the host-buffer C-ABI call
+(ki_solve_refined), host<->device copies of the geometry, right-hand sides
+and solutions inside the timed region.  --impl reference times the CPU
+reference path (the oracle port: a C++ restatement of the reference's factor
+and solve, linked to OpenBLAS) on all host cores, at the ID tolerance at
+which its plain solve reaches the same residual (target / 10), and reports
+the residual it reached.  The GPU arm also compares its solutions with that
+CPU path on the same nodes and right-hand sides (`parity`).  With N > 1
+(torchrun) every rank factors and solves its own copy of the problem
+(replicas; the path has no exchange step), rank 0 prints the line.
 """
 import argparse
 import json
@@ -50,8 +55,8 @@ def parse():
                     help="mixed: do not also time the FP64 form at the same residual")
     ap.add_argument("--learned-rank", default="on", choices=["on", "off"],
                     help="mixed: size sketched IDs with the shipped rank predictor")
-    ap.add_argument("--compare-learned", action="store_true",
-                    help="mixed: also time the mixed form without the rank predictor")
+    ap.add_argument("--no-compare-learned", action="store_true",
+                    help="mixed: do not also time the mixed form without the rank predictor")
     ap.add_argument("--workload", default="laplace2d_disc_ellipses",
                     choices=["laplace2d_disc_ellipses", "stokes2d_disc_circles", "laplace2d_star",
                              "laplace3d_ellipsoid"])
@@ -62,6 +67,14 @@ def parse():
     ap.add_argument("--residual-rows", type=int, default=2048)
     ap.add_argument("--cpu-sample-n", type=int, default=1 << 20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-tol", type=float, default=None,
+                    help="ID tolerance of the CPU reference path (default: target / 10, the "
+                         "decade at which its plain solve reaches the target residual)")
+    ap.add_argument("--ref-residual-rows", type=int, default=256,
+                    help="rows of the dense FP64 operator sampled to report the residual the "
+                         "CPU reference path reaches")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the solution comparison against the CPU reference path")
     return ap.parse_args()
 
 
@@ -241,8 +254,35 @@ def cpu_oracle_run(prob, rhs, tol, threads, **kw):
     return t1 - t0, st, mu, alpha
 
 
+def metric_name(target):
+    """The metric string both arms print (the driver pairs them by it)."""
+    return "factor+solve DOF/s (unknowns x rhs / s) at %g relative residual" % target
+
+
+def ref_tol(args):
+    return args.ref_tol if args.ref_tol is not None else args.target / 10
+
+
+def oracle_residual(wl, mu, alpha, nrows, threads, seed=9):
+    """Relative residual ||[K U; Psi -I][mu; alpha] - [f; 0]|| / ||f|| of a
+    CPU solution, estimated from `nrows` uniformly sampled rows of the dense
+    FP64 operator (the border rows are computed in full); max and median over
+    the right-hand sides."""
+    import oracle
+    N = wl.n
+    rng = np.random.default_rng(seed)
+    rows = np.sort(rng.choice(N, size=min(nrows, N), replace=False))
+    res, res_b = oracle.residual_rows(wl.prob, mu, alpha, wl.rhs, rows, solution_dim=wl.sol_dim,
+                                      threads=threads)
+    sq = N / rows.size * (res ** 2).sum(0) + (res_b ** 2).sum(0)
+    est = np.sqrt(sq) / np.linalg.norm(wl.rhs, axis=0)
+    return float(est.max()), float(np.median(est))
+
+
 def run_reference(args, rank, world):
-    """CPU arm: the oracle port on the host cores (all threads)."""
+    """CPU arm: the reference's factor-and-solve restated in C++ (the oracle
+    port: same tree, same LAPACK calls), on all host cores, at the ID
+    tolerance at which its plain solve reaches the metric's residual."""
     import __graft_entry__ as g
     pkg = g.load_package()
     if rank != 0:
@@ -250,32 +290,102 @@ def run_reference(args, rank, world):
     import oracle
     oracle.build_port()
     threads = os.cpu_count() or 1
+    tol = ref_tol(args)
     n = min(args.n, args.cpu_sample_n)
     wl = Workload(pkg, args.workload, n, args.holes, args.nrhs)
     n = wl.n
-    for _ in range(max(0, min(args.warmup, 1))):
-        cpu_oracle_run(wl.prob, wl.rhs, args.tol, threads, **wl.oracle_kw())
+    for _ in range(max(0, args.warmup)):
+        cpu_oracle_run(wl.prob, wl.rhs, tol, threads, **wl.oracle_kw())
     times = []
+    mu = alpha = None
     for _ in range(args.steps):
-        dt, st, _, _ = cpu_oracle_run(wl.prob, wl.rhs, args.tol, threads, **wl.oracle_kw())
+        dt, st, mu, alpha = cpu_oracle_run(wl.prob, wl.rhs, tol, threads, **wl.oracle_kw())
         times.append(dt)
     t = float(np.mean(times))
     value = n * args.nrhs / t
+    # the residual the timed solutions reach (outside the timed region)
+    rmax, rmed = oracle_residual(wl, mu, alpha, args.ref_residual_rows, threads)
     line = {
-        "metric": "factor+solve DOF/s (unknowns x rhs / s) at ID tol %g" % args.tol,
-        "value": value, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
+        "metric": metric_name(args.target),
+        "value": value, "unit": "DOF/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "impl": "reference",
         "config": {"workload": args.workload, "holes": args.holes,
-                   "unknowns": n, "nrhs": args.nrhs, "id_tol": args.tol,
-                   "full_workload_unknowns": args.n},
+                   "unknowns": n, "nrhs": args.nrhs, "id_tol": tol,
+                   "target_residual": args.target,
+                   "residual_reached_max": rmax, "residual_reached_median": rmed,
+                   "residual_rows_sampled": args.ref_residual_rows,
+                   "id_tol_choice": "target / 10: the plain FP64 factor+solve at ID tol 1e-8 "
+                                    "leaves a ~6e-8 residual on this workload, at 1e-9 ~3e-9",
+                   "full_workload_unknowns": args.n, "ranks_launched": world,
+                   "ranks_working": 1},
         "cpu_baseline": {"value": value, "unit": "DOF/s", "cores": threads, "kind": "port",
                          "sample": "%d unknowns (the full workload's geometry at this size), "
-                                   "%d rhs, factor+solve per step" % (n, args.nrhs)},
+                                   "%d rhs, factor+solve per step, ID tol %g" % (n, args.nrhs, tol)},
         "e2e": {"value": value, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def max_rel_diff(a, b, scale=None):
+    """max over columns of max|a - b| / max|scale| (column-wise relative
+    max-norm; scale defaults to b)."""
+    b = np.asarray(b, np.float64).reshape(b.shape[0], -1)
+    a = np.asarray(a, np.float64).reshape(b.shape)
+    sc = b if scale is None else np.asarray(scale, np.float64).reshape(-1, b.shape[1])
+    den = np.abs(sc).max(0)
+    den[den == 0] = 1.0
+    return float((np.abs(a - b).max(0) / den).max())
+
+
+def parity_check(pkg, args, wl, w2, kw, refine, mu, alpha, pmu, palpha, threads):
+    """Solutions of the GPU forms against the CPU reference path on the same
+    nodes and right-hand sides (w2, the CPU workload: the full workload unless
+    --cpu-sample-n caps it).  Bar: 10 x the ID tolerance of the metric.
+      main_form_vs_reference: the timed form's solution (refined to the target
+        for the mixed / refined forms) against the CPU path at --ref-tol;
+      fp64_plain_vs_reference_same_tol: the plain FP64 GPU factor+solve (the
+        reference's arithmetic) against the CPU path at the same ID tolerance,
+        with both trees' statistics."""
+    p = w2.prob
+    geo = (p.points, p.normals, p.weights, p.curvatures)
+    nb = w2.n_border
+    bar = 10 * args.tol
+    if w2.n != wl.n:
+        fac = pkg.Factor(*geo, **w2.factor_kw(kw["id_tol"], kw["precision"]))
+        if refine:
+            out = fac.solve_refined(w2.rhs, tol=args.target, max_steps=args.max_steps)
+            mu, alpha = out[0], (out[1] if len(out) == 3 else None)
+        else:
+            r = fac.solve(w2.rhs)
+            mu, alpha = r if isinstance(r, tuple) else (r, None)
+        fac.close()
+    res = {"bar": bar, "unknowns": w2.n, "nrhs": w2.rhs.shape[1],
+           "norm": "max over rhs of max|x_gpu - x_ref| / max|x_ref| (alpha: / max|mu_ref|)"}
+    main = {"form": args.precision, "reference_id_tol": ref_tol(args),
+            "max_rel_diff_mu": max_rel_diff(mu, pmu)}
+    if nb:
+        # the border unknowns of exterior-source data vanish analytically
+        # (|alpha| ~ 1e-13): measured on the scale of the density
+        main["max_rel_diff_alpha"] = max_rel_diff(alpha, palpha, scale=pmu)
+    res["main_form_vs_reference"] = main
+    fac = pkg.Factor(*geo, **w2.factor_kw(args.tol, pkg.PRECISION_FP64))
+    r = fac.solve(w2.rhs)
+    gmu, galpha = r if isinstance(r, tuple) else (r, None)
+    gi = fac.info()
+    fac.close()
+    _, st, qmu, qalpha = cpu_oracle_run(w2.prob, w2.rhs, args.tol, threads, **w2.oracle_kw())
+    plain = {"id_tol": args.tol, "max_rel_diff_mu": max_rel_diff(gmu, qmu),
+             "tree_gpu": [gi["n_levels"], gi["n_root"], gi["n_compressed"], gi["n_redundant"]],
+             "tree_reference": [st["levels"], st["root"], st["compressed"], st["redundant"]],
+             "tree_fields": "levels, root skeleton, compressed boxes, redundant DOFs"}
+    if nb:
+        plain["max_rel_diff_alpha"] = max_rel_diff(galpha, qalpha, scale=qmu)
+    res["fp64_plain_vs_reference_same_tol"] = plain
+    diffs = [v for d in (main, plain) for k, v in d.items() if k.startswith("max_rel_diff")]
+    res["pass"] = bool(max(diffs) <= bar)
+    return res
 
 
 def main():
@@ -425,19 +535,22 @@ def main():
     learned = None
     if args.precision == "mixed" and args.learned_rank == "on":
         learned = {"boxes_sketched": info.get("n_sketched"), "fallbacks": info.get("n_fallback")}
-        if args.compare_learned:
-            c = run_form("mixed-plain", max(1, min(args.steps, 2)), 1)
+        if not args.no_compare_learned:
+            c = run_form("mixed-plain", max(1, min(args.steps, 3)), 2)
+            rw = c["infos"][-1] if c["infos"] else {}
             learned.update({"without_predictor_ms_per_step": c["t_dev"] * 1e3,
                             "with_predictor_ms_per_step": t_dev * 1e3,
                             "speedup_from_predictor": c["t_dev"] / t_dev,
-                            "refine_without": c["infos"][-1] if c["infos"] else None})
+                            "residual_without": rw.get("residual")})
     # ---- the FP64 form at the same target residual, for the comparison
     compare = None
     if args.precision == "mixed" and not args.no_compare:
         c = run_form("fp64", max(1, min(args.steps, 3)), 2)
+        rc = c["infos"][-1] if c["infos"] else {}
         compare = {"form": "fp64 factorization at ID tol %g, refined to %g" % (args.tol, args.target),
                    "ms_per_step": c["t_dev"] * 1e3, "value": N * nrhs * world / c["t_dev"],
-                   "unit": "DOF/s", "refine": c["infos"][-1] if c["infos"] else None,
+                   "unit": "DOF/s", "residual_first": rc.get("residual0"),
+                   "residual": rc.get("residual"), "corrections": rc.get("steps"),
                    "speedup_of_mixed": c["t_dev"] / t_dev}
 
     # ---- accuracy of the last solution (sampled dense FP64 residual, analytic field)
@@ -527,21 +640,37 @@ def main():
                 "achieved_definition": kdef,
                 "launches_per_step": a["launches"] / args.steps,
                 "ms_per_step": a["ms"] / args.steps}
+    # the solve's stages against the HBM roofline (algorithmic bytes: factor
+    # matrices read once, right-hand-side rows read and written once)
+    solve_roof = {}
+    for rec in solve_prof:
+        a2 = solve_roof.setdefault(rec["stage"], {"ms": 0.0, "bytes": 0.0, "flops": 0.0,
+                                                  "launches": 0})
+        for q in ("ms", "bytes", "flops", "launches"):
+            a2[q] += rec[q]
+    for k2, v2 in solve_roof.items():
+        gbs = v2["bytes"] / (v2["ms"] / 1e3) / 1e9 if v2["ms"] > 0 and v2["bytes"] > 0 else None
+        v2["achieved_gbs"] = gbs
+        v2["frac_hbm"] = gbs / peaks["hbm_gbs"] if gbs else None
     stage_table = {k: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps,
                        "gflop_per_step": v["flops"] / args.steps / 1e9} for k, v in agg.items()}
     launches = int(round(main_form["launches"]))
 
     cpu = None
+    parity = None
     if not args.no_cpu_baseline:
         try:
             n_cpu = min(args.n, args.cpu_sample_n)
             w2 = Workload(pkg, args.workload, n_cpu, args.holes, nrhs)
             n_cpu = w2.n
             thr = os.cpu_count() or 1
-            dt, st, _, _ = cpu_oracle_run(w2.prob, w2.rhs, args.tol, thr, **w2.oracle_kw())
+            rt = ref_tol(args)
+            dt, st, pmu, palpha = cpu_oracle_run(w2.prob, w2.rhs, rt, thr, **w2.oracle_kw())
             cpu = {"value": n_cpu * nrhs / dt, "unit": "DOF/s", "cores": thr, "kind": "port",
-                   "sample": "%d unknowns of the same geometry family, %d rhs, one factor+solve (%.1f s)"
-                             % (n_cpu, nrhs, dt)}
+                   "sample": "%d unknowns of the same geometry family, %d rhs, one factor+solve at "
+                             "ID tol %g (%.1f s)" % (n_cpu, nrhs, rt, dt)}
+            if not args.no_parity:
+                parity = parity_check(pkg, args, wl, w2, kw, refine, mu, alpha, pmu, palpha, thr)
         except Exception as e:  # reported, not fatal
             cpu = {"value": None, "unit": "DOF/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": "failed: %s" % e}
@@ -549,13 +678,26 @@ def main():
     units = N * nrhs * world
     h2d = N * nrhs * 8 + prob.n * (2 * wl.dim + 2) * 8
     d2h = N * nrhs * 8 + max(1, nb) * nrhs * 8
-    if refine:
-        metric = "factor+solve DOF/s (unknowns x rhs / s) at %g relative residual" % args.target
-    else:
-        metric = "factor+solve DOF/s (unknowns x rhs / s) at ID tol %g" % args.tol
+    metric = (metric_name(args.target) if refine else
+              "factor+solve DOF/s (unknowns x rhs / s) at ID tol %g" % args.tol)
     dtype = {"fp64": "f64", "fp32": "f32",
              "mixed": "f32 factorization and solves, f64 residuals (FMM)"}[args.precision]
     refines = main_form["infos"]
+    config = {"workload": args.workload, "holes": args.holes, "unknowns": N,
+              "description": WORKLOAD_NOTES[args.workload],
+              "nrhs": nrhs, "precision": args.precision,
+              "id_tol": args.mixed_tol if args.precision == "mixed" else args.tol,
+              "target_residual": args.target if refine else None,
+              "leaf": wl.leaf, "proxy": wl.proxy or (128 if wl.dim == 2 else 32),
+              "l2": "factor working set >> 129 MB L2 (no flush needed)",
+              "levels": info["n_levels"], "root_skeleton": info["n_root"],
+              "compressed_boxes": info["n_compressed"]}
+    if args.precision == "mixed":
+        config["id_tol_note"] = ("the FP32 factorization runs at ID tol %g, not %g: FP32 rounding "
+                                 "(2^-24 relative) bounds the tolerance an FP32 ID can honour, and "
+                                 "ki_factor_create refuses FP32 id_tol < 5e-8; the %g residual is "
+                                 "reached by FP64-residual refinement" % (args.mixed_tol, args.tol,
+                                                                          args.target))
     line = {
         "metric": metric,
         "value": units / t_dev, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
@@ -563,21 +705,15 @@ def main():
         "scaling": "weak", "vs_baseline": None,
         "dtype": dtype,
         "data": "synthetic (seeded boundary and sources)",
-        "config": {"workload": args.workload, "holes": args.holes, "unknowns": N,
-                   "description": WORKLOAD_NOTES[args.workload],
-                   "nrhs": nrhs, "precision": args.precision,
-                   "id_tol": args.mixed_tol if args.precision == "mixed" else args.tol,
-                   "target_residual": args.target if refine else None,
-                   "leaf": wl.leaf, "proxy": wl.proxy or (128 if wl.dim == 2 else 32),
-                   "l2": "factor working set >> 129 MB L2 (no flush needed)",
-                   "levels": info["n_levels"], "root_skeleton": info["n_root"],
-                   "compressed_boxes": info["n_compressed"]},
-        "e2e": {"value": units / t_e2e, "unit": "DOF/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e * 1e3},
+        "config": config,
         "gpu_launches": launches,
         "gpu_launches_note": "kernels the library launched per timed step (its launch counter, "
                              "ki_launch_count): tree sort, factorization levels, solves, FMM "
                              "applies, residual norms",
+        "stages": stage_table,
+        "solve_stages": solve_prof,
+        "level_stats": level_stats,
+        "host_wall_ms_per_step": main_form["host"],
         "refinement": {"steps_per_solve": [r["steps"] for r in refines],
                        "residual_first_solve": [r["residual0"] for r in refines],
                        "residual_final": [r["residual"] for r in refines],
@@ -587,16 +723,19 @@ def main():
                                             "updates by the FP32 12-term FMM)"
                        if (wl.dim == 2 and wl.sol_dim == 1 and N >= 4096) else "dense FP64"}
         if refine else None,
-        "fp64_form_same_residual": compare,
-        "learned_rank": learned,
-        "host_wall_ms_per_step": main_form["host"],
         "roofline": roofline,
-        "stages": stage_table,
-        "solve_stages": solve_prof,
-        "level_stats": level_stats,
+        "solve_roofline": {"peak_gbs": peaks["hbm_gbs"], "peak_source": peak_src,
+                           "solves": len([r for r in solve_prof if r["stage"] == "sweep_up"]),
+                           "stages": solve_roof},
+        "e2e": {"value": units / t_e2e, "unit": "DOF/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e * 1e3},
+        # compact summaries last: they stay in the tail of the line
+        "learned_rank": learned,
+        "fp64_form_same_residual": compare,
         "accuracy": {"residual_est_max": rmax, "residual_est_median": rmed,
                      "residual_rows_sampled": args.residual_rows, "pde_rel_err": pde_err,
                      "refined_residual": rinfo["residual"] if rinfo else None},
+        "parity": parity,
         "clocks": main_form["clk"],
         "cpu_baseline": cpu,
     }

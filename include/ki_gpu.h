@@ -56,15 +56,15 @@ typedef enum {
  */
 typedef struct {
   int n_points;              /* boundary nodes */
-  int domain_dimension;      /* 2 */
-  int solution_dimension;    /* 1 (Laplace) or 2 (Stokes) */
+  int domain_dimension;      /* d = 2 (curves) or 3 (surfaces) */
+  int solution_dimension;    /* 1 (Laplace) or d (Stokes: 2 in 2D, 3 in 3D) */
   int pde;                   /* ki_pde */
-  const double* points;      /* 2*n_points, interleaved (x, y) */
-  const double* normals;     /* 2*n_points, interleaved */
+  const double* points;      /* d*n_points, interleaved (x, y[, z]) */
+  const double* normals;     /* d*n_points, interleaved */
   const double* weights;     /* n_points quadrature weights */
-  const double* curvatures;  /* n_points, may be NULL (treated as 0) */
+  const double* curvatures;  /* n_points, may be NULL (treated as 0; unused in 3D) */
   int n_holes;               /* multiply connected: number of holes */
-  const double* hole_centers;    /* 2*n_holes */
+  const double* hole_centers;    /* d*n_holes */
   const int* hole_node_start;    /* first node of each hole */
   const int* hole_node_count;    /* nodes of each hole */
   int max_leaf_dofs;

@@ -158,3 +158,43 @@ def laplace_forward(prob, targets, mu):
     r2 = (d ** 2).sum(-1)
     K = -prob.weights[None] / (2 * np.pi) * rn / r2
     return K @ mu
+
+
+def residual_rows(prob, mu, alpha, rhs, rows, solution_dim=1, threads=None):
+    """Rows of the bordered system's residual, computed with the port's FP64
+    kernel entries: returns (res (len(rows), nrhs), res_border (n_border,
+    nrhs)) with res = K[rows] mu + U[rows] alpha - f[rows] and res_border =
+    Psi mu - alpha.  O(len(rows) * N) work (plus O(N^2) for a 3D diagonal)."""
+    lib = ctypes.CDLL(build_port())
+    dim = int(np.asarray(prob.points).shape[1])
+    N = prob.n * solution_dim
+    mu = np.asfortranarray(np.asarray(mu, np.float64).reshape(N, -1))
+    nrhs = mu.shape[1]
+    f = np.asfortranarray(np.asarray(rhs, np.float64).reshape(N, nrhs))
+    c = 1 if solution_dim == 1 else (3 if dim == 2 else 6)
+    nb = c * prob.n_holes
+    al = np.zeros((max(nb, 1), nrhs), order="F")
+    if nb:
+        al[:] = np.asarray(alpha, np.float64).reshape(nb, nrhs)
+    rows = np.ascontiguousarray(rows, np.int32)
+    res = np.zeros((rows.size, nrhs), order="F")
+    res_b = np.zeros((max(nb, 1), nrhs), order="F")
+    curv = prob.curvatures if prob.curvatures is not None else np.zeros(prob.n)
+    hc = np.ascontiguousarray(prob.hole_centers, np.float64).reshape(-1)
+    hs = np.ascontiguousarray(prob.hole_start, np.int32)
+    hn = np.ascontiguousarray(prob.hole_count, np.int32)
+    fn = lib.kiport_residual_rows
+    fn.argtypes = [ctypes.c_int] * 3 + [_P] * 4 + [ctypes.c_int] + [_P] * 6 + [ctypes.c_int, _P,
+                                                                               ctypes.c_int,
+                                                                               ctypes.c_int, _P, _P]
+    fn.restype = ctypes.c_int
+    rc = fn(prob.n, dim, solution_dim, _dp(np.ascontiguousarray(prob.points, np.float64)),
+            _dp(np.ascontiguousarray(prob.normals, np.float64)),
+            _dp(np.ascontiguousarray(prob.weights, np.float64)),
+            _dp(np.ascontiguousarray(curv, np.float64)), prob.n_holes, _dp(hc), _dp(hs), _dp(hn),
+            _dp(mu), _dp(al), _dp(f), nrhs, _dp(rows), rows.size, threads or os.cpu_count() or 1,
+            _dp(res), _dp(res_b))
+    if rc != 0:
+        lib.kiport_last_error.restype = ctypes.c_char_p
+        raise RuntimeError("oracle residual failed: " + lib.kiport_last_error().decode())
+    return res, res_b[:nb]

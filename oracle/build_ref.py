@@ -48,7 +48,13 @@ PATCHED = {
 
 
 def reference_root():
+    """Where the reference sources are read: KI_REFERENCE_ROOT, else the
+    checkout this recipe was written against."""
     return os.environ.get("KI_REFERENCE_ROOT", "/root/reference")
+
+
+def reference_present():
+    return os.path.isdir(os.path.join(reference_root(), "kern_interp"))
 
 
 def openblas_path():

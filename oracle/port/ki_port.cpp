@@ -416,6 +416,95 @@ void compute_diag3(Geometry* g, int n_outer, const std::vector<int>& hs, const s
   }
 }
 
+// Border matrices of a multiply connected boundary (initialize_U_mat /
+// initialize_Psi_mat, kern_interp/linear_solve.cpp:19-199), hole membership
+// from node ranges: U restricted to the DOF rows `rows` (|rows| x n_border)
+// and the whole Psi (n_border x N).  Columns per hole: 1 (Laplace), 3 (2D
+// Stokes: Stokeslets in x and y, rotlet), 6 (3D Stokes: 3 Stokeslets, 3
+// rotlets).
+void border_matrices(const Geometry& g, int n_holes, const double* hole_centers,
+                     const int* hole_start, const int* hole_count, const std::vector<int>& rows,
+                     Mat* Um, Mat* Psi) {
+  const int d = g.dim, sd = g.sol_dim;
+  const int c = sd == 1 ? 1 : (d == 2 ? 3 : 6);
+  const int N = g.n_points * sd;
+  const double* points = g.pts;
+  const double* weights = g.wts;
+  *Um = Mat((int)rows.size(), c * n_holes);
+  *Psi = Mat(c * n_holes, N);
+  for (int h = 0; h < n_holes; h++) {
+    const double* hc = hole_centers + d * h;
+    for (size_t i = 0; i < rows.size(); i++) {
+      const int p = rows[i] / sd, a = rows[i] % sd;
+      Mat& U = *Um;
+      if (d == 3) {
+        // linear_solve.cpp:26-36 (Laplace), :49-76 (Stokes)
+        double r[3] = {points[3 * p] - hc[0], points[3 * p + 1] - hc[1], points[3 * p + 2] - hc[2]};
+        double rn = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+        if (sd == 1) {
+          U((int)i, h) = 1.0 / rn;
+          continue;
+        }
+        for (int b = 0; b < 3; b++)
+          U((int)i, 6 * h + b) =
+              (1.0 / (8.0 * M_PI)) * ((a == b ? 1 : 0) / rn + r[a] * r[b] / std::pow(rn, 3));
+        double rot = -1.0 / (8.0 * M_PI * std::pow(rn, 3));
+        if (a == 0) {
+          U((int)i, 6 * h + 4) = rot * (-r[2]);
+          U((int)i, 6 * h + 5) = rot * (r[1]);
+        } else if (a == 1) {
+          U((int)i, 6 * h + 3) = rot * (r[2]);
+          U((int)i, 6 * h + 5) = rot * (-r[0]);
+        } else {
+          U((int)i, 6 * h + 3) = rot * (-r[1]);
+          U((int)i, 6 * h + 4) = rot * (r[0]);
+        }
+        continue;
+      }
+      double rx = points[2 * p] - hc[0], ry = points[2 * p + 1] - hc[1];
+      double rn = std::sqrt(rx * rx + ry * ry);
+      if (sd == 1) {
+        U((int)i, h) = std::log(rn);          // linear_solve.cpp:37-45
+      } else {                                 // linear_solve.cpp:77-97
+        double sc = 1.0 / (4 * M_PI), r2 = rn * rn;
+        if (a == 0) {
+          U((int)i, 3 * h) = sc * (std::log(1 / rn) + rx * rx / r2);
+          U((int)i, 3 * h + 1) = sc * (rx * ry / r2);
+          U((int)i, 3 * h + 2) = ry * (sc / r2);
+        } else {
+          U((int)i, 3 * h) = sc * (ry * rx / r2);
+          U((int)i, 3 * h + 1) = sc * (std::log(1 / rn) + ry * ry / r2);
+          U((int)i, 3 * h + 2) = -rx * (sc / r2);
+        }
+      }
+    }
+    // linear_solve.cpp:114-129, 131-143 (Laplace); :146-163 (3D Stokes),
+    // :164-177 (2D Stokes, absolute-coordinate rotation row)
+    for (int p = hole_start[h]; p < hole_start[h] + hole_count[h]; p++) {
+      double w = weights[p];
+      if (sd == 1) {
+        (*Psi)(h, p) = w;
+      } else if (d == 2) {
+        (*Psi)(3 * h, 2 * p) = w;
+        (*Psi)(3 * h + 1, 2 * p + 1) = w;
+        (*Psi)(3 * h + 2, 2 * p) = w * points[2 * p + 1];
+        (*Psi)(3 * h + 2, 2 * p + 1) = -w * points[2 * p];
+      } else {
+        double r[3] = {points[3 * p] - hc[0], points[3 * p + 1] - hc[1], points[3 * p + 2] - hc[2]};
+        (*Psi)(6 * h, 3 * p) = w;
+        (*Psi)(6 * h + 1, 3 * p + 1) = w;
+        (*Psi)(6 * h + 2, 3 * p + 2) = w;
+        (*Psi)(6 * h + 4, 3 * p) = -w * (-r[2]);
+        (*Psi)(6 * h + 5, 3 * p) = -w * (r[1]);
+        (*Psi)(6 * h + 3, 3 * p + 1) = -w * (r[2]);
+        (*Psi)(6 * h + 5, 3 * p + 1) = -w * (-r[0]);
+        (*Psi)(6 * h + 3, 3 * p + 2) = -w * (-r[1]);
+        (*Psi)(6 * h + 4, 3 * p + 2) = -w * (r[0]);
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------------ Tree --
 struct Node {
   int level = 0;
@@ -982,84 +1071,10 @@ int kiport_solve(int n_points, int domain_dim, int solution_dim, int pde,
       compute_diag3(&t.g, n_holes > 0 ? hole_start[0] : n_points, hs, hn, t.p.threads);
     }
     t.build();
-    if (n_holes > 0 && domain_dim == 3) {
-      // initialize_U_mat / initialize_Psi_mat, 3D (linear_solve.cpp:26-36, 49-76,
-      // 114-129, 146-163), hole membership from node ranges
-      int c = solution_dim == 1 ? 1 : 6;
-      t.U = Mat(N, c * n_holes);
-      t.Psi = Mat(c * n_holes, N);
-      for (int h = 0; h < n_holes; h++) {
-        const double* hc = hole_centers + 3 * h;
-        for (int p = 0; p < n_points; p++) {
-          double r[3] = {points[3 * p] - hc[0], points[3 * p + 1] - hc[1], points[3 * p + 2] - hc[2]};
-          double rn = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
-          if (solution_dim == 1) {
-            t.U(p, h) = 1.0 / rn;
-            continue;
-          }
-          for (int a = 0; a < 3; a++)
-            for (int b = 0; b < 3; b++)
-              t.U(3 * p + a, 6 * h + b) =
-                  (1.0 / (8.0 * M_PI)) * ((a == b ? 1 : 0) / rn + r[a] * r[b] / std::pow(rn, 3));
-          double rot = -1.0 / (8.0 * M_PI * std::pow(rn, 3));
-          t.U(3 * p, 6 * h + 4) = rot * (-r[2]);
-          t.U(3 * p, 6 * h + 5) = rot * (r[1]);
-          t.U(3 * p + 1, 6 * h + 3) = rot * (r[2]);
-          t.U(3 * p + 1, 6 * h + 5) = rot * (-r[0]);
-          t.U(3 * p + 2, 6 * h + 3) = rot * (-r[1]);
-          t.U(3 * p + 2, 6 * h + 4) = rot * (r[0]);
-        }
-        for (int p = hole_start[h]; p < hole_start[h] + hole_count[h]; p++) {
-          double w = weights[p];
-          if (solution_dim == 1) {
-            t.Psi(h, p) = w;
-            continue;
-          }
-          double r[3] = {points[3 * p] - hc[0], points[3 * p + 1] - hc[1], points[3 * p + 2] - hc[2]};
-          t.Psi(6 * h, 3 * p) = w;
-          t.Psi(6 * h + 1, 3 * p + 1) = w;
-          t.Psi(6 * h + 2, 3 * p + 2) = w;
-          t.Psi(6 * h + 4, 3 * p) = -w * (-r[2]);
-          t.Psi(6 * h + 5, 3 * p) = -w * (r[1]);
-          t.Psi(6 * h + 3, 3 * p + 1) = -w * (r[2]);
-          t.Psi(6 * h + 5, 3 * p + 1) = -w * (-r[0]);
-          t.Psi(6 * h + 3, 3 * p + 2) = -w * (-r[1]);
-          t.Psi(6 * h + 4, 3 * p + 2) = -w * (r[0]);
-        }
-      }
-    } else if (n_holes > 0) {
-      int c = solution_dim == 1 ? 1 : 3;
-      t.U = Mat(N, c * n_holes);
-      t.Psi = Mat(c * n_holes, N);
-      for (int h = 0; h < n_holes; h++) {
-        const double* hc = hole_centers + 2 * h;
-        for (int p = 0; p < n_points; p++) {
-          double rx = points[2 * p] - hc[0], ry = points[2 * p + 1] - hc[1];
-          double rn = std::sqrt(rx * rx + ry * ry);
-          if (solution_dim == 1) {
-            t.U(p, h) = std::log(rn);          // initialize_U_mat, linear_solve.cpp:37-45
-          } else {                               // linear_solve.cpp:77-97
-            double sc = 1.0 / (4 * M_PI), r2 = rn * rn;
-            t.U(2 * p, 3 * h) = sc * (std::log(1 / rn) + rx * rx / r2);
-            t.U(2 * p + 1, 3 * h) = sc * (ry * rx / r2);
-            t.U(2 * p, 3 * h + 1) = sc * (rx * ry / r2);
-            t.U(2 * p + 1, 3 * h + 1) = sc * (std::log(1 / rn) + ry * ry / r2);
-            t.U(2 * p, 3 * h + 2) = ry * (sc / r2);
-            t.U(2 * p + 1, 3 * h + 2) = -rx * (sc / r2);
-          }
-        }
-        for (int p = hole_start[h]; p < hole_start[h] + hole_count[h]; p++) {
-          double w = weights[p];
-          if (solution_dim == 1) {
-            t.Psi(h, p) = w;
-          } else {
-            t.Psi(3 * h, 2 * p) = w;
-            t.Psi(3 * h + 1, 2 * p + 1) = w;
-            t.Psi(3 * h + 2, 2 * p) = w * points[2 * p + 1];
-            t.Psi(3 * h + 2, 2 * p + 1) = -w * points[2 * p];
-          }
-        }
-      }
+    if (n_holes > 0) {
+      std::vector<int> all(N);
+      for (int i = 0; i < N; i++) all[i] = i;
+      border_matrices(t.g, n_holes, hole_centers, hole_start, hole_count, all, &t.U, &t.Psi);
     }
     t.skeletonize();
     double t1 = omp_get_wtime();
@@ -1121,6 +1136,82 @@ int kiport_dense_dim(int n_points, int domain_dim, int solution_dim, const doubl
   Mat K = kernel_block(g, all, all);
   std::memcpy(out, K.data(), sizeof(double) * (size_t)N * N);
   return 0;
+}
+
+// Residual rows of the (bordered) boundary-integral system, for checking a
+// solution at sizes where the dense operator does not fit:
+//   res[i, c]   = sum_j K(rows[i], j) mu[j, c] + sum_b U(rows[i], b) alpha[b, c] - f[rows[i], c]
+//   res_b[b, c] = sum_j Psi(b, j) mu[j, c] - alpha[b, c]          (n_holes > 0)
+// K is Kernel::operator() (kern_interp/kernel/kernel.cpp:304-429; 3D with the
+// row-sum diagonal, O(N^2)), U/Psi initialize_U_mat/initialize_Psi_mat.
+// Column-major mu (N x nrhs), alpha (n_border x nrhs), f (N x nrhs), res
+// (nrows x nrhs), res_b (n_border x nrhs).
+int kiport_residual_rows(int n_points, int domain_dim, int solution_dim, const double* points,
+                         const double* normals, const double* weights, const double* curvatures,
+                         int n_holes, const double* hole_centers, const int* hole_start,
+                         const int* hole_count, const double* mu, const double* alpha,
+                         const double* f, int nrhs, const int* rows, int nrows, int threads,
+                         double* res, double* res_b) {
+  try {
+    Geometry g;
+    g.n_points = n_points;
+    g.dim = domain_dim;
+    g.sol_dim = solution_dim;
+    g.pts = points;
+    g.nrm = normals;
+    g.wts = weights;
+    g.curv = curvatures;
+    threads = std::max(1, threads);
+    const int N = n_points * solution_dim;
+    if (domain_dim == 3) {
+      std::vector<int> hs(hole_start, hole_start + n_holes), hn(hole_count, hole_count + n_holes);
+      compute_diag3(&g, n_holes > 0 ? hole_start[0] : n_points, hs, hn, threads);
+    }
+    const int d = domain_dim, dpp = d == 3 ? (solution_dim == 1 ? 1 : 9) : 0;
+    // densities point-major so that one source's columns are contiguous
+    std::vector<double> mt((size_t)N * nrhs);
+    for (int c = 0; c < nrhs; c++)
+      for (int j = 0; j < N; j++) mt[(size_t)j * nrhs + c] = mu[j + (size_t)N * c];
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 1)
+    for (int i = 0; i < nrows; i++) {
+      std::vector<double> acc(nrhs, 0.0);
+      const int t = rows[i], tp = t / solution_dim;
+      for (int j = 0; j < N; j++) {
+        const int sp = j / solution_dim;
+        const double* dg = dpp ? g.diag.data() + (size_t)dpp * sp : nullptr;
+        const double e = entry(g, t, j, points + d * tp, normals + d * tp, points + d * sp,
+                               normals + d * sp, weights[sp], curvatures ? curvatures[sp] : 0., dg);
+        const double* m = mt.data() + (size_t)j * nrhs;
+        for (int c = 0; c < nrhs; c++) acc[c] += e * m[c];
+      }
+      for (int c = 0; c < nrhs; c++) res[i + (size_t)nrows * c] = acc[c] - f[t + (size_t)N * c];
+    }
+    if (n_holes > 0) {
+      Mat U, Psi;
+      std::vector<int> rv(rows, rows + nrows);
+      border_matrices(g, n_holes, hole_centers, hole_start, hole_count, rv, &U, &Psi);
+      const int nb = U.w;
+      for (int c = 0; c < nrhs; c++) {
+        for (int i = 0; i < nrows; i++) {
+          double a = 0.;
+          for (int b = 0; b < nb; b++) a += U(i, b) * alpha[b + (size_t)nb * c];
+          res[i + (size_t)nrows * c] += a;
+        }
+        for (int b = 0; b < nb; b++) {
+          // Psi's row b is nonzero only on its hole's DOFs
+          const int h = b / (nb / n_holes);
+          const int j0 = hole_start[h] * solution_dim, j1 = j0 + hole_count[h] * solution_dim;
+          double a = 0.;
+          for (int j = j0; j < j1; j++) a += Psi(b, j) * mu[j + (size_t)N * c];
+          res_b[b + (size_t)nb * c] = a - alpha[b + (size_t)nb * c];
+        }
+      }
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
 }
 
 }  // extern "C"

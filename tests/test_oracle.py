@@ -70,7 +70,12 @@ def test_port_dense_residual(oracle_mod, pkg):
 def test_reference_matches_port_random_star(oracle_mod, pkg):
     """Where the reference tree is present, the compiled reference and the port
     agree on a freshly generated boundary (not a stored fixture)."""
-    if not os.path.isdir(os.environ.get("KI_REFERENCE_ROOT", "/root/reference") + "/kern_interp"):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "_ki_build_ref", os.path.join(os.path.dirname(oracle_mod.__file__), "build_ref.py"))
+    br = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(br)
+    if not br.reference_present():
         pytest.skip("reference sources not present")
     prob = pkg.geometry.star(96, 16, amp=0.25, k=4)
     f = pkg.geometry.laplace_source_rhs(prob, np.array([[-2.5, 1.5]]))
@@ -78,3 +83,70 @@ def test_reference_matches_port_random_star(oracle_mod, pkg):
     b, _, sb = oracle_mod.solve(prob, f, 1e-9, threads=4, impl="port")
     assert np.abs(a - b).max() <= 1e-10 * np.abs(a).max()
     assert sa["root"] == sb["root"]
+
+
+
+def _border_dense(prob, sd):
+    """U (N x n_border) and Psi (n_border x N) of a 2D multiply connected
+    boundary, restated in numpy from initialize_U_mat / initialize_Psi_mat
+    (kern_interp/linear_solve.cpp:37-45, 77-97, 131-143, 164-177)."""
+    n, H = prob.n, prob.n_holes
+    N = n * sd
+    c = 1 if sd == 1 else 3
+    U = np.zeros((N, c * H))
+    Psi = np.zeros((c * H, N))
+    for h in range(H):
+        rx = prob.points[:, 0] - prob.hole_centers[h, 0]
+        ry = prob.points[:, 1] - prob.hole_centers[h, 1]
+        r2 = rx * rx + ry * ry
+        s0, n0 = prob.hole_start[h], prob.hole_count[h]
+        w = prob.weights[s0:s0 + n0]
+        if sd == 1:
+            U[:, h] = 0.5 * np.log(r2)
+            Psi[h, s0:s0 + n0] = w
+            continue
+        sc = 1.0 / (4 * np.pi)
+        lg = -0.5 * np.log(r2)
+        U[0::2, 3 * h] = sc * (lg + rx * rx / r2)
+        U[1::2, 3 * h] = sc * (rx * ry / r2)
+        U[0::2, 3 * h + 1] = sc * (rx * ry / r2)
+        U[1::2, 3 * h + 1] = sc * (lg + ry * ry / r2)
+        U[0::2, 3 * h + 2] = ry * sc / r2
+        U[1::2, 3 * h + 2] = -rx * sc / r2
+        Psi[3 * h, 2 * s0:2 * (s0 + n0):2] = w
+        Psi[3 * h + 1, 2 * s0 + 1:2 * (s0 + n0):2] = w
+        Psi[3 * h + 2, 2 * s0:2 * (s0 + n0):2] = w * prob.points[s0:s0 + n0, 1]
+        Psi[3 * h + 2, 2 * s0 + 1:2 * (s0 + n0):2] = -w * prob.points[s0:s0 + n0, 0]
+    return U, Psi
+
+
+@pytest.mark.parametrize("kind", ["laplace2d_holes", "stokes2d_holes", "laplace3d"])
+def test_port_residual_rows_match_dense(oracle_mod, pkg, kind):
+    """kiport_residual_rows (the residual check used at sizes where the dense
+    operator does not fit) equals the dense bordered residual
+    [K U; Psi -I][mu; alpha] - [f; 0] on the rows asked for."""
+    g = pkg.geometry
+    rng = np.random.default_rng(5)
+    sd = 1
+    if kind == "laplace2d_holes":
+        prob = g.disc_with_ellipses(1024, 3, seed=7)
+    elif kind == "stokes2d_holes":
+        prob, sd = g.disc_with_circles(512, 3, seed=7), 2
+    else:
+        prob = g.ellipsoid(800)
+    N = prob.n * sd
+    K = oracle_mod.dense_matrix(prob, solution_dim=sd)
+    if kind == "laplace3d":
+        U, Psi = np.zeros((N, 0)), np.zeros((0, N))
+    else:
+        U, Psi = _border_dense(prob, sd)
+    nb = U.shape[1]
+    mu = rng.standard_normal((N, 3))
+    alpha = rng.standard_normal((nb, 3))
+    f = rng.standard_normal((N, 3))
+    rows = np.sort(rng.choice(N, 40, replace=False))
+    res, res_b = oracle_mod.residual_rows(prob, mu, alpha, f, rows, solution_dim=sd, threads=4)
+    full = K @ mu + U @ alpha - f
+    np.testing.assert_allclose(res, full[rows], rtol=0, atol=1e-12 * np.abs(full).max())
+    if nb:
+        np.testing.assert_allclose(res_b, Psi @ mu - alpha, rtol=0, atol=1e-12 * np.abs(alpha).max())

@@ -57,5 +57,9 @@ def test_bench_reference_arm_torchrun_world2():
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
     assert len(lines) == 1
     d = json.loads(lines[0])
-    assert d["impl"] == "reference" and d["n_gpus"] == 2
+    # rank 0 alone does the CPU work: one worker, two ranks launched
+    assert d["impl"] == "reference" and d["n_gpus"] == 1
+    assert d["config"]["ranks_launched"] == 2 and d["config"]["ranks_working"] == 1
+    assert d["metric"].endswith("relative residual")
+    assert d["config"]["residual_reached_max"] <= d["config"]["target_residual"]
     assert d["cpu_baseline"]["kind"] == "port" and d["value"] > 0
