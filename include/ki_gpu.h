@@ -268,6 +268,16 @@ int ki_factor_set_profiling(ki_factor* f, int on);
 int ki_measure_fma_peak(double* fp64_gflops, double* fp32_gflops);
 
 /*
+ * Health check of the tensor-core path (no reference counterpart): runs the
+ * machinery of the FP32 factorization's tensor-core ID sketch (tcgen05 TF32
+ * MMAs from shared-memory operand tiles into TMEM accumulators, entries
+ * split hi + lo) on fixed data on the current GPU and returns in
+ * *max_rel_err its largest difference from the same product summed in FP64,
+ * relative to the largest entry (about 1e-6 when the path works).
+ */
+int ki_tensor_core_check(double* max_rel_err);
+
+/*
  * Learned rank predictor (no reference counterpart): a 12-64-64-1 MLP
  * (ReLU hidden layers, logistic output) mapping per-box features to the rank
  * fraction k/n of the box's interpolative decomposition, trained and

@@ -30,7 +30,7 @@ PRECISION_FP64, PRECISION_FP32 = 0, 1
 EXPORTED = ["ki_factor_create", "ki_factor_destroy", "ki_factor_get_info", "ki_solve",
             "ki_solve_device", "ki_apply", "ki_eval_targets", "ki_last_error", "ki_version",
             "ki_factor_get_profile", "ki_factor_set_profiling", "ki_apply_rows",
-            "ki_measure_fma_peak", "ki_solve_refined", "ki_solve_refined_device",
+            "ki_measure_fma_peak", "ki_tensor_core_check", "ki_solve_refined", "ki_solve_refined_device",
             "ki_solve_device_noalloc", "ki_apply_fmm", "ki_apply_fmm_ex", "ki_trim_memory",
             "ki_launch_count", "ki_rank_model_floats",
             "ki_rank_model_train", "ki_rank_model_predict", "ki_rank_model_grad",
@@ -110,6 +110,7 @@ def load_library(path=None):
     lib.ki_rank_model_grad.argtypes = [V, V, V, I, V, F]
     lib.ki_factor_get_box_log.argtypes = [V, V, I, ctypes.POINTER(I)]
     lib.ki_measure_fma_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    lib.ki_tensor_core_check.argtypes = [ctypes.POINTER(ctypes.c_double)]
     lib.ki_last_error.restype = ctypes.c_char_p
     lib.ki_version.restype = ctypes.c_char_p
     for name in EXPORTED:
@@ -357,6 +358,15 @@ def rank_model_grad(model, features, ratios):
     _check(load_library().ki_rank_model_grad(_ptr(np.ascontiguousarray(model, np.float32)), _ptr(X),
                                              _ptr(y), X.shape[0], _ptr(g), ctypes.byref(loss)))
     return float(loss.value), g
+
+
+def tensor_core_check():
+    """Largest relative difference of the tensor-core sketch machinery
+    (tcgen05 TF32 MMAs into TMEM) from the same product in FP64, on fixed
+    data on the current GPU (ki_tensor_core_check)."""
+    e = ctypes.c_double()
+    _check(load_library().ki_tensor_core_check(ctypes.byref(e)))
+    return e.value
 
 
 def measure_fma_peak():

@@ -68,6 +68,7 @@ int guarded(F&& f) {
       return fail(KI_ERR_OOM, m);
     if (m.find("singular") != std::string::npos || m.find("non-finite") != std::string::npos)
       return fail(KI_ERR_NUMERIC, m);
+    if (m.find("timed out") != std::string::npos) return fail(KI_ERR_TIMEOUT, m);
     return fail(KI_ERR_CUDA, m);
   } catch (...) {
     return fail(KI_ERR_CUDA, "unknown error");
@@ -1609,11 +1610,11 @@ int ki_factor_get_profile(ki_factor* f, char* buf, int len) {
         snprintf(tmp, sizeof(tmp),
                  "%s{\"level\": %d, \"boxes\": %d, \"id_boxes\": %d, \"compressed\": %d, "
                  "\"max_n\": %d, \"mean_n\": %.1f, \"max_m\": %d, \"mean_m\": %.1f, "
-                 "\"max_k\": %d, \"mean_k\": %.1f, \"paths\": [%d, %d, %d, %d]}",
+                 "\"max_k\": %d, \"mean_k\": %.1f, \"paths\": [%d, %d, %d, %d, %d]}",
                  i ? ", " : "", q.level, q.boxes, q.id_boxes, q.compressed, q.max_n,
                  q.sum_n / std::max(1, q.id_boxes), q.max_m, q.sum_m / std::max(1, q.id_boxes),
                  q.max_k, q.sum_k / std::max(1, q.id_boxes), q.mode_count[0], q.mode_count[1],
-                 q.mode_count[2], q.mode_count[3]);
+                 q.mode_count[2], q.mode_count[3], q.mode_count[4]);
         lv += tmp;
       }
       lv += "]";
@@ -1642,6 +1643,13 @@ int ki_measure_fma_peak(double* fp64_gflops, double* fp32_gflops) {
     KI_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     *fp64_gflops = fma_peak_gflops<double>(sms, 20000);
     *fp32_gflops = fma_peak_gflops<float>(sms, 200000);
+  });
+}
+
+int ki_tensor_core_check(double* max_rel_err) {
+  return guarded([&] {
+    if (!max_rel_err) throw ArgError("NULL argument");
+    *max_rel_err = ki::tensor_core_selfcheck();
   });
 }
 

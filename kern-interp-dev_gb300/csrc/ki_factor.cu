@@ -38,6 +38,7 @@
 #include "ki_common.cuh"
 #include "ki_dense.h"
 #include "ki_mlp.h"
+#include "ki_tc.cuh"
 #include "ki_tree_gpu.h"
 
 namespace ki {
@@ -819,6 +820,235 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? kIdMinBlocks<T> : 1) k_id
   for (int i = tid; i < n; i += nth) pact[i] = act[perm[i]];
 }
 
+// ------------------------------------------------ tensor-core ID sketch --
+// Y = Omega M (l x n) for the narrow boxes of a sketched (randomized) ID, on
+// the tensor cores: M's rows are generated 32 at a time into shared memory
+// (the A operand, box columns x block rows, K-major), Omega's matching
+// columns (the same +-1 signs as k_id's fold) form the B operand, and
+// tcgen05 kind::tf32 MMAs accumulate Y^T (box columns x sketch rows) in
+// TMEM.  Each entry enters as hi + lo, both rounded to TF32, so it is
+// represented to 2^-22 relative; the signs are exact.  The tensor core's
+// FP32 accumulation does not round to nearest: over the few hundred ID rows
+// of a box it loses about a decimal digit against the CUDA-core fold, which
+// is why this path is opt-in.  Y goes row-major into the task's global
+// scratch, where k_id's pivoted QR (flags 4) picks it up.  Boxes of up to
+// 128 columns use one M = 128 accumulator tile, up to 256 columns two.
+constexpr int kTcRows = 32;         // ID-matrix rows per MMA block (K of 4 MMAs)
+constexpr int kTcThreads = 256;
+constexpr long long kTcWaitCycles = 2000000000LL;   // ~1 s at 2 GHz: bounded waits
+
+__host__ __device__ constexpr size_t tc_sketch_smem(int tiles, int nq) {
+  return (size_t)tiles * 2 * 128 * kTcRows * sizeof(float) + (size_t)nq * kTcRows * sizeof(float);
+}
+
+__device__ __forceinline__ uint32_t tc_tmem_cols(int used) {
+  uint32_t c = 32;
+  while ((int)c < used) c <<= 1;
+  return c;
+}
+
+// Sign of Omega(q, row) for a box (k_id's fold uses the same hash): bit q % 32
+// of word q / 32 of the row's lowbias32 hash (C. Wellons).
+__device__ __forceinline__ float sketch_sign(int64_t act, int row, int q) {
+  uint32_t x = (uint32_t)(act * 2654435761u) ^ (uint32_t)(row * 40503u) ^
+               (uint32_t)((q >> 5) * 2246822519u);
+  x ^= x >> 16; x *= 0x7feb352du; x ^= x >> 15; x *= 0x846ca68bu; x ^= x >> 16;
+  return ((x >> (q & 31)) & 1u) ? -1.f : 1.f;
+}
+
+// Issue the MMAs of one 32-row block (one thread): D_t (+)= A_t B for the
+// tiles t, with A_t = A_hi,t + A_lo,t.
+__device__ __forceinline__ void tc_issue_block(uint32_t tmem, const float* a_hi, const float* a_lo,
+                                               const float* b, int tiles, int nq, bool first) {
+  const uint32_t sbo = 32 * kTcRows;   // bytes between 8-row groups: kTcRows / 4 core matrices
+  const uint32_t idesc = tc::idesc_tf32(128, nq);
+  const uint32_t tile_bytes = 128 * kTcRows * sizeof(float);
+  for (int tt = 0; tt < tiles; tt++)
+    for (int s = 0; s < kTcRows / 8; s++) {
+      const uint64_t bd = tc::smem_desc(tc::smem_u32(b) + 256 * s, tc::kLbo, sbo);
+      const uint64_t ah = tc::smem_desc(tc::smem_u32(a_hi) + tt * tile_bytes + 256 * s, tc::kLbo, sbo);
+      const uint64_t al = tc::smem_desc(tc::smem_u32(a_lo) + tt * tile_bytes + 256 * s, tc::kLbo, sbo);
+      tc::mma_tf32(tmem + tt * nq, ah, bd, idesc, (first && s == 0) ? 0u : 1u);
+      tc::mma_tf32(tmem + tt * nq, al, bd, idesc, 1u);
+    }
+}
+
+// The A and B operands of one block.  Warps fill whole core matrices (8 rows
+// x 4 block rows; lane -> (row 8 rb + lane / 4, block row 4 kb + lane % 4)).
+// entry(c, i) gives A's value at box column c, block row i (0 outside).
+template <typename Entry>
+__device__ __forceinline__ void tc_fill_block(float* a_hi, float* a_lo, float* b, int tiles, int nq,
+                                              Entry entry, int64_t act, int r0, int l) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const uint32_t sbo = 32 * kTcRows, tile_bytes = 128 * kTcRows * sizeof(float);
+  constexpr int kb_n = kTcRows / 4;
+  for (int u = warp; u < tiles * 16 * kb_n; u += nw) {
+    const int rb = u / kb_n, kb = u % kb_n;
+    const float v = entry(rb * 8 + (lane >> 2), kb * 4 + (lane & 3));
+    const float hi = tc::to_tf32(v);
+    const float lo = tc::to_tf32(v - hi);
+    const uint32_t off = (uint32_t)(rb >> 4) * tile_bytes + tc::core_offset(rb & 15, kb, sbo) + 4 * lane;
+    *reinterpret_cast<float*>(reinterpret_cast<char*>(a_hi) + off) = hi;
+    *reinterpret_cast<float*>(reinterpret_cast<char*>(a_lo) + off) = lo;
+  }
+  for (int u = warp; u < (nq / 8) * kb_n; u += nw) {
+    const int qb = u / kb_n, kb = u % kb_n;
+    const int q = qb * 8 + (lane >> 2), i = kb * 4 + (lane & 3);
+    const float sv = q < l ? sketch_sign(act, r0 + i, q) : 0.f;
+    *reinterpret_cast<float*>(reinterpret_cast<char*>(b) + tc::core_offset(qb, kb, sbo) + 4 * lane) = sv;
+  }
+}
+
+template <int TILES>
+__global__ void __launch_bounds__(kTcThreads) k_sketch_tc(const IdTask* tasks, const int* list,
+                                                          const int* m_arr, const int* sketch_l,
+                                                          const int* ipool, const int* iscratch,
+                                                          float* tws, Points<float> P, int sol_dim,
+                                                          ProxyTab<float> px, int* err) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tmem_base;
+  __shared__ ProxyBox<float> s_box;
+  const int ti = list[blockIdx.x];
+  const IdTask t = tasks[ti];
+  const int n = t.n, m = m_arr[ti], l = sketch_l[ti];
+  const int nq = (l + 15) & ~15;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nI = (m - (t.mode == 0 ? 2 * px.n * sol_dim : 0)) / 2;
+  const int* rows = iscratch + t.rows;
+  const int* act = ipool + t.act;
+  float* a_hi = reinterpret_cast<float*>(tc_smem);
+  float* a_lo = a_hi + TILES * 128 * kTcRows;
+  float* bs = a_lo + TILES * 128 * kTcRows;
+  const uint32_t ncols = tc_tmem_cols(TILES * nq);
+  if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
+  if (tid == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+    s_box = proxy_box<float>(t.cx, t.cy, t.cz, t.rad_proxy, px.n);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  const ProxyBox<float> pb = s_box;
+  uint32_t phase = 0;
+  bool ok = true;
+  for (int r0 = 0; r0 < m; r0 += kTcRows) {
+    if (r0 > 0) {
+      // the previous block's MMAs have read the operands
+      ok = tc::mbar_wait(&bar, phase, kTcWaitCycles) && ok;
+      phase ^= 1;
+    }
+    tc_fill_block(a_hi, a_lo, bs, TILES, nq,
+                  [&](int c, int i) {
+                    const int row = r0 + i;
+                    return (c < n && row < m) ? id_entry<float>(P, sol_dim, row, nI, rows, act[c], px, pb)
+                                              : 0.f;
+                  },
+                  t.act, r0, l);
+    tc::fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      tc_issue_block(tmem, a_hi, a_lo, bs, TILES, nq, r0 == 0);
+      tc::mma_commit(&bar);
+    }
+  }
+  ok = tc::mbar_wait(&bar, phase, kTcWaitCycles) && ok;
+  tc::fence_after_sync();
+  // Y^T in TMEM: lane = box column, column = sketch row; 16-column chunks,
+  // warps w and w + 4 share lanes 32 (w % 4).. and split the chunks
+  float* gws = tws + t.ws;
+  const int chunks = TILES * (nq / 16);
+  for (int ch = warp >> 2; ch < chunks; ch += kTcThreads / 128) {
+    const int tt = ch / (nq / 16), q0 = (ch % (nq / 16)) * 16;
+    float v[16];
+    tc::tmem_ld16(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(tt * nq + q0), v);
+    const int c = tt * 128 + 32 * (warp & 3) + lane;
+    if (ok && c < n) {
+#pragma unroll
+      for (int j = 0; j < 16; j++)
+        if (q0 + j < l) gws[(size_t)(q0 + j) * n + c] = v[j];
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+  if (!ok && tid == 0) atomicMax(err, (int)kDevTimeout);
+}
+
+// Self-check of the tensor-core sketch machinery on fixed data: two tiles
+// (M = 256 rows), nq = 48 columns, K = 64 (two blocks), the operands built
+// by tc_fill_block and multiplied by tc_issue_block exactly as k_sketch_tc
+// does; d (256 x 48, row-major) receives the TMEM result, ref the same
+// product summed in FP64 on the CUDA cores.
+constexpr int kTcCheckRows = 256, kTcCheckQ = 48, kTcCheckL = 45, kTcCheckK = 64;
+__device__ __forceinline__ float tc_check_entry(int c, int i) {
+  return __sinf(0.05f * c + 0.31f * i) * (1.0f + 0.001f * c) + 1e-3f * (float)((c * 7 + i * 13) % 17);
+}
+__global__ void __launch_bounds__(kTcThreads) k_tc_selfcheck(float* d, double* ref, int* err) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tmem_base;
+  constexpr int TILES = 2, nq = kTcCheckQ, l = kTcCheckL;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  float* a_hi = reinterpret_cast<float*>(tc_smem);
+  float* a_lo = a_hi + TILES * 128 * kTcRows;
+  float* bs = a_lo + TILES * 128 * kTcRows;
+  const uint32_t ncols = tc_tmem_cols(TILES * nq);
+  if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
+  if (tid == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  uint32_t phase = 0;
+  bool ok = true;
+  const int64_t act = 12345;
+  for (int r0 = 0; r0 < kTcCheckK; r0 += kTcRows) {
+    if (r0 > 0) {
+      ok = tc::mbar_wait(&bar, phase, kTcWaitCycles) && ok;
+      phase ^= 1;
+    }
+    tc_fill_block(a_hi, a_lo, bs, TILES, nq, [&](int c, int i) { return tc_check_entry(c, r0 + i); },
+                  act, r0, l);
+    tc::fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      tc_issue_block(tmem, a_hi, a_lo, bs, TILES, nq, r0 == 0);
+      tc::mma_commit(&bar);
+    }
+  }
+  ok = tc::mbar_wait(&bar, phase, kTcWaitCycles) && ok;
+  tc::fence_after_sync();
+  const int chunks = TILES * (nq / 16);
+  for (int ch = warp >> 2; ch < chunks; ch += kTcThreads / 128) {
+    const int tt = ch / (nq / 16), q0 = (ch % (nq / 16)) * 16;
+    float v[16];
+    tc::tmem_ld16(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(tt * nq + q0), v);
+    const int c = tt * 128 + 32 * (warp & 3) + lane;
+#pragma unroll
+    for (int j = 0; j < 16; j++) d[(size_t)c * nq + q0 + j] = v[j];
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+  // the same product in FP64 on the CUDA cores
+  for (int e = tid; e < kTcCheckRows * nq; e += blockDim.x) {
+    const int c = e / nq, q = e % nq;
+    double acc = 0.0;
+    if (q < l)
+      for (int i = 0; i < kTcCheckK; i++) acc += (double)tc_check_entry(c, i) * sketch_sign(act, i, q);
+    ref[e] = acc;
+  }
+  if (!ok && tid == 0) atomicMax(err, (int)kDevTimeout);
+}
+
 // Features of the learned rank predictor for every ID box of a level (one
 // warp per box, four per CTA), and with a model the predicted sketch size
 // l = min(n, ceil((1 + margin) k^) + oversample), k^ = n * MLP(features):
@@ -1342,9 +1572,13 @@ template <typename T> constexpr int kSchurMaxThreads = sizeof(T) == 4 ? 1024 : k
 // (X up to 64 rows and kGjCols W columns with W warps).
 constexpr int kGjCols = 8;
 template <typename T> constexpr int kSchurMinBlocks = sizeof(T) == 4 ? 1 : 2;
+// phase (Gauss-Jordan path in shared memory only): 0 the whole elimination;
+// 1 up to X = K_rr - T^T K_sr - K~_rs T, which is stored in t.X (r x r) with
+// K_ss, K~_rs and K~_sr^T in t.ws (k x k | r x k | r x k), for k_gj to
+// invert into t.Xi; 2 the products with the inverse, from those stores.
 template <typename T>
 __global__ void __launch_bounds__(kSchurMaxThreads<T>, kSchurMinBlocks<T>) k_schur(const SchurTask<T>* tasks, int task_base,
-                                                     int smem, int* err) {
+                                                     int smem, int* err, int phase) {
   extern __shared__ __align__(16) unsigned char sc_smem[];
   const SchurTask<T> t = tasks[task_base + blockIdx.x];
   const int n = t.n, k = t.k, r = n - k;
@@ -1362,6 +1596,23 @@ __global__ void __launch_bounds__(kSchurMaxThreads<T>, kSchurMinBlocks<T>) k_sch
   T* Lt = Wrs + (size_t)ld * k;       // r x k : K_sr^T, then K~_sr^T, then L^T
   T* X = smem ? Lt + (size_t)ld * k : t.X;   // r x r
   const int* pm = t.perm;
+  if (phase == 2) {
+    // K_ss | K~_rs | K~_sr^T from t.ws, X^-1 from t.Xi, X itself from t.X
+    T* X0 = X + (size_t)ld * r + 5 * (size_t)r;
+    const T* g = t.ws;
+    for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) Kss[idx] = g[idx];
+    for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
+      const int i = idx % r, j = idx / r;
+      Wrs[i + (size_t)ld * j] = g[k * k + idx];
+      Lt[i + (size_t)ld * j] = g[k * k + r * k + idx];
+    }
+    for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) {
+      const int i = idx % r, j = idx / r;
+      X[i + (size_t)ld * j] = t.Xi[idx];
+      X0[i + (size_t)ld * j] = t.X[idx];
+    }
+    __syncthreads();
+  } else {
   for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) {
     const int i = idx % k, j = idx / k;
     Kss[idx] = t.K[pm[i] + (size_t)n * pm[j]];
@@ -1392,20 +1643,35 @@ __global__ void __launch_bounds__(kSchurMaxThreads<T>, kSchurMinBlocks<T>) k_sch
   // X -= K~_rs T
   cta_gemm<T>(r, r, k, T(-1), Wrs, ld, false, Tm, kt, false, T(1), X, ld);
   __syncthreads();
+  if (phase == 1) {
+    T* g = t.ws;
+    for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) g[idx] = Kss[idx];
+    for (int idx = threadIdx.x; idx < r * k; idx += blockDim.x) {
+      const int i = idx % r, j = idx / r;
+      g[k * k + idx] = Wrs[i + (size_t)ld * j];
+      g[k * k + r * k + idx] = Lt[i + (size_t)ld * j];
+    }
+    for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x)
+      t.X[idx] = X[idx % r + (size_t)ld * (idx / r)];
+    return;
+  }
+  }   // phase != 2
   if (smem && t.gj) {
     // shared memory after X: scratch (5r) | X0 (r x r) | U0 (r x k) | L0 (k x r)
     T* colj = X + (size_t)ld * r;
     T* X0 = colj + 5 * (size_t)r;
     T* U0 = X0 + (size_t)ld * r;
     T* L0 = U0 + (size_t)ld * k;
-    for (int idx = threadIdx.x; idx < ld * r; idx += blockDim.x) X0[idx] = X[idx];
-    __syncthreads();
-    // X <- X^-1: in registers where the block's tile covers X, else in shared memory
-    const int W = blockDim.x >> 5;
-    const int info = (r <= 64 && r <= W * kGjCols)
-                         ? cta_gj_inverse_reg<T, 2, kGjCols>(r, X, ld, t.piv, colj)
-                         : cta_gj_inverse<T>(r, X, ld, t.piv, colj, s_val, &s_idx);
-    if (info != 0 && threadIdx.x == 0) atomicMax(err, (int)kDevSingular);
+    if (phase == 0) {
+      for (int idx = threadIdx.x; idx < ld * r; idx += blockDim.x) X0[idx] = X[idx];
+      __syncthreads();
+      // X <- X^-1: in registers where the block's tile covers X, else in shared memory
+      const int W = blockDim.x >> 5;
+      const int info = (r <= 64 && r <= W * kGjCols)
+                           ? cta_gj_inverse_reg<T, 2, kGjCols>(r, X, ld, t.piv, colj)
+                           : cta_gj_inverse<T>(r, X, ld, t.piv, colj, s_val, &s_idx);
+      if (info != 0 && threadIdx.x == 0) atomicMax(err, (int)kDevSingular);
+    }
     // U0 = X^-1 K~_rs (r x k), L0 = K~_sr X^-1 (k x r)
     cta_gemm<T>(r, k, r, T(1), X, ld, false, Wrs, ld, false, T(0), U0, ld);
     cta_gemm<T>(k, r, r, T(1), Lt, ld, true, X, ld, false, T(0), L0, k);
@@ -1424,8 +1690,9 @@ __global__ void __launch_bounds__(kSchurMaxThreads<T>, kSchurMinBlocks<T>) k_sch
     cta_gemm_to<T>(r, k, r, T(1), X, ld, false, Wrs, ld, false, T(1), U0, ld, t.U, r);
     cta_gemm_to<T>(k, r, r, T(1), Lt, ld, true, X, ld, false, T(1), L0, k, t.L, k);
     cta_gemm<T>(k, k, r, T(-1), Lt, ld, true, U0, ld, false, T(1), t.Atil, k);
-    for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x)
-      t.Xi[idx] = X[idx % r + (size_t)ld * (idx / r)];
+    if (phase == 0)
+      for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x)
+        t.Xi[idx] = X[idx % r + (size_t)ld * (idx / r)];
     return;
   }
   int info = cta_lu<T>(r, X, ld, t.piv, &s_flag, &s_red, &s_idx);
@@ -1448,6 +1715,142 @@ __global__ void __launch_bounds__(kSchurMaxThreads<T>, kSchurMinBlocks<T>) k_sch
   if (smem)
     for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x)
       t.X[idx] = X[idx % r + (size_t)ld * (idx / r)];
+}
+
+// Gauss-Jordan inverse of one FP32 redundant block X (r x r, column-major in
+// t.X, r <= 32 MA) per CTA into t.Xi, with partial pivoting by rows that are
+// not swapped but recorded (X^-1(spinv[i], spiv[c]) = a(i, c) at the end):
+// the arithmetic of cta_gj_inverse_reg, with the block in registers (lane =
+// rows lane, lane + 32, ..; warp w = columns CW w .. CW w + CW - 1) and only
+// the warps that own columns doing work.  Per column j the warp owning it
+// picks the pivot among the unused rows and publishes the column (the
+// multipliers) and the pivot index in shared memory; one barrier; each warp
+// takes its slab of the pivot row from the owning lane by shuffles and
+// eliminates.  A zero pivot is reported (kDevSingular) and skipped.
+constexpr int kGjLeanCols = 16;
+template <int MA, int CW>
+__global__ void __launch_bounds__(32 * (32 * MA / CW)) k_gj(const SchurTask<float>* tasks, int task_base,
+                                                            int* err) {
+  __shared__ float s_col[2][32 * MA];
+  __shared__ int s_p[2];
+  __shared__ int s_spiv[32 * MA], s_spinv[32 * MA];
+  const SchurTask<float> t = tasks[task_base + blockIdx.x];
+  const int r = t.n - t.k;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  // warps without columns only keep the barriers company
+  const bool active = w * CW < r;
+  float a[MA][CW];
+#pragma unroll
+  for (int ia = 0; ia < MA; ia++)
+#pragma unroll
+    for (int c = 0; c < CW; c++) {
+      const int i = lane + 32 * ia, gc = CW * w + c;
+      a[ia][c] = (active && i < r && gc < r) ? t.X[i + (size_t)r * gc] : 0.f;
+    }
+  // column jn of the owner warp's registers into f (dynamic column index:
+  // a select over the unrolled slab)
+  auto column = [&](int jn, float (&f)[MA]) {
+    const int jj = jn - CW * w;
+#pragma unroll
+    for (int ia = 0; ia < MA; ia++) {
+      float v = 0.f;
+#pragma unroll
+      for (int c = 0; c < CW; c++) v = (c == jj) ? a[ia][c] : v;
+      f[ia] = v;
+    }
+  };
+  float fcol[MA];
+  if (w == 0) column(0, fcol);
+  unsigned used = 0;   // bit ia: row lane + 32 ia already a pivot row
+  int info = 0;
+  for (int j = 0; j < r; j++) {
+    const int buf = j & 1;
+    const int ow = j / CW;
+    if (w == ow) {
+      float best = -1.f;
+      int bi = r;
+#pragma unroll
+      for (int ia = 0; ia < MA; ia++) {
+        const int i = lane + 32 * ia;
+        if (i < r && !((used >> ia) & 1u)) {
+          float v = fabsf(fcol[ia]);
+          if (!(v == v)) v = 3e38f;   // a NaN orders first, so the choice stays a valid row
+          if (v > best) { best = v; bi = i; }
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+      }
+#pragma unroll
+      for (int ia = 0; ia < MA; ia++) s_col[buf][lane + 32 * ia] = fcol[ia];
+      if (lane == 0) {
+        s_p[buf] = bi;
+        s_spiv[j] = bi;
+        s_spinv[bi] = j;
+        t.piv[j] = bi;
+      }
+    }
+    __syncthreads();
+    const int p = s_p[buf];
+    const int pa = p >> 5, pl = p & 31;
+    if (pl == lane) used |= 1u << pa;
+    const float pv = s_col[buf][p];
+    const int jn = j + 1;
+    const bool own_next = jn < r && w == jn / CW;
+    if (pv == 0.f) {   // the same branch in every thread
+      if (info == 0) info = j + 1;
+      if (own_next) column(jn, fcol);
+      continue;
+    }
+    if (!active) continue;
+    const float inv = 1.f / pv;
+    float m[MA];
+    bool isp[MA];
+#pragma unroll
+    for (int ia = 0; ia < MA; ia++) {
+      isp[ia] = (ia == pa) && (pl == lane);
+      m[ia] = isp[ia] ? 1.f : -s_col[buf][lane + 32 * ia];
+    }
+    // every row: a(i, c) -= f_i rp_c; the pivot row: rp_c (rp = scaled pivot row)
+#pragma unroll
+    for (int c = 0; c < CW; c++) {
+      float src = a[0][c];
+#pragma unroll
+      for (int ia = 1; ia < MA; ia++) src = (pa == ia) ? a[ia][c] : src;
+      const float rp = __shfl_sync(0xffffffffu, src, pl) * inv;
+#pragma unroll
+      for (int ia = 0; ia < MA; ia++) a[ia][c] = fmaf(m[ia], rp, isp[ia] ? 0.f : a[ia][c]);
+    }
+    if (w == ow) {
+      // column j of the inverse: inv in the pivot row, -f_i inv elsewhere
+      const int jj = j - CW * w;
+#pragma unroll
+      for (int ia = 0; ia < MA; ia++) {
+        const float v = isp[ia] ? inv : m[ia] * inv;
+#pragma unroll
+        for (int c = 0; c < CW; c++) a[ia][c] = (c == jj) ? v : a[ia][c];
+      }
+    }
+    if (own_next) column(jn, fcol);
+  }
+  __syncthreads();   // every step's pivots recorded
+  if (!active) return;
+  float* Xi = t.Xi;
+#pragma unroll
+  for (int ia = 0; ia < MA; ia++) {
+    const int i = lane + 32 * ia;
+    if (i >= r) continue;
+    const int ri = s_spinv[i];
+#pragma unroll
+    for (int c = 0; c < CW; c++) {
+      const int gc = CW * w + c;
+      if (gc < r) Xi[ri + (size_t)r * s_spiv[gc]] = a[ia][c];
+    }
+  }
+  if (info != 0 && lane == 0) atomicMax(err, (int)kDevSingular);
 }
 
 // ------------------------------------------------- multi-CTA dense helpers --
@@ -2720,16 +3123,24 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     const int few_rows = ((int)itasks.size() < n_sm && prm.rank_model) ? 384 : INT_MAX;
     std::vector<int> grp(itasks.size());
     std::vector<char> few(itasks.size(), 0);   // wide only for the level's few boxes
+    // KI_TC_SKETCH=1: FP32 sketched boxes of up to 256 columns form their
+    // sketch on the tensor cores (k_sketch_tc) instead of k_id's fold
+    const char* tc_env = std::getenv("KI_TC_SKETCH");
+    const bool tc_sketch = tc_env && std::string(tc_env) == "1";
     for (size_t i = 0; i < itasks.size(); i++) {
       int n = itasks[i].n;
       int md = id_smem_bytes<T>(n, 0) <= full_cap ? 0 : 1;
       const bool tall = mh[i] > kWideRows || (md == 1 && id_smem_bytes<T>(n, 2) > smem_cap);
       few[i] = !tall && mh[i] > few_rows;
       const bool wide = tall || few[i];
+      const bool tc = sizeof(T) == 4 && tc_sketch && prm.rank_model && !wide && md == 0 &&
+                      lh[i] > 0 && lh[i] < n && n <= 256;
       // narrow groups: 0 triangle in shared memory, 1 packed triangle in
-      // shared memory (mode 2 of k_id); wide groups: 2 / 3 by triangle size
-      grp[i] = wide ? 2 + md : md;
+      // shared memory (mode 2 of k_id), 4 tensor-core sketch then the
+      // pivoted QR of the sketch; wide groups: 2 / 3 by triangle size
+      grp[i] = wide ? 2 + md : (tc ? 4 : md);
     }
+    auto is_wide = [](int g) { return g == 2 || g == 3; };
     std::vector<int> mode_of(itasks.size());
     {
       std::vector<size_t> order(itasks.size());
@@ -2752,10 +3163,10 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         // (boxes routed wide only because the level is small keep the narrow
         // path's sketch size)
         int lo = lh[o];
-        if (grp[o] >= 2 && prm.rank_model && !few[o])
+        if (is_wide(grp[o]) && prm.rank_model && !few[o])
           lo = std::min(itasks[o].n, (int)std::ceil((1.f + 2 * prm.sketch_margin) * khat[o]) +
                                          2 * prm.sketch_oversample);
-        l2.push_back(grp[o] == 1 || (grp[o] >= 2 && lo > 384) ? 0 : lo);
+        l2.push_back(grp[o] == 1 || (is_wide(grp[o]) && lo > 384) ? 0 : lo);
         f2.insert(f2.end(), fh.begin() + kMlpIn * o, fh.begin() + kMlpIn * (o + 1));
       }
       itasks.swap(it2);
@@ -2821,13 +3232,44 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     F->fork();
     launch_range(0, 2, nullptr);
     launch_range(1, 2, nullptr);
+    if constexpr (sizeof(T) == 4) {
+      // tensor-core sketches (one CTA per box, by accumulator tiles), then
+      // the pivoted QR of each sketch, in order on one aux stream
+      std::vector<int> list[2];
+      for (size_t i = 0; i < itasks.size(); i++)
+        if (grp[i] == 4) list[itasks[i].n > 128].push_back((int)i);
+      if (!list[0].empty() || !list[1].empty()) {
+        cudaStream_t ts = F->aux[0];
+        std::string tn = "id_tc_sketch@L" + std::to_string(l);
+        double tc_flops = 0;   // Y = Omega M: 2 l m n per box
+        for (const auto& lst : list)
+          for (int i : lst) tc_flops += 2.0 * lh[i] * (double)mh[i] * itasks[i].n;
+        F->stage_begin(tn.c_str(), tc_flops, 0, ts);
+        for (int tl = 0; tl < 2; tl++) {
+          if (list[tl].empty()) continue;
+          int* d_list = (int*)F->alloc(sizeof(int) * list[tl].size());
+          upload(d_list, list[tl], ts);
+          int nq_max = 16;
+          for (int i : list[tl]) nq_max = std::max(nq_max, (lh[i] + 15) & ~15);
+          const size_t sm = tc_sketch_smem(tl + 1, nq_max);
+          auto kern = tl ? k_sketch_tc<2> : k_sketch_tc<1>;
+          KI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+          ki::launch(kern, (unsigned)list[tl].size(), kTcThreads, sm, ts, (const IdTask*)d_it,
+                     (const int*)d_list, (const int*)d_m, (const int*)d_lsk, (const int*)ipool,
+                     (const int*)d_irows, (float*)d_tws, P, sd, ptab, F->d_err);
+          KI_CUDA(cudaGetLastError());
+        }
+        F->stage_end(ts);
+        launch_range(4, 4, ts);
+      }
+    }
     // (d) wide boxes: explicit ID matrix, blocked Householder QR, then CPQR
     {
       std::vector<WideTask> wt, wsk;   // blocked-QR boxes, sketched boxes
       int64_t mtot = 0, ptot = 0;
       int maxn = 0, max_chunks = 0, max_cb = 0, max_l = 0;
       for (size_t i = 0; i < itasks.size(); i++) {
-        if (grp[i] < 2) continue;
+        if (!is_wide(grp[i])) continue;
         WideTask w{};
         w.task = (int)i;
         w.n = itasks[i].n;
@@ -2930,7 +3372,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       // boxes whose sketch did not reveal the rank (k = -1): the plain ID
       std::vector<int> fb;
       for (size_t i = 0; i < kh.size(); i++) {
-        if (lh[i] > 0 && (lh[i] < itasks[i].n || grp[i] >= 2)) F->n_sketched++;
+        if (lh[i] > 0 && (lh[i] < itasks[i].n || is_wide(grp[i]))) F->n_sketched++;
         if (kh[i] < 0) fb.push_back((int)i);
       }
       if (!fb.empty()) {
@@ -3151,6 +3593,11 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       if (n_sm > 0)
         KI_CUDA(cudaFuncSetAttribute(k_schur<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
       auto per_sm = [](size_t bytes) { return std::max(1, (int)(228 * 1024 / (bytes + 1024))); };
+      // FP32 Gauss-Jordan bins with redundant blocks of up to 128 rows: the
+      // products before and after the inverse in k_schur (phases 1 and 2),
+      // the inverse itself by k_gj (KI_SCHUR_SPLIT=0: all in k_schur)
+      const char* split_env = std::getenv("KI_SCHUR_SPLIT");
+      const bool split_ok = sizeof(T) == 4 && !(split_env && std::string(split_env) == "0");
       for (int b0 = 0; b0 < n_sm;) {
         const int ps = per_sm(schur_task_bytes<T>(st2[b0]));
         int b1 = b0 + 1;
@@ -3158,15 +3605,33 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         const size_t bsm = schur_task_bytes<T>(st2[b1 - 1]);
         // a bin of fewer boxes than SMs runs one CTA per SM whatever its footprint
         static const int n_sm = device_sm_count();
-        ki::launch(k_schur<T>, (unsigned)(b1 - b0), schur_threads<T>(b1 - b0 < n_sm ? 1 : ps), bsm,
-            F->aux[(next++) % Factorization<T>::kAux],
-            d_st, b0, 1, F->d_err);
+        const int thr = schur_threads<T>(b1 - b0 < n_sm ? 1 : ps);
+        cudaStream_t bst = F->aux[(next++) % Factorization<T>::kAux];
+        int r_max = 0;
+        bool all_gj = split_ok;
+        for (int q = b0; q < b1; q++) {
+          r_max = std::max(r_max, st2[q].n - st2[q].k);
+          all_gj = all_gj && st2[q].gj;
+        }
+        if (all_gj && r_max <= 128) {
+          ki::launch(k_schur<T>, (unsigned)(b1 - b0), thr, bsm, bst, d_st, b0, 1, F->d_err, 1);
+          if constexpr (sizeof(T) == 4) {
+            const SchurTask<float>* d_st32 = reinterpret_cast<const SchurTask<float>*>(d_st);
+            const int ma = (r_max + 31) / 32;
+            auto gj = ma <= 1 ? k_gj<1, kGjLeanCols> : ma == 2 ? k_gj<2, kGjLeanCols>
+                    : ma == 3 ? k_gj<3, kGjLeanCols> : k_gj<4, kGjLeanCols>;
+            ki::launch(gj, (unsigned)(b1 - b0), 32 * (32 * ma / kGjLeanCols), 0, bst, d_st32, b0, F->d_err);
+          }
+          ki::launch(k_schur<T>, (unsigned)(b1 - b0), thr, bsm, bst, d_st, b0, 1, F->d_err, 2);
+        } else {
+          ki::launch(k_schur<T>, (unsigned)(b1 - b0), thr, bsm, bst, d_st, b0, 1, F->d_err, 0);
+        }
         b0 = b1;
       }
       if (n_glob > 0)
         ki::launch(k_schur<T>, (unsigned)n_glob, schur_threads<T>(1), 0,
             F->aux[(next++) % Factorization<T>::kAux],
-            d_st, n_sm, 0, F->d_err);
+            d_st, n_sm, 0, F->d_err, 0);
       for (size_t q = n_sm + n_glob; q < st2.size(); q++)
         schur_wide<T>(st2[q], F->d_err, F->aux[(next++) % Factorization<T>::kAux]);
       F->join(Factorization<T>::kAux);
@@ -3340,6 +3805,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
   KI_CUDA(cudaMemcpyAsync(&herr, F->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
   KI_CUDA(cudaStreamSynchronize(s));
   F->factor_prof = F->collect();
+  if (herr == kDevTimeout)
+    throw std::runtime_error("a bounded device wait timed out (tensor-core sketch of an ID)");
   if (herr == kDevSingular) throw std::runtime_error("singular pivot in a Schur or root LU factorization");
   if (herr == kDevNonFinite) throw std::runtime_error("non-finite values in the factorization");
   F->factor_seconds =
@@ -3490,6 +3957,41 @@ void solve_device_arena(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, Scra
     throw;
   }
   F.stream = saved;
+}
+
+double tensor_core_selfcheck() {
+  const size_t nd = (size_t)kTcCheckRows * kTcCheckQ;
+  float* d = nullptr;
+  double* ref = nullptr;
+  int* err = nullptr;
+  KI_CUDA(cudaMalloc(&d, sizeof(float) * nd));
+  KI_CUDA(cudaMalloc(&ref, sizeof(double) * nd));
+  KI_CUDA(cudaMalloc(&err, sizeof(int)));
+  std::vector<float> hd(nd);
+  std::vector<double> hr(nd);
+  int herr = 0;
+  cudaError_t e = cudaMemset(err, 0, sizeof(int));
+  const size_t sm = tc_sketch_smem(2, kTcCheckQ);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_tc_selfcheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e == cudaSuccess) {
+    ki::launch(k_tc_selfcheck, 1, kTcThreads, sm, (cudaStream_t)0, d, ref, err);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(hd.data(), d, sizeof(float) * nd, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(hr.data(), ref, sizeof(double) * nd, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  cudaFree(ref);
+  cudaFree(err);
+  if (e != cudaSuccess) throw std::runtime_error(std::string("CUDA error: ") + cudaGetErrorString(e));
+  if (herr == kDevTimeout) throw std::runtime_error("the tensor-core self-check timed out");
+  double dmax = 0, rmax = 0;
+  for (size_t i = 0; i < nd; i++) {
+    dmax = std::max(dmax, std::fabs((double)hd[i] - hr[i]));
+    rmax = std::max(rmax, std::fabs(hr[i]));
+  }
+  return rmax > 0 ? dmax / rmax : dmax;
 }
 
 template size_t solve_arena_bytes<double>(const Factorization<double>&, int);

@@ -32,7 +32,7 @@ struct Params {
 
 // Device status word written by kernels that can fail (non-finite data,
 // singular pivot); read back by the host after each stage.
-enum DeviceError : int { kDevOk = 0, kDevNonFinite = 1, kDevSingular = 2 };
+enum DeviceError : int { kDevOk = 0, kDevNonFinite = 1, kDevSingular = 2, kDevTimeout = 3 };
 
 // Per-level description of the compressed boxes, kept for the solve sweeps.
 struct LevelFactor {
@@ -62,7 +62,9 @@ struct LevelStat {
   int level = 0, boxes = 0, id_boxes = 0, compressed = 0;
   int max_n = 0, max_m = 0, max_k = 0;
   double sum_n = 0, sum_m = 0, sum_k = 0;
-  int mode_count[4] = {0, 0, 0, 0};   // narrow/smem, narrow/global, wide/smem, wide/global
+  // narrow/smem, narrow/global, wide/smem, wide/global, narrow with a
+  // tensor-core sketch
+  int mode_count[5] = {0, 0, 0, 0, 0};
 };
 
 template <typename T>
@@ -172,6 +174,11 @@ struct ScratchArena {
     return base + off;
   }
 };
+
+// Runs the tensor-core sketch machinery (tcgen05 TF32 MMAs, TMEM
+// accumulators) on fixed data on the current device and returns its largest
+// difference from the same product in FP64, relative to the largest entry.
+double tensor_core_selfcheck();
 
 // Device bytes solve_device_arena takes from its arena for ncols columns
 // (including 256-byte alignment of every piece).
