@@ -899,154 +899,171 @@ __device__ __forceinline__ void tc_fill_block(float* a_hi, float* a_lo, float* b
   }
 }
 
-template <int TILES>
+// The product D = A B^T (A: rows x m, B: l x m, generated blockwise by
+// fill) of one CTA on the tensor cores.  Blocks of kTcRows columns of A and
+// B alternate between two operand stages and two TMEM accumulators, so that
+// the fill of a block overlaps the MMAs of the one before; each block's
+// partial sums are read back from TMEM and added in FP32 registers (round to
+// nearest), so TMEM accumulates only the 8 MMAs of one block.  Thread (warp
+// w, lane) owns row 32 (w % 4) + lane of each 128-row tile and the 16-column
+// chunks w / 4, w / 4 + 2, ..: CH of them (tiles x nq <= 32 CH).  The caller
+// provides 2 tc_sketch_smem(TILES, nq) bytes of dynamic shared memory.
+// Returns false when a bounded wait gave up.
+template <int TILES, int CH, typename Entry>
+__device__ __forceinline__ bool tc_sketch_core(unsigned char* smem, uint64_t* bar, uint32_t* tmem_slot,
+                                               int m, int l, int64_t act, Entry entry,
+                                               float (&acc)[CH][16]) {
+  const int nq = (l + 15) & ~15;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const size_t stage_floats = tc_sketch_smem(TILES, nq) / sizeof(float);
+  const int acc_cols = TILES * nq;   // TMEM columns of one accumulator
+  const uint32_t ncols = tc_tmem_cols(2 * acc_cols);
+  if (warp == 0) tc::tmem_alloc(tmem_slot, ncols);
+  if (tid == 0) {
+    tc::mbar_init(&bar[0], 1);
+    tc::mbar_init(&bar[1], 1);
+    tc::fence_mbar_init();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+  const int chunks = TILES * (nq / 16);
+#pragma unroll
+  for (int q = 0; q < CH; q++)
+#pragma unroll
+    for (int j = 0; j < 16; j++) acc[q][j] = 0.f;
+  uint32_t parity = 0;   // bit st: phase parity awaited on bar[st]
+  bool ok = true;
+  auto drain = [&](int st) {
+    ok = tc::mbar_wait(&bar[st], (parity >> st) & 1u, kTcWaitCycles) && ok;
+    parity ^= 1u << st;
+    tc::fence_after_sync();
+#pragma unroll
+    for (int q = 0; q < CH; q++) {
+      const int ch = (warp >> 2) + 2 * q;
+      if (ch < chunks) {   // uniform per warp
+        const int tt = ch / (nq / 16), q0 = (ch % (nq / 16)) * 16;
+        float v[16];
+        tc::tmem_ld16(tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
+                          (uint32_t)(st * acc_cols + tt * nq + q0), v);
+#pragma unroll
+        for (int j = 0; j < 16; j++) acc[q][j] += v[j];
+      }
+    }
+    tc::fence_before_sync();
+  };
+  int blk = 0;
+  for (int r0 = 0; r0 < m; r0 += kTcRows, blk++) {
+    const int st = blk & 1;
+    if (blk >= 2) drain(st);   // block blk - 2: its operands and accumulator are free
+    float* a_hi = reinterpret_cast<float*>(smem) + st * stage_floats;
+    float* a_lo = a_hi + TILES * 128 * kTcRows;
+    float* bs = a_lo + TILES * 128 * kTcRows;
+    tc_fill_block(a_hi, a_lo, bs, TILES, nq, [&](int c, int i) { return entry(c, r0 + i); }, act, r0, l);
+    tc::fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      tc_issue_block(tmem + st * acc_cols, a_hi, a_lo, bs, TILES, nq, true);
+      tc::mma_commit(&bar[st]);
+    }
+  }
+  // the last one or two blocks, in issue order
+  if (blk >= 2) drain(blk & 1);
+  if (blk >= 1) drain((blk + 1) & 1);
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+  return ok;
+}
+
+// Y = Omega M of one box per CTA (the boxes of `list`), written row-major
+// (l x n) into the task's global scratch.
+template <int TILES, int CH>
 __global__ void __launch_bounds__(kTcThreads) k_sketch_tc(const IdTask* tasks, const int* list,
                                                           const int* m_arr, const int* sketch_l,
                                                           const int* ipool, const int* iscratch,
                                                           float* tws, Points<float> P, int sol_dim,
                                                           ProxyTab<float> px, int* err) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
-  __shared__ uint64_t bar;
-  __shared__ uint32_t tmem_base;
+  __shared__ uint64_t bar[2];
+  __shared__ uint32_t tmem_slot;
   __shared__ ProxyBox<float> s_box;
   const int ti = list[blockIdx.x];
   const IdTask t = tasks[ti];
   const int n = t.n, m = m_arr[ti], l = sketch_l[ti];
   const int nq = (l + 15) & ~15;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nI = (m - (t.mode == 0 ? 2 * px.n * sol_dim : 0)) / 2;
   const int* rows = iscratch + t.rows;
   const int* act = ipool + t.act;
-  float* a_hi = reinterpret_cast<float*>(tc_smem);
-  float* a_lo = a_hi + TILES * 128 * kTcRows;
-  float* bs = a_lo + TILES * 128 * kTcRows;
-  const uint32_t ncols = tc_tmem_cols(TILES * nq);
-  if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
-  if (tid == 0) {
-    tc::mbar_init(&bar, 1);
-    tc::fence_mbar_init();
-    s_box = proxy_box<float>(t.cx, t.cy, t.cz, t.rad_proxy, px.n);
-  }
-  tc::fence_before_sync();
+  if (threadIdx.x == 0) s_box = proxy_box<float>(t.cx, t.cy, t.cz, t.rad_proxy, px.n);
   __syncthreads();
-  tc::fence_after_sync();
-  const uint32_t tmem = tmem_base;
   const ProxyBox<float> pb = s_box;
-  uint32_t phase = 0;
-  bool ok = true;
-  for (int r0 = 0; r0 < m; r0 += kTcRows) {
-    if (r0 > 0) {
-      // the previous block's MMAs have read the operands
-      ok = tc::mbar_wait(&bar, phase, kTcWaitCycles) && ok;
-      phase ^= 1;
-    }
-    tc_fill_block(a_hi, a_lo, bs, TILES, nq,
-                  [&](int c, int i) {
-                    const int row = r0 + i;
-                    return (c < n && row < m) ? id_entry<float>(P, sol_dim, row, nI, rows, act[c], px, pb)
-                                              : 0.f;
-                  },
-                  t.act, r0, l);
-    tc::fence_proxy_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-      tc::fence_after_sync();
-      tc_issue_block(tmem, a_hi, a_lo, bs, TILES, nq, r0 == 0);
-      tc::mma_commit(&bar);
-    }
-  }
-  ok = tc::mbar_wait(&bar, phase, kTcWaitCycles) && ok;
-  tc::fence_after_sync();
-  // Y^T in TMEM: lane = box column, column = sketch row; 16-column chunks,
-  // warps w and w + 4 share lanes 32 (w % 4).. and split the chunks
+  float acc[CH][16];
+  const bool ok = tc_sketch_core<TILES, CH>(
+      tc_smem, bar, &tmem_slot, m, l, t.act,
+      [&](int c, int row) {
+        return (c < n && row < m) ? id_entry<float>(P, sol_dim, row, nI, rows, act[c], px, pb) : 0.f;
+      },
+      acc);
+  // Y^T: lane = box column, chunk column = sketch row
   float* gws = tws + t.ws;
   const int chunks = TILES * (nq / 16);
-  for (int ch = warp >> 2; ch < chunks; ch += kTcThreads / 128) {
+#pragma unroll
+  for (int q = 0; q < CH; q++) {
+    const int ch = (warp >> 2) + 2 * q;
+    if (ch >= chunks) continue;
     const int tt = ch / (nq / 16), q0 = (ch % (nq / 16)) * 16;
-    float v[16];
-    tc::tmem_ld16(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(tt * nq + q0), v);
     const int c = tt * 128 + 32 * (warp & 3) + lane;
     if (ok && c < n) {
 #pragma unroll
       for (int j = 0; j < 16; j++)
-        if (q0 + j < l) gws[(size_t)(q0 + j) * n + c] = v[j];
+        if (q0 + j < l) gws[(size_t)(q0 + j) * n + c] = acc[q][j];
     }
   }
-  tc::fence_before_sync();
-  __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, ncols);
-  if (!ok && tid == 0) atomicMax(err, (int)kDevTimeout);
+  if (!ok && threadIdx.x == 0) atomicMax(err, (int)kDevTimeout);
 }
 
-// Self-check of the tensor-core sketch machinery on fixed data: two tiles
-// (M = 256 rows), nq = 48 columns, K = 64 (two blocks), the operands built
-// by tc_fill_block and multiplied by tc_issue_block exactly as k_sketch_tc
-// does; d (256 x 48, row-major) receives the TMEM result, ref the same
-// product summed in FP64 on the CUDA cores.
-constexpr int kTcCheckRows = 256, kTcCheckQ = 48, kTcCheckL = 45, kTcCheckK = 64;
+// Self-check of the tensor-core sketch routine on fixed data: two tiles
+// (256 rows), l = 45 sketch rows (nq = 48), 200 columns of A (7 blocks,
+// both stages and accumulators, a ragged last block); d (256 x 48,
+// row-major) receives the result, ref the same product summed in FP64 on the
+// CUDA cores.
+constexpr int kTcCheckRows = 256, kTcCheckQ = 48, kTcCheckL = 45, kTcCheckK = 200;
 __device__ __forceinline__ float tc_check_entry(int c, int i) {
   return __sinf(0.05f * c + 0.31f * i) * (1.0f + 0.001f * c) + 1e-3f * (float)((c * 7 + i * 13) % 17);
 }
 __global__ void __launch_bounds__(kTcThreads) k_tc_selfcheck(float* d, double* ref, int* err) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
-  __shared__ uint64_t bar;
-  __shared__ uint32_t tmem_base;
-  constexpr int TILES = 2, nq = kTcCheckQ, l = kTcCheckL;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  float* a_hi = reinterpret_cast<float*>(tc_smem);
-  float* a_lo = a_hi + TILES * 128 * kTcRows;
-  float* bs = a_lo + TILES * 128 * kTcRows;
-  const uint32_t ncols = tc_tmem_cols(TILES * nq);
-  if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
-  if (tid == 0) {
-    tc::mbar_init(&bar, 1);
-    tc::fence_mbar_init();
-  }
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
-  const uint32_t tmem = tmem_base;
-  uint32_t phase = 0;
-  bool ok = true;
+  __shared__ uint64_t bar[2];
+  __shared__ uint32_t tmem_slot;
+  constexpr int TILES = 2, nq = kTcCheckQ, CH = (TILES * nq + 31) / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t act = 12345;
-  for (int r0 = 0; r0 < kTcCheckK; r0 += kTcRows) {
-    if (r0 > 0) {
-      ok = tc::mbar_wait(&bar, phase, kTcWaitCycles) && ok;
-      phase ^= 1;
-    }
-    tc_fill_block(a_hi, a_lo, bs, TILES, nq, [&](int c, int i) { return tc_check_entry(c, r0 + i); },
-                  act, r0, l);
-    tc::fence_proxy_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-      tc::fence_after_sync();
-      tc_issue_block(tmem, a_hi, a_lo, bs, TILES, nq, r0 == 0);
-      tc::mma_commit(&bar);
-    }
-  }
-  ok = tc::mbar_wait(&bar, phase, kTcWaitCycles) && ok;
-  tc::fence_after_sync();
+  float acc[CH][16];
+  const bool ok = tc_sketch_core<TILES, CH>(
+      tc_smem, bar, &tmem_slot, kTcCheckK, kTcCheckL, act,
+      [&](int c, int i) { return i < kTcCheckK ? tc_check_entry(c, i) : 0.f; }, acc);
   const int chunks = TILES * (nq / 16);
-  for (int ch = warp >> 2; ch < chunks; ch += kTcThreads / 128) {
+#pragma unroll
+  for (int q = 0; q < CH; q++) {
+    const int ch = (warp >> 2) + 2 * q;
+    if (ch >= chunks) continue;
     const int tt = ch / (nq / 16), q0 = (ch % (nq / 16)) * 16;
-    float v[16];
-    tc::tmem_ld16(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(tt * nq + q0), v);
     const int c = tt * 128 + 32 * (warp & 3) + lane;
 #pragma unroll
-    for (int j = 0; j < 16; j++) d[(size_t)c * nq + q0 + j] = v[j];
+    for (int j = 0; j < 16; j++) d[(size_t)c * nq + q0 + j] = acc[q][j];
   }
-  tc::fence_before_sync();
-  __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, ncols);
   // the same product in FP64 on the CUDA cores
-  for (int e = tid; e < kTcCheckRows * nq; e += blockDim.x) {
+  for (int e = threadIdx.x; e < kTcCheckRows * nq; e += blockDim.x) {
     const int c = e / nq, q = e % nq;
-    double acc = 0.0;
-    if (q < l)
-      for (int i = 0; i < kTcCheckK; i++) acc += (double)tc_check_entry(c, i) * sketch_sign(act, i, q);
-    ref[e] = acc;
+    double a2 = 0.0;
+    if (q < kTcCheckL)
+      for (int i = 0; i < kTcCheckK; i++) a2 += (double)tc_check_entry(c, i) * sketch_sign(act, i, q);
+    ref[e] = a2;
   }
-  if (!ok && tid == 0) atomicMax(err, (int)kDevTimeout);
+  if (!ok && threadIdx.x == 0) atomicMax(err, (int)kDevTimeout);
 }
 
 // Features of the learned rank predictor for every ID box of a level (one
@@ -3134,7 +3151,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       few[i] = !tall && mh[i] > few_rows;
       const bool wide = tall || few[i];
       const bool tc = sizeof(T) == 4 && tc_sketch && prm.rank_model && !wide && md == 0 &&
-                      lh[i] > 0 && lh[i] < n && n <= 256;
+                      lh[i] > 0 && lh[i] < n && n <= 256 &&
+                      (n > 128 ? 2 : 1) * ((lh[i] + 15) & ~15) <= 128;
       // narrow groups: 0 triangle in shared memory, 1 packed triangle in
       // shared memory (mode 2 of k_id), 4 tensor-core sketch then the
       // pivoted QR of the sketch; wide groups: 2 / 3 by triangle size
@@ -3251,8 +3269,10 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
           upload(d_list, list[tl], ts);
           int nq_max = 16;
           for (int i : list[tl]) nq_max = std::max(nq_max, (lh[i] + 15) & ~15);
-          const size_t sm = tc_sketch_smem(tl + 1, nq_max);
-          auto kern = tl ? k_sketch_tc<2> : k_sketch_tc<1>;
+          const size_t sm = 2 * tc_sketch_smem(tl + 1, nq_max);   // two stages
+          const int ch = ((tl + 1) * nq_max + 31) / 32;   // accumulator chunks per thread
+          auto kern = tl ? (ch <= 2 ? k_sketch_tc<2, 2> : k_sketch_tc<2, 4>)
+                         : (ch <= 1 ? k_sketch_tc<1, 1> : ch <= 2 ? k_sketch_tc<1, 2> : k_sketch_tc<1, 4>);
           KI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
           ki::launch(kern, (unsigned)list[tl].size(), kTcThreads, sm, ts, (const IdTask*)d_it,
                      (const int*)d_list, (const int*)d_m, (const int*)d_lsk, (const int*)ipool,
@@ -3260,7 +3280,14 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
           KI_CUDA(cudaGetLastError());
         }
         F->stage_end(ts);
-        launch_range(4, 4, ts);
+        // the pivoted QRs of the sketches, size bins spread over the aux
+        // streams (each after the sketches)
+        cudaEvent_t tev;
+        KI_CUDA(cudaEventCreateWithFlags(&tev, cudaEventDisableTiming));
+        KI_CUDA(cudaEventRecord(tev, ts));
+        for (int i = 1; i + 1 < Factorization<T>::kAux; i++) KI_CUDA(cudaStreamWaitEvent(F->aux[i], tev, 0));
+        KI_CUDA(cudaEventDestroy(tev));
+        launch_range(4, 4, nullptr);
       }
     }
     // (d) wide boxes: explicit ID matrix, blocked Householder QR, then CPQR
@@ -3971,7 +3998,7 @@ double tensor_core_selfcheck() {
   std::vector<double> hr(nd);
   int herr = 0;
   cudaError_t e = cudaMemset(err, 0, sizeof(int));
-  const size_t sm = tc_sketch_smem(2, kTcCheckQ);
+  const size_t sm = 2 * tc_sketch_smem(2, kTcCheckQ);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_tc_selfcheck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e == cudaSuccess) {
