@@ -1025,6 +1025,188 @@ __global__ void __launch_bounds__(kTcThreads) k_sketch_tc(const IdTask* tasks, c
   if (!ok && threadIdx.x == 0) atomicMax(err, (int)kDevTimeout);
 }
 
+// Column-pivoted Householder QR of a box's sketch Y (l x n, row-major at the
+// start of the task's global scratch; l <= LMAX, n <= 256) and its
+// interpolation matrix, with k_id's semantics: xGEQP3 / xLAQP2 pivot order
+// (first logical column of largest partial norm) and norm downdating with
+// recomputation after cancellation, rank k = first j >= 1 with
+// |R_jj| < tol |R_00|, and a sketch that does not reveal the rank within l
+// pivots flagged k = -1 (the plain ID then recompresses the box).  One CTA
+// per box, lane = column of its warp's 32-column slab, the column in
+// registers.  Columns do not move: each keeps its logical position, which
+// is swapped as xGEQP3 swaps columns; perm (logical -> column) lives in
+// shared memory.  Two barriers per pivot among the box's warps.  Then
+// T = R11^-1 R12 by back substitution, every redundant column in its own
+// lane, R's first k rows staged in shared memory (dynamic: l x n floats).
+template <int LMAX>
+__global__ void __launch_bounds__(256) k_cpqr(const IdTask* tasks, const int* list, const int* sketch_l,
+                                              int* ipool, int* iscratch, float* tws, double tol,
+                                              int* k_out) {
+  extern __shared__ __align__(16) float cq_smem[];   // Rs: l x n (row a, column c)
+  __shared__ float s_wbest[8];
+  __shared__ int s_wpos[8];
+  __shared__ float s_u[LMAX];
+  __shared__ float s_tau, s_beta;
+  __shared__ int s_perm[256];
+  __shared__ int s_k;
+  const int ti = list[blockIdx.x];
+  const IdTask t = tasks[ti];
+  const int n = t.n, l = sketch_l[ti];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, W = blockDim.x >> 5;
+  const int c = 32 * w + lane;            // this lane's column
+  const bool has = c < n;
+  float* gws = tws + t.ws;
+  float y[LMAX];
+#pragma unroll
+  for (int i = 0; i < LMAX; i++) y[i] = (has && i < l) ? gws[(size_t)i * n + c] : 0.f;
+  float vn1 = 0.f;
+#pragma unroll
+  for (int i = 0; i < LMAX; i++) vn1 = fmaf(y[i], y[i], vn1);
+  vn1 = sqrtf(vn1);
+  float vn2 = vn1;
+  int pos = c;                            // logical position of this column
+  for (int e = threadIdx.x; e < n; e += blockDim.x) s_perm[e] = e;
+  if (threadIdx.x == 0) s_k = 0;
+  __syncthreads();
+  const float ftol = (float)tol;
+  float thresh = 0.f;
+  const int jmax = min(n, l);
+  int k = 0;
+  bool done = false;
+  for (int j = 0; j < jmax && !done; j++) {
+    // 1. pivot: largest vn1 over logical positions >= j, ties to the lowest
+    float best = -1.f;
+    int bpos = n;
+    if (has && pos >= j) { best = vn1; bpos = pos; }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int op = __shfl_xor_sync(0xffffffffu, bpos, o);
+      if (ob > best || (ob == best && op < bpos)) { best = ob; bpos = op; }
+    }
+    if (lane == 0) { s_wbest[w] = best; s_wpos[w] = bpos; }
+    __syncthreads();
+    best = s_wbest[0];
+    bpos = s_wpos[0];
+    for (int q = 1; q < W; q++) {
+      const float ob = s_wbest[q];
+      const int op = s_wpos[q];
+      if (ob > best || (ob == best && op < bpos)) { best = ob; bpos = op; }
+    }
+    const int pc = s_perm[bpos], qc = s_perm[j];   // pivot column, column at position j
+    // xGEQP3's interchange of logical positions j and bpos
+    if (c == pc) pos = j;
+    else if (c == qc) pos = bpos;
+    // 2. the pivot column's reflector (rows j..l-1), by its lane
+    if (c == pc) {
+      float sg = 0.f, alpha = 0.f;
+#pragma unroll
+      for (int i = 0; i < LMAX; i++) {
+        if (i > j && i < l) sg = fmaf(y[i], y[i], sg);
+        if (i == j) alpha = y[i];
+      }
+      float tau = 0.f, beta = alpha, scale = 0.f;
+      if (sg != 0.f) {
+        const float nrm = sqrtf(alpha * alpha + sg);
+        beta = alpha >= 0.f ? -nrm : nrm;
+        tau = (beta - alpha) / beta;
+        scale = 1.f / (alpha - beta);
+      }
+#pragma unroll
+      for (int i = 0; i < LMAX; i++) {
+        if (i > j && i < l) s_u[i] = y[i] * scale;
+        if (i == j) y[i] = beta;
+      }
+      s_tau = tau;
+      s_beta = beta;
+    }
+    __syncthreads();
+    // every thread has read perm[j], perm[bpos]: apply the interchange (read
+    // after the next step's first barrier)
+    if (c == pc) {
+      s_perm[j] = pc;
+      s_perm[bpos] = qc;
+    }
+    const float beta = s_beta, tau = s_tau;
+    if (j == 0) thresh = fabsf(ftol * beta);
+    if (j >= 1 && fabsf(beta) < thresh) {
+      k = j;
+      done = true;
+      break;
+    }
+    // 3. the remaining columns: y -= tau (u . y) u on rows j..l-1, then
+    // their norms downdated (xLAQP2)
+    if (has && pos > j && tau != 0.f) {
+      float wsum = 0.f;
+#pragma unroll
+      for (int i = 0; i < LMAX; i++) {
+        if (i == j) wsum += y[i];
+        else if (i > j && i < l) wsum = fmaf(s_u[i], y[i], wsum);
+      }
+      wsum *= tau;
+#pragma unroll
+      for (int i = 0; i < LMAX; i++) {
+        if (i == j) y[i] -= wsum;
+        else if (i > j && i < l) y[i] = fmaf(-wsum, s_u[i], y[i]);
+      }
+    }
+    if (has && pos > j && vn1 != 0.f) {
+      float rjc = 0.f;
+#pragma unroll
+      for (int i = 0; i < LMAX; i++) rjc = (i == j) ? y[i] : rjc;
+      float temp = fabsf(rjc) / vn1;
+      temp = 1.f - temp * temp;
+      temp = temp < 0.f ? 0.f : temp;
+      const float qv = vn1 / vn2;
+      const float temp2 = temp * qv * qv;
+      if (temp2 <= tol3z<float>()) {
+        float s2 = 0.f;
+#pragma unroll
+        for (int i = 0; i < LMAX; i++)
+          if (i > j && i < l) s2 = fmaf(y[i], y[i], s2);
+        vn1 = sqrtf(s2);
+        vn2 = vn1;
+      } else {
+        vn1 = vn1 * sqrtf(temp);
+      }
+    }
+  }
+  int* gperm = iscratch + t.perm;
+  if (!done && jmax == l && l < n) {
+    // the sketch did not reveal the rank: recompress with the plain ID
+    if (threadIdx.x == 0) k_out[ti] = -1;
+    return;
+  }
+  __syncthreads();   // final perm
+  if (threadIdx.x == 0) k_out[ti] = k;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) gperm[e] = s_perm[e];
+  if (k == 0) return;
+  // R's first k rows (columns in place) into shared memory
+  float* Rs = cq_smem;
+  if (has) {
+#pragma unroll
+    for (int i = 0; i < LMAX; i++)
+      if (i < k) Rs[(size_t)i * n + c] = y[i];
+  }
+  __syncthreads();
+  // T(:, q - k) = R11^-1 R(0:k, column at position q), q >= k: back
+  // substitution over the column's own entries in Rs, R11(a, b) =
+  // Rs[a][perm[b]] (broadcast reads)
+  float* Tout = gws + (size_t)n * n;
+  if (has && pos >= k) {
+    for (int a = k - 1; a >= 0; a--) {
+      float s = Rs[(size_t)a * n + c];
+      for (int b = a + 1; b < k; b++) s = fmaf(-Rs[(size_t)a * n + s_perm[b]], Rs[(size_t)b * n + c], s);
+      s = s / Rs[(size_t)a * n + s_perm[a]];
+      Rs[(size_t)a * n + c] = s;
+      Tout[a + (size_t)k * (pos - k)] = s;
+    }
+  }
+  int* pact = ipool + t.pact;
+  const int* act = ipool + t.act;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) pact[e] = act[s_perm[e]];
+}
+
 // Self-check of the tensor-core sketch routine on fixed data: two tiles
 // (256 rows), l = 45 sketch rows (nq = 48), 200 columns of A (7 blocks,
 // both stages and accumulators, a ragged last block); d (256 x 48,
@@ -3151,7 +3333,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       few[i] = !tall && mh[i] > few_rows;
       const bool wide = tall || few[i];
       const bool tc = sizeof(T) == 4 && tc_sketch && prm.rank_model && !wide && md == 0 &&
-                      lh[i] > 0 && lh[i] < n && n <= 256 &&
+                      lh[i] > 0 && lh[i] < n && lh[i] <= 64 && n <= 256 &&
                       (n > 128 ? 2 : 1) * ((lh[i] + 15) & ~15) <= 128;
       // narrow groups: 0 triangle in shared memory, 1 packed triangle in
       // shared memory (mode 2 of k_id), 4 tensor-core sketch then the
@@ -3280,14 +3462,33 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
           KI_CUDA(cudaGetLastError());
         }
         F->stage_end(ts);
-        // the pivoted QRs of the sketches, size bins spread over the aux
-        // streams (each after the sketches)
-        cudaEvent_t tev;
-        KI_CUDA(cudaEventCreateWithFlags(&tev, cudaEventDisableTiming));
-        KI_CUDA(cudaEventRecord(tev, ts));
-        for (int i = 1; i + 1 < Factorization<T>::kAux; i++) KI_CUDA(cudaStreamWaitEvent(F->aux[i], tev, 0));
-        KI_CUDA(cudaEventDestroy(tev));
-        launch_range(4, 4, nullptr);
+        // the pivoted QRs of the sketches (k_cpqr), by sketch rows (32 / 64)
+        // and 32-column slabs
+        std::vector<int> cls[2][8];
+        for (const auto& lst : list)
+          for (int i : lst) cls[lh[i] > 32][(itasks[i].n + 31) / 32 - 1].push_back(i);
+        std::string qn = "id_cpqr@L" + std::to_string(l);
+        F->stage_begin(qn.c_str(), 0, 0, ts);
+        for (int lb = 0; lb < 2; lb++)
+          for (int wq = 0; wq < 8; wq++) {
+            const auto& v = cls[lb][wq];
+            if (v.empty()) continue;
+            int* d_l2 = (int*)F->alloc(sizeof(int) * v.size());
+            upload(d_l2, v, ts);
+            int lm = 0, nm = 0;
+            for (int i : v) {
+              lm = std::max(lm, lh[i]);
+              nm = std::max(nm, itasks[i].n);
+            }
+            const size_t sm = sizeof(float) * (size_t)lm * nm;
+            auto kern = lb ? k_cpqr<64> : k_cpqr<32>;
+            if (sm > 48 * 1024)
+              KI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            ki::launch(kern, (unsigned)v.size(), 32 * (wq + 1), sm, ts, (const IdTask*)d_it,
+                       (const int*)d_l2, (const int*)d_lsk, ipool, d_irows, (float*)d_tws, prm.id_tol, d_k);
+            KI_CUDA(cudaGetLastError());
+          }
+        F->stage_end(ts);
       }
     }
     // (d) wide boxes: explicit ID matrix, blocked Householder QR, then CPQR
