@@ -1621,9 +1621,9 @@ int ki_factor_get_profile(ki_factor* f, char* buf, int len) {
       char host[384];
       snprintf(host, sizeof(host),
                "{\"create_prep_ms\": %.3f, \"factor_call_ms\": %.3f, \"tree_ms\": %.3f, "
-               "\"tree_codes_ms\": %.3f, \"fmm_wait_ms\": %.3f}",
+               "\"tree_gpu_ms\": %.3f, \"tree_built_on_gpu\": %d, \"fmm_wait_ms\": %.3f}",
                f->host_prep_ms, f->host_factor_ms, F.tree_seconds * 1e3,
-               F.tree_codes_seconds * 1e3, f->fmm_wait_ms);
+               F.tree_codes_seconds * 1e3, F.tree_gpu ? 1 : 0, f->fmm_wait_ms);
       j = "{\"factor\": " + dump(F.factor_prof) + ", \"solve\": " + dump(F.solve_prof) +
           ", \"refine\": " + dump(f->refine_prof) + ", \"levels\": " + lv +
           ", \"host\": " + host + "}";

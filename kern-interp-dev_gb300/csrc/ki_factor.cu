@@ -2987,9 +2987,9 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     }
     KI_CUDA(cudaGetLastError());
   }
-  // the tree: descent codes sorted on the GPU, boxes and lists on the host
-  // (KI_TREE_BUILD=host: the host partition build, also the fallback when
-  // the codes' depth does not reach the leaves)
+  // the tree on the GPU: descent codes, their sort, boxes, neighbour lists
+  // and leaf DOF lists (KI_TREE_BUILD=host: the host partition build, also
+  // the fallback when the codes' depth does not reach the leaves)
   {
     const char* tb = std::getenv("KI_TREE_BUILD");
     bool built = false;
@@ -2997,13 +2997,10 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       double c0 = 0, side0 = 0;
       tree_root(points, n_points, dim, &c0, &side0);
       const int depth = tree_code_depth(dim);
-      std::vector<uint64_t> codes(n_points);
-      std::vector<int> order(n_points);
-      tree_codes_sorted(d_pts_in, n_points, dim, c0, side0, depth, codes.data(), order.data(), s);
+      built = tree_build_gpu(d_pts_in, n_points, dim, prm.sol_dim, prm.max_leaf_dofs, c0, side0,
+                             depth, &tree, s);
       F->tree_codes_seconds =
           std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
-      built = tree.build_from_codes(n_points, dim, prm.sol_dim, prm.max_leaf_dofs, codes.data(),
-                                    order.data(), depth, c0, side0);
     }
     if (!built) tree.build(points, n_points, dim, prm.sol_dim, prm.max_leaf_dofs);
     F->tree_gpu = built;
@@ -3232,8 +3229,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         it.mode = 0;
         it.rad_filter = std::sqrt((double)dim) * prm.radius_ratio * (bx.side / 2);
         it.rad_proxy = (bx.side / 2) * std::sqrt((double)dim) * prm.radius_ratio;
-        for (int o : bx.coarse_nbrs) add_seg(tree.boxes[o].orig_start, tree.boxes[o].orig_count);
-        for (int o : bx.same_nbrs) {
+        for (int o : tree.coarse_nbrs(b)) add_seg(tree.boxes[o].orig_start, tree.boxes[o].orig_count);
+        for (int o : tree.same_nbrs(b)) {
           const Box& ob = tree.boxes[o];
           if (ob.leaf) add_seg(ob.orig_start, ob.orig_count);
           else add_seg(hb[o].act, hb[o].n);

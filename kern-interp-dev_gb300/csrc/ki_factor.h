@@ -126,8 +126,8 @@ struct Factorization {
   std::vector<StageSum> collect();   // synchronizes the stream
   double factor_seconds = 0;
   double tree_seconds = 0;   // tree build (codes on the GPU, boxes on the host)
-  bool tree_gpu = false;      // the codes path built the tree (else the host partition)
-  double tree_codes_seconds = 0;   // from the start of the factorization to the sorted codes on the host
+  bool tree_gpu = false;      // the tree was built on the GPU (else by the host partition)
+  double tree_codes_seconds = 0;   // from the start of the factorization to the GPU-built tree on the host
   size_t device_bytes = 0;
   std::vector<void*> owned;   // device allocations to free
 

@@ -135,87 +135,6 @@ void Tree::build(const double* pts, int n_points_, int dim_, int sol_dim_, int m
   finish(work, range);
 }
 
-bool Tree::build_from_codes(int n_points_, int dim_, int sol_dim_, int max_leaf_dofs_,
-                            const uint64_t* codes, const int* order, int depth, double c0,
-                            double side0) {
-  check_args(dim_, n_points_, max_leaf_dofs_);
-  dim = dim_;
-  n_points = n_points_;
-  sol_dim = sol_dim_;
-  n_dofs = n_points * sol_dim;
-  max_leaf_dofs = max_leaf_dofs_;
-  boxes.clear();
-  levels.clear();
-  const int nch = 1 << dim;
-  std::vector<std::pair<int, int>> range;
-  boxes.reserve((size_t)2 * nch * (n_points / max_leaf_dofs + 1) + 1);
-  range.reserve(boxes.capacity());
-  Box root;
-  root.level = 0;
-  for (int d = 0; d < dim; d++) root.c[d] = c0;
-  root.side = side0;
-  root.orig_count = n_dofs;
-  boxes.push_back(root);
-  range.push_back({0, n_points});
-  levels.push_back({0});
-  std::vector<int> starts;
-  for (size_t l = 0; l < levels.size(); l++) {
-    const std::vector<int>& lv = levels[l];
-    // the child boundaries of every box of the level that splits (binary
-    // searches, in parallel): the range shares the codes' first l digits and
-    // digit l + 1 ascends
-    const int shift = dim * (depth - 1 - (int)l);
-    starts.assign(lv.size() * (nch + 1), -1);
-    std::atomic<bool> too_deep(false);
-    parallel_ranges((int)lv.size(), [&](int i0, int i1) {
-      for (int i = i0; i < i1; i++) {
-        const int b = lv[i];
-        if (boxes[b].orig_count <= max_leaf_dofs) continue;
-        if ((int)l >= depth) {
-          too_deep = true;
-          continue;
-        }
-        int* st = starts.data() + (size_t)i * (nch + 1);
-        const int lo = range[b].first, hi = range[b].second;
-        st[0] = lo;
-        st[nch] = hi;
-        for (int ci = 1; ci < nch; ci++)
-          st[ci] = (int)(std::partition_point(codes + st[ci - 1], codes + hi,
-                                              [&](uint64_t k) {
-                                                return (int)((k >> shift) & (nch - 1)) < ci;
-                                              }) -
-                         codes);
-      }
-    }, 1024);
-    if (too_deep) {   // the codes end here: the caller builds by partition
-      boxes.clear();
-      levels.clear();
-      return false;
-    }
-    std::vector<int> next;
-    for (size_t i = 0; i < lv.size(); i++) {
-      const int* st = starts.data() + i * (nch + 1);
-      if (st[0] < 0) continue;
-      const int b = lv[i];
-      boxes[b].leaf = false;
-      for (int ci = 0; ci < nch; ci++) {
-        const int id = add_child(&boxes, b, ci, (int)l + 1, dim, (st[ci + 1] - st[ci]) * sol_dim);
-        range.push_back({st[ci], st[ci + 1]});
-        next.push_back(id);
-      }
-    }
-    if (!next.empty()) levels.push_back(next);
-  }
-  // a leaf's points ascending by index (the codes ordered them by deeper digits)
-  std::vector<int> work(order, order + n_points);
-  parallel_ranges((int)boxes.size(), [&](int b0, int b1) {
-    for (int b = b0; b < b1; b++)
-      if (boxes[b].leaf) std::sort(work.begin() + range[b].first, work.begin() + range[b].second);
-  });
-  finish(work, range);
-  return true;
-}
-
 void Tree::finish(const std::vector<int>& work, const std::vector<std::pair<int, int>>& range) {
   const int nch = 1 << dim;
   // Leaf DOF ranges in depth-first order.  Both builds keep `work` in that
@@ -241,36 +160,51 @@ void Tree::finish(const std::vector<int>& work, const std::vector<std::pair<int,
   // parent's same-level neighbours' children (centre distance below
   // side*sqrt(dim)); a box's coarser touching leaves are found among the
   // parent's coarser leaves and the parent's same-level neighbours that are
-  // leaves.
+  // leaves.  Flat storage, tree_nbr_cap(dim) slots per box.
+  const int cap = tree_nbr_cap(dim);
+  nbr_same.assign(boxes.size() * (size_t)cap, -1);
+  nbr_coarse.assign(boxes.size() * (size_t)cap, -1);
+  n_same.assign(boxes.size(), 0);
+  n_coarse.assign(boxes.size(), 0);
   const double sq = std::sqrt((double)dim);
+  std::atomic<bool> overflow(false);
   for (size_t l = 1; l < levels.size(); l++) {
     const std::vector<int>& lv = levels[l];
     parallel_ranges((int)lv.size(), [&](int i0, int i1) {
     for (int i = i0; i < i1; i++) {
       const int b = lv[i];
-      Box& bx = boxes[b];
+      const Box& bx = boxes[b];
       const Box& par = boxes[bx.parent];
-      bx.same_nbrs.reserve(dim == 2 ? 8 : 26);   // at most the 3^dim - 1 surrounding boxes
+      int* same = nbr_same.data() + (size_t)b * cap;
+      int* coarse = nbr_coarse.data() + (size_t)b * cap;
+      int ns = 0, nc = 0;
+      auto push = [&](int* list, int* cnt, int v) {
+        if (*cnt < cap) list[(*cnt)++] = v;
+        else overflow = true;
+      };
       for (int ci = 0; ci < nch; ci++)
-        if (par.child[ci] != b) bx.same_nbrs.push_back(par.child[ci]);
-      for (int pn : par.same_nbrs) {
+        if (par.child[ci] != b) push(same, &ns, par.child[ci]);
+      for (int pn : same_nbrs(bx.parent)) {
         const Box& pb = boxes[pn];
         if (pb.leaf) {
-          if (touching(bx, pb, dim)) bx.coarse_nbrs.push_back(pn);
+          if (touching(bx, pb, dim)) push(coarse, &nc, pn);
           continue;
         }
         for (int ci = 0; ci < nch; ci++) {
           const Box& cb = boxes[pb.child[ci]];
           double d2 = 0;
           for (int d = 0; d < dim; d++) d2 += (bx.c[d] - cb.c[d]) * (bx.c[d] - cb.c[d]);
-          if (std::sqrt(d2) < bx.side * sq + 1e-9) bx.same_nbrs.push_back(pb.child[ci]);
+          if (std::sqrt(d2) < bx.side * sq + 1e-9) push(same, &ns, pb.child[ci]);
         }
       }
-      for (int pn : par.coarse_nbrs)
-        if (touching(bx, boxes[pn], dim)) bx.coarse_nbrs.push_back(pn);
+      for (int pn : coarse_nbrs(bx.parent))
+        if (touching(bx, boxes[pn], dim)) push(coarse, &nc, pn);
+      n_same[b] = ns;
+      n_coarse[b] = nc;
     }
     });
   }
+  if (overflow) throw std::logic_error("tree: more neighbours than 3^dim - 1");
 }
 
 }  // namespace ki

@@ -34,9 +34,21 @@ struct Box {
   int orig_start = 0;   // leaf DOF range in dof_sorted (leaves only)
   int orig_count = 0;   // DOFs in the box (all boxes)
   int level_pos = 0;    // index within levels[level]
-  std::vector<int> same_nbrs;    // neighbouring boxes of the same level
-  std::vector<int> coarse_nbrs;  // touching leaves of coarser levels
 };
+
+// A box's neighbour list: a view into the tree's flat storage.
+struct IdList {
+  const int* p = nullptr;
+  int n = 0;
+  const int* begin() const { return p; }
+  const int* end() const { return p + n; }
+  int size() const { return n; }
+};
+
+// Neighbours per box are bounded by the 3^dim - 1 cells around it: the
+// same-level ones within side*sqrt(dim), and the touching coarser leaves
+// (each larger than the box, so one per direction).
+inline int tree_nbr_cap(int dim) { return dim == 2 ? 8 : 26; }
 
 struct Tree {
   int dim = 2, n_points = 0, sol_dim = 1, n_dofs = 0;
@@ -44,20 +56,22 @@ struct Tree {
   std::vector<Box> boxes;
   std::vector<std::vector<int>> levels;   // box ids per level, Morton order
   std::vector<int> dof_sorted;            // leaves' DOFs, leaf after leaf
+  // neighbour lists, tree_nbr_cap(dim) slots per box: same-level
+  // neighbours and touching leaves of coarser levels, with their counts
+  std::vector<int> nbr_same, nbr_coarse;
+  std::vector<int> n_same, n_coarse;
 
   int n_children() const { return 1 << dim; }
+  // neighbouring boxes of the same level
+  IdList same_nbrs(int b) const {
+    return IdList{nbr_same.data() + (size_t)b * tree_nbr_cap(dim), n_same[b]};
+  }
+  // touching leaves of coarser levels
+  IdList coarse_nbrs(int b) const {
+    return IdList{nbr_coarse.data() + (size_t)b * tree_nbr_cap(dim), n_coarse[b]};
+  }
   // points: interleaved (x, y[, z]), n_points of them; dim 2 or 3.
   void build(const double* points, int n_points, int dim, int sol_dim, int max_leaf_dofs);
-  // The same tree from the points' descent codes: code = the child indices
-  // of the boxes containing the point at levels 1..depth, dim bits each,
-  // level 1 most significant (computed with tree_root's box and the split
-  // rule's centre arithmetic), sorted ascending with ties by point index,
-  // `order` the point indices in that order.  Returns false (tree left
-  // empty) when a box at level `depth` would still be split.
-  // centre / side: the root box tree_root gave for these points.
-  bool build_from_codes(int n_points, int dim, int sol_dim, int max_leaf_dofs,
-                        const uint64_t* codes, const int* order, int depth, double centre,
-                        double side);
   int num_levels() const { return (int)levels.size(); }
 
  private:
