@@ -37,12 +37,28 @@ inline int child_of(const double* p, const double* c, int dim) {
 
 void tree_root(const double* pts, int n_points, int dim, double* centre, double* side) {
   if (n_points <= 0) throw std::invalid_argument("no boundary points");
-  double mn = pts[0], mx = pts[0];
-  for (int i = 0; i < dim * n_points; i++) {
-    if (!std::isfinite(pts[i])) throw std::invalid_argument("non-finite boundary coordinate");
-    mn = std::min(mn, pts[i]);
-    mx = std::max(mx, pts[i]);
-  }
+  // min and max over every coordinate, in parallel chunks (exact, so the
+  // result does not depend on the split)
+  const int n = dim * n_points;
+  const int chunk = 1 << 16, nchunk = (n + chunk - 1) / chunk;
+  std::vector<double> cmn(nchunk), cmx(nchunk);
+  std::atomic<bool> bad(false);
+  parallel_ranges(nchunk, [&](int c0, int c1) {
+    for (int c = c0; c < c1; c++) {
+      double mn = pts[(size_t)c * chunk], mx = mn;
+      const int e = std::min(n, (c + 1) * chunk);
+      for (int i = c * chunk; i < e; i++) {
+        if (!std::isfinite(pts[i])) bad = true;
+        mn = std::min(mn, pts[i]);
+        mx = std::max(mx, pts[i]);
+      }
+      cmn[c] = mn;
+      cmx[c] = mx;
+    }
+  }, 2);
+  if (bad) throw std::invalid_argument("non-finite boundary coordinate");
+  const double mn = *std::min_element(cmn.begin(), cmn.end());
+  const double mx = *std::max_element(cmx.begin(), cmx.end());
   const double tmin = mn - 0.01, tmax = mx + 0.01;
   *centre = (tmin + tmax) / 2.0;
   *side = tmax - tmin;

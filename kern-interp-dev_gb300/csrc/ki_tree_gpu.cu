@@ -330,6 +330,10 @@ __global__ void k_tree_leaf_sort(const int* leaf_list, int nleaf, const int* lo,
   }
 }
 
+__global__ void k_tree_fill(int* a, int n, int v) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = v;
+}
+
 __global__ void k_tree_dofs(const int* order, int n, int sol_dim, int* dofs) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n * sol_dim; i += gridDim.x * blockDim.x)
     dofs[i] = order[i / sol_dim] * sol_dim + i % sol_dim;
@@ -451,14 +455,12 @@ bool tree_build_gpu(const double* d_points, int n, int dim, int sol_dim, int max
                  split + base, rank, dim, shift, side_of[l], next_base, child, lo + next_base,
                  hi + next_base, cen + (size_t)dim * next_base, parent + next_base, base);
       KI_TREE_CUDA(cudaGetLastError());
-      std::vector<int> lev(next_cnt, l + 1);
-      KI_TREE_CUDA(cudaMemcpyAsync(level_of + next_base, lev.data(), sizeof(int) * next_cnt,
-                                   cudaMemcpyHostToDevice, s));
+      ki::launch(k_tree_fill, std::min(1024, (next_cnt + 255) / 256), 256, 0, s, level_of + next_base,
+                 next_cnt, l + 1);
       lbase.push_back(next_base);
       lcount.push_back(next_cnt);
       side_of.push_back(side_of[l] / 2.0);
       total = next_base + next_cnt;
-      KI_TREE_CUDA(cudaStreamSynchronize(s));   // lev leaves scope
     }
     const int L = (int)lbase.size();
     // split flags of the last level were written by its flag launch; leaf = !split
