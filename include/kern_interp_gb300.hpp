@@ -215,6 +215,15 @@ class QuadTree {
     domain_dimension = domain_dimension_;
   }
 
+  // QuadTree::perturb (quadtree.cpp:581-890): the tree now describes
+  // new_boundary (points identified by index; the boundary must outlive the
+  // tree's use of it), and the next skeletonize keeps the factors of the
+  // boxes the change left alone (ki_factor_update).
+  void perturb(const Boundary& new_boundary) {
+    if (!boundary_) throw std::invalid_argument("perturb: tree not initialized");
+    boundary_ = &new_boundary;
+  }
+
   // The GPU factorization (NULL before skeletonize).
   ki_factor* factor() const { return factor_; }
   const Boundary* boundary() const { return boundary_; }
@@ -230,7 +239,7 @@ class QuadTree {
 
  private:
   friend class SkelFactorization;
-  Boundary* boundary_ = nullptr;
+  const Boundary* boundary_ = nullptr;
   ki_factor* factor_ = nullptr;
 };
 
@@ -253,8 +262,11 @@ class SkelFactorization {
     if (using_hif) throw std::invalid_argument("SkelFactorization: HIF levels are not supported");
   }
 
-  // Factor the boundary the tree was initialized with (the kernel gives the
-  // PDE and dimensions); the factorization is stored in the tree.
+  // Factor the boundary the tree was initialized with, or perturbed to (the
+  // kernel gives the PDE and dimensions); the factorization is stored in the
+  // tree.  A tree factorized before is re-factorized keeping the factors of
+  // unchanged boxes, as the reference's skeletonize skips boxes still
+  // compressed (skel_factorization.cpp:199-208).
   void skeletonize(const Kernel& K, QuadTree* tree) const {
     if (!tree || !tree->boundary_) throw std::invalid_argument("skeletonize: tree not initialized");
     const Boundary& b = *tree->boundary_;
@@ -292,10 +304,12 @@ class SkelFactorization {
     d.min_dofs_to_compress = min_dofs_to_compress;
     d.id_tol = id_tol;
     d.precision = precision;
-    tree->reset();
     tree->solution_dimension = K.solution_dimension;
     tree->domain_dimension = dim;
-    detail::check(ki_factor_create(&d, &tree->factor_));
+    if (tree->factor_)
+      detail::check(ki_factor_update(tree->factor_, &d));
+    else
+      detail::check(ki_factor_create(&d, &tree->factor_));
   }
 
   // x = A^-1 b for every column of b (simply connected problems).

@@ -96,6 +96,8 @@ typedef struct {
   long device_bytes;    /* device memory held by the factorization */
   int n_sketched;       /* boxes compressed from a sketch (learned rank) */
   int n_fallback;       /* sketches recompressed by the plain ID */
+  int n_reused;         /* boxes whose factors ki_factor_update copied from the
+                           previous factorization */
 } ki_factor_info;
 
 /*
@@ -104,6 +106,30 @@ typedef struct {
  * skel_factorization/skel_factorization.cpp:173-551) on the current GPU.
  */
 int ki_factor_create(const ki_problem_desc* desc, ki_factor** out);
+
+/*
+ * Re-factorize the handle for a perturbed boundary: QuadTree::perturb
+ * (quadtree/quadtree.cpp:581-890) followed by SkelFactorization::skeletonize,
+ * which skips the boxes perturb left compressed (skel_factorization/
+ * skel_factorization.cpp:199-208).  desc describes the new boundary (the same
+ * fields as for ki_factor_create).  The tree is rebuilt for the new points;
+ * a box keeps its previous factors, copied on the device without an ID or
+ * elimination, when the previous tree has a box at the same level and
+ * centre, its DOFs and their data (coordinates, normals, weights,
+ * curvatures, the 3D diagonal) are bitwise unchanged, its children were
+ * kept, and its near-field neighbours are the same boxes with unchanged
+ * DOFs.  Every other box, the top levels whose ID reads the whole level, the
+ * root block and the border of a multiply connected problem are computed
+ * afresh.  Points are identified by index, so the new boundary should list
+ * its unmoved points at their old indices; a boundary of a different
+ * size, kind, precision, parameter set or rank model is factorized from
+ * scratch (info.n_reused = 0).  The result is a factorization of the new
+ * problem like ki_factor_create's; its recomputed boxes may be launched in
+ * other groupings than a fresh factorization's, so the two agree to rounding
+ * and the ID tolerance, not bit for bit.  On failure the handle keeps its
+ * previous factorization.  No solve on the handle may be in flight.
+ */
+int ki_factor_update(ki_factor* f, const ki_problem_desc* desc);
 
 /* Release a factorization (QuadTree destructor). */
 int ki_factor_destroy(ki_factor* f);

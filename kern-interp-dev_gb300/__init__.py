@@ -34,7 +34,7 @@ EXPORTED = ["ki_factor_create", "ki_factor_destroy", "ki_factor_get_info", "ki_s
             "ki_solve_device_noalloc", "ki_apply_fmm", "ki_apply_fmm_ex", "ki_trim_memory",
             "ki_launch_count", "ki_rank_model_floats",
             "ki_rank_model_train", "ki_rank_model_predict", "ki_rank_model_grad",
-            "ki_factor_get_box_log"]
+            "ki_factor_get_box_log", "ki_factor_update"]
 RANK_MODEL_PATH = os.path.join(HERE, "rank_model.npy")
 BOX_LOG_COLUMNS = 15   # 12 features, n, k, level
 
@@ -69,7 +69,8 @@ class _Info(ctypes.Structure):
                 ("n_compressed", ctypes.c_int), ("n_redundant", ctypes.c_long),
                 ("n_root", ctypes.c_int), ("n_border", ctypes.c_int),
                 ("factor_seconds", ctypes.c_double), ("device_bytes", ctypes.c_long),
-                ("n_sketched", ctypes.c_int), ("n_fallback", ctypes.c_int)]
+                ("n_sketched", ctypes.c_int), ("n_fallback", ctypes.c_int),
+                ("n_reused", ctypes.c_int)]
 
 
 _lib = None
@@ -88,6 +89,7 @@ def load_library(path=None):
     I = ctypes.c_int
     lib.ki_factor_create.argtypes = [ctypes.POINTER(_Desc), ctypes.POINTER(V)]
     lib.ki_factor_destroy.argtypes = [V]
+    lib.ki_factor_update.argtypes = [V, ctypes.POINTER(_Desc)]
     lib.ki_factor_get_info.argtypes = [V, ctypes.POINTER(_Info)]
     lib.ki_solve.argtypes = [V, V, I, I, V, I, V, I]
     lib.ki_solve_device.argtypes = [V, V, I, I, V, I, V, I, V]
@@ -146,33 +148,57 @@ class Factor:
         dim = int(domain_dimension or np.asarray(points).shape[-1])
         if dim not in (2, 3):
             raise ValueError("points must be (n, 2) or (n, 3)")
-        self._keep = [np.ascontiguousarray(points, np.float64).reshape(-1),
-                      np.ascontiguousarray(normals, np.float64).reshape(-1),
-                      np.ascontiguousarray(weights, np.float64).reshape(-1)]
-        self._keep.append(None if curvatures is None else
-                          np.ascontiguousarray(curvatures, np.float64).reshape(-1))
+        if isinstance(rank_model, str) and rank_model == "default":
+            rank_model = load_rank_model()
+        rm = None if rank_model is None else np.ascontiguousarray(rank_model, np.float32)
+        self._params = (dim, solution_dimension, pde, max_leaf_dofs, num_proxy_points,
+                        radius_ratio, min_dofs_to_compress, id_tol, precision, rm)
+        d = self._desc(points, normals, weights, curvatures, hole_centers, hole_start, hole_count)
+        h = ctypes.c_void_p()
+        _check(lib.ki_factor_create(ctypes.byref(d), ctypes.byref(h)))
+        self._h = h
+        self._set_sizes()
+
+    def _desc(self, points, normals, weights, curvatures, hole_centers, hole_start, hole_count):
+        """The ki_problem_desc of a boundary with this factor's parameters (the
+        arrays it points to are kept in self._keep)."""
+        dim, sd, pde, mld, npx, rr, mdc, tol, prec, rm = self._params
+        keep = [np.ascontiguousarray(points, np.float64).reshape(-1),
+                np.ascontiguousarray(normals, np.float64).reshape(-1),
+                np.ascontiguousarray(weights, np.float64).reshape(-1)]
+        keep.append(None if curvatures is None else
+                    np.ascontiguousarray(curvatures, np.float64).reshape(-1))
         nh = 0 if hole_centers is None else int(np.asarray(hole_centers).shape[0])
         hc = np.ascontiguousarray(hole_centers, np.float64).reshape(-1) if nh else None
         hs = np.ascontiguousarray(hole_start, np.int32) if nh else None
         hn = np.ascontiguousarray(hole_count, np.int32) if nh else None
-        self._keep += [hc, hs, hn]
-        if isinstance(rank_model, str) and rank_model == "default":
-            rank_model = load_rank_model()
-        rm = None if rank_model is None else np.ascontiguousarray(rank_model, np.float32)
-        self._keep.append(rm)
+        keep += [hc, hs, hn, rm]
+        self._keep = keep
+        self._n_holes = nh
+        n = keep[2].shape[0]
+        return _Desc(n, dim, sd, pde, _ptr(keep[0]), _ptr(keep[1]), _ptr(keep[2]),
+                     _ptr(keep[3]), nh, _ptr(hc), _ptr(hs), _ptr(hn), mld, npx, rr, mdc, tol,
+                     prec, _ptr(rm))
+
+    def _set_sizes(self):
+        dim, sd = self._params[0], self._params[1]
         n = self._keep[2].shape[0]
-        d = _Desc(n, dim, solution_dimension, pde, _ptr(self._keep[0]), _ptr(self._keep[1]),
-                  _ptr(self._keep[2]), _ptr(self._keep[3]), nh, _ptr(hc), _ptr(hs), _ptr(hn),
-                  max_leaf_dofs, num_proxy_points, radius_ratio, min_dofs_to_compress,
-                  id_tol, precision, _ptr(rm))
-        h = ctypes.c_void_p()
-        _check(lib.ki_factor_create(ctypes.byref(d), ctypes.byref(h)))
-        self._h = h
-        self.n_dofs = n * solution_dimension
+        self.n_dofs = n * sd
         self.n_points = n
-        self.solution_dimension = solution_dimension
+        self.solution_dimension = sd
         self.domain_dimension = dim
-        self.n_border = nh * (1 if solution_dimension == 1 else (3 if dim == 2 else 6))
+        self.n_border = self._n_holes * (1 if sd == 1 else (3 if dim == 2 else 6))
+
+    def update(self, points, normals, weights, curvatures=None, hole_centers=None, hole_start=None,
+               hole_count=None):
+        """Re-factorize for a perturbed boundary (ki_factor_update: the
+        reference's QuadTree::perturb then skeletonize), keeping the factors of
+        the boxes the perturbation left unchanged; the parameters are the
+        constructor's.  Returns info()["n_reused"], the boxes kept."""
+        d = self._desc(points, normals, weights, curvatures, hole_centers, hole_start, hole_count)
+        _check(load_library().ki_factor_update(self._h, ctypes.byref(d)))
+        self._set_sizes()
+        return self.info()["n_reused"]
 
     def close(self):
         if getattr(self, "_h", None):
@@ -426,9 +452,21 @@ class QuadTree:
     def initialize_tree(self, boundary, solution_dimension, domain_dimension):
         if domain_dimension not in (2, 3):
             raise KiError(KI_ERR_ARG, "domain_dimension must be 2 or 3")
+        if self.factor is not None:
+            self.factor.close()
+            self.factor = None
         self.boundary = boundary
         self.solution_dimension = solution_dimension
         self.domain_dimension = domain_dimension
+
+    def perturb(self, perturbed_boundary):
+        """QuadTree::perturb (quadtree.cpp:581-890): the tree now describes
+        perturbed_boundary (points identified by index), and the next
+        skeletonize keeps the factors of the boxes the change left alone
+        (ki_factor_update)."""
+        if self.boundary is None:
+            raise KiError(KI_ERR_STATE, "perturb: tree not initialized")
+        self.boundary = perturbed_boundary
 
 
 class SkelFactorization:
@@ -446,19 +484,31 @@ class SkelFactorization:
         self.precision = precision
 
     def skeletonize(self, kernel, quadtree):
+        """Factor the tree's boundary.  A tree factorized before (and
+        perturbed since) is re-factorized keeping the unchanged boxes' factors,
+        as the reference's skeletonize skips boxes still compressed
+        (skel_factorization.cpp:199-208); other parameters than the previous
+        factorization's start afresh."""
         b = quadtree.boundary
         holes = b.holes
         hc = np.array([h[0] for h in holes]) if holes else None
         hs = np.array([h[1] for h in holes], np.int32) if holes else None
         hn = np.array([h[2] for h in holes], np.int32) if holes else None
-        if quadtree.factor is not None:
-            quadtree.factor.close()
         dim = quadtree.domain_dimension
-        quadtree.factor = Factor(b.points.reshape(-1, dim), b.normals.reshape(-1, dim), b.weights,
-                                 b.curvatures, self.id_tol, kernel.solution_dimension, kernel.pde,
-                                 hc, hs, hn, quadtree.max_leaf_dofs, self.num_proxy_points,
-                                 self.radius_ratio, self.min_dofs_to_compress, self.precision,
-                                 domain_dimension=dim)
+        pts, nrm = b.points.reshape(-1, dim), b.normals.reshape(-1, dim)
+        params = (dim, kernel.solution_dimension, kernel.pde, quadtree.max_leaf_dofs,
+                  self.num_proxy_points, self.radius_ratio, self.min_dofs_to_compress,
+                  self.id_tol, self.precision, None)
+        fac = quadtree.factor
+        if fac is not None and fac._params[:9] == params[:9] and fac._params[9] is None:
+            fac.update(pts, nrm, b.weights, b.curvatures, hc, hs, hn)
+            return
+        if fac is not None:
+            fac.close()
+        quadtree.factor = Factor(pts, nrm, b.weights, b.curvatures, self.id_tol,
+                                 kernel.solution_dimension, kernel.pde, hc, hs, hn,
+                                 quadtree.max_leaf_dofs, self.num_proxy_points, self.radius_ratio,
+                                 self.min_dofs_to_compress, self.precision, domain_dimension=dim)
 
     def solve(self, quadtree, b):
         return quadtree.factor.solve(b)
@@ -474,11 +524,14 @@ def linear_solve(skel_factorization, quadtree, f):
 
 def boundary_integral_solve(kernel, boundary, quadtree, id_tol, fact_threads, domain_points,
                             **params):
-    """Factor, solve with boundary.boundary_values and evaluate at the domain
-    points (linear_solve.cpp:257-303; without the is_in_domain masking, which
-    needs the reference's concrete Boundary classes)."""
+    """Factor the tree (initialized with `boundary` here when it was not
+    initialized before; a perturbed tree is re-factorized), solve with
+    boundary.boundary_values and evaluate at the domain points
+    (linear_solve.cpp:257-303; without the is_in_domain masking, which needs
+    the reference's concrete Boundary classes)."""
     skel = SkelFactorization(id_tol, fact_threads, **params)
-    quadtree.initialize_tree(boundary, kernel.solution_dimension, kernel.domain_dimension)
+    if quadtree.boundary is None:
+        quadtree.initialize_tree(boundary, kernel.solution_dimension, kernel.domain_dimension)
     skel.skeletonize(kernel, quadtree)
     res = linear_solve(skel, quadtree, boundary.boundary_values)
     targets = np.asarray(domain_points, np.float64).reshape(-1, kernel.domain_dimension)

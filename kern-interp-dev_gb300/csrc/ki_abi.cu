@@ -485,6 +485,7 @@ struct ki_factor {
   double* d_holes = nullptr;
   double* d_pts = nullptr;     // interleaved coordinates (dim per point)
   float* d_rank_model = nullptr;   // learned rank predictor (FP32 factorizations)
+  std::vector<float> rank_model_host;   // its host copy (empty without one)
   int* d_hstart = nullptr;     // hole node ranges
   int* d_hcount = nullptr;
   ki::Points<double> P{};
@@ -501,6 +502,38 @@ struct ki_factor {
   // copies, geometry upload), the factorization call, waiting for the FMM
   // worker
   double host_prep_ms = 0, host_factor_ms = 0, fmm_wait_ms = 0;
+  // exchange every member with o (ki_factor_update installs a new state in
+  // the caller's handle; the old one leaves with o)
+  void swap_state(ki_factor& o) {
+    using std::swap;
+    swap(precision, o.precision);
+    swap(dim, o.dim);
+    swap(sol_dim, o.sol_dim);
+    swap(n_points, o.n_points);
+    swap(n_dofs, o.n_dofs);
+    swap(n_holes, o.n_holes);
+    swap(n_border, o.n_border);
+    swap(stream, o.stream);
+    swap(f64, o.f64);
+    swap(f32, o.f32);
+    swap(d_geo, o.d_geo);
+    swap(d_holes, o.d_holes);
+    swap(d_pts, o.d_pts);
+    swap(d_rank_model, o.d_rank_model);
+    swap(rank_model_host, o.rank_model_host);
+    swap(d_hstart, o.d_hstart);
+    swap(d_hcount, o.d_hcount);
+    swap(P, o.P);
+    swap(profile_refine, o.profile_refine);
+    swap(refine_open, o.refine_open);
+    swap(refine_prof, o.refine_prof);
+    swap(fmm_ready, o.fmm_ready);
+    swap(fmm_stream, o.fmm_stream);
+    swap(fmm, o.fmm);
+    swap(host_prep_ms, o.host_prep_ms);
+    swap(host_factor_ms, o.host_factor_ms);
+    swap(fmm_wait_ms, o.fmm_wait_ms);
+  }
   ~ki_factor() {
     for (auto& r : refine_open) {
       cudaEventDestroy(r.a);
@@ -1156,164 +1189,197 @@ void apply_bordered(ki_factor* f, const double* mu, const double* alpha, int nco
 
 extern "C" {
 
+namespace {
+
+// A new handle's state for desc (ki_factor_create).  With prev (a handle of
+// the same problem before a boundary perturbation, same precision, sizes,
+// parameters and rank model), the boxes of prev's factorization that the
+// perturbation left unchanged are copied rather than recomputed.
+void build_factor(ki_factor* f, const ki_problem_desc* desc, const ki_factor* prev) {
+  const auto t_create = std::chrono::steady_clock::now();
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
+    cudaGetLastError();
+    throw std::runtime_error("no CUDA device available");
+  }
+  f->precision = desc->precision;
+  const int dim = desc->domain_dimension;
+  f->dim = dim;
+  f->sol_dim = desc->solution_dimension;
+  f->n_points = desc->n_points;
+  f->n_dofs = desc->n_points * desc->solution_dimension;
+  f->n_holes = desc->n_holes;
+  f->n_border = desc->n_holes * ki::border_cols_per_hole(dim, desc->solution_dimension);
+  KI_CHECK_CUDA(cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking));
+  ki::Params prm;
+  prm.dim = dim;
+  prm.sol_dim = desc->solution_dimension;
+  prm.max_leaf_dofs = desc->max_leaf_dofs ? desc->max_leaf_dofs : 64;
+  // reference defaults: NUM_PROXY_POINTS = 128 (2D); the 3D proxy sphere is
+  // the Kernel constructor's 8 x 4 grid (kern_interp/kernel/kernel.h:44-62)
+  prm.num_proxy_points = desc->num_proxy_points ? desc->num_proxy_points : (dim == 2 ? 128 : 32);
+  prm.radius_ratio = desc->radius_ratio > 0 ? desc->radius_ratio : 2.0;
+  prm.min_dofs_to_compress = desc->min_dofs_to_compress ? desc->min_dofs_to_compress : 64;
+  prm.id_tol = desc->id_tol;
+  if (desc->rank_model && desc->precision == KI_PRECISION_FP32) {
+    for (int i = 0; i < ki::kMlpModelFloats; i++)
+      if (!std::isfinite(desc->rank_model[i])) throw ArgError("non-finite rank model");
+    KI_CHECK_CUDA(cudaMalloc(&f->d_rank_model, sizeof(float) * ki::kMlpModelFloats));
+    KI_CHECK_CUDA(cudaMemcpy(f->d_rank_model, desc->rank_model, sizeof(float) * ki::kMlpModelFloats,
+                             cudaMemcpyHostToDevice));
+    prm.rank_model = f->d_rank_model;
+    f->rank_model_host.assign(desc->rank_model, desc->rank_model + ki::kMlpModelFloats);
+  }
+  ki::HoleDesc holes;
+  holes.n_holes = desc->n_holes;
+  for (int h = 0; h < desc->n_holes; h++) {
+    for (int d = 0; d < dim; d++) holes.centers.push_back(desc->hole_centers[dim * h + d]);
+    holes.start.push_back(desc->hole_node_start[h]);
+    holes.count.push_back(desc->hole_node_count[h]);
+  }
+  // the caller's arrays uploaded once, interleaved as given: points (dim n) |
+  // normals (dim n) | weights (n) | curvatures (n); the factorization reads
+  // them in place, and the FP64 SoA geometry of the apply / evaluation
+  // kernels is formed from them on the device
+  const int n = desc->n_points;
+  {
+    const size_t nn = (size_t)n;
+    KI_CHECK_CUDA(cudaMalloc(&f->d_pts, sizeof(double) * (2 * dim + 2) * nn));
+    double* d_in = f->d_pts;
+    KI_CHECK_CUDA(cudaMemcpyAsync(d_in, desc->points, sizeof(double) * dim * nn,
+                                  cudaMemcpyHostToDevice, f->stream));
+    KI_CHECK_CUDA(cudaMemcpyAsync(d_in + dim * nn, desc->normals, sizeof(double) * dim * nn,
+                                  cudaMemcpyHostToDevice, f->stream));
+    KI_CHECK_CUDA(cudaMemcpyAsync(d_in + 2 * dim * nn, desc->weights, sizeof(double) * nn,
+                                  cudaMemcpyHostToDevice, f->stream));
+    if (desc->curvatures)
+      KI_CHECK_CUDA(cudaMemcpyAsync(d_in + (2 * dim + 1) * nn, desc->curvatures,
+                                    sizeof(double) * nn, cudaMemcpyHostToDevice, f->stream));
+    KI_CHECK_CUDA(cudaMalloc(&f->d_geo, sizeof(double) * 8 * nn));
+    ki::launch(k_geo_soa, std::min(2048, (n + 255) / 256), 256, 0, f->stream,
+        d_in, n, dim, desc->curvatures != nullptr, f->d_geo);
+    KI_CHECK_CUDA(cudaGetLastError());
+  }
+  f->P = ki::Points<double>{f->d_geo, f->d_geo + n, f->d_geo + 2 * (size_t)n,
+                            f->d_geo + 3 * (size_t)n, f->d_geo + 4 * (size_t)n,
+                            f->d_geo + 5 * (size_t)n};
+  f->P.dim = dim;
+  if (dim == 3) {
+    f->P.z = f->d_geo + 6 * (size_t)n;
+    f->P.nz = f->d_geo + 7 * (size_t)n;
+  }
+  if (desc->n_holes > 0) {
+    KI_CHECK_CUDA(cudaMalloc(&f->d_holes, sizeof(double) * dim * desc->n_holes));
+    KI_CHECK_CUDA(cudaMemcpy(f->d_holes, desc->hole_centers, sizeof(double) * dim * desc->n_holes,
+                             cudaMemcpyHostToDevice));
+    KI_CHECK_CUDA(cudaMalloc(&f->d_hstart, sizeof(int) * 2 * desc->n_holes));
+    f->d_hcount = f->d_hstart + desc->n_holes;
+    KI_CHECK_CUDA(cudaMemcpy(f->d_hstart, desc->hole_node_start, sizeof(int) * desc->n_holes,
+                             cudaMemcpyHostToDevice));
+    KI_CHECK_CUDA(cudaMemcpy(f->d_hcount, desc->hole_node_count, sizeof(int) * desc->n_holes,
+                             cudaMemcpyHostToDevice));
+  }
+
+  // 2D Laplace: the FMM for refinement residuals, planned and uploaded by a
+  // worker thread on its own stream, concurrent with the factorization (it
+  // copies the caller's arrays first, and this call returns only after the
+  // copy; it plans once the factorization's tree is built, so that the two
+  // do not compete for the host cores)
+  std::promise<void> copied;
+  std::future<void> copied_f = copied.get_future();
+  std::promise<void> tree_done;
+  std::shared_future<void> tree_done_f = tree_done.get_future().share();
+  bool tree_signalled = false;
+  auto signal_tree = [&] {
+    if (!tree_signalled) {
+      tree_signalled = true;
+      tree_done.set_value();
+    }
+  };
+  bool planning = false;
+  if (fmm_capable(f) && f->n_dofs >= 4096 && !std::getenv("KI_NO_FMM_PREPLAN")) {
+    planning = true;
+    const double *pp = desc->points, *nn = desc->normals, *ww = desc->weights,
+                 *kk = desc->curvatures;
+    const int order = fmm_order();
+    KI_CHECK_CUDA(cudaStreamCreateWithFlags(&f->fmm_stream, cudaStreamNonBlocking));
+    cudaStream_t us = f->fmm_stream;
+    int dev = 0;
+    KI_CHECK_CUDA(cudaGetDevice(&dev));
+    f->fmm_ready = std::async(std::launch::async, [pp, nn, ww, kk, n, order, us, dev, &copied,
+                                                    tree_done_f] {
+      std::vector<double> P, Nn, W, K;
+      try {
+        P.assign(pp, pp + 2 * (size_t)n);
+        Nn.assign(nn, nn + 2 * (size_t)n);
+        W.assign(ww, ww + n);
+        if (kk) K.assign(kk, kk + n);
+        else K.assign(n, 0.0);
+      } catch (...) {
+        copied.set_value();
+        throw;
+      }
+      copied.set_value();
+      tree_done_f.wait();
+      auto plan = ki::fmm2d_plan(P.data(), Nn.data(), W.data(), K.data(), n, order);
+      KI_CHECK_CUDA(cudaSetDevice(dev));   // the caller's device, not the thread default
+      return ki::fmm2d_upload(*plan, us);
+    });
+  }
+  struct WaitCopy {   // the caller's arrays stay valid until the worker has copied them;
+                      // the worker is released from its wait on every path out
+    bool on;
+    std::future<void>& fut;
+    std::function<void()> release;
+    ~WaitCopy() {
+      release();
+      if (on) fut.wait();
+    }
+  } wait_copy{planning, copied_f, signal_tree};
+  const auto t_factor = std::chrono::steady_clock::now();
+  f->host_prep_ms = std::chrono::duration<double, std::milli>(t_factor - t_create).count();
+  // prev's factorization serves only a problem of the same kind and size
+  // with the same rank model (factorize checks the parameters)
+  const bool reuse = prev && prev->precision == f->precision && prev->dim == f->dim &&
+                     prev->sol_dim == f->sol_dim && prev->n_points == f->n_points &&
+                     prev->rank_model_host == f->rank_model_host;
+  if (f->precision == KI_PRECISION_FP64)
+    f->f64 = ki::factorize<double>(prm, n, desc->points, desc->normals, desc->weights,
+                                   desc->curvatures, holes, f->stream, f->d_pts, signal_tree,
+                                   reuse ? prev->f64.get() : nullptr);
+  else
+    f->f32 = ki::factorize<float>(prm, n, desc->points, desc->normals, desc->weights,
+                                  desc->curvatures, holes, f->stream, f->d_pts, signal_tree,
+                                  reuse ? prev->f32.get() : nullptr);
+  f->host_factor_ms = std::chrono::duration<double, std::milli>(
+                          std::chrono::steady_clock::now() - t_factor).count();
+  // the FP64 3D diagonal of the factorization serves the FP64 apply
+  f->P.diag = f->f64 ? f->f64->d_diag64 : f->f32->d_diag64;
+}
+
+}  // namespace
+
 int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
   return guarded([&] {
     if (!out) throw ArgError("out is NULL");
     *out = nullptr;
     check_desc(desc);
-    const auto t_create = std::chrono::steady_clock::now();
-    int dev_count = 0;
-    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
-      cudaGetLastError();
-      throw std::runtime_error("no CUDA device available");
-    }
     std::unique_ptr<ki_factor> f(new ki_factor());
-    f->precision = desc->precision;
-    const int dim = desc->domain_dimension;
-    f->dim = dim;
-    f->sol_dim = desc->solution_dimension;
-    f->n_points = desc->n_points;
-    f->n_dofs = desc->n_points * desc->solution_dimension;
-    f->n_holes = desc->n_holes;
-    f->n_border = desc->n_holes * ki::border_cols_per_hole(dim, desc->solution_dimension);
-    KI_CHECK_CUDA(cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking));
-    ki::Params prm;
-    prm.dim = dim;
-    prm.sol_dim = desc->solution_dimension;
-    prm.max_leaf_dofs = desc->max_leaf_dofs ? desc->max_leaf_dofs : 64;
-    // reference defaults: NUM_PROXY_POINTS = 128 (2D); the 3D proxy sphere is
-    // the Kernel constructor's 8 x 4 grid (kern_interp/kernel/kernel.h:44-62)
-    prm.num_proxy_points = desc->num_proxy_points ? desc->num_proxy_points : (dim == 2 ? 128 : 32);
-    prm.radius_ratio = desc->radius_ratio > 0 ? desc->radius_ratio : 2.0;
-    prm.min_dofs_to_compress = desc->min_dofs_to_compress ? desc->min_dofs_to_compress : 64;
-    prm.id_tol = desc->id_tol;
-    if (desc->rank_model && desc->precision == KI_PRECISION_FP32) {
-      for (int i = 0; i < ki::kMlpModelFloats; i++)
-        if (!std::isfinite(desc->rank_model[i])) throw ArgError("non-finite rank model");
-      KI_CHECK_CUDA(cudaMalloc(&f->d_rank_model, sizeof(float) * ki::kMlpModelFloats));
-      KI_CHECK_CUDA(cudaMemcpy(f->d_rank_model, desc->rank_model, sizeof(float) * ki::kMlpModelFloats,
-                               cudaMemcpyHostToDevice));
-      prm.rank_model = f->d_rank_model;
-    }
-    ki::HoleDesc holes;
-    holes.n_holes = desc->n_holes;
-    for (int h = 0; h < desc->n_holes; h++) {
-      for (int d = 0; d < dim; d++) holes.centers.push_back(desc->hole_centers[dim * h + d]);
-      holes.start.push_back(desc->hole_node_start[h]);
-      holes.count.push_back(desc->hole_node_count[h]);
-    }
-    // the caller's arrays uploaded once, interleaved as given: points (dim n) |
-    // normals (dim n) | weights (n) | curvatures (n); the factorization reads
-    // them in place, and the FP64 SoA geometry of the apply / evaluation
-    // kernels is formed from them on the device
-    const int n = desc->n_points;
-    {
-      const size_t nn = (size_t)n;
-      KI_CHECK_CUDA(cudaMalloc(&f->d_pts, sizeof(double) * (2 * dim + 2) * nn));
-      double* d_in = f->d_pts;
-      KI_CHECK_CUDA(cudaMemcpyAsync(d_in, desc->points, sizeof(double) * dim * nn,
-                                    cudaMemcpyHostToDevice, f->stream));
-      KI_CHECK_CUDA(cudaMemcpyAsync(d_in + dim * nn, desc->normals, sizeof(double) * dim * nn,
-                                    cudaMemcpyHostToDevice, f->stream));
-      KI_CHECK_CUDA(cudaMemcpyAsync(d_in + 2 * dim * nn, desc->weights, sizeof(double) * nn,
-                                    cudaMemcpyHostToDevice, f->stream));
-      if (desc->curvatures)
-        KI_CHECK_CUDA(cudaMemcpyAsync(d_in + (2 * dim + 1) * nn, desc->curvatures,
-                                      sizeof(double) * nn, cudaMemcpyHostToDevice, f->stream));
-      KI_CHECK_CUDA(cudaMalloc(&f->d_geo, sizeof(double) * 8 * nn));
-      ki::launch(k_geo_soa, std::min(2048, (n + 255) / 256), 256, 0, f->stream,
-          d_in, n, dim, desc->curvatures != nullptr, f->d_geo);
-      KI_CHECK_CUDA(cudaGetLastError());
-    }
-    f->P = ki::Points<double>{f->d_geo, f->d_geo + n, f->d_geo + 2 * (size_t)n,
-                              f->d_geo + 3 * (size_t)n, f->d_geo + 4 * (size_t)n,
-                              f->d_geo + 5 * (size_t)n};
-    f->P.dim = dim;
-    if (dim == 3) {
-      f->P.z = f->d_geo + 6 * (size_t)n;
-      f->P.nz = f->d_geo + 7 * (size_t)n;
-    }
-    if (desc->n_holes > 0) {
-      KI_CHECK_CUDA(cudaMalloc(&f->d_holes, sizeof(double) * dim * desc->n_holes));
-      KI_CHECK_CUDA(cudaMemcpy(f->d_holes, desc->hole_centers, sizeof(double) * dim * desc->n_holes,
-                               cudaMemcpyHostToDevice));
-      KI_CHECK_CUDA(cudaMalloc(&f->d_hstart, sizeof(int) * 2 * desc->n_holes));
-      f->d_hcount = f->d_hstart + desc->n_holes;
-      KI_CHECK_CUDA(cudaMemcpy(f->d_hstart, desc->hole_node_start, sizeof(int) * desc->n_holes,
-                               cudaMemcpyHostToDevice));
-      KI_CHECK_CUDA(cudaMemcpy(f->d_hcount, desc->hole_node_count, sizeof(int) * desc->n_holes,
-                               cudaMemcpyHostToDevice));
-    }
-
-    // 2D Laplace: the FMM for refinement residuals, planned and uploaded by a
-    // worker thread on its own stream, concurrent with the factorization (it
-    // copies the caller's arrays first, and this call returns only after the
-    // copy; it plans once the factorization's tree is built, so that the two
-    // do not compete for the host cores)
-    std::promise<void> copied;
-    std::future<void> copied_f = copied.get_future();
-    std::promise<void> tree_done;
-    std::shared_future<void> tree_done_f = tree_done.get_future().share();
-    bool tree_signalled = false;
-    auto signal_tree = [&] {
-      if (!tree_signalled) {
-        tree_signalled = true;
-        tree_done.set_value();
-      }
-    };
-    bool planning = false;
-    if (fmm_capable(f.get()) && f->n_dofs >= 4096 && !std::getenv("KI_NO_FMM_PREPLAN")) {
-      planning = true;
-      const double *pp = desc->points, *nn = desc->normals, *ww = desc->weights,
-                   *kk = desc->curvatures;
-      const int order = fmm_order();
-      KI_CHECK_CUDA(cudaStreamCreateWithFlags(&f->fmm_stream, cudaStreamNonBlocking));
-      cudaStream_t us = f->fmm_stream;
-      int dev = 0;
-      KI_CHECK_CUDA(cudaGetDevice(&dev));
-      f->fmm_ready = std::async(std::launch::async, [pp, nn, ww, kk, n, order, us, dev, &copied,
-                                                      tree_done_f] {
-        std::vector<double> P, Nn, W, K;
-        try {
-          P.assign(pp, pp + 2 * (size_t)n);
-          Nn.assign(nn, nn + 2 * (size_t)n);
-          W.assign(ww, ww + n);
-          if (kk) K.assign(kk, kk + n);
-          else K.assign(n, 0.0);
-        } catch (...) {
-          copied.set_value();
-          throw;
-        }
-        copied.set_value();
-        tree_done_f.wait();
-        auto plan = ki::fmm2d_plan(P.data(), Nn.data(), W.data(), K.data(), n, order);
-        KI_CHECK_CUDA(cudaSetDevice(dev));   // the caller's device, not the thread default
-        return ki::fmm2d_upload(*plan, us);
-      });
-    }
-    struct WaitCopy {   // the caller's arrays stay valid until the worker has copied them;
-                        // the worker is released from its wait on every path out
-      bool on;
-      std::future<void>& fut;
-      std::function<void()> release;
-      ~WaitCopy() {
-        release();
-        if (on) fut.wait();
-      }
-    } wait_copy{planning, copied_f, signal_tree};
-    const auto t_factor = std::chrono::steady_clock::now();
-    f->host_prep_ms = std::chrono::duration<double, std::milli>(t_factor - t_create).count();
-    if (f->precision == KI_PRECISION_FP64)
-      f->f64 = ki::factorize<double>(prm, n, desc->points, desc->normals, desc->weights,
-                                     desc->curvatures, holes, f->stream, f->d_pts, signal_tree);
-    else
-      f->f32 = ki::factorize<float>(prm, n, desc->points, desc->normals, desc->weights,
-                                    desc->curvatures, holes, f->stream, f->d_pts, signal_tree);
-    f->host_factor_ms = std::chrono::duration<double, std::milli>(
-                            std::chrono::steady_clock::now() - t_factor).count();
-    // the FP64 3D diagonal of the factorization serves the FP64 apply
-    f->P.diag = f->f64 ? f->f64->d_diag64 : f->f32->d_diag64;
+    build_factor(f.get(), desc, nullptr);
     *out = f.release();
+  });
+}
+
+int ki_factor_update(ki_factor* f, const ki_problem_desc* desc) {
+  return guarded([&] {
+    if (!f) throw ArgError("f is NULL");
+    check_desc(desc);
+    // the old state stays in f until the new one is complete: a failure
+    // leaves the handle as it was
+    std::unique_ptr<ki_factor> nf(new ki_factor());
+    nf->profile_refine = f->profile_refine;
+    build_factor(nf.get(), desc, f);
+    f->swap_state(*nf);
   });
 }
 
@@ -1336,6 +1402,7 @@ int ki_factor_get_info(const ki_factor* f, ki_factor_info* info) {
       info->device_bytes = (long)F.device_bytes;
       info->n_sketched = F.n_sketched;
       info->n_fallback = F.n_fallback;
+      info->n_reused = F.n_reused;
     };
     if (f->f64) fill(*f->f64);
     if (f->f32) fill(*f->f32);

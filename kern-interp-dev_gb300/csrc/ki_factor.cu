@@ -34,6 +34,7 @@
 #include <numeric>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 
 #include "ki_common.cuh"
 #include "ki_dense.h"
@@ -2781,6 +2782,154 @@ struct HostBox {
   const void* tile = nullptr;  // accumulated self-block on the device
 };
 
+// ------------------------------------------------ re-factorization support --
+// The per-point arrays two factorizations compare: `per` values per point in
+// each (the 3D diagonal has 1 or 9).
+template <typename T>
+struct PointArrays {
+  static constexpr int kMax = 12;
+  const T* a[kMax];
+  const T* b[kMax];
+  int per[kMax];
+  int count;
+};
+
+// changed[p] = 1 when any listed array differs bitwise at point p.
+template <typename T>
+__global__ void k_points_changed(PointArrays<T> pa, int n, unsigned char* changed) {
+  using W = typename std::conditional<sizeof(T) == 8, unsigned long long, unsigned int>::type;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    bool d = false;
+    for (int q = 0; q < pa.count; q++)
+      for (int e = 0; e < pa.per[q]; e++) {
+        const size_t i = (size_t)p * pa.per[q] + e;
+        d = d || reinterpret_cast<const W*>(pa.a[q])[i] != reinterpret_cast<const W*>(pa.b[q])[i];
+      }
+    changed[p] = d;
+  }
+}
+
+// One device-to-device copy of `words` 4-byte words.
+struct CopySeg {
+  const void* src;
+  void* dst;
+  int64_t words;
+};
+
+// One CTA per segment.
+__global__ void k_copy_segments(const CopySeg* segs) {
+  const CopySeg sg = segs[blockIdx.x];
+  const uint32_t* a = static_cast<const uint32_t*>(sg.src);
+  uint32_t* d = static_cast<uint32_t*>(sg.dst);
+  for (int64_t i = threadIdx.x; i < sg.words; i += blockDim.x) d[i] = a[i];
+}
+
+bool same_params(const Params& a, const Params& b) {
+  return a.dim == b.dim && a.sol_dim == b.sol_dim && a.max_leaf_dofs == b.max_leaf_dofs &&
+         a.num_proxy_points == b.num_proxy_points && a.radius_ratio == b.radius_ratio &&
+         a.min_dofs_to_compress == b.min_dofs_to_compress && a.id_tol == b.id_tol &&
+         (a.rank_model != nullptr) == (b.rank_model != nullptr) &&
+         a.sketch_margin == b.sketch_margin && a.sketch_oversample == b.sketch_oversample;
+}
+
+// Boxes of `tree` (the perturbed boundary's) whose ID and Schur elimination
+// would see exactly the inputs they saw in `prev`, so that prev's factors
+// serve unchanged: per box, prev's box to copy from, or -1.  The reference
+// marks the boxes to recompute from the changed leaves up (every ancestor,
+// and each marked box's same-level or finer neighbours:
+// QuadTree::mark_neighbors_and_parents, kern_interp/quadtree/quadtree.cpp:
+// 483-497); here the rule is stated per box from what its factors read.
+//  - Boxes correspond by position: the roots when their centres and sides
+//    are equal, then child for child while both are split.
+//  - A leaf is unchanged when prev's box is a leaf with the same DOF list and
+//    none of its points' data changed (changed[p]).
+//  - A box's active list (and the self block assembled from its children)
+//    is unchanged when it is an unchanged leaf, or it is split in both trees
+//    and every child passes up the same list and block: a child that was
+//    reused, or one too small to compress (fewer than min_dofs DOFs) whose
+//    own active list is unchanged.
+//  - Its ID's rows are the proxy surface and the near field, the active DOFs
+//    of the same-level neighbours and the DOFs of the touching coarser leaves
+//    (Kernel::get_id_mat, kernel/kernel.cpp:441-563): unchanged when both
+//    neighbour lists correspond one to one and every neighbour's DOFs are
+//    unchanged.  Levels whose ID reads every box of the level (1, and 2 in
+//    2D) are always recomputed.
+template <typename T>
+std::vector<int> plan_reuse(const Factorization<T>& prev, const Tree& tree,
+                            const std::vector<unsigned char>& changed, int min_dofs) {
+  const Tree& ot = prev.tree;
+  const int nb = (int)tree.boxes.size(), dim = tree.dim, sd = tree.sol_dim;
+  std::vector<int> out(nb, -1);
+  if (ot.dim != dim || ot.sol_dim != sd || ot.n_dofs != tree.n_dofs || ot.levels.empty() ||
+      tree.levels.empty() || prev.box_factors.size() != ot.boxes.size())
+    return out;
+  std::vector<int> old_of(nb, -1);
+  {
+    const Box& r = tree.boxes[tree.levels[0][0]];
+    const Box& o = ot.boxes[ot.levels[0][0]];
+    if (r.side == o.side && r.c[0] == o.c[0] && r.c[1] == o.c[1] && r.c[2] == o.c[2])
+      old_of[tree.levels[0][0]] = ot.levels[0][0];
+  }
+  const int nch = tree.n_children();
+  for (const auto& lv : tree.levels)
+    for (int b : lv) {
+      const int ob = old_of[b];
+      if (ob < 0 || tree.boxes[b].leaf || ot.boxes[ob].leaf) continue;
+      for (int ci = 0; ci < nch; ci++) old_of[tree.boxes[b].child[ci]] = ot.boxes[ob].child[ci];
+    }
+  std::vector<char> leaf_same(nb, 0), act_same(nb, 0), out_same(nb, 0);
+  for (int b = 0; b < nb; b++) {
+    const Box& bx = tree.boxes[b];
+    const int ob = old_of[b];
+    if (!bx.leaf || ob < 0 || !ot.boxes[ob].leaf || ot.boxes[ob].orig_count != bx.orig_count) continue;
+    bool s = true;
+    for (int i = 0; i < bx.orig_count && s; i++) {
+      const int d = tree.dof_sorted[bx.orig_start + i];
+      s = d == ot.dof_sorted[ot.boxes[ob].orig_start + i] && !changed[d / sd];
+    }
+    leaf_same[b] = s;
+  }
+  // neighbour lists that correspond one to one (as sets of prev's boxes)
+  auto same_list = [&](IdList a, IdList o) {
+    if (a.size() != o.size()) return false;
+    std::vector<int> x, y(o.begin(), o.end());
+    for (int q : a) {
+      if (old_of[q] < 0) return false;
+      x.push_back(old_of[q]);
+    }
+    std::sort(x.begin(), x.end());
+    std::sort(y.begin(), y.end());
+    return x == y;
+  };
+  for (int l = tree.num_levels() - 1; l >= 1; l--) {
+    for (int b : tree.levels[l]) {
+      const Box& bx = tree.boxes[b];
+      const int ob = old_of[b];
+      if (ob < 0 || ot.boxes[ob].leaf != bx.leaf) continue;
+      bool s = bx.leaf ? (bool)leaf_same[b] : true;
+      if (!bx.leaf)
+        for (int ci = 0; ci < nch; ci++) s = s && out_same[bx.child[ci]];
+      act_same[b] = s;
+    }
+    const bool proxy_level = !(l == 1 || (l == 2 && dim == 2));
+    for (int b : tree.levels[l]) {
+      if (!act_same[b]) continue;
+      const int ob = old_of[b];
+      const bool id_box = prev.box_factors[ob].n >= min_dofs;   // went through an ID
+      bool near = proxy_level && same_list(tree.coarse_nbrs(b), ot.coarse_nbrs(ob)) &&
+                  same_list(tree.same_nbrs(b), ot.same_nbrs(ob));
+      if (near) {
+        for (int o : tree.coarse_nbrs(b)) near = near && leaf_same[o];
+        for (int o : tree.same_nbrs(b))
+          near = near && (tree.boxes[o].leaf ? leaf_same[o] : act_same[o]);
+      }
+      if (id_box && near) out[b] = ob;
+      out_same[b] = !id_box || out[b] >= 0;
+    }
+  }
+  return out;
+}
+
 }  // namespace
 
 // Shared-memory bytes k_sweep needs to stage a factor matrix of `entries`
@@ -2937,7 +3086,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
                                             const double* normals, const double* weights,
                                             const double* curvatures, const HoleDesc& holes,
                                             cudaStream_t stream, const double* d_inputs,
-                                            const std::function<void()>& after_tree) {
+                                            const std::function<void()>& after_tree,
+                                            const Factorization<T>* prev) {
   auto t_start = std::chrono::steady_clock::now();
   auto F = std::make_unique<Factorization<T>>();
   F->prm = prm;
@@ -3099,6 +3249,48 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
   std::vector<SweepTask<T>> all_sw;   // every level's sweep descriptors
   for (size_t b = 0; b < tree.boxes.size(); b++)
     if (tree.boxes[b].leaf) hb[b].n = tree.boxes[b].orig_count;
+  F->d_ipool = ipool;
+  F->box_factors.assign(tree.boxes.size(), BoxFactor<T>{});
+
+  // re-factorization: per box, the box of prev whose factors are copied
+  // (-1: computed here)
+  std::vector<int> reuse_of(tree.boxes.size(), -1);
+  if (prev && prev->n_points == n_points && same_params(prev->prm, prm)) {
+    PointArrays<T> pa{};
+    auto add = [&](const T* a, const T* b, int per) {
+      if (!a || !b) return;
+      pa.a[pa.count] = a;
+      pa.b[pa.count] = b;
+      pa.per[pa.count++] = per;
+    };
+    add(F->d_x, prev->d_x, 1);
+    add(F->d_y, prev->d_y, 1);
+    add(F->d_nx, prev->d_nx, 1);
+    add(F->d_ny, prev->d_ny, 1);
+    add(F->d_w, prev->d_w, 1);
+    add(F->d_kappa, prev->d_kappa, 1);
+    add(F->d_xl, prev->d_xl, 1);
+    add(F->d_yl, prev->d_yl, 1);
+    if (dim == 3) {
+      add(F->d_z, prev->d_z, 1);
+      add(F->d_nz, prev->d_nz, 1);
+      add(F->d_zl, prev->d_zl, 1);
+      if (F->diag_per_point == prev->diag_per_point) add(F->d_diag, prev->d_diag, F->diag_per_point);
+    }
+    // 3D: the diagonal (a sum over the point's curve or surface) is part of
+    // every point's data; without a comparable one nothing is reused
+    if (dim == 2 || F->diag_per_point == prev->diag_per_point) {
+      unsigned char* d_ch = (unsigned char*)F->alloc(std::max(1, n_points));
+      ki::launch(k_points_changed<T>, std::min(1024, (n_points + 255) / 256), 256, 0, s, pa, n_points, d_ch);
+      KI_CUDA(cudaGetLastError());
+      std::vector<unsigned char> ch(n_points);
+      KI_CUDA(cudaMemcpyAsync(ch.data(), d_ch, n_points, cudaMemcpyDeviceToHost, s));
+      KI_CUDA(cudaStreamSynchronize(s));
+      reuse_of = plan_reuse(*prev, tree, ch, prm.min_dofs_to_compress);
+    }
+  }
+  // boxes whose factors are copied: no self block, ID or elimination here
+  auto copied = [&](int b) { return reuse_of[b] >= 0 && prev->box_factors[reuse_of[b]].compressed; };
 
   F->levels.resize(L);
   std::vector<void*> level_scratch;
@@ -3148,7 +3340,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     // ---- self blocks of every box with active DOFs
     std::vector<AsmTask<T>> asm_tasks;
     int64_t kbn_total = 0;
-    for (int b : lv) kbn_total += (int64_t)hb[b].n * hb[b].n;
+    for (int b : lv)
+      if (!copied(b)) kbn_total += (int64_t)hb[b].n * hb[b].n;
     T* d_kbn = (T*)F->alloc(Tsz * (kbn_total + 1));
     std::vector<T*> kbn_of(lv.size(), nullptr);
     {
@@ -3157,7 +3350,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         int b = lv[i];
         const Box& bx = tree.boxes[b];
         HostBox& h = hb[b];
-        if (h.n == 0) continue;
+        if (h.n == 0 || copied(b)) continue;
         AsmTask<T> at{};
         at.act = h.act;
         at.n = h.n;
@@ -3194,8 +3387,18 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
 
     // ---- ID tasks
     std::vector<int> comp;  // boxes to compress
-    for (int b : lv)
-      if (hb[b].n >= prm.min_dofs_to_compress && hb[b].n > 0) comp.push_back(b);
+    std::vector<int> kept;  // boxes whose factors are copied from prev
+    for (int b : lv) {
+      if (hb[b].n < prm.min_dofs_to_compress || hb[b].n == 0) continue;
+      if (reuse_of[b] < 0) {
+        comp.push_back(b);
+        continue;
+      }
+      if (hb[b].n != prev->box_factors[reuse_of[b]].n)
+        throw std::logic_error("re-factorization: a reused box's active set changed size");
+      F->n_reused++;
+      if (copied(b)) kept.push_back(b);
+    }
     std::vector<IdTask> itasks;
     std::vector<int64_t> seg_off;
     std::vector<int> seg_len;
@@ -3249,436 +3452,442 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       itasks.push_back(it);
     }
     LevelFactor& LF = F->levels[l];
-    if (itasks.empty()) continue;
-    // scratch
-    int* d_irows = (int*)F->alloc(sizeof(int) * (rows_cap + perm_cap + 16));
-    T* d_tws = (T*)F->alloc(Tsz * (ws_cap + 16));
-    for (auto& it : itasks) {
-      it.perm += rows_cap;
-      it.pact = pact_top;
-      pact_top += it.n;
-    }
-    for (size_t i = 0; i < comp.size(); i++) hb[comp[i]].pact = itasks[i].pact;
-    const size_t smem_cap = 225 * 1024;
-    IdTask* d_it = (IdTask*)F->alloc(sizeof(IdTask) * itasks.size());
-    int64_t* d_soff = (int64_t*)F->alloc(sizeof(int64_t) * (seg_off.size() + 1));
-    int* d_slen = (int*)F->alloc(sizeof(int) * (seg_len.size() + 1));
-    int* d_k = (int*)F->alloc(sizeof(int) * itasks.size());
-    int* d_m = (int*)F->alloc(sizeof(int) * itasks.size());
-    upload(d_it, itasks, s);
-    upload(d_soff, seg_off, s);
-    upload(d_slen, seg_len, s);
-    std::string id_name = "id@L" + std::to_string(l);
-    F->stage_begin(id_name.c_str(), 0, 0);
-    size_t id_rec = F->prof_open.size() - 1;
-    // (a) row lists of every box (m is needed to pick the path)
-    KI_CUDA(cudaFuncSetAttribute(k_id<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
-    KI_CUDA(cudaFuncSetAttribute(k_id<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
-    if constexpr (sizeof(T) == 4) {
-      KI_CUDA(cudaFuncSetAttribute(k_id<T, 32, kIdBigThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem_cap));
-      KI_CUDA(cudaFuncSetAttribute(k_id<T, 64, kIdBigThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem_cap));
-    }
-    ki::launch(k_id<T, 32>, (unsigned)itasks.size(), kThreads, 0, s, d_it, 0, d_soff, d_slen, ipool, d_irows, d_tws,
-                                                         P, sd, ptab, prm.id_tol,
-                                                         d_k, d_m, 0, 1, nullptr);
-    KI_CUDA(cudaGetLastError());
-    // per-box features of the rank predictor and, with a model, the sketch sizes
-    const int ntask = (int)itasks.size();
-    float* d_feat = (float*)F->alloc(sizeof(float) * kMlpIn * (size_t)ntask);
-    int* d_lsk = (int*)F->alloc(sizeof(int) * (size_t)ntask);
-    float* d_khat = (float*)F->alloc(sizeof(float) * (size_t)ntask);
-    ki::launch(k_box_features<T>, (ntask + 3) / 4, 128, 0, s,
-        d_it, ntask, ipool, P, sd, d_m, 2 * np * sd, L > 1 ? (float)l / (float)(L - 1) : 0.f,
-        (float)(-std::log10(prm.id_tol) / 10.0), prm.rank_model, prm.sketch_margin,
-        prm.sketch_oversample, d_feat, d_lsk, d_khat);
-    KI_CUDA(cudaGetLastError());
-    std::vector<int> mh(itasks.size()), kh(itasks.size()), lh(itasks.size());
-    std::vector<float> fh(kMlpIn * (size_t)ntask), khat(itasks.size());
-    KI_CUDA(cudaMemcpyAsync(khat.data(), d_khat, sizeof(float) * khat.size(), cudaMemcpyDeviceToHost, s));
-    KI_CUDA(cudaMemcpyAsync(lh.data(), d_lsk, sizeof(int) * lh.size(), cudaMemcpyDeviceToHost, s));
-    KI_CUDA(cudaMemcpyAsync(fh.data(), d_feat, sizeof(float) * fh.size(), cudaMemcpyDeviceToHost, s));
-    KI_CUDA(cudaMemcpyAsync(mh.data(), d_m, sizeof(int) * mh.size(), cudaMemcpyDeviceToHost, s));
-    KI_CUDA(cudaStreamSynchronize(s));
-    // (b) groups: [narrow, R in smem][narrow, R global][wide, R in smem][wide, R global];
-    //     wide = tall ID matrix (folded by the multi-CTA blocked QR) or a
-    //     triangle too large for shared memory
-    // row threshold of the wide path (environment override KI_WIDE_ROWS, used
-    // by the tests to drive every box through it)
-    int kWideRows = 1536;
-    if (const char* e = std::getenv("KI_WIDE_ROWS")) kWideRows = std::atoi(e);
-    // largest shared footprint with the full triangle in shared memory
-    // (environment override KI_ID_FULL_CAP, used by the tests)
-    size_t full_cap = smem_cap;
-    if (const char* e = std::getenv("KI_ID_FULL_CAP")) full_cap = (size_t)std::atol(e);
-    // a level of fewer boxes than SMs leaves most SMs idle while one CTA per
-    // box folds its rows: with a learned rank its tall boxes take the wide
-    // path instead (the sketch formed by many CTAs per box)
-    static const int n_sm = device_sm_count();
-    const int few_rows = ((int)itasks.size() < n_sm && prm.rank_model) ? 384 : INT_MAX;
-    std::vector<int> grp(itasks.size());
-    std::vector<char> few(itasks.size(), 0);   // wide only for the level's few boxes
-    // KI_TC_SKETCH=1: FP32 sketched boxes of up to 256 columns form their
-    // sketch on the tensor cores (k_sketch_tc) instead of k_id's fold
-    const char* tc_env = std::getenv("KI_TC_SKETCH");
-    const bool tc_sketch = tc_env && std::string(tc_env) == "1";
-    for (size_t i = 0; i < itasks.size(); i++) {
-      int n = itasks[i].n;
-      int md = id_smem_bytes<T>(n, 0) <= full_cap ? 0 : 1;
-      const bool tall = mh[i] > kWideRows || (md == 1 && id_smem_bytes<T>(n, 2) > smem_cap);
-      few[i] = !tall && mh[i] > few_rows;
-      const bool wide = tall || few[i];
-      const bool tc = sizeof(T) == 4 && tc_sketch && prm.rank_model && !wide && md == 0 &&
-                      lh[i] > 0 && lh[i] < n && lh[i] <= 64 && n <= 256 &&
-                      (n > 128 ? 2 : 1) * ((lh[i] + 15) & ~15) <= 128;
-      // narrow groups: 0 triangle in shared memory, 1 packed triangle in
-      // shared memory (mode 2 of k_id), 4 tensor-core sketch then the
-      // pivoted QR of the sketch; wide groups: 2 / 3 by triangle size
-      grp[i] = wide ? 2 + md : (tc ? 4 : md);
-    }
-    auto is_wide = [](int g) { return g == 2 || g == 3; };
-    std::vector<int> mode_of(itasks.size());
-    {
-      std::vector<size_t> order(itasks.size());
-      std::iota(order.begin(), order.end(), 0);
-      std::stable_sort(order.begin(), order.end(), [&](size_t a2, size_t b2) {
-        return grp[a2] != grp[b2] ? grp[a2] < grp[b2] : itasks[a2].n < itasks[b2].n;
-      });
-      std::vector<IdTask> it2;
-      std::vector<int> comp2, grp2, m2, l2;
-      std::vector<float> f2;
-      for (size_t o : order) {
-        it2.push_back(itasks[o]);
-        comp2.push_back(comp[o]);
-        grp2.push_back(grp[o]);
-        m2.push_back(mh[o]);
-        // sketches for the shared-memory triangles (group 0) and the wide
-        // boxes (groups 2, 3; k_wide_sketch, up to 384 rows; their sketches are
-        // cheap next to a fallback, so they get twice the margin and
-        // oversampling), not for packed triangles
-        // (boxes routed wide only because the level is small keep the narrow
-        // path's sketch size)
-        int lo = lh[o];
-        if (is_wide(grp[o]) && prm.rank_model && !few[o])
-          lo = std::min(itasks[o].n, (int)std::ceil((1.f + 2 * prm.sketch_margin) * khat[o]) +
-                                         2 * prm.sketch_oversample);
-        l2.push_back(grp[o] == 1 || (is_wide(grp[o]) && lo > 384) ? 0 : lo);
-        f2.insert(f2.end(), fh.begin() + kMlpIn * o, fh.begin() + kMlpIn * (o + 1));
+    if (itasks.empty() && kept.empty()) continue;
+    int* d_irows = nullptr;   // ID row lists and permutations
+    T* d_tws = nullptr;       // ID workspaces (their Tout feeds the elimination)
+    std::vector<int> kh;      // ranks of the ID boxes
+    if (!itasks.empty()) {
+      // scratch
+      d_irows = (int*)F->alloc(sizeof(int) * (rows_cap + perm_cap + 16));
+      d_tws = (T*)F->alloc(Tsz * (ws_cap + 16));
+      for (auto& it : itasks) {
+        it.perm += rows_cap;
+        it.pact = pact_top;
+        pact_top += it.n;
       }
-      itasks.swap(it2);
-      comp.swap(comp2);
-      grp.swap(grp2);
-      mh.swap(m2);
-      lh.swap(l2);
-      fh.swap(f2);
-      for (size_t i = 0; i < comp.size(); i++) {
-        hb[comp[i]].pact = itasks[i].pact;
-        mode_of[i] = grp[i];
-      }
+      for (size_t i = 0; i < comp.size(); i++) hb[comp[i]].pact = itasks[i].pact;
+      const size_t smem_cap = 225 * 1024;
+      IdTask* d_it = (IdTask*)F->alloc(sizeof(IdTask) * itasks.size());
+      int64_t* d_soff = (int64_t*)F->alloc(sizeof(int64_t) * (seg_off.size() + 1));
+      int* d_slen = (int*)F->alloc(sizeof(int) * (seg_len.size() + 1));
+      int* d_k = (int*)F->alloc(sizeof(int) * itasks.size());
+      int* d_m = (int*)F->alloc(sizeof(int) * itasks.size());
       upload(d_it, itasks, s);
-      upload(d_m, mh, s);
-      upload(d_lsk, lh, s);
-    }
-    const bool sketching = prm.rank_model != nullptr;
-    int next_aux = 0, n_streams = Factorization<T>::kAux - 1;
-    auto launch_range = [&](int g, int flags, cudaStream_t fixed) {
-      // tasks of group g are contiguous and sorted by n within the group (see
-      // the ordering above); launch them in bins of similar shared-memory
-      // size so that small boxes are not limited by the largest one's footprint
-      int first = -1, cnt = 0;
-      for (size_t i = 0; i < itasks.size(); i++)
-        if (grp[i] == g) {
-          if (first < 0) first = (int)i;
-          cnt++;
-        }
-      if (cnt == 0) return;
-      const int kmode = g == 1 ? 2 : (g & 1);   // group -> k_id storage mode
-      // 64-row fold blocks (half the serial steps) where they fit
-      auto fold_rows = [&](int n) {
-        return (kmode != 1 && (flags & 2) && id_smem_bytes<T>(n, kmode, 64) <= smem_cap) ? 64 : 32;
-      };
-      int b0 = first;
-      while (b0 < first + cnt) {
-        const int fr = fold_rows(itasks[b0].n);
-        size_t sm0 = id_smem_bytes<T>(itasks[b0].n, kmode, fr, flags);
-        // CTAs per SM at this footprint; extend the bin while it stays the same
-        int per_sm = std::max(1, (int)(228 * 1024 / (sm0 + 1024)));
-        int b1 = b0 + 1;
-        size_t sm = sm0;
-        while (b1 < first + cnt) {
-          if (fold_rows(itasks[b1].n) != fr) break;
-          size_t s1 = id_smem_bytes<T>(itasks[b1].n, kmode, fr, flags);
-          if (std::max(1, (int)(228 * 1024 / (s1 + 1024))) != per_sm) break;
-          sm = std::max(sm, s1);
-          b1++;
-        }
-        if (sm > smem_cap) throw std::runtime_error("box too large for the ID kernel");
-        cudaStream_t st = fixed ? fixed : F->aux[(next_aux++) % n_streams];
-        launch_k_id<T>(fr, (unsigned)(b1 - b0), sm, st, (const IdTask*)d_it, b0,
-                       (const int64_t*)d_soff, (const int*)d_slen, ipool, d_irows, d_tws, P, sd, ptab,
-                       prm.id_tol, d_k, d_m, kmode, flags,
-                       (const int*)(sketching && g != 1 ? d_lsk : nullptr));
-        KI_CUDA(cudaGetLastError());
-        b0 = b1;
+      upload(d_soff, seg_off, s);
+      upload(d_slen, seg_len, s);
+      std::string id_name = "id@L" + std::to_string(l);
+      F->stage_begin(id_name.c_str(), 0, 0);
+      size_t id_rec = F->prof_open.size() - 1;
+      // (a) row lists of every box (m is needed to pick the path)
+      KI_CUDA(cudaFuncSetAttribute(k_id<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
+      KI_CUDA(cudaFuncSetAttribute(k_id<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
+      if constexpr (sizeof(T) == 4) {
+        KI_CUDA(cudaFuncSetAttribute(k_id<T, 32, kIdBigThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem_cap));
+        KI_CUDA(cudaFuncSetAttribute(k_id<T, 64, kIdBigThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem_cap));
       }
-    };
-    // (c) narrow boxes: fused on-the-fly assembly + TSQR + CPQR, one CTA each;
-    //     size bins on aux streams 0..2, the wide path on aux stream 3, all
-    //     concurrent
-    F->fork();
-    launch_range(0, 2, nullptr);
-    launch_range(1, 2, nullptr);
-    if constexpr (sizeof(T) == 4) {
-      // tensor-core sketches (one CTA per box, by accumulator tiles), then
-      // the pivoted QR of each sketch, in order on one aux stream
-      std::vector<int> list[2];
-      for (size_t i = 0; i < itasks.size(); i++)
-        if (grp[i] == 4) list[itasks[i].n > 128].push_back((int)i);
-      if (!list[0].empty() || !list[1].empty()) {
-        cudaStream_t ts = F->aux[0];
-        std::string tn = "id_tc_sketch@L" + std::to_string(l);
-        double tc_flops = 0;   // Y = Omega M: 2 l m n per box
-        for (const auto& lst : list)
-          for (int i : lst) tc_flops += 2.0 * lh[i] * (double)mh[i] * itasks[i].n;
-        F->stage_begin(tn.c_str(), tc_flops, 0, ts);
-        for (int tl = 0; tl < 2; tl++) {
-          if (list[tl].empty()) continue;
-          int* d_list = (int*)F->alloc(sizeof(int) * list[tl].size());
-          upload(d_list, list[tl], ts);
-          int nq_max = 16;
-          for (int i : list[tl]) nq_max = std::max(nq_max, (lh[i] + 15) & ~15);
-          const size_t sm = 2 * tc_sketch_smem(tl + 1, nq_max);   // two stages
-          const int ch = ((tl + 1) * nq_max + 31) / 32;   // accumulator chunks per thread
-          auto kern = tl ? (ch <= 2 ? k_sketch_tc<2, 2> : k_sketch_tc<2, 4>)
-                         : (ch <= 1 ? k_sketch_tc<1, 1> : ch <= 2 ? k_sketch_tc<1, 2> : k_sketch_tc<1, 4>);
-          KI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-          ki::launch(kern, (unsigned)list[tl].size(), kTcThreads, sm, ts, (const IdTask*)d_it,
-                     (const int*)d_list, (const int*)d_m, (const int*)d_lsk, (const int*)ipool,
-                     (const int*)d_irows, (float*)d_tws, P, sd, ptab, F->d_err);
-          KI_CUDA(cudaGetLastError());
+      ki::launch(k_id<T, 32>, (unsigned)itasks.size(), kThreads, 0, s, d_it, 0, d_soff, d_slen, ipool, d_irows, d_tws,
+                                                           P, sd, ptab, prm.id_tol,
+                                                           d_k, d_m, 0, 1, nullptr);
+      KI_CUDA(cudaGetLastError());
+      // per-box features of the rank predictor and, with a model, the sketch sizes
+      const int ntask = (int)itasks.size();
+      float* d_feat = (float*)F->alloc(sizeof(float) * kMlpIn * (size_t)ntask);
+      int* d_lsk = (int*)F->alloc(sizeof(int) * (size_t)ntask);
+      float* d_khat = (float*)F->alloc(sizeof(float) * (size_t)ntask);
+      ki::launch(k_box_features<T>, (ntask + 3) / 4, 128, 0, s,
+          d_it, ntask, ipool, P, sd, d_m, 2 * np * sd, L > 1 ? (float)l / (float)(L - 1) : 0.f,
+          (float)(-std::log10(prm.id_tol) / 10.0), prm.rank_model, prm.sketch_margin,
+          prm.sketch_oversample, d_feat, d_lsk, d_khat);
+      KI_CUDA(cudaGetLastError());
+      kh.assign(itasks.size(), 0);
+      std::vector<int> mh(itasks.size()), lh(itasks.size());
+      std::vector<float> fh(kMlpIn * (size_t)ntask), khat(itasks.size());
+      KI_CUDA(cudaMemcpyAsync(khat.data(), d_khat, sizeof(float) * khat.size(), cudaMemcpyDeviceToHost, s));
+      KI_CUDA(cudaMemcpyAsync(lh.data(), d_lsk, sizeof(int) * lh.size(), cudaMemcpyDeviceToHost, s));
+      KI_CUDA(cudaMemcpyAsync(fh.data(), d_feat, sizeof(float) * fh.size(), cudaMemcpyDeviceToHost, s));
+      KI_CUDA(cudaMemcpyAsync(mh.data(), d_m, sizeof(int) * mh.size(), cudaMemcpyDeviceToHost, s));
+      KI_CUDA(cudaStreamSynchronize(s));
+      // (b) groups: [narrow, R in smem][narrow, R global][wide, R in smem][wide, R global];
+      //     wide = tall ID matrix (folded by the multi-CTA blocked QR) or a
+      //     triangle too large for shared memory
+      // row threshold of the wide path (environment override KI_WIDE_ROWS, used
+      // by the tests to drive every box through it)
+      int kWideRows = 1536;
+      if (const char* e = std::getenv("KI_WIDE_ROWS")) kWideRows = std::atoi(e);
+      // largest shared footprint with the full triangle in shared memory
+      // (environment override KI_ID_FULL_CAP, used by the tests)
+      size_t full_cap = smem_cap;
+      if (const char* e = std::getenv("KI_ID_FULL_CAP")) full_cap = (size_t)std::atol(e);
+      // a level of fewer boxes than SMs leaves most SMs idle while one CTA per
+      // box folds its rows: with a learned rank its tall boxes take the wide
+      // path instead (the sketch formed by many CTAs per box)
+      static const int n_sm = device_sm_count();
+      const int few_rows = ((int)itasks.size() < n_sm && prm.rank_model) ? 384 : INT_MAX;
+      std::vector<int> grp(itasks.size());
+      std::vector<char> few(itasks.size(), 0);   // wide only for the level's few boxes
+      // KI_TC_SKETCH=1: FP32 sketched boxes of up to 256 columns form their
+      // sketch on the tensor cores (k_sketch_tc) instead of k_id's fold
+      const char* tc_env = std::getenv("KI_TC_SKETCH");
+      const bool tc_sketch = tc_env && std::string(tc_env) == "1";
+      for (size_t i = 0; i < itasks.size(); i++) {
+        int n = itasks[i].n;
+        int md = id_smem_bytes<T>(n, 0) <= full_cap ? 0 : 1;
+        const bool tall = mh[i] > kWideRows || (md == 1 && id_smem_bytes<T>(n, 2) > smem_cap);
+        few[i] = !tall && mh[i] > few_rows;
+        const bool wide = tall || few[i];
+        const bool tc = sizeof(T) == 4 && tc_sketch && prm.rank_model && !wide && md == 0 &&
+                        lh[i] > 0 && lh[i] < n && lh[i] <= 64 && n <= 256 &&
+                        (n > 128 ? 2 : 1) * ((lh[i] + 15) & ~15) <= 128;
+        // narrow groups: 0 triangle in shared memory, 1 packed triangle in
+        // shared memory (mode 2 of k_id), 4 tensor-core sketch then the
+        // pivoted QR of the sketch; wide groups: 2 / 3 by triangle size
+        grp[i] = wide ? 2 + md : (tc ? 4 : md);
+      }
+      auto is_wide = [](int g) { return g == 2 || g == 3; };
+      std::vector<int> mode_of(itasks.size());
+      {
+        std::vector<size_t> order(itasks.size());
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](size_t a2, size_t b2) {
+          return grp[a2] != grp[b2] ? grp[a2] < grp[b2] : itasks[a2].n < itasks[b2].n;
+        });
+        std::vector<IdTask> it2;
+        std::vector<int> comp2, grp2, m2, l2;
+        std::vector<float> f2;
+        for (size_t o : order) {
+          it2.push_back(itasks[o]);
+          comp2.push_back(comp[o]);
+          grp2.push_back(grp[o]);
+          m2.push_back(mh[o]);
+          // sketches for the shared-memory triangles (group 0) and the wide
+          // boxes (groups 2, 3; k_wide_sketch, up to 384 rows; their sketches are
+          // cheap next to a fallback, so they get twice the margin and
+          // oversampling), not for packed triangles
+          // (boxes routed wide only because the level is small keep the narrow
+          // path's sketch size)
+          int lo = lh[o];
+          if (is_wide(grp[o]) && prm.rank_model && !few[o])
+            lo = std::min(itasks[o].n, (int)std::ceil((1.f + 2 * prm.sketch_margin) * khat[o]) +
+                                           2 * prm.sketch_oversample);
+          l2.push_back(grp[o] == 1 || (is_wide(grp[o]) && lo > 384) ? 0 : lo);
+          f2.insert(f2.end(), fh.begin() + kMlpIn * o, fh.begin() + kMlpIn * (o + 1));
         }
-        F->stage_end(ts);
-        // the pivoted QRs of the sketches (k_cpqr), by sketch rows (32 / 64)
-        // and 32-column slabs
-        std::vector<int> cls[2][8];
-        for (const auto& lst : list)
-          for (int i : lst) cls[lh[i] > 32][(itasks[i].n + 31) / 32 - 1].push_back(i);
-        std::string qn = "id_cpqr@L" + std::to_string(l);
-        F->stage_begin(qn.c_str(), 0, 0, ts);
-        for (int lb = 0; lb < 2; lb++)
-          for (int wq = 0; wq < 8; wq++) {
-            const auto& v = cls[lb][wq];
-            if (v.empty()) continue;
-            int* d_l2 = (int*)F->alloc(sizeof(int) * v.size());
-            upload(d_l2, v, ts);
-            int lm = 0, nm = 0;
-            for (int i : v) {
-              lm = std::max(lm, lh[i]);
-              nm = std::max(nm, itasks[i].n);
-            }
-            const size_t sm = sizeof(float) * (size_t)lm * nm;
-            auto kern = lb ? k_cpqr<64> : k_cpqr<32>;
-            if (sm > 48 * 1024)
-              KI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            ki::launch(kern, (unsigned)v.size(), 32 * (wq + 1), sm, ts, (const IdTask*)d_it,
-                       (const int*)d_l2, (const int*)d_lsk, ipool, d_irows, (float*)d_tws, prm.id_tol, d_k);
+        itasks.swap(it2);
+        comp.swap(comp2);
+        grp.swap(grp2);
+        mh.swap(m2);
+        lh.swap(l2);
+        fh.swap(f2);
+        for (size_t i = 0; i < comp.size(); i++) {
+          hb[comp[i]].pact = itasks[i].pact;
+          mode_of[i] = grp[i];
+        }
+        upload(d_it, itasks, s);
+        upload(d_m, mh, s);
+        upload(d_lsk, lh, s);
+      }
+      const bool sketching = prm.rank_model != nullptr;
+      int next_aux = 0, n_streams = Factorization<T>::kAux - 1;
+      auto launch_range = [&](int g, int flags, cudaStream_t fixed) {
+        // tasks of group g are contiguous and sorted by n within the group (see
+        // the ordering above); launch them in bins of similar shared-memory
+        // size so that small boxes are not limited by the largest one's footprint
+        int first = -1, cnt = 0;
+        for (size_t i = 0; i < itasks.size(); i++)
+          if (grp[i] == g) {
+            if (first < 0) first = (int)i;
+            cnt++;
+          }
+        if (cnt == 0) return;
+        const int kmode = g == 1 ? 2 : (g & 1);   // group -> k_id storage mode
+        // 64-row fold blocks (half the serial steps) where they fit
+        auto fold_rows = [&](int n) {
+          return (kmode != 1 && (flags & 2) && id_smem_bytes<T>(n, kmode, 64) <= smem_cap) ? 64 : 32;
+        };
+        int b0 = first;
+        while (b0 < first + cnt) {
+          const int fr = fold_rows(itasks[b0].n);
+          size_t sm0 = id_smem_bytes<T>(itasks[b0].n, kmode, fr, flags);
+          // CTAs per SM at this footprint; extend the bin while it stays the same
+          int per_sm = std::max(1, (int)(228 * 1024 / (sm0 + 1024)));
+          int b1 = b0 + 1;
+          size_t sm = sm0;
+          while (b1 < first + cnt) {
+            if (fold_rows(itasks[b1].n) != fr) break;
+            size_t s1 = id_smem_bytes<T>(itasks[b1].n, kmode, fr, flags);
+            if (std::max(1, (int)(228 * 1024 / (s1 + 1024))) != per_sm) break;
+            sm = std::max(sm, s1);
+            b1++;
+          }
+          if (sm > smem_cap) throw std::runtime_error("box too large for the ID kernel");
+          cudaStream_t st = fixed ? fixed : F->aux[(next_aux++) % n_streams];
+          launch_k_id<T>(fr, (unsigned)(b1 - b0), sm, st, (const IdTask*)d_it, b0,
+                         (const int64_t*)d_soff, (const int*)d_slen, ipool, d_irows, d_tws, P, sd, ptab,
+                         prm.id_tol, d_k, d_m, kmode, flags,
+                         (const int*)(sketching && g != 1 ? d_lsk : nullptr));
+          KI_CUDA(cudaGetLastError());
+          b0 = b1;
+        }
+      };
+      // (c) narrow boxes: fused on-the-fly assembly + TSQR + CPQR, one CTA each;
+      //     size bins on aux streams 0..2, the wide path on aux stream 3, all
+      //     concurrent
+      F->fork();
+      launch_range(0, 2, nullptr);
+      launch_range(1, 2, nullptr);
+      if constexpr (sizeof(T) == 4) {
+        // tensor-core sketches (one CTA per box, by accumulator tiles), then
+        // the pivoted QR of each sketch, in order on one aux stream
+        std::vector<int> list[2];
+        for (size_t i = 0; i < itasks.size(); i++)
+          if (grp[i] == 4) list[itasks[i].n > 128].push_back((int)i);
+        if (!list[0].empty() || !list[1].empty()) {
+          cudaStream_t ts = F->aux[0];
+          std::string tn = "id_tc_sketch@L" + std::to_string(l);
+          double tc_flops = 0;   // Y = Omega M: 2 l m n per box
+          for (const auto& lst : list)
+            for (int i : lst) tc_flops += 2.0 * lh[i] * (double)mh[i] * itasks[i].n;
+          F->stage_begin(tn.c_str(), tc_flops, 0, ts);
+          for (int tl = 0; tl < 2; tl++) {
+            if (list[tl].empty()) continue;
+            int* d_list = (int*)F->alloc(sizeof(int) * list[tl].size());
+            upload(d_list, list[tl], ts);
+            int nq_max = 16;
+            for (int i : list[tl]) nq_max = std::max(nq_max, (lh[i] + 15) & ~15);
+            const size_t sm = 2 * tc_sketch_smem(tl + 1, nq_max);   // two stages
+            const int ch = ((tl + 1) * nq_max + 31) / 32;   // accumulator chunks per thread
+            auto kern = tl ? (ch <= 2 ? k_sketch_tc<2, 2> : k_sketch_tc<2, 4>)
+                           : (ch <= 1 ? k_sketch_tc<1, 1> : ch <= 2 ? k_sketch_tc<1, 2> : k_sketch_tc<1, 4>);
+            KI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            ki::launch(kern, (unsigned)list[tl].size(), kTcThreads, sm, ts, (const IdTask*)d_it,
+                       (const int*)d_list, (const int*)d_m, (const int*)d_lsk, (const int*)ipool,
+                       (const int*)d_irows, (float*)d_tws, P, sd, ptab, F->d_err);
             KI_CUDA(cudaGetLastError());
           }
-        F->stage_end(ts);
-      }
-    }
-    // (d) wide boxes: explicit ID matrix, blocked Householder QR, then CPQR
-    {
-      std::vector<WideTask> wt, wsk;   // blocked-QR boxes, sketched boxes
-      int64_t mtot = 0, ptot = 0;
-      int maxn = 0, max_chunks = 0, max_cb = 0, max_l = 0;
-      for (size_t i = 0; i < itasks.size(); i++) {
-        if (!is_wide(grp[i])) continue;
-        WideTask w{};
-        w.task = (int)i;
-        w.n = itasks[i].n;
-        w.m = mh[i];
-        w.nI = (mh[i] - (itasks[i].mode == 0 ? 2 * np * sd : 0)) / 2;
-        w.act = itasks[i].act;
-        w.rows = itasks[i].rows;
-        w.cx = itasks[i].cx;
-        w.cy = itasks[i].cy;
-        w.cz = itasks[i].cz;
-        w.rad = itasks[i].rad_proxy;
-        w.R = itasks[i].ws;
-        if (sketching && lh[i] > 0 && lh[i] <= w.n && lh[i] <= 384) {
-          w.l = lh[i];
-          w.chunks = (w.m + kSketchRows - 1) / kSketchRows;
-          w.part = ptot;
-          ptot += (int64_t)w.chunks * w.l * w.n;
-          max_chunks = std::max(max_chunks, w.chunks);
-          max_cb = std::max(max_cb, (w.n + kSketchCols - 1) / kSketchCols);
-          max_l = std::max(max_l, w.l);
-          wsk.push_back(w);
-          continue;
+          F->stage_end(ts);
+          // the pivoted QRs of the sketches (k_cpqr), by sketch rows (32 / 64)
+          // and 32-column slabs
+          std::vector<int> cls[2][8];
+          for (const auto& lst : list)
+            for (int i : lst) cls[lh[i] > 32][(itasks[i].n + 31) / 32 - 1].push_back(i);
+          std::string qn = "id_cpqr@L" + std::to_string(l);
+          F->stage_begin(qn.c_str(), 0, 0, ts);
+          for (int lb = 0; lb < 2; lb++)
+            for (int wq = 0; wq < 8; wq++) {
+              const auto& v = cls[lb][wq];
+              if (v.empty()) continue;
+              int* d_l2 = (int*)F->alloc(sizeof(int) * v.size());
+              upload(d_l2, v, ts);
+              int lm = 0, nm = 0;
+              for (int i : v) {
+                lm = std::max(lm, lh[i]);
+                nm = std::max(nm, itasks[i].n);
+              }
+              const size_t sm = sizeof(float) * (size_t)lm * nm;
+              auto kern = lb ? k_cpqr<64> : k_cpqr<32>;
+              if (sm > 48 * 1024)
+                KI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+              ki::launch(kern, (unsigned)v.size(), 32 * (wq + 1), sm, ts, (const IdTask*)d_it,
+                         (const int*)d_l2, (const int*)d_lsk, ipool, d_irows, (float*)d_tws, prm.id_tol, d_k);
+              KI_CUDA(cudaGetLastError());
+            }
+          F->stage_end(ts);
         }
-        w.M = mtot;
-        mtot += (int64_t)w.m * w.n;
-        maxn = std::max(maxn, w.n);
-        wt.push_back(w);
       }
-      cudaStream_t ws3 = F->aux[Factorization<T>::kAux - 1];
-      if (!wt.empty() || !wsk.empty()) {
-        std::string wq = "wide_qr@L" + std::to_string(l);
-        F->stage_begin(wq.c_str(), 0, 0, ws3);
-        T* d_wpool = nullptr;
-        WideTask* d_wt = nullptr;
-        if (!wt.empty()) {
-          for (auto& w : wt) {
-            w.Tf = mtot;
-            mtot += kQrNb * kQrNb;
+      // (d) wide boxes: explicit ID matrix, blocked Householder QR, then CPQR
+      {
+        std::vector<WideTask> wt, wsk;   // blocked-QR boxes, sketched boxes
+        int64_t mtot = 0, ptot = 0;
+        int maxn = 0, max_chunks = 0, max_cb = 0, max_l = 0;
+        for (size_t i = 0; i < itasks.size(); i++) {
+          if (!is_wide(grp[i])) continue;
+          WideTask w{};
+          w.task = (int)i;
+          w.n = itasks[i].n;
+          w.m = mh[i];
+          w.nI = (mh[i] - (itasks[i].mode == 0 ? 2 * np * sd : 0)) / 2;
+          w.act = itasks[i].act;
+          w.rows = itasks[i].rows;
+          w.cx = itasks[i].cx;
+          w.cy = itasks[i].cy;
+          w.cz = itasks[i].cz;
+          w.rad = itasks[i].rad_proxy;
+          w.R = itasks[i].ws;
+          if (sketching && lh[i] > 0 && lh[i] <= w.n && lh[i] <= 384) {
+            w.l = lh[i];
+            w.chunks = (w.m + kSketchRows - 1) / kSketchRows;
+            w.part = ptot;
+            ptot += (int64_t)w.chunks * w.l * w.n;
+            max_chunks = std::max(max_chunks, w.chunks);
+            max_cb = std::max(max_cb, (w.n + kSketchCols - 1) / kSketchCols);
+            max_l = std::max(max_l, w.l);
+            wsk.push_back(w);
+            continue;
           }
-          KI_CUDA(pool_malloc((void**)&d_wpool, sizeof(T) * (mtot + 16), ws3));
-          KI_CUDA(pool_malloc((void**)&d_wt, sizeof(WideTask) * wt.size(), ws3));
-          upload(d_wt, wt, ws3);
-          ki::launch(k_wide_assemble<T>, dim3((unsigned)wt.size(), (maxn + 7) / 8), 256, 0, ws3,
-              d_wt, d_wpool, ipool, d_irows, P, sd, ptab);
-          for (int p0 = 0; p0 < maxn; p0 += kQrNb) {
-            ki::launch(k_qr_panel<T>, (unsigned)wt.size(), 256, 0, ws3, d_wt, d_wpool, p0);
-            int tiles = (maxn - p0 - kQrNb + kQrTile - 1) / kQrTile;
-            if (tiles > 0) ki::launch(k_qr_update<T>, dim3((unsigned)wt.size(), tiles), 256, 0, ws3, d_wt, d_wpool, p0);
+          w.M = mtot;
+          mtot += (int64_t)w.m * w.n;
+          maxn = std::max(maxn, w.n);
+          wt.push_back(w);
+        }
+        cudaStream_t ws3 = F->aux[Factorization<T>::kAux - 1];
+        if (!wt.empty() || !wsk.empty()) {
+          std::string wq = "wide_qr@L" + std::to_string(l);
+          F->stage_begin(wq.c_str(), 0, 0, ws3);
+          T* d_wpool = nullptr;
+          WideTask* d_wt = nullptr;
+          if (!wt.empty()) {
+            for (auto& w : wt) {
+              w.Tf = mtot;
+              mtot += kQrNb * kQrNb;
+            }
+            KI_CUDA(pool_malloc((void**)&d_wpool, sizeof(T) * (mtot + 16), ws3));
+            KI_CUDA(pool_malloc((void**)&d_wt, sizeof(WideTask) * wt.size(), ws3));
+            upload(d_wt, wt, ws3);
+            ki::launch(k_wide_assemble<T>, dim3((unsigned)wt.size(), (maxn + 7) / 8), 256, 0, ws3,
+                d_wt, d_wpool, ipool, d_irows, P, sd, ptab);
+            for (int p0 = 0; p0 < maxn; p0 += kQrNb) {
+              ki::launch(k_qr_panel<T>, (unsigned)wt.size(), 256, 0, ws3, d_wt, d_wpool, p0);
+              int tiles = (maxn - p0 - kQrNb + kQrTile - 1) / kQrTile;
+              if (tiles > 0) ki::launch(k_qr_update<T>, dim3((unsigned)wt.size(), tiles), 256, 0, ws3, d_wt, d_wpool, p0);
+            }
+            ki::launch(k_wide_triangle<T>, (unsigned)wt.size(), 256, 0, ws3, d_wt, d_wpool, d_tws);
+            KI_CUDA(cudaGetLastError());
           }
-          ki::launch(k_wide_triangle<T>, (unsigned)wt.size(), 256, 0, ws3, d_wt, d_wpool, d_tws);
-          KI_CUDA(cudaGetLastError());
+          T* d_spool = nullptr;
+          WideTask* d_wsk = nullptr;
+          if (!wsk.empty()) {
+            KI_CUDA(pool_malloc((void**)&d_spool, sizeof(T) * (ptot + 16), ws3));
+            KI_CUDA(pool_malloc((void**)&d_wsk, sizeof(WideTask) * wsk.size(), ws3));
+            upload(d_wsk, wsk, ws3);
+            const size_t skm = sizeof(T) * ((size_t)max_l * kSketchCols + kSketchSub * kSketchCols) +
+                               sizeof(uint32_t) * kSketchSub * ((max_l + 31) / 32);
+            KI_CUDA(cudaFuncSetAttribute(k_wide_sketch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem_cap));
+            ki::launch(k_wide_sketch<T>, dim3((unsigned)wsk.size(), max_chunks, max_cb), 256, skm, ws3,
+                d_wsk, d_spool, ipool, d_irows, P, sd, ptab);
+            ki::launch(k_wide_sketch_reduce<T>, (unsigned)wsk.size(), 256, 0, ws3, d_wsk, d_spool, d_tws);
+            KI_CUDA(cudaGetLastError());
+          }
+          F->stage_end(ws3);
+          std::string wc = "wide_cpqr@L" + std::to_string(l);
+          F->stage_begin(wc.c_str(), 0, 0, ws3);
+          // the pivoted QRs of the wide boxes' sketches / triangles, bins spread
+          // over every aux stream (after the sketches on ws3; the upper levels
+          // have no narrow boxes to share them with), joined back into ws3
+          cudaEvent_t wev[Factorization<T>::kAux];
+          for (auto& e : wev) KI_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+          KI_CUDA(cudaEventRecord(wev[0], ws3));
+          for (int i = 0; i + 1 < Factorization<T>::kAux; i++) KI_CUDA(cudaStreamWaitEvent(F->aux[i], wev[0], 0));
+          n_streams = Factorization<T>::kAux;
+          launch_range(2, 4, nullptr);
+          launch_range(3, 4, nullptr);
+          n_streams = Factorization<T>::kAux - 1;
+          for (int i = 0; i + 1 < Factorization<T>::kAux; i++) {
+            KI_CUDA(cudaEventRecord(wev[i + 1], F->aux[i]));
+            KI_CUDA(cudaStreamWaitEvent(ws3, wev[i + 1], 0));
+          }
+          for (auto& e : wev) KI_CUDA(cudaEventDestroy(e));
+          F->stage_end(ws3);
+          if (d_wpool) KI_CUDA(cudaFreeAsync(d_wpool, ws3));
+          if (d_wt) KI_CUDA(cudaFreeAsync(d_wt, ws3));
+          if (d_spool) KI_CUDA(cudaFreeAsync(d_spool, ws3));
+          if (d_wsk) KI_CUDA(cudaFreeAsync(d_wsk, ws3));
         }
-        T* d_spool = nullptr;
-        WideTask* d_wsk = nullptr;
-        if (!wsk.empty()) {
-          KI_CUDA(pool_malloc((void**)&d_spool, sizeof(T) * (ptot + 16), ws3));
-          KI_CUDA(pool_malloc((void**)&d_wsk, sizeof(WideTask) * wsk.size(), ws3));
-          upload(d_wsk, wsk, ws3);
-          const size_t skm = sizeof(T) * ((size_t)max_l * kSketchCols + kSketchSub * kSketchCols) +
-                             sizeof(uint32_t) * kSketchSub * ((max_l + 31) / 32);
-          KI_CUDA(cudaFuncSetAttribute(k_wide_sketch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem_cap));
-          ki::launch(k_wide_sketch<T>, dim3((unsigned)wsk.size(), max_chunks, max_cb), 256, skm, ws3,
-              d_wsk, d_spool, ipool, d_irows, P, sd, ptab);
-          ki::launch(k_wide_sketch_reduce<T>, (unsigned)wsk.size(), 256, 0, ws3, d_wsk, d_spool, d_tws);
-          KI_CUDA(cudaGetLastError());
-        }
-        F->stage_end(ws3);
-        std::string wc = "wide_cpqr@L" + std::to_string(l);
-        F->stage_begin(wc.c_str(), 0, 0, ws3);
-        // the pivoted QRs of the wide boxes' sketches / triangles, bins spread
-        // over every aux stream (after the sketches on ws3; the upper levels
-        // have no narrow boxes to share them with), joined back into ws3
-        cudaEvent_t wev[Factorization<T>::kAux];
-        for (auto& e : wev) KI_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-        KI_CUDA(cudaEventRecord(wev[0], ws3));
-        for (int i = 0; i + 1 < Factorization<T>::kAux; i++) KI_CUDA(cudaStreamWaitEvent(F->aux[i], wev[0], 0));
-        n_streams = Factorization<T>::kAux;
-        launch_range(2, 4, nullptr);
-        launch_range(3, 4, nullptr);
-        n_streams = Factorization<T>::kAux - 1;
-        for (int i = 0; i + 1 < Factorization<T>::kAux; i++) {
-          KI_CUDA(cudaEventRecord(wev[i + 1], F->aux[i]));
-          KI_CUDA(cudaStreamWaitEvent(ws3, wev[i + 1], 0));
-        }
-        for (auto& e : wev) KI_CUDA(cudaEventDestroy(e));
-        F->stage_end(ws3);
-        if (d_wpool) KI_CUDA(cudaFreeAsync(d_wpool, ws3));
-        if (d_wt) KI_CUDA(cudaFreeAsync(d_wt, ws3));
-        if (d_spool) KI_CUDA(cudaFreeAsync(d_spool, ws3));
-        if (d_wsk) KI_CUDA(cudaFreeAsync(d_wsk, ws3));
       }
-    }
-    F->join(Factorization<T>::kAux);
-    F->stage_end();
-    KI_CUDA(cudaGetLastError());
-    KI_CUDA(cudaMemcpyAsync(kh.data(), d_k, sizeof(int) * kh.size(), cudaMemcpyDeviceToHost, s));
-    KI_CUDA(cudaStreamSynchronize(s));
-    if (sketching) {
-      // boxes whose sketch did not reveal the rank (k = -1): the plain ID
-      std::vector<int> fb;
+      F->join(Factorization<T>::kAux);
+      F->stage_end();
+      KI_CUDA(cudaGetLastError());
+      KI_CUDA(cudaMemcpyAsync(kh.data(), d_k, sizeof(int) * kh.size(), cudaMemcpyDeviceToHost, s));
+      KI_CUDA(cudaStreamSynchronize(s));
+      if (sketching) {
+        // boxes whose sketch did not reveal the rank (k = -1): the plain ID
+        std::vector<int> fb;
+        for (size_t i = 0; i < kh.size(); i++) {
+          if (lh[i] > 0 && (lh[i] < itasks[i].n || is_wide(grp[i]))) F->n_sketched++;
+          if (kh[i] < 0) fb.push_back((int)i);
+        }
+        if (!fb.empty()) {
+          // mode 0 (triangle in shared memory) where it fits, else mode 1
+          // (triangle in the task's global scratch)
+          std::vector<IdTask> t2;
+          std::vector<int> m2;
+          size_t sm[2] = {0, 0};
+          int cnt0 = 0;
+          for (int pass = 0; pass < 2; pass++)
+            for (int i : fb) {
+              const int md = id_smem_bytes<T>(itasks[i].n, 0, 32, 2) <= smem_cap ? 0 : 1;
+              if (md != pass) continue;
+              t2.push_back(itasks[i]);
+              m2.push_back(mh[i]);
+              sm[md] = std::max(sm[md], id_smem_bytes<T>(itasks[i].n, md, 32, 2));
+              if (md == 0) cnt0++;
+            }
+          if (sm[1] > smem_cap) throw std::runtime_error("box too large for the ID kernel");
+          std::vector<int> fb2;
+          for (int pass = 0; pass < 2; pass++)
+            for (int i : fb)
+              if ((id_smem_bytes<T>(itasks[i].n, 0, 32, 2) <= smem_cap ? 0 : 1) == pass) fb2.push_back(i);
+          fb.swap(fb2);
+          IdTask* d_t2 = (IdTask*)F->alloc(sizeof(IdTask) * t2.size());
+          int* d_m2 = (int*)F->alloc(sizeof(int) * t2.size());
+          int* d_k2 = (int*)F->alloc(sizeof(int) * t2.size());
+          upload(d_t2, t2, s);
+          upload(d_m2, m2, s);
+          std::string fname = "id_fallback@L" + std::to_string(l);
+          F->stage_begin(fname.c_str(), 0, 0);
+          if (cnt0 > 0)
+            launch_k_id<T>(32, (unsigned)cnt0, sm[0], s, (const IdTask*)d_t2, 0, (const int64_t*)d_soff,
+                           (const int*)d_slen, ipool, d_irows, d_tws, P, sd, ptab, prm.id_tol, d_k2, d_m2,
+                           0, 2, (const int*)nullptr);
+          if ((int)t2.size() > cnt0)
+            launch_k_id<T>(32, (unsigned)(t2.size() - cnt0), sm[1], s, (const IdTask*)d_t2, cnt0,
+                           (const int64_t*)d_soff, (const int*)d_slen, ipool, d_irows, d_tws, P, sd, ptab,
+                           prm.id_tol, d_k2, d_m2, 1, 2, (const int*)nullptr);
+          F->stage_end();
+          KI_CUDA(cudaGetLastError());
+          std::vector<int> k2(t2.size());
+          KI_CUDA(cudaMemcpyAsync(k2.data(), d_k2, sizeof(int) * k2.size(), cudaMemcpyDeviceToHost, s));
+          KI_CUDA(cudaStreamSynchronize(s));
+          for (size_t j = 0; j < fb.size(); j++) kh[fb[j]] = k2[j];
+          F->n_fallback += (int)fb.size();
+        }
+      }
+      // box log: the predictor's features, n, the rank and the level of every ID box
       for (size_t i = 0; i < kh.size(); i++) {
-        if (lh[i] > 0 && (lh[i] < itasks[i].n || is_wide(grp[i]))) F->n_sketched++;
-        if (kh[i] < 0) fb.push_back((int)i);
+        F->box_log.insert(F->box_log.end(), fh.begin() + kMlpIn * i, fh.begin() + kMlpIn * (i + 1));
+        F->box_log.push_back((float)itasks[i].n);
+        F->box_log.push_back((float)kh[i]);
+        F->box_log.push_back((float)l);
       }
-      if (!fb.empty()) {
-        // mode 0 (triangle in shared memory) where it fits, else mode 1
-        // (triangle in the task's global scratch)
-        std::vector<IdTask> t2;
-        std::vector<int> m2;
-        size_t sm[2] = {0, 0};
-        int cnt0 = 0;
-        for (int pass = 0; pass < 2; pass++)
-          for (int i : fb) {
-            const int md = id_smem_bytes<T>(itasks[i].n, 0, 32, 2) <= smem_cap ? 0 : 1;
-            if (md != pass) continue;
-            t2.push_back(itasks[i]);
-            m2.push_back(mh[i]);
-            sm[md] = std::max(sm[md], id_smem_bytes<T>(itasks[i].n, md, 32, 2));
-            if (md == 0) cnt0++;
-          }
-        if (sm[1] > smem_cap) throw std::runtime_error("box too large for the ID kernel");
-        std::vector<int> fb2;
-        for (int pass = 0; pass < 2; pass++)
-          for (int i : fb)
-            if ((id_smem_bytes<T>(itasks[i].n, 0, 32, 2) <= smem_cap ? 0 : 1) == pass) fb2.push_back(i);
-        fb.swap(fb2);
-        IdTask* d_t2 = (IdTask*)F->alloc(sizeof(IdTask) * t2.size());
-        int* d_m2 = (int*)F->alloc(sizeof(int) * t2.size());
-        int* d_k2 = (int*)F->alloc(sizeof(int) * t2.size());
-        upload(d_t2, t2, s);
-        upload(d_m2, m2, s);
-        std::string fname = "id_fallback@L" + std::to_string(l);
-        F->stage_begin(fname.c_str(), 0, 0);
-        if (cnt0 > 0)
-          launch_k_id<T>(32, (unsigned)cnt0, sm[0], s, (const IdTask*)d_t2, 0, (const int64_t*)d_soff,
-                         (const int*)d_slen, ipool, d_irows, d_tws, P, sd, ptab, prm.id_tol, d_k2, d_m2,
-                         0, 2, (const int*)nullptr);
-        if ((int)t2.size() > cnt0)
-          launch_k_id<T>(32, (unsigned)(t2.size() - cnt0), sm[1], s, (const IdTask*)d_t2, cnt0,
-                         (const int64_t*)d_soff, (const int*)d_slen, ipool, d_irows, d_tws, P, sd, ptab,
-                         prm.id_tol, d_k2, d_m2, 1, 2, (const int*)nullptr);
-        F->stage_end();
-        KI_CUDA(cudaGetLastError());
-        std::vector<int> k2(t2.size());
-        KI_CUDA(cudaMemcpyAsync(k2.data(), d_k2, sizeof(int) * k2.size(), cudaMemcpyDeviceToHost, s));
-        KI_CUDA(cudaStreamSynchronize(s));
-        for (size_t j = 0; j < fb.size(); j++) kh[fb[j]] = k2[j];
-        F->n_fallback += (int)fb.size();
+      {
+        LevelStat ls;
+        ls.level = l;
+        ls.boxes = (int)lv.size();
+        ls.id_boxes = (int)itasks.size();
+        for (size_t i = 0; i < itasks.size(); i++) {
+          ls.max_n = std::max(ls.max_n, itasks[i].n);
+          ls.max_m = std::max(ls.max_m, mh[i]);
+          ls.max_k = std::max(ls.max_k, kh[i]);
+          ls.sum_n += itasks[i].n;
+          ls.sum_m += mh[i];
+          ls.sum_k += kh[i];
+          ls.compressed += kh[i] > 0;
+          ls.mode_count[grp[i]]++;
+        }
+        F->level_stats.push_back(ls);
       }
-    }
-    // box log: the predictor's features, n, the rank and the level of every ID box
-    for (size_t i = 0; i < kh.size(); i++) {
-      F->box_log.insert(F->box_log.end(), fh.begin() + kMlpIn * i, fh.begin() + kMlpIn * (i + 1));
-      F->box_log.push_back((float)itasks[i].n);
-      F->box_log.push_back((float)kh[i]);
-      F->box_log.push_back((float)l);
-    }
-    {
-      LevelStat ls;
-      ls.level = l;
-      ls.boxes = (int)lv.size();
-      ls.id_boxes = (int)itasks.size();
-      for (size_t i = 0; i < itasks.size(); i++) {
-        ls.max_n = std::max(ls.max_n, itasks[i].n);
-        ls.max_m = std::max(ls.max_m, mh[i]);
-        ls.max_k = std::max(ls.max_k, kh[i]);
-        ls.sum_n += itasks[i].n;
-        ls.sum_m += mh[i];
-        ls.sum_k += kh[i];
-        ls.compressed += kh[i] > 0;
-        ls.mode_count[grp[i]]++;
+      {
+        double fl = 0, by = 0;
+        for (size_t i = 0; i < itasks.size(); i++) {
+          double m = mh[i], n = itasks[i].n, k = kh[i] > 0 ? kh[i] : std::min(m, n), r = n - k;
+          fl += std::max(0.0, 4 * m * n * k - 2 * k * k * (m + n) + 4.0 / 3.0 * k * k * k + k * k * r);
+          by += sizeof(T) * (double)k * r;
+        }
+        F->prof_open[id_rec].flops = fl;
+        F->prof_open[id_rec].bytes = by;
       }
-      F->level_stats.push_back(ls);
-    }
-    {
-      double fl = 0, by = 0;
-      for (size_t i = 0; i < itasks.size(); i++) {
-        double m = mh[i], n = itasks[i].n, k = kh[i] > 0 ? kh[i] : std::min(m, n), r = n - k;
-        fl += std::max(0.0, 4 * m * n * k - 2 * k * k * (m + n) + 4.0 / 3.0 * k * k * k + k * k * r);
-        by += sizeof(T) * (double)k * r;
-      }
-      F->prof_open[id_rec].flops = fl;
-      F->prof_open[id_rec].bytes = by;
     }
 
     // ---- Schur elimination of the compressed boxes
@@ -3694,8 +3903,16 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       kk_tot += k * k;
       ws_tot += n * n + 3 * r * k;
     }
-    LF.n_comp = (int)ci_list.size();
-    if (ci_list.empty()) continue;
+    for (int b : kept) {
+      const BoxFactor<T>& pf = prev->box_factors[reuse_of[b]];
+      const int64_t k = pf.k, r = pf.n - pf.k;
+      tr_tot += k * r;
+      x_tot += r * r;
+      r_tot += r;
+      kk_tot += k * k;
+    }
+    LF.n_comp = (int)(ci_list.size() + kept.size());
+    if (LF.n_comp == 0) continue;
     T* d_Tp = (T*)F->alloc(Tsz * (tr_tot + 1));
     T* d_LUp = (T*)F->alloc(Tsz * (2 * tr_tot + 1));
     T* d_Xp = (T*)F->alloc(Tsz * (x_tot + 1));
@@ -3704,9 +3921,11 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     T* d_sws = (T*)F->alloc(Tsz * (ws_tot + 1));
     std::vector<SchurTask<T>> st;
     std::vector<SweepTask<T>> sw;
+    std::vector<int> sw_box;   // box of each sweep descriptor
     int64_t o_tr = 0, o_x = 0, o_r = 0, o_kk = 0, o_ws = 0;
     for (int i : ci_list) {
       int b = comp[i];
+      sw_box.push_back(b);
       int n = itasks[i].n, k = kh[i], r = n - k;
       size_t pos = tree.boxes[b].level_pos;
       SchurTask<T> t{};
@@ -3751,6 +3970,55 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       LF.sum_n += n;
       LF.sum_r += r;
     }
+    // boxes kept from prev: their lists and factors copied into this level's
+    // pools (after the recomputed boxes, whose Schur tasks match sw[0..st))
+    std::vector<CopySeg> segs;
+    auto copy_seg = [&](const void* src, void* dst, int64_t bytes) {
+      if (bytes > 0) segs.push_back(CopySeg{src, dst, bytes / 4});
+    };
+    for (int b : kept) {
+      const BoxFactor<T>& pf = prev->box_factors[reuse_of[b]];
+      const int n = pf.n, k = pf.k, r = n - k;
+      sw_box.push_back(b);
+      SweepTask<T> w{};
+      w.n = n;
+      w.k = k;
+      const int64_t pact = pact_top;
+      pact_top += n;
+      w.pact = ipool + pact;
+      w.Tm = d_Tp + o_tr;
+      w.L = d_LUp + 2 * o_tr;
+      w.U = d_LUp + 2 * o_tr + (int64_t)k * r;
+      w.X = d_Xp + o_x;
+      w.piv = d_pivp + o_r;
+      w.Xi_formed = 1;
+      T* At = d_At + o_kk;
+      o_tr += (int64_t)k * r;
+      o_x += (int64_t)r * r;
+      o_r += r;
+      o_kk += (int64_t)k * k;
+      copy_seg(prev->d_ipool + pf.pact, ipool + pact, sizeof(int) * (int64_t)n);
+      copy_seg(pf.Tm, const_cast<T*>(w.Tm), Tsz * (int64_t)k * r);
+      copy_seg(pf.L, const_cast<T*>(w.L), Tsz * (int64_t)k * r);
+      copy_seg(pf.U, const_cast<T*>(w.U), Tsz * (int64_t)k * r);
+      copy_seg(pf.X, const_cast<T*>(w.X), Tsz * (int64_t)r * r);
+      copy_seg(pf.piv, const_cast<int*>(w.piv), sizeof(int) * (int64_t)r);
+      copy_seg(pf.tile, At, Tsz * (int64_t)k * k);
+      sw.push_back(w);
+      HostBox& h = hb[b];
+      h.compressed = true;
+      h.k = k;
+      h.pact = pact;
+      h.tile = At;
+      F->n_compressed++;
+      F->n_redundant += r;
+      LF.max_n = std::max(LF.max_n, n);
+      LF.max_mat = std::max(LF.max_mat, std::max(r * r, k * r));
+      LF.sum_kr += (double)k * r;
+      LF.sum_r2 += (double)r * r;
+      LF.sum_n += n;
+      LF.sum_r += r;
+    }
     if (sizeof(T) < sizeof(double)) {
       // FP32: explicit inverses of the redundant blocks for the sweeps (the
       // FP64 form keeps the reference's LU substitution)
@@ -3765,10 +4033,26 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         const int64_t r = sw[q].n - sw[q].k;
         if (r <= kInvMax) {
           sw[q].Xi = d_xi + o;
-          st[q].Xi = d_xi + o;
+          if (q < st.size()) st[q].Xi = d_xi + o;
           o += r * r;
         }
       }
+      for (size_t q = st.size(); q < sw.size(); q++) {
+        const BoxFactor<T>& pf = prev->box_factors[reuse_of[sw_box[q]]];
+        if (!sw[q].Xi || !pf.Xi) throw std::logic_error("re-factorization: inverse missing");
+        const int64_t r = sw[q].n - sw[q].k;
+        copy_seg(pf.Xi, const_cast<T*>(sw[q].Xi), Tsz * r * r);
+      }
+    }
+    if (!segs.empty()) {
+      CopySeg* d_seg = (CopySeg*)F->alloc(sizeof(CopySeg) * segs.size());
+      upload(d_seg, segs, s);
+      double by = 0;
+      for (const auto& q : segs) by += 8.0 * q.words;
+      F->stage_begin(("reuse@L" + std::to_string(l)).c_str(), 0, by);
+      ki::launch(k_copy_segments, (unsigned)segs.size(), 256, 0, s, (const CopySeg*)d_seg);
+      F->stage_end();
+      KI_CUDA(cudaGetLastError());
     }
     SchurTask<T>* d_st = (SchurTask<T>*)F->alloc(sizeof(SchurTask<T>) * st.size());
     double sf = 0, sb = 0;
@@ -3895,7 +4179,23 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       }
     }
     for (int i : ci_list) F->rank_hist.push_back(kh[i]);
+    for (int b : kept) F->rank_hist.push_back(hb[b].k);
+    for (size_t q = 0; q < sw.size(); q++) {
+      const HostBox& h = hb[sw_box[q]];
+      BoxFactor<T>& bf = F->box_factors[sw_box[q]];
+      bf.compressed = true;
+      bf.k = h.k;
+      bf.pact = h.pact;
+      bf.tile = (const T*)h.tile;
+      bf.Tm = sw[q].Tm;
+      bf.L = sw[q].L;
+      bf.U = sw[q].U;
+      bf.X = sw[q].X;
+      bf.piv = sw[q].piv;
+      bf.Xi = sw[q].Xi;
+    }
   }
+  for (size_t b = 0; b < tree.boxes.size(); b++) F->box_factors[b].n = hb[b].n;
 
   // all levels' sweep descriptors, ascending n, in bins of equal CTAs per SM
   // at 32 columns (the diagonal solves of different levels touch disjoint
@@ -4228,10 +4528,12 @@ template void solve_device_arena<float>(Factorization<float>&, float*, int, floa
 
 template std::unique_ptr<Factorization<double>> factorize<double>(
     const Params&, int, const double*, const double*, const double*, const double*,
-    const HoleDesc&, cudaStream_t, const double*, const std::function<void()>&);
+    const HoleDesc&, cudaStream_t, const double*, const std::function<void()>&,
+    const Factorization<double>*);
 template std::unique_ptr<Factorization<float>> factorize<float>(
     const Params&, int, const double*, const double*, const double*, const double*,
-    const HoleDesc&, cudaStream_t, const double*, const std::function<void()>&);
+    const HoleDesc&, cudaStream_t, const double*, const std::function<void()>&,
+    const Factorization<float>*);
 template void solve_device<double>(Factorization<double>&, double*, int, double*, const double*);
 template void solve_device<float>(Factorization<float>&, float*, int, float*, const float*);
 template struct Factorization<double>;

@@ -43,6 +43,25 @@ struct LevelFactor {
   double sum_kr = 0, sum_r2 = 0, sum_n = 0, sum_r = 0;   // over the compressed boxes (sweep work)
 };
 
+// Per box of the tree, the factors a later re-factorization of a perturbed
+// boundary copies instead of recomputing (SkelFactorization::skeletonize
+// skips boxes still `compressed` after QuadTree::perturb,
+// kern_interp/skel_factorization/skel_factorization.cpp:199-208).
+template <typename T>
+struct BoxFactor {
+  int n = 0;                 // active DOFs at the box's level
+  int k = 0;                 // skeleton size (compressed boxes)
+  bool compressed = false;
+  int64_t pact = 0;          // pool offset of the permuted active list (skeleton first)
+  const T* tile = nullptr;   // compressed: Schur-updated skeleton block K~ss (k x k)
+  const T* Tm = nullptr;     // interpolation matrix (k x r)
+  const T* L = nullptr;      // k x r
+  const T* U = nullptr;      // r x k
+  const T* X = nullptr;      // LU of the redundant block (r x r)
+  const int* piv = nullptr;  // its pivots (r)
+  const T* Xi = nullptr;     // explicit inverse of the redundant block (FP32) or null
+};
+
 // Device-time record of one launch group (CUDA events on the factor's stream).
 struct StageRec {
   std::string stage;
@@ -130,6 +149,12 @@ struct Factorization {
   double tree_codes_seconds = 0;   // from the start of the factorization to the GPU-built tree on the host
   size_t device_bytes = 0;
   std::vector<void*> owned;   // device allocations to free
+  // re-factorization: every box's factors (index = box of `tree`), the
+  // integer pool their lists live in, and how many boxes this factorization
+  // copied from the one it updated
+  std::vector<BoxFactor<T>> box_factors;
+  const int* d_ipool = nullptr;
+  int n_reused = 0;
 
   ~Factorization();
   void* alloc(size_t bytes);
@@ -156,12 +181,22 @@ template <typename T>
 // d_inputs (optional): the same four arrays already on the device, laid out
 // points (dim n) | normals (dim n) | weights (n) | curvatures (n), kept alive
 // by the caller for the factorization's lifetime; otherwise they are copied.
+// prev (optional): a factorization of the same problem before a boundary
+// perturbation (QuadTree::perturb, kern_interp/quadtree/quadtree.cpp:581-890).
+// A box whose active DOFs, their data (the precision-T point arrays the
+// kernels read) and its near field are unchanged -- it has a box of prev's
+// tree at the same level and centre, the same leaf DOF list or the same
+// reused children, and neighbours that are unchanged in the same sense --
+// gets prev's factors copied instead of an ID and a Schur elimination.  Used
+// only when prev has the same number of points and the same parameters;
+// prev must stay alive until this returns.
 std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, const double* points,
                                             const double* normals, const double* weights,
                                             const double* curvatures, const HoleDesc& holes,
                                             cudaStream_t stream,
                                             const double* d_inputs = nullptr,
-                                            const std::function<void()>& after_tree = nullptr);
+                                            const std::function<void()>& after_tree = nullptr,
+                                            const Factorization<T>* prev = nullptr);
 
 // A bump allocator over caller-provided device memory.
 struct ScratchArena {

@@ -187,6 +187,24 @@ def disc_with_ellipses(n_unknowns=1 << 20, n_holes=64, radius=2.0, seed=1, q=16)
                    hole_count=np.array(counts, np.int32), name="disc_with_ellipses")
 
 
+def move_hole(prob, h, delta):
+    """The boundary with hole h translated by `delta` (its nodes and centre;
+    normals, weights and curvatures unchanged), every other node bitwise as
+    before and at the same index: a perturbation frame of the reference's
+    updating experiments, which move one hole's centre per frame
+    (kern_interp/boundaries/ex2boundary.cpp:39-56,
+    kern_interp/experiments/experiment_two.cpp:54-60)."""
+    s, c = int(prob.hole_start[h]), int(prob.hole_count[h])
+    d = np.asarray(delta, np.float64)
+    pts = prob.points.copy()
+    pts[s:s + c] += d[None]
+    cs = prob.hole_centers.copy()
+    cs[h] += d
+    return Problem(pts, prob.normals.copy(), prob.weights.copy(), prob.curvatures.copy(),
+                   hole_centers=cs, hole_start=prob.hole_start.copy(),
+                   hole_count=prob.hole_count.copy(), name=prob.name + "_moved")
+
+
 def sample_circles(n_holes, rng, r_lo=0.005, r_hi=0.02, domain_radius=1.0, gap=0.005,
                    max_tries=2000000):
     """Non-overlapping circles with radii U(r_lo, r_hi), centres rejection-

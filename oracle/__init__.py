@@ -77,6 +77,48 @@ class _Lib:
         self.solve_fn = f
 
 
+def ref_update_solve(frames, rhs, tol, threads=1, solution_dim=1, pde=0):
+    """The reference's incremental re-factorization (compiled reference only,
+    default tree/proxy parameters): frames[0] initialized and skeletonized,
+    every later frame applied with QuadTree::perturb and skeletonized again
+    (kiref_update_solve in ref_driver.cpp).  frames: problems of one size and
+    hole layout; rhs: one (N,) right-hand side per frame.  Returns (mu
+    (frames, N), alpha (frames, n_border), seconds (frames,), compressed
+    boxes (frames,))."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_ki_build_ref", os.path.join(HERE, "build_ref.py"))
+    br = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(br)
+    load_openblas()
+    lib = ctypes.CDLL(br.build())
+    fn = lib.kiref_update_solve
+    fn.argtypes = [ctypes.c_int] * 5 + [_P] * 4 + [ctypes.c_int] + [_P] * 4 + \
+                  [ctypes.c_double, ctypes.c_int] + [_P] * 3
+    fn.restype = ctypes.c_int
+    p0 = frames[0]
+    dim = int(np.asarray(p0.points).shape[1])
+    nf, n = len(frames), p0.n
+    N = n * solution_dim
+    c = 1 if solution_dim == 1 else (3 if dim == 2 else 6)
+    nb = c * p0.n_holes
+    cat = lambda k: np.ascontiguousarray(np.concatenate(
+        [np.asarray(getattr(p, k), np.float64).reshape(-1) for p in frames]))
+    pts, nrm, wts, cur, hc = (cat(k) for k in
+                              ("points", "normals", "weights", "curvatures", "hole_centers"))
+    hs = np.ascontiguousarray(p0.hole_start, np.int32)
+    hn = np.ascontiguousarray(p0.hole_count, np.int32)
+    b = np.ascontiguousarray(np.concatenate([np.asarray(r, np.float64).reshape(-1) for r in rhs]))
+    mu = np.zeros(nf * N)
+    alpha = np.zeros(max(1, nf * nb))
+    st = np.zeros(2 * nf)
+    rc = fn(n, dim, solution_dim, pde, nf, _dp(pts), _dp(nrm), _dp(wts), _dp(cur), p0.n_holes,
+            _dp(hc), _dp(hs), _dp(hn), _dp(b), tol, threads, _dp(mu), _dp(alpha), _dp(st))
+    if rc != 0:
+        raise RuntimeError("reference update solve failed")
+    return (mu.reshape(nf, N), alpha[:nf * nb].reshape(nf, nb), st[0::2].copy(),
+            st[1::2].astype(int))
+
+
 def solve(prob, rhs, tol, threads=1, leaf=64, proxy=None, ratio=2.0, min_compress=64,
           solution_dim=1, pde=0, impl="port"):
     """Factor + solve with the oracle.  rhs: (N, nrhs).  Returns (mu, alpha,

@@ -165,6 +165,122 @@ int kiref_solve(int n_points, int domain_dim, int solution_dim, int pde,
   return 0;
 }
 
+// Incremental re-factorization as the reference's updating experiments run
+// it (kern_interp/experiments/experiment_two.cpp:49-70, the updating test
+// kern_interp/kern_interp_test.cpp:424-465): frame 0 is initialized and
+// skeletonized; each later frame's boundary data replace the previous ones,
+// then Kernel::update_data, QuadTree::perturb and a skeletonize that skips
+// the boxes perturb left compressed, then the bordered or plain solve of the
+// frame's one right-hand side.  Arrays hold `frames` frames back to back
+// (points/normals dim n, weights/curvatures n, hole centres dim n_holes,
+// rhs N; the hole node ranges are the same in every frame).  Outputs per
+// frame: mu (N), alpha (border columns), stats[2 f] skeletonize seconds and
+// stats[2 f + 1] boxes compressed after it.
+int kiref_update_solve(int n_points, int domain_dim, int solution_dim, int pde, int frames,
+                       const double* points, const double* normals, const double* weights,
+                       const double* curvatures, int n_holes, const double* hole_centers,
+                       const int* hole_start, const int* hole_count, const double* rhs,
+                       double id_tol, int threads, double* mu_out, double* alpha_out,
+                       double* stats) {
+  const int d = domain_dim;
+  const int N = n_points * solution_dim;
+  openblas_set_num_threads(1);
+  ArrayBoundary boundary;
+  auto load = [&](int f) {
+    boundary.points.assign(points + (size_t)f * n_points * d, points + (size_t)(f + 1) * n_points * d);
+    boundary.normals.assign(normals + (size_t)f * n_points * d,
+                            normals + (size_t)(f + 1) * n_points * d);
+    boundary.weights.assign(weights + (size_t)f * n_points, weights + (size_t)(f + 1) * n_points);
+    if (curvatures)
+      boundary.curvatures.assign(curvatures + (size_t)f * n_points,
+                                 curvatures + (size_t)(f + 1) * n_points);
+    boundary.holes.clear();
+    for (int h = 0; h < n_holes; h++) {
+      kern_interp::Hole hole;
+      const double* c0 = hole_centers + ((size_t)f * n_holes + h) * d;
+      hole.center = PointVec(std::vector<double>(c0, c0 + d));
+      hole.radius = 0.;
+      hole.num_nodes = hole_count[h];
+      boundary.holes.push_back(hole);
+    }
+    boundary.num_outer_nodes = n_holes > 0 ? hole_start[0] : n_points;
+    boundary.boundary_values = kern_interp::ki_Mat(N, 1);
+  };
+  load(0);
+  kern_interp::Kernel kernel(solution_dim, d, (kern_interp::Kernel::Pde)pde, &boundary,
+                             std::vector<double>());
+  kern_interp::QuadTree quadtree;
+  quadtree.initialize_tree(&boundary, solution_dim, d);
+  kern_interp::SkelFactorization skel(id_tol, threads);
+  for (int f = 0; f < frames; f++) {
+    if (f > 0) {
+      load(f);
+      kernel.update_data(&boundary);
+      quadtree.perturb(boundary);
+    }
+    if (d == 3) {
+      if (solution_dim == 1) kernel.compute_diag_entries_3dlaplace(&boundary);
+      else kernel.compute_diag_entries_3dstokes(&boundary);
+    }
+    const double* pts = points + (size_t)f * n_points * d;
+    const double* w = weights + (size_t)f * n_points;
+    const double* hc = hole_centers + (size_t)f * n_holes * d;
+    if (n_holes > 0) {
+      quadtree.U = kern_interp::initialize_U_mat(kernel.pde, boundary.holes, boundary.points, d);
+      const int c = quadtree.U.width() / n_holes;
+      kern_interp::ki_Mat Psi(c * n_holes, N);
+      for (int h = 0; h < n_holes; h++)
+        for (int p = hole_start[h]; p < hole_start[h] + hole_count[h]; p++) {
+          if (solution_dim == 1) {
+            Psi.set(h, p, w[p]);
+          } else if (d == 2) {
+            Psi.set(3 * h, 2 * p, w[p]);
+            Psi.set(3 * h + 1, 2 * p + 1, w[p]);
+            Psi.set(3 * h + 2, 2 * p, w[p] * pts[2 * p + 1]);
+            Psi.set(3 * h + 2, 2 * p + 1, -w[p] * pts[2 * p]);
+          } else {
+            double r[3];
+            for (int q = 0; q < 3; q++) r[q] = pts[3 * p + q] - hc[3 * h + q];
+            Psi.set(6 * h, 3 * p, w[p]);
+            Psi.set(6 * h + 1, 3 * p + 1, w[p]);
+            Psi.set(6 * h + 2, 3 * p + 2, w[p]);
+            Psi.set(6 * h + 4, 3 * p, w[p] * r[2]);
+            Psi.set(6 * h + 5, 3 * p, -w[p] * r[1]);
+            Psi.set(6 * h + 3, 3 * p + 1, -w[p] * r[2]);
+            Psi.set(6 * h + 5, 3 * p + 1, w[p] * r[0]);
+            Psi.set(6 * h + 3, 3 * p + 2, w[p] * r[1]);
+            Psi.set(6 * h + 4, 3 * p + 2, -w[p] * r[0]);
+          }
+        }
+      quadtree.Psi = Psi;
+    }
+    double t0 = omp_get_wtime();
+    skel.skeletonize(kernel, &quadtree);
+    double t1 = omp_get_wtime();
+    kern_interp::ki_Mat fv(N, 1);
+    std::memcpy(fv.mat, rhs + (size_t)f * N, sizeof(double) * N);
+    kern_interp::ki_Mat mu(N, 1);
+    if (n_holes > 0) {
+      kern_interp::ki_Mat alpha(quadtree.U.width(), 1);
+      skel.multiply_connected_solve(quadtree, &mu, &alpha, fv);
+      if (alpha_out)
+        std::memcpy(alpha_out + (size_t)f * quadtree.U.width(), alpha.mat,
+                    sizeof(double) * quadtree.U.width());
+    } else {
+      skel.solve(quadtree, &mu, fv);
+    }
+    std::memcpy(mu_out + (size_t)f * N, mu.mat, sizeof(double) * N);
+    int compressed = 0;
+    for (auto* level : quadtree.levels)
+      for (auto* node : level->nodes) compressed += node->compressed;
+    if (stats) {
+      stats[2 * f] = t1 - t0;
+      stats[2 * f + 1] = compressed;
+    }
+  }
+  return 0;
+}
+
 // Dense Nystrom matrix K(all, all) of the reference kernel
 // (Kernel::operator(), kern_interp/kernel/kernel.cpp:304-360), column-major.
 int kiref_dense(int n_points, int domain_dim, int solution_dim, int pde,

@@ -52,6 +52,27 @@ def golden_cases():
 
 
 @pytest.fixture(scope="session")
+def golden_updates():
+    """name -> (frames, rhs, params, stored arrays) of the re-factorization
+    fixtures: frame 0 is the stored problem, each later frame the one before
+    with the stored hole moved by the stored delta (an exact translation);
+    rhs (N, 1) serves every frame."""
+    sys.path.insert(0, GOLDEN)
+    import make_golden
+    geo = make_golden.load_geometry()
+    out = {}
+    for name, _, _, p, _ in make_golden.update_cases():
+        data = np.load(os.path.join(GOLDEN, name + ".npz"))
+        dim = data["points"].shape[1]
+        prob = geo.Problem(data["points"], data["normals"], data["weights"], data["curvatures"],
+                           hole_centers=data["hole_centers"].reshape(-1, dim),
+                           hole_start=data["hole_start"], hole_count=data["hole_count"], name=name)
+        moves = list(zip(data["move_hole"].tolist(), data["move_delta"]))
+        out[name] = (make_golden.update_frames(geo, prob, moves), data["rhs"], p, data)
+    return out
+
+
+@pytest.fixture(scope="session")
 def have_gpu():
     try:
         import torch

@@ -9,6 +9,12 @@ the input arrays themselves (boundary generators are not bit-reproducible
 across CPU architectures: libm and numpy differ in the last bits), and a
 SHA-1 of those inputs.  The inputs were made by
 kern-interp-dev_gb300/geometry.py (seeded).
+
+The update_* fixtures hold the reference's incremental re-factorization
+(QuadTree::perturb then skeletonize, oracle.ref_update_solve) over frames
+that each move one hole, beside a fresh reference factorization of every
+frame: frame 0's arrays, the moves, one right-hand side, and per frame the
+two solutions and the two skeletonize times.
 """
 import hashlib
 import importlib.util
@@ -93,6 +99,66 @@ def cases():
     return out
 
 
+def update_cases():
+    """(name, problem, rhs, params, moves) of the re-factorization fixtures:
+    frame 0 is the problem, each later frame moves one hole by (hole, delta)
+    from the frame before (geometry.move_hole: an exact translation, so the
+    frames rebuild bit for bit from frame 0 on any machine); one right-hand
+    side serves every frame."""
+    g = load_geometry()
+    out = []
+    prob = g.disc_with_ellipses(1 << 13, 6, seed=1)
+    rng = np.random.default_rng(2)
+    out.append(("update_disc6_8k", prob, g.laplace_source_rhs(prob, g.random_sources(1, rng)),
+                dict(tol=1e-8, solution_dim=1, pde=0),
+                [(2, (0.01, 0.0)), (4, (0.0, -0.01))]))
+    prob = g.disc_with_circles(1 << 12, 6, seed=4)
+    out.append(("update_stokes_circles_4k", prob, stokes_rhs(prob),
+                dict(tol=1e-8, solution_dim=2, pde=3),
+                [(1, (0.003, 0.0)), (3, (0.0, 0.003))]))
+    return out
+
+
+def update_frames(g, prob, moves):
+    frames = [prob]
+    for h, d in moves:
+        frames.append(g.move_hole(frames[-1], h, d))
+    return frames
+
+
+def main_update(only=None):
+    """The reference's incremental re-factorization over the frames
+    (oracle.ref_update_solve: QuadTree::perturb + skeletonize) and a fresh
+    reference factorization of every frame."""
+    import oracle
+    g = load_geometry()
+    for name, prob, rhs, p, moves in update_cases():
+        if only and name not in only:
+            continue
+        frames = update_frames(g, prob, moves)
+        mu_inc, al_inc, sec_inc, comp_inc = oracle.ref_update_solve(
+            frames, [rhs[:, 0]] * len(frames), p["tol"], threads=8,
+            solution_dim=p["solution_dim"], pde=p["pde"])
+        mu_fr, al_fr, sec_fr = [], [], []
+        for fr in frames:
+            mu, al, st = oracle.solve(fr, rhs[:, :1], p["tol"], threads=8,
+                                      solution_dim=p["solution_dim"], pde=p["pde"], impl="ref")
+            mu_fr.append(mu[:, 0])
+            al_fr.append(al[:, 0])
+            sec_fr.append(st["factor_s"])
+        np.savez_compressed(os.path.join(HERE, name + ".npz"),
+                            points=prob.points, normals=prob.normals, weights=prob.weights,
+                            curvatures=prob.curvatures, hole_centers=prob.hole_centers,
+                            hole_start=prob.hole_start, hole_count=prob.hole_count,
+                            rhs=rhs[:, :1], input_sha1=input_hash(prob, rhs[:, :1]),
+                            move_hole=np.array([h for h, _ in moves], np.int32),
+                            move_delta=np.array([d for _, d in moves], np.float64),
+                            mu_update=mu_inc, alpha_update=al_inc, mu_fresh=np.stack(mu_fr),
+                            alpha_fresh=np.stack(al_fr), seconds_update=sec_inc,
+                            seconds_fresh=np.array(sec_fr), compressed_update=comp_inc)
+        print(name, prob.n, "update s", sec_inc, "fresh s", sec_fr)
+
+
 def main(only=None):
     import oracle
     for name, prob, rhs, p in cases():
@@ -118,4 +184,10 @@ def main(only=None):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or None)
+    names = sys.argv[1:]
+    solve_names = [n for n in names if not n.startswith("update_")]
+    update_names = [n for n in names if n.startswith("update_")]
+    if not names or solve_names:
+        main(solve_names or None)
+    if not names or update_names:
+        main_update(update_names or None)

@@ -50,3 +50,54 @@ def test_mirror_boundary_integral_solve_interior_field(pkg):
     ue = g.laplace_source_field(tg, src)
     assert np.abs(u - ue).max() <= 1e-9 * np.abs(ue).max()
     qt.factor.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim", [2, 3])
+def test_mirror_perturbation_frames_match_fresh_trees(pkg, dim):
+    """The reference's updating test (SphereUpdateLosesNoAcc,
+    kern_interp/kern_interp_test.cpp:424-465) through the mirror, Stokes at
+    id_tol 1e-3: one tree initialized once and perturbed frame after frame
+    (a hole moved per frame, as in kern_interp/experiments/
+    experiment_two.cpp:54-60), each frame's boundary_integral_solve against
+    a fresh tree's, relative difference <= 50 id_tol."""
+    g = pkg.geometry
+    rng = np.random.default_rng(11)
+    id_tol = 1e-3
+    if dim == 3:
+        prob = g.spheres_with_holes(4096, [((0.35, 0.0, 0.0), 0.15, 1024),
+                                           ((-0.4, 0.1, 0.0), 0.12, 1024)])
+        tg = np.array([[0.0, 0.5, 0.3], [0.0, -0.5, -0.2], [0.1, 0.0, 0.6], [0.6, 0.3, 0.2]])
+        src = [np.array([2.5, 0.3, 0.0]), np.array([-0.5, 2.8, 0.4])]
+        frc = [np.array([1.0, 0.5, -0.2]), np.array([0.0, 1.0, 0.3])]
+        rhs_of = lambda p: g.stokes3_rhs(p, src, frc)[:, :1]
+        step = 0.03
+    else:
+        prob = g.disc_with_circles(1 << 13, 10, seed=2)
+        tg = rng.uniform(-0.6, 0.6, (40, 2))
+        tg = tg[np.min(np.linalg.norm(tg[:, None] - prob.hole_centers[None], axis=2), 1) > 0.08][:8]
+        src = [np.array([2.5, 0.0]), np.array([-1.0, 2.7])]
+        frc = [np.array([1.0, 0.5]), np.array([0.3, -1.0])]
+        rhs_of = lambda p: g.stokes_rhs(p, src, frc)[:, :1]
+        step = 0.003
+    qt = pkg.QuadTree()
+    qt.initialize_tree(pkg.Boundary.from_problem(prob), dim, dim)
+    cur = prob
+    kept = []
+    for frame in range(4):
+        h = int(rng.integers(0, cur.n_holes))
+        delta = np.zeros(dim)
+        delta[frame % dim] = step if frame % 2 == 0 else -step
+        cur = g.move_hole(cur, h, delta)
+        b = pkg.Boundary.from_problem(cur, boundary_values=rhs_of(cur))
+        kernel = pkg.Kernel(dim, dim, pkg.Kernel.STOKES, b, tg)
+        qt.perturb(b)
+        u = pkg.boundary_integral_solve(kernel, b, qt, id_tol, 4, tg)
+        kept.append(qt.factor.info()["n_reused"])
+        fresh = pkg.QuadTree()
+        u2 = pkg.boundary_integral_solve(kernel, b, fresh, id_tol, 4, tg)
+        fresh.factor.close()
+        assert np.linalg.norm(u2 - u) / np.linalg.norm(u2) <= 50 * id_tol, frame
+    qt.factor.close()
+    # the first frame factorizes a tree never factorized; the others reuse boxes
+    assert kept[0] == 0 and min(kept[1:]) > 0, kept

@@ -44,6 +44,37 @@ def test_port_matches_reference_fixture(golden_cases, oracle_mod, name):
         assert np.abs(alpha - data["alpha"]).max() <= 1e-9 * max(1.0, np.abs(data["alpha"]).max())
 
 
+def test_update_fixture_inputs_intact(golden_updates):
+    import make_golden
+    for name, (frames, rhs, p, data) in golden_updates.items():
+        assert str(data["input_sha1"]) == make_golden.input_hash(frames[0], rhs), name
+        # each frame moves exactly one hole's nodes
+        for f in range(1, len(frames)):
+            moved = np.any(frames[f].points != frames[f - 1].points, axis=1)
+            h = int(data["move_hole"][f - 1])
+            s, c = int(data["hole_start"][h]), int(data["hole_count"][h])
+            assert moved[s:s + c].all() and moved.sum() == c
+
+
+@pytest.mark.parametrize("name", ["update_disc6_8k", "update_stokes_circles_4k"])
+def test_port_matches_reference_update_fixture(golden_updates, oracle_mod, name):
+    """The oracle's fresh factorization of every perturbed frame against the
+    reference's fresh one (to rounding), and the reference's own incremental
+    re-factorization (QuadTree::perturb + skeletonize) within its updating
+    test's bound of the fresh one (50 id_tol,
+    kern_interp/kern_interp_test.cpp:459-463)."""
+    frames, rhs, p, data = golden_updates[name]
+    for f, prob in enumerate(frames):
+        mu, alpha, _ = oracle_mod.solve(prob, rhs, p["tol"], threads=4,
+                                        solution_dim=p["solution_dim"], pde=p["pde"])
+        ref = data["mu_fresh"][f]
+        assert np.abs(mu[:, 0] - ref).max() <= 1e-9 * np.abs(ref).max(), f
+        assert np.abs(alpha[:, 0] - data["alpha_fresh"][f]).max() <= 1e-9 * np.abs(ref).max(), f
+        inc = np.concatenate([data["mu_update"][f], data["alpha_update"][f]])
+        fresh = np.concatenate([ref, data["alpha_fresh"][f]])
+        assert np.linalg.norm(inc - fresh) / np.linalg.norm(fresh) <= 50 * p["tol"], f
+
+
 def test_port_pde_error_star(golden_cases, oracle_mod, pkg):
     """Interior field of an exterior source recovered to ~1e-12 (the reference's
     analytic-agreement tests, kern_interp/kern_interp_test.cpp:171-190)."""
