@@ -8,11 +8,17 @@
 // doubles points (dim n), normals (dim n), weights (n), curvatures (n),
 // f (sd n), targets (dim n_targets), hole centres (dim n_holes); int32 hole
 // node counts (n_holes).
+// Optionally followed by int32 n_frames and, per frame, doubles points
+// (dim n) and hole centres (dim n_holes): perturbation frames, each applied
+// with QuadTree::perturb and skeletonize on the first tree, as the
+// reference's updating experiments do.
 // Output (binary): doubles mu (sd n), alpha (border columns), u at the
-// targets (sd n_targets).  Exit status 3 when the library reports an error.
+// targets (sd n_targets), then per frame mu and alpha.  Exit status 3 when
+// the library reports an error.
 #include <cstdio>
 #include <fstream>
 #include <iostream>
+#include <memory>
 #include <vector>
 
 #include "kern_interp_gb300.hpp"
@@ -87,6 +93,27 @@ int main(int argc, char** argv) {
     out.write(reinterpret_cast<const char*>(mu.mat), sizeof(double) * mu.height());
     if (nh) out.write(reinterpret_cast<const char*>(alpha.mat), sizeof(double) * alpha.height());
     out.write(reinterpret_cast<const char*>(u.mat), sizeof(double) * u.height());
+
+    // perturbation frames on the first tree (the boundaries outlive its use)
+    int n_frames = 0;
+    in.read(reinterpret_cast<char*>(&n_frames), sizeof(int));
+    if (!in) n_frames = 0;
+    std::vector<std::unique_ptr<ArrayBoundary>> frames;
+    for (int fr = 0; fr < n_frames; fr++) {
+      frames.emplace_back(new ArrayBoundary(b));
+      ArrayBoundary& bf = *frames.back();
+      bf.points = take<double>(in, (size_t)dim * n);
+      const std::vector<double> c = take<double>(in, (size_t)dim * nh);
+      for (int q = 0; q < nh; q++)
+        bf.holes[q].center = PointVec(std::vector<double>(c.begin() + q * dim, c.begin() + (q + 1) * dim));
+      quadtree.perturb(bf);
+      Kernel kf(sd, dim, sd == 1 ? Kernel::LAPLACE : Kernel::STOKES, &bf, targets);
+      skel.skeletonize(kf, &quadtree);
+      ki_Mat muf, alf;
+      linear_solve(skel, quadtree, bf.boundary_values, &muf, nh ? &alf : nullptr);
+      out.write(reinterpret_cast<const char*>(muf.mat), sizeof(double) * muf.height());
+      if (nh) out.write(reinterpret_cast<const char*>(alf.mat), sizeof(double) * alf.height());
+    }
     return 0;
   } catch (const std::exception& e) {
     std::cerr << "facade_driver: " << e.what() << "\n";

@@ -24,7 +24,8 @@ def _compile(tmp):
     return exe
 
 
-def _write_input(path, prob, f, targets, tol, leaf=0, proxy=0, ratio=0.0, min_compress=0, sd=1):
+def _write_input(path, prob, f, targets, tol, leaf=0, proxy=0, ratio=0.0, min_compress=0, sd=1,
+                 frames=()):
     dim = prob.points.shape[1]
     nh = prob.n_holes
     n_outer = int(prob.hole_start[0]) if nh else prob.n
@@ -37,6 +38,11 @@ def _write_input(path, prob, f, targets, tol, leaf=0, proxy=0, ratio=0.0, min_co
                   np.asarray(prob.hole_centers, np.float64).reshape(-1)[:dim * nh]):
             np.ascontiguousarray(a, np.float64).reshape(-1).tofile(fh)
         np.asarray(prob.hole_count[:nh], np.int32).tofile(fh)
+        if frames:
+            np.array([len(frames)], np.int32).tofile(fh)
+            for fr in frames:
+                np.ascontiguousarray(fr.points, np.float64).reshape(-1).tofile(fh)
+                np.ascontiguousarray(fr.hole_centers, np.float64).reshape(-1)[:dim * nh].tofile(fh)
 
 
 def _have_gpu():
@@ -105,3 +111,28 @@ def test_facade_driver_matches_reference_fixture(pkg, golden_cases, name):
     if name == "star_c1":
         ue = g.laplace_source_field(targets, np.array([[3.0, 3.0]]))[:, 0]
         assert np.abs(u - ue).max() <= 1e-8 * np.abs(ue).max()
+
+
+@pytest.mark.gpu
+def test_facade_perturbation_frames_match_reference_fixture(pkg, golden_updates):
+    """QuadTree::perturb + skeletonize through the C++ surface, frame after
+    frame on one tree, against the compiled reference's fresh factorization
+    of each frame (10 id_tol, as for the other fixtures)."""
+    frames, rhs, p, data = golden_updates["update_disc6_8k"]
+    prob = frames[0]
+    with tempfile.TemporaryDirectory() as tmp:
+        exe = _compile(tmp)
+        inp, out = os.path.join(tmp, "in.bin"), os.path.join(tmp, "out.bin")
+        _write_input(inp, prob, rhs[:, 0], np.zeros((0, 2)), p["tol"], frames=frames[1:])
+        r = subprocess.run([exe, inp, out], capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        res = np.fromfile(out, np.float64)
+    N, nb = prob.n, prob.n_holes
+    per = N + nb
+    assert res.size == per + per * (len(frames) - 1)
+    for f in range(len(frames)):
+        mu = res[per * f:per * f + N]
+        alpha = res[per * f + N:per * (f + 1)]
+        ref = data["mu_fresh"][f]
+        assert np.abs(mu - ref).max() <= 10 * p["tol"] * np.abs(ref).max(), f
+        assert np.abs(alpha - data["alpha_fresh"][f]).max() <= 10 * p["tol"] * np.abs(ref).max(), f
