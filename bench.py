@@ -73,6 +73,8 @@ def parse():
     ap.add_argument("--ref-residual-rows", type=int, default=256,
                     help="rows of the dense FP64 operator sampled to report the residual the "
                          "CPU reference path reaches")
+    ap.add_argument("--no-update", action="store_true",
+                    help="skip the incremental re-factorization measurement (workloads with holes)")
     ap.add_argument("--no-parity", action="store_true",
                     help="skip the solution comparison against the CPU reference path")
     return ap.parse_args()
@@ -398,6 +400,65 @@ def parity_check(pkg, args, wl, w2, kw, refine, mu, alpha, pmu, palpha, threads)
     return res
 
 
+def measure_update(pkg, wl, kw, refine, args, frames=3):
+    """Incremental re-factorization (ki_factor_update, the reference's
+    QuadTree::perturb + skeletonize): frame after frame one hole is moved by
+    a small step, the previous frame's factorization is updated, and a fresh
+    factorization of the same frame is made; device-synchronized wall times
+    of both, the boxes kept, and the two solutions of the frame's first
+    right-hand side compared (refined to the target when the form refines)."""
+    import torch
+    g = pkg.geometry
+    rng = np.random.default_rng(5)
+    step = 0.004 if wl.sol_dim == 1 else 0.002
+
+    def arrays(p):
+        return (p.points, p.normals, p.weights, p.curvatures)
+
+    def holes(p):
+        return dict(hole_centers=p.hole_centers, hole_start=p.hole_start, hole_count=p.hole_count)
+
+    def solve(fac, b):
+        if refine:
+            out = fac.solve_refined(b, tol=args.target, max_steps=args.max_steps)
+            return np.concatenate([o.reshape(-1) for o in out[:-1]])
+        out = fac.solve(b)
+        return np.concatenate([o.reshape(-1) for o in (out if isinstance(out, tuple) else (out,))])
+
+    base = {k: v for k, v in kw.items() if k not in ("hole_centers", "hole_start", "hole_count")}
+    cur = wl.prob
+    fac = pkg.Factor(*arrays(cur), **base, **holes(cur))
+    n_comp = fac.info()["n_compressed"]
+    upd, fresh, kept, diff = [], [], [], []
+    for f in range(frames):
+        h = int(rng.integers(0, cur.n_holes))
+        d = np.zeros(wl.dim)
+        d[f % wl.dim] = step if f % 2 == 0 else -step
+        cur = g.move_hole(cur, h, d)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        kept.append(fac.update(*arrays(cur), **holes(cur)))
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        fr = pkg.Factor(*arrays(cur), **base, **holes(cur))
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        upd.append((t1 - t0) * 1e3)
+        fresh.append((t2 - t1) * 1e3)
+        b = wl.rhs[:, :1]
+        xu, xf = solve(fac, b), solve(fr, b)
+        diff.append(float(np.linalg.norm(xu - xf) / np.linalg.norm(xf)))
+        fr.close()
+    fac.close()
+    return {"what": "one hole moved by %g per frame (geometry.move_hole), the previous frame's "
+                    "factorization updated (ki_factor_update) vs a fresh factorization "
+                    "(ki_factor_create) of the same frame; wall ms, device synchronized" % step,
+            "frames": frames, "update_ms": upd, "fresh_ms": fresh,
+            "speedup_median": float(np.median(np.array(fresh) / np.array(upd))),
+            "boxes_kept": kept, "boxes_compressed": n_comp,
+            "solution_rel_diff": diff}
+
+
 def main():
     args = parse()
     import __graft_entry__ as g
@@ -582,6 +643,9 @@ def main():
     ue = wl.field(pkg, tg)
     pde_err = float(np.abs(u - ue).max() / np.abs(ue).max())
     fac.close()
+    update = None
+    if wl.prob.n_holes and not args.no_update:
+        update = measure_update(pkg, wl, kw, refine, args)
 
     if rank != 0:
         rep.finish()
@@ -742,6 +806,7 @@ def main():
         # compact summaries last: they stay in the tail of the line
         "learned_rank": learned,
         "fp64_form_same_residual": compare,
+        "incremental_update": update,
         "accuracy": {"residual_est_max": rmax, "residual_est_median": rmed,
                      "residual_rows_sampled": args.residual_rows, "pde_rel_err": pde_err,
                      "refined_residual": rinfo["residual"] if rinfo else None},

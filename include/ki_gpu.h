@@ -318,6 +318,8 @@ int ki_tensor_core_check(double* max_rel_err);
  *   `epochs` steps of rate `lr`, and written to `model`; `loss` receives the
  *   final mean squared error.  Deterministic for given inputs.
  * ki_rank_model_predict: ratios (n) for n feature rows.
+ * ki_rank_model_predict_bf16: the same as the FP32 factorizations infer them:
+ *   BF16 operands on the tensor cores (tcgen05 MMAs, FP32 accumulation).
  * ki_rank_model_grad: the loss and its gradient with respect to the blob
  *   (the standardization entries get zero) -- for checking the kernels.
  * ki_factor_get_box_log: per ID box of the factorization, 15 floats: the 12
@@ -328,6 +330,7 @@ int ki_rank_model_floats(void);
 int ki_rank_model_train(const float* features, const float* ratios, int n, int epochs, float lr,
                         unsigned seed, float* model, float* loss);
 int ki_rank_model_predict(const float* model, const float* features, int n, float* ratios);
+int ki_rank_model_predict_bf16(const float* model, const float* features, int n, float* ratios);
 int ki_rank_model_grad(const float* model, const float* features, const float* ratios, int n,
                        float* grad, float* loss);
 int ki_factor_get_box_log(const ki_factor* f, float* out, int max_rows, int* rows);
@@ -346,6 +349,28 @@ int ki_trim_memory(void);
  * through one counted helper).  No reference counterpart.
  */
 long long ki_launch_count(void);
+
+/*
+ * Autotuner (no reference counterpart; the reference has nothing to tune):
+ * per box-size bucket, the launch shape of the factorization's ID bins (fold
+ * rows x threads), Schur bins (threads, Gauss-Jordan split) and solve sweeps
+ * (threads) that runs fastest on the current GPU.
+ *
+ * ki_autotune: factorizes desc `repeats` times per candidate and knob (knob
+ *   after knob, each later knob under the choices already made), with every
+ *   launch group on one stream and timed by CUDA events, and, for the sweeps,
+ *   solves nrhs right-hand sides; keeps per bucket the fastest candidate in
+ *   the library's table (buckets it did not see keep theirs) and writes
+ *   {"table": {...}, "ms": {"id:17": [ms per candidate], ...}} to out.
+ * ki_tune_set: replaces the table with a flat JSON object {"id:17": 2, ...}
+ *   (the "table" part of ki_autotune's output); {} restores the built-in
+ *   heuristics.  KI_ERR_ARG on malformed input.
+ * ki_tune_get: the current table as such a JSON object.
+ * The table is process-wide; set it before factorizing.
+ */
+int ki_autotune(const ki_problem_desc* desc, int nrhs, int repeats, char* out, int len);
+int ki_tune_set(const char* json);
+int ki_tune_get(char* buf, int len);
 
 /* Message of the last failure on the calling thread ("" if none). */
 const char* ki_last_error(void);

@@ -16,6 +16,7 @@ ki_Mat layout).  There is no CPU fallback: every call runs on the GPU, and
 loading fails loudly when the library is missing.
 """
 import ctypes
+import json
 import os
 
 import numpy as np
@@ -34,8 +35,11 @@ EXPORTED = ["ki_factor_create", "ki_factor_destroy", "ki_factor_get_info", "ki_s
             "ki_solve_device_noalloc", "ki_apply_fmm", "ki_apply_fmm_ex", "ki_trim_memory",
             "ki_launch_count", "ki_rank_model_floats",
             "ki_rank_model_train", "ki_rank_model_predict", "ki_rank_model_grad",
-            "ki_factor_get_box_log", "ki_factor_update"]
+            "ki_factor_get_box_log", "ki_factor_update", "ki_autotune", "ki_tune_set",
+            "ki_tune_get", "ki_rank_model_predict_bf16"]
 RANK_MODEL_PATH = os.path.join(HERE, "rank_model.npy")
+# the autotuner's table (ki_autotune's output), loaded with the library
+TUNE_PATH = os.path.join(HERE, "tune_gb300.json")
 BOX_LOG_COLUMNS = 15   # 12 features, n, k, level
 
 
@@ -90,6 +94,9 @@ def load_library(path=None):
     lib.ki_factor_create.argtypes = [ctypes.POINTER(_Desc), ctypes.POINTER(V)]
     lib.ki_factor_destroy.argtypes = [V]
     lib.ki_factor_update.argtypes = [V, ctypes.POINTER(_Desc)]
+    lib.ki_autotune.argtypes = [ctypes.POINTER(_Desc), I, I, ctypes.c_char_p, I]
+    lib.ki_tune_set.argtypes = [ctypes.c_char_p]
+    lib.ki_tune_get.argtypes = [ctypes.c_char_p, I]
     lib.ki_factor_get_info.argtypes = [V, ctypes.POINTER(_Info)]
     lib.ki_solve.argtypes = [V, V, I, I, V, I, V, I]
     lib.ki_solve_device.argtypes = [V, V, I, I, V, I, V, I, V]
@@ -109,6 +116,7 @@ def load_library(path=None):
     F = ctypes.POINTER(ctypes.c_float)
     lib.ki_rank_model_train.argtypes = [V, V, I, I, ctypes.c_float, ctypes.c_uint, V, F]
     lib.ki_rank_model_predict.argtypes = [V, V, I, V]
+    lib.ki_rank_model_predict_bf16.argtypes = [V, V, I, V]
     lib.ki_rank_model_grad.argtypes = [V, V, V, I, V, F]
     lib.ki_factor_get_box_log.argtypes = [V, V, I, ctypes.POINTER(I)]
     lib.ki_measure_fma_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
@@ -119,6 +127,11 @@ def load_library(path=None):
         getattr(lib, name)
     if path is None:
         _lib = lib
+        # the autotuner's table for this GPU model, when one was recorded
+        if os.path.exists(TUNE_PATH) and not os.environ.get("KI_NO_TUNE_TABLE"):
+            with open(TUNE_PATH) as fh:
+                table = json.load(fh)["table"]
+            _check_lib(lib, lib.ki_tune_set(json.dumps(table).encode()))
     return lib
 
 
@@ -127,8 +140,68 @@ def _check(rc):
         raise KiError(rc, load_library().ki_last_error().decode())
 
 
+def _check_lib(lib, rc):
+    if rc != KI_OK:
+        raise KiError(rc, lib.ki_last_error().decode())
+
+
 def _ptr(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _make_desc(params, points, normals, weights, curvatures, hole_centers, hole_start,
+               hole_count):
+    """(ki_problem_desc, arrays it points to) for a boundary; params =
+    (dim, solution_dimension, pde, max_leaf_dofs, num_proxy_points,
+    radius_ratio, min_dofs_to_compress, id_tol, precision, rank model)."""
+    dim, sd, pde, mld, npx, rr, mdc, tol, prec, rm = params
+    keep = [np.ascontiguousarray(points, np.float64).reshape(-1),
+            np.ascontiguousarray(normals, np.float64).reshape(-1),
+            np.ascontiguousarray(weights, np.float64).reshape(-1)]
+    keep.append(None if curvatures is None else
+                np.ascontiguousarray(curvatures, np.float64).reshape(-1))
+    nh = 0 if hole_centers is None else int(np.asarray(hole_centers).shape[0])
+    hc = np.ascontiguousarray(hole_centers, np.float64).reshape(-1) if nh else None
+    hs = np.ascontiguousarray(hole_start, np.int32) if nh else None
+    hn = np.ascontiguousarray(hole_count, np.int32) if nh else None
+    keep += [hc, hs, hn, rm]
+    n = keep[2].shape[0]
+    return (_Desc(n, dim, sd, pde, _ptr(keep[0]), _ptr(keep[1]), _ptr(keep[2]), _ptr(keep[3]),
+                  nh, _ptr(hc), _ptr(hs), _ptr(hn), mld, npx, rr, mdc, tol, prec, _ptr(rm)),
+            keep)
+
+
+def tune_set(table):
+    """Replace the library's autotuning table ({"id:17": 2, ...}; {} restores
+    the built-in heuristics)."""
+    _check(load_library().ki_tune_set(json.dumps(table).encode()))
+
+
+def tune_get():
+    buf = ctypes.create_string_buffer(1 << 16)
+    _check(load_library().ki_tune_get(buf, len(buf)))
+    return json.loads(buf.value.decode())
+
+
+def autotune(points, normals, weights, curvatures=None, nrhs=16, repeats=2, id_tol=1e-10,
+             solution_dimension=1, pde=PDE_LAPLACE, hole_centers=None, hole_start=None,
+             hole_count=None, max_leaf_dofs=64, num_proxy_points=0, radius_ratio=2.0,
+             min_dofs_to_compress=64, precision=PRECISION_FP64, rank_model=None):
+    """ki_autotune on this boundary (the Factor constructor's arguments):
+    returns {"table": ..., "ms": ...}; the library keeps the table."""
+    lib = load_library()
+    dim = int(np.asarray(points).shape[-1])
+    if isinstance(rank_model, str) and rank_model == "default":
+        rank_model = load_rank_model()
+    rm = None if rank_model is None else np.ascontiguousarray(rank_model, np.float32)
+    params = (dim, solution_dimension, pde, max_leaf_dofs, num_proxy_points, radius_ratio,
+              min_dofs_to_compress, id_tol, precision, rm)
+    d, keep = _make_desc(params, points, normals, weights, curvatures, hole_centers, hole_start,
+                         hole_count)
+    buf = ctypes.create_string_buffer(1 << 18)
+    _check(lib.ki_autotune(ctypes.byref(d), nrhs, repeats, buf, len(buf)))
+    del keep
+    return json.loads(buf.value.decode())
 
 
 class Factor:
@@ -162,23 +235,10 @@ class Factor:
     def _desc(self, points, normals, weights, curvatures, hole_centers, hole_start, hole_count):
         """The ki_problem_desc of a boundary with this factor's parameters (the
         arrays it points to are kept in self._keep)."""
-        dim, sd, pde, mld, npx, rr, mdc, tol, prec, rm = self._params
-        keep = [np.ascontiguousarray(points, np.float64).reshape(-1),
-                np.ascontiguousarray(normals, np.float64).reshape(-1),
-                np.ascontiguousarray(weights, np.float64).reshape(-1)]
-        keep.append(None if curvatures is None else
-                    np.ascontiguousarray(curvatures, np.float64).reshape(-1))
-        nh = 0 if hole_centers is None else int(np.asarray(hole_centers).shape[0])
-        hc = np.ascontiguousarray(hole_centers, np.float64).reshape(-1) if nh else None
-        hs = np.ascontiguousarray(hole_start, np.int32) if nh else None
-        hn = np.ascontiguousarray(hole_count, np.int32) if nh else None
-        keep += [hc, hs, hn, rm]
-        self._keep = keep
-        self._n_holes = nh
-        n = keep[2].shape[0]
-        return _Desc(n, dim, sd, pde, _ptr(keep[0]), _ptr(keep[1]), _ptr(keep[2]),
-                     _ptr(keep[3]), nh, _ptr(hc), _ptr(hs), _ptr(hn), mld, npx, rr, mdc, tol,
-                     prec, _ptr(rm))
+        d, self._keep = _make_desc(self._params, points, normals, weights, curvatures,
+                                   hole_centers, hole_start, hole_count)
+        self._n_holes = d.n_holes
+        return d
 
     def _set_sizes(self):
         dim, sd = self._params[0], self._params[1]
@@ -367,11 +427,14 @@ def rank_model_train(features, ratios, epochs=2000, lr=3e-3, seed=0):
     return m, float(loss.value)
 
 
-def rank_model_predict(model, features):
+def rank_model_predict(model, features, bf16=False):
+    """Predicted rank fractions: FP32 on the CUDA cores, or (bf16) BF16 on the
+    tensor cores as the FP32 factorizations infer them."""
     X = np.ascontiguousarray(features, np.float32)
     out = np.zeros(X.shape[0], np.float32)
-    _check(load_library().ki_rank_model_predict(_ptr(np.ascontiguousarray(model, np.float32)),
-                                                _ptr(X), X.shape[0], _ptr(out)))
+    lib = load_library()
+    fn = lib.ki_rank_model_predict_bf16 if bf16 else lib.ki_rank_model_predict
+    _check(fn(_ptr(np.ascontiguousarray(model, np.float32)), _ptr(X), X.shape[0], _ptr(out)))
     return out
 
 

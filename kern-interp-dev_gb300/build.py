@@ -19,7 +19,7 @@ OBJ = os.path.join(ROOT, "_build", "obj")
 
 CU_SOURCES = ["ki_factor.cu", "ki_dense.cu", "ki_abi.cu", "ki_fmm.cu", "ki_pool.cu", "ki_mlp.cu",
               "ki_tree_gpu.cu"]
-CPP_SOURCES = ["ki_tree.cpp"]
+CPP_SOURCES = ["ki_tree.cpp", "ki_tune.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

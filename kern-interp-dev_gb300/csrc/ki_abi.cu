@@ -11,6 +11,7 @@
 #include <functional>
 #include <future>
 #include <memory>
+#include <map>
 #include <mutex>
 #include <new>
 #include <stdexcept>
@@ -24,6 +25,7 @@
 #include "ki_factor.h"
 #include "ki_fmm.h"
 #include "ki_mlp.h"
+#include "ki_tune.h"
 
 namespace {
 
@@ -1187,6 +1189,30 @@ void apply_bordered(ki_factor* f, const double* mu, const double* alpha, int nco
 }
 }  // namespace
 
+namespace {
+
+// Timing of one factorization (and, for the sweep knob, one solve of nrhs
+// columns) with the tuner's recording on: device ms per (knob, bucket).
+template <typename T>
+void tune_times(ki_factor* f, ki::Factorization<T>& F, int knob, const double* d_b, double* d_x,
+                double* d_al, int nrhs, std::map<int, double>* out) {
+  // the factorization's records (its border sweeps included), and for the
+  // sweep knob a solve's
+  std::vector<ki::StageSum> recs = F.factor_prof;
+  if (knob == ki::kTuneSweep) {
+    solve_impl<T>(f, F, d_b, f->n_dofs, nrhs, d_x, f->n_dofs, d_al, std::max(1, f->n_border), f->stream);
+    KI_CHECK_CUDA(cudaStreamSynchronize(f->stream));
+    const std::vector<ki::StageSum> sv = F.collect();
+    recs.insert(recs.end(), sv.begin(), sv.end());
+  }
+  for (const auto& r : recs) {
+    int k = -1, b = -1;
+    if (ki::tune_parse_stage(r.stage, &k, &b) && k == knob) (*out)[b] += r.ms;
+  }
+}
+
+}  // namespace
+
 extern "C" {
 
 namespace {
@@ -1195,7 +1221,8 @@ namespace {
 // the same problem before a boundary perturbation, same precision, sizes,
 // parameters and rank model), the boxes of prev's factorization that the
 // perturbation left unchanged are copied rather than recomputed.
-void build_factor(ki_factor* f, const ki_problem_desc* desc, const ki_factor* prev) {
+void build_factor(ki_factor* f, const ki_problem_desc* desc, const ki_factor* prev,
+                  bool plan_fmm = true) {
   const auto t_create = std::chrono::steady_clock::now();
   int dev_count = 0;
   if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
@@ -1297,7 +1324,7 @@ void build_factor(ki_factor* f, const ki_problem_desc* desc, const ki_factor* pr
     }
   };
   bool planning = false;
-  if (fmm_capable(f) && f->n_dofs >= 4096 && !std::getenv("KI_NO_FMM_PREPLAN")) {
+  if (plan_fmm && fmm_capable(f) && f->n_dofs >= 4096 && !std::getenv("KI_NO_FMM_PREPLAN")) {
     planning = true;
     const double *pp = desc->points, *nn = desc->normals, *ww = desc->weights,
                  *kk = desc->curvatures;
@@ -1367,6 +1394,93 @@ int ki_factor_create(const ki_problem_desc* desc, ki_factor** out) {
     std::unique_ptr<ki_factor> f(new ki_factor());
     build_factor(f.get(), desc, nullptr);
     *out = f.release();
+  });
+}
+
+int ki_tune_set(const char* json) {
+  return guarded([&] {
+    if (!json) throw ArgError("json is NULL");
+    try {
+      ki::tune_from_json(json);
+    } catch (const std::invalid_argument& e) {
+      throw ArgError(e.what());
+    }
+  });
+}
+
+int ki_tune_get(char* buf, int len) {
+  return guarded([&] {
+    const std::string js = ki::tune_to_json();
+    if (!buf || len < (int)js.size() + 1) throw ArgError("buffer too small: need " + std::to_string(js.size() + 1));
+    std::memcpy(buf, js.c_str(), js.size() + 1);
+  });
+}
+
+int ki_autotune(const ki_problem_desc* desc, int nrhs, int repeats, char* out, int len) {
+  return guarded([&] {
+    check_desc(desc);
+    if (nrhs <= 0 || repeats <= 0) throw ArgError("nrhs and repeats must be positive");
+    if (!out || len <= 0) throw ArgError("output buffer is NULL");
+    struct Restore {
+      ~Restore() {
+        ki::tune_set_recording(false);
+        for (int k = 0; k < ki::kTuneKnobs; k++) ki::tune_force(k, -1);
+      }
+    } restore;
+    ki::tune_set_recording(true);
+    const bool fp64 = desc->precision == KI_PRECISION_FP64;
+    const size_t N = (size_t)desc->n_points * desc->solution_dimension;
+    const int nb_max = std::max(1, desc->n_holes * 6);
+    // right-hand sides: a fixed pseudo-random set (the sweeps' cost does not
+    // depend on the values)
+    std::vector<double> hb(N * nrhs);
+    uint64_t st = 0x9e3779b97f4a7c15ull;
+    for (auto& v : hb) {
+      st = st * 6364136223846793005ull + 1442695040888963407ull;
+      v = (double)(st >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+    }
+    DevBuf<double> d_b(N * nrhs, nullptr), d_x(N * nrhs, nullptr), d_al((size_t)nb_max * nrhs, nullptr);
+    KI_CHECK_CUDA(cudaMemcpy(d_b.p, hb.data(), sizeof(double) * hb.size(), cudaMemcpyHostToDevice));
+    std::string report = "{";
+    for (int knob = 0; knob < ki::kTuneKnobs; knob++) {
+      int ncand = ki::kTuneCandidates[knob];
+      if (fp64 && knob != ki::kTuneSweep) ncand = 2;   // FP64: fold rows / 128-256 threads only
+      std::map<int, std::vector<double>> ms;            // bucket -> best ms per candidate
+      for (int c = 0; c < ncand; c++) {
+        ki::tune_force(knob, c);
+        for (int rep = 0; rep < repeats; rep++) {
+          std::unique_ptr<ki_factor> f(new ki_factor());
+          build_factor(f.get(), desc, nullptr, false);
+          std::map<int, double> t;
+          if (f->f64) tune_times<double>(f.get(), *f->f64, knob, d_b.p, d_x.p, d_al.p, nrhs, &t);
+          else tune_times<float>(f.get(), *f->f32, knob, d_b.p, d_x.p, d_al.p, nrhs, &t);
+          for (const auto& kv : t) {
+            auto& v = ms[kv.first];
+            if (v.empty()) v.assign(ncand, -1.0);
+            if (v[c] < 0 || kv.second < v[c]) v[c] = kv.second;
+          }
+        }
+      }
+      ki::tune_force(knob, -1);
+      for (const auto& kv : ms) {
+        int best = -1;
+        for (int c = 0; c < ncand; c++)
+          if (kv.second[c] >= 0 && (best < 0 || kv.second[c] < kv.second[best])) best = c;
+        if (best >= 0) ki::tune_set(knob, kv.first, best);
+        report += (report.size() > 1 ? ", " : "") + std::string("\"") +
+                  ki::tune_stage(knob, kv.first).substr(5) + "\": [";
+        for (int c = 0; c < ncand; c++) {
+          char num[32];
+          std::snprintf(num, sizeof(num), "%s%.6f", c ? ", " : "", kv.second[c]);
+          report += num;
+        }
+        report += "]";
+      }
+    }
+    report += "}";
+    const std::string js = "{\"table\": " + ki::tune_to_json() + ", \"ms\": " + report + "}";
+    if (len < (int)js.size() + 1) throw ArgError("buffer too small: need " + std::to_string(js.size() + 1));
+    std::memcpy(out, js.c_str(), js.size() + 1);
   });
 }
 
@@ -1774,6 +1888,26 @@ int ki_rank_model_predict(const float* model, const float* features, int n, floa
     ki::mlp_predict(dm.p, dx.p, n, dy.p, s);
     KI_CHECK_CUDA(cudaMemcpyAsync(ratios, dy.p, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
     KI_CHECK_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int ki_rank_model_predict_bf16(const float* model, const float* features, int n, float* ratios) {
+  return guarded([&] {
+    if (!model || !features || !ratios) throw ArgError("NULL argument");
+    if (n < 0) throw ArgError("bad n");
+    if (n == 0) return;
+    cudaStream_t s = nullptr;
+    DevBuf<float> dm(ki::kMlpModelFloats, s), dx((size_t)n * ki::kMlpIn, s), dy(n, s);
+    DevBuf<int> de(1, s);
+    KI_CHECK_CUDA(cudaMemsetAsync(de.p, 0, sizeof(int), s));
+    KI_CHECK_CUDA(cudaMemcpyAsync(dm.p, model, sizeof(float) * ki::kMlpModelFloats, cudaMemcpyHostToDevice, s));
+    KI_CHECK_CUDA(cudaMemcpyAsync(dx.p, features, sizeof(float) * (size_t)n * ki::kMlpIn, cudaMemcpyHostToDevice, s));
+    ki::mlp_predict_bf16(dm.p, dx.p, n, dy.p, de.p, s);
+    int herr = 0;
+    KI_CHECK_CUDA(cudaMemcpyAsync(&herr, de.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    KI_CHECK_CUDA(cudaMemcpyAsync(ratios, dy.p, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+    KI_CHECK_CUDA(cudaStreamSynchronize(s));
+    if (herr) throw std::runtime_error("a bounded device wait timed out (tensor-core MLP inference)");
   });
 }
 

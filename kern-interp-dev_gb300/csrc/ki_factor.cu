@@ -41,6 +41,7 @@
 #include "ki_mlp.h"
 #include "ki_tc.cuh"
 #include "ki_tree_gpu.h"
+#include "ki_tune.h"
 
 namespace ki {
 
@@ -114,6 +115,10 @@ std::vector<StageSum> Factorization<T>::collect() {
 
 template <typename T>
 void Factorization<T>::fork() {
+  if (serial) {
+    for (int i = 0; i < kAux; i++) aux[i] = stream;
+    return;
+  }
   if (!fork_ev) {
     KI_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
     for (int i = 0; i < kAux; i++) {
@@ -127,6 +132,7 @@ void Factorization<T>::fork() {
 
 template <typename T>
 void Factorization<T>::join(int used) {
+  if (serial) return;
   for (int i = 0; i < used && i < kAux; i++) {
     KI_CUDA(cudaEventRecord(join_ev[i], aux[i]));
     KI_CUDA(cudaStreamWaitEvent(stream, join_ev[i], 0));
@@ -137,7 +143,7 @@ template <typename T>
 Factorization<T>::~Factorization() {
   if (stream) cudaStreamSynchronize(stream);
   for (int i = 0; i < kAux; i++) {
-    if (aux[i]) {
+    if (aux[i] && aux[i] != stream) {   // serial factorizations alias `stream`
       cudaStreamSynchronize(aux[i]);
       cudaStreamDestroy(aux[i]);
     }
@@ -1375,6 +1381,22 @@ __global__ void __launch_bounds__(128) k_box_features(const IdTask* tasks, int n
   }
 }
 
+// Sketch sizes from the predicted rank fractions (the tensor-core
+// inference): k^ = n ratio, l = min(n, ceil((1 + margin) k^) + oversample),
+// as k_box_features forms them; a ratio outside [0, 1] (an inference whose
+// wait gave up) takes the whole box, l = n.
+__global__ void k_sketch_sizes(const IdTask* tasks, int ntask, const float* ratio, float margin,
+                               int oversample, int* l_out, float* khat_out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ntask) return;
+  const int n = tasks[i].n;
+  float r = ratio[i];
+  if (!(r >= 0.f && r <= 1.f)) r = 1.f;
+  const float khat = (float)n * r;
+  l_out[i] = min(n, (int)ceilf((1.f + margin) * khat) + oversample);
+  khat_out[i] = khat;
+}
+
 // Streaming multiprocessors of the current device.
 inline int device_sm_count() {
   int dev = 0, n = 0;
@@ -1383,13 +1405,14 @@ inline int device_sm_count() {
   return n;
 }
 
-// k_id with fr-row fold blocks over `grid` boxes; FP32 launches of fewer
-// boxes than SMs use kIdBigThreads threads per CTA.
+// k_id with fr-row fold blocks over `grid` boxes.  threads: kThreads or (FP32)
+// kIdBigThreads, 0 for the heuristic: FP32 launches of fewer boxes than SMs
+// use kIdBigThreads threads per CTA.
 template <typename T, typename... A>
-void launch_k_id(int fr, unsigned grid, size_t smem, cudaStream_t st, A&&... args) {
+void launch_k_id(int fr, int threads, unsigned grid, size_t smem, cudaStream_t st, A&&... args) {
   static const int n_sm = device_sm_count();
   if constexpr (sizeof(T) == 4) {
-    if ((int)grid < n_sm) {
+    if (threads == 0 ? (int)grid < n_sm : threads == kIdBigThreads) {
       if (fr == 64)
         ki::launch(k_id<T, 64, kIdBigThreads>, grid, kIdBigThreads, smem, st, std::forward<A>(args)...);
       else
@@ -2932,6 +2955,13 @@ std::vector<int> plan_reuse(const Factorization<T>& prev, const Tree& tree,
 
 }  // namespace
 
+// Threads of a k_sweep launch: the autotuner's choice for the bucket, else
+// kThreads.
+inline int sweep_threads(int bucket) {
+  const int ch = tune_choice(kTuneSweep, bucket);
+  return ch < 0 ? kThreads : (ch == 0 ? 128 : (ch == 1 ? 256 : 512));
+}
+
 // Shared-memory bytes k_sweep needs to stage a factor matrix of `entries`
 // entries (the largest of r^2 and k r over the launch's boxes), and the
 // largest dynamic shared memory a staged sweep may use.
@@ -2965,7 +2995,12 @@ void launch_diag_all(Factorization<T>& F, T* x, int ncols, cudaStream_t s) {
     if (staged) sm += mats;
     if (sm > 48 * 1024)
       KI_CUDA(cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    ki::launch(k_sweep<T>, grid, kThreads, sm, st, all + b[0], x, ncols, ncols, cw, kDiag, staged);
+    const int bucket = sweep_bucket(sizeof(T) == 8, b[2]);
+    const bool rec = tune_recording();
+    if (rec) F.stage_begin(tune_stage(kTuneSweep, bucket).c_str(), 0, 0, st);
+    ki::launch(k_sweep<T>, grid, sweep_threads(bucket), sm, st, all + b[0], x, ncols, ncols, cw, kDiag,
+               staged);
+    if (rec) F.stage_end(st);
     KI_CUDA(cudaGetLastError());
   }
   if (par) F.join(std::min(next, Factorization<T>::kAux));
@@ -2988,8 +3023,12 @@ void launch_sweep(Factorization<T>& F, int l, int mode, T* x, int ncols, cudaStr
   if (staged) sm += mats;
   if (sm > 48 * 1024)
     KI_CUDA(cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  ki::launch(k_sweep<T>, grid, kThreads, sm, s, reinterpret_cast<SweepTask<T>*>(LF.d_tasks), x, ncols,
-                                        ncols, cw, mode, staged);
+  const int bucket = sweep_bucket(sizeof(T) == 8, LF.max_n);
+  const bool rec = tune_recording();
+  if (rec) F.stage_begin(tune_stage(kTuneSweep, bucket).c_str(), 0, 0, s);
+  ki::launch(k_sweep<T>, grid, sweep_threads(bucket), sm, s, reinterpret_cast<SweepTask<T>*>(LF.d_tasks),
+             x, ncols, ncols, cw, mode, staged);
+  if (rec) F.stage_end(s);
   KI_CUDA(cudaGetLastError());
 }
 
@@ -3092,6 +3131,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
   auto F = std::make_unique<Factorization<T>>();
   F->prm = prm;
   F->stream = stream;
+  F->serial = tune_recording();
   F->n_points = n_points;
   Tree& tree = F->tree;
   const int dim = prm.dim;
@@ -3496,11 +3536,22 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       float* d_feat = (float*)F->alloc(sizeof(float) * kMlpIn * (size_t)ntask);
       int* d_lsk = (int*)F->alloc(sizeof(int) * (size_t)ntask);
       float* d_khat = (float*)F->alloc(sizeof(float) * (size_t)ntask);
+      // the network runs in BF16 on the tensor cores (KI_MLP_FP32=1: in FP32
+      // inside k_box_features)
+      const char* mlp_env = std::getenv("KI_MLP_FP32");
+      const bool tc_mlp = prm.rank_model && !(mlp_env && std::string(mlp_env) == "1");
       ki::launch(k_box_features<T>, (ntask + 3) / 4, 128, 0, s,
           d_it, ntask, ipool, P, sd, d_m, 2 * np * sd, L > 1 ? (float)l / (float)(L - 1) : 0.f,
-          (float)(-std::log10(prm.id_tol) / 10.0), prm.rank_model, prm.sketch_margin,
-          prm.sketch_oversample, d_feat, d_lsk, d_khat);
+          (float)(-std::log10(prm.id_tol) / 10.0), tc_mlp ? nullptr : prm.rank_model,
+          prm.sketch_margin, prm.sketch_oversample, d_feat, d_lsk, d_khat);
       KI_CUDA(cudaGetLastError());
+      if (tc_mlp) {
+        float* d_ratio = (float*)F->alloc(sizeof(float) * (size_t)ntask);
+        mlp_predict_bf16(prm.rank_model, d_feat, ntask, d_ratio, F->d_err, s);
+        ki::launch(k_sketch_sizes, (ntask + 127) / 128, 128, 0, s, (const IdTask*)d_it, ntask,
+                   (const float*)d_ratio, prm.sketch_margin, prm.sketch_oversample, d_lsk, d_khat);
+        KI_CUDA(cudaGetLastError());
+      }
       kh.assign(itasks.size(), 0);
       std::vector<int> mh(itasks.size()), lh(itasks.size());
       std::vector<float> fh(kMlpIn * (size_t)ntask), khat(itasks.size());
@@ -3623,10 +3674,30 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
           }
           if (sm > smem_cap) throw std::runtime_error("box too large for the ID kernel");
           cudaStream_t st = fixed ? fixed : F->aux[(next_aux++) % n_streams];
-          launch_k_id<T>(fr, (unsigned)(b1 - b0), sm, st, (const IdTask*)d_it, b0,
+          // the autotuner's shape for this bin (fold rows, threads), where the
+          // fold fits every box of the bin (sorted by n: the last is the largest)
+          const int bucket = id_bucket(sizeof(T) == 8, g, itasks[b1 - 1].n);
+          const int ch = tune_choice(kTuneId, bucket);
+          int fr_use = fr, thr_use = 0;
+          size_t sm_use = sm;
+          if (ch >= 0) {
+            const int want = (ch & 1) ? 64 : 32;
+            const size_t s_want = id_smem_bytes<T>(itasks[b1 - 1].n, kmode, want, flags);
+            if (want == 32 || (kmode != 1 && (flags & 2) && s_want <= smem_cap)) {
+              fr_use = want;
+              sm_use = 0;
+              for (int q = b0; q < b1; q++)
+                sm_use = std::max(sm_use, id_smem_bytes<T>(itasks[q].n, kmode, want, flags));
+            }
+            thr_use = (sizeof(T) == 4 && (ch & 2)) ? kIdBigThreads : kThreads;
+          }
+          const bool rec = tune_recording();
+          if (rec) F->stage_begin(tune_stage(kTuneId, bucket).c_str(), 0, 0, st);
+          launch_k_id<T>(fr_use, thr_use, (unsigned)(b1 - b0), sm_use, st, (const IdTask*)d_it, b0,
                          (const int64_t*)d_soff, (const int*)d_slen, ipool, d_irows, d_tws, P, sd, ptab,
                          prm.id_tol, d_k, d_m, kmode, flags,
                          (const int*)(sketching && g != 1 ? d_lsk : nullptr));
+          if (rec) F->stage_end(st);
           KI_CUDA(cudaGetLastError());
           b0 = b1;
         }
@@ -3687,7 +3758,11 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
               }
               const size_t sm = sizeof(float) * (size_t)lm * nm;
               auto kern = lb ? k_cpqr<64> : k_cpqr<32>;
-              if (sm > 48 * 1024)
+              // the kernel's static shared memory counts against the 48 KB
+              // a launch gets without the opt-in attribute
+              cudaFuncAttributes fa{};
+              KI_CUDA(cudaFuncGetAttributes(&fa, kern));
+              if (sm + fa.sharedSizeBytes > 48 * 1024)
                 KI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
               ki::launch(kern, (unsigned)v.size(), 32 * (wq + 1), sm, ts, (const IdTask*)d_it,
                          (const int*)d_l2, (const int*)d_lsk, ipool, d_irows, (float*)d_tws, prm.id_tol, d_k);
@@ -3838,11 +3913,11 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
           std::string fname = "id_fallback@L" + std::to_string(l);
           F->stage_begin(fname.c_str(), 0, 0);
           if (cnt0 > 0)
-            launch_k_id<T>(32, (unsigned)cnt0, sm[0], s, (const IdTask*)d_t2, 0, (const int64_t*)d_soff,
+            launch_k_id<T>(32, 0, (unsigned)cnt0, sm[0], s, (const IdTask*)d_t2, 0, (const int64_t*)d_soff,
                            (const int*)d_slen, ipool, d_irows, d_tws, P, sd, ptab, prm.id_tol, d_k2, d_m2,
                            0, 2, (const int*)nullptr);
           if ((int)t2.size() > cnt0)
-            launch_k_id<T>(32, (unsigned)(t2.size() - cnt0), sm[1], s, (const IdTask*)d_t2, cnt0,
+            launch_k_id<T>(32, 0, (unsigned)(t2.size() - cnt0), sm[1], s, (const IdTask*)d_t2, cnt0,
                            (const int64_t*)d_soff, (const int*)d_slen, ipool, d_irows, d_tws, P, sd, ptab,
                            prm.id_tol, d_k2, d_m2, 1, 2, (const int*)nullptr);
           F->stage_end();
@@ -4122,8 +4197,22 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
           r_max = std::max(r_max, st2[q].n - st2[q].k);
           all_gj = all_gj && st2[q].gj;
         }
+        // the autotuner's threads (and, FP32, whether the bin may split)
+        const int bucket = schur_bucket(sizeof(T) == 8, r_max, ps);
+        const int ch = tune_choice(kTuneSchur, bucket);
+        int thr_use = thr;
+        if (ch >= 0) {
+          if (sizeof(T) == 4) {
+            thr_use = ch % 3 == 0 ? 256 : (ch % 3 == 1 ? 512 : 1024);
+            all_gj = all_gj && ch < 3;
+          } else {
+            thr_use = ch == 0 ? 128 : 256;
+          }
+        }
+        const bool rec = tune_recording();
+        if (rec) F->stage_begin(tune_stage(kTuneSchur, bucket).c_str(), 0, 0, bst);
         if (all_gj && r_max <= 128) {
-          ki::launch(k_schur<T>, (unsigned)(b1 - b0), thr, bsm, bst, d_st, b0, 1, F->d_err, 1);
+          ki::launch(k_schur<T>, (unsigned)(b1 - b0), thr_use, bsm, bst, d_st, b0, 1, F->d_err, 1);
           if constexpr (sizeof(T) == 4) {
             const SchurTask<float>* d_st32 = reinterpret_cast<const SchurTask<float>*>(d_st);
             const int ma = (r_max + 31) / 32;
@@ -4131,10 +4220,11 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
                     : ma == 3 ? k_gj<3, kGjLeanCols> : k_gj<4, kGjLeanCols>;
             ki::launch(gj, (unsigned)(b1 - b0), 32 * (32 * ma / kGjLeanCols), 0, bst, d_st32, b0, F->d_err);
           }
-          ki::launch(k_schur<T>, (unsigned)(b1 - b0), thr, bsm, bst, d_st, b0, 1, F->d_err, 2);
+          ki::launch(k_schur<T>, (unsigned)(b1 - b0), thr_use, bsm, bst, d_st, b0, 1, F->d_err, 2);
         } else {
-          ki::launch(k_schur<T>, (unsigned)(b1 - b0), thr, bsm, bst, d_st, b0, 1, F->d_err, 0);
+          ki::launch(k_schur<T>, (unsigned)(b1 - b0), thr_use, bsm, bst, d_st, b0, 1, F->d_err, 0);
         }
+        if (rec) F->stage_end(bst);
         b0 = b1;
       }
       if (n_glob > 0)
@@ -4331,7 +4421,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
   KI_CUDA(cudaStreamSynchronize(s));
   F->factor_prof = F->collect();
   if (herr == kDevTimeout)
-    throw std::runtime_error("a bounded device wait timed out (tensor-core sketch of an ID)");
+    throw std::runtime_error("a bounded device wait timed out (a tensor-core kernel: the rank "
+                             "predictor's inference or an ID sketch)");
   if (herr == kDevSingular) throw std::runtime_error("singular pivot in a Schur or root LU factorization");
   if (herr == kDevNonFinite) throw std::runtime_error("non-finite values in the factorization");
   F->factor_seconds =

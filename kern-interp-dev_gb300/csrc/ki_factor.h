@@ -97,6 +97,9 @@ struct Factorization {
   cudaEvent_t fork_ev = nullptr, join_ev[kAux] = {};
   void fork();                        // aux streams wait for `stream`
   void join(int used);                // `stream` waits for aux[0..used)
+  // every launch group on `stream` (the autotuner's timing runs: each
+  // group's events then time it alone)
+  bool serial = false;
   int N = 0;           // DOFs
   int n_points = 0;
   // point data (device, SoA, precision T)

@@ -3,6 +3,9 @@
 // deterministic for a given input.
 #include "ki_launch.cuh"
 #include "ki_mlp.h"
+#include "ki_tc.cuh"
+
+#include <cuda_bf16.h>
 
 #include <cmath>
 #include <stdexcept>
@@ -212,6 +215,135 @@ float mlp_train(float* d_model, const float* d_x, const float* d_y, int n, int e
   loss = loss_grad(w, d_model, d_x, d_y, n);
   KI_MLP_CUDA(cudaFreeAsync(mom, s));
   return loss;
+}
+
+namespace {
+
+// ------------------------------------------- BF16 inference on tensor cores --
+// 128 samples per CTA, one per thread: the standardized features (12, padded
+// to K = 16) and the hidden activations are BF16 operand tiles in shared
+// memory, the weights BF16 tiles, the two layers tcgen05 MMAs (kind::f16,
+// M = 128, N = 64) into FP32 TMEM accumulators; biases, ReLU and the output
+// layer in FP32 on the CUDA cores.
+constexpr int kTcSamples = 128;
+constexpr uint32_t kSbo16 = 256;    // 8-row groups of a K = 16 tile (two core matrices)
+constexpr uint32_t kSbo64 = 1024;   // K = 64 (eight core matrices)
+constexpr uint32_t kOffX = 0, kOffW1 = kOffX + kTcSamples * 32, kOffH = kOffW1 + kMlpHidden * 32,
+                   kOffW2 = kOffH + kTcSamples * 128, kOffPar = kOffW2 + kMlpHidden * 128,
+                   kOffBar = kOffPar + 1024, kTcSmem = kOffBar + 16;
+// bounded waits for the MMAs (SM cycles): far above their microseconds
+constexpr long long kMlpWaitCycles = 200000000LL;
+
+__device__ __forceinline__ void put_bf16(unsigned char* tile, int row, int k, uint32_t sbo, float v) {
+  *reinterpret_cast<__nv_bfloat16*>(tile + tc::kmajor_offset_bf16(row, k, sbo)) = __float2bfloat16_rn(v);
+}
+
+__global__ void __launch_bounds__(kTcSamples) k_mlp_tc(const float* model, const float* x, int n,
+                                                       float* out, int* err) {
+  extern __shared__ __align__(128) unsigned char tsm[];
+  unsigned char* Xs = tsm + kOffX;
+  unsigned char* W1s = tsm + kOffW1;
+  unsigned char* Hs = tsm + kOffH;
+  unsigned char* W2s = tsm + kOffW2;
+  float* b1 = reinterpret_cast<float*>(tsm + kOffPar);
+  float* b2 = b1 + kMlpHidden;
+  float* w3 = b2 + kMlpHidden;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tsm + kOffBar);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(tsm + kOffBar + 8);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int i = blockIdx.x * kTcSamples + tid;
+  for (int e = tid; e < kMlpHidden; e += blockDim.x) {
+    b1[e] = model[kMlpB1 + e];
+    b2[e] = model[kMlpB2 + e];
+    w3[e] = model[kMlpW3 + e];
+  }
+  for (int k = 0; k < 16; k++) {
+    float v = 0.f;
+    if (i < n && k < kMlpIn) v = (x[(size_t)i * kMlpIn + k] - model[kMlpMean + k]) / model[kMlpScale + k];
+    put_bf16(Xs, tid, k, kSbo16, v);
+  }
+  for (int e = tid; e < kMlpHidden * 16; e += blockDim.x) {
+    const int j = e / 16, k = e % 16;
+    put_bf16(W1s, j, k, kSbo16, k < kMlpIn ? model[kMlpW1 + j * kMlpIn + k] : 0.f);
+  }
+  for (int e = tid; e < kMlpHidden * kMlpHidden; e += blockDim.x) {
+    const int j = e / kMlpHidden, k = e % kMlpHidden;
+    put_bf16(W2s, j, k, kSbo64, model[kMlpW2 + j * kMlpHidden + k]);
+  }
+  if (warp == 0) tc::tmem_alloc(tslot, 128);
+  if (tid == 0) {
+    tc::mbar_init(bar, 1);
+    tc::fence_mbar_init();
+  }
+  tc::fence_proxy_async_smem();   // the operand tiles, visible to the tensor core
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = tc::idesc_bf16(kTcSamples, kMlpHidden);
+  // layer 1: D1 (TMEM columns 0-63) = X W1^T
+  if (tid == 0) {
+    tc::mma_bf16(tmem, tc::smem_desc(tc::smem_u32(Xs), tc::kLbo, kSbo16),
+                 tc::smem_desc(tc::smem_u32(W1s), tc::kLbo, kSbo16), idesc, 0);
+    tc::mma_commit(bar);
+  }
+  bool ok = tc::mbar_wait(bar, 0, kMlpWaitCycles);
+  tc::fence_after_sync();
+  const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+  float v[16];
+  if (ok) {
+    for (int c = 0; c < kMlpHidden; c += 16) {
+      tc::tmem_ld16(tmem + lane_base + c, v);
+      for (int q = 0; q < 16; q++) {
+        const float z = v[q] + b1[c + q];
+        put_bf16(Hs, tid, c + q, kSbo64, z > 0.f ? z : 0.f);
+      }
+    }
+  }
+  tc::fence_proxy_async_smem();
+  tc::fence_before_sync();
+  const bool ok1 = __syncthreads_and(ok);
+  tc::fence_after_sync();
+  // layer 2: D2 (columns 64-127) = H W2^T, four K = 16 steps
+  if (ok1 && tid == 0) {
+    for (int j = 0; j < kMlpHidden / 16; j++)
+      tc::mma_bf16(tmem + 64, tc::smem_desc(tc::smem_u32(Hs) + 256u * j, tc::kLbo, kSbo64),
+                   tc::smem_desc(tc::smem_u32(W2s) + 256u * j, tc::kLbo, kSbo64), idesc, j > 0);
+    tc::mma_commit(bar);
+  }
+  ok = ok1 && tc::mbar_wait(bar, 1, kMlpWaitCycles);
+  tc::fence_after_sync();
+  float zo = model[kMlpB3];
+  if (ok) {
+    for (int c = 0; c < kMlpHidden; c += 16) {
+      tc::tmem_ld16(tmem + lane_base + 64 + c, v);
+      for (int q = 0; q < 16; q++) {
+        const float z = v[q] + b2[c + q];
+        zo += w3[c + q] * (z > 0.f ? z : 0.f);
+      }
+    }
+  }
+  ok = __syncthreads_and(ok);
+  if (!ok) {
+    // a wait gave up: wait (bounded again) for the last MMA group issued
+    // before the accumulators are freed, and report
+    if (tid == 0) atomicMax(err, 3);
+    tc::mbar_wait(bar, ok1 ? 1 : 0, kMlpWaitCycles);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 128);
+  if (ok && i < n) out[i] = 1.f / (1.f + expf(-zo));
+}
+
+}  // namespace
+
+void mlp_predict_bf16(const float* d_model, const float* d_x, int n, float* d_out, int* d_err,
+                      cudaStream_t s) {
+  if (n <= 0) return;
+  ki::launch(k_mlp_tc, (n + kTcSamples - 1) / kTcSamples, kTcSamples, kTcSmem, s, d_model, d_x, n,
+             d_out, d_err);
+  KI_MLP_CUDA(cudaGetLastError());
 }
 
 void mlp_predict(const float* d_model, const float* d_x, int n, float* d_out, cudaStream_t s) {

@@ -50,5 +50,10 @@ float mlp_train(float* d_model, const float* d_x, const float* d_y, int n, int e
                 cudaStream_t s);
 // Predictions for n samples.
 void mlp_predict(const float* d_model, const float* d_x, int n, float* d_out, cudaStream_t s);
+// The same in BF16 on the tensor cores (tcgen05, FP32 accumulation; the
+// factorization's inference): 128 samples per CTA.  A bounded MMA wait that
+// gives up sets *d_err to 3 and leaves those outputs unwritten.
+void mlp_predict_bf16(const float* d_model, const float* d_x, int n, float* d_out, int* d_err,
+                      cudaStream_t s);
 
 }  // namespace ki

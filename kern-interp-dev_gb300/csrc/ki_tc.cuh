@@ -58,6 +58,22 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
          ((uint32_t)(M >> 4) << 24);
 }
 
+// Instruction descriptor of a dense kind::f16 MMA with BF16 operands: D in
+// FP32 (bits 4-5 = 1), A and B BF16 (bits 7-9, 10-12 = 1), both K-major.
+// One MMA consumes K = 16 BF16 values, again two core matrices of 16 bytes
+// per row, so the tile layout and the 256-byte K steps are those of TF32.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+// Byte offset of BF16 element (row, k) in a K-major tile whose 8-row groups
+// are `sbo` bytes apart (core matrix: 8 rows x 8 values).
+__host__ __device__ __forceinline__ uint32_t kmajor_offset_bf16(int row, int k, uint32_t sbo) {
+  return (uint32_t)(row >> 3) * sbo + (uint32_t)(k >> 3) * kLbo + (uint32_t)(row & 7) * 16u +
+         (uint32_t)(k & 7) * 2u;
+}
+
 // Round to the nearest TF32 value (ties away from zero), returned in an FP32
 // container with the low 13 bits clear, so the tensor core reads it exactly.
 __device__ __forceinline__ float to_tf32(float x) {
@@ -141,6 +157,16 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+      ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// The same with BF16 operands (kind::f16).
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
       ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
 }

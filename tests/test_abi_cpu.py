@@ -95,3 +95,23 @@ def test_no_gpu_reports_cuda_error(pkg, lib, have_gpu):
     d, keep = _desc(pkg, prob)
     h = ctypes.c_void_p()
     assert lib.ki_factor_create(ctypes.byref(d), ctypes.byref(h)) == pkg.KI_ERR_CUDA
+
+
+def test_tune_table_round_trip_and_rejects(pkg, lib):
+    """The autotuner's table (ki_tune_set / ki_tune_get) needs no GPU: a table
+    set comes back as set, {} clears it, malformed or out-of-range input is
+    rejected with KI_ERR_ARG and leaves the table as it was."""
+    saved = pkg.tune_get()
+    try:
+        table = {"id:17": 3, "schur:42": 5, "sweep:3": 0, "id:300": 1}
+        pkg.tune_set(table)
+        assert pkg.tune_get() == table
+        for bad in ['{"id:17": 4}', '{"nope:1": 0}', '{"id:999": 0}', '{"id:1" 0}', '[1]',
+                    '{"schur:3": 1,}', '{"sweep:1": 0} x']:
+            rc = lib.ki_tune_set(bad.encode())
+            assert rc == pkg.KI_ERR_ARG, bad
+            assert pkg.tune_get() == table, bad
+        pkg.tune_set({})
+        assert pkg.tune_get() == {}
+    finally:
+        pkg.tune_set(saved)

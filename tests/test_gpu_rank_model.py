@@ -133,3 +133,37 @@ def test_underpredicting_model_falls_back_to_the_plain_id(pkg):
     mu_p = plain.solve(f)[0]
     mu_f = fb.solve(f)[0]
     assert np.abs(mu_f - mu_p).max() <= 1e-4 * np.abs(mu_p).max()
+
+
+def bf16(a):
+    """Round FP32 values to BF16 (nearest, ties to even), returned as FP32."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def test_tensor_core_bf16_inference(pkg):
+    """The factorization's inference (BF16 operands, tcgen05 MMAs into FP32
+    TMEM accumulators) against a NumPy restatement with the same BF16
+    roundings, and within 0.01 of the FP32 network, on a trained model and a
+    ragged sample count (not a multiple of the 128 samples of a CTA).  The
+    restatement agrees to 1e-3, not exactly: an FP32 sum that lands on the
+    other side of a BF16 rounding boundary moves one activation by one BF16
+    step."""
+    rng = np.random.default_rng(5)
+    X = (rng.standard_normal((1000, F)) * 1.5 + 0.5).astype(np.float32)
+    y = (1 / (1 + np.exp(-X[:, 0] + 0.5 * X[:, 3]))).astype(np.float32)
+    model, _ = pkg.rank_model_train(X, y, epochs=200, seed=2)
+    p = {k: v.astype(np.float32) for k, v in unpack(model).items()}
+    Xr = X[:777]
+    xn = bf16((Xr - p["mean"]) / p["scale"]).astype(np.float64)
+    z1 = xn @ bf16(p["W1"]).astype(np.float64).T + p["b1"]
+    h = bf16(np.maximum(z1, 0).astype(np.float32)).astype(np.float64)
+    z2 = h @ bf16(p["W2"]).astype(np.float64).T + p["b2"]
+    zo = np.maximum(z2, 0) @ p["W3"] + p["b3"][0]
+    emul = 1 / (1 + np.exp(-zo))
+    tc = pkg.rank_model_predict(model, Xr, bf16=True)
+    fp32 = pkg.rank_model_predict(model, Xr)
+    assert np.abs(tc - emul).max() <= 1e-3, np.abs(tc - emul).max()
+    assert np.abs(tc - fp32).max() <= 1e-2, np.abs(tc - fp32).max()
+    assert pkg.rank_model_predict(model, X[:0], bf16=True).size == 0
