@@ -257,9 +257,11 @@ typedef struct {
  * correction d whose residual change is small enough is followed by the
  * update r -= A_low d, A_low the FMM in FP32 arithmetic at 12 terms
  * (relative error eps_low = 1e-5 or better), instead of a new FP64 product:
- * the update is taken while the accumulated bound eps_low * sum over
+ * the update is kept while the accumulated bound eps_low * sum over
  * updates of (||r_before|| + ||r_after||) / ||b|| (so that ||A d|| <=
- * ||r_before|| + ||r_after||) stays below tol / 20 per column; the
+ * ||r_before|| + ||r_after||) stays below tol / 20 per column -- it is
+ * tried when eps_low ||r_before|| / ||b|| fits, and an update whose actual
+ * bound does not fit is followed by the FP64 product after all; the
  * reported residual is the updated one plus that bound.
  * KI_REFINE_UPDATE=0 recomputes the FP64 residual after every correction.
  */

@@ -412,8 +412,9 @@ def rank_model_floats():
 
 
 def load_rank_model(path=None):
-    """The trained rank-predictor blob shipped with the package."""
-    return np.load(path or RANK_MODEL_PATH).astype(np.float32)
+    """The trained rank-predictor blob shipped with the package (or the one
+    at `path`, or at $KI_RANK_MODEL)."""
+    return np.load(path or os.environ.get("KI_RANK_MODEL") or RANK_MODEL_PATH).astype(np.float32)
 
 
 def rank_model_train(features, ratios, epochs=2000, lr=3e-3, seed=0):

@@ -1027,20 +1027,27 @@ void refined_solve(ki_factor* f, const double* b, int ncols, double* mu, double*
   };
   int steps = 0, updates = 0;
   while (bound() > tol && steps < max_steps) {
-    // an update is taken when even ||r_after|| = ||r_before|| keeps the
-    // accumulated bound below tol / 20 in every column
+    // an update is tried when the bound stays below tol / 20 in every
+    // column for a correction that removes most of the residual
+    // (||r_after|| << ||r_before||); if the actual ||r_after|| pushes it
+    // over, the FP64 residual is recomputed (and the bound reset) after all
     bool update = may_update;
     for (int c = 0; c < ncols && update; c++)
-      update = drift[c] + kLowRelErr * 2.0 * rel[c] <= tol / 20;
+      update = drift[c] + kLowRelErr * rel[c] <= tol / 20;
     corr(update);
     steps++;
+    bool recompute = !update;
     if (update) {
       rel_old = rel;
       res = update_residual(f, b, dcol.p, nb > 0 ? dal.p : nullptr, ncols, r1.p, r2.p, y1.p,
                             y2.p, work.p, &rel, s, rec);
-      for (int c = 0; c < ncols; c++) drift[c] += kLowRelErr * (rel_old[c] + rel[c]);
+      for (int c = 0; c < ncols; c++) {
+        drift[c] += kLowRelErr * (rel_old[c] + rel[c]);
+        recompute = recompute || drift[c] > tol / 20;
+      }
       updates++;
-    } else {
+    }
+    if (recompute) {
       res = residual_norms(f, b, mu, alpha, ncols, r1.p, r2.p, work.p, &rel, s, tol, rec);
       std::fill(drift.begin(), drift.end(), 0.0);
     }

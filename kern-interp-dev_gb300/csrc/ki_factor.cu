@@ -161,6 +161,12 @@ Factorization<T>::~Factorization() {
 namespace {
 
 constexpr int kThreads = 256;
+// A sketched ID's rank counts only when the sketch revealed it with at least
+// this many sketch rows to spare: a rank found in the sketch's last rows can
+// be an artefact of the sketch's own smallest singular values (the
+// oversampling of a randomized range finder, Halko, Martinsson and Tropp
+// 2011, section 4.2), and the box is recompressed by the plain ID instead.
+constexpr int kSketchGuard = 5;
 constexpr int kFoldRows = 32;   // rows of the ID matrix generated per TSQR fold
 
 template <typename T> __device__ __forceinline__ T tol3z();
@@ -798,8 +804,9 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? kIdMinBlocks<T> : 1) k_id
   }
   __syncthreads();
   const int k = s_k;
-  if (sketch && k == 0 && jmax == rowsR && rowsR < n) {
-    // the sketch did not reveal the rank: recompress with the plain ID
+  if (sketch && rowsR < n && (k == 0 ? jmax == rowsR : k > rowsR - kSketchGuard)) {
+    // the sketch did not reveal the rank with kSketchGuard rows to spare:
+    // recompress with the plain ID
     if (tid == 0) k_out[task] = -1;
     return;
   }
@@ -1179,8 +1186,9 @@ __global__ void __launch_bounds__(256) k_cpqr(const IdTask* tasks, const int* li
     }
   }
   int* gperm = iscratch + t.perm;
-  if (!done && jmax == l && l < n) {
-    // the sketch did not reveal the rank: recompress with the plain ID
+  if (l < n && (done ? k > l - kSketchGuard : jmax == l)) {
+    // the sketch did not reveal the rank with kSketchGuard rows to spare:
+    // recompress with the plain ID
     if (threadIdx.x == 0) k_out[ti] = -1;
     return;
   }
@@ -1457,8 +1465,6 @@ struct WideTask {
 };
 
 constexpr int kQrNb = 32;     // panel width
-constexpr int kQrTile = 32;   // trailing-update column tile
-constexpr int kQrRows = 64;   // rows staged per trailing-update pass
 
 template <typename T>
 __global__ void k_wide_assemble(const WideTask* tasks, T* wpool, const int* ipool, const int* iscratch,
@@ -1659,82 +1665,164 @@ __global__ void __launch_bounds__(256) k_qr_panel(const WideTask* tasks, T* wpoo
   }
 }
 
-// Trailing update A(p:m, c0:c0+32) <- (I - V T V^T)^T A(p:m, c0:c0+32).
+// Trailing update of the blocked QR, A(p:m, p+w:n) <- (I - V T V^T)^T
+// A(p:m, p+w:n), in three register-tiled launches over many CTAs per box:
+//   k_qr_wpart  partial products V^T A over chunks of kQrChunk rows;
+//   k_qr_wsum   W = the partials summed in a fixed order, then W <- T^T W;
+//   k_qr_apply  A -= V W in tiles of kQrTileRows x kQrTileCols.
+// V (the panel's reflectors) is unit lower trapezoidal: V(row, l) is the
+// stored tail below the diagonal (row > p + l), 1 on it, 0 above.
+constexpr int kQrChunk = 2048;     // rows per partial product
+constexpr int kQrWCols = 64;       // trailing columns per CTA of k_qr_wpart / k_qr_wsum
+constexpr int kQrSub = 32;         // rows staged per step of k_qr_wpart
+constexpr int kQrTileRows = 64;    // k_qr_apply tile
+constexpr int kQrTileCols = 64;
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_qr_update(const WideTask* tasks, T* wpool, int p) {
+__device__ __forceinline__ T qr_v(const T* A, int m, int p, int row, int l) {
+  return row > p + l ? A[row + (size_t)m * (p + l)] : (row == p + l ? T(1) : T(0));
+}
+
+// Grid (box, column block of kQrWCols, row chunk).  Thread (4 reflectors x
+// 4 columns) of the 32 x 64 block; rows staged kQrSub at a time.
+template <typename T>
+__global__ void __launch_bounds__(128) k_qr_wpart(const WideTask* tasks, const T* wpool, T* parts,
+                                                  int p) {
   const WideTask t = tasks[blockIdx.x];
   const int m = t.m, n = t.n;
   if (p >= n) return;
   const int w = min(kQrNb, n - p);
-  const int c0 = p + w + blockIdx.y * kQrTile;
-  if (c0 >= n) return;
-  const int tc = min(kQrTile, n - c0);
-  T* A = wpool + t.M;
+  const int c0 = p + w + blockIdx.y * kQrWCols;
+  const int r0 = p + blockIdx.z * kQrChunk;
+  if (c0 >= n || r0 >= m) return;
+  const int r1 = min(m, r0 + kQrChunk), nc = min(kQrWCols, n - c0);
+  const T* A = wpool + t.M;
+  __shared__ T Vs[kQrSub][kQrNb + 1];
+  __shared__ T As[kQrSub][kQrWCols + 1];
+  const int tid = threadIdx.x, lr = (tid >> 4) * 4, lc = (tid & 15) * 4;
+  T acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) acc[a][b] = T(0);
+  for (int rb = r0; rb < r1; rb += kQrSub) {
+    __syncthreads();
+    for (int e = tid; e < kQrSub * kQrNb; e += blockDim.x) {
+      const int i = e % kQrSub, l = e / kQrSub, row = rb + i;   // rows fastest: coalesced
+      Vs[i][l] = (row < r1 && l < w) ? qr_v(A, m, p, row, l) : T(0);
+    }
+    for (int e = tid; e < kQrSub * kQrWCols; e += blockDim.x) {
+      const int i = e % kQrSub, c = e / kQrSub, row = rb + i;
+      As[i][c] = (row < r1 && c < nc) ? A[row + (size_t)m * (c0 + c)] : T(0);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int i = 0; i < kQrSub; i++) {
+      T v[4], x[4];
+#pragma unroll
+      for (int a = 0; a < 4; a++) v[a] = Vs[i][lr + a];
+#pragma unroll
+      for (int b = 0; b < 4; b++) x[b] = As[i][lc + b];
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) acc[a][b] += v[a] * x[b];
+    }
+  }
+  // partial z of the box: kQrNb x n, row-major (reflector l, column c)
+  T* out = parts + t.part + (size_t)blockIdx.z * kQrNb * n;
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++)
+      if (lr + a < w && lc + b < nc) out[(size_t)(lr + a) * n + c0 + lc + b] = acc[a][b];
+}
+
+// Grid (box, column block): one thread per trailing column sums the row
+// chunks' partials in chunk order, applies T^T (T upper triangular:
+// (T^T W)_l = sum_(r <= l) T(r, l) W_r) and writes W into partial 0.
+template <typename T>
+__global__ void __launch_bounds__(kQrWCols) k_qr_wsum(const WideTask* tasks, const T* wpool, T* parts,
+                                                      int p) {
+  const WideTask t = tasks[blockIdx.x];
+  const int m = t.m, n = t.n;
+  if (p >= n) return;
+  const int w = min(kQrNb, n - p);
+  const int c = p + w + blockIdx.y * kQrWCols + threadIdx.x;
+  if (c >= n) return;
+  const int chunks = (m - p + kQrChunk - 1) / kQrChunk;
   const T* Tf = wpool + t.Tf;
-  __shared__ T Vs[kQrRows][kQrNb + 1];
-  __shared__ T As[kQrRows][kQrTile + 1];
-  __shared__ T Ws[kQrNb][kQrTile + 1];
+  T* W = parts + t.part;
+  T s[kQrNb];
+#pragma unroll
+  for (int l = 0; l < kQrNb; l++) s[l] = T(0);
+  for (int z = 0; z < chunks; z++) {
+    const T* pz = W + (size_t)z * kQrNb * n;
+#pragma unroll
+    for (int l = 0; l < kQrNb; l++)
+      if (l < w) s[l] += pz[(size_t)l * n + c];
+  }
+#pragma unroll
+  for (int l = 0; l < kQrNb; l++) {
+    if (l >= w) break;
+    T acc = T(0);
+#pragma unroll
+    for (int r = 0; r < kQrNb; r++)
+      if (r <= l) acc += Tf[r + kQrNb * l] * s[r];
+    W[(size_t)l * n + c] = acc;
+  }
+}
+
+// Grid (box, row tile, column tile): A(rows, cols) -= V(rows, :) W(:, cols).
+// Thread: 4 consecutive rows x 8 columns (16 threads cover a tile column's
+// 64 rows, coalesced); V^T and W staged in shared memory.
+template <typename T>
+__global__ void __launch_bounds__(128) k_qr_apply(const WideTask* tasks, T* wpool, const T* parts, int p) {
+  const WideTask t = tasks[blockIdx.x];
+  const int m = t.m, n = t.n;
+  if (p >= n) return;
+  const int w = min(kQrNb, n - p);
+  const int rt = p + blockIdx.y * kQrTileRows, ct = p + w + blockIdx.z * kQrTileCols;
+  if (rt >= m || ct >= n) return;
+  const int nr = min(kQrTileRows, m - rt), nc = min(kQrTileCols, n - ct);
+  T* A = wpool + t.M;
+  const T* W = parts + t.part;
+  __shared__ T Vt[kQrNb][kQrTileRows];
+  __shared__ T Ws[kQrNb][kQrTileCols];
   const int tid = threadIdx.x;
-  // W = V^T A  (w x tc); thread owns entries e = tid + 256 q
-  T acc[4] = {T(0), T(0), T(0), T(0)};
-  for (int r0 = p; r0 < m; r0 += kQrRows) {
-    for (int e = tid; e < kQrRows * kQrNb; e += blockDim.x) {
-      int i = e / kQrNb, l = e % kQrNb, row = r0 + i;
-      T v = T(0);
-      if (row < m && l < w) v = row > p + l ? A[row + (size_t)m * (p + l)] : (row == p + l ? T(1) : T(0));
-      Vs[i][l] = v;
-    }
-    for (int e = tid; e < kQrRows * kQrTile; e += blockDim.x) {
-      int i = e / kQrTile, c = e % kQrTile, row = r0 + i;
-      As[i][c] = (row < m && c < tc) ? A[row + (size_t)m * (c0 + c)] : T(0);
-    }
-    __syncthreads();
-    for (int q = 0; q < 4; q++) {
-      int e = tid + 256 * q, l = e / kQrTile, c = e % kQrTile;
-      T s0 = T(0), s1 = T(0);
-      for (int i = 0; i < kQrRows; i += 2) {
-        s0 += Vs[i][l] * As[i][c];
-        s1 += Vs[i + 1][l] * As[i + 1][c];
-      }
-      acc[q] += s0 + s1;
-    }
-    __syncthreads();
+  for (int e = tid; e < kQrNb * kQrTileRows; e += blockDim.x) {
+    const int i = e % kQrTileRows, l = e / kQrTileRows;
+    Vt[l][i] = (i < nr && l < w) ? qr_v(A, m, p, rt + i, l) : T(0);
   }
-  for (int q = 0; q < 4; q++) {
-    int e = tid + 256 * q;
-    Ws[e / kQrTile][e % kQrTile] = acc[q];
+  for (int e = tid; e < kQrNb * kQrTileCols; e += blockDim.x) {
+    const int c = e % kQrTileCols, l = e / kQrTileCols;
+    Ws[l][c] = (c < nc && l < w) ? W[(size_t)l * n + ct + c] : T(0);
   }
   __syncthreads();
-  // W <- T^T W (T upper triangular -> T^T lower)
-  for (int q = 0; q < 4; q++) {
-    int e = tid + 256 * q, l = e / kQrTile, c = e % kQrTile;
-    T s = T(0);
-    for (int r = 0; r <= l && r < w; r++) s += Tf[r + kQrNb * l] * Ws[r][c];
-    acc[q] = l < w ? s : T(0);
+  const int r4 = (tid & 15) * 4, c8 = (tid >> 4) * 8;
+  T acc[4][8];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 8; b++) acc[a][b] = T(0);
+  for (int l = 0; l < w; l++) {
+    T v[4], x[8];
+#pragma unroll
+    for (int a = 0; a < 4; a++) v[a] = Vt[l][r4 + a];
+#pragma unroll
+    for (int b = 0; b < 8; b++) x[b] = Ws[l][c8 + b];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int b = 0; b < 8; b++) acc[a][b] += v[a] * x[b];
   }
-  __syncthreads();
-  for (int q = 0; q < 4; q++) {
-    int e = tid + 256 * q;
-    Ws[e / kQrTile][e % kQrTile] = acc[q];
-  }
-  __syncthreads();
-  // A -= V W
-  for (int r0 = p; r0 < m; r0 += kQrRows) {
-    for (int e = tid; e < kQrRows * kQrNb; e += blockDim.x) {
-      int i = e / kQrNb, l = e % kQrNb, row = r0 + i;
-      T v = T(0);
-      if (row < m && l < w) v = row > p + l ? A[row + (size_t)m * (p + l)] : (row == p + l ? T(1) : T(0));
-      Vs[i][l] = v;
-    }
-    __syncthreads();
-    for (int e = tid; e < kQrRows * kQrTile; e += blockDim.x) {
-      int i = e / kQrTile, c = e % kQrTile, row = r0 + i;
-      if (row >= m || c >= tc) continue;
-      T s = T(0);
-      for (int l = 0; l < w; l++) s += Vs[i][l] * Ws[l][c];
-      A[row + (size_t)m * (c0 + c)] -= s;
-    }
-    __syncthreads();
+#pragma unroll
+  for (int b = 0; b < 8; b++) {
+    if (c8 + b >= nc) continue;
+    T* col = A + (size_t)m * (ct + c8 + b) + rt;
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+      if (r4 + a < nr) col[r4 + a] -= acc[a][b];
   }
 }
 
@@ -3813,20 +3901,40 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
           T* d_wpool = nullptr;
           WideTask* d_wt = nullptr;
           if (!wt.empty()) {
+            // the trailing updates' row-chunk partials of V^T A (part 0 then
+            // holds W), per box chunks x kQrNb x n
+            int64_t ptot_qr = 0;
+            int max_m = 0;
             for (auto& w : wt) {
               w.Tf = mtot;
               mtot += kQrNb * kQrNb;
+              w.part = ptot_qr;
+              ptot_qr += (int64_t)((w.m + kQrChunk - 1) / kQrChunk) * kQrNb * w.n;
+              max_m = std::max(max_m, w.m);
             }
+            T* d_qparts = nullptr;
             KI_CUDA(pool_malloc((void**)&d_wpool, sizeof(T) * (mtot + 16), ws3));
+            KI_CUDA(pool_malloc((void**)&d_qparts, sizeof(T) * (ptot_qr + 16), ws3));
             KI_CUDA(pool_malloc((void**)&d_wt, sizeof(WideTask) * wt.size(), ws3));
             upload(d_wt, wt, ws3);
             ki::launch(k_wide_assemble<T>, dim3((unsigned)wt.size(), (maxn + 7) / 8), 256, 0, ws3,
                 d_wt, d_wpool, ipool, d_irows, P, sd, ptab);
+            const unsigned nb_w = (unsigned)wt.size();
             for (int p0 = 0; p0 < maxn; p0 += kQrNb) {
-              ki::launch(k_qr_panel<T>, (unsigned)wt.size(), 256, 0, ws3, d_wt, d_wpool, p0);
-              int tiles = (maxn - p0 - kQrNb + kQrTile - 1) / kQrTile;
-              if (tiles > 0) ki::launch(k_qr_update<T>, dim3((unsigned)wt.size(), tiles), 256, 0, ws3, d_wt, d_wpool, p0);
+              ki::launch(k_qr_panel<T>, nb_w, 256, 0, ws3, d_wt, d_wpool, p0);
+              const int trail = maxn - p0 - kQrNb;   // trailing columns of the widest box
+              if (trail <= 0) continue;
+              const unsigned cblk = (unsigned)((trail + kQrWCols - 1) / kQrWCols);
+              const unsigned chunks = (unsigned)((max_m - p0 + kQrChunk - 1) / kQrChunk);
+              ki::launch(k_qr_wpart<T>, dim3(nb_w, cblk, chunks), 128, 0, ws3, (const WideTask*)d_wt,
+                         (const T*)d_wpool, d_qparts, p0);
+              ki::launch(k_qr_wsum<T>, dim3(nb_w, cblk), kQrWCols, 0, ws3, (const WideTask*)d_wt,
+                         (const T*)d_wpool, d_qparts, p0);
+              ki::launch(k_qr_apply<T>, dim3(nb_w, (unsigned)((max_m - p0 + kQrTileRows - 1) / kQrTileRows),
+                                             (unsigned)((trail + kQrTileCols - 1) / kQrTileCols)),
+                         128, 0, ws3, (const WideTask*)d_wt, d_wpool, (const T*)d_qparts, p0);
             }
+            KI_CUDA(cudaFreeAsync(d_qparts, ws3));
             ki::launch(k_wide_triangle<T>, (unsigned)wt.size(), 256, 0, ws3, d_wt, d_wpool, d_tws);
             KI_CUDA(cudaGetLastError());
           }

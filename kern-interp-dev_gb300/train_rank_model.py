@@ -172,14 +172,20 @@ def main():
     ap.add_argument("--eval-nodes", type=int, default=32768)
     ap.add_argument("--out", default=os.path.join(HERE, "rank_model.npy"))
     ap.add_argument("--report", default=None)
+    ap.add_argument("--model", default=None,
+                    help="evaluate this trained blob instead of building a corpus and training")
     a = ap.parse_args()
     import __graft_entry__ as g
     pkg = g.load_package()
-    X, y = corpus(pkg, a.stars, a.ellipsoids, log=lambda *v: print(*v, flush=True))
-    model, loss = pkg.rank_model_train(X, y, epochs=a.epochs, lr=3e-3, seed=0)
-    rep = {"corpus": {"stars": a.stars, "ellipsoids": a.ellipsoids, "boxes": int(len(y)),
-                      "train_mse": float(loss)}}
-    print("training set: %d boxes, final MSE %.3e" % (len(y), loss), flush=True)
+    if a.model:
+        model = pkg.load_rank_model(a.model)
+        rep = {"corpus": {"model": os.path.basename(a.model)}}
+    else:
+        X, y = corpus(pkg, a.stars, a.ellipsoids, log=lambda *v: print(*v, flush=True))
+        model, loss = pkg.rank_model_train(X, y, epochs=a.epochs, lr=3e-3, seed=0)
+        rep = {"corpus": {"stars": a.stars, "ellipsoids": a.ellipsoids, "boxes": int(len(y)),
+                          "train_mse": float(loss)}}
+        print("training set: %d boxes, final MSE %.3e" % (len(y), loss), flush=True)
     held = pkg.geometry.disc_with_ellipses(1 << 18, 64, seed=1)
     fac = pkg.Factor(held.points, held.normals, held.weights, held.curvatures, id_tol=1e-6,
                      precision=pkg.PRECISION_FP64, hole_centers=held.hole_centers,
@@ -192,8 +198,9 @@ def main():
     rep["held_out_stokes3"] = evaluate_stokes3(pkg, model, a.eval_nodes,
                                                log=lambda *v: print(*v, flush=True))
     print(json.dumps(rep["held_out_stokes3"]), flush=True)
-    np.save(a.out, model)
-    print("wrote", a.out)
+    if not a.model:
+        np.save(a.out, model)
+        print("wrote", a.out)
     if a.report:
         with open(a.report, "w") as fh:
             json.dump(rep, fh, indent=1)
