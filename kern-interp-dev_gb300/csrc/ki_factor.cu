@@ -1588,80 +1588,192 @@ __device__ void block_sum_vec(T (&vals)[kQrNb], T* red /* [nwarps][kQrNb] */, T*
   __syncthreads();
 }
 
+// Grid barrier of a cooperative launch (every CTA resident by construction):
+// the CTA arrives on a counter, the last arriver resets it and advances the
+// generation, the others wait for the advance -- for at most `limit` SM
+// cycles.  A wait that gives up sets the abort flag and the device status
+// (kDevTimeout); from then on every CTA's barrier returns false at once and
+// the CTAs leave the kernel.
+struct GridBar {
+  unsigned int count;
+  unsigned int gen;
+  int abort;
+};
+constexpr long long kGridBarCycles = 4000000000LL;   // ~2 s at 2 GHz, far above a barrier
+
+__device__ bool grid_sync_bounded(GridBar* bar, unsigned nblocks, int* err) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* vgen = &bar->gen;
+    volatile int* vab = &bar->abort;
+    int ok = *vab == 0;
+    if (ok) {
+      const unsigned g = *vgen;
+      __threadfence();
+      if (atomicAdd(&bar->count, 1u) == nblocks - 1) {
+        atomicExch(&bar->count, 0u);
+        __threadfence();
+        atomicAdd(&bar->gen, 1u);
+      } else {
+        const long long t0 = clock64();
+        while (*vgen == g) {
+          if (*vab) { ok = 0; break; }
+          if (clock64() - t0 > kGridBarCycles) {
+            atomicExch(&bar->abort, 1);
+            atomicMax(err, (int)kDevTimeout);
+            ok = 0;
+            break;
+          }
+        }
+      }
+      __threadfence();
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
 // Householder QR of the panel M(p:m, p:p+w) in place (LAPACK xGEQR2 layout:
 // reflector tails below the diagonal, R on and above), plus the forward
-// column-wise WY factor T (xLARFT) of the panel.
+// column-wise WY factor T (xLARFT) of the panel, for every wide box of a
+// level at once: one cooperative launch, the rows of each box's panel split
+// over consecutive CTAs (`rows` rows each, chunk 0 from row p).  Per
+// reflector j: each CTA forms its rows' share of ||column j below the
+// diagonal||^2; after a grid barrier every CTA of the box sums the shares in
+// chunk order (the same value everywhere), forms beta, tau and v, and its
+// share of v^T against the panel's other columns; after a second barrier it
+// sums those, updates its rows, and chunk 0 (which holds rows p .. p+31)
+// updates row j and the WY factor.  Values written by other CTAs are read
+// past L1 (__ldcg).
+constexpr int kPanelRed = 40;   // per-CTA stride of the partial sums: 1 norm + 32 products
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_qr_panel(const WideTask* tasks, T* wpool, int p) {
-  const WideTask t = tasks[blockIdx.x];
-  if (p >= t.n) return;
-  const int m = t.m, w = min(kQrNb, t.n - p);
+__global__ void __launch_bounds__(256) k_qr_panel_coop(const WideTask* tasks, int ntask, T* wpool,
+                                                      int p, int rows, T* red, GridBar* bar,
+                                                      int* err) {
+  int box = 0, first = 0, cnt = 0;
+  for (int acc = 0; box < ntask; box++) {
+    const WideTask& tb = tasks[box];
+    cnt = p < min(tb.n, tb.m) ? (tb.m - p + rows - 1) / rows : 0;
+    if ((int)blockIdx.x < acc + cnt) {
+      first = acc;
+      break;
+    }
+    acc += cnt;
+  }
+  // (the grid is the sum of the counts, so every CTA has a box; one without
+  // would take part in the barriers only)
+  WideTask t{};
+  if (box < ntask) t = tasks[box];
+  const int m = t.m, n = t.n, w = box < ntask ? min(kQrNb, min(n, m) - p) : 0;
+  const int chunk = blockIdx.x - first;
+  const int r0 = p + chunk * rows, r1 = min(m, r0 + rows);
   T* A = wpool + t.M;
   T* Tf = wpool + t.Tf;
-  __shared__ T red[8 * kQrNb];
+  T* my = red + (size_t)blockIdx.x * kPanelRed;
+  const T* box_red = red + (size_t)first * kPanelRed;
+  __shared__ T sred[8 * kQrNb];
   __shared__ T s_sum[kQrNb];
+  __shared__ T s_row[kQrNb];   // row j of the panel (read before anyone updates it)
   __shared__ T s_w[kQrNb];
   __shared__ T s_tau, s_beta, s_scale;
+  const int nwarp = blockDim.x >> 5;
   T vals[kQrNb];
-  for (int jj = 0; jj < w; jj++) {
+  for (int jj = 0; jj < kQrNb; jj++) {
+    const bool live = jj < w;
     const int j = p + jj;
-    // reflector of column j
-    T sg = T(0);
-    for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) sg += A[i + (size_t)m * j] * A[i + (size_t)m * j];
-    T s1 = warp_sum(sg);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s1;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      T sigma = T(0);
-      for (int q = 0; q < (int)(blockDim.x >> 5); q++) sigma += red[q];
-      T alpha = A[j + (size_t)m * j];
-      T tau = T(0), beta = alpha, scale = T(0);
-      if (sigma != T(0)) {
-        T nrm = sqrt(alpha * alpha + sigma);
-        beta = alpha >= T(0) ? -nrm : nrm;
-        tau = (beta - alpha) / beta;
-        scale = T(1) / (alpha - beta);
+    const int i0 = max(r0, j + 1);   // this CTA's rows below the diagonal
+    // (A) this CTA's share of the column's squared norm below the diagonal
+    if (live) {
+      T sq = T(0);
+      for (int i = i0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const T x = A[i + (size_t)m * j];
+        sq += x * x;
       }
-      s_tau = tau; s_beta = beta; s_scale = scale;
+      sq = warp_sum(sq);
+      if ((threadIdx.x & 31) == 0) sred[threadIdx.x >> 5] = sq;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        T s2 = T(0);
+        for (int q = 0; q < nwarp; q++) s2 += sred[q];
+        my[0] = s2;
+      }
     }
-    __syncthreads();
-    const T tau = s_tau, scale = s_scale;
-    // one pass over the rows (v = scaled column j): z_l = V(:,l)^T v (WY
-    // factor, l < jj) and d_c = c^T v for the remaining panel columns
-    const int nz = jj, nd = w - jj - 1;
+    if (!grid_sync_bounded(bar, gridDim.x, err)) return;
+    // (B) beta, tau, v on this CTA's rows, and its share of v^T (panel columns)
+    if (live) {
+      if (threadIdx.x < w) s_row[threadIdx.x] = __ldcg(A + j + (size_t)m * (p + threadIdx.x));
+      if (threadIdx.x == 0) {
+        T sigma = T(0);
+        for (int c = 0; c < cnt; c++) sigma += __ldcg(box_red + (size_t)c * kPanelRed);
+        const T alpha = __ldcg(A + j + (size_t)m * j);
+        T tau = T(0), beta = alpha, scale = T(0);
+        if (sigma != T(0)) {
+          const T nrm = sqrt(alpha * alpha + sigma);
+          beta = alpha >= T(0) ? -nrm : nrm;
+          tau = (beta - alpha) / beta;
+          scale = T(1) / (alpha - beta);
+        }
+        s_tau = tau;
+        s_beta = beta;
+        s_scale = scale;
+      }
+      __syncthreads();
+      const T scale = s_scale;
+      // products: z_l = V(:, l)^T v for the earlier reflectors (l < jj),
+      // d = c^T v for the later panel columns, packed as q < jj then q - jj
+      const int nz = jj, nd = w - jj - 1;
 #pragma unroll
-    for (int q = 0; q < kQrNb; q++) vals[q] = T(0);
-    for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
-      T v = A[i + (size_t)m * j] * scale;
-      A[i + (size_t)m * j] = v;
+      for (int q = 0; q < kQrNb; q++) vals[q] = T(0);
+      for (int i = i0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const T v = A[i + (size_t)m * j] * scale;
+        A[i + (size_t)m * j] = v;
 #pragma unroll
-      for (int q = 0; q < kQrNb; q++) {
-        int col = q < nz ? p + q : j + 1 + (q - nz);
-        if (q < nz + nd) vals[q] += A[i + (size_t)m * col] * v;
+        for (int q = 0; q < kQrNb; q++) {
+          const int col = q < nz ? p + q : j + 1 + (q - nz);
+          if (q < nz + nd) vals[q] += A[i + (size_t)m * col] * v;
+        }
       }
+      block_sum_vec<T>(vals, sred, s_sum);
+      if (threadIdx.x < kQrNb) my[1 + threadIdx.x] = s_sum[threadIdx.x];
     }
-    block_sum_vec<T>(vals, red, s_sum);
-    if (threadIdx.x < nd) s_w[threadIdx.x] = (A[j + (size_t)m * (j + 1 + threadIdx.x)] + s_sum[nz + threadIdx.x]) * tau;
-    __syncthreads();
-    // remaining panel columns: c -= w_c v, all columns in one pass
-    for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
-      T v = A[i + (size_t)m * j];
-      for (int q = 0; q < nd; q++) A[i + (size_t)m * (j + 1 + q)] -= s_w[q] * v;
-    }
-    if (threadIdx.x < nd) A[j + (size_t)m * (j + 1 + threadIdx.x)] -= s_w[threadIdx.x];
-    if (threadIdx.x == 32) A[j + (size_t)m * j] = s_beta;
-    // WY factor column jj: T(0:jj, jj) = -tau T(0:jj,0:jj) z, z_l += V(j, l)
-    if (threadIdx.x == 64) {
-      T z[kQrNb];
-      for (int l = 0; l < nz; l++) z[l] = s_sum[l] + A[j + (size_t)m * (p + l)];
-      for (int l = 0; l < nz; l++) {
-        T acc = T(0);
-        for (int q = l; q < nz; q++) acc += Tf[l + kQrNb * q] * z[q];
-        Tf[l + kQrNb * jj] = -tau * acc;
+    if (!grid_sync_bounded(bar, gridDim.x, err)) return;
+    // (C) the box's sums, this CTA's rows of the later panel columns, and
+    // (chunk 0) row j and the WY factor's column jj
+    if (live) {
+      const T tau = s_tau;
+      const int nz = jj, nd = w - jj - 1;
+      if (threadIdx.x < kQrNb) {
+        T tot = T(0);
+        for (int c = 0; c < cnt; c++) tot += __ldcg(box_red + (size_t)c * kPanelRed + 1 + threadIdx.x);
+        s_sum[threadIdx.x] = tot;
       }
-      Tf[jj + kQrNb * jj] = tau;
+      __syncthreads();
+      if (threadIdx.x < nd) s_w[threadIdx.x] = (s_row[jj + 1 + threadIdx.x] + s_sum[nz + threadIdx.x]) * tau;
+      __syncthreads();
+      for (int i = i0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const T v = A[i + (size_t)m * j];
+        for (int q = 0; q < nd; q++) A[i + (size_t)m * (j + 1 + q)] -= s_w[q] * v;
+      }
+      if (chunk == 0) {
+        if (threadIdx.x < nd) A[j + (size_t)m * (j + 1 + threadIdx.x)] = s_row[jj + 1 + threadIdx.x] - s_w[threadIdx.x];
+        if (threadIdx.x == 32) A[j + (size_t)m * j] = s_beta;
+        if (threadIdx.x == 64) {
+          // T(0:jj, jj) = -tau T(0:jj, 0:jj) z, z_l = V(j, l) + V(j+1:, l)^T v
+          T z[kQrNb];
+          for (int l = 0; l < nz; l++) z[l] = s_sum[l] + s_row[l];
+          for (int l = 0; l < nz; l++) {
+            T acc = T(0);
+            for (int q = l; q < nz; q++) acc += Tf[l + kQrNb * q] * z[q];
+            Tf[l + kQrNb * jj] = -tau * acc;
+          }
+          Tf[jj + kQrNb * jj] = tau;
+        }
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 
@@ -1690,8 +1802,8 @@ __global__ void __launch_bounds__(128) k_qr_wpart(const WideTask* tasks, const T
                                                   int p) {
   const WideTask t = tasks[blockIdx.x];
   const int m = t.m, n = t.n;
-  if (p >= n) return;
-  const int w = min(kQrNb, n - p);
+  if (p >= min(n, m)) return;
+  const int w = min(kQrNb, min(n, m) - p);   // reflectors of the panel (rows below p permitting)
   const int c0 = p + w + blockIdx.y * kQrWCols;
   const int r0 = p + blockIdx.z * kQrChunk;
   if (c0 >= n || r0 >= m) return;
@@ -1746,8 +1858,8 @@ __global__ void __launch_bounds__(kQrWCols) k_qr_wsum(const WideTask* tasks, con
                                                       int p) {
   const WideTask t = tasks[blockIdx.x];
   const int m = t.m, n = t.n;
-  if (p >= n) return;
-  const int w = min(kQrNb, n - p);
+  if (p >= min(n, m)) return;
+  const int w = min(kQrNb, min(n, m) - p);   // reflectors of the panel (rows below p permitting)
   const int c = p + w + blockIdx.y * kQrWCols + threadIdx.x;
   if (c >= n) return;
   const int chunks = (m - p + kQrChunk - 1) / kQrChunk;
@@ -1780,8 +1892,8 @@ template <typename T>
 __global__ void __launch_bounds__(128) k_qr_apply(const WideTask* tasks, T* wpool, const T* parts, int p) {
   const WideTask t = tasks[blockIdx.x];
   const int m = t.m, n = t.n;
-  if (p >= n) return;
-  const int w = min(kQrNb, n - p);
+  if (p >= min(n, m)) return;
+  const int w = min(kQrNb, min(n, m) - p);   // reflectors of the panel (rows below p permitting)
   const int rt = p + blockIdx.y * kQrTileRows, ct = p + w + blockIdx.z * kQrTileCols;
   if (rt >= m || ct >= n) return;
   const int nr = min(kQrTileRows, m - rt), nc = min(kQrTileCols, n - ct);
@@ -1823,6 +1935,247 @@ __global__ void __launch_bounds__(128) k_qr_apply(const WideTask* tasks, T* wpoo
 #pragma unroll
     for (int a = 0; a < 4; a++)
       if (r4 + a < nr) col[r4 + a] -= acc[a][b];
+  }
+}
+
+// Column-pivoted QR of wide boxes' triangles (or formed sketches) over many
+// CTAs per box: the rank decision, permutation, T = R11^-1 R12 and permuted
+// active list k_id writes with flags 4, for boxes too large for one CTA to
+// pivot quickly.  R (rows x n, row-major, ld n) sits in the task's scratch,
+// T is written after it.  One cooperative launch for all such boxes of a
+// level; each CTA owns kCpqrCols consecutive columns of its box, one thread
+// per column.  Columns do not move: pivoting marks a column done and
+// records it as the next logical position.  Per step j: each CTA's largest
+// partial norm among its active columns (the first column on ties); after a
+// grid barrier every CTA of the box picks the box's pivot from those in CTA
+// order, and the pivot's owner forms the reflector of its column below row j
+// (xLARFG) into the box's shared vector; after a second barrier every CTA
+// checks the rank rule (|R_jj| < tol |R_00| at j >= 1 stops, before the
+// reflector is applied) and applies the reflector to its active columns with
+// xLAQP2's norm downdating.  The remaining columns follow the pivots in
+// column order.  Boxes that stopped wait in the barriers; when every box has
+// stopped all CTAs leave the loop together.  Values other CTAs wrote are
+// read past L1.
+constexpr int kCpqrCols = 64;
+// Wide boxes of at least this many columns take the cooperative pivoted QR.
+constexpr int kCoopCpqrMinN = 384;
+
+struct CpqrTask {
+  int task;          // the level's IdTask index (rank out)
+  int n, rows;       // columns; rows of R (n for a triangle, l for a sketch)
+  int jmax;          // pivot steps available: min(n, m, rows)
+  int sketch;        // R is a sketch with fewer rows than columns (rank guard)
+  int first, ctas;   // the box's CTAs in the grid
+  int64_t R;         // scratch offset of R; T at R + n n
+  int64_t perm, pact, act;   // iscratch / ipool offsets
+  int64_t v;         // offset in the launch's vector pool: rows + 2 values
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kCpqrCols) k_cpqr_coop(const CpqrTask* tasks, int ntask, T* tws,
+                                                         int* iscratch, int* ipool, T* vpool,
+                                                         long long* ckey,
+                                                         int* ccol, int* boxes_done, double tol,
+                                                         int* k_out, GridBar* bar, int* err) {
+  extern __shared__ __align__(16) unsigned char cc_smem[];
+  int b = 0;
+  while (b < ntask && (int)blockIdx.x >= tasks[b].first + tasks[b].ctas) b++;
+  CpqrTask t{};
+  if (b < ntask) t = tasks[b];
+  const int n = t.n, rows = t.rows;
+  const int cta = blockIdx.x - t.first;
+  const int c = cta * kCpqrCols + threadIdx.x;
+  const bool mine = b < ntask && c < n;
+  T* R = tws + t.R;
+  T* vb = vpool + t.v;
+  int* perm = iscratch + t.perm;
+  T* vs = reinterpret_cast<T*>(cc_smem);   // the reflector, rows values
+  __shared__ long long s_key[kCpqrCols / 32];
+  __shared__ int s_col[kCpqrCols / 32];
+  __shared__ int s_p, s_stop;
+  __shared__ T s_red[kCpqrCols / 32];
+  __shared__ T s_beta, s_tau;
+  // partial norms of my column (the triangle is zero below the diagonal)
+  T vn1 = T(0), vn2 = T(0);
+  bool active = mine;
+  if (mine) {
+    const int ilast = t.sketch ? rows - 1 : min(c, rows - 1);
+    T s2 = T(0);
+    for (int i = 0; i <= ilast; i++) s2 += R[(size_t)i * n + c] * R[(size_t)i * n + c];
+    vn1 = sqrt(s2);
+    vn2 = vn1;
+  }
+  T thresh = T(0);
+  int k = 0;
+  bool stopped = b >= ntask;   // a CTA without a box only joins the barriers
+  int jmax_all = 0;
+  for (int q = 0; q < ntask; q++) jmax_all = max(jmax_all, tasks[q].jmax);
+  for (int j = 0; j < jmax_all; j++) {
+    // (A) this CTA's candidate
+    if (!stopped) {
+      long long key = active ? norm_key(vn1) : -1;
+      int col = c;
+      for (int o = 16; o > 0; o >>= 1) {
+        const long long ok = __shfl_down_sync(0xffffffffu, key, o);
+        const int oc = __shfl_down_sync(0xffffffffu, col, o);
+        if (ok > key || (ok == key && oc < col)) { key = ok; col = oc; }
+      }
+      if ((threadIdx.x & 31) == 0) {
+        s_key[threadIdx.x >> 5] = key;
+        s_col[threadIdx.x >> 5] = col;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        long long bk = s_key[0];
+        int bc = s_col[0];
+        for (int w = 1; w < kCpqrCols / 32; w++)
+          if (s_key[w] > bk || (s_key[w] == bk && s_col[w] < bc)) { bk = s_key[w]; bc = s_col[w]; }
+        ckey[blockIdx.x] = bk;
+        ccol[blockIdx.x] = bc;
+      }
+    }
+    if (!grid_sync_bounded(bar, gridDim.x, err)) return;
+    if (__ldcg(boxes_done) == ntask) break;   // every box has stopped (uniform)
+    // (B) the box's pivot; its owner forms the reflector
+    if (!stopped) {
+      if (threadIdx.x == 0) {
+        long long bk = -2;
+        int bc = n;
+        for (int q = 0; q < t.ctas; q++) {
+          const long long kq = __ldcg(ckey + t.first + q);
+          const int cq = __ldcg(ccol + t.first + q);
+          if (kq > bk || (kq == bk && cq < bc)) { bk = kq; bc = cq; }
+        }
+        s_p = bc;
+      }
+      __syncthreads();
+      const int p = s_p;
+      if (p / kCpqrCols == cta) {
+        T sg = T(0);
+        for (int i = j + 1 + threadIdx.x; i < rows; i += blockDim.x) sg += R[(size_t)i * n + p] * R[(size_t)i * n + p];
+        sg = warp_sum(sg);
+        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = sg;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          T sigma = T(0);
+          for (int w = 0; w < kCpqrCols / 32; w++) sigma += s_red[w];
+          const T alpha = R[(size_t)j * n + p];
+          T tau = T(0), beta = alpha, scale = T(0);
+          if (sigma != T(0)) {
+            const T nrm = sqrt(alpha * alpha + sigma);
+            beta = alpha >= T(0) ? -nrm : nrm;
+            tau = (beta - alpha) / beta;
+            scale = T(1) / (alpha - beta);
+          }
+          vb[rows] = beta;
+          vb[rows + 1] = tau;
+          s_tau = scale;   // the owner's scale, below
+          perm[j] = p;
+        }
+        __syncthreads();
+        const T scale = s_tau;
+        for (int i = j + 1 + threadIdx.x; i < rows; i += blockDim.x) vb[i] = R[(size_t)i * n + p] * scale;
+        if (c == p) active = false;
+      }
+    }
+    if (!grid_sync_bounded(bar, gridDim.x, err)) return;
+    // (C) rank rule, then the reflector on this CTA's active columns
+    if (!stopped) {
+      if (threadIdx.x == 0) {
+        s_beta = __ldcg(vb + rows);
+        s_tau = __ldcg(vb + rows + 1);
+      }
+      __syncthreads();
+      const T beta = s_beta, tau = s_tau;
+      if (j == 0) thresh = fabs(T(tol) * beta);
+      if (j >= 1 && fabs(beta) < thresh) {
+        k = j;
+        stopped = true;
+        if (cta == 0 && threadIdx.x == 0) atomicAdd(boxes_done, 1);
+      } else {
+        const int p = s_p;
+        if (c == p) R[(size_t)j * n + p] = beta;
+        for (int i = j + 1 + threadIdx.x; i < rows; i += blockDim.x) vs[i] = __ldcg(vb + i);
+        __syncthreads();
+        if (active && tau != T(0)) {
+          T w0 = R[(size_t)j * n + c], w1 = T(0);
+          int i = j + 1;
+          for (; i + 1 < rows; i += 2) {
+            w0 += vs[i] * R[(size_t)i * n + c];
+            w1 += vs[i + 1] * R[(size_t)(i + 1) * n + c];
+          }
+          for (; i < rows; i++) w0 += vs[i] * R[(size_t)i * n + c];
+          const T w = (w0 + w1) * tau;
+          R[(size_t)j * n + c] -= w;
+          for (int q = j + 1; q < rows; q++) R[(size_t)q * n + c] -= w * vs[q];
+        }
+        if (active) {
+          const T rjc = R[(size_t)j * n + c];
+          if (vn1 != T(0)) {
+            T temp = fabs(rjc) / vn1;
+            temp = T(1) - temp * temp;
+            temp = temp < T(0) ? T(0) : temp;
+            const T qq = vn1 / vn2;
+            if (temp * qq * qq <= tol3z<T>()) {
+              T s2 = T(0);
+              for (int q = j + 1; q < rows; q++) s2 += R[(size_t)q * n + c] * R[(size_t)q * n + c];
+              vn1 = sqrt(s2);
+              vn2 = vn1;
+            } else {
+              vn1 = vn1 * sqrt(temp);
+            }
+          }
+        }
+        if (j == t.jmax - 1) {   // pivots exhausted without the rule firing
+          stopped = true;
+          if (cta == 0 && threadIdx.x == 0) atomicAdd(boxes_done, 1);
+        }
+      }
+    }
+  }
+  // k = 0: the rule never fired (no compression); a sketch must reveal the
+  // rank with kSketchGuard rows to spare
+  const bool fallback =
+      b < ntask && t.sketch && rows < n && (k == 0 ? t.jmax == rows : k > rows - kSketchGuard);
+  const bool need = b < ntask && !fallback && k > 0;
+  if (b < ntask && cta == 0 && threadIdx.x == 0) k_out[t.task] = fallback ? -1 : k;
+  // the redundant columns, in column order, after the k skeleton columns
+  // perm[0 .. k) (the pivot of step k, chosen before the rule fired, is
+  // redundant): the box's first CTA marks those in shared memory and one
+  // thread lists the rest (~n steps)
+  if (need && cta == 0) {
+    unsigned char* skel = cc_smem;   // n bytes
+    for (int q = threadIdx.x; q < n; q += blockDim.x) skel[q] = 0;
+    __syncthreads();
+    for (int a = threadIdx.x; a < k; a += blockDim.x) skel[__ldcg(perm + a)] = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int pos = k;
+      for (int q = 0; q < n; q++)
+        if (!skel[q]) perm[pos++] = q;
+    }
+  }
+  // every CTA (of every box, and the ones without a box) passes this barrier
+  // once: the box's CTAs then read the tail of perm
+  if (!grid_sync_bounded(bar, gridDim.x, err)) return;
+  if (!need) return;
+  int* sp = reinterpret_cast<int*>(cc_smem);   // perm, n ints
+  for (int e = threadIdx.x; e < n; e += blockDim.x) sp[e] = __ldcg(perm + e);
+  __syncthreads();
+  const int r = n - k;
+  T* Tout = R + (size_t)n * n;
+  const int* act = ipool + t.act;
+  int* pact = ipool + t.pact;
+  for (int e = cta * kCpqrCols + threadIdx.x; e < n; e += t.ctas * kCpqrCols) pact[e] = act[sp[e]];
+  // T = R11^-1 R12: one redundant column per thread, back substitution with
+  // the pivot columns' upper triangle
+  for (int cr = cta * kCpqrCols + threadIdx.x; cr < r; cr += t.ctas * kCpqrCols) {
+    const int pc = sp[k + cr];
+    for (int a = k - 1; a >= 0; a--) {
+      T s = __ldcg(R + (size_t)a * n + pc);
+      for (int l = a + 1; l < k; l++) s -= __ldcg(R + (size_t)a * n + sp[l]) * Tout[l + (size_t)k * cr];
+      Tout[a + (size_t)k * cr] = s / __ldcg(R + (size_t)a * n + sp[a]);
+    }
   }
 }
 
@@ -3920,9 +4273,53 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
             ki::launch(k_wide_assemble<T>, dim3((unsigned)wt.size(), (maxn + 7) / 8), 256, 0, ws3,
                 d_wt, d_wpool, ipool, d_irows, P, sd, ptab);
             const unsigned nb_w = (unsigned)wt.size();
+            // the panels: cooperative launches, `prow` rows per CTA (one box's
+            // rows always fit the resident CTAs), over batches of consecutive
+            // boxes whose CTAs at the first panel fit them
+            int per_sm_coop = 0;
+            KI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_coop, k_qr_panel_coop<T>, 256, 0));
+            static const int n_sm_coop = device_sm_count();
+            const int resident = std::max(1, per_sm_coop) * n_sm_coop;
+            const int prow = std::max(512, ((max_m + resident - 1) / resident + 31) & ~31);
+            auto box_ctas = [&](const WideTask& w, int p0) {
+              return p0 < std::min(w.n, w.m) ? (w.m - p0 + prow - 1) / prow : 0;
+            };
+            std::vector<std::pair<int, int>> batches;   // [first box, end)
+            int batch_max = 0;
+            for (int b0 = 0; b0 < (int)wt.size();) {
+              int b1 = b0, c = 0;
+              while (b1 < (int)wt.size() && (b1 == b0 || c + box_ctas(wt[b1], 0) <= resident)) {
+                c += box_ctas(wt[b1], 0);
+                b1++;
+              }
+              batches.push_back({b0, b1});
+              batch_max = std::max(batch_max, c);
+              b0 = b1;
+            }
+            T* d_pred = nullptr;
+            GridBar* d_bar = nullptr;
+            KI_CUDA(pool_malloc((void**)&d_pred, sizeof(T) * (size_t)kPanelRed * (batch_max + 1), ws3));
+            KI_CUDA(pool_malloc((void**)&d_bar, sizeof(GridBar), ws3));
+            KI_CUDA(cudaMemsetAsync(d_bar, 0, sizeof(GridBar), ws3));
             for (int p0 = 0; p0 < maxn; p0 += kQrNb) {
-              ki::launch(k_qr_panel<T>, nb_w, 256, 0, ws3, d_wt, d_wpool, p0);
-              const int trail = maxn - p0 - kQrNb;   // trailing columns of the widest box
+              for (const auto& bt : batches) {
+                int g = 0;
+                for (int q = bt.first; q < bt.second; q++) g += box_ctas(wt[q], p0);
+                // no box of the batch with rows left below p0: nothing to reflect
+                if (g == 0) continue;
+                const WideTask* a_t = d_wt + bt.first;
+                T* a_pool = d_wpool;
+                int a_p = p0, a_rows = prow, a_n = bt.second - bt.first;
+                int* a_err = F->d_err;
+                void* args[] = {(void*)&a_t, (void*)&a_n, (void*)&a_pool, (void*)&a_p, (void*)&a_rows,
+                                (void*)&d_pred, (void*)&d_bar, (void*)&a_err};
+                ki::launch_counter().fetch_add(1, std::memory_order_relaxed);
+                KI_CUDA(cudaLaunchCooperativeKernel((const void*)k_qr_panel_coop<T>, dim3((unsigned)g),
+                                                    dim3(256), args, 0, ws3));
+              }
+              // trailing columns of the widest box (a box with fewer rows than
+              // columns has fewer reflectors in its last panel: one more block)
+              const int trail = maxn - p0 - 1;
               if (trail <= 0) continue;
               const unsigned cblk = (unsigned)((trail + kQrWCols - 1) / kQrWCols);
               const unsigned chunks = (unsigned)((max_m - p0 + kQrChunk - 1) / kQrChunk);
@@ -3935,6 +4332,8 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
                          128, 0, ws3, (const WideTask*)d_wt, d_wpool, (const T*)d_qparts, p0);
             }
             KI_CUDA(cudaFreeAsync(d_qparts, ws3));
+            KI_CUDA(cudaFreeAsync(d_pred, ws3));
+            KI_CUDA(cudaFreeAsync(d_bar, ws3));
             ki::launch(k_wide_triangle<T>, (unsigned)wt.size(), 256, 0, ws3, d_wt, d_wpool, d_tws);
             KI_CUDA(cudaGetLastError());
           }
@@ -3956,6 +4355,103 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
           F->stage_end(ws3);
           std::string wc = "wide_cpqr@L" + std::to_string(l);
           F->stage_begin(wc.c_str(), 0, 0, ws3);
+          // the largest boxes' pivoted QRs over many CTAs each (k_cpqr_coop),
+          // in cooperative launches of at most the resident CTAs, on ws3;
+          // they leave the per-box k_id bins while those launch (group 5,
+          // never launched; they are the last of their groups, which are
+          // sorted by n), and get their group back afterwards
+          std::vector<std::pair<int, int>> big_grp;
+          {
+            // (environment override KI_COOP_CPQR_MIN_N, used by the tests to
+            // drive every wide box through it)
+            int coop_min = kCoopCpqrMinN;
+            if (const char* e = std::getenv("KI_COOP_CPQR_MIN_N")) coop_min = std::atoi(e);
+            std::vector<int> big;
+            for (size_t i = 0; i < itasks.size(); i++)
+              if (is_wide(grp[i]) && itasks[i].n >= coop_min) big.push_back((int)i);
+            if (!big.empty()) {
+              const bool any_sk = sketching;
+              size_t sm_max = 0;
+              std::vector<CpqrTask> ct;
+              int64_t vtot = 0;
+              for (int i : big) {
+                CpqrTask c{};
+                c.task = i;
+                c.n = itasks[i].n;
+                const bool sk = any_sk && lh[i] > 0 && lh[i] <= itasks[i].n && lh[i] <= 384;
+                c.rows = sk ? lh[i] : itasks[i].n;
+                c.sketch = sk && lh[i] < itasks[i].n;
+                c.jmax = std::min(std::min(c.n, mh[i]), c.rows);
+                c.R = itasks[i].ws;
+                c.perm = itasks[i].perm;
+                c.pact = itasks[i].pact;
+                c.act = itasks[i].act;
+                c.ctas = (c.n + kCpqrCols - 1) / kCpqrCols;
+                c.v = vtot;
+                vtot += c.rows + 2;
+                sm_max = std::max(sm_max, std::max(sizeof(T) * (size_t)c.rows, sizeof(int) * (size_t)c.n));
+                ct.push_back(c);
+                big_grp.push_back({i, grp[i]});
+                grp[i] = 5;
+              }
+              if (sm_max > 48 * 1024)
+                KI_CUDA(cudaFuncSetAttribute(k_cpqr_coop<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sm_max));
+              int per_sm = 0;
+              KI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cpqr_coop<T>, kCpqrCols, sm_max));
+              static const int n_sm_cp = device_sm_count();
+              const int resident = std::max(1, per_sm) * n_sm_cp;
+              T* d_cv = nullptr;
+              long long* d_ckey = nullptr;
+              int* d_ccol = nullptr;
+              int* d_cdone = nullptr;
+              GridBar* d_cbar = nullptr;
+              int total_ctas = 0;
+              for (const auto& c : ct) total_ctas += c.ctas;
+              KI_CUDA(pool_malloc((void**)&d_cv, sizeof(T) * (size_t)(vtot + 1), ws3));
+              KI_CUDA(pool_malloc((void**)&d_ckey, sizeof(long long) * (size_t)total_ctas, ws3));
+              KI_CUDA(pool_malloc((void**)&d_ccol, sizeof(int) * (size_t)total_ctas, ws3));
+              KI_CUDA(pool_malloc((void**)&d_cdone, sizeof(int) + sizeof(GridBar) + 16, ws3));
+              d_cbar = reinterpret_cast<GridBar*>(d_cdone + 4);
+              // launches of consecutive boxes up to the resident CTAs each
+              for (size_t g0 = 0; g0 < ct.size();) {
+                size_t g1 = g0;
+                int ctas = 0;
+                while (g1 < ct.size() && (g1 == g0 || ctas + ct[g1].ctas <= resident)) {
+                  ct[g1].first = ctas;
+                  ctas += ct[g1].ctas;
+                  g1++;
+                }
+                if (ctas > resident)
+                  throw std::runtime_error("a box too large for the cooperative pivoted QR");
+                std::vector<CpqrTask> part(ct.begin() + g0, ct.begin() + g1);
+                CpqrTask* d_ct = nullptr;
+                KI_CUDA(pool_malloc((void**)&d_ct, sizeof(CpqrTask) * part.size(), ws3));
+                upload(d_ct, part, ws3);
+                KI_CUDA(cudaMemsetAsync(d_cdone, 0, sizeof(int) + sizeof(GridBar) + 16, ws3));
+                const CpqrTask* a_ct = d_ct;
+                int a_nt = (int)part.size();
+                T* a_tws = d_tws;
+                int* a_irows = d_irows;
+                int* a_ipool = ipool;
+                double a_tol = prm.id_tol;
+                int* a_k = d_k;
+                int* a_err = F->d_err;
+                void* args[] = {(void*)&a_ct, (void*)&a_nt, (void*)&a_tws, (void*)&a_irows, (void*)&a_ipool,
+                                (void*)&d_cv, (void*)&d_ckey, (void*)&d_ccol, (void*)&d_cdone,
+                                (void*)&a_tol, (void*)&a_k, (void*)&d_cbar, (void*)&a_err};
+                ki::launch_counter().fetch_add(1, std::memory_order_relaxed);
+                KI_CUDA(cudaLaunchCooperativeKernel((const void*)k_cpqr_coop<T>, dim3(ctas), dim3(kCpqrCols),
+                                                    args, sm_max, ws3));
+                KI_CUDA(cudaFreeAsync(d_ct, ws3));
+                g0 = g1;
+              }
+              KI_CUDA(cudaFreeAsync(d_cv, ws3));
+              KI_CUDA(cudaFreeAsync(d_ckey, ws3));
+              KI_CUDA(cudaFreeAsync(d_ccol, ws3));
+              KI_CUDA(cudaFreeAsync(d_cdone, ws3));
+            }
+          }
           // the pivoted QRs of the wide boxes' sketches / triangles, bins spread
           // over every aux stream (after the sketches on ws3; the upper levels
           // have no narrow boxes to share them with), joined back into ws3
@@ -3966,6 +4462,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
           n_streams = Factorization<T>::kAux;
           launch_range(2, 4, nullptr);
           launch_range(3, 4, nullptr);
+          for (const auto& bg : big_grp) grp[bg.first] = bg.second;
           n_streams = Factorization<T>::kAux - 1;
           for (int i = 0; i + 1 < Factorization<T>::kAux; i++) {
             KI_CUDA(cudaEventRecord(wev[i + 1], F->aux[i]));

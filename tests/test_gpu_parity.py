@@ -127,18 +127,21 @@ def test_gpu_matches_oracle_disc64_262k_32rhs(pkg, oracle_mod):
     assert np.abs(al2 - al_ref9).max() <= 10 * tol * np.abs(mu_ref9).max()
 
 
-@pytest.mark.parametrize("wide_rows,schur_cap,full_cap,schur_wide_n",
-                         [("0", "0", "230400", "0"), ("400", "225000", "230400", "288"),
-                          ("100000", "0", "0", "100000")])
+@pytest.mark.parametrize("wide_rows,schur_cap,full_cap,schur_wide_n,coop_min",
+                         [("0", "0", "230400", "0", "384"), ("400", "225000", "230400", "288", "384"),
+                          ("100000", "0", "0", "100000", "384"), ("0", "225000", "230400", "288", "0")])
 def test_gpu_wide_path_matches_oracle(pkg, oracle_mod, monkeypatch, wide_rows, schur_cap,
-                                      full_cap, schur_wide_n):
+                                      full_cap, schur_wide_n, coop_min):
     """Boxes with tall ID matrices go through the explicit-matrix blocked QR
-    and large boxes through the multi-CTA Schur elimination; forcing the
-    thresholds down drives (nearly) every box through them."""
+    (cooperative panels, tiled trailing updates) and large boxes through the
+    multi-CTA Schur elimination; forcing the thresholds down drives (nearly)
+    every box through them, and (coop_min 0) every wide box's pivoted QR
+    through the cooperative multi-CTA kernel."""
     monkeypatch.setenv("KI_WIDE_ROWS", wide_rows)
     monkeypatch.setenv("KI_SCHUR_SMEM_CAP", schur_cap)
     monkeypatch.setenv("KI_ID_FULL_CAP", full_cap)            # 0: packed triangles
     monkeypatch.setenv("KI_SCHUR_WIDE_N", schur_wide_n)       # 0: device-wide Schur
+    monkeypatch.setenv("KI_COOP_CPQR_MIN_N", coop_min)
     g = pkg.geometry
     prob = g.disc_with_ellipses(1 << 13, 6, seed=5)
     f = g.laplace_source_rhs(prob, np.array([[3.0, 1.0]]))
@@ -341,3 +344,25 @@ def test_gpu_3d_ellipsoid_against_oracle_and_field(pkg, oracle_mod, sd, n, leaf)
     err = np.abs(fac.eval_targets(tg, mu) - ue).max()
     err_ref = np.abs(fac.eval_targets(tg, ref) - ue).max()
     assert err <= 1.5 * err_ref + 10 * tol * np.abs(ue).max(), (err, err_ref)
+
+
+def test_gpu_wide_path_many_boxes_matches_oracle(pkg, oracle_mod, monkeypatch):
+    """Every box through the wide path on a tree with more wide boxes per
+    level than the GPU holds resident CTAs: the cooperative panel QR then
+    runs in several launches per panel (batches of boxes)."""
+    monkeypatch.setenv("KI_WIDE_ROWS", "0")
+    g = pkg.geometry
+    prob = g.disc_with_ellipses(1 << 16, 16, seed=5)
+    f = g.laplace_source_rhs(prob, np.array([[3.0, 1.0]]))
+    tol = 1e-8
+    ref, al_ref, st = oracle_mod.solve(prob, f, tol, threads=16)
+    fac = pkg.Factor(prob.points, prob.normals, prob.weights, prob.curvatures, id_tol=tol,
+                     hole_centers=prob.hole_centers, hole_start=prob.hole_start,
+                     hole_count=prob.hole_count)
+    mu, al = fac.solve(f)
+    paths = [lv["paths"] for lv in fac.profile()["levels"]]
+    info = fac.info()
+    fac.close()
+    assert max(p[2] + p[3] for p in paths) > 350, paths   # GB300: 304 resident CTAs
+    assert rel_max(mu, ref) <= 10 * tol
+    assert abs(info["n_compressed"] - st["compressed"]) <= 0.01 * st["compressed"]

@@ -135,7 +135,9 @@ def test_underpredicting_model_falls_back_to_the_plain_id(pkg):
     assert abs(info["n_root"] - plain.info()["n_root"]) <= max(2, 0.01 * plain.info()["n_root"])
     mu_p = plain.solve(f)[0]
     mu_f = fb.solve(f)[0]
-    assert np.abs(mu_f - mu_p).max() <= 1e-4 * np.abs(mu_p).max()
+    # two FP32 approximate inverses (plain solves, no refinement) whose
+    # skeletons may differ by a DOF
+    assert np.abs(mu_f - mu_p).max() <= 3e-4 * np.abs(mu_p).max()
 
 
 def bf16(a):
