@@ -31,7 +31,14 @@ typedef enum {
   KI_ERR_STATE = 6     /* call not valid for this handle (e.g. wrong problem kind) */
 } ki_status;
 
-/* Kernel::Pde (kern_interp/kernel/kernel.h:19-24). */
+/* Kernel::Pde (kern_interp/kernel/kernel.h:19-24).  LAPLACE and STOKES in 2D
+ * and 3D; LAPLACE_NEUMANN (the interior Neumann problem's adjoint double
+ * layer plus the rank-one weight term, kernel.cpp:44-54; domain targets take
+ * the single layer) and GAUSS (exp(-|r|^2), 5 on the diagonal, three proxy
+ * rings, kernel.cpp:55-60 and :661-672) in 2D with solution_dimension 1.
+ * These two have no border: holes are ignored (initialize_U_mat gives them
+ * an empty U, linear_solve.cpp:101-104), and their refinement residual is
+ * the dense FP64 apply (the FMM serves 2D LAPLACE). */
 typedef enum {
   KI_PDE_LAPLACE = 0,
   KI_PDE_LAPLACE_NEUMANN = 1,
@@ -60,8 +67,8 @@ typedef struct {
   int solution_dimension;    /* 1 (Laplace) or d (Stokes: 2 in 2D, 3 in 3D) */
   int pde;                   /* ki_pde */
   const double* points;      /* d*n_points, interleaved (x, y[, z]) */
-  const double* normals;     /* d*n_points, interleaved */
-  const double* weights;     /* n_points quadrature weights */
+  const double* normals;     /* d*n_points, interleaved (GAUSS: may be NULL, read as 0) */
+  const double* weights;     /* n_points quadrature weights (GAUSS: may be NULL) */
   const double* curvatures;  /* n_points, may be NULL (treated as 0; unused in 3D) */
   int n_holes;               /* multiply connected: number of holes */
   const double* hole_centers;    /* d*n_holes */

@@ -155,9 +155,10 @@ def _make_desc(params, points, normals, weights, curvatures, hole_centers, hole_
     (dim, solution_dimension, pde, max_leaf_dofs, num_proxy_points,
     radius_ratio, min_dofs_to_compress, id_tol, precision, rank model)."""
     dim, sd, pde, mld, npx, rr, mdc, tol, prec, rm = params
+    # normals / weights may be None for the Gaussian kernel (read as zeros)
     keep = [np.ascontiguousarray(points, np.float64).reshape(-1),
-            np.ascontiguousarray(normals, np.float64).reshape(-1),
-            np.ascontiguousarray(weights, np.float64).reshape(-1)]
+            None if normals is None else np.ascontiguousarray(normals, np.float64).reshape(-1),
+            None if weights is None else np.ascontiguousarray(weights, np.float64).reshape(-1)]
     keep.append(None if curvatures is None else
                 np.ascontiguousarray(curvatures, np.float64).reshape(-1))
     nh = 0 if hole_centers is None else int(np.asarray(hole_centers).shape[0])
@@ -165,7 +166,7 @@ def _make_desc(params, points, normals, weights, curvatures, hole_centers, hole_
     hs = np.ascontiguousarray(hole_start, np.int32) if nh else None
     hn = np.ascontiguousarray(hole_count, np.int32) if nh else None
     keep += [hc, hs, hn, rm]
-    n = keep[2].shape[0]
+    n = keep[0].shape[0] // dim
     return (_Desc(n, dim, sd, pde, _ptr(keep[0]), _ptr(keep[1]), _ptr(keep[2]), _ptr(keep[3]),
                   nh, _ptr(hc), _ptr(hs), _ptr(hn), mld, npx, rr, mdc, tol, prec, _ptr(rm)),
             keep)
@@ -242,12 +243,13 @@ class Factor:
 
     def _set_sizes(self):
         dim, sd = self._params[0], self._params[1]
-        n = self._keep[2].shape[0]
+        n = self._keep[0].shape[0] // dim
         self.n_dofs = n * sd
         self.n_points = n
         self.solution_dimension = sd
         self.domain_dimension = dim
-        self.n_border = self._n_holes * (1 if sd == 1 else (3 if dim == 2 else 6))
+        # the library's count: the Neumann and Gaussian kernels have no border
+        self.n_border = self.info()["n_border"]
 
     def update(self, points, normals, weights, curvatures=None, hole_centers=None, hole_start=None,
                hole_count=None):

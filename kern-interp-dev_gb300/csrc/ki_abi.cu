@@ -114,12 +114,14 @@ constexpr int kApplyCols = 8;
 // Kernel entry between a target (point data t*, DOF parity tpar) and a source
 // point (s*, parity spar), 2D or 3D (Kernel::operator() / get_3d,
 // kern_interp/kernel/kernel.cpp:304-429).  diag: the source point's 3D
-// diagonal data (used only when the two points coincide).
-__device__ __forceinline__ double pair_entry(int dim, int sol_dim, int tpar, int spar, double tx,
-                                             double ty, double tz, double tnx, double tny,
-                                             double tnz, double sx, double sy, double sz,
-                                             double snx, double sny, double snz, double sw,
-                                             double sk, const double* diag) {
+// diagonal data (used only when the two points coincide).  pde: the 2D
+// scalar kernel (Points::pde); fwd: a domain target (the Neumann problem's
+// single layer there).
+__device__ __forceinline__ double pair_entry(int dim, int sol_dim, int pde, bool fwd, int tpar,
+                                             int spar, double tx, double ty, double tz, double tnx,
+                                             double tny, double tnz, double sx, double sy,
+                                             double sz, double snx, double sny, double snz,
+                                             double sw, double sk, const double* diag) {
   if (dim == 3) {
     if (sol_dim == 1)
       return ki::laplace3_entry<double>(tx - sx, ty - sy, tz - sz, snx, sny, snz, sw,
@@ -127,7 +129,11 @@ __device__ __forceinline__ double pair_entry(int dim, int sol_dim, int tpar, int
     return ki::stokes3_entry<double>(tpar, spar, tx - sx, ty - sy, tz - sz, tnx, tny, tnz, snx,
                                      sny, snz, sw, diag);
   }
-  if (sol_dim == 1) return ki::laplace_entry<double>(tx, ty, sx, sy, snx, sny, sw, sk);
+  if (sol_dim == 1) {
+    if (pde == ki::kPdeNeumann && fwd) return ki::neumann_forward_r<double>(tx - sx, ty - sy, sw);
+    if (pde) return ki::scalar2_entry_r<double>(pde, tx - sx, ty - sy, tnx, tny, snx, sny, sw, sk);
+    return ki::laplace_entry<double>(tx, ty, sx, sy, snx, sny, sw, sk);
+  }
   return ki::stokes_entry<double>(tpar, spar, tx, ty, tnx, tny, sx, sy, snx, sny, sw, sk);
 }
 
@@ -186,7 +192,8 @@ __global__ void k_dense_apply(ki::Points<double> P, int n_points, int sol_dim, c
       const double* dg = dpp ? P.diag + (size_t)dpp * (base + i) : nullptr;
       for (int sp = 0; sp < sol_dim; sp++) {
         int sdof = (base + i) * sol_dim + sp;
-        double kv = pair_entry(dim, sol_dim, tpar, sp, tx, ty, tz, tnx, tny, tnz, sx[i], sy[i],
+        double kv = pair_entry(dim, sol_dim, P.pde, tg != nullptr, tpar, sp, tx, ty, tz, tnx,
+                               tny, tnz, sx[i], sy[i],
                                sz[i], snx[i], sny[i], snz[i], sw[i], sk[i], dg);
         for (int c = 0; c < nc; c++) acc[c] += kv * x[sdof + (size_t)ldx * (c0 + c)];
       }
@@ -475,6 +482,7 @@ struct ki_factor {
   int precision = KI_PRECISION_FP64;
   int dim = 2;
   int sol_dim = 1;
+  int pde = KI_PDE_LAPLACE;
   int n_points = 0;
   int n_dofs = 0;
   int n_holes = 0;
@@ -511,6 +519,7 @@ struct ki_factor {
     swap(precision, o.precision);
     swap(dim, o.dim);
     swap(sol_dim, o.sol_dim);
+    swap(pde, o.pde);
     swap(n_points, o.n_points);
     swap(n_dofs, o.n_dofs);
     swap(n_holes, o.n_holes);
@@ -589,21 +598,31 @@ void solve_impl(ki_factor* f, ki::Factorization<T>& F, const double* d_b, int ld
   }
 }
 
+static_assert(KI_PDE_LAPLACE_NEUMANN == ki::kPdeNeumann && KI_PDE_GAUSS == ki::kPdeGauss,
+              "Points::pde takes the ki_pde values");
+
 void check_desc(const ki_problem_desc* d) {
   if (!d) throw ArgError("desc is NULL");
   if (d->domain_dimension != 2 && d->domain_dimension != 3)
     throw ArgError("domain_dimension must be 2 or 3");
   const int dim = d->domain_dimension;
   if (d->n_points <= 0) throw ArgError("n_points must be positive");
-  if (!d->points || !d->normals || !d->weights) throw ArgError("points/normals/weights must be non-NULL");
   if (d->pde == KI_PDE_LAPLACE) {
     if (d->solution_dimension != 1) throw ArgError("Laplace needs solution_dimension 1");
   } else if (d->pde == KI_PDE_STOKES) {
     if (d->solution_dimension != dim)
       throw ArgError("Stokes needs solution_dimension equal to domain_dimension");
+  } else if (d->pde == KI_PDE_LAPLACE_NEUMANN || d->pde == KI_PDE_GAUSS) {
+    if (dim != 2 || d->solution_dimension != 1)
+      throw ArgError("the Neumann and Gaussian kernels need domain_dimension 2 and "
+                     "solution_dimension 1");
   } else {
-    throw ArgError("pde must be KI_PDE_LAPLACE or KI_PDE_STOKES");
+    throw ArgError("unknown pde");
   }
+  // the Gaussian kernel reads neither normals nor weights: NULL reads as zeros,
+  // as the reference's empty arrays do (Kernel::boundary_normals, kernel.cpp:12-22)
+  if (!d->points || (d->pde != KI_PDE_GAUSS && (!d->normals || !d->weights)))
+    throw ArgError("points/normals/weights must be non-NULL");
   if (!(d->id_tol > 0) || !std::isfinite(d->id_tol)) throw ArgError("id_tol must be positive");
   if (d->precision != KI_PRECISION_FP64 && d->precision != KI_PRECISION_FP32)
     throw ArgError("unknown precision");
@@ -623,10 +642,10 @@ void check_desc(const ki_problem_desc* d) {
       throw ArgError("3D num_proxy_points must be 2 q^2 (a theta x phi grid of 2q x q points)");
   }
   for (long i = 0; i < (long)dim * d->n_points; i++)
-    if (!std::isfinite(d->points[i]) || !std::isfinite(d->normals[i]))
+    if (!std::isfinite(d->points[i]) || (d->normals && !std::isfinite(d->normals[i])))
       throw ArgError("non-finite point or normal");
   for (int i = 0; i < d->n_points; i++) {
-    if (!std::isfinite(d->weights[i])) throw ArgError("non-finite weight");
+    if (d->weights && !std::isfinite(d->weights[i])) throw ArgError("non-finite weight");
     if (d->curvatures && !std::isfinite(d->curvatures[i])) throw ArgError("non-finite curvature");
   }
   if (d->max_leaf_dofs < 0 || d->num_proxy_points < 0 || d->min_dofs_to_compress < 0 ||
@@ -1086,7 +1105,9 @@ void refined_solve(ki_factor* f, const double* b, int ncols, double* mu, double*
 // DOF, sources through shared memory; KI_RESIDUAL_APPLY=dense forces it),
 // border columns, Psi rows.
 namespace {
-bool fmm_capable(const ki_factor* f) { return f->dim == 2 && f->sol_dim == 1; }
+bool fmm_capable(const ki_factor* f) {
+  return f->dim == 2 && f->sol_dim == 1 && f->pde == KI_PDE_LAPLACE;
+}
 
 // Expansion terms of the FMM plan (translation matrices for every lower
 // order are leading blocks, so one plan serves any accuracy).
@@ -1228,9 +1249,23 @@ namespace {
 // the same problem before a boundary perturbation, same precision, sizes,
 // parameters and rank model), the boxes of prev's factorization that the
 // perturbation left unchanged are copied rather than recomputed.
-void build_factor(ki_factor* f, const ki_problem_desc* desc, const ki_factor* prev,
+void build_factor(ki_factor* f, const ki_problem_desc* desc_in, const ki_factor* prev,
                   bool plan_fmm = true) {
   const auto t_create = std::chrono::steady_clock::now();
+  // the Neumann and Gaussian problems have no border: the reference's
+  // initialize_U_mat / initialize_Psi_mat give them empty matrices
+  // (kern_interp/linear_solve.cpp:101-104, :193-196), so holes are ignored;
+  // absent normals and weights (Gaussian kernel) read as zeros
+  ki_problem_desc dd = *desc_in;
+  const ki_problem_desc* desc = &dd;
+  const bool scalar_other = dd.pde == KI_PDE_LAPLACE_NEUMANN || dd.pde == KI_PDE_GAUSS;
+  if (scalar_other) dd.n_holes = 0;
+  std::vector<double> zeros;
+  if (!dd.normals || !dd.weights) {
+    zeros.assign((size_t)dd.domain_dimension * dd.n_points, 0.0);
+    if (!dd.normals) dd.normals = zeros.data();
+    if (!dd.weights) dd.weights = zeros.data();
+  }
   int dev_count = 0;
   if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
     cudaGetLastError();
@@ -1240,6 +1275,7 @@ void build_factor(ki_factor* f, const ki_problem_desc* desc, const ki_factor* pr
   const int dim = desc->domain_dimension;
   f->dim = dim;
   f->sol_dim = desc->solution_dimension;
+  f->pde = desc->pde;
   f->n_points = desc->n_points;
   f->n_dofs = desc->n_points * desc->solution_dimension;
   f->n_holes = desc->n_holes;
@@ -1248,6 +1284,7 @@ void build_factor(ki_factor* f, const ki_problem_desc* desc, const ki_factor* pr
   ki::Params prm;
   prm.dim = dim;
   prm.sol_dim = desc->solution_dimension;
+  prm.pde = scalar_other ? desc->pde : 0;   // ki::kPdeNeumann / ki::kPdeGauss
   prm.max_leaf_dofs = desc->max_leaf_dofs ? desc->max_leaf_dofs : 64;
   // reference defaults: NUM_PROXY_POINTS = 128 (2D); the 3D proxy sphere is
   // the Kernel constructor's 8 x 4 grid (kern_interp/kernel/kernel.h:44-62)
@@ -1298,6 +1335,7 @@ void build_factor(ki_factor* f, const ki_problem_desc* desc, const ki_factor* pr
                             f->d_geo + 3 * (size_t)n, f->d_geo + 4 * (size_t)n,
                             f->d_geo + 5 * (size_t)n};
   f->P.dim = dim;
+  f->P.pde = prm.pde;
   if (dim == 3) {
     f->P.z = f->d_geo + 6 * (size_t)n;
     f->P.nz = f->d_geo + 7 * (size_t)n;
@@ -1375,7 +1413,8 @@ void build_factor(ki_factor* f, const ki_problem_desc* desc, const ki_factor* pr
   // prev's factorization serves only a problem of the same kind and size
   // with the same rank model (factorize checks the parameters)
   const bool reuse = prev && prev->precision == f->precision && prev->dim == f->dim &&
-                     prev->sol_dim == f->sol_dim && prev->n_points == f->n_points &&
+                     prev->sol_dim == f->sol_dim && prev->pde == f->pde &&
+                     prev->n_points == f->n_points &&
                      prev->rank_model_host == f->rank_model_host;
   if (f->precision == KI_PRECISION_FP64)
     f->f64 = ki::factorize<double>(prm, n, desc->points, desc->normals, desc->weights,

@@ -30,7 +30,14 @@ struct Points {
   const T* xl = nullptr;
   const T* yl = nullptr;
   const T* zl = nullptr;
+  // 2D scalar kernels other than the Laplace double layer (Kernel::Pde,
+  // kern_interp/kernel/kernel.h:19-24): kPdeNeumann, kPdeGauss; 0 otherwise
+  int pde = 0;
 };
+
+// Kernel::Pde values of the scalar 2D kernels that Points::pde selects.
+constexpr int kPdeNeumann = 1;
+constexpr int kPdeGauss = 2;
 
 // Coordinate difference a - b from (hi, lo) pairs: hi[a] - hi[b] is exact for
 // nearby points (Sterbenz), so the difference keeps full relative accuracy.
@@ -54,6 +61,39 @@ __device__ __forceinline__ T laplace_entry_r(T r1, T r2, T snx, T sny, T sw, T s
 template <typename T>
 __device__ __forceinline__ T laplace_entry(T tx, T ty, T sx, T sy, T snx, T sny, T sw, T sk) {
   return laplace_entry_r<T>(tx - sx, ty - sy, snx, sny, sw, sk);
+}
+
+// Interior Neumann problem (Kernel::one_d_kern, LAPLACE_NEUMANN,
+// kern_interp/kernel/kernel.cpp:44-54): the adjoint double layer
+// w/(2 pi) (r.n_t)/|r|^2 plus the rank-one term w that removes the constant
+// null space; a coincident pair takes w - 1/2 + kappa w/(4 pi).  Domain
+// targets (forward) take the single layer w/(2 pi) log|r|.
+template <typename T>
+__device__ __forceinline__ T neumann_entry_r(T r1, T r2, T tnx, T tny, T sw, T sk) {
+  if (r1 == T(0) && r2 == T(0)) return sw - T(0.5) + T(0.5) * sk * sw * T(1.0 / (2 * kPi));
+  return sw + sw * T(1.0 / (2 * kPi)) * (r1 * tnx + r2 * tny) / (r1 * r1 + r2 * r2);
+}
+template <typename T>
+__device__ __forceinline__ T neumann_forward_r(T r1, T r2, T sw) {
+  return sw * T(1.0 / (2 * kPi)) * log(sqrt(r1 * r1 + r2 * r2));
+}
+
+// Gaussian covariance kernel (Kernel::one_d_kern, GAUSS, kernel.cpp:55-60):
+// exp(-|r|^2), 5 on the diagonal; no quadrature weight, the same for domain
+// targets.
+template <typename T>
+__device__ __forceinline__ T gauss_entry_r(T r1, T r2) {
+  if (r1 == T(0) && r2 == T(0)) return T(5);
+  return exp(-(r1 * r1 + r2 * r2));
+}
+
+// Scalar 2D entry of Points::pde between target (normal tn) and source.
+template <typename T>
+__device__ __forceinline__ T scalar2_entry_r(int pde, T r1, T r2, T tnx, T tny, T snx, T sny, T sw,
+                                             T sk) {
+  if (pde == kPdeNeumann) return neumann_entry_r<T>(r1, r2, tnx, tny, sw, sk);
+  if (pde == kPdeGauss) return gauss_entry_r<T>(r1, r2);
+  return laplace_entry_r<T>(r1, r2, snx, sny, sw, sk);
 }
 
 template <typename T>
@@ -122,6 +162,10 @@ __device__ __forceinline__ T kernel_entry(const Points<T>& P, int sol_dim, int t
                             P.diag ? P.diag + 9 * (size_t)sp : nullptr);
   }
   if (sol_dim == 1) {
+    if (P.pde)
+      return scalar2_entry_r<T>(P.pde, pdiff(P.x, P.xl, tdof, sdof), pdiff(P.y, P.yl, tdof, sdof),
+                                P.nx[tdof], P.ny[tdof], P.nx[sdof], P.ny[sdof], P.w[sdof],
+                                P.kappa[sdof]);
     return laplace_entry_r<T>(pdiff(P.x, P.xl, tdof, sdof), pdiff(P.y, P.yl, tdof, sdof),
                               P.nx[sdof], P.ny[sdof], P.w[sdof], P.kappa[sdof]);
   }

@@ -261,7 +261,17 @@ struct ProxyTab {
   const T* uz;   // 3D only
   const T* wu;   // 3D only
   int n;
+  // 2D concentric proxy rings per direction: 1, or 3 for the Gaussian kernel
+  // (radii rad - 1, rad, rad + 1; Kernel::get_proxy_mat, kernel.cpp:661-672)
+  int rings = 1;
 };
+
+// Rows of the proxy blocks (box -> proxy, then proxy -> box) of a box's ID
+// matrix.
+template <typename T>
+__host__ __device__ __forceinline__ int proxy_rows(const ProxyTab<T>& px, int sol_dim) {
+  return 2 * px.n * px.rings * sol_dim;
+}
 
 // A box's proxy geometry in the factor precision: the centre split as
 // hi + lo (so that box-point offsets b - c keep full relative accuracy in
@@ -301,8 +311,14 @@ __device__ __forceinline__ T id_entry(const Points<T>& P, int sol_dim, int row, 
   const T bcx = (P.x[ap] - c.hx) + ((P.xl ? P.xl[ap] : T(0)) - c.lx);
   const T bcy = (P.y[ap] - c.hy) + ((P.yl ? P.yl[ap] : T(0)) - c.ly);
   const T bnx = P.nx[ap], bny = P.ny[ap], bw = P.w[ap];
-  const int half = sol_dim * nprox;
+  const int half = sol_dim * nprox * px.rings;
   const int qq = q < half ? q : q - half;
+  if (px.rings > 1) {
+    // Gaussian kernel: proxy point (ring, direction) = qq as ring-minor
+    const int i = qq / px.rings, ring = qq - px.rings * i;
+    const T rr = c.rad + T(ring - 1);
+    return gauss_entry_r<T>(rr * px.ux[i] - bcx, rr * px.uy[i] - bcy);
+  }
   const int i = sol_dim == 1 ? qq : qq / sol_dim, par = qq - sol_dim * i;
   const T ux = px.ux[i], uy = px.uy[i];
   const T rx = c.rad * ux - bcx, ry = c.rad * uy - bcy;   // proxy - box
@@ -322,8 +338,8 @@ __device__ __forceinline__ T id_entry(const Points<T>& P, int sol_dim, int row, 
     return stokes3_entry<T>(apar, par, -rx, -ry, -rz, bnx, bny, bnz, ux, uy, uz, pw, nullptr);
   }
   if (sol_dim == 1) {
-    if (q < half) return laplace_entry_r<T>(rx, ry, bnx, bny, bw, T(0));
-    return laplace_entry_r<T>(-rx, -ry, ux, uy, c.pw2, T(0));
+    if (q < half) return scalar2_entry_r<T>(P.pde, rx, ry, ux, uy, bnx, bny, bw, T(0));
+    return scalar2_entry_r<T>(P.pde, -rx, -ry, bnx, bny, ux, uy, c.pw2, T(0));
   }
   const int apar = adof & 1;
   if (q < half) return stokes_entry_r<T>(par, apar, rx, ry, ux, uy, bnx, bny, bw, T(0));
@@ -416,7 +432,7 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? kIdMinBlocks<T> : 1) k_id
   T* Tout = gws + (size_t)n * n;
 
   // 1. candidate rows, optionally filtered to the proxy circle, order kept
-  const int nprox_rows = t.mode == 0 ? 2 * px.n * sol_dim : 0;
+  const int nprox_rows = t.mode == 0 ? proxy_rows(px, sol_dim) : 0;
   if (flags & 1) {
   if (tid == 0) s_cnt = 0;
   // the box centre split hi + lo and the filter radius, for the FP32 filter
@@ -1008,7 +1024,7 @@ __global__ void __launch_bounds__(kTcThreads) k_sketch_tc(const IdTask* tasks, c
   const int n = t.n, m = m_arr[ti], l = sketch_l[ti];
   const int nq = (l + 15) & ~15;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nI = (m - (t.mode == 0 ? 2 * px.n * sol_dim : 0)) / 2;
+  const int nI = (m - (t.mode == 0 ? proxy_rows(px, sol_dim) : 0)) / 2;
   const int* rows = iscratch + t.rows;
   const int* act = ipool + t.act;
   if (threadIdx.x == 0) s_box = proxy_box<float>(t.cx, t.cy, t.cz, t.rad_proxy, px.n);
@@ -3292,6 +3308,7 @@ bool same_params(const Params& a, const Params& b) {
   return a.dim == b.dim && a.sol_dim == b.sol_dim && a.max_leaf_dofs == b.max_leaf_dofs &&
          a.num_proxy_points == b.num_proxy_points && a.radius_ratio == b.radius_ratio &&
          a.min_dofs_to_compress == b.min_dofs_to_compress && a.id_tol == b.id_tol &&
+         a.pde == b.pde &&
          (a.rank_model != nullptr) == (b.rank_model != nullptr) &&
          a.sketch_margin == b.sketch_margin && a.sketch_oversample == b.sketch_oversample;
 }
@@ -3652,6 +3669,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
   P.xl = F->d_xl;
   P.yl = F->d_yl;
   P.zl = F->d_zl;
+  P.pde = dim == 2 && prm.sol_dim == 1 ? prm.pde : 0;
   F->d_err = (int*)F->alloc(sizeof(int));
   KI_CUDA(cudaMemsetAsync(F->d_err, 0, sizeof(int), s));
 
@@ -3692,6 +3710,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
   const int np = prm.num_proxy_points;
   T* d_ptab = (T*)F->alloc(sizeof(T) * 4 * std::max(np, 1));
   ProxyTab<T> ptab{d_ptab, d_ptab + np, d_ptab + 2 * np, d_ptab + 3 * np, np};
+  if (dim == 2 && prm.pde == kPdeGauss) ptab.rings = 3;
   {
     std::vector<double> pt(4 * std::max(np, 1), 0.0);
     if (dim == 2) {
@@ -3982,7 +4001,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       const char* mlp_env = std::getenv("KI_MLP_FP32");
       const bool tc_mlp = prm.rank_model && !(mlp_env && std::string(mlp_env) == "1");
       ki::launch(k_box_features<T>, (ntask + 3) / 4, 128, 0, s,
-          d_it, ntask, ipool, P, sd, d_m, 2 * np * sd, L > 1 ? (float)l / (float)(L - 1) : 0.f,
+          d_it, ntask, ipool, P, sd, d_m, proxy_rows(ptab, sd), L > 1 ? (float)l / (float)(L - 1) : 0.f,
           (float)(-std::log10(prm.id_tol) / 10.0), tc_mlp ? nullptr : prm.rank_model,
           prm.sketch_margin, prm.sketch_oversample, d_feat, d_lsk, d_khat);
       KI_CUDA(cudaGetLastError());
@@ -4223,7 +4242,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
           w.task = (int)i;
           w.n = itasks[i].n;
           w.m = mh[i];
-          w.nI = (mh[i] - (itasks[i].mode == 0 ? 2 * np * sd : 0)) / 2;
+          w.nI = (mh[i] - (itasks[i].mode == 0 ? proxy_rows(ptab, sd) : 0)) / 2;
           w.act = itasks[i].act;
           w.rows = itasks[i].rows;
           w.cx = itasks[i].cx;

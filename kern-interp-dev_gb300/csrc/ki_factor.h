@@ -17,6 +17,7 @@ namespace ki {
 struct Params {
   int dim = 2;                // domain dimension: 2 or 3
   int sol_dim = 1;            // 1: Laplace, 2: Stokes (2D), 3: Stokes (3D)
+  int pde = 0;                // 2D scalar kernel (Points::pde): 0, kPdeNeumann, kPdeGauss
   int max_leaf_dofs = 64;     // MAX_LEAF_DOFS
   int num_proxy_points = 128; // NUM_PROXY_POINTS (2D); 3D: theta x phi grid, 2 q^2 points
   double radius_ratio = 2.0;  // RADIUS_RATIO: proxy radius = ratio*sqrt(dim)*side/2

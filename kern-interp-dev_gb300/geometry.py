@@ -311,6 +311,29 @@ def laplace_source_rhs(prob, sources):
     return np.log(np.hypot(d[..., 0], d[..., 1])) / (2 * np.pi)
 
 
+def laplace_neumann_rhs(prob, sources):
+    """Normal derivatives (along the boundary's normals) of u(x) = log|x - y|
+    / (2 pi) for each source y (one column per source): the data of an
+    interior Neumann problem whose solution is that field, up to a constant."""
+    sources = np.atleast_2d(sources)
+    d = prob.points[:, None, :] - sources[None, :, :]
+    r2 = (d ** 2).sum(-1)
+    return (d * prob.normals[:, None, :]).sum(-1) / r2 / (2 * np.pi)
+
+
+def uniform_grid(n):
+    """The reference's UniformDist point set (kern_interp/boundaries/
+    uniformdist.cpp:8-19): ceil(sqrt(n))^2 points 0.00123 + (i, j)/sqrt(n),
+    i outer; no normals, weights or curvatures (zeros), no holes.  The
+    Gaussian covariance kernel's test set."""
+    s = np.sqrt(n)
+    m = int(np.ceil(s))
+    i, j = np.meshgrid(np.arange(m), np.arange(m), indexing="ij")
+    pts = np.stack([0.00123 + i.reshape(-1) / s, 0.00123 + j.reshape(-1) / s], 1)
+    z = np.zeros(pts.shape[0])
+    return Problem(pts, np.zeros_like(pts), z, z.copy(), name="uniform_grid")
+
+
 def laplace_source_field(targets, sources):
     sources = np.atleast_2d(sources)
     d = targets[:, None, :] - sources[None, :, :]

@@ -146,7 +146,8 @@ def solve(prob, rhs, tol, threads=1, leaf=64, proxy=None, ratio=2.0, min_compres
     N = prob.n * solution_dim
     nrhs = rhs.shape[1]
     c = 1 if solution_dim == 1 else (3 if dim == 2 else 6)
-    nb = c * prob.n_holes
+    # the Neumann (1) and Gaussian (2) kernels have no border (empty U)
+    nb = 0 if pde in (1, 2) else c * prob.n_holes
     pts = np.ascontiguousarray(prob.points, np.float64)
     nrm = np.ascontiguousarray(prob.normals, np.float64)
     wts = np.ascontiguousarray(prob.weights, np.float64)

@@ -212,6 +212,14 @@ inline double entry(const Geometry& g, int tgt_dof, int src_dof, const double* t
            sw * tn[tpar] * sn[spar];
   }
   double r1 = tp[0] - sp[0], r2 = tp[1] - sp[1];
+  if (g.sol_dim == 1 && g.pde == 1) {   // LAPLACE_NEUMANN (kernel.cpp:44-54), not forward
+    if (r1 == 0. && r2 == 0.) return sw - 0.5 + 0.5 * sc * sw * (1.0 / (2 * M_PI));
+    return sw + sw * (1.0 / (2 * M_PI)) * (r1 * tn[0] + r2 * tn[1]) / (r1 * r1 + r2 * r2);
+  }
+  if (g.sol_dim == 1 && g.pde == 2) {   // GAUSS (kernel.cpp:55-60)
+    if (r1 == 0. && r2 == 0.) return 5.;
+    return std::exp(-(r1 * r1 + r2 * r2));
+  }
   if (g.sol_dim == 1) {
     if (r1 == 0. && r2 == 0.) return 0.5 + 0.5 * sc * sw * (1.0 / (2 * M_PI));
     return -sw * (1.0 / (2 * M_PI)) * (r1 * sn[0] + r2 * sn[1]) / (r1 * r1 + r2 * r2);
@@ -249,10 +257,28 @@ Mat kernel_block(const Geometry& g, const std::vector<int>& tgt, const std::vect
   return R;
 }
 
-// Kernel::get_proxy_mat (kernel/kernel.cpp:646-717), 2D.
+// Kernel::get_proxy_mat (kernel/kernel.cpp:646-717), 2D.  The Gaussian
+// kernel takes three rings per angle, radii r - 1, r, r + 1 (ring-minor rows).
 Mat proxy_block(const Geometry& g, const double* c, int P, double r, const std::vector<int>& box) {
   double pw = 2.0 * M_PI * r / P;
   int c_dim = g.sol_dim;
+  if (c_dim == 1 && g.pde == 2) {
+    Mat R(6 * P, (int)box.size());
+    for (size_t j = 0; j < box.size(); j++) {
+      const double* b = g.pts + 2 * box[j];
+      for (int i = 0; i < P; i++) {
+        double ang = 2 * M_PI * i * (1.0 / P);
+        for (int k = 0; k < 3; k++) {
+          double rr = r + (k - 1);
+          double pp[2] = {c[0] + rr * std::cos(ang), c[1] + rr * std::sin(ang)};
+          double pn[2] = {std::cos(ang), std::sin(ang)};
+          R(3 * i + k, (int)j) = entry(g, 0, 0, pp, pn, b, b, 0., 0);
+          R(3 * P + 3 * i + k, (int)j) = entry(g, 0, 0, b, b, pp, pn, pw, 0);
+        }
+      }
+    }
+    return R;
+  }
   int lda = c_dim * 2 * P;
   Mat R(lda, (int)box.size());
   for (size_t j = 0; j < box.size(); j++) {
@@ -1050,6 +1076,9 @@ int kiport_solve(int n_points, int domain_dim, int solution_dim, int pde,
     t.g.dim = domain_dim;
     t.g.sol_dim = solution_dim;
     t.g.pde = pde;
+    // the Neumann and Gaussian problems have no border (initialize_U_mat gives
+    // them an empty U, linear_solve.cpp:101-104)
+    if (pde == 1 || pde == 2) n_holes = 0;
     t.g.pts = points;
     t.g.nrm = normals;
     t.g.wts = weights;

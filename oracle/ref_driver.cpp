@@ -90,7 +90,10 @@ int kiref_solve(int n_points, int domain_dim, int solution_dim, int pde,
   kern_interp::QuadTree quadtree;
   quadtree.initialize_tree(&boundary, solution_dim, d);
 
-  if (n_holes > 0) {
+  // the Neumann and Gaussian kernels get an empty U (initialize_U_mat,
+  // kern_interp/linear_solve.cpp:101-104): no border, holes ignored
+  if (n_holes > 0 && pde != kern_interp::Kernel::Pde::LAPLACE_NEUMANN &&
+      pde != kern_interp::Kernel::Pde::GAUSS) {
     quadtree.U = kern_interp::initialize_U_mat(kernel.pde, boundary.holes,
                                                boundary.points, d);
     // Psi from node ranges (Laplace: weights; Stokes: reference layout,
@@ -134,7 +137,9 @@ int kiref_solve(int n_points, int domain_dim, int solution_dim, int pde,
     kern_interp::ki_Mat f(N, 1);
     std::memcpy(f.mat, rhs + (size_t)col * N, sizeof(double) * N);
     kern_interp::ki_Mat mu(N, 1);
-    if (n_holes > 0) {
+    // as linear_solve decides (kern_interp/linear_solve.cpp:236): the bordered
+    // solve only when U has columns
+    if (quadtree.U.width() > 0) {
       kern_interp::ki_Mat alpha(quadtree.U.width(), 1);
       skel.multiply_connected_solve(quadtree, &mu, &alpha, f);
       if (alpha_out)

@@ -96,6 +96,23 @@ def cases():
     out.append(("stokes3_sphere_hole", prob,
                 g.stokes3_rhs(prob, np.array([[2.0, 1.0, 1.0]]), np.array([[1.0, 0.5, -0.3]])),
                 dict(tol=1e-7, proxy=0, ratio=2.0, leaf=64, min_compress=64, solution_dim=3, pde=3)))
+    # the other scalar 2D kernels (Kernel::Pde LAPLACE_NEUMANN = 1, GAUSS = 2):
+    # interior Neumann data of exterior sources (the holes of the second case
+    # are ignored, as the reference gives these kernels no border), and the
+    # Gaussian covariance matrix on the reference's UniformDist grid with a
+    # seeded random right-hand side at the covariance experiment's tolerance
+    # (kern_interp/experiments/covar.cpp:22-44)
+    prob = g.star(128, 16)
+    out.append(("neumann_star_2048", prob,
+                g.laplace_neumann_rhs(prob, np.array([[3.0, 1.0], [-2.0, 2.5]])),
+                dict(tol=1e-10, proxy=128, ratio=2.0, leaf=64, min_compress=64, solution_dim=1, pde=1)))
+    prob = g.disc_with_circles(2048, 2, seed=5)
+    out.append(("neumann_disc_circles_2048", prob,
+                g.laplace_neumann_rhs(prob, np.array([[2.5, -1.0]])),
+                dict(tol=1e-10, proxy=128, ratio=2.0, leaf=64, min_compress=64, solution_dim=1, pde=1)))
+    prob = g.uniform_grid(4096)
+    out.append(("gauss_uniform_4096", prob, np.random.default_rng(7).standard_normal((prob.n, 1)),
+                dict(tol=1e-6, proxy=128, ratio=2.0, leaf=64, min_compress=64, solution_dim=1, pde=2)))
     return out
 
 

@@ -48,7 +48,10 @@ def _desc(pkg, prob, **kw):
                                  dict(domain_dimension=3, num_proxy_points=30),
                                  dict(domain_dimension=3, pde=3, solution_dimension=2),
                                  dict(n_points=0), dict(id_tol=0.0),
-                                 dict(id_tol=float("nan")), dict(pde=1), dict(precision=7),
+                                 dict(id_tol=float("nan")), dict(pde=5), dict(precision=7),
+                                 dict(pde=1, solution_dimension=2),
+                                 dict(pde=2, domain_dimension=3, num_proxy_points=32),
+                                 dict(pde=1, normals=None), dict(pde=0, weights=None),
                                  dict(solution_dimension=2), dict(max_leaf_dofs=-1),
                                  dict(n_holes=1)])
 def test_bad_arguments_rejected(pkg, lib, bad):
@@ -59,6 +62,24 @@ def test_bad_arguments_rejected(pkg, lib, bad):
     assert rc == pkg.KI_ERR_ARG
     assert lib.ki_last_error()
     assert not h.value
+
+
+@pytest.mark.parametrize("pde", [1, 2])
+def test_neumann_and_gauss_pass_validation(pkg, lib, have_gpu, pde):
+    """The Neumann and Gaussian kernels (2D, scalar) pass argument checks;
+    the Gaussian kernel reads neither normals nor weights, so NULL is
+    accepted for both (the reference reads its empty arrays as zeros)."""
+    if have_gpu:
+        pytest.skip("a GPU would factorize; this checks validation only")
+    prob = pkg.geometry.star(8, 16)
+    kw = dict(pde=pde)
+    if pde == 2:
+        kw.update(normals=None, weights=None)
+    d, keep = _desc(pkg, prob, **kw)
+    h = ctypes.c_void_p()
+    rc = lib.ki_factor_create(ctypes.byref(d), ctypes.byref(h))
+    assert rc != pkg.KI_ERR_ARG, lib.ki_last_error()
+    assert b"CUDA" in lib.ki_last_error()
 
 
 def test_non_finite_input_rejected(pkg, lib):

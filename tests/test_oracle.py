@@ -25,7 +25,8 @@ def test_generators_reproduce_fixture_inputs(golden_cases, pkg):
                                   "star_2048_tol1e-4", "star_64_root_leaf", "disc6_8k",
                                   "stokes_star_2048", "laplace3_ellipsoid_3000",
                                   "stokes3_ellipsoid_1500", "laplace3_sphere_hole",
-                                  "stokes3_sphere_hole"])
+                                  "stokes3_sphere_hole", "neumann_star_2048",
+                                  "neumann_disc_circles_2048", "gauss_uniform_4096"])
 def test_port_matches_reference_fixture(golden_cases, oracle_mod, name):
     prob, rhs, p, data, _ = golden_cases[name]
     mu, alpha, st = oracle_mod.solve(prob, rhs, p["tol"], threads=4, leaf=p["leaf"],
