@@ -3083,6 +3083,59 @@ __global__ void k_reduce_partial(const T* A, int na, const T* B, int nc, int N,
   }
 }
 
+// The same partial sums register-tiled: each thread owns up to two 4 x 2
+// output tiles (a, c), so a row of the staged operands costs 6 shared-memory
+// loads per 8 FMAs instead of 16.  Operands padded to multiples of 4 (A) and
+// 2 (B) columns with zeros; used when ceil(na/4) ceil(nc/2) <= 2 blockDim.
+template <typename T>
+__global__ void __launch_bounds__(256) k_reduce_tiled(const T* A, int na, const T* B, int nc, int N,
+                                                      const unsigned char* mask, T* partial) {
+  extern __shared__ unsigned char red_smem[];
+  const int lda = (na + 3) & ~3, ldb = (nc + 1) & ~1;
+  T* As = reinterpret_cast<T*>(red_smem);   // 32 x lda
+  T* Bs = As + 32 * (size_t)lda;            // 32 x ldb
+  const int nga = lda / 4, ntile = nga * (ldb / 2);
+  const int r0 = blockIdx.x * kRedRows;
+  const int r1 = min(N, r0 + kRedRows);
+  T acc[2][4][2];
+  for (int q = 0; q < 2; q++)
+    for (int u = 0; u < 4; u++) acc[q][u][0] = acc[q][u][1] = T(0);
+  for (int t0 = r0; t0 < r1; t0 += 32) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * lda; e += blockDim.x) {
+      const int i = t0 + e / lda, a = e % lda;
+      As[e] = (i < r1 && a < na && !mask[i]) ? A[(size_t)i * na + a] : T(0);
+    }
+    for (int e = threadIdx.x; e < 32 * ldb; e += blockDim.x) {
+      const int i = t0 + e / ldb, c = e % ldb;
+      Bs[e] = (i < r1 && c < nc) ? B[(size_t)i * nc + c] : T(0);
+    }
+    __syncthreads();
+    for (int q = 0; q < 2; q++) {
+      const int tile = threadIdx.x + q * blockDim.x;
+      if (tile >= ntile) break;
+      const int a0 = 4 * (tile % nga), c0 = 2 * (tile / nga);
+      for (int i = 0; i < 32; i++) {
+        const T* ar = As + i * lda + a0;
+        const T b0 = Bs[i * ldb + c0], b1 = Bs[i * ldb + c0 + 1];
+        for (int u = 0; u < 4; u++) {
+          acc[q][u][0] += ar[u] * b0;
+          acc[q][u][1] += ar[u] * b1;
+        }
+      }
+    }
+  }
+  T* out = partial + (size_t)blockIdx.x * na * nc;
+  for (int q = 0; q < 2; q++) {
+    const int tile = threadIdx.x + q * blockDim.x;
+    if (tile >= ntile) break;
+    const int a0 = 4 * (tile % nga), c0 = 2 * (tile / nga);
+    for (int u = 0; u < 4; u++)
+      for (int v = 0; v < 2; v++)
+        if (a0 + u < na && c0 + v < nc) out[(a0 + u) + (size_t)na * (c0 + v)] = acc[q][u][v];
+  }
+}
+
 template <typename T>
 __global__ void k_reduce_final(const T* partial, int nparts, int nout, T* out) {
   for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < nout; o += gridDim.x * blockDim.x) {
@@ -3124,15 +3177,19 @@ __global__ void k_mc_rhs(const T* x, int ldx, const int* idx, int nr, const T* t
   }
 }
 
-// x(i, :) -= U~(i, :) alpha for redundant rows (N = w - U~_r alpha).
-// x (DOF-major N x nc) -= U~ alpha on the rows whose mask is clear (U~: N x
-// nb row-major, alpha = rows nr.. of M, ns x nc column-major).  Lanes are
-// columns (blockIdx.y: a 32-column chunk), a warp takes one row at a time
-// with the U~ row broadcast, alpha staged in shared memory 64 border
-// columns at a time; each CTA owns a contiguous range of rows.
+// The redundant rows of the bordered solve's result, D^-1 (w - U~ alpha)
+// formed as D^-1 w - (D^-1 U~) alpha (D^-1 is block diagonal on the
+// redundant rows, so the two agree; the second form needs no second pass of
+// diagonal solves): x(i, :) = Dw(i, :) - DU(i, :) alpha on the rows whose
+// mask is clear (DU: N x nb row-major, nb <= 64; alpha = rows nr.. of M,
+// ns x nc column-major).  Lanes are columns (blockIdx.y: a 32-column chunk);
+// a warp takes one row at a time, its DU row loaded by the lanes and
+// broadcast by shuffles; alpha staged in shared memory; each CTA owns a
+// contiguous range of rows.
 template <typename T>
-__global__ void __launch_bounds__(256) k_mc_update(T* x, int nc, const T* Um, int nb, const T* M,
-                                                   int nr, int N, const unsigned char* mask) {
+__global__ void __launch_bounds__(256) k_mc_final(T* x, int nc, const T* Dw, const T* DU, int nb,
+                                                  const T* M, int nr, int N,
+                                                  const unsigned char* mask) {
   __shared__ T A[64 * 32];
   const int ns = nr + nb;
   const int c0 = blockIdx.y * 32;
@@ -3140,30 +3197,29 @@ __global__ void __launch_bounds__(256) k_mc_update(T* x, int nc, const T* Um, in
   const int c = c0 + lane;
   const int per = (N + gridDim.x - 1) / gridDim.x;
   const int i0 = blockIdx.x * per, i1 = min(N, i0 + per);
-  for (int b0 = 0; b0 < nb; b0 += 64) {
-    const int bn = min(64, nb - b0);
-    __syncthreads();
-    for (int e = threadIdx.x; e < 64 * 32; e += blockDim.x) {
-      const int b = e / 32, cc = e % 32;
-      A[e] = (b < bn && c0 + cc < nc) ? M[nr + b0 + b + (size_t)ns * (c0 + cc)] : T(0);
-    }
-    __syncthreads();
-    for (int i = i0 + warp; i < i1; i += nw) {
-      if (mask[i]) continue;
-      const T* u = Um + (size_t)i * nb + b0;
-      T acc = T(0);
-      for (int b = 0; b < bn; b++) acc += u[b] * A[b * 32 + lane];
-      if (c < nc) x[(size_t)i * nc + c] -= acc;
-    }
+  for (int e = threadIdx.x; e < 64 * 32; e += blockDim.x) {
+    const int b = e / 32, cc = e % 32;
+    A[e] = (b < nb && c0 + cc < nc) ? M[nr + b + (size_t)ns * (c0 + cc)] : T(0);
+  }
+  __syncthreads();
+  for (int i = i0 + warp; i < i1; i += nw) {
+    if (mask[i]) continue;
+    const T* u = DU + (size_t)i * nb;
+    const T u0 = lane < nb ? u[lane] : T(0);
+    const T u1 = 32 + lane < nb ? u[32 + lane] : T(0);
+    T acc = T(0);
+    for (int b = 0; b < min(nb, 32); b++) acc += __shfl_sync(0xffffffffu, u0, b) * A[b * 32 + lane];
+    for (int b = 32; b < nb; b++) acc += __shfl_sync(0xffffffffu, u1, b - 32) * A[b * 32 + lane];
+    if (c < nc) x[(size_t)i * nc + c] = Dw[(size_t)i * nc + c] - acc;
   }
 }
 
 template <typename T>
-void mc_update(T* x, int nc, const T* Um, int nb, const T* M, int nr, int N,
-               const unsigned char* mask, cudaStream_t s) {
+void mc_final(T* x, int nc, const T* Dw, const T* DU, int nb, const T* M, int nr, int N,
+              const unsigned char* mask, cudaStream_t s) {
   if (N <= 0 || nc <= 0 || nb <= 0) return;
   dim3 g((unsigned)std::max(1, std::min(4096, (N + 255) / 256)), (unsigned)((nc + 31) / 32));
-  ki::launch(k_mc_update<T>, g, 256, 0, s, x, nc, Um, nb, M, nr, N, mask);
+  ki::launch(k_mc_final<T>, g, 256, 0, s, x, nc, Dw, DU, nb, M, nr, N, mask);
 }
 
 // x(allskel, :) = M(0:nr, :), alpha (row-major nb x nc) = M(nr:, :)
@@ -3536,7 +3592,10 @@ __global__ void k_zero_rows(T* X, int nc, const unsigned char* mask, int N) {
 // keeps na x nc accumulators per block: borders up to 4,096 products use
 // it, wider ones the split-K GEMM.
 constexpr int kRedWideChunk = 16384;
-inline bool reduce_is_narrow(int na, int nc) { return (long)na * nc <= 16 * 256; }
+// (the staged rows, 32 x (na + nc) values, stay within 100 KB of shared memory)
+inline bool reduce_is_narrow(int na, int nc) {
+  return (long)na * nc <= 16 * 256 && na + nc <= 384;
+}
 
 // Elements of the partial-sum buffer reduce_rows takes for (na, nc).
 inline size_t reduce_rows_elems(int N, int na, int nc) {
@@ -3557,10 +3616,18 @@ void reduce_rows(Factorization<T>& F, const T* A, int na, T* B, int nc, T* out, 
   T* partial = sc.take(reduce_rows_elems(N, na, nc));
   if (reduce_is_narrow(na, nc)) {
     const int parts = (N + kRedRows - 1) / kRedRows;
-    size_t sm = sizeof(T) * 32 * (size_t)(na + nc);
-    if (sm > 48 * 1024)
-      KI_CUDA(cudaFuncSetAttribute(k_reduce_partial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    ki::launch(k_reduce_partial<T>, parts, 256, sm, s, A, na, (const T*)B, nc, N, F.d_is_skel, partial);
+    const int lda = (na + 3) & ~3, ldb = (nc + 1) & ~1;
+    if ((lda / 4) * (ldb / 2) <= 2 * 256) {
+      const size_t sm = sizeof(T) * 32 * (size_t)(lda + ldb);   // <= 32 x 4,100 values
+      if (sm > 48 * 1024)
+        KI_CUDA(cudaFuncSetAttribute(k_reduce_tiled<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      ki::launch(k_reduce_tiled<T>, parts, 256, sm, s, A, na, (const T*)B, nc, N, F.d_is_skel, partial);
+    } else {
+      size_t sm = sizeof(T) * 32 * (size_t)(na + nc);
+      if (sm > 48 * 1024)
+        KI_CUDA(cudaFuncSetAttribute(k_reduce_partial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      ki::launch(k_reduce_partial<T>, parts, 256, sm, s, A, na, (const T*)B, nc, N, F.d_is_skel, partial);
+    }
     ki::launch(k_reduce_final<T>, std::max(1, (na * nc + 255) / 256), 256, 0, s, (const T*)partial, parts,
                na * nc, out);
     KI_CUDA(cudaGetLastError());
@@ -5015,7 +5082,9 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
         T* corr = (T*)F->alloc(Tsz * (size_t)nb * nb);
         {
           Scratch<T> sc(s);
-          T* dD = sc.take((size_t)N * nb);
+          // D^-1 U~ is kept: the solve forms its redundant rows' result from it
+          T* dD = (T*)F->alloc(Tsz * (size_t)N * nb);
+          F->d_DinvU = dD;
           KI_CUDA(cudaMemcpyAsync(dD, F->d_Umod, Tsz * (size_t)N * nb, cudaMemcpyDeviceToDevice, s));
           F->stage_begin("border_Dinv", 0, 0);
           launch_diag_all<T>(*F, dD, nb, s);
@@ -5144,18 +5213,17 @@ static void solve_core(Factorization<T>& F, T* d_x, int ncols, T* d_alpha, const
       d_x, ncols, F.d_root_idx, nr, t, nb, ncols, M, d_g);
   dense_lu_solve<T>(F.d_root_lu, ns, F.d_root_piv, M, ns, ncols, false, s);
   se();
+  // redundant rows: D^-1 (w - U~_r alpha) = D^-1 w - (D^-1 U~)_r alpha
   sb("border_update");
   if (nb <= 64) {
-    mc_update<T>(d_x, ncols, F.d_Umod, nb, M, nr, N, F.d_is_skel, s);   // w - U~_r alpha
+    mc_final<T>(d_x, ncols, Dw, F.d_DinvU, nb, M, nr, N, F.d_is_skel, s);
   } else {
-    // x (DOF-major = column-major ncols x N) -= alpha^T U~^T; skeleton rows
-    // are overwritten afterwards, so they need no mask
-    gemm<T>(s, ncols, N, nb, T(-1), M + nr, ns, true, F.d_Umod, nb, false, T(1), d_x, ncols);
+    // x (DOF-major = column-major ncols x N) = Dw - alpha^T (D^-1 U~)^T;
+    // skeleton rows are overwritten afterwards, so they need no mask
+    KI_CUDA(cudaMemcpyAsync(d_x, Dw, sizeof(T) * (size_t)N * ncols, cudaMemcpyDeviceToDevice, s));
+    gemm<T>(s, ncols, N, nb, T(-1), M + nr, ns, true, F.d_DinvU, nb, false, T(1), d_x, ncols);
   }
   KI_CUDA(cudaGetLastError());
-  se();
-  sb_diag("border_diag");
-  launch_diag_all<T>(F, d_x, ncols, s);
   se();
   ki::launch(k_mc_finish<T>, std::max(1, std::min(4096, (ns * ncols + 255) / 256)), 256, 0, s,
       d_x, ncols, F.d_root_idx, M, nr, nb, d_alpha);

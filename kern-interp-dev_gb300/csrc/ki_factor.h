@@ -129,6 +129,7 @@ struct Factorization {
   // bordered data (multiply connected)
   T* d_Umod = nullptr;        // N x nb, DOF-major: swept U
   T* d_PsiTmod = nullptr;     // N x nb, DOF-major: swept Psi^T
+  T* d_DinvU = nullptr;       // N x nb, DOF-major: D^-1 U~ on the redundant rows
   unsigned char* d_is_skel = nullptr;  // N flags
   int* d_err = nullptr;       // device status word
   // statistics
