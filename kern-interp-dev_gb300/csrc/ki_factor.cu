@@ -2713,6 +2713,20 @@ enum SweepMode : int {
   kDiag = 4,       // x_r <- X^-1 x_r
 };
 
+// Asynchronous global -> shared copy of one 4- or 8-byte element (cp.async,
+// L1-allocating: the only form for copies under 16 bytes); completed by
+// cp_async_wait_all, then a barrier makes the data visible to the CTA.
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* dst, const T* src) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(tc::smem_u32(dst)), "l"(src),
+               "n"((int)sizeof(T))
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 // x is DOF-major: row = DOF, ld = ldx; a CTA handles one box and a chunk of
 // `cw` columns starting at blockIdx.y * cw.
 // x_r <- X_rr^-1 x_r for one box's redundant rows (n x nc column-major block
@@ -2768,22 +2782,55 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
   // column.
   const int ld = n | 1;
   T* ms = sx + 2 * (size_t)ld * cw;
-  auto stage = [&](const T* g, int count) -> const T* {
+  // stage_mats 2: every factor matrix the mode uses is copied in up front,
+  // together with the box's rows, by asynchronous copies that are all in
+  // flight at once (one global-memory latency per box instead of one per
+  // phase); stage_mats 1: one matrix at a time, before its phase
+  const T* pre[3] = {nullptr, nullptr, nullptr};   // staged Tm / L-or-U / Xi
+  if (stage_mats == 2) {
+    for (int idx = threadIdx.x; idx < n * nc; idx += blockDim.x) {
+      int i = idx / nc, c = idx % nc;
+      cp_async_elem(sx + i + (size_t)ld * c, x + (size_t)t.pact[i] * ldx + c0 + c);
+    }
+    const T* src[3] = {nullptr, nullptr, nullptr};
+    int cnt[3] = {0, 0, 0};
+    if (mode != kDiag) {
+      src[0] = t.Tm;
+      cnt[0] = k * r;
+      src[1] = (mode == kPsi || mode == kDown) ? t.U : t.L;
+      cnt[1] = k * r;
+    }
+    if ((mode == kUpDiag || mode == kDiag) && t.Xi) {
+      src[2] = t.Xi;
+      cnt[2] = r * r;
+    }
+    T* dst = ms;
+    for (int q = 0; q < 3; q++) {
+      if (!src[q]) continue;
+      for (int e = threadIdx.x; e < cnt[q]; e += blockDim.x) cp_async_elem(dst + e, src[q] + e);
+      pre[q] = dst;
+      dst += cnt[q];
+    }
+    cp_async_wait_all();
+  } else {
+    for (int idx = threadIdx.x; idx < n * nc; idx += blockDim.x) {
+      int i = idx / nc, c = idx % nc;
+      sx[i + (size_t)ld * c] = x[(size_t)t.pact[i] * ldx + c0 + c];
+    }
+  }
+  __syncthreads();
+  auto stage = [&](const T* g, int count, int q) -> const T* {
+    if (stage_mats == 2) return pre[q];
     if (!stage_mats) return g;
     for (int e = threadIdx.x; e < count; e += blockDim.x) ms[e] = g[e];
     __syncthreads();
     return ms;
   };
-  for (int idx = threadIdx.x; idx < n * nc; idx += blockDim.x) {
-    int i = idx / nc, c = idx % nc;
-    sx[i + (size_t)ld * c] = x[(size_t)t.pact[i] * ldx + c0 + c];
-  }
-  __syncthreads();
   T* xs = sx;
   T* xr = sx + k;
   if (mode == kUpDiag || mode == kUp || mode == kPsi) {
     // x_r -= T^T x_s
-    const T* Tm = stage(t.Tm, k * r);
+    const T* Tm = stage(t.Tm, k * r, 0);
     for (int idx = threadIdx.x; idx < r * nc; idx += blockDim.x) {
       int i = idx % r, c = idx / r;
       T acc = T(0);
@@ -2793,7 +2840,7 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
     }
     __syncthreads();
     // x_s -= L x_r   or   x_s -= U^T x_r
-    const T* M = stage(mode == kPsi ? t.U : t.L, k * r);
+    const T* M = stage(mode == kPsi ? t.U : t.L, k * r, 1);
     for (int idx = threadIdx.x; idx < k * nc; idx += blockDim.x) {
       int l = idx % k, c = idx / k;
       T acc = T(0);
@@ -2807,10 +2854,10 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
     }
     __syncthreads();
     if (mode == kUpDiag)
-      diag_solve(t, xr, ld, nc, sx + (size_t)ld * nc, t.Xi ? stage(t.Xi, r * r) : nullptr);
+      diag_solve(t, xr, ld, nc, sx + (size_t)ld * nc, t.Xi ? stage(t.Xi, r * r, 2) : nullptr);
   } else if (mode == kDown) {
     // x_r -= U x_s
-    const T* U = stage(t.U, r * k);
+    const T* U = stage(t.U, r * k, 1);
     for (int idx = threadIdx.x; idx < r * nc; idx += blockDim.x) {
       int i = idx % r, c = idx / r;
       T acc = T(0);
@@ -2819,7 +2866,7 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
     }
     __syncthreads();
     // x_s -= T x_r
-    const T* Tm = stage(t.Tm, k * r);
+    const T* Tm = stage(t.Tm, k * r, 0);
     for (int idx = threadIdx.x; idx < k * nc; idx += blockDim.x) {
       int l = idx % k, c = idx / k;
       T acc = T(0);
@@ -2828,7 +2875,7 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
     }
     __syncthreads();
   } else if (mode == kDiag) {
-    diag_solve(t, xr, ld, nc, sx + (size_t)ld * nc, t.Xi ? stage(t.Xi, r * r) : nullptr);
+    diag_solve(t, xr, ld, nc, sx + (size_t)ld * nc, t.Xi ? stage(t.Xi, r * r, 2) : nullptr);
   }
   __syncthreads();
   const int lo = mode == kDiag ? k : 0;   // the diagonal solve changes x_r only
@@ -3504,8 +3551,9 @@ void launch_diag_all(Factorization<T>& F, T* x, int ncols, cudaStream_t s) {
     dim3 grid(b[1], (ncols + cw - 1) / cw);
     size_t sm = 2 * sizeof(T) * (size_t)ldmax * cw;
     if (sm > 200 * 1024) throw std::runtime_error("box too large for the sweep kernel");
+    // kDiag stages X^-1 alone (b[3]: the largest r^2), all at once
     const size_t mats = sweep_stage_bytes<T>(b[3]);
-    const int staged = sm + mats <= kSweepStageCap;
+    const int staged = sm + mats <= kSweepStageCap ? 2 : 0;
     if (staged) sm += mats;
     if (sm > 48 * 1024)
       KI_CUDA(cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
@@ -3532,9 +3580,10 @@ void launch_sweep(Factorization<T>& F, int l, int mode, T* x, int ncols, cudaStr
   dim3 grid(LF.n_comp, (ncols + cw - 1) / cw);
   size_t sm = 2 * sizeof(T) * (size_t)ldmax * cw;
   if (sm > 200 * 1024) throw std::runtime_error("box too large for the sweep kernel");
+  const size_t all = sweep_stage_bytes<T>(LF.max_all);
   const size_t mats = sweep_stage_bytes<T>(LF.max_mat);
-  const int staged = sm + mats <= kSweepStageCap;
-  if (staged) sm += mats;
+  const int staged = sm + all <= kSweepStageCap ? 2 : (sm + mats <= kSweepStageCap ? 1 : 0);
+  if (staged) sm += staged == 2 ? all : mats;
   if (sm > 48 * 1024)
     KI_CUDA(cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   const int bucket = sweep_bucket(sizeof(T) == 8, LF.max_n);
@@ -4731,6 +4780,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       F->n_redundant += r;
       LF.max_n = std::max(LF.max_n, n);
       LF.max_mat = std::max(LF.max_mat, std::max(r * r, k * r));
+      LF.max_all = std::max(LF.max_all, 2 * k * r + r * r);
       LF.sum_kr += (double)k * r;
       LF.sum_r2 += (double)r * r;
       LF.sum_n += n;
@@ -4780,6 +4830,7 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
       F->n_redundant += r;
       LF.max_n = std::max(LF.max_n, n);
       LF.max_mat = std::max(LF.max_mat, std::max(r * r, k * r));
+      LF.max_all = std::max(LF.max_all, 2 * k * r + r * r);
       LF.sum_kr += (double)k * r;
       LF.sum_r2 += (double)r * r;
       LF.sum_n += n;

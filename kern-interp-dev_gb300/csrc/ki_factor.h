@@ -41,6 +41,7 @@ struct LevelFactor {
   void* d_tasks = nullptr; // device array of per-box sweep descriptors
   int max_n = 0;           // largest active set among them
   int max_mat = 0;         // largest factor matrix among them: max(r^2, k r) entries
+  int max_all = 0;         // largest 2 k r + r^2 (every factor matrix of a box)
   double sum_kr = 0, sum_r2 = 0, sum_n = 0, sum_r = 0;   // over the compressed boxes (sweep work)
 };
 
