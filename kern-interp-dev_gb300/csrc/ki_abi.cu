@@ -442,6 +442,128 @@ struct DevBuf {
 
 int grid_for(size_t n) { return (int)std::min<size_t>(4096, (n + 255) / 256 + 1); }
 
+// 3D Laplace dense apply y = K x over all boundary DOFs in FP32-pair
+// arithmetic (the FP32 pipes run at 64 x the FP64 rate on this part): the
+// entry -w_s/(4 pi) (r.n_s)/|r|^3, r = t - s (Kernel::three_d_laplace,
+// kern_interp/kernel/kernel.cpp:104-121), from coordinates split hi + lo;
+// 1/|r| by one Newton step, y (1 + e/2) with e = 1 - |r|^2 y^2 formed
+// exactly enough from the FP32 estimate y (relative error ~2^-23 -> ~2^-46);
+// products, dot products and sums carry their rounding errors in the low
+// parts.  Each entry keeps ~1e-13 relative accuracy (less where r.n_s
+// cancels: ~2^-48 of |r| |n_s| absolute), far below what a refinement
+// residual needs.  A coincident pair takes the source's diagonal entry.
+// One thread per target DOF, kP3Cols columns per blockIdx.y, sources staged
+// per tile in shared memory, blockIdx.z a chunk of the sources (partials
+// reduced by k_chunk_reduce in a fixed order).
+constexpr int kP3Threads = 128;
+constexpr int kP3Tile = 128;
+constexpr int kP3Cols = 4;
+
+__device__ __forceinline__ void pair_mul(float ah, float al, float bh, float bl, float& h,
+                                         float& l) {
+  h = __fmul_rn(ah, bh);
+  l = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, __fmaf_rn(ah, bh, -h)));
+}
+
+__global__ void __launch_bounds__(kP3Threads) k_dense_apply3_pair(
+    ki::Points<double> P, int n_points, const double* x, int ldx, int ncols, double* out, int ldo,
+    size_t chunk_stride, int chunk_pts) {
+  __shared__ float4 s_ph[kP3Tile], s_pl[kP3Tile];   // source coordinates hi, lo
+  __shared__ float4 s_nh[kP3Tile], s_nl[kP3Tile];   // -w/(4 pi) n_s hi, lo
+  __shared__ float2 s_dg[kP3Tile];                  // diagonal entry
+  __shared__ float2 s_x[kP3Cols][kP3Tile];          // densities
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c0 = blockIdx.y * kP3Cols;
+  const int nc = min(kP3Cols, ncols - c0);
+  const int s_lo = blockIdx.z * chunk_pts, s_hi = min(n_points, s_lo + chunk_pts);
+  const int tt = t < n_points ? t : 0;
+  const float2 tx = ki::split_pair(P.x[tt]), ty = ki::split_pair(P.y[tt]),
+               tz = ki::split_pair(P.z[tt]);
+  float ah[kP3Cols], al[kP3Cols];
+  for (int c = 0; c < kP3Cols; c++) ah[c] = al[c] = 0.f;
+  constexpr double kC = -1.0 / (4.0 * ki::kPi);
+  for (int base = s_lo; base < s_hi; base += kP3Tile) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < kP3Tile; i += blockDim.x) {
+      const int sp = base + i;
+      if (sp < s_hi) {
+        const float2 a = ki::split_pair(P.x[sp]), b = ki::split_pair(P.y[sp]),
+                     d = ki::split_pair(P.z[sp]);
+        s_ph[i] = make_float4(a.x, b.x, d.x, 0.f);
+        s_pl[i] = make_float4(a.y, b.y, d.y, 0.f);
+        const double cw = kC * P.w[sp];
+        const float2 u = ki::split_pair(cw * P.nx[sp]), v = ki::split_pair(cw * P.ny[sp]),
+                     q = ki::split_pair(cw * P.nz[sp]);
+        s_nh[i] = make_float4(u.x, v.x, q.x, 0.f);
+        s_nl[i] = make_float4(u.y, v.y, q.y, 0.f);
+        s_dg[i] = ki::split_pair(P.diag ? P.diag[sp] : 0.0);
+        for (int c = 0; c < kP3Cols; c++)
+          s_x[c][i] = ki::split_pair(c < nc ? x[sp + (size_t)ldx * (c0 + c)] : 0.0);
+      }
+    }
+    __syncthreads();
+    if (t >= n_points) continue;
+    const int lim = min(kP3Tile, s_hi - base);
+    for (int i = 0; i < lim; i++) {
+      const float4 ph = s_ph[i], pl = s_pl[i];
+      // r = t - s as pairs
+      float dxh, dxl, dyh, dyl, dzh, dzl;
+      ki::two_diff(tx.x, ph.x, dxh, dxl);
+      ki::two_diff(ty.x, ph.y, dyh, dyl);
+      ki::two_diff(tz.x, ph.z, dzh, dzl);
+      ki::fast_two_sum(dxh, __fadd_rn(dxl, __fsub_rn(tx.y, pl.x)), dxh, dxl);
+      ki::fast_two_sum(dyh, __fadd_rn(dyl, __fsub_rn(ty.y, pl.y)), dyh, dyl);
+      ki::fast_two_sum(dzh, __fadd_rn(dzl, __fsub_rn(tz.y, pl.z)), dzh, dzl);
+      // |r|^2
+      const float a = __fmul_rn(dxh, dxh), b = __fmul_rn(dyh, dyh), d = __fmul_rn(dzh, dzh);
+      float s1h, s1l, r2h, r2l;
+      ki::two_sum(a, b, s1h, s1l);
+      ki::two_sum(s1h, d, r2h, r2l);
+      float lo = __fadd_rn(__fmaf_rn(dxh, dxh, -a), __fadd_rn(__fmaf_rn(dyh, dyh, -b),
+                                                             __fmaf_rn(dzh, dzh, -d)));
+      lo = __fmaf_rn(2.f * dxh, dxl, __fmaf_rn(2.f * dyh, dyl, __fmaf_rn(2.f * dzh, dzl, lo)));
+      r2l = __fadd_rn(r2l, __fadd_rn(s1l, lo));
+      ki::fast_two_sum(r2h, r2l, r2h, r2l);
+      float kh, kl;
+      if (r2h == 0.f) {
+        kh = s_dg[i].x;
+        kl = s_dg[i].y;
+      } else {
+        // 1/|r|: y0 (FP32 estimate), then y0 + y0 e / 2 with e = 1 - r2 y0^2
+        const float y0 = rsqrtf(r2h);
+        const float p = __fmul_rn(y0, y0), pe = __fmaf_rn(y0, y0, -p);
+        const float q = __fmul_rn(r2h, p);
+        const float qe = __fmaf_rn(r2h, pe, __fmaf_rn(r2l, p, __fmaf_rn(r2h, p, -q)));
+        const float e = __fsub_rn(__fsub_rn(1.f, q), qe);
+        float yh, yl;
+        ki::fast_two_sum(y0, __fmul_rn(__fmul_rn(0.5f, y0), e), yh, yl);
+        // 1/|r|^3
+        float y2h, y2l, y3h, y3l;
+        pair_mul(yh, yl, yh, yl, y2h, y2l);
+        pair_mul(y2h, y2l, yh, yl, y3h, y3l);
+        // r . (-w n / 4 pi)
+        const float4 nh = s_nh[i], nl = s_nl[i];
+        float m1h, m1l, m2h, m2l, m3h, m3l;
+        pair_mul(dxh, dxl, nh.x, nl.x, m1h, m1l);
+        pair_mul(dyh, dyl, nh.y, nl.y, m2h, m2l);
+        pair_mul(dzh, dzl, nh.z, nl.z, m3h, m3l);
+        float sh, sl, uh, ul;
+        ki::two_sum(m1h, m2h, sh, sl);
+        ki::two_sum(sh, m3h, uh, ul);
+        ul = __fadd_rn(ul, __fadd_rn(sl, __fadd_rn(m1l, __fadd_rn(m2l, m3l))));
+        ki::fast_two_sum(uh, ul, uh, ul);
+        pair_mul(uh, ul, y3h, y3l, kh, kl);
+      }
+      const float2 kv = make_float2(kh, kl);
+      for (int c = 0; c < kP3Cols; c++) ki::pair_fma(ah[c], al[c], kv, s_x[c][i]);
+    }
+  }
+  if (t < n_points) {
+    double* o = out + chunk_stride * blockIdx.z;
+    for (int c = 0; c < nc; c++) o[t + (size_t)ldo * (c0 + c)] = (double)ah[c] + (double)al[c];
+  }
+}
+
 // y (nrows x ncols, ldy) = dense FP64 product for the given targets (see
 // k_dense_apply): all boundary DOFs (rows == tg == null, nrows = N), listed
 // DOFs, or domain points.  Few target rows get the source range split into
@@ -452,6 +574,36 @@ void dense_product(const ki::Points<double>& P, int n_points, int sol_dim, const
                    const double* tg, cudaStream_t s) {
   const int N = (rows || tg) ? nrows : n_points * sol_dim;
   if (N == 0 || ncols == 0) return;
+  // 3D Laplace over all boundary DOFs: the FP32-pair kernel (KI_DENSE3=fp64
+  // keeps the FP64 one)
+  static const bool fp64_only = [] {
+    const char* e = std::getenv("KI_DENSE3");
+    return e && std::string(e) == "fp64";
+  }();
+  if (P.dim == 3 && sol_dim == 1 && !rows && !tg && !fp64_only) {
+    const int gx = (N + kP3Threads - 1) / kP3Threads;
+    const int gy = (ncols + kP3Cols - 1) / kP3Cols;
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess)
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int chunks = std::max(1, std::min((8 * sms + gx * gy - 1) / (gx * gy), n_points / kP3Tile));
+    chunks = std::min(chunks, 1024);
+    const int chunk_pts = (n_points + chunks - 1) / chunks;
+    chunks = (n_points + chunk_pts - 1) / chunk_pts;
+    if (chunks == 1) {
+      ki::launch(k_dense_apply3_pair, dim3(gx, gy, 1), kP3Threads, 0, s, P, n_points, x, ldx,
+                 ncols, y, ldy, (size_t)0, chunk_pts);
+      KI_CHECK_CUDA(cudaGetLastError());
+      return;
+    }
+    const size_t stride = (size_t)N * ncols;
+    DevBuf<double> part(stride * chunks, s);
+    ki::launch(k_dense_apply3_pair, dim3(gx, gy, chunks), kP3Threads, 0, s, P, n_points, x, ldx,
+               ncols, part.p, N, stride, chunk_pts);
+    ki::launch(k_chunk_reduce, grid_for(stride), 256, 0, s, part.p, chunks, N, ncols, y, ldy);
+    KI_CHECK_CUDA(cudaGetLastError());
+    return;
+  }
   const int gx = (N + kApplyThreads - 1) / kApplyThreads;
   const int gy = (ncols + kApplyCols - 1) / kApplyCols;
   int dev = 0, sms = 152;

@@ -109,3 +109,17 @@ def test_refined_3d_and_device_entry(pkg):
     assert np.abs(x2 - mu).max() <= 1e-14 * np.abs(mu).max()
     res = np.abs(fac.apply(mu) - f).max() / np.abs(f).max()
     assert res <= 1e-10
+
+
+def test_3d_laplace_apply_in_pair_arithmetic_matches_the_fp64_matrix(pkg, oracle_mod):
+    """The 3D Laplace residual operator runs in FP32-pair arithmetic (the FP32
+    pipes, ~1e-13 per entry): against the FP64 dense matrix of the oracle
+    (the same row-sum diagonal), on several right-hand sides."""
+    g = pkg.geometry
+    prob = g.ellipsoid(3000, (1.0, 0.7, 0.5))
+    K = oracle_mod.dense_matrix(prob)
+    fac = pkg.Factor(prob.points, prob.normals, prob.weights, None, id_tol=1e-6)
+    x = np.random.default_rng(2).standard_normal((prob.n, 5))
+    y = fac.apply(x)
+    ref = K @ x
+    assert np.abs(y - ref).max() <= 1e-11 * np.abs(ref).max(), np.abs(y - ref).max()
