@@ -459,12 +459,6 @@ constexpr int kP3Threads = 128;
 constexpr int kP3Tile = 128;
 constexpr int kP3Cols = 4;
 
-__device__ __forceinline__ void pair_mul(float ah, float al, float bh, float bl, float& h,
-                                         float& l) {
-  h = __fmul_rn(ah, bh);
-  l = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, __fmaf_rn(ah, bh, -h)));
-}
-
 __global__ void __launch_bounds__(kP3Threads) k_dense_apply3_pair(
     ki::Points<double> P, int n_points, const double* x, int ldx, int ncols, double* out, int ldo,
     size_t chunk_stride, int chunk_pts) {
@@ -505,54 +499,10 @@ __global__ void __launch_bounds__(kP3Threads) k_dense_apply3_pair(
     if (t >= n_points) continue;
     const int lim = min(kP3Tile, s_hi - base);
     for (int i = 0; i < lim; i++) {
-      const float4 ph = s_ph[i], pl = s_pl[i];
-      // r = t - s as pairs
-      float dxh, dxl, dyh, dyl, dzh, dzl;
-      ki::two_diff(tx.x, ph.x, dxh, dxl);
-      ki::two_diff(ty.x, ph.y, dyh, dyl);
-      ki::two_diff(tz.x, ph.z, dzh, dzl);
-      ki::fast_two_sum(dxh, __fadd_rn(dxl, __fsub_rn(tx.y, pl.x)), dxh, dxl);
-      ki::fast_two_sum(dyh, __fadd_rn(dyl, __fsub_rn(ty.y, pl.y)), dyh, dyl);
-      ki::fast_two_sum(dzh, __fadd_rn(dzl, __fsub_rn(tz.y, pl.z)), dzh, dzl);
-      // |r|^2
-      const float a = __fmul_rn(dxh, dxh), b = __fmul_rn(dyh, dyh), d = __fmul_rn(dzh, dzh);
-      float s1h, s1l, r2h, r2l;
-      ki::two_sum(a, b, s1h, s1l);
-      ki::two_sum(s1h, d, r2h, r2l);
-      float lo = __fadd_rn(__fmaf_rn(dxh, dxh, -a), __fadd_rn(__fmaf_rn(dyh, dyh, -b),
-                                                             __fmaf_rn(dzh, dzh, -d)));
-      lo = __fmaf_rn(2.f * dxh, dxl, __fmaf_rn(2.f * dyh, dyl, __fmaf_rn(2.f * dzh, dzl, lo)));
-      r2l = __fadd_rn(r2l, __fadd_rn(s1l, lo));
-      ki::fast_two_sum(r2h, r2l, r2h, r2l);
       float kh, kl;
-      if (r2h == 0.f) {
-        kh = s_dg[i].x;
+      if (!ki::pair_dipole3(tx, ty, tz, s_ph[i], s_pl[i], s_nh[i], s_nl[i], kh, kl)) {
+        kh = s_dg[i].x;   // coincident pair: the source's diagonal entry
         kl = s_dg[i].y;
-      } else {
-        // 1/|r|: y0 (FP32 estimate), then y0 + y0 e / 2 with e = 1 - r2 y0^2
-        const float y0 = rsqrtf(r2h);
-        const float p = __fmul_rn(y0, y0), pe = __fmaf_rn(y0, y0, -p);
-        const float q = __fmul_rn(r2h, p);
-        const float qe = __fmaf_rn(r2h, pe, __fmaf_rn(r2l, p, __fmaf_rn(r2h, p, -q)));
-        const float e = __fsub_rn(__fsub_rn(1.f, q), qe);
-        float yh, yl;
-        ki::fast_two_sum(y0, __fmul_rn(__fmul_rn(0.5f, y0), e), yh, yl);
-        // 1/|r|^3
-        float y2h, y2l, y3h, y3l;
-        pair_mul(yh, yl, yh, yl, y2h, y2l);
-        pair_mul(y2h, y2l, yh, yl, y3h, y3l);
-        // r . (-w n / 4 pi)
-        const float4 nh = s_nh[i], nl = s_nl[i];
-        float m1h, m1l, m2h, m2l, m3h, m3l;
-        pair_mul(dxh, dxl, nh.x, nl.x, m1h, m1l);
-        pair_mul(dyh, dyl, nh.y, nl.y, m2h, m2l);
-        pair_mul(dzh, dzl, nh.z, nl.z, m3h, m3l);
-        float sh, sl, uh, ul;
-        ki::two_sum(m1h, m2h, sh, sl);
-        ki::two_sum(sh, m3h, uh, ul);
-        ul = __fadd_rn(ul, __fadd_rn(sl, __fadd_rn(m1l, __fadd_rn(m2l, m3l))));
-        ki::fast_two_sum(uh, ul, uh, ul);
-        pair_mul(uh, ul, y3h, y3l, kh, kl);
       }
       const float2 kv = make_float2(kh, kl);
       for (int c = 0; c < kP3Cols; c++) ki::pair_fma(ah[c], al[c], kv, s_x[c][i]);

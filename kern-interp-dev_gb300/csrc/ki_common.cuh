@@ -225,6 +225,65 @@ __device__ __forceinline__ void fast_two_sum(float a, float b, float& hi, float&
   lo = __fsub_rn(b, __fsub_rn(hi, a));
 }
 
+// h + l = (ah + al)(bh + bl) to ~2^-47 relative: the high product split
+// exactly by an fma, the cross terms added to its error.
+__device__ __forceinline__ void pair_mul(float ah, float al, float bh, float bl, float& h,
+                                         float& l) {
+  h = __fmul_rn(ah, bh);
+  l = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, __fmaf_rn(ah, bh, -h)));
+}
+
+// The 3D double-layer pair term (r . c) / |r|^3, r = t - s, in FP32-pair
+// arithmetic: t = (tx, ty, tz) and s = (sh + sl) as hi/lo pairs, c = ch + cl
+// (the source's normal scaled by its weight and -1/(4 pi)).  r by
+// two-differences of the hi parts plus the lo differences; |r|^2 with exact
+// squares; 1/|r| by one Newton step y0 (1 + e/2), e = 1 - |r|^2 y0^2, from
+// the FP32 estimate y0 (relative error ~2^-23 -> ~2^-46); the dot product
+// and the products with their rounding errors carried.  ~1e-13 relative
+// (where r . c cancels, ~2^-48 of |r| |c| absolute).  Returns false, with
+// nothing written, when r is exactly zero.
+__device__ __forceinline__ bool pair_dipole3(float2 tx, float2 ty, float2 tz, float4 sh, float4 sl,
+                                             float4 ch, float4 cl, float& kh, float& kl) {
+  float dxh, dxl, dyh, dyl, dzh, dzl;
+  two_diff(tx.x, sh.x, dxh, dxl);
+  two_diff(ty.x, sh.y, dyh, dyl);
+  two_diff(tz.x, sh.z, dzh, dzl);
+  fast_two_sum(dxh, __fadd_rn(dxl, __fsub_rn(tx.y, sl.x)), dxh, dxl);
+  fast_two_sum(dyh, __fadd_rn(dyl, __fsub_rn(ty.y, sl.y)), dyh, dyl);
+  fast_two_sum(dzh, __fadd_rn(dzl, __fsub_rn(tz.y, sl.z)), dzh, dzl);
+  const float a = __fmul_rn(dxh, dxh), b = __fmul_rn(dyh, dyh), d = __fmul_rn(dzh, dzh);
+  float s1h, s1l, r2h, r2l;
+  two_sum(a, b, s1h, s1l);
+  two_sum(s1h, d, r2h, r2l);
+  float lo = __fadd_rn(__fmaf_rn(dxh, dxh, -a),
+                       __fadd_rn(__fmaf_rn(dyh, dyh, -b), __fmaf_rn(dzh, dzh, -d)));
+  lo = __fmaf_rn(2.f * dxh, dxl, __fmaf_rn(2.f * dyh, dyl, __fmaf_rn(2.f * dzh, dzl, lo)));
+  r2l = __fadd_rn(r2l, __fadd_rn(s1l, lo));
+  fast_two_sum(r2h, r2l, r2h, r2l);
+  if (r2h == 0.f) return false;
+  const float y0 = rsqrtf(r2h);
+  const float p = __fmul_rn(y0, y0), pe = __fmaf_rn(y0, y0, -p);
+  const float q = __fmul_rn(r2h, p);
+  const float qe = __fmaf_rn(r2h, pe, __fmaf_rn(r2l, p, __fmaf_rn(r2h, p, -q)));
+  const float e = __fsub_rn(__fsub_rn(1.f, q), qe);
+  float yh, yl;
+  fast_two_sum(y0, __fmul_rn(__fmul_rn(0.5f, y0), e), yh, yl);
+  float y2h, y2l, y3h, y3l;
+  pair_mul(yh, yl, yh, yl, y2h, y2l);
+  pair_mul(y2h, y2l, yh, yl, y3h, y3l);
+  float m1h, m1l, m2h, m2l, m3h, m3l;
+  pair_mul(dxh, dxl, ch.x, cl.x, m1h, m1l);
+  pair_mul(dyh, dyl, ch.y, cl.y, m2h, m2l);
+  pair_mul(dzh, dzl, ch.z, cl.z, m3h, m3l);
+  float uh, ul, vh, vl;
+  two_sum(m1h, m2h, uh, ul);
+  two_sum(uh, m3h, vh, vl);
+  vl = __fadd_rn(vl, __fadd_rn(ul, __fadd_rn(m1l, __fadd_rn(m2l, m3l))));
+  fast_two_sum(vh, vl, vh, vl);
+  pair_mul(vh, vl, y3h, y3l, kh, kl);
+  return true;
+}
+
 // Squared distance |t - s|^2 of two points given as FP32 pairs
 // (hi x, hi y, lo x, lo y), as a pair (value r2.x + r2.y).
 __device__ __forceinline__ float2 pair_dist2(const float4& t, const float4& s) {

@@ -3078,6 +3078,70 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag3(const double* pts, const
   }
 }
 
+// The 3D Laplace row sums of k_diag3 in FP32-pair arithmetic (the pair term
+// of ki::pair_dipole3, ~1e-13 relative each; the FP32 pipes run at 64 x the
+// FP64 rate on this part).  blockIdx.y takes the sources of one chunk of
+// `chunk_pts` indices; each target's partial sum goes to part[y][t], and
+// k_diag3_finish adds the chunks in order.  A source that coincides with the
+// target is skipped.
+__global__ void __launch_bounds__(kDiagThreads) k_diag3_pair(const double* pts, const double* nrm,
+                                                             const double* w, int n_points,
+                                                             const int* grp_lo, const int* grp_hi,
+                                                             int chunk_pts, double* part) {
+  __shared__ float4 s_ph[kDiagTile], s_pl[kDiagTile], s_nh[kDiagTile], s_nl[kDiagTile];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool on = t < n_points;
+  const int tc = on ? t : n_points - 1;
+  const int z0 = blockIdx.y * chunk_pts, z1 = min(n_points, z0 + chunk_pts);
+  const int lo = max(grp_lo[tc], z0), hi = min(grp_hi[tc], z1);
+  const int t0 = blockIdx.x * blockDim.x, t1 = min(n_points, t0 + (int)blockDim.x) - 1;
+  const int blo = max(grp_lo[t0], z0), bhi = min(max(grp_hi[t0], grp_hi[t1]), z1);
+  const float2 tx = split_pair(pts[3 * (size_t)tc]), ty = split_pair(pts[3 * (size_t)tc + 1]),
+               tz = split_pair(pts[3 * (size_t)tc + 2]);
+  constexpr double kC = -1.0 / (4.0 * kPi);
+  float ah = 0.f, al = 0.f;
+  for (int base = blo; base < bhi; base += kDiagTile) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < kDiagTile; i += blockDim.x) {
+      const int p = base + i;
+      if (p < bhi) {
+        const float2 a = split_pair(pts[3 * (size_t)p]), b = split_pair(pts[3 * (size_t)p + 1]),
+                     c = split_pair(pts[3 * (size_t)p + 2]);
+        s_ph[i] = make_float4(a.x, b.x, c.x, 0.f);
+        s_pl[i] = make_float4(a.y, b.y, c.y, 0.f);
+        const double cw = kC * w[p];
+        const float2 u = split_pair(cw * nrm[3 * (size_t)p]),
+                     v = split_pair(cw * nrm[3 * (size_t)p + 1]),
+                     q = split_pair(cw * nrm[3 * (size_t)p + 2]);
+        s_nh[i] = make_float4(u.x, v.x, q.x, 0.f);
+        s_nl[i] = make_float4(u.y, v.y, q.y, 0.f);
+      }
+    }
+    __syncthreads();
+    const int i0 = max(0, lo - base), i1 = min(kDiagTile, hi - base);
+    for (int i = i0; i < i1; i++) {
+      if (base + i == t) continue;
+      float kh, kl;
+      if (!pair_dipole3(tx, ty, tz, s_ph[i], s_pl[i], s_nh[i], s_nl[i], kh, kl)) continue;
+      float sh, sl;
+      two_sum(ah, kh, sh, sl);
+      al = __fadd_rn(al, __fadd_rn(sl, kl));
+      ah = sh;
+    }
+  }
+  if (on) part[(size_t)blockIdx.y * n_points + t] = (double)ah + (double)al;
+}
+
+// out[t] = (1 on the outer surface, 0 on holes) - the chunks' row sums, added in order.
+__global__ void k_diag3_finish(const double* part, int nchunks, int n_points, int n_outer,
+                               double* out) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_points; t += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int z = 0; z < nchunks; z++) acc += part[(size_t)z * n_points + t];
+    out[t] = (t < n_outer ? 1.0 : 0.0) - acc;
+  }
+}
+
 template <typename T>
 __global__ void k_convert(const double* a, size_t n, T* b) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -3806,8 +3870,26 @@ std::unique_ptr<Factorization<T>> factorize(const Params& prm, int n_points, con
     KI_CUDA(cudaMemcpyAsync(d_g + n_points, ghi.data(), sizeof(int) * n_points, cudaMemcpyHostToDevice, s));
     F->d_diag64 = (double*)F->alloc(sizeof(double) * (size_t)dpp * n_points);
     F->stage_begin("diag3", (sd == 1 ? 20.0 : 80.0) * (double)n_points * n_points, 0);
-    ki::launch(k_diag3, (n_points + kDiagThreads - 1) / kDiagThreads, kDiagThreads, 0, s,
-        d_pts_in, d_nrm_in, d_w_in, n_points, d_g, d_g + n_points, n_outer, sd, F->d_diag64);
+    const int gx = (n_points + kDiagThreads - 1) / kDiagThreads;
+    const char* dmode = std::getenv("KI_DIAG3");
+    if (sd == 1 && !(dmode && std::string(dmode) == "fp64")) {
+      // Laplace: FP32-pair row sums, the sources split into chunks so that
+      // the grid covers the GPU (KI_DIAG3=fp64: the FP64 kernel)
+      int sms = 152, dev = 0;
+      if (cudaGetDevice(&dev) == cudaSuccess)
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      int chunks = std::max(1, std::min((8 * sms + gx - 1) / gx, n_points / kDiagTile));
+      const int chunk_pts = (n_points + chunks - 1) / chunks;
+      chunks = (n_points + chunk_pts - 1) / chunk_pts;
+      double* part = (double*)F->alloc(sizeof(double) * (size_t)chunks * n_points);
+      ki::launch(k_diag3_pair, dim3(gx, chunks), kDiagThreads, 0, s, d_pts_in, d_nrm_in, d_w_in,
+                 n_points, d_g, d_g + n_points, chunk_pts, part);
+      ki::launch(k_diag3_finish, std::min(2048, (n_points + 255) / 256), 256, 0, s, part, chunks,
+                 n_points, n_outer, F->d_diag64);
+    } else {
+      ki::launch(k_diag3, gx, kDiagThreads, 0, s, d_pts_in, d_nrm_in, d_w_in, n_points, d_g,
+                 d_g + n_points, n_outer, sd, F->d_diag64);
+    }
     F->stage_end();
     KI_CUDA(cudaGetLastError());
     // synchronize on the (host) group arrays before they go out of scope
