@@ -344,7 +344,12 @@ void dense_lu_solve(const T* LU, int n, const int* piv, T* B, int ldb, int nrhs,
   if (n == 0 || nrhs == 0) return;
   dim3 cb((nrhs + 127) / 128);
   const int cw = fused_solve_cols(nrhs);
-  if (!trans && fused_solve_smem<T>(n, cw) <= 160 * 1024) {
+  // the fused kernel streams all of L and U through each of its few CTAs:
+  // for factors over 16 MB (n > 2,048 in FP32) the multi-launch path, whose
+  // updates spread every block row over the GPU, is the faster one (a
+  // 7,656-row root solve with one right-hand side: 91 ms fused)
+  const bool small = (double)n * n * sizeof(T) <= 16.0 * 1024 * 1024;
+  if (!trans && small && fused_solve_smem<T>(n, cw) <= 160 * 1024) {
     KI_DENSE_CUDA(cudaFuncSetAttribute(k_lu_solve_fused<T>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
     ki::launch(k_lu_solve_fused<T>, (nrhs + cw - 1) / cw, 256, fused_solve_smem<T>(n, cw), s, LU, n, piv,
