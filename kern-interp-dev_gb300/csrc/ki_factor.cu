@@ -2739,15 +2739,13 @@ __device__ void diag_solve(const SweepTask<T>& t, T* xr, int n, int nc, T* tmp,
   const int r = t.n - t.k;
   if (t.Xi) {
     if (!Xi) Xi = t.Xi;
-    for (int idx = threadIdx.x; idx < r * nc; idx += blockDim.x) {
-      const int i = idx % r, c = idx / r;
+    cta_for_2d(r, nc, [&](int i, int c) {
       T acc = T(0);
       for (int j = 0; j < r; j++) acc += Xi[i + (size_t)r * j] * xr[j + (size_t)n * c];
-      tmp[idx] = acc;
-    }
+      tmp[i + (size_t)r * c] = acc;
+    });
     __syncthreads();
-    for (int idx = threadIdx.x; idx < r * nc; idx += blockDim.x)
-      xr[idx % r + (size_t)n * (idx / r)] = tmp[idx];
+    cta_for_2d(r, nc, [&](int i, int c) { xr[i + (size_t)n * c] = tmp[i + (size_t)r * c]; });
     __syncthreads();
   } else {
     cta_lu_solve_par<T>(r, t.X, r, t.piv, false, xr, n, nc);
@@ -2788,10 +2786,9 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
   // phase); stage_mats 1: one matrix at a time, before its phase
   const T* pre[3] = {nullptr, nullptr, nullptr};   // staged Tm / L-or-U / Xi
   if (stage_mats == 2) {
-    for (int idx = threadIdx.x; idx < n * nc; idx += blockDim.x) {
-      int i = idx / nc, c = idx % nc;
+    cta_for_2d(nc, n, [&](int c, int i) {
       cp_async_elem(sx + i + (size_t)ld * c, x + (size_t)t.pact[i] * ldx + c0 + c);
-    }
+    });
     const T* src[3] = {nullptr, nullptr, nullptr};
     int cnt[3] = {0, 0, 0};
     if (mode != kDiag) {
@@ -2813,10 +2810,9 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
     }
     cp_async_wait_all();
   } else {
-    for (int idx = threadIdx.x; idx < n * nc; idx += blockDim.x) {
-      int i = idx / nc, c = idx % nc;
+    cta_for_2d(nc, n, [&](int c, int i) {
       sx[i + (size_t)ld * c] = x[(size_t)t.pact[i] * ldx + c0 + c];
-    }
+    });
   }
   __syncthreads();
   auto stage = [&](const T* g, int count, int q) -> const T* {
@@ -2831,18 +2827,16 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
   if (mode == kUpDiag || mode == kUp || mode == kPsi) {
     // x_r -= T^T x_s
     const T* Tm = stage(t.Tm, k * r, 0);
-    for (int idx = threadIdx.x; idx < r * nc; idx += blockDim.x) {
-      int i = idx % r, c = idx / r;
+    cta_for_2d(r, nc, [&](int i, int c) {
       T acc = T(0);
       const T* tc = Tm + (size_t)k * i;
       for (int l = 0; l < k; l++) acc += tc[l] * xs[l + (size_t)ld * c];
       xr[i + (size_t)ld * c] -= acc;
-    }
+    });
     __syncthreads();
     // x_s -= L x_r   or   x_s -= U^T x_r
     const T* M = stage(mode == kPsi ? t.U : t.L, k * r, 1);
-    for (int idx = threadIdx.x; idx < k * nc; idx += blockDim.x) {
-      int l = idx % k, c = idx / k;
+    cta_for_2d(k, nc, [&](int l, int c) {
       T acc = T(0);
       if (mode == kPsi) {
         const T* uc = M + (size_t)r * l;
@@ -2851,38 +2845,36 @@ __global__ void k_sweep(const SweepTask<T>* tasks, T* x, int ldx, int ncols, int
         for (int i = 0; i < r; i++) acc += M[l + (size_t)k * i] * xr[i + (size_t)ld * c];
       }
       xs[l + (size_t)ld * c] -= acc;
-    }
+    });
     __syncthreads();
     if (mode == kUpDiag)
       diag_solve(t, xr, ld, nc, sx + (size_t)ld * nc, t.Xi ? stage(t.Xi, r * r, 2) : nullptr);
   } else if (mode == kDown) {
     // x_r -= U x_s
     const T* U = stage(t.U, r * k, 1);
-    for (int idx = threadIdx.x; idx < r * nc; idx += blockDim.x) {
-      int i = idx % r, c = idx / r;
+    cta_for_2d(r, nc, [&](int i, int c) {
       T acc = T(0);
       for (int l = 0; l < k; l++) acc += U[i + (size_t)r * l] * xs[l + (size_t)ld * c];
       xr[i + (size_t)ld * c] -= acc;
-    }
+    });
     __syncthreads();
     // x_s -= T x_r
     const T* Tm = stage(t.Tm, k * r, 0);
-    for (int idx = threadIdx.x; idx < k * nc; idx += blockDim.x) {
-      int l = idx % k, c = idx / k;
+    cta_for_2d(k, nc, [&](int l, int c) {
       T acc = T(0);
       for (int i = 0; i < r; i++) acc += Tm[l + (size_t)k * i] * xr[i + (size_t)ld * c];
       xs[l + (size_t)ld * c] -= acc;
-    }
+    });
     __syncthreads();
   } else if (mode == kDiag) {
     diag_solve(t, xr, ld, nc, sx + (size_t)ld * nc, t.Xi ? stage(t.Xi, r * r, 2) : nullptr);
   }
   __syncthreads();
   const int lo = mode == kDiag ? k : 0;   // the diagonal solve changes x_r only
-  for (int idx = threadIdx.x; idx < (n - lo) * nc; idx += blockDim.x) {
-    int i = lo + idx / nc, c = idx % nc;
+  cta_for_2d(nc, n - lo, [&](int c, int ii) {
+    const int i = lo + ii;
     x[(size_t)t.pact[i] * ldx + c0 + c] = sx[i + (size_t)ld * c];
-  }
+  });
 }
 
 // ws (n x ncols, column-major) <-> rows idx of the DOF-major x
