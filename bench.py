@@ -355,8 +355,16 @@ def parity_check(pkg, args, wl, w2, kw, refine, mu, alpha, pmu, palpha, threads)
     """Solutions of the GPU forms against the CPU reference path on the same
     nodes and right-hand sides (w2, the CPU workload: the full workload unless
     --cpu-sample-n caps it).  Bar: 10 x the ID tolerance of the metric.
-      main_form_vs_reference: the timed form's solution (refined to the target
-        for the mixed / refined forms) against the CPU path at --ref-tol;
+      main_form_vs_reference: the timed form's solution against the CPU path.
+        A refined form meets a residual target, and a solution whose residual
+        is near 1e-8 is up to cond(K) x 1e-8 from the exact discrete solution
+        -- the CPU path at --ref-tol is itself ~1e-7 away at its ~3e-9
+        residual -- so it passes when (a) its residual (dense FP64 rows on
+        the CPU) meets the target and (b) its distance to the CPU path at
+        --ref-tol / 10 (error well under the bar) is within the error the
+        target allows: max(bar, target x error-per-residual of the CPU path
+        at --ref-tol, measured against the same GPU factorization refined to
+        1e-12);
       fp64_plain_vs_reference_same_tol: the plain FP64 GPU factor+solve (the
         reference's arithmetic) against the CPU path at the same ID tolerance,
         with both trees' statistics."""
@@ -375,8 +383,28 @@ def parity_check(pkg, args, wl, w2, kw, refine, mu, alpha, pmu, palpha, threads)
         fac.close()
     res = {"bar": bar, "unknowns": w2.n, "nrhs": w2.rhs.shape[1],
            "norm": "max over rhs of max|x_gpu - x_ref| / max|x_ref| (alpha: / max|mu_ref|)"}
-    main = {"form": args.precision, "reference_id_tol": ref_tol(args),
-            "max_rel_diff_mu": max_rel_diff(mu, pmu)}
+    main = {"form": args.precision, "reference_id_tol": ref_tol(args)}
+    if refine:
+        fkw = w2.factor_kw(kw["id_tol"], kw["precision"])
+        if "rank_model" in kw:
+            fkw["rank_model"] = kw["rank_model"]
+        fac = pkg.Factor(*geo, **fkw)
+        out = fac.solve_refined(w2.rhs, tol=1e-12, max_steps=args.max_steps + 4)
+        err_ref = max_rel_diff(pmu, out[0])
+        fac.close()
+        res_ref = oracle_residual(w2, pmu, palpha, 256, threads)[0]
+        res_gpu = oracle_residual(w2, mu, alpha if alpha is not None else
+                                  np.zeros((0, np.asarray(mu).reshape(w2.n * w2.sol_dim, -1).shape[1])),
+                                  256, threads)[0]
+        per = err_ref / max(res_ref, 1e-300)
+        main.update({"residual": res_gpu, "target_residual": args.target,
+                     "reference_residual_at_ref_tol": res_ref,
+                     "reference_error_at_ref_tol": err_ref, "error_per_residual": per,
+                     "error_bar": max(bar, args.target * per)})
+        rt2 = ref_tol(args) / 10
+        _, _, pmu, palpha = cpu_oracle_run(w2.prob, w2.rhs, rt2, threads, **w2.oracle_kw())
+        main["reference_id_tol"] = rt2
+    main["max_rel_diff_mu"] = max_rel_diff(mu, pmu)
     if nb:
         # the border unknowns of exterior-source data vanish analytically
         # (|alpha| ~ 1e-13): measured on the scale of the density
@@ -395,8 +423,16 @@ def parity_check(pkg, args, wl, w2, kw, refine, mu, alpha, pmu, palpha, threads)
     if nb:
         plain["max_rel_diff_alpha"] = max_rel_diff(galpha, qalpha, scale=qmu)
     res["fp64_plain_vs_reference_same_tol"] = plain
-    diffs = [v for d in (main, plain) for k, v in d.items() if k.startswith("max_rel_diff")]
-    res["pass"] = bool(max(diffs) <= bar)
+    plain_ok = (max(v for k, v in plain.items() if k.startswith("max_rel_diff")) <= bar and
+                plain["tree_gpu"] == plain["tree_reference"])
+    main_diffs = [v for k, v in main.items() if k.startswith("max_rel_diff")]
+    if refine:
+        main["pass"] = bool(main["residual"] <= args.target and
+                            max(main_diffs) <= main["error_bar"])
+    else:
+        main["pass"] = bool(max(main_diffs) <= bar)
+    plain["pass"] = bool(plain_ok)
+    res["pass"] = bool(main["pass"] and plain_ok)
     return res
 
 
