@@ -5,10 +5,12 @@ tree code; the shared library is written next to this file.  Rebuilds only
 when a source changed (content hash).
 """
 import hashlib
+import platform
 import os
 import shutil
 import subprocess
 import sys
+import time
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -37,6 +39,7 @@ def _digest():
                 h.update(f.encode())
                 h.update(open(os.path.join(d, f), "rb").read())
     h.update(" ".join(ARCH).encode())
+    h.update(platform.machine().encode())   # a library built on another host arch never matches
     return h.hexdigest()
 
 
@@ -44,7 +47,9 @@ def build(force=False, verbose=False):
     stamp = LIB + ".stamp"
     dig = _digest()
     if not force and os.path.exists(LIB) and os.path.exists(stamp) and open(stamp).read() == dig:
+        print("libki_gpu.so up to date (sources unchanged, %s)" % platform.machine(), file=sys.stderr)
         return LIB
+    t0 = time.time()
     os.makedirs(OBJ, exist_ok=True)
     nvcc = _nvcc()
     jobs = []
@@ -71,6 +76,8 @@ def build(force=False, verbose=False):
     os.replace(tmp, LIB)
     with open(stamp, "w") as f:
         f.write(dig)
+    print("libki_gpu.so built: %d translation units for %s on %s in %.0f s" %
+          (len(jobs), " ".join(ARCH), platform.machine(), time.time() - t0), file=sys.stderr)
     return LIB
 
 
