@@ -228,6 +228,10 @@ class QuadTree {
   ki_factor* factor() const { return factor_; }
   const Boundary* boundary() const { return boundary_; }
   int n_border() const {
+    // the factorization's own count once it exists (the Neumann and Gaussian
+    // kernels have no border whatever holes the boundary has)
+    ki_factor_info info;
+    if (factor_ && ki_factor_get_info(factor_, &info) == KI_OK) return info.n_border;
     if (!boundary_ || boundary_->holes.empty()) return 0;
     const int c = solution_dimension == 1 ? 1 : (domain_dimension == 2 ? 3 : 6);
     return c * (int)boundary_->holes.size();

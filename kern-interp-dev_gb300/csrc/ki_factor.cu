@@ -2008,7 +2008,7 @@ __global__ void __launch_bounds__(kCpqrCols) k_cpqr_coop(const CpqrTask* tasks, 
   T* vs = reinterpret_cast<T*>(cc_smem);   // the reflector, rows values
   __shared__ long long s_key[kCpqrCols / 32];
   __shared__ int s_col[kCpqrCols / 32];
-  __shared__ int s_p, s_stop;
+  __shared__ int s_p;
   __shared__ T s_red[kCpqrCols / 32];
   __shared__ T s_beta, s_tau;
   // partial norms of my column (the triangle is zero below the diagonal)
