@@ -189,7 +189,9 @@ int ki_solve_device_noalloc(ki_factor* f, const double* d_b, int ldb, int nrhs, 
  * HOST memory (n_dofs x ncols): the reference's dense residual check
  * (solve_err, linear_solve.cpp:379-425, via Kernel::operator(),
  * kernel/kernel.cpp:304-360).  When the problem has holes the border term
- * U*alpha is added if alpha != NULL.  Cost O(n_dofs^2 * ncols).
+ * U*alpha is added if alpha != NULL.  Cost O(n_dofs^2 * ncols).  3D Laplace
+ * computes its entries and sums in FP32-pair arithmetic (~1e-13 relative
+ * per entry; KI_DENSE3=fp64 keeps FP64).
  */
 int ki_apply(ki_factor* f, const double* x, int ldx, int ncols, const double* alpha,
              int ldalpha, double* y, int ldy);
@@ -258,8 +260,8 @@ typedef struct {
  * kern_interp/linear_solve.cpp:202-227) and checks the residual separately
  * (solve_err, :339-426).  HOST buffers as in ki_solve.  The residual's
  * operator product is the FMM of ki_apply_fmm for 2D Laplace problems with
- * at least 4096 unknowns (O(n_dofs * nrhs) per step), else the dense FP64
- * product (O(n_dofs^2 * nrhs)); the environment variable
+ * at least 4096 unknowns (O(n_dofs * nrhs) per step), else the dense
+ * product of ki_apply (O(n_dofs^2 * nrhs)); the environment variable
  * KI_RESIDUAL_APPLY=dense|fmm overrides the choice.  With the FMM, a
  * correction d whose residual change is small enough is followed by the
  * update r -= A_low d, A_low the FMM in FP32 arithmetic at 12 terms
