@@ -30,6 +30,13 @@ constexpr int kNb = 32;
       throw std::runtime_error(std::string("CUDA error: ") + cudaGetErrorString(e_));     \
   } while (0)
 
+// Unblocked LU of the panel A(p:n, p:p+w) with partial pivoting (dgetf2
+// order: pivot = first index of the largest |A(i, j)|, i >= j), one CTA.
+// Each column costs three barriers and one pass over the rows: the pass
+// that scales column j and updates the panel's later columns also finds
+// each thread's candidate pivot of column j + 1 in the rows it just updated
+// (every row is read and written by one thread only, so no barrier is needed
+// between the update and that search).
 template <typename T>
 __global__ void __launch_bounds__(1024) k_lu_panel(T* A, int n, int lda, int p, int w, int* piv,
                                                    int* err) {
@@ -38,17 +45,19 @@ __global__ void __launch_bounds__(1024) k_lu_panel(T* A, int n, int lda, int p, 
   __shared__ int s_p;
   __shared__ T s_pv;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int nth = blockDim.x;
+  // this thread's candidate pivot of column p
+  T best = T(-1);
+  int bi = p;
+  for (int i = p + (int)threadIdx.x; i < n; i += nth) {
+    const T v = fabs(A[i + (size_t)lda * p]);
+    if (v > best) { best = v; bi = i; }
+  }
   for (int j = p; j < p + w; j++) {
     // pivot: argmax |A(i, j)|, i >= j (first index on ties)
-    T best = T(-1);
-    int bi = j;
-    for (int i = j + threadIdx.x; i < n; i += blockDim.x) {
-      T v = fabs(A[i + (size_t)lda * j]);
-      if (v > best) { best = v; bi = i; }
-    }
     for (int o = 16; o > 0; o >>= 1) {
-      T ov = __shfl_down_sync(0xffffffff, best, o);
-      int oi = __shfl_down_sync(0xffffffff, bi, o);
+      const T ov = __shfl_down_sync(0xffffffff, best, o);
+      const int oi = __shfl_down_sync(0xffffffff, bi, o);
       if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
     }
     if (lane == 0) { s_val[warp] = best; s_idx[warp] = bi; }
@@ -57,36 +66,45 @@ __global__ void __launch_bounds__(1024) k_lu_panel(T* A, int n, int lda, int p, 
       best = lane < nw ? s_val[lane] : T(-1);
       bi = lane < nw ? s_idx[lane] : n;
       for (int o = 16; o > 0; o >>= 1) {
-        T ov = __shfl_down_sync(0xffffffff, best, o);
-        int oi = __shfl_down_sync(0xffffffff, bi, o);
+        const T ov = __shfl_down_sync(0xffffffff, best, o);
+        const int oi = __shfl_down_sync(0xffffffff, bi, o);
         if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
       }
       if (lane == 0) { s_p = bi; s_pv = best; piv[j] = bi; }
     }
     __syncthreads();
     const int pr = s_p;
+    const bool next = j + 1 < p + w;
+    best = T(-1);
+    bi = j + 1;
     if (s_pv == T(0)) {
+      // singular column: flagged, no elimination; the next column's candidates
       if (threadIdx.x == 0) atomicMax(err, 2);
-      __syncthreads();
+      if (next)
+        for (int i = j + 1 + (int)threadIdx.x; i < n; i += nth) {
+          const T v = fabs(A[i + (size_t)lda * (j + 1)]);
+          if (v > best) { best = v; bi = i; }
+        }
       continue;
     }
     if (pr != j)
-      for (int c = p + threadIdx.x; c < p + w; c += blockDim.x) {
-        T t = A[j + (size_t)lda * c];
+      for (int c = p + (int)threadIdx.x; c < p + w; c += nth) {
+        const T t = A[j + (size_t)lda * c];
         A[j + (size_t)lda * c] = A[pr + (size_t)lda * c];
         A[pr + (size_t)lda * c] = t;
       }
     __syncthreads();
     const T d = A[j + (size_t)lda * j];
-    for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) A[i + (size_t)lda * j] /= d;
-    __syncthreads();
-    const int cols = p + w - j - 1;
-    if (cols > 0)
-      for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) {
-        T l = A[i + (size_t)lda * j];
-        for (int c = j + 1; c < p + w; c++) A[i + (size_t)lda * c] -= l * A[j + (size_t)lda * c];
+    // scale column j, update the later panel columns, and search column j + 1
+    for (int i = j + 1 + (int)threadIdx.x; i < n; i += nth) {
+      const T l = A[i + (size_t)lda * j] / d;
+      A[i + (size_t)lda * j] = l;
+      for (int c = j + 1; c < p + w; c++) A[i + (size_t)lda * c] -= l * A[j + (size_t)lda * c];
+      if (next) {
+        const T v = fabs(A[i + (size_t)lda * (j + 1)]);
+        if (v > best) { best = v; bi = i; }
       }
-    __syncthreads();
+    }
   }
 }
 
