@@ -99,6 +99,38 @@ def test_port_dense_residual(oracle_mod, pkg):
     assert np.linalg.norm(r) / np.linalg.norm(f) <= 50 * tol
 
 
+def test_port_neumann_field_and_gauss_backward_error(oracle_mod, pkg):
+    """The other scalar kernels in the port, pinned by the physics and by
+    dense algebra rather than by the reference alone.  Neumann
+    (Kernel::one_d_kern, kernel.cpp:44-54): the single-layer field of the
+    density solves the interior Neumann problem of an exterior source, so
+    differences of the field at interior points match the source's field.
+    Gauss (:55-60, three proxy rings :661-672): the compressed solve's
+    backward error against the dense covariance matrix (exp(-r^2), 5 on the
+    diagonal) <= 50 id_tol."""
+    g = pkg.geometry
+    prob = g.star(64, 16)
+    src = np.array([[3.0, 1.0]])
+    f = g.laplace_neumann_rhs(prob, src)
+    mu, alpha, _ = oracle_mod.solve(prob, f, 1e-10, threads=2, pde=1)
+    assert alpha.size == 0
+    tg = g.disc_targets(40, np.random.default_rng(4), radius=0.45)
+    d = tg[:, None, :] - prob.points[None]
+    u = (prob.weights[None] / (2 * np.pi) * np.log(np.sqrt((d ** 2).sum(-1)))) @ mu[:, 0]
+    ue = g.laplace_source_field(tg, src)[:, 0]
+    err = np.abs((u - u[0]) - (ue - ue[0])).max() / np.abs(ue - ue[0]).max()
+    assert err <= 1e-8, err
+
+    grid = g.uniform_grid(1024)
+    b = np.random.default_rng(7).standard_normal((grid.n, 1))
+    tol = 1e-6
+    x, _, _ = oracle_mod.solve(grid, b, tol, threads=2, pde=2)
+    r2 = ((grid.points[:, None, :] - grid.points[None, :, :]) ** 2).sum(-1)
+    K = np.exp(-r2)
+    np.fill_diagonal(K, 5.0)
+    assert np.linalg.norm(K @ x - b) / np.linalg.norm(b) <= 50 * tol
+
+
 def test_reference_matches_port_random_star(oracle_mod, pkg):
     """Where the reference tree is present, the compiled reference and the port
     agree on a freshly generated boundary (not a stored fixture)."""
